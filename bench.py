@@ -1,0 +1,308 @@
+"""Benchmark of the KMeans Lloyd hot path on one GB300.
+
+Workload (default): anisotropic_1024x128 -- n=4,000,000 rows x d=128
+features, k=1024 clusters, X stored f32 (2.05 GB, larger than L2), 1024
+anisotropic Gaussian blobs, init = first k rows of a seeded permutation, tol 0
+so every iteration runs. A step is one Lloyd iteration over all n rows
+(assignment + centroid update + inertia + shift).
+
+  value   Lloyd iterations/s of the chosen form with X already resident in
+          HBM: one fit call running W warm-up iterations, then one fit call
+          running exactly K iterations timed with CUDA events on the stream
+          the library launches on.
+  e2e     the same metric through the public API with host buffers: one fit
+          call on a pinned host X (H2D of X, K iterations, D2H of labels and
+          centres inside the timed region).
+  forms   bf16  = FK_PRECISION_MIXED_BF16 on the f32x64 entry point
+                  (KMeans<f64> semantics, BF16 tcgen05 contraction + FP64
+                  re-check); labels identical to the FP64 oracle.
+          fp32  = plain KMeans<f32> (direct-form FP32 on CUDA cores).
+          fp64  = plain KMeans<f64> on the widened X.
+
+--impl reference times the CPU restatement of the reference (oracle/, the
+reference is Rust and cannot be built here) on a bounded row sample of the
+same workload with all host threads, and reports iterations/s extrapolated
+to the full n.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--form", default="auto", choices=["auto", "bf16", "fp32", "fp64"])
+    ap.add_argument("--scale", type=float, default=1.0, help="fraction of the full row count")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    return ap.parse_args()
+
+
+METRIC = "KMeans Lloyd iters/s & pt·k/s: BF16+FP64 recheck vs plain FP32, labels=FP64"
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d.get("hbm_gbs", 6800.0), d.get("bf16_tflops", 1900.0), d.get("bf16_tflops_sustained", 1700.0), \
+            "measured"
+    return 6800.0, 1900.0, 1700.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks + throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu=0):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = max(mx, float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_workload(scale):
+    from ferrolearn_gb300 import workloads as W
+    return W.anisotropic_1024x128(scale=scale)
+
+
+def cpu_baseline(w, seconds, threads):
+    """Oracle (CPU restatement of kmeans.rs) on a bounded row sample; iters/s extrapolated to the full n."""
+    from oracle import oracle as O
+    x64 = w["x"].astype(np.float64)
+    c = w["init"]
+    n = x64.shape[0]
+    rows = 2048
+    while True:
+        t0 = time.perf_counter()
+        O.lloyd_step(x64[:rows], c, nthreads=threads)
+        dt = time.perf_counter() - t0
+        if dt >= seconds / 4 or rows >= n:
+            break
+        rows = min(n, int(rows * max(2.0, (seconds / 4) / max(dt, 1e-3))))
+    reps = max(1, int(seconds / max(dt, 1e-3)))
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        O.lloyd_step(x64[:rows], c, nthreads=threads)
+    dt = (time.perf_counter() - t0) / reps
+    per_iter = dt * n / rows
+    return {"value": 1.0 / per_iter, "unit": "iters/s", "cores": threads, "kind": "port",
+            "sample": f"{rows} of {n} rows, {reps} Lloyd iterations (FP64 direct form, OpenMP chunked like "
+                      f"assign_parallel, serial update); per-iteration time extrapolated x{n / rows:.1f}",
+            "seconds_per_full_iteration": per_iter}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    w = make_workload(args.scale)
+    threads = os.cpu_count() or 1
+    from oracle import oracle as O
+    x64 = w["x"].astype(np.float64)
+    n = x64.shape[0]
+    rows = max(1024, min(n, int(20000 * args.scale) if args.scale < 1 else 20000))
+    c = w["init"]
+    for _ in range(max(1, args.warmup)):
+        O.lloyd_step(x64[:rows], c, nthreads=threads)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        O.lloyd_step(x64[:rows], c, nthreads=threads)
+    dt = (time.perf_counter() - t0) / args.steps
+    per_iter = dt * n / rows
+    v = 1.0 / per_iter
+    out = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "iters/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_iter * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": w["name"], "n": n, "d": int(x64.shape[1]), "k": w["k"], "X": "f32 widened to f64",
+                   "l2": "inputs larger than L2"},
+        "cpu_baseline": {"value": v, "unit": "iters/s", "cores": threads, "kind": "port",
+                         "sample": f"{rows} of {n} rows per step, extrapolated x{n / rows:.1f}"},
+        "e2e": {"value": v, "unit": "iters/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out))
+
+
+def run_ours(args):
+    import torch
+
+    import ferrolearn_gb300 as F
+    from ferrolearn_gb300 import _native
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if world > 1:
+        import torch.distributed as dist
+        local = int(os.environ.get("LOCAL_RANK", "0"))
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev = torch.cuda.current_device()
+    hbm, bf16, bf16s, peak_src = load_peaks()
+    w = make_workload(args.scale)
+    x32 = w["x"]
+    n, d = x32.shape
+    k = w["k"]
+    form = args.form if args.form != "auto" else "bf16"
+    stream = torch.cuda.Stream()
+    ctx = F.Context(dev, stream=stream.cuda_stream)
+
+    def build_model(max_iter):
+        if form == "fp32":
+            m = F.KMeans(k, dtype="f32").with_init_centers(w["init"].astype(np.float32))
+        elif form == "fp64":
+            m = F.KMeans(k, dtype="f64").with_init_centers(w["init"])
+        else:
+            m = F.KMeans(k, dtype="f32x64").with_init_centers(w["init"]).with_precision("bf16")
+        return m.with_max_iter(max_iter).with_tol(0.0).with_n_init(1)
+
+    if form == "fp64":
+        xd = torch.from_numpy(x32).to(dev).double()
+    else:
+        xd = torch.from_numpy(x32).to(dev)
+    torch.cuda.synchronize()
+
+    # warm-up (untimed), also measures the per-phase split of one short fit
+    wm = build_model(args.warmup).with_timing(True).fit(xd, ctx=ctx)
+    l0 = _native.lib().fk_debug_launch_count()
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    model = build_model(args.steps).with_timing(True)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(dev) as clocks:
+        start.record(stream)
+        fitted = model.fit(xd, ctx=ctx)
+        end.record(stream)
+        torch.cuda.synchronize()
+    launches = int(_native.lib().fk_debug_launch_count() - l0)
+    ms = start.elapsed_time(end)
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    rep = fitted.report
+    iters = fitted.n_iter()
+    assert iters == args.steps, (iters, args.steps)
+    ips = world * iters / (ms / 1e3)
+    # dominant kernel: the assignment (per-phase CUDA events inside the library)
+    assign_ms = rep["ms_assign"] / iters
+    flops = 2.0 * n * k * d
+    if form == "bf16":
+        roof = {"bound": "tensor", "achieved": flops / (assign_ms / 1e3) / 1e12, "peak": bf16s, "unit": "TFLOP/s",
+                "peak_source": f"bf16_tflops_sustained ({peak_src})"}
+    else:
+        roof = {"bound": "tensor", "achieved": flops / (assign_ms / 1e3) / 1e12, "peak": bf16s, "unit": "TFLOP/s",
+                "peak_source": f"bf16_tflops_sustained ({peak_src}); SIMT form compared against the tensor peak"}
+    roof["frac"] = roof["achieved"] / roof["peak"]
+    roof["traffic"] = None
+    roof["kernel"] = "assignment phase (per-phase events)"
+    roof["ms_per_launch"] = assign_ms
+
+    out = {
+        "metric": METRIC, "value": ips, "unit": "iters/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / iters, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": {"bf16": "bf16+f64", "fp32": "f32", "fp64": "f64"}[form], "data": "synthetic",
+        "form": form,
+        "config": {"workload": w["name"], "n": n, "d": d, "k": k, "X": "f32", "init": "first k rows of a seeded "
+                   "permutation", "tol": 0.0, "l2": "inputs larger than L2 (X 2.05 GB)", "parallelism": "replicas"},
+        "pt_k_per_s": ips * n * k,
+        "phase_ms_per_iter": {"assign": assign_ms, "update": rep["ms_update"] / iters},
+        "recheck": {"rows": rep["rows_rechecked"], "full_rescan": rep["rows_full_rescan"],
+                    "near_ties": rep["near_tie_rows"],
+                    "fraction": rep["rows_rechecked"] / max(1, rep["rows_assigned"])},
+        "gpu_launches": launches,
+        "clocks": clocks.summary(),
+        "roofline": roof,
+    }
+
+    if not args.no_e2e and rank == 0:
+        xh = torch.from_numpy(x32).pin_memory() if form != "fp64" else torch.from_numpy(
+            x32.astype(np.float64)).pin_memory()
+        xh_np = xh.numpy()
+        m2 = build_model(args.steps)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        f2 = m2.fit(xh_np, ctx=ctx)
+        t1 = time.perf_counter()
+        h2d = xh_np.nbytes + w["init"].nbytes
+        d2h = n * 8 + k * d * 8
+        out["e2e"] = {"value": f2.n_iter() / (t1 - t0), "unit": "iters/s",
+                      "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": d2h / args.steps,
+                      "note": "one fit call on a pinned host X running K iterations; copies amortised per step"}
+    if not args.no_cpu and rank == 0 and world == 1:
+        out["cpu_baseline"] = cpu_baseline(w, args.cpu_seconds, os.cpu_count() or 1)
+    if rank == 0:
+        print(json.dumps(out))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,12 @@
+"""GB300-native (sm_103a) KMeans Lloyd path, a drop-in for ferrolearn-cluster's KMeans.
+
+The compute runs in hand-written CUDA kernels inside the in-tree library
+_build/libferrokmeans.so, reached through its C ABI (include/ferrokmeans.h).
+This package is the host-side mirror of the reference's KMeans API.
+"""
+from .kmeans import (  # noqa: F401
+    MIXED_BF16, MIXED_FP32, PLAIN, Context, CudaError, DeviceOutOfMemory, DeviceTimeout, FerroError, FittedKMeans,
+    InsufficientSamples, InvalidParameter, KMeans, NullPointer, NumericalInstability, ShapeMismatch, Unsupported,
+    default_context, draws, kmeans_plus_plus, lloyd_step)
+
+__version__ = "0.1.0"

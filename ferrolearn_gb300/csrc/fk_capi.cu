@@ -1,0 +1,733 @@
+// fk_capi.cu -- the extern "C" boundary and the Lloyd driver.
+//
+// The driver restates Fit::fit (kmeans.rs:417-512) on the GPU: validation in
+// the reference's order, n_init runs seeded base+run, the Lloyd loop whose
+// labels/inertia come from the assignment against the pre-update centres
+// while the returned centres are the post-update ones, convergence when
+// sqrt(max shift^2) < tol (absolute), and the strictly-lowest inertia run
+// kept (earliest wins ties). All per-iteration work stays on the device; the
+// only host traffic per iteration is one 64-byte scalar block read back.
+#include <cmath>
+#include <cstdarg>
+#include <cstring>
+#include <vector>
+
+#include "fk_internal.cuh"
+
+namespace fk {
+
+static thread_local std::string g_last_error;
+unsigned long long g_launch_count = 0;
+
+void set_error(const char *fmt, ...) {
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+}
+
+// CUDA is first touched here, not at context creation, so argument errors
+// are reported the same way on machines without a GPU.
+void Ctx::bind() {
+    FK_CUDA(cudaSetDevice(device));
+    if (initialized) return;
+    cudaDeviceProp prop;
+    FK_CUDA(cudaGetDeviceProperties(&prop, device));
+    num_sms = prop.multiProcessorCount;
+    cc_major = prop.major;
+    cc_minor = prop.minor;
+    if (!stream) {
+        FK_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+        own_stream = true;
+    }
+    FK_CUDA(cudaMallocHost((void **)&host_scalars, sizeof(DevScalars)));
+    initialized = true;
+}
+
+void *Ctx::get(BufSlot s, size_t bytes) {
+    if (bytes == 0) bytes = 16;
+    if (cap[s] >= bytes) return buf[s];
+    if (buf[s]) {
+        FK_CUDA(cudaStreamSynchronize(stream));
+        FK_CUDA(cudaFree(buf[s]));
+        buf[s] = nullptr;
+        cap[s] = 0;
+    }
+    size_t want = bytes + bytes / 8;  // headroom for slightly larger calls
+    void *p = nullptr;
+    cudaError_t e = cudaMalloc(&p, want);
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        e = cudaMalloc(&p, bytes);
+        want = bytes;
+    }
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        set_error("cudaMalloc of %zu bytes failed: %s", bytes, cudaGetErrorString(e));
+        fail(FK_ERR_OOM);
+    }
+    buf[s] = p;
+    cap[s] = want;
+    return p;
+}
+
+namespace {
+
+bool is_device_ptr(const void *p) {
+    if (!p) return false;
+    cudaPointerAttributes a;
+    cudaError_t e = cudaPointerGetAttributes(&a, p);
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+template <typename T>
+const T *stage_in(Ctx &ctx, BufSlot slot, const T *p, size_t count) {
+    if (is_device_ptr(p)) return p;
+    T *d = (T *)ctx.get(slot, sizeof(T) * count);
+    if (count) FK_CUDA(cudaMemcpyAsync(d, p, sizeof(T) * count, cudaMemcpyHostToDevice, ctx.stream));
+    return d;
+}
+
+template <typename T>
+void copy_out(Ctx &ctx, T *dst, const T *dev_src, size_t count) {
+    if (!count || !dst) return;
+    FK_CUDA(cudaMemcpyAsync(dst, dev_src, sizeof(T) * count, cudaMemcpyDefault, ctx.stream));
+}
+
+// Phase timer: records a pair of events on the stream and leaves the
+// reading to flush_timers(), so timing never adds a host synchronisation
+// inside the Lloyd loop.
+struct Timer {
+    Ctx *ctx = nullptr;
+    cudaEvent_t b = nullptr;
+    double *acc = nullptr;
+    cudaEvent_t a = nullptr;
+    Timer(bool enable, Ctx &c, double *accum) {
+        if (!enable || !accum) return;
+        ctx = &c;
+        acc = accum;
+        FK_CUDA(cudaEventCreate(&a));
+        FK_CUDA(cudaEventCreate(&b));
+        FK_CUDA(cudaEventRecord(a, c.stream));
+    }
+    ~Timer() {
+        if (!ctx) return;
+        if (cudaEventRecord(b, ctx->stream) == cudaSuccess) {
+            ctx->pending.push_back({a, b, acc});
+        } else {
+            cudaEventDestroy(a);
+            cudaEventDestroy(b);
+        }
+    }
+};
+
+void flush_timers(Ctx &ctx) {
+    for (auto &p : ctx.pending) {
+        float ms = 0.f;
+        if (cudaEventSynchronize(p.b) == cudaSuccess && cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess)
+            *p.acc += ms;
+        cudaEventDestroy(p.a);
+        cudaEventDestroy(p.b);
+    }
+    ctx.pending.clear();
+}
+
+template <typename T> struct FMax;
+template <> struct FMax<double> { static double v() { return 1.7976931348623157e308; } };
+template <> struct FMax<float> { static float v() { return 3.40282347e38f; } };
+
+template <typename TC>
+TC shift_from_bits(unsigned long long bits);
+template <>
+double shift_from_bits<double>(unsigned long long bits) {
+    double v;
+    memcpy(&v, &bits, sizeof v);
+    return std::sqrt(v);
+}
+template <>
+float shift_from_bits<float>(unsigned long long bits) {
+    uint32_t b = (uint32_t)bits;
+    float v;
+    memcpy(&v, &b, sizeof v);
+    return std::sqrt(v);
+}
+
+uint64_t splitmix64(uint64_t *s) {
+    uint64_t z = (*s += 0x9E3779B97F4A7C15ULL);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    return z ^ (z >> 31);
+}
+
+void host_draws(uint64_t seed, int64_t count, double *out) {
+    uint64_t st = seed;
+    for (int64_t i = 0; i < count; i++) out[i] = (double)(splitmix64(&st) >> 11) * (1.0 / 9007199254740992.0);
+}
+
+int kpp_trials_host(int64_t k) {
+    long long t = 2 + (long long)std::floor(std::log((double)k));
+    return t < 1 ? 1 : (int)t;
+}
+
+bool precision_ok(int prec, bool f64_semantics) {
+    if (prec == FK_PRECISION_PLAIN) return true;
+    if (prec == FK_PRECISION_MIXED_BF16 || prec == FK_PRECISION_MIXED_FP32) return f64_semantics;
+    return false;
+}
+
+// ------------------------------------------------------------ one step --
+// Assignment against c (labels, inertia into scalars), then the update into
+// nc (+ shift bits). Mixed precisions fold the inertia into the update pass.
+template <typename TX, typename TC>
+void lloyd_iteration(Ctx &ctx, const TX *x, int64_t n, int d, const TC *c, int k, int prec, TC *nc,
+                     int32_t *labels, DevScalars *sc, const SortPlan &plan, bool x_changed, fk_fit_report *rep,
+                     bool timing) {
+    cudaStream_t s = ctx.stream;
+    int32_t *members = (int32_t *)ctx.get(BUF_MEMBERS, sizeof(int32_t) * (size_t)n);
+    int32_t *seg = (int32_t *)ctx.get(BUF_SEGHIST, sizeof(int32_t) * (size_t)plan.k * plan.nseg);
+    int32_t *tmp = (int32_t *)ctx.get(BUF_SCAN_TMP, plan.scan_tmp_bytes);
+    {
+        Timer t(timing, ctx, rep ? &rep->ms_assign : nullptr);
+        if (prec == FK_PRECISION_PLAIN) {
+            TC *mind = (TC *)ctx.get(BUF_MIND, sizeof(TC) * (size_t)n);
+            double *part = (double *)ctx.get(BUF_PARTIAL, sizeof(double) * (size_t)sum_fixed_partials(n));
+            launch_assign_direct<TX, TC>(x, n, d, c, k, labels, mind, s);
+            launch_sum_fixed<TC>(mind, n, part, &sc->inertia, s);
+        } else {
+            if constexpr (std::is_same<TC, double>::value) {
+                run_assign_mixed<TX>(ctx, x, n, d, c, k, prec, labels, nullptr, sc, x_changed);
+            }
+        }
+    }
+    {
+        Timer t(timing, ctx, rep ? &rep->ms_update : nullptr);
+        launch_sort_by_cluster(plan, labels, seg, tmp, members, s);
+        launch_update_centroids<TX, TC>(plan, x, d, members, seg, c, nc, sc, s);
+        if (prec != FK_PRECISION_PLAIN) {
+            if constexpr (std::is_same<TC, double>::value) {
+                launch_mixed_inertia<TX>(ctx, plan, x, d, members, seg, c, sc);
+            }
+        }
+    }
+}
+
+void read_scalars(Ctx &ctx, DevScalars *dev) {
+    FK_CUDA(cudaMemcpyAsync(ctx.host_scalars, dev, sizeof(DevScalars), cudaMemcpyDeviceToHost, ctx.stream));
+    FK_CUDA(cudaStreamSynchronize(ctx.stream));
+    if (ctx.host_scalars->error_word) {
+        set_error("a bounded device wait gave up (code %llu)", ctx.host_scalars->error_word);
+        fail(FK_ERR_TIMEOUT);
+    }
+}
+
+void accumulate_report(fk_fit_report *rep, const DevScalars &h, int64_t n) {
+    if (!rep) return;
+    rep->rows_assigned += n;
+    rep->rows_rechecked += (int64_t)h.recheck_rows;
+    rep->rows_full_rescan += (int64_t)h.full_rows;
+    rep->near_tie_rows += (int64_t)h.near_tie_rows;
+}
+
+// ------------------------------------------------------------------ fit --
+template <typename TX, typename TC>
+fk_status fit_impl(fk_ctx *ctxp, const TX *x_in, int64_t n, int64_t d, const fk_kmeans_params *p,
+                   const TC *init_in, TC *centers_out, uint64_t *labels_out, TC *inertia_out, int64_t *n_iter_out,
+                   fk_fit_report *rep) {
+    Ctx &ctx = *reinterpret_cast<Ctx *>(ctxp);
+    const int64_t k = p->n_clusters;
+    // Validation order of kmeans.rs:421-449.
+    if (k <= 0) {
+        set_error("Invalid parameter `n_clusters`: must be at least 1");
+        return FK_ERR_INVALID_PARAMETER;
+    }
+    if (n <= 0) {
+        set_error("Insufficient samples: need at least %lld, got 0 (KMeans requires at least n_clusters samples)",
+                  (long long)k);
+        return FK_ERR_INSUFFICIENT_SAMPLES;
+    }
+    if (n < k) {
+        set_error("Insufficient samples: need at least %lld, got %lld (KMeans requires at least n_clusters samples)",
+                  (long long)k, (long long)n);
+        return FK_ERR_INSUFFICIENT_SAMPLES;
+    }
+    if (p->n_init <= 0) {
+        set_error("Invalid parameter `n_init`: must be at least 1");
+        return FK_ERR_INVALID_PARAMETER;
+    }
+    if (p->max_iter < 0 || d < 0) {
+        set_error("Invalid parameter `max_iter`/`d`: negative");
+        return FK_ERR_INVALID_PARAMETER;
+    }
+    if (!x_in || !centers_out || !labels_out || !inertia_out || !n_iter_out) {
+        set_error("required pointer is NULL");
+        return FK_ERR_NULL_POINTER;
+    }
+    constexpr bool f64sem = std::is_same<TC, double>::value;
+    if (!precision_ok(p->precision, f64sem)) {
+        set_error("precision %d is not available for this entry point", p->precision);
+        return FK_ERR_UNSUPPORTED;
+    }
+    if (k > (1 << 20) || n > INT32_MAX || d > (1 << 16)) {
+        set_error("shape n=%lld d=%lld k=%lld exceeds the supported range", (long long)n, (long long)d, (long long)k);
+        return FK_ERR_UNSUPPORTED;
+    }
+    ctx.bind();
+    if (rep) {
+        memset(rep, 0, sizeof(*rep));
+        rep->precision_used = p->precision;
+    }
+    const bool timing = p->collect_timing != 0 && rep != nullptr;
+    cudaStream_t s = ctx.stream;
+    cudaEvent_t t_begin = nullptr, t_end = nullptr;
+    if (timing) {
+        FK_CUDA(cudaEventCreate(&t_begin));
+        FK_CUDA(cudaEventCreate(&t_end));
+        FK_CUDA(cudaEventRecord(t_begin, s));
+    }
+    const size_t kd = (size_t)k * d;
+    const TX *x = stage_in<TX>(ctx, BUF_X, x_in, (size_t)n * d);
+    TC *c = (TC *)ctx.get(BUF_C0, sizeof(TC) * kd);
+    TC *nc = (TC *)ctx.get(BUF_C1, sizeof(TC) * kd);
+    TC *cbest = (TC *)ctx.get(BUF_CBEST, sizeof(TC) * kd);
+    int32_t *labels = (int32_t *)ctx.get(BUF_LABELS, sizeof(int32_t) * (size_t)n);
+    int32_t *lbest = (int32_t *)ctx.get(BUF_LBEST, sizeof(int32_t) * (size_t)n);
+    DevScalars *sc = (DevScalars *)ctx.get(BUF_SCALARS, sizeof(DevScalars));
+    FK_CUDA(cudaMemsetAsync(labels, 0, sizeof(int32_t) * (size_t)n, s));
+    SortPlan plan = make_sort_plan(n, (int)k);
+
+    const TC *init = init_in ? stage_in<TC>(ctx, BUF_OUT2, init_in, kd * (size_t)p->n_init) : nullptr;
+    const double *draws_dev = nullptr;
+    int64_t n_draws = 0;
+    if (!init) {
+        // k-means++ draws: caller's flat stream, or splitmix64 per run.
+        n_draws = p->draws ? p->n_draws : 1 + (k - 1) * kpp_trials_host(k);
+        if (p->draws) draws_dev = stage_in<double>(ctx, BUF_DRAWS, p->draws, (size_t)n_draws);
+    }
+    int64_t draws_pos = 0;
+    std::vector<double> hdraws;
+
+    bool have = false;
+    TC best_inertia = FMax<TC>::v();
+    int64_t best_iter = 0;
+    bool x_changed = true;
+    for (int64_t run = 0; run < p->n_init; run++) {
+        if (init) {
+            FK_CUDA(cudaMemcpyAsync(c, init + (size_t)run * kd, sizeof(TC) * kd, cudaMemcpyDeviceToDevice, s));
+        } else {
+            Timer t(timing, ctx, rep ? &rep->ms_init : nullptr);
+            const double *dr;
+            int64_t ndr;
+            if (p->draws) {
+                if (draws_pos >= n_draws) {
+                    set_error("injected draw stream exhausted before run %lld", (long long)run);
+                    fail(FK_ERR_INVALID_PARAMETER);
+                }
+                dr = draws_dev + draws_pos;
+                ndr = n_draws - draws_pos;
+            } else {
+                uint64_t seed = (p->has_random_state ? p->random_state : 0) + (uint64_t)run;
+                hdraws.resize((size_t)n_draws);
+                host_draws(seed, n_draws, hdraws.data());
+                double *dd = (double *)ctx.get(BUF_DRAWS, sizeof(double) * (size_t)n_draws);
+                FK_CUDA(cudaMemcpyAsync(dd, hdraws.data(), sizeof(double) * (size_t)n_draws,
+                                        cudaMemcpyHostToDevice, s));
+                FK_CUDA(cudaStreamSynchronize(s));  // hdraws is reused next run
+                dr = dd;
+                ndr = n_draws;
+            }
+            int64_t used = 0;
+            if constexpr (std::is_same<TX, TC>::value) {
+                run_kmeanspp<TC>(ctx, x, n, (int)d, (int)k, dr, ndr, c, &used);
+            } else {
+                // k-means++ on the exactly widened matrix.
+                TC *xw = (TC *)ctx.get(BUF_XC, sizeof(TC) * (size_t)n * d);
+                launch_convert<TX, TC>(x, (int64_t)n * d, xw, s);
+                run_kmeanspp<TC>(ctx, xw, n, (int)d, (int)k, dr, ndr, c, &used);
+            }
+            if (p->draws) draws_pos += used;
+        }
+        int64_t n_iter = 0;
+        TC inertia = FMax<TC>::v();
+        for (int64_t it = 0; it < p->max_iter; it++) {
+            FK_CUDA(cudaMemsetAsync(sc, 0, sizeof(DevScalars), s));
+            lloyd_iteration<TX, TC>(ctx, x, n, (int)d, c, (int)k, p->precision, nc, labels, sc, plan, x_changed, rep,
+                                    timing);
+            x_changed = false;
+            read_scalars(ctx, sc);
+            accumulate_report(rep, *ctx.host_scalars, n);
+            inertia = (TC)ctx.host_scalars->inertia;
+            TC shift = shift_from_bits<TC>(ctx.host_scalars->shift_bits);
+            std::swap(c, nc);
+            n_iter = it + 1;
+            if (shift < (TC)p->tol) break;
+        }
+        if (rep) rep->iterations_total += n_iter;
+        if (!have || inertia < best_inertia) {
+            have = true;
+            best_inertia = inertia;
+            best_iter = n_iter;
+            if (rep) rep->best_run = run;
+            FK_CUDA(cudaMemcpyAsync(cbest, c, sizeof(TC) * kd, cudaMemcpyDeviceToDevice, s));
+            FK_CUDA(cudaMemcpyAsync(lbest, labels, sizeof(int32_t) * (size_t)n, cudaMemcpyDeviceToDevice, s));
+        }
+    }
+    // Keep the context's buffer pointers consistent after the swaps.
+    ctx.buf[BUF_C0] = c;
+    ctx.buf[BUF_C1] = nc;
+    if (ctx.cap[BUF_C0] != ctx.cap[BUF_C1]) {
+        size_t m = ctx.cap[BUF_C0] < ctx.cap[BUF_C1] ? ctx.cap[BUF_C0] : ctx.cap[BUF_C1];
+        ctx.cap[BUF_C0] = ctx.cap[BUF_C1] = m;
+    }
+    copy_out<TC>(ctx, centers_out, cbest, kd);
+    if (is_device_ptr(labels_out)) {
+        launch_labels_to_u64(lbest, n, labels_out, s);
+    } else {
+        uint64_t *l64 = (uint64_t *)ctx.get(BUF_OUT, sizeof(uint64_t) * (size_t)n);
+        launch_labels_to_u64(lbest, n, l64, s);
+        copy_out<uint64_t>(ctx, labels_out, l64, (size_t)n);
+    }
+    if (timing) {
+        FK_CUDA(cudaEventRecord(t_end, s));
+        FK_CUDA(cudaEventSynchronize(t_end));
+        float ms = 0.f;
+        FK_CUDA(cudaEventElapsedTime(&ms, t_begin, t_end));
+        rep->ms_total = ms;
+        cudaEventDestroy(t_begin);
+        cudaEventDestroy(t_end);
+    }
+    FK_CUDA(cudaStreamSynchronize(s));
+    flush_timers(ctx);
+    *inertia_out = best_inertia;
+    *n_iter_out = best_iter;
+    return FK_OK;
+}
+
+// ----------------------------------------------------------------- step --
+template <typename TX, typename TC>
+fk_status step_impl(fk_ctx *ctxp, const TX *x_in, int64_t n, int64_t d, const TC *c_in, int64_t k, int32_t prec,
+                    uint64_t *labels_out, TC *centers_out, TC *inertia_out, TC *shift_out, fk_fit_report *rep) {
+    Ctx &ctx = *reinterpret_cast<Ctx *>(ctxp);
+    if (k <= 0) {
+        set_error("Invalid parameter `n_clusters`: must be at least 1");
+        return FK_ERR_INVALID_PARAMETER;
+    }
+    if (n <= 0 || n < k) {
+        set_error("Insufficient samples: need at least %lld, got %lld", (long long)k, (long long)n);
+        return FK_ERR_INSUFFICIENT_SAMPLES;
+    }
+    if (!x_in || !c_in || !labels_out || !centers_out || !inertia_out || !shift_out) {
+        set_error("required pointer is NULL");
+        return FK_ERR_NULL_POINTER;
+    }
+    if (!precision_ok(prec, std::is_same<TC, double>::value)) {
+        set_error("precision %d is not available for this entry point", prec);
+        return FK_ERR_UNSUPPORTED;
+    }
+    ctx.bind();
+    if (rep) {
+        memset(rep, 0, sizeof(*rep));
+        rep->precision_used = prec;
+    }
+    cudaStream_t s = ctx.stream;
+    const size_t kd = (size_t)k * d;
+    const TX *x = stage_in<TX>(ctx, BUF_X, x_in, (size_t)n * d);
+    TC *c = (TC *)ctx.get(BUF_C0, sizeof(TC) * kd);
+    TC *nc = (TC *)ctx.get(BUF_C1, sizeof(TC) * kd);
+    FK_CUDA(cudaMemcpyAsync(c, c_in, sizeof(TC) * kd, cudaMemcpyDefault, s));
+    int32_t *labels = (int32_t *)ctx.get(BUF_LABELS, sizeof(int32_t) * (size_t)n);
+    DevScalars *sc = (DevScalars *)ctx.get(BUF_SCALARS, sizeof(DevScalars));
+    FK_CUDA(cudaMemsetAsync(sc, 0, sizeof(DevScalars), s));
+    SortPlan plan = make_sort_plan(n, (int)k);
+    lloyd_iteration<TX, TC>(ctx, x, n, (int)d, c, (int)k, prec, nc, labels, sc, plan, true, rep, false);
+    read_scalars(ctx, sc);
+    accumulate_report(rep, *ctx.host_scalars, n);
+    copy_out<TC>(ctx, centers_out, nc, kd);
+    if (is_device_ptr(labels_out)) {
+        launch_labels_to_u64(labels, n, labels_out, s);
+    } else {
+        uint64_t *l64 = (uint64_t *)ctx.get(BUF_OUT, sizeof(uint64_t) * (size_t)n);
+        launch_labels_to_u64(labels, n, l64, s);
+        copy_out<uint64_t>(ctx, labels_out, l64, (size_t)n);
+    }
+    FK_CUDA(cudaStreamSynchronize(s));
+    *inertia_out = (TC)ctx.host_scalars->inertia;
+    *shift_out = shift_from_bits<TC>(ctx.host_scalars->shift_bits);
+    return FK_OK;
+}
+
+// -------------------------------------------------------------- predict --
+template <typename TX, typename TC>
+fk_status predict_impl(fk_ctx *ctxp, const TC *c_in, int64_t k, int64_t d_fit, const TX *x_in, int64_t n,
+                       int64_t d, int32_t prec, uint64_t *labels_out) {
+    Ctx &ctx = *reinterpret_cast<Ctx *>(ctxp);
+    if (d != d_fit) {
+        set_error("Shape mismatch in number of features must match fitted KMeans model: expected [%lld], got [%lld]",
+                  (long long)d_fit, (long long)d);
+        return FK_ERR_SHAPE_MISMATCH;
+    }
+    if (k <= 0 || n < 0) {
+        set_error("Invalid parameter: k must be >= 1 and n >= 0");
+        return FK_ERR_INVALID_PARAMETER;
+    }
+    if (n == 0) return FK_OK;
+    if (!x_in || !c_in || !labels_out) {
+        set_error("required pointer is NULL");
+        return FK_ERR_NULL_POINTER;
+    }
+    if (!precision_ok(prec, std::is_same<TC, double>::value)) {
+        set_error("precision %d is not available for this entry point", prec);
+        return FK_ERR_UNSUPPORTED;
+    }
+    ctx.bind();
+    cudaStream_t s = ctx.stream;
+    const TX *x = stage_in<TX>(ctx, BUF_X, x_in, (size_t)n * d);
+    const TC *c = stage_in<TC>(ctx, BUF_C0, c_in, (size_t)k * d);
+    int32_t *labels = (int32_t *)ctx.get(BUF_LABELS, sizeof(int32_t) * (size_t)n);
+    if (prec == FK_PRECISION_PLAIN) {
+        launch_assign_direct<TX, TC>(x, n, (int)d, c, (int)k, labels, nullptr, s);
+    } else {
+        if constexpr (std::is_same<TC, double>::value) {
+            DevScalars *sc = (DevScalars *)ctx.get(BUF_SCALARS, sizeof(DevScalars));
+            FK_CUDA(cudaMemsetAsync(sc, 0, sizeof(DevScalars), s));
+            run_assign_mixed<TX>(ctx, x, n, (int)d, c, (int)k, prec, labels, nullptr, sc, true);
+        }
+    }
+    if (is_device_ptr(labels_out)) {
+        launch_labels_to_u64(labels, n, labels_out, s);
+    } else {
+        uint64_t *l64 = (uint64_t *)ctx.get(BUF_OUT, sizeof(uint64_t) * (size_t)n);
+        launch_labels_to_u64(labels, n, l64, s);
+        copy_out<uint64_t>(ctx, labels_out, l64, (size_t)n);
+    }
+    FK_CUDA(cudaStreamSynchronize(s));
+    return FK_OK;
+}
+
+template <typename T>
+fk_status transform_impl(fk_ctx *ctxp, const T *c_in, int64_t k, int64_t d_fit, const T *x_in, int64_t n, int64_t d,
+                         T *out) {
+    Ctx &ctx = *reinterpret_cast<Ctx *>(ctxp);
+    if (d != d_fit) {
+        set_error("Shape mismatch in number of features must match fitted KMeans model: expected [%lld], got [%lld]",
+                  (long long)d_fit, (long long)d);
+        return FK_ERR_SHAPE_MISMATCH;
+    }
+    if (k <= 0 || n < 0) {
+        set_error("Invalid parameter: k must be >= 1 and n >= 0");
+        return FK_ERR_INVALID_PARAMETER;
+    }
+    if (n == 0) return FK_OK;
+    if (!x_in || !c_in || !out) {
+        set_error("required pointer is NULL");
+        return FK_ERR_NULL_POINTER;
+    }
+    ctx.bind();
+    cudaStream_t s = ctx.stream;
+    const T *x = stage_in<T>(ctx, BUF_X, x_in, (size_t)n * d);
+    const T *c = stage_in<T>(ctx, BUF_C0, c_in, (size_t)k * d);
+    T *o = is_device_ptr(out) ? out : (T *)ctx.get(BUF_OUT, sizeof(T) * (size_t)n * k);
+    launch_transform_direct<T>(x, n, (int)d, c, (int)k, o, s);
+    if (o != out) copy_out<T>(ctx, out, o, (size_t)n * k);
+    FK_CUDA(cudaStreamSynchronize(s));
+    return FK_OK;
+}
+
+template <typename T>
+fk_status kpp_impl(fk_ctx *ctxp, const T *x_in, int64_t n, int64_t d, int64_t k, const double *draws, int64_t n_draws,
+                   uint64_t seed, T *centers_out, int64_t *draws_used) {
+    Ctx &ctx = *reinterpret_cast<Ctx *>(ctxp);
+    if (k <= 0) {
+        set_error("Invalid parameter `n_clusters`: must be at least 1");
+        return FK_ERR_INVALID_PARAMETER;
+    }
+    if (n <= 0) {
+        set_error("Insufficient samples: need at least 1, got 0");
+        return FK_ERR_INSUFFICIENT_SAMPLES;
+    }
+    if (!x_in || !centers_out) {
+        set_error("required pointer is NULL");
+        return FK_ERR_NULL_POINTER;
+    }
+    ctx.bind();
+    cudaStream_t s = ctx.stream;
+    const T *x = stage_in<T>(ctx, BUF_X, x_in, (size_t)n * d);
+    std::vector<double> hd;
+    const double *dr;
+    if (draws) {
+        dr = stage_in<double>(ctx, BUF_DRAWS, draws, (size_t)n_draws);
+    } else {
+        n_draws = 1 + (k - 1) * kpp_trials_host(k);
+        hd.resize((size_t)n_draws);
+        host_draws(seed, n_draws, hd.data());
+        double *dd = (double *)ctx.get(BUF_DRAWS, sizeof(double) * (size_t)n_draws);
+        FK_CUDA(cudaMemcpyAsync(dd, hd.data(), sizeof(double) * (size_t)n_draws, cudaMemcpyHostToDevice, s));
+        dr = dd;
+    }
+    T *o = is_device_ptr(centers_out) ? centers_out : (T *)ctx.get(BUF_OUT, sizeof(T) * (size_t)k * d);
+    int64_t used = 0;
+    run_kmeanspp<T>(ctx, x, n, (int)d, (int)k, dr, n_draws, o, &used);
+    if (o != centers_out) copy_out<T>(ctx, centers_out, o, (size_t)k * d);
+    FK_CUDA(cudaStreamSynchronize(s));
+    if (draws_used) *draws_used = used;
+    return FK_OK;
+}
+
+template <typename F>
+fk_status guarded(fk_ctx *ctx, F &&f) {
+    if (!ctx) {
+        set_error("context is NULL");
+        return FK_ERR_NULL_POINTER;
+    }
+    try {
+        g_last_error.clear();
+        return f();
+    } catch (const Error &e) {
+        return e.code;
+    } catch (const std::bad_alloc &) {
+        set_error("host allocation failed");
+        return FK_ERR_OOM;
+    } catch (...) {
+        set_error("unexpected exception");
+        return FK_ERR_CUDA;
+    }
+}
+
+}  // namespace
+}  // namespace fk
+
+using fk::guarded;
+
+extern "C" {
+
+fk_status fk_ctx_create(fk_ctx **out, int32_t device, void *cuda_stream) {
+    if (!out) {
+        fk::set_error("out is NULL");
+        return FK_ERR_NULL_POINTER;
+    }
+    *out = nullptr;
+    fk::Ctx *c = new (std::nothrow) fk::Ctx();
+    if (!c) return FK_ERR_OOM;
+    c->device = device;
+    c->stream = (cudaStream_t)cuda_stream;
+    *out = reinterpret_cast<fk_ctx *>(c);
+    return FK_OK;
+}
+
+fk_status fk_ctx_destroy(fk_ctx *ctx) {
+    if (!ctx) return FK_OK;
+    fk::Ctx *c = reinterpret_cast<fk::Ctx *>(ctx);
+    if (!c->initialized) {
+        delete c;
+        return FK_OK;
+    }
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    for (int i = 0; i < fk::BUF_COUNT; i++)
+        if (c->buf[i]) cudaFree(c->buf[i]);
+    if (c->host_scalars) cudaFreeHost(c->host_scalars);
+    if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return FK_OK;
+}
+
+const char *fk_last_error_message(void) { return fk::g_last_error.c_str(); }
+
+const char *fk_version(void) { return "ferrokmeans-gb300 0.1.0 (sm_103a)"; }
+
+uint64_t fk_debug_launch_count(void) { return __atomic_load_n(&fk::g_launch_count, __ATOMIC_RELAXED); }
+
+void fk_kmeans_params_default(fk_kmeans_params *p, int64_t n_clusters) {
+    if (!p) return;
+    memset(p, 0, sizeof(*p));
+    p->n_clusters = n_clusters;
+    p->max_iter = 300;
+    p->tol = 1e-4;
+    p->n_init = 10;
+    p->has_random_state = 0;
+    p->precision = FK_PRECISION_PLAIN;
+}
+
+fk_status fk_draws_f64(uint64_t seed, int64_t count, double *out) {
+    if (!out && count > 0) return FK_ERR_NULL_POINTER;
+    fk::host_draws(seed, count, out);
+    return FK_OK;
+}
+
+fk_status fk_kmeans_fit_f64(fk_ctx *ctx, const double *x, int64_t n, int64_t d, const fk_kmeans_params *params,
+                            const double *init, double *c_out, uint64_t *l_out, double *in_out, int64_t *it_out,
+                            fk_fit_report *rep) {
+    if (!params) return FK_ERR_NULL_POINTER;
+    return guarded(ctx, [&] { return fk::fit_impl<double, double>(ctx, x, n, d, params, init, c_out, l_out, in_out, it_out, rep); });
+}
+
+fk_status fk_kmeans_fit_f32(fk_ctx *ctx, const float *x, int64_t n, int64_t d, const fk_kmeans_params *params,
+                            const float *init, float *c_out, uint64_t *l_out, float *in_out, int64_t *it_out,
+                            fk_fit_report *rep) {
+    if (!params) return FK_ERR_NULL_POINTER;
+    return guarded(ctx, [&] { return fk::fit_impl<float, float>(ctx, x, n, d, params, init, c_out, l_out, in_out, it_out, rep); });
+}
+
+fk_status fk_kmeans_fit_f32x64(fk_ctx *ctx, const float *x, int64_t n, int64_t d, const fk_kmeans_params *params,
+                               const double *init, double *c_out, uint64_t *l_out, double *in_out, int64_t *it_out,
+                               fk_fit_report *rep) {
+    if (!params) return FK_ERR_NULL_POINTER;
+    return guarded(ctx, [&] { return fk::fit_impl<float, double>(ctx, x, n, d, params, init, c_out, l_out, in_out, it_out, rep); });
+}
+
+fk_status fk_lloyd_step_f64(fk_ctx *ctx, const double *x, int64_t n, int64_t d, const double *c, int64_t k,
+                            int32_t prec, uint64_t *l, double *nc, double *in, double *sh, fk_fit_report *rep) {
+    return guarded(ctx, [&] { return fk::step_impl<double, double>(ctx, x, n, d, c, k, prec, l, nc, in, sh, rep); });
+}
+
+fk_status fk_lloyd_step_f32(fk_ctx *ctx, const float *x, int64_t n, int64_t d, const float *c, int64_t k,
+                            int32_t prec, uint64_t *l, float *nc, float *in, float *sh, fk_fit_report *rep) {
+    return guarded(ctx, [&] { return fk::step_impl<float, float>(ctx, x, n, d, c, k, prec, l, nc, in, sh, rep); });
+}
+
+fk_status fk_lloyd_step_f32x64(fk_ctx *ctx, const float *x, int64_t n, int64_t d, const double *c, int64_t k,
+                               int32_t prec, uint64_t *l, double *nc, double *in, double *sh, fk_fit_report *rep) {
+    return guarded(ctx, [&] { return fk::step_impl<float, double>(ctx, x, n, d, c, k, prec, l, nc, in, sh, rep); });
+}
+
+fk_status fk_kmeans_predict_f64(fk_ctx *ctx, const double *c, int64_t k, int64_t d_fit, const double *x, int64_t n,
+                                int64_t d, int32_t prec, uint64_t *l) {
+    return guarded(ctx, [&] { return fk::predict_impl<double, double>(ctx, c, k, d_fit, x, n, d, prec, l); });
+}
+
+fk_status fk_kmeans_predict_f32(fk_ctx *ctx, const float *c, int64_t k, int64_t d_fit, const float *x, int64_t n,
+                                int64_t d, int32_t prec, uint64_t *l) {
+    return guarded(ctx, [&] { return fk::predict_impl<float, float>(ctx, c, k, d_fit, x, n, d, prec, l); });
+}
+
+fk_status fk_kmeans_predict_f32x64(fk_ctx *ctx, const double *c, int64_t k, int64_t d_fit, const float *x, int64_t n,
+                                   int64_t d, int32_t prec, uint64_t *l) {
+    return guarded(ctx, [&] { return fk::predict_impl<float, double>(ctx, c, k, d_fit, x, n, d, prec, l); });
+}
+
+fk_status fk_kmeans_transform_f64(fk_ctx *ctx, const double *c, int64_t k, int64_t d_fit, const double *x, int64_t n,
+                                  int64_t d, double *out) {
+    return guarded(ctx, [&] { return fk::transform_impl<double>(ctx, c, k, d_fit, x, n, d, out); });
+}
+
+fk_status fk_kmeans_transform_f32(fk_ctx *ctx, const float *c, int64_t k, int64_t d_fit, const float *x, int64_t n,
+                                  int64_t d, float *out) {
+    return guarded(ctx, [&] { return fk::transform_impl<float>(ctx, c, k, d_fit, x, n, d, out); });
+}
+
+fk_status fk_kmeans_plus_plus_f64(fk_ctx *ctx, const double *x, int64_t n, int64_t d, int64_t k, const double *draws,
+                                  int64_t n_draws, uint64_t seed, double *out, int64_t *used) {
+    return guarded(ctx, [&] { return fk::kpp_impl<double>(ctx, x, n, d, k, draws, n_draws, seed, out, used); });
+}
+
+fk_status fk_kmeans_plus_plus_f32(fk_ctx *ctx, const float *x, int64_t n, int64_t d, int64_t k, const double *draws,
+                                  int64_t n_draws, uint64_t seed, float *out, int64_t *used) {
+    return guarded(ctx, [&] { return fk::kpp_impl<float>(ctx, x, n, d, k, draws, n_draws, seed, out, used); });
+}
+
+}  // extern "C"

@@ -1,0 +1,150 @@
+// fk_internal.cuh -- shared declarations of the KMeans Lloyd library.
+//
+// Layout in HBM (per context, grow-only buffers reused across calls):
+//   x        n*d   TX   row-major (TX = float or double), copied once per call
+//   centers  k*d   TC   current / next centres (double-buffered)
+//   labels   n     int32
+//   mind     n     TC   per-row minimum distance of the last assignment
+//   members  n     int32  row indices grouped by cluster (stable, row order)
+//   seg_hist k*S   int32  per-(cluster, segment) counts / offsets, S segments
+//   scalars         one fk_dev_scalars block read back once per iteration
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "../../include/ferrokmeans.h"
+
+namespace fk {
+
+// ----------------------------------------------------------------- errors --
+void set_error(const char *fmt, ...);
+
+struct Error {
+    fk_status code;
+};
+
+#define FK_CUDA(call)                                                                   \
+    do {                                                                                \
+        cudaError_t _e = (call);                                                        \
+        if (_e != cudaSuccess) {                                                        \
+            ::fk::set_error("%s failed: %s (%s:%d)", #call, cudaGetErrorString(_e),    \
+                            __FILE__, __LINE__);                                        \
+            throw ::fk::Error{_e == cudaErrorMemoryAllocation ? FK_ERR_OOM : FK_ERR_CUDA}; \
+        }                                                                               \
+    } while (0)
+
+// Count of kernel launches issued by this library (diagnostics).
+extern unsigned long long g_launch_count;
+#define FK_LAUNCH_CHECK()                      \
+    do {                                       \
+        FK_CUDA(cudaGetLastError());           \
+        __atomic_add_fetch(&::fk::g_launch_count, 1ULL, __ATOMIC_RELAXED); \
+    } while (0)
+
+[[noreturn]] inline void fail(fk_status code) { throw Error{code}; }
+
+// ------------------------------------------------------- device scalars --
+// Written by the reduction kernels, read back with one copy per iteration.
+struct DevScalars {
+    double inertia;                 // deterministic sum of the per-row minima
+    unsigned long long shift_bits;  // max_c ||new-old||^2 as raw bits (>= 0)
+    unsigned long long recheck_rows;
+    unsigned long long full_rows;
+    unsigned long long near_tie_rows;
+    unsigned long long flag_count;  // number of rows queued for re-check
+    unsigned long long full_count;  // number of rows queued for a full re-scan
+    unsigned long long error_word;  // nonzero: a bounded device wait gave up
+};
+
+// ---------------------------------------------------------------- context --
+enum BufSlot {
+    BUF_X = 0, BUF_XC, BUF_C0, BUF_C1, BUF_CBEST, BUF_LABELS, BUF_LBEST, BUF_MIND,
+    BUF_MEMBERS, BUF_SEGHIST, BUF_SCAN_TMP, BUF_COUNTS, BUF_PARTIAL, BUF_SCALARS,
+    BUF_OUT, BUF_OUT2, BUF_KPP0, BUF_KPP1, BUF_KPP2, BUF_KPP3, BUF_DRAWS,
+    BUF_XB, BUF_XNORM, BUF_CB, BUF_CAUX, BUF_TOP2, BUF_FLAGS, BUF_FULL, BUF_CF32,
+    BUF_COUNT
+};
+
+struct Ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    void *buf[BUF_COUNT] = {};
+    size_t cap[BUF_COUNT] = {};
+    DevScalars *host_scalars = nullptr;  // pinned
+    int num_sms = 0;
+    int cc_major = 0, cc_minor = 0;
+    void *tmap_fn = nullptr;             // cuTensorMapEncodeTiled entry point
+    bool initialized = false;
+    struct PendingTimer {
+        cudaEvent_t a, b;
+        double *acc;
+    };
+    std::vector<PendingTimer> pending;  // phase timers read after the loop
+
+    void *get(BufSlot s, size_t bytes);  // grow-only device buffer
+    void bind();                         // make the device current
+};
+
+// ----------------------------------------------------------- kernel APIs --
+// Direct-form assignment (kmeans.rs:295-352): labels + per-row minimum in TC.
+// TX is the storage type of x, TC the arithmetic type (float or double).
+template <typename TX, typename TC>
+void launch_assign_direct(const TX *x, int64_t n, int d, const TC *c, int k, int32_t *labels,
+                          TC *mind, cudaStream_t s);
+// Transform (kmeans.rs:568-617): out[i*k+c] = sqrt(direct distance).
+template <typename T>
+void launch_transform_direct(const T *x, int64_t n, int d, const T *c, int k, T *out,
+                             cudaStream_t s);
+// Deterministic fixed-order sum of v[0..n) in double into *out.
+template <typename T>
+void launch_sum_fixed(const T *v, int64_t n, double *partial, double *out, cudaStream_t s);
+int64_t sum_fixed_partials(int64_t n);
+
+// Stable counting sort of labels into members + per-cluster [start, end).
+struct SortPlan {
+    int64_t n = 0;
+    int k = 0;
+    int64_t seg_len = 0;
+    int64_t nseg = 0;
+    size_t scan_tmp_bytes = 0;
+};
+SortPlan make_sort_plan(int64_t n, int k);
+void launch_sort_by_cluster(const SortPlan &p, const int32_t *labels, int32_t *seg_hist,
+                            int32_t *scan_tmp, int32_t *members, cudaStream_t s);
+
+// recompute_centroids_into (kmeans.rs:358-401): per-cluster row-order sums in
+// TC, divide, empty -> keep old, then max shift into scalars->shift_bits.
+template <typename TX, typename TC>
+void launch_update_centroids(const SortPlan &p, const TX *x, int d, const int32_t *members,
+                             const int32_t *seg_hist, const TC *old_c, TC *new_c,
+                             DevScalars *scalars, cudaStream_t s);
+
+void launch_labels_to_u64(const int32_t *l, int64_t n, uint64_t *out, cudaStream_t s);
+template <typename TS, typename TD>
+void launch_convert(const TS *src, int64_t count, TD *dst, cudaStream_t s);
+
+// k-means++ (kmeans.rs:169-253).
+template <typename T>
+void run_kmeanspp(Ctx &ctx, const T *x, int64_t n, int d, int k, const double *draws_dev,
+                  int64_t n_draws, T *centers_out, int64_t *draws_used);
+
+// Mixed-precision assignment (BF16 tcgen05 / FP32 SIMT approximate pass,
+// FP64 exact re-check). Results identical to the FP64 direct form.
+template <typename TX>
+void run_assign_mixed(Ctx &ctx, const TX *x, int64_t n, int d, const double *c, int k,
+                      int precision, int32_t *labels, double *mind, DevScalars *scalars,
+                      bool x_changed);
+// Inertia of the mixed precisions: sum over clusters and features of
+// (x_ij - c_j)^2 over the cluster's rows, accumulated per (cluster, feature)
+// in compensated f32 and folded in f64 (relative error about 1e-7).
+template <typename TX>
+void launch_mixed_inertia(Ctx &ctx, const SortPlan &p, const TX *x, int d, const int32_t *members,
+                          const int32_t *seg_hist, const double *c, DevScalars *scalars);
+
+}  // namespace fk

@@ -1,0 +1,290 @@
+// fk_update.cu -- centroid update: stable counting sort by cluster, then one
+// sequential row-order sum per (cluster, feature) -- the exact summation order
+// of recompute_centroids_into (kmeans.rs:370-375) -- so the new centres are
+// bit-identical to the reference's for F = f32 and F = f64. Then divide, keep
+// the old centre of an empty cluster (kmeans.rs:378-386) and take the max
+// squared shift (kmeans.rs:389-400).
+//
+// Sort: rows are cut into segments of seg_len rows; one warp per segment
+// counts labels (shared-memory histogram), an exclusive scan over the
+// (cluster-major, segment-minor) count matrix gives every (cluster, segment)
+// its output offset, and a second pass scatters row indices in row order
+// (warp match + prefix popcount keeps equal labels in lane order). The
+// result: members[] lists each cluster's rows in increasing row index.
+#include "fk_internal.cuh"
+
+namespace fk {
+namespace {
+
+// --------------------------------------------------------------- scan --
+constexpr int SCAN_THREADS = 1024;
+constexpr int SCAN_ITEMS = 4;
+constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
+
+// Exclusive scan of one value per thread across the block; returns the
+// prefix, and the block total in *total.
+__device__ __forceinline__ int block_excl_scan(int v, int *sh, int *total) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int incl = v;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        int t = __shfl_up_sync(0xffffffffu, incl, off);
+        if (lane >= off) incl += t;
+    }
+    if (lane == 31) sh[w] = incl;
+    __syncthreads();
+    if (w == 0) {
+        int nw = blockDim.x >> 5;
+        int s = lane < nw ? sh[lane] : 0;
+        int si = s;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            int t = __shfl_up_sync(0xffffffffu, si, off);
+            if (lane >= off) si += t;
+        }
+        if (lane < nw) sh[lane] = si - s;  // exclusive warp offsets
+        if (lane == nw - 1) sh[32] = si;
+    }
+    __syncthreads();
+    int r = sh[w] + incl - v;
+    *total = sh[32];
+    __syncthreads();
+    return r;
+}
+
+__global__ void scan_reduce_kernel(const int32_t *__restrict__ a, int64_t m, int32_t *__restrict__ bsum) {
+    __shared__ int sh[33];
+    int64_t base = (int64_t)blockIdx.x * SCAN_TILE + (int64_t)threadIdx.x * SCAN_ITEMS;
+    int s = 0;
+#pragma unroll
+    for (int e = 0; e < SCAN_ITEMS; e++)
+        if (base + e < m) s += a[base + e];
+    int total;
+    block_excl_scan(s, sh, &total);
+    if (threadIdx.x == 0) bsum[blockIdx.x] = total;
+}
+
+__global__ void scan_top_kernel(int32_t *__restrict__ bsum, int64_t nb) {
+    __shared__ int sh[33];
+    int carry = 0;
+    for (int64_t b0 = 0; b0 < nb; b0 += SCAN_THREADS) {
+        int64_t i = b0 + threadIdx.x;
+        int v = i < nb ? bsum[i] : 0;
+        int total;
+        int ex = block_excl_scan(v, sh, &total);
+        if (i < nb) bsum[i] = carry + ex;
+        carry += total;
+    }
+}
+
+__global__ void scan_down_kernel(int32_t *__restrict__ a, int64_t m, const int32_t *__restrict__ bsum) {
+    __shared__ int sh[33];
+    int64_t base = (int64_t)blockIdx.x * SCAN_TILE + (int64_t)threadIdx.x * SCAN_ITEMS;
+    int v[SCAN_ITEMS];
+    int s = 0;
+#pragma unroll
+    for (int e = 0; e < SCAN_ITEMS; e++) {
+        v[e] = base + e < m ? a[base + e] : 0;
+        s += v[e];
+    }
+    int total;
+    int ex = block_excl_scan(s, sh, &total) + bsum[blockIdx.x];
+#pragma unroll
+    for (int e = 0; e < SCAN_ITEMS; e++) {
+        if (base + e < m) a[base + e] = ex;
+        ex += v[e];
+    }
+}
+
+// --------------------------------------------------------- segment sort --
+__global__ void seg_hist_kernel(const int32_t *__restrict__ labels, int64_t n, int k, int64_t seg_len,
+                                int64_t nseg, int32_t *__restrict__ hist) {
+    extern __shared__ int cnt[];
+    const int lane = threadIdx.x;
+    const int64_t s = blockIdx.x;
+    for (int c = lane; c < k; c += 32) cnt[c] = 0;
+    __syncwarp();
+    int64_t lo = s * seg_len, hi = min(n, lo + seg_len);
+    for (int64_t i = lo + lane; i < hi; i += 32) atomicAdd(&cnt[labels[i]], 1);
+    __syncwarp();
+    for (int c = lane; c < k; c += 32) hist[(int64_t)c * nseg + s] = cnt[c];
+}
+
+__global__ void seg_scatter_kernel(const int32_t *__restrict__ labels, int64_t n, int k, int64_t seg_len,
+                                   int64_t nseg, const int32_t *__restrict__ offs,
+                                   int32_t *__restrict__ members) {
+    extern __shared__ int cnt[];
+    const int lane = threadIdx.x;
+    const int64_t s = blockIdx.x;
+    for (int c = lane; c < k; c += 32) cnt[c] = offs[(int64_t)c * nseg + s];
+    __syncwarp();
+    const unsigned lt = (1u << lane) - 1u;
+    int64_t lo = s * seg_len, hi = min(n, lo + seg_len);
+    for (int64_t base = lo; base < hi; base += 32) {
+        int64_t i = base + lane;
+        bool active = i < hi;
+        unsigned act = __ballot_sync(0xffffffffu, active);
+        int rank = 0, l = 0;
+        unsigned peers = 0;
+        if (active) {
+            l = labels[i];
+            peers = __match_any_sync(act, l);
+            rank = __popc(peers & lt);
+            members[cnt[l] + rank] = (int32_t)i;
+        }
+        __syncwarp();
+        if (active && rank == 0) cnt[l] += __popc(peers);
+        __syncwarp();
+    }
+}
+
+// ------------------------------------------------------- centroid sums --
+template <typename T> struct UArith;
+template <> struct UArith<float> {
+    static __device__ __forceinline__ float add(float a, float b) { return __fadd_rn(a, b); }
+    static __device__ __forceinline__ float sub(float a, float b) { return __fsub_rn(a, b); }
+    static __device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
+    static __device__ __forceinline__ float div(float a, float b) { return __fdiv_rn(a, b); }
+};
+template <> struct UArith<double> {
+    static __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
+    static __device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
+    static __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
+    static __device__ __forceinline__ double div(double a, double b) { return __ddiv_rn(a, b); }
+};
+
+constexpr int UPD_R = 32;  // member rows loaded per batch
+
+// One block per (cluster, feature slab); thread j keeps the running sum of
+// feature j over the cluster's rows in row order.
+template <typename TX, typename TC>
+__global__ void centroid_sum_kernel(const TX *__restrict__ x, int d, int k, int64_t n,
+                                    const int32_t *__restrict__ members,
+                                    const int32_t *__restrict__ offs, int64_t nseg,
+                                    const TC *__restrict__ old_c, TC *__restrict__ new_c) {
+    using A = UArith<TC>;
+    __shared__ int32_t sidx[UPD_R];
+    const int c = blockIdx.x;
+    const int j = blockIdx.y * blockDim.x + threadIdx.x;
+    const int64_t start = offs[(int64_t)c * nseg];
+    const int64_t end = (c + 1 < k) ? (int64_t)offs[(int64_t)(c + 1) * nseg] : n;
+    TC s = TC(0);
+    for (int64_t base = start; base < end; base += UPD_R) {
+        const int cnt = (int)min((int64_t)UPD_R, end - base);
+        __syncthreads();
+        if (threadIdx.x < UPD_R && threadIdx.x < cnt) sidx[threadIdx.x] = members[base + threadIdx.x];
+        __syncthreads();
+        if (j < d) {
+            TX v[UPD_R];
+#pragma unroll
+            for (int r = 0; r < UPD_R; r++) v[r] = r < cnt ? x[(int64_t)sidx[r] * d + j] : TX(0);
+#pragma unroll
+            for (int r = 0; r < UPD_R; r++)
+                if (r < cnt) s = A::add(s, (TC)v[r]);
+        }
+    }
+    if (j < d) {
+        const int64_t cntc = end - start;
+        new_c[(int64_t)c * d + j] = cntc > 0 ? A::div(s, (TC)cntc) : old_c[(int64_t)c * d + j];
+    }
+}
+
+// squared_euclidean(new, old) per cluster, folded over j; max over clusters as
+// raw bits (non-negative IEEE values order like unsigned integers). NaN
+// shifts are skipped, as `shift > max_shift` is false for NaN.
+template <typename TC> struct ShiftBits;
+template <> struct ShiftBits<double> {
+    static __device__ __forceinline__ unsigned long long bits(double v) {
+        return (unsigned long long)__double_as_longlong(v);
+    }
+};
+template <> struct ShiftBits<float> {
+    static __device__ __forceinline__ unsigned long long bits(float v) {
+        return (unsigned long long)(unsigned)__float_as_uint(v);
+    }
+};
+
+template <typename TC>
+__global__ void max_shift_kernel(const TC *__restrict__ new_c, const TC *__restrict__ old_c, int k, int d,
+                                 unsigned long long *shift_bits) {
+    using A = UArith<TC>;
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= k) return;
+    TC acc = TC(0);
+    for (int j = 0; j < d; j++) {
+        TC t = A::sub(new_c[(int64_t)c * d + j], old_c[(int64_t)c * d + j]);
+        acc = A::add(acc, A::mul(t, t));
+    }
+    if (acc > TC(0)) atomicMax(shift_bits, ShiftBits<TC>::bits(acc));
+}
+
+void launch_scan(int32_t *a, int64_t m, int32_t *tmp, cudaStream_t s) {
+    int64_t nb = (m + SCAN_TILE - 1) / SCAN_TILE;
+    scan_reduce_kernel<<<(unsigned)nb, SCAN_THREADS, 0, s>>>(a, m, tmp);
+    FK_LAUNCH_CHECK();
+    scan_top_kernel<<<1, SCAN_THREADS, 0, s>>>(tmp, nb);
+    FK_LAUNCH_CHECK();
+    scan_down_kernel<<<(unsigned)nb, SCAN_THREADS, 0, s>>>(a, m, tmp);
+    FK_LAUNCH_CHECK();
+}
+
+}  // namespace
+
+SortPlan make_sort_plan(int64_t n, int k) {
+    SortPlan p;
+    p.n = n;
+    p.k = k;
+    int64_t L = 4 * (int64_t)k;
+    if (L < 1024) L = 1024;
+    // Keep k * nseg (the count matrix) within 64M entries.
+    while ((int64_t)k * ((n + L - 1) / L) > (int64_t)64 << 20) L *= 2;
+    L = (L + 31) / 32 * 32;
+    p.seg_len = L;
+    p.nseg = n > 0 ? (n + L - 1) / L : 1;
+    int64_t m = (int64_t)k * p.nseg;
+    p.scan_tmp_bytes = sizeof(int32_t) * (size_t)((m + SCAN_TILE - 1) / SCAN_TILE + 1);
+    return p;
+}
+
+static void set_smem_attr(const void *fn, size_t bytes) {
+    if (bytes > 48 * 1024) FK_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+}
+
+void launch_sort_by_cluster(const SortPlan &p, const int32_t *labels, int32_t *seg_hist, int32_t *scan_tmp,
+                            int32_t *members, cudaStream_t s) {
+    if (p.n == 0) return;
+    size_t smem = sizeof(int) * (size_t)p.k;
+    set_smem_attr((const void *)seg_hist_kernel, smem);
+    set_smem_attr((const void *)seg_scatter_kernel, smem);
+    seg_hist_kernel<<<(unsigned)p.nseg, 32, smem, s>>>(labels, p.n, p.k, p.seg_len, p.nseg, seg_hist);
+    FK_LAUNCH_CHECK();
+    launch_scan(seg_hist, (int64_t)p.k * p.nseg, scan_tmp, s);
+    seg_scatter_kernel<<<(unsigned)p.nseg, 32, smem, s>>>(labels, p.n, p.k, p.seg_len, p.nseg, seg_hist, members);
+    FK_LAUNCH_CHECK();
+}
+
+template <typename TX, typename TC>
+void launch_update_centroids(const SortPlan &p, const TX *x, int d, const int32_t *members,
+                             const int32_t *seg_hist, const TC *old_c, TC *new_c, DevScalars *scalars,
+                             cudaStream_t s) {
+    FK_CUDA(cudaMemsetAsync(&scalars->shift_bits, 0, sizeof(unsigned long long), s));
+    if (d == 0 || p.k == 0) return;
+    int threads = d >= 256 ? 256 : (d + 31) / 32 * 32;
+    dim3 grid((unsigned)p.k, (unsigned)((d + threads - 1) / threads));
+    centroid_sum_kernel<TX, TC><<<grid, threads, 0, s>>>(x, d, p.k, p.n, members, seg_hist, p.nseg, old_c, new_c);
+    FK_LAUNCH_CHECK();
+    max_shift_kernel<TC><<<(p.k + 127) / 128, 128, 0, s>>>(new_c, old_c, p.k, d, &scalars->shift_bits);
+    FK_LAUNCH_CHECK();
+}
+
+template void launch_update_centroids<double, double>(const SortPlan &, const double *, int, const int32_t *,
+                                                      const int32_t *, const double *, double *, DevScalars *,
+                                                      cudaStream_t);
+template void launch_update_centroids<float, float>(const SortPlan &, const float *, int, const int32_t *,
+                                                    const int32_t *, const float *, float *, DevScalars *,
+                                                    cudaStream_t);
+template void launch_update_centroids<float, double>(const SortPlan &, const float *, int, const int32_t *,
+                                                     const int32_t *, const double *, double *, DevScalars *,
+                                                     cudaStream_t);
+
+}  // namespace fk

@@ -1,0 +1,185 @@
+/*
+ * ferrokmeans.h -- C ABI of the GB300 (sm_103a) KMeans Lloyd library.
+ *
+ * This is the drop-in boundary for ferrolearn-cluster's KMeans hot path
+ * (ferrolearn-cluster/src/kmeans.rs). Every entry point below names the
+ * reference item it replaces. Plain pointers and sizes only; arrays are
+ * row-major and C-contiguous. Any input or output pointer may be host memory
+ * or device memory of the context's GPU: the library checks each pointer and
+ * copies only what lives on the host. Calls are synchronous (they return when
+ * the results are in the caller's buffers), like the Rust methods.
+ *
+ * Status codes map one-to-one onto ferrolearn_core::error::FerroError
+ * (ferrolearn-core/src/error.rs:30-91) plus CUDA-side failures; the message of
+ * the last failure on the calling thread is returned by fk_last_error_message.
+ */
+#ifndef FERROKMEANS_H
+#define FERROKMEANS_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum fk_status {
+    FK_OK = 0,
+    FK_ERR_INVALID_PARAMETER = 1,     /* FerroError::InvalidParameter     */
+    FK_ERR_INSUFFICIENT_SAMPLES = 2,  /* FerroError::InsufficientSamples  */
+    FK_ERR_SHAPE_MISMATCH = 3,        /* FerroError::ShapeMismatch        */
+    FK_ERR_NUMERICAL_INSTABILITY = 4, /* FerroError::NumericalInstability */
+    FK_ERR_CUDA = 10,                 /* a CUDA runtime call failed        */
+    FK_ERR_OOM = 11,                  /* device allocation failed          */
+    FK_ERR_TIMEOUT = 12,              /* a bounded device wait gave up     */
+    FK_ERR_UNSUPPORTED = 13,          /* shape/precision not supported     */
+    FK_ERR_NULL_POINTER = 14          /* a required pointer was NULL       */
+} fk_status;
+
+/* Arithmetic of the distance contraction. The result semantics are always
+ * those of the reference's KMeans<F> (F = f64 for the _f64/_f32x64 entry
+ * points, F = f32 for _f32):
+ *  FK_PRECISION_PLAIN       direct-form sum (x_j - c_j)^2 in F on CUDA cores,
+ *                           bit-identical to kmeans.rs:159-163.
+ *  FK_PRECISION_MIXED_BF16  BF16 tensor-core contraction (tcgen05, TMEM) with
+ *                           a derived per-row error bound; rows whose top-2
+ *                           margin is inside the bound are re-scored exactly
+ *                           in FP64 direct form. F = f64 only.
+ *  FK_PRECISION_MIXED_FP32  FP32 CUDA-core contraction with the same bound
+ *                           and FP64 re-check. F = f64 only.               */
+typedef enum fk_precision {
+    FK_PRECISION_PLAIN = 0,
+    FK_PRECISION_MIXED_BF16 = 1,
+    FK_PRECISION_MIXED_FP32 = 3
+} fk_precision;
+
+/* Hyper-parameters of KMeans<F> (kmeans.rs:55-68), plus the explicit-init
+ * hooks the reference lacks. */
+typedef struct fk_kmeans_params {
+    int64_t n_clusters;        /* KMeans::n_clusters                      */
+    int64_t max_iter;          /* KMeans::max_iter      (default 300)     */
+    double tol;                /* KMeans::tol           (default 1e-4)    */
+    int64_t n_init;            /* KMeans::n_init        (default 10)      */
+    uint64_t random_state;     /* KMeans::random_state when has_random_state */
+    int32_t has_random_state;  /* 0 = None (seed 0, kmeans.rs:451)        */
+    int32_t precision;         /* fk_precision                            */
+    /* Optional uniform [0,1) stream consumed by k-means++ in place of the
+     * per-run generator (one flat stream across runs). NULL = the library's
+     * splitmix64 stream seeded with random_state + run (see fk_draws_f64). */
+    const double *draws;
+    int64_t n_draws;
+    int32_t collect_timing;    /* 1 = fill the per-phase device times     */
+    int32_t reserved;
+} fk_kmeans_params;
+
+/* Diagnostics of one fit / step. All counters are summed over iterations. */
+typedef struct fk_fit_report {
+    int64_t best_run;          /* index of the run that was kept           */
+    int64_t iterations_total;  /* Lloyd iterations over all runs           */
+    int64_t rows_assigned;     /* rows x iterations                        */
+    int64_t rows_rechecked;    /* mixed: rows re-scored in FP64            */
+    int64_t rows_full_rescan;  /* mixed: rows re-scored against all k      */
+    int64_t near_tie_rows;     /* mixed: re-scored rows whose FP64 margin
+                                  is below 1e-12 relative                  */
+    double ms_init;            /* device time, k-means++                   */
+    double ms_assign;          /* device time, assignment (+ re-check)     */
+    double ms_update;          /* device time, sort + centroid update      */
+    double ms_total;           /* device time of the whole call            */
+    int32_t precision_used;
+    int32_t reserved;
+} fk_fit_report;
+
+typedef struct fk_ctx fk_ctx;
+
+/* Context: binds a GPU and a CUDA stream (cudaStream_t passed as void*;
+ * NULL = the context creates its own non-blocking stream) and caches device
+ * buffers across calls. One context per host thread. */
+fk_status fk_ctx_create(fk_ctx **out, int32_t device, void *cuda_stream);
+fk_status fk_ctx_destroy(fk_ctx *ctx);
+/* Message of the last failure on this thread ("" if none). */
+const char *fk_last_error_message(void);
+const char *fk_version(void);
+/* Diagnostics: number of kernel launches this library has issued so far in
+ * the process (all contexts). No reference counterpart. */
+uint64_t fk_debug_launch_count(void);
+
+/* KMeans::new(n_clusters) defaults (kmeans.rs:76-84). */
+void fk_kmeans_params_default(fk_kmeans_params *p, int64_t n_clusters);
+
+/* The library's uniform stream (splitmix64, (u64 >> 11) * 2^-53). Host-only,
+ * no GPU needed. k-means++ maps random_range(0..n) to min(floor(u*n), n-1). */
+fk_status fk_draws_f64(uint64_t seed, int64_t count, double *out);
+
+/* Fit::fit for KMeans<f64> (kmeans.rs:417-512). x: n*d; init_centers:
+ * n_init*k*d explicit initial centres per run, or NULL for k-means++ on the
+ * GPU. Outputs: centers_out k*d, labels_out n (usize), inertia_out, n_iter_out.
+ * labels/inertia are those of the last assignment of the kept run, against
+ * its pre-update centres, exactly as kmeans.rs:470-494. report may be NULL. */
+fk_status fk_kmeans_fit_f64(fk_ctx *ctx, const double *x, int64_t n, int64_t d,
+                            const fk_kmeans_params *params, const double *init_centers,
+                            double *centers_out, uint64_t *labels_out, double *inertia_out,
+                            int64_t *n_iter_out, fk_fit_report *report);
+
+/* Fit::fit for KMeans<f32>: every sum, centre and distance in f32. */
+fk_status fk_kmeans_fit_f32(fk_ctx *ctx, const float *x, int64_t n, int64_t d,
+                            const fk_kmeans_params *params, const float *init_centers,
+                            float *centers_out, uint64_t *labels_out, float *inertia_out,
+                            int64_t *n_iter_out, fk_fit_report *report);
+
+/* Fit::fit for KMeans<f64> on X stored as f32 (each x widened exactly to f64):
+ * identical results to fk_kmeans_fit_f64 on the widened matrix, with half the
+ * bytes resident. This is the entry point of the mixed precisions. */
+fk_status fk_kmeans_fit_f32x64(fk_ctx *ctx, const float *x, int64_t n, int64_t d,
+                               const fk_kmeans_params *params, const double *init_centers,
+                               double *centers_out, uint64_t *labels_out, double *inertia_out,
+                               int64_t *n_iter_out, fk_fit_report *report);
+
+/* One Lloyd iteration, the loop body of kmeans.rs:468-488: assignment against
+ * centers_in (labels_out, inertia_out), then recompute_centroids_into
+ * (centers_out; empty clusters keep their centre) and the max centre shift
+ * sqrt(max_c ||new-old||^2) (max_shift_out). report may be NULL. */
+fk_status fk_lloyd_step_f64(fk_ctx *ctx, const double *x, int64_t n, int64_t d,
+                            const double *centers_in, int64_t k, int32_t precision,
+                            uint64_t *labels_out, double *centers_out, double *inertia_out,
+                            double *max_shift_out, fk_fit_report *report);
+fk_status fk_lloyd_step_f32(fk_ctx *ctx, const float *x, int64_t n, int64_t d,
+                            const float *centers_in, int64_t k, int32_t precision,
+                            uint64_t *labels_out, float *centers_out, float *inertia_out,
+                            float *max_shift_out, fk_fit_report *report);
+fk_status fk_lloyd_step_f32x64(fk_ctx *ctx, const float *x, int64_t n, int64_t d,
+                               const double *centers_in, int64_t k, int32_t precision,
+                               uint64_t *labels_out, double *centers_out, double *inertia_out,
+                               double *max_shift_out, fk_fit_report *report);
+
+/* Predict::predict (kmeans.rs:538-552): nearest centre per row. d must equal
+ * d_fit, else FK_ERR_SHAPE_MISMATCH. */
+fk_status fk_kmeans_predict_f64(fk_ctx *ctx, const double *centers, int64_t k, int64_t d_fit,
+                                const double *x, int64_t n, int64_t d, int32_t precision,
+                                uint64_t *labels_out);
+fk_status fk_kmeans_predict_f32(fk_ctx *ctx, const float *centers, int64_t k, int64_t d_fit,
+                                const float *x, int64_t n, int64_t d, int32_t precision,
+                                uint64_t *labels_out);
+fk_status fk_kmeans_predict_f32x64(fk_ctx *ctx, const double *centers, int64_t k, int64_t d_fit,
+                                   const float *x, int64_t n, int64_t d, int32_t precision,
+                                   uint64_t *labels_out);
+
+/* Transform::transform (kmeans.rs:568-617): out[i*k+c] = sqrt(sum_j (x_ij-c_cj)^2). */
+fk_status fk_kmeans_transform_f64(fk_ctx *ctx, const double *centers, int64_t k, int64_t d_fit,
+                                  const double *x, int64_t n, int64_t d, double *out);
+fk_status fk_kmeans_transform_f32(fk_ctx *ctx, const float *centers, int64_t k, int64_t d_fit,
+                                  const float *x, int64_t n, int64_t d, float *out);
+
+/* kmeans_plus_plus (kmeans.rs:169-253) on the GPU: greedy k-means++ with
+ * 2+floor(ln k) trials per centre. draws: uniform stream (NULL = splitmix64
+ * seeded with seed). draws_used_out (nullable) receives the count consumed. */
+fk_status fk_kmeans_plus_plus_f64(fk_ctx *ctx, const double *x, int64_t n, int64_t d, int64_t k,
+                                  const double *draws, int64_t n_draws, uint64_t seed,
+                                  double *centers_out, int64_t *draws_used_out);
+fk_status fk_kmeans_plus_plus_f32(fk_ctx *ctx, const float *x, int64_t n, int64_t d, int64_t k,
+                                  const double *draws, int64_t n_draws, uint64_t seed,
+                                  float *centers_out, int64_t *draws_used_out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FERROKMEANS_H */

@@ -1,0 +1,300 @@
+/*
+ * kmeans_oracle.c -- CPU restatement of ferrolearn-cluster's KMeans Lloyd
+ * path, used ONLY as test infrastructure: the parity tests, the smoke check
+ * and the CPU-baseline leg of the benchmark call it as the checker. Nothing
+ * in the product library links or calls this file.
+ *
+ * It restates ferrolearn-cluster/src/kmeans.rs statement by statement:
+ *   squared_euclidean          kmeans.rs:159-163  (left fold from 0, no FMA)
+ *   kmeans_plus_plus           kmeans.rs:169-253  (uniform draws injected)
+ *   assign_clusters_into       kmeans.rs:279-291
+ *   nearest_center             kmeans.rs:295-309  (strict < from F::MAX)
+ *   assign_serial/_parallel    kmeans.rs:312-352
+ *   recompute_centroids_into   kmeans.rs:358-401  (row-order sums in F)
+ *   Fit::fit                   kmeans.rs:417-512  (n_init runs, best strict-<)
+ *   Predict::predict           kmeans.rs:538-552
+ *   Transform::transform       kmeans.rs:568-617
+ *
+ * It must be compiled with -ffp-contract=off so that a*b+c is never fused:
+ * Rust never contracts, and labels depend on the exact rounding of the
+ * direct-form distance.
+ *
+ * Random numbers: the reference draws from rand 0.9 StdRng (ChaCha12), which
+ * is not available here. The oracle instead consumes an explicit stream of
+ * uniform doubles in [0,1): random_range(0..n) becomes min(floor(u*n), n-1)
+ * and random::<f64>() becomes u. The GPU library consumes the same stream, so
+ * both sides start from identical inputs. The default stream is splitmix64
+ * (orc_draws_f64 below), identical to the library's host generator.
+ *
+ * The parallel assignment mirrors assign_parallel's chunking
+ * (chunk = max(n/threads, 64)) with OpenMP; the per-chunk inertia partials
+ * are folded left to right, which is one of the orders Rayon's reduce can
+ * produce. Below the PARALLEL_WORK_THRESHOLD the serial fold is used exactly.
+ */
+#include <float.h>
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define ORC_PARALLEL_WORK_THRESHOLD 100000 /* kmeans.rs:261 */
+
+enum { ORC_OK = 0, ORC_ERR_INVALID_PARAMETER = 1, ORC_ERR_INSUFFICIENT_SAMPLES = 2,
+       ORC_ERR_SHAPE_MISMATCH = 3, ORC_ERR_OOM = 11, ORC_ERR_NULL = 14 };
+
+/* ---------------------------------------------------------------- draws -- */
+/* splitmix64 stream: state advances by the golden gamma, output mixed. */
+typedef struct { uint64_t state; const double *inj; int64_t n_inj; int64_t pos; } orc_draws;
+
+static uint64_t orc_splitmix64(uint64_t *s) {
+    uint64_t z = (*s += 0x9E3779B97F4A7C15ULL);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    return z ^ (z >> 31);
+}
+
+static double orc_next(orc_draws *g) {
+    if (g->inj) {
+        double u = (g->pos < g->n_inj) ? g->inj[g->pos] : 0.0;
+        g->pos++;
+        return u;
+    }
+    g->pos++;
+    return (double)(orc_splitmix64(&g->state) >> 11) * (1.0 / 9007199254740992.0);
+}
+
+static int64_t orc_range(orc_draws *g, int64_t n) {
+    double u = orc_next(g);
+    int64_t i = (int64_t)floor(u * (double)n);
+    if (i < 0) i = 0;
+    if (i >= n) i = n - 1;
+    return i;
+}
+
+/* Exposed so tests can check that the library's host stream is identical. */
+void orc_draws_f64(uint64_t seed, int64_t count, double *out) {
+    orc_draws g = {seed, NULL, 0, 0};
+    for (int64_t i = 0; i < count; i++) out[i] = orc_next(&g);
+}
+
+/* ----------------------------------------------------- templated body -- */
+#define ORC_DEFINE(T, SUF, TMAX)                                                        \
+static T orc_sqeuc_##SUF(const T *a, const T *b, int64_t d) {                          \
+    T acc = (T)0;                                                                       \
+    for (int64_t j = 0; j < d; j++) { T t = a[j] - b[j]; acc = acc + t * t; }           \
+    return acc;                                                                         \
+}                                                                                       \
+                                                                                        \
+static void orc_nearest_##SUF(const T *row, const T *c, int64_t k, int64_t d,          \
+                              int64_t *lab, T *dist) {                                 \
+    int64_t best = 0; T bd = TMAX;                                                      \
+    for (int64_t q = 0; q < k; q++) {                                                   \
+        T v = orc_sqeuc_##SUF(row, c + q * d, d);                                       \
+        if (v < bd) { bd = v; best = q; }                                               \
+    }                                                                                   \
+    *lab = best; *dist = bd;                                                            \
+}                                                                                       \
+                                                                                        \
+/* assign_clusters_into (kmeans.rs:279-352): labels + inertia; mind optional */         \
+T orc_assign_##SUF(const T *x, int64_t n, int64_t d, const T *c, int64_t k,             \
+                   int64_t *labels, T *mind, int nthreads) {                           \
+    if (n * d < ORC_PARALLEL_WORK_THRESHOLD || nthreads <= 1) {                         \
+        T inertia = (T)0;                                                               \
+        for (int64_t i = 0; i < n; i++) {                                               \
+            T dist; orc_nearest_##SUF(x + i * d, c, k, d, &labels[i], &dist);           \
+            if (mind) mind[i] = dist;                                                   \
+            inertia = inertia + dist;                                                   \
+        }                                                                               \
+        return inertia;                                                                 \
+    }                                                                                   \
+    int64_t chunk = n / nthreads; if (chunk < 64) chunk = 64;                           \
+    int64_t nchunks = (n + chunk - 1) / chunk;                                          \
+    T *part = (T *)malloc(sizeof(T) * (size_t)nchunks);                                 \
+    _Pragma("omp parallel for schedule(dynamic,1) num_threads(nthreads)")               \
+    for (int64_t ch = 0; ch < nchunks; ch++) {                                          \
+        int64_t lo = ch * chunk, hi = lo + chunk < n ? lo + chunk : n;                  \
+        T loc = (T)0;                                                                   \
+        for (int64_t i = lo; i < hi; i++) {                                             \
+            T dist; orc_nearest_##SUF(x + i * d, c, k, d, &labels[i], &dist);           \
+            if (mind) mind[i] = dist;                                                   \
+            loc = loc + dist;                                                           \
+        }                                                                               \
+        part[ch] = loc;                                                                 \
+    }                                                                                   \
+    T inertia = (T)0;                                                                   \
+    for (int64_t ch = 0; ch < nchunks; ch++) inertia = inertia + part[ch];              \
+    free(part);                                                                         \
+    return inertia;                                                                     \
+}                                                                                       \
+                                                                                        \
+/* recompute_centroids_into (kmeans.rs:358-401); returns sqrt(max shift^2) */           \
+T orc_update_##SUF(const T *x, int64_t n, int64_t d, const int64_t *labels,             \
+                   const T *old_c, int64_t k, T *new_c, T *counts) {                    \
+    memset(new_c, 0, sizeof(T) * (size_t)(k * d));                                      \
+    for (int64_t q = 0; q < k; q++) counts[q] = (T)0;                                   \
+    for (int64_t i = 0; i < n; i++) {                                                   \
+        int64_t l = labels[i];                                                          \
+        counts[l] = counts[l] + (T)1;                                                   \
+        for (int64_t j = 0; j < d; j++) new_c[l * d + j] = new_c[l * d + j] + x[i * d + j]; \
+    }                                                                                   \
+    for (int64_t q = 0; q < k; q++) {                                                   \
+        if (counts[q] > (T)0) {                                                         \
+            for (int64_t j = 0; j < d; j++) new_c[q * d + j] = new_c[q * d + j] / counts[q]; \
+        } else {                                                                        \
+            memcpy(new_c + q * d, old_c + q * d, sizeof(T) * (size_t)d);               \
+        }                                                                               \
+    }                                                                                   \
+    T ms = (T)0;                                                                        \
+    for (int64_t q = 0; q < k; q++) {                                                   \
+        T s = orc_sqeuc_##SUF(new_c + q * d, old_c + q * d, d);                         \
+        if (s > ms) ms = s;                                                             \
+    }                                                                                   \
+    return orc_sqrt_##SUF(ms);                                                          \
+}                                                                                       \
+                                                                                        \
+/* kmeans_plus_plus (kmeans.rs:169-253) with an injected uniform stream */              \
+static void orc_kpp_##SUF(const T *x, int64_t n, int64_t d, int64_t k, orc_draws *g,   \
+                          T *centers) {                                                 \
+    memset(centers, 0, sizeof(T) * (size_t)(k * d));                                    \
+    if (n == 0) return;                                                                 \
+    int64_t first = orc_range(g, n);                                                    \
+    memcpy(centers, x + first * d, sizeof(T) * (size_t)d);                              \
+    if (k == 1) return;                                                                 \
+    T *mind = (T *)malloc(sizeof(T) * (size_t)n);                                       \
+    T *nd = (T *)malloc(sizeof(T) * (size_t)n);                                         \
+    T *bestd = (T *)malloc(sizeof(T) * (size_t)n);                                      \
+    for (int64_t i = 0; i < n; i++) mind[i] = orc_sqeuc_##SUF(x + i * d, centers, d);   \
+    int64_t n_trials = 2 + (int64_t)floor(log((double)k));                              \
+    if (n_trials < 1) n_trials = 1;                                                     \
+    for (int64_t c = 1; c < k; c++) {                                                   \
+        T total = (T)0;                                                                 \
+        for (int64_t i = 0; i < n; i++) total = total + mind[i];                        \
+        if (total <= (T)0) {                                                            \
+            int64_t idx = orc_range(g, n);                                              \
+            memcpy(centers + c * d, x + idx * d, sizeof(T) * (size_t)d);                \
+            continue;                                                                   \
+        }                                                                               \
+        int64_t best_cand = 0; int have = 0; T best_pot = (T)0;                         \
+        for (int64_t t = 0; t < n_trials; t++) {                                        \
+            T thr = (T)orc_next(g) * total;                                             \
+            T cum = (T)0; int64_t cand = n - 1;                                         \
+            for (int64_t i = 0; i < n; i++) {                                           \
+                cum = cum + mind[i];                                                    \
+                if (cum >= thr) { cand = i; break; }                                    \
+            }                                                                           \
+            T pot = (T)0;                                                               \
+            for (int64_t i = 0; i < n; i++) {                                           \
+                T v = orc_sqeuc_##SUF(x + i * d, x + cand * d, d);                      \
+                nd[i] = v < mind[i] ? v : mind[i];                                      \
+                pot = pot + nd[i];                                                      \
+            }                                                                           \
+            if (!have || pot < best_pot) {                                              \
+                have = 1; best_pot = pot; best_cand = cand;                             \
+                T *tmp = bestd; bestd = nd; nd = tmp;                                   \
+            }                                                                           \
+        }                                                                               \
+        memcpy(centers + c * d, x + best_cand * d, sizeof(T) * (size_t)d);             \
+        { T *tmp = mind; mind = bestd; bestd = tmp; }                                   \
+    }                                                                                   \
+    free(mind); free(nd); free(bestd);                                                  \
+}                                                                                       \
+                                                                                        \
+int orc_kmeanspp_##SUF(const T *x, int64_t n, int64_t d, int64_t k,                     \
+                       const double *draws, int64_t n_draws, uint64_t seed,            \
+                       T *centers, int64_t *draws_used) {                               \
+    if (!x || !centers) return ORC_ERR_NULL;                                            \
+    orc_draws g = {seed, draws, n_draws, 0};                                            \
+    orc_kpp_##SUF(x, n, d, k, &g, centers);                                             \
+    if (draws_used) *draws_used = g.pos;                                                \
+    return ORC_OK;                                                                      \
+}                                                                                       \
+                                                                                        \
+/* One Lloyd iteration exactly as the body of kmeans.rs:468-488 */                      \
+int orc_lloyd_step_##SUF(const T *x, int64_t n, int64_t d, const T *centers, int64_t k, \
+                         int64_t *labels, T *new_c, T *inertia, T *max_shift,          \
+                         int nthreads) {                                                \
+    T *counts = (T *)malloc(sizeof(T) * (size_t)k);                                     \
+    if (!counts) return ORC_ERR_OOM;                                                    \
+    *inertia = orc_assign_##SUF(x, n, d, centers, k, labels, NULL, nthreads);           \
+    *max_shift = orc_update_##SUF(x, n, d, labels, centers, k, new_c, counts);          \
+    free(counts);                                                                       \
+    return ORC_OK;                                                                      \
+}                                                                                       \
+                                                                                        \
+/* Fit::fit (kmeans.rs:417-512). init: n_init*k*d centers, or NULL for k-means++ */     \
+int orc_fit_##SUF(const T *x, int64_t n, int64_t d, int64_t k, int64_t max_iter,        \
+                  T tol, int64_t n_init, const T *init, const double *draws,           \
+                  int64_t n_draws, uint64_t seed, T *out_c, int64_t *out_labels,        \
+                  T *out_inertia, int64_t *out_n_iter, int64_t *out_best_run,          \
+                  int nthreads) {                                                       \
+    if (k == 0) return ORC_ERR_INVALID_PARAMETER;                                       \
+    if (n == 0 || n < k) return ORC_ERR_INSUFFICIENT_SAMPLES;                           \
+    if (n_init == 0) return ORC_ERR_INVALID_PARAMETER;                                  \
+    T *c = (T *)malloc(sizeof(T) * (size_t)(k * d));                                    \
+    T *nc = (T *)malloc(sizeof(T) * (size_t)(k * d));                                   \
+    T *counts = (T *)malloc(sizeof(T) * (size_t)k);                                     \
+    int64_t *lab = (int64_t *)calloc((size_t)n, sizeof(int64_t));                       \
+    if (!c || !nc || !counts || !lab) return ORC_ERR_OOM;                               \
+    int have = 0; T best_in = TMAX;                                                     \
+    orc_draws g = {0, draws, n_draws, 0};                                               \
+    for (int64_t run = 0; run < n_init; run++) {                                        \
+        if (init) {                                                                     \
+            memcpy(c, init + run * k * d, sizeof(T) * (size_t)(k * d));               \
+        } else {                                                                        \
+            if (!draws) { g.state = seed + (uint64_t)run; g.pos = 0; }                  \
+            orc_kpp_##SUF(x, n, d, k, &g, c);                                           \
+        }                                                                               \
+        int64_t n_iter = 0; T inertia = TMAX;                                           \
+        for (int64_t it = 0; it < max_iter; it++) {                                     \
+            inertia = orc_assign_##SUF(x, n, d, c, k, lab, NULL, nthreads);             \
+            T ms = orc_update_##SUF(x, n, d, lab, c, k, nc, counts);                    \
+            T *tmp = c; c = nc; nc = tmp;                                               \
+            n_iter = it + 1;                                                            \
+            if (ms < tol) break;                                                        \
+        }                                                                               \
+        if (!have || inertia < best_in) {                                               \
+            have = 1; best_in = inertia;                                                \
+            memcpy(out_c, c, sizeof(T) * (size_t)(k * d));                              \
+            memcpy(out_labels, lab, sizeof(int64_t) * (size_t)n);                       \
+            *out_inertia = inertia; *out_n_iter = n_iter;                               \
+            if (out_best_run) *out_best_run = run;                                      \
+        }                                                                               \
+    }                                                                                   \
+    free(c); free(nc); free(counts); free(lab);                                         \
+    return ORC_OK;                                                                      \
+}                                                                                       \
+                                                                                        \
+/* Predict::predict (kmeans.rs:538-552) */                                              \
+int orc_predict_##SUF(const T *c, int64_t k, int64_t d_fit, const T *x, int64_t n,      \
+                      int64_t d, int64_t *labels, int nthreads) {                       \
+    if (d != d_fit) return ORC_ERR_SHAPE_MISMATCH;                                      \
+    orc_assign_##SUF(x, n, d, c, k, labels, NULL, nthreads);                            \
+    return ORC_OK;                                                                      \
+}                                                                                       \
+                                                                                        \
+/* Transform::transform (kmeans.rs:568-617) */                                          \
+int orc_transform_##SUF(const T *c, int64_t k, int64_t d_fit, const T *x, int64_t n,    \
+                        int64_t d, T *out, int nthreads) {                              \
+    if (d != d_fit) return ORC_ERR_SHAPE_MISMATCH;                                      \
+    _Pragma("omp parallel for schedule(static) num_threads(nthreads)")                  \
+    for (int64_t i = 0; i < n; i++)                                                     \
+        for (int64_t q = 0; q < k; q++)                                                 \
+            out[i * k + q] = orc_sqrt_##SUF(orc_sqeuc_##SUF(x + i * d, c + q * d, d));  \
+    return ORC_OK;                                                                      \
+}
+
+static double orc_sqrt_f64(double v) { return sqrt(v); }
+static float orc_sqrt_f32(float v) { return sqrtf(v); }
+
+ORC_DEFINE(double, f64, DBL_MAX)
+ORC_DEFINE(float, f32, FLT_MAX)
+
+/* Direct-form FP64 distance from an f32 row to an f64 centre, used for the
+ * "X stored f32, oracle in f64" parity cases: the row is widened exactly. */
+int orc_widen_f32(const float *x, int64_t count, double *out) {
+    for (int64_t i = 0; i < count; i++) out[i] = (double)x[i];
+    return ORC_OK;
+}

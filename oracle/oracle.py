@@ -1,0 +1,159 @@
+"""ctypes wrapper around the CPU oracle (oracle/kmeans_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke() and
+by bench.py's CPU-baseline leg, always as the checker. The product library
+(ferrolearn_gb300) never imports this module.
+
+Each function restates one item of ferrolearn-cluster/src/kmeans.rs (the C
+file cites the lines). Arrays are numpy, row-major, f64 or f32.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _build.build()
+        _lib = C.CDLL(path)
+        i64, u64, p = C.c_int64, C.c_uint64, C.c_void_p
+        for suf, T in (("f64", C.c_double), ("f32", C.c_float)):
+            getattr(_lib, f"orc_assign_{suf}").argtypes = [p, i64, i64, p, i64, p, p, C.c_int]
+            getattr(_lib, f"orc_assign_{suf}").restype = T
+            getattr(_lib, f"orc_update_{suf}").argtypes = [p, i64, i64, p, p, i64, p, p]
+            getattr(_lib, f"orc_update_{suf}").restype = T
+            getattr(_lib, f"orc_kmeanspp_{suf}").argtypes = [p, i64, i64, i64, p, i64, u64, p, p]
+            getattr(_lib, f"orc_lloyd_step_{suf}").argtypes = [p, i64, i64, p, i64, p, p, p, p, C.c_int]
+            getattr(_lib, f"orc_fit_{suf}").argtypes = [p, i64, i64, i64, i64, T, i64, p, p, i64, u64,
+                                                        p, p, p, p, p, C.c_int]
+            getattr(_lib, f"orc_predict_{suf}").argtypes = [p, i64, i64, p, i64, i64, p, C.c_int]
+            getattr(_lib, f"orc_transform_{suf}").argtypes = [p, i64, i64, p, i64, i64, p, C.c_int]
+        _lib.orc_draws_f64.argtypes = [u64, i64, p]
+        _lib.orc_draws_f64.restype = None
+    return _lib
+
+
+def _threads(nthreads):
+    if nthreads is None:
+        return os.cpu_count() or 1
+    return int(nthreads)
+
+
+def _suffix(dtype):
+    if dtype == np.float64:
+        return "f64", C.c_double
+    if dtype == np.float32:
+        return "f32", C.c_float
+    raise TypeError(f"oracle supports float64/float32, got {dtype}")
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+class OracleError(Exception):
+    def __init__(self, code):
+        super().__init__(f"oracle status {code}")
+        self.code = code
+
+
+def draws(seed, count):
+    out = np.empty(count, dtype=np.float64)
+    lib().orc_draws_f64(seed, count, _ptr(out))
+    return out
+
+
+def assign(x, centers, nthreads=None):
+    """assign_clusters_into (kmeans.rs:279-352) -> (labels int64, inertia)."""
+    x = np.ascontiguousarray(x)
+    c = np.ascontiguousarray(centers, dtype=x.dtype)
+    suf, _ = _suffix(x.dtype)
+    n, d = x.shape
+    labels = np.empty(n, dtype=np.int64)
+    inertia = getattr(lib(), f"orc_assign_{suf}")(_ptr(x), n, d, _ptr(c), c.shape[0], _ptr(labels), None,
+                                                  _threads(nthreads))
+    return labels, inertia
+
+
+def lloyd_step(x, centers, nthreads=None):
+    """One iteration of kmeans.rs:468-488: (labels, new_centers, inertia, max_shift)."""
+    x = np.ascontiguousarray(x)
+    c = np.ascontiguousarray(centers, dtype=x.dtype)
+    suf, T = _suffix(x.dtype)
+    n, d = x.shape
+    k = c.shape[0]
+    labels = np.empty(n, dtype=np.int64)
+    nc = np.empty_like(c)
+    inertia, shift = T(), T()
+    rc = getattr(lib(), f"orc_lloyd_step_{suf}")(_ptr(x), n, d, _ptr(c), k, _ptr(labels), _ptr(nc),
+                                                 C.byref(inertia), C.byref(shift), _threads(nthreads))
+    if rc:
+        raise OracleError(rc)
+    return labels, nc, inertia.value, shift.value
+
+
+def kmeanspp(x, k, draws_arr=None, seed=0):
+    """kmeans_plus_plus (kmeans.rs:169-253) -> (centers, draws consumed)."""
+    x = np.ascontiguousarray(x)
+    suf, _ = _suffix(x.dtype)
+    n, d = x.shape
+    out = np.empty((k, d), dtype=x.dtype)
+    used = C.c_int64()
+    dr = None if draws_arr is None else np.ascontiguousarray(draws_arr, dtype=np.float64)
+    rc = getattr(lib(), f"orc_kmeanspp_{suf}")(_ptr(x), n, d, k, _ptr(dr), 0 if dr is None else dr.size,
+                                               seed, _ptr(out), C.byref(used))
+    if rc:
+        raise OracleError(rc)
+    return out, used.value
+
+
+def fit(x, k, max_iter=300, tol=1e-4, n_init=10, init=None, draws_arr=None, seed=0, nthreads=None):
+    """Fit::fit (kmeans.rs:417-512) -> dict(centers, labels, inertia, n_iter, best_run)."""
+    x = np.ascontiguousarray(x)
+    suf, T = _suffix(x.dtype)
+    n, d = x.shape if x.ndim == 2 else (0, 0)
+    out_c = np.empty((max(k, 0), d), dtype=x.dtype)
+    out_l = np.empty(n, dtype=np.int64)
+    inertia, n_iter, best = T(), C.c_int64(), C.c_int64()
+    ini = None if init is None else np.ascontiguousarray(init, dtype=x.dtype)
+    dr = None if draws_arr is None else np.ascontiguousarray(draws_arr, dtype=np.float64)
+    rc = getattr(lib(), f"orc_fit_{suf}")(_ptr(x), n, d, k, max_iter, T(tol), n_init, _ptr(ini), _ptr(dr),
+                                          0 if dr is None else dr.size, seed, _ptr(out_c), _ptr(out_l),
+                                          C.byref(inertia), C.byref(n_iter), C.byref(best),
+                                          _threads(nthreads))
+    if rc:
+        raise OracleError(rc)
+    return dict(centers=out_c, labels=out_l, inertia=inertia.value, n_iter=n_iter.value,
+                best_run=best.value)
+
+
+def predict(centers, x, nthreads=None):
+    x = np.ascontiguousarray(x)
+    c = np.ascontiguousarray(centers, dtype=x.dtype)
+    suf, _ = _suffix(x.dtype)
+    n, d = x.shape
+    labels = np.empty(n, dtype=np.int64)
+    rc = getattr(lib(), f"orc_predict_{suf}")(_ptr(c), c.shape[0], c.shape[1], _ptr(x), n, d, _ptr(labels),
+                                              _threads(nthreads))
+    if rc:
+        raise OracleError(rc)
+    return labels
+
+
+def transform(centers, x, nthreads=None):
+    x = np.ascontiguousarray(x)
+    c = np.ascontiguousarray(centers, dtype=x.dtype)
+    suf, _ = _suffix(x.dtype)
+    n, d = x.shape
+    out = np.empty((n, c.shape[0]), dtype=x.dtype)
+    rc = getattr(lib(), f"orc_transform_{suf}")(_ptr(c), c.shape[0], c.shape[1], _ptr(x), n, d, _ptr(out),
+                                                _threads(nthreads))
+    if rc:
+        raise OracleError(rc)
+    return out

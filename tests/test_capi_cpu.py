@@ -1,0 +1,85 @@
+"""C-ABI checks that need no GPU: the library builds and loads, exports every
+symbol include/ferrokmeans.h declares, maps argument errors onto the
+FerroError variants in the reference's validation order (kmeans.rs:421-449,
+542-548, 572-578), and its host-side uniform stream equals the oracle's."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+import ferrolearn_gb300 as F
+from ferrolearn_gb300 import _native
+from oracle import oracle as O
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _header_symbols():
+    syms = set()
+    for name in os.listdir(os.path.join(ROOT, "include")):
+        if name.endswith(".h"):
+            text = open(os.path.join(ROOT, "include", name)).read()
+            text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+            syms |= set(re.findall(r"\b(fk_[a-z0-9_]+)\s*\(", text))
+    return syms
+
+
+def test_library_exports_every_declared_symbol():
+    lib = _native.lib()
+    syms = _header_symbols()
+    assert len(syms) >= 19
+    missing = [s for s in sorted(syms) if not hasattr(lib, s)]
+    assert not missing, missing
+    assert set(_native.EXPORTS) <= syms
+
+
+def test_version_and_defaults():
+    lib = _native.lib()
+    assert b"sm_103a" in lib.fk_version()
+    p = _native.KMeansParams()
+    lib.fk_kmeans_params_default(C.byref(p), 7)
+    # KMeans::new defaults, kmeans.rs:76-84
+    assert (p.n_clusters, p.max_iter, p.tol, p.n_init, p.has_random_state) == (7, 300, 1e-4, 10, 0)
+
+
+def test_draw_stream_matches_oracle():
+    assert np.array_equal(F.draws(123, 1000), O.draws(123, 1000))
+    u = F.draws(0, 10000)
+    assert (u >= 0).all() and (u < 1).all()
+
+
+@pytest.mark.parametrize("k,x,exc", [
+    (0, np.ones((3, 2)), F.InvalidParameter),              # kmeans.rs:421-426
+    (3, np.zeros((0, 2)), F.InsufficientSamples),          # kmeans.rs:428-434
+    (5, np.ones((2, 2)), F.InsufficientSamples),           # kmeans.rs:436-442
+])
+def test_fit_validation_errors(k, x, exc):
+    for dtype in ("f64", "f32", "f32x64"):
+        with pytest.raises(exc):
+            F.KMeans(k, dtype=dtype).fit(x)
+
+
+def test_fit_n_init_zero():
+    with pytest.raises(F.InvalidParameter):  # kmeans.rs:444-449
+        F.KMeans(2).with_n_init(0).fit(np.ones((4, 2)))
+
+
+def test_zero_clusters_checked_before_samples():
+    # n_clusters is validated first even when the data is also empty.
+    with pytest.raises(F.InvalidParameter):
+        F.KMeans(0).fit(np.zeros((0, 2)))
+
+
+def test_predict_transform_shape_mismatch():
+    fitted = F.FittedKMeans(np.ones((2, 2)), np.zeros(4, dtype=np.int64), 0.0, 1, "f64")
+    with pytest.raises(F.ShapeMismatch):
+        fitted.predict(np.ones((2, 3)))
+    with pytest.raises(F.ShapeMismatch):
+        fitted.transform(np.ones((2, 3)))
+
+
+def test_mixed_precision_rejected_for_f32_semantics():
+    with pytest.raises(F.Unsupported):
+        F.KMeans(2, dtype="f32").with_precision("bf16").fit(np.ones((4, 2), dtype=np.float32))
