@@ -22,7 +22,7 @@ EXPORTS = [
     "fk_lloyd_step_f64", "fk_lloyd_step_f32", "fk_lloyd_step_f32x64",
     "fk_kmeans_predict_f64", "fk_kmeans_predict_f32", "fk_kmeans_predict_f32x64",
     "fk_kmeans_transform_f64", "fk_kmeans_transform_f32",
-    "fk_kmeans_plus_plus_f64", "fk_kmeans_plus_plus_f32",
+    "fk_kmeans_plus_plus_f64", "fk_kmeans_plus_plus_f32", "fk_debug_tc_probe",
 ]
 
 
@@ -96,6 +96,8 @@ def _declare(lib):
         f = getattr(lib, f"fk_kmeans_plus_plus_{suf}")
         f.argtypes = [p, p, i64, i64, i64, p, i64, u64, p, p]
         f.restype = st
+    lib.fk_debug_tc_probe.argtypes = [p, p, i64, i64, p, i64, p, p, p, p, p, p]
+    lib.fk_debug_tc_probe.restype = st
 
 
 def lib():

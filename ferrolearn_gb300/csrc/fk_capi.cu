@@ -208,11 +208,12 @@ void lloyd_iteration(Ctx &ctx, const TX *x, int64_t n, int d, const TC *c, int k
     {
         Timer t(timing, ctx, rep ? &rep->ms_update : nullptr);
         launch_sort_by_cluster(plan, labels, seg, tmp, members, s);
-        launch_update_centroids<TX, TC>(plan, x, d, members, seg, c, nc, sc, s);
-        if (prec != FK_PRECISION_PLAIN) {
-            if constexpr (std::is_same<TC, double>::value) {
-                launch_mixed_inertia<TX>(ctx, plan, x, d, members, seg, c, sc);
-            }
+        if (prec == FK_PRECISION_PLAIN) {
+            launch_update_centroids<TX, TC>(plan, x, d, members, seg, c, nc, sc, s);
+        } else {
+            double *part = (double *)ctx.get(BUF_OUT2, sizeof(double) * (size_t)plan.k * d + 64);
+            launch_update_centroids<TX, TC>(plan, x, d, members, seg, c, nc, sc, s, part);
+            launch_mixed_inertia(ctx, part, (int64_t)plan.k * d, sc);
         }
     }
 }
@@ -723,6 +724,16 @@ fk_status fk_kmeans_transform_f32(fk_ctx *ctx, const float *c, int64_t k, int64_
 fk_status fk_kmeans_plus_plus_f64(fk_ctx *ctx, const double *x, int64_t n, int64_t d, int64_t k, const double *draws,
                                   int64_t n_draws, uint64_t seed, double *out, int64_t *used) {
     return guarded(ctx, [&] { return fk::kpp_impl<double>(ctx, x, n, d, k, draws, n_draws, seed, out, used); });
+}
+
+fk_status fk_debug_tc_probe(fk_ctx *ctx, const float *x_dev, int64_t n, int64_t d, const double *c_dev, int64_t k,
+                             float *dump, uint16_t *xb, uint16_t *cb, uint16_t *aug, void *top, int32_t *plan) {
+    return guarded(ctx, [&] {
+        fk::Ctx &c = *reinterpret_cast<fk::Ctx *>(ctx);
+        c.bind();
+        fk::debug_tc_probe(c, x_dev, n, (int)d, c_dev, (int)k, dump, xb, cb, aug, (fk::Top2 *)top, plan);
+        return FK_OK;
+    });
 }
 
 fk_status fk_kmeans_plus_plus_f32(fk_ctx *ctx, const float *x, int64_t n, int64_t d, int64_t k, const double *draws,

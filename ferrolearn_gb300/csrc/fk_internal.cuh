@@ -61,6 +61,48 @@ struct DevScalars {
     unsigned long long error_word;  // nonzero: a bounded device wait gave up
 };
 
+// --------------------------------------------------- mixed precision --
+// Bound ingredients of one assignment (floats rounded up; maxima via atomics).
+struct MixedStats {
+    float xn_max;  // max_i ||xh_i||           (set once per X)
+    float cn_max;  // max_c ||c' ||            (per iteration from here on)
+    float ec_max;  // max_c ||c' - ch||
+    float ch_max;  // max_c ||ch||
+    float h_max;   // max_c ||c'||^2 / 2
+    float co_max;  // max_c ||c||  (uncentred, for the FP64 rounding term)
+    float big;     // BIG of this iteration
+    float pad;
+};
+
+// Best and second-best score of one row over one slice of the centres.
+struct alignas(16) Top2 {
+    float v1, v2;
+    int i1, i2;
+};
+
+// Launch plan of the tensor-core assignment (fk_tc.cu).
+struct MixedPlan {
+    int64_t n = -1;
+    int d = -1, k = -1;
+    int d_pad = 0;        // d rounded up to a multiple of 64 (one 128-byte swizzle atom)
+    int k_pad = 0;        // parts * kp
+    int parts = 1;        // centre slices, one per CTA group
+    int kp = 0;           // centres per slice (multiple of 256)
+    int nblocks = 0;      // kp / 256 accumulator blocks
+    int64_t tiles = 0;    // ceil(n / 128)
+    int ctas_per_part = 0;
+    int grid = 0;
+    size_t smem = 0;
+    const void *x = nullptr;
+    double mu_norm = 0.0;
+    const void *tm_x_ptr = nullptr, *tm_c_ptr = nullptr, *tm_aug_ptr = nullptr;
+    alignas(64) unsigned char tm_x[128];
+    alignas(64) unsigned char tm_c[128];
+    alignas(64) unsigned char tm_aug[128];
+    alignas(64) unsigned char tm_ones[128];
+    void *ones = nullptr;  // 128 x 16 BF16 rows of [1,1,1,0,...] (device)
+};
+
 // ---------------------------------------------------------------- context --
 enum BufSlot {
     BUF_X = 0, BUF_XC, BUF_C0, BUF_C1, BUF_CBEST, BUF_LABELS, BUF_LBEST, BUF_MIND,
@@ -86,6 +128,7 @@ struct Ctx {
         double *acc;
     };
     std::vector<PendingTimer> pending;  // phase timers read after the loop
+    MixedPlan mixed;
 
     void *get(BufSlot s, size_t bytes);  // grow-only device buffer
     void bind();                         // make the device current
@@ -120,10 +163,12 @@ void launch_sort_by_cluster(const SortPlan &p, const int32_t *labels, int32_t *s
 
 // recompute_centroids_into (kmeans.rs:358-401): per-cluster row-order sums in
 // TC, divide, empty -> keep old, then max shift into scalars->shift_bits.
+// With inertia_part != nullptr the same pass also accumulates, per (cluster,
+// feature), the compensated-f32 sum of (x_ij - c_j)^2 against the old centre.
 template <typename TX, typename TC>
 void launch_update_centroids(const SortPlan &p, const TX *x, int d, const int32_t *members,
                              const int32_t *seg_hist, const TC *old_c, TC *new_c,
-                             DevScalars *scalars, cudaStream_t s);
+                             DevScalars *scalars, cudaStream_t s, double *inertia_part = nullptr);
 
 void launch_labels_to_u64(const int32_t *l, int64_t n, uint64_t *out, cudaStream_t s);
 template <typename TS, typename TD>
@@ -140,11 +185,18 @@ template <typename TX>
 void run_assign_mixed(Ctx &ctx, const TX *x, int64_t n, int d, const double *c, int k,
                       int precision, int32_t *labels, double *mind, DevScalars *scalars,
                       bool x_changed);
-// Inertia of the mixed precisions: sum over clusters and features of
-// (x_ij - c_j)^2 over the cluster's rows, accumulated per (cluster, feature)
-// in compensated f32 and folded in f64 (relative error about 1e-7).
-template <typename TX>
-void launch_mixed_inertia(Ctx &ctx, const SortPlan &p, const TX *x, int d, const int32_t *members,
-                          const int32_t *seg_hist, const double *c, DevScalars *scalars);
+// Inertia of the mixed precisions: the per-(cluster, feature) partials of
+// the update pass folded in f64 (relative error about 1e-7).
+void launch_mixed_inertia(Ctx &ctx, const double *part, int64_t m, DevScalars *scalars);
+
+// Tensor-core assignment (fk_tc.cu): plan, then one persistent launch that
+// writes one Top2 record per (slice, row).
+void plan_tc(Ctx &ctx, MixedPlan &mp, int64_t n, int d, int k);
+// dump (tests only, nullable): raw accumulators of CTA 0's first tile.
+void launch_tc_assign(Ctx &ctx, MixedPlan &mp, const void *xb, const void *cb, const void *caug, Top2 *out,
+                      DevScalars *sc, float *dump = nullptr);
+
+void debug_tc_probe(Ctx &ctx, const float *x, int64_t n, int d, const double *c, int k, float *dump_out,
+                    uint16_t *xb_out, uint16_t *cb_out, uint16_t *aug_out, Top2 *top_out, int *plan_out);
 
 }  // namespace fk

@@ -1,30 +1,475 @@
-// fk_mixed.cu -- mixed-precision assignment (approximate pass + exact FP64
-// re-check). Placeholder until the approximate kernels land.
+// fk_mixed.cu -- mixed-precision assignment with an exact FP64 re-check.
+//
+// The approximate pass scores every (row, centre) pair as
+//     T_c = xh . ch + a_c,   a_c = BIG - ||c'||^2 / 2,
+// where x' = x - mu and c' = c - mu are centred by the column mean mu, xh and
+// ch are their BF16 roundings, and BIG is a per-iteration constant that makes
+// every T_c positive. Maximising T_c minimises ||x - c||^2. The contraction
+// runs on the tensor cores (fk_tc.cu); a_c enters as three extra BF16 columns
+// multiplied by a constant column of ones, so the epilogue only ranks values.
+//
+// Per row, with the pass's best and second-best values v1 >= v2, the error
+// bound (in T units)
+//     E = ex * Cn + xn * Ec + ACC * (xn * Chn + BIG) + REPR * BIG
+// (ex = ||x' - xh||, xn = ||xh||, Cn = max ||c'||, Ec = max ||c' - ch||,
+// Chn = max ||ch||; ACC and REPR generous multiples of 2^-22 covering the FP32
+// accumulation and the three-term BF16 split of a_c), the key-truncation
+// quantum q and the FP64 oracle's own rounding delta give the threshold
+// thr = 2E + q + delta. If v1 - v2 > thr no other centre can win in the FP64
+// direct form, so the label is final. Otherwise, if the best value outside the
+// top two is also below v1 - thr, only the top two are re-scored exactly;
+// else the row is re-scored against every centre. Every re-score is the
+// direct-form sum (x_j - c_j)^2 in FP64 with no FMA and the lowest index on
+// ties, i.e. exactly kmeans.rs:159-163 / 295-309, so the labels equal the
+// FP64 oracle's in every case.
+#include <cfloat>
+#include <cmath>
+#include <cuda_bf16.h>
+
+#include <cstddef>
+#include <vector>
+
 #include "fk_internal.cuh"
 
 namespace fk {
+namespace {
 
-template <typename TX>
-void run_assign_mixed(Ctx &, const TX *, int64_t, int, const double *, int, int, int32_t *, double *, DevScalars *,
-                      bool) {
-    set_error("mixed precision is not built yet");
-    fail(FK_ERR_UNSUPPORTED);
+constexpr double ACC_REL_PER_K = 0.0000002384185791015625;  // 2^-22 per accumulated column
+constexpr double REPR_REL = 0.0000002384185791015625;       // 2^-22
+
+__device__ __forceinline__ void atomic_max_pos(float *addr, float v) {
+    // non-negative floats order like their bit patterns
+    if (v >= 0.f) atomicMax((unsigned int *)addr, __float_as_uint(v));
 }
 
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+    for (int off = 16; off >= 1; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    return v;
+}
+
+// ----------------------------------------------------------- row prep --
+// Column means in f64 (order irrelevant: mu only centres the data).
 template <typename TX>
-void launch_mixed_inertia(Ctx &, const SortPlan &, const TX *, int, const int32_t *, const int32_t *, const double *,
-                          DevScalars *) {
-    set_error("mixed precision is not built yet");
-    fail(FK_ERR_UNSUPPORTED);
+__global__ void col_mean_partial_kernel(const TX *__restrict__ x, int64_t n, int d, int64_t rows_per,
+                                        double *__restrict__ part) {
+    int j = threadIdx.x + blockIdx.y * blockDim.x;
+    if (j >= d) return;
+    int64_t lo = (int64_t)blockIdx.x * rows_per, hi = min(n, lo + rows_per);
+    double s = 0.0;
+    for (int64_t i = lo; i < hi; i++) {
+        double v = (double)x[i * d + j];
+        if (isfinite(v)) s += v;  // mu only centres the data; non-finite rows are re-scored in full
+    }
+    part[(int64_t)blockIdx.x * d + j] = s;
+}
+
+__global__ void col_mean_final_kernel(const double *__restrict__ part, int nparts, int64_t n, int d,
+                                      double *__restrict__ mu, float *__restrict__ mu32) {
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= d) return;
+    double s = 0.0;
+    for (int p = 0; p < nparts; p++) s += part[(int64_t)p * d + j];
+    double m = s / (double)n;
+    mu[j] = m;
+    mu32[j] = (float)m;
+}
+
+// One warp per row: BF16 copy of x - mu (row stride d_pad, zero padded) and
+// the row's bound ingredients {||xh||, ||x' - xh||, ||x||} rounded up.
+template <typename TX>
+__global__ void prep_rows_kernel(const TX *__restrict__ x, int64_t n, int d, int d_pad,
+                                 const double *__restrict__ mu, __nv_bfloat16 *__restrict__ xb,
+                                 float4 *__restrict__ rowinfo, MixedStats *stats) {
+    const int lane = threadIdx.x & 31;
+    const int64_t row = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (row >= n) return;
+    double xn2 = 0.0, ex2 = 0.0, xo2 = 0.0;
+    for (int j = lane; j < d_pad; j += 32) {
+        __nv_bfloat16 h = __float2bfloat16_rn(0.f);
+        if (j < d) {
+            double xv = (double)x[row * d + j];
+            double xc = xv - mu[j];
+            h = __float2bfloat16_rn((float)xc);
+            double hv = (double)__bfloat162float(h);
+            double e = xc - hv;
+            xn2 += hv * hv;
+            ex2 += e * e;
+            xo2 += xv * xv;
+        }
+        xb[row * d_pad + j] = h;
+    }
+    xn2 = warp_sum_d(xn2);
+    ex2 = warp_sum_d(ex2);
+    xo2 = warp_sum_d(xo2);
+    if (lane == 0) {
+        const double up = 1.0 + 1e-12;
+        float xn = __double2float_ru(sqrt(xn2) * up);
+        float ex = __double2float_ru(sqrt(ex2) * up);
+        float xo = __double2float_ru(sqrt(xo2) * up);
+        rowinfo[row] = make_float4(xn, ex, xo, 0.f);
+        if (xn == xn) atomic_max_pos(&stats->xn_max, xn);  // NaN rows are re-scored in full anyway
+    }
+}
+
+// -------------------------------------------------------- centre prep --
+// One warp per (padded) centre row: BF16 copy of c - mu, and the maxima of
+// ||c'||, ||c' - ch||, ||ch||, ||c'||^2 / 2, ||c|| over the real centres.
+__global__ void prep_centres_kernel(const double *__restrict__ c, int k, int k_pad, int d, int d_pad,
+                                    const double *__restrict__ mu, __nv_bfloat16 *__restrict__ cb,
+                                    double *__restrict__ half_norm, MixedStats *stats) {
+    const int lane = threadIdx.x & 31;
+    const int q = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (q >= k_pad) return;
+    double cn2 = 0.0, ec2 = 0.0, ch2 = 0.0, co2 = 0.0;
+    for (int j = lane; j < d_pad; j += 32) {
+        __nv_bfloat16 h = __float2bfloat16_rn(0.f);
+        if (q < k && j < d) {
+            double cv = c[(int64_t)q * d + j];
+            double cc = cv - mu[j];
+            h = __float2bfloat16_rn((float)cc);
+            double hv = (double)__bfloat162float(h);
+            cn2 += cc * cc;
+            ec2 += (cc - hv) * (cc - hv);
+            ch2 += hv * hv;
+            co2 += cv * cv;
+        }
+        cb[(int64_t)q * d_pad + j] = h;
+    }
+    cn2 = warp_sum_d(cn2);
+    ec2 = warp_sum_d(ec2);
+    ch2 = warp_sum_d(ch2);
+    co2 = warp_sum_d(co2);
+    if (lane == 0 && q < k) {
+        const double up = 1.0 + 1e-12;
+        half_norm[q] = 0.5 * cn2;
+        atomic_max_pos(&stats->cn_max, __double2float_ru(sqrt(cn2) * up));
+        atomic_max_pos(&stats->ec_max, __double2float_ru(sqrt(ec2) * up));
+        atomic_max_pos(&stats->ch_max, __double2float_ru(sqrt(ch2) * up));
+        atomic_max_pos(&stats->h_max, __double2float_ru(0.5 * cn2 * up));
+        atomic_max_pos(&stats->co_max, __double2float_ru(sqrt(co2) * up));
+    }
+}
+
+// a_c = BIG - ||c'||^2/2 split into three BF16 terms (columns 0..2 of the
+// 16-column augmentation row); padded centres get a_c = 0, so they score 0.
+__global__ void prep_aug_kernel(const double *__restrict__ half_norm, int k, int k_pad,
+                                __nv_bfloat16 *__restrict__ caug, MixedStats *stats) {
+    int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= k_pad) return;
+    double big = ((double)stats->xn_max * (double)stats->ch_max + (double)stats->h_max) * (1.0 + 1e-3) + 64.0;
+    if (q == 0) stats->big = (float)big;
+    __nv_bfloat16 t[16];
+#pragma unroll
+    for (int j = 0; j < 16; j++) t[j] = __float2bfloat16_rn(0.f);
+    if (q < k) {
+        double a = big - half_norm[q];
+        __nv_bfloat16 a1 = __float2bfloat16_rn((float)a);
+        double r1 = a - (double)__bfloat162float(a1);
+        __nv_bfloat16 a2 = __float2bfloat16_rn((float)r1);
+        double r2 = r1 - (double)__bfloat162float(a2);
+        __nv_bfloat16 a3 = __float2bfloat16_rn((float)r2);
+        t[0] = a1;
+        t[1] = a2;
+        t[2] = a3;
+    }
+#pragma unroll
+    for (int j = 0; j < 16; j++) caug[(int64_t)q * 16 + j] = t[j];
+}
+
+// --------------------------------------------------------------- finalize --
+__device__ __forceinline__ void merge_top2(float &v1, int &i1, float &v2, int &i2, float w1, int j1, float w2, int j2,
+                                           float &u3) {
+    // Merge candidate pair (w1 >= w2) into (v1 >= v2); u3 tracks an upper
+    // bound of every value that is not kept in the top two.
+    if (w1 > v1) {
+        if (v1 > w2) {
+            u3 = fmaxf(u3, fmaxf(v2, w2));
+            v2 = v1;
+            i2 = i1;
+        } else {
+            u3 = fmaxf(u3, v1);
+            v2 = w2;
+            i2 = j2;
+        }
+        v1 = w1;
+        i1 = j1;
+    } else if (w1 > v2) {
+        u3 = fmaxf(u3, fmaxf(v2, w2));
+        v2 = w1;
+        i2 = j1;
+    } else {
+        u3 = fmaxf(u3, w1);
+    }
+}
+
+__global__ void finalize_kernel(const Top2 *__restrict__ parts, int nparts, int64_t n, int k, int d,
+                                const float4 *__restrict__ rowinfo, const MixedStats *stats, double acc_rel,
+                                double mu_norm, int32_t *__restrict__ labels, int4 *__restrict__ pair_list,
+                                int32_t *__restrict__ full_list, DevScalars *sc) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    // Each slice's third-best value is at most its second-best.
+    Top2 t = parts[i];
+    float v1 = t.v1, v2 = t.v2, u3 = t.v2;
+    int i1 = t.i1, i2 = t.i2;
+    for (int p = 1; p < nparts; p++) {
+        Top2 o = parts[(int64_t)p * n + i];
+        u3 = fmaxf(u3, o.v2);
+        merge_top2(v1, i1, v2, i2, o.v1, o.i1, o.v2, o.i2, u3);
+    }
+    const float4 ri = rowinfo[i];
+    const double xn = ri.x, ex = ri.y, xo = ri.z;
+    const double cn = stats->cn_max, ec = stats->ec_max, ch = stats->ch_max, big = stats->big;
+    const double co = stats->co_max;
+    double e = ex * cn + xn * ec + acc_rel * (xn * ch + big) + REPR_REL * big;
+    double q = (double)v1 * 0.000030517578125;                      // key truncation, 2^-15 relative
+    double xo_b = xo > xn + ex + mu_norm ? xo : xn + ex + mu_norm;  // ||x|| (both bounds are valid)
+    double delta = (double)(d + 4) * 1.1102230246251565e-16 * (xo_b + co) * (xo_b + co);  // FP64 rounding, D units
+    double thr = (2.0 * e + q + 0.5 * delta) * (1.0 + 1e-6) + 1e-30;
+    double m12 = (double)v1 - (double)v2;
+    if (i1 >= 0 && i1 < k && m12 > thr) {
+        labels[i] = i1;
+        return;
+    }
+    double m13 = (double)v1 - (double)u3;
+    if (i1 >= 0 && i1 < k && i2 >= 0 && i2 < k && i1 != i2 && m13 > thr) {
+        unsigned long long slot = atomicAdd(&sc->flag_count, 1ULL);
+        pair_list[slot] = make_int4((int)i, i1, i2, 0);
+    } else {
+        unsigned long long slot = atomicAdd(&sc->full_count, 1ULL);
+        full_list[slot] = (int32_t)i;
+    }
+}
+
+// ------------------------------------------------------------ re-checks --
+template <typename TX>
+__device__ __forceinline__ double sqeuc64(const TX *__restrict__ x, const double *__restrict__ c, int d) {
+    double acc = 0.0;
+    for (int j = 0; j < d; j++) {
+        double t = __dsub_rn((double)x[j], c[j]);
+        acc = __dadd_rn(acc, __dmul_rn(t, t));
+    }
+    return acc;
+}
+
+__device__ __forceinline__ bool near_tie(double a, double b) {
+    double lo = a < b ? a : b;
+    return fabs(a - b) <= 1e-12 * lo;
+}
+
+// One thread per listed row: exact FP64 distances to its two candidates.
+template <typename TX>
+__global__ void pair_rescore_kernel(const TX *__restrict__ x, int d, const double *__restrict__ c,
+                                    const int4 *__restrict__ list, DevScalars *sc, int32_t *__restrict__ labels) {
+    const unsigned long long cnt = sc->flag_count;
+    for (unsigned long long s = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; s < cnt;
+         s += (unsigned long long)gridDim.x * blockDim.x) {
+        int4 e = list[s];
+        const TX *row = x + (int64_t)e.x * d;
+        int a = e.y < e.z ? e.y : e.z, b = e.y < e.z ? e.z : e.y;
+        double da = sqeuc64(row, c + (int64_t)a * d, d);
+        double db = sqeuc64(row, c + (int64_t)b * d, d);
+        // strict < from F::MAX over increasing index
+        int best = 0;
+        double bd = DBL_MAX;
+        if (da < bd) { bd = da; best = a; }
+        if (db < bd) { bd = db; best = b; }
+        labels[e.x] = best;
+        atomicAdd(&sc->recheck_rows, 1ULL);
+        if (near_tie(da, db)) atomicAdd(&sc->near_tie_rows, 1ULL);
+    }
+}
+
+// One warp per listed row: exact FP64 distances to every centre.
+template <typename TX>
+__global__ void full_rescore_kernel(const TX *__restrict__ x, int d, const double *__restrict__ c, int k,
+                                    const int32_t *__restrict__ list, DevScalars *sc, int32_t *__restrict__ labels) {
+    const unsigned long long cnt = sc->full_count;
+    const int lane = threadIdx.x & 31;
+    const unsigned long long wid = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const unsigned long long nw = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
+    for (unsigned long long s = wid; s < cnt; s += nw) {
+        const int64_t r = list[s];
+        const TX *row = x + r * d;
+        double b1 = DBL_MAX, b2 = DBL_MAX;
+        int i1 = INT32_MAX;
+        for (int q = lane; q < k; q += 32) {
+            double v = sqeuc64(row, c + (int64_t)q * d, d);
+            if (v < b1) { b2 = b1; b1 = v; i1 = q; }
+            else if (v < b2) { b2 = v; }
+        }
+#pragma unroll
+        for (int off = 16; off >= 1; off >>= 1) {
+            double o1 = __shfl_xor_sync(0xffffffffu, b1, off);
+            double o2 = __shfl_xor_sync(0xffffffffu, b2, off);
+            int oi = __shfl_xor_sync(0xffffffffu, i1, off);
+            if (o1 < b1 || (o1 == b1 && oi < i1)) {
+                b2 = fmin(b1, o2);
+                b1 = o1;
+                i1 = oi;
+            } else {
+                b2 = fmin(b2, o1);
+            }
+        }
+        if (lane == 0) {
+            labels[r] = i1 == INT32_MAX ? 0 : i1;
+            atomicAdd(&sc->recheck_rows, 1ULL);
+            atomicAdd(&sc->full_rows, 1ULL);
+            if (i1 != INT32_MAX && b2 < DBL_MAX && near_tie(b1, b2)) atomicAdd(&sc->near_tie_rows, 1ULL);
+        }
+    }
+}
+
+// ---------------------------------------------------- mixed inertia --
+__global__ void inertia_final_kernel(const double *__restrict__ part, int64_t m, double *out) {
+    __shared__ double sh[32];
+    double s = 0.0;
+    for (int64_t i = threadIdx.x; i < m; i += blockDim.x) s += part[i];
+    s = warp_sum_d(s);
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) sh[w] = s;
+    __syncthreads();
+    if (w == 0) {
+        double r = lane < (int)(blockDim.x >> 5) ? sh[lane] : 0.0;
+        r = warp_sum_d(r);
+        if (lane == 0) *out = r;
+    }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------- driver --
+template <typename TX>
+void run_assign_mixed(Ctx &ctx, const TX *x, int64_t n, int d, const double *c, int k, int precision,
+                      int32_t *labels, double *, DevScalars *sc, bool x_changed) {
+    cudaStream_t s = ctx.stream;
+    MixedPlan &mp = ctx.mixed;
+    if (precision != FK_PRECISION_MIXED_BF16) {
+        set_error("precision %d is not built", precision);
+        fail(FK_ERR_UNSUPPORTED);
+    }
+    if (d < 1 || d > 256) {
+        set_error("the BF16 tensor-core path supports 1 <= d <= 256 (got %d)", d);
+        fail(FK_ERR_UNSUPPORTED);
+    }
+    const bool replan = x_changed || mp.n != n || mp.d != d || mp.k != k || mp.x != (const void *)x;
+    if (replan) plan_tc(ctx, mp, n, d, k);
+    mp.x = (const void *)x;
+    auto *stats = (MixedStats *)ctx.get(BUF_CF32, sizeof(MixedStats));
+    double *mu = (double *)ctx.get(BUF_COUNTS, sizeof(double) * 2 * (size_t)d + sizeof(float) * (size_t)d + 64);
+    float *mu32 = (float *)(mu + 2 * d);
+    __nv_bfloat16 *xb = (__nv_bfloat16 *)ctx.get(BUF_XB, sizeof(__nv_bfloat16) * (size_t)n * mp.d_pad);
+    float4 *rowinfo = (float4 *)ctx.get(BUF_XNORM, sizeof(float4) * (size_t)n);
+    if (replan) {
+        FK_CUDA(cudaMemsetAsync(stats, 0, sizeof(MixedStats), s));
+        const int64_t rows_per = 4096;
+        const int nparts = (int)((n + rows_per - 1) / rows_per);
+        double *part = (double *)ctx.get(BUF_PARTIAL, sizeof(double) * (size_t)nparts * d);
+        dim3 g1(nparts, (d + 127) / 128);
+        col_mean_partial_kernel<TX><<<g1, 128, 0, s>>>(x, n, d, rows_per, part);
+        FK_LAUNCH_CHECK();
+        col_mean_final_kernel<<<(d + 127) / 128, 128, 0, s>>>(part, nparts, n, d, mu, mu32);
+        FK_LAUNCH_CHECK();
+        prep_rows_kernel<TX><<<(unsigned)((n + 7) / 8), 256, 0, s>>>(x, n, d, mp.d_pad, mu, xb, rowinfo, stats);
+        FK_LAUNCH_CHECK();
+        // ||mu|| for the bound on ||x|| (host side, tiny)
+        std::vector<double> hmu(d);
+        FK_CUDA(cudaMemcpyAsync(hmu.data(), mu, sizeof(double) * d, cudaMemcpyDeviceToHost, s));
+        FK_CUDA(cudaStreamSynchronize(s));
+        double m2 = 0.0;
+        for (double v : hmu) m2 += v * v;
+        mp.mu_norm = std::sqrt(m2) * (1.0 + 1e-12);
+    } else {
+        // centre statistics are per iteration; the row maximum stays
+        FK_CUDA(cudaMemsetAsync((char *)stats + offsetof(MixedStats, cn_max), 0,
+                                sizeof(MixedStats) - offsetof(MixedStats, cn_max), s));
+    }
+    __nv_bfloat16 *cb = (__nv_bfloat16 *)ctx.get(BUF_CB, sizeof(__nv_bfloat16) * (size_t)mp.k_pad * mp.d_pad);
+    __nv_bfloat16 *caug = (__nv_bfloat16 *)ctx.get(BUF_CAUX, sizeof(__nv_bfloat16) * (size_t)mp.k_pad * 16 + 8192);
+    double *half_norm = (double *)ctx.get(BUF_MIND, sizeof(double) * (size_t)mp.k_pad);
+    prep_centres_kernel<<<(mp.k_pad + 7) / 8, 256, 0, s>>>(c, k, mp.k_pad, d, mp.d_pad, mu, cb, half_norm, stats);
+    FK_LAUNCH_CHECK();
+    prep_aug_kernel<<<(mp.k_pad + 255) / 256, 256, 0, s>>>(half_norm, k, mp.k_pad, caug, stats);
+    FK_LAUNCH_CHECK();
+
+    Top2 *top = (Top2 *)ctx.get(BUF_TOP2, sizeof(Top2) * (size_t)n * mp.parts);
+    launch_tc_assign(ctx, mp, xb, cb, caug, top, sc);
+
+    int4 *pairs = (int4 *)ctx.get(BUF_FLAGS, sizeof(int4) * (size_t)n);
+    int32_t *full = (int32_t *)ctx.get(BUF_FULL, sizeof(int32_t) * (size_t)n);
+    const double acc_rel = (double)(mp.d_pad + 32) * ACC_REL_PER_K;
+    finalize_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(top, mp.parts, n, k, d, rowinfo, stats, acc_rel,
+                                                               mp.mu_norm, labels, pairs, full, sc);
+    FK_LAUNCH_CHECK();
+    const int grid = ctx.num_sms * 4;
+    pair_rescore_kernel<TX><<<grid, 256, 0, s>>>(x, d, c, pairs, sc, labels);
+    FK_LAUNCH_CHECK();
+    full_rescore_kernel<TX><<<grid, 256, 0, s>>>(x, d, c, k, full, sc, labels);
+    FK_LAUNCH_CHECK();
+}
+
+void launch_mixed_inertia(Ctx &ctx, const double *part, int64_t m, DevScalars *sc) {
+    inertia_final_kernel<<<1, 1024, 0, ctx.stream>>>(part, m, &sc->inertia);
+    FK_LAUNCH_CHECK();
 }
 
 template void run_assign_mixed<float>(Ctx &, const float *, int64_t, int, const double *, int, int, int32_t *,
                                       double *, DevScalars *, bool);
+
+// Diagnostics for the tests: one tensor-core pass over x (f32, on the device)
+// against c (f64), returning the raw accumulators of CTA 0's first tile and
+// the BF16 operands they were computed from.
+void debug_tc_probe(Ctx &ctx, const float *x, int64_t n, int d, const double *c, int k, float *dump_out,
+                    uint16_t *xb_out, uint16_t *cb_out, uint16_t *aug_out, Top2 *top_out, int *plan_out) {
+    cudaStream_t s = ctx.stream;
+    MixedPlan &mp = ctx.mixed;
+    plan_tc(ctx, mp, n, d, k);
+    mp.x = nullptr;
+    DevScalars *sc = (DevScalars *)ctx.get(BUF_SCALARS, sizeof(DevScalars));
+    FK_CUDA(cudaMemsetAsync(sc, 0, sizeof(DevScalars), s));
+    auto *stats = (MixedStats *)ctx.get(BUF_CF32, sizeof(MixedStats));
+    FK_CUDA(cudaMemsetAsync(stats, 0, sizeof(MixedStats), s));
+    double *mu = (double *)ctx.get(BUF_COUNTS, sizeof(double) * 2 * (size_t)d + sizeof(float) * (size_t)d + 64);
+    float *mu32 = (float *)(mu + 2 * d);
+    __nv_bfloat16 *xb = (__nv_bfloat16 *)ctx.get(BUF_XB, sizeof(__nv_bfloat16) * (size_t)n * mp.d_pad);
+    float4 *rowinfo = (float4 *)ctx.get(BUF_XNORM, sizeof(float4) * (size_t)n);
+    const int64_t rows_per = 4096;
+    const int nparts = (int)((n + rows_per - 1) / rows_per);
+    double *part = (double *)ctx.get(BUF_PARTIAL, sizeof(double) * (size_t)nparts * d);
+    col_mean_partial_kernel<float><<<dim3(nparts, (d + 127) / 128), 128, 0, s>>>(x, n, d, rows_per, part);
+    FK_LAUNCH_CHECK();
+    col_mean_final_kernel<<<(d + 127) / 128, 128, 0, s>>>(part, nparts, n, d, mu, mu32);
+    FK_LAUNCH_CHECK();
+    prep_rows_kernel<float><<<(unsigned)((n + 7) / 8), 256, 0, s>>>(x, n, d, mp.d_pad, mu, xb, rowinfo, stats);
+    FK_LAUNCH_CHECK();
+    __nv_bfloat16 *cb = (__nv_bfloat16 *)ctx.get(BUF_CB, sizeof(__nv_bfloat16) * (size_t)mp.k_pad * mp.d_pad);
+    __nv_bfloat16 *caug = (__nv_bfloat16 *)ctx.get(BUF_CAUX, sizeof(__nv_bfloat16) * (size_t)mp.k_pad * 16 + 8192);
+    double *half_norm = (double *)ctx.get(BUF_MIND, sizeof(double) * (size_t)mp.k_pad);
+    prep_centres_kernel<<<(mp.k_pad + 7) / 8, 256, 0, s>>>(c, k, mp.k_pad, d, mp.d_pad, mu, cb, half_norm, stats);
+    FK_LAUNCH_CHECK();
+    prep_aug_kernel<<<(mp.k_pad + 255) / 256, 256, 0, s>>>(half_norm, k, mp.k_pad, caug, stats);
+    FK_LAUNCH_CHECK();
+    Top2 *top = (Top2 *)ctx.get(BUF_TOP2, sizeof(Top2) * (size_t)n * mp.parts);
+    float *dump = (float *)ctx.get(BUF_OUT, sizeof(float) * 128 * (size_t)mp.kp);
+    FK_CUDA(cudaMemsetAsync(dump, 0, sizeof(float) * 128 * (size_t)mp.kp, s));
+    launch_tc_assign(ctx, mp, xb, cb, caug, top, sc, dump);
+    FK_CUDA(cudaMemcpyAsync(dump_out, dump, sizeof(float) * 128 * (size_t)mp.kp, cudaMemcpyDeviceToHost, s));
+    const int64_t rows = n < 128 ? n : 128;
+    FK_CUDA(cudaMemcpyAsync(xb_out, xb, sizeof(uint16_t) * (size_t)rows * mp.d_pad, cudaMemcpyDeviceToHost, s));
+    FK_CUDA(cudaMemcpyAsync(cb_out, cb, sizeof(uint16_t) * (size_t)mp.k_pad * mp.d_pad, cudaMemcpyDeviceToHost, s));
+    FK_CUDA(cudaMemcpyAsync(aug_out, caug, sizeof(uint16_t) * (size_t)mp.k_pad * 16, cudaMemcpyDeviceToHost, s));
+    FK_CUDA(cudaMemcpyAsync(top_out, top, sizeof(Top2) * (size_t)n * mp.parts, cudaMemcpyDeviceToHost, s));
+    FK_CUDA(cudaMemcpyAsync(ctx.host_scalars, sc, sizeof(DevScalars), cudaMemcpyDeviceToHost, s));
+    FK_CUDA(cudaStreamSynchronize(s));
+    plan_out[0] = mp.d_pad;
+    plan_out[1] = mp.kp;
+    plan_out[2] = mp.parts;
+    plan_out[3] = mp.k_pad;
+    plan_out[4] = mp.grid;
+    plan_out[5] = (int)ctx.host_scalars->error_word;
+}
 template void run_assign_mixed<double>(Ctx &, const double *, int64_t, int, const double *, int, int, int32_t *,
                                        double *, DevScalars *, bool);
-template void launch_mixed_inertia<float>(Ctx &, const SortPlan &, const float *, int, const int32_t *,
-                                          const int32_t *, const double *, DevScalars *);
-template void launch_mixed_inertia<double>(Ctx &, const SortPlan &, const double *, int, const int32_t *,
-                                           const int32_t *, const double *, DevScalars *);
 
 }  // namespace fk

@@ -1,0 +1,529 @@
+// fk_tc.cu -- fused BF16 assignment on the 5th-generation tensor cores.
+//
+// One persistent launch, one CTA per SM (10 warps, ~215 KB shared memory,
+// 512 TMEM columns). The centres are cut into `parts` slices of kp centres;
+// CTA (slice p, index q) keeps its slice resident in shared memory for the
+// whole launch and streams the row tiles q, q+Q, q+2Q, ... of X through a
+// two-stage TMA ring, so X is read once per slice and the n x k score matrix
+// never leaves the SM.
+//
+//   warp 0   TMA producer: the resident slice once, then 128-row X tiles
+//            (cp.async.bulk.tensor, 128-byte swizzle, mbarrier complete_tx).
+//   warp 1   TMEM allocator and MMA issuer: per (tile, 256-centre block),
+//            d_pad/16 tcgen05.mma (M=128, N=256, K=16, BF16 in, FP32 out)
+//            plus one K=16 MMA that adds a_c = BIG - ||c'||^2/2 through a
+//            constant "ones" operand; tcgen05.commit signals the epilogue.
+//            Two TMEM accumulators (2 x 256 columns) alternate, so the MMAs
+//            of block b+1 overlap the epilogue of block b.
+//   warps 2-9 epilogue: tcgen05.ld (32x32b, one row per thread), then a
+//            running top-2 per row. Scores are positive by construction, so
+//            their IEEE bits order like unsigned integers; the low 8 bits
+//            are replaced by the column code (255 - column), making every
+//            key unique, and the top-2 update is three integer min/max
+//            operations. The truncation quantum (2^-15 relative) is part of
+//            the error bound the re-check uses.
+//
+// Every wait on an mbarrier is bounded (about two seconds of SM clock); on
+// expiry the CTA records an error word, stops issuing work, drains what it
+// has in flight and frees its TMEM, so a fault in the pipeline can never hang
+// the GPU. The host turns the error word into FK_ERR_TIMEOUT.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cuda_bf16.h>
+
+#include <cstring>
+
+#include "fk_internal.cuh"
+
+namespace fk {
+namespace {
+
+constexpr int BM = 128;           // rows per tile = TMEM lanes
+constexpr int BN = 256;           // centres per accumulator block
+constexpr int NTHREADS = 320;     // 10 warps
+constexpr int XSTAGES = 2;        // X ring depth
+constexpr uint32_t TMEM_COLS = 512;
+constexpr uint32_t X_ATOM_BYTES = BM * 128;  // 128 rows x 64 BF16
+constexpr uint32_t ONES_BYTES = BM * 32;     // 128 rows x 16 BF16
+constexpr uint32_t MERGE_BYTES = BM * sizeof(Top2);
+constexpr uint32_t BAR_BYTES = 256;
+constexpr long long WAIT_LIMIT_CYCLES = 4000000000LL;
+
+// Instruction descriptor, kind::f16: D = F32 (bits 4-5 = 1), A = B = BF16
+// (bits 7-9 = 1, 10-12 = 1), both K-major, N >> 3 at bits 17-22, M >> 4 at
+// bits 24-28.
+constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
+                           ((uint32_t)(BM >> 4) << 24);
+constexpr uint32_t LAYOUT_SW128 = 2;
+constexpr uint32_t LAYOUT_SW32 = 6;
+
+struct TcParams {
+    int64_t n;
+    int64_t tiles;
+    int n_atoms;       // d_pad / 64
+    int kp;            // centres per slice
+    int nblocks;       // kp / 256
+    int parts;
+    int ctas_per_part;
+    uint32_t off_c, off_x, off_aug, off_ones, off_merge, off_bar;
+    uint32_t c_atom_bytes;  // kp * 128
+    uint32_t x_stage_bytes;
+    uint32_t c_tx_bytes;
+    Top2 *out;
+    unsigned long long *err;
+    float *dump;  // optional: raw accumulators of the first tile of CTA 0 (tests only)
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait: false if the CTA is aborting or this wait ran out of time.
+__device__ __noinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile uint32_t *abort_flag,
+                                       unsigned long long *err, unsigned long long code) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const long long t0 = clock64();
+    uint32_t spins = 0;
+    while (true) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if ((++spins & 63u) == 0u) {
+            if (*abort_flag) return false;
+            if (clock64() - t0 > WAIT_LIMIT_CYCLES) {
+                *abort_flag = 1u;
+                atomicOr(err, code);
+                return false;
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, uint32_t bar, int x, int y) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];" ::
+            "r"(dst),
+        "l"((uint64_t)map), "r"(bar), "r"(x), "r"(y)
+        : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// Shared-memory matrix descriptor (sm_100 format): start address >> 4 in
+// bits 0-13, leading-byte offset >> 4 in 16-29 (unused for swizzled K-major
+// tiles whose K extent fits one atom), stride-byte offset >> 4 in 32-45
+// (distance between 8-row groups), version 1 at bit 46, layout at 61-63.
+__device__ __forceinline__ uint64_t sdesc(uint32_t saddr, uint32_t sbo, uint32_t layout) {
+    uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFFu);
+    d |= (uint64_t)1u << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+    d |= (uint64_t)1u << 46;
+    d |= (uint64_t)layout << 61;
+    return d;
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+        "l"(adesc), "l"(bdesc), "r"(IDESC), "r"(accumulate)
+        : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+                 : "memory");
+}
+
+// 32 consecutive columns of this thread's TMEM lane. The wait is tied to the
+// registers so no use of them can be scheduled before it.
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+    asm volatile(
+        "tcgen05.wait::ld.sync.aligned;"
+        : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7]),
+          "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]), "+r"(r[14]), "+r"(r[15]),
+          "+r"(r[16]), "+r"(r[17]), "+r"(r[18]), "+r"(r[19]), "+r"(r[20]), "+r"(r[21]), "+r"(r[22]), "+r"(r[23]),
+          "+r"(r[24]), "+r"(r[25]), "+r"(r[26]), "+r"(r[27]), "+r"(r[28]), "+r"(r[29]), "+r"(r[30]), "+r"(r[31])
+        :
+        : "memory");
+}
+
+__device__ __forceinline__ void epi_bar() { asm volatile("bar.sync 1, 256;" ::: "memory"); }
+
+// Running top-2 merge of a candidate pair (w1 >= w2, as ordered keys).
+__device__ __forceinline__ void merge2(uint32_t &R1, int &I1, uint32_t &R2, int &I2, uint32_t w1, int j1, uint32_t w2,
+                                       int j2) {
+    if (w1 > R1) {
+        if (R1 > w2) {
+            R2 = R1;
+            I2 = I1;
+        } else {
+            R2 = w2;
+            I2 = j2;
+        }
+        R1 = w1;
+        I1 = j1;
+    } else if (w1 > R2) {
+        R2 = w1;
+        I2 = j1;
+    }
+}
+
+// Ranks the 128 columns [HALF*128, HALF*128+128) of one accumulator block.
+template <int HALF>
+__device__ __forceinline__ void rank_half(uint32_t col_addr, uint32_t &b1, uint32_t &b2) {
+    uint32_t a1[4] = {0u, 0u, 0u, 0u}, a2[4] = {0u, 0u, 0u, 0u};
+#pragma unroll
+    for (int ch = 0; ch < 4; ch++) {
+        uint32_t r[32];
+        tmem_ld32(col_addr + ch * 32, r);
+#pragma unroll
+        for (int e = 0; e < 32; e++) {
+            constexpr uint32_t hi = 0xFFFFFF00u;
+            const uint32_t code = 255u - (uint32_t)(HALF * 128 + ch * 32 + e);
+            const uint32_t key = (r[e] | 0xFFu) & (hi | code);
+            const int qd = e & 3;
+            const uint32_t lo = min(a1[qd], key);
+            a1[qd] = max(a1[qd], key);
+            a2[qd] = max(a2[qd], lo);
+        }
+    }
+    b1 = a1[0];
+    b2 = a2[0];
+#pragma unroll
+    for (int qd = 1; qd < 4; qd++) {
+        const uint32_t n1 = max(b1, a1[qd]);
+        b2 = max(max(b2, a2[qd]), min(b1, a1[qd]));
+        b1 = n1;
+    }
+}
+
+__global__ void __launch_bounds__(NTHREADS, 1)
+    tc_assign_kernel(const __grid_constant__ CUtensorMap tm_x, const __grid_constant__ CUtensorMap tm_c,
+                     const __grid_constant__ CUtensorMap tm_aug, const __grid_constant__ CUtensorMap tm_ones,
+                     const TcParams p) {
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    const uint32_t sb = smem_u32(smem);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int part = blockIdx.x % p.parts;
+    const int64_t q = blockIdx.x / p.parts;
+    const int64_t tstride = p.ctas_per_part;
+
+    const uint32_t bar_c = sb + p.off_bar;
+    auto bar_xfull = [&](int s) { return bar_c + 8u * (1u + (uint32_t)s); };
+    auto bar_xempty = [&](int s) { return bar_c + 8u * (1u + XSTAGES + (uint32_t)s); };
+    auto bar_afull = [&](int b) { return bar_c + 8u * (1u + 2 * XSTAGES + (uint32_t)b); };
+    auto bar_aempty = [&](int b) { return bar_c + 8u * (3u + 2 * XSTAGES + (uint32_t)b); };
+    uint32_t *slot = (uint32_t *)(smem + p.off_bar + 128);
+    volatile uint32_t *abort_flag = slot + 1;
+
+    if (threadIdx.x == 0) {
+        mbar_init(bar_c, 1);
+        for (int s = 0; s < XSTAGES; s++) {
+            mbar_init(bar_xfull(s), 1);
+            mbar_init(bar_xempty(s), 1);
+        }
+        for (int b = 0; b < 2; b++) {
+            mbar_init(bar_afull(b), 1);
+            mbar_init(bar_aempty(b), 8);
+        }
+        *abort_flag = 0u;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(slot)),
+                     "r"(TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *slot;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            // Resident slice of the centres, its augmentation rows, and the ones tile.
+            mbar_expect_tx(bar_c, p.c_tx_bytes);
+            const int crow0 = part * p.kp;
+            for (int a = 0; a < p.n_atoms; a++)
+                for (int r = 0; r < p.kp; r += BN)
+                    tma_load_2d(sb + p.off_c + (uint32_t)a * p.c_atom_bytes + (uint32_t)r * 128u, &tm_c, bar_c, a * 64,
+                                crow0 + r);
+            for (int r = 0; r < p.kp; r += BN) tma_load_2d(sb + p.off_aug + (uint32_t)r * 32u, &tm_aug, bar_c, 0, crow0 + r);
+            tma_load_2d(sb + p.off_ones, &tm_ones, bar_c, 0, 0);
+            int it = 0;
+            for (int64_t t = q; t < p.tiles; t += tstride, ++it) {
+                const int s = it % XSTAGES;
+                const uint32_t ph = (uint32_t)(it / XSTAGES) & 1u;
+                if (!mbar_wait(bar_xempty(s), ph ^ 1u, abort_flag, p.err, 1ull)) break;
+                mbar_expect_tx(bar_xfull(s), p.x_stage_bytes);
+                for (int a = 0; a < p.n_atoms; a++)
+                    tma_load_2d(sb + p.off_x + (uint32_t)s * p.x_stage_bytes + (uint32_t)a * X_ATOM_BYTES, &tm_x,
+                                bar_xfull(s), a * 64, (int)(t * BM));
+            }
+            // Drain: every issued X load must land before the CTA can exit.
+            const int issued = it;
+            for (int j = issued > XSTAGES ? issued - XSTAGES : 0; j < issued; j++)
+                mbar_wait(bar_xfull(j % XSTAGES), (uint32_t)(j / XSTAGES) & 1u, abort_flag, p.err, 0ull);
+            mbar_wait(bar_c, 0u, abort_flag, p.err, 0ull);
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            int it = 0;
+            uint32_t item = 0;
+            int last_s = -1;
+            uint32_t last_ph = 0;
+            if (mbar_wait(bar_c, 0u, abort_flag, p.err, 2ull)) {
+                tc_fence_after();
+                bool ok = true;
+                for (int64_t t = q; t < p.tiles && ok; t += tstride, ++it) {
+                    const int s = it % XSTAGES;
+                    const uint32_t ph = (uint32_t)(it / XSTAGES) & 1u;
+                    if (!mbar_wait(bar_xfull(s), ph, abort_flag, p.err, 4ull)) break;
+                    tc_fence_after();
+                    const uint32_t xs = sb + p.off_x + (uint32_t)s * p.x_stage_bytes;
+                    for (int b = 0; b < p.nblocks; b++, item++) {
+                        const int buf = (int)(item & 1u);
+                        const uint32_t aph = (item >> 1) & 1u;
+                        if (!mbar_wait(bar_aempty(buf), aph ^ 1u, abort_flag, p.err, 8ull)) {
+                            ok = false;
+                            break;
+                        }
+                        tc_fence_after();
+                        const uint32_t dt = tmem + (uint32_t)buf * BN;
+                        const uint32_t cs = sb + p.off_c + (uint32_t)b * BN * 128u;
+                        for (int a = 0; a < p.n_atoms; a++) {
+#pragma unroll
+                            for (int kk = 0; kk < 4; kk++) {
+                                const uint64_t ad = sdesc(xs + (uint32_t)a * X_ATOM_BYTES + kk * 32u, 1024u, LAYOUT_SW128);
+                                const uint64_t bd = sdesc(cs + (uint32_t)a * p.c_atom_bytes + kk * 32u, 1024u, LAYOUT_SW128);
+                                mma_bf16(dt, ad, bd, (a | kk) != 0 ? 1u : 0u);
+                            }
+                        }
+                        mma_bf16(dt, sdesc(sb + p.off_ones, 256u, LAYOUT_SW32),
+                                 sdesc(sb + p.off_aug + (uint32_t)b * BN * 32u, 256u, LAYOUT_SW32), 1u);
+                        mma_commit(bar_afull(buf));
+                    }
+                    if (!ok) break;
+                    mma_commit(bar_xempty(s));
+                    last_s = s;
+                    last_ph = ph;
+                }
+            }
+            // Drain: the last commit covers every MMA issued before it.
+            if (last_s >= 0) mbar_wait(bar_xempty(last_s), last_ph, abort_flag, p.err, 0ull);
+        }
+    } else {
+        const int ew = warp - 2;
+        const int quarter = warp & 3;
+        const int half = ew >> 2;
+        const int row_local = quarter * 32 + lane;
+        const uint32_t lane_addr = tmem + ((uint32_t)(quarter * 32) << 16);
+        Top2 *merge = (Top2 *)(smem + p.off_merge);
+        uint32_t item = 0;
+        bool dead = false;
+        for (int64_t t = q; t < p.tiles; t += tstride) {
+            uint32_t R1 = 0u, R2 = 0u;
+            int I1 = -1, I2 = -1;
+            for (int b = 0; b < p.nblocks; b++, item++) {
+                const int buf = (int)(item & 1u);
+                const uint32_t aph = (item >> 1) & 1u;
+                if (!dead && !mbar_wait(bar_afull(buf), aph, abort_flag, p.err, 16ull)) dead = true;
+                if (dead) continue;
+                tc_fence_after();
+                const uint32_t col = lane_addr + (uint32_t)buf * BN + (uint32_t)half * 128u;
+                if (p.dump && blockIdx.x == 0 && t == q) {
+                    for (int ch = 0; ch < 4; ch++) {
+                        uint32_t r[32];
+                        tmem_ld32(col + ch * 32, r);
+                        for (int e = 0; e < 32; e++)
+                            p.dump[(int64_t)row_local * (p.nblocks * BN) + b * BN + half * 128 + ch * 32 + e] =
+                                __uint_as_float(r[e]);
+                    }
+                }
+                uint32_t b1, b2;
+                if (half == 0)
+                    rank_half<0>(col, b1, b2);
+                else
+                    rank_half<1>(col, b1, b2);
+                tc_fence_before();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(bar_aempty(buf));
+                const int base = part * p.kp + b * BN + 255;
+                merge2(R1, I1, R2, I2, b1 & 0xFFFFFF00u, base - (int)(b1 & 0xFFu), b2 & 0xFFFFFF00u,
+                       base - (int)(b2 & 0xFFu));
+            }
+            if (half == 1) merge[row_local] = Top2{__uint_as_float(R1), __uint_as_float(R2), I1, I2};
+            epi_bar();
+            if (half == 0) {
+                const Top2 o = merge[row_local];
+                merge2(R1, I1, R2, I2, __float_as_uint(o.v1), o.i1, __float_as_uint(o.v2), o.i2);
+                const int64_t row = t * BM + row_local;
+                if (row < p.n && !dead) p.out[(int64_t)part * p.n + row] = Top2{__uint_as_float(R1), __uint_as_float(R2), I1, I2};
+            }
+            epi_bar();
+        }
+    }
+
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
+    }
+}
+
+// ------------------------------------------------------------- host side --
+PFN_cuTensorMapEncodeTiled_v12000 get_encode(Ctx &ctx) {
+    if (!ctx.tmap_fn) {
+        void *fn = nullptr;
+        cudaDriverEntryPointQueryResult qr;
+        FK_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &qr));
+        if (!fn || qr != cudaDriverEntryPointSuccess) {
+            set_error("cuTensorMapEncodeTiled is not available from the driver");
+            fail(FK_ERR_CUDA);
+        }
+        ctx.tmap_fn = fn;
+    }
+    return (PFN_cuTensorMapEncodeTiled_v12000)ctx.tmap_fn;
+}
+
+void encode_2d(Ctx &ctx, void *out, const void *ptr, uint64_t inner, uint64_t outer, uint64_t row_bytes,
+               uint32_t box_inner, uint32_t box_outer, CUtensorMapSwizzle swz) {
+    auto enc = get_encode(ctx);
+    CUtensorMap m;
+    cuuint64_t dims[2] = {inner, outer};
+    cuuint64_t strides[1] = {row_bytes};
+    cuuint32_t box[2] = {box_inner, box_outer};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = enc(&m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(ptr), dims, strides, box, estr,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, swz, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        set_error("cuTensorMapEncodeTiled failed (%d) for a %llux%llu tensor", (int)r, (unsigned long long)outer,
+                  (unsigned long long)inner);
+        fail(FK_ERR_CUDA);
+    }
+    memcpy(out, &m, sizeof(m));
+}
+
+constexpr size_t SMEM_LIMIT = 227 * 1024;
+
+}  // namespace
+
+void plan_tc(Ctx &ctx, MixedPlan &mp, int64_t n, int d, int k) {
+    mp.n = n;
+    mp.d = d;
+    mp.k = k;
+    mp.d_pad = (d + 63) / 64 * 64;
+    const int n_atoms = mp.d_pad / 64;
+    const size_t x_stage = (size_t)n_atoms * X_ATOM_BYTES;
+    const size_t fixed = 1024 + XSTAGES * x_stage + ONES_BYTES + MERGE_BYTES + BAR_BYTES;
+    const size_t per_centre = (size_t)n_atoms * 128 + 32;
+    if (fixed + BN * per_centre > SMEM_LIMIT) {
+        set_error("the resident-slice tensor-core kernel supports d <= 192 (got %d)", d);
+        fail(FK_ERR_UNSUPPORTED);
+    }
+    const int kp_max = (int)((SMEM_LIMIT - fixed) / per_centre) / BN * BN;
+    mp.parts = (k + kp_max - 1) / kp_max;
+    mp.kp = ((k + mp.parts - 1) / mp.parts + BN - 1) / BN * BN;
+    mp.k_pad = mp.parts * mp.kp;
+    mp.nblocks = mp.kp / BN;
+    mp.tiles = (n + BM - 1) / BM;
+    int sms = ctx.num_sms > 0 ? ctx.num_sms : 1;
+    mp.ctas_per_part = sms / mp.parts > 0 ? sms / mp.parts : 1;
+    if ((int64_t)mp.ctas_per_part > mp.tiles) mp.ctas_per_part = (int)mp.tiles;
+    mp.grid = mp.ctas_per_part * mp.parts;
+    mp.smem = fixed + (size_t)mp.kp * per_centre;
+    mp.tm_x_ptr = mp.tm_c_ptr = mp.tm_aug_ptr = nullptr;
+    if (!mp.ones) {
+        uint16_t h[BM * 16];
+        for (int r = 0; r < BM; r++)
+            for (int j = 0; j < 16; j++) h[r * 16 + j] = j < 3 ? 0x3F80 : 0;  // BF16 1.0 = 0x3F80
+        FK_CUDA(cudaMalloc(&mp.ones, sizeof(h)));
+        FK_CUDA(cudaMemcpy(mp.ones, h, sizeof(h), cudaMemcpyHostToDevice));
+        encode_2d(ctx, mp.tm_ones, mp.ones, 16, BM, 32, 16, BM, CU_TENSOR_MAP_SWIZZLE_32B);
+    }
+}
+
+void launch_tc_assign(Ctx &ctx, MixedPlan &mp, const void *xb, const void *cb, const void *caug, Top2 *out,
+                      DevScalars *sc, float *dump) {
+    if (mp.tm_x_ptr != xb) {
+        encode_2d(ctx, mp.tm_x, xb, (uint64_t)mp.d_pad, (uint64_t)mp.n, (uint64_t)mp.d_pad * 2, 64, BM,
+                  CU_TENSOR_MAP_SWIZZLE_128B);
+        mp.tm_x_ptr = xb;
+    }
+    if (mp.tm_c_ptr != cb) {
+        encode_2d(ctx, mp.tm_c, cb, (uint64_t)mp.d_pad, (uint64_t)mp.k_pad, (uint64_t)mp.d_pad * 2, 64, BN,
+                  CU_TENSOR_MAP_SWIZZLE_128B);
+        mp.tm_c_ptr = cb;
+    }
+    if (mp.tm_aug_ptr != caug) {
+        encode_2d(ctx, mp.tm_aug, caug, 16, (uint64_t)mp.k_pad, 32, 16, BN, CU_TENSOR_MAP_SWIZZLE_32B);
+        mp.tm_aug_ptr = caug;
+    }
+    TcParams p;
+    memset(&p, 0, sizeof(p));
+    p.n = mp.n;
+    p.tiles = mp.tiles;
+    p.n_atoms = mp.d_pad / 64;
+    p.kp = mp.kp;
+    p.nblocks = mp.nblocks;
+    p.parts = mp.parts;
+    p.ctas_per_part = mp.ctas_per_part;
+    p.c_atom_bytes = (uint32_t)mp.kp * 128u;
+    p.x_stage_bytes = (uint32_t)p.n_atoms * X_ATOM_BYTES;
+    p.off_c = 0;
+    p.off_x = p.off_c + (uint32_t)p.n_atoms * p.c_atom_bytes;
+    p.off_aug = p.off_x + XSTAGES * p.x_stage_bytes;
+    p.off_ones = p.off_aug + (uint32_t)mp.kp * 32u;
+    p.off_merge = p.off_ones + ONES_BYTES;
+    p.off_bar = p.off_merge + MERGE_BYTES;
+    p.c_tx_bytes = (uint32_t)p.n_atoms * p.c_atom_bytes + (uint32_t)mp.kp * 32u + ONES_BYTES;
+    p.out = out;
+    p.err = &sc->error_word;
+    p.dump = dump;
+    const size_t smem = (size_t)p.off_bar + BAR_BYTES + 1024;
+    if (smem > SMEM_LIMIT) {
+        set_error("tensor-core plan needs %zu bytes of shared memory", smem);
+        fail(FK_ERR_UNSUPPORTED);
+    }
+    FK_CUDA(cudaFuncSetAttribute((const void *)tc_assign_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem));
+    const CUtensorMap *tx = (const CUtensorMap *)mp.tm_x, *tcm = (const CUtensorMap *)mp.tm_c,
+                      *ta = (const CUtensorMap *)mp.tm_aug, *to = (const CUtensorMap *)mp.tm_ones;
+    tc_assign_kernel<<<mp.grid, NTHREADS, smem, ctx.stream>>>(*tx, *tcm, *ta, *to, p);
+    FK_LAUNCH_CHECK();
+}
+
+}  // namespace fk

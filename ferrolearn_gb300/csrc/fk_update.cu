@@ -156,12 +156,15 @@ template <> struct UArith<double> {
 constexpr int UPD_R = 32;  // member rows loaded per batch
 
 // One block per (cluster, feature slab); thread j keeps the running sum of
-// feature j over the cluster's rows in row order.
-template <typename TX, typename TC>
+// feature j over the cluster's rows in row order. With INERTIA, thread j also
+// accumulates (x_ij - c_j)^2 against the old centre in compensated f32
+// (Kahan), for the mixed precisions' inertia.
+template <typename TX, typename TC, bool INERTIA>
 __global__ void centroid_sum_kernel(const TX *__restrict__ x, int d, int k, int64_t n,
                                     const int32_t *__restrict__ members,
                                     const int32_t *__restrict__ offs, int64_t nseg,
-                                    const TC *__restrict__ old_c, TC *__restrict__ new_c) {
+                                    const TC *__restrict__ old_c, TC *__restrict__ new_c,
+                                    double *__restrict__ inertia_part) {
     using A = UArith<TC>;
     __shared__ int32_t sidx[UPD_R];
     const int c = blockIdx.x;
@@ -169,6 +172,8 @@ __global__ void centroid_sum_kernel(const TX *__restrict__ x, int d, int k, int6
     const int64_t start = offs[(int64_t)c * nseg];
     const int64_t end = (c + 1 < k) ? (int64_t)offs[(int64_t)(c + 1) * nseg] : n;
     TC s = TC(0);
+    float isum = 0.f, icomp = 0.f;
+    const float cj = (INERTIA && j < d) ? (float)old_c[(int64_t)c * d + j] : 0.f;
     for (int64_t base = start; base < end; base += UPD_R) {
         const int cnt = (int)min((int64_t)UPD_R, end - base);
         __syncthreads();
@@ -181,11 +186,24 @@ __global__ void centroid_sum_kernel(const TX *__restrict__ x, int d, int k, int6
 #pragma unroll
             for (int r = 0; r < UPD_R; r++)
                 if (r < cnt) s = A::add(s, (TC)v[r]);
+            if (INERTIA) {
+#pragma unroll
+                for (int r = 0; r < UPD_R; r++) {
+                    if (r < cnt) {
+                        float df = __fsub_rn((float)v[r], cj);
+                        float y = __fsub_rn(__fmul_rn(df, df), icomp);
+                        float t = __fadd_rn(isum, y);
+                        icomp = __fsub_rn(__fsub_rn(t, isum), y);
+                        isum = t;
+                    }
+                }
+            }
         }
     }
     if (j < d) {
         const int64_t cntc = end - start;
         new_c[(int64_t)c * d + j] = cntc > 0 ? A::div(s, (TC)cntc) : old_c[(int64_t)c * d + j];
+        if (INERTIA) inertia_part[(int64_t)c * d + j] = (double)isum - (double)icomp;
     }
 }
 
@@ -266,12 +284,17 @@ void launch_sort_by_cluster(const SortPlan &p, const int32_t *labels, int32_t *s
 template <typename TX, typename TC>
 void launch_update_centroids(const SortPlan &p, const TX *x, int d, const int32_t *members,
                              const int32_t *seg_hist, const TC *old_c, TC *new_c, DevScalars *scalars,
-                             cudaStream_t s) {
+                             cudaStream_t s, double *inertia_part) {
     FK_CUDA(cudaMemsetAsync(&scalars->shift_bits, 0, sizeof(unsigned long long), s));
     if (d == 0 || p.k == 0) return;
     int threads = d >= 256 ? 256 : (d + 31) / 32 * 32;
     dim3 grid((unsigned)p.k, (unsigned)((d + threads - 1) / threads));
-    centroid_sum_kernel<TX, TC><<<grid, threads, 0, s>>>(x, d, p.k, p.n, members, seg_hist, p.nseg, old_c, new_c);
+    if (inertia_part)
+        centroid_sum_kernel<TX, TC, true><<<grid, threads, 0, s>>>(x, d, p.k, p.n, members, seg_hist, p.nseg, old_c,
+                                                                   new_c, inertia_part);
+    else
+        centroid_sum_kernel<TX, TC, false><<<grid, threads, 0, s>>>(x, d, p.k, p.n, members, seg_hist, p.nseg, old_c,
+                                                                    new_c, nullptr);
     FK_LAUNCH_CHECK();
     max_shift_kernel<TC><<<(p.k + 127) / 128, 128, 0, s>>>(new_c, old_c, p.k, d, &scalars->shift_bits);
     FK_LAUNCH_CHECK();
@@ -279,12 +302,12 @@ void launch_update_centroids(const SortPlan &p, const TX *x, int d, const int32_
 
 template void launch_update_centroids<double, double>(const SortPlan &, const double *, int, const int32_t *,
                                                       const int32_t *, const double *, double *, DevScalars *,
-                                                      cudaStream_t);
+                                                      cudaStream_t, double *);
 template void launch_update_centroids<float, float>(const SortPlan &, const float *, int, const int32_t *,
                                                     const int32_t *, const float *, float *, DevScalars *,
-                                                    cudaStream_t);
+                                                    cudaStream_t, double *);
 template void launch_update_centroids<float, double>(const SortPlan &, const float *, int, const int32_t *,
                                                      const int32_t *, const double *, double *, DevScalars *,
-                                                     cudaStream_t);
+                                                     cudaStream_t, double *);
 
 }  // namespace fk

@@ -178,6 +178,17 @@ fk_status fk_kmeans_plus_plus_f32(fk_ctx *ctx, const float *x, int64_t n, int64_
                                   const double *draws, int64_t n_draws, uint64_t seed,
                                   float *centers_out, int64_t *draws_used_out);
 
+/* Diagnostics for the tests (no reference counterpart): one BF16 tensor-core
+ * assignment pass of x (n*d f32, device memory) against c (k*d f64, device
+ * memory). Returns the raw FP32 accumulators of the first 128-row tile of the
+ * first centre slice (dump: 128 x kp), the BF16 operands (xb: first 128 rows
+ * x d_pad; cb: k_pad x d_pad; aug: k_pad x 16), the per-slice top-2 records
+ * (top: parts x n x 16 bytes) and the plan {d_pad, kp, parts, k_pad, grid,
+ * error word}. Buffers are sized by the caller from the plan's upper bounds. */
+fk_status fk_debug_tc_probe(fk_ctx *ctx, const float *x_dev, int64_t n, int64_t d, const double *c_dev,
+                            int64_t k, float *dump, uint16_t *xb, uint16_t *cb, uint16_t *aug, void *top,
+                            int32_t *plan);
+
 #ifdef __cplusplus
 }
 #endif
