@@ -74,10 +74,11 @@ struct MixedStats {
     float pad;
 };
 
-// Best and second-best score of one row over one slice of the centres.
+// Best and second-best score of one row over one slice of the centres, and
+// u3, an upper bound of every other score in the slice.
 struct alignas(16) Top2 {
-    float v1, v2;
-    int i1, i2;
+    float v1, v2, u3, pad;
+    int i1, i2, pad1, pad2;
 };
 
 // Launch plan of the tensor-core assignment (fk_tc.cu).
@@ -108,7 +109,7 @@ enum BufSlot {
     BUF_X = 0, BUF_XC, BUF_C0, BUF_C1, BUF_CBEST, BUF_LABELS, BUF_LBEST, BUF_MIND,
     BUF_MEMBERS, BUF_SEGHIST, BUF_SCAN_TMP, BUF_COUNTS, BUF_PARTIAL, BUF_SCALARS,
     BUF_OUT, BUF_OUT2, BUF_KPP0, BUF_KPP1, BUF_KPP2, BUF_KPP3, BUF_DRAWS,
-    BUF_XB, BUF_XNORM, BUF_CB, BUF_CAUX, BUF_TOP2, BUF_FLAGS, BUF_FULL, BUF_CF32,
+    BUF_XB, BUF_XNORM, BUF_CB, BUF_CAUX, BUF_TOP2, BUF_FLAGS, BUF_FULL, BUF_CF32, BUF_CF32C,
     BUF_COUNT
 };
 

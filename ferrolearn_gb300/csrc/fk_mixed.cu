@@ -27,6 +27,7 @@
 #include <cuda_bf16.h>
 
 #include <cstddef>
+#include <type_traits>
 #include <vector>
 
 #include "fk_internal.cuh"
@@ -117,11 +118,12 @@ __global__ void prep_rows_kernel(const TX *__restrict__ x, int64_t n, int d, int
 // ||c'||, ||c' - ch||, ||ch||, ||c'||^2 / 2, ||c|| over the real centres.
 __global__ void prep_centres_kernel(const double *__restrict__ c, int k, int k_pad, int d, int d_pad,
                                     const double *__restrict__ mu, __nv_bfloat16 *__restrict__ cb,
-                                    double *__restrict__ half_norm, MixedStats *stats) {
+                                    double *__restrict__ half_norm, float *__restrict__ c32,
+                                    float *__restrict__ ec32, MixedStats *stats) {
     const int lane = threadIdx.x & 31;
     const int q = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     if (q >= k_pad) return;
-    double cn2 = 0.0, ec2 = 0.0, ch2 = 0.0, co2 = 0.0;
+    double cn2 = 0.0, ec2 = 0.0, ch2 = 0.0, co2 = 0.0, e32 = 0.0;
     for (int j = lane; j < d_pad; j += 32) {
         __nv_bfloat16 h = __float2bfloat16_rn(0.f);
         if (q < k && j < d) {
@@ -133,6 +135,9 @@ __global__ void prep_centres_kernel(const double *__restrict__ c, int k, int k_p
             ec2 += (cc - hv) * (cc - hv);
             ch2 += hv * hv;
             co2 += cv * cv;
+            float f = (float)cv;
+            c32[(int64_t)q * d + j] = f;
+            e32 += (cv - (double)f) * (cv - (double)f);
         }
         cb[(int64_t)q * d_pad + j] = h;
     }
@@ -140,8 +145,10 @@ __global__ void prep_centres_kernel(const double *__restrict__ c, int k, int k_p
     ec2 = warp_sum_d(ec2);
     ch2 = warp_sum_d(ch2);
     co2 = warp_sum_d(co2);
+    e32 = warp_sum_d(e32);
     if (lane == 0 && q < k) {
         const double up = 1.0 + 1e-12;
+        ec32[q] = __double2float_ru(sqrt(e32) * up);
         half_norm[q] = 0.5 * cn2;
         atomic_max_pos(&stats->cn_max, __double2float_ru(sqrt(cn2) * up));
         atomic_max_pos(&stats->ec_max, __double2float_ru(sqrt(ec2) * up));
@@ -178,17 +185,17 @@ __global__ void prep_aug_kernel(const double *__restrict__ half_norm, int k, int
 }
 
 // --------------------------------------------------------------- finalize --
-__device__ __forceinline__ void merge_top2(float &v1, int &i1, float &v2, int &i2, float w1, int j1, float w2, int j2,
-                                           float &u3) {
-    // Merge candidate pair (w1 >= w2) into (v1 >= v2); u3 tracks an upper
-    // bound of every value that is not kept in the top two.
+// Merge of two slice records: (v1 >= v2, i1, i2) with u3 bounding the rest,
+// and the same for the other slice.
+__device__ __forceinline__ void merge_top2(float &v1, int &i1, float &v2, int &i2, float &u3, float w1, int j1,
+                                           float w2, int j2, float wu) {
     if (w1 > v1) {
         if (v1 > w2) {
             u3 = fmaxf(u3, fmaxf(v2, w2));
             v2 = v1;
             i2 = i1;
         } else {
-            u3 = fmaxf(u3, v1);
+            u3 = fmaxf(u3, fmaxf(v1, wu));
             v2 = w2;
             i2 = j2;
         }
@@ -209,14 +216,12 @@ __global__ void finalize_kernel(const Top2 *__restrict__ parts, int nparts, int6
                                 int32_t *__restrict__ full_list, DevScalars *sc) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    // Each slice's third-best value is at most its second-best.
     Top2 t = parts[i];
-    float v1 = t.v1, v2 = t.v2, u3 = t.v2;
+    float v1 = t.v1, v2 = t.v2, u3 = t.u3;
     int i1 = t.i1, i2 = t.i2;
     for (int p = 1; p < nparts; p++) {
         Top2 o = parts[(int64_t)p * n + i];
-        u3 = fmaxf(u3, o.v2);
-        merge_top2(v1, i1, v2, i2, o.v1, o.i1, o.v2, o.i2, u3);
+        merge_top2(v1, i1, v2, i2, u3, o.v1, o.i1, o.v2, o.i2, o.u3);
     }
     const float4 ri = rowinfo[i];
     const double xn = ri.x, ex = ri.y, xo = ri.z;
@@ -258,9 +263,31 @@ __device__ __forceinline__ bool near_tie(double a, double b) {
     return fabs(a - b) <= 1e-12 * lo;
 }
 
-// One thread per listed row: exact FP64 distances to its two candidates.
+// FP32 direct form with a rigorous bound of its distance from the exact
+// real distance: (d+3) 2^-23 d32 for the roundings of the differences, the
+// squares and the running sum, plus the effect of the centre's rounding to
+// f32 (ec = ||c - c32||), plus the FP64 oracle's own rounding.
+__device__ __forceinline__ float sqeuc32(const float *__restrict__ x, const float *__restrict__ c, int d) {
+    float acc = 0.f;
+    for (int j = 0; j < d; j++) {
+        float t = x[j] - c[j];
+        acc = fmaf(t, t, acc);
+    }
+    return acc;
+}
+
+__device__ __forceinline__ double bound32(double d32, double ec, int d) {
+    double r = sqrt(d32 > 0.0 ? d32 : 0.0);
+    return ((double)(d + 3) * 1.1920928955078125e-07 * d32 + 2.0 * r * ec + 3.0 * ec * ec +
+            (double)(d + 4) * 2.220446049250313e-16 * d32) * 1.01 + 1e-30;
+}
+
+// One thread per listed row: FP32 distances to the two candidates decide the
+// row when their bounded intervals do not overlap; otherwise both are scored
+// exactly in FP64 (direct form, strict < over increasing index).
 template <typename TX>
 __global__ void pair_rescore_kernel(const TX *__restrict__ x, int d, const double *__restrict__ c,
+                                    const float *__restrict__ c32, const float *__restrict__ ec32,
                                     const int4 *__restrict__ list, DevScalars *sc, int32_t *__restrict__ labels) {
     const unsigned long long cnt = sc->flag_count;
     for (unsigned long long s = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; s < cnt;
@@ -268,9 +295,21 @@ __global__ void pair_rescore_kernel(const TX *__restrict__ x, int d, const doubl
         int4 e = list[s];
         const TX *row = x + (int64_t)e.x * d;
         int a = e.y < e.z ? e.y : e.z, b = e.y < e.z ? e.z : e.y;
+        if constexpr (std::is_same<TX, float>::value) {
+            const double da = sqeuc32(row, c32 + (int64_t)a * d, d);
+            const double db = sqeuc32(row, c32 + (int64_t)b * d, d);
+            const double ea = bound32(da, ec32[a], d), eb = bound32(db, ec32[b], d);
+            if (da + ea < db - eb) {  // false for any NaN or infinity
+                labels[e.x] = a;
+                continue;
+            }
+            if (db + eb < da - ea) {
+                labels[e.x] = b;
+                continue;
+            }
+        }
         double da = sqeuc64(row, c + (int64_t)a * d, d);
         double db = sqeuc64(row, c + (int64_t)b * d, d);
-        // strict < from F::MAX over increasing index
         int best = 0;
         double bd = DBL_MAX;
         if (da < bd) { bd = da; best = a; }
@@ -281,9 +320,14 @@ __global__ void pair_rescore_kernel(const TX *__restrict__ x, int d, const doubl
     }
 }
 
-// One warp per listed row: exact FP64 distances to every centre.
+// One warp per listed row: FP32 distances to every centre give an upper
+// bound UB of the minimum; only centres whose lower bound reaches UB (or
+// whose FP32 value is not finite) are scored exactly in FP64, and the lowest
+// index wins among equal FP64 distances below F::MAX, exactly as
+// nearest_center.
 template <typename TX>
-__global__ void full_rescore_kernel(const TX *__restrict__ x, int d, const double *__restrict__ c, int k,
+__global__ void full_rescore_kernel(const TX *__restrict__ x, int d, const double *__restrict__ c,
+                                    const float *__restrict__ c32, const float *__restrict__ ec32, int k,
                                     const int32_t *__restrict__ list, DevScalars *sc, int32_t *__restrict__ labels) {
     const unsigned long long cnt = sc->full_count;
     const int lane = threadIdx.x & 31;
@@ -292,9 +336,25 @@ __global__ void full_rescore_kernel(const TX *__restrict__ x, int d, const doubl
     for (unsigned long long s = wid; s < cnt; s += nw) {
         const int64_t r = list[s];
         const TX *row = x + r * d;
+        double ub = INFINITY;
+        if constexpr (std::is_same<TX, float>::value) {
+            for (int q = lane; q < k; q += 32) {
+                double v = sqeuc32(row, c32 + (int64_t)q * d, d);
+                double e = bound32(v, ec32[q], d);
+                double hi = v + e;
+                if (hi < ub) ub = hi;  // NaN never lowers the bound
+            }
+#pragma unroll
+            for (int off = 16; off >= 1; off >>= 1) ub = fmin(ub, __shfl_xor_sync(0xffffffffu, ub, off));
+        }
         double b1 = DBL_MAX, b2 = DBL_MAX;
         int i1 = INT32_MAX;
         for (int q = lane; q < k; q += 32) {
+            if constexpr (std::is_same<TX, float>::value) {
+                double v = sqeuc32(row, c32 + (int64_t)q * d, d);
+                double e = bound32(v, ec32[q], d);
+                if (v - e > ub) continue;  // certainly above the minimum
+            }
             double v = sqeuc64(row, c + (int64_t)q * d, d);
             if (v < b1) { b2 = b1; b1 = v; i1 = q; }
             else if (v < b2) { b2 = v; }
@@ -388,7 +448,10 @@ void run_assign_mixed(Ctx &ctx, const TX *x, int64_t n, int d, const double *c, 
     __nv_bfloat16 *cb = (__nv_bfloat16 *)ctx.get(BUF_CB, sizeof(__nv_bfloat16) * (size_t)mp.k_pad * mp.d_pad);
     __nv_bfloat16 *caug = (__nv_bfloat16 *)ctx.get(BUF_CAUX, sizeof(__nv_bfloat16) * (size_t)mp.k_pad * 16 + 8192);
     double *half_norm = (double *)ctx.get(BUF_MIND, sizeof(double) * (size_t)mp.k_pad);
-    prep_centres_kernel<<<(mp.k_pad + 7) / 8, 256, 0, s>>>(c, k, mp.k_pad, d, mp.d_pad, mu, cb, half_norm, stats);
+    float *c32 = (float *)ctx.get(BUF_CF32C, sizeof(float) * ((size_t)k * d + (size_t)k) + 64);
+    float *ec32 = c32 + (size_t)k * d;
+    prep_centres_kernel<<<(mp.k_pad + 7) / 8, 256, 0, s>>>(c, k, mp.k_pad, d, mp.d_pad, mu, cb, half_norm, c32, ec32,
+                                                           stats);
     FK_LAUNCH_CHECK();
     prep_aug_kernel<<<(mp.k_pad + 255) / 256, 256, 0, s>>>(half_norm, k, mp.k_pad, caug, stats);
     FK_LAUNCH_CHECK();
@@ -403,9 +466,9 @@ void run_assign_mixed(Ctx &ctx, const TX *x, int64_t n, int d, const double *c, 
                                                                mp.mu_norm, labels, pairs, full, sc);
     FK_LAUNCH_CHECK();
     const int grid = ctx.num_sms * 4;
-    pair_rescore_kernel<TX><<<grid, 256, 0, s>>>(x, d, c, pairs, sc, labels);
+    pair_rescore_kernel<TX><<<grid, 256, 0, s>>>(x, d, c, c32, ec32, pairs, sc, labels);
     FK_LAUNCH_CHECK();
-    full_rescore_kernel<TX><<<grid, 256, 0, s>>>(x, d, c, k, full, sc, labels);
+    full_rescore_kernel<TX><<<grid, 256, 0, s>>>(x, d, c, c32, ec32, k, full, sc, labels);
     FK_LAUNCH_CHECK();
 }
 
@@ -446,7 +509,9 @@ void debug_tc_probe(Ctx &ctx, const float *x, int64_t n, int d, const double *c,
     __nv_bfloat16 *cb = (__nv_bfloat16 *)ctx.get(BUF_CB, sizeof(__nv_bfloat16) * (size_t)mp.k_pad * mp.d_pad);
     __nv_bfloat16 *caug = (__nv_bfloat16 *)ctx.get(BUF_CAUX, sizeof(__nv_bfloat16) * (size_t)mp.k_pad * 16 + 8192);
     double *half_norm = (double *)ctx.get(BUF_MIND, sizeof(double) * (size_t)mp.k_pad);
-    prep_centres_kernel<<<(mp.k_pad + 7) / 8, 256, 0, s>>>(c, k, mp.k_pad, d, mp.d_pad, mu, cb, half_norm, stats);
+    float *c32 = (float *)ctx.get(BUF_CF32C, sizeof(float) * ((size_t)k * d + (size_t)k) + 64);
+    prep_centres_kernel<<<(mp.k_pad + 7) / 8, 256, 0, s>>>(c, k, mp.k_pad, d, mp.d_pad, mu, cb, half_norm, c32,
+                                                           c32 + (size_t)k * d, stats);
     FK_LAUNCH_CHECK();
     prep_aug_kernel<<<(mp.k_pad + 255) / 256, 256, 0, s>>>(half_norm, k, mp.k_pad, caug, stats);
     FK_LAUNCH_CHECK();

@@ -178,28 +178,37 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
 
 __device__ __forceinline__ void epi_bar() { asm volatile("bar.sync 1, 256;" ::: "memory"); }
 
-// Running top-2 merge of a candidate pair (w1 >= w2, as ordered keys).
-__device__ __forceinline__ void merge2(uint32_t &R1, int &I1, uint32_t &R2, int &I2, uint32_t w1, int j1, uint32_t w2,
-                                       int j2) {
+// Running top-2 merge with a bound of the rest. (R1 >= R2, I1, I2) are the
+// best two keys so far and U bounds every key seen but not kept. The merged
+// result (w1 >= w2, j1, j2) comes with wu, a bound of its own rest (wu <= w2).
+__device__ __forceinline__ void merge_res(uint32_t &R1, int &I1, uint32_t &R2, int &I2, uint32_t &U, uint32_t w1,
+                                          int j1, uint32_t w2, int j2, uint32_t wu) {
     if (w1 > R1) {
         if (R1 > w2) {
+            U = max(U, max(R2, w2));
             R2 = R1;
             I2 = I1;
         } else {
+            U = max(U, max(R1, wu));
             R2 = w2;
             I2 = j2;
         }
         R1 = w1;
         I1 = j1;
     } else if (w1 > R2) {
+        U = max(U, max(R2, w2));
         R2 = w1;
         I2 = j1;
+    } else {
+        U = max(U, w1);
     }
 }
 
-// Ranks the 128 columns [HALF*128, HALF*128+128) of one accumulator block.
+// Ranks the 128 columns [HALF*128, HALF*128+128) of one accumulator block:
+// four interleaved top-2 chains (three integer min/max per element), merged
+// with the bound of the rest. Returns keys (value bits | code).
 template <int HALF>
-__device__ __forceinline__ void rank_half(uint32_t col_addr, uint32_t &b1, uint32_t &b2) {
+__device__ __forceinline__ void rank_half(uint32_t col_addr, uint32_t &b1, uint32_t &b2, uint32_t &bu) {
     uint32_t a1[4] = {0u, 0u, 0u, 0u}, a2[4] = {0u, 0u, 0u, 0u};
 #pragma unroll
     for (int ch = 0; ch < 4; ch++) {
@@ -218,12 +227,10 @@ __device__ __forceinline__ void rank_half(uint32_t col_addr, uint32_t &b1, uint3
     }
     b1 = a1[0];
     b2 = a2[0];
+    bu = a2[0];
+    int d1 = 0, d2 = 0;  // indices are carried inside the keys
 #pragma unroll
-    for (int qd = 1; qd < 4; qd++) {
-        const uint32_t n1 = max(b1, a1[qd]);
-        b2 = max(max(b2, a2[qd]), min(b1, a1[qd]));
-        b1 = n1;
-    }
+    for (int qd = 1; qd < 4; qd++) merge_res(b1, d1, b2, d2, bu, a1[qd], 0, a2[qd], 0, a2[qd]);
 }
 
 __global__ void __launch_bounds__(NTHREADS, 1)
@@ -353,7 +360,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         uint32_t item = 0;
         bool dead = false;
         for (int64_t t = q; t < p.tiles; t += tstride) {
-            uint32_t R1 = 0u, R2 = 0u;
+            uint32_t R1 = 0u, R2 = 0u, U = 0u;
             int I1 = -1, I2 = -1;
             for (int b = 0; b < p.nblocks; b++, item++) {
                 const int buf = (int)(item & 1u);
@@ -371,25 +378,29 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                                 __uint_as_float(r[e]);
                     }
                 }
-                uint32_t b1, b2;
+                uint32_t b1, b2, bu;
                 if (half == 0)
-                    rank_half<0>(col, b1, b2);
+                    rank_half<0>(col, b1, b2, bu);
                 else
-                    rank_half<1>(col, b1, b2);
+                    rank_half<1>(col, b1, b2, bu);
                 tc_fence_before();
                 __syncwarp();
                 if (lane == 0) mbar_arrive(bar_aempty(buf));
                 const int base = part * p.kp + b * BN + 255;
-                merge2(R1, I1, R2, I2, b1 & 0xFFFFFF00u, base - (int)(b1 & 0xFFu), b2 & 0xFFFFFF00u,
-                       base - (int)(b2 & 0xFFu));
+                merge_res(R1, I1, R2, I2, U, b1 & 0xFFFFFF00u, base - (int)(b1 & 0xFFu), b2 & 0xFFFFFF00u,
+                          base - (int)(b2 & 0xFFu), bu & 0xFFFFFF00u);
             }
-            if (half == 1) merge[row_local] = Top2{__uint_as_float(R1), __uint_as_float(R2), I1, I2};
+            if (half == 1)
+                merge[row_local] = Top2{__uint_as_float(R1), __uint_as_float(R2), __uint_as_float(U), 0.f, I1, I2, 0, 0};
             epi_bar();
             if (half == 0) {
                 const Top2 o = merge[row_local];
-                merge2(R1, I1, R2, I2, __float_as_uint(o.v1), o.i1, __float_as_uint(o.v2), o.i2);
+                merge_res(R1, I1, R2, I2, U, __float_as_uint(o.v1), o.i1, __float_as_uint(o.v2), o.i2,
+                          __float_as_uint(o.u3));
                 const int64_t row = t * BM + row_local;
-                if (row < p.n && !dead) p.out[(int64_t)part * p.n + row] = Top2{__uint_as_float(R1), __uint_as_float(R2), I1, I2};
+                if (row < p.n && !dead)
+                    p.out[(int64_t)part * p.n + row] =
+                        Top2{__uint_as_float(R1), __uint_as_float(R2), __uint_as_float(U), 0.f, I1, I2, 0, 0};
             }
             epi_bar();
         }

@@ -42,7 +42,7 @@ def _probe(x32, c64):
     xb = np.zeros(128 * d_pad, dtype=np.uint16)
     cb = np.zeros(kmax * d_pad, dtype=np.uint16)
     aug = np.zeros(kmax * 16, dtype=np.uint16)
-    top = np.zeros(n * 8 * 4, dtype=np.float32)
+    top = np.zeros(n * 8 * 8, dtype=np.float32)
     plan = np.zeros(8, dtype=np.int32)
     st = _native.lib().fk_debug_tc_probe(ctx.handle, C.c_void_p(xd.data_ptr()), n, d, C.c_void_p(cd.data_ptr()), k,
                                          dump.ctypes.data_as(C.c_void_p), xb.ctypes.data_as(C.c_void_p),
@@ -56,7 +56,7 @@ def _probe(x32, c64):
     cbf = _bf16_to_f32(cb[: k_pad * d_pad]).reshape(k_pad, d_pad).astype(np.float64)
     augf = _bf16_to_f32(aug[: k_pad * 16]).reshape(k_pad, 16).astype(np.float64)
     acc = dump[: 128 * kp].reshape(128, kp)[:rows]
-    recs = top[: parts * n * 4].view(np.uint32).reshape(parts, n, 4)
+    recs = top[: parts * n * 8].view(np.uint32).reshape(parts, n, 8)
     return dict(acc=acc, xb=xbf, cb=cbf, aug=augf, kp=kp, parts=parts, k_pad=k_pad, recs=recs)
 
 
@@ -92,7 +92,9 @@ def test_tc_top2_records(n, d, k):
     torch = pytest.importorskip("torch")  # noqa: F841
     recs = r["recs"]
     v1 = recs[..., 0].view(np.float32)
-    i1 = recs[..., 2].view(np.int32)
+    u3 = recs[..., 2].view(np.float32)
+    i1 = recs[..., 4].view(np.int32)
+    i2 = recs[..., 5].view(np.int32)
     # the best over all slices must be a centre whose exact score is within the
     # truncation + accumulation slack of the true maximum (rows of the first tile)
     rows = r["xb"].shape[0]
@@ -107,6 +109,11 @@ def test_tc_top2_records(n, d, k):
         assert np.all(np.abs(v1[p, :rows] - m) <= 2 ** -14 * np.abs(m) + 1e-5 * best)
         picked = sl[np.arange(rows), i1[p, :rows] - lo]
         assert np.all(m - picked <= 2 ** -14 * np.abs(m) + 1e-5 * best)
+        # u3 bounds every score of the slice other than the two kept ones
+        rest = sl.copy()
+        rest[np.arange(rows), i1[p, :rows] - lo] = -np.inf
+        rest[np.arange(rows), i2[p, :rows] - lo] = -np.inf
+        assert np.all(rest.max(1) <= u3[p, :rows] + 2 ** -14 * np.abs(m) + 1e-5 * best)
 
 
 @pytest.mark.parametrize("n,d,k", [(4096, 128, 1024), (5000, 64, 100), (3000, 16, 9), (2500, 100, 300)])
