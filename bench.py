@@ -267,7 +267,7 @@ def run_ours(args):
         "pt_k_per_s": ips * n * k,
         "phase_ms_per_iter": {"assign": assign_ms, "update": rep["ms_update"] / iters},
         "recheck": {"rows": rep["rows_rechecked"], "full_rescan": rep["rows_full_rescan"],
-                    "near_ties": rep["near_tie_rows"],
+                    "fp64_rows": rep["rows_fp64"], "near_ties": rep["near_tie_rows"],
                     "fraction": rep["rows_rechecked"] / max(1, rep["rows_assigned"])},
         "gpu_launches": launches,
         "clocks": clocks.summary(),

@@ -23,6 +23,7 @@ EXPORTS = [
     "fk_kmeans_predict_f64", "fk_kmeans_predict_f32", "fk_kmeans_predict_f32x64",
     "fk_kmeans_transform_f64", "fk_kmeans_transform_f32",
     "fk_kmeans_plus_plus_f64", "fk_kmeans_plus_plus_f32", "fk_debug_tc_probe",
+    "fk_debug_measure_peaks",
 ]
 
 
@@ -49,6 +50,7 @@ class FitReport(C.Structure):
         ("rows_assigned", C.c_int64),
         ("rows_rechecked", C.c_int64),
         ("rows_full_rescan", C.c_int64),
+        ("rows_fp64", C.c_int64),
         ("near_tie_rows", C.c_int64),
         ("ms_init", C.c_double),
         ("ms_assign", C.c_double),
@@ -98,6 +100,8 @@ def _declare(lib):
         f.restype = st
     lib.fk_debug_tc_probe.argtypes = [p, p, i64, i64, p, i64, p, p, p, p, p, p]
     lib.fk_debug_tc_probe.restype = st
+    lib.fk_debug_measure_peaks.argtypes = [p, p]
+    lib.fk_debug_measure_peaks.restype = st
 
 
 def lib():

@@ -230,8 +230,9 @@ void read_scalars(Ctx &ctx, DevScalars *dev) {
 void accumulate_report(fk_fit_report *rep, const DevScalars &h, int64_t n) {
     if (!rep) return;
     rep->rows_assigned += n;
-    rep->rows_rechecked += (int64_t)h.recheck_rows;
-    rep->rows_full_rescan += (int64_t)h.full_rows;
+    rep->rows_rechecked += (int64_t)(h.flag_count + h.full_count);
+    rep->rows_full_rescan += (int64_t)h.full_count;
+    rep->rows_fp64 += (int64_t)h.recheck_rows;
     rep->near_tie_rows += (int64_t)h.near_tie_rows;
 }
 
@@ -724,6 +725,15 @@ fk_status fk_kmeans_transform_f32(fk_ctx *ctx, const float *c, int64_t k, int64_
 fk_status fk_kmeans_plus_plus_f64(fk_ctx *ctx, const double *x, int64_t n, int64_t d, int64_t k, const double *draws,
                                   int64_t n_draws, uint64_t seed, double *out, int64_t *used) {
     return guarded(ctx, [&] { return fk::kpp_impl<double>(ctx, x, n, d, k, draws, n_draws, seed, out, used); });
+}
+
+fk_status fk_debug_measure_peaks(fk_ctx *ctx, double *out) {
+    return guarded(ctx, [&] {
+        fk::Ctx &c = *reinterpret_cast<fk::Ctx *>(ctx);
+        c.bind();
+        fk::measure_peaks(c, out);
+        return FK_OK;
+    });
 }
 
 fk_status fk_debug_tc_probe(fk_ctx *ctx, const float *x_dev, int64_t n, int64_t d, const double *c_dev, int64_t k,

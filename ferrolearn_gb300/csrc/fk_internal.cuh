@@ -197,6 +197,7 @@ void plan_tc(Ctx &ctx, MixedPlan &mp, int64_t n, int d, int k);
 void launch_tc_assign(Ctx &ctx, MixedPlan &mp, const void *xb, const void *cb, const void *caug, Top2 *out,
                       DevScalars *sc, float *dump = nullptr);
 
+void measure_peaks(Ctx &ctx, double *out);
 void debug_tc_probe(Ctx &ctx, const float *x, int64_t n, int d, const double *c, int k, float *dump_out,
                     uint16_t *xb_out, uint16_t *cb_out, uint16_t *aug_out, Top2 *top_out, int *plan_out);
 

@@ -76,8 +76,11 @@ typedef struct fk_fit_report {
     int64_t best_run;          /* index of the run that was kept           */
     int64_t iterations_total;  /* Lloyd iterations over all runs           */
     int64_t rows_assigned;     /* rows x iterations                        */
-    int64_t rows_rechecked;    /* mixed: rows re-scored in FP64            */
-    int64_t rows_full_rescan;  /* mixed: rows re-scored against all k      */
+    int64_t rows_rechecked;    /* mixed: rows whose margin fell inside the
+                                  bound and were re-scored (FP32 + FP64)   */
+    int64_t rows_full_rescan;  /* mixed: of those, rows re-scored against
+                                  every centre                             */
+    int64_t rows_fp64;         /* mixed: rows that needed FP64 scores      */
     int64_t near_tie_rows;     /* mixed: re-scored rows whose FP64 margin
                                   is below 1e-12 relative                  */
     double ms_init;            /* device time, k-means++                   */
@@ -177,6 +180,11 @@ fk_status fk_kmeans_plus_plus_f64(fk_ctx *ctx, const double *x, int64_t n, int64
 fk_status fk_kmeans_plus_plus_f32(fk_ctx *ctx, const float *x, int64_t n, int64_t d, int64_t k,
                                   const double *draws, int64_t n_draws, uint64_t seed,
                                   float *centers_out, int64_t *draws_used_out);
+
+/* Diagnostics (no reference counterpart): CUDA-core throughput of this GPU,
+ * out[0] FP32 FMA flop/s, [1] FP64 FMA flop/s, [2] FP64 add op/s, [3] FP32
+ * add op/s, [4] FP64 add latency in cycles, [5] FP32 add latency. */
+fk_status fk_debug_measure_peaks(fk_ctx *ctx, double *out);
 
 /* Diagnostics for the tests (no reference counterpart): one BF16 tensor-core
  * assignment pass of x (n*d f32, device memory) against c (k*d f64, device
