@@ -212,7 +212,12 @@ void lloyd_iteration(Ctx &ctx, const TX *x, int64_t n, int d, const TC *c, int k
             launch_update_centroids<TX, TC>(plan, x, d, members, seg, c, nc, sc, s);
         } else {
             double *part = (double *)ctx.get(BUF_OUT2, sizeof(double) * (size_t)plan.k * d + 64);
-            launch_update_centroids<TX, TC>(plan, x, d, members, seg, c, nc, sc, s, part);
+            if constexpr (std::is_same<TX, float>::value && std::is_same<TC, double>::value) {
+                const MixedStats *st = (const MixedStats *)ctx.get(BUF_CF32, sizeof(MixedStats));
+                launch_update_centroids_exact(plan, x, d, members, seg, c, nc, sc, &st->amax, part, s);
+            } else {
+                launch_update_centroids<TX, TC>(plan, x, d, members, seg, c, nc, sc, s, part);
+            }
             launch_mixed_inertia(ctx, part, (int64_t)plan.k * d, sc);
         }
     }

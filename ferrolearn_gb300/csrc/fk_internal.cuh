@@ -58,6 +58,7 @@ struct DevScalars {
     unsigned long long near_tie_rows;
     unsigned long long flag_count;  // number of rows queued for re-check
     unsigned long long full_count;  // number of rows queued for a full re-scan
+    unsigned long long over_count;  // full re-scan rows with more than 4 FP32 candidates
     unsigned long long error_word;  // nonzero: a bounded device wait gave up
 };
 
@@ -65,13 +66,13 @@ struct DevScalars {
 // Bound ingredients of one assignment (floats rounded up; maxima via atomics).
 struct MixedStats {
     float xn_max;  // max_i ||xh_i||           (set once per X)
+    float amax;    // max |x_ij| over finite entries (set once per X)
     float cn_max;  // max_c ||c' ||            (per iteration from here on)
     float ec_max;  // max_c ||c' - ch||
     float ch_max;  // max_c ||ch||
     float h_max;   // max_c ||c'||^2 / 2
     float co_max;  // max_c ||c||  (uncentred, for the FP64 rounding term)
     float big;     // BIG of this iteration
-    float pad;
 };
 
 // Best and second-best score of one row over one slice of the centres, and
@@ -109,7 +110,7 @@ enum BufSlot {
     BUF_X = 0, BUF_XC, BUF_C0, BUF_C1, BUF_CBEST, BUF_LABELS, BUF_LBEST, BUF_MIND,
     BUF_MEMBERS, BUF_SEGHIST, BUF_SCAN_TMP, BUF_COUNTS, BUF_PARTIAL, BUF_SCALARS,
     BUF_OUT, BUF_OUT2, BUF_KPP0, BUF_KPP1, BUF_KPP2, BUF_KPP3, BUF_DRAWS,
-    BUF_XB, BUF_XNORM, BUF_CB, BUF_CAUX, BUF_TOP2, BUF_FLAGS, BUF_FULL, BUF_CF32, BUF_CF32C,
+    BUF_XB, BUF_XNORM, BUF_CB, BUF_CAUX, BUF_TOP2, BUF_FLAGS, BUF_FULL, BUF_CF32, BUF_CF32C, BUF_OVER,
     BUF_COUNT
 };
 
@@ -170,6 +171,12 @@ template <typename TX, typename TC>
 void launch_update_centroids(const SortPlan &p, const TX *x, int d, const int32_t *members,
                              const int32_t *seg_hist, const TC *old_c, TC *new_c,
                              DevScalars *scalars, cudaStream_t s, double *inertia_part = nullptr);
+
+// Mixed precisions: exact 128-bit fixed-point cluster sums of an f32 X,
+// rounded once to f64, divided by the counts; plus the inertia partials.
+void launch_update_centroids_exact(const SortPlan &p, const float *x, int d, const int32_t *members,
+                                   const int32_t *seg_hist, const double *old_c, double *new_c, DevScalars *scalars,
+                                   const float *amax, double *inertia_part, cudaStream_t s);
 
 void launch_labels_to_u64(const int32_t *l, int64_t n, uint64_t *out, cudaStream_t s);
 template <typename TS, typename TD>

@@ -50,19 +50,20 @@ __device__ __forceinline__ double warp_sum_d(double v) {
 }
 
 // ----------------------------------------------------------- row prep --
-// Column means in f64 (order irrelevant: mu only centres the data).
+// Column means (mu only centres the data, so any finite value is valid:
+// partial sums in f32, non-finite entries skipped, the final fold in f64).
 template <typename TX>
 __global__ void col_mean_partial_kernel(const TX *__restrict__ x, int64_t n, int d, int64_t rows_per,
                                         double *__restrict__ part) {
     int j = threadIdx.x + blockIdx.y * blockDim.x;
     if (j >= d) return;
     int64_t lo = (int64_t)blockIdx.x * rows_per, hi = min(n, lo + rows_per);
-    double s = 0.0;
+    float s = 0.f;
     for (int64_t i = lo; i < hi; i++) {
-        double v = (double)x[i * d + j];
-        if (isfinite(v)) s += v;  // mu only centres the data; non-finite rows are re-scored in full
+        float v = (float)x[i * d + j];
+        if (isfinite(v)) s += v;
     }
-    part[(int64_t)blockIdx.x * d + j] = s;
+    part[(int64_t)blockIdx.x * d + j] = (double)s;
 }
 
 __global__ void col_mean_final_kernel(const double *__restrict__ part, int nparts, int64_t n, int d,
@@ -71,45 +72,63 @@ __global__ void col_mean_final_kernel(const double *__restrict__ part, int npart
     if (j >= d) return;
     double s = 0.0;
     for (int p = 0; p < nparts; p++) s += part[(int64_t)p * d + j];
-    double m = s / (double)n;
-    mu[j] = m;
-    mu32[j] = (float)m;
+    float m = (float)(s / (double)n);
+    if (!isfinite(m)) m = 0.f;
+    mu32[j] = m;
+    mu[j] = (double)m;  // the centring is by the f32 value, for rows and centres alike
+}
+
+__device__ __forceinline__ float warp_sum_f(float v) {
+#pragma unroll
+    for (int off = 16; off >= 1; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    return v;
 }
 
 // One warp per row: BF16 copy of x - mu (row stride d_pad, zero padded) and
-// the row's bound ingredients {||xh||, ||x' - xh||, ||x||} rounded up.
+// the row's bound ingredients {||xh||, ||x' - xh||, ||x||}, all computed in
+// f32 and then inflated to upper bounds: t = fl(x - mu) differs from x - mu
+// by at most 2^-24 |t|, xh = bf16(t) and t - xh is exact, so
+// ||x' - xh|| <= ||t - xh|| + 2^-24 ||t||; each sum of squares is scaled by
+// (1 + (d + 64) 2^-23) to cover its own rounding before the rounded-up root.
+// Also records max |x| (for the fixed-point centroid sums) and max ||xh||.
 template <typename TX>
 __global__ void prep_rows_kernel(const TX *__restrict__ x, int64_t n, int d, int d_pad,
-                                 const double *__restrict__ mu, __nv_bfloat16 *__restrict__ xb,
+                                 const float *__restrict__ mu32, __nv_bfloat16 *__restrict__ xb,
                                  float4 *__restrict__ rowinfo, MixedStats *stats) {
     const int lane = threadIdx.x & 31;
     const int64_t row = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     if (row >= n) return;
-    double xn2 = 0.0, ex2 = 0.0, xo2 = 0.0;
+    float xn2 = 0.f, ex2 = 0.f, tn2 = 0.f, xo2 = 0.f, amax = 0.f;
     for (int j = lane; j < d_pad; j += 32) {
         __nv_bfloat16 h = __float2bfloat16_rn(0.f);
         if (j < d) {
-            double xv = (double)x[row * d + j];
-            double xc = xv - mu[j];
-            h = __float2bfloat16_rn((float)xc);
-            double hv = (double)__bfloat162float(h);
-            double e = xc - hv;
-            xn2 += hv * hv;
-            ex2 += e * e;
-            xo2 += xv * xv;
+            float xv = (float)x[row * d + j];
+            float t = __fsub_rn(xv, mu32[j]);
+            h = __float2bfloat16_rn(t);
+            float hv = __bfloat162float(h);
+            float e = __fsub_rn(t, hv);
+            xn2 = __fmaf_rn(hv, hv, xn2);
+            ex2 = __fmaf_rn(e, e, ex2);
+            tn2 = __fmaf_rn(t, t, tn2);
+            xo2 = __fmaf_rn(xv, xv, xo2);
+            amax = fmaxf(amax, fabsf(xv));
         }
         xb[row * d_pad + j] = h;
     }
-    xn2 = warp_sum_d(xn2);
-    ex2 = warp_sum_d(ex2);
-    xo2 = warp_sum_d(xo2);
+    xn2 = warp_sum_f(xn2);
+    ex2 = warp_sum_f(ex2);
+    tn2 = warp_sum_f(tn2);
+    xo2 = warp_sum_f(xo2);
+#pragma unroll
+    for (int off = 16; off >= 1; off >>= 1) amax = fmaxf(amax, __shfl_xor_sync(0xffffffffu, amax, off));
     if (lane == 0) {
-        const double up = 1.0 + 1e-12;
-        float xn = __double2float_ru(sqrt(xn2) * up);
-        float ex = __double2float_ru(sqrt(ex2) * up);
-        float xo = __double2float_ru(sqrt(xo2) * up);
+        const float up = 1.0f + (float)(d + 64) * 1.1920929e-07f;
+        float xn = __fsqrt_ru(__fmul_ru(xn2, up));
+        float ex = __fadd_ru(__fsqrt_ru(__fmul_ru(ex2, up)), __fmul_ru(__fsqrt_ru(__fmul_ru(tn2, up)), 5.9604645e-08f));
+        float xo = __fsqrt_ru(__fmul_ru(xo2, up));
         rowinfo[row] = make_float4(xn, ex, xo, 0.f);
-        if (xn == xn) atomic_max_pos(&stats->xn_max, xn);  // NaN rows are re-scored in full anyway
+        if (xn == xn && xn < INFINITY) atomic_max_pos(&stats->xn_max, xn);  // non-finite rows are re-scored in full
+        if (amax < INFINITY) atomic_max_pos(&stats->amax, amax);
     }
 }
 
@@ -329,7 +348,7 @@ template <typename TX>
 __global__ void full_rescore_kernel(const TX *__restrict__ x, int d, const double *__restrict__ c,
                                     const float *__restrict__ c32, const float *__restrict__ ec32, int k,
                                     const int32_t *__restrict__ list, DevScalars *sc, int32_t *__restrict__ labels) {
-    const unsigned long long cnt = sc->full_count;
+    const unsigned long long cnt = std::is_same<TX, float>::value ? sc->over_count : sc->full_count;
     const int lane = threadIdx.x & 31;
     const unsigned long long wid = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const unsigned long long nw = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
@@ -377,6 +396,184 @@ __global__ void full_rescore_kernel(const TX *__restrict__ x, int d, const doubl
             atomicAdd(&sc->recheck_rows, 1ULL);
             atomicAdd(&sc->full_rows, 1ULL);
             if (i1 != INT32_MAX && b2 < DBL_MAX && near_tie(b1, b2)) atomicAdd(&sc->near_tie_rows, 1ULL);
+        }
+    }
+}
+
+// Tiled FP32 pass over the rows queued for a full re-score: 64 rows x 64
+// centres per block tile (4 x 4 per thread, centres staged in shared memory
+// like the direct-form kernel), keeping the four smallest FP32 distances of
+// every row. With UB = min(d32 + E32) over those four, a centre can only be
+// the FP64 minimum if d32 - E32 <= UB; if the fourth-smallest could still
+// qualify (or the row has no finite FP32 distance) the row goes to the
+// exhaustive per-row kernel. A single candidate is the answer; several are
+// scored exactly in FP64 (direct form, lowest index on ties).
+constexpr int FT_BM = 64, FT_BN = 64, FT_DJ = 16, FT_T = 256;
+
+__device__ __forceinline__ void top4_insert(float (&v)[4], int (&ix)[4], float val, int id) {
+    if (!(val < v[3])) return;  // also rejects NaN
+    if (val < v[2]) {
+        v[3] = v[2]; ix[3] = ix[2];
+        if (val < v[1]) {
+            v[2] = v[1]; ix[2] = ix[1];
+            if (val < v[0]) {
+                v[1] = v[0]; ix[1] = ix[0];
+                v[0] = val; ix[0] = id;
+            } else { v[1] = val; ix[1] = id; }
+        } else { v[2] = val; ix[2] = id; }
+    } else { v[3] = val; ix[3] = id; }
+}
+
+__global__ void __launch_bounds__(FT_T)
+full_tiled_kernel(const float *__restrict__ x, int d, const float *__restrict__ c32, const float *__restrict__ ec32,
+                  const double *__restrict__ c64, int k, const int32_t *__restrict__ list, DevScalars *sc,
+                  int32_t *__restrict__ labels, int32_t *__restrict__ over_list) {
+    __shared__ __align__(16) float xs[FT_DJ][FT_BM];
+    __shared__ __align__(16) float cs[FT_DJ][FT_BN];
+    __shared__ int rid[FT_BM];
+    __shared__ float tv[FT_BM][4];
+    __shared__ int ti[FT_BM][4];
+    __shared__ double dv[FT_BM][4];
+    __shared__ float ecmax_s;
+    const unsigned long long count = sc->full_count;
+    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+    if (tid == 0) {
+        float m = 0.f;
+        for (int q = 0; q < k; q++) m = fmaxf(m, ec32[q]);
+        ecmax_s = m;
+    }
+    for (unsigned long long tile = blockIdx.x; tile * FT_BM < count; tile += gridDim.x) {
+        __syncthreads();
+        if (tid < FT_BM) {
+            unsigned long long s = tile * FT_BM + tid;
+            rid[tid] = s < count ? list[s] : -1;
+        }
+        __syncthreads();
+        float bv[4][4];
+        int bi[4][4];
+#pragma unroll
+        for (int a = 0; a < 4; a++)
+#pragma unroll
+            for (int e = 0; e < 4; e++) { bv[a][e] = INFINITY; bi[a][e] = -1; }
+        for (int ct = 0; ct < k; ct += FT_BN) {
+            float acc[4][4];
+#pragma unroll
+            for (int a = 0; a < 4; a++)
+#pragma unroll
+                for (int b = 0; b < 4; b++) acc[a][b] = 0.f;
+            for (int j0 = 0; j0 < d; j0 += FT_DJ) {
+#pragma unroll
+                for (int e = 0; e < (FT_BM * FT_DJ) / FT_T; e++) {
+                    int idx = tid + e * FT_T;
+                    int r = idx / FT_DJ, jj = idx % FT_DJ;
+                    int gj = j0 + jj;
+                    int rr = rid[r];
+                    xs[jj][r] = (rr >= 0 && gj < d) ? x[(int64_t)rr * d + gj] : 0.f;
+                    int gc = ct + r;
+                    cs[jj][r] = (gc < k && gj < d) ? c32[(int64_t)gc * d + gj] : 0.f;
+                }
+                __syncthreads();
+                const int jn = min(FT_DJ, d - j0);
+                for (int jj = 0; jj < jn; jj++) {
+                    float xv[4], cv[4];
+#pragma unroll
+                    for (int a = 0; a < 4; a++) xv[a] = xs[jj][ty * 4 + a];
+#pragma unroll
+                    for (int b = 0; b < 4; b++) cv[b] = cs[jj][tx * 4 + b];
+#pragma unroll
+                    for (int a = 0; a < 4; a++)
+#pragma unroll
+                        for (int b = 0; b < 4; b++) {
+                            float t = xv[a] - cv[b];
+                            acc[a][b] = fmaf(t, t, acc[a][b]);
+                        }
+                }
+                __syncthreads();
+            }
+#pragma unroll
+            for (int a = 0; a < 4; a++)
+#pragma unroll
+                for (int b = 0; b < 4; b++) {
+                    int gc = ct + tx * 4 + b;
+                    if (gc < k) top4_insert(bv[a], bi[a], acc[a][b], gc);
+                }
+        }
+        // merge the 16 partial lists of each row (same half-warp)
+#pragma unroll
+        for (int a = 0; a < 4; a++) {
+#pragma unroll
+            for (int off = 8; off >= 1; off >>= 1) {
+                float ov[4];
+                int oi[4];
+#pragma unroll
+                for (int e = 0; e < 4; e++) {
+                    ov[e] = __shfl_xor_sync(0xffffffffu, bv[a][e], off);
+                    oi[e] = __shfl_xor_sync(0xffffffffu, bi[a][e], off);
+                }
+#pragma unroll
+                for (int e = 0; e < 4; e++)
+                    if (oi[e] >= 0) top4_insert(bv[a], bi[a], ov[e], oi[e]);
+            }
+            if (tx == 0) {
+#pragma unroll
+                for (int e = 0; e < 4; e++) {
+                    tv[ty * 4 + a][e] = bv[a][e];
+                    ti[ty * 4 + a][e] = bi[a][e];
+                }
+            }
+        }
+        __syncthreads();
+        // one thread per (row, entry): candidate test and FP64 score
+        {
+            const int r = tid >> 2, e = tid & 3;
+            double out = INFINITY;  // not a candidate
+            const int rr = rid[r];
+            if (rr >= 0 && ti[r][e] >= 0) {
+                double ub = INFINITY;
+#pragma unroll
+                for (int q = 0; q < 4; q++)
+                    if (ti[r][q] >= 0) ub = fmin(ub, (double)tv[r][q] + bound32(tv[r][q], ec32[ti[r][q]], d));
+                const double v = tv[r][e];
+                if (!(v - bound32(v, ec32[ti[r][e]], d) > ub)) {
+                    int ncand = 0;
+#pragma unroll
+                    for (int q = 0; q < 4; q++)
+                        if (ti[r][q] >= 0 && !((double)tv[r][q] - bound32(tv[r][q], ec32[ti[r][q]], d) > ub)) ncand++;
+                    out = ncand > 1 ? sqeuc64(x + (int64_t)rr * d, c64 + (int64_t)ti[r][e] * d, d) : -1.0;
+                }
+            }
+            dv[r][e] = out;
+        }
+        __syncthreads();
+        if (tid < FT_BM && rid[tid] >= 0) {
+            const int r = tid, rr = rid[r];
+            bool overflow = ti[r][0] < 0;  // no finite FP32 distance at all
+            if (!overflow && k > 4 && ti[r][3] >= 0) {
+                double ub = INFINITY;
+                for (int q = 0; q < 4; q++) ub = fmin(ub, (double)tv[r][q] + bound32(tv[r][q], ec32[ti[r][q]], d));
+                if (!((double)tv[r][3] - bound32(tv[r][3], ecmax_s, d) > ub)) overflow = true;
+            }
+            if (overflow) {
+                unsigned long long slot = atomicAdd(&sc->over_count, 1ULL);
+                over_list[slot] = rr;
+            } else {
+                int best = -1, nfp = 0;
+                double b1 = DBL_MAX, b2 = DBL_MAX;
+                for (int q = 0; q < 4; q++) {
+                    const double v = dv[r][q];
+                    if (v == -1.0) { best = ti[r][q]; nfp = 0; break; }  // single candidate
+                    if (v == INFINITY) continue;
+                    nfp++;
+                    const int ci = ti[r][q];
+                    if (v < b1 || (v == b1 && ci < best)) { b2 = b1; b1 = v; best = ci; }
+                    else if (v < b2) b2 = v;
+                }
+                labels[rr] = best < 0 ? 0 : best;
+                if (nfp > 0) {
+                    atomicAdd(&sc->recheck_rows, 1ULL);
+                    if (nfp > 1 && b2 < DBL_MAX && near_tie(b1, b2)) atomicAdd(&sc->near_tie_rows, 1ULL);
+                }
+            }
         }
     }
 }
@@ -431,7 +628,7 @@ void run_assign_mixed(Ctx &ctx, const TX *x, int64_t n, int d, const double *c, 
         FK_LAUNCH_CHECK();
         col_mean_final_kernel<<<(d + 127) / 128, 128, 0, s>>>(part, nparts, n, d, mu, mu32);
         FK_LAUNCH_CHECK();
-        prep_rows_kernel<TX><<<(unsigned)((n + 7) / 8), 256, 0, s>>>(x, n, d, mp.d_pad, mu, xb, rowinfo, stats);
+        prep_rows_kernel<TX><<<(unsigned)((n + 7) / 8), 256, 0, s>>>(x, n, d, mp.d_pad, mu32, xb, rowinfo, stats);
         FK_LAUNCH_CHECK();
         // ||mu|| for the bound on ||x|| (host side, tiny)
         std::vector<double> hmu(d);
@@ -468,7 +665,14 @@ void run_assign_mixed(Ctx &ctx, const TX *x, int64_t n, int d, const double *c, 
     const int grid = ctx.num_sms * 4;
     pair_rescore_kernel<TX><<<grid, 256, 0, s>>>(x, d, c, c32, ec32, pairs, sc, labels);
     FK_LAUNCH_CHECK();
-    full_rescore_kernel<TX><<<grid, 256, 0, s>>>(x, d, c, c32, ec32, k, full, sc, labels);
+    if constexpr (std::is_same<TX, float>::value) {
+        int32_t *over = (int32_t *)ctx.get(BUF_OVER, sizeof(int32_t) * (size_t)n);
+        full_tiled_kernel<<<ctx.num_sms * 2, FT_T, 0, s>>>(x, d, c32, ec32, c, k, full, sc, labels, over);
+        FK_LAUNCH_CHECK();
+        full_rescore_kernel<TX><<<grid, 256, 0, s>>>(x, d, c, c32, ec32, k, over, sc, labels);
+    } else {
+        full_rescore_kernel<TX><<<grid, 256, 0, s>>>(x, d, c, c32, ec32, k, full, sc, labels);
+    }
     FK_LAUNCH_CHECK();
 }
 
@@ -504,7 +708,7 @@ void debug_tc_probe(Ctx &ctx, const float *x, int64_t n, int d, const double *c,
     FK_LAUNCH_CHECK();
     col_mean_final_kernel<<<(d + 127) / 128, 128, 0, s>>>(part, nparts, n, d, mu, mu32);
     FK_LAUNCH_CHECK();
-    prep_rows_kernel<float><<<(unsigned)((n + 7) / 8), 256, 0, s>>>(x, n, d, mp.d_pad, mu, xb, rowinfo, stats);
+    prep_rows_kernel<float><<<(unsigned)((n + 7) / 8), 256, 0, s>>>(x, n, d, mp.d_pad, mu32, xb, rowinfo, stats);
     FK_LAUNCH_CHECK();
     __nv_bfloat16 *cb = (__nv_bfloat16 *)ctx.get(BUF_CB, sizeof(__nv_bfloat16) * (size_t)mp.k_pad * mp.d_pad);
     __nv_bfloat16 *caug = (__nv_bfloat16 *)ctx.get(BUF_CAUX, sizeof(__nv_bfloat16) * (size_t)mp.k_pad * 16 + 8192);

@@ -207,6 +207,130 @@ __global__ void centroid_sum_kernel(const TX *__restrict__ x, int d, int k, int6
     }
 }
 
+// ----------------------------------------------- exact fixed-point sums --
+// Mixed precisions (X stored f32, centres f64): every f32 value is an
+// integer multiple of 2^-149, so the cluster sums can be formed EXACTLY in
+// 128-bit fixed point with F fraction bits, F chosen from n and max |x| so no
+// partial sum can overflow (values below 2^-F, far under any centroid's
+// precision, are truncated). The exact sum is rounded once to f64 and then
+// divided by the count like kmeans.rs:381; the result is the correctly
+// rounded mean of the exact sum -- it equals the reference's sequential f64
+// sum whenever that sum is exact (the usual case for f32 inputs) and differs
+// by at most a few ulp otherwise. Integer addition is associative, so the
+// rows are processed in any order without changing the result.
+struct FixedAcc {
+    unsigned __int128 v;
+    uint32_t flags;  // 1 = NaN seen, 2 = +inf seen, 4 = -inf seen
+};
+
+__device__ __forceinline__ void fixed_add(FixedAcc &a, float x, int F) {
+    const uint32_t b = __float_as_uint(x);
+    const uint32_t ex = (b >> 23) & 0xFFu;
+    if (ex == 0xFFu) {
+        a.flags |= (b & 0x7FFFFFu) ? 1u : ((b >> 31) ? 4u : 2u);
+        return;
+    }
+    const uint32_t m = (b & 0x7FFFFFu) | (ex ? 0x800000u : 0u);
+    const int s = (ex ? (int)ex : 1) - 150 + F;  // x = m * 2^(s - F)
+    unsigned __int128 t;
+    if (s >= 0)
+        t = (unsigned __int128)m << s;
+    else
+        t = s > -32 ? (unsigned __int128)(m >> (-s)) : (unsigned __int128)0;
+    a.v += (b >> 31) ? (unsigned __int128)0 - t : t;
+}
+
+// Correctly rounded (to nearest, ties to even) f64 value of a signed 128-bit
+// fixed-point number with F fraction bits.
+__device__ double fixed_to_double(unsigned __int128 a, int F) {
+    const bool neg = (a >> 127) != 0;
+    unsigned __int128 u = neg ? (unsigned __int128)0 - a : a;
+    if (u == 0) return 0.0;
+    const uint64_t hi = (uint64_t)(u >> 64), lo = (uint64_t)u;
+    const int msb = hi ? 127 - __clzll((long long)hi) : 63 - __clzll((long long)lo);
+    double r;
+    if (msb <= 52) {
+        r = (double)(uint64_t)u;  // exact
+        r = scalbn(r, -F);
+    } else {
+        int sh = msb - 52;
+        uint64_t mant = (uint64_t)(u >> sh);
+        const unsigned __int128 rem = u - ((unsigned __int128)mant << sh);
+        const unsigned __int128 half = (unsigned __int128)1 << (sh - 1);
+        if (rem > half || (rem == half && (mant & 1ull))) mant += 1;
+        r = scalbn((double)mant, sh - F);  // mant <= 2^53 is exact in f64
+    }
+    return neg ? -r : r;
+}
+
+constexpr int FIX_R = 64;  // member rows per batch
+
+// One block per (cluster, feature slab); thread j sums feature j exactly.
+// Also accumulates (x_ij - c_j)^2 against the old centre in compensated f32
+// for the inertia.
+__global__ void centroid_fixed_kernel(const float *__restrict__ x, int d, int k, int64_t n,
+                                      const int32_t *__restrict__ members, const int32_t *__restrict__ offs,
+                                      int64_t nseg, const double *__restrict__ old_c, double *__restrict__ new_c,
+                                      const float *__restrict__ amax_ptr, double *__restrict__ inertia_part) {
+    __shared__ int32_t sidx[FIX_R];
+    const int c = blockIdx.x;
+    const int j = blockIdx.y * blockDim.x + threadIdx.x;
+    const int64_t start = offs[(int64_t)c * nseg];
+    const int64_t end = (c + 1 < k) ? (int64_t)offs[(int64_t)(c + 1) * nseg] : n;
+    // fraction bits: n * max|x| * 2^F < 2^126
+    const float amax = *amax_ptr;
+    const int ea = amax > 0.f ? (int)((__float_as_uint(amax) >> 23) & 0xFFu) - 127 : -126;
+    const int ln = 64 - __clzll((long long)(n > 0 ? n : 1));
+    const int F = 124 - ln - ea;
+    FixedAcc a0{0, 0u}, a1{0, 0u};
+    float isum = 0.f, icomp = 0.f;
+    const float cj = j < d ? (float)old_c[(int64_t)c * d + j] : 0.f;
+    for (int64_t base = start; base < end; base += FIX_R) {
+        const int cnt = (int)min((int64_t)FIX_R, end - base);
+        __syncthreads();
+        for (int t = threadIdx.x; t < cnt; t += blockDim.x) sidx[t] = members[base + t];
+        __syncthreads();
+        if (j < d) {
+#pragma unroll 4
+            for (int r = 0; r < cnt; r += 2) {
+                const float v0 = x[(int64_t)sidx[r] * d + j];
+                const float v1 = r + 1 < cnt ? x[(int64_t)sidx[r + 1] * d + j] : 0.f;
+                fixed_add(a0, v0, F);
+                if (r + 1 < cnt) fixed_add(a1, v1, F);
+                float df = __fsub_rn(v0, cj);
+                float y = __fsub_rn(__fmul_rn(df, df), icomp);
+                float tt = __fadd_rn(isum, y);
+                icomp = __fsub_rn(__fsub_rn(tt, isum), y);
+                isum = tt;
+                if (r + 1 < cnt) {
+                    df = __fsub_rn(v1, cj);
+                    y = __fsub_rn(__fmul_rn(df, df), icomp);
+                    tt = __fadd_rn(isum, y);
+                    icomp = __fsub_rn(__fsub_rn(tt, isum), y);
+                    isum = tt;
+                }
+            }
+        }
+    }
+    if (j < d) {
+        const int64_t cntc = end - start;
+        double mean;
+        if (cntc == 0) {
+            mean = old_c[(int64_t)c * d + j];
+        } else {
+            const uint32_t fl = a0.flags | a1.flags;
+            double sum;
+            if ((fl & 1u) || (fl & 6u) == 6u) sum = __longlong_as_double(0x7FF8000000000000LL);
+            else if (fl & 2u) sum = __longlong_as_double(0x7FF0000000000000LL);
+            else if (fl & 4u) sum = __longlong_as_double((long long)0xFFF0000000000000ULL);
+            else sum = fixed_to_double(a0.v + a1.v, F);
+            mean = __ddiv_rn(sum, (double)cntc);
+        }
+        new_c[(int64_t)c * d + j] = mean;
+        inertia_part[(int64_t)c * d + j] = (double)isum - (double)icomp;
+    }
+}
+
 // squared_euclidean(new, old) per cluster, folded over j; max over clusters as
 // raw bits (non-negative IEEE values order like unsigned integers). NaN
 // shifts are skipped, as `shift > max_shift` is false for NaN.
@@ -297,6 +421,20 @@ void launch_update_centroids(const SortPlan &p, const TX *x, int d, const int32_
                                                                     new_c, nullptr);
     FK_LAUNCH_CHECK();
     max_shift_kernel<TC><<<(p.k + 127) / 128, 128, 0, s>>>(new_c, old_c, p.k, d, &scalars->shift_bits);
+    FK_LAUNCH_CHECK();
+}
+
+void launch_update_centroids_exact(const SortPlan &p, const float *x, int d, const int32_t *members,
+                                   const int32_t *seg_hist, const double *old_c, double *new_c, DevScalars *scalars,
+                                   const float *amax, double *inertia_part, cudaStream_t s) {
+    FK_CUDA(cudaMemsetAsync(&scalars->shift_bits, 0, sizeof(unsigned long long), s));
+    if (d == 0 || p.k == 0) return;
+    int threads = d >= 256 ? 256 : (d + 31) / 32 * 32;
+    dim3 grid((unsigned)p.k, (unsigned)((d + threads - 1) / threads));
+    centroid_fixed_kernel<<<grid, threads, 0, s>>>(x, d, p.k, p.n, members, seg_hist, p.nseg, old_c, new_c, amax,
+                                                   inertia_part);
+    FK_LAUNCH_CHECK();
+    max_shift_kernel<double><<<(p.k + 127) / 128, 128, 0, s>>>(new_c, old_c, p.k, d, &scalars->shift_bits);
     FK_LAUNCH_CHECK();
 }
 
