@@ -54,6 +54,7 @@ class FitReport(C.Structure):
         ("near_tie_rows", C.c_int64),
         ("ms_init", C.c_double),
         ("ms_assign", C.c_double),
+        ("ms_contract", C.c_double),
         ("ms_update", C.c_double),
         ("ms_total", C.c_double),
         ("precision_used", C.c_int32),

@@ -100,44 +100,6 @@ void copy_out(Ctx &ctx, T *dst, const T *dev_src, size_t count) {
     FK_CUDA(cudaMemcpyAsync(dst, dev_src, sizeof(T) * count, cudaMemcpyDefault, ctx.stream));
 }
 
-// Phase timer: records a pair of events on the stream and leaves the
-// reading to flush_timers(), so timing never adds a host synchronisation
-// inside the Lloyd loop.
-struct Timer {
-    Ctx *ctx = nullptr;
-    cudaEvent_t b = nullptr;
-    double *acc = nullptr;
-    cudaEvent_t a = nullptr;
-    Timer(bool enable, Ctx &c, double *accum) {
-        if (!enable || !accum) return;
-        ctx = &c;
-        acc = accum;
-        FK_CUDA(cudaEventCreate(&a));
-        FK_CUDA(cudaEventCreate(&b));
-        FK_CUDA(cudaEventRecord(a, c.stream));
-    }
-    ~Timer() {
-        if (!ctx) return;
-        if (cudaEventRecord(b, ctx->stream) == cudaSuccess) {
-            ctx->pending.push_back({a, b, acc});
-        } else {
-            cudaEventDestroy(a);
-            cudaEventDestroy(b);
-        }
-    }
-};
-
-void flush_timers(Ctx &ctx) {
-    for (auto &p : ctx.pending) {
-        float ms = 0.f;
-        if (cudaEventSynchronize(p.b) == cudaSuccess && cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess)
-            *p.acc += ms;
-        cudaEventDestroy(p.a);
-        cudaEventDestroy(p.b);
-    }
-    ctx.pending.clear();
-}
-
 template <typename T> struct FMax;
 template <> struct FMax<double> { static double v() { return 1.7976931348623157e308; } };
 template <> struct FMax<float> { static float v() { return 3.40282347e38f; } };
@@ -192,6 +154,7 @@ void lloyd_iteration(Ctx &ctx, const TX *x, int64_t n, int d, const TC *c, int k
     int32_t *members = (int32_t *)ctx.get(BUF_MEMBERS, sizeof(int32_t) * (size_t)n);
     int32_t *seg = (int32_t *)ctx.get(BUF_SEGHIST, sizeof(int32_t) * (size_t)plan.k * plan.nseg);
     int32_t *tmp = (int32_t *)ctx.get(BUF_SCAN_TMP, plan.scan_tmp_bytes);
+    ctx.contract_acc = (timing && rep) ? &rep->ms_contract : nullptr;
     {
         Timer t(timing, ctx, rep ? &rep->ms_assign : nullptr);
         if (prec == FK_PRECISION_PLAIN) {

@@ -131,10 +131,49 @@ struct Ctx {
     };
     std::vector<PendingTimer> pending;  // phase timers read after the loop
     MixedPlan mixed;
+    double *contract_acc = nullptr;  // when set: device time of the contraction kernel
 
     void *get(BufSlot s, size_t bytes);  // grow-only device buffer
     void bind();                         // make the device current
 };
+
+// Phase timer: records a pair of events on the stream and leaves the
+// reading to flush_timers(), so timing never adds a host synchronisation
+// inside the Lloyd loop.
+struct Timer {
+    Ctx *ctx = nullptr;
+    cudaEvent_t b = nullptr;
+    double *acc = nullptr;
+    cudaEvent_t a = nullptr;
+    Timer(bool enable, Ctx &c, double *accum) {
+        if (!enable || !accum) return;
+        ctx = &c;
+        acc = accum;
+        FK_CUDA(cudaEventCreate(&a));
+        FK_CUDA(cudaEventCreate(&b));
+        FK_CUDA(cudaEventRecord(a, c.stream));
+    }
+    ~Timer() {
+        if (!ctx) return;
+        if (cudaEventRecord(b, ctx->stream) == cudaSuccess) {
+            ctx->pending.push_back({a, b, acc});
+        } else {
+            cudaEventDestroy(a);
+            cudaEventDestroy(b);
+        }
+    }
+};
+
+inline void flush_timers(Ctx &ctx) {
+    for (auto &p : ctx.pending) {
+        float ms = 0.f;
+        if (cudaEventSynchronize(p.b) == cudaSuccess && cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess)
+            *p.acc += ms;
+        cudaEventDestroy(p.a);
+        cudaEventDestroy(p.b);
+    }
+    ctx.pending.clear();
+}
 
 // ----------------------------------------------------------- kernel APIs --
 // Direct-form assignment (kmeans.rs:295-352): labels + per-row minimum in TC.

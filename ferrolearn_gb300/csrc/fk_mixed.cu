@@ -26,6 +26,7 @@
 #include <cmath>
 #include <cuda_bf16.h>
 
+#include <algorithm>
 #include <cstddef>
 #include <type_traits>
 #include <vector>
@@ -54,25 +55,27 @@ __device__ __forceinline__ double warp_sum_d(double v) {
 // partial sums in f32, non-finite entries skipped, the final fold in f64).
 template <typename TX>
 __global__ void col_mean_partial_kernel(const TX *__restrict__ x, int64_t n, int d, int64_t rows_per,
-                                        double *__restrict__ part) {
+                                        int64_t stride, double *__restrict__ part) {
     int j = threadIdx.x + blockIdx.y * blockDim.x;
     if (j >= d) return;
-    int64_t lo = (int64_t)blockIdx.x * rows_per, hi = min(n, lo + rows_per);
+    int64_t lo = (int64_t)blockIdx.x * rows_per, hi = lo + rows_per;
     float s = 0.f;
-    for (int64_t i = lo; i < hi; i++) {
+    for (int64_t t = lo; t < hi; t++) {
+        const int64_t i = t * stride;
+        if (i >= n) break;
         float v = (float)x[i * d + j];
         if (isfinite(v)) s += v;
     }
     part[(int64_t)blockIdx.x * d + j] = (double)s;
 }
 
-__global__ void col_mean_final_kernel(const double *__restrict__ part, int nparts, int64_t n, int d,
+__global__ void col_mean_final_kernel(const double *__restrict__ part, int nparts, int64_t rows, int d,
                                       double *__restrict__ mu, float *__restrict__ mu32) {
     int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= d) return;
     double s = 0.0;
     for (int p = 0; p < nparts; p++) s += part[(int64_t)p * d + j];
-    float m = (float)(s / (double)n);
+    float m = (float)(s / (double)rows);
     if (!isfinite(m)) m = 0.f;
     mu32[j] = m;
     mu[j] = (double)m;  // the centring is by the f32 value, for rows and centres alike
@@ -95,40 +98,55 @@ template <typename TX>
 __global__ void prep_rows_kernel(const TX *__restrict__ x, int64_t n, int d, int d_pad,
                                  const float *__restrict__ mu32, __nv_bfloat16 *__restrict__ xb,
                                  float4 *__restrict__ rowinfo, MixedStats *stats) {
-    const int lane = threadIdx.x & 31;
-    const int64_t row = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    if (row >= n) return;
-    float xn2 = 0.f, ex2 = 0.f, tn2 = 0.f, xo2 = 0.f, amax = 0.f;
-    for (int j = lane; j < d_pad; j += 32) {
-        __nv_bfloat16 h = __float2bfloat16_rn(0.f);
-        if (j < d) {
-            float xv = (float)x[row * d + j];
-            float t = __fsub_rn(xv, mu32[j]);
-            h = __float2bfloat16_rn(t);
-            float hv = __bfloat162float(h);
-            float e = __fsub_rn(t, hv);
-            xn2 = __fmaf_rn(hv, hv, xn2);
-            ex2 = __fmaf_rn(e, e, ex2);
-            tn2 = __fmaf_rn(t, t, tn2);
-            xo2 = __fmaf_rn(xv, xv, xo2);
-            amax = fmaxf(amax, fabsf(xv));
+    __shared__ float sh_xn[32], sh_am[32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    float xn_hi = 0.f, am_hi = 0.f;
+    for (int64_t row = (int64_t)blockIdx.x * (blockDim.x >> 5) + w; row < n; row += nwarps) {
+        float xn2 = 0.f, ex2 = 0.f, tn2 = 0.f, xo2 = 0.f, amax = 0.f;
+        for (int j = lane; j < d_pad; j += 32) {
+            __nv_bfloat16 h = __float2bfloat16_rn(0.f);
+            if (j < d) {
+                float xv = (float)x[row * d + j];
+                float t = __fsub_rn(xv, mu32[j]);
+                h = __float2bfloat16_rn(t);
+                float hv = __bfloat162float(h);
+                float e = __fsub_rn(t, hv);
+                xn2 = __fmaf_rn(hv, hv, xn2);
+                ex2 = __fmaf_rn(e, e, ex2);
+                tn2 = __fmaf_rn(t, t, tn2);
+                xo2 = __fmaf_rn(xv, xv, xo2);
+                amax = fmaxf(amax, fabsf(xv));
+            }
+            xb[row * d_pad + j] = h;
         }
-        xb[row * d_pad + j] = h;
-    }
-    xn2 = warp_sum_f(xn2);
-    ex2 = warp_sum_f(ex2);
-    tn2 = warp_sum_f(tn2);
-    xo2 = warp_sum_f(xo2);
+        xn2 = warp_sum_f(xn2);
+        ex2 = warp_sum_f(ex2);
+        tn2 = warp_sum_f(tn2);
+        xo2 = warp_sum_f(xo2);
 #pragma unroll
-    for (int off = 16; off >= 1; off >>= 1) amax = fmaxf(amax, __shfl_xor_sync(0xffffffffu, amax, off));
-    if (lane == 0) {
+        for (int off = 16; off >= 1; off >>= 1) amax = fmaxf(amax, __shfl_xor_sync(0xffffffffu, amax, off));
         const float up = 1.0f + (float)(d + 64) * 1.1920929e-07f;
         float xn = __fsqrt_ru(__fmul_ru(xn2, up));
         float ex = __fadd_ru(__fsqrt_ru(__fmul_ru(ex2, up)), __fmul_ru(__fsqrt_ru(__fmul_ru(tn2, up)), 5.9604645e-08f));
         float xo = __fsqrt_ru(__fmul_ru(xo2, up));
-        rowinfo[row] = make_float4(xn, ex, xo, 0.f);
-        if (xn == xn && xn < INFINITY) atomic_max_pos(&stats->xn_max, xn);  // non-finite rows are re-scored in full
-        if (amax < INFINITY) atomic_max_pos(&stats->amax, amax);
+        if (lane == 0) rowinfo[row] = make_float4(xn, ex, xo, 0.f);
+        if (xn < INFINITY) xn_hi = fmaxf(xn_hi, xn);  // NaN / inf rows are re-scored in full
+        if (amax < INFINITY) am_hi = fmaxf(am_hi, amax);
+    }
+    if (lane == 0) {
+        sh_xn[w] = xn_hi;
+        sh_am[w] = am_hi;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float a = 0.f, b = 0.f;
+        for (int q = 0; q < (int)(blockDim.x >> 5); q++) {
+            a = fmaxf(a, sh_xn[q]);
+            b = fmaxf(b, sh_am[q]);
+        }
+        atomic_max_pos(&stats->xn_max, a);
+        atomic_max_pos(&stats->amax, b);
     }
 }
 
@@ -301,41 +319,56 @@ __device__ __forceinline__ double bound32(double d32, double ec, int d) {
             (double)(d + 4) * 2.220446049250313e-16 * d32) * 1.01 + 1e-30;
 }
 
-// One thread per listed row: FP32 distances to the two candidates decide the
-// row when their bounded intervals do not overlap; otherwise both are scored
-// exactly in FP64 (direct form, strict < over increasing index).
+// One warp per listed row (coalesced over the features): FP32 distances to
+// the two candidates decide the row when their bounded intervals do not
+// overlap; otherwise lanes 0 and 1 score the two exactly in FP64 (direct
+// form, strict < over increasing index).
 template <typename TX>
 __global__ void pair_rescore_kernel(const TX *__restrict__ x, int d, const double *__restrict__ c,
                                     const float *__restrict__ c32, const float *__restrict__ ec32,
                                     const int4 *__restrict__ list, DevScalars *sc, int32_t *__restrict__ labels) {
     const unsigned long long cnt = sc->flag_count;
-    for (unsigned long long s = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; s < cnt;
-         s += (unsigned long long)gridDim.x * blockDim.x) {
-        int4 e = list[s];
+    const int lane = threadIdx.x & 31;
+    const unsigned long long wid = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const unsigned long long nw = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
+    for (unsigned long long s = wid; s < cnt; s += nw) {
+        const int4 e = list[s];
         const TX *row = x + (int64_t)e.x * d;
-        int a = e.y < e.z ? e.y : e.z, b = e.y < e.z ? e.z : e.y;
+        const int a = e.y < e.z ? e.y : e.z, b = e.y < e.z ? e.z : e.y;
         if constexpr (std::is_same<TX, float>::value) {
-            const double da = sqeuc32(row, c32 + (int64_t)a * d, d);
-            const double db = sqeuc32(row, c32 + (int64_t)b * d, d);
+            const float *ca = c32 + (int64_t)a * d, *cb = c32 + (int64_t)b * d;
+            float sa = 0.f, sb = 0.f;
+            for (int j = lane; j < d; j += 32) {
+                const float xv = row[j];
+                const float ta = xv - ca[j], tb = xv - cb[j];
+                sa = fmaf(ta, ta, sa);
+                sb = fmaf(tb, tb, sb);
+            }
+            sa = warp_sum_f(sa);
+            sb = warp_sum_f(sb);
+            const double da = sa, db = sb;
             const double ea = bound32(da, ec32[a], d), eb = bound32(db, ec32[b], d);
             if (da + ea < db - eb) {  // false for any NaN or infinity
-                labels[e.x] = a;
+                if (lane == 0) labels[e.x] = a;
                 continue;
             }
             if (db + eb < da - ea) {
-                labels[e.x] = b;
+                if (lane == 0) labels[e.x] = b;
                 continue;
             }
         }
-        double da = sqeuc64(row, c + (int64_t)a * d, d);
-        double db = sqeuc64(row, c + (int64_t)b * d, d);
-        int best = 0;
-        double bd = DBL_MAX;
-        if (da < bd) { bd = da; best = a; }
-        if (db < bd) { bd = db; best = b; }
-        labels[e.x] = best;
-        atomicAdd(&sc->recheck_rows, 1ULL);
-        if (near_tie(da, db)) atomicAdd(&sc->near_tie_rows, 1ULL);
+        double dv = 0.0;
+        if (lane < 2) dv = sqeuc64(row, c + (int64_t)(lane == 0 ? a : b) * d, d);
+        const double da = __shfl_sync(0xffffffffu, dv, 0), db = __shfl_sync(0xffffffffu, dv, 1);
+        if (lane == 0) {
+            int best = 0;
+            double bd = DBL_MAX;
+            if (da < bd) { bd = da; best = a; }
+            if (db < bd) { bd = db; best = b; }
+            labels[e.x] = best;
+            atomicAdd(&sc->recheck_rows, 1ULL);
+            if (near_tie(da, db)) atomicAdd(&sc->near_tie_rows, 1ULL);
+        }
     }
 }
 
@@ -620,15 +653,20 @@ void run_assign_mixed(Ctx &ctx, const TX *x, int64_t n, int d, const double *c, 
     float4 *rowinfo = (float4 *)ctx.get(BUF_XNORM, sizeof(float4) * (size_t)n);
     if (replan) {
         FK_CUDA(cudaMemsetAsync(stats, 0, sizeof(MixedStats), s));
-        const int64_t rows_per = 4096;
-        const int nparts = (int)((n + rows_per - 1) / rows_per);
+        // the centring vector only needs to be finite: a strided sample of at
+        // most 65536 rows is enough
+        const int64_t stride = n > 65536 ? n / 65536 : 1;
+        const int64_t rows = (n + stride - 1) / stride;
+        const int64_t rows_per = 1024;
+        const int nparts = (int)((rows + rows_per - 1) / rows_per);
         double *part = (double *)ctx.get(BUF_PARTIAL, sizeof(double) * (size_t)nparts * d);
         dim3 g1(nparts, (d + 127) / 128);
-        col_mean_partial_kernel<TX><<<g1, 128, 0, s>>>(x, n, d, rows_per, part);
+        col_mean_partial_kernel<TX><<<g1, 128, 0, s>>>(x, n, d, rows_per, stride, part);
         FK_LAUNCH_CHECK();
-        col_mean_final_kernel<<<(d + 127) / 128, 128, 0, s>>>(part, nparts, n, d, mu, mu32);
+        col_mean_final_kernel<<<(d + 127) / 128, 128, 0, s>>>(part, nparts, rows, d, mu, mu32);
         FK_LAUNCH_CHECK();
-        prep_rows_kernel<TX><<<(unsigned)((n + 7) / 8), 256, 0, s>>>(x, n, d, mp.d_pad, mu32, xb, rowinfo, stats);
+        const int64_t pblocks = std::min<int64_t>((n + 7) / 8, (int64_t)ctx.num_sms * 16);
+        prep_rows_kernel<TX><<<(unsigned)pblocks, 256, 0, s>>>(x, n, d, mp.d_pad, mu32, xb, rowinfo, stats);
         FK_LAUNCH_CHECK();
         // ||mu|| for the bound on ||x|| (host side, tiny)
         std::vector<double> hmu(d);
@@ -654,7 +692,10 @@ void run_assign_mixed(Ctx &ctx, const TX *x, int64_t n, int d, const double *c, 
     FK_LAUNCH_CHECK();
 
     Top2 *top = (Top2 *)ctx.get(BUF_TOP2, sizeof(Top2) * (size_t)n * mp.parts);
-    launch_tc_assign(ctx, mp, xb, cb, caug, top, sc);
+    {
+        Timer t(ctx.contract_acc != nullptr, ctx, ctx.contract_acc);
+        launch_tc_assign(ctx, mp, xb, cb, caug, top, sc);
+    }
 
     int4 *pairs = (int4 *)ctx.get(BUF_FLAGS, sizeof(int4) * (size_t)n);
     int32_t *full = (int32_t *)ctx.get(BUF_FULL, sizeof(int32_t) * (size_t)n);
@@ -704,7 +745,7 @@ void debug_tc_probe(Ctx &ctx, const float *x, int64_t n, int d, const double *c,
     const int64_t rows_per = 4096;
     const int nparts = (int)((n + rows_per - 1) / rows_per);
     double *part = (double *)ctx.get(BUF_PARTIAL, sizeof(double) * (size_t)nparts * d);
-    col_mean_partial_kernel<float><<<dim3(nparts, (d + 127) / 128), 128, 0, s>>>(x, n, d, rows_per, part);
+    col_mean_partial_kernel<float><<<dim3(nparts, (d + 127) / 128), 128, 0, s>>>(x, n, d, rows_per, 1, part);
     FK_LAUNCH_CHECK();
     col_mean_final_kernel<<<(d + 127) / 128, 128, 0, s>>>(part, nparts, n, d, mu, mu32);
     FK_LAUNCH_CHECK();

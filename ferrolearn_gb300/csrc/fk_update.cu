@@ -219,9 +219,14 @@ __global__ void centroid_sum_kernel(const TX *__restrict__ x, int d, int k, int6
 // by at most a few ulp otherwise. Integer addition is associative, so the
 // rows are processed in any order without changing the result.
 struct FixedAcc {
-    unsigned __int128 v;
-    uint32_t flags;  // 1 = NaN seen, 2 = +inf seen, 4 = -inf seen
+    uint64_t plo, phi;  // sum of the positive values
+    uint64_t nlo, nhi;  // sum of the magnitudes of the negative values
+    uint32_t flags;     // 1 = NaN seen, 2 = +inf seen, 4 = -inf seen
 };
+
+__device__ __forceinline__ void add128(uint64_t &lo, uint64_t &hi, uint64_t tlo, uint64_t thi) {
+    asm("add.cc.u64 %0, %0, %2;\n\taddc.u64 %1, %1, %3;" : "+l"(lo), "+l"(hi) : "l"(tlo), "l"(thi));
+}
 
 __device__ __forceinline__ void fixed_add(FixedAcc &a, float x, int F) {
     const uint32_t b = __float_as_uint(x);
@@ -230,14 +235,23 @@ __device__ __forceinline__ void fixed_add(FixedAcc &a, float x, int F) {
         a.flags |= (b & 0x7FFFFFu) ? 1u : ((b >> 31) ? 4u : 2u);
         return;
     }
-    const uint32_t m = (b & 0x7FFFFFu) | (ex ? 0x800000u : 0u);
-    const int s = (ex ? (int)ex : 1) - 150 + F;  // x = m * 2^(s - F)
-    unsigned __int128 t;
-    if (s >= 0)
-        t = (unsigned __int128)m << s;
+    const uint64_t m = (uint64_t)((b & 0x7FFFFFu) | (ex ? 0x800000u : 0u));
+    const int s = (ex ? (int)ex : 1) - 150 + F;  // x = m * 2^(s - F); m < 2^24, s <= 101
+    uint64_t tlo, thi;
+    if (s >= 64) {
+        tlo = 0;
+        thi = m << (s - 64);
+    } else if (s >= 0) {
+        tlo = m << s;
+        thi = s > 40 ? m >> (64 - s) : 0;
+    } else {
+        tlo = s > -32 ? m >> (-s) : 0;
+        thi = 0;
+    }
+    if (b >> 31)
+        add128(a.nlo, a.nhi, tlo, thi);
     else
-        t = s > -32 ? (unsigned __int128)(m >> (-s)) : (unsigned __int128)0;
-    a.v += (b >> 31) ? (unsigned __int128)0 - t : t;
+        add128(a.plo, a.phi, tlo, thi);
 }
 
 // Correctly rounded (to nearest, ties to even) f64 value of a signed 128-bit
@@ -282,7 +296,7 @@ __global__ void centroid_fixed_kernel(const float *__restrict__ x, int d, int k,
     const int ea = amax > 0.f ? (int)((__float_as_uint(amax) >> 23) & 0xFFu) - 127 : -126;
     const int ln = 64 - __clzll((long long)(n > 0 ? n : 1));
     const int F = 124 - ln - ea;
-    FixedAcc a0{0, 0u}, a1{0, 0u};
+    FixedAcc a0{0, 0, 0, 0, 0u};
     float isum = 0.f, icomp = 0.f;
     const float cj = j < d ? (float)old_c[(int64_t)c * d + j] : 0.f;
     for (int64_t base = start; base < end; base += FIX_R) {
@@ -291,24 +305,15 @@ __global__ void centroid_fixed_kernel(const float *__restrict__ x, int d, int k,
         for (int t = threadIdx.x; t < cnt; t += blockDim.x) sidx[t] = members[base + t];
         __syncthreads();
         if (j < d) {
-#pragma unroll 4
-            for (int r = 0; r < cnt; r += 2) {
+#pragma unroll 8
+            for (int r = 0; r < cnt; r++) {
                 const float v0 = x[(int64_t)sidx[r] * d + j];
-                const float v1 = r + 1 < cnt ? x[(int64_t)sidx[r + 1] * d + j] : 0.f;
                 fixed_add(a0, v0, F);
-                if (r + 1 < cnt) fixed_add(a1, v1, F);
-                float df = __fsub_rn(v0, cj);
-                float y = __fsub_rn(__fmul_rn(df, df), icomp);
-                float tt = __fadd_rn(isum, y);
+                const float df = __fsub_rn(v0, cj);
+                const float y = __fsub_rn(__fmul_rn(df, df), icomp);
+                const float tt = __fadd_rn(isum, y);
                 icomp = __fsub_rn(__fsub_rn(tt, isum), y);
                 isum = tt;
-                if (r + 1 < cnt) {
-                    df = __fsub_rn(v1, cj);
-                    y = __fsub_rn(__fmul_rn(df, df), icomp);
-                    tt = __fadd_rn(isum, y);
-                    icomp = __fsub_rn(__fsub_rn(tt, isum), y);
-                    isum = tt;
-                }
             }
         }
     }
@@ -318,12 +323,16 @@ __global__ void centroid_fixed_kernel(const float *__restrict__ x, int d, int k,
         if (cntc == 0) {
             mean = old_c[(int64_t)c * d + j];
         } else {
-            const uint32_t fl = a0.flags | a1.flags;
+            const uint32_t fl = a0.flags;
             double sum;
             if ((fl & 1u) || (fl & 6u) == 6u) sum = __longlong_as_double(0x7FF8000000000000LL);
             else if (fl & 2u) sum = __longlong_as_double(0x7FF0000000000000LL);
             else if (fl & 4u) sum = __longlong_as_double((long long)0xFFF0000000000000ULL);
-            else sum = fixed_to_double(a0.v + a1.v, F);
+            else {
+                const unsigned __int128 pos = ((unsigned __int128)a0.phi << 64) | a0.plo;
+                const unsigned __int128 neg = ((unsigned __int128)a0.nhi << 64) | a0.nlo;
+                sum = fixed_to_double(pos - neg, F);
+            }
             mean = __ddiv_rn(sum, (double)cntc);
         }
         new_c[(int64_t)c * d + j] = mean;

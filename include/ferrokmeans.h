@@ -85,6 +85,8 @@ typedef struct fk_fit_report {
                                   is below 1e-12 relative                  */
     double ms_init;            /* device time, k-means++                   */
     double ms_assign;          /* device time, assignment (+ re-check)     */
+    double ms_contract;        /* mixed: device time of the tensor-core
+                                  contraction kernel alone                 */
     double ms_update;          /* device time, sort + centroid update      */
     double ms_total;           /* device time of the whole call            */
     int32_t precision_used;
