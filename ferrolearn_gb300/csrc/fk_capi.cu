@@ -177,7 +177,8 @@ void lloyd_iteration(Ctx &ctx, const TX *x, int64_t n, int d, const TC *c, int k
             double *part = (double *)ctx.get(BUF_OUT2, sizeof(double) * (size_t)plan.k * d + 64);
             if constexpr (std::is_same<TX, float>::value && std::is_same<TC, double>::value) {
                 const MixedStats *st = (const MixedStats *)ctx.get(BUF_CF32, sizeof(MixedStats));
-                launch_update_centroids_exact(plan, x, d, members, seg, c, nc, sc, &st->amax, part, s);
+                void *scratch = ctx.get(BUF_FIXPART, update_exact_scratch_bytes(plan.k, d));
+                launch_update_centroids_exact(plan, x, d, members, seg, c, nc, sc, &st->amax, part, scratch, s);
             } else {
                 launch_update_centroids<TX, TC>(plan, x, d, members, seg, c, nc, sc, s, part);
             }

@@ -110,7 +110,7 @@ enum BufSlot {
     BUF_X = 0, BUF_XC, BUF_C0, BUF_C1, BUF_CBEST, BUF_LABELS, BUF_LBEST, BUF_MIND,
     BUF_MEMBERS, BUF_SEGHIST, BUF_SCAN_TMP, BUF_COUNTS, BUF_PARTIAL, BUF_SCALARS,
     BUF_OUT, BUF_OUT2, BUF_KPP0, BUF_KPP1, BUF_KPP2, BUF_KPP3, BUF_DRAWS,
-    BUF_XB, BUF_XNORM, BUF_CB, BUF_CAUX, BUF_TOP2, BUF_FLAGS, BUF_FULL, BUF_CF32, BUF_CF32C, BUF_OVER,
+    BUF_XB, BUF_XNORM, BUF_CB, BUF_CAUX, BUF_TOP2, BUF_FLAGS, BUF_FULL, BUF_CF32, BUF_CF32C, BUF_OVER, BUF_FIXPART,
     BUF_COUNT
 };
 
@@ -213,9 +213,10 @@ void launch_update_centroids(const SortPlan &p, const TX *x, int d, const int32_
 
 // Mixed precisions: exact 128-bit fixed-point cluster sums of an f32 X,
 // rounded once to f64, divided by the counts; plus the inertia partials.
+size_t update_exact_scratch_bytes(int k, int d);
 void launch_update_centroids_exact(const SortPlan &p, const float *x, int d, const int32_t *members,
                                    const int32_t *seg_hist, const double *old_c, double *new_c, DevScalars *scalars,
-                                   const float *amax, double *inertia_part, cudaStream_t s);
+                                   const float *amax, double *inertia_part, void *scratch, cudaStream_t s);
 
 void launch_labels_to_u64(const int32_t *l, int64_t n, uint64_t *out, cudaStream_t s);
 template <typename TS, typename TD>

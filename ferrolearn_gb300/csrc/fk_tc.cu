@@ -154,26 +154,35 @@ __device__ __forceinline__ void mma_commit(uint32_t bar) {
                  : "memory");
 }
 
-// 32 consecutive columns of this thread's TMEM lane. The wait is tied to the
-// registers so no use of them can be scheduled before it.
+// 32 consecutive columns of this thread's TMEM lane; the load and its wait
+// are one asm statement, so the registers are defined only after the wait.
 __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
     asm volatile(
         "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
         "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n\t"
+        "tcgen05.wait::ld.sync.aligned;"
         : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
           "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
           "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
           "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-        : "r"(taddr));
-    asm volatile(
-        "tcgen05.wait::ld.sync.aligned;"
-        : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7]),
-          "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]), "+r"(r[14]), "+r"(r[15]),
-          "+r"(r[16]), "+r"(r[17]), "+r"(r[18]), "+r"(r[19]), "+r"(r[20]), "+r"(r[21]), "+r"(r[22]), "+r"(r[23]),
-          "+r"(r[24]), "+r"(r[25]), "+r"(r[26]), "+r"(r[27]), "+r"(r[28]), "+r"(r[29]), "+r"(r[30]), "+r"(r[31])
-        :
+        : "r"(taddr)
         : "memory");
+}
+
+// key = (bits & 0xFFFFFF00) | code, as (bits | 0xFF) & (0xFFFFFF00 | code):
+// one lop3 with the per-column constant as its immediate.
+template <uint32_t MASKC>
+__device__ __forceinline__ float make_key(uint32_t bits, uint32_t ff) {
+    uint32_t k;
+    asm("lop3.b32 %0, %1, %2, %3, 0xA8;" : "=r"(k) : "r"(bits), "r"(ff), "n"(MASKC));
+    return __uint_as_float(k);
+}
+
+__device__ __forceinline__ float fmax3(float a, float b, float c) {
+    float r;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
 }
 
 __device__ __forceinline__ void epi_bar() { asm volatile("bar.sync 1, 256;" ::: "memory"); }
@@ -205,32 +214,62 @@ __device__ __forceinline__ void merge_res(uint32_t &R1, int &I1, uint32_t &R2, i
 }
 
 // Ranks the 128 columns [HALF*128, HALF*128+128) of one accumulator block:
-// four interleaved top-2 chains (three integer min/max per element), merged
-// with the bound of the rest. Returns keys (value bits | code).
+// four interleaved top-2 chains (three float min/max per element on the keys,
+// which are positive floats), merged with the bound of the rest. A NaN score
+// (NaN row) is ignored by fminf/fmaxf; such rows have non-finite bound
+// ingredients and are always re-scored in full. Returns keys.
+template <int HALF, int CH, int E>
+__device__ __forceinline__ void rank_pair(const uint32_t (&r)[32], uint32_t ff, float &a1, float &a2) {
+    // top-2 of {a1 >= a2, k0, k1}: a1' = max(a1, max(k0,k1)),
+    // a2' = max(min(a1, max(k0,k1)), a2, min(k0,k1))
+    const float k0 = make_key<0xFFFFFF00u | (255u - (uint32_t)(HALF * 128 + CH * 32 + E))>(r[E], ff);
+    const float k1 = make_key<0xFFFFFF00u | (255u - (uint32_t)(HALF * 128 + CH * 32 + E + 1))>(r[E + 1], ff);
+    const float m = fmaxf(k0, k1), l = fminf(k0, k1);
+    a2 = fmax3(fminf(a1, m), a2, l);
+    a1 = fmaxf(a1, m);
+}
+
+template <int HALF, int CH, int E>
+struct RankChunk {
+    static __device__ __forceinline__ void run(const uint32_t (&r)[32], uint32_t ff, float (&a1)[4], float (&a2)[4]) {
+        rank_pair<HALF, CH, E>(r, ff, a1[(E >> 1) & 3], a2[(E >> 1) & 3]);
+        RankChunk<HALF, CH, E + 2>::run(r, ff, a1, a2);
+    }
+};
+template <int HALF, int CH>
+struct RankChunk<HALF, CH, 32> {
+    static __device__ __forceinline__ void run(const uint32_t (&)[32], uint32_t, float (&)[4], float (&)[4]) {}
+};
+
+template <int HALF, int CH>
+__device__ __forceinline__ void rank_chunk(uint32_t col_addr, uint32_t ff, float (&a1)[4], float (&a2)[4]) {
+    uint32_t r[32];
+    tmem_ld32(col_addr + CH * 32, r);
+    RankChunk<HALF, CH, 0>::run(r, ff, a1, a2);
+}
+
+// Ranks the 128 columns [HALF*128, HALF*128+128) of one accumulator block:
+// four interleaved top-2 chains over keys (positive floats, so float and
+// unsigned order agree), two elements per step with three-input max, merged
+// with the bound of the rest. A NaN score (NaN row) is ignored by the float
+// min/max; such rows have non-finite bound ingredients and are always
+// re-scored in full. Returns keys.
 template <int HALF>
 __device__ __forceinline__ void rank_half(uint32_t col_addr, uint32_t &b1, uint32_t &b2, uint32_t &bu) {
-    uint32_t a1[4] = {0u, 0u, 0u, 0u}, a2[4] = {0u, 0u, 0u, 0u};
-#pragma unroll
-    for (int ch = 0; ch < 4; ch++) {
-        uint32_t r[32];
-        tmem_ld32(col_addr + ch * 32, r);
-#pragma unroll
-        for (int e = 0; e < 32; e++) {
-            constexpr uint32_t hi = 0xFFFFFF00u;
-            const uint32_t code = 255u - (uint32_t)(HALF * 128 + ch * 32 + e);
-            const uint32_t key = (r[e] | 0xFFu) & (hi | code);
-            const int qd = e & 3;
-            const uint32_t lo = min(a1[qd], key);
-            a1[qd] = max(a1[qd], key);
-            a2[qd] = max(a2[qd], lo);
-        }
-    }
-    b1 = a1[0];
-    b2 = a2[0];
-    bu = a2[0];
+    float a1[4] = {0.f, 0.f, 0.f, 0.f}, a2[4] = {0.f, 0.f, 0.f, 0.f};
+    uint32_t ff;
+    asm volatile("mov.u32 %0, 255;" : "=r"(ff));
+    rank_chunk<HALF, 0>(col_addr, ff, a1, a2);
+    rank_chunk<HALF, 1>(col_addr, ff, a1, a2);
+    rank_chunk<HALF, 2>(col_addr, ff, a1, a2);
+    rank_chunk<HALF, 3>(col_addr, ff, a1, a2);
+    b1 = __float_as_uint(a1[0]);
+    b2 = __float_as_uint(a2[0]);
+    bu = b2;
     int d1 = 0, d2 = 0;  // indices are carried inside the keys
 #pragma unroll
-    for (int qd = 1; qd < 4; qd++) merge_res(b1, d1, b2, d2, bu, a1[qd], 0, a2[qd], 0, a2[qd]);
+    for (int qd = 1; qd < 4; qd++)
+        merge_res(b1, d1, b2, d2, bu, __float_as_uint(a1[qd]), 0, __float_as_uint(a2[qd]), 0, __float_as_uint(a2[qd]));
 }
 
 __global__ void __launch_bounds__(NTHREADS, 1)

@@ -277,26 +277,40 @@ __device__ double fixed_to_double(unsigned __int128 a, int F) {
     return neg ? -r : r;
 }
 
-constexpr int FIX_R = 64;  // member rows per batch
+constexpr int FIX_R = 64;       // member rows whose indices are staged per batch
+constexpr int FIX_SPLIT = 16;   // blocks per cluster (the sums are order-free)
+constexpr int FIX_U = 8;        // rows loaded ahead per thread
 
-// One block per (cluster, feature slab); thread j sums feature j exactly.
-// Also accumulates (x_ij - c_j)^2 against the old centre in compensated f32
-// for the inertia.
-__global__ void centroid_fixed_kernel(const float *__restrict__ x, int d, int k, int64_t n,
-                                      const int32_t *__restrict__ members, const int32_t *__restrict__ offs,
-                                      int64_t nseg, const double *__restrict__ old_c, double *__restrict__ new_c,
-                                      const float *__restrict__ amax_ptr, double *__restrict__ inertia_part) {
-    __shared__ int32_t sidx[FIX_R];
-    const int c = blockIdx.x;
-    const int j = blockIdx.y * blockDim.x + threadIdx.x;
-    const int64_t start = offs[(int64_t)c * nseg];
-    const int64_t end = (c + 1 < k) ? (int64_t)offs[(int64_t)(c + 1) * nseg] : n;
-    // fraction bits: n * max|x| * 2^F < 2^126
+struct alignas(16) FixedPart {
+    unsigned long long lo, hi;  // signed 128-bit partial sum (two's complement)
+    float isum, icomp;          // compensated f32 partial inertia
+    uint32_t flags, pad;
+};
+
+__device__ __forceinline__ int fixed_bits(const float *amax_ptr, int64_t n) {
+    // fraction bits: n * max|x| * 2^F < 2^126, so no partial sum can overflow
     const float amax = *amax_ptr;
     const int ea = amax > 0.f ? (int)((__float_as_uint(amax) >> 23) & 0xFFu) - 127 : -126;
     const int ln = 64 - __clzll((long long)(n > 0 ? n : 1));
-    const int F = 124 - ln - ea;
-    FixedAcc a0{0, 0, 0, 0, 0u};
+    return 124 - ln - ea;
+}
+
+// Block (cluster c, part y) sums feature j over its share of the cluster's
+// rows exactly, and the compensated-f32 inertia partial against the old centre.
+__global__ void centroid_fixed_part_kernel(const float *__restrict__ x, int d, int k, int64_t n,
+                                           const int32_t *__restrict__ members, const int32_t *__restrict__ offs,
+                                           int64_t nseg, const double *__restrict__ old_c,
+                                           const float *__restrict__ amax_ptr, FixedPart *__restrict__ parts) {
+    __shared__ int32_t sidx[FIX_R];
+    const int c = blockIdx.x, y = blockIdx.y;
+    const int j = blockIdx.z * blockDim.x + threadIdx.x;
+    const int64_t cstart = offs[(int64_t)c * nseg];
+    const int64_t cend = (c + 1 < k) ? (int64_t)offs[(int64_t)(c + 1) * nseg] : n;
+    const int64_t share = (cend - cstart + FIX_SPLIT - 1) / FIX_SPLIT;
+    const int64_t start = cstart + (int64_t)y * share;
+    const int64_t end = min(cend, start + share);
+    const int F = fixed_bits(amax_ptr, n);
+    FixedAcc a{0, 0, 0, 0, 0u};
     float isum = 0.f, icomp = 0.f;
     const float cj = j < d ? (float)old_c[(int64_t)c * d + j] : 0.f;
     for (int64_t base = start; base < end; base += FIX_R) {
@@ -305,39 +319,67 @@ __global__ void centroid_fixed_kernel(const float *__restrict__ x, int d, int k,
         for (int t = threadIdx.x; t < cnt; t += blockDim.x) sidx[t] = members[base + t];
         __syncthreads();
         if (j < d) {
-#pragma unroll 8
-            for (int r = 0; r < cnt; r++) {
-                const float v0 = x[(int64_t)sidx[r] * d + j];
-                fixed_add(a0, v0, F);
-                const float df = __fsub_rn(v0, cj);
-                const float y = __fsub_rn(__fmul_rn(df, df), icomp);
-                const float tt = __fadd_rn(isum, y);
-                icomp = __fsub_rn(__fsub_rn(tt, isum), y);
-                isum = tt;
+            for (int r0 = 0; r0 < cnt; r0 += FIX_U) {
+                float v[FIX_U];
+#pragma unroll
+                for (int u = 0; u < FIX_U; u++) v[u] = r0 + u < cnt ? x[(int64_t)sidx[r0 + u] * d + j] : 0.f;
+#pragma unroll
+                for (int u = 0; u < FIX_U; u++) {
+                    if (r0 + u < cnt) {
+                        fixed_add(a, v[u], F);
+                        const float df = __fsub_rn(v[u], cj);
+                        const float yy = __fsub_rn(__fmul_rn(df, df), icomp);
+                        const float tt = __fadd_rn(isum, yy);
+                        icomp = __fsub_rn(__fsub_rn(tt, isum), yy);
+                        isum = tt;
+                    }
+                }
             }
         }
     }
     if (j < d) {
-        const int64_t cntc = end - start;
-        double mean;
-        if (cntc == 0) {
-            mean = old_c[(int64_t)c * d + j];
-        } else {
-            const uint32_t fl = a0.flags;
-            double sum;
-            if ((fl & 1u) || (fl & 6u) == 6u) sum = __longlong_as_double(0x7FF8000000000000LL);
-            else if (fl & 2u) sum = __longlong_as_double(0x7FF0000000000000LL);
-            else if (fl & 4u) sum = __longlong_as_double((long long)0xFFF0000000000000ULL);
-            else {
-                const unsigned __int128 pos = ((unsigned __int128)a0.phi << 64) | a0.plo;
-                const unsigned __int128 neg = ((unsigned __int128)a0.nhi << 64) | a0.nlo;
-                sum = fixed_to_double(pos - neg, F);
-            }
-            mean = __ddiv_rn(sum, (double)cntc);
-        }
-        new_c[(int64_t)c * d + j] = mean;
-        inertia_part[(int64_t)c * d + j] = (double)isum - (double)icomp;
+        unsigned long long lo = a.plo, hi = a.phi;
+        asm("sub.cc.u64 %0, %0, %2;\n\tsubc.u64 %1, %1, %3;" : "+l"(lo), "+l"(hi) : "l"(a.nlo), "l"(a.nhi));
+        parts[((int64_t)c * FIX_SPLIT + y) * d + j] = FixedPart{lo, hi, isum, icomp, a.flags, 0u};
     }
+}
+
+// Per (cluster, feature): exact sum of the parts, rounded once to f64, then
+// divided by the count (empty cluster: keep the old centre); the inertia
+// partials folded in a fixed order.
+__global__ void centroid_fixed_combine_kernel(int d, int k, int64_t n, const int32_t *__restrict__ offs, int64_t nseg,
+                                              const double *__restrict__ old_c, double *__restrict__ new_c,
+                                              const float *__restrict__ amax_ptr, const FixedPart *__restrict__ parts,
+                                              double *__restrict__ inertia_part) {
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (int64_t)k * d) return;
+    const int c = (int)(idx / d), j = (int)(idx % d);
+    const int64_t cstart = offs[(int64_t)c * nseg];
+    const int64_t cend = (c + 1 < k) ? (int64_t)offs[(int64_t)(c + 1) * nseg] : n;
+    const int F = fixed_bits(amax_ptr, n);
+    unsigned long long lo = 0, hi = 0;
+    uint32_t fl = 0;
+    double inert = 0.0;
+    for (int y = 0; y < FIX_SPLIT; y++) {
+        const FixedPart q = parts[((int64_t)c * FIX_SPLIT + y) * d + j];
+        asm("add.cc.u64 %0, %0, %2;\n\taddc.u64 %1, %1, %3;" : "+l"(lo), "+l"(hi) : "l"(q.lo), "l"(q.hi));
+        fl |= q.flags;
+        inert += (double)q.isum - (double)q.icomp;
+    }
+    const int64_t cntc = cend - cstart;
+    double mean;
+    if (cntc == 0) {
+        mean = old_c[idx];
+    } else {
+        double sum;
+        if ((fl & 1u) || (fl & 6u) == 6u) sum = __longlong_as_double(0x7FF8000000000000LL);
+        else if (fl & 2u) sum = __longlong_as_double(0x7FF0000000000000LL);
+        else if (fl & 4u) sum = __longlong_as_double((long long)0xFFF0000000000000ULL);
+        else sum = fixed_to_double(((unsigned __int128)hi << 64) | lo, F);
+        mean = __ddiv_rn(sum, (double)cntc);
+    }
+    new_c[idx] = mean;
+    inertia_part[idx] = inert;
 }
 
 // squared_euclidean(new, old) per cluster, folded over j; max over clusters as
@@ -433,15 +475,22 @@ void launch_update_centroids(const SortPlan &p, const TX *x, int d, const int32_
     FK_LAUNCH_CHECK();
 }
 
+size_t update_exact_scratch_bytes(int k, int d) { return sizeof(FixedPart) * (size_t)k * FIX_SPLIT * d; }
+
 void launch_update_centroids_exact(const SortPlan &p, const float *x, int d, const int32_t *members,
                                    const int32_t *seg_hist, const double *old_c, double *new_c, DevScalars *scalars,
-                                   const float *amax, double *inertia_part, cudaStream_t s) {
+                                   const float *amax, double *inertia_part, void *scratch, cudaStream_t s) {
+    FixedPart *parts = (FixedPart *)scratch;
     FK_CUDA(cudaMemsetAsync(&scalars->shift_bits, 0, sizeof(unsigned long long), s));
     if (d == 0 || p.k == 0) return;
     int threads = d >= 256 ? 256 : (d + 31) / 32 * 32;
-    dim3 grid((unsigned)p.k, (unsigned)((d + threads - 1) / threads));
-    centroid_fixed_kernel<<<grid, threads, 0, s>>>(x, d, p.k, p.n, members, seg_hist, p.nseg, old_c, new_c, amax,
-                                                   inertia_part);
+    dim3 grid((unsigned)p.k, FIX_SPLIT, (unsigned)((d + threads - 1) / threads));
+    centroid_fixed_part_kernel<<<grid, threads, 0, s>>>(x, d, p.k, p.n, members, seg_hist, p.nseg, old_c, amax,
+                                                        parts);
+    FK_LAUNCH_CHECK();
+    const int64_t kd = (int64_t)p.k * d;
+    centroid_fixed_combine_kernel<<<(unsigned)((kd + 255) / 256), 256, 0, s>>>(d, p.k, p.n, seg_hist, p.nseg, old_c,
+                                                                               new_c, amax, parts, inertia_part);
     FK_LAUNCH_CHECK();
     max_shift_kernel<double><<<(p.k + 127) / 128, 128, 0, s>>>(new_c, old_c, p.k, d, &scalars->shift_bits);
     FK_LAUNCH_CHECK();
