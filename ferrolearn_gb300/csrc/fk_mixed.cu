@@ -313,10 +313,20 @@ __device__ __forceinline__ float sqeuc32(const float *__restrict__ x, const floa
     return acc;
 }
 
-__device__ __forceinline__ double bound32(double d32, double ec, int d) {
-    double r = sqrt(d32 > 0.0 ? d32 : 0.0);
-    return ((double)(d + 3) * 1.1920928955078125e-07 * d32 + 2.0 * r * ec + 3.0 * ec * ec +
-            (double)(d + 4) * 2.220446049250313e-16 * d32) * 1.01 + 1e-30;
+// Upper bound, in f32 with upward rounding, of |d32 - D| + |D64 - D| where D
+// is the exact real distance and D64 the oracle's FP64 direct form:
+// ((d+4) 2^-23 d32 + 2 sqrt(d32) ec + 3 ec^2) * 1.01.
+__device__ __forceinline__ float bound32(float d32, float ec, int d) {
+    const float dd = d32 > 0.f ? d32 : 0.f;
+    float e = __fmul_ru((float)(d + 4) * 1.1920929e-07f, dd);
+    e = __fadd_ru(e, __fmul_ru(__fmul_ru(2.0f, __fsqrt_ru(dd)), ec));
+    e = __fadd_ru(e, __fmul_ru(3.0f, __fmul_ru(ec, ec)));
+    return __fadd_ru(__fmul_ru(e, 1.01f), 1e-30f);
+}
+
+// a certainly below b (false for any NaN or infinity)
+__device__ __forceinline__ bool below(float da, float ea, float db, float eb) {
+    return __fadd_ru(da, ea) < __fsub_rd(db, eb);
 }
 
 // One warp per listed row (coalesced over the features): FP32 distances to
@@ -346,13 +356,12 @@ __global__ void pair_rescore_kernel(const TX *__restrict__ x, int d, const doubl
             }
             sa = warp_sum_f(sa);
             sb = warp_sum_f(sb);
-            const double da = sa, db = sb;
-            const double ea = bound32(da, ec32[a], d), eb = bound32(db, ec32[b], d);
-            if (da + ea < db - eb) {  // false for any NaN or infinity
+            const float ea = bound32(sa, ec32[a], d), eb = bound32(sb, ec32[b], d);
+            if (below(sa, ea, sb, eb)) {
                 if (lane == 0) labels[e.x] = a;
                 continue;
             }
-            if (db + eb < da - ea) {
+            if (below(sb, eb, sa, ea)) {
                 if (lane == 0) labels[e.x] = b;
                 continue;
             }
@@ -388,24 +397,22 @@ __global__ void full_rescore_kernel(const TX *__restrict__ x, int d, const doubl
     for (unsigned long long s = wid; s < cnt; s += nw) {
         const int64_t r = list[s];
         const TX *row = x + r * d;
-        double ub = INFINITY;
+        float ub = INFINITY;
         if constexpr (std::is_same<TX, float>::value) {
             for (int q = lane; q < k; q += 32) {
-                double v = sqeuc32(row, c32 + (int64_t)q * d, d);
-                double e = bound32(v, ec32[q], d);
-                double hi = v + e;
+                float v = sqeuc32(row, c32 + (int64_t)q * d, d);
+                float hi = __fadd_ru(v, bound32(v, ec32[q], d));
                 if (hi < ub) ub = hi;  // NaN never lowers the bound
             }
 #pragma unroll
-            for (int off = 16; off >= 1; off >>= 1) ub = fmin(ub, __shfl_xor_sync(0xffffffffu, ub, off));
+            for (int off = 16; off >= 1; off >>= 1) ub = fminf(ub, __shfl_xor_sync(0xffffffffu, ub, off));
         }
         double b1 = DBL_MAX, b2 = DBL_MAX;
         int i1 = INT32_MAX;
         for (int q = lane; q < k; q += 32) {
             if constexpr (std::is_same<TX, float>::value) {
-                double v = sqeuc32(row, c32 + (int64_t)q * d, d);
-                double e = bound32(v, ec32[q], d);
-                if (v - e > ub) continue;  // certainly above the minimum
+                float v = sqeuc32(row, c32 + (int64_t)q * d, d);
+                if (__fsub_rd(v, bound32(v, ec32[q], d)) > ub) continue;  // certainly above the minimum
             }
             double v = sqeuc64(row, c + (int64_t)q * d, d);
             if (v < b1) { b2 = b1; b1 = v; i1 = q; }
@@ -562,16 +569,16 @@ full_tiled_kernel(const float *__restrict__ x, int d, const float *__restrict__ 
             double out = INFINITY;  // not a candidate
             const int rr = rid[r];
             if (rr >= 0 && ti[r][e] >= 0) {
-                double ub = INFINITY;
+                float ub = INFINITY;
 #pragma unroll
                 for (int q = 0; q < 4; q++)
-                    if (ti[r][q] >= 0) ub = fmin(ub, (double)tv[r][q] + bound32(tv[r][q], ec32[ti[r][q]], d));
-                const double v = tv[r][e];
-                if (!(v - bound32(v, ec32[ti[r][e]], d) > ub)) {
+                    if (ti[r][q] >= 0) ub = fminf(ub, __fadd_ru(tv[r][q], bound32(tv[r][q], ec32[ti[r][q]], d)));
+                const float v = tv[r][e];
+                if (!(__fsub_rd(v, bound32(v, ec32[ti[r][e]], d)) > ub)) {
                     int ncand = 0;
 #pragma unroll
                     for (int q = 0; q < 4; q++)
-                        if (ti[r][q] >= 0 && !((double)tv[r][q] - bound32(tv[r][q], ec32[ti[r][q]], d) > ub)) ncand++;
+                        if (ti[r][q] >= 0 && !(__fsub_rd(tv[r][q], bound32(tv[r][q], ec32[ti[r][q]], d)) > ub)) ncand++;
                     out = ncand > 1 ? sqeuc64(x + (int64_t)rr * d, c64 + (int64_t)ti[r][e] * d, d) : -1.0;
                 }
             }
@@ -582,9 +589,9 @@ full_tiled_kernel(const float *__restrict__ x, int d, const float *__restrict__ 
             const int r = tid, rr = rid[r];
             bool overflow = ti[r][0] < 0;  // no finite FP32 distance at all
             if (!overflow && k > 4 && ti[r][3] >= 0) {
-                double ub = INFINITY;
-                for (int q = 0; q < 4; q++) ub = fmin(ub, (double)tv[r][q] + bound32(tv[r][q], ec32[ti[r][q]], d));
-                if (!((double)tv[r][3] - bound32(tv[r][3], ecmax_s, d) > ub)) overflow = true;
+                float ub = INFINITY;
+                for (int q = 0; q < 4; q++) ub = fminf(ub, __fadd_ru(tv[r][q], bound32(tv[r][q], ec32[ti[r][q]], d)));
+                if (!(__fsub_rd(tv[r][3], bound32(tv[r][3], ecmax_s, d)) > ub)) overflow = true;
             }
             if (overflow) {
                 unsigned long long slot = atomicAdd(&sc->over_count, 1ULL);
@@ -657,7 +664,7 @@ void run_assign_mixed(Ctx &ctx, const TX *x, int64_t n, int d, const double *c, 
         // most 65536 rows is enough
         const int64_t stride = n > 65536 ? n / 65536 : 1;
         const int64_t rows = (n + stride - 1) / stride;
-        const int64_t rows_per = 1024;
+        const int64_t rows_per = 64;
         const int nparts = (int)((rows + rows_per - 1) / rows_per);
         double *part = (double *)ctx.get(BUF_PARTIAL, sizeof(double) * (size_t)nparts * d);
         dim3 g1(nparts, (d + 127) / 128);
