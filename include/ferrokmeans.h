@@ -183,6 +183,28 @@ fk_status fk_kmeans_plus_plus_f32(fk_ctx *ctx, const float *x, int64_t n, int64_
                                   const double *draws, int64_t n_draws, uint64_t seed,
                                   float *centers_out, int64_t *draws_used_out);
 
+/* Allocation-free scoring (no counterpart in the reference): nearest-centre
+ * labels (uint64) and the inertia (sum of the minimum squared distances,
+ * f64) of n rows of x against k centres, with the plain FP64 arithmetic of
+ * kmeans.rs (direct form, lowest index on ties). For callers that cannot
+ * allocate device memory at call time (serving loops where an allocation
+ * would synchronise the device, fixed memory budgets, hosts whose allocator
+ * belongs to another framework): x, centers, labels_out and inertia_out must
+ * all be device memory of the current device, and the scratch is one
+ * fixed-size device array compiled into the library (about 6.3 MB per GPU,
+ * held until the process exits). Limits: n <= 524288 rows, else
+ * FK_ERR_INVALID_PARAMETER with a message naming the limit. The work is
+ * queued on cuda_stream (NULL = the legacy default stream) and the outputs
+ * are valid once that stream reaches this point; the call itself does not
+ * wait. The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress), so make that first call before any stream capture.
+ * All calls share the one array: calls that overlap on the GPU (different
+ * streams, or threads without ordering) race and must be serialised by the
+ * caller. */
+fk_status fk_kmeans_score_f64_noalloc(const double *x, int64_t n, int64_t d, const double *centers,
+                                      int64_t k, uint64_t *labels_out, double *inertia_out,
+                                      void *cuda_stream);
+
 /* Diagnostics (no reference counterpart): CUDA-core throughput of this GPU,
  * out[0] FP32 FMA flop/s, [1] FP64 FMA flop/s, [2] FP64 add op/s, [3] FP32
  * add op/s, [4] FP64 add latency in cycles, [5] FP32 add latency. */
