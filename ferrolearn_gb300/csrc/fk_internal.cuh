@@ -59,6 +59,8 @@ struct DevScalars {
     unsigned long long flag_count;  // number of rows queued for re-check
     unsigned long long full_count;  // number of rows queued for a full re-scan
     unsigned long long over_count;  // full re-scan rows with more than 4 FP32 candidates
+    unsigned long long quad_count;  // second pass: rows with at most 4 candidates
+    unsigned long long ex_count;    // second pass: rows with more than 4 candidates
     unsigned long long error_word;  // nonzero: a bounded device wait gave up
 };
 
@@ -72,7 +74,10 @@ struct MixedStats {
     float ch_max;  // max_c ||ch||
     float h_max;   // max_c ||c'||^2 / 2
     float co_max;  // max_c ||c||  (uncentred, for the FP64 rounding term)
-    float big;     // BIG of this iteration
+    float big;     // BIG of this iteration: 1.5 * 2^E, every score lies in [2^E, 2^(E+1))
+    float cgrid;   // 3 * 2^(E+6): (T + cgrid) - cgrid rounds T to a multiple of 2^(E-16)
+    float ulp;     // 2^(E-23), the unit in the last place of every score
+    float pad;
 };
 
 // Best and second-best score of one row over one slice of the centres, and
@@ -80,6 +85,13 @@ struct MixedStats {
 struct alignas(16) Top2 {
     float v1, v2, u3, pad;
     int i1, i2, pad1, pad2;
+};
+
+// Best four scores of one row over one slice, and u5, a bound of the rest.
+struct alignas(16) Top4 {
+    float v[4];
+    int i[4];
+    float u5, pad0, pad1, pad2;
 };
 
 // Launch plan of the tensor-core assignment (fk_tc.cu).
@@ -97,7 +109,8 @@ struct MixedPlan {
     size_t smem = 0;
     const void *x = nullptr;
     double mu_norm = 0.0;
-    const void *tm_x_ptr = nullptr, *tm_c_ptr = nullptr, *tm_aug_ptr = nullptr;
+    const void *tm_x_ptr = nullptr, *tm_c_ptr = nullptr, *tm_aug_ptr = nullptr, *tm_x2_ptr = nullptr;
+    alignas(64) unsigned char tm_x2[128];
     alignas(64) unsigned char tm_x[128];
     alignas(64) unsigned char tm_c[128];
     alignas(64) unsigned char tm_aug[128];
@@ -110,7 +123,7 @@ enum BufSlot {
     BUF_X = 0, BUF_XC, BUF_C0, BUF_C1, BUF_CBEST, BUF_LABELS, BUF_LBEST, BUF_MIND,
     BUF_MEMBERS, BUF_SEGHIST, BUF_SCAN_TMP, BUF_COUNTS, BUF_PARTIAL, BUF_SCALARS,
     BUF_OUT, BUF_OUT2, BUF_KPP0, BUF_KPP1, BUF_KPP2, BUF_KPP3, BUF_DRAWS,
-    BUF_XB, BUF_XNORM, BUF_CB, BUF_CAUX, BUF_TOP2, BUF_FLAGS, BUF_FULL, BUF_CF32, BUF_CF32C, BUF_OVER, BUF_FIXPART,
+    BUF_XB, BUF_XNORM, BUF_CB, BUF_CAUX, BUF_TOP2, BUF_FLAGS, BUF_FULL, BUF_CF32, BUF_CF32C, BUF_OVER, BUF_FIXPART, BUF_XB2, BUF_TOP4, BUF_QUAD, BUF_EX,
     BUF_COUNT
 };
 
@@ -241,8 +254,11 @@ void launch_mixed_inertia(Ctx &ctx, const double *part, int64_t m, DevScalars *s
 // writes one Top2 record per (slice, row).
 void plan_tc(Ctx &ctx, MixedPlan &mp, int64_t n, int d, int k);
 // dump (tests only, nullable): raw accumulators of CTA 0's first tile.
+// out4 != nullptr selects the second pass (top-4 records over the gathered
+// rows whose count is read from n_dev at launch; mp.n is their capacity).
 void launch_tc_assign(Ctx &ctx, MixedPlan &mp, const void *xb, const void *cb, const void *caug, Top2 *out,
-                      DevScalars *sc, float *dump = nullptr);
+                      DevScalars *sc, const MixedStats *stats, float *dump = nullptr, Top4 *out4 = nullptr,
+                      const unsigned long long *n_dev = nullptr);
 
 void measure_peaks(Ctx &ctx, double *out);
 void debug_tc_probe(Ctx &ctx, const float *x, int64_t n, int d, const double *c, int k, float *dump_out,

@@ -197,12 +197,22 @@ __global__ void prep_centres_kernel(const double *__restrict__ c, int k, int k_p
 
 // a_c = BIG - ||c'||^2/2 split into three BF16 terms (columns 0..2 of the
 // 16-column augmentation row); padded centres get a_c = 0, so they score 0.
+// BIG = 1.5 * 2^E with 2^E >= 2.02 (max||xh|| max||ch|| + max||c'||^2/2) + 256,
+// so every real score T = xh.ch + a_c lies in [2^E, 2^(E+1)) with room to
+// spare: all scores of a launch share one exponent, which lets the epilogue
+// round them to a common grid and insert the column code exactly.
 __global__ void prep_aug_kernel(const double *__restrict__ half_norm, int k, int k_pad,
                                 __nv_bfloat16 *__restrict__ caug, MixedStats *stats) {
     int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= k_pad) return;
-    double big = ((double)stats->xn_max * (double)stats->ch_max + (double)stats->h_max) * (1.0 + 1e-3) + 64.0;
-    if (q == 0) stats->big = (float)big;
+    const double span = (double)stats->xn_max * (double)stats->ch_max + (double)stats->h_max;
+    const int e = (int)ceil(log2(2.02 * span + 256.0));
+    const double big = 1.5 * ldexp(1.0, e);
+    if (q == 0) {
+        stats->big = (float)big;
+        stats->cgrid = (float)(3.0 * ldexp(1.0, e + 6));
+        stats->ulp = (float)ldexp(1.0, e - 23);
+    }
     __nv_bfloat16 t[16];
 #pragma unroll
     for (int j = 0; j < 16; j++) t[j] = __float2bfloat16_rn(0.f);
@@ -222,6 +232,24 @@ __global__ void prep_aug_kernel(const double *__restrict__ half_norm, int k, int
 }
 
 // --------------------------------------------------------------- finalize --
+// Threshold on a score margin above which no other centre can win in the
+// FP64 direct form (see the file header): 2E + key quantum + FP64 rounding.
+__device__ __forceinline__ double row_threshold(const float4 ri, const MixedStats *stats, double acc_rel, double mu_norm,
+                                                int d, float v1) {
+    const double xn = ri.x, ex = ri.y, xo = ri.z;
+    const double cn = stats->cn_max, ec = stats->ec_max, ch = stats->ch_max, big = stats->big;
+    const double co = stats->co_max;
+    double e = ex * cn + xn * ec + acc_rel * (xn * ch + big) + REPR_REL * big;
+    // keys: each score rounded to a multiple of 128 ulp (error <= 64 ulp) plus a
+    // column code below 128 ulp, so a key is within 192 ulp of its score
+    double q = 384.0 * (double)stats->ulp;
+    double xo_b = xo > xn + ex + mu_norm ? xo : xn + ex + mu_norm;  // ||x|| (both bounds are valid)
+    double delta = (double)(d + 4) * 1.1102230246251565e-16 * (xo_b + co) * (xo_b + co);  // FP64 rounding, D units
+    double thr = (2.0 * e + q + 0.5 * delta) * (1.0 + 1e-6) + 1e-30;
+    if (!(v1 >= stats->big * 0.6f)) thr = INFINITY;  // not a real score (NaN row, all slices padded)
+    return thr;
+}
+
 // Merge of two slice records: (v1 >= v2, i1, i2) with u3 bounding the rest,
 // and the same for the other slice.
 __device__ __forceinline__ void merge_top2(float &v1, int &i1, float &v2, int &i2, float &u3, float w1, int j1,
@@ -260,15 +288,7 @@ __global__ void finalize_kernel(const Top2 *__restrict__ parts, int nparts, int6
         Top2 o = parts[(int64_t)p * n + i];
         merge_top2(v1, i1, v2, i2, u3, o.v1, o.i1, o.v2, o.i2, o.u3);
     }
-    const float4 ri = rowinfo[i];
-    const double xn = ri.x, ex = ri.y, xo = ri.z;
-    const double cn = stats->cn_max, ec = stats->ec_max, ch = stats->ch_max, big = stats->big;
-    const double co = stats->co_max;
-    double e = ex * cn + xn * ec + acc_rel * (xn * ch + big) + REPR_REL * big;
-    double q = (double)v1 * 0.000030517578125;                      // key truncation, 2^-15 relative
-    double xo_b = xo > xn + ex + mu_norm ? xo : xn + ex + mu_norm;  // ||x|| (both bounds are valid)
-    double delta = (double)(d + 4) * 1.1102230246251565e-16 * (xo_b + co) * (xo_b + co);  // FP64 rounding, D units
-    double thr = (2.0 * e + q + 0.5 * delta) * (1.0 + 1e-6) + 1e-30;
+    const double thr = row_threshold(rowinfo[i], stats, acc_rel, mu_norm, d, v1);
     double m12 = (double)v1 - (double)v2;
     if (i1 >= 0 && i1 < k && m12 > thr) {
         labels[i] = i1;
@@ -466,8 +486,9 @@ __device__ __forceinline__ void top4_insert(float (&v)[4], int (&ix)[4], float v
 
 __global__ void __launch_bounds__(FT_T)
 full_tiled_kernel(const float *__restrict__ x, int d, const float *__restrict__ c32, const float *__restrict__ ec32,
-                  const double *__restrict__ c64, int k, const int32_t *__restrict__ list, DevScalars *sc,
-                  int32_t *__restrict__ labels, int32_t *__restrict__ over_list) {
+                  const double *__restrict__ c64, int k, const int32_t *__restrict__ list,
+                  const unsigned long long *count_ptr, DevScalars *sc, int32_t *__restrict__ labels,
+                  int32_t *__restrict__ over_list) {
     __shared__ __align__(16) float xs[FT_DJ][FT_BM];
     __shared__ __align__(16) float cs[FT_DJ][FT_BN];
     __shared__ int rid[FT_BM];
@@ -475,7 +496,7 @@ full_tiled_kernel(const float *__restrict__ x, int d, const float *__restrict__ 
     __shared__ int ti[FT_BM][4];
     __shared__ double dv[FT_BM][4];
     __shared__ float ecmax_s;
-    const unsigned long long count = sc->full_count;
+    const unsigned long long count = *count_ptr;
     const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
     if (tid == 0) {
         float m = 0.f;
@@ -618,6 +639,166 @@ full_tiled_kernel(const float *__restrict__ x, int d, const float *__restrict__ 
     }
 }
 
+// ------------------------------------------------------- second pass --
+// Rows whose third-best BF16 score was inside the bound are gathered and
+// scored again by the tensor cores with a top-4 epilogue; then only the (at
+// most four) centres inside the bound are re-scored.
+__global__ void gather_rows_kernel(const uint4 *__restrict__ xb, int row_vecs, const int32_t *__restrict__ list,
+                                   const unsigned long long *count_ptr, uint4 *__restrict__ xb2) {
+    const unsigned long long cnt = *count_ptr;
+    const int lane = threadIdx.x & 31;
+    const unsigned long long wid = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const unsigned long long nw = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
+    for (unsigned long long s = wid; s < cnt; s += nw) {
+        const int64_t r = list[s];
+        for (int v = lane; v < row_vecs; v += 32) xb2[(int64_t)s * row_vecs + v] = xb[r * row_vecs + v];
+    }
+}
+
+struct Quad {
+    int row, m, i0, i1, i2, i3, pad0, pad1;
+};
+
+__device__ __forceinline__ uint32_t ins4u(uint32_t (&R)[4], int (&I)[4], uint32_t w, int j) {
+#pragma unroll
+    for (int p = 0; p < 4; p++) {
+        if (w > R[p]) {
+            const uint32_t tw = R[p];
+            const int tj = I[p];
+            R[p] = w;
+            I[p] = j;
+            w = tw;
+            j = tj;
+        }
+    }
+    return w;
+}
+
+__global__ void finalize4_kernel(const Top4 *__restrict__ parts, int nparts, int64_t cap, int k, int d,
+                                 const int32_t *__restrict__ list, const float4 *__restrict__ rowinfo,
+                                 const MixedStats *stats, double acc_rel, double mu_norm, int32_t *__restrict__ labels,
+                                 Quad *__restrict__ quads, int32_t *__restrict__ ex_list, DevScalars *sc) {
+    const unsigned long long cnt = sc->full_count;
+    for (unsigned long long s = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; s < cnt;
+         s += (unsigned long long)gridDim.x * blockDim.x) {
+        uint32_t R[4], U;
+        int I[4];
+        {
+            const Top4 t = parts[s];
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                R[j] = __float_as_uint(t.v[j]);
+                I[j] = t.i[j];
+            }
+            U = __float_as_uint(t.u5);
+        }
+        for (int p = 1; p < nparts; p++) {
+            const Top4 o = parts[(int64_t)p * cap + s];
+            U = max(U, __float_as_uint(o.u5));
+#pragma unroll
+            for (int j = 0; j < 4; j++) U = max(U, ins4u(R, I, __float_as_uint(o.v[j]), o.i[j]));
+        }
+        const int32_t row = list[s];
+        const float v1 = __uint_as_float(R[0]);
+        const double thr = row_threshold(rowinfo[row], stats, acc_rel, mu_norm, d, v1);
+        const bool rest_out = (double)v1 - (double)__uint_as_float(U) > thr;
+        int m = 0;
+        bool valid = true;
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            if ((double)v1 - (double)__uint_as_float(R[j]) <= thr) {
+                m++;
+                if (I[j] < 0 || I[j] >= k) valid = false;
+            }
+        }
+        if (!rest_out || !valid || m == 0) {
+            unsigned long long slot = atomicAdd(&sc->ex_count, 1ULL);
+            ex_list[slot] = row;
+        } else if (m == 1) {
+            labels[row] = I[0];
+        } else {
+            unsigned long long slot = atomicAdd(&sc->quad_count, 1ULL);
+            quads[slot] = Quad{row, m, I[0], I[1], I[2], I[3], 0, 0};
+        }
+    }
+}
+
+// One warp per row with at most four candidates: FP32 distances (lanes over
+// the features) with rigorous bounds; the candidates whose lower bound
+// reaches the smallest upper bound are scored exactly in FP64 (one lane
+// each, direct form), lowest index on ties.
+__global__ void quad_rescore_kernel(const float *__restrict__ x, int d, const double *__restrict__ c,
+                                    const float *__restrict__ c32, const float *__restrict__ ec32,
+                                    const Quad *__restrict__ quads, DevScalars *sc, int32_t *__restrict__ labels) {
+    const unsigned long long cnt = sc->quad_count;
+    const int lane = threadIdx.x & 31;
+    const unsigned long long wid = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const unsigned long long nw = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
+    for (unsigned long long s = wid; s < cnt; s += nw) {
+        const Quad qd = quads[s];
+        const int ids[4] = {qd.i0, qd.i1, qd.i2, qd.i3};
+        const float *row = x + (int64_t)qd.row * d;
+        float dist[4], err[4];
+        float ub = INFINITY;
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            float acc = 0.f;
+            if (j < qd.m) {
+                const float *cc = c32 + (int64_t)ids[j] * d;
+                for (int f = lane; f < d; f += 32) {
+                    const float t = row[f] - cc[f];
+                    acc = fmaf(t, t, acc);
+                }
+            }
+            acc = warp_sum_f(acc);
+            dist[j] = acc;
+            err[j] = j < qd.m ? bound32(acc, ec32[ids[j]], d) : 0.f;
+            if (j < qd.m) ub = fminf(ub, __fadd_ru(acc, err[j]));
+        }
+        int nsurv = 0, only = -1;
+#pragma unroll
+        for (int j = 0; j < 4; j++)
+            if (j < qd.m && !(__fsub_rd(dist[j], err[j]) > ub)) {
+                nsurv++;
+                only = ids[j];
+            }
+        if (nsurv == 1) {
+            if (lane == 0) labels[qd.row] = only;
+            continue;
+        }
+        // FP64 on the survivors (or on all candidates if some FP32 value was not finite)
+        double v = DBL_MAX;
+        int id = INT32_MAX;
+        if (lane < qd.m) {
+            const bool surv = nsurv == 0 || !(__fsub_rd(dist[lane], err[lane]) > ub);
+            if (surv) {
+                id = ids[lane];
+                v = sqeuc64(row, c + (int64_t)id * d, d);
+                if (!(v < DBL_MAX)) id = INT32_MAX;  // not below F::MAX: never chosen
+            }
+        }
+        double b2 = DBL_MAX;
+#pragma unroll
+        for (int off = 16; off >= 1; off >>= 1) {
+            const double ov = __shfl_xor_sync(0xffffffffu, v, off);
+            const int oi = __shfl_xor_sync(0xffffffffu, id, off);
+            const double ob2 = __shfl_xor_sync(0xffffffffu, b2, off);
+            if (ov < v || (ov == v && oi < id)) {
+                b2 = fmin(v, ob2);
+                v = ov;
+                id = oi;
+            } else {
+                b2 = fmin(b2, ov);
+            }
+        }
+        if (lane == 0) {
+            labels[qd.row] = id == INT32_MAX ? 0 : id;
+            atomicAdd(&sc->recheck_rows, 1ULL);
+            if (id != INT32_MAX && b2 < DBL_MAX && near_tie(v, b2)) atomicAdd(&sc->near_tie_rows, 1ULL);
+        }
+    }
+}
+
 // ---------------------------------------------------- mixed inertia --
 __global__ void inertia_final_kernel(const double *__restrict__ part, int64_t m, double *out) {
     __shared__ double sh[32];
@@ -701,7 +882,7 @@ void run_assign_mixed(Ctx &ctx, const TX *x, int64_t n, int d, const double *c, 
     Top2 *top = (Top2 *)ctx.get(BUF_TOP2, sizeof(Top2) * (size_t)n * mp.parts);
     {
         Timer t(ctx.contract_acc != nullptr, ctx, ctx.contract_acc);
-        launch_tc_assign(ctx, mp, xb, cb, caug, top, sc);
+        launch_tc_assign(ctx, mp, xb, cb, caug, top, sc, stats);
     }
 
     int4 *pairs = (int4 *)ctx.get(BUF_FLAGS, sizeof(int4) * (size_t)n);
@@ -714,8 +895,22 @@ void run_assign_mixed(Ctx &ctx, const TX *x, int64_t n, int d, const double *c, 
     pair_rescore_kernel<TX><<<grid, 256, 0, s>>>(x, d, c, c32, ec32, pairs, sc, labels);
     FK_LAUNCH_CHECK();
     if constexpr (std::is_same<TX, float>::value) {
+        // second tensor pass over the rows whose third score was inside the bound
+        __nv_bfloat16 *xb2 = (__nv_bfloat16 *)ctx.get(BUF_XB2, sizeof(__nv_bfloat16) * (size_t)n * mp.d_pad);
+        Top4 *top4 = (Top4 *)ctx.get(BUF_TOP4, sizeof(Top4) * (size_t)n * mp.parts);
+        Quad *quads = (Quad *)ctx.get(BUF_QUAD, sizeof(Quad) * (size_t)n);
+        int32_t *ex = (int32_t *)ctx.get(BUF_EX, sizeof(int32_t) * (size_t)n);
         int32_t *over = (int32_t *)ctx.get(BUF_OVER, sizeof(int32_t) * (size_t)n);
-        full_tiled_kernel<<<ctx.num_sms * 2, FT_T, 0, s>>>(x, d, c32, ec32, c, k, full, sc, labels, over);
+        gather_rows_kernel<<<grid, 256, 0, s>>>((const uint4 *)xb, mp.d_pad * 2 / 16, full, &sc->full_count,
+                                                (uint4 *)xb2);
+        FK_LAUNCH_CHECK();
+        launch_tc_assign(ctx, mp, xb2, cb, caug, nullptr, sc, stats, nullptr, top4, &sc->full_count);
+        finalize4_kernel<<<grid, 256, 0, s>>>(top4, mp.parts, n, k, d, full, rowinfo, stats, acc_rel, mp.mu_norm,
+                                              labels, quads, ex, sc);
+        FK_LAUNCH_CHECK();
+        quad_rescore_kernel<<<grid, 256, 0, s>>>(x, d, c, c32, ec32, quads, sc, labels);
+        FK_LAUNCH_CHECK();
+        full_tiled_kernel<<<ctx.num_sms * 2, FT_T, 0, s>>>(x, d, c32, ec32, c, k, ex, &sc->ex_count, sc, labels, over);
         FK_LAUNCH_CHECK();
         full_rescore_kernel<TX><<<grid, 256, 0, s>>>(x, d, c, c32, ec32, k, over, sc, labels);
     } else {
@@ -770,7 +965,7 @@ void debug_tc_probe(Ctx &ctx, const float *x, int64_t n, int d, const double *c,
     Top2 *top = (Top2 *)ctx.get(BUF_TOP2, sizeof(Top2) * (size_t)n * mp.parts);
     float *dump = (float *)ctx.get(BUF_OUT, sizeof(float) * 128 * (size_t)mp.kp);
     FK_CUDA(cudaMemsetAsync(dump, 0, sizeof(float) * 128 * (size_t)mp.kp, s));
-    launch_tc_assign(ctx, mp, xb, cb, caug, top, sc, dump);
+    launch_tc_assign(ctx, mp, xb, cb, caug, top, sc, stats, dump);
     FK_CUDA(cudaMemcpyAsync(dump_out, dump, sizeof(float) * 128 * (size_t)mp.kp, cudaMemcpyDeviceToHost, s));
     const int64_t rows = n < 128 ? n : 128;
     FK_CUDA(cudaMemcpyAsync(xb_out, xb, sizeof(uint16_t) * (size_t)rows * mp.d_pad, cudaMemcpyDeviceToHost, s));

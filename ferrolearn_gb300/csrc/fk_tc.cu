@@ -45,7 +45,7 @@ constexpr int XSTAGES = 2;        // X ring depth
 constexpr uint32_t TMEM_COLS = 512;
 constexpr uint32_t X_ATOM_BYTES = BM * 128;  // 128 rows x 64 BF16
 constexpr uint32_t ONES_BYTES = BM * 32;     // 128 rows x 16 BF16
-constexpr uint32_t MERGE_BYTES = BM * sizeof(Top2);
+constexpr uint32_t MERGE_BYTES = BM * sizeof(Top4);
 constexpr uint32_t BAR_BYTES = 256;
 constexpr long long WAIT_LIMIT_CYCLES = 4000000000LL;
 
@@ -58,8 +58,10 @@ constexpr uint32_t LAYOUT_SW128 = 2;
 constexpr uint32_t LAYOUT_SW32 = 6;
 
 struct TcParams {
-    int64_t n;
+    int64_t n;                       // rows (or the capacity when n_dev is set)
     int64_t tiles;
+    const unsigned long long *n_dev; // optional: the row count is read here at launch
+    int64_t out_stride;              // records of slice p start at p * out_stride
     int n_atoms;       // d_pad / 64
     int kp;            // centres per slice
     int nblocks;       // kp / 256
@@ -69,8 +71,10 @@ struct TcParams {
     uint32_t c_atom_bytes;  // kp * 128
     uint32_t x_stage_bytes;
     uint32_t c_tx_bytes;
-    Top2 *out;
+    Top2 *out;                // top-2 records (main pass)
+    Top4 *out4;               // top-4 records (second pass)
     unsigned long long *err;
+    const MixedStats *stats;  // cgrid, ulp of this launch
     float *dump;  // optional: raw accumulators of the first tile of CTA 0 (tests only)
 };
 
@@ -154,14 +158,13 @@ __device__ __forceinline__ void mma_commit(uint32_t bar) {
                  : "memory");
 }
 
-// 32 consecutive columns of this thread's TMEM lane; the load and its wait
-// are one asm statement, so the registers are defined only after the wait.
+// 32 consecutive columns of this thread's TMEM lane (asynchronous: the
+// registers are valid only after tmem_wait on the same array).
 __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
     asm volatile(
         "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
         "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n\t"
-        "tcgen05.wait::ld.sync.aligned;"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
         : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
           "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
           "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
@@ -170,13 +173,17 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
         : "memory");
 }
 
-// key = (bits & 0xFFFFFF00) | code, as (bits | 0xFF) & (0xFFFFFF00 | code):
-// one lop3 with the per-column constant as its immediate.
-template <uint32_t MASKC>
-__device__ __forceinline__ float make_key(uint32_t bits, uint32_t ff) {
-    uint32_t k;
-    asm("lop3.b32 %0, %1, %2, %3, 0xA8;" : "=r"(k) : "r"(bits), "r"(ff), "n"(MASKC));
-    return __uint_as_float(k);
+// Waits for every outstanding TMEM load; tied to r so that no use of r can be
+// scheduled before it.
+__device__ __forceinline__ void tmem_wait(uint32_t (&r)[32]) {
+    asm volatile(
+        "tcgen05.wait::ld.sync.aligned;"
+        : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7]),
+          "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]), "+r"(r[14]), "+r"(r[15]),
+          "+r"(r[16]), "+r"(r[17]), "+r"(r[18]), "+r"(r[19]), "+r"(r[20]), "+r"(r[21]), "+r"(r[22]), "+r"(r[23]),
+          "+r"(r[24]), "+r"(r[25]), "+r"(r[26]), "+r"(r[27]), "+r"(r[28]), "+r"(r[29]), "+r"(r[30]), "+r"(r[31])
+        :
+        : "memory");
 }
 
 __device__ __forceinline__ float fmax3(float a, float b, float c) {
@@ -218,12 +225,24 @@ __device__ __forceinline__ void merge_res(uint32_t &R1, int &I1, uint32_t &R2, i
 // which are positive floats), merged with the bound of the rest. A NaN score
 // (NaN row) is ignored by fminf/fmaxf; such rows have non-finite bound
 // ingredients and are always re-scored in full. Returns keys.
+// Key of one score: every score of the launch lies in [2^E, 2^(E+1)), so
+// (T + cgrid) - cgrid rounds it to a multiple of 128 ulp (its low 7 bits
+// become zero) and adding code * ulp writes the column code into those bits
+// exactly. Both steps run on the FMA pipe; keys are positive floats, so
+// their float and unsigned orders agree. Padded columns (T = 0) get tiny
+// keys; NaN scores (NaN rows) give NaN keys, ignored by the min/max below.
+template <int CODE>
+__device__ __forceinline__ float make_key(uint32_t bits, float cgrid, float ulp) {
+    const float t = __fsub_rn(__fadd_rn(__uint_as_float(bits), cgrid), cgrid);
+    return __fmaf_rn(ulp, (float)CODE, t);
+}
+
 template <int HALF, int CH, int E>
-__device__ __forceinline__ void rank_pair(const uint32_t (&r)[32], uint32_t ff, float &a1, float &a2) {
+__device__ __forceinline__ void rank_pair(const uint32_t (&r)[32], float cgrid, float ulp, float &a1, float &a2) {
     // top-2 of {a1 >= a2, k0, k1}: a1' = max(a1, max(k0,k1)),
     // a2' = max(min(a1, max(k0,k1)), a2, min(k0,k1))
-    const float k0 = make_key<0xFFFFFF00u | (255u - (uint32_t)(HALF * 128 + CH * 32 + E))>(r[E], ff);
-    const float k1 = make_key<0xFFFFFF00u | (255u - (uint32_t)(HALF * 128 + CH * 32 + E + 1))>(r[E + 1], ff);
+    const float k0 = make_key<127 - ((CH * 32 + E) & 127)>(r[E], cgrid, ulp);
+    const float k1 = make_key<127 - ((CH * 32 + E + 1) & 127)>(r[E + 1], cgrid, ulp);
     const float m = fmaxf(k0, k1), l = fminf(k0, k1);
     a2 = fmax3(fminf(a1, m), a2, l);
     a1 = fmaxf(a1, m);
@@ -231,38 +250,39 @@ __device__ __forceinline__ void rank_pair(const uint32_t (&r)[32], uint32_t ff, 
 
 template <int HALF, int CH, int E>
 struct RankChunk {
-    static __device__ __forceinline__ void run(const uint32_t (&r)[32], uint32_t ff, float (&a1)[4], float (&a2)[4]) {
-        rank_pair<HALF, CH, E>(r, ff, a1[(E >> 1) & 3], a2[(E >> 1) & 3]);
-        RankChunk<HALF, CH, E + 2>::run(r, ff, a1, a2);
+    static __device__ __forceinline__ void run(const uint32_t (&r)[32], float cg, float ulp, float (&a1)[4],
+                                               float (&a2)[4]) {
+        rank_pair<HALF, CH, E>(r, cg, ulp, a1[(E >> 1) & 3], a2[(E >> 1) & 3]);
+        RankChunk<HALF, CH, E + 2>::run(r, cg, ulp, a1, a2);
     }
 };
 template <int HALF, int CH>
 struct RankChunk<HALF, CH, 32> {
-    static __device__ __forceinline__ void run(const uint32_t (&)[32], uint32_t, float (&)[4], float (&)[4]) {}
+    static __device__ __forceinline__ void run(const uint32_t (&)[32], float, float, float (&)[4], float (&)[4]) {}
 };
 
-template <int HALF, int CH>
-__device__ __forceinline__ void rank_chunk(uint32_t col_addr, uint32_t ff, float (&a1)[4], float (&a2)[4]) {
-    uint32_t r[32];
-    tmem_ld32(col_addr + CH * 32, r);
-    RankChunk<HALF, CH, 0>::run(r, ff, a1, a2);
-}
-
 // Ranks the 128 columns [HALF*128, HALF*128+128) of one accumulator block:
-// four interleaved top-2 chains over keys (positive floats, so float and
-// unsigned order agree), two elements per step with three-input max, merged
-// with the bound of the rest. A NaN score (NaN row) is ignored by the float
-// min/max; such rows have non-finite bound ingredients and are always
-// re-scored in full. Returns keys.
+// four interleaved top-2 chains over the keys, two elements per step with a
+// three-input max, the next 32 columns loading from TMEM while the current
+// ones are ranked; then the chains are merged with the bound of the rest.
+// Returns keys; the low 7 bits of a key are 127 - (column within the half).
 template <int HALF>
-__device__ __forceinline__ void rank_half(uint32_t col_addr, uint32_t &b1, uint32_t &b2, uint32_t &bu) {
+__device__ __forceinline__ void rank_half(uint32_t col_addr, float cgrid, float ulp, uint32_t &b1, uint32_t &b2,
+                                          uint32_t &bu) {
     float a1[4] = {0.f, 0.f, 0.f, 0.f}, a2[4] = {0.f, 0.f, 0.f, 0.f};
-    uint32_t ff;
-    asm volatile("mov.u32 %0, 255;" : "=r"(ff));
-    rank_chunk<HALF, 0>(col_addr, ff, a1, a2);
-    rank_chunk<HALF, 1>(col_addr, ff, a1, a2);
-    rank_chunk<HALF, 2>(col_addr, ff, a1, a2);
-    rank_chunk<HALF, 3>(col_addr, ff, a1, a2);
+    uint32_t ra[32], rb[32];
+    tmem_ld32(col_addr, ra);
+    tmem_wait(ra);
+    tmem_ld32(col_addr + 32, rb);
+    RankChunk<HALF, 0, 0>::run(ra, cgrid, ulp, a1, a2);
+    tmem_wait(rb);
+    tmem_ld32(col_addr + 64, ra);
+    RankChunk<HALF, 1, 0>::run(rb, cgrid, ulp, a1, a2);
+    tmem_wait(ra);
+    tmem_ld32(col_addr + 96, rb);
+    RankChunk<HALF, 2, 0>::run(ra, cgrid, ulp, a1, a2);
+    tmem_wait(rb);
+    RankChunk<HALF, 3, 0>::run(rb, cgrid, ulp, a1, a2);
     b1 = __float_as_uint(a1[0]);
     b2 = __float_as_uint(a2[0]);
     bu = b2;
@@ -272,10 +292,86 @@ __device__ __forceinline__ void rank_half(uint32_t col_addr, uint32_t &b1, uint3
         merge_res(b1, d1, b2, d2, bu, __float_as_uint(a1[qd]), 0, __float_as_uint(a2[qd]), 0, __float_as_uint(a2[qd]));
 }
 
+// ------------------------------------------------ top-4 (second pass) --
+// Sorted insertion of key k into a[0] >= a[1] >= a[2] >= a[3] (7 min/max).
+__device__ __forceinline__ void ins4(float (&a)[4], float k) {
+    float t = fmaxf(a[0], k);
+    k = fminf(a[0], k);
+    a[0] = t;
+    t = fmaxf(a[1], k);
+    k = fminf(a[1], k);
+    a[1] = t;
+    t = fmaxf(a[2], k);
+    k = fminf(a[2], k);
+    a[2] = t;
+    a[3] = fmaxf(a[3], k);
+}
+
+// Inserts (w, j) into the sorted running list (R, I); returns what falls out.
+__device__ __forceinline__ uint32_t ins4i(uint32_t (&R)[4], int (&I)[4], uint32_t w, int j) {
+#pragma unroll
+    for (int p = 0; p < 4; p++) {
+        if (w > R[p]) {
+            const uint32_t tw = R[p];
+            const int tj = I[p];
+            R[p] = w;
+            I[p] = j;
+            w = tw;
+            j = tj;
+        }
+    }
+    return w;
+}
+
+template <int CH>
+__device__ __forceinline__ void rank_chunk4(const uint32_t (&r)[32], float cgrid, float ulp, float (&c0)[4],
+                                            float (&c1)[4]) {
+#pragma unroll
+    for (int e = 0; e < 32; e++) {
+        const float t = __fsub_rn(__fadd_rn(__uint_as_float(r[e]), cgrid), cgrid);
+        const float key = __fmaf_rn(ulp, (float)(127 - ((CH * 32 + e) & 127)), t);
+        if (e & 1)
+            ins4(c1, key);
+        else
+            ins4(c0, key);
+    }
+}
+
+// Top-4 keys of the 128 columns of one accumulator half, and a bound of the
+// rest (two chains; a chain's elements outside its top-4 are <= its 4th).
+__device__ __forceinline__ void rank_half4(uint32_t col_addr, float cgrid, float ulp, uint32_t (&K)[4], uint32_t &ku) {
+    float c0[4] = {0.f, 0.f, 0.f, 0.f}, c1[4] = {0.f, 0.f, 0.f, 0.f};
+    uint32_t ra[32], rb[32];
+    tmem_ld32(col_addr, ra);
+    tmem_wait(ra);
+    tmem_ld32(col_addr + 32, rb);
+    rank_chunk4<0>(ra, cgrid, ulp, c0, c1);
+    tmem_wait(rb);
+    tmem_ld32(col_addr + 64, ra);
+    rank_chunk4<1>(rb, cgrid, ulp, c0, c1);
+    tmem_wait(ra);
+    tmem_ld32(col_addr + 96, rb);
+    rank_chunk4<2>(ra, cgrid, ulp, c0, c1);
+    tmem_wait(rb);
+    rank_chunk4<3>(rb, cgrid, ulp, c0, c1);
+    int dummy[4] = {0, 0, 0, 0};
+#pragma unroll
+    for (int p = 0; p < 4; p++) K[p] = __float_as_uint(c0[p]);
+    ku = max(__float_as_uint(c0[3]), __float_as_uint(c1[3]));
+#pragma unroll
+    for (int p = 0; p < 4; p++) ku = max(ku, ins4i(K, dummy, __float_as_uint(c1[p]), 0));
+}
+
+template <int TOPK>
 __global__ void __launch_bounds__(NTHREADS, 1)
     tc_assign_kernel(const __grid_constant__ CUtensorMap tm_x, const __grid_constant__ CUtensorMap tm_c,
                      const __grid_constant__ CUtensorMap tm_aug, const __grid_constant__ CUtensorMap tm_ones,
-                     const TcParams p) {
+                     TcParams p) {
+    if (p.n_dev) {
+        const unsigned long long cnt = *p.n_dev;
+        p.n = (int64_t)(cnt < (unsigned long long)p.n ? cnt : (unsigned long long)p.n);
+        p.tiles = (p.n + BM - 1) / BM;
+    }
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     const uint32_t sb = smem_u32(smem);
@@ -389,13 +485,14 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             // Drain: the last commit covers every MMA issued before it.
             if (last_s >= 0) mbar_wait(bar_xempty(last_s), last_ph, abort_flag, p.err, 0ull);
         }
-    } else {
+    } else if (TOPK == 2) {
         const int ew = warp - 2;
         const int quarter = warp & 3;
         const int half = ew >> 2;
         const int row_local = quarter * 32 + lane;
         const uint32_t lane_addr = tmem + ((uint32_t)(quarter * 32) << 16);
         Top2 *merge = (Top2 *)(smem + p.off_merge);
+        const float cgrid = p.stats->cgrid, ulp = p.stats->ulp;
         uint32_t item = 0;
         bool dead = false;
         for (int64_t t = q; t < p.tiles; t += tstride) {
@@ -412,6 +509,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                     for (int ch = 0; ch < 4; ch++) {
                         uint32_t r[32];
                         tmem_ld32(col + ch * 32, r);
+                        tmem_wait(r);
                         for (int e = 0; e < 32; e++)
                             p.dump[(int64_t)row_local * (p.nblocks * BN) + b * BN + half * 128 + ch * 32 + e] =
                                 __uint_as_float(r[e]);
@@ -419,15 +517,15 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                 }
                 uint32_t b1, b2, bu;
                 if (half == 0)
-                    rank_half<0>(col, b1, b2, bu);
+                    rank_half<0>(col, cgrid, ulp, b1, b2, bu);
                 else
-                    rank_half<1>(col, b1, b2, bu);
+                    rank_half<1>(col, cgrid, ulp, b1, b2, bu);
                 tc_fence_before();
                 __syncwarp();
                 if (lane == 0) mbar_arrive(bar_aempty(buf));
-                const int base = part * p.kp + b * BN + 255;
-                merge_res(R1, I1, R2, I2, U, b1 & 0xFFFFFF00u, base - (int)(b1 & 0xFFu), b2 & 0xFFFFFF00u,
-                          base - (int)(b2 & 0xFFu), bu & 0xFFFFFF00u);
+                const int base = part * p.kp + b * BN + half * 128 + 127;
+                merge_res(R1, I1, R2, I2, U, b1 & 0xFFFFFF80u, base - (int)(b1 & 0x7Fu), b2 & 0xFFFFFF80u,
+                          base - (int)(b2 & 0x7Fu), bu & 0xFFFFFF80u);
             }
             if (half == 1)
                 merge[row_local] = Top2{__uint_as_float(R1), __uint_as_float(R2), __uint_as_float(U), 0.f, I1, I2, 0, 0};
@@ -438,8 +536,69 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                           __float_as_uint(o.u3));
                 const int64_t row = t * BM + row_local;
                 if (row < p.n && !dead)
-                    p.out[(int64_t)part * p.n + row] =
+                    p.out[(int64_t)part * p.out_stride + row] =
                         Top2{__uint_as_float(R1), __uint_as_float(R2), __uint_as_float(U), 0.f, I1, I2, 0, 0};
+            }
+            epi_bar();
+        }
+    } else {
+        const int ew = warp - 2;
+        const int quarter = warp & 3;
+        const int half = ew >> 2;
+        const int row_local = quarter * 32 + lane;
+        const uint32_t lane_addr = tmem + ((uint32_t)(quarter * 32) << 16);
+        Top4 *merge = (Top4 *)(smem + p.off_merge);
+        const float cgrid = p.stats->cgrid, ulp = p.stats->ulp;
+        uint32_t item = 0;
+        bool dead = false;
+        for (int64_t t = q; t < p.tiles; t += tstride) {
+            uint32_t R[4] = {0u, 0u, 0u, 0u}, U = 0u;
+            int I[4] = {-1, -1, -1, -1};
+            for (int b = 0; b < p.nblocks; b++, item++) {
+                const int buf = (int)(item & 1u);
+                const uint32_t aph = (item >> 1) & 1u;
+                if (!dead && !mbar_wait(bar_afull(buf), aph, abort_flag, p.err, 16ull)) dead = true;
+                if (dead) continue;
+                tc_fence_after();
+                const uint32_t col = lane_addr + (uint32_t)buf * BN + (uint32_t)half * 128u;
+                uint32_t K[4], ku;
+                rank_half4(col, cgrid, ulp, K, ku);
+                tc_fence_before();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(bar_aempty(buf));
+                const int base = part * p.kp + b * BN + half * 128 + 127;
+                U = max(U, ku & 0xFFFFFF80u);
+#pragma unroll
+                for (int j = 0; j < 4; j++)
+                    U = max(U, ins4i(R, I, K[j] & 0xFFFFFF80u, base - (int)(K[j] & 0x7Fu)));
+            }
+            if (half == 1) {
+                Top4 rec;
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    rec.v[j] = __uint_as_float(R[j]);
+                    rec.i[j] = I[j];
+                }
+                rec.u5 = __uint_as_float(U);
+                merge[row_local] = rec;
+            }
+            epi_bar();
+            if (half == 0) {
+                const Top4 o = merge[row_local];
+                U = max(U, __float_as_uint(o.u5));
+#pragma unroll
+                for (int j = 0; j < 4; j++) U = max(U, ins4i(R, I, __float_as_uint(o.v[j]), o.i[j]));
+                const int64_t row = t * BM + row_local;
+                if (row < p.n && !dead) {
+                    Top4 rec;
+#pragma unroll
+                    for (int j = 0; j < 4; j++) {
+                        rec.v[j] = __uint_as_float(R[j]);
+                        rec.i[j] = I[j];
+                    }
+                    rec.u5 = __uint_as_float(U);
+                    p.out4[(int64_t)part * p.out_stride + row] = rec;
+                }
             }
             epi_bar();
         }
@@ -515,7 +674,7 @@ void plan_tc(Ctx &ctx, MixedPlan &mp, int64_t n, int d, int k) {
     if ((int64_t)mp.ctas_per_part > mp.tiles) mp.ctas_per_part = (int)mp.tiles;
     mp.grid = mp.ctas_per_part * mp.parts;
     mp.smem = fixed + (size_t)mp.kp * per_centre;
-    mp.tm_x_ptr = mp.tm_c_ptr = mp.tm_aug_ptr = nullptr;
+    mp.tm_x_ptr = mp.tm_c_ptr = mp.tm_aug_ptr = mp.tm_x2_ptr = nullptr;
     if (!mp.ones) {
         uint16_t h[BM * 16];
         for (int r = 0; r < BM; r++)
@@ -527,11 +686,15 @@ void plan_tc(Ctx &ctx, MixedPlan &mp, int64_t n, int d, int k) {
 }
 
 void launch_tc_assign(Ctx &ctx, MixedPlan &mp, const void *xb, const void *cb, const void *caug, Top2 *out,
-                      DevScalars *sc, float *dump) {
-    if (mp.tm_x_ptr != xb) {
-        encode_2d(ctx, mp.tm_x, xb, (uint64_t)mp.d_pad, (uint64_t)mp.n, (uint64_t)mp.d_pad * 2, 64, BM,
+                      DevScalars *sc, const MixedStats *stats, float *dump, Top4 *out4,
+                      const unsigned long long *n_dev) {
+    // the second pass reads its own gathered rows: a separate tensor map
+    unsigned char *tmx = out4 ? mp.tm_x2 : mp.tm_x;
+    const void *&tmx_ptr = out4 ? mp.tm_x2_ptr : mp.tm_x_ptr;
+    if (tmx_ptr != xb) {
+        encode_2d(ctx, tmx, xb, (uint64_t)mp.d_pad, (uint64_t)mp.n, (uint64_t)mp.d_pad * 2, 64, BM,
                   CU_TENSOR_MAP_SWIZZLE_128B);
-        mp.tm_x_ptr = xb;
+        tmx_ptr = xb;
     }
     if (mp.tm_c_ptr != cb) {
         encode_2d(ctx, mp.tm_c, cb, (uint64_t)mp.d_pad, (uint64_t)mp.k_pad, (uint64_t)mp.d_pad * 2, 64, BN,
@@ -561,18 +724,28 @@ void launch_tc_assign(Ctx &ctx, MixedPlan &mp, const void *xb, const void *cb, c
     p.off_bar = p.off_merge + MERGE_BYTES;
     p.c_tx_bytes = (uint32_t)p.n_atoms * p.c_atom_bytes + (uint32_t)mp.kp * 32u + ONES_BYTES;
     p.out = out;
+    p.out4 = out4;
+    p.n_dev = n_dev;
+    p.out_stride = mp.n;
     p.err = &sc->error_word;
+    p.stats = stats;
     p.dump = dump;
     const size_t smem = (size_t)p.off_bar + BAR_BYTES + 1024;
     if (smem > SMEM_LIMIT) {
         set_error("tensor-core plan needs %zu bytes of shared memory", smem);
         fail(FK_ERR_UNSUPPORTED);
     }
-    FK_CUDA(cudaFuncSetAttribute((const void *)tc_assign_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)smem));
-    const CUtensorMap *tx = (const CUtensorMap *)mp.tm_x, *tcm = (const CUtensorMap *)mp.tm_c,
+    const CUtensorMap *tx = (const CUtensorMap *)tmx, *tcm = (const CUtensorMap *)mp.tm_c,
                       *ta = (const CUtensorMap *)mp.tm_aug, *to = (const CUtensorMap *)mp.tm_ones;
-    tc_assign_kernel<<<mp.grid, NTHREADS, smem, ctx.stream>>>(*tx, *tcm, *ta, *to, p);
+    if (out4) {
+        FK_CUDA(cudaFuncSetAttribute((const void *)tc_assign_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)smem));
+        tc_assign_kernel<4><<<mp.grid, NTHREADS, smem, ctx.stream>>>(*tx, *tcm, *ta, *to, p);
+    } else {
+        FK_CUDA(cudaFuncSetAttribute((const void *)tc_assign_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)smem));
+        tc_assign_kernel<2><<<mp.grid, NTHREADS, smem, ctx.stream>>>(*tx, *tcm, *ta, *to, p);
+    }
     FK_LAUNCH_CHECK();
 }
 

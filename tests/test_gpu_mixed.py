@@ -194,3 +194,42 @@ def test_mixed_predict_matches_oracle():
     fitted = F.FittedKMeans(cen.astype(np.float64), np.zeros(6000, dtype=np.int64), 0.0, 0, "f32x64",
                             precision=F.MIXED_BF16)
     assert np.array_equal(fitted.predict(x32), O.predict(cen, x32.astype(np.float64)))
+
+
+def _equidistant_rows(c, ids, count, rng, spread=0.5):
+    """Rows at equal (real) distance from the centres ids: the circumcentre of
+    their affine hull plus offsets orthogonal to it."""
+    base = c[ids[0]]
+    dirs = np.stack([c[i] - base for i in ids[1:]])  # (m-1, d)
+    gram = dirs @ dirs.T
+    rhs = 0.5 * np.array([dv @ dv for dv in dirs])
+    coef = np.linalg.solve(gram, rhs)
+    centre = base + coef @ dirs
+    q, _ = np.linalg.qr(dirs.T)
+    rows = []
+    for _ in range(count):
+        u = rng.normal(size=c.shape[1])
+        u -= q @ (q.T @ u)
+        rows.append(centre + spread * u)
+    return np.array(rows)
+
+
+def test_mixed_multiway_ties_use_the_second_pass():
+    # rows equidistant from three and from six centres: the first pass cannot
+    # separate them, the top-4 second pass (or the exhaustive path for six)
+    # must, and the labels must still be the FP64 oracle's
+    rng = np.random.default_rng(8)
+    d, k = 64, 300
+    c = rng.uniform(-10, 10, size=(k, d))
+    c[[1, 2, 3, 4, 6, 7]] = c[1] + rng.normal(0, 0.5, size=(6, d))  # six close centres
+    x = c[rng.integers(0, k, 6000)] + rng.normal(0, 1, size=(6000, d))
+    x[:300] = _equidistant_rows(c, [5, 40, 77], 300, rng)
+    x[300:360] = _equidistant_rows(c, [1, 2, 3, 4, 6, 7], 60, rng)
+    x32 = x.astype(np.float32)
+    x64 = x32.astype(np.float64)
+    gl, gc, gi, gs, rep = F.lloyd_step(x32, c, dtype="f32x64", precision="bf16")
+    ol, oc, oi, os_ = O.lloyd_step(x64, c)
+    assert np.array_equal(gl, ol)
+    assert _close(gc, oc)
+    assert rep["rows_full_rescan"] >= 300
+    assert rep["rows_fp64"] >= 100
