@@ -271,7 +271,9 @@ def run_ours(args):
         "phase_ms_per_iter": {"assign": assign_ms, "contract": contract_ms if form == "bf16" else None,
                               "update": rep["ms_update"] / iters},
         "recheck": {"rows": rep["rows_rechecked"], "full_rescan": rep["rows_full_rescan"],
-                    "fp64_rows": rep["rows_fp64"], "near_ties": rep["near_tie_rows"],
+                    "fp64_rows": rep["rows_fp64"], "second_pass": rep["rows_second_pass"],
+                    "four_candidates": rep["rows_four"], "exhaustive": rep["rows_exhaustive"],
+                    "near_ties": rep["near_tie_rows"],
                     "fraction": rep["rows_rechecked"] / max(1, rep["rows_assigned"])},
         "gpu_launches": launches,
         "clocks": clocks.summary(),

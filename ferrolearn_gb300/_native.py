@@ -51,6 +51,9 @@ class FitReport(C.Structure):
         ("rows_rechecked", C.c_int64),
         ("rows_full_rescan", C.c_int64),
         ("rows_fp64", C.c_int64),
+        ("rows_second_pass", C.c_int64),
+        ("rows_four", C.c_int64),
+        ("rows_exhaustive", C.c_int64),
         ("near_tie_rows", C.c_int64),
         ("ms_init", C.c_double),
         ("ms_assign", C.c_double),

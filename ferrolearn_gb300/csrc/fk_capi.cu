@@ -202,6 +202,9 @@ void accumulate_report(fk_fit_report *rep, const DevScalars &h, int64_t n) {
     rep->rows_rechecked += (int64_t)(h.flag_count + h.full_count);
     rep->rows_full_rescan += (int64_t)h.full_count;
     rep->rows_fp64 += (int64_t)h.recheck_rows;
+    rep->rows_second_pass += (int64_t)h.full_count;
+    rep->rows_four += (int64_t)h.quad_count;
+    rep->rows_exhaustive += (int64_t)h.ex_count;
     rep->near_tie_rows += (int64_t)h.near_tie_rows;
 }
 

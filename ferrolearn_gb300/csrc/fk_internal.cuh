@@ -58,7 +58,6 @@ struct DevScalars {
     unsigned long long near_tie_rows;
     unsigned long long flag_count;  // number of rows queued for re-check
     unsigned long long full_count;  // number of rows queued for a full re-scan
-    unsigned long long over_count;  // full re-scan rows with more than 4 FP32 candidates
     unsigned long long quad_count;  // second pass: rows with at most 4 candidates
     unsigned long long ex_count;    // second pass: rows with more than 4 candidates
     unsigned long long error_word;  // nonzero: a bounded device wait gave up
@@ -123,7 +122,7 @@ enum BufSlot {
     BUF_X = 0, BUF_XC, BUF_C0, BUF_C1, BUF_CBEST, BUF_LABELS, BUF_LBEST, BUF_MIND,
     BUF_MEMBERS, BUF_SEGHIST, BUF_SCAN_TMP, BUF_COUNTS, BUF_PARTIAL, BUF_SCALARS,
     BUF_OUT, BUF_OUT2, BUF_KPP0, BUF_KPP1, BUF_KPP2, BUF_KPP3, BUF_DRAWS,
-    BUF_XB, BUF_XNORM, BUF_CB, BUF_CAUX, BUF_TOP2, BUF_FLAGS, BUF_FULL, BUF_CF32, BUF_CF32C, BUF_OVER, BUF_FIXPART, BUF_XB2, BUF_TOP4, BUF_QUAD, BUF_EX,
+    BUF_XB, BUF_XNORM, BUF_CB, BUF_CAUX, BUF_TOP2, BUF_FLAGS, BUF_FULL, BUF_CF32, BUF_CF32C, BUF_FIXPART, BUF_XB2, BUF_TOP4, BUF_QUAD, BUF_EX,
     BUF_COUNT
 };
 

@@ -18,7 +18,10 @@
 // thr = 2E + q + delta. If v1 - v2 > thr no other centre can win in the FP64
 // direct form, so the label is final. Otherwise, if the best value outside the
 // top two is also below v1 - thr, only the top two are re-scored exactly;
-// else the row is re-scored against every centre. Every re-score is the
+// else the row goes through a second tensor-core pass that keeps the best four
+// scores, and only the centres inside the bound among those four are
+// re-scored (rows with more than four such centres, or a non-finite score,
+// are re-scored against every centre). Every re-score is the
 // direct-form sum (x_j - c_j)^2 in FP64 with no FMA and the lowest index on
 // ties, i.e. exactly kmeans.rs:159-163 / 295-309, so the labels equal the
 // FP64 oracle's in every case.
@@ -156,7 +159,7 @@ __global__ void prep_rows_kernel(const TX *__restrict__ x, int64_t n, int d, int
 __global__ void prep_centres_kernel(const double *__restrict__ c, int k, int k_pad, int d, int d_pad,
                                     const double *__restrict__ mu, __nv_bfloat16 *__restrict__ cb,
                                     double *__restrict__ half_norm, float *__restrict__ c32,
-                                    float *__restrict__ ec32, MixedStats *stats) {
+                                    float *__restrict__ ec32, float *__restrict__ c32t, MixedStats *stats) {
     const int lane = threadIdx.x & 31;
     const int q = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     if (q >= k_pad) return;
@@ -174,6 +177,7 @@ __global__ void prep_centres_kernel(const double *__restrict__ c, int k, int k_p
             co2 += cv * cv;
             float f = (float)cv;
             c32[(int64_t)q * d + j] = f;
+            c32t[(int64_t)j * k + q] = f;
             e32 += (cv - (double)f) * (cv - (double)f);
         }
         cb[(int64_t)q * d_pad + j] = h;
@@ -409,8 +413,9 @@ __global__ void pair_rescore_kernel(const TX *__restrict__ x, int d, const doubl
 template <typename TX>
 __global__ void full_rescore_kernel(const TX *__restrict__ x, int d, const double *__restrict__ c,
                                     const float *__restrict__ c32, const float *__restrict__ ec32, int k,
-                                    const int32_t *__restrict__ list, DevScalars *sc, int32_t *__restrict__ labels) {
-    const unsigned long long cnt = std::is_same<TX, float>::value ? sc->over_count : sc->full_count;
+                                    const int32_t *__restrict__ list, const unsigned long long *count_ptr,
+                                    DevScalars *sc, int32_t *__restrict__ labels) {
+    const unsigned long long cnt = *count_ptr;
     const int lane = threadIdx.x & 31;
     const unsigned long long wid = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const unsigned long long nw = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
@@ -460,181 +465,104 @@ __global__ void full_rescore_kernel(const TX *__restrict__ x, int d, const doubl
     }
 }
 
-// Tiled FP32 pass over the rows queued for a full re-score: 64 rows x 64
-// centres per block tile (4 x 4 per thread, centres staged in shared memory
-// like the direct-form kernel), keeping the four smallest FP32 distances of
-// every row. With UB = min(d32 + E32) over those four, a centre can only be
-// the FP64 minimum if d32 - E32 <= UB; if the fourth-smallest could still
-// qualify (or the row has no finite FP32 distance) the row goes to the
-// exhaustive per-row kernel. A single candidate is the answer; several are
-// scored exactly in FP64 (direct form, lowest index on ties).
-constexpr int FT_BM = 64, FT_BN = 64, FT_DJ = 16, FT_T = 256;
-
-__device__ __forceinline__ void top4_insert(float (&v)[4], int (&ix)[4], float val, int id) {
-    if (!(val < v[3])) return;  // also rejects NaN
-    if (val < v[2]) {
-        v[3] = v[2]; ix[3] = ix[2];
-        if (val < v[1]) {
-            v[2] = v[1]; ix[2] = ix[1];
-            if (val < v[0]) {
-                v[1] = v[0]; ix[1] = ix[0];
-                v[0] = val; ix[0] = id;
-            } else { v[1] = val; ix[1] = id; }
-        } else { v[2] = val; ix[2] = id; }
-    } else { v[3] = val; ix[3] = id; }
-}
-
-__global__ void __launch_bounds__(FT_T)
-full_tiled_kernel(const float *__restrict__ x, int d, const float *__restrict__ c32, const float *__restrict__ ec32,
-                  const double *__restrict__ c64, int k, const int32_t *__restrict__ list,
-                  const unsigned long long *count_ptr, DevScalars *sc, int32_t *__restrict__ labels,
-                  int32_t *__restrict__ over_list) {
-    __shared__ __align__(16) float xs[FT_DJ][FT_BM];
-    __shared__ __align__(16) float cs[FT_DJ][FT_BN];
-    __shared__ int rid[FT_BM];
-    __shared__ float tv[FT_BM][4];
-    __shared__ int ti[FT_BM][4];
-    __shared__ double dv[FT_BM][4];
-    __shared__ float ecmax_s;
-    const unsigned long long count = *count_ptr;
-    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
-    if (tid == 0) {
-        float m = 0.f;
-        for (int q = 0; q < k; q++) m = fmaxf(m, ec32[q]);
-        ecmax_s = m;
-    }
-    for (unsigned long long tile = blockIdx.x; tile * FT_BM < count; tile += gridDim.x) {
-        __syncthreads();
-        if (tid < FT_BM) {
-            unsigned long long s = tile * FT_BM + tid;
-            rid[tid] = s < count ? list[s] : -1;
-        }
-        __syncthreads();
-        float bv[4][4];
-        int bi[4][4];
+// One warp per listed row, f32 rows: FP32 distances to every centre, lanes
+// over centres reading the transposed f32 centres (coalesced), 32 distances
+// per lane in registers per batch of 1024 centres; the smallest upper bound
+// UB over all centres, then FP64 (direct form, one lane per centre) for every
+// centre whose lower bound reaches UB or whose FP32 value is not finite.
+__global__ void exhaustive_rescore_kernel(const float *__restrict__ x, int d, const double *__restrict__ c,
+                                          const float *__restrict__ c32t, const float *__restrict__ ec32, int k,
+                                          const int32_t *__restrict__ list, const unsigned long long *count_ptr,
+                                          DevScalars *sc, int32_t *__restrict__ labels) {
+    const unsigned long long cnt = *count_ptr;
+    const int lane = threadIdx.x & 31;
+    const unsigned long long wid = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const unsigned long long nw = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
+    for (unsigned long long s = wid; s < cnt; s += nw) {
+        const int64_t r = list[s];
+        const float *row = x + r * d;
+        // pass 1: smallest upper bound over all centres
+        float ub = INFINITY;
+        float acc[32];
+        for (int c0 = 0; c0 < k; c0 += 1024) {
 #pragma unroll
-        for (int a = 0; a < 4; a++)
+            for (int u = 0; u < 32; u++) acc[u] = 0.f;
+            for (int j = 0; j < d; j++) {
+                const float xv = row[j];
+                const float *ct = c32t + (int64_t)j * k;
 #pragma unroll
-            for (int e = 0; e < 4; e++) { bv[a][e] = INFINITY; bi[a][e] = -1; }
-        for (int ct = 0; ct < k; ct += FT_BN) {
-            float acc[4][4];
-#pragma unroll
-            for (int a = 0; a < 4; a++)
-#pragma unroll
-                for (int b = 0; b < 4; b++) acc[a][b] = 0.f;
-            for (int j0 = 0; j0 < d; j0 += FT_DJ) {
-#pragma unroll
-                for (int e = 0; e < (FT_BM * FT_DJ) / FT_T; e++) {
-                    int idx = tid + e * FT_T;
-                    int r = idx / FT_DJ, jj = idx % FT_DJ;
-                    int gj = j0 + jj;
-                    int rr = rid[r];
-                    xs[jj][r] = (rr >= 0 && gj < d) ? x[(int64_t)rr * d + gj] : 0.f;
-                    int gc = ct + r;
-                    cs[jj][r] = (gc < k && gj < d) ? c32[(int64_t)gc * d + gj] : 0.f;
+                for (int u = 0; u < 32; u++) {
+                    const int q = c0 + u * 32 + lane;
+                    if (q < k) {
+                        const float t = xv - ct[q];
+                        acc[u] = fmaf(t, t, acc[u]);
+                    }
                 }
-                __syncthreads();
-                const int jn = min(FT_DJ, d - j0);
-                for (int jj = 0; jj < jn; jj++) {
-                    float xv[4], cv[4];
+            }
 #pragma unroll
-                    for (int a = 0; a < 4; a++) xv[a] = xs[jj][ty * 4 + a];
+            for (int u = 0; u < 32; u++) {
+                const int q = c0 + u * 32 + lane;
+                if (q < k) {
+                    const float hi = __fadd_ru(acc[u], bound32(acc[u], ec32[q], d));
+                    if (hi < ub) ub = hi;  // NaN never lowers the bound
+                }
+            }
+        }
 #pragma unroll
-                    for (int b = 0; b < 4; b++) cv[b] = cs[jj][tx * 4 + b];
+        for (int off = 16; off >= 1; off >>= 1) ub = fminf(ub, __shfl_xor_sync(0xffffffffu, ub, off));
+        // pass 2: FP64 on the survivors (the distances of the first batch are
+        // still in registers when k <= 1024; larger k recomputes them)
+        double b1 = DBL_MAX, b2 = DBL_MAX;
+        int i1 = INT32_MAX;
+        for (int c0 = 0; c0 < k; c0 += 1024) {
+            if (c0 > 0 || k > 1024) {
 #pragma unroll
-                    for (int a = 0; a < 4; a++)
+                for (int u = 0; u < 32; u++) acc[u] = 0.f;
+                for (int j = 0; j < d; j++) {
+                    const float xv = row[j];
+                    const float *ct = c32t + (int64_t)j * k;
 #pragma unroll
-                        for (int b = 0; b < 4; b++) {
-                            float t = xv[a] - cv[b];
-                            acc[a][b] = fmaf(t, t, acc[a][b]);
+                    for (int u = 0; u < 32; u++) {
+                        const int q = c0 + u * 32 + lane;
+                        if (q < k) {
+                            const float t = xv - ct[q];
+                            acc[u] = fmaf(t, t, acc[u]);
                         }
+                    }
                 }
-                __syncthreads();
             }
+            uint32_t cand = 0;
 #pragma unroll
-            for (int a = 0; a < 4; a++)
-#pragma unroll
-                for (int b = 0; b < 4; b++) {
-                    int gc = ct + tx * 4 + b;
-                    if (gc < k) top4_insert(bv[a], bi[a], acc[a][b], gc);
-                }
-        }
-        // merge the 16 partial lists of each row (same half-warp)
-#pragma unroll
-        for (int a = 0; a < 4; a++) {
-#pragma unroll
-            for (int off = 8; off >= 1; off >>= 1) {
-                float ov[4];
-                int oi[4];
-#pragma unroll
-                for (int e = 0; e < 4; e++) {
-                    ov[e] = __shfl_xor_sync(0xffffffffu, bv[a][e], off);
-                    oi[e] = __shfl_xor_sync(0xffffffffu, bi[a][e], off);
-                }
-#pragma unroll
-                for (int e = 0; e < 4; e++)
-                    if (oi[e] >= 0) top4_insert(bv[a], bi[a], ov[e], oi[e]);
+            for (int u = 0; u < 32; u++) {
+                const int q = c0 + u * 32 + lane;
+                if (q < k && !(__fsub_rd(acc[u], bound32(acc[u], ec32[q], d)) > ub)) cand |= 1u << u;
             }
-            if (tx == 0) {
-#pragma unroll
-                for (int e = 0; e < 4; e++) {
-                    tv[ty * 4 + a][e] = bv[a][e];
-                    ti[ty * 4 + a][e] = bi[a][e];
-                }
+            while (cand) {  // increasing centre index within this lane
+                const int u = __ffs(cand) - 1;
+                cand &= cand - 1;
+                const int q = c0 + u * 32 + lane;
+                const double v = sqeuc64(row, c + (int64_t)q * d, d);
+                if (v < b1) { b2 = b1; b1 = v; i1 = q; }
+                else if (v < b2) { b2 = v; }
             }
         }
-        __syncthreads();
-        // one thread per (row, entry): candidate test and FP64 score
-        {
-            const int r = tid >> 2, e = tid & 3;
-            double out = INFINITY;  // not a candidate
-            const int rr = rid[r];
-            if (rr >= 0 && ti[r][e] >= 0) {
-                float ub = INFINITY;
 #pragma unroll
-                for (int q = 0; q < 4; q++)
-                    if (ti[r][q] >= 0) ub = fminf(ub, __fadd_ru(tv[r][q], bound32(tv[r][q], ec32[ti[r][q]], d)));
-                const float v = tv[r][e];
-                if (!(__fsub_rd(v, bound32(v, ec32[ti[r][e]], d)) > ub)) {
-                    int ncand = 0;
-#pragma unroll
-                    for (int q = 0; q < 4; q++)
-                        if (ti[r][q] >= 0 && !(__fsub_rd(tv[r][q], bound32(tv[r][q], ec32[ti[r][q]], d)) > ub)) ncand++;
-                    out = ncand > 1 ? sqeuc64(x + (int64_t)rr * d, c64 + (int64_t)ti[r][e] * d, d) : -1.0;
-                }
-            }
-            dv[r][e] = out;
-        }
-        __syncthreads();
-        if (tid < FT_BM && rid[tid] >= 0) {
-            const int r = tid, rr = rid[r];
-            bool overflow = ti[r][0] < 0;  // no finite FP32 distance at all
-            if (!overflow && k > 4 && ti[r][3] >= 0) {
-                float ub = INFINITY;
-                for (int q = 0; q < 4; q++) ub = fminf(ub, __fadd_ru(tv[r][q], bound32(tv[r][q], ec32[ti[r][q]], d)));
-                if (!(__fsub_rd(tv[r][3], bound32(tv[r][3], ecmax_s, d)) > ub)) overflow = true;
-            }
-            if (overflow) {
-                unsigned long long slot = atomicAdd(&sc->over_count, 1ULL);
-                over_list[slot] = rr;
+        for (int off = 16; off >= 1; off >>= 1) {
+            double o1 = __shfl_xor_sync(0xffffffffu, b1, off);
+            double o2 = __shfl_xor_sync(0xffffffffu, b2, off);
+            int oi = __shfl_xor_sync(0xffffffffu, i1, off);
+            if (o1 < b1 || (o1 == b1 && oi < i1)) {
+                b2 = fmin(b1, o2);
+                b1 = o1;
+                i1 = oi;
             } else {
-                int best = -1, nfp = 0;
-                double b1 = DBL_MAX, b2 = DBL_MAX;
-                for (int q = 0; q < 4; q++) {
-                    const double v = dv[r][q];
-                    if (v == -1.0) { best = ti[r][q]; nfp = 0; break; }  // single candidate
-                    if (v == INFINITY) continue;
-                    nfp++;
-                    const int ci = ti[r][q];
-                    if (v < b1 || (v == b1 && ci < best)) { b2 = b1; b1 = v; best = ci; }
-                    else if (v < b2) b2 = v;
-                }
-                labels[rr] = best < 0 ? 0 : best;
-                if (nfp > 0) {
-                    atomicAdd(&sc->recheck_rows, 1ULL);
-                    if (nfp > 1 && b2 < DBL_MAX && near_tie(b1, b2)) atomicAdd(&sc->near_tie_rows, 1ULL);
-                }
+                b2 = fmin(b2, o1);
             }
+        }
+        if (lane == 0) {
+            labels[r] = i1 == INT32_MAX ? 0 : i1;
+            atomicAdd(&sc->recheck_rows, 1ULL);
+            if (i1 != INT32_MAX && b2 < DBL_MAX && near_tie(b1, b2)) atomicAdd(&sc->near_tie_rows, 1ULL);
         }
     }
 }
@@ -871,10 +799,11 @@ void run_assign_mixed(Ctx &ctx, const TX *x, int64_t n, int d, const double *c, 
     __nv_bfloat16 *cb = (__nv_bfloat16 *)ctx.get(BUF_CB, sizeof(__nv_bfloat16) * (size_t)mp.k_pad * mp.d_pad);
     __nv_bfloat16 *caug = (__nv_bfloat16 *)ctx.get(BUF_CAUX, sizeof(__nv_bfloat16) * (size_t)mp.k_pad * 16 + 8192);
     double *half_norm = (double *)ctx.get(BUF_MIND, sizeof(double) * (size_t)mp.k_pad);
-    float *c32 = (float *)ctx.get(BUF_CF32C, sizeof(float) * ((size_t)k * d + (size_t)k) + 64);
+    float *c32 = (float *)ctx.get(BUF_CF32C, sizeof(float) * (2 * (size_t)k * d + (size_t)k) + 64);
     float *ec32 = c32 + (size_t)k * d;
+    float *c32t = ec32 + k;
     prep_centres_kernel<<<(mp.k_pad + 7) / 8, 256, 0, s>>>(c, k, mp.k_pad, d, mp.d_pad, mu, cb, half_norm, c32, ec32,
-                                                           stats);
+                                                           c32t, stats);
     FK_LAUNCH_CHECK();
     prep_aug_kernel<<<(mp.k_pad + 255) / 256, 256, 0, s>>>(half_norm, k, mp.k_pad, caug, stats);
     FK_LAUNCH_CHECK();
@@ -900,7 +829,6 @@ void run_assign_mixed(Ctx &ctx, const TX *x, int64_t n, int d, const double *c, 
         Top4 *top4 = (Top4 *)ctx.get(BUF_TOP4, sizeof(Top4) * (size_t)n * mp.parts);
         Quad *quads = (Quad *)ctx.get(BUF_QUAD, sizeof(Quad) * (size_t)n);
         int32_t *ex = (int32_t *)ctx.get(BUF_EX, sizeof(int32_t) * (size_t)n);
-        int32_t *over = (int32_t *)ctx.get(BUF_OVER, sizeof(int32_t) * (size_t)n);
         gather_rows_kernel<<<grid, 256, 0, s>>>((const uint4 *)xb, mp.d_pad * 2 / 16, full, &sc->full_count,
                                                 (uint4 *)xb2);
         FK_LAUNCH_CHECK();
@@ -910,11 +838,9 @@ void run_assign_mixed(Ctx &ctx, const TX *x, int64_t n, int d, const double *c, 
         FK_LAUNCH_CHECK();
         quad_rescore_kernel<<<grid, 256, 0, s>>>(x, d, c, c32, ec32, quads, sc, labels);
         FK_LAUNCH_CHECK();
-        full_tiled_kernel<<<ctx.num_sms * 2, FT_T, 0, s>>>(x, d, c32, ec32, c, k, ex, &sc->ex_count, sc, labels, over);
-        FK_LAUNCH_CHECK();
-        full_rescore_kernel<TX><<<grid, 256, 0, s>>>(x, d, c, c32, ec32, k, over, sc, labels);
+        exhaustive_rescore_kernel<<<grid, 256, 0, s>>>(x, d, c, c32t, ec32, k, ex, &sc->ex_count, sc, labels);
     } else {
-        full_rescore_kernel<TX><<<grid, 256, 0, s>>>(x, d, c, c32, ec32, k, full, sc, labels);
+        full_rescore_kernel<TX><<<grid, 256, 0, s>>>(x, d, c, c32, ec32, k, full, &sc->full_count, sc, labels);
     }
     FK_LAUNCH_CHECK();
 }
@@ -956,9 +882,9 @@ void debug_tc_probe(Ctx &ctx, const float *x, int64_t n, int d, const double *c,
     __nv_bfloat16 *cb = (__nv_bfloat16 *)ctx.get(BUF_CB, sizeof(__nv_bfloat16) * (size_t)mp.k_pad * mp.d_pad);
     __nv_bfloat16 *caug = (__nv_bfloat16 *)ctx.get(BUF_CAUX, sizeof(__nv_bfloat16) * (size_t)mp.k_pad * 16 + 8192);
     double *half_norm = (double *)ctx.get(BUF_MIND, sizeof(double) * (size_t)mp.k_pad);
-    float *c32 = (float *)ctx.get(BUF_CF32C, sizeof(float) * ((size_t)k * d + (size_t)k) + 64);
+    float *c32 = (float *)ctx.get(BUF_CF32C, sizeof(float) * (2 * (size_t)k * d + (size_t)k) + 64);
     prep_centres_kernel<<<(mp.k_pad + 7) / 8, 256, 0, s>>>(c, k, mp.k_pad, d, mp.d_pad, mu, cb, half_norm, c32,
-                                                           c32 + (size_t)k * d, stats);
+                                                           c32 + (size_t)k * d, c32 + (size_t)k * d + k, stats);
     FK_LAUNCH_CHECK();
     prep_aug_kernel<<<(mp.k_pad + 255) / 256, 256, 0, s>>>(half_norm, k, mp.k_pad, caug, stats);
     FK_LAUNCH_CHECK();

@@ -81,6 +81,12 @@ typedef struct fk_fit_report {
     int64_t rows_full_rescan;  /* mixed: of those, rows re-scored against
                                   every centre                             */
     int64_t rows_fp64;         /* mixed: rows that needed FP64 scores      */
+    int64_t rows_second_pass;  /* mixed: rows scored again by the top-4
+                                  tensor pass (= rows_full_rescan)         */
+    int64_t rows_four;         /* mixed: of those, rows resolved among at
+                                  most four candidates                     */
+    int64_t rows_exhaustive;   /* mixed: rows re-scored against every
+                                  centre after the second pass             */
     int64_t near_tie_rows;     /* mixed: re-scored rows whose FP64 margin
                                   is below 1e-12 relative                  */
     double ms_init;            /* device time, k-means++                   */
