@@ -102,7 +102,7 @@ def _declare(lib):
         f = getattr(lib, f"fk_kmeans_plus_plus_{suf}")
         f.argtypes = [p, p, i64, i64, i64, p, i64, u64, p, p]
         f.restype = st
-    lib.fk_debug_tc_probe.argtypes = [p, p, i64, i64, p, i64, p, p, p, p, p, p]
+    lib.fk_debug_tc_probe.argtypes = [p, p, i64, i64, p, i64, i32, p, p, p, p, p, p, p]
     lib.fk_debug_tc_probe.restype = st
     lib.fk_debug_measure_peaks.argtypes = [p, p]
     lib.fk_debug_measure_peaks.restype = st

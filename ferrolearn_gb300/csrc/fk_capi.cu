@@ -137,9 +137,15 @@ int kpp_trials_host(int64_t k) {
     return t < 1 ? 1 : (int)t;
 }
 
-bool precision_ok(int prec, bool f64_semantics) {
+// Plain: every entry point. BF16: f64 semantics (f64 or f32x64). FP8: X
+// stored as f32 with f64 semantics (f32x64) only.
+template <typename TX, typename TC>
+bool precision_ok(int prec) {
+    constexpr bool f64_semantics = std::is_same<TC, double>::value;
+    constexpr bool x_f32 = std::is_same<TX, float>::value;
     if (prec == FK_PRECISION_PLAIN) return true;
-    if (prec == FK_PRECISION_MIXED_BF16 || prec == FK_PRECISION_MIXED_FP32) return f64_semantics;
+    if (prec == FK_PRECISION_MIXED_BF16) return f64_semantics;
+    if (prec == FK_PRECISION_MIXED_FP8) return f64_semantics && x_f32;
     return false;
 }
 
@@ -242,8 +248,7 @@ fk_status fit_impl(fk_ctx *ctxp, const TX *x_in, int64_t n, int64_t d, const fk_
         set_error("required pointer is NULL");
         return FK_ERR_NULL_POINTER;
     }
-    constexpr bool f64sem = std::is_same<TC, double>::value;
-    if (!precision_ok(p->precision, f64sem)) {
+    if (!precision_ok<TX, TC>(p->precision)) {
         set_error("precision %d is not available for this entry point", p->precision);
         return FK_ERR_UNSUPPORTED;
     }
@@ -399,7 +404,7 @@ fk_status step_impl(fk_ctx *ctxp, const TX *x_in, int64_t n, int64_t d, const TC
         set_error("required pointer is NULL");
         return FK_ERR_NULL_POINTER;
     }
-    if (!precision_ok(prec, std::is_same<TC, double>::value)) {
+    if (!precision_ok<TX, TC>(prec)) {
         set_error("precision %d is not available for this entry point", prec);
         return FK_ERR_UNSUPPORTED;
     }
@@ -454,7 +459,7 @@ fk_status predict_impl(fk_ctx *ctxp, const TC *c_in, int64_t k, int64_t d_fit, c
         set_error("required pointer is NULL");
         return FK_ERR_NULL_POINTER;
     }
-    if (!precision_ok(prec, std::is_same<TC, double>::value)) {
+    if (!precision_ok<TX, TC>(prec)) {
         set_error("precision %d is not available for this entry point", prec);
         return FK_ERR_UNSUPPORTED;
     }
@@ -709,11 +714,13 @@ fk_status fk_debug_measure_peaks(fk_ctx *ctx, double *out) {
 }
 
 fk_status fk_debug_tc_probe(fk_ctx *ctx, const float *x_dev, int64_t n, int64_t d, const double *c_dev, int64_t k,
-                             float *dump, uint16_t *xb, uint16_t *cb, uint16_t *aug, void *top, int32_t *plan) {
+                             int32_t precision, float *dump, void *xq, void *cq, uint16_t *aug, uint16_t *xaug,
+                             void *top, int32_t *plan) {
     return guarded(ctx, [&] {
         fk::Ctx &c = *reinterpret_cast<fk::Ctx *>(ctx);
         c.bind();
-        fk::debug_tc_probe(c, x_dev, n, (int)d, c_dev, (int)k, dump, xb, cb, aug, (fk::Top2 *)top, plan);
+        fk::debug_tc_probe(c, x_dev, n, (int)d, c_dev, (int)k, precision, dump, xq, cq, aug, xaug, (fk::Top2 *)top,
+                           plan);
         return FK_OK;
     });
 }

@@ -68,6 +68,7 @@ struct DevScalars {
 struct MixedStats {
     float xn_max;  // max_i ||xh_i||           (set once per X)
     float amax;    // max |x_ij| over finite entries (set once per X)
+    float tmax;    // max |x_ij - mu_j| over finite entries (set once per X)
     float cn_max;  // max_c ||c' ||            (per iteration from here on)
     float ec_max;  // max_c ||c' - ch||
     float ch_max;  // max_c ||ch||
@@ -76,6 +77,8 @@ struct MixedStats {
     float big;     // BIG of this iteration: 1.5 * 2^E, every score lies in [2^E, 2^(E+1))
     float cgrid;   // 3 * 2^(E+6): (T + cgrid) - cgrid rounds T to a multiple of 2^(E-16)
     float ulp;     // 2^(E-23), the unit in the last place of every score
+    float tscale;  // FP8: the centres' power-of-two scale t (1 for BF16)
+    float inv_t;   // 1 / tscale
     float pad;
 };
 
@@ -109,7 +112,11 @@ struct MixedPlan {
     const void *x = nullptr;
     double mu_norm = 0.0;
     const void *tm_x_ptr = nullptr, *tm_c_ptr = nullptr, *tm_aug_ptr = nullptr, *tm_x2_ptr = nullptr;
+    const void *tm_xaug_ptr = nullptr, *tm_xaug2_ptr = nullptr;
+    bool fp8 = false;
     alignas(64) unsigned char tm_x2[128];
+    alignas(64) unsigned char tm_xaug[128];
+    alignas(64) unsigned char tm_xaug2[128];
     alignas(64) unsigned char tm_x[128];
     alignas(64) unsigned char tm_c[128];
     alignas(64) unsigned char tm_aug[128];
@@ -122,7 +129,8 @@ enum BufSlot {
     BUF_X = 0, BUF_XC, BUF_C0, BUF_C1, BUF_CBEST, BUF_LABELS, BUF_LBEST, BUF_MIND,
     BUF_MEMBERS, BUF_SEGHIST, BUF_SCAN_TMP, BUF_COUNTS, BUF_PARTIAL, BUF_SCALARS,
     BUF_OUT, BUF_OUT2, BUF_KPP0, BUF_KPP1, BUF_KPP2, BUF_KPP3, BUF_DRAWS,
-    BUF_XB, BUF_XNORM, BUF_CB, BUF_CAUX, BUF_TOP2, BUF_FLAGS, BUF_FULL, BUF_CF32, BUF_CF32C, BUF_FIXPART, BUF_XB2, BUF_TOP4, BUF_QUAD, BUF_EX,
+    BUF_XB, BUF_XNORM, BUF_CB, BUF_CAUX, BUF_TOP2, BUF_FLAGS, BUF_FULL, BUF_CF32, BUF_CF32C, BUF_FIXPART, BUF_XB2, BUF_TOP4, BUF_QUAD, BUF_EX, BUF_XAUG, BUF_XAUG2, BUF_ROWSCALE,
+    BUF_ROWSCALE2,
     BUF_COUNT
 };
 
@@ -251,16 +259,20 @@ void launch_mixed_inertia(Ctx &ctx, const double *part, int64_t m, DevScalars *s
 
 // Tensor-core assignment (fk_tc.cu): plan, then one persistent launch that
 // writes one Top2 record per (slice, row).
-void plan_tc(Ctx &ctx, MixedPlan &mp, int64_t n, int d, int k);
+void plan_tc(Ctx &ctx, MixedPlan &mp, int64_t n, int d, int k, bool fp8 = false);
 // dump (tests only, nullable): raw accumulators of CTA 0's first tile.
 // out4 != nullptr selects the second pass (top-4 records over the gathered
 // rows whose count is read from n_dev at launch; mp.n is their capacity).
+// FP8 (mp.fp8): xaug is the per-row augmentation tensor (n x 16 BF16) and
+// rowscale the per-row power of two mapping scores to the row's units.
 void launch_tc_assign(Ctx &ctx, MixedPlan &mp, const void *xb, const void *cb, const void *caug, Top2 *out,
                       DevScalars *sc, const MixedStats *stats, float *dump = nullptr, Top4 *out4 = nullptr,
-                      const unsigned long long *n_dev = nullptr);
+                      const unsigned long long *n_dev = nullptr, const void *xaug = nullptr,
+                      const float *rowscale = nullptr);
 
 void measure_peaks(Ctx &ctx, double *out);
-void debug_tc_probe(Ctx &ctx, const float *x, int64_t n, int d, const double *c, int k, float *dump_out,
-                    uint16_t *xb_out, uint16_t *cb_out, uint16_t *aug_out, Top2 *top_out, int *plan_out);
+void debug_tc_probe(Ctx &ctx, const float *x, int64_t n, int d, const double *c, int k, int precision,
+                    float *dump_out, void *xq_out, void *cq_out, uint16_t *aug_out, uint16_t *xaug_out,
+                    Top2 *top_out, int *plan_out);
 
 }  // namespace fk

@@ -28,6 +28,7 @@
 #include <cfloat>
 #include <cmath>
 #include <cuda_bf16.h>
+#include <cuda_fp8.h>
 
 #include <algorithm>
 #include <cstddef>
@@ -84,6 +85,35 @@ __global__ void col_mean_final_kernel(const double *__restrict__ part, int npart
     mu[j] = (double)m;  // the centring is by the f32 value, for rows and centres alike
 }
 
+// FP8: max |x - mu| over the same strided sample, the anchor of every scale
+// of the launch (the centres' t and the range of the per-row scales).
+template <typename TX>
+__global__ void sample_tmax_kernel(const TX *__restrict__ x, int64_t n, int d, int64_t stride, int64_t rows,
+                                   const float *__restrict__ mu32, MixedStats *stats) {
+    float m = 0.f;
+    const int64_t total = rows * (int64_t)d;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = (e / d) * stride;
+        const int j = (int)(e % d);
+        if (i < n) {
+            const float t = fabsf(__fsub_rn((float)x[i * d + j], mu32[j]));
+            if (t < INFINITY) m = fmaxf(m, t);
+        }
+    }
+#pragma unroll
+    for (int off = 16; off >= 1; off >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, off));
+    if ((threadIdx.x & 31) == 0 && m > 0.f) atomicMax((unsigned int *)&stats->tmax, __float_as_uint(m));
+}
+
+// Exponent of the FP8 centre scale t = 2^sh_t: max |t| / t in [128, 256).
+__device__ __forceinline__ int fp8_scale_exp(float tmax) {
+    int sh = 0;
+    if (tmax > 0.f && tmax < INFINITY) sh = ilogbf(tmax) - 7;
+    return sh < -120 ? -120 : (sh > 120 ? 120 : sh);
+}
+constexpr int FP8_ROW_BELOW = 40;  // per-row scales stay within [2^(sh_t-40), 2^(sh_t+60)]
+constexpr int FP8_ROW_ABOVE = 60;
+
 __device__ __forceinline__ float warp_sum_f(float v) {
 #pragma unroll
     for (int off = 16; off >= 1; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
@@ -97,31 +127,65 @@ __device__ __forceinline__ float warp_sum_f(float v) {
 // ||x' - xh|| <= ||t - xh|| + 2^-24 ||t||; each sum of squares is scaled by
 // (1 + (d + 64) 2^-23) to cover its own rounding before the rounded-up root.
 // Also records max |x| (for the fixed-point centroid sums) and max ||xh||.
-template <typename TX>
+// FP8 rows: t = fl(x - mu) is scaled by a power of two s = 2^sh chosen per
+// row so that max |t| / s lies in [128, 256) (inside E4M3's +-448), each t / s
+// (exact) is rounded to E4M3 (saturating), and the dequantised value s * q
+// stands where the BF16 value stands above; rowinfo.w = 2^-sh and the row's
+// augmentation row is [2^-sh, 2^-sh, 2^-sh, 0, ...] (BF16, exact), so the
+// tensor cores see every score of the row divided by s (and by the centres'
+// scale t). sh is kept within [sh_t - 40, sh_t + 60] (and [-120, 120]) so
+// that every scaled score stays a normal float.
+template <typename TX, bool FP8>
 __global__ void prep_rows_kernel(const TX *__restrict__ x, int64_t n, int d, int d_pad,
-                                 const float *__restrict__ mu32, __nv_bfloat16 *__restrict__ xb,
-                                 float4 *__restrict__ rowinfo, MixedStats *stats) {
+                                 const float *__restrict__ mu32, void *__restrict__ xq_out,
+                                 __nv_bfloat16 *__restrict__ xaug, float4 *__restrict__ rowinfo, MixedStats *stats) {
     __shared__ float sh_xn[32], sh_am[32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
     float xn_hi = 0.f, am_hi = 0.f;
     for (int64_t row = (int64_t)blockIdx.x * (blockDim.x >> 5) + w; row < n; row += nwarps) {
-        float xn2 = 0.f, ex2 = 0.f, tn2 = 0.f, xo2 = 0.f, amax = 0.f;
+        float xn2 = 0.f, ex2 = 0.f, tn2 = 0.f, xo2 = 0.f, amax = 0.f, tmax = 0.f;  // tmax: FP8 only
+        float scale = 1.f, inv = 1.f;
+        if (FP8) {
+            for (int j = lane; j < d; j += 32) {
+                const float tv = fabsf(__fsub_rn((float)x[row * d + j], mu32[j]));
+                if (tv < INFINITY) tmax = fmaxf(tmax, tv);
+            }
+#pragma unroll
+            for (int off = 16; off >= 1; off >>= 1) tmax = fmaxf(tmax, __shfl_xor_sync(0xffffffffu, tmax, off));
+            const int sh_t = fp8_scale_exp(stats->tmax);
+            int sh = tmax > 0.f ? fp8_scale_exp(tmax) : sh_t;
+            sh = max(min(sh, sh_t + FP8_ROW_ABOVE), sh_t - FP8_ROW_BELOW);
+            sh = max(min(sh, 120), -120);
+            scale = ldexpf(1.f, sh);
+            inv = ldexpf(1.f, -sh);
+            tmax = 0.f;
+        }
         for (int j = lane; j < d_pad; j += 32) {
-            __nv_bfloat16 h = __float2bfloat16_rn(0.f);
+            float hv = 0.f;
             if (j < d) {
-                float xv = (float)x[row * d + j];
-                float t = __fsub_rn(xv, mu32[j]);
-                h = __float2bfloat16_rn(t);
-                float hv = __bfloat162float(h);
-                float e = __fsub_rn(t, hv);
+                const float xv = (float)x[row * d + j];
+                const float t = __fsub_rn(xv, mu32[j]);
+                if (FP8) {
+                    const __nv_fp8_e4m3 q8(__fmul_rn(t, inv));
+                    ((unsigned char *)xq_out)[row * d_pad + j] = q8.__x;
+                    hv = __fmul_rn((float)q8, scale);
+                } else {
+                    const __nv_bfloat16 h = __float2bfloat16_rn(t);
+                    ((__nv_bfloat16 *)xq_out)[row * d_pad + j] = h;
+                    hv = __bfloat162float(h);
+                }
+                const float e = __fsub_rn(t, hv);
                 xn2 = __fmaf_rn(hv, hv, xn2);
                 ex2 = __fmaf_rn(e, e, ex2);
                 tn2 = __fmaf_rn(t, t, tn2);
                 xo2 = __fmaf_rn(xv, xv, xo2);
                 amax = fmaxf(amax, fabsf(xv));
+            } else if (FP8) {
+                ((unsigned char *)xq_out)[row * d_pad + j] = 0;
+            } else {
+                ((__nv_bfloat16 *)xq_out)[row * d_pad + j] = __float2bfloat16_rn(0.f);
             }
-            xb[row * d_pad + j] = h;
         }
         xn2 = warp_sum_f(xn2);
         ex2 = warp_sum_f(ex2);
@@ -133,7 +197,9 @@ __global__ void prep_rows_kernel(const TX *__restrict__ x, int64_t n, int d, int
         float xn = __fsqrt_ru(__fmul_ru(xn2, up));
         float ex = __fadd_ru(__fsqrt_ru(__fmul_ru(ex2, up)), __fmul_ru(__fsqrt_ru(__fmul_ru(tn2, up)), 5.9604645e-08f));
         float xo = __fsqrt_ru(__fmul_ru(xo2, up));
-        if (lane == 0) rowinfo[row] = make_float4(xn, ex, xo, 0.f);
+        if (lane == 0) rowinfo[row] = make_float4(xn, ex, xo, inv);
+        if (FP8 && lane < 16)
+            xaug[row * 16 + lane] = lane < 3 ? __float2bfloat16_rn(inv) : __float2bfloat16_rn(0.f);
         if (xn < INFINITY) xn_hi = fmaxf(xn_hi, xn);  // NaN / inf rows are re-scored in full
         if (amax < INFINITY) am_hi = fmaxf(am_hi, amax);
     }
@@ -156,21 +222,46 @@ __global__ void prep_rows_kernel(const TX *__restrict__ x, int64_t n, int d, int
 // -------------------------------------------------------- centre prep --
 // One warp per (padded) centre row: BF16 copy of c - mu, and the maxima of
 // ||c'||, ||c' - ch||, ||ch||, ||c'||^2 / 2, ||c|| over the real centres.
+// FP8 centres: one power-of-two scale t for all centres, from the data's range
+// (centres are means of rows, so they stay inside it; a centre outside would
+// saturate, which the exact error ||c' - ch|| below accounts for).
+template <bool FP8>
 __global__ void prep_centres_kernel(const double *__restrict__ c, int k, int k_pad, int d, int d_pad,
-                                    const double *__restrict__ mu, __nv_bfloat16 *__restrict__ cb,
+                                    const double *__restrict__ mu, void *__restrict__ cq_out,
                                     double *__restrict__ half_norm, float *__restrict__ c32,
                                     float *__restrict__ ec32, float *__restrict__ c32t, MixedStats *stats) {
     const int lane = threadIdx.x & 31;
     const int q = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     if (q >= k_pad) return;
+    float tsc = 1.f, tinv = 1.f;
+    if (FP8) {
+        const int sh = fp8_scale_exp(stats->tmax);
+        tsc = ldexpf(1.f, sh);
+        tinv = ldexpf(1.f, -sh);
+        if (q == 0 && lane == 0) {
+            stats->tscale = tsc;
+            stats->inv_t = tinv;
+        }
+    } else if (q == 0 && lane == 0) {
+        stats->tscale = 1.f;
+        stats->inv_t = 1.f;
+    }
     double cn2 = 0.0, ec2 = 0.0, ch2 = 0.0, co2 = 0.0, e32 = 0.0;
     for (int j = lane; j < d_pad; j += 32) {
         __nv_bfloat16 h = __float2bfloat16_rn(0.f);
+        unsigned char h8 = 0;
         if (q < k && j < d) {
             double cv = c[(int64_t)q * d + j];
             double cc = cv - mu[j];
-            h = __float2bfloat16_rn((float)cc);
-            double hv = (double)__bfloat162float(h);
+            double hv;
+            if (FP8) {
+                const __nv_fp8_e4m3 q8((float)(cc * (double)tinv));
+                h8 = q8.__x;
+                hv = (double)(float)q8 * (double)tsc;
+            } else {
+                h = __float2bfloat16_rn((float)cc);
+                hv = (double)__bfloat162float(h);
+            }
             cn2 += cc * cc;
             ec2 += (cc - hv) * (cc - hv);
             ch2 += hv * hv;
@@ -180,7 +271,10 @@ __global__ void prep_centres_kernel(const double *__restrict__ c, int k, int k_p
             c32t[(int64_t)j * k + q] = f;
             e32 += (cv - (double)f) * (cv - (double)f);
         }
-        cb[(int64_t)q * d_pad + j] = h;
+        if (FP8)
+            ((unsigned char *)cq_out)[(int64_t)q * d_pad + j] = h8;
+        else
+            ((__nv_bfloat16 *)cq_out)[(int64_t)q * d_pad + j] = h;
     }
     cn2 = warp_sum_d(cn2);
     ec2 = warp_sum_d(ec2);
@@ -205,13 +299,25 @@ __global__ void prep_centres_kernel(const double *__restrict__ c, int k, int k_p
 // so every real score T = xh.ch + a_c lies in [2^E, 2^(E+1)) with room to
 // spare: all scores of a launch share one exponent, which lets the epilogue
 // round them to a common grid and insert the column code exactly.
-__global__ void prep_aug_kernel(const double *__restrict__ half_norm, int k, int k_pad,
+__global__ void prep_aug_kernel(const double *__restrict__ half_norm, int k, int k_pad, bool fp8,
                                 __nv_bfloat16 *__restrict__ caug, MixedStats *stats) {
     int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= k_pad) return;
     const double span = (double)stats->xn_max * (double)stats->ch_max + (double)stats->h_max;
-    const int e = (int)ceil(log2(2.02 * span + 256.0));
-    const double big = 1.5 * ldexp(1.0, e);
+    const double tsc = (double)stats->tscale;  // FP8: 256 t^2 is the floor of 2^E in the centres' units
+    const double le = ceil(log2(2.02 * span + 256.0 * tsc * tsc));
+    const int e = le < 200.0 ? (int)le : 200;  // NaN / inf span: 200, then BIG = inf below
+    double big = 1.5 * ldexp(1.0, e);
+    // The accumulators hold T r, r = 1 (BF16) or 2^-(sh_row + sh_t) (FP8); keys
+    // need T r + 3 * 2^(e+6) r to stay finite and 2^(e-23) r to stay normal.
+    // Outside that range BIG is infinite and every row is re-scored exactly.
+    int rmax_exp = 0, rmin_exp = 0;
+    if (fp8) {
+        const int sh_t = ilogbf(stats->tscale);
+        rmax_exp = -(max(sh_t - FP8_ROW_BELOW, -120) + sh_t);
+        rmin_exp = -(min(sh_t + FP8_ROW_ABOVE, 120) + sh_t);
+    }
+    if (e + 9 + rmax_exp > 126 || e - 23 + rmin_exp < -126) big = INFINITY;
     if (q == 0) {
         stats->big = (float)big;
         stats->cgrid = (float)(3.0 * ldexp(1.0, e + 6));
@@ -221,7 +327,7 @@ __global__ void prep_aug_kernel(const double *__restrict__ half_norm, int k, int
 #pragma unroll
     for (int j = 0; j < 16; j++) t[j] = __float2bfloat16_rn(0.f);
     if (q < k) {
-        double a = big - half_norm[q];
+        double a = (big - half_norm[q]) * (double)stats->inv_t;  // FP8: in units of the centres' scale
         __nv_bfloat16 a1 = __float2bfloat16_rn((float)a);
         double r1 = a - (double)__bfloat162float(a1);
         __nv_bfloat16 a2 = __float2bfloat16_rn((float)r1);
@@ -291,6 +397,12 @@ __global__ void finalize_kernel(const Top2 *__restrict__ parts, int nparts, int6
     for (int p = 1; p < nparts; p++) {
         Top2 o = parts[(int64_t)p * n + i];
         merge_top2(v1, i1, v2, i2, u3, o.v1, o.i1, o.v2, o.i2, o.u3);
+    }
+    {  // FP8 rows are scored in units of 1/(s_i t): back to score units (exact powers of two)
+        const float unit = stats->tscale / rowinfo[i].w;
+        v1 *= unit;
+        v2 *= unit;
+        u3 *= unit;
     }
     const double thr = row_threshold(rowinfo[i], stats, acc_rel, mu_norm, d, v1);
     double m12 = (double)v1 - (double)v2;
@@ -627,14 +739,16 @@ __global__ void finalize4_kernel(const Top4 *__restrict__ parts, int nparts, int
             for (int j = 0; j < 4; j++) U = max(U, ins4u(R, I, __float_as_uint(o.v[j]), o.i[j]));
         }
         const int32_t row = list[s];
-        const float v1 = __uint_as_float(R[0]);
-        const double thr = row_threshold(rowinfo[row], stats, acc_rel, mu_norm, d, v1);
-        const bool rest_out = (double)v1 - (double)__uint_as_float(U) > thr;
+        const float4 ri = rowinfo[row];
+        const float unit = stats->tscale / ri.w;  // FP8: back to score units
+        const float v1 = __uint_as_float(R[0]) * unit;
+        const double thr = row_threshold(ri, stats, acc_rel, mu_norm, d, v1);
+        const bool rest_out = (double)v1 - (double)(__uint_as_float(U) * unit) > thr;
         int m = 0;
         bool valid = true;
 #pragma unroll
         for (int j = 0; j < 4; j++) {
-            if ((double)v1 - (double)__uint_as_float(R[j]) <= thr) {
+            if ((double)v1 - (double)(__uint_as_float(R[j]) * unit) <= thr) {
                 m++;
                 if (I[j] < 0 || I[j] >= k) valid = false;
             }
@@ -746,29 +860,40 @@ __global__ void inertia_final_kernel(const double *__restrict__ part, int64_t m,
 }  // namespace
 
 // ---------------------------------------------------------------- driver --
+namespace {
+
+// Device buffers of one mixed assignment.
+struct MixedBufs {
+    MixedStats *stats;
+    double *mu;
+    float *mu32;
+    void *xq;               // BF16 or E4M3 rows, n x d_pad
+    __nv_bfloat16 *xaug;    // FP8: per-row augmentation rows, n x 16
+    float4 *rowinfo;
+    void *cq;               // BF16 or E4M3 centres, k_pad x d_pad
+    __nv_bfloat16 *caug;    // k_pad x 16
+    double *half_norm;
+    float *c32, *ec32, *c32t;
+};
+
+// Plans the launch and prepares the rows (when X changed) and the centres.
 template <typename TX>
-void run_assign_mixed(Ctx &ctx, const TX *x, int64_t n, int d, const double *c, int k, int precision,
-                      int32_t *labels, double *, DevScalars *sc, bool x_changed) {
+MixedBufs prepare_mixed(Ctx &ctx, const TX *x, int64_t n, int d, const double *c, int k, bool fp8, bool x_changed) {
     cudaStream_t s = ctx.stream;
     MixedPlan &mp = ctx.mixed;
-    if (precision != FK_PRECISION_MIXED_BF16) {
-        set_error("precision %d is not built", precision);
-        fail(FK_ERR_UNSUPPORTED);
-    }
-    if (d < 1 || d > 256) {
-        set_error("the BF16 tensor-core path supports 1 <= d <= 256 (got %d)", d);
-        fail(FK_ERR_UNSUPPORTED);
-    }
-    const bool replan = x_changed || mp.n != n || mp.d != d || mp.k != k || mp.x != (const void *)x;
-    if (replan) plan_tc(ctx, mp, n, d, k);
+    const bool replan = x_changed || mp.n != n || mp.d != d || mp.k != k || mp.x != (const void *)x || mp.fp8 != fp8;
+    if (replan) plan_tc(ctx, mp, n, d, k, fp8);
     mp.x = (const void *)x;
-    auto *stats = (MixedStats *)ctx.get(BUF_CF32, sizeof(MixedStats));
-    double *mu = (double *)ctx.get(BUF_COUNTS, sizeof(double) * 2 * (size_t)d + sizeof(float) * (size_t)d + 64);
-    float *mu32 = (float *)(mu + 2 * d);
-    __nv_bfloat16 *xb = (__nv_bfloat16 *)ctx.get(BUF_XB, sizeof(__nv_bfloat16) * (size_t)n * mp.d_pad);
-    float4 *rowinfo = (float4 *)ctx.get(BUF_XNORM, sizeof(float4) * (size_t)n);
+    const size_t es = fp8 ? 1 : 2;
+    MixedBufs B;
+    B.stats = (MixedStats *)ctx.get(BUF_CF32, sizeof(MixedStats));
+    B.mu = (double *)ctx.get(BUF_COUNTS, sizeof(double) * 2 * (size_t)d + sizeof(float) * (size_t)d + 64);
+    B.mu32 = (float *)(B.mu + 2 * d);
+    B.xq = ctx.get(BUF_XB, es * (size_t)n * mp.d_pad);
+    B.xaug = fp8 ? (__nv_bfloat16 *)ctx.get(BUF_XAUG, sizeof(__nv_bfloat16) * 16 * (size_t)n) : nullptr;
+    B.rowinfo = (float4 *)ctx.get(BUF_XNORM, sizeof(float4) * (size_t)n);
     if (replan) {
-        FK_CUDA(cudaMemsetAsync(stats, 0, sizeof(MixedStats), s));
+        FK_CUDA(cudaMemsetAsync(B.stats, 0, sizeof(MixedStats), s));
         // the centring vector only needs to be finite: a strided sample of at
         // most 65536 rows is enough
         const int64_t stride = n > 65536 ? n / 65536 : 1;
@@ -779,68 +904,142 @@ void run_assign_mixed(Ctx &ctx, const TX *x, int64_t n, int d, const double *c, 
         dim3 g1(nparts, (d + 127) / 128);
         col_mean_partial_kernel<TX><<<g1, 128, 0, s>>>(x, n, d, rows_per, stride, part);
         FK_LAUNCH_CHECK();
-        col_mean_final_kernel<<<(d + 127) / 128, 128, 0, s>>>(part, nparts, rows, d, mu, mu32);
+        col_mean_final_kernel<<<(d + 127) / 128, 128, 0, s>>>(part, nparts, rows, d, B.mu, B.mu32);
         FK_LAUNCH_CHECK();
+        if (fp8) {
+            sample_tmax_kernel<TX><<<ctx.num_sms * 2, 256, 0, s>>>(x, n, d, stride, rows, B.mu32, B.stats);
+            FK_LAUNCH_CHECK();
+        }
         const int64_t pblocks = std::min<int64_t>((n + 7) / 8, (int64_t)ctx.num_sms * 16);
-        prep_rows_kernel<TX><<<(unsigned)pblocks, 256, 0, s>>>(x, n, d, mp.d_pad, mu32, xb, rowinfo, stats);
+        if (fp8)
+            prep_rows_kernel<TX, true><<<(unsigned)pblocks, 256, 0, s>>>(x, n, d, mp.d_pad, B.mu32, B.xq, B.xaug,
+                                                                          B.rowinfo, B.stats);
+        else
+            prep_rows_kernel<TX, false><<<(unsigned)pblocks, 256, 0, s>>>(x, n, d, mp.d_pad, B.mu32, B.xq, nullptr,
+                                                                           B.rowinfo, B.stats);
         FK_LAUNCH_CHECK();
         // ||mu|| for the bound on ||x|| (host side, tiny)
         std::vector<double> hmu(d);
-        FK_CUDA(cudaMemcpyAsync(hmu.data(), mu, sizeof(double) * d, cudaMemcpyDeviceToHost, s));
+        FK_CUDA(cudaMemcpyAsync(hmu.data(), B.mu, sizeof(double) * d, cudaMemcpyDeviceToHost, s));
         FK_CUDA(cudaStreamSynchronize(s));
         double m2 = 0.0;
         for (double v : hmu) m2 += v * v;
         mp.mu_norm = std::sqrt(m2) * (1.0 + 1e-12);
     } else {
-        // centre statistics are per iteration; the row maximum stays
-        FK_CUDA(cudaMemsetAsync((char *)stats + offsetof(MixedStats, cn_max), 0,
+        // centre statistics are per iteration; the row maxima stay
+        FK_CUDA(cudaMemsetAsync((char *)B.stats + offsetof(MixedStats, cn_max), 0,
                                 sizeof(MixedStats) - offsetof(MixedStats, cn_max), s));
     }
-    __nv_bfloat16 *cb = (__nv_bfloat16 *)ctx.get(BUF_CB, sizeof(__nv_bfloat16) * (size_t)mp.k_pad * mp.d_pad);
-    __nv_bfloat16 *caug = (__nv_bfloat16 *)ctx.get(BUF_CAUX, sizeof(__nv_bfloat16) * (size_t)mp.k_pad * 16 + 8192);
-    double *half_norm = (double *)ctx.get(BUF_MIND, sizeof(double) * (size_t)mp.k_pad);
-    float *c32 = (float *)ctx.get(BUF_CF32C, sizeof(float) * (2 * (size_t)k * d + (size_t)k) + 64);
-    float *ec32 = c32 + (size_t)k * d;
-    float *c32t = ec32 + k;
-    prep_centres_kernel<<<(mp.k_pad + 7) / 8, 256, 0, s>>>(c, k, mp.k_pad, d, mp.d_pad, mu, cb, half_norm, c32, ec32,
-                                                           c32t, stats);
+    B.cq = ctx.get(BUF_CB, es * (size_t)mp.k_pad * mp.d_pad);
+    B.caug = (__nv_bfloat16 *)ctx.get(BUF_CAUX, sizeof(__nv_bfloat16) * (size_t)mp.k_pad * 16 + 8192);
+    B.half_norm = (double *)ctx.get(BUF_MIND, sizeof(double) * (size_t)mp.k_pad);
+    B.c32 = (float *)ctx.get(BUF_CF32C, sizeof(float) * (2 * (size_t)k * d + (size_t)k) + 64);
+    B.ec32 = B.c32 + (size_t)k * d;
+    B.c32t = B.ec32 + k;
+    if (fp8)
+        prep_centres_kernel<true><<<(mp.k_pad + 7) / 8, 256, 0, s>>>(c, k, mp.k_pad, d, mp.d_pad, B.mu, B.cq,
+                                                                     B.half_norm, B.c32, B.ec32, B.c32t, B.stats);
+    else
+        prep_centres_kernel<false><<<(mp.k_pad + 7) / 8, 256, 0, s>>>(c, k, mp.k_pad, d, mp.d_pad, B.mu, B.cq,
+                                                                      B.half_norm, B.c32, B.ec32, B.c32t, B.stats);
     FK_LAUNCH_CHECK();
-    prep_aug_kernel<<<(mp.k_pad + 255) / 256, 256, 0, s>>>(half_norm, k, mp.k_pad, caug, stats);
+    prep_aug_kernel<<<(mp.k_pad + 255) / 256, 256, 0, s>>>(B.half_norm, k, mp.k_pad, fp8, B.caug, B.stats);
     FK_LAUNCH_CHECK();
+    return B;
+}
+
+__global__ void gather_aux_kernel(const __nv_bfloat16 *__restrict__ xaug, const float *__restrict__ rowscale,
+                                  const int32_t *__restrict__ list, const unsigned long long *count_ptr,
+                                  __nv_bfloat16 *__restrict__ xaug2, float *__restrict__ rowscale2) {
+    const unsigned long long cnt = *count_ptr;
+    for (unsigned long long s = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; s < cnt;
+         s += (unsigned long long)gridDim.x * blockDim.x) {
+        const int64_t r = list[s];
+#pragma unroll
+        for (int j = 0; j < 16; j++) xaug2[(int64_t)s * 16 + j] = xaug[r * 16 + j];
+        rowscale2[s] = rowscale[r];
+    }
+}
+
+// FP8: r = 2^-sh_row * 2^-sh_t, the factor between a row's scores and its
+// accumulators (exact: a product of powers of two in range).
+__global__ void rowscale_kernel(const float4 *__restrict__ rowinfo, int64_t n, const MixedStats *stats,
+                                float *__restrict__ rowscale) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) rowscale[i] = rowinfo[i].w * stats->inv_t;
+}
+
+}  // namespace
+
+template <typename TX>
+void run_assign_mixed(Ctx &ctx, const TX *x, int64_t n, int d, const double *c, int k, int precision,
+                      int32_t *labels, double *, DevScalars *sc, bool x_changed) {
+    cudaStream_t s = ctx.stream;
+    MixedPlan &mp = ctx.mixed;
+    if (precision != FK_PRECISION_MIXED_BF16 && precision != FK_PRECISION_MIXED_FP8) {
+        set_error("precision %d is not built", precision);
+        fail(FK_ERR_UNSUPPORTED);
+    }
+    const bool fp8 = precision == FK_PRECISION_MIXED_FP8;
+    if (fp8 && !std::is_same<TX, float>::value) {
+        set_error("the FP8 form needs X stored as f32 (the f32x64 entry points)");
+        fail(FK_ERR_UNSUPPORTED);
+    }
+    if (d < 1 || d > (fp8 ? 384 : 192)) {
+        set_error("the tensor-core path supports 1 <= d <= %d for this precision (got %d)", fp8 ? 384 : 192, d);
+        fail(FK_ERR_UNSUPPORTED);
+    }
+    MixedBufs B = prepare_mixed<TX>(ctx, x, n, d, c, k, fp8, x_changed);
+    float *rowscale = nullptr;
+    if (fp8) {
+        rowscale = (float *)ctx.get(BUF_ROWSCALE, sizeof(float) * (size_t)n);
+        rowscale_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(B.rowinfo, n, B.stats, rowscale);
+        FK_LAUNCH_CHECK();
+    }
 
     Top2 *top = (Top2 *)ctx.get(BUF_TOP2, sizeof(Top2) * (size_t)n * mp.parts);
     {
         Timer t(ctx.contract_acc != nullptr, ctx, ctx.contract_acc);
-        launch_tc_assign(ctx, mp, xb, cb, caug, top, sc, stats);
+        launch_tc_assign(ctx, mp, B.xq, B.cq, B.caug, top, sc, B.stats, nullptr, nullptr, nullptr, B.xaug, rowscale);
     }
 
     int4 *pairs = (int4 *)ctx.get(BUF_FLAGS, sizeof(int4) * (size_t)n);
     int32_t *full = (int32_t *)ctx.get(BUF_FULL, sizeof(int32_t) * (size_t)n);
-    const double acc_rel = (double)(mp.d_pad + 32) * ACC_REL_PER_K;
-    finalize_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(top, mp.parts, n, k, d, rowinfo, stats, acc_rel,
+    const double acc_rel = (double)((size_t)mp.d_pad + 32) * ACC_REL_PER_K;
+    finalize_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(top, mp.parts, n, k, d, B.rowinfo, B.stats, acc_rel,
                                                                mp.mu_norm, labels, pairs, full, sc);
     FK_LAUNCH_CHECK();
     const int grid = ctx.num_sms * 4;
-    pair_rescore_kernel<TX><<<grid, 256, 0, s>>>(x, d, c, c32, ec32, pairs, sc, labels);
+    pair_rescore_kernel<TX><<<grid, 256, 0, s>>>(x, d, c, B.c32, B.ec32, pairs, sc, labels);
     FK_LAUNCH_CHECK();
     if constexpr (std::is_same<TX, float>::value) {
         // second tensor pass over the rows whose third score was inside the bound
-        __nv_bfloat16 *xb2 = (__nv_bfloat16 *)ctx.get(BUF_XB2, sizeof(__nv_bfloat16) * (size_t)n * mp.d_pad);
+        const size_t es = fp8 ? 1 : 2;
+        void *xb2 = ctx.get(BUF_XB2, es * (size_t)n * mp.d_pad);
         Top4 *top4 = (Top4 *)ctx.get(BUF_TOP4, sizeof(Top4) * (size_t)n * mp.parts);
         Quad *quads = (Quad *)ctx.get(BUF_QUAD, sizeof(Quad) * (size_t)n);
         int32_t *ex = (int32_t *)ctx.get(BUF_EX, sizeof(int32_t) * (size_t)n);
-        gather_rows_kernel<<<grid, 256, 0, s>>>((const uint4 *)xb, mp.d_pad * 2 / 16, full, &sc->full_count,
+        __nv_bfloat16 *xaug2 = nullptr;
+        float *rowscale2 = nullptr;
+        gather_rows_kernel<<<grid, 256, 0, s>>>((const uint4 *)B.xq, (int)(es * mp.d_pad / 16), full, &sc->full_count,
                                                 (uint4 *)xb2);
         FK_LAUNCH_CHECK();
-        launch_tc_assign(ctx, mp, xb2, cb, caug, nullptr, sc, stats, nullptr, top4, &sc->full_count);
-        finalize4_kernel<<<grid, 256, 0, s>>>(top4, mp.parts, n, k, d, full, rowinfo, stats, acc_rel, mp.mu_norm,
+        if (fp8) {
+            xaug2 = (__nv_bfloat16 *)ctx.get(BUF_XAUG2, sizeof(__nv_bfloat16) * 16 * (size_t)n);
+            rowscale2 = (float *)ctx.get(BUF_ROWSCALE2, sizeof(float) * (size_t)n);
+            gather_aux_kernel<<<grid, 256, 0, s>>>(B.xaug, rowscale, full, &sc->full_count, xaug2, rowscale2);
+            FK_LAUNCH_CHECK();
+        }
+        launch_tc_assign(ctx, mp, xb2, B.cq, B.caug, nullptr, sc, B.stats, nullptr, top4, &sc->full_count, xaug2,
+                         rowscale2);
+        finalize4_kernel<<<grid, 256, 0, s>>>(top4, mp.parts, n, k, d, full, B.rowinfo, B.stats, acc_rel, mp.mu_norm,
                                               labels, quads, ex, sc);
         FK_LAUNCH_CHECK();
-        quad_rescore_kernel<<<grid, 256, 0, s>>>(x, d, c, c32, ec32, quads, sc, labels);
+        quad_rescore_kernel<<<grid, 256, 0, s>>>(x, d, c, B.c32, B.ec32, quads, sc, labels);
         FK_LAUNCH_CHECK();
-        exhaustive_rescore_kernel<<<grid, 256, 0, s>>>(x, d, c, c32t, ec32, k, ex, &sc->ex_count, sc, labels);
+        exhaustive_rescore_kernel<<<grid, 256, 0, s>>>(x, d, c, B.c32t, B.ec32, k, ex, &sc->ex_count, sc, labels);
     } else {
-        full_rescore_kernel<TX><<<grid, 256, 0, s>>>(x, d, c, c32, ec32, k, full, &sc->full_count, sc, labels);
+        full_rescore_kernel<TX><<<grid, 256, 0, s>>>(x, d, c, B.c32, B.ec32, k, full, &sc->full_count, sc, labels);
     }
     FK_LAUNCH_CHECK();
 }
@@ -852,51 +1051,40 @@ void launch_mixed_inertia(Ctx &ctx, const double *part, int64_t m, DevScalars *s
 
 template void run_assign_mixed<float>(Ctx &, const float *, int64_t, int, const double *, int, int, int32_t *,
                                       double *, DevScalars *, bool);
+template void run_assign_mixed<double>(Ctx &, const double *, int64_t, int, const double *, int, int, int32_t *,
+                                       double *, DevScalars *, bool);
 
 // Diagnostics for the tests: one tensor-core pass over x (f32, on the device)
 // against c (f64), returning the raw accumulators of CTA 0's first tile and
-// the BF16 operands they were computed from.
-void debug_tc_probe(Ctx &ctx, const float *x, int64_t n, int d, const double *c, int k, float *dump_out,
-                    uint16_t *xb_out, uint16_t *cb_out, uint16_t *aug_out, Top2 *top_out, int *plan_out) {
+// the quantised operands they were computed from.
+void debug_tc_probe(Ctx &ctx, const float *x, int64_t n, int d, const double *c, int k, int precision,
+                    float *dump_out, void *xq_out, void *cq_out, uint16_t *aug_out, uint16_t *xaug_out,
+                    Top2 *top_out, int *plan_out) {
     cudaStream_t s = ctx.stream;
     MixedPlan &mp = ctx.mixed;
-    plan_tc(ctx, mp, n, d, k);
-    mp.x = nullptr;
+    const bool fp8 = precision == FK_PRECISION_MIXED_FP8;
     DevScalars *sc = (DevScalars *)ctx.get(BUF_SCALARS, sizeof(DevScalars));
     FK_CUDA(cudaMemsetAsync(sc, 0, sizeof(DevScalars), s));
-    auto *stats = (MixedStats *)ctx.get(BUF_CF32, sizeof(MixedStats));
-    FK_CUDA(cudaMemsetAsync(stats, 0, sizeof(MixedStats), s));
-    double *mu = (double *)ctx.get(BUF_COUNTS, sizeof(double) * 2 * (size_t)d + sizeof(float) * (size_t)d + 64);
-    float *mu32 = (float *)(mu + 2 * d);
-    __nv_bfloat16 *xb = (__nv_bfloat16 *)ctx.get(BUF_XB, sizeof(__nv_bfloat16) * (size_t)n * mp.d_pad);
-    float4 *rowinfo = (float4 *)ctx.get(BUF_XNORM, sizeof(float4) * (size_t)n);
-    const int64_t rows_per = 4096;
-    const int nparts = (int)((n + rows_per - 1) / rows_per);
-    double *part = (double *)ctx.get(BUF_PARTIAL, sizeof(double) * (size_t)nparts * d);
-    col_mean_partial_kernel<float><<<dim3(nparts, (d + 127) / 128), 128, 0, s>>>(x, n, d, rows_per, 1, part);
-    FK_LAUNCH_CHECK();
-    col_mean_final_kernel<<<(d + 127) / 128, 128, 0, s>>>(part, nparts, n, d, mu, mu32);
-    FK_LAUNCH_CHECK();
-    prep_rows_kernel<float><<<(unsigned)((n + 7) / 8), 256, 0, s>>>(x, n, d, mp.d_pad, mu32, xb, rowinfo, stats);
-    FK_LAUNCH_CHECK();
-    __nv_bfloat16 *cb = (__nv_bfloat16 *)ctx.get(BUF_CB, sizeof(__nv_bfloat16) * (size_t)mp.k_pad * mp.d_pad);
-    __nv_bfloat16 *caug = (__nv_bfloat16 *)ctx.get(BUF_CAUX, sizeof(__nv_bfloat16) * (size_t)mp.k_pad * 16 + 8192);
-    double *half_norm = (double *)ctx.get(BUF_MIND, sizeof(double) * (size_t)mp.k_pad);
-    float *c32 = (float *)ctx.get(BUF_CF32C, sizeof(float) * (2 * (size_t)k * d + (size_t)k) + 64);
-    prep_centres_kernel<<<(mp.k_pad + 7) / 8, 256, 0, s>>>(c, k, mp.k_pad, d, mp.d_pad, mu, cb, half_norm, c32,
-                                                           c32 + (size_t)k * d, c32 + (size_t)k * d + k, stats);
-    FK_LAUNCH_CHECK();
-    prep_aug_kernel<<<(mp.k_pad + 255) / 256, 256, 0, s>>>(half_norm, k, mp.k_pad, caug, stats);
-    FK_LAUNCH_CHECK();
+    MixedBufs B = prepare_mixed<float>(ctx, x, n, d, c, k, fp8, true);
+    mp.x = nullptr;
+    float *rowscale = nullptr;
+    if (fp8) {
+        rowscale = (float *)ctx.get(BUF_ROWSCALE, sizeof(float) * (size_t)n);
+        rowscale_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(B.rowinfo, n, B.stats, rowscale);
+        FK_LAUNCH_CHECK();
+    }
     Top2 *top = (Top2 *)ctx.get(BUF_TOP2, sizeof(Top2) * (size_t)n * mp.parts);
     float *dump = (float *)ctx.get(BUF_OUT, sizeof(float) * 128 * (size_t)mp.kp);
     FK_CUDA(cudaMemsetAsync(dump, 0, sizeof(float) * 128 * (size_t)mp.kp, s));
-    launch_tc_assign(ctx, mp, xb, cb, caug, top, sc, stats, dump);
+    launch_tc_assign(ctx, mp, B.xq, B.cq, B.caug, top, sc, B.stats, dump, nullptr, nullptr, B.xaug, rowscale);
+    const size_t es = fp8 ? 1 : 2;
     FK_CUDA(cudaMemcpyAsync(dump_out, dump, sizeof(float) * 128 * (size_t)mp.kp, cudaMemcpyDeviceToHost, s));
     const int64_t rows = n < 128 ? n : 128;
-    FK_CUDA(cudaMemcpyAsync(xb_out, xb, sizeof(uint16_t) * (size_t)rows * mp.d_pad, cudaMemcpyDeviceToHost, s));
-    FK_CUDA(cudaMemcpyAsync(cb_out, cb, sizeof(uint16_t) * (size_t)mp.k_pad * mp.d_pad, cudaMemcpyDeviceToHost, s));
-    FK_CUDA(cudaMemcpyAsync(aug_out, caug, sizeof(uint16_t) * (size_t)mp.k_pad * 16, cudaMemcpyDeviceToHost, s));
+    FK_CUDA(cudaMemcpyAsync(xq_out, B.xq, es * (size_t)rows * mp.d_pad, cudaMemcpyDeviceToHost, s));
+    FK_CUDA(cudaMemcpyAsync(cq_out, B.cq, es * (size_t)mp.k_pad * mp.d_pad, cudaMemcpyDeviceToHost, s));
+    FK_CUDA(cudaMemcpyAsync(aug_out, B.caug, sizeof(uint16_t) * (size_t)mp.k_pad * 16, cudaMemcpyDeviceToHost, s));
+    if (fp8)
+        FK_CUDA(cudaMemcpyAsync(xaug_out, B.xaug, sizeof(uint16_t) * 16 * (size_t)rows, cudaMemcpyDeviceToHost, s));
     FK_CUDA(cudaMemcpyAsync(top_out, top, sizeof(Top2) * (size_t)n * mp.parts, cudaMemcpyDeviceToHost, s));
     FK_CUDA(cudaMemcpyAsync(ctx.host_scalars, sc, sizeof(DevScalars), cudaMemcpyDeviceToHost, s));
     FK_CUDA(cudaStreamSynchronize(s));
@@ -907,7 +1095,5 @@ void debug_tc_probe(Ctx &ctx, const float *x, int64_t n, int d, const double *c,
     plan_out[4] = mp.grid;
     plan_out[5] = (int)ctx.host_scalars->error_word;
 }
-template void run_assign_mixed<double>(Ctx &, const double *, int64_t, int, const double *, int, int, int32_t *,
-                                       double *, DevScalars *, bool);
 
 }  // namespace fk

@@ -54,6 +54,9 @@ constexpr long long WAIT_LIMIT_CYCLES = 4000000000LL;
 // bits 24-28.
 constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
                            ((uint32_t)(BM >> 4) << 24);
+// kind::f8f6f4 with A = B = E4M3 (format 0), D = F32, same shape fields.
+constexpr uint32_t IDESC_FP8 = (1u << 4) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
+constexpr uint32_t XAUG_BYTES = BM * 32;     // per-row augmentation tile (FP8): 128 rows x 16 BF16
 constexpr uint32_t LAYOUT_SW128 = 2;
 constexpr uint32_t LAYOUT_SW32 = 6;
 
@@ -75,6 +78,8 @@ struct TcParams {
     Top4 *out4;               // top-4 records (second pass)
     unsigned long long *err;
     const MixedStats *stats;  // cgrid, ulp of this launch
+    const float *rowscale;    // FP8: per-row power of two 1/(s_i t) that maps scores to this row's units
+    uint32_t off_xaug;        // FP8: per-stage augmentation tiles
     float *dump;  // optional: raw accumulators of the first tile of CTA 0 (tests only)
 };
 
@@ -150,6 +155,15 @@ __device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t adesc, uint64
         "setp.ne.b32 p, %4, 0;\n\t"
         "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
         "l"(adesc), "l"(bdesc), "r"(IDESC), "r"(accumulate)
+        : "memory");
+}
+
+__device__ __forceinline__ void mma_fp8(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+        "l"(adesc), "l"(bdesc), "r"(IDESC_FP8), "r"(accumulate)
         : "memory");
 }
 
@@ -362,7 +376,10 @@ __device__ __forceinline__ void rank_half4(uint32_t col_addr, float cgrid, float
     for (int p = 0; p < 4; p++) ku = max(ku, ins4i(K, dummy, __float_as_uint(c1[p]), 0));
 }
 
-template <int TOPK>
+// FP8: X and the centres are E4M3 (1 byte, 128 per swizzle atom) and the
+// augmentation operand is a per-row BF16 tile loaded with each X tile (the
+// row's scale times [1,1,1,0,...]); BF16: a constant ones tile.
+template <int TOPK, bool FP8>
 __global__ void __launch_bounds__(NTHREADS, 1)
     tc_assign_kernel(const __grid_constant__ CUtensorMap tm_x, const __grid_constant__ CUtensorMap tm_c,
                      const __grid_constant__ CUtensorMap tm_aug, const __grid_constant__ CUtensorMap tm_ones,
@@ -419,19 +436,21 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             const int crow0 = part * p.kp;
             for (int a = 0; a < p.n_atoms; a++)
                 for (int r = 0; r < p.kp; r += BN)
-                    tma_load_2d(sb + p.off_c + (uint32_t)a * p.c_atom_bytes + (uint32_t)r * 128u, &tm_c, bar_c, a * 64,
-                                crow0 + r);
+                    tma_load_2d(sb + p.off_c + (uint32_t)a * p.c_atom_bytes + (uint32_t)r * 128u, &tm_c, bar_c,
+                                a * (FP8 ? 128 : 64), crow0 + r);
             for (int r = 0; r < p.kp; r += BN) tma_load_2d(sb + p.off_aug + (uint32_t)r * 32u, &tm_aug, bar_c, 0, crow0 + r);
-            tma_load_2d(sb + p.off_ones, &tm_ones, bar_c, 0, 0);
+            if (!FP8) tma_load_2d(sb + p.off_ones, &tm_ones, bar_c, 0, 0);
             int it = 0;
             for (int64_t t = q; t < p.tiles; t += tstride, ++it) {
                 const int s = it % XSTAGES;
                 const uint32_t ph = (uint32_t)(it / XSTAGES) & 1u;
                 if (!mbar_wait(bar_xempty(s), ph ^ 1u, abort_flag, p.err, 1ull)) break;
-                mbar_expect_tx(bar_xfull(s), p.x_stage_bytes);
+                mbar_expect_tx(bar_xfull(s), p.x_stage_bytes + (FP8 ? XAUG_BYTES : 0u));
                 for (int a = 0; a < p.n_atoms; a++)
                     tma_load_2d(sb + p.off_x + (uint32_t)s * p.x_stage_bytes + (uint32_t)a * X_ATOM_BYTES, &tm_x,
-                                bar_xfull(s), a * 64, (int)(t * BM));
+                                bar_xfull(s), a * (FP8 ? 128 : 64), (int)(t * BM));
+                if (FP8)
+                    tma_load_2d(sb + p.off_xaug + (uint32_t)s * XAUG_BYTES, &tm_ones, bar_xfull(s), 0, (int)(t * BM));
             }
             // Drain: every issued X load must land before the CTA can exit.
             const int issued = it;
@@ -469,10 +488,14 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                             for (int kk = 0; kk < 4; kk++) {
                                 const uint64_t ad = sdesc(xs + (uint32_t)a * X_ATOM_BYTES + kk * 32u, 1024u, LAYOUT_SW128);
                                 const uint64_t bd = sdesc(cs + (uint32_t)a * p.c_atom_bytes + kk * 32u, 1024u, LAYOUT_SW128);
-                                mma_bf16(dt, ad, bd, (a | kk) != 0 ? 1u : 0u);
+                                if (FP8)
+                                    mma_fp8(dt, ad, bd, (a | kk) != 0 ? 1u : 0u);
+                                else
+                                    mma_bf16(dt, ad, bd, (a | kk) != 0 ? 1u : 0u);
                             }
                         }
-                        mma_bf16(dt, sdesc(sb + p.off_ones, 256u, LAYOUT_SW32),
+                        const uint32_t aug_a = FP8 ? sb + p.off_xaug + (uint32_t)s * XAUG_BYTES : sb + p.off_ones;
+                        mma_bf16(dt, sdesc(aug_a, 256u, LAYOUT_SW32),
                                  sdesc(sb + p.off_aug + (uint32_t)b * BN * 32u, 256u, LAYOUT_SW32), 1u);
                         mma_commit(bar_afull(buf));
                     }
@@ -498,6 +521,13 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         for (int64_t t = q; t < p.tiles; t += tstride) {
             uint32_t R1 = 0u, R2 = 0u, U = 0u;
             int I1 = -1, I2 = -1;
+            float cg = cgrid, ul = ulp;
+            if (FP8) {
+                const int64_t rrow = t * BM + row_local;
+                const float rs = rrow < p.n ? p.rowscale[rrow] : 1.f;
+                cg = cgrid * rs;
+                ul = ulp * rs;
+            }
             for (int b = 0; b < p.nblocks; b++, item++) {
                 const int buf = (int)(item & 1u);
                 const uint32_t aph = (item >> 1) & 1u;
@@ -517,9 +547,9 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                 }
                 uint32_t b1, b2, bu;
                 if (half == 0)
-                    rank_half<0>(col, cgrid, ulp, b1, b2, bu);
+                    rank_half<0>(col, cg, ul, b1, b2, bu);
                 else
-                    rank_half<1>(col, cgrid, ulp, b1, b2, bu);
+                    rank_half<1>(col, cg, ul, b1, b2, bu);
                 tc_fence_before();
                 __syncwarp();
                 if (lane == 0) mbar_arrive(bar_aempty(buf));
@@ -554,6 +584,13 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         for (int64_t t = q; t < p.tiles; t += tstride) {
             uint32_t R[4] = {0u, 0u, 0u, 0u}, U = 0u;
             int I[4] = {-1, -1, -1, -1};
+            float cg = cgrid, ul = ulp;
+            if (FP8) {
+                const int64_t rrow = t * BM + row_local;
+                const float rs = rrow < p.n ? p.rowscale[rrow] : 1.f;
+                cg = cgrid * rs;
+                ul = ulp * rs;
+            }
             for (int b = 0; b < p.nblocks; b++, item++) {
                 const int buf = (int)(item & 1u);
                 const uint32_t aph = (item >> 1) & 1u;
@@ -562,7 +599,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                 tc_fence_after();
                 const uint32_t col = lane_addr + (uint32_t)buf * BN + (uint32_t)half * 128u;
                 uint32_t K[4], ku;
-                rank_half4(col, cgrid, ulp, K, ku);
+                rank_half4(col, cg, ul, K, ku);
                 tc_fence_before();
                 __syncwarp();
                 if (lane == 0) mbar_arrive(bar_aempty(buf));
@@ -628,14 +665,15 @@ PFN_cuTensorMapEncodeTiled_v12000 get_encode(Ctx &ctx) {
 }
 
 void encode_2d(Ctx &ctx, void *out, const void *ptr, uint64_t inner, uint64_t outer, uint64_t row_bytes,
-               uint32_t box_inner, uint32_t box_outer, CUtensorMapSwizzle swz) {
+               uint32_t box_inner, uint32_t box_outer, CUtensorMapSwizzle swz,
+               CUtensorMapDataType dt = CU_TENSOR_MAP_DATA_TYPE_BFLOAT16) {
     auto enc = get_encode(ctx);
     CUtensorMap m;
     cuuint64_t dims[2] = {inner, outer};
     cuuint64_t strides[1] = {row_bytes};
     cuuint32_t box[2] = {box_inner, box_outer};
     cuuint32_t estr[2] = {1, 1};
-    CUresult r = enc(&m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(ptr), dims, strides, box, estr,
+    CUresult r = enc(&m, dt, 2, const_cast<void *>(ptr), dims, strides, box, estr,
                      CU_TENSOR_MAP_INTERLEAVE_NONE, swz, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) {
@@ -650,17 +688,20 @@ constexpr size_t SMEM_LIMIT = 227 * 1024;
 
 }  // namespace
 
-void plan_tc(Ctx &ctx, MixedPlan &mp, int64_t n, int d, int k) {
+void plan_tc(Ctx &ctx, MixedPlan &mp, int64_t n, int d, int k, bool fp8) {
     mp.n = n;
     mp.d = d;
     mp.k = k;
-    mp.d_pad = (d + 63) / 64 * 64;
-    const int n_atoms = mp.d_pad / 64;
+    mp.fp8 = fp8;
+    const int per_atom = fp8 ? 128 : 64;  // elements per 128-byte swizzle atom
+    mp.d_pad = (d + per_atom - 1) / per_atom * per_atom;
+    const int n_atoms = mp.d_pad / per_atom;
     const size_t x_stage = (size_t)n_atoms * X_ATOM_BYTES;
-    const size_t fixed = 1024 + XSTAGES * x_stage + ONES_BYTES + MERGE_BYTES + BAR_BYTES;
+    const size_t fixed = 1024 + XSTAGES * x_stage + (fp8 ? XSTAGES * XAUG_BYTES : ONES_BYTES) + MERGE_BYTES + BAR_BYTES;
     const size_t per_centre = (size_t)n_atoms * 128 + 32;
     if (fixed + BN * per_centre > SMEM_LIMIT) {
-        set_error("the resident-slice tensor-core kernel supports d <= 192 (got %d)", d);
+        set_error("the resident-slice tensor-core kernel supports d <= %d for this precision (got %d)",
+                  fp8 ? 384 : 192, d);
         fail(FK_ERR_UNSUPPORTED);
     }
     const int kp_max = (int)((SMEM_LIMIT - fixed) / per_centre) / BN * BN;
@@ -674,7 +715,7 @@ void plan_tc(Ctx &ctx, MixedPlan &mp, int64_t n, int d, int k) {
     if ((int64_t)mp.ctas_per_part > mp.tiles) mp.ctas_per_part = (int)mp.tiles;
     mp.grid = mp.ctas_per_part * mp.parts;
     mp.smem = fixed + (size_t)mp.kp * per_centre;
-    mp.tm_x_ptr = mp.tm_c_ptr = mp.tm_aug_ptr = mp.tm_x2_ptr = nullptr;
+    mp.tm_x_ptr = mp.tm_c_ptr = mp.tm_aug_ptr = mp.tm_x2_ptr = mp.tm_xaug_ptr = mp.tm_xaug2_ptr = nullptr;
     if (!mp.ones) {
         uint16_t h[BM * 16];
         for (int r = 0; r < BM; r++)
@@ -687,29 +728,42 @@ void plan_tc(Ctx &ctx, MixedPlan &mp, int64_t n, int d, int k) {
 
 void launch_tc_assign(Ctx &ctx, MixedPlan &mp, const void *xb, const void *cb, const void *caug, Top2 *out,
                       DevScalars *sc, const MixedStats *stats, float *dump, Top4 *out4,
-                      const unsigned long long *n_dev) {
-    // the second pass reads its own gathered rows: a separate tensor map
+                      const unsigned long long *n_dev, const void *xaug, const float *rowscale) {
+    const bool fp8 = mp.fp8;
+    const CUtensorMapDataType dt = fp8 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
+    const uint64_t es = fp8 ? 1 : 2;
+    const uint32_t box_in = fp8 ? 128 : 64;
+    // the second pass reads its own gathered rows: separate tensor maps
     unsigned char *tmx = out4 ? mp.tm_x2 : mp.tm_x;
     const void *&tmx_ptr = out4 ? mp.tm_x2_ptr : mp.tm_x_ptr;
     if (tmx_ptr != xb) {
-        encode_2d(ctx, tmx, xb, (uint64_t)mp.d_pad, (uint64_t)mp.n, (uint64_t)mp.d_pad * 2, 64, BM,
-                  CU_TENSOR_MAP_SWIZZLE_128B);
+        encode_2d(ctx, tmx, xb, (uint64_t)mp.d_pad, (uint64_t)mp.n, (uint64_t)mp.d_pad * es, box_in, BM,
+                  CU_TENSOR_MAP_SWIZZLE_128B, dt);
         tmx_ptr = xb;
     }
     if (mp.tm_c_ptr != cb) {
-        encode_2d(ctx, mp.tm_c, cb, (uint64_t)mp.d_pad, (uint64_t)mp.k_pad, (uint64_t)mp.d_pad * 2, 64, BN,
-                  CU_TENSOR_MAP_SWIZZLE_128B);
+        encode_2d(ctx, mp.tm_c, cb, (uint64_t)mp.d_pad, (uint64_t)mp.k_pad, (uint64_t)mp.d_pad * es, box_in, BN,
+                  CU_TENSOR_MAP_SWIZZLE_128B, dt);
         mp.tm_c_ptr = cb;
     }
     if (mp.tm_aug_ptr != caug) {
         encode_2d(ctx, mp.tm_aug, caug, 16, (uint64_t)mp.k_pad, 32, 16, BN, CU_TENSOR_MAP_SWIZZLE_32B);
         mp.tm_aug_ptr = caug;
     }
+    unsigned char *tmo = mp.tm_ones;
+    if (fp8) {
+        tmo = out4 ? mp.tm_xaug2 : mp.tm_xaug;
+        const void *&pp = out4 ? mp.tm_xaug2_ptr : mp.tm_xaug_ptr;
+        if (pp != xaug) {
+            encode_2d(ctx, tmo, xaug, 16, (uint64_t)mp.n, 32, 16, BM, CU_TENSOR_MAP_SWIZZLE_32B);
+            pp = xaug;
+        }
+    }
     TcParams p;
     memset(&p, 0, sizeof(p));
     p.n = mp.n;
     p.tiles = mp.tiles;
-    p.n_atoms = mp.d_pad / 64;
+    p.n_atoms = (int)((uint64_t)mp.d_pad * es / 128);
     p.kp = mp.kp;
     p.nblocks = mp.nblocks;
     p.parts = mp.parts;
@@ -720,15 +774,17 @@ void launch_tc_assign(Ctx &ctx, MixedPlan &mp, const void *xb, const void *cb, c
     p.off_x = p.off_c + (uint32_t)p.n_atoms * p.c_atom_bytes;
     p.off_aug = p.off_x + XSTAGES * p.x_stage_bytes;
     p.off_ones = p.off_aug + (uint32_t)mp.kp * 32u;
-    p.off_merge = p.off_ones + ONES_BYTES;
+    p.off_xaug = p.off_ones;
+    p.off_merge = p.off_ones + (fp8 ? XSTAGES * XAUG_BYTES : ONES_BYTES);
     p.off_bar = p.off_merge + MERGE_BYTES;
-    p.c_tx_bytes = (uint32_t)p.n_atoms * p.c_atom_bytes + (uint32_t)mp.kp * 32u + ONES_BYTES;
+    p.c_tx_bytes = (uint32_t)p.n_atoms * p.c_atom_bytes + (uint32_t)mp.kp * 32u + (fp8 ? 0u : ONES_BYTES);
     p.out = out;
     p.out4 = out4;
     p.n_dev = n_dev;
     p.out_stride = mp.n;
     p.err = &sc->error_word;
     p.stats = stats;
+    p.rowscale = rowscale;
     p.dump = dump;
     const size_t smem = (size_t)p.off_bar + BAR_BYTES + 1024;
     if (smem > SMEM_LIMIT) {
@@ -736,16 +792,15 @@ void launch_tc_assign(Ctx &ctx, MixedPlan &mp, const void *xb, const void *cb, c
         fail(FK_ERR_UNSUPPORTED);
     }
     const CUtensorMap *tx = (const CUtensorMap *)tmx, *tcm = (const CUtensorMap *)mp.tm_c,
-                      *ta = (const CUtensorMap *)mp.tm_aug, *to = (const CUtensorMap *)mp.tm_ones;
-    if (out4) {
-        FK_CUDA(cudaFuncSetAttribute((const void *)tc_assign_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)smem));
-        tc_assign_kernel<4><<<mp.grid, NTHREADS, smem, ctx.stream>>>(*tx, *tcm, *ta, *to, p);
-    } else {
-        FK_CUDA(cudaFuncSetAttribute((const void *)tc_assign_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)smem));
-        tc_assign_kernel<2><<<mp.grid, NTHREADS, smem, ctx.stream>>>(*tx, *tcm, *ta, *to, p);
-    }
+                      *ta = (const CUtensorMap *)mp.tm_aug, *to = (const CUtensorMap *)tmo;
+    auto go = [&](auto kern) {
+        FK_CUDA(cudaFuncSetAttribute((const void *)kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        kern<<<mp.grid, NTHREADS, smem, ctx.stream>>>(*tx, *tcm, *ta, *to, p);
+    };
+    if (out4)
+        fp8 ? go(tc_assign_kernel<4, true>) : go(tc_assign_kernel<4, false>);
+    else
+        fp8 ? go(tc_assign_kernel<2, true>) : go(tc_assign_kernel<2, false>);
     FK_LAUNCH_CHECK();
 }
 

@@ -14,7 +14,8 @@ and FerroError (ferrolearn-core/src/error.rs:30-91) as exceptions.
 Two builder methods have no reference counterpart: with_init_centers (the
 reference always seeds with k-means++ from rand's StdRng, which cannot be
 reproduced here, so parity runs inject the initial centres) and
-with_precision (the mixed BF16 / FP32 contractions with FP64 re-check).
+with_precision (the mixed BF16 / FP8 tensor-core contractions with exact
+re-check).
 
 F is chosen with dtype: "f64" (KMeans<f64>), "f32" (KMeans<f32>) or
 "f32x64" (KMeans<f64> semantics on X stored as f32, each value widened
@@ -29,10 +30,10 @@ from . import _native
 
 PLAIN = 0
 MIXED_BF16 = 1
-MIXED_FP32 = 3
+MIXED_FP8 = 2
 
-_PREC_NAMES = {"plain": PLAIN, "bf16": MIXED_BF16, "mixed_bf16": MIXED_BF16, "fp32": MIXED_FP32,
-               "mixed_fp32": MIXED_FP32}
+_PREC_NAMES = {"plain": PLAIN, "bf16": MIXED_BF16, "mixed_bf16": MIXED_BF16, "fp8": MIXED_FP8,
+               "mixed_fp8": MIXED_FP8}
 
 
 class FerroError(Exception):

@@ -17,6 +17,14 @@ can run the same distribution at a size the CPU oracle finishes quickly.
                       covariance A A^T, A_ij ~ N(0, 0.3^2) (128x128), centres
                       U[-15,15]^128; init = first k rows of a seeded
                       permutation; 50 iterations (tol 0).
+  bisector_4096x256   n=8,000,000 d=256 k=4096, X stored f32: 4096 blobs,
+                      std 1.0, centres U[-30,30]^256, plus 10% of the rows
+                      placed on the perpendicular bisector of two seeded
+                      centres (equidistant in real arithmetic; f32 storage
+                      leaves them within rounding of a tie); init = first k
+                      rows of a seeded permutation; 20 iterations (tol 0);
+                      then predict on 2,000,000 fresh rows of the same
+                      mixture.
 """
 import numpy as np
 
@@ -71,3 +79,44 @@ def anisotropic_1024x128(scale=1.0, seed=0, k=1024, d=128):
     init = _perm_init(x, k, seed + 1).astype(np.float64)
     return dict(x=x, k=k, init=init, max_iter=50, tol=0.0, n_init=1, name="anisotropic_1024x128",
                 desc=f"n={n} d={d} k={k}, X f32, 1024 anisotropic blobs (A A^T, A~N(0,0.3^2)), 50 iterations")
+
+
+def _bisector_rows(centres, m, rng):
+    """m rows on the perpendicular bisector of two seeded centres each:
+    (a + b) / 2 + u with u a N(0, 1) vector projected orthogonal to b - a."""
+    k, d = centres.shape
+    a = rng.integers(0, k, size=m)
+    b = (a + 1 + rng.integers(0, k - 1, size=m)) % k
+    ca, cb = centres[a].astype(np.float64), centres[b].astype(np.float64)
+    w = cb - ca
+    u = rng.standard_normal(size=(m, d))
+    u -= ((u * w).sum(1) / (w * w).sum(1))[:, None] * w
+    return 0.5 * (ca + cb) + u
+
+
+def _bisector_mixture(n, centres, rng, frac=0.1, chunk=1 << 20):
+    k, d = centres.shape
+    x = np.empty((n, d), dtype=np.float32)
+    m_bis = int(round(frac * n))
+    lab = rng.integers(0, k, size=n - m_bis)
+    for lo in range(0, n - m_bis, chunk):
+        hi = min(n - m_bis, lo + chunk)
+        x[lo:hi] = centres[lab[lo:hi]] + rng.standard_normal(size=(hi - lo, d), dtype=np.float32)
+    for lo in range(n - m_bis, n, chunk):
+        hi = min(n, lo + chunk)
+        x[lo:hi] = _bisector_rows(centres, hi - lo, rng)
+    return np.ascontiguousarray(x[rng.permutation(n)])
+
+
+def bisector_4096x256(scale=1.0, seed=0, k=4096, d=256, predict_scale=None):
+    n = max(k, int(round(8_000_000 * scale)))
+    rng = np.random.default_rng(seed)
+    centres = rng.uniform(-30.0, 30.0, size=(k, d)).astype(np.float32)
+    x = _bisector_mixture(n, centres, rng)
+    init = _perm_init(x, k, seed + 1).astype(np.float64)
+    ps = scale if predict_scale is None else predict_scale
+    n_pred = max(1, int(round(2_000_000 * ps)))
+    x_pred = _bisector_mixture(n_pred, centres, np.random.default_rng(seed + 2))
+    return dict(x=x, k=k, init=init, max_iter=20, tol=0.0, n_init=1, x_predict=x_pred, name="bisector_4096x256",
+                desc=f"n={n} d={d} k={k}, X f32, 4096 blobs std 1 + 10% bisector rows, 20 iterations, "
+                     f"predict on {n_pred} rows")

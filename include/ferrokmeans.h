@@ -44,12 +44,13 @@ typedef enum fk_status {
  *                           a derived per-row error bound; rows whose top-2
  *                           margin is inside the bound are re-scored exactly
  *                           in FP64 direct form. F = f64 only.
- *  FK_PRECISION_MIXED_FP32  FP32 CUDA-core contraction with the same bound
- *                           and FP64 re-check. F = f64 only.               */
+ *  FK_PRECISION_MIXED_FP8   FP8 E4M3 tensor-core contraction (per-row
+ *                           power-of-two scales) with the same bound and
+ *                           exact re-check; X stored as f32 (_f32x64).      */
 typedef enum fk_precision {
     FK_PRECISION_PLAIN = 0,
     FK_PRECISION_MIXED_BF16 = 1,
-    FK_PRECISION_MIXED_FP32 = 3
+    FK_PRECISION_MIXED_FP8 = 2
 } fk_precision;
 
 /* Hyper-parameters of KMeans<F> (kmeans.rs:55-68), plus the explicit-init
@@ -218,14 +219,16 @@ fk_status fk_debug_measure_peaks(fk_ctx *ctx, double *out);
 
 /* Diagnostics for the tests (no reference counterpart): one BF16 tensor-core
  * assignment pass of x (n*d f32, device memory) against c (k*d f64, device
- * memory). Returns the raw FP32 accumulators of the first 128-row tile of the
- * first centre slice (dump: 128 x kp), the BF16 operands (xb: first 128 rows
- * x d_pad; cb: k_pad x d_pad; aug: k_pad x 16), the per-slice top-2 records
+ * memory), precision FK_PRECISION_MIXED_BF16 or _FP8. Returns the raw FP32
+ * accumulators of the first 128-row tile of the first centre slice (dump:
+ * 128 x kp), the quantised operands (xq: first 128 rows x d_pad elements;
+ * cq: k_pad x d_pad; aug: k_pad x 16 BF16; xaug (FP8): first 128 rows x 16
+ * BF16), the per-slice top-2 records
  * (top: parts x n x 16 bytes) and the plan {d_pad, kp, parts, k_pad, grid,
  * error word}. Buffers are sized by the caller from the plan's upper bounds. */
 fk_status fk_debug_tc_probe(fk_ctx *ctx, const float *x_dev, int64_t n, int64_t d, const double *c_dev,
-                            int64_t k, float *dump, uint16_t *xb, uint16_t *cb, uint16_t *aug, void *top,
-                            int32_t *plan);
+                            int64_t k, int32_t precision, float *dump, void *xq, void *cq, uint16_t *aug,
+                            uint16_t *xaug, void *top, int32_t *plan);
 
 #ifdef __cplusplus
 }

@@ -83,3 +83,17 @@ def test_predict_transform_shape_mismatch():
 def test_mixed_precision_rejected_for_f32_semantics():
     with pytest.raises(F.Unsupported):
         F.KMeans(2, dtype="f32").with_precision("bf16").fit(np.ones((4, 2), dtype=np.float32))
+
+
+@pytest.mark.parametrize("dtype", ["f32", "f64"])
+def test_fp8_needs_f32_storage_with_f64_semantics(dtype):
+    x = np.ones((4, 2), dtype=np.float32 if dtype == "f32" else np.float64)
+    with pytest.raises(F.Unsupported):
+        F.KMeans(2, dtype=dtype).with_precision("fp8").fit(x)
+    with pytest.raises(F.Unsupported):
+        F.lloyd_step(x, np.ones((2, 2)), dtype=dtype, precision="fp8")
+
+
+def test_unknown_precision_code_rejected():
+    with pytest.raises(F.Unsupported):
+        F.KMeans(2, dtype="f32x64").with_precision(3).fit(np.ones((4, 2), dtype=np.float32))

@@ -38,35 +38,58 @@ def _bf16_to_f32(u16):
     return (u16.astype(np.uint32) << 16).view(np.float32)
 
 
-def _probe(x32, c64):
+def _e4m3_to_f64(u8):
+    """E4M3 (1 sign, 4 exponent bits with bias 7, 3 mantissa bits; no
+    infinities, S.1111.111 is NaN) decoded exactly."""
+    u = u8.astype(np.int64)
+    e = (u >> 3) & 15
+    m = (u & 7).astype(np.float64)
+    v = np.where(e == 0, m / 8.0 * 2.0 ** -6, (1.0 + m / 8.0) * np.exp2(e.astype(np.float64) - 7.0))
+    v = np.where((e == 15) & ((u & 7) == 7), np.nan, v)
+    return np.where(u & 0x80, -v, v)
+
+
+def _probe(x32, c64, precision="bf16"):
     torch = pytest.importorskip("torch")
     ctx = F.default_context()
     n, d = x32.shape
     k = c64.shape[0]
+    fp8 = precision == "fp8"
     xd = torch.from_numpy(np.ascontiguousarray(x32)).cuda()
     cd = torch.from_numpy(np.ascontiguousarray(c64)).cuda()
-    d_pad = (d + 63) // 64 * 64
+    per_atom = 128 if fp8 else 64
+    d_pad = (d + per_atom - 1) // per_atom * per_atom
     kmax = (k + 255) // 256 * 256 * 2 + 512
+    et = np.uint8 if fp8 else np.uint16
     dump = np.zeros(128 * kmax, dtype=np.float32)
-    xb = np.zeros(128 * d_pad, dtype=np.uint16)
-    cb = np.zeros(kmax * d_pad, dtype=np.uint16)
+    xq = np.zeros(128 * d_pad, dtype=et)
+    cq = np.zeros(kmax * d_pad, dtype=et)
     aug = np.zeros(kmax * 16, dtype=np.uint16)
+    xaug = np.zeros(128 * 16, dtype=np.uint16)
     top = np.zeros(n * 8 * 8, dtype=np.float32)
     plan = np.zeros(8, dtype=np.int32)
+    vp = lambda a: a.ctypes.data_as(C.c_void_p)  # noqa: E731
     st = _native.lib().fk_debug_tc_probe(ctx.handle, C.c_void_p(xd.data_ptr()), n, d, C.c_void_p(cd.data_ptr()), k,
-                                         dump.ctypes.data_as(C.c_void_p), xb.ctypes.data_as(C.c_void_p),
-                                         cb.ctypes.data_as(C.c_void_p), aug.ctypes.data_as(C.c_void_p),
-                                         top.ctypes.data_as(C.c_void_p), plan.ctypes.data_as(C.c_void_p))
+                                         F.MIXED_FP8 if fp8 else F.MIXED_BF16, vp(dump), vp(xq), vp(cq), vp(aug),
+                                         vp(xaug), vp(top), vp(plan))
     assert st == 0, _native.last_error()
-    d_pad, kp, parts, k_pad, grid, err = plan[:6]
-    assert err == 0
+    d_pad_dev, kp, parts, k_pad, grid, err = plan[:6]
+    assert err == 0 and d_pad_dev == d_pad
     rows = min(n, 128)
-    xbf = _bf16_to_f32(xb[: rows * d_pad]).reshape(rows, d_pad).astype(np.float64)
-    cbf = _bf16_to_f32(cb[: k_pad * d_pad]).reshape(k_pad, d_pad).astype(np.float64)
+    dec = _e4m3_to_f64 if fp8 else (lambda u: _bf16_to_f32(u).astype(np.float64))
+    xqf = dec(xq[: rows * d_pad]).reshape(rows, d_pad)
+    cqf = dec(cq[: k_pad * d_pad]).reshape(k_pad, d_pad)
     augf = _bf16_to_f32(aug[: k_pad * 16]).reshape(k_pad, 16).astype(np.float64)
+    if fp8:
+        xaugf = _bf16_to_f32(xaug[: rows * 16]).reshape(rows, 16).astype(np.float64)
+    else:
+        xaugf = np.zeros((rows, 16))
+        xaugf[:, :3] = 1.0
     acc = dump[: 128 * kp].reshape(128, kp)[:rows]
     recs = top[: parts * n * 8].view(np.uint32).reshape(parts, n, 8)
-    return dict(acc=acc, xb=xbf, cb=cbf, aug=augf, kp=kp, parts=parts, k_pad=k_pad, recs=recs)
+    scores = xqf @ cqf.T + xaugf @ augf.T  # exact in f64: the accumulator units of each row
+    return dict(acc=acc, xq=xqf, cq=cqf, aug=augf, xaug=xaugf, scores=scores, kp=kp, parts=parts, k_pad=k_pad,
+                recs=recs)
 
 
 def _aniso(n, d, k, seed):
@@ -77,28 +100,42 @@ def _aniso(n, d, k, seed):
     return x.astype(np.float32), cen
 
 
-@pytest.mark.parametrize("n,d,k", [(300, 128, 300), (200, 64, 1024), (150, 16, 40), (260, 128, 1024), (129, 100, 7)])
-def test_tc_accumulators_exact(n, d, k):
+PRECISIONS = ["bf16", "fp8"]
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+@pytest.mark.parametrize("n,d,k", [(300, 128, 300), (200, 64, 1024), (150, 16, 40), (260, 128, 1024), (129, 100, 7),
+                                   (140, 256, 600)])
+def test_tc_accumulators_exact(n, d, k, precision):
+    if precision == "bf16" and d > 192:
+        pytest.skip("the BF16 kernel keeps d <= 192")
     x32, cen = _aniso(n, d, k, seed=n + d + k)
     c = x32[np.random.default_rng(0).choice(n, size=min(k, n), replace=False)].astype(np.float64)
     if c.shape[0] < k:
         c = np.concatenate([c, cen[: k - c.shape[0]]])
-    r = _probe(x32, c)
+    r = _probe(x32, c, precision)
     kp = r["kp"]
-    ref = r["xb"] @ r["cb"][:kp].T + r["aug"][:kp].sum(1)[None, :]
+    ref = r["scores"][:, :kp]
     big = np.abs(ref).max()
-    err = np.abs(r["acc"].astype(np.float64) - ref).max()
-    assert err <= 1e-5 * big, (err, big)
+    err = np.abs(r["acc"].astype(np.float64) - ref)
+    assert err.max() <= 1e-5 * big, (err.max(), big)
+    # the accumulation-error model of the re-check bound: (d_pad + 32) 2^-22
+    # times (||xq|| max ||cq|| + the augmentation term), row by row
+    d_pad = r["xq"].shape[1]
+    xn = np.linalg.norm(r["xq"], axis=1)[:, None]
+    chn = np.linalg.norm(r["cq"][:kp], axis=1).max()
+    augv = np.abs(r["xaug"]) @ np.abs(r["aug"][:kp]).T
+    bound = (d_pad + 32) * 2.0 ** -22 * (xn * chn + augv)
+    assert np.all(err <= bound), (err / bound).max()
 
 
+@pytest.mark.parametrize("precision", PRECISIONS)
 @pytest.mark.parametrize("n,d,k", [(1000, 128, 1024), (700, 64, 300), (333, 32, 5)])
-def test_tc_top2_records(n, d, k):
+def test_tc_top2_records(n, d, k, precision):
     x32, cen = _aniso(n, d, k, seed=7 + d)
     c = cen.astype(np.float64)
-    r = _probe(x32, c)
+    r = _probe(x32, c, precision)
     kp, parts = r["kp"], r["parts"]
-    # full exact scores from the device operands (all rows)
-    torch = pytest.importorskip("torch")  # noqa: F841
     recs = r["recs"]
     v1 = recs[..., 0].view(np.float32)
     u3 = recs[..., 2].view(np.float32)
@@ -106,8 +143,8 @@ def test_tc_top2_records(n, d, k):
     i2 = recs[..., 5].view(np.int32)
     # the best over all slices must be a centre whose exact score is within the
     # truncation + accumulation slack of the true maximum (rows of the first tile)
-    rows = r["xb"].shape[0]
-    scores = r["xb"] @ r["cb"].T + r["aug"].sum(1)[None, :]
+    scores = r["scores"]
+    rows = scores.shape[0]
     best = scores[:, :k].max(1)
     for p in range(parts):
         lo, hi = p * kp, min(k, (p + 1) * kp)
@@ -115,23 +152,44 @@ def test_tc_top2_records(n, d, k):
             continue
         sl = scores[:, lo:hi]
         m = sl.max(1)
-        assert np.all(np.abs(v1[p, :rows] - m) <= 2 ** -14 * np.abs(m) + 1e-5 * best)
+        tol = 2 ** -14 * np.abs(m) + 1e-5 * best
+        assert np.all(np.abs(v1[p, :rows] - m) <= tol)
         picked = sl[np.arange(rows), i1[p, :rows] - lo]
-        assert np.all(m - picked <= 2 ** -14 * np.abs(m) + 1e-5 * best)
+        assert np.all(m - picked <= tol)
         # u3 bounds every score of the slice other than the two kept ones
         rest = sl.copy()
         rest[np.arange(rows), i1[p, :rows] - lo] = -np.inf
         rest[np.arange(rows), i2[p, :rows] - lo] = -np.inf
-        assert np.all(rest.max(1) <= u3[p, :rows] + 2 ** -14 * np.abs(m) + 1e-5 * best)
+        assert np.all(rest.max(1) <= u3[p, :rows] + tol)
 
 
-@pytest.mark.parametrize("n,d,k", [(4096, 128, 1024), (5000, 64, 100), (3000, 16, 9), (2500, 100, 300)])
-def test_mixed_steps_match_fp64_oracle(n, d, k):
+def test_fp8_operands_are_scaled_roundings():
+    # each row's E4M3 values times its power-of-two scale approximate x - mu
+    # within E4M3's relative rounding (2^-4) or its subnormal step
+    x32, cen = _aniso(256, 256, 64, seed=2)
+    r = _probe(x32, cen.astype(np.float64), "fp8")
+    xq, xaug = r["xq"], r["xaug"]
+    s = 1.0 / xaug[:, 0]  # the augmentation row holds 2^-sh
+    assert np.all(np.log2(s) == np.round(np.log2(s)))
+    deq = xq[:, :256] * s[:, None]
+    mu = x32.astype(np.float64).mean(0)  # the device centres by the f32 mean of the same rows
+    t = x32[:128].astype(np.float64) - mu
+    assert np.all(np.abs(xq).max(1) <= 256) and np.all(np.abs(xq).max(1) >= 128)
+    # half an E4M3 ulp in the row's top binade is 1/16 of the row's max |t|
+    assert np.all(np.abs(deq - t) <= np.abs(t).max(1, keepdims=True) / 16 * 1.001 + 1e-4)
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+@pytest.mark.parametrize("n,d,k", [(4096, 128, 1024), (5000, 64, 100), (3000, 16, 9), (2500, 100, 300),
+                                   (3000, 256, 700)])
+def test_mixed_steps_match_fp64_oracle(n, d, k, precision):
+    if precision == "bf16" and d > 192:
+        pytest.skip("the BF16 kernel keeps d <= 192")
     x32, _ = _aniso(n, d, k, seed=11 * d + k)
     x64 = x32.astype(np.float64)
     c = x64[np.random.default_rng(1).choice(n, size=k, replace=False)].copy()
     for _ in range(3):
-        gl, gc, gi, gs, rep = F.lloyd_step(x32, c, dtype="f32x64", precision="bf16")
+        gl, gc, gi, gs, rep = F.lloyd_step(x32, c, dtype="f32x64", precision=precision)
         ol, oc, oi, os_ = O.lloyd_step(x64, c)
         assert np.array_equal(gl, ol)
         assert _close(gc, oc)
@@ -152,7 +210,8 @@ def test_mixed_fit_anisotropic_small():
     assert abs(g.inertia() - o["inertia"]) <= INERTIA_RTOL_MIXED * o["inertia"]
 
 
-def test_mixed_exact_ties_and_nan_rows_are_rechecked():
+@pytest.mark.parametrize("precision", PRECISIONS)
+def test_mixed_exact_ties_and_nan_rows_are_rechecked(precision):
     rng = np.random.default_rng(5)
     d, k = 64, 40
     c = rng.uniform(-10, 10, size=(k, d))
@@ -166,7 +225,7 @@ def test_mixed_exact_ties_and_nan_rows_are_rechecked():
     x[-1, 5] = np.nan
     x32 = x.astype(np.float32)
     x64 = x32.astype(np.float64)
-    gl, gc, gi, gs, rep = F.lloyd_step(x32, c, dtype="f32x64", precision="bf16")
+    gl, gc, gi, gs, rep = F.lloyd_step(x32, c, dtype="f32x64", precision=precision)
     ol, oc, oi, os_ = O.lloyd_step(x64, c)
     assert np.array_equal(gl, ol)
     assert _close(gc, oc)
@@ -174,7 +233,8 @@ def test_mixed_exact_ties_and_nan_rows_are_rechecked():
     assert rep["rows_full_rescan"] >= 1
 
 
-def test_fixed_point_sums_handle_extremes():
+@pytest.mark.parametrize("precision", PRECISIONS)
+def test_fixed_point_sums_handle_extremes(precision):
     # tiny, huge, signed zero, infinities: the update must follow IEEE f64
     # summation of the f32 values (here all sums are exact in f64)
     x = np.zeros((8, 4), dtype=np.float32)
@@ -183,16 +243,17 @@ def test_fixed_point_sums_handle_extremes():
     x[:, 2] = [np.inf, -np.inf, 0, 0, 0, 0, 0, 0]
     x[:, 3] = -0.0
     c = np.zeros((1, 4))
-    gl, gc, gi, gs, rep = F.lloyd_step(x, c, dtype="f32x64", precision="bf16")
+    gl, gc, gi, gs, rep = F.lloyd_step(x, c, dtype="f32x64", precision=precision)
     ol, oc, oi, os_ = O.lloyd_step(x.astype(np.float64), c)
     assert np.array_equal(gl, ol)
     assert np.array_equal(gc, oc, equal_nan=True)
 
 
-def test_mixed_predict_matches_oracle():
+@pytest.mark.parametrize("precision", [F.MIXED_BF16, F.MIXED_FP8])
+def test_mixed_predict_matches_oracle(precision):
     x32, cen = _aniso(6000, 128, 500, seed=3)
     fitted = F.FittedKMeans(cen.astype(np.float64), np.zeros(6000, dtype=np.int64), 0.0, 0, "f32x64",
-                            precision=F.MIXED_BF16)
+                            precision=precision)
     assert np.array_equal(fitted.predict(x32), O.predict(cen, x32.astype(np.float64)))
 
 
@@ -214,7 +275,8 @@ def _equidistant_rows(c, ids, count, rng, spread=0.5):
     return np.array(rows)
 
 
-def test_mixed_multiway_ties_use_the_second_pass():
+@pytest.mark.parametrize("precision", PRECISIONS)
+def test_mixed_multiway_ties_use_the_second_pass(precision):
     # rows equidistant from three and from six centres: the first pass cannot
     # separate them, the top-4 second pass (or the exhaustive path for six)
     # must, and the labels must still be the FP64 oracle's
@@ -227,9 +289,26 @@ def test_mixed_multiway_ties_use_the_second_pass():
     x[300:360] = _equidistant_rows(c, [1, 2, 3, 4, 6, 7], 60, rng)
     x32 = x.astype(np.float32)
     x64 = x32.astype(np.float64)
-    gl, gc, gi, gs, rep = F.lloyd_step(x32, c, dtype="f32x64", precision="bf16")
+    gl, gc, gi, gs, rep = F.lloyd_step(x32, c, dtype="f32x64", precision=precision)
     ol, oc, oi, os_ = O.lloyd_step(x64, c)
     assert np.array_equal(gl, ol)
     assert _close(gc, oc)
     assert rep["rows_full_rescan"] >= 300
     assert rep["rows_fp64"] >= 100
+
+
+def test_fp8_bisector_fit_and_predict_match_fp64_oracle():
+    # the large-k FP8 workload's distribution at a size the oracle finishes
+    # quickly: 10% of the rows on bisectors of two centres
+    w = W.bisector_4096x256(scale=0.003, k=512)  # 24,000 rows, 6,000 to predict
+    x32, k = w["x"], w["k"]
+    g = F.KMeans(k, dtype="f32x64").with_precision("fp8").with_max_iter(3).with_tol(0.0).with_n_init(1) \
+        .with_init_centers(w["init"]).fit(x32)
+    o = O.fit(x32.astype(np.float64), k, max_iter=3, tol=0.0, n_init=1, init=w["init"][None])
+    assert np.array_equal(g.labels(), o["labels"])
+    assert _close(g.cluster_centers(), o["centers"])
+    assert g.n_iter() == o["n_iter"] == 3
+    assert abs(g.inertia() - o["inertia"]) <= INERTIA_RTOL_MIXED * o["inertia"]
+    assert g.report["rows_rechecked"] >= int(0.1 * x32.shape[0])  # every bisector row at least
+    xp = w["x_predict"]
+    assert np.array_equal(g.predict(xp), O.predict(g.cluster_centers(), xp.astype(np.float64)))
