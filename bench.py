@@ -16,8 +16,16 @@ so every iteration runs. A step is one Lloyd iteration over all n rows
   forms   bf16  = FK_PRECISION_MIXED_BF16 on the f32x64 entry point
                   (KMeans<f64> semantics, BF16 tcgen05 contraction + FP64
                   re-check); labels identical to the FP64 oracle.
+          fp8   = FK_PRECISION_MIXED_FP8, the same with an E4M3 contraction
+                  (per-row power-of-two scales).
           fp32  = plain KMeans<f32> (direct-form FP32 on CUDA cores).
           fp64  = plain KMeans<f64> on the widened X.
+
+Other workloads (--workload; parity cases of the same path, measured on
+request): bisector = n=8,000,000 d=256 k=4096 with 10% bisector rows, FP8,
+20 iterations, then predict on 2,000,000 fresh rows (reported as
+predict_rows_per_s); dirichlet = n=1,000,000 d=64 k=256, plain f32 / f64,
+k-means++ init on the GPU (timed separately as kpp_ms).
 
 --impl reference times the CPU restatement of the reference (oracle/, the
 reference is Rust and cannot be built here) on a bounded row sample of the
@@ -44,7 +52,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--form", default="auto", choices=["auto", "bf16", "fp32", "fp64"])
+    ap.add_argument("--form", default="auto", choices=["auto", "bf16", "fp8", "fp32", "fp64"])
+    ap.add_argument("--workload", default="anisotropic", choices=["anisotropic", "bisector", "dirichlet"])
     ap.add_argument("--scale", type=float, default=1.0, help="fraction of the full row count")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true")
@@ -119,9 +128,32 @@ class ClockSampler:
         return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def make_workload(scale):
+def make_workload(args):
     from ferrolearn_gb300 import workloads as W
-    return W.anisotropic_1024x128(scale=scale)
+    if args.workload == "bisector":
+        return W.bisector_4096x256(scale=args.scale)
+    if args.workload == "dirichlet":
+        return W.dirichlet_256x64(scale=args.scale, dtype=np.float32)
+    return W.anisotropic_1024x128(scale=args.scale)
+
+
+DEFAULT_FORM = {"anisotropic": "bf16", "bisector": "fp8", "dirichlet": "fp32"}
+
+
+def initial_centres(w, xd, ctx):
+    """The workload's initial centres, or k-means++ on the GPU (timed) where it
+    names none; returns (centres f64, ms of the k-means++ call or None)."""
+    if w["init"] is not None:
+        return w["init"], None
+    import torch
+
+    import ferrolearn_gb300 as F
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    c, _ = F.kmeans_plus_plus(xd, w["k"], seed=w.get("seed", 0), dtype="f32", ctx=ctx)
+    ms = (time.perf_counter() - t0) * 1e3
+    w["init"] = c.astype(np.float64)
+    return w["init"], ms
 
 
 def cpu_baseline(w, seconds, threads):
@@ -154,7 +186,9 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    w = make_workload(args.scale)
+    w = make_workload(args)
+    if w["init"] is None:
+        w["init"] = w["x"][np.random.default_rng(1).permutation(w["x"].shape[0])[: w["k"]]].astype(np.float64)
     threads = os.cpu_count() or 1
     from oracle import oracle as O
     x64 = w["x"].astype(np.float64)
@@ -197,31 +231,32 @@ def run_ours(args):
         dist.init_process_group("nccl")
     dev = torch.cuda.current_device()
     hbm, bf16, bf16s, peak_src = load_peaks()
-    w = make_workload(args.scale)
+    w = make_workload(args)
     x32 = w["x"]
     n, d = x32.shape
     k = w["k"]
-    form = args.form if args.form != "auto" else "bf16"
+    form = args.form if args.form != "auto" else DEFAULT_FORM[args.workload]
     stream = torch.cuda.Stream()
     ctx = F.Context(dev, stream=stream.cuda_stream)
-
-    def build_model(max_iter):
-        if form == "fp32":
-            m = F.KMeans(k, dtype="f32").with_init_centers(w["init"].astype(np.float32))
-        elif form == "fp64":
-            m = F.KMeans(k, dtype="f64").with_init_centers(w["init"])
-        else:
-            m = F.KMeans(k, dtype="f32x64").with_init_centers(w["init"]).with_precision("bf16")
-        return m.with_max_iter(max_iter).with_tol(0.0).with_n_init(1)
 
     if form == "fp64":
         xd = torch.from_numpy(x32).to(dev).double()
     else:
         xd = torch.from_numpy(x32).to(dev)
     torch.cuda.synchronize()
+    init, kpp_ms = initial_centres(w, xd if form != "fp64" else torch.from_numpy(x32).to(dev), ctx)
 
-    # warm-up (untimed), also measures the per-phase split of one short fit
-    wm = build_model(args.warmup).with_timing(True).fit(xd, ctx=ctx)
+    def build_model(max_iter):
+        if form == "fp32":
+            m = F.KMeans(k, dtype="f32").with_init_centers(init.astype(np.float32))
+        elif form == "fp64":
+            m = F.KMeans(k, dtype="f64").with_init_centers(init)
+        else:
+            m = F.KMeans(k, dtype="f32x64").with_init_centers(init).with_precision(form)
+        return m.with_max_iter(max_iter).with_tol(0.0).with_n_init(1)
+
+    # warm-up (untimed)
+    build_model(args.warmup).with_timing(True).fit(xd, ctx=ctx)
     l0 = _native.lib().fk_debug_launch_count()
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     model = build_model(args.steps).with_timing(True)
@@ -246,39 +281,59 @@ def run_ours(args):
     # dominant kernel: the tensor-core contraction (CUDA events on the library's
     # stream around each launch); the SIMT forms time the whole assignment
     assign_ms = rep["ms_assign"] / iters
+    mixed = form in ("bf16", "fp8")
     contract_ms = rep["ms_contract"] / iters if rep["ms_contract"] > 0 else assign_ms
     flops = 2.0 * n * k * d
     if form == "bf16":
         roof = {"bound": "tensor", "achieved": flops / (contract_ms / 1e3) / 1e12, "peak": bf16s, "unit": "TFLOP/s",
                 "peak_source": f"bf16_tflops_sustained ({peak_src})"}
+    elif form == "fp8":
+        roof = {"bound": "tensor", "achieved": flops / (contract_ms / 1e3) / 1e12, "peak": 2.0 * bf16s,
+                "unit": "TFLOP/s", "peak_source": f"2 x bf16_tflops_sustained ({peak_src}): the dense E4M3 rate is "
+                                                  "twice the BF16 rate on this part"}
     else:
         roof = {"bound": "tensor", "achieved": flops / (assign_ms / 1e3) / 1e12, "peak": bf16s, "unit": "TFLOP/s",
                 "peak_source": f"bf16_tflops_sustained ({peak_src}); SIMT form compared against the tensor peak"}
     roof["frac"] = roof["achieved"] / roof["peak"]
     roof["traffic"] = None
-    roof["kernel"] = "tc_assign_kernel (BF16 tcgen05 contraction + top-2 epilogue)" if form == "bf16" else \
+    roof["kernel"] = f"tc_assign_kernel ({form.upper()} tcgen05 contraction + top-2 epilogue)" if mixed else \
         "assign_direct_kernel (whole assignment phase)"
-    roof["ms_per_launch"] = contract_ms if form == "bf16" else assign_ms
+    roof["ms_per_launch"] = contract_ms if mixed else assign_ms
 
     out = {
         "metric": METRIC, "value": ips, "unit": "iters/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / iters, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": {"bf16": "bf16+f64", "fp32": "f32", "fp64": "f64"}[form], "data": "synthetic",
-        "form": form,
-        "config": {"workload": w["name"], "n": n, "d": d, "k": k, "X": "f32", "init": "first k rows of a seeded "
-                   "permutation", "tol": 0.0, "l2": "inputs larger than L2 (X 2.05 GB)", "parallelism": "replicas"},
+        "vs_baseline": None, "dtype": {"bf16": "bf16+f64", "fp8": "e4m3+f64", "fp32": "f32", "fp64": "f64"}[form],
+        "data": "synthetic", "form": form,
+        "config": {"workload": w["name"], "n": n, "d": d, "k": k, "X": "f32",
+                   "init": "k-means++ on the GPU" if kpp_ms is not None else "first k rows of a seeded permutation",
+                   "tol": 0.0, "l2": f"inputs larger than L2 (X {x32.nbytes / 1e9:.2f} GB)",
+                   "parallelism": "replicas"},
         "pt_k_per_s": ips * n * k,
-        "phase_ms_per_iter": {"assign": assign_ms, "contract": contract_ms if form == "bf16" else None,
+        "phase_ms_per_iter": {"assign": assign_ms, "contract": contract_ms if mixed else None,
                               "update": rep["ms_update"] / iters},
         "recheck": {"rows": rep["rows_rechecked"], "full_rescan": rep["rows_full_rescan"],
                     "fp64_rows": rep["rows_fp64"], "second_pass": rep["rows_second_pass"],
-                    "four_candidates": rep["rows_four"], "exhaustive": rep["rows_exhaustive"],
+                    "few_candidates": rep["rows_few"], "exhaustive": rep["rows_exhaustive"],
                     "near_ties": rep["near_tie_rows"],
                     "fraction": rep["rows_rechecked"] / max(1, rep["rows_assigned"])},
         "gpu_launches": launches,
         "clocks": clocks.summary(),
         "roofline": roof,
     }
+    if kpp_ms is not None:
+        out["kpp_ms"] = kpp_ms
+    if "x_predict" in w and rank == 0:
+        xp = torch.from_numpy(w["x_predict"]).to(dev)
+        fitted.predict(xp, ctx=ctx)  # warm-up (plans the launch for this row count)
+        torch.cuda.synchronize()
+        start.record(stream)
+        fitted.predict(xp, ctx=ctx)
+        end.record(stream)
+        torch.cuda.synchronize()
+        pms = start.elapsed_time(end)
+        out["predict"] = {"rows": int(xp.shape[0]), "ms": pms, "rows_per_s": xp.shape[0] / (pms / 1e3),
+                          "note": "KMeans::predict on fresh rows resident in HBM, labels to host memory"}
 
     if not args.no_e2e and rank == 0:
         xh = torch.from_numpy(x32).pin_memory() if form != "fp64" else torch.from_numpy(

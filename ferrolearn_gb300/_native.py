@@ -52,7 +52,7 @@ class FitReport(C.Structure):
         ("rows_full_rescan", C.c_int64),
         ("rows_fp64", C.c_int64),
         ("rows_second_pass", C.c_int64),
-        ("rows_four", C.c_int64),
+        ("rows_few", C.c_int64),
         ("rows_exhaustive", C.c_int64),
         ("near_tie_rows", C.c_int64),
         ("ms_init", C.c_double),

@@ -209,7 +209,7 @@ void accumulate_report(fk_fit_report *rep, const DevScalars &h, int64_t n) {
     rep->rows_full_rescan += (int64_t)h.full_count;
     rep->rows_fp64 += (int64_t)h.recheck_rows;
     rep->rows_second_pass += (int64_t)h.full_count;
-    rep->rows_four += (int64_t)h.quad_count;
+    rep->rows_few += (int64_t)h.quad_count;
     rep->rows_exhaustive += (int64_t)h.ex_count;
     rep->near_tie_rows += (int64_t)h.near_tie_rows;
 }
@@ -610,6 +610,8 @@ fk_status fk_ctx_destroy(fk_ctx *ctx) {
     for (int i = 0; i < fk::BUF_COUNT; i++)
         if (c->buf[i]) cudaFree(c->buf[i]);
     if (c->host_scalars) cudaFreeHost(c->host_scalars);
+    if (c->mixed.ones) cudaFree(c->mixed.ones);
+    if (c->mixed2.ones) cudaFree(c->mixed2.ones);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return FK_OK;

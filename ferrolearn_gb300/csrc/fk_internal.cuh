@@ -58,7 +58,7 @@ struct DevScalars {
     unsigned long long near_tie_rows;
     unsigned long long flag_count;  // number of rows queued for re-check
     unsigned long long full_count;  // number of rows queued for a full re-scan
-    unsigned long long quad_count;  // second pass: rows with at most 4 candidates
+    unsigned long long quad_count;  // second pass: rows with 2 to 8 candidates
     unsigned long long ex_count;    // second pass: rows with more than 4 candidates
     unsigned long long error_word;  // nonzero: a bounded device wait gave up
 };
@@ -89,11 +89,12 @@ struct alignas(16) Top2 {
     int i1, i2, pad1, pad2;
 };
 
-// Best four scores of one row over one slice, and u5, a bound of the rest.
-struct alignas(16) Top4 {
-    float v[4];
-    int i[4];
-    float u5, pad0, pad1, pad2;
+// Best eight scores of one row over one slice (second pass), and u9, a bound
+// of the rest.
+struct alignas(16) Top8 {
+    float v[8];
+    int i[8];
+    float u9, pad0, pad1, pad2;
 };
 
 // Launch plan of the tensor-core assignment (fk_tc.cu).
@@ -108,15 +109,14 @@ struct MixedPlan {
     int64_t tiles = 0;    // ceil(n / 128)
     int ctas_per_part = 0;
     int grid = 0;
+    int topk = 2;         // epilogue records: 2 (Top2, main pass) or 8 (Top8, second pass)
+    int xst = 2;          // depth of the X tile ring (1 when two stages leave no room for 256 centres)
     size_t smem = 0;
     const void *x = nullptr;
     double mu_norm = 0.0;
-    const void *tm_x_ptr = nullptr, *tm_c_ptr = nullptr, *tm_aug_ptr = nullptr, *tm_x2_ptr = nullptr;
-    const void *tm_xaug_ptr = nullptr, *tm_xaug2_ptr = nullptr;
+    const void *tm_x_ptr = nullptr, *tm_c_ptr = nullptr, *tm_aug_ptr = nullptr, *tm_xaug_ptr = nullptr;
     bool fp8 = false;
-    alignas(64) unsigned char tm_x2[128];
     alignas(64) unsigned char tm_xaug[128];
-    alignas(64) unsigned char tm_xaug2[128];
     alignas(64) unsigned char tm_x[128];
     alignas(64) unsigned char tm_c[128];
     alignas(64) unsigned char tm_aug[128];
@@ -129,8 +129,9 @@ enum BufSlot {
     BUF_X = 0, BUF_XC, BUF_C0, BUF_C1, BUF_CBEST, BUF_LABELS, BUF_LBEST, BUF_MIND,
     BUF_MEMBERS, BUF_SEGHIST, BUF_SCAN_TMP, BUF_COUNTS, BUF_PARTIAL, BUF_SCALARS,
     BUF_OUT, BUF_OUT2, BUF_KPP0, BUF_KPP1, BUF_KPP2, BUF_KPP3, BUF_DRAWS,
-    BUF_XB, BUF_XNORM, BUF_CB, BUF_CAUX, BUF_TOP2, BUF_FLAGS, BUF_FULL, BUF_CF32, BUF_CF32C, BUF_FIXPART, BUF_XB2, BUF_TOP4, BUF_QUAD, BUF_EX, BUF_XAUG, BUF_XAUG2, BUF_ROWSCALE,
-    BUF_ROWSCALE2,
+    BUF_XB, BUF_XNORM, BUF_CB, BUF_CAUX, BUF_TOP2, BUF_FLAGS, BUF_FULL, BUF_CF32, BUF_CF32C, BUF_FIXPART,
+    BUF_XB2, BUF_TOP8, BUF_OCT, BUF_EX, BUF_XAUG, BUF_ROWSCALE, BUF_ROWINFO2, BUF_STATS2, BUF_CB2, BUF_CAUG2,
+    BUF_HALF2,
     BUF_COUNT
 };
 
@@ -150,7 +151,8 @@ struct Ctx {
         double *acc;
     };
     std::vector<PendingTimer> pending;  // phase timers read after the loop
-    MixedPlan mixed;
+    MixedPlan mixed;   // main pass
+    MixedPlan mixed2;  // second pass (BF16, top-8 records) over the rows the main pass left open
     double *contract_acc = nullptr;  // when set: device time of the contraction kernel
 
     void *get(BufSlot s, size_t bytes);  // grow-only device buffer
@@ -258,15 +260,15 @@ void run_assign_mixed(Ctx &ctx, const TX *x, int64_t n, int d, const double *c, 
 void launch_mixed_inertia(Ctx &ctx, const double *part, int64_t m, DevScalars *scalars);
 
 // Tensor-core assignment (fk_tc.cu): plan, then one persistent launch that
-// writes one Top2 record per (slice, row).
-void plan_tc(Ctx &ctx, MixedPlan &mp, int64_t n, int d, int k, bool fp8 = false);
+// writes one record per (slice, row): Top2 (topk 2) or Top8 (topk 8).
+void plan_tc(Ctx &ctx, MixedPlan &mp, int64_t n, int d, int k, bool fp8, int topk);
 // dump (tests only, nullable): raw accumulators of CTA 0's first tile.
-// out4 != nullptr selects the second pass (top-4 records over the gathered
-// rows whose count is read from n_dev at launch; mp.n is their capacity).
-// FP8 (mp.fp8): xaug is the per-row augmentation tensor (n x 16 BF16) and
-// rowscale the per-row power of two mapping scores to the row's units.
+// n_dev (nullable): the row count is read there at launch (mp.n is then the
+// capacity). FP8 (mp.fp8): xaug is the per-row augmentation tensor (n x 16
+// BF16) and rowscale the per-row power of two mapping scores to the row's
+// accumulator units.
 void launch_tc_assign(Ctx &ctx, MixedPlan &mp, const void *xb, const void *cb, const void *caug, Top2 *out,
-                      DevScalars *sc, const MixedStats *stats, float *dump = nullptr, Top4 *out4 = nullptr,
+                      Top8 *out8, DevScalars *sc, const MixedStats *stats, float *dump = nullptr,
                       const unsigned long long *n_dev = nullptr, const void *xaug = nullptr,
                       const float *rowscale = nullptr);
 

@@ -135,15 +135,20 @@ __device__ __forceinline__ float warp_sum_f(float v) {
 // tensor cores see every score of the row divided by s (and by the centres'
 // scale t). sh is kept within [sh_t - 40, sh_t + 60] (and [-120, 120]) so
 // that every scaled score stays a normal float.
+// With a list (second pass), output slot s holds row list[s], s < *count.
 template <typename TX, bool FP8>
 __global__ void prep_rows_kernel(const TX *__restrict__ x, int64_t n, int d, int d_pad,
                                  const float *__restrict__ mu32, void *__restrict__ xq_out,
-                                 __nv_bfloat16 *__restrict__ xaug, float4 *__restrict__ rowinfo, MixedStats *stats) {
+                                 __nv_bfloat16 *__restrict__ xaug, float4 *__restrict__ rowinfo, MixedStats *stats,
+                                 const int32_t *__restrict__ list = nullptr,
+                                 const unsigned long long *count = nullptr) {
     __shared__ float sh_xn[32], sh_am[32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    const int64_t slots = list ? (int64_t)*count : n;
     float xn_hi = 0.f, am_hi = 0.f;
-    for (int64_t row = (int64_t)blockIdx.x * (blockDim.x >> 5) + w; row < n; row += nwarps) {
+    for (int64_t slot = (int64_t)blockIdx.x * (blockDim.x >> 5) + w; slot < slots; slot += nwarps) {
+        const int64_t row = list ? (int64_t)list[slot] : slot;
         float xn2 = 0.f, ex2 = 0.f, tn2 = 0.f, xo2 = 0.f, amax = 0.f, tmax = 0.f;  // tmax: FP8 only
         float scale = 1.f, inv = 1.f;
         if (FP8) {
@@ -168,11 +173,11 @@ __global__ void prep_rows_kernel(const TX *__restrict__ x, int64_t n, int d, int
                 const float t = __fsub_rn(xv, mu32[j]);
                 if (FP8) {
                     const __nv_fp8_e4m3 q8(__fmul_rn(t, inv));
-                    ((unsigned char *)xq_out)[row * d_pad + j] = q8.__x;
+                    ((unsigned char *)xq_out)[slot * d_pad + j] = q8.__x;
                     hv = __fmul_rn((float)q8, scale);
                 } else {
                     const __nv_bfloat16 h = __float2bfloat16_rn(t);
-                    ((__nv_bfloat16 *)xq_out)[row * d_pad + j] = h;
+                    ((__nv_bfloat16 *)xq_out)[slot * d_pad + j] = h;
                     hv = __bfloat162float(h);
                 }
                 const float e = __fsub_rn(t, hv);
@@ -182,9 +187,9 @@ __global__ void prep_rows_kernel(const TX *__restrict__ x, int64_t n, int d, int
                 xo2 = __fmaf_rn(xv, xv, xo2);
                 amax = fmaxf(amax, fabsf(xv));
             } else if (FP8) {
-                ((unsigned char *)xq_out)[row * d_pad + j] = 0;
+                ((unsigned char *)xq_out)[slot * d_pad + j] = 0;
             } else {
-                ((__nv_bfloat16 *)xq_out)[row * d_pad + j] = __float2bfloat16_rn(0.f);
+                ((__nv_bfloat16 *)xq_out)[slot * d_pad + j] = __float2bfloat16_rn(0.f);
             }
         }
         xn2 = warp_sum_f(xn2);
@@ -197,9 +202,9 @@ __global__ void prep_rows_kernel(const TX *__restrict__ x, int64_t n, int d, int
         float xn = __fsqrt_ru(__fmul_ru(xn2, up));
         float ex = __fadd_ru(__fsqrt_ru(__fmul_ru(ex2, up)), __fmul_ru(__fsqrt_ru(__fmul_ru(tn2, up)), 5.9604645e-08f));
         float xo = __fsqrt_ru(__fmul_ru(xo2, up));
-        if (lane == 0) rowinfo[row] = make_float4(xn, ex, xo, inv);
+        if (lane == 0) rowinfo[slot] = make_float4(xn, ex, xo, inv);
         if (FP8 && lane < 16)
-            xaug[row * 16 + lane] = lane < 3 ? __float2bfloat16_rn(inv) : __float2bfloat16_rn(0.f);
+            xaug[slot * 16 + lane] = lane < 3 ? __float2bfloat16_rn(inv) : __float2bfloat16_rn(0.f);
         if (xn < INFINITY) xn_hi = fmaxf(xn_hi, xn);  // NaN / inf rows are re-scored in full
         if (amax < INFINITY) am_hi = fmaxf(am_hi, amax);
     }
@@ -267,8 +272,10 @@ __global__ void prep_centres_kernel(const double *__restrict__ c, int k, int k_p
             ch2 += hv * hv;
             co2 += cv * cv;
             float f = (float)cv;
-            c32[(int64_t)q * d + j] = f;
-            c32t[(int64_t)j * k + q] = f;
+            if (c32) {
+                c32[(int64_t)q * d + j] = f;
+                c32t[(int64_t)j * k + q] = f;
+            }
             e32 += (cv - (double)f) * (cv - (double)f);
         }
         if (FP8)
@@ -283,7 +290,7 @@ __global__ void prep_centres_kernel(const double *__restrict__ c, int k, int k_p
     e32 = warp_sum_d(e32);
     if (lane == 0 && q < k) {
         const double up = 1.0 + 1e-12;
-        ec32[q] = __double2float_ru(sqrt(e32) * up);
+        if (ec32) ec32[q] = __double2float_ru(sqrt(e32) * up);
         half_norm[q] = 0.5 * cn2;
         atomic_max_pos(&stats->cn_max, __double2float_ru(sqrt(cn2) * up));
         atomic_max_pos(&stats->ec_max, __double2float_ru(sqrt(ec2) * up));
@@ -680,28 +687,21 @@ __global__ void exhaustive_rescore_kernel(const float *__restrict__ x, int d, co
 }
 
 // ------------------------------------------------------- second pass --
-// Rows whose third-best BF16 score was inside the bound are gathered and
-// scored again by the tensor cores with a top-4 epilogue; then only the (at
-// most four) centres inside the bound are re-scored.
-__global__ void gather_rows_kernel(const uint4 *__restrict__ xb, int row_vecs, const int32_t *__restrict__ list,
-                                   const unsigned long long *count_ptr, uint4 *__restrict__ xb2) {
-    const unsigned long long cnt = *count_ptr;
-    const int lane = threadIdx.x & 31;
-    const unsigned long long wid = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const unsigned long long nw = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
-    for (unsigned long long s = wid; s < cnt; s += nw) {
-        const int64_t r = list[s];
-        for (int v = lane; v < row_vecs; v += 32) xb2[(int64_t)s * row_vecs + v] = xb[r * row_vecs + v];
-    }
-}
-
-struct Quad {
-    int row, m, i0, i1, i2, i3, pad0, pad1;
+// Rows whose third-best score was inside the bound are scored again by the
+// tensor cores in BF16 (after an FP8 main pass too: a bound 16x tighter),
+// from their f32 values, with a top-8 epilogue; then only the (at most
+// eight) centres inside the second pass's bound are re-scored. Slot s of the
+// second pass holds row list[s]; its row data (rowinfo2) and statistics
+// (stats2) are its own.
+struct Oct {
+    int row, m;
+    int ids[8];
+    int pad0, pad1;
 };
 
-__device__ __forceinline__ uint32_t ins4u(uint32_t (&R)[4], int (&I)[4], uint32_t w, int j) {
+__device__ __forceinline__ uint32_t ins8u(uint32_t (&R)[8], int (&I)[8], uint32_t w, int j) {
 #pragma unroll
-    for (int p = 0; p < 4; p++) {
+    for (int p = 0; p < 8; p++) {
         if (w > R[p]) {
             const uint32_t tw = R[p];
             const int tj = I[p];
@@ -714,41 +714,41 @@ __device__ __forceinline__ uint32_t ins4u(uint32_t (&R)[4], int (&I)[4], uint32_
     return w;
 }
 
-__global__ void finalize4_kernel(const Top4 *__restrict__ parts, int nparts, int64_t cap, int k, int d,
-                                 const int32_t *__restrict__ list, const float4 *__restrict__ rowinfo,
-                                 const MixedStats *stats, double acc_rel, double mu_norm, int32_t *__restrict__ labels,
-                                 Quad *__restrict__ quads, int32_t *__restrict__ ex_list, DevScalars *sc) {
+__global__ void finalize8_kernel(const Top8 *__restrict__ parts, int nparts, int64_t cap, int k, int d,
+                                 const int32_t *__restrict__ list, const float4 *__restrict__ rowinfo2,
+                                 const MixedStats *stats2, double acc_rel, double mu_norm,
+                                 int32_t *__restrict__ labels, Oct *__restrict__ octs, int32_t *__restrict__ ex_list,
+                                 DevScalars *sc) {
     const unsigned long long cnt = sc->full_count;
     for (unsigned long long s = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; s < cnt;
          s += (unsigned long long)gridDim.x * blockDim.x) {
-        uint32_t R[4], U;
-        int I[4];
+        uint32_t R[8], U;
+        int I[8];
         {
-            const Top4 t = parts[s];
+            const Top8 t = parts[s];
 #pragma unroll
-            for (int j = 0; j < 4; j++) {
+            for (int j = 0; j < 8; j++) {
                 R[j] = __float_as_uint(t.v[j]);
                 I[j] = t.i[j];
             }
-            U = __float_as_uint(t.u5);
+            U = __float_as_uint(t.u9);
         }
         for (int p = 1; p < nparts; p++) {
-            const Top4 o = parts[(int64_t)p * cap + s];
-            U = max(U, __float_as_uint(o.u5));
+            const Top8 o = parts[(int64_t)p * cap + s];
+            U = max(U, __float_as_uint(o.u9));
 #pragma unroll
-            for (int j = 0; j < 4; j++) U = max(U, ins4u(R, I, __float_as_uint(o.v[j]), o.i[j]));
+            for (int j = 0; j < 8; j++) U = max(U, ins8u(R, I, __float_as_uint(o.v[j]), o.i[j]));
         }
         const int32_t row = list[s];
-        const float4 ri = rowinfo[row];
-        const float unit = stats->tscale / ri.w;  // FP8: back to score units
-        const float v1 = __uint_as_float(R[0]) * unit;
-        const double thr = row_threshold(ri, stats, acc_rel, mu_norm, d, v1);
-        const bool rest_out = (double)v1 - (double)(__uint_as_float(U) * unit) > thr;
+        const float4 ri = rowinfo2[s];
+        const float v1 = __uint_as_float(R[0]);
+        const double thr = row_threshold(ri, stats2, acc_rel, mu_norm, d, v1);
+        const bool rest_out = (double)v1 - (double)__uint_as_float(U) > thr;
         int m = 0;
         bool valid = true;
 #pragma unroll
-        for (int j = 0; j < 4; j++) {
-            if ((double)v1 - (double)(__uint_as_float(R[j]) * unit) <= thr) {
+        for (int j = 0; j < 8; j++) {
+            if ((double)v1 - (double)__uint_as_float(R[j]) <= thr) {
                 m++;
                 if (I[j] < 0 || I[j] >= k) valid = false;
             }
@@ -760,33 +760,38 @@ __global__ void finalize4_kernel(const Top4 *__restrict__ parts, int nparts, int
             labels[row] = I[0];
         } else {
             unsigned long long slot = atomicAdd(&sc->quad_count, 1ULL);
-            quads[slot] = Quad{row, m, I[0], I[1], I[2], I[3], 0, 0};
+            Oct o;
+            o.row = row;
+            o.m = m;
+#pragma unroll
+            for (int j = 0; j < 8; j++) o.ids[j] = I[j];
+            o.pad0 = o.pad1 = 0;
+            octs[slot] = o;
         }
     }
 }
 
-// One warp per row with at most four candidates: FP32 distances (lanes over
+// One warp per row with at most eight candidates: FP32 distances (lanes over
 // the features) with rigorous bounds; the candidates whose lower bound
 // reaches the smallest upper bound are scored exactly in FP64 (one lane
 // each, direct form), lowest index on ties.
-__global__ void quad_rescore_kernel(const float *__restrict__ x, int d, const double *__restrict__ c,
-                                    const float *__restrict__ c32, const float *__restrict__ ec32,
-                                    const Quad *__restrict__ quads, DevScalars *sc, int32_t *__restrict__ labels) {
+__global__ void oct_rescore_kernel(const float *__restrict__ x, int d, const double *__restrict__ c,
+                                   const float *__restrict__ c32, const float *__restrict__ ec32,
+                                   const Oct *__restrict__ octs, DevScalars *sc, int32_t *__restrict__ labels) {
     const unsigned long long cnt = sc->quad_count;
     const int lane = threadIdx.x & 31;
     const unsigned long long wid = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const unsigned long long nw = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
     for (unsigned long long s = wid; s < cnt; s += nw) {
-        const Quad qd = quads[s];
-        const int ids[4] = {qd.i0, qd.i1, qd.i2, qd.i3};
+        const Oct qd = octs[s];
         const float *row = x + (int64_t)qd.row * d;
-        float dist[4], err[4];
+        float dist[8], err[8];
         float ub = INFINITY;
 #pragma unroll
-        for (int j = 0; j < 4; j++) {
+        for (int j = 0; j < 8; j++) {
             float acc = 0.f;
             if (j < qd.m) {
-                const float *cc = c32 + (int64_t)ids[j] * d;
+                const float *cc = c32 + (int64_t)qd.ids[j] * d;
                 for (int f = lane; f < d; f += 32) {
                     const float t = row[f] - cc[f];
                     acc = fmaf(t, t, acc);
@@ -794,16 +799,24 @@ __global__ void quad_rescore_kernel(const float *__restrict__ x, int d, const do
             }
             acc = warp_sum_f(acc);
             dist[j] = acc;
-            err[j] = j < qd.m ? bound32(acc, ec32[ids[j]], d) : 0.f;
+            err[j] = j < qd.m ? bound32(acc, ec32[qd.ids[j]], d) : 0.f;
             if (j < qd.m) ub = fminf(ub, __fadd_ru(acc, err[j]));
         }
         int nsurv = 0, only = -1;
+        float my_dist = 0.f, my_err = 0.f;
+        int my_id = INT32_MAX;
 #pragma unroll
-        for (int j = 0; j < 4; j++)
+        for (int j = 0; j < 8; j++) {
             if (j < qd.m && !(__fsub_rd(dist[j], err[j]) > ub)) {
                 nsurv++;
-                only = ids[j];
+                only = qd.ids[j];
             }
+            if (j == lane) {
+                my_dist = dist[j];
+                my_err = err[j];
+                my_id = qd.ids[j];
+            }
+        }
         if (nsurv == 1) {
             if (lane == 0) labels[qd.row] = only;
             continue;
@@ -812,9 +825,9 @@ __global__ void quad_rescore_kernel(const float *__restrict__ x, int d, const do
         double v = DBL_MAX;
         int id = INT32_MAX;
         if (lane < qd.m) {
-            const bool surv = nsurv == 0 || !(__fsub_rd(dist[lane], err[lane]) > ub);
+            const bool surv = nsurv == 0 || !(__fsub_rd(my_dist, my_err) > ub);
             if (surv) {
-                id = ids[lane];
+                id = my_id;
                 v = sqeuc64(row, c + (int64_t)id * d, d);
                 if (!(v < DBL_MAX)) id = INT32_MAX;  // not below F::MAX: never chosen
             }
@@ -882,7 +895,7 @@ MixedBufs prepare_mixed(Ctx &ctx, const TX *x, int64_t n, int d, const double *c
     cudaStream_t s = ctx.stream;
     MixedPlan &mp = ctx.mixed;
     const bool replan = x_changed || mp.n != n || mp.d != d || mp.k != k || mp.x != (const void *)x || mp.fp8 != fp8;
-    if (replan) plan_tc(ctx, mp, n, d, k, fp8);
+    if (replan) plan_tc(ctx, mp, n, d, k, fp8, 2);
     mp.x = (const void *)x;
     const size_t es = fp8 ? 1 : 2;
     MixedBufs B;
@@ -948,25 +961,51 @@ MixedBufs prepare_mixed(Ctx &ctx, const TX *x, int64_t n, int d, const double *c
     return B;
 }
 
-__global__ void gather_aux_kernel(const __nv_bfloat16 *__restrict__ xaug, const float *__restrict__ rowscale,
-                                  const int32_t *__restrict__ list, const unsigned long long *count_ptr,
-                                  __nv_bfloat16 *__restrict__ xaug2, float *__restrict__ rowscale2) {
-    const unsigned long long cnt = *count_ptr;
-    for (unsigned long long s = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; s < cnt;
-         s += (unsigned long long)gridDim.x * blockDim.x) {
-        const int64_t r = list[s];
-#pragma unroll
-        for (int j = 0; j < 16; j++) xaug2[(int64_t)s * 16 + j] = xaug[r * 16 + j];
-        rowscale2[s] = rowscale[r];
-    }
-}
-
 // FP8: r = 2^-sh_row * 2^-sh_t, the factor between a row's scores and its
 // accumulators (exact: a product of powers of two in range).
 __global__ void rowscale_kernel(const float4 *__restrict__ rowinfo, int64_t n, const MixedStats *stats,
                                 float *__restrict__ rowscale) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) rowscale[i] = rowinfo[i].w * stats->inv_t;
+}
+
+// Second pass over the rows listed in full (count sc->full_count): BF16
+// operands made from their f32 values, a top-8 tensor pass, then the
+// re-score of at most eight candidates, or of every centre.
+void second_pass(Ctx &ctx, const float *x, int64_t n, int d, const double *c, int k, const MixedBufs &B,
+                 double mu_norm, const int32_t *full, int32_t *labels, DevScalars *sc) {
+    cudaStream_t s = ctx.stream;
+    MixedPlan &m2 = ctx.mixed2;
+    if (m2.n != n || m2.d != d || m2.k != k) plan_tc(ctx, m2, n, d, k, false, 8);
+    MixedStats *st2 = (MixedStats *)ctx.get(BUF_STATS2, sizeof(MixedStats));
+    void *xb2 = ctx.get(BUF_XB2, sizeof(__nv_bfloat16) * (size_t)n * m2.d_pad);
+    float4 *ri2 = (float4 *)ctx.get(BUF_ROWINFO2, sizeof(float4) * (size_t)n);
+    void *cb2 = ctx.get(BUF_CB2, sizeof(__nv_bfloat16) * (size_t)m2.k_pad * m2.d_pad);
+    __nv_bfloat16 *caug2 = (__nv_bfloat16 *)ctx.get(BUF_CAUG2, sizeof(__nv_bfloat16) * (size_t)m2.k_pad * 16 + 8192);
+    double *hn2 = (double *)ctx.get(BUF_HALF2, sizeof(double) * (size_t)m2.k_pad);
+    Top8 *top8 = (Top8 *)ctx.get(BUF_TOP8, sizeof(Top8) * (size_t)n * m2.parts);
+    Oct *octs = (Oct *)ctx.get(BUF_OCT, sizeof(Oct) * (size_t)n);
+    int32_t *ex = (int32_t *)ctx.get(BUF_EX, sizeof(int32_t) * (size_t)n);
+    FK_CUDA(cudaMemsetAsync(st2, 0, sizeof(MixedStats), s));
+    const int64_t pblocks = std::min<int64_t>((n + 7) / 8, (int64_t)ctx.num_sms * 16);
+    prep_rows_kernel<float, false><<<(unsigned)pblocks, 256, 0, s>>>(x, n, d, m2.d_pad, B.mu32, xb2, nullptr, ri2,
+                                                                      st2, full, &sc->full_count);
+    FK_LAUNCH_CHECK();
+    prep_centres_kernel<false><<<(m2.k_pad + 7) / 8, 256, 0, s>>>(c, k, m2.k_pad, d, m2.d_pad, B.mu, cb2, hn2,
+                                                                  nullptr, nullptr, nullptr, st2);
+    FK_LAUNCH_CHECK();
+    prep_aug_kernel<<<(m2.k_pad + 255) / 256, 256, 0, s>>>(hn2, k, m2.k_pad, false, caug2, st2);
+    FK_LAUNCH_CHECK();
+    launch_tc_assign(ctx, m2, xb2, cb2, caug2, nullptr, top8, sc, st2, nullptr, &sc->full_count);
+    const double acc_rel2 = (double)((size_t)m2.d_pad + 32) * ACC_REL_PER_K;
+    const int grid = ctx.num_sms * 4;
+    finalize8_kernel<<<grid, 256, 0, s>>>(top8, m2.parts, n, k, d, full, ri2, st2, acc_rel2, mu_norm, labels, octs,
+                                          ex, sc);
+    FK_LAUNCH_CHECK();
+    oct_rescore_kernel<<<grid, 256, 0, s>>>(x, d, c, B.c32, B.ec32, octs, sc, labels);
+    FK_LAUNCH_CHECK();
+    exhaustive_rescore_kernel<<<grid, 256, 0, s>>>(x, d, c, B.c32t, B.ec32, k, ex, &sc->ex_count, sc, labels);
+    FK_LAUNCH_CHECK();
 }
 
 }  // namespace
@@ -985,8 +1024,8 @@ void run_assign_mixed(Ctx &ctx, const TX *x, int64_t n, int d, const double *c, 
         set_error("the FP8 form needs X stored as f32 (the f32x64 entry points)");
         fail(FK_ERR_UNSUPPORTED);
     }
-    if (d < 1 || d > (fp8 ? 384 : 192)) {
-        set_error("the tensor-core path supports 1 <= d <= %d for this precision (got %d)", fp8 ? 384 : 192, d);
+    if (d < 1 || d > 256) {
+        set_error("the tensor-core path supports 1 <= d <= 256 (got %d)", d);
         fail(FK_ERR_UNSUPPORTED);
     }
     MixedBufs B = prepare_mixed<TX>(ctx, x, n, d, c, k, fp8, x_changed);
@@ -1000,7 +1039,7 @@ void run_assign_mixed(Ctx &ctx, const TX *x, int64_t n, int d, const double *c, 
     Top2 *top = (Top2 *)ctx.get(BUF_TOP2, sizeof(Top2) * (size_t)n * mp.parts);
     {
         Timer t(ctx.contract_acc != nullptr, ctx, ctx.contract_acc);
-        launch_tc_assign(ctx, mp, B.xq, B.cq, B.caug, top, sc, B.stats, nullptr, nullptr, nullptr, B.xaug, rowscale);
+        launch_tc_assign(ctx, mp, B.xq, B.cq, B.caug, top, nullptr, sc, B.stats, nullptr, nullptr, B.xaug, rowscale);
     }
 
     int4 *pairs = (int4 *)ctx.get(BUF_FLAGS, sizeof(int4) * (size_t)n);
@@ -1013,35 +1052,11 @@ void run_assign_mixed(Ctx &ctx, const TX *x, int64_t n, int d, const double *c, 
     pair_rescore_kernel<TX><<<grid, 256, 0, s>>>(x, d, c, B.c32, B.ec32, pairs, sc, labels);
     FK_LAUNCH_CHECK();
     if constexpr (std::is_same<TX, float>::value) {
-        // second tensor pass over the rows whose third score was inside the bound
-        const size_t es = fp8 ? 1 : 2;
-        void *xb2 = ctx.get(BUF_XB2, es * (size_t)n * mp.d_pad);
-        Top4 *top4 = (Top4 *)ctx.get(BUF_TOP4, sizeof(Top4) * (size_t)n * mp.parts);
-        Quad *quads = (Quad *)ctx.get(BUF_QUAD, sizeof(Quad) * (size_t)n);
-        int32_t *ex = (int32_t *)ctx.get(BUF_EX, sizeof(int32_t) * (size_t)n);
-        __nv_bfloat16 *xaug2 = nullptr;
-        float *rowscale2 = nullptr;
-        gather_rows_kernel<<<grid, 256, 0, s>>>((const uint4 *)B.xq, (int)(es * mp.d_pad / 16), full, &sc->full_count,
-                                                (uint4 *)xb2);
-        FK_LAUNCH_CHECK();
-        if (fp8) {
-            xaug2 = (__nv_bfloat16 *)ctx.get(BUF_XAUG2, sizeof(__nv_bfloat16) * 16 * (size_t)n);
-            rowscale2 = (float *)ctx.get(BUF_ROWSCALE2, sizeof(float) * (size_t)n);
-            gather_aux_kernel<<<grid, 256, 0, s>>>(B.xaug, rowscale, full, &sc->full_count, xaug2, rowscale2);
-            FK_LAUNCH_CHECK();
-        }
-        launch_tc_assign(ctx, mp, xb2, B.cq, B.caug, nullptr, sc, B.stats, nullptr, top4, &sc->full_count, xaug2,
-                         rowscale2);
-        finalize4_kernel<<<grid, 256, 0, s>>>(top4, mp.parts, n, k, d, full, B.rowinfo, B.stats, acc_rel, mp.mu_norm,
-                                              labels, quads, ex, sc);
-        FK_LAUNCH_CHECK();
-        quad_rescore_kernel<<<grid, 256, 0, s>>>(x, d, c, B.c32, B.ec32, quads, sc, labels);
-        FK_LAUNCH_CHECK();
-        exhaustive_rescore_kernel<<<grid, 256, 0, s>>>(x, d, c, B.c32t, B.ec32, k, ex, &sc->ex_count, sc, labels);
+        second_pass(ctx, x, n, d, c, k, B, mp.mu_norm, full, labels, sc);
     } else {
         full_rescore_kernel<TX><<<grid, 256, 0, s>>>(x, d, c, B.c32, B.ec32, k, full, &sc->full_count, sc, labels);
+        FK_LAUNCH_CHECK();
     }
-    FK_LAUNCH_CHECK();
 }
 
 void launch_mixed_inertia(Ctx &ctx, const double *part, int64_t m, DevScalars *sc) {
@@ -1076,7 +1091,7 @@ void debug_tc_probe(Ctx &ctx, const float *x, int64_t n, int d, const double *c,
     Top2 *top = (Top2 *)ctx.get(BUF_TOP2, sizeof(Top2) * (size_t)n * mp.parts);
     float *dump = (float *)ctx.get(BUF_OUT, sizeof(float) * 128 * (size_t)mp.kp);
     FK_CUDA(cudaMemsetAsync(dump, 0, sizeof(float) * 128 * (size_t)mp.kp, s));
-    launch_tc_assign(ctx, mp, B.xq, B.cq, B.caug, top, sc, B.stats, dump, nullptr, nullptr, B.xaug, rowscale);
+    launch_tc_assign(ctx, mp, B.xq, B.cq, B.caug, top, nullptr, sc, B.stats, dump, nullptr, B.xaug, rowscale);
     const size_t es = fp8 ? 1 : 2;
     FK_CUDA(cudaMemcpyAsync(dump_out, dump, sizeof(float) * 128 * (size_t)mp.kp, cudaMemcpyDeviceToHost, s));
     const int64_t rows = n < 128 ? n : 128;

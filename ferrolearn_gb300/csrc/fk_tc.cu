@@ -41,11 +41,13 @@ namespace {
 constexpr int BM = 128;           // rows per tile = TMEM lanes
 constexpr int BN = 256;           // centres per accumulator block
 constexpr int NTHREADS = 320;     // 10 warps
-constexpr int XSTAGES = 2;        // X ring depth
 constexpr uint32_t TMEM_COLS = 512;
 constexpr uint32_t X_ATOM_BYTES = BM * 128;  // 128 rows x 64 BF16
 constexpr uint32_t ONES_BYTES = BM * 32;     // 128 rows x 16 BF16
-constexpr uint32_t MERGE_BYTES = BM * sizeof(Top4);
+// Shared-memory exchange between the two epilogue halves of a row.
+__host__ __device__ constexpr uint32_t merge_bytes(int topk) {
+    return BM * (uint32_t)(topk == 2 ? sizeof(Top2) : sizeof(Top8));
+}
 constexpr uint32_t BAR_BYTES = 256;
 constexpr long long WAIT_LIMIT_CYCLES = 4000000000LL;
 
@@ -75,7 +77,7 @@ struct TcParams {
     uint32_t x_stage_bytes;
     uint32_t c_tx_bytes;
     Top2 *out;                // top-2 records (main pass)
-    Top4 *out4;               // top-4 records (second pass)
+    Top8 *out8;               // top-8 records (second pass)
     unsigned long long *err;
     const MixedStats *stats;  // cgrid, ulp of this launch
     const float *rowscale;    // FP8: per-row power of two 1/(s_i t) that maps scores to this row's units
@@ -306,25 +308,24 @@ __device__ __forceinline__ void rank_half(uint32_t col_addr, float cgrid, float 
         merge_res(b1, d1, b2, d2, bu, __float_as_uint(a1[qd]), 0, __float_as_uint(a2[qd]), 0, __float_as_uint(a2[qd]));
 }
 
-// ------------------------------------------------ top-4 (second pass) --
-// Sorted insertion of key k into a[0] >= a[1] >= a[2] >= a[3] (7 min/max).
-__device__ __forceinline__ void ins4(float (&a)[4], float k) {
-    float t = fmaxf(a[0], k);
-    k = fminf(a[0], k);
-    a[0] = t;
-    t = fmaxf(a[1], k);
-    k = fminf(a[1], k);
-    a[1] = t;
-    t = fmaxf(a[2], k);
-    k = fminf(a[2], k);
-    a[2] = t;
-    a[3] = fmaxf(a[3], k);
+// ------------------------------------------------ top-8 (second pass) --
+// Sorted insertion of key k into a[0] >= ... >= a[K-1] (2K - 1 min/max).
+template <int K>
+__device__ __forceinline__ void insk(float (&a)[K], float k) {
+#pragma unroll
+    for (int p = 0; p < K - 1; p++) {
+        const float t = fmaxf(a[p], k);
+        k = fminf(a[p], k);
+        a[p] = t;
+    }
+    a[K - 1] = fmaxf(a[K - 1], k);
 }
 
 // Inserts (w, j) into the sorted running list (R, I); returns what falls out.
-__device__ __forceinline__ uint32_t ins4i(uint32_t (&R)[4], int (&I)[4], uint32_t w, int j) {
+template <int K>
+__device__ __forceinline__ uint32_t inski(uint32_t (&R)[K], int (&I)[K], uint32_t w, int j) {
 #pragma unroll
-    for (int p = 0; p < 4; p++) {
+    for (int p = 0; p < K; p++) {
         if (w > R[p]) {
             const uint32_t tw = R[p];
             const int tj = I[p];
@@ -337,49 +338,56 @@ __device__ __forceinline__ uint32_t ins4i(uint32_t (&R)[4], int (&I)[4], uint32_
     return w;
 }
 
-template <int CH>
-__device__ __forceinline__ void rank_chunk4(const uint32_t (&r)[32], float cgrid, float ulp, float (&c0)[4],
-                                            float (&c1)[4]) {
+template <int K, int CH>
+__device__ __forceinline__ void rank_chunkk(const uint32_t (&r)[32], float cgrid, float ulp, float (&c0)[K],
+                                            float (&c1)[K]) {
 #pragma unroll
     for (int e = 0; e < 32; e++) {
         const float t = __fsub_rn(__fadd_rn(__uint_as_float(r[e]), cgrid), cgrid);
         const float key = __fmaf_rn(ulp, (float)(127 - ((CH * 32 + e) & 127)), t);
         if (e & 1)
-            ins4(c1, key);
+            insk<K>(c1, key);
         else
-            ins4(c0, key);
+            insk<K>(c0, key);
     }
 }
 
-// Top-4 keys of the 128 columns of one accumulator half, and a bound of the
-// rest (two chains; a chain's elements outside its top-4 are <= its 4th).
-__device__ __forceinline__ void rank_half4(uint32_t col_addr, float cgrid, float ulp, uint32_t (&K)[4], uint32_t &ku) {
-    float c0[4] = {0.f, 0.f, 0.f, 0.f}, c1[4] = {0.f, 0.f, 0.f, 0.f};
+// Top-K keys of the 128 columns of one accumulator half, and a bound of the
+// rest (two chains; a chain's elements outside its top-K are <= its K-th).
+template <int K>
+__device__ __forceinline__ void rank_halfk(uint32_t col_addr, float cgrid, float ulp, uint32_t (&KK)[K],
+                                           uint32_t &ku) {
+    float c0[K], c1[K];
+#pragma unroll
+    for (int p = 0; p < K; p++) c0[p] = c1[p] = 0.f;
     uint32_t ra[32], rb[32];
     tmem_ld32(col_addr, ra);
     tmem_wait(ra);
     tmem_ld32(col_addr + 32, rb);
-    rank_chunk4<0>(ra, cgrid, ulp, c0, c1);
+    rank_chunkk<K, 0>(ra, cgrid, ulp, c0, c1);
     tmem_wait(rb);
     tmem_ld32(col_addr + 64, ra);
-    rank_chunk4<1>(rb, cgrid, ulp, c0, c1);
+    rank_chunkk<K, 1>(rb, cgrid, ulp, c0, c1);
     tmem_wait(ra);
     tmem_ld32(col_addr + 96, rb);
-    rank_chunk4<2>(ra, cgrid, ulp, c0, c1);
+    rank_chunkk<K, 2>(ra, cgrid, ulp, c0, c1);
     tmem_wait(rb);
-    rank_chunk4<3>(rb, cgrid, ulp, c0, c1);
-    int dummy[4] = {0, 0, 0, 0};
+    rank_chunkk<K, 3>(rb, cgrid, ulp, c0, c1);
+    int dummy[K];
 #pragma unroll
-    for (int p = 0; p < 4; p++) K[p] = __float_as_uint(c0[p]);
-    ku = max(__float_as_uint(c0[3]), __float_as_uint(c1[3]));
+    for (int p = 0; p < K; p++) {
+        KK[p] = __float_as_uint(c0[p]);
+        dummy[p] = 0;
+    }
+    ku = max(__float_as_uint(c0[K - 1]), __float_as_uint(c1[K - 1]));
 #pragma unroll
-    for (int p = 0; p < 4; p++) ku = max(ku, ins4i(K, dummy, __float_as_uint(c1[p]), 0));
+    for (int p = 0; p < K; p++) ku = max(ku, inski<K>(KK, dummy, __float_as_uint(c1[p]), 0));
 }
 
 // FP8: X and the centres are E4M3 (1 byte, 128 per swizzle atom) and the
 // augmentation operand is a per-row BF16 tile loaded with each X tile (the
 // row's scale times [1,1,1,0,...]); BF16: a constant ones tile.
-template <int TOPK, bool FP8>
+template <int TOPK, bool FP8, int XST>
 __global__ void __launch_bounds__(NTHREADS, 1)
     tc_assign_kernel(const __grid_constant__ CUtensorMap tm_x, const __grid_constant__ CUtensorMap tm_c,
                      const __grid_constant__ CUtensorMap tm_aug, const __grid_constant__ CUtensorMap tm_ones,
@@ -399,15 +407,15 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 
     const uint32_t bar_c = sb + p.off_bar;
     auto bar_xfull = [&](int s) { return bar_c + 8u * (1u + (uint32_t)s); };
-    auto bar_xempty = [&](int s) { return bar_c + 8u * (1u + XSTAGES + (uint32_t)s); };
-    auto bar_afull = [&](int b) { return bar_c + 8u * (1u + 2 * XSTAGES + (uint32_t)b); };
-    auto bar_aempty = [&](int b) { return bar_c + 8u * (3u + 2 * XSTAGES + (uint32_t)b); };
+    auto bar_xempty = [&](int s) { return bar_c + 8u * (1u + XST + (uint32_t)s); };
+    auto bar_afull = [&](int b) { return bar_c + 8u * (1u + 2 * XST + (uint32_t)b); };
+    auto bar_aempty = [&](int b) { return bar_c + 8u * (3u + 2 * XST + (uint32_t)b); };
     uint32_t *slot = (uint32_t *)(smem + p.off_bar + 128);
     volatile uint32_t *abort_flag = slot + 1;
 
     if (threadIdx.x == 0) {
         mbar_init(bar_c, 1);
-        for (int s = 0; s < XSTAGES; s++) {
+        for (int s = 0; s < XST; s++) {
             mbar_init(bar_xfull(s), 1);
             mbar_init(bar_xempty(s), 1);
         }
@@ -442,8 +450,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             if (!FP8) tma_load_2d(sb + p.off_ones, &tm_ones, bar_c, 0, 0);
             int it = 0;
             for (int64_t t = q; t < p.tiles; t += tstride, ++it) {
-                const int s = it % XSTAGES;
-                const uint32_t ph = (uint32_t)(it / XSTAGES) & 1u;
+                const int s = it % XST;
+                const uint32_t ph = (uint32_t)(it / XST) & 1u;
                 if (!mbar_wait(bar_xempty(s), ph ^ 1u, abort_flag, p.err, 1ull)) break;
                 mbar_expect_tx(bar_xfull(s), p.x_stage_bytes + (FP8 ? XAUG_BYTES : 0u));
                 for (int a = 0; a < p.n_atoms; a++)
@@ -454,8 +462,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             }
             // Drain: every issued X load must land before the CTA can exit.
             const int issued = it;
-            for (int j = issued > XSTAGES ? issued - XSTAGES : 0; j < issued; j++)
-                mbar_wait(bar_xfull(j % XSTAGES), (uint32_t)(j / XSTAGES) & 1u, abort_flag, p.err, 0ull);
+            for (int j = issued > XST ? issued - XST : 0; j < issued; j++)
+                mbar_wait(bar_xfull(j % XST), (uint32_t)(j / XST) & 1u, abort_flag, p.err, 0ull);
             mbar_wait(bar_c, 0u, abort_flag, p.err, 0ull);
         }
     } else if (warp == 1) {
@@ -468,8 +476,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                 tc_fence_after();
                 bool ok = true;
                 for (int64_t t = q; t < p.tiles && ok; t += tstride, ++it) {
-                    const int s = it % XSTAGES;
-                    const uint32_t ph = (uint32_t)(it / XSTAGES) & 1u;
+                    const int s = it % XST;
+                    const uint32_t ph = (uint32_t)(it / XST) & 1u;
                     if (!mbar_wait(bar_xfull(s), ph, abort_flag, p.err, 4ull)) break;
                     tc_fence_after();
                     const uint32_t xs = sb + p.off_x + (uint32_t)s * p.x_stage_bytes;
@@ -577,13 +585,18 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         const int half = ew >> 2;
         const int row_local = quarter * 32 + lane;
         const uint32_t lane_addr = tmem + ((uint32_t)(quarter * 32) << 16);
-        Top4 *merge = (Top4 *)(smem + p.off_merge);
+        Top8 *merge = (Top8 *)(smem + p.off_merge);
         const float cgrid = p.stats->cgrid, ulp = p.stats->ulp;
         uint32_t item = 0;
         bool dead = false;
         for (int64_t t = q; t < p.tiles; t += tstride) {
-            uint32_t R[4] = {0u, 0u, 0u, 0u}, U = 0u;
-            int I[4] = {-1, -1, -1, -1};
+            uint32_t R[8], U = 0u;
+            int I[8];
+#pragma unroll
+            for (int j = 0; j < 8; j++) {
+                R[j] = 0u;
+                I[j] = -1;
+            }
             float cg = cgrid, ul = ulp;
             if (FP8) {
                 const int64_t rrow = t * BM + row_local;
@@ -598,43 +611,43 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                 if (dead) continue;
                 tc_fence_after();
                 const uint32_t col = lane_addr + (uint32_t)buf * BN + (uint32_t)half * 128u;
-                uint32_t K[4], ku;
-                rank_half4(col, cg, ul, K, ku);
+                uint32_t K[8], ku;
+                rank_halfk<8>(col, cg, ul, K, ku);
                 tc_fence_before();
                 __syncwarp();
                 if (lane == 0) mbar_arrive(bar_aempty(buf));
                 const int base = part * p.kp + b * BN + half * 128 + 127;
                 U = max(U, ku & 0xFFFFFF80u);
 #pragma unroll
-                for (int j = 0; j < 4; j++)
-                    U = max(U, ins4i(R, I, K[j] & 0xFFFFFF80u, base - (int)(K[j] & 0x7Fu)));
+                for (int j = 0; j < 8; j++)
+                    U = max(U, inski<8>(R, I, K[j] & 0xFFFFFF80u, base - (int)(K[j] & 0x7Fu)));
             }
             if (half == 1) {
-                Top4 rec;
+                Top8 rec;
 #pragma unroll
-                for (int j = 0; j < 4; j++) {
+                for (int j = 0; j < 8; j++) {
                     rec.v[j] = __uint_as_float(R[j]);
                     rec.i[j] = I[j];
                 }
-                rec.u5 = __uint_as_float(U);
+                rec.u9 = __uint_as_float(U);
                 merge[row_local] = rec;
             }
             epi_bar();
             if (half == 0) {
-                const Top4 o = merge[row_local];
-                U = max(U, __float_as_uint(o.u5));
+                const Top8 o = merge[row_local];
+                U = max(U, __float_as_uint(o.u9));
 #pragma unroll
-                for (int j = 0; j < 4; j++) U = max(U, ins4i(R, I, __float_as_uint(o.v[j]), o.i[j]));
+                for (int j = 0; j < 8; j++) U = max(U, inski<8>(R, I, __float_as_uint(o.v[j]), o.i[j]));
                 const int64_t row = t * BM + row_local;
                 if (row < p.n && !dead) {
-                    Top4 rec;
+                    Top8 rec;
 #pragma unroll
-                    for (int j = 0; j < 4; j++) {
+                    for (int j = 0; j < 8; j++) {
                         rec.v[j] = __uint_as_float(R[j]);
                         rec.i[j] = I[j];
                     }
-                    rec.u5 = __uint_as_float(U);
-                    p.out4[(int64_t)part * p.out_stride + row] = rec;
+                    rec.u9 = __uint_as_float(U);
+                    p.out8[(int64_t)part * p.out_stride + row] = rec;
                 }
             }
             epi_bar();
@@ -688,22 +701,30 @@ constexpr size_t SMEM_LIMIT = 227 * 1024;
 
 }  // namespace
 
-void plan_tc(Ctx &ctx, MixedPlan &mp, int64_t n, int d, int k, bool fp8) {
+void plan_tc(Ctx &ctx, MixedPlan &mp, int64_t n, int d, int k, bool fp8, int topk) {
     mp.n = n;
     mp.d = d;
     mp.k = k;
     mp.fp8 = fp8;
+    mp.topk = topk;
     const int per_atom = fp8 ? 128 : 64;  // elements per 128-byte swizzle atom
     mp.d_pad = (d + per_atom - 1) / per_atom * per_atom;
     const int n_atoms = mp.d_pad / per_atom;
     const size_t x_stage = (size_t)n_atoms * X_ATOM_BYTES;
-    const size_t fixed = 1024 + XSTAGES * x_stage + (fp8 ? XSTAGES * XAUG_BYTES : ONES_BYTES) + MERGE_BYTES + BAR_BYTES;
     const size_t per_centre = (size_t)n_atoms * 128 + 32;
-    if (fixed + BN * per_centre > SMEM_LIMIT) {
+    // two X stages when 256 resident centres still fit, else one
+    size_t fixed = 0;
+    int xst = 2;
+    for (; xst >= 1; xst--) {
+        fixed = 1024 + xst * x_stage + (fp8 ? xst * XAUG_BYTES : ONES_BYTES) + merge_bytes(topk) + BAR_BYTES;
+        if (fixed + BN * per_centre <= SMEM_LIMIT) break;
+    }
+    if (xst < 1) {
         set_error("the resident-slice tensor-core kernel supports d <= %d for this precision (got %d)",
-                  fp8 ? 384 : 192, d);
+                  fp8 ? 512 : 256, d);
         fail(FK_ERR_UNSUPPORTED);
     }
+    mp.xst = xst;
     const int kp_max = (int)((SMEM_LIMIT - fixed) / per_centre) / BN * BN;
     mp.parts = (k + kp_max - 1) / kp_max;
     mp.kp = ((k + mp.parts - 1) / mp.parts + BN - 1) / BN * BN;
@@ -715,7 +736,7 @@ void plan_tc(Ctx &ctx, MixedPlan &mp, int64_t n, int d, int k, bool fp8) {
     if ((int64_t)mp.ctas_per_part > mp.tiles) mp.ctas_per_part = (int)mp.tiles;
     mp.grid = mp.ctas_per_part * mp.parts;
     mp.smem = fixed + (size_t)mp.kp * per_centre;
-    mp.tm_x_ptr = mp.tm_c_ptr = mp.tm_aug_ptr = mp.tm_x2_ptr = mp.tm_xaug_ptr = mp.tm_xaug2_ptr = nullptr;
+    mp.tm_x_ptr = mp.tm_c_ptr = mp.tm_aug_ptr = mp.tm_xaug_ptr = nullptr;
     if (!mp.ones) {
         uint16_t h[BM * 16];
         for (int r = 0; r < BM; r++)
@@ -727,19 +748,20 @@ void plan_tc(Ctx &ctx, MixedPlan &mp, int64_t n, int d, int k, bool fp8) {
 }
 
 void launch_tc_assign(Ctx &ctx, MixedPlan &mp, const void *xb, const void *cb, const void *caug, Top2 *out,
-                      DevScalars *sc, const MixedStats *stats, float *dump, Top4 *out4,
+                      Top8 *out8, DevScalars *sc, const MixedStats *stats, float *dump,
                       const unsigned long long *n_dev, const void *xaug, const float *rowscale) {
     const bool fp8 = mp.fp8;
+    if ((mp.topk == 2) != (out != nullptr) || (mp.topk == 8) != (out8 != nullptr)) {
+        set_error("tensor-core launch: records do not match the plan");
+        fail(FK_ERR_INVALID_PARAMETER);
+    }
     const CUtensorMapDataType dt = fp8 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
     const uint64_t es = fp8 ? 1 : 2;
     const uint32_t box_in = fp8 ? 128 : 64;
-    // the second pass reads its own gathered rows: separate tensor maps
-    unsigned char *tmx = out4 ? mp.tm_x2 : mp.tm_x;
-    const void *&tmx_ptr = out4 ? mp.tm_x2_ptr : mp.tm_x_ptr;
-    if (tmx_ptr != xb) {
-        encode_2d(ctx, tmx, xb, (uint64_t)mp.d_pad, (uint64_t)mp.n, (uint64_t)mp.d_pad * es, box_in, BM,
+    if (mp.tm_x_ptr != xb) {
+        encode_2d(ctx, mp.tm_x, xb, (uint64_t)mp.d_pad, (uint64_t)mp.n, (uint64_t)mp.d_pad * es, box_in, BM,
                   CU_TENSOR_MAP_SWIZZLE_128B, dt);
-        tmx_ptr = xb;
+        mp.tm_x_ptr = xb;
     }
     if (mp.tm_c_ptr != cb) {
         encode_2d(ctx, mp.tm_c, cb, (uint64_t)mp.d_pad, (uint64_t)mp.k_pad, (uint64_t)mp.d_pad * es, box_in, BN,
@@ -752,11 +774,10 @@ void launch_tc_assign(Ctx &ctx, MixedPlan &mp, const void *xb, const void *cb, c
     }
     unsigned char *tmo = mp.tm_ones;
     if (fp8) {
-        tmo = out4 ? mp.tm_xaug2 : mp.tm_xaug;
-        const void *&pp = out4 ? mp.tm_xaug2_ptr : mp.tm_xaug_ptr;
-        if (pp != xaug) {
-            encode_2d(ctx, tmo, xaug, 16, (uint64_t)mp.n, 32, 16, BM, CU_TENSOR_MAP_SWIZZLE_32B);
-            pp = xaug;
+        tmo = mp.tm_xaug;
+        if (mp.tm_xaug_ptr != xaug) {
+            encode_2d(ctx, mp.tm_xaug, xaug, 16, (uint64_t)mp.n, 32, 16, BM, CU_TENSOR_MAP_SWIZZLE_32B);
+            mp.tm_xaug_ptr = xaug;
         }
     }
     TcParams p;
@@ -772,14 +793,14 @@ void launch_tc_assign(Ctx &ctx, MixedPlan &mp, const void *xb, const void *cb, c
     p.x_stage_bytes = (uint32_t)p.n_atoms * X_ATOM_BYTES;
     p.off_c = 0;
     p.off_x = p.off_c + (uint32_t)p.n_atoms * p.c_atom_bytes;
-    p.off_aug = p.off_x + XSTAGES * p.x_stage_bytes;
+    p.off_aug = p.off_x + (uint32_t)mp.xst * p.x_stage_bytes;
     p.off_ones = p.off_aug + (uint32_t)mp.kp * 32u;
     p.off_xaug = p.off_ones;
-    p.off_merge = p.off_ones + (fp8 ? XSTAGES * XAUG_BYTES : ONES_BYTES);
-    p.off_bar = p.off_merge + MERGE_BYTES;
+    p.off_merge = p.off_ones + (fp8 ? (uint32_t)mp.xst * XAUG_BYTES : ONES_BYTES);
+    p.off_bar = p.off_merge + merge_bytes(mp.topk);
     p.c_tx_bytes = (uint32_t)p.n_atoms * p.c_atom_bytes + (uint32_t)mp.kp * 32u + (fp8 ? 0u : ONES_BYTES);
     p.out = out;
-    p.out4 = out4;
+    p.out8 = out8;
     p.n_dev = n_dev;
     p.out_stride = mp.n;
     p.err = &sc->error_word;
@@ -791,16 +812,25 @@ void launch_tc_assign(Ctx &ctx, MixedPlan &mp, const void *xb, const void *cb, c
         set_error("tensor-core plan needs %zu bytes of shared memory", smem);
         fail(FK_ERR_UNSUPPORTED);
     }
-    const CUtensorMap *tx = (const CUtensorMap *)tmx, *tcm = (const CUtensorMap *)mp.tm_c,
+    const CUtensorMap *tx = (const CUtensorMap *)mp.tm_x, *tcm = (const CUtensorMap *)mp.tm_c,
                       *ta = (const CUtensorMap *)mp.tm_aug, *to = (const CUtensorMap *)tmo;
     auto go = [&](auto kern) {
         FK_CUDA(cudaFuncSetAttribute((const void *)kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         kern<<<mp.grid, NTHREADS, smem, ctx.stream>>>(*tx, *tcm, *ta, *to, p);
     };
-    if (out4)
-        fp8 ? go(tc_assign_kernel<4, true>) : go(tc_assign_kernel<4, false>);
-    else
-        fp8 ? go(tc_assign_kernel<2, true>) : go(tc_assign_kernel<2, false>);
+    // Instantiations: main pass (top-2) BF16 / FP8 with one or two X stages;
+    // second pass (top-8) BF16 with one or two X stages.
+    if (mp.topk == 8) {
+        if (fp8) {
+            set_error("the second pass runs in BF16");
+            fail(FK_ERR_UNSUPPORTED);
+        }
+        mp.xst == 2 ? go(tc_assign_kernel<8, false, 2>) : go(tc_assign_kernel<8, false, 1>);
+    } else if (fp8) {
+        mp.xst == 2 ? go(tc_assign_kernel<2, true, 2>) : go(tc_assign_kernel<2, true, 1>);
+    } else {
+        mp.xst == 2 ? go(tc_assign_kernel<2, false, 2>) : go(tc_assign_kernel<2, false, 1>);
+    }
     FK_LAUNCH_CHECK();
 }
 

@@ -79,13 +79,13 @@ typedef struct fk_fit_report {
     int64_t rows_assigned;     /* rows x iterations                        */
     int64_t rows_rechecked;    /* mixed: rows whose margin fell inside the
                                   bound and were re-scored (FP32 + FP64)   */
-    int64_t rows_full_rescan;  /* mixed: of those, rows re-scored against
-                                  every centre                             */
+    int64_t rows_full_rescan;  /* mixed: of those, rows whose third score
+                                  was also inside the bound                */
     int64_t rows_fp64;         /* mixed: rows that needed FP64 scores      */
-    int64_t rows_second_pass;  /* mixed: rows scored again by the top-4
-                                  tensor pass (= rows_full_rescan)         */
-    int64_t rows_four;         /* mixed: of those, rows resolved among at
-                                  most four candidates                     */
+    int64_t rows_second_pass;  /* mixed: rows scored again by the BF16
+                                  top-8 tensor pass (= rows_full_rescan)   */
+    int64_t rows_few;          /* mixed: of those, rows resolved among at
+                                  most eight candidates                    */
     int64_t rows_exhaustive;   /* mixed: rows re-scored against every
                                   centre after the second pass             */
     int64_t near_tie_rows;     /* mixed: re-scored rows whose FP64 margin

@@ -107,8 +107,6 @@ PRECISIONS = ["bf16", "fp8"]
 @pytest.mark.parametrize("n,d,k", [(300, 128, 300), (200, 64, 1024), (150, 16, 40), (260, 128, 1024), (129, 100, 7),
                                    (140, 256, 600)])
 def test_tc_accumulators_exact(n, d, k, precision):
-    if precision == "bf16" and d > 192:
-        pytest.skip("the BF16 kernel keeps d <= 192")
     x32, cen = _aniso(n, d, k, seed=n + d + k)
     c = x32[np.random.default_rng(0).choice(n, size=min(k, n), replace=False)].astype(np.float64)
     if c.shape[0] < k:
@@ -183,8 +181,6 @@ def test_fp8_operands_are_scaled_roundings():
 @pytest.mark.parametrize("n,d,k", [(4096, 128, 1024), (5000, 64, 100), (3000, 16, 9), (2500, 100, 300),
                                    (3000, 256, 700)])
 def test_mixed_steps_match_fp64_oracle(n, d, k, precision):
-    if precision == "bf16" and d > 192:
-        pytest.skip("the BF16 kernel keeps d <= 192")
     x32, _ = _aniso(n, d, k, seed=11 * d + k)
     x64 = x32.astype(np.float64)
     c = x64[np.random.default_rng(1).choice(n, size=k, replace=False)].copy()
