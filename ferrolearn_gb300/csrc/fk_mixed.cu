@@ -42,6 +42,7 @@ namespace {
 
 constexpr double ACC_REL_PER_K = 0.0000002384185791015625;  // 2^-22 per accumulated column
 constexpr double REPR_REL = 0.0000002384185791015625;       // 2^-22
+constexpr float REPR_REL_F = 0.0000002384185791015625f;     // 2^-22 (exact)
 
 __device__ __forceinline__ void atomic_max_pos(float *addr, float v) {
     // non-negative floats order like their bit patterns
@@ -185,7 +186,7 @@ __global__ void prep_rows_kernel(const TX *__restrict__ x, int64_t n, int d, int
                 ex2 = __fmaf_rn(e, e, ex2);
                 tn2 = __fmaf_rn(t, t, tn2);
                 xo2 = __fmaf_rn(xv, xv, xo2);
-                amax = fmaxf(amax, fabsf(xv));
+                if (fabsf(xv) < INFINITY) amax = fmaxf(amax, fabsf(xv));  // finite values only
             } else if (FP8) {
                 ((unsigned char *)xq_out)[slot * d_pad + j] = 0;
             } else {
@@ -206,7 +207,7 @@ __global__ void prep_rows_kernel(const TX *__restrict__ x, int64_t n, int d, int
         if (FP8 && lane < 16)
             xaug[slot * 16 + lane] = lane < 3 ? __float2bfloat16_rn(inv) : __float2bfloat16_rn(0.f);
         if (xn < INFINITY) xn_hi = fmaxf(xn_hi, xn);  // NaN / inf rows are re-scored in full
-        if (amax < INFINITY) am_hi = fmaxf(am_hi, amax);
+        am_hi = fmaxf(am_hi, amax);
     }
     if (lane == 0) {
         sh_xn[w] = xn_hi;
@@ -351,18 +352,23 @@ __global__ void prep_aug_kernel(const double *__restrict__ half_norm, int k, int
 // --------------------------------------------------------------- finalize --
 // Threshold on a score margin above which no other centre can win in the
 // FP64 direct form (see the file header): 2E + key quantum + FP64 rounding.
-__device__ __forceinline__ double row_threshold(const float4 ri, const MixedStats *stats, double acc_rel, double mu_norm,
-                                                int d, float v1) {
-    const double xn = ri.x, ex = ri.y, xo = ri.z;
-    const double cn = stats->cn_max, ec = stats->ec_max, ch = stats->ch_max, big = stats->big;
-    const double co = stats->co_max;
-    double e = ex * cn + xn * ec + acc_rel * (xn * ch + big) + REPR_REL * big;
+__device__ __forceinline__ float row_threshold(const float4 ri, const MixedStats *stats, float acc_rel, float mu_norm,
+                                               int d, float v1) {
+    // every step rounds upward, so the result bounds the exact expression
+    const float xn = ri.x, ex = ri.y, xo = ri.z;
+    const float cn = stats->cn_max, ec = stats->ec_max, ch = stats->ch_max, big = stats->big;
+    const float co = stats->co_max;
+    const float e = __fadd_ru(__fadd_ru(__fmul_ru(ex, cn), __fmul_ru(xn, ec)),
+                              __fadd_ru(__fmul_ru(acc_rel, __fadd_ru(__fmul_ru(xn, ch), big)),
+                                        __fmul_ru(REPR_REL_F, big)));
     // keys: each score rounded to a multiple of 128 ulp (error <= 64 ulp) plus a
     // column code below 128 ulp, so a key is within 192 ulp of its score
-    double q = 384.0 * (double)stats->ulp;
-    double xo_b = xo > xn + ex + mu_norm ? xo : xn + ex + mu_norm;  // ||x|| (both bounds are valid)
-    double delta = (double)(d + 4) * 1.1102230246251565e-16 * (xo_b + co) * (xo_b + co);  // FP64 rounding, D units
-    double thr = (2.0 * e + q + 0.5 * delta) * (1.0 + 1e-6) + 1e-30;
+    const float q = 384.f * stats->ulp;
+    const float xo_b = fminf(xo, __fadd_ru(__fadd_ru(xn, ex), mu_norm));  // ||x||: both bounds are valid
+    const float sx = __fadd_ru(xo_b, co);
+    const float delta = __fmul_ru(__fmul_ru(__fmul_ru((float)(d + 4), 1.1102230246251565e-16f), sx), sx);  // FP64 rounding
+    float thr = __fadd_ru(__fmul_ru(__fadd_ru(__fadd_ru(__fmul_ru(2.f, e), q), __fmul_ru(0.5f, delta)), 1.0000012f),
+                          1e-30f);
     if (!(v1 >= stats->big * 0.6f)) thr = INFINITY;  // not a real score (NaN row, all slices padded)
     return thr;
 }
@@ -392,39 +398,63 @@ __device__ __forceinline__ void merge_top2(float &v1, int &i1, float &v2, int &i
     }
 }
 
+// Warp-aggregated list append: the lanes of the calling (converged) group
+// with pred set get consecutive slots from one atomic.
+__device__ __forceinline__ unsigned long long warp_reserve(unsigned long long *counter, bool pred) {
+    const unsigned mask = __activemask();
+    const unsigned want = __ballot_sync(mask, pred);
+    const int lane = threadIdx.x & 31;
+    unsigned long long base = 0;
+    if (want) {
+        const int leader = __ffs(want) - 1;
+        if (lane == leader) base = atomicAdd(counter, (unsigned long long)__popc(want));
+        base = __shfl_sync(mask, base, leader);
+    }
+    return base + (unsigned long long)__popc(want & ((1u << lane) - 1u));
+}
+
 __global__ void finalize_kernel(const Top2 *__restrict__ parts, int nparts, int64_t n, int k, int d,
-                                const float4 *__restrict__ rowinfo, const MixedStats *stats, double acc_rel,
-                                double mu_norm, int32_t *__restrict__ labels, int4 *__restrict__ pair_list,
+                                const float4 *__restrict__ rowinfo, const MixedStats *stats, float acc_rel,
+                                float mu_norm, int32_t *__restrict__ labels, int4 *__restrict__ pair_list,
                                 int32_t *__restrict__ full_list, DevScalars *sc) {
-    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    Top2 t = parts[i];
-    float v1 = t.v1, v2 = t.v2, u3 = t.u3;
-    int i1 = t.i1, i2 = t.i2;
-    for (int p = 1; p < nparts; p++) {
-        Top2 o = parts[(int64_t)p * n + i];
-        merge_top2(v1, i1, v2, i2, u3, o.v1, o.i1, o.v2, o.i2, o.u3);
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int cls = -1;  // 0 certain, 1 pair, 2 full
+    int i1 = -1, i2 = -1;
+    if (i < n) {
+        // all loads first (independent), then the merge
+        const float4 ri = rowinfo[i];
+        Top2 t = parts[i];
+        Top2 o1 = nparts > 1 ? parts[(int64_t)n + i] : t;
+        float v1 = t.v1, v2 = t.v2, u3 = t.u3;
+        i1 = t.i1;
+        i2 = t.i2;
+        if (nparts > 1) merge_top2(v1, i1, v2, i2, u3, o1.v1, o1.i1, o1.v2, o1.i2, o1.u3);
+        for (int p = 2; p < nparts; p++) {
+            Top2 o = parts[(int64_t)p * n + i];
+            merge_top2(v1, i1, v2, i2, u3, o.v1, o.i1, o.v2, o.i2, o.u3);
+        }
+        {  // FP8 rows are scored in units of 1/(s_i t): back to score units (exact powers of two)
+            const float unit = stats->tscale / ri.w;
+            v1 *= unit;
+            v2 *= unit;
+            u3 *= unit;
+        }
+        const float thr = row_threshold(ri, stats, acc_rel, mu_norm, d, v1);
+        const float m12 = __fsub_rd(v1, v2);  // lower bounds of the margins
+        const float m13 = __fsub_rd(v1, u3);
+        if (i1 >= 0 && i1 < k && m12 > thr) {
+            cls = 0;
+            labels[i] = i1;
+        } else if (i1 >= 0 && i1 < k && i2 >= 0 && i2 < k && i1 != i2 && m13 > thr) {
+            cls = 1;
+        } else {
+            cls = 2;
+        }
     }
-    {  // FP8 rows are scored in units of 1/(s_i t): back to score units (exact powers of two)
-        const float unit = stats->tscale / rowinfo[i].w;
-        v1 *= unit;
-        v2 *= unit;
-        u3 *= unit;
-    }
-    const double thr = row_threshold(rowinfo[i], stats, acc_rel, mu_norm, d, v1);
-    double m12 = (double)v1 - (double)v2;
-    if (i1 >= 0 && i1 < k && m12 > thr) {
-        labels[i] = i1;
-        return;
-    }
-    double m13 = (double)v1 - (double)u3;
-    if (i1 >= 0 && i1 < k && i2 >= 0 && i2 < k && i1 != i2 && m13 > thr) {
-        unsigned long long slot = atomicAdd(&sc->flag_count, 1ULL);
-        pair_list[slot] = make_int4((int)i, i1, i2, 0);
-    } else {
-        unsigned long long slot = atomicAdd(&sc->full_count, 1ULL);
-        full_list[slot] = (int32_t)i;
-    }
+    const unsigned long long ps = warp_reserve(&sc->flag_count, cls == 1);
+    if (cls == 1) pair_list[ps] = make_int4((int)i, i1, i2, 0);
+    const unsigned long long fs = warp_reserve(&sc->full_count, cls == 2);
+    if (cls == 2) full_list[fs] = (int32_t)i;
 }
 
 // ------------------------------------------------------------ re-checks --
@@ -584,92 +614,100 @@ __global__ void full_rescore_kernel(const TX *__restrict__ x, int d, const doubl
     }
 }
 
-// One warp per listed row, f32 rows: FP32 distances to every centre, lanes
-// over centres reading the transposed f32 centres (coalesced), 32 distances
-// per lane in registers per batch of 1024 centres; the smallest upper bound
-// UB over all centres, then FP64 (direct form, one lane per centre) for every
-// centre whose lower bound reaches UB or whose FP32 value is not finite.
-__global__ void exhaustive_rescore_kernel(const float *__restrict__ x, int d, const double *__restrict__ c,
-                                          const float *__restrict__ c32t, const float *__restrict__ ec32, int k,
-                                          const int32_t *__restrict__ list, const unsigned long long *count_ptr,
-                                          DevScalars *sc, int32_t *__restrict__ labels) {
-    const unsigned long long cnt = *count_ptr;
-    const int lane = threadIdx.x & 31;
-    const unsigned long long wid = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const unsigned long long nw = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
-    for (unsigned long long s = wid; s < cnt; s += nw) {
-        const int64_t r = list[s];
-        const float *row = x + r * d;
-        // pass 1: smallest upper bound over all centres
-        float ub = INFINITY;
-        float acc[32];
-        for (int c0 = 0; c0 < k; c0 += 1024) {
+// One CTA per listed row, f32 rows: the row in shared memory, FP32 distances
+// to every centre (threads over centres, four centres per thread at a time,
+// reading the transposed f32 centres: coalesced and L2-resident), kept in
+// shared memory for chunks of EX_CHUNK centres; the smallest upper bound UB
+// over all centres; then FP64 (direct form) for every centre whose lower
+// bound reaches UB or whose FP32 value is not finite, lowest index on ties.
+constexpr int EX_CHUNK = 8192;
+constexpr int EX_THREADS = 256;
+
+__device__ __forceinline__ void ex_chunk_dists(const float *__restrict__ xs, int d, const float *__restrict__ c32t,
+                                               int k, int c0, int c1, float *__restrict__ dist) {
+    for (int q0 = c0 + (int)threadIdx.x; q0 < c1; q0 += 4 * EX_THREADS) {
+        float a[4] = {0.f, 0.f, 0.f, 0.f};
+        for (int j = 0; j < d; j++) {
+            const float xv = xs[j];
+            const float *ct = c32t + (int64_t)j * k;
 #pragma unroll
-            for (int u = 0; u < 32; u++) acc[u] = 0.f;
-            for (int j = 0; j < d; j++) {
-                const float xv = row[j];
-                const float *ct = c32t + (int64_t)j * k;
-#pragma unroll
-                for (int u = 0; u < 32; u++) {
-                    const int q = c0 + u * 32 + lane;
-                    if (q < k) {
-                        const float t = xv - ct[q];
-                        acc[u] = fmaf(t, t, acc[u]);
-                    }
+            for (int u = 0; u < 4; u++) {
+                const int q = q0 + u * EX_THREADS;
+                if (q < c1) {
+                    const float t = xv - ct[q];
+                    a[u] = fmaf(t, t, a[u]);
                 }
             }
+        }
 #pragma unroll
-            for (int u = 0; u < 32; u++) {
-                const int q = c0 + u * 32 + lane;
-                if (q < k) {
-                    const float hi = __fadd_ru(acc[u], bound32(acc[u], ec32[q], d));
-                    if (hi < ub) ub = hi;  // NaN never lowers the bound
-                }
+        for (int u = 0; u < 4; u++)
+            if (q0 + u * EX_THREADS < c1) dist[q0 + u * EX_THREADS - c0] = a[u];
+    }
+}
+
+__global__ void __launch_bounds__(EX_THREADS) exhaustive_rescore_kernel(
+    const float *__restrict__ x, int d, const double *__restrict__ c, const float *__restrict__ c32t,
+    const float *__restrict__ ec32, int k, const int32_t *__restrict__ list, const unsigned long long *count_ptr,
+    DevScalars *sc, int32_t *__restrict__ labels) {
+    extern __shared__ float ex_smem[];
+    const int d_al = (d + 3) & ~3;
+    float *xs = ex_smem;
+    float *dist = ex_smem + d_al;
+    __shared__ float red_f[EX_THREADS / 32];
+    __shared__ double red_b1[EX_THREADS / 32], red_b2[EX_THREADS / 32];
+    __shared__ int red_i[EX_THREADS / 32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const unsigned long long cnt = *count_ptr;
+    const int nchunks = (k + EX_CHUNK - 1) / EX_CHUNK;
+    for (unsigned long long s = blockIdx.x; s < cnt; s += gridDim.x) {
+        const int64_t r = list[s];
+        const float *row = x + r * d;
+        for (int j = threadIdx.x; j < d; j += EX_THREADS) xs[j] = row[j];
+        __syncthreads();
+        // pass 1: smallest upper bound over all centres (each thread reads back
+        // only the distances it wrote itself)
+        float ub = INFINITY;
+        for (int ch = 0; ch < nchunks; ch++) {
+            const int c0 = ch * EX_CHUNK, c1 = min(k, c0 + EX_CHUNK);
+            ex_chunk_dists(xs, d, c32t, k, c0, c1, dist);
+            for (int q = c0 + (int)threadIdx.x; q < c1; q += EX_THREADS) {
+                const float dv = dist[q - c0];
+                const float hi = __fadd_ru(dv, bound32(dv, ec32[q], d));
+                if (hi < ub) ub = hi;  // NaN never lowers the bound
             }
         }
 #pragma unroll
         for (int off = 16; off >= 1; off >>= 1) ub = fminf(ub, __shfl_xor_sync(0xffffffffu, ub, off));
-        // pass 2: FP64 on the survivors (the distances of the first batch are
-        // still in registers when k <= 1024; larger k recomputes them)
+        if (lane == 0) red_f[w] = ub;
+        __syncthreads();
+        ub = red_f[0];
+#pragma unroll
+        for (int q = 1; q < EX_THREADS / 32; q++) ub = fminf(ub, red_f[q]);
+        // pass 2: FP64 on the survivors, in increasing centre order per thread
         double b1 = DBL_MAX, b2 = DBL_MAX;
         int i1 = INT32_MAX;
-        for (int c0 = 0; c0 < k; c0 += 1024) {
-            if (c0 > 0 || k > 1024) {
-#pragma unroll
-                for (int u = 0; u < 32; u++) acc[u] = 0.f;
-                for (int j = 0; j < d; j++) {
-                    const float xv = row[j];
-                    const float *ct = c32t + (int64_t)j * k;
-#pragma unroll
-                    for (int u = 0; u < 32; u++) {
-                        const int q = c0 + u * 32 + lane;
-                        if (q < k) {
-                            const float t = xv - ct[q];
-                            acc[u] = fmaf(t, t, acc[u]);
-                        }
+        for (int ch = 0; ch < nchunks; ch++) {
+            const int c0 = ch * EX_CHUNK, c1 = min(k, c0 + EX_CHUNK);
+            if (nchunks > 1) ex_chunk_dists(xs, d, c32t, k, c0, c1, dist);
+            for (int q = c0 + (int)threadIdx.x; q < c1; q += EX_THREADS) {
+                const float dv = dist[q - c0];
+                if (!(__fsub_rd(dv, bound32(dv, ec32[q], d)) > ub)) {
+                    const double v = sqeuc64(xs, c + (int64_t)q * d, d);
+                    if (v < b1) {
+                        b2 = b1;
+                        b1 = v;
+                        i1 = q;
+                    } else if (v < b2) {
+                        b2 = v;
                     }
                 }
-            }
-            uint32_t cand = 0;
-#pragma unroll
-            for (int u = 0; u < 32; u++) {
-                const int q = c0 + u * 32 + lane;
-                if (q < k && !(__fsub_rd(acc[u], bound32(acc[u], ec32[q], d)) > ub)) cand |= 1u << u;
-            }
-            while (cand) {  // increasing centre index within this lane
-                const int u = __ffs(cand) - 1;
-                cand &= cand - 1;
-                const int q = c0 + u * 32 + lane;
-                const double v = sqeuc64(row, c + (int64_t)q * d, d);
-                if (v < b1) { b2 = b1; b1 = v; i1 = q; }
-                else if (v < b2) { b2 = v; }
             }
         }
 #pragma unroll
         for (int off = 16; off >= 1; off >>= 1) {
-            double o1 = __shfl_xor_sync(0xffffffffu, b1, off);
-            double o2 = __shfl_xor_sync(0xffffffffu, b2, off);
-            int oi = __shfl_xor_sync(0xffffffffu, i1, off);
+            const double o1 = __shfl_xor_sync(0xffffffffu, b1, off);
+            const double o2 = __shfl_xor_sync(0xffffffffu, b2, off);
+            const int oi = __shfl_xor_sync(0xffffffffu, i1, off);
             if (o1 < b1 || (o1 == b1 && oi < i1)) {
                 b2 = fmin(b1, o2);
                 b1 = o1;
@@ -679,11 +717,37 @@ __global__ void exhaustive_rescore_kernel(const float *__restrict__ x, int d, co
             }
         }
         if (lane == 0) {
+            red_b1[w] = b1;
+            red_b2[w] = b2;
+            red_i[w] = i1;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            b1 = red_b1[0];
+            b2 = red_b2[0];
+            i1 = red_i[0];
+            for (int q = 1; q < EX_THREADS / 32; q++) {
+                const double o1 = red_b1[q], o2 = red_b2[q];
+                const int oi = red_i[q];
+                if (o1 < b1 || (o1 == b1 && oi < i1)) {
+                    b2 = fmin(b1, o2);
+                    b1 = o1;
+                    i1 = oi;
+                } else {
+                    b2 = fmin(b2, o1);
+                }
+            }
             labels[r] = i1 == INT32_MAX ? 0 : i1;
             atomicAdd(&sc->recheck_rows, 1ULL);
+            atomicAdd(&sc->full_rows, 1ULL);
             if (i1 != INT32_MAX && b2 < DBL_MAX && near_tie(b1, b2)) atomicAdd(&sc->near_tie_rows, 1ULL);
         }
+        __syncthreads();  // xs, dist and the reduction slots are reused by the next row
     }
+}
+
+size_t exhaustive_smem_bytes(int d, int k) {
+    return sizeof(float) * ((size_t)((d + 3) & ~3) + (size_t)std::min(k, EX_CHUNK));
 }
 
 // ------------------------------------------------------- second pass --
@@ -716,7 +780,7 @@ __device__ __forceinline__ uint32_t ins8u(uint32_t (&R)[8], int (&I)[8], uint32_
 
 __global__ void finalize8_kernel(const Top8 *__restrict__ parts, int nparts, int64_t cap, int k, int d,
                                  const int32_t *__restrict__ list, const float4 *__restrict__ rowinfo2,
-                                 const MixedStats *stats2, double acc_rel, double mu_norm,
+                                 const MixedStats *stats2, float acc_rel, float mu_norm,
                                  int32_t *__restrict__ labels, Oct *__restrict__ octs, int32_t *__restrict__ ex_list,
                                  DevScalars *sc) {
     const unsigned long long cnt = sc->full_count;
@@ -742,24 +806,27 @@ __global__ void finalize8_kernel(const Top8 *__restrict__ parts, int nparts, int
         const int32_t row = list[s];
         const float4 ri = rowinfo2[s];
         const float v1 = __uint_as_float(R[0]);
-        const double thr = row_threshold(ri, stats2, acc_rel, mu_norm, d, v1);
-        const bool rest_out = (double)v1 - (double)__uint_as_float(U) > thr;
+        const float thr = row_threshold(ri, stats2, acc_rel, mu_norm, d, v1);
+        const bool rest_out = __fsub_rd(v1, __uint_as_float(U)) > thr;
         int m = 0;
         bool valid = true;
 #pragma unroll
         for (int j = 0; j < 8; j++) {
-            if ((double)v1 - (double)__uint_as_float(R[j]) <= thr) {
+            if (!(__fsub_rd(v1, __uint_as_float(R[j])) > thr)) {
                 m++;
                 if (I[j] < 0 || I[j] >= k) valid = false;
             }
         }
-        if (!rest_out || !valid || m == 0) {
-            unsigned long long slot = atomicAdd(&sc->ex_count, 1ULL);
-            ex_list[slot] = row;
+        const bool to_ex = !rest_out || !valid || m == 0;
+        const bool to_oct = !to_ex && m > 1;
+        const unsigned long long es = warp_reserve(&sc->ex_count, to_ex);
+        const unsigned long long os = warp_reserve(&sc->quad_count, to_oct);
+        if (to_ex) {
+            ex_list[es] = row;
         } else if (m == 1) {
             labels[row] = I[0];
         } else {
-            unsigned long long slot = atomicAdd(&sc->quad_count, 1ULL);
+            const unsigned long long slot = os;
             Oct o;
             o.row = row;
             o.m = m;
@@ -855,6 +922,35 @@ __global__ void oct_rescore_kernel(const float *__restrict__ x, int d, const dou
 }
 
 // ---------------------------------------------------- mixed inertia --
+// Two-level fixed-order sum of the per-(cluster, feature) partials: block b
+// folds its contiguous range (four interleaved chains per thread, then a
+// tree), then one block folds the block sums in order. Deterministic.
+constexpr int INERTIA_BLOCKS = 256;
+__global__ void inertia_partial_kernel(const double *__restrict__ part, int64_t m, double *__restrict__ out) {
+    __shared__ double sh[32];
+    const int64_t per = (m + gridDim.x - 1) / gridDim.x;
+    const int64_t lo = (int64_t)blockIdx.x * per, hi = min(m, lo + per);
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+    int64_t i = lo + threadIdx.x;
+    for (; i + 3 * (int64_t)blockDim.x < hi; i += 4 * (int64_t)blockDim.x) {
+        a0 += part[i];
+        a1 += part[i + blockDim.x];
+        a2 += part[i + 2 * blockDim.x];
+        a3 += part[i + 3 * blockDim.x];
+    }
+    for (; i < hi; i += blockDim.x) a0 += part[i];
+    double s = (a0 + a1) + (a2 + a3);
+    s = warp_sum_d(s);
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) sh[w] = s;
+    __syncthreads();
+    if (w == 0) {
+        double r = lane < (int)(blockDim.x >> 5) ? sh[lane] : 0.0;
+        r = warp_sum_d(r);
+        if (lane == 0) out[blockIdx.x] = r;
+    }
+}
+
 __global__ void inertia_final_kernel(const double *__restrict__ part, int64_t m, double *out) {
     __shared__ double sh[32];
     double s = 0.0;
@@ -969,6 +1065,12 @@ __global__ void rowscale_kernel(const float4 *__restrict__ rowinfo, int64_t n, c
     if (i < n) rowscale[i] = rowinfo[i].w * stats->inv_t;
 }
 
+// ||mu|| as an f32 upper bound.
+float mu_norm_up(double v) {
+    const float f = (float)v;
+    return (double)f >= v ? f : std::nextafter(f, INFINITY);
+}
+
 // Second pass over the rows listed in full (count sc->full_count): BF16
 // operands made from their f32 values, a top-8 tensor pass, then the
 // re-score of at most eight candidates, or of every centre.
@@ -997,14 +1099,15 @@ void second_pass(Ctx &ctx, const float *x, int64_t n, int d, const double *c, in
     prep_aug_kernel<<<(m2.k_pad + 255) / 256, 256, 0, s>>>(hn2, k, m2.k_pad, false, caug2, st2);
     FK_LAUNCH_CHECK();
     launch_tc_assign(ctx, m2, xb2, cb2, caug2, nullptr, top8, sc, st2, nullptr, &sc->full_count);
-    const double acc_rel2 = (double)((size_t)m2.d_pad + 32) * ACC_REL_PER_K;
+    const float acc_rel2 = (float)((double)((size_t)m2.d_pad + 32) * ACC_REL_PER_K);  // exact: integer * 2^-22
     const int grid = ctx.num_sms * 4;
-    finalize8_kernel<<<grid, 256, 0, s>>>(top8, m2.parts, n, k, d, full, ri2, st2, acc_rel2, mu_norm, labels, octs,
-                                          ex, sc);
+    finalize8_kernel<<<grid, 256, 0, s>>>(top8, m2.parts, n, k, d, full, ri2, st2, acc_rel2, mu_norm_up(mu_norm),
+                                          labels, octs, ex, sc);
     FK_LAUNCH_CHECK();
     oct_rescore_kernel<<<grid, 256, 0, s>>>(x, d, c, B.c32, B.ec32, octs, sc, labels);
     FK_LAUNCH_CHECK();
-    exhaustive_rescore_kernel<<<grid, 256, 0, s>>>(x, d, c, B.c32t, B.ec32, k, ex, &sc->ex_count, sc, labels);
+    exhaustive_rescore_kernel<<<ctx.num_sms * 2, EX_THREADS, exhaustive_smem_bytes(d, k), s>>>(
+        x, d, c, B.c32t, B.ec32, k, ex, &sc->ex_count, sc, labels);
     FK_LAUNCH_CHECK();
 }
 
@@ -1044,9 +1147,9 @@ void run_assign_mixed(Ctx &ctx, const TX *x, int64_t n, int d, const double *c, 
 
     int4 *pairs = (int4 *)ctx.get(BUF_FLAGS, sizeof(int4) * (size_t)n);
     int32_t *full = (int32_t *)ctx.get(BUF_FULL, sizeof(int32_t) * (size_t)n);
-    const double acc_rel = (double)((size_t)mp.d_pad + 32) * ACC_REL_PER_K;
+    const float acc_rel = (float)((double)((size_t)mp.d_pad + 32) * ACC_REL_PER_K);  // exact: integer * 2^-22
     finalize_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(top, mp.parts, n, k, d, B.rowinfo, B.stats, acc_rel,
-                                                               mp.mu_norm, labels, pairs, full, sc);
+                                                               mu_norm_up(mp.mu_norm), labels, pairs, full, sc);
     FK_LAUNCH_CHECK();
     const int grid = ctx.num_sms * 4;
     pair_rescore_kernel<TX><<<grid, 256, 0, s>>>(x, d, c, B.c32, B.ec32, pairs, sc, labels);
@@ -1060,7 +1163,10 @@ void run_assign_mixed(Ctx &ctx, const TX *x, int64_t n, int d, const double *c, 
 }
 
 void launch_mixed_inertia(Ctx &ctx, const double *part, int64_t m, DevScalars *sc) {
-    inertia_final_kernel<<<1, 1024, 0, ctx.stream>>>(part, m, &sc->inertia);
+    double *blocks = (double *)ctx.get(BUF_INERTIA2, sizeof(double) * INERTIA_BLOCKS);
+    inertia_partial_kernel<<<INERTIA_BLOCKS, 256, 0, ctx.stream>>>(part, m, blocks);
+    FK_LAUNCH_CHECK();
+    inertia_final_kernel<<<1, 256, 0, ctx.stream>>>(blocks, INERTIA_BLOCKS, &sc->inertia);
     FK_LAUNCH_CHECK();
 }
 

@@ -283,9 +283,36 @@ constexpr int FIX_U = 8;        // rows loaded ahead per thread
 
 struct alignas(16) FixedPart {
     unsigned long long lo, hi;  // signed 128-bit partial sum (two's complement)
-    float isum, icomp;          // compensated f32 partial inertia
+    double inert;               // partial inertia (compensated f32 sums, folded in f64)
     uint32_t flags, pad;
 };
+
+// Signed 128-bit fixed-point accumulation of one finite value (non-finite
+// values are skipped: the caller detects them separately).
+__device__ __noinline__ void fixed_add_signed(uint64_t &lo, uint64_t &hi, float x, int F) {
+    const uint32_t b = __float_as_uint(x);
+    const uint32_t ex = (b >> 23) & 0xFFu;
+    if (ex == 0xFFu) return;
+    const uint64_t m = (uint64_t)((b & 0x7FFFFFu) | (ex ? 0x800000u : 0u));
+    const int s = (ex ? (int)ex : 1) - 150 + F;
+    uint64_t tlo, thi;
+    if (s >= 64) {
+        tlo = 0;
+        thi = m << (s - 64);
+    } else if (s >= 0) {
+        tlo = m << s;
+        thi = s > 40 ? m >> (64 - s) : 0;
+    } else {
+        tlo = s > -32 ? m >> (-s) : 0;
+        thi = 0;
+    }
+    if (b >> 31) {  // two's complement of the 128-bit magnitude
+        tlo = ~tlo;
+        thi = ~thi;
+        add128(tlo, thi, 1ull, 0ull);
+    }
+    add128(lo, hi, tlo, thi);
+}
 
 __device__ __forceinline__ int fixed_bits(const float *amax_ptr, int64_t n) {
     // fraction bits: n * max|x| * 2^F < 2^126, so no partial sum can overflow
@@ -340,7 +367,176 @@ __global__ void centroid_fixed_part_kernel(const float *__restrict__ x, int d, i
     if (j < d) {
         unsigned long long lo = a.plo, hi = a.phi;
         asm("sub.cc.u64 %0, %0, %2;\n\tsubc.u64 %1, %1, %3;" : "+l"(lo), "+l"(hi) : "l"(a.nlo), "l"(a.nhi));
-        parts[((int64_t)c * FIX_SPLIT + y) * d + j] = FixedPart{lo, hi, isum, icomp, a.flags, 0u};
+        parts[((int64_t)c * FIX_SPLIT + y) * d + j] = FixedPart{lo, hi, (double)isum - (double)icomp, a.flags, 0u};
+    }
+}
+
+// Vectorised form for d % 4 == 0 (16-byte aligned X): thread (g, sl) owns the
+// four features of float4 slot sl and the rows g, g + G, ... of the block's
+// share (G = 256 / (d / 4) row groups), four rows in flight; the groups'
+// exact sums are then added in shared memory (integer adds: order-free) and
+// their inertia partials folded in group order (deterministic).
+//
+// Exact split on two grids instead of per-element shifts: with 2^ea <= max|x|
+// < 2^(ea+1), kb = ea + 2 and C1 = 1.5 * 2^kb, every finite |x| < 2^kb / 2, so
+// x + C1 stays in [2^kb, 2^(kb+1)] and its bit pattern minus that of C1 is
+// the integer q1 = round(x / 2^(kb-23)) (|q1| <= 2^22); r = x - ((x + C1) - C1)
+// is exact with |r| <= 2^(kb-24), and the same step on C2 = 1.5 * 2^(kb-23)
+// gives q2 (unit 2^(kb-46)) and an exact remainder r2, which is zero unless
+// |x| < 2^(ea-21); the rare non-zero r2 goes through fixed_add. So
+// x = q1 2^(kb-23) + q2 2^(kb-46) + r2 exactly, and the sums of q1, q2 are
+// integers. Non-finite values are detected with x * 0 (NaN for inf and NaN)
+// and their flags recomputed from the rows. The inertia term sums (x - c)^2
+// of four rows in f32 and adds that to a compensated (Kahan) f32 sum.
+constexpr int FIX4_THREADS = 256;
+constexpr int FIX4_U = 4;      // rows per thread and step
+constexpr int FIX4_IDX = 1024; // member indices staged per chunk
+
+struct FixRed {
+    uint64_t lo[4], hi[4];
+    double inert[4];
+    uint32_t flags[4];
+};
+
+// signed 128-bit v = a * 2^sh (sh >= 0) added to (lo, hi)
+__device__ __forceinline__ void add_shifted(uint64_t &lo, uint64_t &hi, long long a, int sh) {
+    const __int128 v = (__int128)a << sh;
+    add128(lo, hi, (uint64_t)v, (uint64_t)((unsigned __int128)v >> 64));
+}
+
+__global__ void __launch_bounds__(FIX4_THREADS) centroid_fixed_part4_kernel(
+    const float *__restrict__ x, int d, int k, int64_t n, const int32_t *__restrict__ members,
+    const int32_t *__restrict__ offs, int64_t nseg, const double *__restrict__ old_c,
+    const float *__restrict__ amax_ptr, FixedPart *__restrict__ parts) {
+    __shared__ FixRed red[FIX4_THREADS];
+    __shared__ int32_t sidx[FIX4_IDX];
+    const int S = d >> 2;
+    const int G = FIX4_THREADS / S;
+    const int g = (int)threadIdx.x / S, sl = (int)threadIdx.x % S;
+    const bool active = g < G;
+    const int c = blockIdx.x, y = blockIdx.y;
+    const int64_t cstart = offs[(int64_t)c * nseg];
+    const int64_t cend = (c + 1 < k) ? (int64_t)offs[(int64_t)(c + 1) * nseg] : n;
+    const int64_t share = (cend - cstart + FIX_SPLIT - 1) / FIX_SPLIT;
+    const int64_t start = cstart + (int64_t)y * share;
+    const int64_t end = min(cend, start + share);
+    const int F = fixed_bits(amax_ptr, n);
+    const float amax = *amax_ptr;
+    const int ea = amax > 0.f ? (int)((__float_as_uint(amax) >> 23) & 0xFFu) - 127 : -126;
+    // grids of the split; outside this exponent range every value takes the exact slow path
+    const bool grids = ea >= -90 && ea <= 100;
+    const int kb = ea + 2;
+    const float C1 = grids ? ldexpf(1.5f, kb) : 0.f, C2 = grids ? ldexpf(1.5f, kb - 23) : 0.f;
+    const int b1 = __float_as_int(C1), b2 = __float_as_int(C2);
+    long long acc1[4], acc2[4];
+    uint64_t slo[4], shi[4];
+    float isum[4], icomp[4], cj[4], probe[4];
+#pragma unroll
+    for (int f = 0; f < 4; f++) {
+        acc1[f] = acc2[f] = 0;
+        slo[f] = shi[f] = 0;
+        isum[f] = icomp[f] = probe[f] = 0.f;
+        cj[f] = active ? (float)old_c[(int64_t)c * d + 4 * sl + f] : 0.f;
+    }
+    // the block's member indices are staged in shared memory; the row loads of
+    // the next step are issued before the current step is processed
+    for (int64_t cb = start; cb < end; cb += FIX4_IDX) {
+        const int cnt = (int)min((int64_t)FIX4_IDX, end - cb);
+        __syncthreads();
+        for (int t = threadIdx.x; t < cnt; t += FIX4_THREADS) sidx[t] = members[cb + t];
+        __syncthreads();
+        if (!active) continue;
+        float4 cur[FIX4_U], nxt[FIX4_U];
+#pragma unroll
+        for (int u = 0; u < FIX4_U; u++) {
+            const int r = g + u * G;
+            cur[u] = r < cnt ? reinterpret_cast<const float4 *>(x + (int64_t)sidx[r] * d)[sl]
+                             : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+        for (int r0 = g; r0 < cnt; r0 += G * FIX4_U) {
+#pragma unroll
+            for (int u = 0; u < FIX4_U; u++) {
+                const int r = r0 + (u + FIX4_U) * G;
+                nxt[u] = r < cnt ? reinterpret_cast<const float4 *>(x + (int64_t)sidx[r] * d)[sl]
+                                 : make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+            float pf[4] = {0.f, 0.f, 0.f, 0.f};
+            int q1s[4] = {0, 0, 0, 0}, q2s[4] = {0, 0, 0, 0};
+#pragma unroll
+            for (int u = 0; u < FIX4_U; u++) {
+                const bool valid = r0 + u * G < cnt;
+                const float e[4] = {cur[u].x, cur[u].y, cur[u].z, cur[u].w};
+#pragma unroll
+                for (int f = 0; f < 4; f++) {
+                    const float xv = e[f];  // rows past the end read as 0
+                    probe[f] = __fmaf_rn(xv, 0.f, probe[f]);
+                    if (grids) {
+                        const float s1 = __fadd_rn(xv, C1);
+                        q1s[f] += __float_as_int(s1) - b1;
+                        const float r = __fsub_rn(xv, __fsub_rn(s1, C1));
+                        const float s2 = __fadd_rn(r, C2);
+                        q2s[f] += __float_as_int(s2) - b2;
+                        const float r2 = __fsub_rn(r, __fsub_rn(s2, C2));
+                        if (r2 != 0.f) fixed_add_signed(slo[f], shi[f], r2, F);
+                    } else {
+                        fixed_add_signed(slo[f], shi[f], xv, F);
+                    }
+                    const float df = __fsub_rn(xv, cj[f]);
+                    pf[f] = valid ? __fmaf_rn(df, df, pf[f]) : pf[f];
+                }
+            }
+#pragma unroll
+            for (int f = 0; f < 4; f++) {
+                acc1[f] += q1s[f];
+                acc2[f] += q2s[f];
+                const float yy = __fsub_rn(pf[f], icomp[f]);
+                const float tt = __fadd_rn(isum[f], yy);
+                icomp[f] = __fsub_rn(__fsub_rn(tt, isum[f]), yy);
+                isum[f] = tt;
+            }
+#pragma unroll
+            for (int u = 0; u < FIX4_U; u++) cur[u] = nxt[u];
+        }
+    }
+    FixRed mine;
+#pragma unroll
+    for (int f = 0; f < 4; f++) {
+        uint64_t lo = slo[f], hi = shi[f];
+        if (grids) {
+            add_shifted(lo, hi, acc1[f], kb - 23 + F);  // kb - 23 + F = 103 - log2 n >= 72
+            add_shifted(lo, hi, acc2[f], kb - 46 + F);
+        }
+        uint32_t fl = 0u;
+        if (active && !(probe[f] == 0.f)) {
+            // a non-finite value in this thread's rows: recompute its flags
+            for (int64_t r = start + g; r < end; r += G) {
+                const float xv = x[(int64_t)members[r] * d + 4 * sl + f];
+                const uint32_t bb = __float_as_uint(xv);
+                if (((bb >> 23) & 0xFFu) == 0xFFu) fl |= (bb & 0x7FFFFFu) ? 1u : ((bb >> 31) ? 4u : 2u);
+            }
+        }
+        mine.lo[f] = lo;
+        mine.hi[f] = hi;
+        mine.inert[f] = (double)isum[f] - (double)icomp[f];
+        mine.flags[f] = fl;
+    }
+    red[threadIdx.x] = mine;
+    __syncthreads();
+    if (g == 0) {
+        FixRed t = red[sl];
+        for (int gg = 1; gg < G; gg++) {
+            const FixRed &o = red[gg * S + sl];
+#pragma unroll
+            for (int f = 0; f < 4; f++) {
+                add128(t.lo[f], t.hi[f], o.lo[f], o.hi[f]);
+                t.inert[f] += o.inert[f];
+                t.flags[f] |= o.flags[f];
+            }
+        }
+#pragma unroll
+        for (int f = 0; f < 4; f++)
+            parts[((int64_t)c * FIX_SPLIT + y) * d + 4 * sl + f] =
+                FixedPart{t.lo[f], t.hi[f], t.inert[f], t.flags[f], 0u};
     }
 }
 
@@ -364,7 +560,7 @@ __global__ void centroid_fixed_combine_kernel(int d, int k, int64_t n, const int
         const FixedPart q = parts[((int64_t)c * FIX_SPLIT + y) * d + j];
         asm("add.cc.u64 %0, %0, %2;\n\taddc.u64 %1, %1, %3;" : "+l"(lo), "+l"(hi) : "l"(q.lo), "l"(q.hi));
         fl |= q.flags;
-        inert += (double)q.isum - (double)q.icomp;
+        inert += q.inert;
     }
     const int64_t cntc = cend - cstart;
     double mean;
@@ -483,10 +679,16 @@ void launch_update_centroids_exact(const SortPlan &p, const float *x, int d, con
     FixedPart *parts = (FixedPart *)scratch;
     FK_CUDA(cudaMemsetAsync(&scalars->shift_bits, 0, sizeof(unsigned long long), s));
     if (d == 0 || p.k == 0) return;
-    int threads = d >= 256 ? 256 : (d + 31) / 32 * 32;
-    dim3 grid((unsigned)p.k, FIX_SPLIT, (unsigned)((d + threads - 1) / threads));
-    centroid_fixed_part_kernel<<<grid, threads, 0, s>>>(x, d, p.k, p.n, members, seg_hist, p.nseg, old_c, amax,
-                                                        parts);
+    if (d % 4 == 0 && d / 4 <= FIX4_THREADS && ((uintptr_t)x & 15u) == 0) {
+        dim3 grid((unsigned)p.k, FIX_SPLIT);
+        centroid_fixed_part4_kernel<<<grid, FIX4_THREADS, 0, s>>>(x, d, p.k, p.n, members, seg_hist, p.nseg, old_c,
+                                                                  amax, parts);
+    } else {
+        int threads = d >= 256 ? 256 : (d + 31) / 32 * 32;
+        dim3 grid((unsigned)p.k, FIX_SPLIT, (unsigned)((d + threads - 1) / threads));
+        centroid_fixed_part_kernel<<<grid, threads, 0, s>>>(x, d, p.k, p.n, members, seg_hist, p.nseg, old_c, amax,
+                                                            parts);
+    }
     FK_LAUNCH_CHECK();
     const int64_t kd = (int64_t)p.k * d;
     centroid_fixed_combine_kernel<<<(unsigned)((kd + 255) / 256), 256, 0, s>>>(d, p.k, p.n, seg_hist, p.nseg, old_c,
