@@ -25,7 +25,11 @@ Other workloads (--workload; parity cases of the same path, measured on
 request): bisector = n=8,000,000 d=256 k=4096 with 10% bisector rows, FP8,
 20 iterations, then predict on 2,000,000 fresh rows (reported as
 predict_rows_per_s); dirichlet = n=1,000,000 d=64 k=256, plain f32 / f64,
-k-means++ init on the GPU (timed separately as kpp_ms).
+k-means++ init on the GPU (timed separately as kpp_ms); batched = 512
+independent problems (n log-uniform in [2,000, 200,000], d in {8,16,32,64},
+k in [4,64]) x 10 k-means++ restarts, one fit_batched call per step (f32
+distances, FP64 centroid sums); value = Lloyd iterations over all 5,120 fits
+per second of the call, pt_k_per_s = sum of n * k * iterations per second.
 
 --impl reference times the CPU restatement of the reference (oracle/, the
 reference is Rust and cannot be built here) on a bounded row sample of the
@@ -53,7 +57,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--form", default="auto", choices=["auto", "bf16", "fp8", "fp32", "fp64"])
-    ap.add_argument("--workload", default="anisotropic", choices=["anisotropic", "bisector", "dirichlet"])
+    ap.add_argument("--workload", default="anisotropic", choices=["anisotropic", "bisector", "dirichlet", "batched"])
     ap.add_argument("--scale", type=float, default=1.0, help="fraction of the full row count")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true")
@@ -137,7 +141,7 @@ def make_workload(args):
     return W.anisotropic_1024x128(scale=args.scale)
 
 
-DEFAULT_FORM = {"anisotropic": "bf16", "bisector": "fp8", "dirichlet": "fp32"}
+DEFAULT_FORM = {"anisotropic": "bf16", "bisector": "fp8", "dirichlet": "fp32", "batched": "fp32"}
 
 
 def initial_centres(w, xd, ctx):
@@ -216,7 +220,92 @@ def run_reference(args):
     print(json.dumps(out))
 
 
+def run_batched(args):
+    """The batched workload: one fit_batched call per step."""
+    import torch
+
+    import ferrolearn_gb300 as F
+    from ferrolearn_gb300 import _native
+    from ferrolearn_gb300 import workloads as W
+
+    dev = torch.cuda.current_device()
+    probs = W.batched_512(scale=args.scale)
+    stream = torch.cuda.Stream()
+    ctx = F.Context(dev, stream=stream.cuda_stream)
+    dprobs = [dict(p, x=torch.from_numpy(p["x"]).to(dev)) for p in probs]
+    torch.cuda.synchronize()
+    for _ in range(max(1, args.warmup)):
+        F.fit_batched(dprobs, reduction="f64", ctx=ctx)
+    l0 = _native.lib().fk_debug_launch_count()
+    times, reps = [], []
+    with ClockSampler(dev) as clocks:
+        for _ in range(args.steps):
+            torch.cuda.synchronize()
+            start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            start.record(stream)
+            _, rep = F.fit_batched(dprobs, reduction="f64", ctx=ctx)
+            end.record(stream)
+            torch.cuda.synchronize()
+            times.append(start.elapsed_time(end))
+            reps.append(rep)
+    launches = int(_native.lib().fk_debug_launch_count() - l0)
+    ms = float(np.sum(times))
+    iters = sum(r["iterations_total"] for r in reps)
+    nk = 0.0
+    for r in reps:
+        f0 = 0
+        for p in probs:
+            nk += float(p["x"].shape[0]) * p["k"] * float(r["fit_n_iter"][f0:f0 + p["n_init"]].sum())
+            f0 += p["n_init"]
+    rep = reps[-1]
+    out = {
+        "metric": METRIC, "value": iters / (ms / 1e3), "unit": "iters/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 (f64 centroid sums)", "data": "synthetic", "form": "batched",
+        "config": {"workload": "batched_512", "problems": len(probs), "fits": rep["fits"],
+                   "rows_total": int(sum(p["x"].shape[0] for p in probs)), "n_init": 10,
+                   "init": "k-means++ per restart (seeded)", "tol": 1e-4, "reduction": "f64",
+                   "l2": "inputs larger than L2", "parallelism": "replicas"},
+        "pt_k_per_s": nk / (ms / 1e3),
+        "iterations_per_step": iters / args.steps,
+        "phase_ms": {k: rep[k] for k in ("ms_upload", "ms_init", "ms_tune", "ms_lloyd", "ms_download", "ms_total")},
+        "graph_launches": rep["graph_launches"], "tiles": rep["tiles"],
+        "gpu_launches": launches, "clocks": clocks.summary(),
+        "roofline": {"bound": "fp32-simt", "achieved": None, "peak": None, "unit": None, "frac": None,
+                     "traffic": None, "note": "see phase_ms; the assignment is FP32 CUDA-core bound"},
+    }
+    if not args.no_e2e:
+        t0 = time.perf_counter()
+        _, r2 = F.fit_batched(probs, reduction="f64", ctx=ctx)
+        t1 = time.perf_counter()
+        out["e2e"] = {"value": r2["iterations_total"] / (t1 - t0), "unit": "iters/s",
+                      "h2d_bytes_per_step": int(sum(p["x"].nbytes for p in probs)),
+                      "d2h_bytes_per_step": int(sum(p["x"].shape[0] * 8 + p["k"] * p["x"].shape[1] * 4
+                                                    for p in probs)),
+                      "note": "one fit_batched call on host arrays"}
+    if not args.no_cpu:
+        from oracle import oracle as O
+        threads = os.cpu_count() or 1
+        t0 = time.perf_counter()
+        it_cpu, nk_cpu, done = 0, 0.0, 0
+        for p in probs:
+            o = O.fit_runs(p["x"], p["k"], max_iter=p["max_iter"], tol=p["tol"], n_init=p["n_init"],
+                           seed=p["random_state"], wide_sums=True, nthreads=threads)
+            it_cpu += int(o["n_iter"].sum())
+            nk_cpu += float(p["x"].shape[0]) * p["k"] * float(o["n_iter"].sum())
+            done += 1
+            if time.perf_counter() - t0 > args.cpu_seconds:
+                break
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": it_cpu / dt, "unit": "iters/s", "cores": threads, "kind": "port",
+                               "pt_k_per_s": nk_cpu / dt,
+                               "sample": f"{done} of {len(probs)} problems, all 10 runs each (oracle fit_runs)"}
+    print(json.dumps(out))
+
+
 def run_ours(args):
+    if args.workload == "batched":
+        return run_batched(args)
     import torch
 
     import ferrolearn_gb300 as F

@@ -5,8 +5,8 @@ _build/libferrokmeans.so, reached through its C ABI (include/ferrokmeans.h).
 This package is the host-side mirror of the reference's KMeans API.
 """
 from .kmeans import (  # noqa: F401
-    MIXED_BF16, MIXED_FP8, PLAIN, Context, CudaError, DeviceOutOfMemory, DeviceTimeout, FerroError, FittedKMeans,
-    InsufficientSamples, InvalidParameter, KMeans, NullPointer, NumericalInstability, ShapeMismatch, Unsupported,
-    default_context, draws, kmeans_plus_plus, lloyd_step)
+    MIXED_BF16, MIXED_FP8, PLAIN, REDUCE_F64, REDUCE_REFERENCE, Context, CudaError, DeviceOutOfMemory, DeviceTimeout,
+    FerroError, FittedKMeans, InsufficientSamples, InvalidParameter, KMeans, NullPointer, NumericalInstability,
+    ShapeMismatch, Unsupported, default_context, draws, fit_batched, kmeans_plus_plus, lloyd_step)
 
 __version__ = "0.1.0"

@@ -23,8 +23,49 @@ EXPORTS = [
     "fk_kmeans_predict_f64", "fk_kmeans_predict_f32", "fk_kmeans_predict_f32x64",
     "fk_kmeans_transform_f64", "fk_kmeans_transform_f32",
     "fk_kmeans_plus_plus_f64", "fk_kmeans_plus_plus_f32", "fk_debug_tc_probe",
-    "fk_debug_measure_peaks", "fk_kmeans_score_f64_noalloc",
+    "fk_debug_measure_peaks", "fk_kmeans_score_f64_noalloc", "fk_kmeans_fit_batched_f32",
 ]
+
+
+class BatchProblem(C.Structure):
+    """fk_batch_problem."""
+
+    _fields_ = [
+        ("x", C.c_void_p),
+        ("n", C.c_int64),
+        ("d", C.c_int64),
+        ("n_clusters", C.c_int64),
+        ("max_iter", C.c_int64),
+        ("tol", C.c_double),
+        ("n_init", C.c_int64),
+        ("random_state", C.c_uint64),
+        ("init", C.c_void_p),
+        ("centers_out", C.c_void_p),
+        ("labels_out", C.c_void_p),
+        ("inertia_out", C.c_void_p),
+        ("n_iter_out", C.c_void_p),
+        ("best_run_out", C.c_void_p),
+    ]
+
+
+class BatchReport(C.Structure):
+    """fk_batch_report."""
+
+    _fields_ = [
+        ("fits", C.c_int64),
+        ("iterations_total", C.c_int64),
+        ("graph_launches", C.c_int64),
+        ("tuned_buckets", C.c_int64),
+        ("bucket_variant", C.c_int32 * 20),
+        ("ms_upload", C.c_double),
+        ("ms_init", C.c_double),
+        ("ms_tune", C.c_double),
+        ("ms_lloyd", C.c_double),
+        ("ms_download", C.c_double),
+        ("ms_total", C.c_double),
+        ("fit_inertia", C.c_void_p),
+        ("fit_n_iter", C.c_void_p),
+    ]
 
 
 class KMeansParams(C.Structure):
@@ -108,6 +149,8 @@ def _declare(lib):
     lib.fk_debug_measure_peaks.restype = st
     lib.fk_kmeans_score_f64_noalloc.argtypes = [p, i64, i64, p, i64, p, p, p]
     lib.fk_kmeans_score_f64_noalloc.restype = st
+    lib.fk_kmeans_fit_batched_f32.argtypes = [p, C.POINTER(BatchProblem), i64, i32, C.POINTER(BatchReport)]
+    lib.fk_kmeans_fit_batched_f32.restype = st
 
 
 def lib():

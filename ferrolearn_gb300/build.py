@@ -22,7 +22,7 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
           "--expt-relaxed-constexpr", "-I", INCLUDE]
-EXACT_UNITS = {"fk_assign.cu", "fk_update.cu", "fk_kpp.cu"}
+EXACT_UNITS = {"fk_assign.cu", "fk_update.cu", "fk_kpp.cu", "fk_batched.cu"}
 
 
 def _nvcc():

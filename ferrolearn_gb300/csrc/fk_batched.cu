@@ -1,0 +1,849 @@
+// fk_batched.cu -- many independent KMeans<f32> fits (uneven n, d, k) in one
+// call: kmeans.rs:417-512 once per (problem, run), all runs at once.
+//
+// Layout in HBM: every problem's rows packed into one f32 buffer (16-byte
+// aligned starts); per fit (problem p, run r) an n_p-long int32 scratch pair
+// (labels | members, reused as the k-means++ D^2 and running-sum arrays) and
+// two k x d centre buffers that alternate between iterations.
+//
+// Launches:
+//   batch_kpp_kernel     one persistent launch; a CTA takes the next fit from
+//                        a work queue (largest first) and runs greedy
+//                        k-means++ for it exactly as kmeans.rs:169-253 in f32:
+//                        the running sum is the reference's sequential fold
+//                        (one lane, the values broadcast by shuffles), each
+//                        trial's potential likewise, trials in parallel warps.
+//   batch_assign_kernel  per Lloyd iteration, one persistent launch per
+//                        (d, k) bucket over a queue of (fit, row range) items,
+//                        largest fits first; the fit's centres in shared
+//                        memory, rows in registers; direct-form f32 distances
+//                        (no FMA), strict < from F::MAX. The tile shape (rows
+//                        per thread x centres per pass) is the autotuner's
+//                        choice for the bucket. Per item a fixed-tree f64
+//                        inertia partial.
+//   batch_update_kernel  per iteration, one persistent launch over the fits:
+//                        counting sort of the labels (stable), then per
+//                        (cluster, feature) the row-order sum -- f32 exactly
+//                        like recompute_centroids_into (kmeans.rs:358-401), or
+//                        f64 with each mean rounded once to f32 -- the empty
+//                        cluster rule, sqrt of the max squared shift, the
+//                        tol test, n_iter and the inertia (partials in item
+//                        order).
+// One iteration (counter reset + bucket launches + update) is captured once
+// in a CUDA graph and replayed until every fit has converged or reached
+// max_iter; converged fits are skipped inside the kernels.
+#include <cfloat>
+#include <cmath>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <numeric>
+#include <vector>
+
+#include "fk_internal.cuh"
+
+namespace fk {
+namespace {
+
+struct BFit {
+    int64_t x_off;  // float offset of the problem's rows in the packed X
+    int64_t s_off;  // offset of this fit's n-long scratch arrays
+    int64_t c_off;  // float offset of this fit's two k x d centre buffers
+    int32_t n, d, k, max_iter;
+    float tol;
+    int32_t first_item, n_items;
+    int32_t trials;
+    uint64_t seed;
+};
+
+struct BState {
+    double inertia;
+    int32_t cur, n_iter, done, pad;
+};
+
+struct BItem {
+    int32_t fit, lo, hi, pad;
+};
+
+constexpr int KPP_T = 256;
+constexpr int ASSIGN_T = 128;
+constexpr int UPDATE_T = 256;
+constexpr int NBUCKETS = 20;  // d in {8, 16, 32, 64, other} x k in {<=16, <=32, <=64, >64}
+constexpr int NVARIANTS = 5;  // (rows per thread, centres per pass): (1,1) (2,1) (1,2) (2,2) (4,1)
+constexpr int MAX_K = 1024, MAX_D = 256, MAX_KD = 32768;
+
+__device__ __forceinline__ uint64_t dev_splitmix64(uint64_t &s) {
+    uint64_t z = (s += 0x9E3779B97F4A7C15ULL);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    return z ^ (z >> 31);
+}
+__device__ __forceinline__ double dev_uniform(uint64_t &s) {
+    return (double)(dev_splitmix64(s) >> 11) * (1.0 / 9007199254740992.0);
+}
+__device__ __forceinline__ int dev_range(double u, int n) {
+    long long i = (long long)floor(u * (double)n);
+    if (i < 0) i = 0;
+    if (i >= n) i = n - 1;
+    return (int)i;
+}
+
+// squared_euclidean (kmeans.rs:159-163) in f32: left fold, no FMA.
+__device__ __forceinline__ float sqeuc_f32(const float *__restrict__ a, const float *__restrict__ b, int d) {
+    float acc = 0.f;
+    for (int j = 0; j < d; j++) {
+        const float t = __fsub_rn(a[j], b[j]);
+        acc = __fadd_rn(acc, __fmul_rn(t, t));
+    }
+    return acc;
+}
+
+// ------------------------------------------------------------- k-means++ --
+// First index i with cum[i] >= thr (cum is non-decreasing); n - 1 if none.
+__device__ int first_reaching(const float *__restrict__ cum, int n, float thr) {
+    int lo = 0, hi = n;  // answer in [lo, hi]
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (cum[mid] >= thr) hi = mid;
+        else lo = mid + 1;
+    }
+    return lo < n ? lo : n - 1;
+}
+
+__global__ void __launch_bounds__(KPP_T) batch_kpp_kernel(const float *__restrict__ X, const BFit *__restrict__ fits,
+                                                          const int *__restrict__ order, int nf, int *counter,
+                                                          int *__restrict__ lab, int *__restrict__ mem,
+                                                          float *__restrict__ C) {
+    __shared__ int q_sh, idx_sh;
+    __shared__ float total_sh;
+    __shared__ int cand_sh[16];
+    __shared__ float pot_sh[16];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const unsigned full = 0xffffffffu;
+    uint64_t rng = 0;  // thread 0 only
+    while (true) {
+        if (tid == 0) q_sh = atomicAdd(counter, 1);
+        __syncthreads();
+        const int q = q_sh;
+        __syncthreads();
+        if (q >= nf) break;
+        const BFit F = fits[order[q]];
+        const int n = F.n, d = F.d, k = F.k;
+        const float *x = X + F.x_off;
+        float *mind = reinterpret_cast<float *>(lab + F.s_off);
+        float *cum = reinterpret_cast<float *>(mem + F.s_off);
+        float *cen = C + F.c_off;  // buffer 0
+        if (tid == 0) {
+            rng = F.seed;
+            idx_sh = dev_range(dev_uniform(rng), n);
+        }
+        __syncthreads();
+        for (int j = tid; j < d; j += KPP_T) cen[j] = x[(int64_t)idx_sh * d + j];
+        if (k > 1)
+            for (int i = tid; i < n; i += KPP_T) mind[i] = sqeuc_f32(x + (int64_t)i * d, x + (int64_t)idx_sh * d, d);
+        __syncthreads();
+        for (int c = 1; c < k; c++) {
+            // running sum of the D^2 array: the reference's sequential f32 fold
+            if (warp == 0) {
+                float run = 0.f;
+                for (int base = 0; base < n; base += 32) {
+                    const int i = base + lane;
+                    const float v = i < n ? mind[i] : 0.f;
+                    const int m = min(32, n - base);
+                    for (int l = 0; l < m; l++) {
+                        run = __fadd_rn(run, __shfl_sync(full, v, l));
+                        if (lane == l) cum[base + l] = run;
+                    }
+                }
+                if (lane == 0) total_sh = run;
+            }
+            __syncthreads();
+            const float total = total_sh;
+            if (total <= 0.f) {  // kmeans.rs:202-206: a uniform random row (NaN falls through)
+                if (tid == 0) idx_sh = dev_range(dev_uniform(rng), n);
+                __syncthreads();
+                for (int j = tid; j < d; j += KPP_T) cen[(int64_t)c * d + j] = x[(int64_t)idx_sh * d + j];
+                __syncthreads();
+                continue;
+            }
+            if (tid == 0) {
+                for (int t = 0; t < F.trials; t++) {
+                    const float thr = __fmul_rn(__double2float_rn(dev_uniform(rng)), total);
+                    cand_sh[t] = first_reaching(cum, n, thr);
+                }
+            }
+            __syncthreads();
+            // one warp per trial: min(d(x, candidate), D^2) and its sequential potential
+            for (int t = warp; t < F.trials; t += KPP_T / 32) {
+                const float *xc = x + (int64_t)cand_sh[t] * d;
+                float pot = 0.f;
+                for (int base = 0; base < n; base += 32) {
+                    const int i = base + lane;
+                    float r = 0.f;
+                    if (i < n) {
+                        const float v = sqeuc_f32(x + (int64_t)i * d, xc, d);
+                        const float mv = mind[i];
+                        r = v < mv ? v : mv;
+                    }
+                    const int m = min(32, n - base);
+                    for (int l = 0; l < m; l++) pot = __fadd_rn(pot, __shfl_sync(full, r, l));
+                }
+                if (lane == 0) pot_sh[t] = pot;
+            }
+            __syncthreads();
+            if (tid == 0) {  // strictly smallest potential, first trial on ties (kmeans.rs:239-243)
+                int best = 0;
+                float bp = pot_sh[0];
+                for (int t = 1; t < F.trials; t++)
+                    if (pot_sh[t] < bp) {
+                        bp = pot_sh[t];
+                        best = t;
+                    }
+                idx_sh = cand_sh[best];
+            }
+            __syncthreads();
+            const float *xb = x + (int64_t)idx_sh * d;
+            for (int j = tid; j < d; j += KPP_T) cen[(int64_t)c * d + j] = xb[j];
+            for (int i = tid; i < n; i += KPP_T) {
+                const float v = sqeuc_f32(x + (int64_t)i * d, xb, d);
+                const float mv = mind[i];
+                mind[i] = v < mv ? v : mv;
+            }
+            __syncthreads();
+        }
+    }
+}
+
+// ------------------------------------------------------------ assignment --
+__device__ __forceinline__ double block_sum_f64(double v, double *sh) {
+#pragma unroll
+    for (int off = 16; off >= 1; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    __syncthreads();
+    if (lane == 0) sh[w] = v;
+    __syncthreads();
+    double r = 0.0;
+    if (threadIdx.x == 0)
+        for (int q = 0; q < (int)(blockDim.x >> 5); q++) r += sh[q];
+    return r;
+}
+
+// D > 0: rows of exactly D features in registers (TR per thread), CP centres
+// per pass; D = 0: any d, one row and one centre at a time.
+template <int D, int TR, int CP>
+__global__ void __launch_bounds__(ASSIGN_T) batch_assign_kernel(const float *__restrict__ X,
+                                                                const BFit *__restrict__ fits,
+                                                                const BState *__restrict__ state,
+                                                                const BItem *__restrict__ items, int nitems,
+                                                                int *counter, const float *__restrict__ C,
+                                                                int *__restrict__ lab, double *__restrict__ partial) {
+    extern __shared__ float cs[];
+    __shared__ int it_sh;
+    __shared__ double red[ASSIGN_T / 32];
+    const int tid = threadIdx.x;
+    int loaded = -1;
+    while (true) {
+        if (tid == 0) it_sh = atomicAdd(counter, 1);
+        __syncthreads();
+        const int it = it_sh;
+        __syncthreads();
+        if (it >= nitems) break;
+        const BItem I = items[it];
+        const int f = I.fit;
+        if (state[f].done) continue;
+        const BFit F = fits[f];
+        const int d = D > 0 ? D : F.d, k = F.k;
+        if (f != loaded) {
+            const float *src = C + F.c_off + (int64_t)state[f].cur * k * d;
+            for (int e = tid; e < k * d; e += ASSIGN_T) cs[e] = src[e];
+            __syncthreads();
+            loaded = f;
+        }
+        const float *x = X + F.x_off;
+        int *L = lab + F.s_off;
+        double s = 0.0;
+        if constexpr (D > 0) {
+            for (int base = I.lo; base < I.hi; base += ASSIGN_T * TR) {
+                float xr[TR][D];
+                int rr[TR];
+#pragma unroll
+                for (int u = 0; u < TR; u++) {
+                    rr[u] = base + tid + u * ASSIGN_T;
+                    const bool ok = rr[u] < I.hi;
+#pragma unroll
+                    for (int j4 = 0; j4 < D / 4; j4++) {
+                        const float4 v = ok ? reinterpret_cast<const float4 *>(x + (int64_t)rr[u] * D)[j4]
+                                            : make_float4(0.f, 0.f, 0.f, 0.f);
+                        xr[u][4 * j4] = v.x;
+                        xr[u][4 * j4 + 1] = v.y;
+                        xr[u][4 * j4 + 2] = v.z;
+                        xr[u][4 * j4 + 3] = v.w;
+                    }
+                }
+                float best[TR];
+                int bi[TR];
+#pragma unroll
+                for (int u = 0; u < TR; u++) {
+                    best[u] = FLT_MAX;
+                    bi[u] = 0;
+                }
+                for (int c = 0; c < k; c += CP) {
+                    float acc[TR][CP];
+#pragma unroll
+                    for (int u = 0; u < TR; u++)
+#pragma unroll
+                        for (int p = 0; p < CP; p++) acc[u][p] = 0.f;
+#pragma unroll
+                    for (int j = 0; j < D; j++) {
+#pragma unroll
+                        for (int p = 0; p < CP; p++) {
+                            const float cv = c + p < k ? cs[(c + p) * D + j] : 0.f;
+#pragma unroll
+                            for (int u = 0; u < TR; u++) {
+                                const float t = __fsub_rn(xr[u][j], cv);
+                                acc[u][p] = __fadd_rn(acc[u][p], __fmul_rn(t, t));
+                            }
+                        }
+                    }
+#pragma unroll
+                    for (int p = 0; p < CP; p++)
+                        if (c + p < k)
+#pragma unroll
+                            for (int u = 0; u < TR; u++)
+                                if (acc[u][p] < best[u]) {
+                                    best[u] = acc[u][p];
+                                    bi[u] = c + p;
+                                }
+                }
+#pragma unroll
+                for (int u = 0; u < TR; u++)
+                    if (rr[u] < I.hi) {
+                        L[rr[u]] = bi[u];
+                        s += (double)best[u];
+                    }
+            }
+        } else {
+            for (int r = I.lo + tid; r < I.hi; r += ASSIGN_T) {
+                const float *xr = x + (int64_t)r * d;
+                float best = FLT_MAX;
+                int bi = 0;
+                for (int c = 0; c < k; c++) {
+                    const float v = sqeuc_f32(xr, cs + c * d, d);
+                    if (v < best) {
+                        best = v;
+                        bi = c;
+                    }
+                }
+                L[r] = bi;
+                s += (double)best;
+            }
+        }
+        const double tot = block_sum_f64(s, red);
+        if (tid == 0) partial[it] = tot;
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------- update --
+template <bool WIDE>
+__global__ void __launch_bounds__(UPDATE_T) batch_update_kernel(const float *__restrict__ X,
+                                                                const BFit *__restrict__ fits,
+                                                                BState *__restrict__ state,
+                                                                const int *__restrict__ order, int nf, int *counter,
+                                                                float *__restrict__ C, const int *__restrict__ lab,
+                                                                int *__restrict__ mem,
+                                                                const double *__restrict__ partial, int *active) {
+    __shared__ int hist[MAX_K], off[MAX_K], runp[MAX_K];
+    __shared__ int q_sh;
+    __shared__ float red[UPDATE_T / 32];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const unsigned full = 0xffffffffu;
+    while (true) {
+        if (tid == 0) q_sh = atomicAdd(counter, 1);
+        __syncthreads();
+        const int q = q_sh;
+        __syncthreads();
+        if (q >= nf) break;
+        const int f = order[q];
+        if (state[f].done) continue;
+        const BFit F = fits[f];
+        const int n = F.n, d = F.d, k = F.k;
+        const int *L = lab + F.s_off;
+        int *M = mem + F.s_off;
+        for (int c = tid; c < k; c += UPDATE_T) hist[c] = 0;
+        __syncthreads();
+        for (int i = tid; i < n; i += UPDATE_T) atomicAdd(&hist[L[i]], 1);
+        __syncthreads();
+        if (tid == 0) {
+            int acc = 0;
+            for (int c = 0; c < k; c++) {
+                off[c] = acc;
+                runp[c] = acc;
+                acc += hist[c];
+            }
+        }
+        __syncthreads();
+        // stable scatter (row order within each cluster), one warp
+        if (warp == 0) {
+            for (int base = 0; base < n; base += 32) {
+                const int i = base + lane;
+                const int l = i < n ? L[i] : -1;
+                const unsigned peers = __match_any_sync(full, l);
+                const int leader = __ffs(peers) - 1;
+                const int rank = __popc(peers & ((1u << lane) - 1u));
+                int b = 0;
+                if (lane == leader && l >= 0) {
+                    b = runp[l];
+                    runp[l] = b + __popc(peers);
+                }
+                b = __shfl_sync(full, b, leader);
+                if (l >= 0) M[b + rank] = i;
+            }
+        }
+        __syncthreads();
+        const int cur = state[f].cur;
+        const float *oldc = C + F.c_off + (int64_t)cur * k * d;
+        float *newc = C + F.c_off + (int64_t)(1 - cur) * k * d;
+        const float *x = X + F.x_off;
+        for (int pr = tid; pr < k * d; pr += UPDATE_T) {
+            const int c = pr / d, j = pr - c * d;
+            const int cnt = hist[c], o = off[c];
+            if (cnt == 0) {
+                newc[pr] = oldc[pr];  // empty cluster keeps its centre
+                continue;
+            }
+            if (WIDE) {
+                double acc = 0.0;
+                int m = 0;
+                for (; m + 4 <= cnt; m += 4) {
+                    const int r0 = M[o + m], r1 = M[o + m + 1], r2 = M[o + m + 2], r3 = M[o + m + 3];
+                    const float v0 = x[(int64_t)r0 * d + j], v1 = x[(int64_t)r1 * d + j];
+                    const float v2 = x[(int64_t)r2 * d + j], v3 = x[(int64_t)r3 * d + j];
+                    acc = __dadd_rn(acc, (double)v0);
+                    acc = __dadd_rn(acc, (double)v1);
+                    acc = __dadd_rn(acc, (double)v2);
+                    acc = __dadd_rn(acc, (double)v3);
+                }
+                for (; m < cnt; m++) acc = __dadd_rn(acc, (double)x[(int64_t)M[o + m] * d + j]);
+                newc[pr] = __double2float_rn(__ddiv_rn(acc, (double)cnt));
+            } else {
+                float acc = 0.f;
+                int m = 0;
+                for (; m + 4 <= cnt; m += 4) {
+                    const int r0 = M[o + m], r1 = M[o + m + 1], r2 = M[o + m + 2], r3 = M[o + m + 3];
+                    const float v0 = x[(int64_t)r0 * d + j], v1 = x[(int64_t)r1 * d + j];
+                    const float v2 = x[(int64_t)r2 * d + j], v3 = x[(int64_t)r3 * d + j];
+                    acc = __fadd_rn(acc, v0);
+                    acc = __fadd_rn(acc, v1);
+                    acc = __fadd_rn(acc, v2);
+                    acc = __fadd_rn(acc, v3);
+                }
+                for (; m < cnt; m++) acc = __fadd_rn(acc, x[(int64_t)M[o + m] * d + j]);
+                newc[pr] = __fdiv_rn(acc, (float)cnt);  // counts as F are exact below 2^24
+            }
+        }
+        __syncthreads();
+        // sqrt of the largest squared shift (NaN shifts never raise it)
+        float ms = 0.f;
+        for (int c = tid; c < k; c += UPDATE_T) {
+            const float sh = sqeuc_f32(newc + (int64_t)c * d, oldc + (int64_t)c * d, d);
+            if (sh > ms) ms = sh;
+        }
+#pragma unroll
+        for (int o2 = 16; o2 >= 1; o2 >>= 1) ms = fmaxf(ms, __shfl_xor_sync(full, ms, o2));
+        if (lane == 0) red[warp] = ms;
+        __syncthreads();
+        if (tid == 0) {
+            float m2 = 0.f;
+            for (int w = 0; w < UPDATE_T / 32; w++) m2 = fmaxf(m2, red[w]);
+            const float shift = __fsqrt_rn(m2);
+            double in = 0.0;
+            for (int it = 0; it < F.n_items; it++) in += partial[F.first_item + it];
+            BState st = state[f];
+            st.inertia = in;
+            st.n_iter += 1;
+            st.cur = 1 - cur;
+            if (shift < F.tol || st.n_iter >= F.max_iter) {
+                st.done = 1;
+                atomicSub(active, 1);
+            }
+            state[f] = st;
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void batch_labels_u64_kernel(const int *__restrict__ l, int n, uint64_t *__restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = (uint64_t)l[i];
+}
+
+// --------------------------------------------------------------- host side --
+int dbucket(int d) { return d == 8 ? 0 : d == 16 ? 1 : d == 32 ? 2 : d == 64 ? 3 : 4; }
+int kbucket(int k) { return k <= 16 ? 0 : k <= 32 ? 1 : k <= 64 ? 2 : 3; }
+int bucket_d(int b) { static const int v[5] = {8, 16, 32, 64, 0}; return v[b / 4]; }
+
+using AssignFn = void (*)(const float *, const BFit *, const BState *, const BItem *, int, int *, const float *,
+                          int *, double *);
+
+template <int D>
+AssignFn pick_variant(int v) {
+    switch (v) {
+        case 0: return batch_assign_kernel<D, 1, 1>;
+        case 1: return batch_assign_kernel<D, 2, 1>;
+        case 2: return batch_assign_kernel<D, 1, 2>;
+        case 3: return batch_assign_kernel<D, 2, 2>;
+        default: return batch_assign_kernel<D, (D <= 32 ? 4 : 2), 1>;
+    }
+}
+
+AssignFn assign_fn(int bucket, int v) {
+    switch (bucket_d(bucket)) {
+        case 8: return pick_variant<8>(v);
+        case 16: return pick_variant<16>(v);
+        case 32: return pick_variant<32>(v);
+        case 64: return v <= 2 ? pick_variant<64>(v) : pick_variant<64>(1);
+        default: return batch_assign_kernel<0, 1, 1>;
+    }
+}
+
+int n_variants(int bucket) {
+    const int d = bucket_d(bucket);
+    return d == 0 ? 1 : d == 64 ? 3 : NVARIANTS;
+}
+
+}  // namespace
+
+fk_status batched_fit_impl(Ctx &ctx, fk_batch_problem *P, int64_t np, int reduction, fk_batch_report *rep) {
+    if (np < 0 || (np > 0 && !P)) {
+        set_error("problems is NULL or n_problems is negative");
+        return FK_ERR_INVALID_PARAMETER;
+    }
+    if (reduction != FK_REDUCE_REFERENCE && reduction != FK_REDUCE_F64) {
+        set_error("unknown reduction %d", reduction);
+        return FK_ERR_INVALID_PARAMETER;
+    }
+    // Validation of every problem first, in the order of kmeans.rs:421-449.
+    for (int64_t p = 0; p < np; p++) {
+        const fk_batch_problem &q = P[p];
+        if (q.n_clusters <= 0) {
+            set_error("problem %lld: Invalid parameter `n_clusters`: must be at least 1", (long long)p);
+            return FK_ERR_INVALID_PARAMETER;
+        }
+        if (q.n <= 0 || q.n < q.n_clusters) {
+            set_error("problem %lld: Insufficient samples: need at least %lld, got %lld", (long long)p,
+                      (long long)q.n_clusters, (long long)(q.n < 0 ? 0 : q.n));
+            return FK_ERR_INSUFFICIENT_SAMPLES;
+        }
+        if (q.n_init <= 0) {
+            set_error("problem %lld: Invalid parameter `n_init`: must be at least 1", (long long)p);
+            return FK_ERR_INVALID_PARAMETER;
+        }
+        if (q.max_iter < 0 || q.d < 1) {
+            set_error("problem %lld: Invalid parameter `max_iter`/`d`", (long long)p);
+            return FK_ERR_INVALID_PARAMETER;
+        }
+        if (!q.x || !q.centers_out || !q.labels_out || !q.inertia_out || !q.n_iter_out) {
+            set_error("problem %lld: required pointer is NULL", (long long)p);
+            return FK_ERR_NULL_POINTER;
+        }
+        if (q.n_clusters > MAX_K || q.d > MAX_D || q.n_clusters * q.d > MAX_KD || q.n > INT32_MAX / 2 ||
+            q.max_iter > INT32_MAX) {
+            set_error("problem %lld: batched fits support k <= %d, d <= %d, k*d <= %d (got k=%lld d=%lld)",
+                      (long long)p, MAX_K, MAX_D, MAX_KD, (long long)q.n_clusters, (long long)q.d);
+            return FK_ERR_UNSUPPORTED;
+        }
+    }
+    if (rep) {
+        double *fi = rep->fit_inertia;
+        int64_t *fn = rep->fit_n_iter;
+        memset(rep, 0, sizeof(*rep));
+        rep->fit_inertia = fi;
+        rep->fit_n_iter = fn;
+        for (int b = 0; b < NBUCKETS; b++) rep->bucket_variant[b] = -1;
+    }
+    if (np == 0) return FK_OK;
+    ctx.bind();
+    cudaStream_t s = ctx.stream;
+    cudaEvent_t ev[6];
+    for (auto &e : ev) FK_CUDA(cudaEventCreate(&e));
+    FK_CUDA(cudaEventRecord(ev[0], s));
+
+    // ---- layout
+    std::vector<int64_t> xoff(np);
+    int64_t xtot = 0;
+    for (int64_t p = 0; p < np; p++) {
+        xoff[p] = xtot;
+        xtot += (P[p].n * P[p].d + 3) / 4 * 4;  // 16-byte aligned starts
+    }
+    std::vector<BFit> fits;
+    std::vector<int> fit_prob, fit_run;
+    int64_t soff = 0, coff = 0;
+    for (int64_t p = 0; p < np; p++) {
+        const fk_batch_problem &q = P[p];
+        for (int64_t r = 0; r < q.n_init; r++) {
+            BFit F;
+            memset(&F, 0, sizeof(F));
+            F.x_off = xoff[p];
+            F.s_off = soff;
+            F.c_off = coff;
+            F.n = (int32_t)q.n;
+            F.d = (int32_t)q.d;
+            F.k = (int32_t)q.n_clusters;
+            F.max_iter = (int32_t)q.max_iter;
+            F.tol = (float)q.tol;
+            F.trials = kpp_trials_host(q.n_clusters);
+            F.seed = q.random_state + (uint64_t)r;
+            fits.push_back(F);
+            fit_prob.push_back((int)p);
+            fit_run.push_back((int)r);
+            soff += q.n;
+            coff += 2 * q.n_clusters * q.d;
+        }
+    }
+    const int nf = (int)fits.size();
+    // work items: chunks of rows, grouped by (d, k) bucket, largest fits first
+    auto cost = [&](int f) { return (double)fits[f].n * fits[f].k * fits[f].d; };
+    std::vector<int> byc(nf);
+    std::iota(byc.begin(), byc.end(), 0);
+    std::stable_sort(byc.begin(), byc.end(), [&](int a, int b) { return cost(a) > cost(b); });
+    std::vector<BItem> items;
+    int bstart[NBUCKETS + 1] = {0};
+    for (int b = 0; b < NBUCKETS; b++) {
+        bstart[b] = (int)items.size();
+        for (int f : byc) {
+            BFit &F = fits[f];
+            if (dbucket(F.d) * 4 + kbucket(F.k) != b) continue;
+            const int ch = std::max(128, std::min(8192, (int)(4194304.0 / ((double)F.k * F.d * 3.0)) / 128 * 128));
+            F.first_item = (int)items.size();
+            for (int lo = 0; lo < F.n; lo += ch) items.push_back(BItem{f, lo, std::min(F.n, lo + ch), 0});
+            F.n_items = (int)items.size() - F.first_item;
+        }
+    }
+    bstart[NBUCKETS] = (int)items.size();
+    std::vector<int> kpp_order;
+    for (int f : byc)
+        if (!P[fit_prob[f]].init) kpp_order.push_back(f);
+
+    // ---- device buffers
+    float *X = (float *)ctx.get(BUF_BX, sizeof(float) * (size_t)xtot + 16);
+    BFit *dfits = (BFit *)ctx.get(BUF_BFITS, sizeof(BFit) * (size_t)nf);
+    BState *dstate = (BState *)ctx.get(BUF_BSTATE, sizeof(BState) * (size_t)nf);
+    BItem *ditems = (BItem *)ctx.get(BUF_BITEMS, sizeof(BItem) * items.size() + 16);
+    double *dpart = (double *)ctx.get(BUF_BPART, sizeof(double) * items.size() + 16);
+    int *dorder = (int *)ctx.get(BUF_BORDER, sizeof(int) * (size_t)(2 * nf) + 16);
+    int *dctr = (int *)ctx.get(BUF_BCTR, sizeof(int) * 32);
+    int *dlab = (int *)ctx.get(BUF_BLAB, sizeof(int) * (size_t)soff + 16);
+    int *dmem = (int *)ctx.get(BUF_BMEM, sizeof(int) * (size_t)soff + 16);
+    float *dC = (float *)ctx.get(BUF_BCEN, sizeof(float) * (size_t)coff + 16);
+    for (int64_t p = 0; p < np; p++)
+        FK_CUDA(cudaMemcpyAsync(X + xoff[p], P[p].x, sizeof(float) * (size_t)(P[p].n * P[p].d), cudaMemcpyDefault,
+                                s));
+    FK_CUDA(cudaMemcpyAsync(dfits, fits.data(), sizeof(BFit) * (size_t)nf, cudaMemcpyHostToDevice, s));
+    if (!items.empty())
+        FK_CUDA(cudaMemcpyAsync(ditems, items.data(), sizeof(BItem) * items.size(), cudaMemcpyHostToDevice, s));
+    std::vector<int> orders(byc);
+    orders.insert(orders.end(), kpp_order.begin(), kpp_order.end());
+    FK_CUDA(cudaMemcpyAsync(dorder, orders.data(), sizeof(int) * orders.size(), cudaMemcpyHostToDevice, s));
+    std::vector<BState> st0(nf);
+    int active = 0;
+    for (int f = 0; f < nf; f++) {
+        st0[f].inertia = (double)FLT_MAX;
+        st0[f].cur = 0;
+        st0[f].n_iter = 0;
+        st0[f].done = fits[f].max_iter == 0 ? 1 : 0;
+        st0[f].pad = 0;
+        active += st0[f].done ? 0 : 1;
+    }
+    FK_CUDA(cudaMemcpyAsync(dstate, st0.data(), sizeof(BState) * (size_t)nf, cudaMemcpyHostToDevice, s));
+    FK_CUDA(cudaMemsetAsync(dlab, 0, sizeof(int) * (size_t)soff, s));
+    FK_CUDA(cudaMemsetAsync(dctr, 0, sizeof(int) * 32, s));
+    FK_CUDA(cudaMemcpyAsync(dctr + 31, &active, sizeof(int), cudaMemcpyHostToDevice, s));
+    for (int f = 0; f < nf; f++) {
+        const fk_batch_problem &q = P[fit_prob[f]];
+        if (q.init) {
+            const int64_t run = fit_run[f];
+            FK_CUDA(cudaMemcpyAsync(dC + fits[f].c_off, q.init + run * q.n_clusters * q.d,
+                                    sizeof(float) * (size_t)(q.n_clusters * q.d), cudaMemcpyDefault, s));
+        }
+    }
+    FK_CUDA(cudaEventRecord(ev[1], s));
+
+    // ---- k-means++ (one persistent launch)
+    if (!kpp_order.empty()) {
+        const int grid = std::min((int)kpp_order.size(), ctx.num_sms * 8);
+        batch_kpp_kernel<<<grid, KPP_T, 0, s>>>(X, dfits, dorder + nf, (int)kpp_order.size(), dctr + 30, dlab, dmem,
+                                                dC);
+        FK_LAUNCH_CHECK();
+        // k-means++ used the label arrays as scratch: fits that run no
+        // iteration report all-zero labels (kmeans.rs:459-466)
+        for (int f = 0; f < nf; f++)
+            if (fits[f].max_iter == 0)
+                FK_CUDA(cudaMemsetAsync(dlab + fits[f].s_off, 0, sizeof(int) * (size_t)fits[f].n, s));
+    }
+    FK_CUDA(cudaEventRecord(ev[2], s));
+
+    // ---- autotuner: time every variant of each new (d, k) bucket on its items
+    int bmaxkd[NBUCKETS] = {0};
+    for (const BFit &F : fits) {
+        const int b = dbucket(F.d) * 4 + kbucket(F.k);
+        bmaxkd[b] = std::max(bmaxkd[b], F.k * F.d);
+    }
+    int64_t tuned = 0;
+    for (int b = 0; b < NBUCKETS; b++) {
+        const int cnt = bstart[b + 1] - bstart[b];
+        if (cnt == 0) continue;
+        const size_t smem = sizeof(float) * (size_t)bmaxkd[b];
+        for (int v = 0; v < n_variants(b); v++)
+            FK_CUDA(cudaFuncSetAttribute((const void *)assign_fn(b, v), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)std::max<size_t>(smem, 1)));
+        if (ctx.batch_variant[b] >= 0) continue;
+        const int grid = std::min(cnt, ctx.num_sms * 8);
+        float bestms = 1e30f;
+        int bestv = 0;
+        for (int v = 0; v < n_variants(b); v++) {
+            FK_CUDA(cudaMemsetAsync(dctr + b, 0, sizeof(int), s));
+            FK_CUDA(cudaEventRecord(ev[4], s));
+            assign_fn(b, v)<<<grid, ASSIGN_T, smem, s>>>(X, dfits, dstate, ditems + bstart[b], cnt, dctr + b, dC,
+                                                          dlab, dpart + bstart[b]);
+            FK_LAUNCH_CHECK();
+            FK_CUDA(cudaEventRecord(ev[5], s));
+            FK_CUDA(cudaEventSynchronize(ev[5]));
+            float ms = 0.f;
+            FK_CUDA(cudaEventElapsedTime(&ms, ev[4], ev[5]));
+            if (ms < bestms) {
+                bestms = ms;
+                bestv = v;
+            }
+        }
+        ctx.batch_variant[b] = bestv;
+        tuned++;
+    }
+    FK_CUDA(cudaEventRecord(ev[3], s));
+
+    // ---- Lloyd iterations: one captured iteration, replayed
+    auto one_iteration = [&]() {
+        FK_CUDA(cudaMemsetAsync(dctr, 0, sizeof(int) * 21, s));
+        for (int b = 0; b < NBUCKETS; b++) {
+            const int cnt = bstart[b + 1] - bstart[b];
+            if (cnt == 0) continue;
+            const int grid = std::min(cnt, ctx.num_sms * 8);
+            assign_fn(b, ctx.batch_variant[b])<<<grid, ASSIGN_T, sizeof(float) * (size_t)bmaxkd[b], s>>>(
+                X, dfits, dstate, ditems + bstart[b], cnt, dctr + b, dC, dlab, dpart + bstart[b]);
+        }
+        const int ug = std::min(nf, ctx.num_sms * 4);
+        if (reduction == FK_REDUCE_F64)
+            batch_update_kernel<true><<<ug, UPDATE_T, 0, s>>>(X, dfits, dstate, dorder, nf, dctr + 20, dC, dlab,
+                                                              dmem, dpart, dctr + 31);
+        else
+            batch_update_kernel<false><<<ug, UPDATE_T, 0, s>>>(X, dfits, dstate, dorder, nf, dctr + 20, dC, dlab,
+                                                               dmem, dpart, dctr + 31);
+    };
+    int max_iter = 0;
+    for (const BFit &F : fits) max_iter = std::max(max_iter, F.max_iter);
+    int64_t replays = 0;
+    if (active > 0) {
+        cudaGraph_t graph = nullptr;
+        cudaGraphExec_t exec = nullptr;
+        FK_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        one_iteration();
+        cudaError_t ce = cudaStreamEndCapture(s, &graph);
+        if (ce != cudaSuccess) {
+            set_error("graph capture failed: %s", cudaGetErrorString(ce));
+            fail(FK_ERR_CUDA);
+        }
+        ce = cudaGraphInstantiate(&exec, graph, 0);
+        if (ce != cudaSuccess) {
+            cudaGraphDestroy(graph);
+            set_error("graph instantiation failed: %s", cudaGetErrorString(ce));
+            fail(FK_ERR_CUDA);
+        }
+        int left = active;
+        const int group = 4;  // replays between checks of the active count
+        while (left > 0 && replays < max_iter) {
+            const int g = (int)std::min<int64_t>(group, max_iter - replays);
+            for (int r = 0; r < g; r++) {
+                ce = cudaGraphLaunch(exec, s);
+                if (ce != cudaSuccess) break;
+                replays++;
+            }
+            if (ce == cudaSuccess) ce = cudaMemcpyAsync(&left, dctr + 31, sizeof(int), cudaMemcpyDeviceToHost, s);
+            if (ce == cudaSuccess) ce = cudaStreamSynchronize(s);
+            if (ce != cudaSuccess) break;
+        }
+        cudaGraphExecDestroy(exec);
+        cudaGraphDestroy(graph);
+        if (ce != cudaSuccess) {
+            set_error("batched Lloyd iterations failed: %s", cudaGetErrorString(ce));
+            fail(FK_ERR_CUDA);
+        }
+    }
+    FK_CUDA(cudaEventRecord(ev[4], s));
+
+    // ---- best run per problem (strictly lowest inertia, first run on ties), outputs
+    std::vector<BState> st(nf);
+    FK_CUDA(cudaMemcpyAsync(st.data(), dstate, sizeof(BState) * (size_t)nf, cudaMemcpyDeviceToHost, s));
+    FK_CUDA(cudaStreamSynchronize(s));
+    int64_t nmax = 1;
+    for (int64_t p = 0; p < np; p++) nmax = std::max(nmax, P[p].n);
+    uint64_t *l64 = (uint64_t *)ctx.get(BUF_OUT, sizeof(uint64_t) * (size_t)nmax);
+    int64_t iters = 0;
+    for (int f = 0; f < nf; f++) iters += st[f].n_iter;
+    int f0 = 0;
+    for (int64_t p = 0; p < np; p++) {
+        const fk_batch_problem &q = P[p];
+        int best = -1;
+        float bi = 0.f;
+        for (int64_t r = 0; r < q.n_init; r++) {
+            const float in = (float)st[f0 + r].inertia;
+            if (best < 0 || in < bi) {
+                best = (int)r;
+                bi = in;
+            }
+        }
+        const int f = f0 + best;
+        const BFit &F = fits[f];
+        FK_CUDA(cudaMemcpyAsync(q.centers_out, dC + F.c_off + (int64_t)st[f].cur * F.k * F.d,
+                                sizeof(float) * (size_t)(F.k * F.d), cudaMemcpyDefault, s));
+        batch_labels_u64_kernel<<<(F.n + 255) / 256, 256, 0, s>>>(dlab + F.s_off, F.n, l64);
+        FK_LAUNCH_CHECK();
+        FK_CUDA(cudaMemcpyAsync(q.labels_out, l64, sizeof(uint64_t) * (size_t)F.n, cudaMemcpyDefault, s));
+        FK_CUDA(cudaStreamSynchronize(s));  // l64 is reused by the next problem
+        *q.inertia_out = bi;
+        *q.n_iter_out = st[f].n_iter;
+        if (q.best_run_out) *q.best_run_out = best;
+        f0 += (int)q.n_init;
+    }
+    FK_CUDA(cudaEventRecord(ev[5], s));
+    FK_CUDA(cudaEventSynchronize(ev[5]));
+    if (rep) {
+        rep->fits = nf;
+        rep->iterations_total = iters;
+        rep->graph_launches = replays;
+        rep->tuned_buckets = tuned;
+        for (int b = 0; b < NBUCKETS; b++)
+            rep->bucket_variant[b] = bstart[b + 1] > bstart[b] ? ctx.batch_variant[b] : -1;
+        float ms = 0.f;
+        FK_CUDA(cudaEventElapsedTime(&ms, ev[0], ev[1]));
+        rep->ms_upload = ms;
+        FK_CUDA(cudaEventElapsedTime(&ms, ev[1], ev[2]));
+        rep->ms_init = ms;
+        FK_CUDA(cudaEventElapsedTime(&ms, ev[2], ev[3]));
+        rep->ms_tune = ms;
+        FK_CUDA(cudaEventElapsedTime(&ms, ev[3], ev[4]));
+        rep->ms_lloyd = ms;
+        FK_CUDA(cudaEventElapsedTime(&ms, ev[4], ev[5]));
+        rep->ms_download = ms;
+        FK_CUDA(cudaEventElapsedTime(&ms, ev[0], ev[5]));
+        rep->ms_total = ms;
+        for (int f = 0; f < nf; f++) {
+            if (rep->fit_inertia) rep->fit_inertia[f] = st[f].inertia;
+            if (rep->fit_n_iter) rep->fit_n_iter[f] = st[f].n_iter;
+        }
+    }
+    for (auto &e : ev) cudaEventDestroy(e);
+    return FK_OK;
+}
+
+}  // namespace fk

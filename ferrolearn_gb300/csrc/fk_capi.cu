@@ -73,6 +73,12 @@ void *Ctx::get(BufSlot s, size_t bytes) {
     return p;
 }
 
+// n_trials of kmeans.rs:198 (2 + floor(ln k), at least 1).
+int kpp_trials_host(int64_t k) {
+    long long t = 2 + (long long)std::floor(std::log((double)k));
+    return t < 1 ? 1 : (int)t;
+}
+
 namespace {
 
 bool is_device_ptr(const void *p) {
@@ -132,10 +138,6 @@ void host_draws(uint64_t seed, int64_t count, double *out) {
     for (int64_t i = 0; i < count; i++) out[i] = (double)(splitmix64(&st) >> 11) * (1.0 / 9007199254740992.0);
 }
 
-int kpp_trials_host(int64_t k) {
-    long long t = 2 + (long long)std::floor(std::log((double)k));
-    return t < 1 ? 1 : (int)t;
-}
 
 // Plain: every entry point. BF16: f64 semantics (f64 or f32x64). FP8: X
 // stored as f32 with f64 semantics (f32x64) only.
@@ -712,6 +714,13 @@ fk_status fk_debug_measure_peaks(fk_ctx *ctx, double *out) {
         c.bind();
         fk::measure_peaks(c, out);
         return FK_OK;
+    });
+}
+
+fk_status fk_kmeans_fit_batched_f32(fk_ctx *ctx, fk_batch_problem *problems, int64_t n_problems, int32_t reduction,
+                                    fk_batch_report *report) {
+    return guarded(ctx, [&] {
+        return fk::batched_fit_impl(*reinterpret_cast<fk::Ctx *>(ctx), problems, n_problems, reduction, report);
     });
 }
 

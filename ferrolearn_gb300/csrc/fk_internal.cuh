@@ -132,6 +132,7 @@ enum BufSlot {
     BUF_XB, BUF_XNORM, BUF_CB, BUF_CAUX, BUF_TOP2, BUF_FLAGS, BUF_FULL, BUF_CF32, BUF_CF32C, BUF_FIXPART,
     BUF_XB2, BUF_TOP8, BUF_OCT, BUF_EX, BUF_XAUG, BUF_ROWSCALE, BUF_ROWINFO2, BUF_STATS2, BUF_CB2, BUF_CAUG2,
     BUF_HALF2, BUF_INERTIA2,
+    BUF_BX, BUF_BFITS, BUF_BSTATE, BUF_BITEMS, BUF_BPART, BUF_BORDER, BUF_BCTR, BUF_BLAB, BUF_BMEM, BUF_BCEN,
     BUF_COUNT
 };
 
@@ -153,6 +154,8 @@ struct Ctx {
     std::vector<PendingTimer> pending;  // phase timers read after the loop
     MixedPlan mixed;   // main pass
     MixedPlan mixed2;  // second pass (BF16, top-8 records) over the rows the main pass left open
+    int batch_variant[20] = {-1, -1, -1, -1, -1, -1, -1, -1, -1, -1,
+                             -1, -1, -1, -1, -1, -1, -1, -1, -1, -1};  // autotuned tile shape per (d, k) bucket
     double *contract_acc = nullptr;  // when set: device time of the contraction kernel
 
     void *get(BufSlot s, size_t bytes);  // grow-only device buffer
@@ -271,6 +274,11 @@ void launch_tc_assign(Ctx &ctx, MixedPlan &mp, const void *xb, const void *cb, c
                       Top8 *out8, DevScalars *sc, const MixedStats *stats, float *dump = nullptr,
                       const unsigned long long *n_dev = nullptr, const void *xaug = nullptr,
                       const float *rowscale = nullptr);
+
+// Batched KMeans<f32> fits (fk_batched.cu).
+fk_status batched_fit_impl(Ctx &ctx, fk_batch_problem *problems, int64_t n_problems, int reduction,
+                           fk_batch_report *report);
+int kpp_trials_host(int64_t k);
 
 void measure_peaks(Ctx &ctx, double *out);
 void debug_tc_probe(Ctx &ctx, const float *x, int64_t n, int d, const double *c, int k, int precision,

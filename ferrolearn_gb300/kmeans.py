@@ -351,3 +351,85 @@ def kmeans_plus_plus(x, k, draws_arr=None, seed=0, dtype="f64", ctx=None):
     _check(fn(ctx.handle, _ptr(x), n, d, k, _ptr(dr), 0 if dr is None else dr.size, seed, _ptr(out),
               C.byref(used)))
     return out, used.value
+
+
+REDUCE_REFERENCE = 0
+REDUCE_F64 = 1
+_REDUCTIONS = {"reference": REDUCE_REFERENCE, "f32": REDUCE_REFERENCE, "f64": REDUCE_F64}
+
+_BUCKET_D = (8, 16, 32, 64, "other")
+_BUCKET_K = ("<=16", "<=32", "<=64", ">64")
+_VARIANTS = ("1 row x 1 centre", "2 rows x 1 centre", "1 row x 2 centres", "2 rows x 2 centres",
+             "4 rows x 1 centre")
+
+
+def fit_batched(problems, reduction="reference", ctx=None):
+    """Many independent KMeans<f32> fits in one call (fk_kmeans_fit_batched_f32).
+
+    problems: a list of dicts with x (n x d f32, numpy or a device tensor), k,
+    and optionally n_init (10), max_iter (300), tol (1e-4), random_state (0),
+    init ((n_init, k, d) or (k, d) initial centres). Each problem is
+    Fit::fit (kmeans.rs:417-512) with F = f32; run r draws k-means++ from the
+    stream seeded with random_state + r. reduction: "reference" (f32 row-order
+    centroid sums, bit-identical to KMeans<f32>) or "f64" (f64 sums, each mean
+    rounded once to f32).
+
+    Returns (list of FittedKMeans, report dict with per-fit inertia / n_iter,
+    the autotuner's tile choice per (d, k) bucket and phase times).
+    """
+    ctx = ctx or default_context()
+    red = _REDUCTIONS[reduction] if isinstance(reduction, str) else int(reduction)
+    n_probs = len(problems)
+    arr = (_native.BatchProblem * max(1, n_probs))()
+    keep, outs = [], []
+    total_fits = 0
+    for i, pr in enumerate(problems):
+        x = _as_matrix(pr["x"], np.float32)
+        n, d = int(x.shape[0]), int(x.shape[1])
+        k = int(pr["k"])
+        n_init = int(pr.get("n_init", 10))
+        init = pr.get("init")
+        if init is not None:
+            ini = np.asarray(init, dtype=np.float32)
+            if ini.ndim == 2:
+                ini = np.broadcast_to(ini, (max(n_init, 1),) + ini.shape)
+            init = np.ascontiguousarray(ini)
+        c_out = np.empty((max(k, 0), d), dtype=np.float32)
+        l_out = np.empty(n, dtype=np.uint64)
+        in_out = np.empty(1, dtype=np.float32)
+        it_out = np.empty(1, dtype=np.int64)
+        br_out = np.empty(1, dtype=np.int64)
+        q = arr[i]
+        q.x = _ptr(x).value if hasattr(x, "data_ptr") else x.ctypes.data
+        q.n, q.d, q.n_clusters = n, d, k
+        q.max_iter = int(pr.get("max_iter", 300))
+        q.tol = float(pr.get("tol", 1e-4))
+        q.n_init = n_init
+        q.random_state = int(pr.get("random_state", 0))
+        q.init = None if init is None else init.ctypes.data
+        q.centers_out = c_out.ctypes.data
+        q.labels_out = l_out.ctypes.data
+        q.inertia_out = in_out.ctypes.data
+        q.n_iter_out = it_out.ctypes.data
+        q.best_run_out = br_out.ctypes.data
+        keep += [x, init]
+        outs.append((c_out, l_out, in_out, it_out, br_out))
+        total_fits += max(n_init, 0)
+    fit_in = np.empty(max(1, total_fits), dtype=np.float64)
+    fit_it = np.empty(max(1, total_fits), dtype=np.int64)
+    rep = _native.BatchReport()
+    rep.fit_inertia = fit_in.ctypes.data
+    rep.fit_n_iter = fit_it.ctypes.data
+    _check(_native.lib().fk_kmeans_fit_batched_f32(ctx.handle, arr, n_probs, red, C.byref(rep)))
+    fitted = [FittedKMeans(c, l.astype(np.int64), float(inr[0]), int(it[0]), "f32",
+                           {"best_run": int(br[0])}) for c, l, inr, it, br in outs]
+    tiles = {}
+    for b in range(20):
+        v = rep.bucket_variant[b]
+        if v >= 0:
+            tiles[f"d={_BUCKET_D[b // 4]},k{_BUCKET_K[b % 4]}"] = _VARIANTS[v]
+    report = dict(fits=rep.fits, iterations_total=rep.iterations_total, graph_launches=rep.graph_launches,
+                  tuned_buckets=rep.tuned_buckets, tiles=tiles, ms_upload=rep.ms_upload, ms_init=rep.ms_init,
+                  ms_tune=rep.ms_tune, ms_lloyd=rep.ms_lloyd, ms_download=rep.ms_download, ms_total=rep.ms_total,
+                  fit_inertia=fit_in[:total_fits].copy(), fit_n_iter=fit_it[:total_fits].copy())
+    return fitted, report

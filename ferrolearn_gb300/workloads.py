@@ -17,6 +17,11 @@ can run the same distribution at a size the CPU oracle finishes quickly.
                       covariance A A^T, A_ij ~ N(0, 0.3^2) (128x128), centres
                       U[-15,15]^128; init = first k rows of a seeded
                       permutation; 50 iterations (tol 0).
+  batched_512         512 independent problems: n log-uniform in
+                      [2,000, 200,000], d from {8, 16, 32, 64}, k uniform
+                      in [4, 64]; each a mixture of k Gaussian blobs with
+                      std 1.0 and centres U[-10,10]^d; f32; 10 seeded
+                      k-means++ restarts each (5,120 fits), tol 1e-4.
   bisector_4096x256   n=8,000,000 d=256 k=4096, X stored f32: 4096 blobs,
                       std 1.0, centres U[-30,30]^256, plus 10% of the rows
                       placed on the perpendicular bisector of two seeded
@@ -120,3 +125,21 @@ def bisector_4096x256(scale=1.0, seed=0, k=4096, d=256, predict_scale=None):
     return dict(x=x, k=k, init=init, max_iter=20, tol=0.0, n_init=1, x_predict=x_pred, name="bisector_4096x256",
                 desc=f"n={n} d={d} k={k}, X f32, 4096 blobs std 1 + 10% bisector rows, 20 iterations, "
                      f"predict on {n_pred} rows")
+
+
+def batched_512(scale=1.0, seed=0, n_problems=512, n_init=10, max_iter=300, tol=1e-4):
+    """The batched workload: a list of problem dicts for fit_batched. scale
+    multiplies every n (kept >= k); n_problems trims the list."""
+    rng = np.random.default_rng(seed)
+    probs = []
+    for p in range(n_problems):
+        n = int(round(np.exp(rng.uniform(np.log(2000.0), np.log(200000.0))) * scale))
+        d = int(rng.choice([8, 16, 32, 64]))
+        k = int(rng.integers(4, 65))
+        n = max(n, k)
+        cen = rng.uniform(-10.0, 10.0, size=(k, d)).astype(np.float32)
+        lab = rng.integers(0, k, size=n)
+        x = cen[lab] + rng.standard_normal(size=(n, d), dtype=np.float32)
+        probs.append(dict(x=np.ascontiguousarray(x, dtype=np.float32), k=k, n_init=n_init, max_iter=max_iter,
+                          tol=tol, random_state=int(seed * 100003 + p)))
+    return probs

@@ -212,6 +212,56 @@ fk_status fk_kmeans_score_f64_noalloc(const double *x, int64_t n, int64_t d, con
                                       int64_t k, uint64_t *labels_out, double *inertia_out,
                                       void *cuda_stream);
 
+/* ------------------------------------------------------- batched fits --
+ * Many independent KMeans<f32> fits in one call (problems of uneven n, d and
+ * k, each with its own n_init runs): Fit::fit (kmeans.rs:417-512) per
+ * problem, all runs of all problems at once. Run r of a problem starts from
+ * init[r] when init is given, else from k-means++ (kmeans.rs:169-253) on the
+ * splitmix64 stream seeded with random_state + r (fk_draws_f64). The best run
+ * is the strictly lowest inertia, first run on ties (kmeans.rs:506-511).
+ * Distances, the argmin and k-means++ are the reference's f32 arithmetic;
+ * the centroid sums follow `reduction`. x and the outputs may be host or
+ * device memory. Limits: k <= 1024, d <= 256, k*d <= 32768 (else
+ * FK_ERR_UNSUPPORTED); validation errors name the problem index. */
+typedef enum fk_reduction {
+    FK_REDUCE_REFERENCE = 0, /* row-order f32 sums (kmeans.rs:358-401 for F = f32) */
+    FK_REDUCE_F64 = 1        /* row-order f64 sums, each mean rounded once to f32;
+                                inertia summed in f64 */
+} fk_reduction;
+
+typedef struct fk_batch_problem {
+    const float *x;          /* n x d, row-major */
+    int64_t n, d;
+    int64_t n_clusters;
+    int64_t max_iter;
+    double tol;
+    int64_t n_init;
+    uint64_t random_state;
+    const float *init;       /* nullable: n_init x k x d initial centres */
+    float *centers_out;      /* k x d (best run) */
+    uint64_t *labels_out;    /* n (best run) */
+    float *inertia_out;
+    int64_t *n_iter_out;
+    int64_t *best_run_out;   /* nullable */
+} fk_batch_problem;
+
+typedef struct fk_batch_report {
+    int64_t fits;                /* sum of n_init */
+    int64_t iterations_total;    /* Lloyd iterations over all fits */
+    int64_t graph_launches;      /* replays of the captured iteration graph */
+    int64_t tuned_buckets;       /* (d, k) buckets the autotuner timed in this call */
+    int32_t bucket_variant[20];  /* tile shape per bucket d{8,16,32,64,other} x
+                                    k{<=16,<=32,<=64,>64}: 0 (1 row, 1 centre per
+                                    pass), 1 (2,1), 2 (1,2), 3 (2,2), 4 (4,1);
+                                    -1 = bucket absent */
+    double ms_upload, ms_init, ms_tune, ms_lloyd, ms_download, ms_total;
+    double *fit_inertia;         /* nullable, caller memory: per fit, problem-major */
+    int64_t *fit_n_iter;         /* nullable, caller memory: per fit */
+} fk_batch_report;
+
+fk_status fk_kmeans_fit_batched_f32(fk_ctx *ctx, fk_batch_problem *problems, int64_t n_problems,
+                                    int32_t reduction, fk_batch_report *report);
+
 /* Diagnostics (no reference counterpart): CUDA-core throughput of this GPU,
  * out[0] FP32 FMA flop/s, [1] FP64 FMA flop/s, [2] FP64 add op/s, [3] FP32
  * add op/s, [4] FP64 add latency in cycles, [5] FP32 add latency. */

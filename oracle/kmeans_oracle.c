@@ -298,3 +298,85 @@ int orc_widen_f32(const float *x, int64_t count, double *out) {
     for (int64_t i = 0; i < count; i++) out[i] = (double)x[i];
     return ORC_OK;
 }
+
+/* --------------------------------------------- batched fits, per run -- */
+/* Fit::fit (kmeans.rs:417-512) for F = f32, every run kept: run r seeds
+ * k-means++ (kmeans.rs:169-253) with splitmix64(seed + r), or takes
+ * init[r]; Lloyd iterations follow kmeans.rs:459-505. wide_sums = 0 is the
+ * reference's own f32 arithmetic (recompute_centroids_into, kmeans.rs:358-401,
+ * row-order f32 sums); wide_sums = 1 is the batched entry point's FP64
+ * reduction variant: the same row-order sums in f64, each mean rounded once
+ * to f32 (sum / count in f64), and the inertia summed in f64 in row order.
+ * Outputs per run: centres (k*d), labels (n), inertia (as f64), n_iter. */
+static float orc_update_f32_wide(const float *x, int64_t n, int64_t d, const int64_t *labels,
+                                 const float *old_c, int64_t k, float *new_c, double *sums, double *counts) {
+    memset(sums, 0, sizeof(double) * (size_t)(k * d));
+    for (int64_t q = 0; q < k; q++) counts[q] = 0.0;
+    for (int64_t i = 0; i < n; i++) {
+        int64_t l = labels[i];
+        counts[l] = counts[l] + 1.0;
+        for (int64_t j = 0; j < d; j++) sums[l * d + j] = sums[l * d + j] + (double)x[i * d + j];
+    }
+    for (int64_t q = 0; q < k; q++) {
+        if (counts[q] > 0.0) {
+            for (int64_t j = 0; j < d; j++) new_c[q * d + j] = (float)(sums[q * d + j] / counts[q]);
+        } else {
+            memcpy(new_c + q * d, old_c + q * d, sizeof(float) * (size_t)d);
+        }
+    }
+    float ms = 0.0f;
+    for (int64_t q = 0; q < k; q++) {
+        float s = orc_sqeuc_f32(new_c + q * d, old_c + q * d, d);
+        if (s > ms) ms = s;
+    }
+    return sqrtf(ms);
+}
+
+int orc_fit_runs_f32(const float *x, int64_t n, int64_t d, int64_t k, int64_t max_iter, float tol,
+                     int64_t n_init, const float *init, uint64_t seed, int wide_sums, float *out_c,
+                     int64_t *out_labels, double *out_inertia, int64_t *out_n_iter, int nthreads) {
+    if (k == 0) return ORC_ERR_INVALID_PARAMETER;
+    if (n == 0 || n < k) return ORC_ERR_INSUFFICIENT_SAMPLES;
+    if (n_init == 0) return ORC_ERR_INVALID_PARAMETER;
+    float *c = (float *)malloc(sizeof(float) * (size_t)(k * d));
+    float *nc = (float *)malloc(sizeof(float) * (size_t)(k * d));
+    float *counts = (float *)malloc(sizeof(float) * (size_t)k);
+    double *sums = (double *)malloc(sizeof(double) * (size_t)(k * d));
+    double *dcounts = (double *)malloc(sizeof(double) * (size_t)k);
+    float *mind = (float *)malloc(sizeof(float) * (size_t)n);
+    int64_t *lab = (int64_t *)calloc((size_t)n, sizeof(int64_t));
+    if (!c || !nc || !counts || !sums || !dcounts || !mind || !lab) return ORC_ERR_OOM;
+    for (int64_t run = 0; run < n_init; run++) {
+        if (init) {
+            memcpy(c, init + run * k * d, sizeof(float) * (size_t)(k * d));
+        } else {
+            orc_draws g = {seed + (uint64_t)run, NULL, 0, 0};
+            orc_kpp_f32(x, n, d, k, &g, c);
+        }
+        memset(lab, 0, sizeof(int64_t) * (size_t)n);
+        int64_t n_iter = 0;
+        double inertia = (double)FLT_MAX;
+        for (int64_t it = 0; it < max_iter; it++) {
+            float ms;
+            if (wide_sums) {
+                orc_assign_f32(x, n, d, c, k, lab, mind, nthreads);
+                double s = 0.0;
+                for (int64_t i = 0; i < n; i++) s += (double)mind[i];
+                inertia = s;
+                ms = orc_update_f32_wide(x, n, d, lab, c, k, nc, sums, dcounts);
+            } else {
+                inertia = (double)orc_assign_f32(x, n, d, c, k, lab, NULL, nthreads);
+                ms = orc_update_f32(x, n, d, lab, c, k, nc, counts);
+            }
+            float *tmp = c; c = nc; nc = tmp;
+            n_iter = it + 1;
+            if (ms < tol) break;
+        }
+        memcpy(out_c + run * k * d, c, sizeof(float) * (size_t)(k * d));
+        memcpy(out_labels + run * n, lab, sizeof(int64_t) * (size_t)n);
+        out_inertia[run] = inertia;
+        out_n_iter[run] = n_iter;
+    }
+    free(c); free(nc); free(counts); free(sums); free(dcounts); free(mind); free(lab);
+    return ORC_OK;
+}

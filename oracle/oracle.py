@@ -36,6 +36,8 @@ def lib():
             getattr(_lib, f"orc_transform_{suf}").argtypes = [p, i64, i64, p, i64, i64, p, C.c_int]
         _lib.orc_draws_f64.argtypes = [u64, i64, p]
         _lib.orc_draws_f64.restype = None
+        _lib.orc_fit_runs_f32.argtypes = [p, i64, i64, i64, i64, C.c_float, i64, p, u64, C.c_int, p, p, p, p,
+                                          C.c_int]
     return _lib
 
 
@@ -157,3 +159,23 @@ def transform(centers, x, nthreads=None):
     if rc:
         raise OracleError(rc)
     return out
+
+
+def fit_runs(x, k, max_iter=300, tol=1e-4, n_init=10, init=None, seed=0, wide_sums=False, nthreads=None):
+    """Fit::fit (kmeans.rs:417-512) for f32 with every run kept (run r seeds
+    k-means++ with seed + r): dict(centers (n_init,k,d), labels (n_init,n),
+    inertia (n_init,) f64, n_iter (n_init,)). wide_sums: centroid sums and
+    inertia in f64 (the batched entry point's FP64 reduction variant)."""
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    n, d = x.shape
+    out_c = np.empty((n_init, k, d), dtype=np.float32)
+    out_l = np.empty((n_init, n), dtype=np.int64)
+    out_i = np.empty(n_init, dtype=np.float64)
+    out_n = np.empty(n_init, dtype=np.int64)
+    ini = None if init is None else np.ascontiguousarray(init, dtype=np.float32)
+    rc = lib().orc_fit_runs_f32(_ptr(x), n, d, k, max_iter, C.c_float(tol), n_init, _ptr(ini), seed,
+                                1 if wide_sums else 0, _ptr(out_c), _ptr(out_l), _ptr(out_i), _ptr(out_n),
+                                _threads(nthreads))
+    if rc:
+        raise OracleError(rc)
+    return dict(centers=out_c, labels=out_l, inertia=out_i, n_iter=out_n)

@@ -97,3 +97,28 @@ def test_fp8_needs_f32_storage_with_f64_semantics(dtype):
 def test_unknown_precision_code_rejected():
     with pytest.raises(F.Unsupported):
         F.KMeans(2, dtype="f32x64").with_precision(3).fit(np.ones((4, 2), dtype=np.float32))
+
+
+def _bp(n=10, d=2, k=2, **kw):
+    p = dict(x=np.ones((n, d), dtype=np.float32), k=k, n_init=2)
+    p.update(kw)
+    return p
+
+
+@pytest.mark.parametrize("prob,exc,needle", [
+    (_bp(k=0), F.InvalidParameter, "problem 1: Invalid parameter `n_clusters`"),
+    (_bp(n=3, k=5), F.InsufficientSamples, "problem 1: Insufficient samples"),
+    (_bp(n_init=0), F.InvalidParameter, "problem 1: Invalid parameter `n_init`"),
+    (_bp(n=2000, d=64, k=1000), F.Unsupported, "k*d <= 32768"),
+])
+def test_batched_validation_names_the_problem(prob, exc, needle):
+    with pytest.raises(exc) as e:
+        F.fit_batched([_bp(), prob])
+    assert needle in str(e.value)
+
+
+def test_batched_empty_and_bad_reduction():
+    fitted, rep = F.fit_batched([])
+    assert fitted == [] and rep["fits"] == 0
+    with pytest.raises(F.InvalidParameter):
+        F.fit_batched([_bp()], reduction=7)
