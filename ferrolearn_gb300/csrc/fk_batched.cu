@@ -22,13 +22,14 @@
 //                        choice for the bucket. Per item a fixed-tree f64
 //                        inertia partial.
 //   batch_update_kernel  per iteration, one persistent launch over the fits:
-//                        counting sort of the labels (stable), then per
-//                        (cluster, feature) the row-order sum -- f32 exactly
-//                        like recompute_centroids_into (kmeans.rs:358-401), or
-//                        f64 with each mean rounded once to f32 -- the empty
-//                        cluster rule, sqrt of the max squared shift, the
-//                        tol test, n_iter and the inertia (partials in item
-//                        order).
+//                        counting sort of the labels (stable, eight warps over
+//                        contiguous row ranges), then per (cluster, feature)
+//                        either the row-order f32 sum exactly like
+//                        recompute_centroids_into (kmeans.rs:358-401), or the
+//                        exact sum (integer, order-free) rounded once to f64
+//                        with the mean rounded once to f32; the empty cluster
+//                        rule, sqrt of the max squared shift, the tol test,
+//                        n_iter and the inertia (partials in item order).
 // One iteration (counter reset + bucket launches + update) is captured once
 // in a CUDA graph and replayed until every fit has converged or reached
 // max_iter; converged fits are skipped inside the kernels.
@@ -53,7 +54,7 @@ struct BFit {
     int32_t n, d, k, max_iter;
     float tol;
     int32_t first_item, n_items;
-    int32_t trials;
+    int32_t trials, prob;
     uint64_t seed;
 };
 
@@ -111,16 +112,72 @@ __device__ int first_reaching(const float *__restrict__ cum, int n, float thr) {
     return lo < n ? lo : n - 1;
 }
 
+// Sequential f32 fold of v[0..n) by one warp, the values broadcast by
+// shuffles (the fold itself stays in order); cum (nullable) receives every
+// running value. Loads run one batch of 256 values ahead of the fold.
+constexpr int FOLD_B = 8;  // 32-value chunks per batch
+
+__device__ __forceinline__ void fold_chunk32(float &run, float v, float &mine) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int l = 0; l < 32; l++) {
+        run = __fadd_rn(run, __shfl_sync(full, v, l));
+        if (lane == l) mine = run;
+    }
+}
+
+__device__ float warp_serial_fold(const float *__restrict__ v, int n, float *__restrict__ cum) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    float run = 0.f;
+    float cur[FOLD_B], nxt[FOLD_B];
+#pragma unroll
+    for (int b = 0; b < FOLD_B; b++) cur[b] = b * 32 + lane < n ? v[b * 32 + lane] : 0.f;
+    for (int base = 0; base < n; base += 32 * FOLD_B) {
+#pragma unroll
+        for (int b = 0; b < FOLD_B; b++) {
+            const int i = base + 32 * FOLD_B + b * 32 + lane;
+            nxt[b] = i < n ? v[i] : 0.f;
+        }
+#pragma unroll
+        for (int b = 0; b < FOLD_B; b++) {
+            const int cb = base + b * 32;
+            if (cb >= n) break;
+            float mine = 0.f;
+            if (cb + 32 <= n) {
+                fold_chunk32(run, cur[b], mine);
+            } else {
+                for (int l = 0; l < n - cb; l++) {
+                    run = __fadd_rn(run, __shfl_sync(full, cur[b], l));
+                    if (lane == l) mine = run;
+                }
+            }
+            if (cum && cb + lane < n) cum[cb + lane] = mine;
+        }
+#pragma unroll
+        for (int b = 0; b < FOLD_B; b++) cur[b] = nxt[b];
+    }
+    return run;
+}
+
+// One CTA per fit. Per new centre: the running sum of D^2 (warp 0), the
+// thresholds and candidates (thread 0), one pass over the rows computing
+// min(d(x, candidate t), D^2) for every trial t into nd (the CTA's scratch),
+// the trials' potentials (one warp each, sequential folds), the choice, and
+// D^2 <- nd[best].
 __global__ void __launch_bounds__(KPP_T) batch_kpp_kernel(const float *__restrict__ X, const BFit *__restrict__ fits,
                                                           const int *__restrict__ order, int nf, int *counter,
                                                           int *__restrict__ lab, int *__restrict__ mem,
-                                                          float *__restrict__ C) {
+                                                          float *__restrict__ C, float *__restrict__ nd_all,
+                                                          int64_t nd_stride) {
     __shared__ int q_sh, idx_sh;
     __shared__ float total_sh;
     __shared__ int cand_sh[16];
-    __shared__ float pot_sh[16];
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const unsigned full = 0xffffffffu;
+    __shared__ float pot_sh[16], thr_sh[16];
+    __shared__ float crow[8 * MAX_D];
+    const int tid = threadIdx.x, warp = tid >> 5;
+    float *nd = nd_all + (int64_t)blockIdx.x * nd_stride;
     uint64_t rng = 0;  // thread 0 only
     while (true) {
         if (tid == 0) q_sh = atomicAdd(counter, 1);
@@ -129,7 +186,7 @@ __global__ void __launch_bounds__(KPP_T) batch_kpp_kernel(const float *__restric
         __syncthreads();
         if (q >= nf) break;
         const BFit F = fits[order[q]];
-        const int n = F.n, d = F.d, k = F.k;
+        const int n = F.n, d = F.d, k = F.k, trials = F.trials;
         const float *x = X + F.x_off;
         float *mind = reinterpret_cast<float *>(lab + F.s_off);
         float *cum = reinterpret_cast<float *>(mem + F.s_off);
@@ -144,19 +201,9 @@ __global__ void __launch_bounds__(KPP_T) batch_kpp_kernel(const float *__restric
             for (int i = tid; i < n; i += KPP_T) mind[i] = sqeuc_f32(x + (int64_t)i * d, x + (int64_t)idx_sh * d, d);
         __syncthreads();
         for (int c = 1; c < k; c++) {
-            // running sum of the D^2 array: the reference's sequential f32 fold
             if (warp == 0) {
-                float run = 0.f;
-                for (int base = 0; base < n; base += 32) {
-                    const int i = base + lane;
-                    const float v = i < n ? mind[i] : 0.f;
-                    const int m = min(32, n - base);
-                    for (int l = 0; l < m; l++) {
-                        run = __fadd_rn(run, __shfl_sync(full, v, l));
-                        if (lane == l) cum[base + l] = run;
-                    }
-                }
-                if (lane == 0) total_sh = run;
+                const float total = warp_serial_fold(mind, n, cum);  // the reference's sequential f32 sum
+                if ((tid & 31) == 0) total_sh = total;
             }
             __syncthreads();
             const float total = total_sh;
@@ -167,49 +214,56 @@ __global__ void __launch_bounds__(KPP_T) batch_kpp_kernel(const float *__restric
                 __syncthreads();
                 continue;
             }
-            if (tid == 0) {
-                for (int t = 0; t < F.trials; t++) {
-                    const float thr = __fmul_rn(__double2float_rn(dev_uniform(rng)), total);
-                    cand_sh[t] = first_reaching(cum, n, thr);
-                }
+            if (tid == 0)  // the draws in order, one per trial (kmeans.rs:213-214)
+                for (int t = 0; t < trials; t++) thr_sh[t] = __fmul_rn(__double2float_rn(dev_uniform(rng)), total);
+            __syncthreads();
+            if (tid < trials) cand_sh[tid] = first_reaching(cum, n, thr_sh[tid]);
+            __syncthreads();
+            for (int e = tid; e < trials * d; e += KPP_T) {
+                const int t = e / d, j = e - t * d;
+                crow[t * d + j] = x[(int64_t)cand_sh[t] * d + j];
             }
             __syncthreads();
-            // one warp per trial: min(d(x, candidate), D^2) and its sequential potential
-            for (int t = warp; t < F.trials; t += KPP_T / 32) {
-                const float *xc = x + (int64_t)cand_sh[t] * d;
-                float pot = 0.f;
-                for (int base = 0; base < n; base += 32) {
-                    const int i = base + lane;
-                    float r = 0.f;
-                    if (i < n) {
-                        const float v = sqeuc_f32(x + (int64_t)i * d, xc, d);
-                        const float mv = mind[i];
-                        r = v < mv ? v : mv;
+            for (int i = tid; i < n; i += KPP_T) {
+                const float *xr = x + (int64_t)i * d;
+                float acc[8];
+#pragma unroll
+                for (int t = 0; t < 8; t++) acc[t] = 0.f;
+                for (int j = 0; j < d; j++) {
+                    const float xv = xr[j];
+#pragma unroll
+                    for (int t = 0; t < 8; t++) {
+                        if (t < trials) {
+                            const float df = __fsub_rn(xv, crow[t * d + j]);
+                            acc[t] = __fadd_rn(acc[t], __fmul_rn(df, df));
+                        }
                     }
-                    const int m = min(32, n - base);
-                    for (int l = 0; l < m; l++) pot = __fadd_rn(pot, __shfl_sync(full, r, l));
                 }
-                if (lane == 0) pot_sh[t] = pot;
+                const float mv = mind[i];
+#pragma unroll
+                for (int t = 0; t < 8; t++)
+                    if (t < trials) nd[(int64_t)t * n + i] = acc[t] < mv ? acc[t] : mv;
+            }
+            __syncthreads();
+            for (int t = warp; t < trials; t += KPP_T / 32) {
+                const float pot = warp_serial_fold(nd + (int64_t)t * n, n, nullptr);
+                if ((tid & 31) == 0) pot_sh[t] = pot;
             }
             __syncthreads();
             if (tid == 0) {  // strictly smallest potential, first trial on ties (kmeans.rs:239-243)
                 int best = 0;
                 float bp = pot_sh[0];
-                for (int t = 1; t < F.trials; t++)
+                for (int t = 1; t < trials; t++)
                     if (pot_sh[t] < bp) {
                         bp = pot_sh[t];
                         best = t;
                     }
-                idx_sh = cand_sh[best];
+                idx_sh = best;
             }
             __syncthreads();
-            const float *xb = x + (int64_t)idx_sh * d;
-            for (int j = tid; j < d; j += KPP_T) cen[(int64_t)c * d + j] = xb[j];
-            for (int i = tid; i < n; i += KPP_T) {
-                const float v = sqeuc_f32(x + (int64_t)i * d, xb, d);
-                const float mv = mind[i];
-                mind[i] = v < mv ? v : mv;
-            }
+            const int best = idx_sh;
+            for (int j = tid; j < d; j += KPP_T) cen[(int64_t)c * d + j] = crow[best * d + j];
+            for (int i = tid; i < n; i += KPP_T) mind[i] = nd[(int64_t)best * n + i];
             __syncthreads();
         }
     }
@@ -346,6 +400,82 @@ __global__ void __launch_bounds__(ASSIGN_T) batch_assign_kernel(const float *__r
 }
 
 // ---------------------------------------------------------------- update --
+// Exact cluster sums for the f64 reduction: x = q1 2^(kb-23) + q2 2^(kb-46)
+// + r2 with integer q1, q2 (the two-grid split: 2^ea <= max|x| < 2^(ea+1),
+// kb = ea + 2, C1 = 1.5 2^kb, C2 = 1.5 2^(kb-23)); r2 is exact and zero
+// unless |x| < 2^(ea-21), and then goes to a 128-bit fixed-point sum with F
+// fraction bits (F = 124 - bitlen(n) - ea, so no sum can overflow; bits
+// below 2^-F are truncated toward zero). Integer sums are order-free, so the
+// result is the exact sum whatever the order, rounded once to f64.
+__device__ __forceinline__ void add128u(uint64_t &lo, uint64_t &hi, uint64_t tlo, uint64_t thi) {
+    asm("add.cc.u64 %0, %0, %2;\n\taddc.u64 %1, %1, %3;" : "+l"(lo), "+l"(hi) : "l"(tlo), "l"(thi));
+}
+
+__device__ __noinline__ void fixed_add_small(uint64_t &lo, uint64_t &hi, float x, int F) {
+    const uint32_t b = __float_as_uint(x);
+    const uint32_t ex = (b >> 23) & 0xFFu;
+    if (ex == 0xFFu) return;
+    const uint64_t m = (uint64_t)((b & 0x7FFFFFu) | (ex ? 0x800000u : 0u));
+    const int s = (ex ? (int)ex : 1) - 150 + F;
+    uint64_t tlo, thi;
+    if (s >= 64) {
+        tlo = 0;
+        thi = m << (s - 64);
+    } else if (s >= 0) {
+        tlo = m << s;
+        thi = s > 40 ? m >> (64 - s) : 0;
+    } else {
+        tlo = s > -32 ? m >> (-s) : 0;
+        thi = 0;
+    }
+    if (b >> 31) {
+        tlo = ~tlo;
+        thi = ~thi;
+        add128u(tlo, thi, 1ull, 0ull);
+    }
+    add128u(lo, hi, tlo, thi);
+}
+
+// Correctly rounded (nearest, ties to even) f64 value of the signed 128-bit
+// fixed-point number (hi:lo) with F fraction bits.
+__device__ double fixed128_to_double(uint64_t lo, uint64_t hi, int F) {
+    const bool neg = (hi >> 63) != 0;
+    if (neg) {
+        lo = ~lo;
+        hi = ~hi;
+        add128u(lo, hi, 1ull, 0ull);
+    }
+    if (lo == 0 && hi == 0) return 0.0;
+    const int msb = hi ? 127 - __clzll((long long)hi) : 63 - __clzll((long long)lo);
+    double r;
+    if (msb <= 52) {
+        r = scalbn((double)lo, -F);
+    } else {
+        const int sh = msb - 52;  // 1 <= sh <= 75
+        uint64_t mant, rem_hi, rem_lo, half_hi, half_lo;
+        if (sh < 64) {
+            mant = (lo >> sh) | (sh ? (hi << (64 - sh)) : 0);
+            rem_lo = lo & ((1ull << sh) - 1ull);
+            rem_hi = 0;
+            half_lo = 1ull << (sh - 1);
+            half_hi = 0;
+        } else {
+            mant = hi >> (sh - 64);
+            rem_lo = lo;
+            rem_hi = sh > 64 ? hi & ((1ull << (sh - 64)) - 1ull) : 0;
+            half_lo = sh == 64 ? (1ull << 63) : 0;
+            half_hi = sh > 64 ? (1ull << (sh - 65)) : 0;
+        }
+        const bool above = rem_hi > half_hi || (rem_hi == half_hi && rem_lo > half_lo);
+        const bool tie = rem_hi == half_hi && rem_lo == half_lo;
+        if (above || (tie && (mant & 1ull))) mant += 1;
+        r = scalbn((double)mant, sh - F);
+    }
+    return neg ? -r : r;
+}
+
+__device__ __forceinline__ int bitlen64(long long v) { return 64 - __clzll(v > 0 ? v : 1); }
+
 template <bool WIDE>
 __global__ void __launch_bounds__(UPDATE_T) batch_update_kernel(const float *__restrict__ X,
                                                                 const BFit *__restrict__ fits,
@@ -353,10 +483,13 @@ __global__ void __launch_bounds__(UPDATE_T) batch_update_kernel(const float *__r
                                                                 const int *__restrict__ order, int nf, int *counter,
                                                                 float *__restrict__ C, const int *__restrict__ lab,
                                                                 int *__restrict__ mem,
-                                                                const double *__restrict__ partial, int *active) {
-    __shared__ int hist[MAX_K], off[MAX_K], runp[MAX_K];
+                                                                const double *__restrict__ partial, int *active,
+                                                                const float *__restrict__ pamax) {
+    constexpr int NW = UPDATE_T / 32;
+    __shared__ int wrun[NW][MAX_K];
+    __shared__ int hist[MAX_K], off[MAX_K];
     __shared__ int q_sh;
-    __shared__ float red[UPDATE_T / 32];
+    __shared__ float red[NW];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const unsigned full = 0xffffffffu;
     while (true) {
@@ -371,41 +504,63 @@ __global__ void __launch_bounds__(UPDATE_T) batch_update_kernel(const float *__r
         const int n = F.n, d = F.d, k = F.k;
         const int *L = lab + F.s_off;
         int *M = mem + F.s_off;
-        for (int c = tid; c < k; c += UPDATE_T) hist[c] = 0;
+        // counting sort, stable: warp w owns the contiguous rows [w R, (w+1) R)
+        const int R = (n + NW - 1) / NW;
+        const int rlo = min(n, warp * R), rhi = min(n, rlo + R);
+        for (int e = tid; e < NW * k; e += UPDATE_T) wrun[e / k][e % k] = 0;
         __syncthreads();
-        for (int i = tid; i < n; i += UPDATE_T) atomicAdd(&hist[L[i]], 1);
+        for (int i = rlo + lane; i < rhi; i += 32) atomicAdd(&wrun[warp][L[i]], 1);
+        __syncthreads();
+        for (int c = tid; c < k; c += UPDATE_T) {
+            int t = 0;
+            for (int w = 0; w < NW; w++) t += wrun[w][c];
+            hist[c] = t;
+        }
         __syncthreads();
         if (tid == 0) {
             int acc = 0;
             for (int c = 0; c < k; c++) {
                 off[c] = acc;
-                runp[c] = acc;
                 acc += hist[c];
             }
         }
         __syncthreads();
-        // stable scatter (row order within each cluster), one warp
-        if (warp == 0) {
-            for (int base = 0; base < n; base += 32) {
-                const int i = base + lane;
-                const int l = i < n ? L[i] : -1;
-                const unsigned peers = __match_any_sync(full, l);
-                const int leader = __ffs(peers) - 1;
-                const int rank = __popc(peers & ((1u << lane) - 1u));
-                int b = 0;
-                if (lane == leader && l >= 0) {
-                    b = runp[l];
-                    runp[l] = b + __popc(peers);
-                }
-                b = __shfl_sync(full, b, leader);
-                if (l >= 0) M[b + rank] = i;
+        for (int c = tid; c < k; c += UPDATE_T) {
+            int start = off[c];
+            for (int w = 0; w < NW; w++) {
+                const int t = wrun[w][c];
+                wrun[w][c] = start;
+                start += t;
             }
+        }
+        __syncthreads();
+        for (int base = rlo; base < rhi; base += 32) {
+            const int i = base + lane;
+            const int l = i < rhi ? L[i] : -1;
+            const unsigned peers = __match_any_sync(full, l);
+            const int leader = __ffs(peers) - 1;
+            const int rank = __popc(peers & ((1u << lane) - 1u));
+            int b = 0;
+            if (lane == leader && l >= 0) {
+                b = wrun[warp][l];
+                wrun[warp][l] = b + __popc(peers);
+            }
+            b = __shfl_sync(full, b, leader);
+            if (l >= 0) M[b + rank] = i;
         }
         __syncthreads();
         const int cur = state[f].cur;
         const float *oldc = C + F.c_off + (int64_t)cur * k * d;
         float *newc = C + F.c_off + (int64_t)(1 - cur) * k * d;
         const float *x = X + F.x_off;
+        // exact-sum constants (f64 reduction)
+        const float amax = WIDE ? pamax[F.prob] : 0.f;
+        const int ea = amax > 0.f ? (int)((__float_as_uint(amax) >> 23) & 0xFFu) - 127 : -126;
+        const bool grids = ea >= -90 && ea <= 100;
+        const int kb = ea + 2;
+        const int Fb = 124 - bitlen64(n) - ea;
+        const float C1 = grids ? ldexpf(1.5f, kb) : 0.f, C2 = grids ? ldexpf(1.5f, kb - 23) : 0.f;
+        const int b1 = __float_as_int(C1), b2 = __float_as_int(C2);
         for (int pr = tid; pr < k * d; pr += UPDATE_T) {
             const int c = pr / d, j = pr - c * d;
             const int cnt = hist[c], o = off[c];
@@ -413,33 +568,67 @@ __global__ void __launch_bounds__(UPDATE_T) batch_update_kernel(const float *__r
                 newc[pr] = oldc[pr];  // empty cluster keeps its centre
                 continue;
             }
+            // values of the cluster's rows in row order, loaded 8 ahead
+            float cur8[8], nxt8[8];
+#pragma unroll
+            for (int u = 0; u < 8; u++) cur8[u] = u < cnt ? x[(int64_t)M[o + u] * d + j] : 0.f;
             if (WIDE) {
-                double acc = 0.0;
-                int m = 0;
-                for (; m + 4 <= cnt; m += 4) {
-                    const int r0 = M[o + m], r1 = M[o + m + 1], r2 = M[o + m + 2], r3 = M[o + m + 3];
-                    const float v0 = x[(int64_t)r0 * d + j], v1 = x[(int64_t)r1 * d + j];
-                    const float v2 = x[(int64_t)r2 * d + j], v3 = x[(int64_t)r3 * d + j];
-                    acc = __dadd_rn(acc, (double)v0);
-                    acc = __dadd_rn(acc, (double)v1);
-                    acc = __dadd_rn(acc, (double)v2);
-                    acc = __dadd_rn(acc, (double)v3);
+                long long a1 = 0, a2 = 0;
+                uint64_t slo = 0, shi = 0;
+                float probe = 0.f;
+                for (int m = 0; m < cnt; m += 8) {
+#pragma unroll
+                    for (int u = 0; u < 8; u++) nxt8[u] = m + 8 + u < cnt ? x[(int64_t)M[o + m + 8 + u] * d + j] : 0.f;
+#pragma unroll
+                    for (int u = 0; u < 8; u++) {
+                        const float xv = cur8[u];  // 0 past the end
+                        probe = __fmaf_rn(xv, 0.f, probe);
+                        if (grids) {
+                            const float s1 = __fadd_rn(xv, C1);
+                            a1 += __float_as_int(s1) - b1;
+                            const float r = __fsub_rn(xv, __fsub_rn(s1, C1));
+                            const float s2 = __fadd_rn(r, C2);
+                            a2 += __float_as_int(s2) - b2;
+                            const float r2 = __fsub_rn(r, __fsub_rn(s2, C2));
+                            if (r2 != 0.f) fixed_add_small(slo, shi, r2, Fb);
+                        } else {
+                            fixed_add_small(slo, shi, xv, Fb);
+                        }
+                    }
+#pragma unroll
+                    for (int u = 0; u < 8; u++) cur8[u] = nxt8[u];
                 }
-                for (; m < cnt; m++) acc = __dadd_rn(acc, (double)x[(int64_t)M[o + m] * d + j]);
-                newc[pr] = __double2float_rn(__ddiv_rn(acc, (double)cnt));
+                double sum;
+                if (!(probe == 0.f)) {  // a non-finite value: IEEE f64 summation of the specials
+                    uint32_t fl = 0u;
+                    for (int m = 0; m < cnt; m++) {
+                        const uint32_t bb = __float_as_uint(x[(int64_t)M[o + m] * d + j]);
+                        if (((bb >> 23) & 0xFFu) == 0xFFu) fl |= (bb & 0x7FFFFFu) ? 1u : ((bb >> 31) ? 4u : 2u);
+                    }
+                    sum = ((fl & 1u) || (fl & 6u) == 6u) ? __longlong_as_double(0x7FF8000000000000LL)
+                          : (fl & 2u) ? __longlong_as_double(0x7FF0000000000000LL)
+                                      : __longlong_as_double((long long)0xFFF0000000000000ULL);
+                } else {
+                    if (grids) {
+                        const __int128 v1 = (__int128)a1 << (kb - 23 + Fb);
+                        const __int128 v2 = (__int128)a2 << (kb - 46 + Fb);
+                        add128u(slo, shi, (uint64_t)v1, (uint64_t)((unsigned __int128)v1 >> 64));
+                        add128u(slo, shi, (uint64_t)v2, (uint64_t)((unsigned __int128)v2 >> 64));
+                    }
+                    sum = fixed128_to_double(slo, shi, Fb);
+                }
+                newc[pr] = __double2float_rn(__ddiv_rn(sum, (double)cnt));
             } else {
                 float acc = 0.f;
-                int m = 0;
-                for (; m + 4 <= cnt; m += 4) {
-                    const int r0 = M[o + m], r1 = M[o + m + 1], r2 = M[o + m + 2], r3 = M[o + m + 3];
-                    const float v0 = x[(int64_t)r0 * d + j], v1 = x[(int64_t)r1 * d + j];
-                    const float v2 = x[(int64_t)r2 * d + j], v3 = x[(int64_t)r3 * d + j];
-                    acc = __fadd_rn(acc, v0);
-                    acc = __fadd_rn(acc, v1);
-                    acc = __fadd_rn(acc, v2);
-                    acc = __fadd_rn(acc, v3);
+                for (int m = 0; m < cnt; m += 8) {
+#pragma unroll
+                    for (int u = 0; u < 8; u++) nxt8[u] = m + 8 + u < cnt ? x[(int64_t)M[o + m + 8 + u] * d + j] : 0.f;
+#pragma unroll
+                    for (int u = 0; u < 8; u++)
+                        if (m + u < cnt) acc = __fadd_rn(acc, cur8[u]);
+#pragma unroll
+                    for (int u = 0; u < 8; u++) cur8[u] = nxt8[u];
                 }
-                for (; m < cnt; m++) acc = __fadd_rn(acc, x[(int64_t)M[o + m] * d + j]);
                 newc[pr] = __fdiv_rn(acc, (float)cnt);  // counts as F are exact below 2^24
             }
         }
@@ -456,7 +645,7 @@ __global__ void __launch_bounds__(UPDATE_T) batch_update_kernel(const float *__r
         __syncthreads();
         if (tid == 0) {
             float m2 = 0.f;
-            for (int w = 0; w < UPDATE_T / 32; w++) m2 = fmaxf(m2, red[w]);
+            for (int w = 0; w < NW; w++) m2 = fmaxf(m2, red[w]);
             const float shift = __fsqrt_rn(m2);
             double in = 0.0;
             for (int it = 0; it < F.n_items; it++) in += partial[F.first_item + it];
@@ -469,6 +658,30 @@ __global__ void __launch_bounds__(UPDATE_T) batch_update_kernel(const float *__r
                 atomicSub(active, 1);
             }
             state[f] = st;
+        }
+        __syncthreads();
+    }
+}
+
+// max |x| over the finite values of each problem (the exact sums' scale)
+__global__ void batch_amax_kernel(const float *__restrict__ X, const int64_t *__restrict__ xoff,
+                                  const int64_t *__restrict__ xlen, int np, float *__restrict__ amax) {
+    __shared__ float red[32];
+    for (int p = blockIdx.x; p < np; p += gridDim.x) {
+        const float *x = X + xoff[p];
+        float m = 0.f;
+        for (int64_t e = threadIdx.x; e < xlen[p]; e += blockDim.x) {
+            const float a = fabsf(x[e]);
+            if (a < INFINITY) m = fmaxf(m, a);
+        }
+#pragma unroll
+        for (int o = 16; o >= 1; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            float r = 0.f;
+            for (int w = 0; w < (int)(blockDim.x >> 5); w++) r = fmaxf(r, red[w]);
+            amax[p] = r;
         }
         __syncthreads();
     }
@@ -595,6 +808,7 @@ fk_status batched_fit_impl(Ctx &ctx, fk_batch_problem *P, int64_t np, int reduct
             F.tol = (float)q.tol;
             F.trials = kpp_trials_host(q.n_clusters);
             F.seed = q.random_state + (uint64_t)r;
+            F.prob = (int32_t)p;
             fits.push_back(F);
             fit_prob.push_back((int)p);
             fit_run.push_back((int)r);
@@ -637,10 +851,24 @@ fk_status batched_fit_impl(Ctx &ctx, fk_batch_problem *P, int64_t np, int reduct
     int *dlab = (int *)ctx.get(BUF_BLAB, sizeof(int) * (size_t)soff + 16);
     int *dmem = (int *)ctx.get(BUF_BMEM, sizeof(int) * (size_t)soff + 16);
     float *dC = (float *)ctx.get(BUF_BCEN, sizeof(float) * (size_t)coff + 16);
+    int64_t *dxo = (int64_t *)ctx.get(BUF_BXOFF, sizeof(int64_t) * (size_t)(2 * np) + sizeof(float) * (size_t)np + 64);
+    float *damax = (float *)(dxo + 2 * np);
     for (int64_t p = 0; p < np; p++)
         FK_CUDA(cudaMemcpyAsync(X + xoff[p], P[p].x, sizeof(float) * (size_t)(P[p].n * P[p].d), cudaMemcpyDefault,
                                 s));
     FK_CUDA(cudaMemcpyAsync(dfits, fits.data(), sizeof(BFit) * (size_t)nf, cudaMemcpyHostToDevice, s));
+    {
+        std::vector<int64_t> xol(2 * np);
+        for (int64_t p = 0; p < np; p++) {
+            xol[p] = xoff[p];
+            xol[np + p] = P[p].n * P[p].d;
+        }
+        FK_CUDA(cudaMemcpyAsync(dxo, xol.data(), sizeof(int64_t) * xol.size(), cudaMemcpyHostToDevice, s));
+        FK_CUDA(cudaStreamSynchronize(s));  // xol is host stack memory
+        batch_amax_kernel<<<(unsigned)std::min<int64_t>(np, ctx.num_sms * 4), 256, 0, s>>>(X, dxo, dxo + np, (int)np,
+                                                                                        damax);
+        FK_LAUNCH_CHECK();
+    }
     if (!items.empty())
         FK_CUDA(cudaMemcpyAsync(ditems, items.data(), sizeof(BItem) * items.size(), cudaMemcpyHostToDevice, s));
     std::vector<int> orders(byc);
@@ -673,8 +901,12 @@ fk_status batched_fit_impl(Ctx &ctx, fk_batch_problem *P, int64_t np, int reduct
     // ---- k-means++ (one persistent launch)
     if (!kpp_order.empty()) {
         const int grid = std::min((int)kpp_order.size(), ctx.num_sms * 8);
+        int64_t nmax_kpp = 1;
+        for (int f : kpp_order) nmax_kpp = std::max<int64_t>(nmax_kpp, fits[f].n);
+        const int64_t nd_stride = 8 * nmax_kpp;  // trials <= 8 (k <= 1024)
+        float *nd = (float *)ctx.get(BUF_BND, sizeof(float) * (size_t)(nd_stride * grid));
         batch_kpp_kernel<<<grid, KPP_T, 0, s>>>(X, dfits, dorder + nf, (int)kpp_order.size(), dctr + 30, dlab, dmem,
-                                                dC);
+                                                dC, nd, nd_stride);
         FK_LAUNCH_CHECK();
         // k-means++ used the label arrays as scratch: fits that run no
         // iteration report all-zero labels (kmeans.rs:459-466)
@@ -735,10 +967,10 @@ fk_status batched_fit_impl(Ctx &ctx, fk_batch_problem *P, int64_t np, int reduct
         const int ug = std::min(nf, ctx.num_sms * 4);
         if (reduction == FK_REDUCE_F64)
             batch_update_kernel<true><<<ug, UPDATE_T, 0, s>>>(X, dfits, dstate, dorder, nf, dctr + 20, dC, dlab,
-                                                              dmem, dpart, dctr + 31);
+                                                              dmem, dpart, dctr + 31, damax);
         else
             batch_update_kernel<false><<<ug, UPDATE_T, 0, s>>>(X, dfits, dstate, dorder, nf, dctr + 20, dC, dlab,
-                                                               dmem, dpart, dctr + 31);
+                                                               dmem, dpart, dctr + 31, damax);
     };
     int max_iter = 0;
     for (const BFit &F : fits) max_iter = std::max(max_iter, F.max_iter);

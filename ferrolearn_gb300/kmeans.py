@@ -371,8 +371,8 @@ def fit_batched(problems, reduction="reference", ctx=None):
     init ((n_init, k, d) or (k, d) initial centres). Each problem is
     Fit::fit (kmeans.rs:417-512) with F = f32; run r draws k-means++ from the
     stream seeded with random_state + r. reduction: "reference" (f32 row-order
-    centroid sums, bit-identical to KMeans<f32>) or "f64" (f64 sums, each mean
-    rounded once to f32).
+    centroid sums, bit-identical to KMeans<f32>) or "f64" (each cluster sum
+    formed exactly and rounded once to f64, the mean rounded once to f32).
 
     Returns (list of FittedKMeans, report dict with per-fit inertia / n_iter,
     the autotuner's tile choice per (d, k) bucket and phase times).

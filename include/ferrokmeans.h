@@ -225,7 +225,8 @@ fk_status fk_kmeans_score_f64_noalloc(const double *x, int64_t n, int64_t d, con
  * FK_ERR_UNSUPPORTED); validation errors name the problem index. */
 typedef enum fk_reduction {
     FK_REDUCE_REFERENCE = 0, /* row-order f32 sums (kmeans.rs:358-401 for F = f32) */
-    FK_REDUCE_F64 = 1        /* row-order f64 sums, each mean rounded once to f32;
+    FK_REDUCE_F64 = 1        /* each cluster sum formed exactly and rounded once
+                                to f64, the mean in f64 rounded once to f32;
                                 inertia summed in f64 */
 } fk_reduction;
 

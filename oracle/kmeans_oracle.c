@@ -305,21 +305,45 @@ int orc_widen_f32(const float *x, int64_t count, double *out) {
  * init[r]; Lloyd iterations follow kmeans.rs:459-505. wide_sums = 0 is the
  * reference's own f32 arithmetic (recompute_centroids_into, kmeans.rs:358-401,
  * row-order f32 sums); wide_sums = 1 is the batched entry point's FP64
- * reduction variant: the same row-order sums in f64, each mean rounded once
- * to f32 (sum / count in f64), and the inertia summed in f64 in row order.
+ * reduction variant: each cluster sum formed exactly (128-bit fixed point
+ * with F = 124 - bitlen(n) - e fraction bits, 2^e <= max|x| < 2^(e+1)),
+ * rounded once to f64, divided by the count in f64 and rounded to f32; the
+ * inertia summed in f64 in row order.
  * Outputs per run: centres (k*d), labels (n), inertia (as f64), n_iter. */
+static int orc_bitlen(int64_t v) { int b = 0; while (v > 0) { b++; v >>= 1; } return b ? b : 1; }
+
 static float orc_update_f32_wide(const float *x, int64_t n, int64_t d, const int64_t *labels,
-                                 const float *old_c, int64_t k, float *new_c, double *sums, double *counts) {
-    memset(sums, 0, sizeof(double) * (size_t)(k * d));
-    for (int64_t q = 0; q < k; q++) counts[q] = 0.0;
+                                 const float *old_c, int64_t k, float *new_c, __int128 *sums,
+                                 unsigned *flags, int64_t *counts, int F) {
+    memset(sums, 0, sizeof(__int128) * (size_t)(k * d));
+    memset(flags, 0, sizeof(unsigned) * (size_t)(k * d));
+    for (int64_t q = 0; q < k; q++) counts[q] = 0;
     for (int64_t i = 0; i < n; i++) {
         int64_t l = labels[i];
-        counts[l] = counts[l] + 1.0;
-        for (int64_t j = 0; j < d; j++) sums[l * d + j] = sums[l * d + j] + (double)x[i * d + j];
+        counts[l] += 1;
+        for (int64_t j = 0; j < d; j++) {
+            float v = x[i * d + j];
+            if (isnan(v)) { flags[l * d + j] |= 1u; continue; }
+            if (isinf(v)) { flags[l * d + j] |= v > 0 ? 2u : 4u; continue; }
+            int e;
+            float fr = frexpf(v, &e);                      /* v = fr * 2^e, 0.5 <= |fr| < 1 */
+            int64_t m = (int64_t)ldexpf(fabsf(fr), 24);    /* exact 24-bit integer */
+            int s = e - 24 + F;                            /* |v| = m * 2^(s - F) */
+            __int128 t = s >= 0 ? ((__int128)m << s) : (s > -64 ? (__int128)(m >> (-s)) : 0);
+            sums[l * d + j] += v < 0 ? -t : t;
+        }
     }
     for (int64_t q = 0; q < k; q++) {
-        if (counts[q] > 0.0) {
-            for (int64_t j = 0; j < d; j++) new_c[q * d + j] = (float)(sums[q * d + j] / counts[q]);
+        if (counts[q] > 0) {
+            for (int64_t j = 0; j < d; j++) {
+                unsigned fl = flags[q * d + j];
+                double sm;
+                if ((fl & 1u) || (fl & 6u) == 6u) sm = NAN;
+                else if (fl & 2u) sm = INFINITY;
+                else if (fl & 4u) sm = -INFINITY;
+                else sm = ldexp((double)sums[q * d + j], -F);  /* the conversion rounds to nearest */
+                new_c[q * d + j] = (float)(sm / (double)counts[q]);
+            }
         } else {
             memcpy(new_c + q * d, old_c + q * d, sizeof(float) * (size_t)d);
         }
@@ -341,11 +365,20 @@ int orc_fit_runs_f32(const float *x, int64_t n, int64_t d, int64_t k, int64_t ma
     float *c = (float *)malloc(sizeof(float) * (size_t)(k * d));
     float *nc = (float *)malloc(sizeof(float) * (size_t)(k * d));
     float *counts = (float *)malloc(sizeof(float) * (size_t)k);
-    double *sums = (double *)malloc(sizeof(double) * (size_t)(k * d));
-    double *dcounts = (double *)malloc(sizeof(double) * (size_t)k);
+    __int128 *sums = (__int128 *)malloc(sizeof(__int128) * (size_t)(k * d));
+    unsigned *flags = (unsigned *)malloc(sizeof(unsigned) * (size_t)(k * d));
+    int64_t *icounts = (int64_t *)malloc(sizeof(int64_t) * (size_t)k);
     float *mind = (float *)malloc(sizeof(float) * (size_t)n);
     int64_t *lab = (int64_t *)calloc((size_t)n, sizeof(int64_t));
-    if (!c || !nc || !counts || !sums || !dcounts || !mind || !lab) return ORC_ERR_OOM;
+    if (!c || !nc || !counts || !sums || !flags || !icounts || !mind || !lab) return ORC_ERR_OOM;
+    float amax = 0.0f;
+    for (int64_t i = 0; i < n * d; i++) {
+        float a = fabsf(x[i]);
+        if (a < INFINITY && a > amax) amax = a;
+    }
+    int ea = -126;
+    if (amax > 0.0f) { frexpf(amax, &ea); ea -= 1; }   /* 2^ea <= amax < 2^(ea+1) */
+    const int F = 124 - orc_bitlen(n) - ea;
     for (int64_t run = 0; run < n_init; run++) {
         if (init) {
             memcpy(c, init + run * k * d, sizeof(float) * (size_t)(k * d));
@@ -363,7 +396,7 @@ int orc_fit_runs_f32(const float *x, int64_t n, int64_t d, int64_t k, int64_t ma
                 double s = 0.0;
                 for (int64_t i = 0; i < n; i++) s += (double)mind[i];
                 inertia = s;
-                ms = orc_update_f32_wide(x, n, d, lab, c, k, nc, sums, dcounts);
+                ms = orc_update_f32_wide(x, n, d, lab, c, k, nc, sums, flags, icounts, F);
             } else {
                 inertia = (double)orc_assign_f32(x, n, d, c, k, lab, NULL, nthreads);
                 ms = orc_update_f32(x, n, d, lab, c, k, nc, counts);
@@ -377,6 +410,6 @@ int orc_fit_runs_f32(const float *x, int64_t n, int64_t d, int64_t k, int64_t ma
         out_inertia[run] = inertia;
         out_n_iter[run] = n_iter;
     }
-    free(c); free(nc); free(counts); free(sums); free(dcounts); free(mind); free(lab);
+    free(c); free(nc); free(counts); free(sums); free(flags); free(icounts); free(mind); free(lab);
     return ORC_OK;
 }
