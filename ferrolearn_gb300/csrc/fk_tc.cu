@@ -236,7 +236,7 @@ __device__ __forceinline__ void merge_res(uint32_t &R1, int &I1, uint32_t &R2, i
     }
 }
 
-// Ranks the 128 columns [HALF*128, HALF*128+128) of one accumulator block:
+// Ranks the 128 columns of one half of an accumulator block:
 // four interleaved top-2 chains (three float min/max per element on the keys,
 // which are positive floats), merged with the bound of the rest. A NaN score
 // (NaN row) is ignored by fminf/fmaxf; such rows have non-finite bound
@@ -253,7 +253,7 @@ __device__ __forceinline__ float make_key(uint32_t bits, float cgrid, float ulp)
     return __fmaf_rn(ulp, (float)CODE, t);
 }
 
-template <int HALF, int CH, int E>
+template <int CH, int E>
 __device__ __forceinline__ void rank_pair(const uint32_t (&r)[32], float cgrid, float ulp, float &a1, float &a2) {
     // top-2 of {a1 >= a2, k0, k1}: a1' = max(a1, max(k0,k1)),
     // a2' = max(min(a1, max(k0,k1)), a2, min(k0,k1))
@@ -264,25 +264,26 @@ __device__ __forceinline__ void rank_pair(const uint32_t (&r)[32], float cgrid, 
     a1 = fmaxf(a1, m);
 }
 
-template <int HALF, int CH, int E>
+template <int CH, int E>
 struct RankChunk {
     static __device__ __forceinline__ void run(const uint32_t (&r)[32], float cg, float ulp, float (&a1)[4],
                                                float (&a2)[4]) {
-        rank_pair<HALF, CH, E>(r, cg, ulp, a1[(E >> 1) & 3], a2[(E >> 1) & 3]);
-        RankChunk<HALF, CH, E + 2>::run(r, cg, ulp, a1, a2);
+        rank_pair<CH, E>(r, cg, ulp, a1[(E >> 1) & 3], a2[(E >> 1) & 3]);
+        RankChunk<CH, E + 2>::run(r, cg, ulp, a1, a2);
     }
 };
-template <int HALF, int CH>
-struct RankChunk<HALF, CH, 32> {
+template <int CH>
+struct RankChunk<CH, 32> {
     static __device__ __forceinline__ void run(const uint32_t (&)[32], float, float, float (&)[4], float (&)[4]) {}
 };
 
-// Ranks the 128 columns [HALF*128, HALF*128+128) of one accumulator block:
+// Ranks the 128 columns of one half of an accumulator block:
 // four interleaved top-2 chains over the keys, two elements per step with a
 // three-input max, the next 32 columns loading from TMEM while the current
 // ones are ranked; then the chains are merged with the bound of the rest.
 // Returns keys; the low 7 bits of a key are 127 - (column within the half).
-template <int HALF>
+// Both halves run the same code (the codes are local to the half), so the
+// eight epilogue warps share one copy of it in the instruction cache.
 __device__ __forceinline__ void rank_half(uint32_t col_addr, float cgrid, float ulp, uint32_t &b1, uint32_t &b2,
                                           uint32_t &bu) {
     float a1[4] = {0.f, 0.f, 0.f, 0.f}, a2[4] = {0.f, 0.f, 0.f, 0.f};
@@ -290,15 +291,15 @@ __device__ __forceinline__ void rank_half(uint32_t col_addr, float cgrid, float 
     tmem_ld32(col_addr, ra);
     tmem_wait(ra);
     tmem_ld32(col_addr + 32, rb);
-    RankChunk<HALF, 0, 0>::run(ra, cgrid, ulp, a1, a2);
+    RankChunk<0, 0>::run(ra, cgrid, ulp, a1, a2);
     tmem_wait(rb);
     tmem_ld32(col_addr + 64, ra);
-    RankChunk<HALF, 1, 0>::run(rb, cgrid, ulp, a1, a2);
+    RankChunk<1, 0>::run(rb, cgrid, ulp, a1, a2);
     tmem_wait(ra);
     tmem_ld32(col_addr + 96, rb);
-    RankChunk<HALF, 2, 0>::run(ra, cgrid, ulp, a1, a2);
+    RankChunk<2, 0>::run(ra, cgrid, ulp, a1, a2);
     tmem_wait(rb);
-    RankChunk<HALF, 3, 0>::run(rb, cgrid, ulp, a1, a2);
+    RankChunk<3, 0>::run(rb, cgrid, ulp, a1, a2);
     b1 = __float_as_uint(a1[0]);
     b2 = __float_as_uint(a2[0]);
     bu = b2;
@@ -554,10 +555,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                     }
                 }
                 uint32_t b1, b2, bu;
-                if (half == 0)
-                    rank_half<0>(col, cg, ul, b1, b2, bu);
-                else
-                    rank_half<1>(col, cg, ul, b1, b2, bu);
+                rank_half(col, cg, ul, b1, b2, bu);
                 tc_fence_before();
                 __syncwarp();
                 if (lane == 0) mbar_arrive(bar_aempty(buf));
