@@ -3,28 +3,32 @@
 // The approximate pass scores every (row, centre) pair as
 //     T_c = xh . ch + a_c,   a_c = BIG - ||c'||^2 / 2,
 // where x' = x - mu and c' = c - mu are centred by the column mean mu, xh and
-// ch are their BF16 roundings, and BIG is a per-iteration constant that makes
-// every T_c positive. Maximising T_c minimises ||x - c||^2. The contraction
-// runs on the tensor cores (fk_tc.cu); a_c enters as three extra BF16 columns
-// multiplied by a constant column of ones, so the epilogue only ranks values.
+// ch are their BF16 roundings (or E4M3 values times power-of-two scales:
+// per row for X, one per launch for the centres), and BIG is a per-iteration
+// constant that makes every T_c positive. Maximising T_c minimises
+// ||x - c||^2. The contraction runs on the tensor cores (fk_tc.cu); a_c
+// enters as three extra BF16 columns multiplied by a constant column of ones
+// (by the row's scale for FP8), so the epilogue only ranks values.
 //
 // Per row, with the pass's best and second-best values v1 >= v2, the error
 // bound (in T units)
 //     E = ex * Cn + xn * Ec + ACC * (xn * Chn + BIG) + REPR * BIG
 // (ex = ||x' - xh||, xn = ||xh||, Cn = max ||c'||, Ec = max ||c' - ch||,
 // Chn = max ||ch||; ACC and REPR generous multiples of 2^-22 covering the FP32
-// accumulation and the three-term BF16 split of a_c), the key-truncation
-// quantum q and the FP64 oracle's own rounding delta give the threshold
-// thr = 2E + q + delta. If v1 - v2 > thr no other centre can win in the FP64
-// direct form, so the label is final. Otherwise, if the best value outside the
-// top two is also below v1 - thr, only the top two are re-scored exactly;
-// else the row goes through a second tensor-core pass that keeps the best four
-// scores, and only the centres inside the bound among those four are
-// re-scored (rows with more than four such centres, or a non-finite score,
-// are re-scored against every centre). Every re-score is the
-// direct-form sum (x_j - c_j)^2 in FP64 with no FMA and the lowest index on
-// ties, i.e. exactly kmeans.rs:159-163 / 295-309, so the labels equal the
-// FP64 oracle's in every case.
+// accumulation and the three-term BF16 split of a_c), the key-grid quantum q
+// and the FP64 oracle's own rounding delta give the threshold
+// thr = 2E + q + delta (evaluated in f32 with upward rounding). If
+// v1 - v2 > thr no other centre can win in the FP64 direct form, so the label
+// is final. Otherwise, if the best value outside the top two is also below
+// v1 - thr, only the top two are re-scored exactly; else the row goes through
+// a second tensor-core pass in BF16 (its own operands, made from the row's
+// f32 values, and its own bound -- 16x tighter than the FP8 one) that keeps
+// the best eight scores, and only the centres inside that pass's bound are
+// re-scored (rows with more than eight such centres, or a non-finite score,
+// are re-scored against every centre, one CTA per row). Every re-score ends
+// in the direct-form sum (x_j - c_j)^2 in FP64 with no FMA and the lowest
+// index on ties, i.e. exactly kmeans.rs:159-163 / 295-309, so the labels
+// equal the FP64 oracle's in every case.
 #include <cfloat>
 #include <cmath>
 #include <cuda_bf16.h>

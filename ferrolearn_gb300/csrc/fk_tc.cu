@@ -1,27 +1,30 @@
-// fk_tc.cu -- fused BF16 assignment on the 5th-generation tensor cores.
+// fk_tc.cu -- fused BF16 / FP8 assignment on the 5th-generation tensor cores.
 //
-// One persistent launch, one CTA per SM (10 warps, ~215 KB shared memory,
-// 512 TMEM columns). The centres are cut into `parts` slices of kp centres;
-// CTA (slice p, index q) keeps its slice resident in shared memory for the
-// whole launch and streams the row tiles q, q+Q, q+2Q, ... of X through a
-// two-stage TMA ring, so X is read once per slice and the n x k score matrix
-// never leaves the SM.
+// One persistent launch, one CTA per SM (10 warps, up to ~215 KB shared
+// memory, 512 TMEM columns). The centres are cut into `parts` slices of kp
+// centres; CTA (slice p, index q) keeps its slice resident in shared memory
+// for the whole launch and streams the row tiles q, q+Q, q+2Q, ... of X
+// through a TMA ring of one or two stages, so X is read once per slice (the
+// other slices' CTAs find it in L2) and the n x k score matrix never leaves
+// the SM.
 //
 //   warp 0   TMA producer: the resident slice once, then 128-row X tiles
-//            (cp.async.bulk.tensor, 128-byte swizzle, mbarrier complete_tx).
+//            (cp.async.bulk.tensor, 128-byte swizzle, mbarrier complete_tx);
+//            FP8 also loads each tile's per-row augmentation rows.
 //   warp 1   TMEM allocator and MMA issuer: per (tile, 256-centre block),
-//            d_pad/16 tcgen05.mma (M=128, N=256, K=16, BF16 in, FP32 out)
-//            plus one K=16 MMA that adds a_c = BIG - ||c'||^2/2 through a
-//            constant "ones" operand; tcgen05.commit signals the epilogue.
-//            Two TMEM accumulators (2 x 256 columns) alternate, so the MMAs
-//            of block b+1 overlap the epilogue of block b.
-//   warps 2-9 epilogue: tcgen05.ld (32x32b, one row per thread), then a
-//            running top-2 per row. Scores are positive by construction, so
-//            their IEEE bits order like unsigned integers; the low 8 bits
-//            are replaced by the column code (255 - column), making every
-//            key unique, and the top-2 update is three integer min/max
-//            operations. The truncation quantum (2^-15 relative) is part of
-//            the error bound the re-check uses.
+//            tcgen05.mma M=128 N=256 (kind::f16 K=16 for BF16, kind::f8f6f4
+//            K=32 for E4M3) over d_pad, plus one BF16 K=16 MMA that adds
+//            a_c = BIG - ||c'||^2/2 (ones operand for BF16, the row's scale
+//            for FP8); tcgen05.commit signals the epilogue. Two TMEM
+//            accumulators (2 x 256 columns) alternate, so the MMAs of block
+//            b+1 overlap the epilogue of block b.
+//   warps 2-9 epilogue: tcgen05.ld (32x32b, one row per thread), every score
+//            turned into a key -- rounded to a 128-ulp grid with the column
+//            code in the freed 7 bits (three FMA-pipe operations; all scores
+//            of a launch share one binade) -- and ranked: a running top-2
+//            with a bound of the rest (main pass, three-input float max) or a
+//            running top-8 (second pass). The grid quantum is part of the
+//            error bound of the re-check.
 //
 // Every wait on an mbarrier is bounded (about two seconds of SM clock); on
 // expiry the CTA records an error word, stops issuing work, drains what it
