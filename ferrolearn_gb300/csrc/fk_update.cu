@@ -11,6 +11,8 @@
 // its output offset, and a second pass scatters row indices in row order
 // (warp match + prefix popcount keeps equal labels in lane order). The
 // result: members[] lists each cluster's rows in increasing row index.
+#include <algorithm>
+
 #include "fk_internal.cuh"
 
 namespace fk {
@@ -278,7 +280,7 @@ __device__ double fixed_to_double(unsigned __int128 a, int F) {
 }
 
 constexpr int FIX_R = 64;       // member rows whose indices are staged per batch
-constexpr int FIX_SPLIT = 16;   // blocks per cluster (the sums are order-free)
+constexpr int FIX_SPLIT = 16;   // at most this many blocks per cluster (gridDim.y; the sums are order-free)
 constexpr int FIX_U = 8;        // rows loaded ahead per thread
 
 struct alignas(16) FixedPart {
@@ -333,7 +335,7 @@ __global__ void centroid_fixed_part_kernel(const float *__restrict__ x, int d, i
     const int j = blockIdx.z * blockDim.x + threadIdx.x;
     const int64_t cstart = offs[(int64_t)c * nseg];
     const int64_t cend = (c + 1 < k) ? (int64_t)offs[(int64_t)(c + 1) * nseg] : n;
-    const int64_t share = (cend - cstart + FIX_SPLIT - 1) / FIX_SPLIT;
+    const int64_t share = (cend - cstart + gridDim.y - 1) / gridDim.y;
     const int64_t start = cstart + (int64_t)y * share;
     const int64_t end = min(cend, start + share);
     const int F = fixed_bits(amax_ptr, n);
@@ -367,7 +369,7 @@ __global__ void centroid_fixed_part_kernel(const float *__restrict__ x, int d, i
     if (j < d) {
         unsigned long long lo = a.plo, hi = a.phi;
         asm("sub.cc.u64 %0, %0, %2;\n\tsubc.u64 %1, %1, %3;" : "+l"(lo), "+l"(hi) : "l"(a.nlo), "l"(a.nhi));
-        parts[((int64_t)c * FIX_SPLIT + y) * d + j] = FixedPart{lo, hi, (double)isum - (double)icomp, a.flags, 0u};
+        parts[((int64_t)c * gridDim.y + y) * d + j] = FixedPart{lo, hi, (double)isum - (double)icomp, a.flags, 0u};
     }
 }
 
@@ -404,7 +406,7 @@ __device__ __forceinline__ void add_shifted(uint64_t &lo, uint64_t &hi, long lon
     add128(lo, hi, (uint64_t)v, (uint64_t)((unsigned __int128)v >> 64));
 }
 
-__global__ void __launch_bounds__(FIX4_THREADS) centroid_fixed_part4_kernel(
+__global__ void __launch_bounds__(FIX4_THREADS, 3) centroid_fixed_part4_kernel(
     const float *__restrict__ x, int d, int k, int64_t n, const int32_t *__restrict__ members,
     const int32_t *__restrict__ offs, int64_t nseg, const double *__restrict__ old_c,
     const float *__restrict__ amax_ptr, FixedPart *__restrict__ parts) {
@@ -417,7 +419,7 @@ __global__ void __launch_bounds__(FIX4_THREADS) centroid_fixed_part4_kernel(
     const int c = blockIdx.x, y = blockIdx.y;
     const int64_t cstart = offs[(int64_t)c * nseg];
     const int64_t cend = (c + 1 < k) ? (int64_t)offs[(int64_t)(c + 1) * nseg] : n;
-    const int64_t share = (cend - cstart + FIX_SPLIT - 1) / FIX_SPLIT;
+    const int64_t share = (cend - cstart + gridDim.y - 1) / gridDim.y;
     const int64_t start = cstart + (int64_t)y * share;
     const int64_t end = min(cend, start + share);
     const int F = fixed_bits(amax_ptr, n);
@@ -430,6 +432,7 @@ __global__ void __launch_bounds__(FIX4_THREADS) centroid_fixed_part4_kernel(
     const int b1 = __float_as_int(C1), b2 = __float_as_int(C2);
     long long acc1[4], acc2[4];
     uint64_t slo[4], shi[4];
+    uint32_t tail = 0u;
     float isum[4], icomp[4], cj[4], probe[4];
 #pragma unroll
     for (int f = 0; f < 4; f++) {
@@ -461,7 +464,7 @@ __global__ void __launch_bounds__(FIX4_THREADS) centroid_fixed_part4_kernel(
                                  : make_float4(0.f, 0.f, 0.f, 0.f);
             }
             float pf[4] = {0.f, 0.f, 0.f, 0.f};
-            int q1s[4] = {0, 0, 0, 0}, q2s[4] = {0, 0, 0, 0};
+            uint32_t q1s[4] = {0u, 0u, 0u, 0u}, q2s[4] = {0u, 0u, 0u, 0u};  // wrap harmlessly without grids
 #pragma unroll
             for (int u = 0; u < FIX4_U; u++) {
                 const bool valid = r0 + u * G < cnt;
@@ -470,25 +473,21 @@ __global__ void __launch_bounds__(FIX4_THREADS) centroid_fixed_part4_kernel(
                 for (int f = 0; f < 4; f++) {
                     const float xv = e[f];  // rows past the end read as 0
                     probe[f] = __fmaf_rn(xv, 0.f, probe[f]);
-                    if (grids) {
-                        const float s1 = __fadd_rn(xv, C1);
-                        q1s[f] += __float_as_int(s1) - b1;
-                        const float r = __fsub_rn(xv, __fsub_rn(s1, C1));
-                        const float s2 = __fadd_rn(r, C2);
-                        q2s[f] += __float_as_int(s2) - b2;
-                        const float r2 = __fsub_rn(r, __fsub_rn(s2, C2));
-                        if (r2 != 0.f) fixed_add_signed(slo[f], shi[f], r2, F);
-                    } else {
-                        fixed_add_signed(slo[f], shi[f], xv, F);
-                    }
+                    const float s1 = __fadd_rn(xv, C1);
+                    q1s[f] += __float_as_uint(s1) - (uint32_t)b1;
+                    const float r = __fsub_rn(xv, __fsub_rn(s1, C1));
+                    const float s2 = __fadd_rn(r, C2);
+                    q2s[f] += __float_as_uint(s2) - (uint32_t)b2;
+                    const float r2 = __fsub_rn(r, __fsub_rn(s2, C2));
+                    tail |= __float_as_uint(r2) << 1;  // r2 != 0 (a -0 remainder adds nothing)
                     const float df = __fsub_rn(xv, cj[f]);
                     pf[f] = valid ? __fmaf_rn(df, df, pf[f]) : pf[f];
                 }
             }
 #pragma unroll
             for (int f = 0; f < 4; f++) {
-                acc1[f] += q1s[f];
-                acc2[f] += q2s[f];
+                acc1[f] += (int32_t)q1s[f];
+                acc2[f] += (int32_t)q2s[f];
                 const float yy = __fsub_rn(pf[f], icomp[f]);
                 const float tt = __fadd_rn(isum[f], yy);
                 icomp[f] = __fsub_rn(__fsub_rn(tt, isum[f]), yy);
@@ -496,6 +495,28 @@ __global__ void __launch_bounds__(FIX4_THREADS) centroid_fixed_part4_kernel(
             }
 #pragma unroll
             for (int u = 0; u < FIX4_U; u++) cur[u] = nxt[u];
+        }
+    }
+    // rare remainders (|x| < 2^(ea-21)), or every value when the grids do
+    // not apply: the exact 128-bit path, over this thread's rows again
+    if (active && (tail != 0u || !grids)) {
+        for (int64_t cb = start; cb < end; cb += FIX4_IDX) {
+            const int cnt = (int)min((int64_t)FIX4_IDX, end - cb);
+            for (int r = g; r < cnt; r += G) {
+                const float4 v = reinterpret_cast<const float4 *>(x + (int64_t)members[cb + r] * d)[sl];
+                const float e[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+                for (int f = 0; f < 4; f++) {
+                    float rem = e[f];
+                    if (grids) {
+                        const float s1 = __fadd_rn(e[f], C1);
+                        const float rr = __fsub_rn(e[f], __fsub_rn(s1, C1));
+                        const float s2 = __fadd_rn(rr, C2);
+                        rem = __fsub_rn(rr, __fsub_rn(s2, C2));
+                    }
+                    if (rem != 0.f) fixed_add_signed(slo[f], shi[f], rem, F);
+                }
+            }
         }
     }
     FixRed mine;
@@ -535,7 +556,7 @@ __global__ void __launch_bounds__(FIX4_THREADS) centroid_fixed_part4_kernel(
         }
 #pragma unroll
         for (int f = 0; f < 4; f++)
-            parts[((int64_t)c * FIX_SPLIT + y) * d + 4 * sl + f] =
+            parts[((int64_t)c * gridDim.y + y) * d + 4 * sl + f] =
                 FixedPart{t.lo[f], t.hi[f], t.inert[f], t.flags[f], 0u};
     }
 }
@@ -543,7 +564,8 @@ __global__ void __launch_bounds__(FIX4_THREADS) centroid_fixed_part4_kernel(
 // Per (cluster, feature): exact sum of the parts, rounded once to f64, then
 // divided by the count (empty cluster: keep the old centre); the inertia
 // partials folded in a fixed order.
-__global__ void centroid_fixed_combine_kernel(int d, int k, int64_t n, const int32_t *__restrict__ offs, int64_t nseg,
+__global__ void centroid_fixed_combine_kernel(int d, int k, int splits, int64_t n, const int32_t *__restrict__ offs,
+                                              int64_t nseg,
                                               const double *__restrict__ old_c, double *__restrict__ new_c,
                                               const float *__restrict__ amax_ptr, const FixedPart *__restrict__ parts,
                                               double *__restrict__ inertia_part) {
@@ -556,8 +578,8 @@ __global__ void centroid_fixed_combine_kernel(int d, int k, int64_t n, const int
     unsigned long long lo = 0, hi = 0;
     uint32_t fl = 0;
     double inert = 0.0;
-    for (int y = 0; y < FIX_SPLIT; y++) {
-        const FixedPart q = parts[((int64_t)c * FIX_SPLIT + y) * d + j];
+    for (int y = 0; y < splits; y++) {
+        const FixedPart q = parts[((int64_t)c * splits + y) * d + j];
         asm("add.cc.u64 %0, %0, %2;\n\taddc.u64 %1, %1, %3;" : "+l"(lo), "+l"(hi) : "l"(q.lo), "l"(q.hi));
         fl |= q.flags;
         inert += q.inert;
@@ -679,20 +701,22 @@ void launch_update_centroids_exact(const SortPlan &p, const float *x, int d, con
     FixedPart *parts = (FixedPart *)scratch;
     FK_CUDA(cudaMemsetAsync(&scalars->shift_bits, 0, sizeof(unsigned long long), s));
     if (d == 0 || p.k == 0) return;
+    // blocks per cluster: about 1024 rows each, at most FIX_SPLIT
+    const int splits = (int)std::max<int64_t>(1, std::min<int64_t>(FIX_SPLIT, (p.n / p.k + 1023) / 1024));
     if (d % 4 == 0 && d / 4 <= FIX4_THREADS && ((uintptr_t)x & 15u) == 0) {
-        dim3 grid((unsigned)p.k, FIX_SPLIT);
+        dim3 grid((unsigned)p.k, (unsigned)splits);
         centroid_fixed_part4_kernel<<<grid, FIX4_THREADS, 0, s>>>(x, d, p.k, p.n, members, seg_hist, p.nseg, old_c,
                                                                   amax, parts);
     } else {
         int threads = d >= 256 ? 256 : (d + 31) / 32 * 32;
-        dim3 grid((unsigned)p.k, FIX_SPLIT, (unsigned)((d + threads - 1) / threads));
+        dim3 grid((unsigned)p.k, (unsigned)splits, (unsigned)((d + threads - 1) / threads));
         centroid_fixed_part_kernel<<<grid, threads, 0, s>>>(x, d, p.k, p.n, members, seg_hist, p.nseg, old_c, amax,
                                                             parts);
     }
     FK_LAUNCH_CHECK();
     const int64_t kd = (int64_t)p.k * d;
-    centroid_fixed_combine_kernel<<<(unsigned)((kd + 255) / 256), 256, 0, s>>>(d, p.k, p.n, seg_hist, p.nseg, old_c,
-                                                                               new_c, amax, parts, inertia_part);
+    centroid_fixed_combine_kernel<<<(unsigned)((kd + 255) / 256), 256, 0, s>>>(d, p.k, splits, p.n, seg_hist, p.nseg,
+                                                                               old_c, new_c, amax, parts, inertia_part);
     FK_LAUNCH_CHECK();
     max_shift_kernel<double><<<(p.k + 127) / 128, 128, 0, s>>>(new_c, old_c, p.k, d, &scalars->shift_bits);
     FK_LAUNCH_CHECK();
