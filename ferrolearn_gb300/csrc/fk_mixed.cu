@@ -330,6 +330,8 @@ __global__ void prep_aug_kernel(const double *__restrict__ half_norm, int k, int
         rmin_exp = -(min(sh_t + FP8_ROW_ABOVE, 120) + sh_t);
     }
     if (e + 9 + rmax_exp > 126 || e - 23 + rmin_exp < -126) big = INFINITY;
+    // BIG, cgrid and ulp are kept in score units as f32: they must be normal
+    if (e + 9 > 126 || e - 23 < -126) big = INFINITY;
     if (q == 0) {
         stats->big = (float)big;
         stats->cgrid = (float)(3.0 * ldexp(1.0, e + 6));

@@ -308,3 +308,23 @@ def test_fp8_bisector_fit_and_predict_match_fp64_oracle():
     assert g.report["rows_rechecked"] >= int(0.1 * x32.shape[0])  # every bisector row at least
     xp = w["x_predict"]
     assert np.array_equal(g.predict(xp), O.predict(g.cluster_centers(), xp.astype(np.float64)))
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+@pytest.mark.parametrize("scale", [1e-35, 1e-20, 1e15, 1e18])
+def test_mixed_extreme_scales_fall_back_exactly(precision, scale):
+    # scores that leave the f32 range of the keys (or underflow) must send the
+    # rows to the exact re-score, never to a wrong label
+    rng = np.random.default_rng(12)
+    d, k = 16, 9
+    cen = rng.uniform(-10, 10, size=(k, d))
+    x = (cen[rng.integers(0, k, 3000)] + rng.normal(0, 1, size=(3000, d))) * scale
+    x32 = x.astype(np.float32)
+    x64 = x32.astype(np.float64)
+    c = x64[rng.choice(3000, size=k, replace=False)].copy()
+    for _ in range(2):
+        gl, gc, gi, gs, rep = F.lloyd_step(x32, c, dtype="f32x64", precision=precision)
+        ol, oc, oi, os_ = O.lloyd_step(x64, c)
+        assert np.array_equal(gl, ol)
+        assert _close(gc, oc)
+        c = oc
