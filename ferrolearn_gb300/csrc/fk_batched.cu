@@ -68,6 +68,8 @@ struct BItem {
 };
 
 constexpr int KPP_T = 256;
+constexpr int KPP_TILE = 8192;  // floats of shared memory for a tile of rows (padded stride d + 1)
+static_assert(KPP_TILE % 256 == 0, "tile prefetch assumes 256 threads");
 constexpr int ASSIGN_T = 128;
 constexpr int UPDATE_T = 256;
 constexpr int NBUCKETS = 20;  // d in {8, 16, 32, 64, other} x k in {<=16, <=32, <=64, >64}
@@ -112,53 +114,116 @@ __device__ int first_reaching(const float *__restrict__ cum, int n, float thr) {
     return lo < n ? lo : n - 1;
 }
 
-// Sequential f32 fold of v[0..n) by one warp, the values broadcast by
-// shuffles (the fold itself stays in order); cum (nullable) receives every
-// running value. Loads run one batch of 256 values ahead of the fold.
-constexpr int FOLD_B = 8;  // 32-value chunks per batch
+// Sequential f32 fold of v[0..n) by one warp (the reference's in-order
+// sum): the warp stages 256 values at a time in its shared-memory slice
+// (coalesced loads, one batch ahead), then every lane runs the same chain
+// over broadcast reads; with cum, lane 0 also records each running value in
+// the slice and the warp writes them out coalesced.
+constexpr int FOLD_N = 256;
 
-__device__ __forceinline__ void fold_chunk32(float &run, float v, float &mine) {
-    const unsigned full = 0xffffffffu;
-    const int lane = threadIdx.x & 31;
-#pragma unroll
-    for (int l = 0; l < 32; l++) {
-        run = __fadd_rn(run, __shfl_sync(full, v, l));
-        if (lane == l) mine = run;
-    }
-}
-
-__device__ float warp_serial_fold(const float *__restrict__ v, int n, float *__restrict__ cum) {
-    const unsigned full = 0xffffffffu;
+__device__ float warp_serial_fold(const float *__restrict__ v, int n, float *__restrict__ cum,
+                                  float *__restrict__ stage, float *__restrict__ cbuf) {
     const int lane = threadIdx.x & 31;
     float run = 0.f;
-    float cur[FOLD_B], nxt[FOLD_B];
+    float cur[FOLD_N / 32], nxt[FOLD_N / 32];
 #pragma unroll
-    for (int b = 0; b < FOLD_B; b++) cur[b] = b * 32 + lane < n ? v[b * 32 + lane] : 0.f;
-    for (int base = 0; base < n; base += 32 * FOLD_B) {
+    for (int b = 0; b < FOLD_N / 32; b++) cur[b] = b * 32 + lane < n ? v[b * 32 + lane] : 0.f;
+    for (int base = 0; base < n; base += FOLD_N) {
 #pragma unroll
-        for (int b = 0; b < FOLD_B; b++) {
-            const int i = base + 32 * FOLD_B + b * 32 + lane;
+        for (int b = 0; b < FOLD_N / 32; b++) {
+            const int i = base + FOLD_N + b * 32 + lane;
             nxt[b] = i < n ? v[i] : 0.f;
         }
+        __syncwarp();
 #pragma unroll
-        for (int b = 0; b < FOLD_B; b++) {
-            const int cb = base + b * 32;
-            if (cb >= n) break;
-            float mine = 0.f;
-            if (cb + 32 <= n) {
-                fold_chunk32(run, cur[b], mine);
-            } else {
-                for (int l = 0; l < n - cb; l++) {
-                    run = __fadd_rn(run, __shfl_sync(full, cur[b], l));
-                    if (lane == l) mine = run;
-                }
+        for (int b = 0; b < FOLD_N / 32; b++) stage[b * 32 + lane] = cur[b];
+        __syncwarp();
+        const int m = min(FOLD_N, n - base);
+        if (m == FOLD_N) {
+#pragma unroll 16
+            for (int q = 0; q < FOLD_N / 4; q++) {
+                const float4 f = reinterpret_cast<const float4 *>(stage)[q];
+                run = __fadd_rn(run, f.x);
+                if (cum && lane == 0) cbuf[4 * q] = run;
+                run = __fadd_rn(run, f.y);
+                if (cum && lane == 0) cbuf[4 * q + 1] = run;
+                run = __fadd_rn(run, f.z);
+                if (cum && lane == 0) cbuf[4 * q + 2] = run;
+                run = __fadd_rn(run, f.w);
+                if (cum && lane == 0) cbuf[4 * q + 3] = run;
             }
-            if (cum && cb + lane < n) cum[cb + lane] = mine;
+        } else {
+            for (int e = 0; e < m; e++) {
+                run = __fadd_rn(run, stage[e]);
+                if (cum && lane == 0) cbuf[e] = run;
+            }
+        }
+        if (cum) {
+            __syncwarp();
+#pragma unroll
+            for (int b = 0; b < FOLD_N / 32; b++)
+                if (b * 32 + lane < m) cum[base + b * 32 + lane] = cbuf[b * 32 + lane];
         }
 #pragma unroll
-        for (int b = 0; b < FOLD_B; b++) cur[b] = nxt[b];
+        for (int b = 0; b < FOLD_N / 32; b++) cur[b] = nxt[b];
     }
     return run;
+}
+
+// Distances (direct form) of every row to ntr candidate rows (crow, ntr x d,
+// shared memory) over tiles of rows staged in shared memory (coalesced loads,
+// padded stride d + 1: conflict-free reads; the next tile is loaded into
+// registers while the current one is scored); the (row, candidate) pairs of
+// a tile are spread evenly over the threads. mode 0: mind[i] = d(x_i,
+// crow[0]); mode 1: nd[t n + i] = min(d(x_i, crow[t]), mind[i]).
+constexpr int KPP_PF = KPP_TILE / 256;  // prefetched floats per thread
+
+__device__ void tile_distances(const float *__restrict__ x, int n, int d, const float *__restrict__ crow, int ntr,
+                               int mode, float *__restrict__ mind, float *__restrict__ nd, float *__restrict__ tile) {
+    const int tid = threadIdx.x;
+    const int TR = KPP_TILE / (d + 1) < 256 ? KPP_TILE / (d + 1) : 256;  // rows per tile
+    float pf[KPP_PF];
+    auto fetch = [&](int i0) {
+        const int cnt = min(TR, n - i0) * d;
+#pragma unroll
+        for (int u = 0; u < KPP_PF; u++) {
+            const int e = tid + u * KPP_T;
+            pf[u] = e < cnt ? x[(int64_t)i0 * d + e] : 0.f;
+        }
+    };
+    if (n > 0) fetch(0);
+    for (int i0 = 0; i0 < n; i0 += TR) {
+        const int rows = min(TR, n - i0);
+        __syncthreads();
+#pragma unroll
+        for (int u = 0; u < KPP_PF; u++) {
+            const int e = tid + u * KPP_T;
+            if (e < rows * d) {
+                const int rr = e / d, j = e - rr * d;
+                tile[rr * (d + 1) + j] = pf[u];
+            }
+        }
+        __syncthreads();
+        if (i0 + TR < n) fetch(i0 + TR);
+        for (int pr = tid; pr < rows * ntr; pr += KPP_T) {
+            const int r = pr % rows, t = pr / rows;
+            const float *xr = tile + r * (d + 1);
+            const float *cr = crow + t * d;
+            float acc = 0.f;
+            for (int j = 0; j < d; j++) {
+                const float df = __fsub_rn(xr[j], cr[j]);
+                acc = __fadd_rn(acc, __fmul_rn(df, df));
+            }
+            const int i = i0 + r;
+            if (mode == 0) {
+                mind[i] = acc;
+            } else {
+                const float mv = mind[i];
+                nd[(int64_t)t * n + i] = acc < mv ? acc : mv;
+            }
+        }
+    }
+    __syncthreads();
 }
 
 // One CTA per fit. Per new centre: the running sum of D^2 (warp 0), the
@@ -176,7 +241,10 @@ __global__ void __launch_bounds__(KPP_T) batch_kpp_kernel(const float *__restric
     __shared__ int cand_sh[16];
     __shared__ float pot_sh[16], thr_sh[16];
     __shared__ float crow[8 * MAX_D];
+    __shared__ float tile[KPP_TILE];
+    __shared__ __align__(16) float fold_sm[KPP_T / 32][2 * FOLD_N];
     const int tid = threadIdx.x, warp = tid >> 5;
+    float *stage = fold_sm[warp], *cbuf = fold_sm[warp] + FOLD_N;
     float *nd = nd_all + (int64_t)blockIdx.x * nd_stride;
     uint64_t rng = 0;  // thread 0 only
     while (true) {
@@ -196,13 +264,16 @@ __global__ void __launch_bounds__(KPP_T) batch_kpp_kernel(const float *__restric
             idx_sh = dev_range(dev_uniform(rng), n);
         }
         __syncthreads();
-        for (int j = tid; j < d; j += KPP_T) cen[j] = x[(int64_t)idx_sh * d + j];
-        if (k > 1)
-            for (int i = tid; i < n; i += KPP_T) mind[i] = sqeuc_f32(x + (int64_t)i * d, x + (int64_t)idx_sh * d, d);
+        for (int j = tid; j < d; j += KPP_T) {
+            const float v = x[(int64_t)idx_sh * d + j];
+            cen[j] = v;
+            crow[j] = v;
+        }
         __syncthreads();
+        if (k > 1) tile_distances(x, n, d, crow, 1, 0, mind, nullptr, tile);
         for (int c = 1; c < k; c++) {
             if (warp == 0) {
-                const float total = warp_serial_fold(mind, n, cum);  // the reference's sequential f32 sum
+                const float total = warp_serial_fold(mind, n, cum, stage, cbuf);  // the reference's sequential f32 sum
                 if ((tid & 31) == 0) total_sh = total;
             }
             __syncthreads();
@@ -224,29 +295,9 @@ __global__ void __launch_bounds__(KPP_T) batch_kpp_kernel(const float *__restric
                 crow[t * d + j] = x[(int64_t)cand_sh[t] * d + j];
             }
             __syncthreads();
-            for (int i = tid; i < n; i += KPP_T) {
-                const float *xr = x + (int64_t)i * d;
-                float acc[8];
-#pragma unroll
-                for (int t = 0; t < 8; t++) acc[t] = 0.f;
-                for (int j = 0; j < d; j++) {
-                    const float xv = xr[j];
-#pragma unroll
-                    for (int t = 0; t < 8; t++) {
-                        if (t < trials) {
-                            const float df = __fsub_rn(xv, crow[t * d + j]);
-                            acc[t] = __fadd_rn(acc[t], __fmul_rn(df, df));
-                        }
-                    }
-                }
-                const float mv = mind[i];
-#pragma unroll
-                for (int t = 0; t < 8; t++)
-                    if (t < trials) nd[(int64_t)t * n + i] = acc[t] < mv ? acc[t] : mv;
-            }
-            __syncthreads();
+            tile_distances(x, n, d, crow, trials, 1, mind, nd, tile);
             for (int t = warp; t < trials; t += KPP_T / 32) {
-                const float pot = warp_serial_fold(nd + (int64_t)t * n, n, nullptr);
+                const float pot = warp_serial_fold(nd + (int64_t)t * n, n, nullptr, stage, cbuf);
                 if ((tid & 31) == 0) pot_sh[t] = pot;
             }
             __syncthreads();
@@ -900,7 +951,7 @@ fk_status batched_fit_impl(Ctx &ctx, fk_batch_problem *P, int64_t np, int reduct
 
     // ---- k-means++ (one persistent launch)
     if (!kpp_order.empty()) {
-        const int grid = std::min((int)kpp_order.size(), ctx.num_sms * 8);
+        const int grid = std::min((int)kpp_order.size(), ctx.num_sms * 2);
         int64_t nmax_kpp = 1;
         for (int f : kpp_order) nmax_kpp = std::max<int64_t>(nmax_kpp, fits[f].n);
         const int64_t nd_stride = 8 * nmax_kpp;  // trials <= 8 (k <= 1024)
