@@ -260,8 +260,17 @@ template <int CH, int E>
 __device__ __forceinline__ void rank_pair(const uint32_t (&r)[32], float cgrid, float ulp, float &a1, float &a2) {
     // top-2 of {a1 >= a2, k0, k1}: a1' = max(a1, max(k0,k1)),
     // a2' = max(min(a1, max(k0,k1)), a2, min(k0,k1))
-    const float k0 = make_key<127 - ((CH * 32 + E) & 127)>(r[E], cgrid, ulp);
-    const float k1 = make_key<127 - ((CH * 32 + E + 1) & 127)>(r[E + 1], cgrid, ulp);
+    // the grid rounding of both scores as two packed f32x2 operations
+    // (each half is an IEEE round-to-nearest f32 operation), then the codes
+    uint64_t p, cg2;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(p) : "r"(r[E]), "r"(r[E + 1]));
+    asm("mov.b64 %0, {%1, %1};" : "=l"(cg2) : "f"(cgrid));
+    asm("add.rn.f32x2 %0, %0, %1;" : "+l"(p) : "l"(cg2));
+    asm("sub.rn.f32x2 %0, %0, %1;" : "+l"(p) : "l"(cg2));
+    float t0, t1;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(t0), "=f"(t1) : "l"(p));
+    const float k0 = __fmaf_rn(ulp, (float)(127 - ((CH * 32 + E) & 127)), t0);
+    const float k1 = __fmaf_rn(ulp, (float)(127 - ((CH * 32 + E + 1) & 127)), t1);
     const float m = fmaxf(k0, k1), l = fminf(k0, k1);
     a2 = fmax3(fminf(a1, m), a2, l);
     a1 = fmaxf(a1, m);
