@@ -393,6 +393,7 @@ __global__ void centroid_fixed_part_kernel(const float *__restrict__ x, int d, i
 constexpr int FIX4_THREADS = 256;
 constexpr int FIX4_U = 4;      // rows per thread and step
 constexpr int FIX4_IDX = 1024; // member indices staged per chunk
+constexpr int TAIL_CAP = 512;  // remainders listed per block before falling back to a rescan
 
 struct FixRed {
     uint64_t lo[4], hi[4];
@@ -412,6 +413,9 @@ __global__ void __launch_bounds__(FIX4_THREADS, 3) centroid_fixed_part4_kernel(
     const float *__restrict__ amax_ptr, FixedPart *__restrict__ parts) {
     __shared__ FixRed red[FIX4_THREADS];
     __shared__ int32_t sidx[FIX4_IDX];
+    __shared__ float tail_v[TAIL_CAP];
+    __shared__ int tail_f[TAIL_CAP];
+    __shared__ int tail_n;
     const int S = d >> 2;
     const int G = FIX4_THREADS / S;
     const int g = (int)threadIdx.x / S, sl = (int)threadIdx.x % S;
@@ -432,7 +436,7 @@ __global__ void __launch_bounds__(FIX4_THREADS, 3) centroid_fixed_part4_kernel(
     const int b1 = __float_as_int(C1), b2 = __float_as_int(C2);
     long long acc1[4], acc2[4];
     uint64_t slo[4], shi[4];
-    uint32_t tail = 0u;
+    if (threadIdx.x == 0) tail_n = 0;
     float isum[4], icomp[4], cj[4], probe[4];
 #pragma unroll
     for (int f = 0; f < 4; f++) {
@@ -479,7 +483,13 @@ __global__ void __launch_bounds__(FIX4_THREADS, 3) centroid_fixed_part4_kernel(
                     const float s2 = __fadd_rn(r, C2);
                     q2s[f] += __float_as_uint(s2) - (uint32_t)b2;
                     const float r2 = __fsub_rn(r, __fsub_rn(s2, C2));
-                    tail |= __float_as_uint(r2) << 1;  // r2 != 0 (a -0 remainder adds nothing)
+                    if (r2 != 0.f) {  // rare: |x| < 2^(ea-21); kept for the exact path below
+                        const int slot = atomicAdd(&tail_n, 1);
+                        if (slot < TAIL_CAP) {
+                            tail_v[slot] = r2;
+                            tail_f[slot] = 4 * sl + f;
+                        }
+                    }
                     const float df = __fsub_rn(xv, cj[f]);
                     pf[f] = valid ? __fmaf_rn(df, df, pf[f]) : pf[f];
                 }
@@ -497,9 +507,21 @@ __global__ void __launch_bounds__(FIX4_THREADS, 3) centroid_fixed_part4_kernel(
             for (int u = 0; u < FIX4_U; u++) cur[u] = nxt[u];
         }
     }
-    // rare remainders (|x| < 2^(ea-21)), or every value when the grids do
-    // not apply: the exact 128-bit path, over this thread's rows again
-    if (active && (tail != 0u || !grids)) {
+    // rare remainders (|x| < 2^(ea-21)) go through the exact 128-bit path:
+    // from the block's list, or -- when the list overflowed or the grids do
+    // not apply -- by scoring this thread's rows again
+    __syncthreads();
+    const int tn = tail_n;
+    if (g == 0 && active && tn <= TAIL_CAP) {
+        for (int e = 0; e < tn; e++) {
+            const int fe = tail_f[e];
+            if ((fe >> 2) != sl) continue;
+#pragma unroll
+            for (int f = 0; f < 4; f++)
+                if ((fe & 3) == f) fixed_add_signed(slo[f], shi[f], tail_v[e], F);
+        }
+    }
+    if (active && (tn > TAIL_CAP || !grids)) {
         for (int64_t cb = start; cb < end; cb += FIX4_IDX) {
             const int cnt = (int)min((int64_t)FIX4_IDX, end - cb);
             for (int r = g; r < cnt; r += G) {
