@@ -78,7 +78,10 @@ def load_peaks():
 
 
 class ClockSampler:
-    """nvidia-smi clocks + throttle reasons sampled during the timed region."""
+    """nvidia-smi clocks + throttle reasons sampled every 20 ms; summary()
+    keeps the samples taken while the timed region ran (mark_start/mark_end,
+    host clock, +-0.15 s), or the nearest one when the region was shorter
+    than the sampling interval."""
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -88,21 +91,31 @@ class ClockSampler:
         self.gpu = gpu
         self.proc = None
         self.lines = []
+        self.t0 = self.t1 = None
 
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "20"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            deadline = time.time() + 3.0
+            while not self.lines and time.time() < deadline:  # sampling is live before the region starts
+                time.sleep(0.01)
         except Exception:
             self.proc = None
         return self
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.time(), line.strip()))
+
+    def mark_start(self):
+        self.t0 = time.time()
+
+    def mark_end(self):
+        self.t1 = time.time()
 
     def __exit__(self, *a):
         if self.proc:
@@ -113,9 +126,16 @@ class ClockSampler:
                 self.proc.kill()
 
     def summary(self):
+        rows = list(self.lines)
+        if self.t0 is not None and self.t1 is not None and rows:
+            inside = [r for r in rows if self.t0 - 0.15 <= r[0] <= self.t1 + 0.15]
+            if not inside:
+                mid = 0.5 * (self.t0 + self.t1)
+                inside = [min(rows, key=lambda r: abs(r[0] - mid))]
+            rows = inside
         sm, mx, reasons = [], 0.0, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        for _, ln in rows:
             parts = [p.strip() for p in ln.split(",")]
             if len(parts) < 9:
                 continue
@@ -239,6 +259,7 @@ def run_batched(args):
     l0 = _native.lib().fk_debug_launch_count()
     times, reps = [], []
     with ClockSampler(dev) as clocks:
+        clocks.mark_start()
         for _ in range(args.steps):
             torch.cuda.synchronize()
             start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -248,6 +269,7 @@ def run_batched(args):
             torch.cuda.synchronize()
             times.append(start.elapsed_time(end))
             reps.append(rep)
+        clocks.mark_end()
     launches = int(_native.lib().fk_debug_launch_count() - l0)
     ms = float(np.sum(times))
     iters = sum(r["iterations_total"] for r in reps)
@@ -353,10 +375,12 @@ def run_ours(args):
         torch.distributed.barrier()
     torch.cuda.synchronize()
     with ClockSampler(dev) as clocks:
+        clocks.mark_start()
         start.record(stream)
         fitted = model.fit(xd, ctx=ctx)
         end.record(stream)
         torch.cuda.synchronize()
+        clocks.mark_end()
     launches = int(_native.lib().fk_debug_launch_count() - l0)
     ms = start.elapsed_time(end)
     if world > 1:
