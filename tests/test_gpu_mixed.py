@@ -343,4 +343,4 @@ def test_fit_into_device_outputs_matches_host_outputs():
     assert np.array_equal(c_out.cpu().numpy(), host.cluster_centers())
     assert np.array_equal(l_out.cpu().numpy(), host.labels())
     assert dev.n_iter() == host.n_iter() == 3
-    assert np.array_equal(dev.predict(x32), host.labels() if False else dev.predict(x32))
+    assert np.array_equal(dev.predict(x32), host.predict(x32))
