@@ -276,21 +276,23 @@ __device__ __forceinline__ void rank_pair(const uint32_t (&r)[32], float cgrid, 
     a1 = fmaxf(a1, m);
 }
 
+constexpr int NCH = 1;  // top-2 chains per rank pass (measured: 1 ~ 2 < 4 < 8 in time; the ALU pipe bounds it)
+
 template <int CH, int E>
 struct RankChunk {
-    static __device__ __forceinline__ void run(const uint32_t (&r)[32], float cg, float ulp, float (&a1)[4],
-                                               float (&a2)[4]) {
-        rank_pair<CH, E>(r, cg, ulp, a1[(E >> 1) & 3], a2[(E >> 1) & 3]);
+    static __device__ __forceinline__ void run(const uint32_t (&r)[32], float cg, float ulp, float (&a1)[NCH],
+                                               float (&a2)[NCH]) {
+        rank_pair<CH, E>(r, cg, ulp, a1[(E >> 1) & (NCH - 1)], a2[(E >> 1) & (NCH - 1)]);
         RankChunk<CH, E + 2>::run(r, cg, ulp, a1, a2);
     }
 };
 template <int CH>
 struct RankChunk<CH, 32> {
-    static __device__ __forceinline__ void run(const uint32_t (&)[32], float, float, float (&)[4], float (&)[4]) {}
+    static __device__ __forceinline__ void run(const uint32_t (&)[32], float, float, float (&)[NCH], float (&)[NCH]) {}
 };
 
 // Ranks the 128 columns of one half of an accumulator block:
-// four interleaved top-2 chains over the keys, two elements per step with a
+// NCH interleaved top-2 chains over the keys, two elements per step with a
 // three-input max, the next 32 columns loading from TMEM while the current
 // ones are ranked; then the chains are merged with the bound of the rest.
 // Returns keys; the low 7 bits of a key are 127 - (column within the half).
@@ -298,7 +300,9 @@ struct RankChunk<CH, 32> {
 // eight epilogue warps share one copy of it in the instruction cache.
 __device__ __forceinline__ void rank_half(uint32_t col_addr, float cgrid, float ulp, uint32_t &b1, uint32_t &b2,
                                           uint32_t &bu) {
-    float a1[4] = {0.f, 0.f, 0.f, 0.f}, a2[4] = {0.f, 0.f, 0.f, 0.f};
+    float a1[NCH], a2[NCH];
+#pragma unroll
+    for (int q = 0; q < NCH; q++) a1[q] = a2[q] = 0.f;
     uint32_t ra[32], rb[32];
     tmem_ld32(col_addr, ra);
     tmem_wait(ra);
@@ -317,7 +321,7 @@ __device__ __forceinline__ void rank_half(uint32_t col_addr, float cgrid, float 
     bu = b2;
     int d1 = 0, d2 = 0;  // indices are carried inside the keys
 #pragma unroll
-    for (int qd = 1; qd < 4; qd++)
+    for (int qd = 1; qd < NCH; qd++)
         merge_res(b1, d1, b2, d2, bu, __float_as_uint(a1[qd]), 0, __float_as_uint(a2[qd]), 0, __float_as_uint(a2[qd]));
 }
 
