@@ -358,14 +358,18 @@ __device__ __forceinline__ uint32_t inski(uint32_t (&R)[K], int (&I)[K], uint32_
 template <int K, int CH>
 __device__ __forceinline__ void rank_chunkk(const uint32_t (&r)[32], float cgrid, float ulp, float (&c0)[K],
                                             float (&c1)[K]) {
+    uint64_t cg2;
+    asm("mov.b64 %0, {%1, %1};" : "=l"(cg2) : "f"(cgrid));
 #pragma unroll
-    for (int e = 0; e < 32; e++) {
-        const float t = __fsub_rn(__fadd_rn(__uint_as_float(r[e]), cgrid), cgrid);
-        const float key = __fmaf_rn(ulp, (float)(127 - ((CH * 32 + e) & 127)), t);
-        if (e & 1)
-            insk<K>(c1, key);
-        else
-            insk<K>(c0, key);
+    for (int e = 0; e < 32; e += 2) {
+        uint64_t p;  // grid rounding of two scores as packed f32x2 operations
+        asm("mov.b64 %0, {%1, %2};" : "=l"(p) : "r"(r[e]), "r"(r[e + 1]));
+        asm("add.rn.f32x2 %0, %0, %1;" : "+l"(p) : "l"(cg2));
+        asm("sub.rn.f32x2 %0, %0, %1;" : "+l"(p) : "l"(cg2));
+        float t0, t1;
+        asm("mov.b64 {%0, %1}, %2;" : "=f"(t0), "=f"(t1) : "l"(p));
+        insk<K>(c0, __fmaf_rn(ulp, (float)(127 - ((CH * 32 + e) & 127)), t0));
+        insk<K>(c1, __fmaf_rn(ulp, (float)(127 - ((CH * 32 + e + 1) & 127)), t1));
     }
 }
 
