@@ -1,0 +1,59 @@
+"""The sklearn-style wrapper (ferrolearn_gb300.sklearn.KMeans), the drop-in for
+ferrolearn-python's KMeans (_clusterers.py:15-84): constructor keywords and
+defaults, parameter handling, validation on the CPU; fit / predict /
+transform / pickling against the library's own API on the GPU."""
+import pickle
+
+import numpy as np
+import pytest
+
+import ferrolearn_gb300 as F
+from ferrolearn_gb300.sklearn import KMeans
+from oracle import oracle as O
+
+
+def test_defaults_match_the_reference_wrapper():
+    km = KMeans()
+    assert (km.n_clusters, km.max_iter, km.tol, km.n_init, km.random_state) == (8, 300, 1e-4, 10, None)
+
+
+def test_sklearn_parameter_protocol():
+    pytest.importorskip("sklearn")
+    from sklearn.base import clone
+    km = KMeans(n_clusters=3, random_state=7, precision="bf16")
+    p = km.get_params()
+    assert p["n_clusters"] == 3 and p["random_state"] == 7 and p["precision"] == "bf16"
+    c = clone(km).set_params(n_init=2)
+    assert c.n_init == 2 and c.n_clusters == 3
+
+
+def test_validation_errors_before_any_device_work():
+    x = np.ones((5, 2))
+    with pytest.raises(F.InvalidParameter):
+        KMeans(n_clusters=0).fit(x)
+    with pytest.raises(F.InsufficientSamples):
+        KMeans(n_clusters=9).fit(x)
+    with pytest.raises(ValueError):
+        KMeans().fit(np.ones(5))
+    with pytest.raises(AttributeError):
+        KMeans().predict(x)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["plain", "bf16"])
+def test_wrapper_fit_predict_transform_on_gpu(precision):
+    rng = np.random.default_rng(4)
+    cen = rng.uniform(-10, 10, size=(5, 6))
+    x = cen[rng.integers(0, 5, 1500)] + rng.normal(0, 1, size=(1500, 6))
+    if precision != "plain":
+        x = x.astype(np.float32).astype(np.float64)
+    km = KMeans(n_clusters=5, n_init=3, random_state=11, precision=precision).fit(x)
+    ref = F.KMeans(5, dtype="f64").with_n_init(3).with_random_state(11).fit(x)
+    assert np.array_equal(km.labels_, ref.labels())
+    assert np.allclose(km.cluster_centers_, ref.cluster_centers(), rtol=1e-12, atol=0)
+    assert km.n_iter_ == ref.n_iter()
+    assert np.array_equal(km.predict(x), O.predict(km.cluster_centers_, x))
+    assert np.allclose(km.transform(x[:20]), O.transform(km.cluster_centers_, x[:20]), rtol=1e-12, atol=1e-12)
+    assert np.array_equal(km.fit_predict(x), km.labels_)
+    km2 = pickle.loads(pickle.dumps(km))
+    assert np.array_equal(km2.predict(x), km.predict(x))
