@@ -37,6 +37,7 @@ same workload with all host threads, and reports iterations/s extrapolated
 to the full n.
 """
 import argparse
+import faulthandler
 import json
 import os
 import subprocess
@@ -469,12 +470,16 @@ def run_ours(args):
     if not args.no_cpu and rank == 0 and world == 1:
         out["cpu_baseline"] = cpu_baseline(w, args.cpu_seconds, os.cpu_count() or 1)
     if rank == 0:
-        print(json.dumps(out))
+        print(json.dumps(out), flush=True)
+    # release the library's buffers while the stream and the CUDA context are alive
+    torch.cuda.synchronize()
+    ctx.close()
     if world > 1:
         torch.distributed.destroy_process_group()
 
 
 def main():
+    faulthandler.enable()  # a native crash prints the Python stack
     args = parse()
     if args.impl == "reference":
         run_reference(args)

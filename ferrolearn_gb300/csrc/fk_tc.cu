@@ -47,9 +47,11 @@ constexpr int NTHREADS = 320;     // 10 warps
 constexpr uint32_t TMEM_COLS = 512;
 constexpr uint32_t X_ATOM_BYTES = BM * 128;  // 128 rows x 64 BF16
 constexpr uint32_t ONES_BYTES = BM * 32;     // 128 rows x 16 BF16
-// Shared-memory exchange between the two epilogue halves of a row.
+// Shared-memory exchange between the two epilogue halves of a row: three
+// rotating slots for the top-2 records (see the tile merge in the kernel),
+// one for the top-8 records.
 __host__ __device__ constexpr uint32_t merge_bytes(int topk) {
-    return BM * (uint32_t)(topk == 2 ? sizeof(Top2) : sizeof(Top8));
+    return BM * (uint32_t)(topk == 2 ? 3 * sizeof(Top2) : sizeof(Top8));
 }
 constexpr uint32_t BAR_BYTES = 256;
 constexpr long long WAIT_LIMIT_CYCLES = 4000000000LL;
@@ -112,9 +114,10 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
 }
 
 // Bounded wait: false if the CTA is aborting or this wait ran out of time.
-__device__ __noinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile uint32_t *abort_flag,
-                                       unsigned long long *err, unsigned long long code) {
-    if (mbar_try_wait(bar, parity)) return true;
+// The first test is inlined at every call site; only a wait that does not
+// succeed at once pays for the call (the epilogue waits once per block).
+__device__ __noinline__ bool mbar_wait_slow(uint32_t bar, uint32_t parity, volatile uint32_t *abort_flag,
+                                            unsigned long long *err, unsigned long long code) {
     const long long t0 = clock64();
     uint32_t spins = 0;
     while (true) {
@@ -128,6 +131,11 @@ __device__ __noinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile u
             }
         }
     }
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile uint32_t *abort_flag,
+                                          unsigned long long *err, unsigned long long code) {
+    return mbar_try_wait(bar, parity) || mbar_wait_slow(bar, parity, abort_flag, err, code);
 }
 
 __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, uint32_t bar, int x, int y) {
@@ -545,9 +553,9 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         const uint32_t lane_addr = tmem + ((uint32_t)(quarter * 32) << 16);
         Top2 *merge = (Top2 *)(smem + p.off_merge);
         const float cgrid = p.stats->cgrid, ulp = p.stats->ulp;
-        uint32_t item = 0;
+        uint32_t item = 0, tile_it = 0;
         bool dead = false;
-        for (int64_t t = q; t < p.tiles; t += tstride) {
+        for (int64_t t = q; t < p.tiles; t += tstride, tile_it++) {
             uint32_t R1 = 0u, R2 = 0u, U = 0u;
             int I1 = -1, I2 = -1;
             float cg = cgrid, ul = ulp;
@@ -561,6 +569,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                 const int buf = (int)(item & 1u);
                 const uint32_t aph = (item >> 1) & 1u;
                 if (!dead && !mbar_wait(bar_afull(buf), aph, abort_flag, p.err, 16ull)) dead = true;
+                dead = __any_sync(0xffffffffu, dead);  // warp-uniform, for the barriers below
                 if (dead) continue;
                 tc_fence_after();
                 const uint32_t col = lane_addr + (uint32_t)buf * BN + (uint32_t)half * 128u;
@@ -583,11 +592,24 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                 merge_res(R1, I1, R2, I2, U, b1 & 0xFFFFFF80u, base - (int)(b1 & 0x7Fu), b2 & 0xFFFFFF80u,
                           base - (int)(b2 & 0x7Fu), bu & 0xFFFFFF80u);
             }
-            if (half == 1)
-                merge[row_local] = Top2{__uint_as_float(R1), __uint_as_float(R2), __uint_as_float(U), 0.f, I1, I2, 0, 0};
-            epi_bar();
-            if (half == 0) {
-                const Top2 o = merge[row_local];
+            // Tile merge: half 1 publishes its record in slot tile_it % 3 and
+            // arrives on named barrier 1 + tile_it % 3 without waiting; half 0
+            // waits there, merges and stores. Half 1 cannot reach the same slot
+            // and barrier again (three tiles on) before half 0 has passed this
+            // merge: that tile's accumulators need every epilogue warp to have
+            // released the buffer of an earlier tile of this CTA. An aborting
+            // warp is no longer held back by the MMAs, so it waits instead.
+            const uint32_t sl = tile_it % 3u;
+            Top2 *slot = merge + sl * BM;
+            if (half == 1) {
+                slot[row_local] = Top2{__uint_as_float(R1), __uint_as_float(R2), __uint_as_float(U), 0.f, I1, I2, 0, 0};
+                if (dead)
+                    asm volatile("bar.sync %0, 256;" ::"r"(1u + sl) : "memory");
+                else
+                    asm volatile("bar.arrive %0, 256;" ::"r"(1u + sl) : "memory");
+            } else {
+                asm volatile("bar.sync %0, 256;" ::"r"(1u + sl) : "memory");
+                const Top2 o = slot[row_local];
                 merge_res(R1, I1, R2, I2, U, __float_as_uint(o.v1), o.i1, __float_as_uint(o.v2), o.i2,
                           __float_as_uint(o.u3));
                 const int64_t row = t * BM + row_local;
@@ -595,7 +617,6 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                     p.out[(int64_t)part * p.out_stride + row] =
                         Top2{__uint_as_float(R1), __uint_as_float(R2), __uint_as_float(U), 0.f, I1, I2, 0, 0};
             }
-            epi_bar();
         }
     } else {
         const int ew = warp - 2;
@@ -626,6 +647,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                 const int buf = (int)(item & 1u);
                 const uint32_t aph = (item >> 1) & 1u;
                 if (!dead && !mbar_wait(bar_afull(buf), aph, abort_flag, p.err, 16ull)) dead = true;
+                dead = __any_sync(0xffffffffu, dead);  // warp-uniform, for the barriers below
                 if (dead) continue;
                 tc_fence_after();
                 const uint32_t col = lane_addr + (uint32_t)buf * BN + (uint32_t)half * 128u;

@@ -21,8 +21,10 @@ F is chosen with dtype: "f64" (KMeans<f64>), "f32" (KMeans<f32>) or
 "f32x64" (KMeans<f64> semantics on X stored as f32, each value widened
 exactly; the entry point of the mixed precisions).
 """
+import atexit
 import ctypes as C
 import threading
+import weakref
 
 import numpy as np
 
@@ -105,6 +107,7 @@ class Context:
         _check(self._lib.fk_ctx_create(C.byref(h), int(device), C.c_void_p(stream) if stream else None))
         self.handle = h
         self.device = device
+        _live.add(self)
 
     def close(self):
         if self.handle:
@@ -114,6 +117,21 @@ class Context:
     def __del__(self):
         try:
             self.close()
+        except Exception:
+            pass
+
+
+# Contexts still open at interpreter exit are closed by an exit handler, while
+# the CUDA runtime and the streams they use are intact (a context released
+# later, during module teardown, would free device memory in arbitrary order).
+_live = weakref.WeakSet()
+
+
+@atexit.register
+def _close_live_contexts():
+    for ctx in list(_live):
+        try:
+            ctx.close()
         except Exception:
             pass
 
