@@ -152,12 +152,18 @@ bool precision_ok(int prec) {
 }
 
 // ------------------------------------------------------------ one step --
+// Update modes of the mixed path with f32 X: the full exact pass (optionally
+// keeping its exact sums), or the incremental one from the rows whose label
+// changed since the previous assignment (no inertia: the fit computes it
+// once, for the assignment it keeps).
+enum UpdateMode { UPDATE_FULL = 0, UPDATE_FULL_STATE = 1, UPDATE_INCREMENTAL = 2 };
+
 // Assignment against c (labels, inertia into scalars), then the update into
 // nc (+ shift bits). Mixed precisions fold the inertia into the update pass.
 template <typename TX, typename TC>
 void lloyd_iteration(Ctx &ctx, const TX *x, int64_t n, int d, const TC *c, int k, int prec, TC *nc,
                      int32_t *labels, DevScalars *sc, const SortPlan &plan, bool x_changed, fk_fit_report *rep,
-                     bool timing) {
+                     bool timing, int mode = UPDATE_FULL, const int32_t *prev_labels = nullptr) {
     cudaStream_t s = ctx.stream;
     int32_t *members = (int32_t *)ctx.get(BUF_MEMBERS, sizeof(int32_t) * (size_t)n);
     int32_t *seg = (int32_t *)ctx.get(BUF_SEGHIST, sizeof(int32_t) * (size_t)plan.k * plan.nseg);
@@ -178,6 +184,25 @@ void lloyd_iteration(Ctx &ctx, const TX *x, int64_t n, int d, const TC *c, int k
     }
     {
         Timer t(timing, ctx, rep ? &rep->ms_update : nullptr);
+        if constexpr (std::is_same<TX, float>::value && std::is_same<TC, double>::value) {
+            if (mode != UPDATE_FULL) {
+                const MixedStats *st = (const MixedStats *)ctx.get(BUF_CF32, sizeof(MixedStats));
+                ExactState *state = (ExactState *)ctx.get(BUF_XSTATE, sizeof(ExactState) * (size_t)k * d);
+                long long *counts = (long long *)ctx.get(BUF_XCOUNTS, sizeof(long long) * (size_t)k);
+                if (mode == UPDATE_INCREMENTAL) {
+                    launch_update_centroids_incremental(ctx, x, n, d, k, prev_labels, labels, c, nc, sc, &st->amax,
+                                                        state, counts);
+                } else {
+                    launch_sort_by_cluster(plan, labels, seg, tmp, members, s);
+                    double *part = (double *)ctx.get(BUF_OUT2, sizeof(double) * (size_t)plan.k * d + 64);
+                    void *scratch = ctx.get(BUF_FIXPART, update_exact_scratch_bytes(plan.k, d));
+                    launch_update_centroids_exact(plan, x, d, members, seg, c, nc, sc, &st->amax, part, scratch, s,
+                                                  state, counts);
+                    launch_mixed_inertia(ctx, part, (int64_t)plan.k * d, sc);
+                }
+                return;
+            }
+        }
         launch_sort_by_cluster(plan, labels, seg, tmp, members, s);
         if (prec == FK_PRECISION_PLAIN) {
             launch_update_centroids<TX, TC>(plan, x, d, members, seg, c, nc, sc, s);
@@ -273,8 +298,12 @@ fk_status fit_impl(fk_ctx *ctxp, const TX *x_in, int64_t n, int64_t d, const fk_
     }
     const size_t kd = (size_t)k * d;
     const TX *x = stage_in<TX>(ctx, BUF_X, x_in, (size_t)n * d);
-    TC *c = (TC *)ctx.get(BUF_C0, sizeof(TC) * kd);
-    TC *nc = (TC *)ctx.get(BUF_C1, sizeof(TC) * kd);
+    // Three rotating centre buffers: iteration it reads cb3[it % 3] and writes
+    // cb3[(it + 1) % 3], so neither the kept iteration's input nor its output
+    // is overwritten by the successor queued before the convergence test.
+    TC *cb3[3] = {(TC *)ctx.get(BUF_C0, sizeof(TC) * kd), (TC *)ctx.get(BUF_C1, sizeof(TC) * kd),
+                  (TC *)ctx.get(BUF_C2, sizeof(TC) * kd)};
+    TC *c = cb3[0];
     TC *cbest = (TC *)ctx.get(BUF_CBEST, sizeof(TC) * kd);
     // labels alternate between iterations: the next iteration is queued
     // before the previous one's convergence test has been read back
@@ -309,9 +338,15 @@ fk_status fit_impl(fk_ctx *ctxp, const TX *x_in, int64_t n, int64_t d, const fk_
     TC best_inertia = FMax<TC>::v();
     int64_t best_iter = 0;
     bool x_changed = true;
+    // Mixed path on f32 X: after a run's first (full) update, the exact sums
+    // are updated from the rows whose label changed. Decided once the first
+    // preparation has shown X finite and inside the split's exponent range.
+    bool inc_candidate = false, incremental = false;
+    if constexpr (std::is_same<TX, float>::value && std::is_same<TC, double>::value)
+        inc_candidate = p->precision != FK_PRECISION_PLAIN && incremental_shape_ok((const float *)x, (int)d);
     for (int64_t run = 0; run < p->n_init; run++) {
         if (init) {
-            FK_CUDA(cudaMemcpyAsync(c, init + (size_t)run * kd, sizeof(TC) * kd, cudaMemcpyDeviceToDevice, s));
+            FK_CUDA(cudaMemcpyAsync(cb3[0], init + (size_t)run * kd, sizeof(TC) * kd, cudaMemcpyDeviceToDevice, s));
         } else {
             Timer t(timing, ctx, rep ? &rep->ms_init : nullptr);
             const double *dr;
@@ -336,23 +371,23 @@ fk_status fit_impl(fk_ctx *ctxp, const TX *x_in, int64_t n, int64_t d, const fk_
             }
             int64_t used = 0;
             if constexpr (std::is_same<TX, TC>::value) {
-                run_kmeanspp<TC>(ctx, x, n, (int)d, (int)k, dr, ndr, c, &used);
+                run_kmeanspp<TC>(ctx, x, n, (int)d, (int)k, dr, ndr, cb3[0], &used);
             } else {
                 // k-means++ on the exactly widened matrix.
                 TC *xw = (TC *)ctx.get(BUF_XC, sizeof(TC) * (size_t)n * d);
                 launch_convert<TX, TC>(x, (int64_t)n * d, xw, s);
-                run_kmeanspp<TC>(ctx, xw, n, (int)d, (int)k, dr, ndr, c, &used);
+                run_kmeanspp<TC>(ctx, xw, n, (int)d, (int)k, dr, ndr, cb3[0], &used);
             }
             if (p->draws) draws_pos += used;
         }
         int64_t n_iter = 0;
         TC inertia = FMax<TC>::v();
-        // Iteration it reads cbuf[it & 1] and writes cbuf[(it + 1) & 1] and
+        // Iteration it reads cb3[it % 3] and writes cb3[(it + 1) % 3] and
         // labels2[it & 1]; its scalars are copied to pinned host memory right
         // after it, and read once the next iteration has been queued, so the
         // GPU never waits for the host. A converged iteration's successor is
-        // discarded (it touched neither the converged centres nor labels).
-        TC *cbuf[2] = {c, nc};
+        // discarded (it touched neither the converged centres, nor their
+        // input, nor the labels).
         auto finish = [&](int64_t r) {
             FK_CUDA(cudaEventSynchronize(iter_done[r & 1]));
             const DevScalars &h = ctx.host_scalars[1 + (r & 1)];
@@ -370,8 +405,23 @@ fk_status fit_impl(fk_ctx *ctxp, const TX *x_in, int64_t n, int64_t d, const fk_
         for (int64_t it = 0; it < p->max_iter && !stop; it++) {
             const int par = (int)(it & 1);
             FK_CUDA(cudaMemsetAsync(sc, 0, sizeof(DevScalars), s));
-            lloyd_iteration<TX, TC>(ctx, x, n, (int)d, cbuf[par], (int)k, p->precision, cbuf[par ^ 1],
-                                    labels2 + (size_t)par * n, sc, plan, x_changed, rep, timing);
+            // the first two iterations move many rows (a third of them is
+            // common in the second): the full pass is cheaper there
+            const int mode = !inc_candidate ? UPDATE_FULL
+                             : (it < 2 || !incremental) ? UPDATE_FULL_STATE
+                                                        : UPDATE_INCREMENTAL;
+            lloyd_iteration<TX, TC>(ctx, x, n, (int)d, cb3[it % 3], (int)k, p->precision, cb3[(it + 1) % 3],
+                                    labels2 + (size_t)par * n, sc, plan, x_changed, rep, timing, mode,
+                                    labels2 + (size_t)(par ^ 1) * n);
+            if (x_changed && inc_candidate) {
+                // once per fit: X finite and the split's grids valid?
+                MixedStats hs;
+                FK_CUDA(cudaMemcpyAsync(&hs, ctx.get(BUF_CF32, sizeof(MixedStats)), sizeof(MixedStats),
+                                        cudaMemcpyDeviceToHost, s));
+                FK_CUDA(cudaStreamSynchronize(s));
+                const int ea = hs.amax > 0.f ? std::ilogb(hs.amax) : -126;
+                incremental = hs.nonfinite == 0.f && ea >= -90 && ea <= 100;
+            }
             x_changed = false;
             FK_CUDA(cudaMemcpyAsync(&ctx.host_scalars[1 + par], sc, sizeof(DevScalars), cudaMemcpyDeviceToHost, s));
             FK_CUDA(cudaEventRecord(iter_done[par], s));
@@ -379,10 +429,18 @@ fk_status fit_impl(fk_ctx *ctxp, const TX *x_in, int64_t n, int64_t d, const fk_
             if (it > 0) stop = finish(it - 1);
         }
         if (!stop && launched > 0) finish(launched - 1);
-        // the result of iteration n_iter - 1: centres in cbuf[n_iter & 1]
-        c = cbuf[n_iter & 1];
-        nc = cbuf[(n_iter & 1) ^ 1];
+        // the result of iteration n_iter - 1: centres in cb3[n_iter % 3]
+        c = cb3[n_iter % 3];
         int32_t *labels = labels2 + (size_t)((n_iter > 0 ? n_iter - 1 : 0) & 1) * n;
+        if (incremental && n_iter > 0) {
+            // the incremental updates skip the per-iteration inertia: that of
+            // the kept assignment, against its centres cb3[(n_iter - 1) % 3]
+            if constexpr (std::is_same<TX, float>::value && std::is_same<TC, double>::value) {
+                launch_row_inertia(ctx, x, n, (int)d, labels, cb3[(n_iter - 1) % 3], (int)k, sc);
+                read_scalars(ctx, sc);
+                inertia = (TC)ctx.host_scalars->inertia;
+            }
+        }
         if (rep) rep->iterations_total += n_iter;
         if (!have || inertia < best_inertia) {
             have = true;
@@ -392,13 +450,6 @@ fk_status fit_impl(fk_ctx *ctxp, const TX *x_in, int64_t n, int64_t d, const fk_
             FK_CUDA(cudaMemcpyAsync(cbest, c, sizeof(TC) * kd, cudaMemcpyDeviceToDevice, s));
             FK_CUDA(cudaMemcpyAsync(lbest, labels, sizeof(int32_t) * (size_t)n, cudaMemcpyDeviceToDevice, s));
         }
-    }
-    // Keep the context's buffer pointers consistent after the swaps.
-    ctx.buf[BUF_C0] = c;
-    ctx.buf[BUF_C1] = nc;
-    if (ctx.cap[BUF_C0] != ctx.cap[BUF_C1]) {
-        size_t m = ctx.cap[BUF_C0] < ctx.cap[BUF_C1] ? ctx.cap[BUF_C0] : ctx.cap[BUF_C1];
-        ctx.cap[BUF_C0] = ctx.cap[BUF_C1] = m;
     }
     copy_out<TC>(ctx, centers_out, cbest, kd);
     if (is_device_ptr(labels_out)) {

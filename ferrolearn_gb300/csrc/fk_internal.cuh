@@ -69,6 +69,7 @@ struct MixedStats {
     float xn_max;  // max_i ||xh_i||           (set once per X)
     float amax;    // max |x_ij| over finite entries (set once per X)
     float tmax;    // max |x_ij - mu_j| over finite entries (set once per X)
+    float nonfinite;  // 1 if some row of X holds a non-finite value or overflows ||x|| (set once per X)
     float cn_max;  // max_c ||c' ||            (per iteration from here on)
     float ec_max;  // max_c ||c' - ch||
     float ch_max;  // max_c ||ch||
@@ -79,7 +80,6 @@ struct MixedStats {
     float ulp;     // 2^(E-23), the unit in the last place of every score
     float tscale;  // FP8: the centres' power-of-two scale t (1 for BF16)
     float inv_t;   // 1 / tscale
-    float pad;
 };
 
 // Best and second-best score of one row over one slice of the centres, and
@@ -131,7 +131,8 @@ enum BufSlot {
     BUF_OUT, BUF_OUT2, BUF_KPP0, BUF_KPP1, BUF_KPP2, BUF_KPP3, BUF_DRAWS,
     BUF_XB, BUF_XNORM, BUF_CB, BUF_CAUX, BUF_TOP2, BUF_FLAGS, BUF_FULL, BUF_CF32, BUF_CF32C, BUF_FIXPART,
     BUF_XB2, BUF_TOP8, BUF_OCT, BUF_EX, BUF_XAUG, BUF_ROWSCALE, BUF_ROWINFO2, BUF_STATS2, BUF_CB2, BUF_CAUG2,
-    BUF_HALF2, BUF_INERTIA2,
+    BUF_HALF2, BUF_INERTIA2, BUF_C2, BUF_XSTATE, BUF_XCOUNTS, BUF_MOVED, BUF_MOVED_ENT, BUF_MOVED_HIST, BUF_MOVED_TMP,
+    BUF_CSPLIT, BUF_RINERT,
     BUF_BX, BUF_BFITS, BUF_BSTATE, BUF_BITEMS, BUF_BPART, BUF_BORDER, BUF_BCTR, BUF_BLAB, BUF_BMEM, BUF_BCEN, BUF_BND, BUF_BXOFF,
     BUF_COUNT
 };
@@ -239,9 +240,28 @@ void launch_update_centroids(const SortPlan &p, const TX *x, int d, const int32_
 // Mixed precisions: exact 128-bit fixed-point cluster sums of an f32 X,
 // rounded once to f64, divided by the counts; plus the inertia partials.
 size_t update_exact_scratch_bytes(int k, int d);
+// Exact 128-bit fixed-point sum of one (cluster, feature) (two's complement).
+struct ExactState {
+    uint64_t lo, hi;
+};
+// state / counts (nullable): also keep the exact sums and the cluster sizes,
+// which launch_update_centroids_incremental then updates.
 void launch_update_centroids_exact(const SortPlan &p, const float *x, int d, const int32_t *members,
                                    const int32_t *seg_hist, const double *old_c, double *new_c, DevScalars *scalars,
-                                   const float *amax, double *inertia_part, void *scratch, cudaStream_t s);
+                                   const float *amax, double *inertia_part, void *scratch, cudaStream_t s,
+                                   ExactState *state = nullptr, long long *counts = nullptr);
+// The same new centres from the rows whose label changed since the
+// assignment that state / counts describe (they are updated to this one).
+// Needs incremental_shape_ok(x, d), a finite X and the two grids of the split
+// (-90 <= exponent of max|x| <= 100).
+bool incremental_shape_ok(const float *x, int d);
+void launch_update_centroids_incremental(Ctx &ctx, const float *x, int64_t n, int d, int k,
+                                         const int32_t *prev_labels, const int32_t *labels, const double *old_c,
+                                         double *new_c, DevScalars *scalars, const float *amax, ExactState *state,
+                                         long long *counts);
+// sum_i ||x_i - c_{labels_i}||^2 into scalars->inertia (deterministic).
+void launch_row_inertia(Ctx &ctx, const float *x, int64_t n, int d, const int32_t *labels, const double *c, int k,
+                        DevScalars *scalars);
 
 void launch_labels_to_u64(const int32_t *l, int64_t n, uint64_t *out, cudaStream_t s);
 template <typename TS, typename TD>

@@ -125,6 +125,43 @@ __device__ __forceinline__ float warp_sum_f(float v) {
     return v;
 }
 
+__device__ __forceinline__ float half_warp_sum_f(float v) {
+#pragma unroll
+    for (int off = 8; off >= 1; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    return v;
+}
+
+// This lane's part of the FP32 direct-form squared distance between x and c
+// (f32 rows of d features) when `group` lanes share one distance: lane g of
+// the group takes the features g, g + group, ... in 16-byte pieces when d is
+// a multiple of 4 (rows are then 16-byte aligned), else one at a time. The
+// parts are summed by the caller; any summation order stays within the
+// (d + 4) 2^-23 d32 term of bound32.
+__device__ __forceinline__ float sq_partial(const float *__restrict__ x, const float *__restrict__ c, int d, int g,
+                                            int group) {
+    float acc = 0.f;
+    if ((d & 3) == 0) {
+        const float4 *x4 = reinterpret_cast<const float4 *>(x), *c4 = reinterpret_cast<const float4 *>(c);
+        for (int f = g; f < (d >> 2); f += group) {
+            const float4 xv = x4[f], cv = c4[f];
+            float t = xv.x - cv.x;
+            acc = fmaf(t, t, acc);
+            t = xv.y - cv.y;
+            acc = fmaf(t, t, acc);
+            t = xv.z - cv.z;
+            acc = fmaf(t, t, acc);
+            t = xv.w - cv.w;
+            acc = fmaf(t, t, acc);
+        }
+    } else {
+        for (int f = g; f < d; f += group) {
+            const float t = x[f] - c[f];
+            acc = fmaf(t, t, acc);
+        }
+    }
+    return acc;
+}
+
 // One warp per row: BF16 copy of x - mu (row stride d_pad, zero padded) and
 // the row's bound ingredients {||xh||, ||x' - xh||, ||x||}, all computed in
 // f32 and then inflated to upper bounds: t = fl(x - mu) differs from x - mu
@@ -151,7 +188,7 @@ __global__ void prep_rows_kernel(const TX *__restrict__ x, int64_t n, int d, int
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
     const int64_t slots = list ? (int64_t)*count : n;
-    float xn_hi = 0.f, am_hi = 0.f;
+    float xn_hi = 0.f, am_hi = 0.f, nonfin = 0.f;
     for (int64_t slot = (int64_t)blockIdx.x * (blockDim.x >> 5) + w; slot < slots; slot += nwarps) {
         const int64_t row = list ? (int64_t)list[slot] : slot;
         float xn2 = 0.f, ex2 = 0.f, tn2 = 0.f, xo2 = 0.f, amax = 0.f, tmax = 0.f;  // tmax: FP8 only
@@ -211,12 +248,14 @@ __global__ void prep_rows_kernel(const TX *__restrict__ x, int64_t n, int d, int
         if (FP8 && lane < 16)
             xaug[slot * 16 + lane] = lane < 3 ? __float2bfloat16_rn(inv) : __float2bfloat16_rn(0.f);
         if (xn < INFINITY) xn_hi = fmaxf(xn_hi, xn);  // NaN / inf rows are re-scored in full
+        if (!(xo < INFINITY)) nonfin = 1.f;
         am_hi = fmaxf(am_hi, amax);
     }
     if (lane == 0) {
         sh_xn[w] = xn_hi;
         sh_am[w] = am_hi;
     }
+    if (nonfin != 0.f) stats->nonfinite = 1.f;  // benign race: every writer stores 1
     __syncthreads();
     if (threadIdx.x == 0) {
         float a = 0.f, b = 0.f;
@@ -227,6 +266,159 @@ __global__ void prep_rows_kernel(const TX *__restrict__ x, int64_t n, int d, int
         atomic_max_pos(&stats->xn_max, a);
         atomic_max_pos(&stats->amax, b);
     }
+}
+
+// The same outputs as prep_rows_kernel for f32 rows with d a multiple of 4 and
+// d_pad <= 256: lane l owns the 4-feature pieces l and l + 32 of the row,
+// loaded once with 16-byte loads, and the next row's pieces are in flight
+// while this one is processed. The norms are summed in another order than in
+// prep_rows_kernel, which the upward inflation by (d + 64) 2^-23 covers.
+template <bool FP8>
+__global__ void prep_rows4_kernel(const float *__restrict__ x, int64_t n, int d, int d_pad,
+                                  const float *__restrict__ mu32, void *__restrict__ xq_out,
+                                  __nv_bfloat16 *__restrict__ xaug, float4 *__restrict__ rowinfo, MixedStats *stats,
+                                  const int32_t *__restrict__ list, const unsigned long long *count) {
+    __shared__ float sh_xn[32], sh_am[32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    const int64_t slots = list ? (int64_t)*count : n;
+    const int d4 = d >> 2, dp4 = d_pad >> 2;
+    const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 m4[2];
+#pragma unroll
+    for (int i = 0; i < 2; i++) {
+        const int q = lane + 32 * i;
+        m4[i] = q < d4 ? reinterpret_cast<const float4 *>(mu32)[q] : zero4;
+    }
+    auto load_row = [&](int64_t sl, float4 (&v)[2]) {
+        const int64_t row = list ? (int64_t)list[sl] : sl;
+        const float4 *r4 = reinterpret_cast<const float4 *>(x + row * d);
+#pragma unroll
+        for (int i = 0; i < 2; i++) {
+            const int q = lane + 32 * i;
+            v[i] = q < d4 ? r4[q] : zero4;
+        }
+    };
+    float xn_hi = 0.f, am_hi = 0.f, nonfin = 0.f;
+    int64_t slot = (int64_t)blockIdx.x * (blockDim.x >> 5) + w;
+    float4 cur[2] = {zero4, zero4};
+    if (slot < slots) load_row(slot, cur);
+    for (; slot < slots; slot += nwarps) {
+        float4 nxt[2] = {zero4, zero4};
+        if (slot + nwarps < slots) load_row(slot + nwarps, nxt);
+        float xn2 = 0.f, ex2 = 0.f, tn2 = 0.f, xo2 = 0.f, amax = 0.f;
+        float scale = 1.f, inv = 1.f;
+        if (FP8) {
+            float tmax = 0.f;
+#pragma unroll
+            for (int i = 0; i < 2; i++) {
+                if (lane + 32 * i >= d4) continue;
+                const float xs[4] = {cur[i].x, cur[i].y, cur[i].z, cur[i].w};
+                const float ms[4] = {m4[i].x, m4[i].y, m4[i].z, m4[i].w};
+#pragma unroll
+                for (int c = 0; c < 4; c++) {
+                    const float tv = fabsf(__fsub_rn(xs[c], ms[c]));
+                    if (tv < INFINITY) tmax = fmaxf(tmax, tv);
+                }
+            }
+#pragma unroll
+            for (int off = 16; off >= 1; off >>= 1) tmax = fmaxf(tmax, __shfl_xor_sync(0xffffffffu, tmax, off));
+            const int sh_t = fp8_scale_exp(stats->tmax);
+            int sh = tmax > 0.f ? fp8_scale_exp(tmax) : sh_t;
+            sh = max(min(sh, sh_t + FP8_ROW_ABOVE), sh_t - FP8_ROW_BELOW);
+            sh = max(min(sh, 120), -120);
+            scale = ldexpf(1.f, sh);
+            inv = ldexpf(1.f, -sh);
+        }
+#pragma unroll
+        for (int i = 0; i < 2; i++) {
+            const int q = lane + 32 * i;
+            if (q >= dp4) continue;
+            if (q < d4) {
+                const float xs[4] = {cur[i].x, cur[i].y, cur[i].z, cur[i].w};
+                const float ms[4] = {m4[i].x, m4[i].y, m4[i].z, m4[i].w};
+                uint32_t packed[2] = {0u, 0u};
+#pragma unroll
+                for (int c = 0; c < 4; c++) {
+                    const float xv = xs[c];
+                    const float t = __fsub_rn(xv, ms[c]);
+                    float hv;
+                    if (FP8) {
+                        const __nv_fp8_e4m3 q8(__fmul_rn(t, inv));
+                        packed[0] |= (uint32_t)q8.__x << (8 * c);
+                        hv = __fmul_rn((float)q8, scale);
+                    } else {
+                        const __nv_bfloat16 h = __float2bfloat16_rn(t);
+                        packed[c >> 1] |= (uint32_t)__bfloat16_as_ushort(h) << (16 * (c & 1));
+                        hv = __bfloat162float(h);
+                    }
+                    const float e = __fsub_rn(t, hv);
+                    xn2 = __fmaf_rn(hv, hv, xn2);
+                    ex2 = __fmaf_rn(e, e, ex2);
+                    tn2 = __fmaf_rn(t, t, tn2);
+                    xo2 = __fmaf_rn(xv, xv, xo2);
+                    if (fabsf(xv) < INFINITY) amax = fmaxf(amax, fabsf(xv));  // finite values only
+                }
+                if (FP8)
+                    reinterpret_cast<uint32_t *>(xq_out)[slot * dp4 + q] = packed[0];
+                else
+                    reinterpret_cast<uint2 *>(xq_out)[slot * dp4 + q] = make_uint2(packed[0], packed[1]);
+            } else if (FP8) {
+                reinterpret_cast<uint32_t *>(xq_out)[slot * dp4 + q] = 0u;
+            } else {
+                reinterpret_cast<uint2 *>(xq_out)[slot * dp4 + q] = make_uint2(0u, 0u);
+            }
+        }
+        xn2 = warp_sum_f(xn2);
+        ex2 = warp_sum_f(ex2);
+        tn2 = warp_sum_f(tn2);
+        xo2 = warp_sum_f(xo2);
+#pragma unroll
+        for (int off = 16; off >= 1; off >>= 1) amax = fmaxf(amax, __shfl_xor_sync(0xffffffffu, amax, off));
+        const float up = 1.0f + (float)(d + 64) * 1.1920929e-07f;
+        const float xn = __fsqrt_ru(__fmul_ru(xn2, up));
+        const float ex =
+            __fadd_ru(__fsqrt_ru(__fmul_ru(ex2, up)), __fmul_ru(__fsqrt_ru(__fmul_ru(tn2, up)), 5.9604645e-08f));
+        const float xo = __fsqrt_ru(__fmul_ru(xo2, up));
+        if (lane == 0) rowinfo[slot] = make_float4(xn, ex, xo, inv);
+        if (FP8 && lane < 16)
+            xaug[slot * 16 + lane] = lane < 3 ? __float2bfloat16_rn(inv) : __float2bfloat16_rn(0.f);
+        if (xn < INFINITY) xn_hi = fmaxf(xn_hi, xn);  // NaN / inf rows are re-scored in full
+        if (!(xo < INFINITY)) nonfin = 1.f;
+        am_hi = fmaxf(am_hi, amax);
+#pragma unroll
+        for (int i = 0; i < 2; i++) cur[i] = nxt[i];
+    }
+    if (lane == 0) {
+        sh_xn[w] = xn_hi;
+        sh_am[w] = am_hi;
+    }
+    if (nonfin != 0.f) stats->nonfinite = 1.f;  // benign race: every writer stores 1
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float a = 0.f, b = 0.f;
+        for (int q = 0; q < (int)(blockDim.x >> 5); q++) {
+            a = fmaxf(a, sh_xn[q]);
+            b = fmaxf(b, sh_am[q]);
+        }
+        atomic_max_pos(&stats->xn_max, a);
+        atomic_max_pos(&stats->amax, b);
+    }
+}
+
+// Row preparation launch: the 16-byte kernel where it applies.
+template <typename TX, bool FP8>
+void launch_prep_rows(Ctx &ctx, const TX *x, int64_t n, int d, int d_pad, const float *mu32, void *xq,
+                      __nv_bfloat16 *xaug, float4 *rowinfo, MixedStats *stats, const int32_t *list = nullptr,
+                      const unsigned long long *count = nullptr) {
+    const int64_t pblocks = std::min<int64_t>((n + 7) / 8, (int64_t)ctx.num_sms * 16);
+    if (std::is_same<TX, float>::value && (d & 3) == 0 && d_pad <= 256)
+        prep_rows4_kernel<FP8><<<(unsigned)pblocks, 256, 0, ctx.stream>>>(
+            (const float *)x, n, d, d_pad, mu32, xq, xaug, rowinfo, stats, list, count);
+    else
+        prep_rows_kernel<TX, FP8><<<(unsigned)pblocks, 256, 0, ctx.stream>>>(x, n, d, d_pad, mu32, xq, xaug,
+                                                                             rowinfo, stats, list, count);
+    FK_LAUNCH_CHECK();
 }
 
 // -------------------------------------------------------- centre prep --
@@ -419,7 +611,44 @@ __device__ __forceinline__ unsigned long long warp_reserve(unsigned long long *c
     return base + (unsigned long long)__popc(want & ((1u << lane) - 1u));
 }
 
-__global__ void finalize_kernel(const Top2 *__restrict__ parts, int nparts, int64_t n, int k, int d,
+// Block-aggregated appends to two lists: the block's lanes with pa (pb) set
+// get consecutive slots of list A (B) from one atomic per list per block, so
+// the shared counters see a few thousand atomics per pass instead of one per
+// warp. Every thread of the block must call it.
+template <int NT>
+__device__ __forceinline__ void block_reserve2(unsigned long long *ca, bool pa, unsigned long long *cb, bool pb,
+                                               unsigned long long &sa, unsigned long long &sb) {
+    __shared__ unsigned int wa[NT / 32], wb[NT / 32];
+    __shared__ unsigned long long base_a, base_b;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const unsigned ba = __ballot_sync(0xffffffffu, pa), bb = __ballot_sync(0xffffffffu, pb);
+    if (lane == 0) {
+        wa[w] = (unsigned)__popc(ba);
+        wb[w] = (unsigned)__popc(bb);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned ta = 0, tb = 0;
+        for (int i = 0; i < NT / 32; i++) {
+            const unsigned xa = wa[i], xb = wb[i];
+            wa[i] = ta;
+            wb[i] = tb;
+            ta += xa;
+            tb += xb;
+        }
+        base_a = ta ? atomicAdd(ca, (unsigned long long)ta) : 0ull;
+        base_b = tb ? atomicAdd(cb, (unsigned long long)tb) : 0ull;
+    }
+    __syncthreads();
+    const unsigned below = (1u << lane) - 1u;
+    sa = base_a + wa[w] + (unsigned)__popc(ba & below);
+    sb = base_b + wb[w] + (unsigned)__popc(bb & below);
+}
+
+constexpr int FINALIZE_THREADS = 512;
+
+__global__ void __launch_bounds__(FINALIZE_THREADS)
+    finalize_kernel(const Top2 *__restrict__ parts, int nparts, int64_t n, int k, int d,
                                 const float4 *__restrict__ rowinfo, const MixedStats *stats, float acc_rel,
                                 float mu_norm, int32_t *__restrict__ labels, int4 *__restrict__ pair_list,
                                 int32_t *__restrict__ full_list, DevScalars *sc) {
@@ -457,16 +686,20 @@ __global__ void finalize_kernel(const Top2 *__restrict__ parts, int nparts, int6
             cls = 2;
         }
     }
-    const unsigned long long ps = warp_reserve(&sc->flag_count, cls == 1);
+    unsigned long long ps, fs;
+    block_reserve2<FINALIZE_THREADS>(&sc->flag_count, cls == 1, &sc->full_count, cls == 2, ps, fs);
     if (cls == 1) pair_list[ps] = make_int4((int)i, i1, i2, 0);
-    const unsigned long long fs = warp_reserve(&sc->full_count, cls == 2);
     if (cls == 2) full_list[fs] = (int32_t)i;
 }
 
 // ------------------------------------------------------------ re-checks --
+// FP64 direct form in the oracle's order (x widened exactly, one running
+// sum over increasing j). Kept register-light: it runs inside kernels whose
+// FP32 paths need the occupancy.
 template <typename TX>
 __device__ __forceinline__ double sqeuc64(const TX *__restrict__ x, const double *__restrict__ c, int d) {
     double acc = 0.0;
+#pragma unroll 4
     for (int j = 0; j < d; j++) {
         double t = __dsub_rn((double)x[j], c[j]);
         acc = __dadd_rn(acc, __dmul_rn(t, t));
@@ -525,16 +758,11 @@ __global__ void pair_rescore_kernel(const TX *__restrict__ x, int d, const doubl
         const TX *row = x + (int64_t)e.x * d;
         const int a = e.y < e.z ? e.y : e.z, b = e.y < e.z ? e.z : e.y;
         if constexpr (std::is_same<TX, float>::value) {
-            const float *ca = c32 + (int64_t)a * d, *cb = c32 + (int64_t)b * d;
-            float sa = 0.f, sb = 0.f;
-            for (int j = lane; j < d; j += 32) {
-                const float xv = row[j];
-                const float ta = xv - ca[j], tb = xv - cb[j];
-                sa = fmaf(ta, ta, sa);
-                sb = fmaf(tb, tb, sb);
-            }
-            sa = warp_sum_f(sa);
-            sb = warp_sum_f(sb);
+            // lanes 0-15 score centre a, lanes 16-31 centre b, 16-byte loads
+            const int hl = lane & 15;
+            const float *cc = c32 + (int64_t)(lane < 16 ? a : b) * d;
+            const float acc = half_warp_sum_f(sq_partial(row, cc, d, hl, 16));
+            const float sa = __shfl_sync(0xffffffffu, acc, 0), sb = __shfl_sync(0xffffffffu, acc, 16);
             const float ea = bound32(sa, ec32[a], d), eb = bound32(sb, ec32[b], d);
             if (below(sa, ea, sb, eb)) {
                 if (lane == 0) labels[e.x] = a;
@@ -860,20 +1088,19 @@ __global__ void oct_rescore_kernel(const float *__restrict__ x, int d, const dou
         const float *row = x + (int64_t)qd.row * d;
         float dist[8], err[8];
         float ub = INFINITY;
+        {  // candidate lane >> 2 scored by four lanes at once
+            const int cj = lane >> 2;
+            float acc = 0.f;
+            if (cj < qd.m) acc = sq_partial(row, c32 + (int64_t)qd.ids[cj] * d, d, lane & 3, 4);
+            acc += __shfl_xor_sync(0xffffffffu, acc, 2);
+            acc += __shfl_xor_sync(0xffffffffu, acc, 1);
+#pragma unroll
+            for (int j = 0; j < 8; j++) dist[j] = __shfl_sync(0xffffffffu, acc, 4 * j);
+        }
 #pragma unroll
         for (int j = 0; j < 8; j++) {
-            float acc = 0.f;
-            if (j < qd.m) {
-                const float *cc = c32 + (int64_t)qd.ids[j] * d;
-                for (int f = lane; f < d; f += 32) {
-                    const float t = row[f] - cc[f];
-                    acc = fmaf(t, t, acc);
-                }
-            }
-            acc = warp_sum_f(acc);
-            dist[j] = acc;
-            err[j] = j < qd.m ? bound32(acc, ec32[qd.ids[j]], d) : 0.f;
-            if (j < qd.m) ub = fminf(ub, __fadd_ru(acc, err[j]));
+            err[j] = j < qd.m ? bound32(dist[j], ec32[qd.ids[j]], d) : 0.f;
+            if (j < qd.m) ub = fminf(ub, __fadd_ru(dist[j], err[j]));
         }
         int nsurv = 0, only = -1;
         float my_dist = 0.f, my_err = 0.f;
@@ -1025,14 +1252,10 @@ MixedBufs prepare_mixed(Ctx &ctx, const TX *x, int64_t n, int d, const double *c
             sample_tmax_kernel<TX><<<ctx.num_sms * 2, 256, 0, s>>>(x, n, d, stride, rows, B.mu32, B.stats);
             FK_LAUNCH_CHECK();
         }
-        const int64_t pblocks = std::min<int64_t>((n + 7) / 8, (int64_t)ctx.num_sms * 16);
         if (fp8)
-            prep_rows_kernel<TX, true><<<(unsigned)pblocks, 256, 0, s>>>(x, n, d, mp.d_pad, B.mu32, B.xq, B.xaug,
-                                                                          B.rowinfo, B.stats);
+            launch_prep_rows<TX, true>(ctx, x, n, d, mp.d_pad, B.mu32, B.xq, B.xaug, B.rowinfo, B.stats);
         else
-            prep_rows_kernel<TX, false><<<(unsigned)pblocks, 256, 0, s>>>(x, n, d, mp.d_pad, B.mu32, B.xq, nullptr,
-                                                                           B.rowinfo, B.stats);
-        FK_LAUNCH_CHECK();
+            launch_prep_rows<TX, false>(ctx, x, n, d, mp.d_pad, B.mu32, B.xq, nullptr, B.rowinfo, B.stats);
         // ||mu|| for the bound on ||x|| (host side, tiny)
         std::vector<double> hmu(d);
         FK_CUDA(cudaMemcpyAsync(hmu.data(), B.mu, sizeof(double) * d, cudaMemcpyDeviceToHost, s));
@@ -1095,10 +1318,7 @@ void second_pass(Ctx &ctx, const float *x, int64_t n, int d, const double *c, in
     Oct *octs = (Oct *)ctx.get(BUF_OCT, sizeof(Oct) * (size_t)n);
     int32_t *ex = (int32_t *)ctx.get(BUF_EX, sizeof(int32_t) * (size_t)n);
     FK_CUDA(cudaMemsetAsync(st2, 0, sizeof(MixedStats), s));
-    const int64_t pblocks = std::min<int64_t>((n + 7) / 8, (int64_t)ctx.num_sms * 16);
-    prep_rows_kernel<float, false><<<(unsigned)pblocks, 256, 0, s>>>(x, n, d, m2.d_pad, B.mu32, xb2, nullptr, ri2,
-                                                                      st2, full, &sc->full_count);
-    FK_LAUNCH_CHECK();
+    launch_prep_rows<float, false>(ctx, x, n, d, m2.d_pad, B.mu32, xb2, nullptr, ri2, st2, full, &sc->full_count);
     prep_centres_kernel<false><<<(m2.k_pad + 7) / 8, 256, 0, s>>>(c, k, m2.k_pad, d, m2.d_pad, B.mu, cb2, hn2,
                                                                   nullptr, nullptr, nullptr, st2);
     FK_LAUNCH_CHECK();
@@ -1154,8 +1374,8 @@ void run_assign_mixed(Ctx &ctx, const TX *x, int64_t n, int d, const double *c, 
     int4 *pairs = (int4 *)ctx.get(BUF_FLAGS, sizeof(int4) * (size_t)n);
     int32_t *full = (int32_t *)ctx.get(BUF_FULL, sizeof(int32_t) * (size_t)n);
     const float acc_rel = (float)((double)((size_t)mp.d_pad + 32) * ACC_REL_PER_K);  // exact: integer * 2^-22
-    finalize_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(top, mp.parts, n, k, d, B.rowinfo, B.stats, acc_rel,
-                                                               mu_norm_up(mp.mu_norm), labels, pairs, full, sc);
+    finalize_kernel<<<(unsigned)((n + FINALIZE_THREADS - 1) / FINALIZE_THREADS), FINALIZE_THREADS, 0, s>>>(
+        top, mp.parts, n, k, d, B.rowinfo, B.stats, acc_rel, mu_norm_up(mp.mu_norm), labels, pairs, full, sc);
     FK_LAUNCH_CHECK();
     const int grid = ctx.num_sms * 4;
     pair_rescore_kernel<TX><<<grid, 256, 0, s>>>(x, d, c, B.c32, B.ec32, pairs, sc, labels);

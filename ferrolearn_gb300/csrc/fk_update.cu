@@ -590,7 +590,8 @@ __global__ void centroid_fixed_combine_kernel(int d, int k, int splits, int64_t 
                                               int64_t nseg,
                                               const double *__restrict__ old_c, double *__restrict__ new_c,
                                               const float *__restrict__ amax_ptr, const FixedPart *__restrict__ parts,
-                                              double *__restrict__ inertia_part) {
+                                              double *__restrict__ inertia_part, ExactState *__restrict__ state,
+                                              long long *__restrict__ counts) {
     const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= (int64_t)k * d) return;
     const int c = (int)(idx / d), j = (int)(idx % d);
@@ -620,6 +621,10 @@ __global__ void centroid_fixed_combine_kernel(int d, int k, int splits, int64_t 
     }
     new_c[idx] = mean;
     inertia_part[idx] = inert;
+    if (state) {  // the exact sums and counts that later iterations update incrementally
+        state[idx] = ExactState{lo, hi};
+        if (j == 0) counts[c] = cntc;
+    }
 }
 
 // squared_euclidean(new, old) per cluster, folded over j; max over clusters as
@@ -649,6 +654,334 @@ __global__ void max_shift_kernel(const TC *__restrict__ new_c, const TC *__restr
         acc = A::add(acc, A::mul(t, t));
     }
     if (acc > TC(0)) atomicMax(shift_bits, ShiftBits<TC>::bits(acc));
+}
+
+// ------------------------------------------------ incremental exact sums --
+// The mixed path's cluster sums are exact integers (the two-grid split plus
+// the 128-bit fixed-point remainders, see centroid_fixed_part4_kernel), so
+// once they are known for one assignment, the sums of the next one follow
+// from the rows whose label changed: each such row is taken out of its old
+// cluster and added to its new one with the same integer decomposition. The
+// result is bit for bit the sum the full pass would form. Used only when X is
+// finite and the two grids apply (the full pass handles the rest).
+
+constexpr int DIFF_THREADS = 512;
+
+// Rows whose label differs between two assignments, appended as (row, old,
+// new) with one atomic per block; hist counts the entries per cluster (one
+// for the old cluster, one for the new).
+__global__ void __launch_bounds__(DIFF_THREADS)
+    label_diff_kernel(const int32_t *__restrict__ prev, const int32_t *__restrict__ cur, int64_t n,
+                      int4 *__restrict__ moved, unsigned long long *moved_count, int32_t *__restrict__ hist) {
+    __shared__ unsigned int wcnt[DIFF_THREADS / 32];
+    __shared__ unsigned long long base;
+    const int64_t i = (int64_t)blockIdx.x * DIFF_THREADS + threadIdx.x;
+    int o = 0, nw = 0;
+    if (i < n) {
+        o = prev[i];
+        nw = cur[i];
+    }
+    const bool ch = i < n && o != nw;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const unsigned m = __ballot_sync(0xffffffffu, ch);
+    if (lane == 0) wcnt[w] = (unsigned)__popc(m);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned t = 0;
+        for (int q = 0; q < DIFF_THREADS / 32; q++) {
+            const unsigned v = wcnt[q];
+            wcnt[q] = t;
+            t += v;
+        }
+        base = t ? atomicAdd(moved_count, (unsigned long long)t) : 0ull;
+    }
+    __syncthreads();
+    if (ch) {
+        const unsigned long long slot = base + wcnt[w] + (unsigned)__popc(m & ((1u << lane) - 1u));
+        moved[slot] = make_int4((int)i, o, nw, 0);
+        atomicAdd(&hist[nw], 1);
+        atomicAdd(&hist[o], 1);
+    }
+}
+
+// Entries grouped by cluster (order inside a cluster is free: the sums are
+// integers): row << 1 into the new cluster, row << 1 | 1 out of the old one.
+__global__ void moved_scatter_kernel(const int4 *__restrict__ moved, const unsigned long long *moved_count,
+                                     int32_t *__restrict__ cursor, uint32_t *__restrict__ ent) {
+    const unsigned long long cnt = *moved_count;
+    for (unsigned long long q = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; q < cnt;
+         q += (unsigned long long)gridDim.x * blockDim.x) {
+        const int4 e = moved[q];
+        const int pin = atomicAdd(&cursor[e.z], 1);
+        ent[pin] = (uint32_t)e.x << 1;
+        const int pout = atomicAdd(&cursor[e.y], 1);
+        ent[pout] = ((uint32_t)e.x << 1) | 1u;
+    }
+}
+
+// One block per cluster: the signed exact sum of its entries (the same
+// decomposition as centroid_fixed_part4_kernel, d % 4 == 0), added to the
+// cluster's state, and the change of its count.
+__global__ void __launch_bounds__(FIX4_THREADS, 3) exact_delta4_kernel(
+    const float *__restrict__ x, int d, int k, int64_t n, const int32_t *__restrict__ eoff,
+    const unsigned long long *moved_count, const uint32_t *__restrict__ ent, const float *__restrict__ amax_ptr,
+    ExactState *__restrict__ state, long long *__restrict__ counts) {
+    __shared__ FixRed red[FIX4_THREADS];
+    __shared__ uint32_t sent[FIX4_IDX];
+    __shared__ float tail_v[TAIL_CAP];
+    __shared__ int tail_f[TAIL_CAP];
+    __shared__ int tail_n, cdelta;
+    const int c = blockIdx.x;
+    const int64_t total = 2 * (int64_t)*moved_count;
+    const int64_t start = eoff[c];
+    const int64_t end = c + 1 < k ? (int64_t)eoff[c + 1] : total;
+    if (start >= end) return;  // block-uniform
+    const int S = d >> 2;
+    const int G = FIX4_THREADS / S;
+    const int g = (int)threadIdx.x / S, sl = (int)threadIdx.x % S;
+    const bool active = g < G;
+    const int F = fixed_bits(amax_ptr, n);
+    const float amax = *amax_ptr;
+    const int ea = amax > 0.f ? (int)((__float_as_uint(amax) >> 23) & 0xFFu) - 127 : -126;
+    const int kb = ea + 2;  // the caller guarantees -90 <= ea <= 100
+    const float C1 = ldexpf(1.5f, kb), C2 = ldexpf(1.5f, kb - 23);
+    const int b1 = __float_as_int(C1), b2 = __float_as_int(C2);
+    long long acc1[4] = {0, 0, 0, 0}, acc2[4] = {0, 0, 0, 0};
+    int my_delta = 0;
+    if (threadIdx.x == 0) {
+        tail_n = 0;
+        cdelta = 0;
+    }
+    for (int64_t cb = start; cb < end; cb += FIX4_IDX) {
+        const int cnt = (int)min((int64_t)FIX4_IDX, end - cb);
+        __syncthreads();
+        for (int t = threadIdx.x; t < cnt; t += FIX4_THREADS) sent[t] = ent[cb + t];
+        __syncthreads();
+        if (!active) continue;
+        for (int r = g; r < cnt; r += G) {
+            const uint32_t e = sent[r];
+            const bool neg = (e & 1u) != 0u;
+            if (sl == 0) my_delta += neg ? -1 : 1;
+            const float4 v = reinterpret_cast<const float4 *>(x + (int64_t)(e >> 1) * d)[sl];
+            const float ev[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+            for (int f = 0; f < 4; f++) {
+                const float s1 = __fadd_rn(ev[f], C1);
+                const int q1 = (int)(__float_as_uint(s1) - (uint32_t)b1);
+                const float rr = __fsub_rn(ev[f], __fsub_rn(s1, C1));
+                const float s2 = __fadd_rn(rr, C2);
+                const int q2 = (int)(__float_as_uint(s2) - (uint32_t)b2);
+                const float r2 = __fsub_rn(rr, __fsub_rn(s2, C2));
+                acc1[f] += neg ? -q1 : q1;
+                acc2[f] += neg ? -q2 : q2;
+                if (r2 != 0.f) {
+                    const int slot = atomicAdd(&tail_n, 1);
+                    if (slot < TAIL_CAP) {
+                        tail_v[slot] = neg ? -r2 : r2;
+                        tail_f[slot] = 4 * sl + f;
+                    }
+                }
+            }
+        }
+    }
+    __syncthreads();
+    const int tn = tail_n;
+    uint64_t slo[4] = {0, 0, 0, 0}, shi[4] = {0, 0, 0, 0};
+    if (g == 0 && active && tn <= TAIL_CAP) {
+        for (int e = 0; e < tn; e++) {
+            const int fe = tail_f[e];
+            if ((fe >> 2) != sl) continue;
+#pragma unroll
+            for (int f = 0; f < 4; f++)
+                if ((fe & 3) == f) fixed_add_signed(slo[f], shi[f], tail_v[e], F);
+        }
+    }
+    if (active && tn > TAIL_CAP) {  // the list overflowed: this thread's remainders again
+        for (int64_t q = start + g; q < end; q += G) {
+            const uint32_t e = ent[q];
+            const bool neg = (e & 1u) != 0u;
+            const float4 v = reinterpret_cast<const float4 *>(x + (int64_t)(e >> 1) * d)[sl];
+            const float ev[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+            for (int f = 0; f < 4; f++) {
+                const float s1 = __fadd_rn(ev[f], C1);
+                const float rr = __fsub_rn(ev[f], __fsub_rn(s1, C1));
+                const float s2 = __fadd_rn(rr, C2);
+                const float r2 = __fsub_rn(rr, __fsub_rn(s2, C2));
+                if (r2 != 0.f) fixed_add_signed(slo[f], shi[f], neg ? -r2 : r2, F);
+            }
+        }
+    }
+    FixRed mine;
+#pragma unroll
+    for (int f = 0; f < 4; f++) {
+        uint64_t lo = slo[f], hi = shi[f];
+        add_shifted(lo, hi, acc1[f], kb - 23 + F);
+        add_shifted(lo, hi, acc2[f], kb - 46 + F);
+        mine.lo[f] = lo;
+        mine.hi[f] = hi;
+        mine.inert[f] = 0.0;
+        mine.flags[f] = 0u;
+    }
+    red[threadIdx.x] = mine;
+#pragma unroll
+    for (int off = 16; off >= 1; off >>= 1) my_delta += __shfl_xor_sync(0xffffffffu, my_delta, off);
+    if ((threadIdx.x & 31) == 0 && my_delta != 0) atomicAdd(&cdelta, my_delta);
+    __syncthreads();
+    if (g == 0 && active) {
+        FixRed t = red[sl];
+        for (int gg = 1; gg < G; gg++) {
+            const FixRed &o = red[gg * S + sl];
+#pragma unroll
+            for (int f = 0; f < 4; f++) add128(t.lo[f], t.hi[f], o.lo[f], o.hi[f]);
+        }
+#pragma unroll
+        for (int f = 0; f < 4; f++) {
+            ExactState &st = state[(int64_t)c * d + 4 * sl + f];
+            uint64_t lo = st.lo, hi = st.hi;
+            add128(lo, hi, t.lo[f], t.hi[f]);
+            st = ExactState{lo, hi};
+        }
+    }
+    if (threadIdx.x == 0) counts[c] += cdelta;
+}
+
+// Means from the exact state: the sum rounded once to f64, divided by the
+// count (an empty cluster keeps its centre), as centroid_fixed_combine_kernel.
+__global__ void exact_means_kernel(int d, int k, int64_t n, const ExactState *__restrict__ state,
+                                   const long long *__restrict__ counts, const float *__restrict__ amax_ptr,
+                                   const double *__restrict__ old_c, double *__restrict__ new_c) {
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (int64_t)k * d) return;
+    const long long cnt = counts[idx / d];
+    if (cnt <= 0) {
+        new_c[idx] = old_c[idx];
+        return;
+    }
+    const ExactState st = state[idx];
+    const double sum = fixed_to_double(((unsigned __int128)st.hi << 64) | st.lo, fixed_bits(amax_ptr, n));
+    new_c[idx] = __ddiv_rn(sum, (double)cnt);
+}
+
+// ------------------------------------------------------- row inertia --
+// sum_i ||x_i - c_{l_i}||^2 for one assignment: the centres split into f32
+// hi + lo parts (x - c = (x - hi) - lo to about 2^-23 relative), each lane's
+// squares over all its rows summed with compensation (Kahan) in f32, then the
+// lanes in f64; the warps' sums folded in a fixed order per block (a fixed
+// grid makes the result deterministic).
+constexpr int RI_THREADS = 256;
+
+__global__ void split_centres_kernel(const double *__restrict__ c, int64_t kd, float *__restrict__ hi,
+                                     float *__restrict__ lo) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= kd) return;
+    const double v = c[i];
+    const float h = __double2float_rn(v);
+    hi[i] = h;
+    lo[i] = __double2float_rn(__dsub_rn(v, (double)h));
+}
+
+// The same sum for d % 4 == 0 and d <= 256 (every mixed-path shape with f32
+// X): lane l owns the 16-byte pieces l and l + 32 of a row; the next row's
+// label and features load while this row is summed, and its centre pieces
+// right after.
+__global__ void __launch_bounds__(RI_THREADS)
+    row_inertia4_kernel(const float *__restrict__ x, int64_t n, int d, const int32_t *__restrict__ labels,
+                        const float *__restrict__ chi, const float *__restrict__ clo, double *__restrict__ block_part) {
+    __shared__ double wsum[RI_THREADS / 32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int64_t nw = (int64_t)gridDim.x * (RI_THREADS / 32);
+    const int d4 = d >> 2;
+    const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    auto load_x = [&](int64_t r, float4 (&v)[2]) {
+#pragma unroll
+        for (int i = 0; i < 2; i++) {
+            const int q = lane + 32 * i;
+            v[i] = (r < n && q < d4) ? reinterpret_cast<const float4 *>(x + r * d)[q] : z4;
+        }
+    };
+    auto load_c = [&](int64_t r, int lab, float4 (&h)[2], float4 (&l)[2]) {
+#pragma unroll
+        for (int i = 0; i < 2; i++) {
+            const int q = lane + 32 * i;
+            const bool ok = r < n && q < d4;
+            h[i] = ok ? reinterpret_cast<const float4 *>(chi + (int64_t)lab * d)[q] : z4;
+            l[i] = ok ? reinterpret_cast<const float4 *>(clo + (int64_t)lab * d)[q] : z4;
+        }
+    };
+    float s = 0.f, comp = 0.f;  // this lane's compensated sum over all its rows
+    int64_t r = (int64_t)blockIdx.x * (RI_THREADS / 32) + w;
+    float4 xa[2], ha[2], la[2];
+    load_x(r, xa);
+    load_c(r, r < n ? labels[r] : 0, ha, la);
+    for (; r < n; r += nw) {
+        const int64_t rn = r + nw;
+        const int lbn = rn < n ? labels[rn] : 0;
+        float4 xb[2], hb[2], lb[2];
+        load_x(rn, xb);
+#pragma unroll
+        for (int i = 0; i < 2; i++) {
+            const float xs[4] = {xa[i].x, xa[i].y, xa[i].z, xa[i].w};
+            const float hs[4] = {ha[i].x, ha[i].y, ha[i].z, ha[i].w};
+            const float ls[4] = {la[i].x, la[i].y, la[i].z, la[i].w};
+#pragma unroll
+            for (int e = 0; e < 4; e++) {  // padding pieces are zero on both sides
+                const float t = __fsub_rn(__fsub_rn(xs[e], hs[e]), ls[e]);
+                const float y = __fsub_rn(__fmul_rn(t, t), comp);
+                const float u = __fadd_rn(s, y);
+                comp = __fsub_rn(__fsub_rn(u, s), y);
+                s = u;
+            }
+        }
+        load_c(rn, lbn, hb, lb);
+#pragma unroll
+        for (int i = 0; i < 2; i++) {
+            xa[i] = xb[i];
+            ha[i] = hb[i];
+            la[i] = lb[i];
+        }
+    }
+    // FP64 is slow on this part: lanes fold into f64 once, not per row
+    double acc = (double)s - (double)comp;
+#pragma unroll
+    for (int off = 16; off >= 1; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
+    if (lane == 0) wsum[w] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int q = 0; q < RI_THREADS / 32; q++) t += wsum[q];
+        block_part[blockIdx.x] = t;
+    }
+}
+
+__global__ void __launch_bounds__(RI_THREADS)
+    row_inertia_kernel(const float *__restrict__ x, int64_t n, int d, const int32_t *__restrict__ labels,
+                       const float *__restrict__ chi, const float *__restrict__ clo, double *__restrict__ block_part) {
+    __shared__ double wsum[RI_THREADS / 32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int64_t nw = (int64_t)gridDim.x * (RI_THREADS / 32);
+    float s = 0.f, comp = 0.f;  // this lane's compensated sum over all its rows
+    for (int64_t r = (int64_t)blockIdx.x * (RI_THREADS / 32) + w; r < n; r += nw) {
+        const int64_t cl = labels[r];
+        const float *xr = x + r * d, *ch = chi + cl * d, *cl2 = clo + cl * d;
+        for (int j = lane; j < d; j += 32) {
+            const float t = __fsub_rn(__fsub_rn(xr[j], ch[j]), cl2[j]);
+            const float y = __fsub_rn(__fmul_rn(t, t), comp);
+            const float u = __fadd_rn(s, y);
+            comp = __fsub_rn(__fsub_rn(u, s), y);
+            s = u;
+        }
+    }
+    double acc = (double)s - (double)comp;
+#pragma unroll
+    for (int off = 16; off >= 1; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
+    if (lane == 0) wsum[w] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int q = 0; q < RI_THREADS / 32; q++) t += wsum[q];
+        block_part[blockIdx.x] = t;
+    }
 }
 
 void launch_scan(int32_t *a, int64_t m, int32_t *tmp, cudaStream_t s) {
@@ -719,7 +1052,8 @@ size_t update_exact_scratch_bytes(int k, int d) { return sizeof(FixedPart) * (si
 
 void launch_update_centroids_exact(const SortPlan &p, const float *x, int d, const int32_t *members,
                                    const int32_t *seg_hist, const double *old_c, double *new_c, DevScalars *scalars,
-                                   const float *amax, double *inertia_part, void *scratch, cudaStream_t s) {
+                                   const float *amax, double *inertia_part, void *scratch, cudaStream_t s,
+                                   ExactState *state, long long *counts) {
     FixedPart *parts = (FixedPart *)scratch;
     FK_CUDA(cudaMemsetAsync(&scalars->shift_bits, 0, sizeof(unsigned long long), s));
     if (d == 0 || p.k == 0) return;
@@ -737,11 +1071,68 @@ void launch_update_centroids_exact(const SortPlan &p, const float *x, int d, con
     }
     FK_LAUNCH_CHECK();
     const int64_t kd = (int64_t)p.k * d;
-    centroid_fixed_combine_kernel<<<(unsigned)((kd + 255) / 256), 256, 0, s>>>(d, p.k, splits, p.n, seg_hist, p.nseg,
-                                                                               old_c, new_c, amax, parts, inertia_part);
+    centroid_fixed_combine_kernel<<<(unsigned)((kd + 255) / 256), 256, 0, s>>>(
+        d, p.k, splits, p.n, seg_hist, p.nseg, old_c, new_c, amax, parts, inertia_part, state, counts);
     FK_LAUNCH_CHECK();
     max_shift_kernel<double><<<(p.k + 127) / 128, 128, 0, s>>>(new_c, old_c, p.k, d, &scalars->shift_bits);
     FK_LAUNCH_CHECK();
+}
+
+bool incremental_shape_ok(const float *x, int d) {
+    return d > 0 && d % 4 == 0 && d / 4 <= FIX4_THREADS && ((uintptr_t)x & 15u) == 0;
+}
+
+void launch_update_centroids_incremental(Ctx &ctx, const float *x, int64_t n, int d, int k,
+                                         const int32_t *prev_labels, const int32_t *labels, const double *old_c,
+                                         double *new_c, DevScalars *scalars, const float *amax, ExactState *state,
+                                         long long *counts) {
+    cudaStream_t s = ctx.stream;
+    FK_CUDA(cudaMemsetAsync(&scalars->shift_bits, 0, sizeof(unsigned long long), s));
+    if (n == 0 || k == 0 || d == 0) return;
+    int4 *moved = (int4 *)ctx.get(BUF_MOVED, sizeof(int4) * (size_t)n);
+    uint32_t *ent = (uint32_t *)ctx.get(BUF_MOVED_ENT, sizeof(uint32_t) * 2 * (size_t)n);
+    // [0, k): per-cluster entry counts, scanned in place into offsets; then
+    // the scatter cursors; then the moved-row counter
+    const size_t kb = ((size_t)k * sizeof(int32_t) + 255) / 256 * 256;
+    char *ws = (char *)ctx.get(BUF_MOVED_HIST, 2 * kb + 256);
+    int32_t *hist = (int32_t *)ws, *cursor = (int32_t *)(ws + kb);
+    unsigned long long *moved_count = (unsigned long long *)(ws + 2 * kb);
+    const int64_t nb = (k + SCAN_TILE - 1) / SCAN_TILE;
+    int32_t *tmp = (int32_t *)ctx.get(BUF_MOVED_TMP, sizeof(int32_t) * (size_t)(nb + 1));
+    FK_CUDA(cudaMemsetAsync(ws, 0, 2 * kb + 256, s));
+    label_diff_kernel<<<(unsigned)((n + DIFF_THREADS - 1) / DIFF_THREADS), DIFF_THREADS, 0, s>>>(
+        prev_labels, labels, n, moved, moved_count, hist);
+    FK_LAUNCH_CHECK();
+    launch_scan(hist, k, tmp, s);
+    FK_CUDA(cudaMemcpyAsync(cursor, hist, sizeof(int32_t) * (size_t)k, cudaMemcpyDeviceToDevice, s));
+    moved_scatter_kernel<<<(unsigned)(ctx.num_sms * 8), 256, 0, s>>>(moved, moved_count, cursor, ent);
+    FK_LAUNCH_CHECK();
+    exact_delta4_kernel<<<(unsigned)k, FIX4_THREADS, 0, s>>>(x, d, k, n, hist, moved_count, ent, amax, state,
+                                                             counts);
+    FK_LAUNCH_CHECK();
+    const int64_t kd = (int64_t)k * d;
+    exact_means_kernel<<<(unsigned)((kd + 255) / 256), 256, 0, s>>>(d, k, n, state, counts, amax, old_c, new_c);
+    FK_LAUNCH_CHECK();
+    max_shift_kernel<double><<<(k + 127) / 128, 128, 0, s>>>(new_c, old_c, k, d, &scalars->shift_bits);
+    FK_LAUNCH_CHECK();
+}
+
+void launch_row_inertia(Ctx &ctx, const float *x, int64_t n, int d, const int32_t *labels, const double *c, int k,
+                        DevScalars *scalars) {
+    cudaStream_t s = ctx.stream;
+    const int64_t kd = (int64_t)k * d;
+    const int64_t kd4 = (kd + 3) / 4 * 4;  // the lo half starts 16-byte aligned
+    float *split = (float *)ctx.get(BUF_CSPLIT, sizeof(float) * 2 * (size_t)kd4 + 64);
+    split_centres_kernel<<<(unsigned)((kd + 255) / 256), 256, 0, s>>>(c, kd, split, split + kd4);
+    FK_LAUNCH_CHECK();
+    const int blocks = ctx.num_sms * 8;
+    double *part = (double *)ctx.get(BUF_RINERT, sizeof(double) * (size_t)blocks);
+    if (d % 4 == 0 && d <= 256 && ((uintptr_t)x & 15u) == 0)
+        row_inertia4_kernel<<<(unsigned)blocks, RI_THREADS, 0, s>>>(x, n, d, labels, split, split + kd4, part);
+    else
+        row_inertia_kernel<<<(unsigned)blocks, RI_THREADS, 0, s>>>(x, n, d, labels, split, split + kd4, part);
+    FK_LAUNCH_CHECK();
+    launch_mixed_inertia(ctx, part, blocks, scalars);
 }
 
 template void launch_update_centroids<double, double>(const SortPlan &, const double *, int, const int32_t *,

@@ -11,6 +11,8 @@ exact FP64 re-check.
    are the correctly rounded means of exact fixed-point sums, the oracle's
    sequential f64 sums can differ by a few ulp) and the same n_iter; the
    inertia (compensated f32 partials) within 1e-6 relative.
+4. Fits update the exact sums from the rows whose label changed; their
+   centres equal, bit for bit, full recomputations step by step.
 """
 import ctypes as C
 
@@ -344,3 +346,47 @@ def test_fit_into_device_outputs_matches_host_outputs():
     assert np.array_equal(l_out.cpu().numpy(), host.labels())
     assert dev.n_iter() == host.n_iter() == 3
     assert np.array_equal(dev.predict(x32), host.predict(x32))
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+@pytest.mark.parametrize("n,k", [(6000, 24), (20000, 5)])
+def test_incremental_exact_sums_equal_full_recompute(precision, n, k):
+    # after its first iteration a fit adds and removes only the rows whose
+    # label changed; tiny values (remainders below both grids, more than the
+    # per-block list holds when k is small) take the 128-bit path both ways
+    rng = np.random.default_rng(21 + k)
+    d = 32
+    cen = rng.uniform(-20, 20, size=(k, d))
+    x = cen[rng.integers(0, k, n)] + rng.normal(0, 4, size=(n, d))  # overlapping blobs: many moves
+    x[:, 3] = rng.normal(0, 1e-6, n)
+    x[::7, 5] *= 1e-7
+    x32 = x.astype(np.float32)
+    init = x32[rng.choice(n, k, replace=False)].astype(np.float64)
+    iters = 12
+    g = F.KMeans(k, dtype="f32x64").with_precision(precision).with_max_iter(iters).with_tol(0.0).with_n_init(1) \
+        .with_init_centers(init).fit(x32)
+    c = init
+    for _ in range(iters):
+        gl, c_next, gi, gs, rep = F.lloyd_step(x32, c, dtype="f32x64", precision=precision)
+        c = c_next
+    assert np.array_equal(g.cluster_centers(), c)
+    assert np.array_equal(g.labels(), gl)
+    assert abs(g.inertia() - gi) <= INERTIA_RTOL_MIXED * gi
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+def test_incremental_fit_with_tolerance_and_runs_matches_oracle(precision):
+    # n_init runs, each converging at its own iteration (the queued successor
+    # of the converged iteration is discarded), against the FP64 oracle
+    rng = np.random.default_rng(8)
+    n, d, k = 8000, 16, 12
+    cen = rng.uniform(-10, 10, size=(k, d))
+    x32 = (cen[rng.integers(0, k, n)] + rng.normal(0, 2, size=(n, d))).astype(np.float32)
+    inits = np.stack([x32[rng.choice(n, k, replace=False)] for _ in range(3)]).astype(np.float64)
+    g = F.KMeans(k, dtype="f32x64").with_precision(precision).with_max_iter(60).with_tol(1e-3).with_n_init(3) \
+        .with_init_centers(inits).fit(x32)
+    o = O.fit(x32.astype(np.float64), k, max_iter=60, tol=1e-3, n_init=3, init=inits)
+    assert np.array_equal(g.labels(), o["labels"])
+    assert _close(g.cluster_centers(), o["centers"])
+    assert g.n_iter() == o["n_iter"]
+    assert abs(g.inertia() - o["inertia"]) <= INERTIA_RTOL_MIXED * o["inertia"]
