@@ -60,6 +60,7 @@ struct DevScalars {
     unsigned long long full_count;  // number of rows queued for a full re-scan
     unsigned long long quad_count;  // second pass: rows with 2 to 8 candidates
     unsigned long long ex_count;    // second pass: rows with more than 4 candidates
+    unsigned long long f64_count;   // rows whose remaining candidates are scored in FP64
     unsigned long long error_word;  // nonzero: a bounded device wait gave up
 };
 
@@ -132,7 +133,7 @@ enum BufSlot {
     BUF_XB, BUF_XNORM, BUF_CB, BUF_CAUX, BUF_TOP2, BUF_FLAGS, BUF_FULL, BUF_CF32, BUF_CF32C, BUF_FIXPART,
     BUF_XB2, BUF_TOP8, BUF_OCT, BUF_EX, BUF_XAUG, BUF_ROWSCALE, BUF_ROWINFO2, BUF_STATS2, BUF_CB2, BUF_CAUG2,
     BUF_HALF2, BUF_INERTIA2, BUF_C2, BUF_XSTATE, BUF_XCOUNTS, BUF_MOVED, BUF_MOVED_ENT, BUF_MOVED_HIST, BUF_MOVED_TMP,
-    BUF_CSPLIT, BUF_RINERT,
+    BUF_CSPLIT, BUF_RINERT, BUF_F64ITEMS,
     BUF_BX, BUF_BFITS, BUF_BSTATE, BUF_BITEMS, BUF_BPART, BUF_BORDER, BUF_BCTR, BUF_BLAB, BUF_BMEM, BUF_BCEN, BUF_BND, BUF_BXOFF,
     BUF_COUNT
 };

@@ -693,6 +693,30 @@ __global__ void __launch_bounds__(FINALIZE_THREADS)
 }
 
 // ------------------------------------------------------------ re-checks --
+// A row and at most eight candidate centres (second-pass rows, and the rows
+// whose candidates are left to FP64).
+struct alignas(16) Oct {
+    int row, m;
+    int ids[8];
+    int pad0, pad1;
+};
+
+// Queues a row for the FP64 decision among its m candidates (lane 0 of the
+// calling warp appends; any lane may pass the ids).
+__device__ __forceinline__ void queue_f64(Oct *__restrict__ items, DevScalars *sc, int row, int m,
+                                          const int (&ids)[8]) {
+    if ((threadIdx.x & 31) == 0) {
+        const unsigned long long slot = atomicAdd(&sc->f64_count, 1ULL);
+        Oct o;
+        o.row = row;
+        o.m = m;
+#pragma unroll
+        for (int j = 0; j < 8; j++) o.ids[j] = ids[j];
+        o.pad0 = o.pad1 = 0;
+        items[slot] = o;
+    }
+}
+
 // FP64 direct form in the oracle's order (x widened exactly, one running
 // sum over increasing j). Kept register-light: it runs inside kernels whose
 // FP32 paths need the occupancy.
@@ -727,11 +751,17 @@ __device__ __forceinline__ float sqeuc32(const float *__restrict__ x, const floa
 
 // Upper bound, in f32 with upward rounding, of |d32 - D| + |D64 - D| where D
 // is the exact real distance and D64 the oracle's FP64 direct form:
-// ((d+4) 2^-23 d32 + 2 sqrt(d32) ec + 3 ec^2) * 1.01.
+// ((d+4) 2^-23 d32 + 2 sqrt(d32) ec + 3 ec^2) * 1.01. 2 sqrt(d32) is bounded
+// by d32 / s + s >= 2 sqrt(d32) (any s > 0; with s the power of two 2^(E/2),
+// 2^E <= d32, it exceeds 2 sqrt(d32) by at most 25%): two directed-rounding
+// operations instead of a correctly rounded square root.
 __device__ __forceinline__ float bound32(float d32, float ec, int d) {
     const float dd = d32 > 0.f ? d32 : 0.f;
+    const int h = ((int)((__float_as_uint(dd) >> 23) & 0xFFu) - 127) >> 1;  // floor(E / 2), -64..64
+    const float sq2 = dd > 0.f ? __fadd_ru(__fmul_ru(dd, __int_as_float((127 - h) << 23)), __int_as_float((h + 127) << 23))
+                               : 0.f;
     float e = __fmul_ru((float)(d + 4) * 1.1920929e-07f, dd);
-    e = __fadd_ru(e, __fmul_ru(__fmul_ru(2.0f, __fsqrt_ru(dd)), ec));
+    e = __fadd_ru(e, __fmul_ru(sq2, ec));
     e = __fadd_ru(e, __fmul_ru(3.0f, __fmul_ru(ec, ec)));
     return __fadd_ru(__fmul_ru(e, 1.01f), 1e-30f);
 }
@@ -748,7 +778,8 @@ __device__ __forceinline__ bool below(float da, float ea, float db, float eb) {
 template <typename TX>
 __global__ void pair_rescore_kernel(const TX *__restrict__ x, int d, const double *__restrict__ c,
                                     const float *__restrict__ c32, const float *__restrict__ ec32,
-                                    const int4 *__restrict__ list, DevScalars *sc, int32_t *__restrict__ labels) {
+                                    const int4 *__restrict__ list, DevScalars *sc, int32_t *__restrict__ labels,
+                                    Oct *__restrict__ f64_items) {
     const unsigned long long cnt = sc->flag_count;
     const int lane = threadIdx.x & 31;
     const unsigned long long wid = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -773,17 +804,74 @@ __global__ void pair_rescore_kernel(const TX *__restrict__ x, int d, const doubl
                 continue;
             }
         }
-        double dv = 0.0;
-        if (lane < 2) dv = sqeuc64(row, c + (int64_t)(lane == 0 ? a : b) * d, d);
-        const double da = __shfl_sync(0xffffffffu, dv, 0), db = __shfl_sync(0xffffffffu, dv, 1);
-        if (lane == 0) {
-            int best = 0;
-            double bd = DBL_MAX;
-            if (da < bd) { bd = da; best = a; }
-            if (db < bd) { bd = db; best = b; }
-            labels[e.x] = best;
-            atomicAdd(&sc->recheck_rows, 1ULL);
-            if (near_tie(da, db)) atomicAdd(&sc->near_tie_rows, 1ULL);
+        const int ids[8] = {a, b, 0, 0, 0, 0, 0, 0};
+        queue_f64(f64_items, sc, e.x, 2, ids);
+    }
+}
+
+// pair_rescore_kernel for f32 rows with d % 4 == 0 and d <= 128: the same
+// decisions, software-pipelined -- the list entry two rows ahead and the
+// feature and centre pieces one row ahead load while this row is decided.
+// Lanes 0-15 hold centre a, lanes 16-31 centre b, 16-byte pieces hl, hl + 16.
+__global__ void __launch_bounds__(256)
+    pair_rescore4_kernel(const float *__restrict__ x, int d, const double *__restrict__ c,
+                         const float *__restrict__ c32, const float *__restrict__ ec32,
+                         const int4 *__restrict__ list, DevScalars *sc, int32_t *__restrict__ labels,
+                         Oct *__restrict__ f64_items) {
+    const unsigned long long cnt = sc->flag_count;
+    const int lane = threadIdx.x & 31, hl = lane & 15;
+    const unsigned long long nw = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
+    const int d4 = d >> 2;
+    const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    auto entry = [&](unsigned long long q) { return q < cnt ? list[q] : make_int4(-1, 0, 0, 0); };
+    auto pieces = [&](const int4 &e, float4 (&xv)[2], float4 (&cv)[2]) {
+        const int a = min(e.y, e.z), b = max(e.y, e.z);
+#pragma unroll
+        for (int i = 0; i < 2; i++) {
+            const int q = hl + 16 * i;
+            const bool ok = e.x >= 0 && q < d4;
+            xv[i] = ok ? reinterpret_cast<const float4 *>(x + (int64_t)e.x * d)[q] : z4;
+            cv[i] = ok ? reinterpret_cast<const float4 *>(c32 + (int64_t)(lane < 16 ? a : b) * d)[q] : z4;
+        }
+    };
+    unsigned long long s = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int4 e0 = entry(s), e1 = entry(s + nw);
+    float4 xa[2], ca[2];
+    pieces(e0, xa, ca);
+    for (; s < cnt; s += nw) {
+        const int4 e2 = entry(s + 2 * nw);
+        float4 xb[2], cb[2];
+        pieces(e1, xb, cb);
+        float acc = 0.f;  // padding pieces are zero on both sides
+#pragma unroll
+        for (int i = 0; i < 2; i++) {
+            float t = xa[i].x - ca[i].x;
+            acc = fmaf(t, t, acc);
+            t = xa[i].y - ca[i].y;
+            acc = fmaf(t, t, acc);
+            t = xa[i].z - ca[i].z;
+            acc = fmaf(t, t, acc);
+            t = xa[i].w - ca[i].w;
+            acc = fmaf(t, t, acc);
+        }
+        acc = half_warp_sum_f(acc);
+        const float sa = __shfl_sync(0xffffffffu, acc, 0), sb = __shfl_sync(0xffffffffu, acc, 16);
+        const int a = min(e0.y, e0.z), b = max(e0.y, e0.z);
+        const float ea = bound32(sa, ec32[a], d), eb = bound32(sb, ec32[b], d);
+        if (below(sa, ea, sb, eb)) {
+            if (lane == 0) labels[e0.x] = a;
+        } else if (below(sb, eb, sa, ea)) {
+            if (lane == 0) labels[e0.x] = b;
+        } else {
+            const int ids[8] = {a, b, 0, 0, 0, 0, 0, 0};
+            queue_f64(f64_items, sc, e0.x, 2, ids);
+        }
+        e0 = e1;
+        e1 = e2;
+#pragma unroll
+        for (int i = 0; i < 2; i++) {
+            xa[i] = xb[i];
+            ca[i] = cb[i];
         }
     }
 }
@@ -991,11 +1079,6 @@ size_t exhaustive_smem_bytes(int d, int k) {
 // eight) centres inside the second pass's bound are re-scored. Slot s of the
 // second pass holds row list[s]; its row data (rowinfo2) and statistics
 // (stats2) are its own.
-struct Oct {
-    int row, m;
-    int ids[8];
-    int pad0, pad1;
-};
 
 __device__ __forceinline__ uint32_t ins8u(uint32_t (&R)[8], int (&I)[8], uint32_t w, int j) {
 #pragma unroll
@@ -1076,60 +1159,107 @@ __global__ void finalize8_kernel(const Top8 *__restrict__ parts, int nparts, int
 // the features) with rigorous bounds; the candidates whose lower bound
 // reaches the smallest upper bound are scored exactly in FP64 (one lane
 // each, direct form), lowest index on ties.
-__global__ void oct_rescore_kernel(const float *__restrict__ x, int d, const double *__restrict__ c,
-                                   const float *__restrict__ c32, const float *__restrict__ ec32,
-                                   const Oct *__restrict__ octs, DevScalars *sc, int32_t *__restrict__ labels) {
+// Decides one row with at most eight candidates from acc, this lane's part of
+// the FP32 distance to candidate lane >> 2 (four lanes per candidate).
+__device__ __forceinline__ void oct_decide(const Oct &qd, float acc, int d, const float *__restrict__ ec32,
+                                           DevScalars *sc, int32_t *__restrict__ labels, Oct *__restrict__ f64_items) {
+    const int lane = threadIdx.x & 31;
+    acc += __shfl_xor_sync(0xffffffffu, acc, 2);
+    acc += __shfl_xor_sync(0xffffffffu, acc, 1);
+    // lane j < m holds candidate j: its distance, bound and interval
+    const bool cand = lane < qd.m;
+    int my_id = INT32_MAX;
+#pragma unroll
+    for (int j = 0; j < 8; j++)  // qd.ids[lane] without indexing a register array
+        if (cand && j == lane) my_id = qd.ids[j];
+    const float my_dist = __shfl_sync(0xffffffffu, acc, (4 * lane) & 31);
+    const float my_err = cand ? bound32(my_dist, ec32[my_id], d) : 0.f;
+    float ub = cand ? __fadd_ru(my_dist, my_err) : INFINITY;
+#pragma unroll
+    for (int off = 4; off >= 1; off >>= 1) ub = fminf(ub, __shfl_xor_sync(0xffffffffu, ub, off));
+    ub = __shfl_sync(0xffffffffu, ub, 0);  // the minimum over lanes 0-7 (NaN values never lower it)
+    const unsigned surv = __ballot_sync(0xffffffffu, cand && !(__fsub_rd(my_dist, my_err) > ub));
+    const int nsurv = __popc(surv);
+    if (nsurv == 1) {
+        const int only = __shfl_sync(0xffffffffu, my_id, __ffs(surv) - 1);
+        if (lane == 0) labels[qd.row] = only;
+        return;
+    }
+    // the survivors (all candidates if no FP32 value was finite) go to FP64
+    const unsigned take = nsurv == 0 ? __ballot_sync(0xffffffffu, cand) : surv;
+    int ids[8];
+    int m = 0;
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+        const int idj = __shfl_sync(0xffffffffu, my_id, j);
+        ids[j] = 0;
+        if ((take >> j) & 1u) ids[m++] = idj;  // any order: ties go to the lowest index
+    }
+    queue_f64(f64_items, sc, qd.row, m, ids);
+}
+
+__global__ void oct_rescore_kernel(const float *__restrict__ x, int d, const float *__restrict__ c32,
+                                   const float *__restrict__ ec32, const Oct *__restrict__ octs, DevScalars *sc,
+                                   int32_t *__restrict__ labels, Oct *__restrict__ f64_items) {
     const unsigned long long cnt = sc->quad_count;
     const int lane = threadIdx.x & 31;
     const unsigned long long wid = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const unsigned long long nw = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
     for (unsigned long long s = wid; s < cnt; s += nw) {
         const Oct qd = octs[s];
-        const float *row = x + (int64_t)qd.row * d;
-        float dist[8], err[8];
-        float ub = INFINITY;
-        {  // candidate lane >> 2 scored by four lanes at once
-            const int cj = lane >> 2;
-            float acc = 0.f;
-            if (cj < qd.m) acc = sq_partial(row, c32 + (int64_t)qd.ids[cj] * d, d, lane & 3, 4);
-            acc += __shfl_xor_sync(0xffffffffu, acc, 2);
-            acc += __shfl_xor_sync(0xffffffffu, acc, 1);
+        const int cj = lane >> 2;  // candidate cj scored by four lanes at once
+        int cid = 0;
 #pragma unroll
-            for (int j = 0; j < 8; j++) dist[j] = __shfl_sync(0xffffffffu, acc, 4 * j);
-        }
-#pragma unroll
-        for (int j = 0; j < 8; j++) {
-            err[j] = j < qd.m ? bound32(dist[j], ec32[qd.ids[j]], d) : 0.f;
-            if (j < qd.m) ub = fminf(ub, __fadd_ru(dist[j], err[j]));
-        }
-        int nsurv = 0, only = -1;
-        float my_dist = 0.f, my_err = 0.f;
+        for (int j = 0; j < 8; j++)
+            if (j == cj) cid = qd.ids[j];
+        float acc = 0.f;
+        if (cj < qd.m) acc = sq_partial(x + (int64_t)qd.row * d, c32 + (int64_t)cid * d, d, lane & 3, 4);
+        oct_decide(qd, acc, d, ec32, sc, labels, f64_items);
+    }
+}
+
+// The FP64 decisions: one warp per queued row stages the widened row and its
+// candidate centres (rows padded by one double) in shared memory, then lane
+// j < m sums candidate j in the oracle's order (sqeuc64's arithmetic from
+// shared memory, so the dependent FP64 additions are the only wait); the
+// lowest distance below F::MAX wins, the lowest index on ties, else label 0,
+// exactly as nearest_center.
+constexpr int F64_WARPS = 4;
+size_t f64_smem_bytes(int d) { return sizeof(double) * (size_t)F64_WARPS * ((size_t)d + 8 * ((size_t)d + 1)); }
+
+template <typename TX>
+__global__ void __launch_bounds__(F64_WARPS * 32)
+    f64_decide_kernel(const TX *__restrict__ x, int d, const double *__restrict__ c, const Oct *__restrict__ items,
+                      DevScalars *sc, int32_t *__restrict__ labels) {
+    extern __shared__ double f64_smem[];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    double *xs = f64_smem + (size_t)w * ((size_t)d + 8 * ((size_t)d + 1)), *cs = xs + d;
+    const unsigned long long cnt = sc->f64_count;
+    const unsigned long long nw = (unsigned long long)gridDim.x * F64_WARPS;
+    for (unsigned long long q = (unsigned long long)blockIdx.x * F64_WARPS + w; q < cnt; q += nw) {
+        const Oct it = items[q];
+        for (int j = lane; j < d; j += 32) xs[j] = (double)x[(int64_t)it.row * d + j];
         int my_id = INT32_MAX;
 #pragma unroll
-        for (int j = 0; j < 8; j++) {
-            if (j < qd.m && !(__fsub_rd(dist[j], err[j]) > ub)) {
-                nsurv++;
-                only = qd.ids[j];
-            }
-            if (j == lane) {
-                my_dist = dist[j];
-                my_err = err[j];
-                my_id = qd.ids[j];
+        for (int t = 0; t < 8; t++) {
+            if (t < it.m) {
+                for (int j = lane; j < d; j += 32) cs[(size_t)t * (d + 1) + j] = c[(int64_t)it.ids[t] * d + j];
+                if (t == lane) my_id = it.ids[t];
             }
         }
-        if (nsurv == 1) {
-            if (lane == 0) labels[qd.row] = only;
-            continue;
-        }
-        // FP64 on the survivors (or on all candidates if some FP32 value was not finite)
+        __syncwarp();
         double v = DBL_MAX;
         int id = INT32_MAX;
-        if (lane < qd.m) {
-            const bool surv = nsurv == 0 || !(__fsub_rd(my_dist, my_err) > ub);
-            if (surv) {
+        if (lane < it.m) {
+            const double *cr = cs + (size_t)lane * (d + 1);
+            double acc = 0.0;
+            for (int j = 0; j < d; j++) {
+                const double t = __dsub_rn(xs[j], cr[j]);
+                acc = __dadd_rn(acc, __dmul_rn(t, t));
+            }
+            if (acc < DBL_MAX) {  // not below F::MAX (or NaN): never chosen
+                v = acc;
                 id = my_id;
-                v = sqeuc64(row, c + (int64_t)id * d, d);
-                if (!(v < DBL_MAX)) id = INT32_MAX;  // not below F::MAX: never chosen
             }
         }
         double b2 = DBL_MAX;
@@ -1147,11 +1277,22 @@ __global__ void oct_rescore_kernel(const float *__restrict__ x, int d, const dou
             }
         }
         if (lane == 0) {
-            labels[qd.row] = id == INT32_MAX ? 0 : id;
+            labels[it.row] = id == INT32_MAX ? 0 : id;
             atomicAdd(&sc->recheck_rows, 1ULL);
             if (id != INT32_MAX && b2 < DBL_MAX && near_tie(v, b2)) atomicAdd(&sc->near_tie_rows, 1ULL);
         }
+        __syncwarp();  // the staging area is reused for the next row
     }
+}
+
+template <typename TX>
+void launch_f64_decide(Ctx &ctx, const TX *x, int d, const double *c, const Oct *items, DevScalars *sc,
+                       int32_t *labels) {
+    const size_t smem = f64_smem_bytes(d);
+    FK_CUDA(cudaFuncSetAttribute((const void *)f64_decide_kernel<TX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem));
+    f64_decide_kernel<TX><<<ctx.num_sms * 2, F64_WARPS * 32, smem, ctx.stream>>>(x, d, c, items, sc, labels);
+    FK_LAUNCH_CHECK();
 }
 
 // ---------------------------------------------------- mixed inertia --
@@ -1304,7 +1445,7 @@ float mu_norm_up(double v) {
 // operands made from their f32 values, a top-8 tensor pass, then the
 // re-score of at most eight candidates, or of every centre.
 void second_pass(Ctx &ctx, const float *x, int64_t n, int d, const double *c, int k, const MixedBufs &B,
-                 double mu_norm, const int32_t *full, int32_t *labels, DevScalars *sc) {
+                 double mu_norm, const int32_t *full, int32_t *labels, DevScalars *sc, Oct *f64_items) {
     cudaStream_t s = ctx.stream;
     MixedPlan &m2 = ctx.mixed2;
     if (m2.n != n || m2.d != d || m2.k != k) plan_tc(ctx, m2, n, d, k, false, 8);
@@ -1330,7 +1471,7 @@ void second_pass(Ctx &ctx, const float *x, int64_t n, int d, const double *c, in
     finalize8_kernel<<<grid, 256, 0, s>>>(top8, m2.parts, n, k, d, full, ri2, st2, acc_rel2, mu_norm_up(mu_norm),
                                           labels, octs, ex, sc);
     FK_LAUNCH_CHECK();
-    oct_rescore_kernel<<<grid, 256, 0, s>>>(x, d, c, B.c32, B.ec32, octs, sc, labels);
+    oct_rescore_kernel<<<grid, 256, 0, s>>>(x, d, B.c32, B.ec32, octs, sc, labels, f64_items);
     FK_LAUNCH_CHECK();
     exhaustive_rescore_kernel<<<ctx.num_sms * 2, EX_THREADS, exhaustive_smem_bytes(d, k), s>>>(
         x, d, c, B.c32t, B.ec32, k, ex, &sc->ex_count, sc, labels);
@@ -1378,14 +1519,20 @@ void run_assign_mixed(Ctx &ctx, const TX *x, int64_t n, int d, const double *c, 
         top, mp.parts, n, k, d, B.rowinfo, B.stats, acc_rel, mu_norm_up(mp.mu_norm), labels, pairs, full, sc);
     FK_LAUNCH_CHECK();
     const int grid = ctx.num_sms * 4;
-    pair_rescore_kernel<TX><<<grid, 256, 0, s>>>(x, d, c, B.c32, B.ec32, pairs, sc, labels);
+    Oct *f64_items = (Oct *)ctx.get(BUF_F64ITEMS, sizeof(Oct) * (size_t)n);
+    if (std::is_same<TX, float>::value && d % 4 == 0 && d <= 128 && ((uintptr_t)x & 15u) == 0)
+        pair_rescore4_kernel<<<grid, 256, 0, s>>>((const float *)x, d, c, B.c32, B.ec32, pairs, sc, labels,
+                                                  f64_items);
+    else
+        pair_rescore_kernel<TX><<<grid, 256, 0, s>>>(x, d, c, B.c32, B.ec32, pairs, sc, labels, f64_items);
     FK_LAUNCH_CHECK();
     if constexpr (std::is_same<TX, float>::value) {
-        second_pass(ctx, x, n, d, c, k, B, mp.mu_norm, full, labels, sc);
+        second_pass(ctx, x, n, d, c, k, B, mp.mu_norm, full, labels, sc, f64_items);
     } else {
         full_rescore_kernel<TX><<<grid, 256, 0, s>>>(x, d, c, B.c32, B.ec32, k, full, &sc->full_count, sc, labels);
         FK_LAUNCH_CHECK();
     }
+    launch_f64_decide<TX>(ctx, x, d, c, f64_items, sc, labels);
 }
 
 void launch_mixed_inertia(Ctx &ctx, const double *part, int64_t m, DevScalars *sc) {

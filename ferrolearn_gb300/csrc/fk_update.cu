@@ -642,6 +642,34 @@ template <> struct ShiftBits<float> {
     }
 };
 
+// One warp per cluster: the lanes form the squares (x - y)^2 of the features
+// in parallel (coalesced loads) into shared memory, then one lane adds them
+// in feature order -- the same left fold as the one-thread form below.
+constexpr int SHIFT_THREADS = 256;
+
+template <typename TC>
+__global__ void __launch_bounds__(SHIFT_THREADS)
+    max_shift_warp_kernel(const TC *__restrict__ new_c, const TC *__restrict__ old_c, int k, int d,
+                          unsigned long long *shift_bits) {
+    using A = UArith<TC>;
+    extern __shared__ unsigned char shift_smem[];
+    TC *sq = reinterpret_cast<TC *>(shift_smem) + (size_t)(threadIdx.x >> 5) * d;
+    const int lane = threadIdx.x & 31;
+    const int c = blockIdx.x * (SHIFT_THREADS / 32) + (threadIdx.x >> 5);
+    if (c >= k) return;  // warp-uniform; no block barrier below
+    for (int j = lane; j < d; j += 32) {
+        const TC t = A::sub(new_c[(int64_t)c * d + j], old_c[(int64_t)c * d + j]);
+        sq[j] = A::mul(t, t);
+    }
+    __syncwarp();
+    if (lane == 0) {
+        TC acc = TC(0);
+        for (int j = 0; j < d; j++) acc = A::add(acc, sq[j]);
+        if (acc > TC(0)) atomicMax(shift_bits, ShiftBits<TC>::bits(acc));
+    }
+}
+
+
 template <typename TC>
 __global__ void max_shift_kernel(const TC *__restrict__ new_c, const TC *__restrict__ old_c, int k, int d,
                                  unsigned long long *shift_bits) {
@@ -654,6 +682,18 @@ __global__ void max_shift_kernel(const TC *__restrict__ new_c, const TC *__restr
         acc = A::add(acc, A::mul(t, t));
     }
     if (acc > TC(0)) atomicMax(shift_bits, ShiftBits<TC>::bits(acc));
+}
+
+template <typename TC>
+void launch_max_shift(const TC *new_c, const TC *old_c, int k, int d, unsigned long long *shift_bits, cudaStream_t s) {
+    const size_t smem = sizeof(TC) * (size_t)d * (SHIFT_THREADS / 32);
+    if (smem <= 48 * 1024) {
+        max_shift_warp_kernel<TC><<<(k + SHIFT_THREADS / 32 - 1) / (SHIFT_THREADS / 32), SHIFT_THREADS, smem, s>>>(
+            new_c, old_c, k, d, shift_bits);
+    } else {
+        max_shift_kernel<TC><<<(k + 127) / 128, 128, 0, s>>>(new_c, old_c, k, d, shift_bits);
+    }
+    FK_LAUNCH_CHECK();
 }
 
 // ------------------------------------------------ incremental exact sums --
@@ -1044,8 +1084,7 @@ void launch_update_centroids(const SortPlan &p, const TX *x, int d, const int32_
         centroid_sum_kernel<TX, TC, false><<<grid, threads, 0, s>>>(x, d, p.k, p.n, members, seg_hist, p.nseg, old_c,
                                                                     new_c, nullptr);
     FK_LAUNCH_CHECK();
-    max_shift_kernel<TC><<<(p.k + 127) / 128, 128, 0, s>>>(new_c, old_c, p.k, d, &scalars->shift_bits);
-    FK_LAUNCH_CHECK();
+    launch_max_shift<TC>(new_c, old_c, p.k, d, &scalars->shift_bits, s);
 }
 
 size_t update_exact_scratch_bytes(int k, int d) { return sizeof(FixedPart) * (size_t)k * FIX_SPLIT * d; }
@@ -1074,8 +1113,7 @@ void launch_update_centroids_exact(const SortPlan &p, const float *x, int d, con
     centroid_fixed_combine_kernel<<<(unsigned)((kd + 255) / 256), 256, 0, s>>>(
         d, p.k, splits, p.n, seg_hist, p.nseg, old_c, new_c, amax, parts, inertia_part, state, counts);
     FK_LAUNCH_CHECK();
-    max_shift_kernel<double><<<(p.k + 127) / 128, 128, 0, s>>>(new_c, old_c, p.k, d, &scalars->shift_bits);
-    FK_LAUNCH_CHECK();
+    launch_max_shift<double>(new_c, old_c, p.k, d, &scalars->shift_bits, s);
 }
 
 bool incremental_shape_ok(const float *x, int d) {
@@ -1113,8 +1151,7 @@ void launch_update_centroids_incremental(Ctx &ctx, const float *x, int64_t n, in
     const int64_t kd = (int64_t)k * d;
     exact_means_kernel<<<(unsigned)((kd + 255) / 256), 256, 0, s>>>(d, k, n, state, counts, amax, old_c, new_c);
     FK_LAUNCH_CHECK();
-    max_shift_kernel<double><<<(k + 127) / 128, 128, 0, s>>>(new_c, old_c, k, d, &scalars->shift_bits);
-    FK_LAUNCH_CHECK();
+    launch_max_shift<double>(new_c, old_c, k, d, &scalars->shift_bits, s);
 }
 
 void launch_row_inertia(Ctx &ctx, const float *x, int64_t n, int d, const int32_t *labels, const double *c, int k,
