@@ -54,7 +54,8 @@ import numpy as np  # noqa: E402
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=None,
+                    help="timed Lloyd iterations (default: the workload's own count, 50 for anisotropic)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--form", default="auto", choices=["auto", "bf16", "fp8", "fp32", "fp64"])
@@ -63,7 +64,10 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
-    return ap.parse_args()
+    args = ap.parse_args()
+    if args.steps is None:  # the configurations' own iteration counts (anisotropic: 50 Lloyd iterations)
+        args.steps = {"anisotropic": 50, "bisector": 20, "dirichlet": 20, "batched": 20}[args.workload]
+    return args
 
 
 METRIC = "KMeans Lloyd iters/s & pt·k/s: BF16+FP64 recheck vs plain FP32, labels=FP64"

@@ -706,25 +706,42 @@ void launch_max_shift(const TC *new_c, const TC *old_c, int k, int d, unsigned l
 // finite and the two grids apply (the full pass handles the rest).
 
 constexpr int DIFF_THREADS = 512;
+constexpr int DIFF_ROWS = 4;  // rows per thread (16-byte loads of both label arrays)
 
 // Rows whose label differs between two assignments, appended as (row, old,
 // new) with one atomic per block; hist counts the entries per cluster (one
-// for the old cluster, one for the new).
+// for the old cluster, one for the new). Thread t of a block takes the rows
+// 4 t .. 4 t + 3 of the block's 2048.
 __global__ void __launch_bounds__(DIFF_THREADS)
     label_diff_kernel(const int32_t *__restrict__ prev, const int32_t *__restrict__ cur, int64_t n,
                       int4 *__restrict__ moved, unsigned long long *moved_count, int32_t *__restrict__ hist) {
     __shared__ unsigned int wcnt[DIFF_THREADS / 32];
     __shared__ unsigned long long base;
-    const int64_t i = (int64_t)blockIdx.x * DIFF_THREADS + threadIdx.x;
-    int o = 0, nw = 0;
-    if (i < n) {
-        o = prev[i];
-        nw = cur[i];
+    const int64_t i0 = ((int64_t)blockIdx.x * DIFF_THREADS + threadIdx.x) * DIFF_ROWS;
+    int o[DIFF_ROWS] = {0, 0, 0, 0}, nw[DIFF_ROWS] = {0, 0, 0, 0};
+    const bool vec = (((uintptr_t)prev | (uintptr_t)cur) & 15u) == 0;  // i0 % 4 == 0: aligned pieces
+    if (vec && i0 + DIFF_ROWS <= n) {
+        const int4 a = *reinterpret_cast<const int4 *>(prev + i0), b = *reinterpret_cast<const int4 *>(cur + i0);
+        o[0] = a.x; o[1] = a.y; o[2] = a.z; o[3] = a.w;
+        nw[0] = b.x; nw[1] = b.y; nw[2] = b.z; nw[3] = b.w;
+    } else {
+        for (int r = 0; r < DIFF_ROWS; r++)
+            if (i0 + r < n) {
+                o[r] = prev[i0 + r];
+                nw[r] = cur[i0 + r];
+            }
     }
-    const bool ch = i < n && o != nw;
+    unsigned mine = 0;
+#pragma unroll
+    for (int r = 0; r < DIFF_ROWS; r++) mine += (i0 + r < n && o[r] != nw[r]) ? 1u : 0u;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const unsigned m = __ballot_sync(0xffffffffu, ch);
-    if (lane == 0) wcnt[w] = (unsigned)__popc(m);
+    unsigned incl = mine;  // inclusive prefix over the warp
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const unsigned v = __shfl_up_sync(0xffffffffu, incl, off);
+        if (lane >= off) incl += v;
+    }
+    if (lane == 31) wcnt[w] = incl;
     __syncthreads();
     if (threadIdx.x == 0) {
         unsigned t = 0;
@@ -736,11 +753,16 @@ __global__ void __launch_bounds__(DIFF_THREADS)
         base = t ? atomicAdd(moved_count, (unsigned long long)t) : 0ull;
     }
     __syncthreads();
-    if (ch) {
-        const unsigned long long slot = base + wcnt[w] + (unsigned)__popc(m & ((1u << lane) - 1u));
-        moved[slot] = make_int4((int)i, o, nw, 0);
-        atomicAdd(&hist[nw], 1);
-        atomicAdd(&hist[o], 1);
+    if (mine) {
+        unsigned long long slot = base + wcnt[w] + (incl - mine);
+#pragma unroll
+        for (int r = 0; r < DIFF_ROWS; r++) {
+            if (i0 + r < n && o[r] != nw[r]) {
+                moved[slot++] = make_int4((int)(i0 + r), o[r], nw[r], 0);
+                atomicAdd(&hist[nw[r]], 1);
+                atomicAdd(&hist[o[r]], 1);
+            }
+        }
     }
 }
 
@@ -798,11 +820,18 @@ __global__ void __launch_bounds__(FIX4_THREADS, 3) exact_delta4_kernel(
         for (int t = threadIdx.x; t < cnt; t += FIX4_THREADS) sent[t] = ent[cb + t];
         __syncthreads();
         if (!active) continue;
+        uint32_t e_nxt = g < cnt ? sent[g] : 0u;
+        float4 v_nxt = g < cnt ? reinterpret_cast<const float4 *>(x + (int64_t)(e_nxt >> 1) * d)[sl]
+                               : make_float4(0.f, 0.f, 0.f, 0.f);
         for (int r = g; r < cnt; r += G) {
-            const uint32_t e = sent[r];
+            const uint32_t e = e_nxt;
+            const float4 v = v_nxt;
+            if (r + G < cnt) {  // the next row of this thread loads while this one is split
+                e_nxt = sent[r + G];
+                v_nxt = reinterpret_cast<const float4 *>(x + (int64_t)(e_nxt >> 1) * d)[sl];
+            }
             const bool neg = (e & 1u) != 0u;
             if (sl == 0) my_delta += neg ? -1 : 1;
-            const float4 v = reinterpret_cast<const float4 *>(x + (int64_t)(e >> 1) * d)[sl];
             const float ev[4] = {v.x, v.y, v.z, v.w};
 #pragma unroll
             for (int f = 0; f < 4; f++) {
@@ -1138,7 +1167,8 @@ void launch_update_centroids_incremental(Ctx &ctx, const float *x, int64_t n, in
     const int64_t nb = (k + SCAN_TILE - 1) / SCAN_TILE;
     int32_t *tmp = (int32_t *)ctx.get(BUF_MOVED_TMP, sizeof(int32_t) * (size_t)(nb + 1));
     FK_CUDA(cudaMemsetAsync(ws, 0, 2 * kb + 256, s));
-    label_diff_kernel<<<(unsigned)((n + DIFF_THREADS - 1) / DIFF_THREADS), DIFF_THREADS, 0, s>>>(
+    label_diff_kernel<<<(unsigned)((n + DIFF_THREADS * DIFF_ROWS - 1) / (DIFF_THREADS * DIFF_ROWS)), DIFF_THREADS, 0,
+                        s>>>(
         prev_labels, labels, n, moved, moved_count, hist);
     FK_LAUNCH_CHECK();
     launch_scan(hist, k, tmp, s);
