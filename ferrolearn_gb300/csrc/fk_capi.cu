@@ -168,6 +168,8 @@ void lloyd_iteration(Ctx &ctx, const TX *x, int64_t n, int d, const TC *c, int k
     int32_t *members = (int32_t *)ctx.get(BUF_MEMBERS, sizeof(int32_t) * (size_t)n);
     int32_t *seg = (int32_t *)ctx.get(BUF_SEGHIST, sizeof(int32_t) * (size_t)plan.k * plan.nseg);
     int32_t *tmp = (int32_t *)ctx.get(BUF_SCAN_TMP, plan.scan_tmp_bytes);
+    // the contraction's timer writes into this call's report: set only for
+    // the assignment below (a pointer left behind would outlive the report)
     ctx.contract_acc = (timing && rep) ? &rep->ms_contract : nullptr;
     {
         Timer t(timing, ctx, rep ? &rep->ms_assign : nullptr);
@@ -182,6 +184,7 @@ void lloyd_iteration(Ctx &ctx, const TX *x, int64_t n, int d, const TC *c, int k
             }
         }
     }
+    ctx.contract_acc = nullptr;
     {
         Timer t(timing, ctx, rep ? &rep->ms_update : nullptr);
         if constexpr (std::is_same<TX, float>::value && std::is_same<TC, double>::value) {
@@ -645,12 +648,21 @@ fk_status kpp_impl(fk_ctx *ctxp, const T *x_in, int64_t n, int64_t d, int64_t k,
     return FK_OK;
 }
 
-template <typename F>
-fk_status guarded(fk_ctx *ctx, F &&f) {
-    if (!ctx) {
-        set_error("context is NULL");
-        return FK_ERR_NULL_POINTER;
+// Per-call state that points into a caller's report: timers not yet read
+// and the contraction timer's target. Dropped before and after every call,
+// so a call that failed half-way never writes into memory it no longer owns.
+void drop_call_state(fk_ctx *ctxp) {
+    Ctx &ctx = *reinterpret_cast<Ctx *>(ctxp);
+    for (auto &p : ctx.pending) {
+        cudaEventDestroy(p.a);
+        cudaEventDestroy(p.b);
     }
+    ctx.pending.clear();
+    ctx.contract_acc = nullptr;
+}
+
+template <typename F>
+fk_status guarded_body(fk_ctx *ctx, F &&f) {
     try {
         g_last_error.clear();
         return f();
@@ -663,6 +675,18 @@ fk_status guarded(fk_ctx *ctx, F &&f) {
         set_error("unexpected exception");
         return FK_ERR_CUDA;
     }
+}
+
+template <typename F>
+fk_status guarded(fk_ctx *ctx, F &&f) {
+    if (!ctx) {
+        set_error("context is NULL");
+        return FK_ERR_NULL_POINTER;
+    }
+    drop_call_state(ctx);
+    const fk_status st = guarded_body(ctx, f);
+    drop_call_state(ctx);
+    return st;
 }
 
 }  // namespace
