@@ -47,12 +47,52 @@ constexpr int NTHREADS = 320;     // 10 warps
 constexpr uint32_t TMEM_COLS = 512;
 constexpr uint32_t X_ATOM_BYTES = BM * 128;  // 128 rows x 64 BF16
 constexpr uint32_t ONES_BYTES = BM * 32;     // 128 rows x 16 BF16
+// Half 1's top-2 record as it crosses to half 0: the keys, and both centre
+// indices relative to the slice in 16 bits each (0xFFFF: none).
+struct alignas(16) HalfRec {
+    uint32_t v1, v2, u;
+    uint32_t ids;
+};
+__device__ __forceinline__ uint32_t pack_local(int i, int base) { return i < 0 ? 0xFFFFu : (uint32_t)(i - base); }
+__device__ __forceinline__ int unpack_local(uint32_t l, int base) { return l == 0xFFFFu ? -1 : base + (int)l; }
+
 // Shared-memory exchange between the two epilogue halves of a row: three
-// rotating slots for the top-2 records (see the tile merge in the kernel),
-// one for the top-8 records.
-__host__ __device__ constexpr uint32_t merge_bytes(int topk) {
-    return BM * (uint32_t)(topk == 2 ? 3 * sizeof(Top2) : sizeof(Top8));
+// rotating slots for the top-2 pass (see the tile merge in the kernel) --
+// whole records for BF16, 16-byte ones for FP8, whose larger X stages would
+// otherwise leave room for fewer resident centres -- and one slot of top-8
+// records.
+__host__ __device__ constexpr uint32_t merge_bytes(int topk, bool fp8) {
+    return BM * (uint32_t)(topk == 2 ? 3 * (fp8 ? sizeof(HalfRec) : sizeof(Top2)) : sizeof(Top8));
 }
+
+// The record of one slot (FP8: HalfRec; BF16: Top2, no packing).
+template <bool FP8> struct MergeSlot;
+template <> struct MergeSlot<true> {
+    HalfRec r;
+    __device__ __forceinline__ void put(uint32_t v1, int i1, uint32_t v2, int i2, uint32_t u, int base) {
+        r = HalfRec{v1, v2, u, pack_local(i1, base) | (pack_local(i2, base) << 16)};
+    }
+    __device__ __forceinline__ void get(uint32_t &v1, int &i1, uint32_t &v2, int &i2, uint32_t &u, int base) const {
+        v1 = r.v1;
+        v2 = r.v2;
+        u = r.u;
+        i1 = unpack_local(r.ids & 0xFFFFu, base);
+        i2 = unpack_local(r.ids >> 16, base);
+    }
+};
+template <> struct MergeSlot<false> {
+    Top2 r;
+    __device__ __forceinline__ void put(uint32_t v1, int i1, uint32_t v2, int i2, uint32_t u, int) {
+        r = Top2{__uint_as_float(v1), __uint_as_float(v2), __uint_as_float(u), 0.f, i1, i2, 0, 0};
+    }
+    __device__ __forceinline__ void get(uint32_t &v1, int &i1, uint32_t &v2, int &i2, uint32_t &u, int) const {
+        v1 = __float_as_uint(r.v1);
+        v2 = __float_as_uint(r.v2);
+        u = __float_as_uint(r.u3);
+        i1 = r.i1;
+        i2 = r.i2;
+    }
+};
 constexpr uint32_t BAR_BYTES = 256;
 constexpr long long WAIT_LIMIT_CYCLES = 4000000000LL;
 
@@ -551,7 +591,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         const int half = ew >> 2;
         const int row_local = quarter * 32 + lane;
         const uint32_t lane_addr = tmem + ((uint32_t)(quarter * 32) << 16);
-        Top2 *merge = (Top2 *)(smem + p.off_merge);
+        MergeSlot<FP8> *merge = (MergeSlot<FP8> *)(smem + p.off_merge);
+        const int slice0 = part * p.kp;  // the slice's first centre
         const float cgrid = p.stats->cgrid, ulp = p.stats->ulp;
         uint32_t item = 0, tile_it = 0;
         bool dead = false;
@@ -600,18 +641,19 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             // released the buffer of an earlier tile of this CTA. An aborting
             // warp is no longer held back by the MMAs, so it waits instead.
             const uint32_t sl = tile_it % 3u;
-            Top2 *slot = merge + sl * BM;
+            MergeSlot<FP8> *slot = merge + sl * BM;
             if (half == 1) {
-                slot[row_local] = Top2{__uint_as_float(R1), __uint_as_float(R2), __uint_as_float(U), 0.f, I1, I2, 0, 0};
+                slot[row_local].put(R1, I1, R2, I2, U, slice0);
                 if (dead)
                     asm volatile("bar.sync %0, 256;" ::"r"(1u + sl) : "memory");
                 else
                     asm volatile("bar.arrive %0, 256;" ::"r"(1u + sl) : "memory");
             } else {
                 asm volatile("bar.sync %0, 256;" ::"r"(1u + sl) : "memory");
-                const Top2 o = slot[row_local];
-                merge_res(R1, I1, R2, I2, U, __float_as_uint(o.v1), o.i1, __float_as_uint(o.v2), o.i2,
-                          __float_as_uint(o.u3));
+                uint32_t w1, w2, wu;
+                int j1, j2;
+                slot[row_local].get(w1, j1, w2, j2, wu, slice0);
+                merge_res(R1, I1, R2, I2, U, w1, j1, w2, j2, wu);
                 const int64_t row = t * BM + row_local;
                 if (row < p.n && !dead)
                     p.out[(int64_t)part * p.out_stride + row] =
@@ -756,7 +798,7 @@ void plan_tc(Ctx &ctx, MixedPlan &mp, int64_t n, int d, int k, bool fp8, int top
     size_t fixed = 0;
     int xst = 2;
     for (; xst >= 1; xst--) {
-        fixed = 1024 + xst * x_stage + (fp8 ? xst * XAUG_BYTES : ONES_BYTES) + merge_bytes(topk) + BAR_BYTES;
+        fixed = 1024 + xst * x_stage + (fp8 ? xst * XAUG_BYTES : ONES_BYTES) + merge_bytes(topk, fp8) + BAR_BYTES;
         if (fixed + BN * per_centre <= SMEM_LIMIT) break;
     }
     if (xst < 1) {
@@ -837,7 +879,7 @@ void launch_tc_assign(Ctx &ctx, MixedPlan &mp, const void *xb, const void *cb, c
     p.off_ones = p.off_aug + (uint32_t)mp.kp * 32u;
     p.off_xaug = p.off_ones;
     p.off_merge = p.off_ones + (fp8 ? (uint32_t)mp.xst * XAUG_BYTES : ONES_BYTES);
-    p.off_bar = p.off_merge + merge_bytes(mp.topk);
+    p.off_bar = p.off_merge + merge_bytes(mp.topk, mp.fp8);
     p.c_tx_bytes = (uint32_t)p.n_atoms * p.c_atom_bytes + (uint32_t)mp.kp * 32u + (fp8 ? 0u : ONES_BYTES);
     p.out = out;
     p.out8 = out8;
