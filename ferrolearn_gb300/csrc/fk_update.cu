@@ -11,6 +11,14 @@
 // its output offset, and a second pass scatters row indices in row order
 // (warp match + prefix popcount keeps equal labels in lane order). The
 // result: members[] lists each cluster's rows in increasing row index.
+//
+// The mixed precisions (f32 X, f64 centres) sum exactly instead: integer
+// sums on two grids plus 128-bit fixed-point remainders, rounded once to f64
+// (centroid_fixed_part4_kernel). Those sums can be kept and updated from the
+// rows whose label changed (label_diff / moved_scatter / exact_delta4 /
+// exact_means), which a fit does after its first two iterations; it then
+// computes the inertia of the assignment it keeps once, from the rows
+// (row_inertia4_kernel).
 #include <algorithm>
 
 #include "fk_internal.cuh"
