@@ -45,7 +45,6 @@ namespace fk {
 namespace {
 
 constexpr double ACC_REL_PER_K = 0.0000002384185791015625;  // 2^-22 per accumulated column
-constexpr double REPR_REL = 0.0000002384185791015625;       // 2^-22
 constexpr float REPR_REL_F = 0.0000002384185791015625f;     // 2^-22 (exact)
 
 __device__ __forceinline__ void atomic_max_pos(float *addr, float v) {
