@@ -390,3 +390,22 @@ def test_incremental_fit_with_tolerance_and_runs_matches_oracle(precision):
     assert _close(g.cluster_centers(), o["centers"])
     assert g.n_iter() == o["n_iter"]
     assert abs(g.inertia() - o["inertia"]) <= INERTIA_RTOL_MIXED * o["inertia"]
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+def test_mixed_fit_reference_edge_cases(precision):
+    # the reference's known answers (kmeans.rs:784-860) on the mixed forms:
+    # k = n from the rows themselves, identical rows, a single row
+    rng = np.random.default_rng(31)
+    x1 = rng.normal(size=(50, 8)).astype(np.float32)
+    g = F.KMeans(50, dtype="f32x64").with_precision(precision).with_n_init(1) \
+        .with_init_centers(x1.astype(np.float64)[None]).fit(x1)
+    assert g.inertia() == 0.0
+    assert np.array_equal(g.labels(), np.arange(50))
+    same = np.ones((20, 4), dtype=np.float32)
+    g = F.KMeans(3, dtype="f32x64").with_precision(precision).with_n_init(2).with_random_state(5).fit(same)
+    assert g.inertia() == 0.0
+    assert not g.labels().any()
+    g = F.KMeans(1, dtype="f32x64").with_precision(precision).with_n_init(1).fit(x1[:1])
+    assert g.labels().tolist() == [0] and g.inertia() == 0.0
+    assert np.array_equal(g.cluster_centers(), x1[:1].astype(np.float64))
