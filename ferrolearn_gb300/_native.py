@@ -23,7 +23,7 @@ EXPORTS = [
     "fk_kmeans_predict_f64", "fk_kmeans_predict_f32", "fk_kmeans_predict_f32x64",
     "fk_kmeans_transform_f64", "fk_kmeans_transform_f32",
     "fk_kmeans_plus_plus_f64", "fk_kmeans_plus_plus_f32", "fk_debug_tc_probe",
-    "fk_debug_measure_peaks", "fk_kmeans_score_f64_noalloc", "fk_kmeans_fit_batched_f32",
+    "fk_debug_measure_peaks", "fk_kmeans_score_f64_noalloc", "fk_kmeans_fit_batched_f32", "fk_debug_tc_plan",
 ]
 
 
@@ -151,6 +151,8 @@ def _declare(lib):
     lib.fk_kmeans_score_f64_noalloc.restype = st
     lib.fk_kmeans_fit_batched_f32.argtypes = [p, C.POINTER(BatchProblem), i64, i32, C.POINTER(BatchReport)]
     lib.fk_kmeans_fit_batched_f32.restype = st
+    lib.fk_debug_tc_plan.argtypes = [i64, i64, i64, i32, i32, i32, p]
+    lib.fk_debug_tc_plan.restype = st
 
 
 def lib():

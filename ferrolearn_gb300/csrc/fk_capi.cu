@@ -846,6 +846,27 @@ fk_status fk_debug_tc_probe(fk_ctx *ctx, const float *x_dev, int64_t n, int64_t 
     });
 }
 
+fk_status fk_debug_tc_plan(int64_t n, int64_t d, int64_t k, int32_t precision, int32_t topk, int32_t num_sms,
+                           int64_t *out) {
+    if (!out) return FK_ERR_NULL_POINTER;
+    if ((precision != FK_PRECISION_MIXED_BF16 && precision != FK_PRECISION_MIXED_FP8) || (topk != 2 && topk != 8) ||
+        n < 1 || d < 1 || k < 1 || d > (1 << 16) || k > (1 << 20)) {
+        fk::set_error("fk_debug_tc_plan: unsupported arguments");
+        return FK_ERR_INVALID_PARAMETER;
+    }
+    try {
+        fk::g_last_error.clear();
+        fk::MixedPlan mp;
+        fk::plan_shape(mp, n, (int)d, (int)k, precision == FK_PRECISION_MIXED_FP8, topk, num_sms);
+        const int64_t v[10] = {mp.d_pad, mp.kp, mp.parts, mp.k_pad, mp.nblocks, mp.xst, (int64_t)mp.smem,
+                               mp.grid, mp.ctas_per_part, mp.tiles};
+        for (int i = 0; i < 10; i++) out[i] = v[i];
+        return FK_OK;
+    } catch (const fk::Error &e) {
+        return e.code;
+    }
+}
+
 fk_status fk_kmeans_plus_plus_f32(fk_ctx *ctx, const float *x, int64_t n, int64_t d, int64_t k, const double *draws,
                                   int64_t n_draws, uint64_t seed, float *out, int64_t *used) {
     return guarded(ctx, [&] { return fk::kpp_impl<float>(ctx, x, n, d, k, draws, n_draws, seed, out, used); });

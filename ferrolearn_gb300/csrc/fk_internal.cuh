@@ -291,6 +291,9 @@ void plan_tc(Ctx &ctx, MixedPlan &mp, int64_t n, int d, int k, bool fp8, int top
 // capacity). FP8 (mp.fp8): xaug is the per-row augmentation tensor (n x 16
 // BF16) and rowscale the per-row power of two mapping scores to the row's
 // accumulator units.
+// Launch shape only (host arithmetic, no device work); plan_tc adds the
+// device-side constants.
+void plan_shape(MixedPlan &mp, int64_t n, int d, int k, bool fp8, int topk, int sms);
 void launch_tc_assign(Ctx &ctx, MixedPlan &mp, const void *xb, const void *cb, const void *caug, Top2 *out,
                       Top8 *out8, DevScalars *sc, const MixedStats *stats, float *dump = nullptr,
                       const unsigned long long *n_dev = nullptr, const void *xaug = nullptr,

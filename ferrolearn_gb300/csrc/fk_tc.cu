@@ -783,7 +783,9 @@ constexpr size_t SMEM_LIMIT = 227 * 1024;
 
 }  // namespace
 
-void plan_tc(Ctx &ctx, MixedPlan &mp, int64_t n, int d, int k, bool fp8, int topk) {
+// The launch shape of one tensor-core pass (host arithmetic only): the X
+// ring depth, the resident slice of centres that fits next to it, the grid.
+void plan_shape(MixedPlan &mp, int64_t n, int d, int k, bool fp8, int topk, int sms) {
     mp.n = n;
     mp.d = d;
     mp.k = k;
@@ -813,11 +815,15 @@ void plan_tc(Ctx &ctx, MixedPlan &mp, int64_t n, int d, int k, bool fp8, int top
     mp.k_pad = mp.parts * mp.kp;
     mp.nblocks = mp.kp / BN;
     mp.tiles = (n + BM - 1) / BM;
-    int sms = ctx.num_sms > 0 ? ctx.num_sms : 1;
+    if (sms < 1) sms = 1;
     mp.ctas_per_part = sms / mp.parts > 0 ? sms / mp.parts : 1;
     if ((int64_t)mp.ctas_per_part > mp.tiles) mp.ctas_per_part = (int)mp.tiles;
     mp.grid = mp.ctas_per_part * mp.parts;
     mp.smem = fixed + (size_t)mp.kp * per_centre;
+}
+
+void plan_tc(Ctx &ctx, MixedPlan &mp, int64_t n, int d, int k, bool fp8, int topk) {
+    plan_shape(mp, n, d, k, fp8, topk, ctx.num_sms);
     mp.tm_x_ptr = mp.tm_c_ptr = mp.tm_aug_ptr = mp.tm_xaug_ptr = nullptr;
     if (!mp.ones) {
         uint16_t h[BM * 16];

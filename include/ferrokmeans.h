@@ -281,6 +281,15 @@ fk_status fk_debug_tc_probe(fk_ctx *ctx, const float *x_dev, int64_t n, int64_t 
                             int64_t k, int32_t precision, float *dump, void *xq, void *cq, uint16_t *aug,
                             uint16_t *xaug, void *top, int32_t *plan);
 
+/* Diagnostics (no reference counterpart, no GPU needed): the launch plan of
+ * one tensor-core pass for a shape -- precision FK_PRECISION_MIXED_BF16 or
+ * _FP8, topk 2 (main pass) or 8 (second pass), on num_sms SMs. out[0..9] =
+ * {d_pad, kp (resident centres per slice), parts (slices), k_pad, nblocks
+ * (256-centre accumulator blocks per slice), xst (X ring depth), dynamic
+ * shared memory bytes, grid, CTAs per slice, 128-row tiles}. */
+fk_status fk_debug_tc_plan(int64_t n, int64_t d, int64_t k, int32_t precision, int32_t topk, int32_t num_sms,
+                           int64_t *out);
+
 #ifdef __cplusplus
 }
 #endif

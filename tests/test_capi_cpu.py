@@ -122,3 +122,37 @@ def test_batched_empty_and_bad_reduction():
     assert fitted == [] and rep["fits"] == 0
     with pytest.raises(F.InvalidParameter):
         F.fit_batched([_bp()], reduction=7)
+
+
+def _plan(n, d, k, precision, topk, sms=152):
+    import ctypes as C
+    out = (C.c_int64 * 10)()
+    st = _native.lib().fk_debug_tc_plan(n, d, k, precision, topk, sms, out)
+    return st, dict(zip(["d_pad", "kp", "parts", "k_pad", "nblocks", "xst", "smem", "grid", "ctas", "tiles"], out))
+
+
+def test_tensor_core_plans_of_the_workloads():
+    # host-only planning of the resident-slice kernel: the shapes the bench
+    # workloads run (a plan that loses resident centres slows every launch)
+    st, p = _plan(4_000_000, 128, 1024, F.MIXED_BF16, 2)
+    assert st == 0 and (p["d_pad"], p["kp"], p["parts"], p["xst"], p["nblocks"]) == (128, 512, 2, 2, 2)
+    assert p["grid"] == 152 and p["tiles"] == 31250 and p["smem"] <= 227 * 1024
+    st, p = _plan(8_000_000, 256, 4096, F.MIXED_FP8, 2)
+    assert st == 0 and (p["d_pad"], p["kp"], p["parts"], p["xst"]) == (256, 512, 8, 2)
+    assert p["grid"] == 152 and p["smem"] <= 227 * 1024
+    st, p = _plan(2_000_000, 256, 4096, F.MIXED_BF16, 8)  # the second pass of the FP8 form: BF16 rows of
+    # 512 bytes leave room for one X stage and 256 resident centres
+    assert st == 0 and (p["kp"], p["parts"], p["xst"], p["grid"]) == (256, 16, 1, 144) and p["smem"] <= 227 * 1024
+    st, p = _plan(100_000, 128, 1024, F.MIXED_BF16, 8)
+    assert st == 0 and (p["kp"], p["xst"]) == (512, 2)
+    # small shapes: one padded slice, grid no larger than the tiles
+    st, p = _plan(1, 1, 1, F.MIXED_BF16, 2)
+    assert st == 0 and (p["d_pad"], p["kp"], p["parts"], p["k_pad"], p["grid"], p["tiles"]) == (64, 256, 1, 256, 1, 1)
+
+
+def test_tensor_core_plan_rejects_what_the_kernel_cannot_hold():
+    st, _ = _plan(1000, 512, 64, F.MIXED_BF16, 2)  # d beyond the resident-slice kernel's BF16 limit
+    assert st == 13  # FK_ERR_UNSUPPORTED
+    assert "supports d <=" in _native.last_error()
+    st, _ = _plan(1000, 64, 64, 0, 2)  # the plain precision has no tensor-core plan
+    assert st != 0
