@@ -37,6 +37,7 @@ same workload with all host threads, and reports iterations/s extrapolated
 to the full n.
 """
 import argparse
+import ctypes as C
 import faulthandler
 import json
 import os
@@ -414,8 +415,15 @@ def run_ours(args):
                 "unit": "TFLOP/s", "peak_source": f"2 x bf16_tflops_sustained ({peak_src}): the dense E4M3 rate is "
                                                   "twice the BF16 rate on this part"}
     else:
-        roof = {"bound": "tensor", "achieved": flops / (assign_ms / 1e3) / 1e12, "peak": bf16s, "unit": "TFLOP/s",
-                "peak_source": f"bf16_tflops_sustained ({peak_src}); SIMT form compared against the tensor peak"}
+        # the plain forms run on the CUDA cores: their peak is measured here
+        # (fk_debug_measure_peaks: FMA chains on every SM, CUDA events)
+        pk = (C.c_double * 8)()
+        _native.lib().fk_debug_measure_peaks(ctx.handle, pk)
+        simt = (pk[0] if form == "fp32" else pk[1]) / 1e12
+        roof = {"bound": "fp32-simt" if form == "fp32" else "fp64-simt",
+                "achieved": flops / (assign_ms / 1e3) / 1e12, "peak": simt, "unit": "TFLOP/s",
+                "peak_source": f"{form.upper()} FMA peak measured in this run (fk_debug_measure_peaks); achieved "
+                               "counts 2 n k d (the GEMM-equivalent work), the direct form executes 3 n k d"}
     roof["frac"] = roof["achieved"] / roof["peak"]
     roof["traffic"] = None
     roof["kernel"] = f"tc_assign_kernel ({form.upper()} tcgen05 contraction + top-2 epilogue)" if mixed else \
@@ -443,6 +451,17 @@ def run_ours(args):
         "clocks": clocks.summary(),
         "roofline": roof,
     }
+    # the update phase against HBM: a full pass reads X once and writes the
+    # centres (n d sizeof(X) + 4 n + 2 k d 8 bytes); the mixed forms update
+    # incrementally after the second iteration, so their figure is that full
+    # pass's bytes over the average update time (an effective rate)
+    upd_ms = rep["ms_update"] / iters
+    upd_bytes = n * d * x32.itemsize * (2 if form == "fp64" else 1) + 4 * n + 16 * k * d
+    out["update_roofline"] = {"bound": "hbm", "bytes_per_iter": upd_bytes, "ms_per_iter": upd_ms,
+                              "achieved": upd_bytes / (upd_ms / 1e3) / 1e9, "peak": hbm, "unit": "GB/s",
+                              "frac": upd_bytes / (upd_ms / 1e3) / 1e9 / hbm,
+                              "note": "incremental after iteration 2 (effective rate)" if mixed
+                              else "full pass every iteration (row-order sums of the reference)"}
     if kpp_ms is not None:
         out["kpp_ms"] = kpp_ms
     if "x_predict" in w and rank == 0:
