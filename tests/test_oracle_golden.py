@@ -186,3 +186,38 @@ def test_nan_rows_follow_strict_less():
     lab, inertia = O.assign(x, c)
     assert lab.tolist() == [0, 1]
     assert inertia == np.finfo(np.float64).max
+
+
+def test_wide_sum_update_is_the_rounded_exact_mean():
+    # the f64-reduction variant of the oracle (the batched entry point's
+    # FK_REDUCE_F64): each centre is (f32)(round_f64(exact cluster sum) / count),
+    # restated here with exact rational sums
+    from fractions import Fraction
+    rng = np.random.default_rng(44)
+    n, d, k = 300, 3, 5
+    x = (rng.normal(size=(n, d)) * rng.choice([1e-3, 1.0, 1e3], size=(n, 1))).astype(np.float32)
+    init = x[rng.choice(n, k, replace=False)][None]
+    o = O.fit_runs(x, k, max_iter=1, tol=0.0, n_init=1, init=init, wide_sums=True)
+    lab = o["labels"][0]
+    for c in range(k):
+        rows = x[lab == c]
+        for j in range(d):
+            if len(rows) == 0:
+                want = init[0, c, j]
+            else:
+                s = sum((Fraction(float(v)) for v in rows[:, j]), Fraction(0))
+                want = np.float32(float(s) / len(rows))
+            assert o["centers"][0, c, j] == want, (c, j)
+
+
+def test_fit_runs_agrees_with_fit_per_run():
+    # the per-run entry point and Fit::fit with one run give the same run
+    rng = np.random.default_rng(45)
+    x = (rng.normal(size=(400, 4)) + rng.integers(0, 3, size=(400, 1)) * 5).astype(np.float32)
+    inits = np.stack([x[rng.choice(400, 3, replace=False)] for _ in range(2)])
+    runs = O.fit_runs(x, 3, max_iter=20, tol=1e-4, n_init=2, init=inits)
+    for r in range(2):
+        one = O.fit(x, 3, max_iter=20, tol=1e-4, n_init=1, init=inits[r][None])
+        assert np.array_equal(runs["labels"][r], one["labels"])
+        assert np.array_equal(runs["centers"][r], one["centers"])
+        assert runs["n_iter"][r] == one["n_iter"]
