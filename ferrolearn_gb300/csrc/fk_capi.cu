@@ -1,6 +1,6 @@
-// fk_capi.cu -- the extern "C" boundary and the Lloyd driver.
+// fk_capi.cu -- the extern "C" boundary and the host side of the Lloyd loop.
 //
-// The driver restates Fit::fit (kmeans.rs:417-512) on the GPU: validation in
+// The host side restates Fit::fit (kmeans.rs:417-512) on the GPU: validation in
 // the reference's order, n_init runs seeded base+run, the Lloyd loop whose
 // labels/inertia come from the assignment against the pre-update centres
 // while the returned centres are the post-update ones, convergence when

@@ -1341,7 +1341,7 @@ __global__ void inertia_final_kernel(const double *__restrict__ part, int64_t m,
 
 }  // namespace
 
-// ---------------------------------------------------------------- driver --
+// ------------------------------------------------------------- host side --
 namespace {
 
 // Device buffers of one mixed assignment.

@@ -1,6 +1,6 @@
 // fk_peaks.cu -- CUDA-core throughput microbenchmarks for the roofline of the
-// SIMT kernels (the driver measures only HBM copy bandwidth and BF16 tensor
-// throughput). Each thread runs eight independent chains of one operation;
+// SIMT kernels (the measured peaks file holds only HBM copy bandwidth and BF16
+// tensor throughput). Each thread runs eight independent chains of one operation;
 // rates are counted per operation executed (an FMA counts as two flops).
 #include "fk_internal.cuh"
 

@@ -1,7 +1,8 @@
 /*
  * kmeans_oracle.c -- CPU restatement of ferrolearn-cluster's KMeans Lloyd
  * path, used ONLY as test infrastructure: the parity tests, the smoke check
- * and the CPU-baseline leg of the benchmark call it as the checker. Nothing
+ * and the CPU-baseline leg of the benchmark call it as the reference result
+ * to compare against (or, in the benchmark, to time). Nothing
  * in the product library links or calls this file.
  *
  * It restates ferrolearn-cluster/src/kmeans.rs statement by statement:

@@ -1,7 +1,8 @@
 """ctypes wrapper around the CPU oracle (oracle/kmeans_oracle.c).
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke() and
-by bench.py's CPU-baseline leg, always as the checker. The product library
+by bench.py's CPU-baseline leg, always as the result compared against (or
+timed as the CPU baseline). The product library
 (ferrolearn_gb300) never imports this module.
 
 Each function restates one item of ferrolearn-cluster/src/kmeans.rs (the C

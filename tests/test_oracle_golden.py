@@ -1,6 +1,6 @@
 """Pins the CPU oracle against the reference's golden data and known answers.
 
-The oracle (oracle/kmeans_oracle.c) is the checker of every GPU parity test,
+The oracle (oracle/kmeans_oracle.c) is what every GPU parity test compares against,
 so it is validated first against:
   * the reference's KMeans fixture (fixtures/kmeans.json, used by
     ferrolearn-cluster/tests/oracle_tests.rs:66-117), both exactly (starting
