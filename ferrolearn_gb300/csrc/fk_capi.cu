@@ -151,6 +151,21 @@ bool precision_ok(int prec) {
     return false;
 }
 
+// The ranges every entry point accepts: rows index int32 labels, and the
+// kernels index features and clusters with 32-bit integers. Checked before
+// CUDA is touched, like the reference's own argument errors.
+fk_status check_shape(int64_t n, int64_t d, int64_t k) {
+    if (d < 0) {
+        set_error("Invalid parameter `d`: negative");
+        return FK_ERR_INVALID_PARAMETER;
+    }
+    if (k > (1 << 20) || n > INT32_MAX || d > (1 << 16)) {
+        set_error("shape n=%lld d=%lld k=%lld exceeds the supported range", (long long)n, (long long)d, (long long)k);
+        return FK_ERR_UNSUPPORTED;
+    }
+    return FK_OK;
+}
+
 // ------------------------------------------------------------ one step --
 // Update modes of the mixed path with f32 X: the full exact pass (optionally
 // keeping its exact sums), or the incremental one from the rows whose label
@@ -270,8 +285,12 @@ fk_status fit_impl(fk_ctx *ctxp, const TX *x_in, int64_t n, int64_t d, const fk_
         set_error("Invalid parameter `n_init`: must be at least 1");
         return FK_ERR_INVALID_PARAMETER;
     }
-    if (p->max_iter < 0 || d < 0) {
-        set_error("Invalid parameter `max_iter`/`d`: negative");
+    if (p->max_iter < 0) {
+        set_error("Invalid parameter `max_iter`: negative");
+        return FK_ERR_INVALID_PARAMETER;
+    }
+    if (d < 0) {
+        set_error("Invalid parameter `d`: negative");
         return FK_ERR_INVALID_PARAMETER;
     }
     if (!x_in || !centers_out || !labels_out || !inertia_out || !n_iter_out) {
@@ -282,10 +301,11 @@ fk_status fit_impl(fk_ctx *ctxp, const TX *x_in, int64_t n, int64_t d, const fk_
         set_error("precision %d is not available for this entry point", p->precision);
         return FK_ERR_UNSUPPORTED;
     }
-    if (k > (1 << 20) || n > INT32_MAX || d > (1 << 16)) {
-        set_error("shape n=%lld d=%lld k=%lld exceeds the supported range", (long long)n, (long long)d, (long long)k);
-        return FK_ERR_UNSUPPORTED;
+    if (!init_in && p->draws && p->n_draws < 0) {
+        set_error("Invalid parameter `n_draws`: negative");
+        return FK_ERR_INVALID_PARAMETER;
     }
+    if (fk_status st = check_shape(n, d, k)) return st;
     ctx.bind();
     if (rep) {
         memset(rep, 0, sizeof(*rep));
@@ -326,7 +346,9 @@ fk_status fit_impl(fk_ctx *ctxp, const TX *x_in, int64_t n, int64_t d, const fk_
         }
     } ev_guard{iter_done};
 
-    const TC *init = init_in ? stage_in<TC>(ctx, BUF_OUT2, init_in, kd * (size_t)p->n_init) : nullptr;
+    // a slot of its own: the runs after the first read it while the mixed
+    // updates use their own scratch (which may grow and move)
+    const TC *init = init_in ? stage_in<TC>(ctx, BUF_INIT, init_in, kd * (size_t)p->n_init) : nullptr;
     const double *draws_dev = nullptr;
     int64_t n_draws = 0;
     if (!init) {
@@ -499,6 +521,7 @@ fk_status step_impl(fk_ctx *ctxp, const TX *x_in, int64_t n, int64_t d, const TC
         set_error("precision %d is not available for this entry point", prec);
         return FK_ERR_UNSUPPORTED;
     }
+    if (fk_status st = check_shape(n, d, k)) return st;
     ctx.bind();
     if (rep) {
         memset(rep, 0, sizeof(*rep));
@@ -554,6 +577,7 @@ fk_status predict_impl(fk_ctx *ctxp, const TC *c_in, int64_t k, int64_t d_fit, c
         set_error("precision %d is not available for this entry point", prec);
         return FK_ERR_UNSUPPORTED;
     }
+    if (fk_status st = check_shape(n, d, k)) return st;
     ctx.bind();
     cudaStream_t s = ctx.stream;
     const TX *x = stage_in<TX>(ctx, BUF_X, x_in, (size_t)n * d);
@@ -597,6 +621,7 @@ fk_status transform_impl(fk_ctx *ctxp, const T *c_in, int64_t k, int64_t d_fit, 
         set_error("required pointer is NULL");
         return FK_ERR_NULL_POINTER;
     }
+    if (fk_status st = check_shape(n, d, k)) return st;
     ctx.bind();
     cudaStream_t s = ctx.stream;
     const T *x = stage_in<T>(ctx, BUF_X, x_in, (size_t)n * d);
@@ -624,6 +649,11 @@ fk_status kpp_impl(fk_ctx *ctxp, const T *x_in, int64_t n, int64_t d, int64_t k,
         set_error("required pointer is NULL");
         return FK_ERR_NULL_POINTER;
     }
+    if (draws && n_draws < 0) {
+        set_error("Invalid parameter `n_draws`: negative");
+        return FK_ERR_INVALID_PARAMETER;
+    }
+    if (fk_status st = check_shape(n, d, k)) return st;
     ctx.bind();
     cudaStream_t s = ctx.stream;
     const T *x = stage_in<T>(ctx, BUF_X, x_in, (size_t)n * d);

@@ -133,7 +133,7 @@ enum BufSlot {
     BUF_XB, BUF_XNORM, BUF_CB, BUF_CAUX, BUF_TOP2, BUF_FLAGS, BUF_FULL, BUF_CF32, BUF_CF32C, BUF_FIXPART,
     BUF_XB2, BUF_TOP8, BUF_OCT, BUF_EX, BUF_XAUG, BUF_ROWSCALE, BUF_ROWINFO2, BUF_STATS2, BUF_CB2, BUF_CAUG2,
     BUF_HALF2, BUF_INERTIA2, BUF_C2, BUF_XSTATE, BUF_XCOUNTS, BUF_MOVED, BUF_MOVED_ENT, BUF_MOVED_HIST, BUF_MOVED_TMP,
-    BUF_CSPLIT, BUF_RINERT, BUF_F64ITEMS,
+    BUF_CSPLIT, BUF_RINERT, BUF_F64ITEMS, BUF_INIT,
     BUF_BX, BUF_BFITS, BUF_BSTATE, BUF_BITEMS, BUF_BPART, BUF_BORDER, BUF_BCTR, BUF_BLAB, BUF_BMEM, BUF_BCEN, BUF_BND, BUF_BXOFF,
     BUF_COUNT
 };

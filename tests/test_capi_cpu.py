@@ -156,3 +156,38 @@ def test_tensor_core_plan_rejects_what_the_kernel_cannot_hold():
     assert "supports d <=" in _native.last_error()
     st, _ = _plan(1000, 64, 64, 0, 2)  # the plain precision has no tensor-core plan
     assert st != 0
+
+
+def test_out_of_range_arguments_are_refused_before_any_device_work():
+    # every entry point checks the ranges its kernels index (int32 labels,
+    # 32-bit feature and cluster indices) before CUDA is touched: the
+    # pointers below are never read
+    lib = _native.lib()
+    ctx = C.c_void_p()
+    assert lib.fk_ctx_create(C.byref(ctx), 0, None) == 0
+    buf = np.zeros(64)
+    p = buf.ctypes.data
+    big_n, big_d, big_k = 2**31, 2**16 + 1, 2**20 + 1
+    try:
+        assert lib.fk_kmeans_predict_f64(ctx, p, 2, 2, p, big_n, 2, 0, p) == 13
+        assert lib.fk_kmeans_predict_f32(ctx, p, big_k, 2, p, 4, 2, 0, p) == 13
+        assert lib.fk_kmeans_predict_f64(ctx, p, 2, -1, p, 4, -1, 0, p) == 1
+        assert lib.fk_kmeans_transform_f64(ctx, p, big_k, 2, p, 4, 2, p) == 13
+        assert lib.fk_kmeans_transform_f32(ctx, p, 2, big_d, p, 4, big_d, p) == 13
+        assert lib.fk_kmeans_plus_plus_f64(ctx, p, 4, 2, 2, p, -1, 0, p, None) == 1
+        assert "n_draws" in _native.last_error()
+        assert lib.fk_kmeans_plus_plus_f32(ctx, p, 4, big_d, 2, None, 0, 0, p, None) == 13
+        rep = _native.FitReport()
+        assert lib.fk_lloyd_step_f64(ctx, p, big_n, 2, p, 2, 0, p, p, p, p, C.byref(rep)) == 13
+        assert lib.fk_lloyd_step_f32x64(ctx, p, 4, -2, p, 2, 1, p, p, p, p, None) == 1
+        params = _native.KMeansParams()
+        lib.fk_kmeans_params_default(C.byref(params), 2)
+        params.draws = p
+        params.n_draws = -1
+        assert lib.fk_kmeans_fit_f64(ctx, p, 4, 2, C.byref(params), None, p, p, p, p, None) == 1
+        assert "n_draws" in _native.last_error()
+        params.n_draws = 8
+        assert lib.fk_kmeans_fit_f64(ctx, p, big_n, 2, C.byref(params), None, p, p, p, p, None) == 13
+        assert "supported range" in _native.last_error()
+    finally:
+        lib.fk_ctx_destroy(ctx)
