@@ -164,12 +164,55 @@ def _prec(p):
     return int(p)
 
 
-def _as_matrix(x, dt):
+_TORCH_NAMES = {np.dtype(np.float32): ("torch.float32",), np.dtype(np.float64): ("torch.float64",),
+                np.dtype(np.uint64): ("torch.int64", "torch.uint64")}
+
+
+def _check_tensor(t, dt, what, ctx, shape=None, ndim=None):
+    """A torch tensor is handed to the library as raw memory, so its dtype,
+    shape and layout must be exactly what the entry point reads or writes,
+    and a device tensor must live on the context's GPU (the kernels use it in
+    place). Labels are written as uint64; int64 tensors hold the same bits."""
+    names = _TORCH_NAMES[np.dtype(dt)]
+    if str(t.dtype) not in names:
+        raise InvalidParameter(f"{what}: a {t.dtype} tensor where {' or '.join(names)} is expected")
+    if ndim is not None and t.dim() != ndim:
+        raise ShapeMismatch(f"{what}: expected a {ndim}-D tensor, got shape {tuple(t.shape)}")
+    if shape is not None and tuple(t.shape) != tuple(shape):
+        raise ShapeMismatch(f"{what}: expected shape {tuple(shape)}, got {tuple(t.shape)}")
+    if not t.is_contiguous():
+        raise InvalidParameter(f"{what}: the tensor must be contiguous (row-major)")
+    dev = t.device
+    if dev.type == "cuda":
+        if ctx is not None and dev.index != int(ctx.device):
+            raise InvalidParameter(f"{what}: tensor on cuda:{dev.index}, context on cuda:{ctx.device}")
+    elif dev.type != "cpu":
+        raise InvalidParameter(f"{what}: tensors on {dev.type} are not supported")
+    return t
+
+
+def _as_matrix(x, dt, ctx=None):
     if hasattr(x, "data_ptr"):
-        return x  # device tensor: caller guarantees dtype / contiguity
+        return _check_tensor(x, dt, "x", ctx, ndim=2)
     a = np.ascontiguousarray(x, dtype=dt)
     if a.ndim != 2:
         raise ShapeMismatch(f"expected a 2-D array, got shape {a.shape}")
+    return a
+
+
+def _check_out(a, dt, shape, what, ctx):
+    """An output buffer the library writes in place (numpy array or tensor)."""
+    if hasattr(a, "data_ptr"):
+        return _check_tensor(a, dt, what, ctx, shape=shape)
+    if not isinstance(a, np.ndarray):
+        raise InvalidParameter(f"{what}: expected a numpy array or a tensor")
+    ok = (a.dtype == np.dtype(dt)) or (dt == np.uint64 and a.dtype == np.int64)
+    if not ok:
+        raise InvalidParameter(f"{what}: dtype {a.dtype} where {np.dtype(dt)} is written")
+    if a.shape != tuple(shape):
+        raise ShapeMismatch(f"{what}: expected shape {tuple(shape)}, got {a.shape}")
+    if not (a.flags.c_contiguous and a.flags.writeable):
+        raise InvalidParameter(f"{what}: the array must be C-contiguous and writeable")
     return a
 
 
@@ -256,7 +299,7 @@ class KMeans:
         results in place of new host arrays."""
         xt, ct, suf = _dtypes(self.dtype)
         ctx = ctx or default_context()
-        x = _as_matrix(x, xt)
+        x = _as_matrix(x, xt, ctx)
         n, d = int(x.shape[0]), int(x.shape[1])
         k = self.n_clusters
         init = None
@@ -270,6 +313,8 @@ class KMeans:
             init = ini
         if out is not None:
             centers, labels = out
+            _check_out(centers, ct, (max(k, 0), d), "centres out", ctx)
+            _check_out(labels, np.uint64, (n,), "labels out", ctx)
         else:
             centers = np.empty((max(k, 0), d), dtype=ct)
             labels = np.empty(n, dtype=np.uint64)
@@ -316,7 +361,7 @@ class FittedKMeans:
         """Predict::predict (kmeans.rs:538-552)."""
         xt, ct, suf = _dtypes(self.dtype)
         ctx = ctx or default_context()
-        x = _as_matrix(x, xt)
+        x = _as_matrix(x, xt, ctx)
         n, d = int(x.shape[0]), int(x.shape[1])
         labels = np.empty(n, dtype=np.uint64)
         prec = self.precision if precision is None else _prec(precision)
@@ -331,7 +376,7 @@ class FittedKMeans:
         if suf == "f32x64":
             xt, suf = np.float64, "f64"
         ctx = ctx or default_context()
-        x = _as_matrix(x, xt)
+        x = _as_matrix(x, xt, ctx)
         n, d = int(x.shape[0]), int(x.shape[1])
         k = self._centers.shape[0]
         out = np.empty((n, k), dtype=ct)
@@ -344,7 +389,7 @@ def lloyd_step(x, centers, dtype="f64", precision=PLAIN, ctx=None):
     """One Lloyd iteration (kmeans.rs:468-488): (labels, new_centers, inertia, max_shift, report)."""
     xt, ct, suf = _dtypes(dtype)
     ctx = ctx or default_context()
-    x = _as_matrix(x, xt)
+    x = _as_matrix(x, xt, ctx)
     c = np.ascontiguousarray(centers, dtype=ct)
     n, d = x.shape
     k = c.shape[0]
@@ -365,9 +410,9 @@ def kmeans_plus_plus(x, k, draws_arr=None, seed=0, dtype="f64", ctx=None):
     if suf == "f32x64":
         raise Unsupported("k-means++ runs on f64 or f32 matrices")
     ctx = ctx or default_context()
-    x = _as_matrix(x, xt)
+    x = _as_matrix(x, xt, ctx)
     n, d = x.shape
-    out = np.empty((k, d), dtype=ct)
+    out = np.empty((max(int(k), 0), d), dtype=ct)
     used = C.c_int64()
     dr = None if draws_arr is None else np.ascontiguousarray(draws_arr, dtype=np.float64)
     fn = getattr(_native.lib(), f"fk_kmeans_plus_plus_{suf}")
@@ -407,7 +452,7 @@ def fit_batched(problems, reduction="reference", ctx=None):
     keep, outs = [], []
     total_fits = 0
     for i, pr in enumerate(problems):
-        x = _as_matrix(pr["x"], np.float32)
+        x = _as_matrix(pr["x"], np.float32, ctx)
         n, d = int(x.shape[0]), int(x.shape[1])
         k = int(pr["k"])
         n_init = int(pr.get("n_init", 10))

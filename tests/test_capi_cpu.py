@@ -191,3 +191,40 @@ def test_out_of_range_arguments_are_refused_before_any_device_work():
         assert "supported range" in _native.last_error()
     finally:
         lib.fk_ctx_destroy(ctx)
+
+
+def test_tensors_and_output_buffers_are_checked_before_the_call():
+    # a tensor is used as raw memory: a wrong dtype, shape or layout would make
+    # the kernels read or write past it, so the host layer refuses it first
+    torch = pytest.importorskip("torch")
+    x32 = torch.ones((8, 4), dtype=torch.float32)
+    with pytest.raises(F.InvalidParameter, match="torch.float64"):
+        F.KMeans(2, dtype="f64").fit(x32)  # f64 entry point reads 8-byte values
+    with pytest.raises(F.InvalidParameter, match="contiguous"):
+        F.KMeans(2, dtype="f32").fit(torch.ones((4, 8), dtype=torch.float32).t())
+    with pytest.raises(F.ShapeMismatch):
+        F.KMeans(2, dtype="f32").fit(torch.ones(8, dtype=torch.float32))
+    m = F.KMeans(2, dtype="f32x64").with_n_init(1)
+    with pytest.raises(F.ShapeMismatch, match="centres out"):
+        m.fit(x32, out=(torch.empty((3, 4), dtype=torch.float64), torch.empty(8, dtype=torch.int64)))
+    with pytest.raises(F.InvalidParameter, match="centres out"):
+        m.fit(x32, out=(torch.empty((2, 4), dtype=torch.float32), torch.empty(8, dtype=torch.int64)))
+    with pytest.raises(F.ShapeMismatch, match="labels out"):
+        m.fit(x32, out=(torch.empty((2, 4), dtype=torch.float64), torch.empty(7, dtype=torch.int64)))
+    with pytest.raises(F.InvalidParameter, match="labels out"):
+        m.fit(x32, out=(np.empty((2, 4)), np.empty(8, dtype=np.int32)))
+    with pytest.raises(F.InvalidParameter, match="writeable"):
+        ro = np.empty((2, 4))
+        ro.flags.writeable = False
+        m.fit(x32, out=(ro, np.empty(8, dtype=np.uint64)))
+    with pytest.raises(F.InvalidParameter):
+        F.lloyd_step(torch.ones((8, 4), dtype=torch.float64), np.ones((2, 4)), dtype="f32")
+    with pytest.raises(F.InvalidParameter):
+        F.fit_batched([dict(x=torch.ones((8, 4), dtype=torch.float64), k=2)])
+    with pytest.raises(F.InvalidParameter):
+        F.kmeans_plus_plus(torch.ones((8, 4), dtype=torch.float32), 2, dtype="f64")
+    fitted = F.FittedKMeans(np.ones((2, 4)), np.zeros(8, dtype=np.int64), 0.0, 1, "f64")
+    with pytest.raises(F.InvalidParameter):
+        fitted.predict(x32)
+    with pytest.raises(F.InvalidParameter):
+        fitted.transform(x32)
