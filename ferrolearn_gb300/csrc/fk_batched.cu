@@ -830,8 +830,7 @@ fk_status batched_fit_impl(Ctx &ctx, fk_batch_problem *P, int64_t np, int reduct
     if (np == 0) return FK_OK;
     ctx.bind();
     cudaStream_t s = ctx.stream;
-    cudaEvent_t ev[6];
-    for (auto &e : ev) FK_CUDA(cudaEventCreate(&e));
+    Events<6> ev;
     FK_CUDA(cudaEventRecord(ev[0], s));
 
     // ---- layout
@@ -1030,7 +1029,16 @@ fk_status batched_fit_impl(Ctx &ctx, fk_batch_problem *P, int64_t np, int reduct
         cudaGraph_t graph = nullptr;
         cudaGraphExec_t exec = nullptr;
         FK_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-        one_iteration();
+        try {
+            one_iteration();
+        } catch (...) {
+            // end the capture so that the caller's stream stays usable
+            cudaGraph_t partial = nullptr;
+            (void)cudaStreamEndCapture(s, &partial);
+            if (partial) cudaGraphDestroy(partial);
+            (void)cudaGetLastError();
+            throw;
+        }
         cudaError_t ce = cudaStreamEndCapture(s, &graph);
         if (ce != cudaSuccess) {
             set_error("graph capture failed: %s", cudaGetErrorString(ce));
@@ -1125,7 +1133,6 @@ fk_status batched_fit_impl(Ctx &ctx, fk_batch_problem *P, int64_t np, int reduct
             if (rep->fit_n_iter) rep->fit_n_iter[f] = st[f].n_iter;
         }
     }
-    for (auto &e : ev) cudaEventDestroy(e);
     return FK_OK;
 }
 

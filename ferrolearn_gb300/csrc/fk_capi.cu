@@ -10,6 +10,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstring>
+#include <memory>
 #include <vector>
 
 #include "fk_internal.cuh"
@@ -313,11 +314,10 @@ fk_status fit_impl(fk_ctx *ctxp, const TX *x_in, int64_t n, int64_t d, const fk_
     }
     const bool timing = p->collect_timing != 0 && rep != nullptr;
     cudaStream_t s = ctx.stream;
-    cudaEvent_t t_begin = nullptr, t_end = nullptr;
+    std::unique_ptr<Events<2>> tev;  // whole-call timing: [0] begin, [1] end
     if (timing) {
-        FK_CUDA(cudaEventCreate(&t_begin));
-        FK_CUDA(cudaEventCreate(&t_end));
-        FK_CUDA(cudaEventRecord(t_begin, s));
+        tev.reset(new Events<2>());
+        FK_CUDA(cudaEventRecord((*tev)[0], s));
     }
     const size_t kd = (size_t)k * d;
     const TX *x = stage_in<TX>(ctx, BUF_X, x_in, (size_t)n * d);
@@ -335,16 +335,7 @@ fk_status fit_impl(fk_ctx *ctxp, const TX *x_in, int64_t n, int64_t d, const fk_
     DevScalars *sc = (DevScalars *)ctx.get(BUF_SCALARS, sizeof(DevScalars));
     FK_CUDA(cudaMemsetAsync(labels2, 0, sizeof(int32_t) * 2 * (size_t)n, s));
     SortPlan plan = make_sort_plan(n, (int)k);
-    cudaEvent_t iter_done[2];
-    FK_CUDA(cudaEventCreateWithFlags(&iter_done[0], cudaEventDisableTiming));
-    FK_CUDA(cudaEventCreateWithFlags(&iter_done[1], cudaEventDisableTiming));
-    struct EventPair {
-        cudaEvent_t *e;
-        ~EventPair() {
-            cudaEventDestroy(e[0]);
-            cudaEventDestroy(e[1]);
-        }
-    } ev_guard{iter_done};
+    Events<2> iter_done(cudaEventDisableTiming);
 
     // a slot of its own: the runs after the first read it while the mixed
     // updates use their own scratch (which may grow and move)
@@ -485,13 +476,11 @@ fk_status fit_impl(fk_ctx *ctxp, const TX *x_in, int64_t n, int64_t d, const fk_
         copy_out<uint64_t>(ctx, labels_out, l64, (size_t)n);
     }
     if (timing) {
-        FK_CUDA(cudaEventRecord(t_end, s));
-        FK_CUDA(cudaEventSynchronize(t_end));
+        FK_CUDA(cudaEventRecord((*tev)[1], s));
+        FK_CUDA(cudaEventSynchronize((*tev)[1]));
         float ms = 0.f;
-        FK_CUDA(cudaEventElapsedTime(&ms, t_begin, t_end));
+        FK_CUDA(cudaEventElapsedTime(&ms, (*tev)[0], (*tev)[1]));
         rep->ms_total = ms;
-        cudaEventDestroy(t_begin);
-        cudaEventDestroy(t_end);
     }
     FK_CUDA(cudaStreamSynchronize(s));
     flush_timers(ctx);

@@ -164,6 +164,23 @@ struct Ctx {
     void bind();                         // make the device current
 };
 
+// Events owned by one call, destroyed on every way out of it (errors are
+// thrown as Error and caught at the C boundary).
+template <int N>
+struct Events {
+    cudaEvent_t e[N] = {};
+    explicit Events(unsigned flags = cudaEventDefault) {
+        for (auto &x : e) FK_CUDA(cudaEventCreateWithFlags(&x, flags));
+    }
+    ~Events() {
+        for (auto x : e)
+            if (x) cudaEventDestroy(x);
+    }
+    Events(const Events &) = delete;
+    Events &operator=(const Events &) = delete;
+    cudaEvent_t &operator[](int i) { return e[i]; }
+};
+
 // Phase timer: records a pair of events on the stream and leaves the
 // reading to flush_timers(), so timing never adds a host synchronisation
 // inside the Lloyd loop.

@@ -50,18 +50,14 @@ double time_peak(Ctx &ctx, int iters) {
     const int blocks = ctx.num_sms * 4, threads = 256;
     peak_kernel<T, OP><<<blocks, threads, 0, ctx.stream>>>((T)1.0000001, (T)0.5, 2, out);
     FK_LAUNCH_CHECK();
-    cudaEvent_t e0, e1;
-    FK_CUDA(cudaEventCreate(&e0));
-    FK_CUDA(cudaEventCreate(&e1));
-    FK_CUDA(cudaEventRecord(e0, ctx.stream));
+    Events<2> ev;
+    FK_CUDA(cudaEventRecord(ev[0], ctx.stream));
     peak_kernel<T, OP><<<blocks, threads, 0, ctx.stream>>>((T)1.0000001, (T)0.5, iters, out);
     FK_LAUNCH_CHECK();
-    FK_CUDA(cudaEventRecord(e1, ctx.stream));
-    FK_CUDA(cudaEventSynchronize(e1));
+    FK_CUDA(cudaEventRecord(ev[1], ctx.stream));
+    FK_CUDA(cudaEventSynchronize(ev[1]));
     float ms = 0.f;
-    FK_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
+    FK_CUDA(cudaEventElapsedTime(&ms, ev[0], ev[1]));
     const double ops = (double)blocks * threads * iters * 16.0 * CHAINS * (OP == 0 ? 2.0 : 1.0);
     return ops / (ms * 1e-3);
 }
