@@ -83,6 +83,25 @@ def load_peaks():
     return 6800.0, 1900.0, 1700.0, "fallback"
 
 
+def max_over_ranks(value, device):
+    """The slowest rank's value (the job ends with it); the value itself on
+    one rank or without a process group. device: where the collective's
+    tensor lives ("cuda" under NCCL, "cpu" under gloo)."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(value)
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(iters_per_rank, ms_slowest, world):
+    """Whole-job Lloyd iterations/s: every replica's iterations over the
+    slowest replica's time."""
+    return world * iters_per_rank / (ms_slowest / 1e3)
+
+
 class ClockSampler:
     """nvidia-smi clocks + throttle reasons sampled every 20 ms; summary()
     keeps the samples taken while the timed region ran (mark_start/mark_end,
@@ -189,21 +208,22 @@ def initial_centres(w, xd, ctx):
 def cpu_baseline(w, seconds, threads):
     """Oracle (CPU restatement of kmeans.rs) on a bounded row sample; iters/s extrapolated to the full n."""
     from oracle import oracle as O
-    x64 = w["x"].astype(np.float64)
     c = w["init"]
-    n = x64.shape[0]
+    n = w["x"].shape[0]
     rows = 2048
     while True:
+        xs = w["x"][:rows].astype(np.float64)  # only the sampled rows are widened
         t0 = time.perf_counter()
-        O.lloyd_step(x64[:rows], c, nthreads=threads)
+        O.lloyd_step(xs, c, nthreads=threads)
         dt = time.perf_counter() - t0
         if dt >= seconds / 4 or rows >= n:
             break
         rows = min(n, int(rows * max(2.0, (seconds / 4) / max(dt, 1e-3))))
+    xs = w["x"][:rows].astype(np.float64)
     reps = max(1, int(seconds / max(dt, 1e-3)))
     t0 = time.perf_counter()
     for _ in range(reps):
-        O.lloyd_step(x64[:rows], c, nthreads=threads)
+        O.lloyd_step(xs, c, nthreads=threads)
     dt = (time.perf_counter() - t0) / reps
     per_iter = dt * n / rows
     return {"value": 1.0 / per_iter, "unit": "iters/s", "cores": threads, "kind": "port",
@@ -221,15 +241,15 @@ def run_reference(args):
         w["init"] = w["x"][np.random.default_rng(1).permutation(w["x"].shape[0])[: w["k"]]].astype(np.float64)
     threads = os.cpu_count() or 1
     from oracle import oracle as O
-    x64 = w["x"].astype(np.float64)
-    n = x64.shape[0]
+    n, d = w["x"].shape
     rows = max(1024, min(n, int(20000 * args.scale) if args.scale < 1 else 20000))
+    xs = w["x"][:rows].astype(np.float64)  # the sampled rows, widened exactly
     c = w["init"]
     for _ in range(max(1, args.warmup)):
-        O.lloyd_step(x64[:rows], c, nthreads=threads)
+        O.lloyd_step(xs, c, nthreads=threads)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        O.lloyd_step(x64[:rows], c, nthreads=threads)
+        O.lloyd_step(xs, c, nthreads=threads)
     dt = (time.perf_counter() - t0) / args.steps
     per_iter = dt * n / rows
     v = 1.0 / per_iter
@@ -237,7 +257,7 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": v, "unit": "iters/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_iter * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": w["name"], "n": n, "d": int(x64.shape[1]), "k": w["k"], "X": "f32 widened to f64",
+        "config": {"workload": w["name"], "n": n, "d": int(d), "k": w["k"], "X": "f32 widened to f64",
                    "l2": "inputs larger than L2"},
         "cpu_baseline": {"value": v, "unit": "iters/s", "cores": threads, "kind": "port",
                          "sample": f"{rows} of {n} rows per step, extrapolated x{n / rows:.1f}"},
@@ -393,14 +413,11 @@ def run_ours(args):
         clocks.mark_end()
     launches = int(_native.lib().fk_debug_launch_count() - l0)
     ms = start.elapsed_time(end)
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms, "cuda")
     rep = fitted.report
     iters = fitted.n_iter()
     assert iters == args.steps, (iters, args.steps)
-    ips = world * iters / (ms / 1e3)
+    ips = job_rate(iters, ms, world)
     # dominant kernel: the tensor-core contraction (CUDA events on the library's
     # stream around each launch); the SIMT forms time the whole assignment
     assign_ms = rep["ms_assign"] / iters

@@ -46,3 +46,61 @@ def test_reference_arm_line():
     assert out["e2e"]["value"] == out["value"]
     assert out["e2e"]["h2d_bytes_per_step"] == 0 and out["e2e"]["d2h_bytes_per_step"] == 0
     assert out["config"]["workload"] == "anisotropic_1024x128"
+
+
+_RANK_SCRIPT = r"""
+import os, sys, json
+sys.path.insert(0, sys.argv[1])
+import torch.distributed as dist
+import bench
+dist.init_process_group("gloo", init_method="env://")
+rank, world = dist.get_rank(), dist.get_world_size()
+ms = 100.0 + 50.0 * rank  # rank 1 is the slower replica
+slowest = bench.max_over_ranks(ms, "cpu")
+print(json.dumps({"rank": rank, "slowest": slowest, "rate": bench.job_rate(50, slowest, world)}))
+dist.destroy_process_group()
+"""
+
+
+def _free_port():
+    import socket
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+@pytest.mark.timeout(300)
+def test_replicas_time_the_slowest_rank_gloo_world_2():
+    # the N > 1 path: replicas, no data-path collective, one all-reduce (MAX)
+    # of the timed region, whole-job rate = all ranks' iterations over it
+    port = str(_free_port())
+    procs = []
+    for rank in range(2):
+        env = dict(os.environ, RANK=str(rank), WORLD_SIZE="2", LOCAL_RANK=str(rank), MASTER_ADDR="127.0.0.1",
+                   MASTER_PORT=port)
+        procs.append(subprocess.Popen([sys.executable, "-c", _RANK_SCRIPT, ROOT], env=env, stdout=subprocess.PIPE,
+                                      stderr=subprocess.PIPE, text=True, cwd=ROOT))
+    outs = []
+    for p in procs:
+        o, e = p.communicate(timeout=240)
+        assert p.returncode == 0, e[-2000:]
+        outs.append(json.loads([ln for ln in o.splitlines() if ln.startswith("{")][0]))
+    for o in outs:
+        assert o["slowest"] == 150.0
+        assert abs(o["rate"] - 2 * 50 / 0.150) < 1e-9
+
+
+def test_single_rank_needs_no_process_group():
+    sys.path.insert(0, ROOT)
+    import bench
+    assert bench.max_over_ranks(12.5, "cpu") == 12.5
+    assert bench.job_rate(50, 100.0, 1) == 500.0
+
+
+def test_reference_arm_other_ranks_exit_without_work():
+    env = dict(os.environ, RANK="1", WORLD_SIZE="2")
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--scale", "0.005",
+                        "--steps", "1", "--warmup", "1"], capture_output=True, text=True, cwd=ROOT, env=env,
+                       timeout=300)
+    assert r.returncode == 0, r.stderr[-2000:]
+    assert not [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
