@@ -140,16 +140,23 @@ void host_draws(uint64_t seed, int64_t count, double *out) {
 }
 
 
-// Plain: every entry point. BF16: f64 semantics (f64 or f32x64). FP8: X
-// stored as f32 with f64 semantics (f32x64) only.
+// Plain: every entry point. BF16 and FP8: f64 semantics on X stored as f32
+// (the f32x64 entry points), the form whose rows the tensor-core operands,
+// the exact integer centroid sums and the re-check cascade are built for.
 template <typename TX, typename TC>
 bool precision_ok(int prec) {
-    constexpr bool f64_semantics = std::is_same<TC, double>::value;
-    constexpr bool x_f32 = std::is_same<TX, float>::value;
+    constexpr bool mixed_ok = std::is_same<TC, double>::value && std::is_same<TX, float>::value;
     if (prec == FK_PRECISION_PLAIN) return true;
-    if (prec == FK_PRECISION_MIXED_BF16) return f64_semantics;
-    if (prec == FK_PRECISION_MIXED_FP8) return f64_semantics && x_f32;
+    if (prec == FK_PRECISION_MIXED_BF16 || prec == FK_PRECISION_MIXED_FP8) return mixed_ok;
     return false;
+}
+
+void precision_error(int prec) {
+    if (prec == FK_PRECISION_MIXED_BF16 || prec == FK_PRECISION_MIXED_FP8)
+        set_error("precision %d (tensor-core form) reads X stored as f32 with f64 semantics: use the f32x64 "
+                  "entry points", prec);
+    else
+        set_error("precision %d is not available for this entry point", prec);
 }
 
 // The ranges every entry point accepts: rows index int32 labels, and the
@@ -195,8 +202,8 @@ void lloyd_iteration(Ctx &ctx, const TX *x, int64_t n, int d, const TC *c, int k
             launch_assign_direct<TX, TC>(x, n, d, c, k, labels, mind, s);
             launch_sum_fixed<TC>(mind, n, part, &sc->inertia, s);
         } else {
-            if constexpr (std::is_same<TC, double>::value) {
-                run_assign_mixed<TX>(ctx, x, n, d, c, k, prec, labels, nullptr, sc, x_changed);
+            if constexpr (std::is_same<TX, float>::value && std::is_same<TC, double>::value) {
+                run_assign_mixed(ctx, x, n, d, c, k, prec, labels, nullptr, sc, x_changed);
             }
         }
     }
@@ -223,19 +230,17 @@ void lloyd_iteration(Ctx &ctx, const TX *x, int64_t n, int d, const TC *c, int k
             }
         }
         launch_sort_by_cluster(plan, labels, seg, tmp, members, s);
-        if (prec == FK_PRECISION_PLAIN) {
-            launch_update_centroids<TX, TC>(plan, x, d, members, seg, c, nc, sc, s);
-        } else {
-            double *part = (double *)ctx.get(BUF_OUT2, sizeof(double) * (size_t)plan.k * d + 64);
-            if constexpr (std::is_same<TX, float>::value && std::is_same<TC, double>::value) {
+        if constexpr (std::is_same<TX, float>::value && std::is_same<TC, double>::value) {
+            if (prec != FK_PRECISION_PLAIN) {
+                double *part = (double *)ctx.get(BUF_OUT2, sizeof(double) * (size_t)plan.k * d + 64);
                 const MixedStats *st = (const MixedStats *)ctx.get(BUF_CF32, sizeof(MixedStats));
                 void *scratch = ctx.get(BUF_FIXPART, update_exact_scratch_bytes(plan.k, d));
                 launch_update_centroids_exact(plan, x, d, members, seg, c, nc, sc, &st->amax, part, scratch, s);
-            } else {
-                launch_update_centroids<TX, TC>(plan, x, d, members, seg, c, nc, sc, s, part);
+                launch_mixed_inertia(ctx, part, (int64_t)plan.k * d, sc);
+                return;
             }
-            launch_mixed_inertia(ctx, part, (int64_t)plan.k * d, sc);
         }
+        launch_update_centroids<TX, TC>(plan, x, d, members, seg, c, nc, sc, s);
     }
 }
 
@@ -299,7 +304,7 @@ fk_status fit_impl(fk_ctx *ctxp, const TX *x_in, int64_t n, int64_t d, const fk_
         return FK_ERR_NULL_POINTER;
     }
     if (!precision_ok<TX, TC>(p->precision)) {
-        set_error("precision %d is not available for this entry point", p->precision);
+        precision_error(p->precision);
         return FK_ERR_UNSUPPORTED;
     }
     if (!init_in && p->draws && p->n_draws < 0) {
@@ -507,7 +512,7 @@ fk_status step_impl(fk_ctx *ctxp, const TX *x_in, int64_t n, int64_t d, const TC
         return FK_ERR_NULL_POINTER;
     }
     if (!precision_ok<TX, TC>(prec)) {
-        set_error("precision %d is not available for this entry point", prec);
+        precision_error(prec);
         return FK_ERR_UNSUPPORTED;
     }
     if (fk_status st = check_shape(n, d, k)) return st;
@@ -563,7 +568,7 @@ fk_status predict_impl(fk_ctx *ctxp, const TC *c_in, int64_t k, int64_t d_fit, c
         return FK_ERR_NULL_POINTER;
     }
     if (!precision_ok<TX, TC>(prec)) {
-        set_error("precision %d is not available for this entry point", prec);
+        precision_error(prec);
         return FK_ERR_UNSUPPORTED;
     }
     if (fk_status st = check_shape(n, d, k)) return st;
@@ -575,10 +580,10 @@ fk_status predict_impl(fk_ctx *ctxp, const TC *c_in, int64_t k, int64_t d_fit, c
     if (prec == FK_PRECISION_PLAIN) {
         launch_assign_direct<TX, TC>(x, n, (int)d, c, (int)k, labels, nullptr, s);
     } else {
-        if constexpr (std::is_same<TC, double>::value) {
+        if constexpr (std::is_same<TX, float>::value && std::is_same<TC, double>::value) {
             DevScalars *sc = (DevScalars *)ctx.get(BUF_SCALARS, sizeof(DevScalars));
             FK_CUDA(cudaMemsetAsync(sc, 0, sizeof(DevScalars), s));
-            run_assign_mixed<TX>(ctx, x, n, (int)d, c, (int)k, prec, labels, nullptr, sc, true);
+            run_assign_mixed(ctx, x, n, (int)d, c, (int)k, prec, labels, nullptr, sc, true);
         }
     }
     if (is_device_ptr(labels_out)) {

@@ -290,8 +290,9 @@ template <typename T>
 void run_kmeanspp(Ctx &ctx, const T *x, int64_t n, int d, int k, const double *draws_dev,
                   int64_t n_draws, T *centers_out, int64_t *draws_used);
 
-// Mixed-precision assignment (BF16 tcgen05 / FP32 SIMT approximate pass,
-// FP64 exact re-check). Results identical to the FP64 direct form.
+// Mixed-precision assignment (BF16 / FP8 tcgen05 approximate pass, FP32 and
+// FP64 exact re-check) of X stored as f32. Results identical to the FP64
+// direct form.
 template <typename TX>
 void run_assign_mixed(Ctx &ctx, const TX *x, int64_t n, int d, const double *c, int k,
                       int precision, int32_t *labels, double *mind, DevScalars *scalars,

@@ -875,66 +875,6 @@ __global__ void __launch_bounds__(256)
     }
 }
 
-// One warp per listed row: FP32 distances to every centre give an upper
-// bound UB of the minimum; only centres whose lower bound reaches UB (or
-// whose FP32 value is not finite) are scored exactly in FP64, and the lowest
-// index wins among equal FP64 distances below F::MAX, exactly as
-// nearest_center.
-template <typename TX>
-__global__ void full_rescore_kernel(const TX *__restrict__ x, int d, const double *__restrict__ c,
-                                    const float *__restrict__ c32, const float *__restrict__ ec32, int k,
-                                    const int32_t *__restrict__ list, const unsigned long long *count_ptr,
-                                    DevScalars *sc, int32_t *__restrict__ labels) {
-    const unsigned long long cnt = *count_ptr;
-    const int lane = threadIdx.x & 31;
-    const unsigned long long wid = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const unsigned long long nw = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
-    for (unsigned long long s = wid; s < cnt; s += nw) {
-        const int64_t r = list[s];
-        const TX *row = x + r * d;
-        float ub = INFINITY;
-        if constexpr (std::is_same<TX, float>::value) {
-            for (int q = lane; q < k; q += 32) {
-                float v = sqeuc32(row, c32 + (int64_t)q * d, d);
-                float hi = __fadd_ru(v, bound32(v, ec32[q], d));
-                if (hi < ub) ub = hi;  // NaN never lowers the bound
-            }
-#pragma unroll
-            for (int off = 16; off >= 1; off >>= 1) ub = fminf(ub, __shfl_xor_sync(0xffffffffu, ub, off));
-        }
-        double b1 = DBL_MAX, b2 = DBL_MAX;
-        int i1 = INT32_MAX;
-        for (int q = lane; q < k; q += 32) {
-            if constexpr (std::is_same<TX, float>::value) {
-                float v = sqeuc32(row, c32 + (int64_t)q * d, d);
-                if (__fsub_rd(v, bound32(v, ec32[q], d)) > ub) continue;  // certainly above the minimum
-            }
-            double v = sqeuc64(row, c + (int64_t)q * d, d);
-            if (v < b1) { b2 = b1; b1 = v; i1 = q; }
-            else if (v < b2) { b2 = v; }
-        }
-#pragma unroll
-        for (int off = 16; off >= 1; off >>= 1) {
-            double o1 = __shfl_xor_sync(0xffffffffu, b1, off);
-            double o2 = __shfl_xor_sync(0xffffffffu, b2, off);
-            int oi = __shfl_xor_sync(0xffffffffu, i1, off);
-            if (o1 < b1 || (o1 == b1 && oi < i1)) {
-                b2 = fmin(b1, o2);
-                b1 = o1;
-                i1 = oi;
-            } else {
-                b2 = fmin(b2, o1);
-            }
-        }
-        if (lane == 0) {
-            labels[r] = i1 == INT32_MAX ? 0 : i1;
-            atomicAdd(&sc->recheck_rows, 1ULL);
-            atomicAdd(&sc->full_rows, 1ULL);
-            if (i1 != INT32_MAX && b2 < DBL_MAX && near_tie(b1, b2)) atomicAdd(&sc->near_tie_rows, 1ULL);
-        }
-    }
-}
-
 // One CTA per listed row, f32 rows: the row in shared memory, FP32 distances
 // to every centre (threads over centres, four centres per thread at a time,
 // reading the transposed f32 centres: coalesced and L2-resident), kept in
@@ -1488,11 +1428,8 @@ void run_assign_mixed(Ctx &ctx, const TX *x, int64_t n, int d, const double *c, 
         set_error("precision %d is not built", precision);
         fail(FK_ERR_UNSUPPORTED);
     }
+    static_assert(std::is_same<TX, float>::value, "the mixed forms read X stored as f32 (the f32x64 entry points)");
     const bool fp8 = precision == FK_PRECISION_MIXED_FP8;
-    if (fp8 && !std::is_same<TX, float>::value) {
-        set_error("the FP8 form needs X stored as f32 (the f32x64 entry points)");
-        fail(FK_ERR_UNSUPPORTED);
-    }
     if (d < 1 || d > 256) {
         set_error("the tensor-core path supports 1 <= d <= 256 (got %d)", d);
         fail(FK_ERR_UNSUPPORTED);
@@ -1525,12 +1462,7 @@ void run_assign_mixed(Ctx &ctx, const TX *x, int64_t n, int d, const double *c, 
     else
         pair_rescore_kernel<TX><<<grid, 256, 0, s>>>(x, d, c, B.c32, B.ec32, pairs, sc, labels, f64_items);
     FK_LAUNCH_CHECK();
-    if constexpr (std::is_same<TX, float>::value) {
-        second_pass(ctx, x, n, d, c, k, B, mp.mu_norm, full, labels, sc, f64_items);
-    } else {
-        full_rescore_kernel<TX><<<grid, 256, 0, s>>>(x, d, c, B.c32, B.ec32, k, full, &sc->full_count, sc, labels);
-        FK_LAUNCH_CHECK();
-    }
+    second_pass(ctx, x, n, d, c, k, B, mp.mu_norm, full, labels, sc, f64_items);
     launch_f64_decide<TX>(ctx, x, d, c, f64_items, sc, labels);
 }
 
@@ -1544,8 +1476,6 @@ void launch_mixed_inertia(Ctx &ctx, const double *part, int64_t m, DevScalars *s
 
 template void run_assign_mixed<float>(Ctx &, const float *, int64_t, int, const double *, int, int, int32_t *,
                                       double *, DevScalars *, bool);
-template void run_assign_mixed<double>(Ctx &, const double *, int64_t, int, const double *, int, int, int32_t *,
-                                       double *, DevScalars *, bool);
 
 // Diagnostics for the tests: one tensor-core pass over x (f32, on the device)
 // against c (f64), returning the raw accumulators of CTA 0's first tile and

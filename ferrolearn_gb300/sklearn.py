@@ -6,15 +6,19 @@ random_state=None), the same fitted attributes (cluster_centers_, labels_,
 inertia_, n_iter_) and the same methods (fit, predict, transform,
 fit_predict), backed by ferrolearn_gb300.KMeans instead of the PyO3 class
 _RsKMeans. Two keywords are added: `precision` ("plain": the reference's FP64
-arithmetic; "bf16" / "fp8": the tensor-core forms, whose labels equal the FP64
-ones) and `device` (the GPU index).
+arithmetic; "bf16" / "fp8": the tensor-core forms, which read X as float32
+and whose labels equal the FP64 ones on those rows) and `device` (the GPU
+index). A tensor-core fit of data that float32 does not hold exactly warns.
 
 With scikit-learn installed the class derives from its BaseEstimator,
 ClusterMixin and TransformerMixin (get_params / set_params / clone work like
 the reference's); without it the same class stands alone.
 """
+import warnings
+
 import numpy as np
 
+from .kmeans import PLAIN, _prec
 from .kmeans import KMeans as _KMeans
 from .kmeans import default_context
 
@@ -45,8 +49,11 @@ class KMeans(*_BASES):
         self.precision = precision
         self.device = device
 
+    def _plain(self):
+        return _prec(self.precision) == PLAIN
+
     def _model(self):
-        dtype = "f64" if self.precision == "plain" else "f32x64"
+        dtype = "f64" if self._plain() else "f32x64"
         m = _KMeans(self.n_clusters, dtype=dtype).with_max_iter(self.max_iter).with_tol(self.tol) \
             .with_n_init(self.n_init).with_precision(self.precision)
         if self.random_state is not None:
@@ -55,8 +62,15 @@ class KMeans(*_BASES):
 
     def _rows(self, X):
         x = _as_f64(X)
+        if self._plain():
+            return x
         # the mixed precisions read X as f32 (KMeans<f64> semantics on f32 storage)
-        return x if self.precision == "plain" else np.ascontiguousarray(x, dtype=np.float32)
+        x32 = np.ascontiguousarray(x, dtype=np.float32)
+        if not np.array_equal(x32, x, equal_nan=True):
+            warnings.warn(f"precision={self.precision!r} reads X as float32 and X holds values that float32 "
+                          "rounds: the results are those of the rounded rows (use precision='plain' for the "
+                          "float64 rows)", stacklevel=3)
+        return x32
 
     def fit(self, X, y=None):
         x = self._rows(X)

@@ -43,10 +43,12 @@ typedef enum fk_status {
  *  FK_PRECISION_MIXED_BF16  BF16 tensor-core contraction (tcgen05, TMEM) with
  *                           a derived per-row error bound; rows whose top-2
  *                           margin is inside the bound are re-scored exactly
- *                           in FP64 direct form. F = f64 only.
+ *                           in FP64 direct form.
  *  FK_PRECISION_MIXED_FP8   FP8 E4M3 tensor-core contraction (per-row
  *                           power-of-two scales) with the same bound and
- *                           exact re-check; X stored as f32 (_f32x64).      */
+ *                           exact re-check.
+ *  Both mixed forms run on the _f32x64 entry points only (F = f64, X stored
+ *  as f32); the others return FK_ERR_UNSUPPORTED for them.              */
 typedef enum fk_precision {
     FK_PRECISION_PLAIN = 0,
     FK_PRECISION_MIXED_BF16 = 1,

@@ -57,3 +57,24 @@ def test_wrapper_fit_predict_transform_on_gpu(precision):
     assert np.array_equal(km.fit_predict(x), km.labels_)
     km2 = pickle.loads(pickle.dumps(km))
     assert np.array_equal(km2.predict(x), km.predict(x))
+
+
+def test_tensor_core_forms_read_float32_rows():
+    # exact float32 rows pass silently; rounded ones warn before any device work
+    km = KMeans(n_clusters=2, precision="bf16")
+    exact = np.array([[0.5, 1.0], [2.0, -3.25]])
+    import warnings
+    with warnings.catch_warnings():
+        warnings.simplefilter("error")
+        assert km._rows(exact).dtype == np.float32
+    with pytest.warns(UserWarning, match="float32"):
+        km._rows(np.array([[0.1, 1.0], [2.0, 3.0]]))
+    assert KMeans(n_clusters=2)._rows(np.array([[0.1, 1.0]])).dtype == np.float64
+    assert KMeans(n_clusters=2, precision=0)._plain()
+
+
+def test_tensor_core_forms_need_float32_storage():
+    # the library's f64 entry points refuse the mixed forms
+    for prec in ("bf16", "fp8"):
+        with pytest.raises(F.Unsupported, match="f32x64"):
+            F.KMeans(2, dtype="f64").with_precision(prec).fit(np.ones((4, 2)))
