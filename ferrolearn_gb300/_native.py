@@ -24,7 +24,21 @@ EXPORTS = [
     "fk_kmeans_transform_f64", "fk_kmeans_transform_f32",
     "fk_kmeans_plus_plus_f64", "fk_kmeans_plus_plus_f32", "fk_debug_tc_probe",
     "fk_debug_measure_peaks", "fk_kmeans_score_f64_noalloc", "fk_kmeans_fit_batched_f32", "fk_debug_tc_plan",
+    "fk_minibatch_params_default", "fk_minibatch_fit_f64", "fk_minibatch_fit_f32", "fk_minibatch_batch_indices",
 ]
+
+
+class MiniBatchParams(C.Structure):
+    _fields_ = [
+        ("n_clusters", C.c_int64),
+        ("batch_size", C.c_int64),
+        ("max_iter", C.c_int64),
+        ("tol", C.c_double),
+        ("n_init", C.c_int64),
+        ("random_state", C.c_uint64),
+        ("has_random_state", C.c_int32),
+        ("init", C.c_int32),
+    ]
 
 
 class BatchProblem(C.Structure):
@@ -153,6 +167,14 @@ def _declare(lib):
     lib.fk_kmeans_fit_batched_f32.restype = st
     lib.fk_debug_tc_plan.argtypes = [i64, i64, i64, i32, i32, i32, p]
     lib.fk_debug_tc_plan.restype = st
+    lib.fk_minibatch_params_default.argtypes = [C.POINTER(MiniBatchParams), i64]
+    lib.fk_minibatch_params_default.restype = None
+    for suf in ("f64", "f32"):
+        f = getattr(lib, f"fk_minibatch_fit_{suf}")
+        f.argtypes = [p, p, i64, i64, C.POINTER(MiniBatchParams), p, p, p, p, p, p, C.POINTER(FitReport)]
+        f.restype = st
+    lib.fk_minibatch_batch_indices.argtypes = [u64, i64, i64, i64, i64, p]
+    lib.fk_minibatch_batch_indices.restype = st
 
 
 def lib():

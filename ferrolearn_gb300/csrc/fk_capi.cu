@@ -9,8 +9,10 @@
 // only host traffic per iteration is one 64-byte scalar block read back.
 #include <cmath>
 #include <cstdarg>
+#include <algorithm>
 #include <cstring>
 #include <memory>
+#include <unordered_map>
 #include <vector>
 
 #include "fk_internal.cuh"
@@ -672,6 +674,218 @@ fk_status kpp_impl(fk_ctx *ctxp, const T *x_in, int64_t n, int64_t d, int64_t k,
     return FK_OK;
 }
 
+// ----------------------------------------------------------- minibatch --
+// The library's uniform stream from position pos of seed: every draw first
+// advances the state by the golden gamma, so a position is one multiply.
+struct UniformStream {
+    uint64_t state;
+    UniformStream(uint64_t seed, int64_t pos) : state(seed + (uint64_t)pos * 0x9E3779B97F4A7C15ULL) {}
+    double next() { return (double)(splitmix64(&state) >> 11) * (1.0 / 9007199254740992.0); }
+    // random_range(0..n) as min(floor(u n), n - 1)
+    int64_t range(int64_t n) {
+        const int64_t i = (int64_t)std::floor(next() * (double)n);
+        return i < 0 ? 0 : (i >= n ? n - 1 : i);
+    }
+};
+
+// min(count, n) picks of a Fisher-Yates pass over the pool 0..n, pick i
+// swapping position i with i + random_range(0..n - i): random_init_mb
+// (mini_batch_kmeans.rs:324-338) and sample_batch_indices (:451-472). A
+// partial pass keeps only the displaced entries of the pool (a map), so a
+// batch costs O(batch) whatever n; a full pass (count >= n) uses the pool.
+template <typename I>
+int64_t fisher_yates_picks(UniformStream &g, int64_t n, int64_t count, std::unordered_map<int64_t, int64_t> &moved,
+                           std::vector<int64_t> &pool, I *out) {
+    const int64_t m = count < n ? count : n;
+    if (m == n) {
+        pool.resize((size_t)n);
+        for (int64_t i = 0; i < n; i++) pool[(size_t)i] = i;
+        for (int64_t i = 0; i < n; i++) {
+            const int64_t j = i + g.range(n - i);
+            std::swap(pool[(size_t)i], pool[(size_t)j]);
+            out[i] = (I)pool[(size_t)i];
+        }
+        return m;
+    }
+    moved.clear();
+    auto at = [&](int64_t t) {
+        auto it = moved.find(t);
+        return it == moved.end() ? t : it->second;
+    };
+    for (int64_t i = 0; i < m; i++) {
+        const int64_t j = i + g.range(n - i);
+        const int64_t vi = at(i), vj = at(j);
+        moved[i] = vj;
+        moved[j] = vi;
+        out[i] = (I)vj;
+    }
+    return m;
+}
+
+// MiniBatchKMeans::fit (mini_batch_kmeans.rs:492-591) on the GPU. Per run:
+// the initial centres, then per iteration the batch rows gathered, their
+// nearest centres (the direct-form assignment kernel), the in-order update
+// and the max shift; the early stop reads the shift back only when tol > 0
+// (a shift is never below a tol <= 0). The batch indices come from the host
+// stream, uploaded a chunk of iterations at a time.
+template <typename T>
+fk_status minibatch_impl(fk_ctx *ctxp, const T *x_in, int64_t n, int64_t d, const fk_minibatch_params *p,
+                         const T *init_in, T *centers_out, uint64_t *labels_out, T *inertia_out, int64_t *n_iter_out,
+                         int64_t *best_run_out, fk_fit_report *rep) {
+    Ctx &ctx = *reinterpret_cast<Ctx *>(ctxp);
+    const int64_t k = p->n_clusters;
+    // Validation order of mini_batch_kmeans.rs:495-526.
+    if (k <= 0) {
+        set_error("Invalid parameter `n_clusters`: must be at least 1");
+        return FK_ERR_INVALID_PARAMETER;
+    }
+    if (p->batch_size <= 0) {
+        set_error("Invalid parameter `batch_size`: must be at least 1");
+        return FK_ERR_INVALID_PARAMETER;
+    }
+    if (p->n_init <= 0) {
+        set_error("Invalid parameter `n_init`: must be at least 1");
+        return FK_ERR_INVALID_PARAMETER;
+    }
+    if (n <= 0 || n < k) {
+        set_error("Insufficient samples: need at least %lld, got %lld (MiniBatchKMeans requires at least "
+                  "n_clusters samples)", (long long)k, (long long)(n < 0 ? 0 : n));
+        return FK_ERR_INSUFFICIENT_SAMPLES;
+    }
+    if (p->max_iter < 0) {
+        set_error("Invalid parameter `max_iter`: negative");
+        return FK_ERR_INVALID_PARAMETER;
+    }
+    if (p->init != FK_MB_INIT_KMEANS_PLUS_PLUS && p->init != FK_MB_INIT_RANDOM) {
+        set_error("Invalid parameter `init`: %d", p->init);
+        return FK_ERR_INVALID_PARAMETER;
+    }
+    if (!x_in || !centers_out || !labels_out || !inertia_out || !n_iter_out) {
+        set_error("required pointer is NULL");
+        return FK_ERR_NULL_POINTER;
+    }
+    if (fk_status st = check_shape(n, d, k)) return st;
+    ctx.bind();
+    if (rep) {
+        memset(rep, 0, sizeof(*rep));
+        rep->precision_used = FK_PRECISION_PLAIN;
+    }
+    cudaStream_t s = ctx.stream;
+    Events<2> tev;
+    FK_CUDA(cudaEventRecord(tev[0], s));
+    const size_t kd = (size_t)k * d;
+    const int64_t m = std::min(p->batch_size, n);  // rows per batch
+    const int64_t chunk = std::max<int64_t>(1, std::min<int64_t>(p->max_iter, ((int64_t)16 << 20) / m));
+    const T *x = stage_in<T>(ctx, BUF_X, x_in, (size_t)n * d);
+    const T *init = init_in ? stage_in<T>(ctx, BUF_INIT, init_in, kd * (size_t)p->n_init) : nullptr;
+    T *c = (T *)ctx.get(BUF_C0, sizeof(T) * kd);
+    T *old = (T *)ctx.get(BUF_MB_OLD, sizeof(T) * kd);
+    T *cbest = (T *)ctx.get(BUF_CBEST, sizeof(T) * kd);
+    long long *counts = (long long *)ctx.get(BUF_MB_COUNTS, sizeof(long long) * (size_t)k);
+    int32_t *labels = (int32_t *)ctx.get(BUF_LABELS, sizeof(int32_t) * (size_t)n);
+    int32_t *lbest = (int32_t *)ctx.get(BUF_LBEST, sizeof(int32_t) * (size_t)n);
+    T *mind = (T *)ctx.get(BUF_MIND, sizeof(T) * (size_t)n);
+    double *part = (double *)ctx.get(BUF_PARTIAL, sizeof(double) * (size_t)sum_fixed_partials(n));
+    DevScalars *sc = (DevScalars *)ctx.get(BUF_SCALARS, sizeof(DevScalars));
+    int32_t *didx = (int32_t *)ctx.get(BUF_MB_IDX, sizeof(int32_t) * (size_t)std::max(m * chunk, k));
+    T *xb = (T *)ctx.get(BUF_MB_XB, sizeof(T) * (size_t)m * d);
+    int32_t *blab = (int32_t *)ctx.get(BUF_MB_LAB, sizeof(int32_t) * (size_t)m);
+    std::vector<int32_t> hidx;
+    std::unordered_map<int64_t, int64_t> moved;
+    std::vector<int64_t> pool;
+    std::vector<double> hdraws;
+    const std::vector<long long> ones((size_t)k, 1LL);  // per-centre counts start at 1 (:543)
+    const uint64_t base = p->has_random_state ? p->random_state : 0;
+    const T tol = (T)p->tol;
+    bool have = false;
+    T best_inertia = FMax<T>::v();
+    int64_t best_iter = 0, best_run = 0;
+    for (int64_t run = 0; run < p->n_init; run++) {
+        const uint64_t seed = base + (uint64_t)run * 1000003ULL;
+        int64_t pos = 0;  // stream position after the initial centres
+        if (init) {
+            FK_CUDA(cudaMemcpyAsync(c, init + (size_t)run * kd, sizeof(T) * kd, cudaMemcpyDeviceToDevice, s));
+        } else if (p->init == FK_MB_INIT_RANDOM) {
+            UniformStream g(seed, 0);
+            hidx.resize((size_t)k);
+            fisher_yates_picks(g, n, k, moved, pool, hidx.data());
+            pos = k;
+            FK_CUDA(cudaMemcpyAsync(didx, hidx.data(), sizeof(int32_t) * (size_t)k, cudaMemcpyHostToDevice, s));
+            launch_gather_rows<T>(x, (int)d, didx, k, c, s);
+            FK_CUDA(cudaStreamSynchronize(s));  // hidx is refilled below
+        } else {
+            const int64_t n_draws = 1 + (k - 1) * kpp_trials_host(k);
+            hdraws.resize((size_t)n_draws);
+            host_draws(seed, n_draws, hdraws.data());
+            double *dd = (double *)ctx.get(BUF_DRAWS, sizeof(double) * (size_t)n_draws);
+            FK_CUDA(cudaMemcpyAsync(dd, hdraws.data(), sizeof(double) * (size_t)n_draws, cudaMemcpyHostToDevice, s));
+            run_kmeanspp<T>(ctx, x, n, (int)d, (int)k, dd, n_draws, c, &pos);  // synchronises
+        }
+        FK_CUDA(cudaMemcpyAsync(counts, ones.data(), sizeof(long long) * (size_t)k, cudaMemcpyHostToDevice, s));
+        UniformStream g(seed, pos);
+        int64_t n_iter = 0;
+        bool stop = false;
+        for (int64_t it0 = 0; it0 < p->max_iter && !stop; it0 += chunk) {
+            const int64_t ci = std::min(chunk, p->max_iter - it0);
+            FK_CUDA(cudaStreamSynchronize(s));  // the previous upload of hidx has completed
+            hidx.resize((size_t)(ci * m));
+            for (int64_t q = 0; q < ci; q++) fisher_yates_picks(g, n, p->batch_size, moved, pool, hidx.data() + q * m);
+            FK_CUDA(cudaMemcpyAsync(didx, hidx.data(), sizeof(int32_t) * (size_t)(ci * m), cudaMemcpyHostToDevice, s));
+            for (int64_t q = 0; q < ci; q++) {
+                launch_gather_rows<T>(x, (int)d, didx + q * m, m, xb, s);
+                launch_assign_direct<T, T>(xb, m, (int)d, c, (int)k, blab, nullptr, s);
+                launch_minibatch_update<T>(xb, blab, m, (int)d, (int)k, c, old, counts, &sc->shift_bits, s);
+                n_iter += 1;
+                if (tol > T(0)) {
+                    FK_CUDA(cudaMemcpyAsync(&ctx.host_scalars->shift_bits, &sc->shift_bits, sizeof(unsigned long long),
+                                            cudaMemcpyDeviceToHost, s));
+                    FK_CUDA(cudaStreamSynchronize(s));
+                    if (shift_from_bits<T>(ctx.host_scalars->shift_bits) < tol) {
+                        stop = true;
+                        break;
+                    }
+                }
+            }
+        }
+        // assign_clusters_mb (:343-376) over every row: the run's labels and inertia
+        FK_CUDA(cudaMemsetAsync(sc, 0, sizeof(DevScalars), s));
+        launch_assign_direct<T, T>(x, n, (int)d, c, (int)k, labels, mind, s);
+        launch_sum_fixed<T>(mind, n, part, &sc->inertia, s);
+        read_scalars(ctx, sc);
+        const T inertia = (T)ctx.host_scalars->inertia;
+        if (rep) rep->iterations_total += n_iter;
+        if (!have || inertia < best_inertia) {
+            have = true;
+            best_inertia = inertia;
+            best_iter = n_iter;
+            best_run = run;
+            FK_CUDA(cudaMemcpyAsync(cbest, c, sizeof(T) * kd, cudaMemcpyDeviceToDevice, s));
+            FK_CUDA(cudaMemcpyAsync(lbest, labels, sizeof(int32_t) * (size_t)n, cudaMemcpyDeviceToDevice, s));
+        }
+    }
+    copy_out<T>(ctx, centers_out, cbest, kd);
+    if (is_device_ptr(labels_out)) {
+        launch_labels_to_u64(lbest, n, labels_out, s);
+    } else {
+        uint64_t *l64 = (uint64_t *)ctx.get(BUF_OUT, sizeof(uint64_t) * (size_t)n);
+        launch_labels_to_u64(lbest, n, l64, s);
+        copy_out<uint64_t>(ctx, labels_out, l64, (size_t)n);
+    }
+    FK_CUDA(cudaEventRecord(tev[1], s));
+    FK_CUDA(cudaStreamSynchronize(s));
+    if (rep) {
+        float ms = 0.f;
+        FK_CUDA(cudaEventElapsedTime(&ms, tev[0], tev[1]));
+        rep->ms_total = ms;
+        rep->best_run = best_run;
+        rep->rows_assigned = n * p->n_init;
+    }
+    *inertia_out = best_inertia;
+    *n_iter_out = best_iter;
+    if (best_run_out) *best_run_out = best_run;
+    return FK_OK;
+}
+
 // Per-call state that points into a caller's report: timers not yet read
 // and the contraction timer's target. Dropped before and after every call,
 // so a call that failed half-way never writes into memory it no longer owns.
@@ -768,6 +982,56 @@ void fk_kmeans_params_default(fk_kmeans_params *p, int64_t n_clusters) {
     p->n_init = 10;
     p->has_random_state = 0;
     p->precision = FK_PRECISION_PLAIN;
+}
+
+void fk_minibatch_params_default(fk_minibatch_params *p, int64_t n_clusters) {
+    if (!p) return;
+    memset(p, 0, sizeof(*p));
+    p->n_clusters = n_clusters;  // MiniBatchKMeans::new, mini_batch_kmeans.rs:108-118
+    p->batch_size = 1024;
+    p->max_iter = 100;
+    p->tol = 0.0;
+    p->n_init = 3;
+    p->has_random_state = 0;
+    p->init = FK_MB_INIT_KMEANS_PLUS_PLUS;
+}
+
+fk_status fk_minibatch_fit_f64(fk_ctx *ctx, const double *x, int64_t n, int64_t d, const fk_minibatch_params *params,
+                               const double *init, double *c_out, uint64_t *l_out, double *in_out, int64_t *it_out,
+                               int64_t *best_out, fk_fit_report *rep) {
+    if (!params) return FK_ERR_NULL_POINTER;
+    return guarded(ctx, [&] {
+        return fk::minibatch_impl<double>(ctx, x, n, d, params, init, c_out, l_out, in_out, it_out, best_out, rep);
+    });
+}
+
+fk_status fk_minibatch_fit_f32(fk_ctx *ctx, const float *x, int64_t n, int64_t d, const fk_minibatch_params *params,
+                               const float *init, float *c_out, uint64_t *l_out, float *in_out, int64_t *it_out,
+                               int64_t *best_out, fk_fit_report *rep) {
+    if (!params) return FK_ERR_NULL_POINTER;
+    return guarded(ctx, [&] {
+        return fk::minibatch_impl<float>(ctx, x, n, d, params, init, c_out, l_out, in_out, it_out, best_out, rep);
+    });
+}
+
+fk_status fk_minibatch_batch_indices(uint64_t seed, int64_t pos, int64_t n, int64_t batch_size, int64_t iters,
+                                     int64_t *out) {
+    if (n <= 0 || batch_size <= 0 || iters < 0 || pos < 0) {
+        fk::set_error("Invalid parameter: n and batch_size must be at least 1, iters and pos non-negative");
+        return FK_ERR_INVALID_PARAMETER;
+    }
+    if (!out && iters > 0) return FK_ERR_NULL_POINTER;
+    try {
+        fk::UniformStream g(seed, pos);
+        std::unordered_map<int64_t, int64_t> moved;
+        std::vector<int64_t> pool;
+        const int64_t m = std::min(batch_size, n);
+        for (int64_t it = 0; it < iters; it++) fk::fisher_yates_picks(g, n, batch_size, moved, pool, out + it * m);
+    } catch (const std::bad_alloc &) {
+        fk::set_error("host allocation failed");
+        return FK_ERR_OOM;
+    }
+    return FK_OK;
 }
 
 fk_status fk_draws_f64(uint64_t seed, int64_t count, double *out) {

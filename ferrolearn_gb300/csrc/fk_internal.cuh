@@ -134,6 +134,7 @@ enum BufSlot {
     BUF_XB2, BUF_TOP8, BUF_OCT, BUF_EX, BUF_XAUG, BUF_ROWSCALE, BUF_ROWINFO2, BUF_STATS2, BUF_CB2, BUF_CAUG2,
     BUF_HALF2, BUF_INERTIA2, BUF_C2, BUF_XSTATE, BUF_XCOUNTS, BUF_MOVED, BUF_MOVED_ENT, BUF_MOVED_HIST, BUF_MOVED_TMP,
     BUF_CSPLIT, BUF_RINERT, BUF_F64ITEMS, BUF_INIT,
+    BUF_MB_IDX, BUF_MB_XB, BUF_MB_LAB, BUF_MB_OLD, BUF_MB_COUNTS,
     BUF_BX, BUF_BFITS, BUF_BSTATE, BUF_BITEMS, BUF_BPART, BUF_BORDER, BUF_BCTR, BUF_BLAB, BUF_BMEM, BUF_BCEN, BUF_BND, BUF_BXOFF,
     BUF_COUNT
 };
@@ -282,6 +283,16 @@ void launch_row_inertia(Ctx &ctx, const float *x, int64_t n, int d, const int32_
                         DevScalars *scalars);
 
 void launch_labels_to_u64(const int32_t *l, int64_t n, uint64_t *out, cudaStream_t s);
+
+// MiniBatchKMeans (mini_batch_kmeans.rs): rows idx[0..m) of x into out
+// (m x d), and update_centers_mini_batch (:410-447) for one batch -- the
+// centres updated in place in batch order, old = the centres before it,
+// counts = the running per-centre counts, shift_bits = max_c ||c - old||^2.
+template <typename T>
+void launch_gather_rows(const T *x, int d, const int32_t *idx, int64_t m, T *out, cudaStream_t s);
+template <typename T>
+void launch_minibatch_update(const T *xb, const int32_t *labels, int64_t m, int d, int k, T *centres, T *old,
+                             long long *counts, unsigned long long *shift_bits, cudaStream_t s);
 template <typename TS, typename TD>
 void launch_convert(const TS *src, int64_t count, TD *dst, cudaStream_t s);
 

@@ -1071,7 +1071,85 @@ void launch_scan(int32_t *a, int64_t m, int32_t *tmp, cudaStream_t s) {
     FK_LAUNCH_CHECK();
 }
 
+// ------------------------------------------------------ mini-batch --
+// MiniBatchKMeans: the batch's rows gathered into a contiguous block (the
+// assignment kernel then reads them like any matrix).
+template <typename T>
+__global__ void gather_rows_kernel(const T *__restrict__ x, int d, const int32_t *__restrict__ idx, int64_t m,
+                                   T *__restrict__ out) {
+    const int64_t total = m * d;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = e / d;
+        out[e] = x[(int64_t)idx[r] * d + (e - r * d)];
+    }
+}
+
+// update_centers_mini_batch (mini_batch_kmeans.rs:410-447): one block per
+// centre. Every thread walks the whole batch in order (the labels staged in
+// shared memory, so the test is uniform across the block) and owns fixed
+// features, so each feature of the centre receives c += (1 / count)(x - c)
+// for the centre's rows in batch order: count is the centre's running count
+// (starting at 1 before the first batch), 1 / count correctly rounded, no
+// fused multiply-add. old receives the centre before the batch.
+constexpr int MB_THREADS = 128;
+constexpr int MB_LABELS = 2048;
+
+template <typename T>
+__global__ void __launch_bounds__(MB_THREADS)
+    minibatch_update_kernel(const T *__restrict__ xb, const int32_t *__restrict__ labels, int64_t m, int d,
+                            T *__restrict__ centres, T *__restrict__ old, long long *__restrict__ counts) {
+    using A = UArith<T>;
+    __shared__ int32_t lab[MB_LABELS];
+    const int c = blockIdx.x;
+    T *row = centres + (int64_t)c * d;
+    for (int j = threadIdx.x; j < d; j += MB_THREADS) old[(int64_t)c * d + j] = row[j];
+    long long cnt = counts[c];
+    for (int64_t b0 = 0; b0 < m; b0 += MB_LABELS) {
+        const int len = (int)(m - b0 < MB_LABELS ? m - b0 : MB_LABELS);
+        __syncthreads();  // the previous chunk's labels are no longer read
+        for (int i = threadIdx.x; i < len; i += MB_THREADS) lab[i] = labels[b0 + i];
+        __syncthreads();
+        for (int i = 0; i < len; i++) {
+            if (lab[i] != c) continue;
+            cnt += 1;
+            const T lr = A::div(T(1), (T)cnt);
+            const T *xr = xb + (b0 + i) * d;
+            for (int j = threadIdx.x; j < d; j += MB_THREADS) {
+                const T cj = row[j];
+                row[j] = A::add(cj, A::mul(lr, A::sub(xr[j], cj)));
+            }
+        }
+    }
+    if (threadIdx.x == 0) counts[c] = cnt;
+}
+
 }  // namespace
+
+template <typename T>
+void launch_gather_rows(const T *x, int d, const int32_t *idx, int64_t m, T *out, cudaStream_t s) {
+    const int64_t total = m * (int64_t)d;
+    if (total <= 0) return;
+    const unsigned grid = (unsigned)std::min<int64_t>((total + 255) / 256, 4096);
+    gather_rows_kernel<T><<<grid, 256, 0, s>>>(x, d, idx, m, out);
+    FK_LAUNCH_CHECK();
+}
+
+template <typename T>
+void launch_minibatch_update(const T *xb, const int32_t *labels, int64_t m, int d, int k, T *centres, T *old,
+                             long long *counts, unsigned long long *shift_bits, cudaStream_t s) {
+    FK_CUDA(cudaMemsetAsync(shift_bits, 0, sizeof(unsigned long long), s));
+    minibatch_update_kernel<T><<<(unsigned)k, MB_THREADS, 0, s>>>(xb, labels, m, d, centres, old, counts);
+    FK_LAUNCH_CHECK();
+    launch_max_shift<T>(centres, old, k, d, shift_bits, s);
+}
+
+template void launch_gather_rows<double>(const double *, int, const int32_t *, int64_t, double *, cudaStream_t);
+template void launch_gather_rows<float>(const float *, int, const int32_t *, int64_t, float *, cudaStream_t);
+template void launch_minibatch_update<double>(const double *, const int32_t *, int64_t, int, int, double *, double *,
+                                              long long *, unsigned long long *, cudaStream_t);
+template void launch_minibatch_update<float>(const float *, const int32_t *, int64_t, int, int, float *, float *,
+                                             long long *, unsigned long long *, cudaStream_t);
 
 SortPlan make_sort_plan(int64_t n, int k) {
     SortPlan p;

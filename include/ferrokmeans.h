@@ -265,6 +265,56 @@ typedef struct fk_batch_report {
 fk_status fk_kmeans_fit_batched_f32(fk_ctx *ctx, fk_batch_problem *problems, int64_t n_problems,
                                     int32_t reduction, fk_batch_report *report);
 
+/* ------------------------------------------------------ MiniBatchKMeans --
+ * ferrolearn-cluster/src/mini_batch_kmeans.rs. Builder defaults of
+ * MiniBatchKMeans::new (:108-118): batch_size 1024, max_iter 100, tol 0,
+ * n_init 3, random_state None, init k-means++. */
+typedef enum fk_minibatch_init {
+    FK_MB_INIT_KMEANS_PLUS_PLUS = 0, /* MiniBatchKMeansInit::KMeansPlusPlus */
+    FK_MB_INIT_RANDOM = 1            /* MiniBatchKMeansInit::Random         */
+} fk_minibatch_init;
+
+typedef struct fk_minibatch_params {
+    int64_t n_clusters;       /* MiniBatchKMeans::n_clusters             */
+    int64_t batch_size;       /* MiniBatchKMeans::batch_size (1024)      */
+    int64_t max_iter;         /* MiniBatchKMeans::max_iter   (100)       */
+    double tol;               /* MiniBatchKMeans::tol        (0.0)       */
+    int64_t n_init;           /* MiniBatchKMeans::n_init     (3)         */
+    uint64_t random_state;    /* MiniBatchKMeans::random_state, if set   */
+    int32_t has_random_state; /* 0 = None (base seed 0)                  */
+    int32_t init;             /* fk_minibatch_init                       */
+} fk_minibatch_params;
+
+void fk_minibatch_params_default(fk_minibatch_params *p, int64_t n_clusters);
+
+/* MiniBatchKMeans::fit (:492-591): per run, the initial centres (k-means++
+ * or random picks; init_centers, n_init*k*d or NULL, replaces both), then
+ * max_iter mini-batches: sample_batch_indices (:451-472), nearest centre of
+ * each batch row (direct form, strict < from F::MAX), and
+ * update_centers_mini_batch (:410-447) in batch order, stopping when the
+ * max centre shift < tol; the kept run has the strictly lowest inertia of
+ * assign_clusters_mb (:343-376) over all rows. Random numbers: run r draws
+ * the library's uniform stream (fk_draws_f64) seeded with
+ * random_state + r * 1000003 (the run seeds of :532), first for the initial
+ * centres (as fk_kmeans_plus_plus_*, or k partial Fisher-Yates picks), then
+ * for the batches (fk_minibatch_batch_indices). Predict and Transform of the
+ * fitted model are those of KMeans (fk_kmeans_predict_* /
+ * fk_kmeans_transform_*). best_run_out and report may be NULL. */
+fk_status fk_minibatch_fit_f64(fk_ctx *ctx, const double *x, int64_t n, int64_t d,
+                               const fk_minibatch_params *params, const double *init_centers,
+                               double *centers_out, uint64_t *labels_out, double *inertia_out,
+                               int64_t *n_iter_out, int64_t *best_run_out, fk_fit_report *report);
+fk_status fk_minibatch_fit_f32(fk_ctx *ctx, const float *x, int64_t n, int64_t d,
+                               const fk_minibatch_params *params, const float *init_centers,
+                               float *centers_out, uint64_t *labels_out, float *inertia_out,
+                               int64_t *n_iter_out, int64_t *best_run_out, fk_fit_report *report);
+
+/* The batch rows MiniBatchKMeans draws (sample_batch_indices, :451-472)
+ * for `iters` iterations from position pos of the uniform stream of seed:
+ * out holds iters * min(batch_size, n) row indices. Host-only. */
+fk_status fk_minibatch_batch_indices(uint64_t seed, int64_t pos, int64_t n, int64_t batch_size, int64_t iters,
+                                     int64_t *out);
+
 /* Diagnostics (no reference counterpart): CUDA-core throughput of this GPU,
  * out[0] FP32 FMA flop/s, [1] FP64 FMA flop/s, [2] FP64 add op/s, [3] FP32
  * add op/s, [4] FP64 add latency in cycles, [5] FP32 add latency. */

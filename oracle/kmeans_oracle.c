@@ -15,6 +15,14 @@
  *   Fit::fit                   kmeans.rs:417-512  (n_init runs, best strict-<)
  *   Predict::predict           kmeans.rs:538-552
  *   Transform::transform       kmeans.rs:568-617
+ * and, for MiniBatchKMeans, ferrolearn-cluster/src/mini_batch_kmeans.rs:
+ *   kmeans_plus_plus_mb        :230-321  (same statements as kmeans.rs's)
+ *   random_init_mb             :324-338
+ *   assign_clusters_mb         :343-376
+ *   assign_batch               :381-404
+ *   update_centers_mini_batch  :410-447
+ *   sample_batch_indices       :451-472
+ *   MiniBatchKMeans::fit       :492-591
  *
  * It must be compiled with -ffp-contract=off so that a*b+c is never fused:
  * Rust never contracts, and labels depend on the exact rounding of the
@@ -292,6 +300,146 @@ static float orc_sqrt_f32(float v) { return sqrtf(v); }
 
 ORC_DEFINE(double, f64, DBL_MAX)
 ORC_DEFINE(float, f32, FLT_MAX)
+
+/* ------------------------------------------------------ MiniBatchKMeans -- */
+/* ferrolearn-cluster/src/mini_batch_kmeans.rs with the library's uniform
+ * stream in place of StdRng: run r draws from splitmix64 seeded with
+ * random_state + r * 1000003 (the run seeds of :532); the initial centres
+ * come first (kmeans_plus_plus_mb :230-321, the same statements as
+ * kmeans.rs:169-253, or random_init_mb :324-338; explicit centres draw
+ * nothing), then sample_batch_indices (:451-472) once per iteration.
+ * random_range(a..b) is a + min(floor(u (b - a)), b - a - 1). */
+
+/* A stream positioned after `pos` draws of seed: every draw first advances
+ * the state by the golden gamma. */
+static orc_draws orc_stream_at(uint64_t seed, int64_t pos) {
+    orc_draws g = {seed + (uint64_t)pos * 0x9E3779B97F4A7C15ULL, NULL, 0, pos};
+    return g;
+}
+
+/* sample_batch_indices (:451-472): every row in a random order when
+ * batch_size >= n (a full Fisher-Yates pass), else batch_size rows without
+ * replacement (a partial Fisher-Yates pass over a fresh pool 0..n). */
+static int64_t orc_mb_sample(orc_draws *g, int64_t n, int64_t batch_size, int64_t *pool, int64_t *out) {
+    for (int64_t i = 0; i < n; i++) pool[i] = i;
+    const int64_t m = batch_size >= n ? n : batch_size;
+    for (int64_t i = 0; i < m; i++) {
+        int64_t j = i + orc_range(g, n - i);
+        int64_t t = pool[i]; pool[i] = pool[j]; pool[j] = t;
+        out[i] = pool[i];
+    }
+    return m;
+}
+
+/* The batch indices of `iters` iterations from stream position pos (for the
+ * tests of the library's own generator). out: iters * min(batch_size, n). */
+int orc_mb_batch_indices(uint64_t seed, int64_t pos, int64_t n, int64_t batch_size, int64_t iters,
+                         int64_t *out) {
+    if (n <= 0 || batch_size <= 0) return ORC_ERR_INVALID_PARAMETER;
+    int64_t *pool = (int64_t *)malloc(sizeof(int64_t) * (size_t)n);
+    if (!pool) return ORC_ERR_OOM;
+    orc_draws g = orc_stream_at(seed, pos);
+    const int64_t m = batch_size >= n ? n : batch_size;
+    for (int64_t it = 0; it < iters; it++) orc_mb_sample(&g, n, batch_size, pool, out + it * m);
+    free(pool);
+    return ORC_OK;
+}
+
+#define ORC_DEFINE_MB(T, SUF, TMAX)                                                     \
+/* random_init_mb (:324-338): k picks of a partial Fisher-Yates pass */                 \
+static void orc_mb_random_init_##SUF(const T *x, int64_t n, int64_t d, int64_t k,      \
+                                     orc_draws *g, T *centers, int64_t *pool) {         \
+    for (int64_t i = 0; i < n; i++) pool[i] = i;                                        \
+    for (int64_t i = 0; i < k; i++) {                                                   \
+        int64_t j = i + orc_range(g, n - i);                                            \
+        int64_t t = pool[i]; pool[i] = pool[j]; pool[j] = t;                            \
+        memcpy(centers + i * d, x + pool[i] * d, sizeof(T) * (size_t)d);                \
+    }                                                                                   \
+}                                                                                       \
+                                                                                        \
+/* update_centers_mini_batch (:410-447): per sample in batch order,           */        \
+/* count += 1, lr = 1 / count, c += lr (x - c); returns the max over centres  */        \
+/* of sqrt(||c - c_old||^2) (a NaN shift never wins, as `shift > max`).       */        \
+static T orc_mb_update_##SUF(const T *x, const int64_t *idx, const int64_t *lab,        \
+                             int64_t m, int64_t d, T *c, int64_t k, int64_t *counts,    \
+                             T *old) {                                                  \
+    memcpy(old, c, sizeof(T) * (size_t)(k * d));                                        \
+    for (int64_t b = 0; b < m; b++) {                                                   \
+        const int64_t l = lab[b];                                                       \
+        counts[l] += 1;                                                                 \
+        const T lr = (T)1 / (T)counts[l];                                               \
+        const T *row = x + idx[b] * d;                                                  \
+        for (int64_t j = 0; j < d; j++) c[l * d + j] = c[l * d + j] + lr * (row[j] - c[l * d + j]); \
+    }                                                                                   \
+    T ms = (T)0;                                                                        \
+    for (int64_t q = 0; q < k; q++) {                                                   \
+        T s = orc_sqrt_##SUF(orc_sqeuc_##SUF(c + q * d, old + q * d, d));               \
+        if (s > ms) ms = s;                                                             \
+    }                                                                                   \
+    return ms;                                                                          \
+}                                                                                       \
+                                                                                        \
+/* MiniBatchKMeans::fit (:492-591). init_mode 0: k-means++, 1: random; init  */         \
+/* (n_init * k * d) replaces either when given. Labels and inertia of the    */         \
+/* kept run come from assign_clusters_mb (:343-376): nearest centre, strict  */         \
+/* < from F::MAX, inertia summed in row order.                               */         \
+int orc_minibatch_fit_##SUF(const T *x, int64_t n, int64_t d, int64_t k,               \
+                            int64_t batch_size, int64_t max_iter, T tol,               \
+                            int64_t n_init, uint64_t seed, int init_mode,              \
+                            const T *init, T *out_c, int64_t *out_labels,              \
+                            T *out_inertia, int64_t *out_n_iter,                       \
+                            int64_t *out_best_run, int64_t *out_run_n_iter,            \
+                            T *out_run_inertia) {                                       \
+    if (k == 0) return ORC_ERR_INVALID_PARAMETER;                                       \
+    if (batch_size == 0) return ORC_ERR_INVALID_PARAMETER;                              \
+    if (n_init == 0) return ORC_ERR_INVALID_PARAMETER;                                  \
+    if (n == 0 || n < k) return ORC_ERR_INSUFFICIENT_SAMPLES;                           \
+    T *c = (T *)malloc(sizeof(T) * (size_t)(k * d));                                    \
+    T *old = (T *)malloc(sizeof(T) * (size_t)(k * d));                                  \
+    int64_t *counts = (int64_t *)malloc(sizeof(int64_t) * (size_t)k);                   \
+    int64_t *pool = (int64_t *)malloc(sizeof(int64_t) * (size_t)n);                     \
+    int64_t *idx = (int64_t *)malloc(sizeof(int64_t) * (size_t)n);                      \
+    int64_t *blab = (int64_t *)malloc(sizeof(int64_t) * (size_t)n);                     \
+    int64_t *lab = (int64_t *)malloc(sizeof(int64_t) * (size_t)n);                      \
+    if (!c || !old || !counts || !pool || !idx || !blab || !lab) return ORC_ERR_OOM;    \
+    int have = 0; T best_in = TMAX;                                                     \
+    for (int64_t run = 0; run < n_init; run++) {                                        \
+        orc_draws g = orc_stream_at(seed + (uint64_t)run * 1000003ULL, 0);              \
+        if (init) memcpy(c, init + run * k * d, sizeof(T) * (size_t)(k * d));           \
+        else if (init_mode == 1) orc_mb_random_init_##SUF(x, n, d, k, &g, c, pool);     \
+        else orc_kpp_##SUF(x, n, d, k, &g, c);                                          \
+        for (int64_t q = 0; q < k; q++) counts[q] = 1;                                  \
+        int64_t n_iter = 0;                                                             \
+        for (int64_t it = 0; it < max_iter; it++) {                                     \
+            const int64_t m = orc_mb_sample(&g, n, batch_size, pool, idx);              \
+            for (int64_t b = 0; b < m; b++) {                                           \
+                T dist; orc_nearest_##SUF(x + idx[b] * d, c, k, d, &blab[b], &dist);    \
+            }                                                                           \
+            T shift = orc_mb_update_##SUF(x, idx, blab, m, d, c, k, counts, old);       \
+            n_iter += 1;                                                                \
+            if (shift < tol) break;                                                     \
+        }                                                                               \
+        T inertia = (T)0;                                                               \
+        for (int64_t i = 0; i < n; i++) {                                               \
+            T dist; orc_nearest_##SUF(x + i * d, c, k, d, &lab[i], &dist);              \
+            inertia = inertia + dist;                                                   \
+        }                                                                               \
+        if (out_run_n_iter) out_run_n_iter[run] = n_iter;                               \
+        if (out_run_inertia) out_run_inertia[run] = inertia;                            \
+        if (!have || inertia < best_in) {                                               \
+            have = 1; best_in = inertia;                                                \
+            memcpy(out_c, c, sizeof(T) * (size_t)(k * d));                              \
+            memcpy(out_labels, lab, sizeof(int64_t) * (size_t)n);                       \
+            *out_inertia = inertia; *out_n_iter = n_iter;                               \
+            if (out_best_run) *out_best_run = run;                                      \
+        }                                                                               \
+    }                                                                                   \
+    free(c); free(old); free(counts); free(pool); free(idx); free(blab); free(lab);     \
+    return ORC_OK;                                                                      \
+}
+
+ORC_DEFINE_MB(double, f64, DBL_MAX)
+ORC_DEFINE_MB(float, f32, FLT_MAX)
 
 /* Direct-form FP64 distance from an f32 row to an f64 centre, used for the
  * "X stored f32, oracle in f64" parity cases: the row is widened exactly. */

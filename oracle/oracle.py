@@ -35,6 +35,9 @@ def lib():
                                                         p, p, p, p, p, C.c_int]
             getattr(_lib, f"orc_predict_{suf}").argtypes = [p, i64, i64, p, i64, i64, p, C.c_int]
             getattr(_lib, f"orc_transform_{suf}").argtypes = [p, i64, i64, p, i64, i64, p, C.c_int]
+            getattr(_lib, f"orc_minibatch_fit_{suf}").argtypes = [p, i64, i64, i64, i64, i64, T, i64, u64, C.c_int,
+                                                                  p, p, p, p, p, p, p, p]
+        _lib.orc_mb_batch_indices.argtypes = [u64, i64, i64, i64, i64, p]
         _lib.orc_draws_f64.argtypes = [u64, i64, p]
         _lib.orc_draws_f64.restype = None
         _lib.orc_fit_runs_f32.argtypes = [p, i64, i64, i64, i64, C.c_float, i64, p, u64, C.c_int, p, p, p, p,
@@ -180,3 +183,39 @@ def fit_runs(x, k, max_iter=300, tol=1e-4, n_init=10, init=None, seed=0, wide_su
     if rc:
         raise OracleError(rc)
     return dict(centers=out_c, labels=out_l, inertia=out_i, n_iter=out_n)
+
+
+def minibatch_fit(x, k, batch_size=1024, max_iter=100, tol=0.0, n_init=3, seed=0, init="kmeans++", init_centers=None):
+    """MiniBatchKMeans::fit (mini_batch_kmeans.rs:492-591) with the library's
+    uniform stream: dict(centers, labels, inertia, n_iter, best_run,
+    run_n_iter, run_inertia). init: "kmeans++" or "random"; init_centers
+    ((n_init, k, d)) replaces either."""
+    x = np.ascontiguousarray(x)
+    suf, T = _suffix(x.dtype)
+    n, d = x.shape if x.ndim == 2 else (0, 0)
+    out_c = np.empty((max(k, 0), d), dtype=x.dtype)
+    out_l = np.empty(n, dtype=np.int64)
+    inertia, n_iter, best = T(), C.c_int64(), C.c_int64()
+    runs = max(n_init, 1)
+    run_n = np.zeros(runs, dtype=np.int64)
+    run_i = np.zeros(runs, dtype=x.dtype)
+    ini = None if init_centers is None else np.ascontiguousarray(init_centers, dtype=x.dtype)
+    mode = {"kmeans++": 0, "random": 1}[init]
+    rc = getattr(lib(), f"orc_minibatch_fit_{suf}")(_ptr(x), n, d, k, batch_size, max_iter, T(tol), n_init, seed,
+                                                    mode, _ptr(ini), _ptr(out_c), _ptr(out_l), C.byref(inertia),
+                                                    C.byref(n_iter), C.byref(best), _ptr(run_n), _ptr(run_i))
+    if rc:
+        raise OracleError(rc)
+    return dict(centers=out_c, labels=out_l, inertia=inertia.value, n_iter=n_iter.value, best_run=best.value,
+                run_n_iter=run_n, run_inertia=run_i)
+
+
+def minibatch_indices(seed, pos, n, batch_size, iters):
+    """sample_batch_indices (mini_batch_kmeans.rs:451-472) for `iters`
+    iterations from stream position pos: (iters, min(batch_size, n)) int64."""
+    m = min(batch_size, n)
+    out = np.empty((iters, m), dtype=np.int64)
+    rc = lib().orc_mb_batch_indices(seed, pos, n, batch_size, iters, _ptr(out))
+    if rc:
+        raise OracleError(rc)
+    return out
