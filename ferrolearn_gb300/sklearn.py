@@ -13,6 +13,9 @@ index). A tensor-core fit of data that float32 does not hold exactly warns.
 With scikit-learn installed the class derives from its BaseEstimator,
 ClusterMixin and TransformerMixin (get_params / set_params / clone work like
 the reference's); without it the same class stands alone.
+
+MiniBatchKMeans below is the drop-in for the reference's mini-batch wrapper
+(_extras.py:396-420), backed by ferrolearn_gb300.MiniBatchKMeans.
 """
 import warnings
 
@@ -25,8 +28,9 @@ from .kmeans import default_context
 try:  # the wrapper's base classes when scikit-learn is present
     from sklearn.base import BaseEstimator, ClusterMixin, TransformerMixin
     _BASES = (TransformerMixin, ClusterMixin, BaseEstimator)
+    _CLUSTER_BASES = (ClusterMixin, BaseEstimator)
 except ImportError:  # pragma: no cover - exercised where scikit-learn is absent
-    _BASES = (object,)
+    _BASES = _CLUSTER_BASES = (object,)
 
 
 def _as_f64(x):
@@ -115,3 +119,42 @@ class KMeans(*_BASES):
             centres, dtype, precision = saved
             self._fitted = FittedKMeans(centres, np.asarray(self.labels_), self.inertia_, self.n_iter_, dtype,
                                         precision=precision)
+
+
+class MiniBatchKMeans(*_CLUSTER_BASES):
+    """Mini-batch K-Means on one GB300: the drop-in for ferrolearn-python's
+    MiniBatchKMeans wrapper (ferrolearn-python/python/ferrolearn/_extras.py:
+    396-420, the PyO3 class _RsMiniBatchKMeans of src/extras.rs:693-735).
+
+    Same keywords and defaults (n_clusters=8, max_iter=100,
+    random_state=None; the other hyper-parameters are MiniBatchKMeans::new's),
+    the fitted labels_ and n_features_in_, fit / predict / fit_predict; also
+    cluster_centers_, inertia_, n_iter_ and the `device` keyword."""
+
+    def __init__(self, *, n_clusters=8, max_iter=100, random_state=None, device=0):
+        self.n_clusters = n_clusters
+        self.max_iter = max_iter
+        self.random_state = random_state
+        self.device = device
+
+    def fit(self, X, y=None):
+        from .minibatch import MiniBatchKMeans as _MiniBatch
+        x = _as_f64(X)
+        m = _MiniBatch(self.n_clusters).with_max_iter(self.max_iter)
+        if self.random_state is not None:
+            m = m.with_random_state(self.random_state)
+        self._fitted = m.fit(x, ctx=default_context(self.device))
+        self.n_features_in_ = x.shape[1]
+        self.labels_ = np.asarray(self._fitted.labels())
+        self.cluster_centers_ = np.array(self._fitted.cluster_centers())
+        self.inertia_ = float(self._fitted.inertia())
+        self.n_iter_ = int(self._fitted.n_iter())
+        return self
+
+    def predict(self, X):
+        if not hasattr(self, "_fitted"):
+            raise AttributeError("This MiniBatchKMeans instance is not fitted yet. Call 'fit' first.")
+        return np.asarray(self._fitted.predict(_as_f64(X), ctx=default_context(self.device)))
+
+    def fit_predict(self, X, y=None):
+        return self.fit(X).labels_

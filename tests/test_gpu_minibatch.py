@@ -85,3 +85,14 @@ def test_minibatch_device_resident_inputs_and_outputs():
     m.fit(torch.from_numpy(x).cuda(), out=(c_out, l_out))
     assert np.array_equal(c_out.cpu().numpy(), host.cluster_centers())
     assert np.array_equal(l_out.cpu().numpy(), host.labels())
+
+
+def test_minibatch_sklearn_wrapper():
+    from ferrolearn_gb300.sklearn import MiniBatchKMeans
+    x = _blobs(3000, 6, 5, seed=9, dtype=np.float64)
+    km = MiniBatchKMeans(n_clusters=5, random_state=3).fit(x)
+    o = O.minibatch_fit(x, 5, max_iter=100, n_init=3, seed=3)
+    assert np.array_equal(km.labels_, o["labels"])
+    assert np.array_equal(km.cluster_centers_, o["centers"])
+    assert np.array_equal(km.predict(x), O.predict(km.cluster_centers_, x))
+    assert np.array_equal(km.fit_predict(x), km.labels_)

@@ -78,3 +78,20 @@ def test_tensor_core_forms_need_float32_storage():
     for prec in ("bf16", "fp8"):
         with pytest.raises(F.Unsupported, match="f32x64"):
             F.KMeans(2, dtype="f64").with_precision(prec).fit(np.ones((4, 2)))
+
+
+def test_minibatch_wrapper_defaults_and_validation():
+    from ferrolearn_gb300.sklearn import MiniBatchKMeans
+    km = MiniBatchKMeans()
+    # ferrolearn-python/python/ferrolearn/_extras.py:408-417
+    assert (km.n_clusters, km.max_iter, km.random_state) == (8, 100, None)
+    with pytest.raises(F.InvalidParameter):
+        MiniBatchKMeans(n_clusters=0).fit(np.ones((5, 2)))
+    with pytest.raises(F.InsufficientSamples):
+        MiniBatchKMeans(n_clusters=9).fit(np.ones((5, 2)))
+    with pytest.raises(AttributeError):
+        MiniBatchKMeans().predict(np.ones((5, 2)))
+    pytest.importorskip("sklearn")
+    from sklearn.base import clone
+    c = clone(MiniBatchKMeans(n_clusters=3, random_state=4)).set_params(max_iter=7)
+    assert (c.n_clusters, c.random_state, c.max_iter) == (3, 4, 7)
