@@ -166,3 +166,20 @@ def test_dirichlet_scale_sampled_rows():
         rows = x[gl == q]
         oc[q] = rows.sum(0) / len(rows) if len(rows) else c[q]
     assert np.abs(gc - oc).max() <= 1e-12 * np.abs(oc).max()
+
+
+@pytest.mark.skip(reason="not yet run on a GB300")
+@pytest.mark.parametrize("dtype", ["f64", "f32"])
+def test_fit_with_injected_draws_matches_oracle(dtype):
+    # one caller-supplied uniform stream shared by the n_init runs' k-means++
+    # (each run continues where the previous one stopped)
+    npdt = np.float64 if dtype == "f64" else np.float32
+    x = _blobs(2500, 5, 7, seed=21, dtype=npdt)
+    k, n_init = 7, 3
+    dr = F.draws(99, n_init * (1 + (k - 1) * (2 + int(np.floor(np.log(k))))))
+    g = F.KMeans(k, dtype=dtype).with_n_init(n_init).with_draws(dr).fit(x)
+    o = O.fit(x, k, n_init=n_init, draws_arr=dr)
+    assert g.report["best_run"] == o["best_run"]
+    assert np.array_equal(g.labels(), o["labels"])
+    assert np.array_equal(g.cluster_centers(), o["centers"])
+    assert g.n_iter() == o["n_iter"]
