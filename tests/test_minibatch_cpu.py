@@ -140,3 +140,141 @@ def test_library_validation_order(kw, x, exc, needle):
 def test_library_rejects_unknown_init():
     with pytest.raises(F.InvalidParameter):
         F.MiniBatchKMeans(2).with_init("farthest")
+
+
+# A second, literal restatement in Python floats (IEEE f64, no fused
+# multiply-add) for small inputs: it checks the C oracle statement by
+# statement, including the stream positions.
+def _py_stream(seed):
+    state = [seed & (2**64 - 1)]
+    M = 2**64 - 1
+
+    def nxt():
+        state[0] = (state[0] + 0x9E3779B97F4A7C15) & M
+        z = state[0]
+        z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & M
+        z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & M
+        z ^= z >> 31
+        return (z >> 11) * (1.0 / 9007199254740992.0)
+
+    def rng(n):  # random_range(0..n)
+        import math
+        return min(max(int(math.floor(nxt() * n)), 0), n - 1)
+    return nxt, rng
+
+
+def _py_sq(a, b):
+    acc = 0.0
+    for u, v in zip(a, b):
+        t = u - v
+        acc = acc + t * t
+    return acc
+
+
+def _py_nearest(row, cs):
+    best, bd = 0, 1.7976931348623157e308
+    for q, c in enumerate(cs):
+        v = _py_sq(row, c)
+        if v < bd:
+            best, bd = q, v
+    return best, bd
+
+
+def _py_kpp(x, k, nxt, rng):
+    import math
+    n = len(x)
+    cs = [list(x[rng(n)])]
+    if k == 1:
+        return cs
+    mind = [_py_sq(r, cs[0]) for r in x]
+    trials = max(2 + int(math.floor(math.log(k))), 1)
+    for _ in range(1, k):
+        total = 0.0
+        for v in mind:
+            total = total + v
+        if total <= 0.0:
+            cs.append(list(x[rng(n)]))
+            continue
+        best = None
+        for _t in range(trials):
+            thr = nxt() * total
+            cum, cand = 0.0, n - 1
+            for i, v in enumerate(mind):
+                cum = cum + v
+                if cum >= thr:
+                    cand = i
+                    break
+            nd = []
+            for r, m in zip(x, mind):
+                v = _py_sq(r, x[cand])
+                nd.append(v if v < m else m)
+            pot = 0.0
+            for v in nd:
+                pot = pot + v
+            if best is None or pot < best[0]:
+                best = (pot, cand, nd)
+        cs.append(list(x[best[1]]))
+        mind = best[2]
+    return cs
+
+
+def _py_minibatch(x, k, batch, max_iter, tol, n_init, seed, init):
+    x = [list(map(float, r)) for r in x]
+    n = len(x)
+    best = None
+    for run in range(n_init):
+        nxt, rng = _py_stream(seed + run * 1000003)
+        if init == "random":
+            pool = list(range(n))
+            cs = []
+            for i in range(k):
+                j = i + rng(n - i)
+                pool[i], pool[j] = pool[j], pool[i]
+                cs.append(list(x[pool[i]]))
+        else:
+            cs = _py_kpp(x, k, nxt, rng)
+        counts = [1] * k
+        n_iter = 0
+        for _ in range(max_iter):
+            pool = list(range(n))
+            m = min(batch, n)
+            idx = []
+            for i in range(m):
+                j = i + rng(n - i)
+                pool[i], pool[j] = pool[j], pool[i]
+                idx.append(pool[i])
+            labs = [_py_nearest(x[i], cs)[0] for i in idx]
+            old = [list(c) for c in cs]
+            for i, lab in zip(idx, labs):
+                counts[lab] += 1
+                lr = 1.0 / float(counts[lab])
+                cs[lab] = [c + lr * (v - c) for c, v in zip(cs[lab], x[i])]
+            shift = 0.0
+            for c, o in zip(cs, old):
+                s = _py_sq(c, o) ** 0.5
+                if s > shift:
+                    shift = s
+            n_iter += 1
+            if shift < tol:
+                break
+        labels, inertia = [], 0.0
+        for r in x:
+            lab, dist = _py_nearest(r, cs)
+            labels.append(lab)
+            inertia = inertia + dist
+        if best is None or inertia < best["inertia"]:
+            best = dict(centers=np.array(cs), labels=np.array(labels), inertia=inertia, n_iter=n_iter, best_run=run)
+    return best
+
+
+@pytest.mark.parametrize("init", ["kmeans++", "random"])
+@pytest.mark.parametrize("n,d,k,batch,tol", [(60, 3, 4, 16, 0.0), (40, 2, 3, 100, 0.0), (80, 4, 5, 7, 0.05)])
+def test_oracle_matches_a_literal_python_restatement(init, n, d, k, batch, tol):
+    rng = np.random.default_rng(n + d + k)
+    x = rng.normal(size=(n, d)) * 3 + rng.integers(0, 3, size=(n, 1)) * 6
+    want = _py_minibatch(x, k, batch, 12, tol, 2, 17, init)
+    got = O.minibatch_fit(x, k, batch_size=batch, max_iter=12, tol=tol, n_init=2, seed=17, init=init)
+    assert np.array_equal(got["labels"], want["labels"])
+    assert np.array_equal(got["centers"], want["centers"])
+    assert got["inertia"] == want["inertia"] and got["n_iter"] == want["n_iter"]
+    assert got["best_run"] == want["best_run"]
