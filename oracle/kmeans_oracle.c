@@ -23,6 +23,10 @@
  *   update_centers_mini_batch  :410-447
  *   sample_batch_indices       :451-472
  *   MiniBatchKMeans::fit       :492-591
+ * and, for BisectingKMeans, ferrolearn-cluster/src/bisecting_kmeans.rs:
+ *   compute_cluster_stats      :192-222
+ *   run_2means                 :225-312
+ *   BisectingKMeans::fit       :326-505
  *
  * It must be compiled with -ffp-contract=off so that a*b+c is never fused:
  * Rust never contracts, and labels depend on the exact rounding of the
@@ -440,6 +444,172 @@ int orc_minibatch_fit_##SUF(const T *x, int64_t n, int64_t d, int64_t k,        
 
 ORC_DEFINE_MB(double, f64, DBL_MAX)
 ORC_DEFINE_MB(float, f32, FLT_MAX)
+
+/* ------------------------------------------------------ BisectingKMeans -- */
+/* ferrolearn-cluster/src/bisecting_kmeans.rs with the library's uniform
+ * stream in place of StdRng: run r of split s draws from splitmix64 seeded
+ * with random_state + s * 1000 + r (wrapping, :410-412). Selection of the
+ * cluster to split follows Rust's Iterator::max_by_key / max_by, which keep
+ * the LAST of equally maximal elements (:376-396); a cluster whose split
+ * leaves one side empty is pushed back unchanged (:466-481), which the
+ * reference repeats without end when that cluster stays the one selected:
+ * the restatement stops after ORC_BK_MAX_SPLITS splits with
+ * ORC_ERR_NO_PROGRESS instead. */
+#define ORC_ERR_NUMERICAL 4
+#define ORC_ERR_NO_PROGRESS 5
+#define ORC_BK_MAX_SPLITS(n, k) (4 * (n) + 4 * (k) + 16)
+
+#define ORC_DEFINE_BK(T, SUF, TMAX)                                                     \
+/* compute_cluster_stats (:192-222): row-order sums / n, SSE in row order */            \
+static T orc_bk_stats_##SUF(const T *x, int64_t d, const int64_t *idx, int64_t m,       \
+                            T *centre) {                                                \
+    for (int64_t j = 0; j < d; j++) centre[j] = (T)0;                                   \
+    if (m == 0) return (T)0;                                                            \
+    const T nf = (T)m;                                                                  \
+    for (int64_t i = 0; i < m; i++)                                                     \
+        for (int64_t j = 0; j < d; j++) centre[j] = centre[j] + x[idx[i] * d + j];      \
+    for (int64_t j = 0; j < d; j++) centre[j] = centre[j] / nf;                         \
+    T sse = (T)0;                                                                       \
+    for (int64_t i = 0; i < m; i++) sse = sse + orc_sqeuc_##SUF(x + idx[i] * d, centre, d); \
+    return sse;                                                                         \
+}                                                                                       \
+                                                                                        \
+/* run_2means (:225-312): two distinct rows of the subset, then assignments */          \
+/* (d0 <= d1 -> 0) until no label changes, row-order sums / counts in F    */          \
+/* (an empty side keeps its centre); returns the SSE against the final     */          \
+/* centres.                                                                */          \
+static T orc_bk_2means_##SUF(const T *x, int64_t d, const int64_t *idx, int64_t m,      \
+                             int64_t max_iter, orc_draws *g, unsigned char *lab,        \
+                             T *c0, T *c1, T *s0, T *s1) {                              \
+    const int64_t i0 = orc_range(g, m);                                                 \
+    int64_t i1 = orc_range(g, m);                                                       \
+    if (m > 1) while (i1 == i0) i1 = orc_range(g, m);                                   \
+    memcpy(c0, x + idx[i0] * d, sizeof(T) * (size_t)d);                                \
+    memcpy(c1, x + idx[i1] * d, sizeof(T) * (size_t)d);                                \
+    memset(lab, 0, (size_t)m);                                                          \
+    for (int64_t it = 0; it < max_iter; it++) {                                         \
+        int changed = 0;                                                                \
+        for (int64_t i = 0; i < m; i++) {                                               \
+            const T *row = x + idx[i] * d;                                              \
+            const T d0 = orc_sqeuc_##SUF(row, c0, d), d1 = orc_sqeuc_##SUF(row, c1, d); \
+            const unsigned char nl = d0 <= d1 ? 0 : 1;                                  \
+            if (nl != lab[i]) { lab[i] = nl; changed = 1; }                             \
+        }                                                                               \
+        if (!changed) break;                                                            \
+        T n0 = (T)0, n1 = (T)0;                                                         \
+        for (int64_t j = 0; j < d; j++) { s0[j] = (T)0; s1[j] = (T)0; }                 \
+        for (int64_t i = 0; i < m; i++) {                                               \
+            const T *row = x + idx[i] * d;                                              \
+            if (lab[i] == 0) {                                                          \
+                n0 = n0 + (T)1;                                                         \
+                for (int64_t j = 0; j < d; j++) s0[j] = s0[j] + row[j];                 \
+            } else {                                                                    \
+                n1 = n1 + (T)1;                                                         \
+                for (int64_t j = 0; j < d; j++) s1[j] = s1[j] + row[j];                 \
+            }                                                                           \
+        }                                                                               \
+        if (n0 > (T)0) for (int64_t j = 0; j < d; j++) c0[j] = s0[j] / n0;              \
+        if (n1 > (T)0) for (int64_t j = 0; j < d; j++) c1[j] = s1[j] / n1;              \
+    }                                                                                   \
+    T sse = (T)0;                                                                       \
+    for (int64_t i = 0; i < m; i++)                                                     \
+        sse = sse + orc_sqeuc_##SUF(x + idx[i] * d, lab[i] ? c1 : c0, d);               \
+    return sse;                                                                         \
+}                                                                                       \
+                                                                                        \
+/* BisectingKMeans::fit (:326-505). strategy 0: LargestCluster, 1:           */        \
+/* LargestSSE. Outputs: out_c (k*d, the first *out_n_clusters rows used),    */        \
+/* labels (cluster order of the final list), inertia (sum of the clusters'  */        \
+/* SSE in list order).                                                       */        \
+int orc_bisecting_fit_##SUF(const T *x, int64_t n, int64_t d, int64_t k,               \
+                            int64_t max_iter, int64_t n_init, uint64_t seed,           \
+                            int strategy, T *out_c, int64_t *out_labels,               \
+                            T *out_inertia, int64_t *out_n_clusters) {                  \
+    if (k == 0) return ORC_ERR_INVALID_PARAMETER;                                       \
+    if (n_init == 0) return ORC_ERR_INVALID_PARAMETER;                                  \
+    if (n == 0 || n < k) return ORC_ERR_INSUFFICIENT_SAMPLES;                           \
+    int64_t **cidx = (int64_t **)calloc((size_t)k + 1, sizeof(int64_t *));              \
+    int64_t *cm = (int64_t *)calloc((size_t)k + 1, sizeof(int64_t));                    \
+    T *ccen = (T *)malloc(sizeof(T) * (size_t)((k + 1) * d + 1));                       \
+    T *csse = (T *)malloc(sizeof(T) * (size_t)(k + 1));                                 \
+    unsigned char *lab = (unsigned char *)malloc((size_t)n + 1);                        \
+    unsigned char *blab = (unsigned char *)malloc((size_t)n + 1);                       \
+    T *w = (T *)malloc(sizeof(T) * (size_t)(6 * d + 6));                                \
+    if (!cidx || !cm || !ccen || !csse || !lab || !blab || !w) return ORC_ERR_OOM;      \
+    T *c0 = w, *c1 = w + d, *s0 = w + 2 * d, *s1 = w + 3 * d, *b0 = w + 4 * d, *b1 = w + 5 * d; \
+    int rc = ORC_OK;                                                                    \
+    int64_t nc = 1;                                                                     \
+    cidx[0] = (int64_t *)malloc(sizeof(int64_t) * (size_t)n);                           \
+    for (int64_t i = 0; i < n; i++) cidx[0][i] = i;                                     \
+    cm[0] = n;                                                                          \
+    csse[0] = orc_bk_stats_##SUF(x, d, cidx[0], n, ccen);                               \
+    uint64_t split_count = 0;                                                           \
+    while (nc < k) {                                                                    \
+        if ((int64_t)split_count > ORC_BK_MAX_SPLITS(n, k)) { rc = ORC_ERR_NO_PROGRESS; break; } \
+        int64_t t = -1;                                                                 \
+        for (int64_t ci = 0; ci < nc; ci++) {                                           \
+            if (cm[ci] < 2) continue;                                                   \
+            if (t < 0) { t = ci; continue; }                                            \
+            if (strategy == 0) { if (!(cm[t] > cm[ci])) t = ci; }                       \
+            else { if (!(csse[t] > csse[ci])) t = ci; }                                 \
+        }                                                                               \
+        if (t < 0) break;                                                               \
+        const int64_t m = cm[t];                                                        \
+        int have = 0; T best = TMAX;                                                    \
+        for (int64_t run = 0; run < n_init; run++) {                                    \
+            orc_draws g = orc_stream_at(seed + split_count * 1000ULL + (uint64_t)run, 0); \
+            T sse = orc_bk_2means_##SUF(x, d, cidx[t], m, max_iter, &g, lab, c0, c1, s0, s1); \
+            if (sse < best) {                                                           \
+                best = sse; have = 1;                                                   \
+                memcpy(blab, lab, (size_t)m);                                           \
+                memcpy(b0, c0, sizeof(T) * (size_t)d); memcpy(b1, c1, sizeof(T) * (size_t)d); \
+            }                                                                           \
+        }                                                                               \
+        split_count++;                                                                  \
+        if (!have) { rc = ORC_ERR_NUMERICAL; break; }                                   \
+        int64_t m0 = 0;                                                                 \
+        for (int64_t i = 0; i < m; i++) m0 += blab[i] == 0;                             \
+        int64_t *i0 = (int64_t *)malloc(sizeof(int64_t) * (size_t)(m0 + 1));            \
+        int64_t *i1 = (int64_t *)malloc(sizeof(int64_t) * (size_t)(m - m0 + 1));        \
+        int64_t p0 = 0, p1 = 0;                                                         \
+        for (int64_t i = 0; i < m; i++) {                                               \
+            if (blab[i] == 0) i0[p0++] = cidx[t][i]; else i1[p1++] = cidx[t][i];        \
+        }                                                                               \
+        T sse0 = (T)0, sse1 = (T)0;                                                     \
+        for (int64_t i = 0; i < p0; i++) sse0 = sse0 + orc_sqeuc_##SUF(x + i0[i] * d, b0, d); \
+        for (int64_t i = 0; i < p1; i++) sse1 = sse1 + orc_sqeuc_##SUF(x + i1[i] * d, b1, d); \
+        free(cidx[t]);                                                                  \
+        for (int64_t ci = t; ci + 1 < nc; ci++) {                                       \
+            cidx[ci] = cidx[ci + 1]; cm[ci] = cm[ci + 1]; csse[ci] = csse[ci + 1];      \
+            memcpy(ccen + ci * d, ccen + (ci + 1) * d, sizeof(T) * (size_t)d);          \
+        }                                                                               \
+        nc -= 1;                                                                        \
+        if (p0 > 0) {                                                                   \
+            cidx[nc] = i0; cm[nc] = p0; csse[nc] = sse0;                                \
+            memcpy(ccen + nc * d, b0, sizeof(T) * (size_t)d); nc++;                     \
+        } else free(i0);                                                                \
+        if (p1 > 0) {                                                                   \
+            cidx[nc] = i1; cm[nc] = p1; csse[nc] = sse1;                                \
+            memcpy(ccen + nc * d, b1, sizeof(T) * (size_t)d); nc++;                     \
+        } else free(i1);                                                                \
+    }                                                                                   \
+    if (rc == ORC_OK) {                                                                 \
+        T inertia = (T)0;                                                               \
+        for (int64_t ci = 0; ci < nc; ci++) {                                           \
+            memcpy(out_c + ci * d, ccen + ci * d, sizeof(T) * (size_t)d);               \
+            for (int64_t i = 0; i < cm[ci]; i++) out_labels[cidx[ci][i]] = ci;          \
+            inertia = inertia + csse[ci];                                               \
+        }                                                                               \
+        *out_inertia = inertia;                                                         \
+        *out_n_clusters = nc;                                                           \
+    }                                                                                   \
+    for (int64_t ci = 0; ci < nc; ci++) free(cidx[ci]);                                 \
+    free(cidx); free(cm); free(ccen); free(csse); free(lab); free(blab); free(w);       \
+    return rc;                                                                          \
+}
+
+ORC_DEFINE_BK(double, f64, DBL_MAX)
+ORC_DEFINE_BK(float, f32, FLT_MAX)
 
 /* Direct-form FP64 distance from an f32 row to an f64 centre, used for the
  * "X stored f32, oracle in f64" parity cases: the row is widened exactly. */

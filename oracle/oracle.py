@@ -37,6 +37,8 @@ def lib():
             getattr(_lib, f"orc_transform_{suf}").argtypes = [p, i64, i64, p, i64, i64, p, C.c_int]
             getattr(_lib, f"orc_minibatch_fit_{suf}").argtypes = [p, i64, i64, i64, i64, i64, T, i64, u64, C.c_int,
                                                                   p, p, p, p, p, p, p, p]
+            getattr(_lib, f"orc_bisecting_fit_{suf}").argtypes = [p, i64, i64, i64, i64, i64, u64, C.c_int, p, p,
+                                                                  p, p]
         _lib.orc_mb_batch_indices.argtypes = [u64, i64, i64, i64, i64, p]
         _lib.orc_draws_f64.argtypes = [u64, i64, p]
         _lib.orc_draws_f64.restype = None
@@ -219,3 +221,21 @@ def minibatch_indices(seed, pos, n, batch_size, iters):
     if rc:
         raise OracleError(rc)
     return out
+
+
+def bisecting_fit(x, k, max_iter=300, n_init=10, seed=0, strategy="largest_cluster"):
+    """BisectingKMeans::fit (bisecting_kmeans.rs:326-505) with the library's
+    uniform stream (run r of split s seeded with seed + s * 1000 + r):
+    dict(centers (n_clusters, d), labels, inertia, n_clusters)."""
+    x = np.ascontiguousarray(x)
+    suf, T = _suffix(x.dtype)
+    n, d = x.shape if x.ndim == 2 else (0, 0)
+    out_c = np.zeros((max(k, 0), d), dtype=x.dtype)
+    out_l = np.zeros(n, dtype=np.int64)
+    inertia, nc = T(), C.c_int64()
+    strat = {"largest_cluster": 0, "largest_sse": 1}[strategy]
+    rc = getattr(lib(), f"orc_bisecting_fit_{suf}")(_ptr(x), n, d, k, max_iter, n_init, seed, strat, _ptr(out_c),
+                                                    _ptr(out_l), C.byref(inertia), C.byref(nc))
+    if rc:
+        raise OracleError(rc)
+    return dict(centers=out_c[:nc.value].copy(), labels=out_l, inertia=inertia.value, n_clusters=nc.value)
