@@ -25,7 +25,19 @@ EXPORTS = [
     "fk_kmeans_plus_plus_f64", "fk_kmeans_plus_plus_f32", "fk_debug_tc_probe",
     "fk_debug_measure_peaks", "fk_kmeans_score_f64_noalloc", "fk_kmeans_fit_batched_f32", "fk_debug_tc_plan",
     "fk_minibatch_params_default", "fk_minibatch_fit_f64", "fk_minibatch_fit_f32", "fk_minibatch_batch_indices",
+    "fk_bisecting_params_default", "fk_bisecting_fit_f64", "fk_bisecting_fit_f32",
 ]
+
+
+class BisectingParams(C.Structure):
+    _fields_ = [
+        ("n_clusters", C.c_int64),
+        ("max_iter", C.c_int64),
+        ("n_init", C.c_int64),
+        ("random_state", C.c_uint64),
+        ("has_random_state", C.c_int32),
+        ("strategy", C.c_int32),
+    ]
 
 
 class MiniBatchParams(C.Structure):
@@ -175,6 +187,12 @@ def _declare(lib):
         f.restype = st
     lib.fk_minibatch_batch_indices.argtypes = [u64, i64, i64, i64, i64, p]
     lib.fk_minibatch_batch_indices.restype = st
+    lib.fk_bisecting_params_default.argtypes = [C.POINTER(BisectingParams), i64]
+    lib.fk_bisecting_params_default.restype = None
+    for suf in ("f64", "f32"):
+        f = getattr(lib, f"fk_bisecting_fit_{suf}")
+        f.argtypes = [p, p, i64, i64, C.POINTER(BisectingParams), p, p, p, p]
+        f.restype = st
 
 
 def lib():

@@ -886,6 +886,215 @@ fk_status minibatch_impl(fk_ctx *ctxp, const T *x_in, int64_t n, int64_t d, cons
     return FK_OK;
 }
 
+// ------------------------------------------------------------ bisecting --
+// BisectingKMeans::fit (bisecting_kmeans.rs:326-505). The clusters are
+// segments of one row permutation on the device; the host keeps their list
+// (segment, centre slot, SSE) in the reference's order and selects the next
+// cluster as Rust's max_by_key / max_by do (the last of equal maxima). A
+// split runs its n_init 2-means runs together: the two picked rows per run
+// come from the host stream, then per iteration the assignment and changed
+// flags, and the centre sums of the runs that changed; the best run
+// (strictly lowest SSE) partitions the segment into the children (label 0
+// first, each side in row order), whose SSEs are the row-order folds of
+// their rows' distances.
+struct BkCluster {
+    int64_t lo, m;
+    int slot;
+    double sse;  // in F (exact for F = f32 too)
+};
+
+template <typename T>
+fk_status bisecting_impl(fk_ctx *ctxp, const T *x_in, int64_t n, int64_t d, const fk_bisecting_params *p,
+                         T *centers_out, int64_t *labels_out, T *inertia_out, int64_t *n_clusters_out) {
+    Ctx &ctx = *reinterpret_cast<Ctx *>(ctxp);
+    const int64_t k = p->n_clusters;
+    // Validation order of bisecting_kmeans.rs:333-358.
+    if (k <= 0) {
+        set_error("Invalid parameter `n_clusters`: must be at least 1");
+        return FK_ERR_INVALID_PARAMETER;
+    }
+    if (p->n_init <= 0) {
+        set_error("Invalid parameter `n_init`: must be at least 1");
+        return FK_ERR_INVALID_PARAMETER;
+    }
+    if (n <= 0 || n < k) {
+        set_error("Insufficient samples: need at least %lld, got %lld (BisectingKMeans requires at least "
+                  "n_clusters samples)", (long long)k, (long long)(n < 0 ? 0 : n));
+        return FK_ERR_INSUFFICIENT_SAMPLES;
+    }
+    if (p->max_iter < 0) {
+        set_error("Invalid parameter `max_iter`: negative");
+        return FK_ERR_INVALID_PARAMETER;
+    }
+    if (p->strategy != FK_BISECT_LARGEST_CLUSTER && p->strategy != FK_BISECT_LARGEST_SSE) {
+        set_error("Invalid parameter `bisecting_strategy`: %d", p->strategy);
+        return FK_ERR_INVALID_PARAMETER;
+    }
+    if (!x_in || !centers_out || !labels_out || !inertia_out || !n_clusters_out) {
+        set_error("required pointer is NULL");
+        return FK_ERR_NULL_POINTER;
+    }
+    if (fk_status st = check_shape(n, d, k)) return st;
+    if (d > BK_MAX_D || p->n_init > 1024) {
+        set_error("BisectingKMeans on the GPU supports d <= %d and n_init <= 1024 (got d=%lld n_init=%lld)",
+                  BK_MAX_D, (long long)d, (long long)p->n_init);
+        return FK_ERR_UNSUPPORTED;
+    }
+    ctx.bind();
+    cudaStream_t s = ctx.stream;
+    const int runs = (int)p->n_init;
+    const T *x = stage_in<T>(ctx, BUF_X, x_in, (size_t)n * d);
+    int32_t *perm = (int32_t *)ctx.get(BUF_BK_PERM, sizeof(int32_t) * (size_t)n);
+    uint8_t *lab = (uint8_t *)ctx.get(BUF_BK_LAB, (size_t)runs * n);
+    T *cen = (T *)ctx.get(BUF_BK_CEN, sizeof(T) * 2 * (size_t)runs * d);
+    T *dist = (T *)ctx.get(BUF_BK_DIST, sizeof(T) * (size_t)runs * n);
+    int *flags = (int *)ctx.get(BUF_BK_FLAGS, sizeof(int) * 4 * (size_t)runs);
+    int *changed = flags, *active = flags + runs, *picks = flags + 2 * runs;
+    int32_t *scratch = (int32_t *)ctx.get(BUF_BK_SCRATCH, sizeof(int32_t) * bk_partition_scratch_ints(n));
+    T *centres = (T *)ctx.get(BUF_BK_CENTRES, sizeof(T) * (size_t)(k + 1) * d);
+    int64_t *seg = (int64_t *)ctx.get(BUF_BK_SEG, sizeof(int64_t) * (2 * (size_t)k + 2));
+    int64_t *m0_dev = seg + 2 * k;
+    T *fold = (T *)ctx.get(BUF_BK_FOLD, sizeof(T) * (size_t)std::max(runs, 2));
+    {
+        std::vector<int32_t> iota((size_t)n);
+        for (int64_t i = 0; i < n; i++) iota[(size_t)i] = (int32_t)i;
+        FK_CUDA(cudaMemcpyAsync(perm, iota.data(), sizeof(int32_t) * (size_t)n, cudaMemcpyHostToDevice, s));
+        FK_CUDA(cudaStreamSynchronize(s));
+    }
+    // compute_cluster_stats of every row (:192-222): the centre (sums / F::from(n)) and the SSE
+    std::vector<T> hfold((size_t)std::max(runs, 2));
+    FK_CUDA(cudaMemsetAsync(lab, 0, (size_t)n, s));
+    launch_bk_sums<T>(x, (int)d, perm, n, lab, n, cen, nullptr, 1, true, s);
+    launch_bk_dist<T>(x, (int)d, perm, n, cen, lab, n, dist, n, 1, s);
+    launch_bk_fold<T>(dist, n, nullptr, n, 1, false, fold, s);
+    FK_CUDA(cudaMemcpyAsync(centres, cen, sizeof(T) * (size_t)d, cudaMemcpyDeviceToDevice, s));
+    FK_CUDA(cudaMemcpyAsync(hfold.data(), fold, sizeof(T), cudaMemcpyDeviceToHost, s));
+    FK_CUDA(cudaStreamSynchronize(s));
+    std::vector<BkCluster> cl;
+    cl.push_back(BkCluster{0, n, 0, (double)hfold[0]});
+    std::vector<int> free_slots;
+    for (int64_t sl = k; sl >= 1; sl--) free_slots.push_back((int)sl);
+    const uint64_t base = p->has_random_state ? p->random_state : 0;
+    const int64_t max_splits = 4 * n + 4 * k + 16;
+    uint64_t split_count = 0;
+    std::vector<int> hpicks(2 * (size_t)runs), hact((size_t)runs), hch((size_t)runs);
+    while ((int64_t)cl.size() < k) {
+        if ((int64_t)split_count > max_splits) {
+            set_error("the cluster selected for bisection cannot be separated (its rows are identical): the "
+                      "reference does not terminate here");
+            return FK_ERR_NUMERICAL_INSTABILITY;
+        }
+        int64_t t = -1;
+        for (int64_t ci = 0; ci < (int64_t)cl.size(); ci++) {
+            if (cl[(size_t)ci].m < 2) continue;
+            if (t < 0) {
+                t = ci;
+                continue;
+            }
+            const BkCluster &a = cl[(size_t)t], &b = cl[(size_t)ci];
+            const bool a_greater = p->strategy == FK_BISECT_LARGEST_CLUSTER ? a.m > b.m : (T)a.sse > (T)b.sse;
+            if (!a_greater) t = ci;
+        }
+        if (t < 0) break;  // no cluster with two rows left
+        const BkCluster target = cl[(size_t)t];
+        const int64_t m = target.m;
+        int32_t *segp = perm + target.lo;
+        for (int r = 0; r < runs; r++) {
+            UniformStream g(base + split_count * 1000ULL + (uint64_t)r, 0);
+            const int64_t i0 = g.range(m);
+            int64_t i1 = g.range(m);
+            if (m > 1)
+                while (i1 == i0) i1 = g.range(m);
+            hpicks[2 * (size_t)r] = (int)i0;
+            hpicks[2 * (size_t)r + 1] = (int)i1;
+            hact[(size_t)r] = 1;
+        }
+        FK_CUDA(cudaMemcpyAsync(picks, hpicks.data(), sizeof(int) * 2 * (size_t)runs, cudaMemcpyHostToDevice, s));
+        FK_CUDA(cudaMemcpyAsync(active, hact.data(), sizeof(int) * (size_t)runs, cudaMemcpyHostToDevice, s));
+        launch_bk_pick<T>(x, (int)d, segp, picks, runs, cen, s);
+        FK_CUDA(cudaMemset2DAsync(lab, (size_t)n, 0, (size_t)m, (size_t)runs, s));
+        int nact = runs;
+        for (int64_t it = 0; it < p->max_iter && nact > 0; it++) {
+            FK_CUDA(cudaMemsetAsync(changed, 0, sizeof(int) * (size_t)runs, s));
+            launch_bk_assign<T>(x, (int)d, segp, m, cen, lab, n, active, changed, runs, s);
+            FK_CUDA(cudaMemcpyAsync(hch.data(), changed, sizeof(int) * (size_t)runs, cudaMemcpyDeviceToHost, s));
+            FK_CUDA(cudaStreamSynchronize(s));
+            for (int r = 0; r < runs; r++)
+                if (hact[(size_t)r] && !hch[(size_t)r]) {
+                    hact[(size_t)r] = 0;  // no label changed: this run is done (:263)
+                    nact--;
+                }
+            if (nact == 0) break;
+            FK_CUDA(cudaMemcpyAsync(active, hact.data(), sizeof(int) * (size_t)runs, cudaMemcpyHostToDevice, s));
+            launch_bk_sums<T>(x, (int)d, segp, m, lab, n, cen, active, runs, false, s);
+        }
+        // each run's SSE against its final centres (:300-309)
+        launch_bk_dist<T>(x, (int)d, segp, m, cen, lab, n, dist, n, runs, s);
+        launch_bk_fold<T>(dist, n, nullptr, m, runs, false, fold, s);
+        FK_CUDA(cudaMemcpyAsync(hfold.data(), fold, sizeof(T) * (size_t)runs, cudaMemcpyDeviceToHost, s));
+        FK_CUDA(cudaStreamSynchronize(s));
+        int best = -1;
+        T best_sse = FMax<T>::v();
+        for (int r = 0; r < runs; r++)
+            if (hfold[(size_t)r] < best_sse) {
+                best_sse = hfold[(size_t)r];
+                best = r;
+            }
+        split_count++;
+        if (best < 0) {
+            set_error("no 2-means run gave an SSE below F::MAX (non-finite rows)");
+            return FK_ERR_NUMERICAL_INSTABILITY;
+        }
+        const uint8_t *blab = lab + (size_t)best * n;
+        // the children's SSEs (:443-463), then their rows (:430-441)
+        launch_bk_fold<T>(dist + (size_t)best * n, 0, blab, m, 2, true, fold, s);
+        launch_bk_partition(segp, blab, m, scratch, m0_dev, s);
+        int64_t m0 = 0;
+        FK_CUDA(cudaMemcpyAsync(hfold.data(), fold, sizeof(T) * 2, cudaMemcpyDeviceToHost, s));
+        FK_CUDA(cudaMemcpyAsync(&m0, m0_dev, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+        FK_CUDA(cudaStreamSynchronize(s));
+        cl.erase(cl.begin() + t);
+        free_slots.push_back(target.slot);
+        const T *bc = cen + (size_t)best * 2 * d;
+        if (m0 > 0) {
+            const int sl = free_slots.back();
+            free_slots.pop_back();
+            FK_CUDA(cudaMemcpyAsync(centres + (size_t)sl * d, bc, sizeof(T) * (size_t)d, cudaMemcpyDeviceToDevice, s));
+            cl.push_back(BkCluster{target.lo, m0, sl, (double)hfold[0]});
+        }
+        if (m - m0 > 0) {
+            const int sl = free_slots.back();
+            free_slots.pop_back();
+            FK_CUDA(cudaMemcpyAsync(centres + (size_t)sl * d, bc + d, sizeof(T) * (size_t)d, cudaMemcpyDeviceToDevice,
+                                    s));
+            cl.push_back(BkCluster{target.lo + m0, m - m0, sl, (double)hfold[1]});
+        }
+    }
+    // outputs: centres and labels in list order, the SSEs folded in F (:484-498)
+    const int nc = (int)cl.size();
+    std::vector<int64_t> hseg(2 * (size_t)nc);
+    std::vector<int32_t> hslot((size_t)nc);
+    T inertia = T(0);
+    for (int ci = 0; ci < nc; ci++) {
+        hseg[2 * (size_t)ci] = cl[(size_t)ci].lo;
+        hseg[2 * (size_t)ci + 1] = cl[(size_t)ci].m;
+        hslot[(size_t)ci] = cl[(size_t)ci].slot;
+        inertia = inertia + (T)cl[(size_t)ci].sse;
+    }
+    FK_CUDA(cudaMemcpyAsync(seg, hseg.data(), sizeof(int64_t) * hseg.size(), cudaMemcpyHostToDevice, s));
+    FK_CUDA(cudaMemcpyAsync(scratch, hslot.data(), sizeof(int32_t) * hslot.size(), cudaMemcpyHostToDevice, s));
+    T *cout = (T *)ctx.get(BUF_OUT2, sizeof(T) * (size_t)nc * d + 16);
+    launch_gather_rows<T>(centres, (int)d, scratch, nc, cout, s);
+    copy_out<T>(ctx, centers_out, cout, (size_t)nc * d);
+    int64_t *ldev = is_device_ptr(labels_out) ? labels_out : (int64_t *)ctx.get(BUF_BK_LABELS, sizeof(int64_t) * (size_t)n);
+    launch_bk_labels(perm, seg, nc, ldev, s);
+    if (ldev != labels_out) copy_out<int64_t>(ctx, labels_out, ldev, (size_t)n);
+    FK_CUDA(cudaStreamSynchronize(s));
+    *inertia_out = inertia;
+    *n_clusters_out = nc;
+    return FK_OK;
+}
+
 // Per-call state that points into a caller's report: timers not yet read
 // and the contraction timer's target. Dropped before and after every call,
 // so a call that failed half-way never writes into memory it no longer owns.
@@ -1012,6 +1221,28 @@ fk_status fk_minibatch_fit_f32(fk_ctx *ctx, const float *x, int64_t n, int64_t d
     return guarded(ctx, [&] {
         return fk::minibatch_impl<float>(ctx, x, n, d, params, init, c_out, l_out, in_out, it_out, best_out, rep);
     });
+}
+
+void fk_bisecting_params_default(fk_bisecting_params *p, int64_t n_clusters) {
+    if (!p) return;
+    memset(p, 0, sizeof(*p));
+    p->n_clusters = n_clusters;  // BisectingKMeans::new, bisecting_kmeans.rs:93-102
+    p->max_iter = 300;
+    p->n_init = 10;
+    p->has_random_state = 0;
+    p->strategy = FK_BISECT_LARGEST_CLUSTER;
+}
+
+fk_status fk_bisecting_fit_f64(fk_ctx *ctx, const double *x, int64_t n, int64_t d, const fk_bisecting_params *params,
+                               double *c_out, int64_t *l_out, double *in_out, int64_t *nc_out) {
+    if (!params) return FK_ERR_NULL_POINTER;
+    return guarded(ctx, [&] { return fk::bisecting_impl<double>(ctx, x, n, d, params, c_out, l_out, in_out, nc_out); });
+}
+
+fk_status fk_bisecting_fit_f32(fk_ctx *ctx, const float *x, int64_t n, int64_t d, const fk_bisecting_params *params,
+                               float *c_out, int64_t *l_out, float *in_out, int64_t *nc_out) {
+    if (!params) return FK_ERR_NULL_POINTER;
+    return guarded(ctx, [&] { return fk::bisecting_impl<float>(ctx, x, n, d, params, c_out, l_out, in_out, nc_out); });
 }
 
 fk_status fk_minibatch_batch_indices(uint64_t seed, int64_t pos, int64_t n, int64_t batch_size, int64_t iters,

@@ -135,6 +135,8 @@ enum BufSlot {
     BUF_HALF2, BUF_INERTIA2, BUF_C2, BUF_XSTATE, BUF_XCOUNTS, BUF_MOVED, BUF_MOVED_ENT, BUF_MOVED_HIST, BUF_MOVED_TMP,
     BUF_CSPLIT, BUF_RINERT, BUF_F64ITEMS, BUF_INIT,
     BUF_MB_IDX, BUF_MB_XB, BUF_MB_LAB, BUF_MB_OLD, BUF_MB_COUNTS,
+    BUF_BK_PERM, BUF_BK_LAB, BUF_BK_CEN, BUF_BK_DIST, BUF_BK_FLAGS, BUF_BK_SCRATCH, BUF_BK_CENTRES, BUF_BK_SEG,
+    BUF_BK_FOLD, BUF_BK_LABELS,
     BUF_BX, BUF_BFITS, BUF_BSTATE, BUF_BITEMS, BUF_BPART, BUF_BORDER, BUF_BCTR, BUF_BLAB, BUF_BMEM, BUF_BCEN, BUF_BND, BUF_BXOFF,
     BUF_COUNT
 };
@@ -293,6 +295,29 @@ void launch_gather_rows(const T *x, int d, const int32_t *idx, int64_t m, T *out
 template <typename T>
 void launch_minibatch_update(const T *xb, const int32_t *labels, int64_t m, int d, int k, T *centres, T *old,
                              long long *counts, unsigned long long *shift_bits, cudaStream_t s);
+
+// BisectingKMeans (bisecting_kmeans.rs): the n_init 2-means runs of one
+// split over a segment of the row permutation perm (m rows). Per run: two
+// centres (cen, run-major 2 x d), uint8 labels (stride lab_stride), a
+// changed flag; active selects the runs still iterating (NULL: every run).
+constexpr int BK_MAX_D = 1024;  // 2 d (side, feature) chains per CTA
+template <typename T>
+void launch_bk_pick(const T *x, int d, const int32_t *perm, const int32_t *picks, int runs, T *cen, cudaStream_t s);
+template <typename T>
+void launch_bk_assign(const T *x, int d, const int32_t *perm, int64_t m, const T *cen, uint8_t *lab,
+                      int64_t lab_stride, const int *active, int *changed, int runs, cudaStream_t s);
+template <typename T>
+void launch_bk_sums(const T *x, int d, const int32_t *perm, int64_t m, const uint8_t *lab, int64_t lab_stride,
+                    T *cen, const int *active, int runs, bool whole_count, cudaStream_t s);
+template <typename T>
+void launch_bk_dist(const T *x, int d, const int32_t *perm, int64_t m, const T *cen, const uint8_t *lab,
+                    int64_t lab_stride, T *dist, int64_t dist_stride, int runs, cudaStream_t s);
+template <typename T>
+void launch_bk_fold(const T *dist, int64_t dist_stride, const uint8_t *lab, int64_t m, int nsum, bool by_label, T *out,
+                    cudaStream_t s);
+size_t bk_partition_scratch_ints(int64_t m);
+void launch_bk_partition(int32_t *seg, const uint8_t *lab, int64_t m, int32_t *scratch, int64_t *m0, cudaStream_t s);
+void launch_bk_labels(const int32_t *perm, const int64_t *seg, int nclusters, int64_t *labels, cudaStream_t s);
 template <typename TS, typename TD>
 void launch_convert(const TS *src, int64_t count, TD *dst, cudaStream_t s);
 

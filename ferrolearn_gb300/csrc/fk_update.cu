@@ -1124,6 +1124,187 @@ __global__ void __launch_bounds__(MB_THREADS)
     if (threadIdx.x == 0) counts[c] = cnt;
 }
 
+// ------------------------------------------------------- bisecting --
+// BisectingKMeans (bisecting_kmeans.rs): a cluster is a segment of a row
+// permutation; the n_init 2-means runs of one split proceed together
+// (blockIdx.y or blockIdx.x = run), each with its labels (uint8, stride
+// lab_stride), two centres (2 x d, run-major) and a changed flag.
+
+// Each run's centres from its two picked positions of the segment.
+template <typename T>
+__global__ void bk_pick_kernel(const T *__restrict__ x, int d, const int32_t *__restrict__ perm,
+                               const int32_t *__restrict__ picks, T *__restrict__ cen) {
+    const int run = blockIdx.x;
+    T *c = cen + (int64_t)run * 2 * d;
+    const int64_t r0 = perm[picks[2 * run]], r1 = perm[picks[2 * run + 1]];
+    for (int j = threadIdx.x; j < d; j += blockDim.x) {
+        c[j] = x[r0 * d + j];
+        c[d + j] = x[r1 * d + j];
+    }
+}
+
+// run_2means' assignment (:245-262): label 0 when d0 <= d1 (direct forms),
+// else 1; any change sets the run's flag. Runs that stopped are skipped.
+template <typename T>
+__global__ void bk_assign_kernel(const T *__restrict__ x, int d, const int32_t *__restrict__ perm, int64_t m,
+                                 const T *__restrict__ cen, uint8_t *__restrict__ lab, int64_t lab_stride,
+                                 const int *__restrict__ active, int *__restrict__ changed) {
+    using A = UArith<T>;
+    const int run = blockIdx.y;
+    if (!active[run]) return;  // uniform over the block
+    const T *c0 = cen + (int64_t)run * 2 * d;
+    const T *c1 = c0 + d;
+    uint8_t *l = lab + (int64_t)run * lab_stride;
+    int any = 0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
+        const T *row = x + (int64_t)perm[i] * d;
+        T d0 = T(0), d1 = T(0);
+        for (int j = 0; j < d; j++) {
+            const T v = row[j];
+            const T t0 = A::sub(v, c0[j]);
+            d0 = A::add(d0, A::mul(t0, t0));
+            const T t1 = A::sub(v, c1[j]);
+            d1 = A::add(d1, A::mul(t1, t1));
+        }
+        const uint8_t nl = d0 <= d1 ? 0 : 1;
+        if (nl != l[i]) {
+            l[i] = nl;
+            any = 1;
+        }
+    }
+    if (__syncthreads_or(any) && threadIdx.x == 0) changed[run] = 1;
+}
+
+// run_2means' centre update (:264-298) and compute_cluster_stats' centre
+// (:192-211): per side, the segment's rows summed in row order in F, the
+// count as F (+1 per row, or F::from(m) for the whole segment when
+// whole_count), and sum / count for a side with rows (an empty side keeps
+// its centre). One CTA per run: the rows are staged in shared memory a chunk
+// at a time and every thread keeps the chains of fixed (side, feature)
+// pairs, so each sum has the reference's order.
+constexpr int BK_THREADS = 256;
+constexpr int BK_PER = 8;  // (side, feature) pairs per thread: 2 d <= 2048
+
+template <typename T>
+__global__ void __launch_bounds__(BK_THREADS)
+    bk_sums_kernel(const T *__restrict__ x, int d, const int32_t *__restrict__ perm, int64_t m,
+                   const uint8_t *__restrict__ lab, int64_t lab_stride, T *__restrict__ cen,
+                   const int *__restrict__ active, int chunk, int whole_count) {
+    using A = UArith<T>;
+    const int run = blockIdx.x;
+    if (active && !active[run]) return;  // uniform over the block
+    extern __shared__ __align__(16) unsigned char bk_smem[];
+    T *rows = reinterpret_cast<T *>(bk_smem);
+    uint8_t *labs = reinterpret_cast<uint8_t *>(rows + (size_t)chunk * d);
+    const uint8_t *l = lab + (int64_t)run * lab_stride;
+    const int npairs = 2 * d;
+    int side_of[BK_PER], feat_of[BK_PER];
+    T sum[BK_PER];
+#pragma unroll
+    for (int q = 0; q < BK_PER; q++) {
+        const int t = threadIdx.x + q * BK_THREADS;
+        side_of[q] = t < npairs ? t / d : 2;  // 2: no pair
+        feat_of[q] = t < npairs ? t - (t / d) * d : 0;
+        sum[q] = T(0);
+    }
+    T cnt0 = T(0), cnt1 = T(0);
+    for (int64_t b0 = 0; b0 < m; b0 += chunk) {
+        const int len = (int)(m - b0 < chunk ? m - b0 : chunk);
+        __syncthreads();  // the previous chunk is no longer read
+        for (int e = threadIdx.x; e < len * d; e += BK_THREADS) {
+            const int r = e / d;
+            rows[e] = x[(int64_t)perm[b0 + r] * d + (e - r * d)];
+        }
+        for (int r = threadIdx.x; r < len; r += BK_THREADS) labs[r] = l[b0 + r];
+        __syncthreads();
+        for (int r = 0; r < len; r++) {
+            const int side = labs[r];
+            if (side == 0) cnt0 = A::add(cnt0, T(1));
+            else cnt1 = A::add(cnt1, T(1));
+#pragma unroll
+            for (int q = 0; q < BK_PER; q++)
+                if (side_of[q] == side) sum[q] = A::add(sum[q], rows[r * d + feat_of[q]]);
+        }
+    }
+    if (whole_count) cnt0 = (T)m;
+    T *c = cen + (int64_t)run * 2 * d;
+#pragma unroll
+    for (int q = 0; q < BK_PER; q++) {
+        if (side_of[q] > 1) continue;
+        const T cnt = side_of[q] == 0 ? cnt0 : cnt1;
+        if (cnt > T(0)) c[side_of[q] * d + feat_of[q]] = A::div(sum[q], cnt);
+    }
+}
+
+// Each row's direct-form distance to its run's centre of its label.
+template <typename T>
+__global__ void bk_dist_kernel(const T *__restrict__ x, int d, const int32_t *__restrict__ perm, int64_t m,
+                               const T *__restrict__ cen, const uint8_t *__restrict__ lab, int64_t lab_stride,
+                               T *__restrict__ dist, int64_t dist_stride) {
+    using A = UArith<T>;
+    const int run = blockIdx.y;
+    const T *c = cen + (int64_t)run * 2 * d;
+    const uint8_t *l = lab + (int64_t)run * lab_stride;
+    T *o = dist + (int64_t)run * dist_stride;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
+        const T *row = x + (int64_t)perm[i] * d;
+        const T *cc = l[i] ? c + d : c;
+        T acc = T(0);
+        for (int j = 0; j < d; j++) {
+            const T t = A::sub(row[j], cc[j]);
+            acc = A::add(acc, A::mul(t, t));
+        }
+        o[i] = acc;
+    }
+}
+
+// The reference's `sse = sse + ...` folds, in row order: thread t sums
+// dist[t * dist_stride + i] over the rows i < m (by_label = 0: every row),
+// or, with by_label, thread t in {0, 1} sums dist[i] over the rows of label t.
+template <typename T>
+__global__ void bk_fold_kernel(const T *__restrict__ dist, int64_t dist_stride, const uint8_t *__restrict__ lab,
+                               int64_t m, int nsum, int by_label, T *__restrict__ out) {
+    using A = UArith<T>;
+    const int t = threadIdx.x;
+    if (t >= nsum) return;
+    const T *v = by_label ? dist : dist + (int64_t)t * dist_stride;
+    T acc = T(0);
+    if (by_label) {
+        for (int64_t i = 0; i < m; i++)
+            if (lab[i] == t) acc = A::add(acc, v[i]);
+    } else {
+#pragma unroll 8
+        for (int64_t i = 0; i < m; i++) acc = A::add(acc, v[i]);
+    }
+    out[t] = acc;
+}
+
+// Stable partition of a segment by labels (label 0 first, each side in row
+// order): pos holds the exclusive scan of (label == 0).
+__global__ void bk_flag_kernel(const uint8_t *__restrict__ lab, int64_t m, int32_t *__restrict__ flag) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x)
+        flag[i] = lab[i] == 0 ? 1 : 0;
+}
+
+__global__ void bk_zeros_kernel(const int32_t *__restrict__ pos, const uint8_t *__restrict__ lab, int64_t m,
+                                int64_t *__restrict__ m0) {
+    *m0 = (int64_t)pos[m - 1] + (lab[m - 1] == 0 ? 1 : 0);
+}
+
+__global__ void bk_scatter_kernel(const int32_t *__restrict__ seg, const uint8_t *__restrict__ lab,
+                                  const int32_t *__restrict__ pos, int64_t m, const int64_t *__restrict__ m0,
+                                  int32_t *__restrict__ out) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x)
+        out[lab[i] == 0 ? (int64_t)pos[i] : *m0 + (i - (int64_t)pos[i])] = seg[i];
+}
+
+// Final labels: cluster ci (block ci) owns the rows of its segment.
+__global__ void bk_labels_kernel(const int32_t *__restrict__ perm, const int64_t *__restrict__ seg,
+                                 int64_t *__restrict__ labels) {
+    const int64_t lo = seg[2 * blockIdx.x], m = seg[2 * blockIdx.x + 1];
+    for (int64_t i = threadIdx.x; i < m; i += blockDim.x) labels[perm[lo + i]] = blockIdx.x;
+}
+
 }  // namespace
 
 template <typename T>
@@ -1143,6 +1324,98 @@ void launch_minibatch_update(const T *xb, const int32_t *labels, int64_t m, int 
     FK_LAUNCH_CHECK();
     launch_max_shift<T>(centres, old, k, d, shift_bits, s);
 }
+
+int bk_chunk_rows(int d, size_t elem) {
+    const size_t per = (size_t)d * elem + 1;
+    const size_t rows = (40 * 1024) / per;
+    return (int)std::max<size_t>(1, std::min<size_t>(64, rows));
+}
+
+template <typename T>
+void launch_bk_pick(const T *x, int d, const int32_t *perm, const int32_t *picks, int runs, T *cen, cudaStream_t s) {
+    bk_pick_kernel<T><<<(unsigned)runs, 128, 0, s>>>(x, d, perm, picks, cen);
+    FK_LAUNCH_CHECK();
+}
+
+template <typename T>
+void launch_bk_assign(const T *x, int d, const int32_t *perm, int64_t m, const T *cen, uint8_t *lab,
+                      int64_t lab_stride, const int *active, int *changed, int runs, cudaStream_t s) {
+    const unsigned gx = (unsigned)std::max<int64_t>(1, std::min<int64_t>((m + 255) / 256, 1024));
+    bk_assign_kernel<T><<<dim3(gx, (unsigned)runs), 256, 0, s>>>(x, d, perm, m, cen, lab, lab_stride, active, changed);
+    FK_LAUNCH_CHECK();
+}
+
+template <typename T>
+void launch_bk_sums(const T *x, int d, const int32_t *perm, int64_t m, const uint8_t *lab, int64_t lab_stride,
+                    T *cen, const int *active, int runs, bool whole_count, cudaStream_t s) {
+    const int chunk = bk_chunk_rows(d, sizeof(T));
+    const size_t smem = (size_t)chunk * d * sizeof(T) + (size_t)chunk;
+    bk_sums_kernel<T><<<(unsigned)runs, BK_THREADS, smem, s>>>(x, d, perm, m, lab, lab_stride, cen, active, chunk,
+                                                               whole_count ? 1 : 0);
+    FK_LAUNCH_CHECK();
+}
+
+template <typename T>
+void launch_bk_dist(const T *x, int d, const int32_t *perm, int64_t m, const T *cen, const uint8_t *lab,
+                    int64_t lab_stride, T *dist, int64_t dist_stride, int runs, cudaStream_t s) {
+    const unsigned gx = (unsigned)std::max<int64_t>(1, std::min<int64_t>((m + 255) / 256, 1024));
+    bk_dist_kernel<T><<<dim3(gx, (unsigned)runs), 256, 0, s>>>(x, d, perm, m, cen, lab, lab_stride, dist,
+                                                               dist_stride);
+    FK_LAUNCH_CHECK();
+}
+
+template <typename T>
+void launch_bk_fold(const T *dist, int64_t dist_stride, const uint8_t *lab, int64_t m, int nsum, bool by_label, T *out,
+                    cudaStream_t s) {
+    bk_fold_kernel<T><<<1, 32 * ((nsum + 31) / 32), 0, s>>>(dist, dist_stride, lab, m, nsum, by_label ? 1 : 0, out);
+    FK_LAUNCH_CHECK();
+}
+
+size_t bk_partition_scratch_ints(int64_t m) { return 2 * (size_t)m + (size_t)((m + SCAN_TILE - 1) / SCAN_TILE + 1); }
+
+// The segment reordered in place: its label-0 rows first, each side in row
+// order (*m0 receives their count). scratch: bk_partition_scratch_ints(m).
+void launch_bk_partition(int32_t *seg, const uint8_t *lab, int64_t m, int32_t *scratch, int64_t *m0,
+                         cudaStream_t s) {
+    if (m <= 0) return;
+    int32_t *pos = scratch;      // m: exclusive scan of (label == 0)
+    int32_t *out = scratch + m;  // m: the reordered segment
+    int32_t *tmp = out + m;      // the scan's block sums
+    const unsigned g = (unsigned)std::max<int64_t>(1, std::min<int64_t>((m + 255) / 256, 4096));
+    bk_flag_kernel<<<g, 256, 0, s>>>(lab, m, pos);
+    FK_LAUNCH_CHECK();
+    launch_scan(pos, m, tmp, s);
+    bk_zeros_kernel<<<1, 1, 0, s>>>(pos, lab, m, m0);
+    FK_LAUNCH_CHECK();
+    bk_scatter_kernel<<<g, 256, 0, s>>>(seg, lab, pos, m, m0, out);
+    FK_LAUNCH_CHECK();
+    FK_CUDA(cudaMemcpyAsync(seg, out, sizeof(int32_t) * (size_t)m, cudaMemcpyDeviceToDevice, s));
+}
+
+void launch_bk_labels(const int32_t *perm, const int64_t *seg, int nclusters, int64_t *labels, cudaStream_t s) {
+    if (nclusters <= 0) return;
+    bk_labels_kernel<<<(unsigned)nclusters, 256, 0, s>>>(perm, seg, labels);
+    FK_LAUNCH_CHECK();
+}
+
+template void launch_bk_pick<double>(const double *, int, const int32_t *, const int32_t *, int, double *,
+                                     cudaStream_t);
+template void launch_bk_pick<float>(const float *, int, const int32_t *, const int32_t *, int, float *, cudaStream_t);
+template void launch_bk_assign<double>(const double *, int, const int32_t *, int64_t, const double *, uint8_t *,
+                                       int64_t, const int *, int *, int, cudaStream_t);
+template void launch_bk_assign<float>(const float *, int, const int32_t *, int64_t, const float *, uint8_t *, int64_t,
+                                      const int *, int *, int, cudaStream_t);
+template void launch_bk_sums<double>(const double *, int, const int32_t *, int64_t, const uint8_t *, int64_t, double *,
+                                     const int *, int, bool, cudaStream_t);
+template void launch_bk_sums<float>(const float *, int, const int32_t *, int64_t, const uint8_t *, int64_t, float *,
+                                    const int *, int, bool, cudaStream_t);
+template void launch_bk_dist<double>(const double *, int, const int32_t *, int64_t, const double *, const uint8_t *,
+                                     int64_t, double *, int64_t, int, cudaStream_t);
+template void launch_bk_dist<float>(const float *, int, const int32_t *, int64_t, const float *, const uint8_t *,
+                                    int64_t, float *, int64_t, int, cudaStream_t);
+template void launch_bk_fold<double>(const double *, int64_t, const uint8_t *, int64_t, int, bool, double *,
+                                     cudaStream_t);
+template void launch_bk_fold<float>(const float *, int64_t, const uint8_t *, int64_t, int, bool, float *, cudaStream_t);
 
 template void launch_gather_rows<double>(const double *, int, const int32_t *, int64_t, double *, cudaStream_t);
 template void launch_gather_rows<float>(const float *, int, const int32_t *, int64_t, float *, cudaStream_t);

@@ -309,6 +309,48 @@ fk_status fk_minibatch_fit_f32(fk_ctx *ctx, const float *x, int64_t n, int64_t d
                                float *centers_out, uint64_t *labels_out, float *inertia_out,
                                int64_t *n_iter_out, int64_t *best_run_out, fk_fit_report *report);
 
+/* ------------------------------------------------------ BisectingKMeans --
+ * ferrolearn-cluster/src/bisecting_kmeans.rs. Builder defaults of
+ * BisectingKMeans::new (:93-102): max_iter 300, n_init 10, random_state
+ * None, LargestCluster. */
+typedef enum fk_bisecting_strategy {
+    FK_BISECT_LARGEST_CLUSTER = 0, /* BisectingStrategy::LargestCluster */
+    FK_BISECT_LARGEST_SSE = 1      /* BisectingStrategy::LargestSSE     */
+} fk_bisecting_strategy;
+
+typedef struct fk_bisecting_params {
+    int64_t n_clusters;       /* BisectingKMeans::n_clusters (target)      */
+    int64_t max_iter;         /* iterations per 2-means        (300)       */
+    int64_t n_init;           /* 2-means restarts per split    (10)        */
+    uint64_t random_state;    /* BisectingKMeans::random_state, if set     */
+    int32_t has_random_state; /* 0 = None (base seed 0)                    */
+    int32_t strategy;         /* fk_bisecting_strategy                     */
+} fk_bisecting_params;
+
+void fk_bisecting_params_default(fk_bisecting_params *p, int64_t n_clusters);
+
+/* BisectingKMeans::fit (:326-505): from one cluster of every row, split
+ * the cluster with the most rows (or the largest SSE; the last of equal
+ * maxima, as Rust's max_by_key / max_by) by the best of n_init 2-means runs
+ * (run_2means, :225-312: two distinct rows of the cluster, label 0 when
+ * d0 <= d1, row-order sums in F, until no label changes), until n_clusters
+ * clusters or none with two rows is left. Run r of split s draws the
+ * library's uniform stream seeded with random_state + s * 1000 + r (the
+ * seeds of :410-412). Outputs: centers_out (n_clusters * d, the first
+ * *n_clusters_out rows filled), labels_out (n, the final cluster of each
+ * row, isize in the reference), inertia_out (the clusters' SSE summed in
+ * list order). Predict and Transform of the fitted model are those of KMeans
+ * (fk_kmeans_predict_* / fk_kmeans_transform_*). d <= 1024, n_init <= 1024. Where the
+ * reference would not terminate (the selected cluster's rows are identical,
+ * so every split leaves one side empty) the call returns
+ * FK_ERR_NUMERICAL_INSTABILITY. */
+fk_status fk_bisecting_fit_f64(fk_ctx *ctx, const double *x, int64_t n, int64_t d,
+                               const fk_bisecting_params *params, double *centers_out, int64_t *labels_out,
+                               double *inertia_out, int64_t *n_clusters_out);
+fk_status fk_bisecting_fit_f32(fk_ctx *ctx, const float *x, int64_t n, int64_t d,
+                               const fk_bisecting_params *params, float *centers_out, int64_t *labels_out,
+                               float *inertia_out, int64_t *n_clusters_out);
+
 /* The batch rows MiniBatchKMeans draws (sample_batch_indices, :451-472)
  * for `iters` iterations from position pos of the uniform stream of seed:
  * out holds iters * min(batch_size, n) row indices. Host-only. */

@@ -194,3 +194,40 @@ def test_oracle_matches_a_literal_python_restatement(strategy, n, d, k):
     assert np.array_equal(got["labels"], want_l)
     assert np.array_equal(got["centers"], want_c)
     assert got["inertia"] == want_i
+
+
+# The library's side without a GPU: defaults and argument errors in the
+# reference's validation order (bisecting_kmeans.rs:333-358).
+def test_library_defaults_match_the_builder():
+    import ctypes as C
+    import ferrolearn_gb300 as F
+    from ferrolearn_gb300 import _native
+    p = _native.BisectingParams()
+    _native.lib().fk_bisecting_params_default(C.byref(p), 5)
+    assert (p.n_clusters, p.max_iter, p.n_init, p.has_random_state, p.strategy) == (5, 300, 10, 0, 0)  # :93-102
+    m = F.BisectingKMeans(5)
+    assert (m.max_iter, m.n_init, m.random_state, m.strategy) == (300, 10, None, "largest_cluster")
+
+
+@pytest.mark.parametrize("k,x,kw,exc,needle", [
+    (0, np.ones((3, 2)), {}, "InvalidParameter", "n_clusters"),
+    (3, np.ones((9, 2)), dict(n_init=0), "InvalidParameter", "n_init"),
+    (3, np.zeros((0, 2)), {}, "InsufficientSamples", "Insufficient"),
+    (5, np.ones((2, 2)), {}, "InsufficientSamples", "Insufficient"),
+    (0, np.zeros((0, 2)), dict(n_init=0), "InvalidParameter", "n_clusters"),
+    (2, np.ones((4, 1025)), {}, "Unsupported", "d <= 1024"),
+])
+def test_library_validation_order(k, x, kw, exc, needle):
+    import ferrolearn_gb300 as F
+    for dtype in ("f64", "f32"):
+        m = F.BisectingKMeans(k, dtype=dtype)
+        if "n_init" in kw:
+            m.with_n_init(kw["n_init"])
+        with pytest.raises(getattr(F, exc), match=needle):
+            m.fit(x)
+
+
+def test_library_rejects_unknown_strategy():
+    import ferrolearn_gb300 as F
+    with pytest.raises(F.InvalidParameter):
+        F.BisectingKMeans(2).with_bisecting_strategy("smallest")
