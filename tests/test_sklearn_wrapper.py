@@ -95,3 +95,18 @@ def test_minibatch_wrapper_defaults_and_validation():
     from sklearn.base import clone
     c = clone(MiniBatchKMeans(n_clusters=3, random_state=4)).set_params(max_iter=7)
     assert (c.n_clusters, c.random_state, c.max_iter) == (3, 4, 7)
+
+
+def test_pickled_wrapper_keeps_what_predict_needs():
+    # host-side state only: a fitted wrapper survives pickling with its centres,
+    # labels and the precision its predict uses
+    km = KMeans(n_clusters=2, precision="bf16")
+    km.cluster_centers_ = np.array([[0.0, 1.0], [2.0, 3.0]])
+    km.labels_ = np.array([0, 1, 1])
+    km.inertia_, km.n_iter_, km.n_features_in_ = 1.5, 4, 2
+    km._fitted = F.FittedKMeans(km.cluster_centers_.copy(), km.labels_.copy(), 1.5, 4, "f32x64", precision=F.MIXED_BF16)
+    km2 = pickle.loads(pickle.dumps(km))
+    assert np.array_equal(km2._fitted.cluster_centers(), km.cluster_centers_)
+    assert km2._fitted.dtype == "f32x64" and km2._fitted.precision == F.MIXED_BF16
+    assert (km2.inertia_, km2.n_iter_, km2.precision) == (1.5, 4, "bf16")
+    assert np.array_equal(km2._fitted.labels(), km.labels_)
