@@ -751,7 +751,7 @@ PFN_cuTensorMapEncodeTiled_v12000 get_encode(Ctx &ctx) {
         cudaDriverEntryPointQueryResult qr;
         FK_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &qr));
         if (!fn || qr != cudaDriverEntryPointSuccess) {
-            set_error("cuTensorMapEncodeTiled is not available from the driver");
+            set_error("cuTensorMapEncodeTiled is not available from the CUDA driver");
             fail(FK_ERR_CUDA);
         }
         ctx.tmap_fn = fn;
