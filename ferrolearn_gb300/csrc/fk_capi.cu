@@ -84,6 +84,10 @@ int kpp_trials_host(int64_t k) {
 
 namespace {
 
+// True for device (or managed) memory the call can use in place, false for
+// host memory. Device memory of another GPU than the context's is refused
+// with FK_ERR_INVALID_PARAMETER: without peer access a kernel reading it
+// would fault instead of returning an error.
 bool is_device_ptr(const void *p) {
     if (!p) return false;
     cudaPointerAttributes a;
@@ -92,7 +96,16 @@ bool is_device_ptr(const void *p) {
         (void)cudaGetLastError();
         return false;
     }
-    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+    if (a.type == cudaMemoryTypeDevice) {
+        int cur = 0;
+        FK_CUDA(cudaGetDevice(&cur));
+        if (a.device != cur) {
+            set_error("buffer %p is device memory of GPU %d, but the call runs on GPU %d", p, a.device, cur);
+            fail(FK_ERR_INVALID_PARAMETER);
+        }
+        return true;
+    }
+    return a.type == cudaMemoryTypeManaged;
 }
 
 template <typename T>

@@ -1,17 +1,43 @@
-// fk_kpp.cu -- greedy k-means++ on the GPU (kmeans.rs:169-253).
+// fk_kpp.cu -- greedy k-means++ on the GPU (kmeans.rs:169-253), with the
+// reference's arithmetic: every sum is the sequential left fold in F.
 //
-// Per new centre, with no host round trip: fixed-order block sums of the D^2
-// array, a single-block pass that forms the total, reads the next uniform
-// draws and turns each into a threshold u * total (in F, as kmeans.rs:213-214),
-// one block per trial that finds the first row whose running sum reaches the
-// threshold (the sequential cumsum of kmeans.rs:215-223), a pass that forms
-// min(D^2, d(x, candidate)) for every trial and its potential, and a choice of
-// the strictly smallest potential (first trial wins ties, kmeans.rs:239-243).
-// A non-positive total takes one uniform draw as a random row
-// (kmeans.rs:202-206). Distances are the direct form with no FMA, identical
-// to the reference; the sums are exact-order-independent fixed trees in f64,
-// so a candidate can differ from a sequential fold only when a threshold
-// falls within rounding of a running-sum boundary.
+// The reference forms three sums per new centre, each a left fold in F from
+// zero in row order: the total of the D^2 array (kmeans.rs:201), the running
+// cumsum that locates each trial's candidate (:215-223), and each trial's
+// potential (:225-237). A fold in F is not associative, so a tree gives other
+// roundings and, at scale, other candidates. Here each fold is computed
+// exactly as the sequential one, in parallel:
+//
+//   While the running sum p stays in one binade [2^e, 2^(e+1)), p is an
+//   integer P on that binade's ulp grid, and adding v >= 0 rounds to
+//   P + round(v / ulp) -- except for an exact half, where round-to-nearest-even
+//   picks the even result, so the step depends on P's parity. Each element is
+//   therefore a map P -> P + a[P & 1], and so is any run of elements: these
+//   maps compose (associatively), and a composed map is exact whenever the
+//   final P stays below the binade's top (the sum only grows, so every
+//   intermediate stayed inside too).
+//
+// kpp_compose_kernel forms, per chunk of KPP_CH values, the composed map for
+// the three binades around the chunk's estimated starting sum (an f64 prefix
+// of chunk sums; the estimate only steers speed, never the result).
+// kpp_walk_kernel then walks the chunks with one warp per fold: a chunk whose
+// map applies is one integer add; otherwise (the sum changes binade inside
+// it, or is zero or non-finite) the warp walks the chunk 32 values at a time
+// with a warp scan of the same maps, taking one exact F addition at each
+// element where the binade changes. Every state it records is bit for bit
+// the reference's running sum.
+//
+// Per new centre: kpp_select_kernel resolves the previous centre's trials
+// (strictly smallest potential, first trial on ties: kmeans.rs:239-243),
+// draws the thresholds u * total in F (:213-214) and finds each trial's
+// candidate (the first row whose running sum reaches its threshold: a 32-ary
+// search over the recorded chunk states, then the chunk walked exactly);
+// kpp_trials_kernel forms min(D^2, d(x, candidate)) for every trial in one
+// pass over X (direct-form distances, no FMA, identical to the reference);
+// compose and walk give every trial's potential and its chunk states, which
+// the next centre's search uses (the chosen trial's D^2 array becomes the new
+// one without a copy: two buffers alternate). A non-positive total takes one
+// uniform draw as a random row (:202-206).
 #include <cfloat>
 #include <cmath>
 
@@ -30,49 +56,217 @@ template <typename T> __device__ __forceinline__ T kpp_add(T a, T b);
 template <> __device__ __forceinline__ float kpp_add(float a, float b) { return __fadd_rn(a, b); }
 template <> __device__ __forceinline__ double kpp_add(double a, double b) { return __dadd_rn(a, b); }
 
-template <typename T>
-__device__ __forceinline__ T sqeuc(const T *__restrict__ a, const T *__restrict__ b, int d) {
-    T acc = T(0);
-    for (int j = 0; j < d; j++) {
-        T t = kpp_sub(a[j], b[j]);
-        acc = kpp_add(acc, kpp_mul(t, t));
-    }
-    return acc;
-}
-
-constexpr int KPP_BLOCK = 4096;  // rows per partial sum
+constexpr int KPP_CH = 1024;      // values per fold chunk (and rows per trial-pass CTA)
 constexpr int KPP_THREADS = 256;
 constexpr int MAX_TRIALS = 16;
+constexpr int KPP_DJ = 16;        // features staged per step of the trial pass
+constexpr long long KPP_SAT = 1LL << 61;  // saturated increment: never applies
 
-struct KppState {
-    long long cursor;             // uniform draws consumed so far
-    int direct;                   // 1 = this centre was a uniform random row
-    int best_trial;
-    long long cand[MAX_TRIALS];   // candidate row per trial
-    double thr[MAX_TRIALS];       // threshold per trial (value of F, widened)
-    double total;
+// ---------------------------------------------------- binade arithmetic --
+template <typename T> struct Bits;
+template <> struct Bits<float> {
+    using U = uint32_t;
+    static constexpr int MB = 23;      // stored mantissa bits
+    static constexpr int EXPM = 0xFF;  // all-ones exponent (inf / NaN)
+    static __device__ __forceinline__ U bits(float v) { return __float_as_uint(v); }
+    static __device__ __forceinline__ float from(U b) { return __uint_as_float(b); }
+};
+template <> struct Bits<double> {
+    using U = unsigned long long;
+    static constexpr int MB = 52;
+    static constexpr int EXPM = 0x7FF;
+    static __device__ __forceinline__ U bits(double v) { return (U)__double_as_longlong(v); }
+    static __device__ __forceinline__ double from(U b) { return __longlong_as_double((long long)b); }
 };
 
-__device__ __forceinline__ double warp_sum(double v) {
-#pragma unroll
-    for (int off = 16; off >= 1; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
-    return v;
+// Biased exponent of a positive normal finite value, else 0.
+template <typename T>
+__device__ __forceinline__ int normal_exp(T p) {
+    using B = Bits<T>;
+    const typename B::U b = B::bits(p);
+    const int be = (int)((b >> B::MB) & (typename B::U)B::EXPM);
+    const bool neg = (b >> (sizeof(typename B::U) * 8 - 1)) != 0;
+    return (!neg && be >= 1 && be < B::EXPM) ? be : 0;
 }
 
-// Fixed tree over the block: per-warp butterflies, then warp 0 folds.
-__device__ double block_sum(double v, double *sh) {
-    v = warp_sum(v);
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    __syncthreads();
-    if (lane == 0) sh[w] = v;
-    __syncthreads();
-    double r = 0.0;
-    if (w == 0) {
-        r = lane < (int)(blockDim.x >> 5) ? sh[lane] : 0.0;
-        r = warp_sum(r);
-    }
-    return r;
+template <typename T>
+__device__ __forceinline__ bool is_inf_or_nan(T p) {
+    using B = Bits<T>;
+    return (int)((B::bits(p) >> B::MB) & (typename B::U)B::EXPM) == B::EXPM;
 }
+
+// Significand of a normal value as an integer in [2^MB, 2^(MB+1)).
+template <typename T>
+__device__ __forceinline__ long long significand(T p) {
+    using B = Bits<T>;
+    const typename B::U m = ((typename B::U)1 << B::MB) - 1;
+    return (long long)((B::bits(p) & m) | ((typename B::U)1 << B::MB));
+}
+
+template <typename T>
+__device__ __forceinline__ T from_parts(int be, long long P) {
+    using B = Bits<T>;
+    const typename B::U m = ((typename B::U)1 << B::MB) - 1;
+    return B::from(((typename B::U)be << B::MB) | ((typename B::U)P & m));
+}
+
+__device__ __forceinline__ double pow2d(int s) {  // 2^s for s in [-1022, 1023]
+    return __longlong_as_double((long long)(1023 + s) << 52);
+}
+
+// Increment map of one value v >= 0 on the grid of binade be: a0 / a1 for a
+// running sum whose significand is even / odd.
+struct Step {
+    long long a0, a1;
+};
+
+__device__ __forceinline__ Step step_from_scaled(double s) {
+    // s = v / ulp (exact); from 2^60 on (beyond any binade's 2^53 steps) saturate
+    if (!(s < 1152921504606846976.0)) return {KPP_SAT, KPP_SAT};
+    const double fl = floor(s);
+    const double fr = s - fl;  // exact
+    const long long q = (long long)fl;
+    if (fr > 0.5) return {q + 1, q + 1};
+    if (fr < 0.5) return {q, q};
+    return {q + (q & 1), q + ((q + 1) & 1)};  // exact half: the even neighbour
+}
+
+__device__ __forceinline__ Step step_of(float v, int be) {
+    const double vv = (double)v;
+    if (!(vv <= 3.5e38)) return {KPP_SAT, KPP_SAT};  // inf or NaN (v is never negative)
+    if (vv == 0.0) return {0, 0};
+    return step_from_scaled(vv * pow2d(150 - be));  // ulp = 2^(be - 150), exact in f64
+}
+
+__device__ __forceinline__ Step step_of(double v, int be) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    const int ev = (int)((b >> 52) & 0x7FF);
+    if (ev == 0x7FF) return {KPP_SAT, KPP_SAT};  // inf or NaN
+    if (v == 0.0) return {0, 0};
+    if (ev > be + 1) return {KPP_SAT, KPP_SAT};  // v >= 2^(be-1021): leaves the binade
+    if (ev < be - 55) return {0, 0};             // v < ulp / 4: rounds away, never a half
+    double s;                                     // v / ulp, ulp = 2^(be - 1075)
+    if (ev >= 1) {
+        s = __longlong_as_double((long long)((b & 0xFFFFFFFFFFFFFULL) |
+                                             ((unsigned long long)(ev - be + 1075) << 52)));
+    } else {
+        s = v * pow2d(1000) * pow2d(75 - be);  // subnormal v (then be <= 55): two exact scalings
+    }
+    return step_from_scaled(s);
+}
+
+// f then g
+__device__ __forceinline__ Step compose(Step f, Step g) {
+    const long long g0 = (f.a0 & 1) ? g.a1 : g.a0;      // even start: parity after f is f.a0's
+    const long long g1 = ((1 + f.a1) & 1) ? g.a1 : g.a0;  // odd start
+    long long h0 = f.a0 + g0, h1 = f.a1 + g1;
+    if (h0 > KPP_SAT) h0 = KPP_SAT;
+    if (h1 > KPP_SAT) h1 = KPP_SAT;
+    return {h0, h1};
+}
+
+__device__ __forceinline__ Step shfl_up_step(Step s, int off) {
+    return {(long long)__shfl_up_sync(0xffffffffu, (unsigned long long)s.a0, off),
+            (long long)__shfl_up_sync(0xffffffffu, (unsigned long long)s.a1, off)};
+}
+__device__ __forceinline__ Step shfl_down_step(Step s, int off) {
+    return {(long long)__shfl_down_sync(0xffffffffu, (unsigned long long)s.a0, off),
+            (long long)__shfl_down_sync(0xffffffffu, (unsigned long long)s.a1, off)};
+}
+
+// One group of up to 32 values (lane i holds value i of the group, len of
+// them valid) added to the running sum p in order, exactly as the sequential
+// fold. Warp-uniform result. With thr given, *hit receives the first value
+// index whose inclusive running sum reaches *thr (-1 if none).
+template <typename T, bool SEARCH>
+__device__ T walk_group(T p, T v, int len, T thr, int *hit) {
+    const int lane = threadIdx.x & 31;
+    constexpr long long TOP = 1LL << (Bits<T>::MB + 1);
+    int start = 0;
+    if (SEARCH) *hit = -1;
+    while (start < len) {
+        const bool live = lane >= start && lane < len;
+        const int be = normal_exp(p);
+        if (be == 0) {
+            if (p != p) return p;  // a NaN sum stays NaN and reaches no threshold
+            const T vs = __shfl_sync(0xffffffffu, v, start);
+            if (is_inf_or_nan(p)) {
+                // +inf stays +inf until a NaN value arrives, which makes it NaN
+                if (SEARCH) {
+                    const T p1 = kpp_add(p, vs);
+                    if (p1 >= thr) {
+                        *hit = start;
+                        return p1;
+                    }
+                }
+                const unsigned nanm = __ballot_sync(0xffffffffu, live && v != v);
+                if (nanm) p = __shfl_sync(0xffffffffu, v, __ffs(nanm) - 1);
+                return p;
+            }
+            // zero or subnormal sum: one exact addition
+            p = kpp_add(p, vs);
+            if (SEARCH && p >= thr) {
+                *hit = start;
+                return p;
+            }
+            start++;
+            continue;
+        }
+        const long long P = significand(p);
+        Step s = live ? step_of(v, be) : Step{0, 0};
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const Step o = shfl_up_step(s, off);
+            if (lane >= off) s = compose(o, s);
+        }
+        const long long Pl = P + ((P & 1) ? s.a1 : s.a0);
+        const unsigned badm = __ballot_sync(0xffffffffu, live && !(Pl < TOP));
+        const int f0 = badm ? __ffs(badm) - 1 : len;  // first value that leaves the binade
+        if (SEARCH) {
+            const T pl = from_parts<T>(be, Pl < TOP ? Pl : P);
+            const unsigned hm = __ballot_sync(0xffffffffu, live && lane < f0 && pl >= thr);
+            if (hm) {
+                *hit = __ffs(hm) - 1;
+                return __shfl_sync(0xffffffffu, pl, *hit);
+            }
+        }
+        if (f0 > start) {
+            const long long Pb = (long long)__shfl_sync(0xffffffffu, (unsigned long long)Pl, f0 - 1);
+            p = from_parts<T>(be, Pb);
+        }
+        if (f0 >= len) return p;
+        const T vf = __shfl_sync(0xffffffffu, v, f0);
+        p = kpp_add(p, vf);  // the one exact addition where the binade changes
+        if (SEARCH && p >= thr) {
+            *hit = f0;
+            return p;
+        }
+        start = f0 + 1;
+    }
+    return p;
+}
+
+struct Comp {
+    long long a[3][2];  // maps for binades e_lo, e_lo + 1, e_lo + 2
+    int e_lo;           // -1: no map (walk the chunk)
+    int pad;
+};
+
+struct KppState {
+    long long cursor;  // uniform draws consumed so far
+    int direct;        // the current centre was a uniform random row (no trials)
+    int cur;           // buffer holding the current D^2 array ...
+    int cur_trial;     // ... and its trial slice
+    int pending;       // trial results not yet resolved into a centre
+    int wbuf;          // buffer the pending trials were written to
+    int ntr;           // their count
+    int pcentre;       // their centre index (-1: the first D^2 array)
+    int pad;
+    long long cand[MAX_TRIALS];
+    double thr[MAX_TRIALS];
+    double pot[MAX_TRIALS];  // fold of each pending trial's array (F, widened)
+    double total;            // fold of the current D^2 array
+};
 
 __device__ __forceinline__ long long draw_to_range(double u, long long n) {
     long long i = (long long)floor(u * (double)n);
@@ -84,210 +278,335 @@ __device__ __forceinline__ long long draw_to_range(double u, long long n) {
 template <typename T>
 __global__ void kpp_first_kernel(const T *__restrict__ x, long long n, int d, const double *__restrict__ draws,
                                  long long n_draws, KppState *st, T *__restrict__ centers) {
-    // Single block: pick the first row, copy it.
     __shared__ long long first;
     if (threadIdx.x == 0) {
-        double u = n_draws > 0 ? draws[0] : 0.0;
+        const double u = n_draws > 0 ? draws[0] : 0.0;
         first = draw_to_range(u, n);
         st->cursor = 1;
+        st->direct = 0;
+        st->cand[0] = first;
+        st->pending = 1;  // the first D^2 array: no centre to resolve
+        st->wbuf = 0;
+        st->ntr = 1;
+        st->pcentre = -1;
     }
     __syncthreads();
     for (int j = threadIdx.x; j < d; j += blockDim.x) centers[j] = x[first * d + j];
 }
 
-template <typename T>
-__global__ void kpp_init_mind_kernel(const T *__restrict__ x, long long n, int d, const T *__restrict__ c0,
-                                     T *__restrict__ mind) {
-    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) mind[i] = sqeuc(x + i * d, c0, d);
-}
-
-template <typename T>
-__global__ void kpp_partial_kernel(const T *__restrict__ v, long long n, double *__restrict__ part) {
-    __shared__ double sh[32];
-    long long lo = (long long)blockIdx.x * KPP_BLOCK, hi = min(n, lo + KPP_BLOCK);
-    double s = 0.0;
-    for (long long i = lo + threadIdx.x; i < hi; i += blockDim.x) s += (double)v[i];
-    double r = block_sum(s, sh);
-    if (threadIdx.x == 0) part[blockIdx.x] = r;
-}
-
-// Single block: total, thresholds, draw consumption, block prefix sums.
-template <typename T>
-__global__ void kpp_select_kernel(const double *__restrict__ part, long long nb, double *__restrict__ bpre,
-                                  const double *__restrict__ draws, long long n_draws, int n_trials, long long n,
-                                  KppState *st) {
-    __shared__ double sh[33];
-    __shared__ double carry;
-    if (threadIdx.x == 0) carry = 0.0;
+// One CTA per chunk of KPP_CH rows: every trial's min(D^2, d(x, candidate))
+// (INIT: d(x, first row), the first D^2 array) and the chunk's f64 sums.
+template <typename T, bool INIT>
+__global__ void __launch_bounds__(KPP_THREADS)
+    kpp_trials_kernel(const T *__restrict__ x, long long n, int d, T *__restrict__ chains, int tstride,
+                      const KppState *__restrict__ st, int ntr, double *__restrict__ csum, long long nch) {
+    if (!INIT && st->direct) return;
+    __shared__ __align__(16) T xs[KPP_DJ][KPP_THREADS];
+    __shared__ T cs[MAX_TRIALS][KPP_DJ];
+    __shared__ double red[MAX_TRIALS][KPP_THREADS / 32];
+    __shared__ long long cand[MAX_TRIALS];
+    const int tid = threadIdx.x;
+    if (tid < ntr) cand[tid] = st->cand[tid];
+    const int cur = INIT ? 0 : st->cur, cur_trial = INIT ? 0 : st->cur_trial, wbuf = INIT ? 0 : 1 - cur;
+    const T *mind = chains + ((long long)cur * tstride + cur_trial) * n;
+    T *out = chains + (long long)wbuf * tstride * n;
     __syncthreads();
-    // Exclusive prefix of the partial sums (fixed order, chunk by chunk).
-    for (long long b0 = 0; b0 < nb; b0 += blockDim.x) {
-        long long i = b0 + threadIdx.x;
-        double v = i < nb ? part[i] : 0.0;
-        // inclusive warp scan
-        const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-        double inc = v;
+    double psum[MAX_TRIALS];
+#pragma unroll
+    for (int t = 0; t < MAX_TRIALS; t++) psum[t] = 0.0;
+    const long long base = (long long)blockIdx.x * KPP_CH;
+    for (int sub = 0; sub < KPP_CH / KPP_THREADS; sub++) {
+        const long long r0 = base + (long long)sub * KPP_THREADS;
+        if (r0 >= n) break;
+        const long long row = r0 + tid;
+        T acc[MAX_TRIALS];
+#pragma unroll
+        for (int t = 0; t < MAX_TRIALS; t++) acc[t] = T(0);
+        for (int j0 = 0; j0 < d; j0 += KPP_DJ) {
+            const int jn = min(KPP_DJ, d - j0);
+            __syncthreads();
+            for (int e = tid; e < KPP_THREADS * KPP_DJ; e += KPP_THREADS) {
+                const int r = e / KPP_DJ, jj = e - r * KPP_DJ;
+                const long long gr = r0 + r;
+                xs[jj][r] = (gr < n && jj < jn) ? x[gr * d + j0 + jj] : T(0);
+            }
+            for (int e = tid; e < ntr * KPP_DJ; e += KPP_THREADS) {
+                const int t = e / KPP_DJ, jj = e - t * KPP_DJ;
+                cs[t][jj] = jj < jn ? x[cand[t] * d + j0 + jj] : T(0);
+            }
+            __syncthreads();
+            for (int jj = 0; jj < jn; jj++) {
+                const T xv = xs[jj][tid];
+#pragma unroll
+                for (int t = 0; t < MAX_TRIALS; t++) {
+                    if (t < ntr) {
+                        const T df = kpp_sub(xv, cs[t][jj]);
+                        acc[t] = kpp_add(acc[t], kpp_mul(df, df));
+                    }
+                }
+            }
+        }
+        if (row < n) {
+            const T m = INIT ? T(0) : mind[row];
+#pragma unroll
+            for (int t = 0; t < MAX_TRIALS; t++) {
+                if (t < ntr) {
+                    const T v = acc[t];
+                    const T r = INIT ? v : (v < m ? v : m);  // kmeans.rs:230-232
+                    out[(long long)t * n + row] = r;
+                    psum[t] += (double)r;
+                }
+            }
+        }
+    }
+    const int lane = tid & 31, w = tid >> 5;
+#pragma unroll
+    for (int t = 0; t < MAX_TRIALS; t++) {
+        if (t < ntr) {
+            double v = psum[t];
+#pragma unroll
+            for (int off = 16; off >= 1; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+            if (lane == 0) red[t][w] = v;
+        }
+    }
+    __syncthreads();
+    if (tid < ntr) {
+        double v = 0.0;
+        for (int q = 0; q < KPP_THREADS / 32; q++) v += red[tid][q];
+        csum[(long long)tid * nch + blockIdx.x] = v;
+    }
+}
+
+// CTA (chunk j, trial t): the chunk's composed increment maps for the three
+// binades around its estimated starting sum.
+template <typename T>
+__global__ void __launch_bounds__(KPP_THREADS)
+    kpp_compose_kernel(const T *__restrict__ chains, long long n, int tstride, const KppState *__restrict__ st,
+                       bool init, const double *__restrict__ csum, long long nch, Comp *__restrict__ comps) {
+    if (!init && st->direct) return;
+    const int t = blockIdx.y;
+    const long long j = blockIdx.x;
+    const int wbuf = init ? 0 : 1 - st->cur;
+    const T *v = chains + ((long long)wbuf * tstride + t) * n;
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    __shared__ double sh[KPP_THREADS / 32];
+    __shared__ Step ws[KPP_THREADS / 32];
+    __shared__ int e_lo_s;
+    // estimated sum before the chunk: f64 sum of the earlier chunks' sums
+    double e = 0.0;
+    for (long long q = tid; q < j; q += KPP_THREADS) e += csum[(long long)t * nch + q];
+#pragma unroll
+    for (int off = 16; off >= 1; off >>= 1) e += __shfl_xor_sync(0xffffffffu, e, off);
+    if (lane == 0) sh[w] = e;
+    __syncthreads();
+    if (tid == 0) {
+        double s = 0.0;
+        for (int q = 0; q < KPP_THREADS / 32; q++) s += sh[q];
+        const T ef = (T)s;
+        int lo = -1;
+        const int be = normal_exp(ef);
+        if (be > 0) {
+            lo = be > 1 ? be - 1 : 1;
+            if (lo + 2 >= Bits<T>::EXPM) lo = -1;
+        }
+        e_lo_s = lo;
+    }
+    __syncthreads();
+    const int e_lo = e_lo_s;
+    Comp *out = comps + (long long)t * nch + j;
+    if (e_lo < 0) {
+        if (tid == 0) out->e_lo = -1;
+        return;
+    }
+    const long long i0 = j * KPP_CH + (long long)tid * (KPP_CH / KPP_THREADS);
+    T vals[KPP_CH / KPP_THREADS];
+#pragma unroll
+    for (int q = 0; q < KPP_CH / KPP_THREADS; q++) vals[q] = i0 + q < n ? v[i0 + q] : T(0);
+    for (int slot = 0; slot < 3; slot++) {
+        const int be = e_lo + slot;
+        Step s{0, 0};
+#pragma unroll
+        for (int q = 0; q < KPP_CH / KPP_THREADS; q++)
+            if (i0 + q < n) s = compose(s, step_of(vals[q], be));
+        // ordered warp reduction: lane i (earlier) absorbs lane i + off (later)
 #pragma unroll
         for (int off = 1; off < 32; off <<= 1) {
-            double t = __shfl_up_sync(0xffffffffu, inc, off);
-            if (lane >= off) inc += t;
+            const Step o = shfl_down_step(s, off);
+            if ((lane & (2 * off - 1)) == 0) s = compose(s, o);
         }
-        if (lane == 31) sh[w] = inc;
+        if (lane == 0) ws[w] = s;
         __syncthreads();
-        if (threadIdx.x == 0) {
-            double run = 0.0;
-            for (int q = 0; q < (int)(blockDim.x >> 5); q++) {
-                double t = sh[q];
-                sh[q] = run;
-                run += t;
-            }
-            sh[32] = run;
+        if (tid == 0) {
+            Step r = ws[0];
+            for (int q = 1; q < KPP_THREADS / 32; q++) r = compose(r, ws[q]);
+            out->a[slot][0] = r.a0;
+            out->a[slot][1] = r.a1;
         }
-        __syncthreads();
-        if (i < nb) bpre[i] = carry + sh[w] + inc - v;
-        __syncthreads();
-        if (threadIdx.x == 0) carry += sh[32];
         __syncthreads();
     }
-    if (threadIdx.x == 0) {
-        bpre[nb] = carry;
-        T total = (T)carry;
-        st->total = (double)total;
+    if (tid == 0) out->e_lo = e_lo;
+}
+
+// One warp per fold (blockIdx.x = trial): the running sum over every chunk,
+// recorded at each chunk's end, and the whole fold (the trial's potential).
+template <typename T>
+__global__ void __launch_bounds__(32)
+    kpp_walk_kernel(const T *__restrict__ chains, long long n, int tstride, KppState *__restrict__ st, bool init,
+                    const Comp *__restrict__ comps, long long nch, T *__restrict__ states) {
+    if (!init && st->direct) return;
+    const int t = blockIdx.x;
+    const int lane = threadIdx.x;
+    const int wbuf = init ? 0 : 1 - st->cur;
+    const T *v = chains + ((long long)wbuf * tstride + t) * n;
+    const Comp *cp = comps + (long long)t * nch;
+    T *sout = states + ((long long)wbuf * tstride + t) * nch;
+    __shared__ Comp cc[32];
+    constexpr long long TOP = 1LL << (Bits<T>::MB + 1);
+    T p = T(0);
+    int dummy;
+    for (long long jb = 0; jb < nch; jb += 32) {
+        __syncwarp();
+        if (jb + lane < nch) cc[lane] = cp[jb + lane];
+        __syncwarp();
+        const int nb = (int)min(32LL, nch - jb);
+        for (int jj = 0; jj < nb; jj++) {
+            const long long j = jb + jj;
+            const int e_lo = cc[jj].e_lo;
+            const int be = normal_exp(p);
+            bool done = false;
+            if (be > 0 && e_lo >= 0) {
+                const int slot = be - e_lo;
+                if (slot >= 0 && slot < 3) {
+                    const long long P = significand(p);
+                    const long long a = (P & 1) ? cc[jj].a[slot][1] : cc[jj].a[slot][0];
+                    const long long P2 = P + a;
+                    if (P2 < TOP) {
+                        p = from_parts<T>(be, P2);
+                        done = true;
+                    }
+                }
+            }
+            if (!done) {
+                const long long lo = j * KPP_CH, hi = min(n, lo + KPP_CH);
+                for (long long g = lo; g < hi; g += 32) {
+                    const int len = (int)min(32LL, hi - g);
+                    const T val = lane < len ? v[g + lane] : T(0);
+                    p = walk_group<T, false>(p, val, len, T(0), &dummy);
+                }
+            }
+            if (lane == 0) sout[j] = p;
+        }
+    }
+    if (lane == 0) st->pot[t] = (double)p;
+}
+
+// Single CTA, one warp per trial: resolve the pending trials into a centre,
+// then (centre c < k) the thresholds and candidates of centre c.
+template <typename T>
+__global__ void __launch_bounds__(MAX_TRIALS * 32)
+    kpp_select_kernel(const T *__restrict__ x, long long n, int d, const T *__restrict__ chains, int tstride,
+                      const T *__restrict__ states, long long nch, const double *__restrict__ draws,
+                      long long n_draws, int n_trials, int c, int k, KppState *__restrict__ st,
+                      T *__restrict__ centers) {
+    __shared__ long long copy_row;
+    __shared__ int copy_centre;
+    __shared__ int do_search;
+    __shared__ T thr_s[MAX_TRIALS];
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    if (tid == 0) {
+        copy_row = -1;
+        copy_centre = -1;
+        do_search = 0;
+        if (st->pending) {
+            int best = 0;
+            for (int t = 1; t < st->ntr; t++)
+                if (st->pot[t] < st->pot[best]) best = t;  // strictly smaller: the first trial wins ties
+            st->cur = st->wbuf;
+            st->cur_trial = best;
+            st->total = st->pot[best];
+            if (st->pcentre >= 0) {
+                copy_row = st->cand[best];
+                copy_centre = st->pcentre;
+            }
+            st->pending = 0;
+        }
+    }
+    __syncthreads();
+    if (copy_row >= 0)
+        for (int j = tid; j < d; j += blockDim.x) centers[(long long)copy_centre * d + j] = x[copy_row * d + j];
+    __syncthreads();
+    if (c >= k) return;
+    if (tid == 0) {
+        const T total = (T)st->total;
         long long cur = st->cursor;
         if (!(total > T(0))) {
-            double u = cur < n_draws ? draws[cur] : 0.0;
+            // kmeans.rs:202-206: a uniform random row, the D^2 array unchanged
+            const double u = cur < n_draws ? draws[cur] : 0.0;
+            copy_row = draw_to_range(u, n);
+            copy_centre = c;
             st->direct = 1;
-            st->cand[0] = draw_to_range(u, n);
             cur += 1;
         } else {
             st->direct = 0;
             for (int t = 0; t < n_trials; t++) {
-                double u = cur < n_draws ? draws[cur] : 0.0;
-                T thr = (T)u * total;
-                st->thr[t] = (double)thr;
+                const double u = cur < n_draws ? draws[cur] : 0.0;
+                thr_s[t] = kpp_mul((T)u, total);
+                st->thr[t] = (double)thr_s[t];
                 cur += 1;
             }
+            st->pending = 1;
+            st->wbuf = 1 - st->cur;
+            st->ntr = n_trials;
+            st->pcentre = c;
+            do_search = 1;
         }
         st->cursor = cur;
     }
-}
-
-// One block per trial: first row whose running sum reaches the threshold.
-template <typename T>
-__global__ void kpp_find_kernel(const T *__restrict__ mind, long long n, const double *__restrict__ bpre,
-                                long long nb, KppState *st) {
-    if (st->direct) return;
-    const int t = blockIdx.x;
-    __shared__ double sh[33];
-    __shared__ long long found;
-    __shared__ long long b_start;
-    const double thr = st->thr[t];
-    if (threadIdx.x == 0) {
-        // first block whose inclusive prefix reaches thr (binary search)
-        long long lo = 0, hi = nb - 1, ans = nb;
-        while (lo <= hi) {
-            long long mid = (lo + hi) >> 1;
-            if (bpre[mid + 1] >= thr) { ans = mid; hi = mid - 1; } else lo = mid + 1;
-        }
-        b_start = ans;
-        found = -1;
-    }
     __syncthreads();
-    for (long long b = b_start; b < nb; b++) {
-        double run = bpre[b];
-        long long lo = b * KPP_BLOCK, hi = min(n, lo + KPP_BLOCK);
-        for (long long c0 = lo; c0 < hi; c0 += blockDim.x) {
-            long long i = c0 + threadIdx.x;
-            double v = i < hi ? (double)mind[i] : 0.0;
-            const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-            double inc = v;
-#pragma unroll
-            for (int off = 1; off < 32; off <<= 1) {
-                double tt = __shfl_up_sync(0xffffffffu, inc, off);
-                if (lane >= off) inc += tt;
-            }
-            if (lane == 31) sh[w] = inc;
-            __syncthreads();
-            if (threadIdx.x == 0) {
-                double r2 = 0.0;
-                for (int q = 0; q < (int)(blockDim.x >> 5); q++) {
-                    double tt = sh[q];
-                    sh[q] = r2;
-                    r2 += tt;
-                }
-                sh[32] = r2;
-            }
-            __syncthreads();
-            double cum = run + sh[w] + inc;
-            bool hit = (i < hi) && (cum >= thr);
-            unsigned m = __ballot_sync(0xffffffffu, hit);
-            if (lane == 0 && m) atomicMin((unsigned long long *)&found, (unsigned long long)(c0 + w * 32 + __ffs(m) - 1));
-            __syncthreads();
-            if (found >= 0) break;
-            run += sh[32];
-            __syncthreads();
-        }
-        if (found >= 0) break;
+    if (!do_search) {
+        for (int j = tid; j < d; j += blockDim.x) centers[(long long)copy_centre * d + j] = x[copy_row * d + j];
+        return;
     }
-    if (threadIdx.x == 0) st->cand[t] = found >= 0 ? found : n - 1;
-}
-
-// New distances and per-block potential partials for every trial.
-template <typename T>
-__global__ void kpp_trial_kernel(const T *__restrict__ x, long long n, int d, const T *__restrict__ mind,
-                                 int n_trials, const KppState *st, T *__restrict__ nd, double *__restrict__ pot,
-                                 long long nb) {
-    if (st->direct) return;
-    __shared__ double sh[32];
-    long long lo = (long long)blockIdx.x * KPP_BLOCK, hi = min(n, lo + KPP_BLOCK);
-    for (int t = 0; t < n_trials; t++) {
-        const T *cand = x + st->cand[t] * d;
-        double s = 0.0;
-        for (long long i = lo + threadIdx.x; i < hi; i += blockDim.x) {
-            T v = sqeuc(x + i * d, cand, d);
-            T m = mind[i];
-            T r = v < m ? v : m;
-            nd[(long long)t * n + i] = r;
-            s += (double)r;
+    if (w >= n_trials) return;
+    // trial w: the first row whose running sum reaches thr (kmeans.rs:215-223)
+    const T thr = thr_s[w];
+    const long long off = ((long long)st->cur * tstride + st->cur_trial);
+    const T *S = states + off * nch;
+    const T *v = chains + off * n;
+    // First chunk whose end state is not below thr: a 32-ary search (the
+    // states never decrease, and a NaN state stays NaN, so "not below" holds
+    // from one chunk on); that chunk is then walked with the exact test.
+    long long lo = 0, hi = nch;  // the answer lies in [lo, hi]; nch = none
+    while (lo < hi) {
+        const long long step = (hi - lo + 31) / 32;
+        const long long pos = lo + (long long)lane * step;
+        const unsigned m = __ballot_sync(0xffffffffu, pos < hi && !(S[pos] < thr));
+        if (!m) {
+            lo = lo + ((hi - 1 - lo) / step) * step + 1;  // past the last probe
+        } else {
+            const int f = __ffs(m) - 1;
+            const long long pf = lo + (long long)f * step;
+            if (f > 0) lo = lo + (long long)(f - 1) * step + 1;
+            hi = pf;
         }
-        double r = block_sum(s, sh);
-        if (threadIdx.x == 0) pot[(long long)t * nb + blockIdx.x] = r;
     }
-}
-
-template <typename T>
-__global__ void kpp_choose_kernel(const T *__restrict__ x, int d, const double *__restrict__ pot, long long nb,
-                                  int n_trials, KppState *st, T *__restrict__ center_out) {
-    __shared__ double sh[32];
-    __shared__ int best;
-    if (!st->direct) {
-        T best_p = T(0);
-        int bt = -1;
-        for (int t = 0; t < n_trials; t++) {
-            double s = 0.0;
-            for (long long b = threadIdx.x; b < nb; b += blockDim.x) s += pot[(long long)t * nb + b];
-            double r = block_sum(s, sh);
-            if (threadIdx.x == 0) {
-                T p = (T)r;
-                if (bt < 0 || p < best_p) { bt = t; best_p = p; }
+    long long cand = n - 1;
+    if (lo < nch) {
+        const long long j = lo;
+        T p = j > 0 ? S[j - 1] : T(0);
+        const long long a = j * KPP_CH, b = min(n, a + KPP_CH);
+        for (long long g = a; g < b; g += 32) {
+            const int len = (int)min(32LL, b - g);
+            const T val = lane < len ? v[g + lane] : T(0);
+            int hit = -1;
+            p = walk_group<T, true>(p, val, len, thr, &hit);
+            if (hit >= 0) {
+                cand = g + hit;
+                break;
             }
         }
-        if (threadIdx.x == 0) { best = bt; st->best_trial = bt; }
-    } else if (threadIdx.x == 0) {
-        best = -1;
-        st->best_trial = -1;
     }
-    __syncthreads();
-    long long row = st->cand[best < 0 ? 0 : best];
-    for (int j = threadIdx.x; j < d; j += blockDim.x) center_out[j] = x[row * d + j];
-}
-
-template <typename T>
-__global__ void kpp_commit_kernel(T *__restrict__ mind, const T *__restrict__ nd, long long n, const KppState *st) {
-    if (st->direct) return;
-    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) mind[i] = nd[(long long)st->best_trial * n + i];
+    if (lane == 0) st->cand[w] = cand;
 }
 
 }  // namespace
@@ -308,33 +627,40 @@ void run_kmeanspp(Ctx &ctx, const T *x, int64_t n, int d, int k, const double *d
         fail(FK_ERR_UNSUPPORTED);
     }
     FK_CUDA(cudaMemsetAsync(centers_out, 0, sizeof(T) * (size_t)k * d, s));
-    const long long nb = (n + KPP_BLOCK - 1) / KPP_BLOCK;
+    const long long nch = (n + KPP_CH - 1) / KPP_CH;
+    const int ts = n_trials;  // trial slices per buffer
     auto *st = (KppState *)ctx.get(BUF_KPP0, sizeof(KppState));
-    T *mind = (T *)ctx.get(BUF_KPP1, sizeof(T) * (size_t)n);
-    T *nd = (T *)ctx.get(BUF_KPP2, sizeof(T) * (size_t)n * n_trials);
-    double *part = (double *)ctx.get(BUF_KPP3, sizeof(double) * (size_t)(nb * (n_trials + 1) + nb + 1));
-    double *pot = part + nb;
-    double *bpre = pot + nb * n_trials;
+    T *chains = (T *)ctx.get(BUF_KPP1, sizeof(T) * (size_t)n * ts * 2);
+    double *csum = (double *)ctx.get(BUF_KPP2, sizeof(double) * (size_t)nch * ts);
+    Comp *comps = (Comp *)ctx.get(BUF_KPP3, sizeof(Comp) * (size_t)nch * ts + sizeof(T) * (size_t)nch * ts * 2 + 64);
+    T *states = (T *)(comps + (size_t)nch * ts);
     FK_CUDA(cudaMemsetAsync(st, 0, sizeof(KppState), s));
 
     kpp_first_kernel<T><<<1, 128, 0, s>>>(x, n, d, draws_dev, n_draws, st, centers_out);
     FK_LAUNCH_CHECK();
-    if (k > 1) {
-        kpp_init_mind_kernel<T><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(x, n, d, centers_out, mind);
-        FK_LAUNCH_CHECK();
+    if (k == 1) {
+        if (draws_used) *draws_used = 1;
+        return;
     }
-    for (int c = 1; c < k; c++) {
-        kpp_partial_kernel<T><<<(unsigned)nb, KPP_THREADS, 0, s>>>(mind, n, part);
+    // the first D^2 array (distances to the first centre) and its fold
+    kpp_trials_kernel<T, true><<<(unsigned)nch, KPP_THREADS, 0, s>>>(x, n, d, chains, ts, st, 1, csum, nch);
+    FK_LAUNCH_CHECK();
+    kpp_compose_kernel<T><<<dim3((unsigned)nch, 1), KPP_THREADS, 0, s>>>(chains, n, ts, st, true, csum, nch, comps);
+    FK_LAUNCH_CHECK();
+    kpp_walk_kernel<T><<<1, 32, 0, s>>>(chains, n, ts, st, true, comps, nch, states);
+    FK_LAUNCH_CHECK();
+    for (int c = 1; c <= k; c++) {
+        kpp_select_kernel<T><<<1, MAX_TRIALS * 32, 0, s>>>(x, n, d, chains, ts, states, nch, draws_dev, n_draws,
+                                                            n_trials, c, k, st, centers_out);
         FK_LAUNCH_CHECK();
-        kpp_select_kernel<T><<<1, 1024, 0, s>>>(part, nb, bpre, draws_dev, n_draws, n_trials, n, st);
+        if (c == k) break;
+        kpp_trials_kernel<T, false><<<(unsigned)nch, KPP_THREADS, 0, s>>>(x, n, d, chains, ts, st, n_trials, csum,
+                                                                          nch);
         FK_LAUNCH_CHECK();
-        kpp_find_kernel<T><<<n_trials, 1024, 0, s>>>(mind, n, bpre, nb, st);
+        kpp_compose_kernel<T><<<dim3((unsigned)nch, (unsigned)n_trials), KPP_THREADS, 0, s>>>(chains, n, ts, st,
+                                                                                             false, csum, nch, comps);
         FK_LAUNCH_CHECK();
-        kpp_trial_kernel<T><<<(unsigned)nb, KPP_THREADS, 0, s>>>(x, n, d, mind, n_trials, st, nd, pot, nb);
-        FK_LAUNCH_CHECK();
-        kpp_choose_kernel<T><<<1, 1024, 0, s>>>(x, d, pot, nb, n_trials, st, centers_out + (int64_t)c * d);
-        FK_LAUNCH_CHECK();
-        kpp_commit_kernel<T><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(mind, nd, n, st);
+        kpp_walk_kernel<T><<<(unsigned)n_trials, 32, 0, s>>>(chains, n, ts, st, false, comps, nch, states);
         FK_LAUNCH_CHECK();
     }
     if (draws_used) {

@@ -33,7 +33,11 @@ constexpr size_t NOALLOC_BYTES = NOALLOC_OFF_PARTIALS + sizeof(double) * NOALLOC
 static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_BYTES];
 
 // Device address of g_noalloc_scratch, looked up once per device (the host
-// name of the array is only a stand-in, never a device address).
+// name of the array is only a stand-in, never a device address). The address
+// belongs to the device's primary context, the one the CUDA runtime uses: the
+// entry point must be called with that context current, and after
+// cudaDeviceReset (which destroys it) the cached address is stale, so a
+// process that resets a device must not call this entry point on it again.
 constexpr int NOALLOC_MAX_DEVICES = 64;
 void *g_scratch_addr[NOALLOC_MAX_DEVICES] = {};
 std::mutex g_scratch_mu;
@@ -60,13 +64,28 @@ void *scratch_for_current_device() {
     return g_scratch_addr[dev];
 }
 
-bool on_device(const void *p) {
+// Device memory of the current GPU (or managed memory). A buffer on another
+// GPU is refused here: without peer access the kernels would fault on it.
+bool on_device(const void *p, const char *name) {
     cudaPointerAttributes a;
     if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
         (void)cudaGetLastError();
+        set_error("`%s` is not device memory: every buffer passed to the allocation-free entry point must be",
+                  name);
         return false;
     }
-    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+    if (a.type == cudaMemoryTypeDevice) {
+        int cur = 0;
+        FK_CUDA(cudaGetDevice(&cur));
+        if (a.device != cur) {
+            set_error("`%s` is device memory of GPU %d, but the current GPU is %d", name, a.device, cur);
+            return false;
+        }
+        return true;
+    }
+    if (a.type == cudaMemoryTypeManaged) return true;
+    set_error("`%s` is not device memory: every buffer passed to the allocation-free entry point must be", name);
+    return false;
 }
 
 }  // namespace
@@ -99,10 +118,9 @@ extern "C" fk_status fk_kmeans_score_f64_noalloc(const double *x, int64_t n, int
             set_error("shape d=%lld k=%lld exceeds the supported range", (long long)d, (long long)k);
             return FK_ERR_UNSUPPORTED;
         }
-        if (!on_device(x) || !on_device(centers) || !on_device(labels_out) || !on_device(inertia_out)) {
-            set_error("every buffer passed to the allocation-free entry point must be device memory");
+        if (!on_device(x, "x") || !on_device(centers, "centers") || !on_device(labels_out, "labels_out") ||
+            !on_device(inertia_out, "inertia_out"))
             return FK_ERR_INVALID_PARAMETER;
-        }
         unsigned char *base = (unsigned char *)scratch_for_current_device();
         double *mind = (double *)(base + NOALLOC_OFF_MIND);
         int32_t *labels = (int32_t *)(base + NOALLOC_OFF_LABELS);

@@ -207,6 +207,10 @@ fk_status fk_kmeans_plus_plus_f32(fk_ctx *ctx, const float *x, int64_t n, int64_
  * are valid once that stream reaches this point; the call itself does not
  * wait. The first call on a device looks up the array's device address
  * (cudaGetSymbolAddress), so make that first call before any stream capture.
+ * That address belongs to the device's primary context (the CUDA runtime's):
+ * call with that context current, and not again after cudaDeviceReset.
+ * A buffer on another GPU than the current one is refused with
+ * FK_ERR_INVALID_PARAMETER naming the argument.
  * All calls share the one array: calls that overlap on the GPU (different
  * streams, or threads without ordering) race and must be serialised by the
  * caller. */

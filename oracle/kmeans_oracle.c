@@ -179,6 +179,7 @@ static void orc_kpp_##SUF(const T *x, int64_t n, int64_t d, int64_t k, orc_draws
     T *mind = (T *)malloc(sizeof(T) * (size_t)n);                                       \
     T *nd = (T *)malloc(sizeof(T) * (size_t)n);                                         \
     T *bestd = (T *)malloc(sizeof(T) * (size_t)n);                                      \
+    _Pragma("omp parallel for schedule(static)")                                        \
     for (int64_t i = 0; i < n; i++) mind[i] = orc_sqeuc_##SUF(x + i * d, centers, d);   \
     int64_t n_trials = 2 + (int64_t)floor(log((double)k));                              \
     if (n_trials < 1) n_trials = 1;                                                     \
@@ -198,12 +199,14 @@ static void orc_kpp_##SUF(const T *x, int64_t n, int64_t d, int64_t k, orc_draws
                 cum = cum + mind[i];                                                    \
                 if (cum >= thr) { cand = i; break; }                                    \
             }                                                                           \
-            T pot = (T)0;                                                               \
+            /* the distances in parallel, then the potential folded in row order */     \
+            _Pragma("omp parallel for schedule(static)")                                \
             for (int64_t i = 0; i < n; i++) {                                           \
                 T v = orc_sqeuc_##SUF(x + i * d, x + cand * d, d);                      \
                 nd[i] = v < mind[i] ? v : mind[i];                                      \
-                pot = pot + nd[i];                                                      \
             }                                                                           \
+            T pot = (T)0;                                                               \
+            for (int64_t i = 0; i < n; i++) pot = pot + nd[i];                          \
             if (!have || pot < best_pot) {                                              \
                 have = 1; best_pot = pot; best_cand = cand;                             \
                 T *tmp = bestd; bestd = nd; nd = tmp;                                   \
@@ -730,5 +733,54 @@ int orc_fit_runs_f32(const float *x, int64_t n, int64_t d, int64_t k, int64_t ma
         out_n_iter[run] = n_iter;
     }
     free(c); free(nc); free(counts); free(sums); free(flags); free(icounts); free(mind); free(lab);
+    return ORC_OK;
+}
+
+/* recompute_centroids_into (kmeans.rs:358-401) for KMeans<f64> on f32 rows
+ * widened exactly, from given labels, plus the inertia of those labels
+ * against the old centres folded in row order (assign_serial,
+ * kmeans.rs:312-323). The full-size parity checks of the mixed forms use it:
+ * the sums run in row order per (cluster, feature) and the threads split the
+ * features, so no rounding differs from the sequential loop. */
+int orc_update_given_labels_f32x64(const float *x, int64_t n, int64_t d, const int64_t *labels,
+                                   const double *old_c, int64_t k, double *new_c, double *inertia,
+                                   int nthreads) {
+    if (!x || !labels || !old_c || !new_c || !inertia) return ORC_ERR_NULL;
+    for (int64_t i = 0; i < n; i++)
+        if (labels[i] < 0 || labels[i] >= k) return ORC_ERR_INVALID_PARAMETER;
+    double *counts = (double *)calloc((size_t)k, sizeof(double));
+    double *mind = (double *)malloc(sizeof(double) * (size_t)(n > 0 ? n : 1));
+    if (!counts || !mind) { free(counts); free(mind); return ORC_ERR_OOM; }
+    memset(new_c, 0, sizeof(double) * (size_t)(k * d));
+    for (int64_t i = 0; i < n; i++) counts[labels[i]] = counts[labels[i]] + 1.0;
+    if (nthreads < 1) nthreads = 1;
+    _Pragma("omp parallel for schedule(static) num_threads(nthreads)")
+    for (int64_t j = 0; j < d; j++)
+        for (int64_t i = 0; i < n; i++) {
+            const int64_t l = labels[i];
+            new_c[l * d + j] = new_c[l * d + j] + (double)x[i * d + j];
+        }
+    for (int64_t q = 0; q < k; q++) {
+        if (counts[q] > 0.0) {
+            for (int64_t j = 0; j < d; j++) new_c[q * d + j] = new_c[q * d + j] / counts[q];
+        } else {
+            memcpy(new_c + q * d, old_c + q * d, sizeof(double) * (size_t)d);
+        }
+    }
+    _Pragma("omp parallel for schedule(static) num_threads(nthreads)")
+    for (int64_t i = 0; i < n; i++) {
+        const double *c = old_c + labels[i] * d;
+        double acc = 0.0;
+        for (int64_t j = 0; j < d; j++) {
+            const double t = (double)x[i * d + j] - c[j];
+            acc = acc + t * t;
+        }
+        mind[i] = acc;
+    }
+    double s = 0.0;
+    for (int64_t i = 0; i < n; i++) s = s + mind[i];
+    *inertia = s;
+    free(counts);
+    free(mind);
     return ORC_OK;
 }

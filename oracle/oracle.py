@@ -44,6 +44,7 @@ def lib():
         _lib.orc_draws_f64.restype = None
         _lib.orc_fit_runs_f32.argtypes = [p, i64, i64, i64, i64, C.c_float, i64, p, u64, C.c_int, p, p, p, p,
                                           C.c_int]
+        _lib.orc_update_given_labels_f32x64.argtypes = [p, i64, i64, p, p, i64, p, p, C.c_int]
     return _lib
 
 
@@ -104,6 +105,23 @@ def lloyd_step(x, centers, nthreads=None):
     if rc:
         raise OracleError(rc)
     return labels, nc, inertia.value, shift.value
+
+
+def update_given_labels(x32, labels, centers, nthreads=None):
+    """recompute_centroids_into (kmeans.rs:358-401) for KMeans<f64> on f32
+    rows widened exactly, from the given labels, and the inertia of those
+    labels against `centers` folded in row order -> (new_centers, inertia)."""
+    x32 = np.ascontiguousarray(x32, dtype=np.float32)
+    lab = np.ascontiguousarray(labels, dtype=np.int64)
+    c = np.ascontiguousarray(centers, dtype=np.float64)
+    n, d = x32.shape
+    nc = np.empty_like(c)
+    inertia = C.c_double()
+    rc = lib().orc_update_given_labels_f32x64(_ptr(x32), n, d, _ptr(lab), _ptr(c), c.shape[0], _ptr(nc),
+                                              C.byref(inertia), _threads(nthreads))
+    if rc:
+        raise OracleError(rc)
+    return nc, inertia.value
 
 
 def kmeanspp(x, k, draws_arr=None, seed=0):

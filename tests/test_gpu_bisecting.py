@@ -1,17 +1,14 @@
 """BisectingKMeans on the GPU against the oracle's restatement of
 bisecting_kmeans.rs, both drawing the library's uniform stream: the same
 picks per run and split, so centres, labels, the cluster count and the
-inertia (folded in the reference's order) must be identical.
-
-Not yet run on a GB300: the module is skipped until its first GPU run."""
+inertia (folded in the reference's order) must be identical."""
 import numpy as np
 import pytest
 
 import ferrolearn_gb300 as F
 from oracle import oracle as O
 
-pytestmark = [pytest.mark.gpu,
-              pytest.mark.skip(reason="BisectingKMeans kernels not yet run on a GB300")]
+pytestmark = pytest.mark.gpu
 
 
 def _blobs(n, d, k, seed, dtype):

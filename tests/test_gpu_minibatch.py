@@ -1,17 +1,14 @@
 """MiniBatchKMeans on the GPU against the oracle's restatement of
 mini_batch_kmeans.rs, both drawing the library's uniform stream: per run the
 same initial centres and batches, so labels, centres and n_iter must be
-identical and the inertia equal to the last bits of its summation order.
-
-Not yet run on a GB300: the module is skipped until its first GPU run."""
+identical and the inertia equal to the last bits of its summation order."""
 import numpy as np
 import pytest
 
 import ferrolearn_gb300 as F
 from oracle import oracle as O
 
-pytestmark = [pytest.mark.gpu,
-              pytest.mark.skip(reason="MiniBatchKMeans kernels not yet run on a GB300")]
+pytestmark = pytest.mark.gpu
 
 INERTIA_RTOL = {"f64": 1e-12, "f32": 1e-5}
 

@@ -78,16 +78,56 @@ def test_fit_n_init_best_run_and_kmeanspp():
     assert g.n_iter() == o["n_iter"]
 
 
+def _kpp_draws(seed, k):
+    return F.draws(seed, 1 + (k - 1) * (2 + int(np.floor(np.log(k)))))
+
+
 @pytest.mark.parametrize("dtype", ["f64", "f32"])
 def test_kmeanspp_matches_oracle(dtype):
     npdt = np.float64 if dtype == "f64" else np.float32
-    for seed, (n, d, k) in enumerate([(50, 2, 3), (2000, 8, 16), (9000, 16, 40)]):
+    for seed, (n, d, k) in enumerate([(50, 2, 3), (2000, 8, 16), (9000, 16, 40), (70001, 5, 30)]):
         x = _blobs(n, d, k, seed=seed, dtype=npdt)
-        dr = F.draws(seed + 100, 1 + (k - 1) * (2 + int(np.floor(np.log(k)))))
+        dr = _kpp_draws(seed + 100, k)
         gc, gu = F.kmeans_plus_plus(x, k, dr, dtype=dtype)
         oc, ou = O.kmeanspp(x, k, dr)
         assert gu == ou
         assert np.array_equal(gc, oc)
+
+
+@pytest.mark.parametrize("dtype", ["f64", "f32"])
+def test_kmeanspp_edge_cases_match_oracle(dtype):
+    npdt = np.float64 if dtype == "f64" else np.float32
+    rng = np.random.default_rng(7)
+    cases = [
+        np.ones((40, 3)),                                         # total 0 after the first centre: random rows
+        np.repeat(rng.normal(size=(3, 4)), [500, 1, 2000], 0),    # fewer distinct rows than centres
+        rng.integers(-3, 4, size=(30000, 2)).astype(np.float64),  # integer grid: many exact halves and ties
+        np.array([[1.5, -2.0]]),                                  # one row
+        np.concatenate([rng.normal(size=(5000, 3)) * 1e-20, rng.normal(size=(5000, 3)) * 1e15]),
+    ]
+    for i, x in enumerate(cases):
+        x = np.ascontiguousarray(x, dtype=npdt)
+        for k in sorted({1, 2, min(len(x), 9)}):
+            dr = _kpp_draws(300 + 10 * i + k, k)
+            gc, gu = F.kmeans_plus_plus(x, k, dr, dtype=dtype)
+            oc, ou = O.kmeanspp(x, k, dr)
+            assert gu == ou, (i, k)
+            assert np.array_equal(gc, oc), (i, k)
+
+
+@pytest.mark.parametrize("dtype", ["f32", "f64"])
+def test_kmeanspp_at_full_dirichlet_size_matches_oracle(dtype):
+    # n = 1,000,000 rows, d = 64, k = 256: every sum of kmeans.rs:201, 215-223
+    # and 225-237 is a million-term left fold in F, so a fold in any other
+    # order would pick other candidates here
+    npdt = np.float64 if dtype == "f64" else np.float32
+    w = W.dirichlet_256x64(scale=1.0, seed=3, dtype=npdt)
+    x, k = w["x"], w["k"]
+    dr = _kpp_draws(5, k)
+    gc, gu = F.kmeans_plus_plus(x, k, dr, dtype=dtype)
+    oc, ou = O.kmeanspp(x, k, dr)
+    assert gu == ou
+    assert np.array_equal(gc, oc)
 
 
 def test_reference_unit_cases_on_gpu():
@@ -168,7 +208,6 @@ def test_dirichlet_scale_sampled_rows():
     assert np.abs(gc - oc).max() <= 1e-12 * np.abs(oc).max()
 
 
-@pytest.mark.skip(reason="not yet run on a GB300")
 @pytest.mark.parametrize("dtype", ["f64", "f32"])
 def test_fit_with_injected_draws_matches_oracle(dtype):
     # one caller-supplied uniform stream shared by the n_init runs' k-means++

@@ -221,3 +221,18 @@ def test_fit_runs_agrees_with_fit_per_run():
         assert np.array_equal(runs["labels"][r], one["labels"])
         assert np.array_equal(runs["centers"][r], one["centers"])
         assert runs["n_iter"][r] == one["n_iter"]
+
+
+def test_update_given_labels_is_the_reference_update():
+    # the full-size parity checks' update: recompute_centroids_into on f32
+    # rows widened to f64, threads split by feature -- the same centres as the
+    # oracle's own Lloyd step, bit for bit, and its inertia folded in row order
+    rng = np.random.default_rng(11)
+    x = (rng.normal(size=(40000, 9)) * 3).astype(np.float32)
+    c = x[rng.choice(40000, 12, replace=False)].astype(np.float64)
+    c[3] = 1e6  # an empty cluster keeps its centre
+    lab, nc, _, _ = O.lloyd_step(x.astype(np.float64), c)
+    nc2, inertia = O.update_given_labels(x, lab, c)
+    assert np.array_equal(nc, nc2)
+    d = ((x.astype(np.float64) - c[lab]) ** 2).sum(1)
+    assert abs(inertia - d.sum()) <= 1e-12 * d.sum()

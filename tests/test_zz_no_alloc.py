@@ -63,3 +63,4 @@ def test_score_noalloc_rejects_sizes_beyond_its_scratch():
     host = np.zeros(16)
     st = lib.fk_kmeans_score_f64_noalloc(host.ctypes.data_as(C.c_void_p), 4, 1, _p(buf), 1, _p(buf), _p(buf), None)
     assert st == 1
+    assert "`x`" in _native.last_error()
