@@ -57,9 +57,10 @@ template <> __device__ __forceinline__ float kpp_add(float a, float b) { return 
 template <> __device__ __forceinline__ double kpp_add(double a, double b) { return __dadd_rn(a, b); }
 
 constexpr int KPP_CH = 1024;      // values per fold chunk (and rows per trial-pass CTA)
+constexpr int KPP_GROUPS = KPP_CH / 32;  // 32-value groups per chunk
 constexpr int KPP_THREADS = 256;
 constexpr int MAX_TRIALS = 16;
-constexpr int KPP_DJ = 16;        // features staged per step of the trial pass
+constexpr int KPP_PAD = 4;        // row padding of the staged X tile (16 bytes of f32)
 constexpr long long KPP_SAT = 1LL << 61;  // saturated increment: never applies
 
 // ---------------------------------------------------- binade arithmetic --
@@ -110,49 +111,43 @@ __device__ __forceinline__ T from_parts(int be, long long P) {
     return B::from(((typename B::U)be << B::MB) | ((typename B::U)P & m));
 }
 
-__device__ __forceinline__ double pow2d(int s) {  // 2^s for s in [-1022, 1023]
-    return __longlong_as_double((long long)(1023 + s) << 52);
-}
-
 // Increment map of one value v >= 0 on the grid of binade be: a0 / a1 for a
-// running sum whose significand is even / odd.
+// running sum whose significand is even / odd. Integer arithmetic on the
+// value's significand m and exponent: v / ulp = m * 2^(e - be), so the
+// rounded increment is m shifted right by be - e, rounded to nearest, with
+// an exact half left to the sum's parity (ties to even).
 struct Step {
     long long a0, a1;
 };
 
-__device__ __forceinline__ Step step_from_scaled(double s) {
-    // s = v / ulp (exact); from 2^60 on (beyond any binade's 2^53 steps) saturate
-    if (!(s < 1152921504606846976.0)) return {KPP_SAT, KPP_SAT};
-    const double fl = floor(s);
-    const double fr = s - fl;  // exact
-    const long long q = (long long)fl;
-    if (fr > 0.5) return {q + 1, q + 1};
-    if (fr < 0.5) return {q, q};
-    return {q + (q & 1), q + ((q + 1) & 1)};  // exact half: the even neighbour
-}
-
-__device__ __forceinline__ Step step_of(float v, int be) {
-    const double vv = (double)v;
-    if (!(vv <= 3.5e38)) return {KPP_SAT, KPP_SAT};  // inf or NaN (v is never negative)
-    if (vv == 0.0) return {0, 0};
-    return step_from_scaled(vv * pow2d(150 - be));  // ulp = 2^(be - 150), exact in f64
-}
-
-__device__ __forceinline__ Step step_of(double v, int be) {
-    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
-    const int ev = (int)((b >> 52) & 0x7FF);
-    if (ev == 0x7FF) return {KPP_SAT, KPP_SAT};  // inf or NaN
-    if (v == 0.0) return {0, 0};
-    if (ev > be + 1) return {KPP_SAT, KPP_SAT};  // v >= 2^(be-1021): leaves the binade
-    if (ev < be - 55) return {0, 0};             // v < ulp / 4: rounds away, never a half
-    double s;                                     // v / ulp, ulp = 2^(be - 1075)
-    if (ev >= 1) {
-        s = __longlong_as_double((long long)((b & 0xFFFFFFFFFFFFFULL) |
-                                             ((unsigned long long)(ev - be + 1075) << 52)));
+template <typename T>
+__device__ __forceinline__ Step step_of(T v, int be) {
+    using B = Bits<T>;
+    using U = typename B::U;
+    const U b = B::bits(v);
+    const int ev = (int)((b >> B::MB) & (U)B::EXPM);
+    if (ev == B::EXPM) return {KPP_SAT, KPP_SAT};  // inf or NaN
+    const U mask = ((U)1 << B::MB) - 1;
+    if (b >> (sizeof(U) * 8 - 1))                   // negative: only -0 is harmless
+        return (b << 1) == 0 ? Step{0, 0} : Step{KPP_SAT, KPP_SAT};
+    U m = b & mask;
+    int e = ev;
+    if (ev == 0) {
+        if (m == 0) return {0, 0};
+        e = 1;  // subnormal: no hidden bit, the exponent of the smallest normals
     } else {
-        s = v * pow2d(1000) * pow2d(75 - be);  // subnormal v (then be <= 55): two exact scalings
+        m |= (U)1 << B::MB;
     }
-    return step_from_scaled(s);
+    const int sh = e - be;
+    if (sh > 0) return {KPP_SAT, KPP_SAT};  // v >= 2^(be+1): the sum leaves the binade
+    const int r = -sh;
+    if (r == 0) return {(long long)m, (long long)m};
+    if (r > B::MB + 2) return {0, 0};  // v < ulp / 2 by far: rounds away, never a half
+    const long long q = (long long)(m >> r);
+    const U rem = m & (((U)1 << r) - 1), half = (U)1 << (r - 1);
+    if (rem > half) return {q + 1, q + 1};
+    if (rem < half) return {q, q};
+    return {q + (q & 1), q + ((q + 1) & 1)};  // exact half: the even neighbour
 }
 
 // f then g
@@ -246,10 +241,21 @@ __device__ T walk_group(T p, T v, int len, T thr, int *hit) {
     return p;
 }
 
-struct Comp {
-    long long a[3][2];  // maps for binades e_lo, e_lo + 1, e_lo + 2
-    int e_lo;           // -1: no map (walk the chunk)
-    int pad;
+// Maps of one chunk or group for the three binades of its window.
+struct Map3 {
+    Step s[3];
+};
+
+__device__ __forceinline__ Step pick(const Map3 &m, int slot) {
+    return slot == 0 ? m.s[0] : (slot == 1 ? m.s[1] : m.s[2]);
+}
+
+// Where the fold data of one buffer / trial slice live (kpp_layout on the host).
+struct FoldSlices {
+    int *elo;       // [2][ts][nch] lowest binade of each chunk's window (-1: none)
+    Map3 *cmap;     // [2][ts][nch] chunk maps
+    Map3 *gmap;     // [2][ts][nch][32] group maps
+    void *states;   // [2][ts][nch] running sum at each chunk's end (T)
 };
 
 struct KppState {
@@ -267,6 +273,71 @@ struct KppState {
     double pot[MAX_TRIALS];  // fold of each pending trial's array (F, widened)
     double total;            // fold of the current D^2 array
 };
+
+// The values of one chunk (clen of them) added to p in order, exactly as the
+// sequential fold: the groups' maps scanned 32 at a time, and a group whose
+// map does not apply walked value by value. With SEARCH, *hit receives the
+// index (within the chunk) of the first value whose inclusive running sum
+// reaches thr, or -1.
+template <typename T, bool SEARCH>
+__device__ T walk_chunk(T p, const T *__restrict__ cv, int clen, const Map3 *__restrict__ gm, int e_lo, T thr,
+                        int *hit) {
+    const int lane = threadIdx.x & 31;
+    constexpr long long TOP = 1LL << (Bits<T>::MB + 1);
+    const int ng = (clen + 31) / 32;
+    Map3 g{};
+    if (e_lo >= 0 && lane < ng) g = gm[lane];
+    if (SEARCH) *hit = -1;
+    int start = 0;
+    while (start < ng) {
+        const int be = normal_exp(p);
+        const int slot = be - e_lo;
+        if (!(be > 0 && e_lo >= 0 && slot >= 0 && slot < 3)) {
+            // no map for this sum: the first remaining group value by value
+            const int len = min(32, clen - start * 32);
+            const T val = lane < len ? cv[start * 32 + lane] : T(0);
+            int h = -1;
+            p = walk_group<T, SEARCH>(p, val, len, thr, &h);
+            if (SEARCH && h >= 0) {
+                *hit = start * 32 + h;
+                return p;
+            }
+            start++;
+            continue;
+        }
+        const bool live = lane >= start && lane < ng;
+        Step s = live ? pick(g, slot) : Step{0, 0};
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const Step o = shfl_up_step(s, off);
+            if (lane >= off) s = compose(o, s);
+        }
+        const long long P = significand(p);
+        const long long Pl = P + ((P & 1) ? s.a1 : s.a0);
+        const unsigned badm = __ballot_sync(0xffffffffu, live && !(Pl < TOP));
+        const int f0 = badm ? __ffs(badm) - 1 : ng;  // first group whose map does not apply
+        int gsel = f0;                                 // the group to walk value by value
+        if (SEARCH) {
+            const unsigned hm = __ballot_sync(0xffffffffu, live && lane < f0 && from_parts<T>(be, Pl) >= thr);
+            if (hm) gsel = __ffs(hm) - 1;              // the threshold is reached inside this group
+        }
+        if (gsel > start) {
+            const long long Pb = (long long)__shfl_sync(0xffffffffu, (unsigned long long)Pl, gsel - 1);
+            p = from_parts<T>(be, Pb);
+        }
+        if (gsel >= ng) return p;
+        const int len = min(32, clen - gsel * 32);
+        const T val = lane < len ? cv[gsel * 32 + lane] : T(0);
+        int h = -1;
+        p = walk_group<T, SEARCH>(p, val, len, thr, &h);
+        if (SEARCH && h >= 0) {
+            *hit = gsel * 32 + h;
+            return p;
+        }
+        start = gsel + 1;
+    }
+    return p;
+}
 
 __device__ __forceinline__ long long draw_to_range(double u, long long n) {
     long long i = (long long)floor(u * (double)n);
@@ -294,80 +365,97 @@ __global__ void kpp_first_kernel(const T *__restrict__ x, long long n, int d, co
     for (int j = threadIdx.x; j < d; j += blockDim.x) centers[j] = x[first * d + j];
 }
 
-// One CTA per chunk of KPP_CH rows: every trial's min(D^2, d(x, candidate))
-// (INIT: d(x, first row), the first D^2 array) and the chunk's f64 sums.
-template <typename T, bool INIT>
+template <typename T> struct TrialTile;
+template <> struct TrialTile<float> { static constexpr int DJ = 8; };
+template <> struct TrialTile<double> { static constexpr int DJ = 4; };
+
+template <typename T, int TT>
+constexpr size_t trial_smem() {
+    return sizeof(T) * ((size_t)TrialTile<T>::DJ * (KPP_CH + KPP_PAD) + (size_t)TrialTile<T>::DJ * TT);
+}
+
+// One CTA per chunk of KPP_CH rows, 4 rows per thread, all TT trial slots per
+// thread (ntr <= TT of them live): every trial's min(D^2, d(x, candidate))
+// (INIT: d(x, first row), the first D^2 array; kmeans.rs:188-195, 225-233)
+// with the direct form folded over the features in order, and the chunk's
+// sums (only an estimate for the fold's binade windows).
+template <typename T, int TT, bool INIT>
 __global__ void __launch_bounds__(KPP_THREADS)
     kpp_trials_kernel(const T *__restrict__ x, long long n, int d, T *__restrict__ chains, int tstride,
                       const KppState *__restrict__ st, int ntr, double *__restrict__ csum, long long nch) {
     if (!INIT && st->direct) return;
-    __shared__ __align__(16) T xs[KPP_DJ][KPP_THREADS];
-    __shared__ T cs[MAX_TRIALS][KPP_DJ];
-    __shared__ double red[MAX_TRIALS][KPP_THREADS / 32];
-    __shared__ long long cand[MAX_TRIALS];
+    constexpr int DJ = TrialTile<T>::DJ;
+    constexpr int XS = KPP_CH + KPP_PAD;  // row length of the staged tile
+    extern __shared__ __align__(16) unsigned char kpp_smem[];
+    T *xs = reinterpret_cast<T *>(kpp_smem);  // [DJ][XS]: feature-major, rows contiguous
+    T *cs = xs + DJ * XS;                     // [DJ][TT]
+    __shared__ long long cand[TT];
+    __shared__ double red[TT][KPP_THREADS / 32];
     const int tid = threadIdx.x;
-    if (tid < ntr) cand[tid] = st->cand[tid];
+    if (tid < TT) cand[tid] = tid < ntr ? st->cand[tid] : 0;
     const int cur = INIT ? 0 : st->cur, cur_trial = INIT ? 0 : st->cur_trial, wbuf = INIT ? 0 : 1 - cur;
     const T *mind = chains + ((long long)cur * tstride + cur_trial) * n;
     T *out = chains + (long long)wbuf * tstride * n;
-    __syncthreads();
-    double psum[MAX_TRIALS];
-#pragma unroll
-    for (int t = 0; t < MAX_TRIALS; t++) psum[t] = 0.0;
     const long long base = (long long)blockIdx.x * KPP_CH;
-    for (int sub = 0; sub < KPP_CH / KPP_THREADS; sub++) {
-        const long long r0 = base + (long long)sub * KPP_THREADS;
-        if (r0 >= n) break;
-        const long long row = r0 + tid;
-        T acc[MAX_TRIALS];
+    T acc[4][TT];
 #pragma unroll
-        for (int t = 0; t < MAX_TRIALS; t++) acc[t] = T(0);
-        for (int j0 = 0; j0 < d; j0 += KPP_DJ) {
-            const int jn = min(KPP_DJ, d - j0);
-            __syncthreads();
-            for (int e = tid; e < KPP_THREADS * KPP_DJ; e += KPP_THREADS) {
-                const int r = e / KPP_DJ, jj = e - r * KPP_DJ;
-                const long long gr = r0 + r;
-                xs[jj][r] = (gr < n && jj < jn) ? x[gr * d + j0 + jj] : T(0);
-            }
-            for (int e = tid; e < ntr * KPP_DJ; e += KPP_THREADS) {
-                const int t = e / KPP_DJ, jj = e - t * KPP_DJ;
-                cs[t][jj] = jj < jn ? x[cand[t] * d + j0 + jj] : T(0);
-            }
-            __syncthreads();
-            for (int jj = 0; jj < jn; jj++) {
-                const T xv = xs[jj][tid];
+    for (int a = 0; a < 4; a++)
 #pragma unroll
-                for (int t = 0; t < MAX_TRIALS; t++) {
-                    if (t < ntr) {
-                        const T df = kpp_sub(xv, cs[t][jj]);
-                        acc[t] = kpp_add(acc[t], kpp_mul(df, df));
-                    }
-                }
-            }
+        for (int b = 0; b < TT; b++) acc[a][b] = T(0);
+    for (int j0 = 0; j0 < d; j0 += DJ) {
+        const int jn = min(DJ, d - j0);
+        __syncthreads();
+        for (int e = tid; e < KPP_CH * DJ; e += KPP_THREADS) {
+            const int r = e / DJ, jj = e - r * DJ;
+            const long long gr = base + r;
+            xs[jj * XS + r] = (gr < n && jj < jn) ? x[gr * d + j0 + jj] : T(0);
         }
+        for (int e = tid; e < TT * DJ; e += KPP_THREADS) {
+            const int t = e / DJ, jj = e - t * DJ;
+            cs[jj * TT + t] = (t < ntr && jj < jn) ? x[cand[t] * d + j0 + jj] : T(0);
+        }
+        __syncthreads();
+        for (int jj = 0; jj < jn; jj++) {
+            T xv[4], cvv[TT];
+#pragma unroll
+            for (int a = 0; a < 4; a++) xv[a] = xs[jj * XS + tid * 4 + a];
+#pragma unroll
+            for (int b = 0; b < TT; b++) cvv[b] = cs[jj * TT + b];
+#pragma unroll
+            for (int a = 0; a < 4; a++)
+#pragma unroll
+                for (int b = 0; b < TT; b++) {
+                    const T df = kpp_sub(xv[a], cvv[b]);
+                    acc[a][b] = kpp_add(acc[a][b], kpp_mul(df, df));
+                }
+        }
+    }
+    double psum[TT];
+#pragma unroll
+    for (int b = 0; b < TT; b++) psum[b] = 0.0;
+#pragma unroll
+    for (int a = 0; a < 4; a++) {
+        const long long row = base + tid * 4 + a;
         if (row < n) {
             const T m = INIT ? T(0) : mind[row];
 #pragma unroll
-            for (int t = 0; t < MAX_TRIALS; t++) {
-                if (t < ntr) {
-                    const T v = acc[t];
+            for (int b = 0; b < TT; b++) {
+                if (b < ntr) {
+                    const T v = acc[a][b];
                     const T r = INIT ? v : (v < m ? v : m);  // kmeans.rs:230-232
-                    out[(long long)t * n + row] = r;
-                    psum[t] += (double)r;
+                    out[(long long)b * n + row] = r;
+                    psum[b] += (double)r;
                 }
             }
         }
     }
     const int lane = tid & 31, w = tid >> 5;
 #pragma unroll
-    for (int t = 0; t < MAX_TRIALS; t++) {
-        if (t < ntr) {
-            double v = psum[t];
+    for (int b = 0; b < TT; b++) {
+        double v = psum[b];
 #pragma unroll
-            for (int off = 16; off >= 1; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
-            if (lane == 0) red[t][w] = v;
-        }
+        for (int off = 16; off >= 1; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+        if (lane == 0) red[b][w] = v;
     }
     __syncthreads();
     if (tid < ntr) {
@@ -377,125 +465,138 @@ __global__ void __launch_bounds__(KPP_THREADS)
     }
 }
 
-// CTA (chunk j, trial t): the chunk's composed increment maps for the three
-// binades around its estimated starting sum.
+// One warp per (chunk, trial): the maps of the chunk's 32 groups (lane g
+// folds group g) and of the whole chunk (ordered warp reduction), each for
+// the three binades around the chunk's estimated starting sum (an f64 sum of
+// the earlier chunks' sums: only which maps get built depends on it).
 template <typename T>
 __global__ void __launch_bounds__(KPP_THREADS)
     kpp_compose_kernel(const T *__restrict__ chains, long long n, int tstride, const KppState *__restrict__ st,
-                       bool init, const double *__restrict__ csum, long long nch, Comp *__restrict__ comps) {
+                       bool init, const double *__restrict__ csum, long long nch, FoldSlices fs) {
     if (!init && st->direct) return;
+    const int lane = threadIdx.x & 31;
     const int t = blockIdx.y;
-    const long long j = blockIdx.x;
+    const long long j = (long long)blockIdx.x * (KPP_THREADS / 32) + (threadIdx.x >> 5);
+    if (j >= nch) return;  // whole warps; no block-wide barrier below
     const int wbuf = init ? 0 : 1 - st->cur;
-    const T *v = chains + ((long long)wbuf * tstride + t) * n;
-    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
-    __shared__ double sh[KPP_THREADS / 32];
-    __shared__ Step ws[KPP_THREADS / 32];
-    __shared__ int e_lo_s;
-    // estimated sum before the chunk: f64 sum of the earlier chunks' sums
+    const T *v = chains + ((long long)wbuf * tstride + t) * n + j * KPP_CH;
+    const long long off = ((long long)wbuf * tstride + t) * nch + j;
     double e = 0.0;
-    for (long long q = tid; q < j; q += KPP_THREADS) e += csum[(long long)t * nch + q];
+    for (long long q = lane; q < j; q += 32) e += csum[(long long)t * nch + q];
 #pragma unroll
-    for (int off = 16; off >= 1; off >>= 1) e += __shfl_xor_sync(0xffffffffu, e, off);
-    if (lane == 0) sh[w] = e;
-    __syncthreads();
-    if (tid == 0) {
-        double s = 0.0;
-        for (int q = 0; q < KPP_THREADS / 32; q++) s += sh[q];
-        const T ef = (T)s;
-        int lo = -1;
-        const int be = normal_exp(ef);
-        if (be > 0) {
-            lo = be > 1 ? be - 1 : 1;
-            if (lo + 2 >= Bits<T>::EXPM) lo = -1;
-        }
-        e_lo_s = lo;
+    for (int o = 16; o >= 1; o >>= 1) e += __shfl_xor_sync(0xffffffffu, e, o);
+    const int be = normal_exp((T)e);
+    int lo = -1;
+    if (be > 0) {
+        lo = be > 1 ? be - 1 : 1;
+        if (lo + 2 >= Bits<T>::EXPM) lo = -1;
     }
-    __syncthreads();
-    const int e_lo = e_lo_s;
-    Comp *out = comps + (long long)t * nch + j;
-    if (e_lo < 0) {
-        if (tid == 0) out->e_lo = -1;
-        return;
-    }
-    const long long i0 = j * KPP_CH + (long long)tid * (KPP_CH / KPP_THREADS);
-    T vals[KPP_CH / KPP_THREADS];
-#pragma unroll
-    for (int q = 0; q < KPP_CH / KPP_THREADS; q++) vals[q] = i0 + q < n ? v[i0 + q] : T(0);
-    for (int slot = 0; slot < 3; slot++) {
-        const int be = e_lo + slot;
-        Step s{0, 0};
-#pragma unroll
-        for (int q = 0; q < KPP_CH / KPP_THREADS; q++)
-            if (i0 + q < n) s = compose(s, step_of(vals[q], be));
-        // ordered warp reduction: lane i (earlier) absorbs lane i + off (later)
-#pragma unroll
-        for (int off = 1; off < 32; off <<= 1) {
-            const Step o = shfl_down_step(s, off);
-            if ((lane & (2 * off - 1)) == 0) s = compose(s, o);
+    if (lane == 0) fs.elo[off] = lo;
+    if (lo < 0) return;
+    const int clen = (int)min((long long)KPP_CH, n - j * KPP_CH);
+    Step s0{0, 0}, s1{0, 0}, s2{0, 0};
+    const int g0 = lane * 32;
+    for (int q = 0; q < 32; q++) {
+        const int i = g0 + q;
+        if (i < clen) {
+            const T val = v[i];
+            s0 = compose(s0, step_of(val, lo));
+            s1 = compose(s1, step_of(val, lo + 1));
+            s2 = compose(s2, step_of(val, lo + 2));
         }
-        if (lane == 0) ws[w] = s;
-        __syncthreads();
-        if (tid == 0) {
-            Step r = ws[0];
-            for (int q = 1; q < KPP_THREADS / 32; q++) r = compose(r, ws[q]);
-            out->a[slot][0] = r.a0;
-            out->a[slot][1] = r.a1;
-        }
-        __syncthreads();
     }
-    if (tid == 0) out->e_lo = e_lo;
+    Map3 gm;
+    gm.s[0] = s0;
+    gm.s[1] = s1;
+    gm.s[2] = s2;
+    fs.gmap[off * KPP_GROUPS + lane] = gm;
+    // ordered reduction: lane i (earlier groups) absorbs lane i + o (later)
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const Step r0 = shfl_down_step(s0, o), r1 = shfl_down_step(s1, o), r2 = shfl_down_step(s2, o);
+        if ((lane & (2 * o - 1)) == 0) {
+            s0 = compose(s0, r0);
+            s1 = compose(s1, r1);
+            s2 = compose(s2, r2);
+        }
+    }
+    if (lane == 0) {
+        Map3 cm;
+        cm.s[0] = s0;
+        cm.s[1] = s1;
+        cm.s[2] = s2;
+        fs.cmap[off] = cm;
+    }
 }
 
 // One warp per fold (blockIdx.x = trial): the running sum over every chunk,
 // recorded at each chunk's end, and the whole fold (the trial's potential).
+// The chunk maps are scanned 32 chunks at a time; a chunk whose map does not
+// apply (the sum changes binade inside it, or has no map) is walked by its
+// groups (walk_chunk).
 template <typename T>
 __global__ void __launch_bounds__(32)
     kpp_walk_kernel(const T *__restrict__ chains, long long n, int tstride, KppState *__restrict__ st, bool init,
-                    const Comp *__restrict__ comps, long long nch, T *__restrict__ states) {
+                    long long nch, FoldSlices fs) {
     if (!init && st->direct) return;
     const int t = blockIdx.x;
     const int lane = threadIdx.x;
     const int wbuf = init ? 0 : 1 - st->cur;
-    const T *v = chains + ((long long)wbuf * tstride + t) * n;
-    const Comp *cp = comps + (long long)t * nch;
-    T *sout = states + ((long long)wbuf * tstride + t) * nch;
-    __shared__ Comp cc[32];
+    const long long slice = (long long)wbuf * tstride + t;
+    const T *v = chains + slice * n;
+    const int *elo = fs.elo + slice * nch;
+    const Map3 *cmap = fs.cmap + slice * nch;
+    const Map3 *gmap = fs.gmap + slice * nch * KPP_GROUPS;
+    T *sout = reinterpret_cast<T *>(fs.states) + slice * nch;
     constexpr long long TOP = 1LL << (Bits<T>::MB + 1);
     T p = T(0);
-    int dummy;
+    int e_cur = -1;
+    Map3 m_cur{};
+    if (lane < nch) {
+        e_cur = elo[lane];
+        if (e_cur >= 0) m_cur = cmap[lane];
+    }
     for (long long jb = 0; jb < nch; jb += 32) {
-        __syncwarp();
-        if (jb + lane < nch) cc[lane] = cp[jb + lane];
-        __syncwarp();
-        const int nb = (int)min(32LL, nch - jb);
-        for (int jj = 0; jj < nb; jj++) {
-            const long long j = jb + jj;
-            const int e_lo = cc[jj].e_lo;
-            const int be = normal_exp(p);
-            bool done = false;
-            if (be > 0 && e_lo >= 0) {
-                const int slot = be - e_lo;
-                if (slot >= 0 && slot < 3) {
-                    const long long P = significand(p);
-                    const long long a = (P & 1) ? cc[jj].a[slot][1] : cc[jj].a[slot][0];
-                    const long long P2 = P + a;
-                    if (P2 < TOP) {
-                        p = from_parts<T>(be, P2);
-                        done = true;
-                    }
-                }
-            }
-            if (!done) {
-                const long long lo = j * KPP_CH, hi = min(n, lo + KPP_CH);
-                for (long long g = lo; g < hi; g += 32) {
-                    const int len = (int)min(32LL, hi - g);
-                    const T val = lane < len ? v[g + lane] : T(0);
-                    p = walk_group<T, false>(p, val, len, T(0), &dummy);
-                }
-            }
-            if (lane == 0) sout[j] = p;
+        // the next 32 chunks' maps load while these are scanned
+        int e_nxt = -1;
+        Map3 m_nxt{};
+        if (jb + 32 + lane < nch) {
+            e_nxt = elo[jb + 32 + lane];
+            if (e_nxt >= 0) m_nxt = cmap[jb + 32 + lane];
         }
+        const int nb = (int)min(32LL, nch - jb);
+        int start = 0;
+        while (start < nb) {
+            const int be = normal_exp(p);
+            const bool live = lane >= start && lane < nb;
+            const int slot = be - e_cur;
+            const bool ok = be > 0 && e_cur >= 0 && slot >= 0 && slot < 3;
+            Step s = !live ? Step{0, 0} : (ok ? pick(m_cur, slot) : Step{KPP_SAT, KPP_SAT});
+#pragma unroll
+            for (int off = 1; off < 32; off <<= 1) {
+                const Step o = shfl_up_step(s, off);
+                if (lane >= off) s = compose(o, s);
+            }
+            const long long P = be > 0 ? significand(p) : 0;
+            const long long Pl = P + ((P & 1) ? s.a1 : s.a0);
+            const unsigned badm = __ballot_sync(0xffffffffu, live && !(be > 0 && Pl < TOP));
+            const int f0 = badm ? __ffs(badm) - 1 : nb;
+            if (live && lane < f0) sout[jb + lane] = from_parts<T>(be, Pl);
+            if (f0 > start) {
+                const long long Pb = (long long)__shfl_sync(0xffffffffu, (unsigned long long)Pl, f0 - 1);
+                p = from_parts<T>(be, Pb);
+            }
+            if (f0 >= nb) break;
+            const long long j = jb + f0;
+            const int ej = __shfl_sync(0xffffffffu, e_cur, f0);
+            const int clen = (int)min((long long)KPP_CH, n - j * KPP_CH);
+            int dummy;
+            p = walk_chunk<T, false>(p, v + j * KPP_CH, clen, gmap + j * KPP_GROUPS, ej, T(0), &dummy);
+            if (lane == 0) sout[j] = p;
+            start = f0 + 1;
+        }
+        e_cur = e_nxt;
+        m_cur = m_nxt;
     }
     if (lane == 0) st->pot[t] = (double)p;
 }
@@ -505,9 +606,8 @@ __global__ void __launch_bounds__(32)
 template <typename T>
 __global__ void __launch_bounds__(MAX_TRIALS * 32)
     kpp_select_kernel(const T *__restrict__ x, long long n, int d, const T *__restrict__ chains, int tstride,
-                      const T *__restrict__ states, long long nch, const double *__restrict__ draws,
-                      long long n_draws, int n_trials, int c, int k, KppState *__restrict__ st,
-                      T *__restrict__ centers) {
+                      long long nch, FoldSlices fs, const double *__restrict__ draws, long long n_draws,
+                      int n_trials, int c, int k, KppState *__restrict__ st, T *__restrict__ centers) {
     __shared__ long long copy_row;
     __shared__ int copy_centre;
     __shared__ int do_search;
@@ -570,9 +670,9 @@ __global__ void __launch_bounds__(MAX_TRIALS * 32)
     if (w >= n_trials) return;
     // trial w: the first row whose running sum reaches thr (kmeans.rs:215-223)
     const T thr = thr_s[w];
-    const long long off = ((long long)st->cur * tstride + st->cur_trial);
-    const T *S = states + off * nch;
-    const T *v = chains + off * n;
+    const long long slice = (long long)st->cur * tstride + st->cur_trial;
+    const T *S = reinterpret_cast<const T *>(fs.states) + slice * nch;
+    const T *v = chains + slice * n;
     // First chunk whose end state is not below thr: a 32-ary search (the
     // states never decrease, and a NaN state stays NaN, so "not below" holds
     // from one chunk on); that chunk is then walked with the exact test.
@@ -593,20 +693,44 @@ __global__ void __launch_bounds__(MAX_TRIALS * 32)
     long long cand = n - 1;
     if (lo < nch) {
         const long long j = lo;
-        T p = j > 0 ? S[j - 1] : T(0);
-        const long long a = j * KPP_CH, b = min(n, a + KPP_CH);
-        for (long long g = a; g < b; g += 32) {
-            const int len = (int)min(32LL, b - g);
-            const T val = lane < len ? v[g + lane] : T(0);
-            int hit = -1;
-            p = walk_group<T, true>(p, val, len, thr, &hit);
-            if (hit >= 0) {
-                cand = g + hit;
-                break;
-            }
-        }
+        const T p = j > 0 ? S[j - 1] : T(0);
+        const int clen = (int)min((long long)KPP_CH, n - j * KPP_CH);
+        int hit = -1;
+        walk_chunk<T, true>(p, v + j * KPP_CH, clen, fs.gmap + (slice * nch + j) * KPP_GROUPS, fs.elo[slice * nch + j],
+                            thr, &hit);
+        if (hit >= 0) cand = j * KPP_CH + hit;
     }
     if (lane == 0) st->cand[w] = cand;
+}
+
+template <typename T, int TT, bool INIT>
+void launch_trials(const T *x, long long n, int d, T *chains, int ts, const KppState *st, int ntr, double *csum,
+                   long long nch, cudaStream_t s) {
+    constexpr size_t smem = trial_smem<T, TT>();
+    static_assert(smem <= 48 * 1024, "the trial tile fits the default shared-memory limit");
+    kpp_trials_kernel<T, TT, INIT><<<(unsigned)nch, KPP_THREADS, smem, s>>>(x, n, d, chains, ts, st, ntr, csum, nch);
+    FK_LAUNCH_CHECK();
+}
+
+// The trial pass with the smallest trial-slot count that holds ntr trials.
+template <typename T>
+void launch_trials_any(const T *x, long long n, int d, T *chains, int ts, const KppState *st, int ntr, double *csum,
+                       long long nch, cudaStream_t s) {
+    switch (ntr) {
+        case 1: launch_trials<T, 1, false>(x, n, d, chains, ts, st, ntr, csum, nch, s); break;
+        case 2: launch_trials<T, 2, false>(x, n, d, chains, ts, st, ntr, csum, nch, s); break;
+        case 3: launch_trials<T, 3, false>(x, n, d, chains, ts, st, ntr, csum, nch, s); break;
+        case 4: launch_trials<T, 4, false>(x, n, d, chains, ts, st, ntr, csum, nch, s); break;
+        case 5: launch_trials<T, 5, false>(x, n, d, chains, ts, st, ntr, csum, nch, s); break;
+        case 6: launch_trials<T, 6, false>(x, n, d, chains, ts, st, ntr, csum, nch, s); break;
+        case 7: launch_trials<T, 7, false>(x, n, d, chains, ts, st, ntr, csum, nch, s); break;
+        case 8: launch_trials<T, 8, false>(x, n, d, chains, ts, st, ntr, csum, nch, s); break;
+        case 9: launch_trials<T, 9, false>(x, n, d, chains, ts, st, ntr, csum, nch, s); break;
+        case 10: launch_trials<T, 10, false>(x, n, d, chains, ts, st, ntr, csum, nch, s); break;
+        case 11: launch_trials<T, 11, false>(x, n, d, chains, ts, st, ntr, csum, nch, s); break;
+        case 12: launch_trials<T, 12, false>(x, n, d, chains, ts, st, ntr, csum, nch, s); break;
+        default: launch_trials<T, 16, false>(x, n, d, chains, ts, st, ntr, csum, nch, s); break;
+    }
 }
 
 }  // namespace
@@ -629,11 +753,18 @@ void run_kmeanspp(Ctx &ctx, const T *x, int64_t n, int d, int k, const double *d
     FK_CUDA(cudaMemsetAsync(centers_out, 0, sizeof(T) * (size_t)k * d, s));
     const long long nch = (n + KPP_CH - 1) / KPP_CH;
     const int ts = n_trials;  // trial slices per buffer
+    const size_t slices = 2 * (size_t)ts * (size_t)nch;  // per-chunk entries over both buffers
     auto *st = (KppState *)ctx.get(BUF_KPP0, sizeof(KppState));
     T *chains = (T *)ctx.get(BUF_KPP1, sizeof(T) * (size_t)n * ts * 2);
     double *csum = (double *)ctx.get(BUF_KPP2, sizeof(double) * (size_t)nch * ts);
-    Comp *comps = (Comp *)ctx.get(BUF_KPP3, sizeof(Comp) * (size_t)nch * ts + sizeof(T) * (size_t)nch * ts * 2 + 64);
-    T *states = (T *)(comps + (size_t)nch * ts);
+    const size_t b_gmap = sizeof(Map3) * slices * KPP_GROUPS, b_cmap = sizeof(Map3) * slices,
+                 b_states = sizeof(T) * slices, b_elo = sizeof(int) * slices;
+    unsigned char *fold = (unsigned char *)ctx.get(BUF_KPP3, b_gmap + b_cmap + b_states + b_elo + 256);
+    FoldSlices fs;
+    fs.gmap = reinterpret_cast<Map3 *>(fold);
+    fs.cmap = reinterpret_cast<Map3 *>(fold + b_gmap);
+    fs.states = fold + b_gmap + b_cmap;
+    fs.elo = reinterpret_cast<int *>(fold + b_gmap + b_cmap + b_states);
     FK_CUDA(cudaMemsetAsync(st, 0, sizeof(KppState), s));
 
     kpp_first_kernel<T><<<1, 128, 0, s>>>(x, n, d, draws_dev, n_draws, st, centers_out);
@@ -642,25 +773,23 @@ void run_kmeanspp(Ctx &ctx, const T *x, int64_t n, int d, int k, const double *d
         if (draws_used) *draws_used = 1;
         return;
     }
+    const unsigned cgrid = (unsigned)((nch + KPP_THREADS / 32 - 1) / (KPP_THREADS / 32));
     // the first D^2 array (distances to the first centre) and its fold
-    kpp_trials_kernel<T, true><<<(unsigned)nch, KPP_THREADS, 0, s>>>(x, n, d, chains, ts, st, 1, csum, nch);
+    launch_trials<T, 1, true>(x, n, d, chains, ts, st, 1, csum, nch, s);
+    kpp_compose_kernel<T><<<dim3(cgrid, 1), KPP_THREADS, 0, s>>>(chains, n, ts, st, true, csum, nch, fs);
     FK_LAUNCH_CHECK();
-    kpp_compose_kernel<T><<<dim3((unsigned)nch, 1), KPP_THREADS, 0, s>>>(chains, n, ts, st, true, csum, nch, comps);
-    FK_LAUNCH_CHECK();
-    kpp_walk_kernel<T><<<1, 32, 0, s>>>(chains, n, ts, st, true, comps, nch, states);
+    kpp_walk_kernel<T><<<1, 32, 0, s>>>(chains, n, ts, st, true, nch, fs);
     FK_LAUNCH_CHECK();
     for (int c = 1; c <= k; c++) {
-        kpp_select_kernel<T><<<1, MAX_TRIALS * 32, 0, s>>>(x, n, d, chains, ts, states, nch, draws_dev, n_draws,
+        kpp_select_kernel<T><<<1, MAX_TRIALS * 32, 0, s>>>(x, n, d, chains, ts, nch, fs, draws_dev, n_draws,
                                                             n_trials, c, k, st, centers_out);
         FK_LAUNCH_CHECK();
         if (c == k) break;
-        kpp_trials_kernel<T, false><<<(unsigned)nch, KPP_THREADS, 0, s>>>(x, n, d, chains, ts, st, n_trials, csum,
-                                                                          nch);
+        launch_trials_any<T>(x, n, d, chains, ts, st, n_trials, csum, nch, s);
+        kpp_compose_kernel<T><<<dim3(cgrid, (unsigned)n_trials), KPP_THREADS, 0, s>>>(chains, n, ts, st, false, csum,
+                                                                                     nch, fs);
         FK_LAUNCH_CHECK();
-        kpp_compose_kernel<T><<<dim3((unsigned)nch, (unsigned)n_trials), KPP_THREADS, 0, s>>>(chains, n, ts, st,
-                                                                                             false, csum, nch, comps);
-        FK_LAUNCH_CHECK();
-        kpp_walk_kernel<T><<<(unsigned)n_trials, 32, 0, s>>>(chains, n, ts, st, false, comps, nch, states);
+        kpp_walk_kernel<T><<<(unsigned)n_trials, 32, 0, s>>>(chains, n, ts, st, false, nch, fs);
         FK_LAUNCH_CHECK();
     }
     if (draws_used) {
