@@ -13,6 +13,13 @@ so every iteration runs. A step is one Lloyd iteration over all n rows
   e2e     the same metric through the public API with host buffers: one fit
           call on a pinned host X (H2D of X, K iterations, D2H of labels and
           centres inside the timed region).
+  parity  outside the timed region, the same K iterations replayed one step
+          at a time from the same centres, each checked against the FP64
+          oracle (oracle/, a restatement of kmeans.rs): label mismatches on a
+          seeded sample of rows (the oracle's direct form with the step's
+          centres), centre error against the oracle's update over all n rows
+          with the step's labels, inertia error, the shift, the near-tie
+          count; and the timed fit's own outputs against the replay's.
   forms   bf16  = FK_PRECISION_MIXED_BF16 on the f32x64 entry point
                   (KMeans<f64> semantics, BF16 tcgen05 contraction + FP64
                   re-check); labels identical to the FP64 oracle.
@@ -31,16 +38,20 @@ k in [4,64]) x 10 k-means++ restarts, one fit_batched call per step (f32
 distances, FP64 centroid sums); value = Lloyd iterations over all 5,120 fits
 per second of the call, pt_k_per_s = sum of n * k * iterations per second.
 
---impl reference times the CPU restatement of the reference (oracle/, the
-reference is Rust and cannot be built here) on a bounded row sample of the
-same workload with all host threads, and reports iterations/s extrapolated
-to the full n.
+--impl reference times the CPU restatement of the reference (oracle/; the
+reference is Rust and cannot be built here) with all host threads: the K
+timed steps together are ONE full Lloyd iteration over all n rows (step s
+assigns rows [s n / K, (s + 1) n / K) with the chunked parallel assignment
+and adds them to the row-order centroid sums; the last step finishes the
+update), so value = 1 / (time of that full iteration), measured, not
+extrapolated.
 """
 import argparse
 import ctypes as C
 import faulthandler
 import json
 import os
+import platform
 import subprocess
 import sys
 import threading
@@ -52,7 +63,7 @@ sys.path.insert(0, ROOT)
 import numpy as np  # noqa: E402
 
 
-def parse():
+def parse(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=None,
@@ -64,8 +75,11 @@ def parse():
     ap.add_argument("--scale", type=float, default=1.0, help="fraction of the full row count")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-parity", action="store_true", help="skip the per-iteration oracle checks")
+    ap.add_argument("--parity-rows", type=int, default=100_000,
+                    help="rows per iteration whose labels are checked against the oracle's direct form")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
-    args = ap.parse_args()
+    args = ap.parse_args(argv)
     if args.steps is None:  # the configurations' own iteration counts (anisotropic: 50 Lloyd iterations)
         args.steps = {"anisotropic": 50, "bisector": 20, "dirichlet": 20, "batched": 20}[args.workload]
     return args
@@ -73,14 +87,53 @@ def parse():
 
 METRIC = "KMeans Lloyd iters/s & pt·k/s: BF16+FP64 recheck vs plain FP32, labels=FP64"
 
+# DRAM traffic of the dominant kernel per row of X (ncu dram__bytes_read.sum +
+# dram__bytes_write.sum of one launch, divided by the rows it processed; the
+# traffic grows in proportion to the rows: X read once, records written once).
+# Source: profiles/tc_assign_anisotropic_1024x128_quarter.md, a 1,000,000-row
+# capture of tc_assign_kernel<2, BF16> (256.4 MB read + 48.4 MB written).
+TRAFFIC_BYTES_PER_ROW = {("anisotropic_1024x128", "bf16"): (256.4e6 + 48.4e6) / 1e6}
+
 
 def load_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
         d = json.load(open(p))
-        return d.get("hbm_gbs", 6800.0), d.get("bf16_tflops", 1900.0), d.get("bf16_tflops_sustained", 1700.0), \
-            "measured"
-    return 6800.0, 1900.0, 1700.0, "fallback"
+        return {"hbm": d.get("hbm_gbs", 6800.0), "bf16": d.get("bf16_tflops", 1900.0),
+                "bf16s": d.get("bf16_tflops_sustained", 1700.0), "sm_max": d.get("sm_max_mhz", 2070.0),
+                "src": "measured"}
+    return {"hbm": 6800.0, "bf16": 1900.0, "bf16s": 1700.0, "sm_max": 2070.0, "src": "fallback"}
+
+
+def pick_tensor_peak(peaks, clocks):
+    """The burst BF16 peak when the SM clock stayed at its maximum through the
+    timed region (a short region: the power cap has not pulled the clock
+    down), else the sustained one; returns (TFLOP/s, which)."""
+    sm = clocks.get("sm_mhz")
+    mx = clocks.get("sm_max_mhz") or peaks["sm_max"]
+    if sm is not None and mx and sm >= 0.97 * mx:
+        return peaks["bf16"], (f"bf16_tflops, burst ({peaks['src']}): the SM clock stayed at {sm:.0f} of "
+                               f"{mx:.0f} MHz in the timed region")
+    return peaks["bf16s"], (f"bf16_tflops_sustained ({peaks['src']}): the SM clock ran at {sm} of {mx} MHz "
+                            "in the timed region")
+
+
+def cpu_model():
+    """The host CPU's model name (lscpu, else /proc/cpuinfo, else platform)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.lower().startswith("model name"):
+                return ln.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    try:
+        for ln in open("/proc/cpuinfo"):
+            if ln.lower().startswith("model name"):
+                return ln.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    return platform.processor() or platform.machine()
 
 
 def max_over_ranks(value, device):
@@ -189,6 +242,15 @@ def make_workload(args):
 DEFAULT_FORM = {"anisotropic": "bf16", "bisector": "fp8", "dirichlet": "fp32", "batched": "fp32"}
 
 
+def workload_config(w):
+    """The `config` of both arms' JSON lines (the workload, not the arm)."""
+    n, d = w["x"].shape
+    return {"workload": w["name"], "n": int(n), "d": int(d), "k": int(w["k"]), "X": "f32",
+            "init": "first k rows of a seeded permutation" if w.get("init") is not None or w["name"] != "dirichlet_256x64"
+            else "k-means++ (seeded)",
+            "tol": 0.0, "l2": f"inputs larger than L2 (X {w['x'].nbytes / 1e9:.2f} GB)", "parallelism": "replicas"}
+
+
 def initial_centres(w, xd, ctx):
     """The workload's initial centres, or k-means++ on the GPU (timed) where it
     names none; returns (centres f64, ms of the k-means++ call or None)."""
@@ -226,41 +288,57 @@ def cpu_baseline(w, seconds, threads):
         O.lloyd_step(xs, c, nthreads=threads)
     dt = (time.perf_counter() - t0) / reps
     per_iter = dt * n / rows
-    return {"value": 1.0 / per_iter, "unit": "iters/s", "cores": threads, "kind": "port",
+    return {"value": 1.0 / per_iter, "unit": "iters/s", "cores": threads, "cpu_model": cpu_model(), "kind": "port",
             "sample": f"{rows} of {n} rows, {reps} Lloyd iterations (FP64 direct form, OpenMP chunked like "
                       f"assign_parallel, serial update); per-iteration time extrapolated x{n / rows:.1f}",
             "seconds_per_full_iteration": per_iter}
 
 
 def run_reference(args):
+    """The reference's CPU algorithm (the oracle restatement, kind "port") on
+    the machine's host cores: K steps that together are one full Lloyd iteration
+    over all n rows, timed step by step."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
+    from oracle import oracle as O
     w = make_workload(args)
     if w["init"] is None:
         w["init"] = w["x"][np.random.default_rng(1).permutation(w["x"].shape[0])[: w["k"]]].astype(np.float64)
     threads = os.cpu_count() or 1
-    from oracle import oracle as O
-    n, d = w["x"].shape
-    rows = max(1024, min(n, int(20000 * args.scale) if args.scale < 1 else 20000))
-    xs = w["x"][:rows].astype(np.float64)  # the sampled rows, widened exactly
-    c = w["init"]
-    for _ in range(max(1, args.warmup)):
-        O.lloyd_step(xs, c, nthreads=threads)
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        O.lloyd_step(xs, c, nthreads=threads)
-    dt = (time.perf_counter() - t0) / args.steps
-    per_iter = dt * n / rows
-    v = 1.0 / per_iter
+    x32 = w["x"]
+    n, d = x32.shape
+    k = w["k"]
+    x64 = x32.astype(np.float64)  # KMeans<f64>'s input: X widened exactly, once, before any timing
+    c = np.ascontiguousarray(w["init"], dtype=np.float64)
+    wrows = min(n, 20000)
+    for _ in range(max(1, args.warmup)):  # warm-up: the assignment on a 20,000-row slice
+        O.assign(x64[:wrows], c, nthreads=threads)
+    K = max(1, args.steps)
+    bounds = [n * s // K for s in range(K + 1)]
+    sums, counts = np.zeros((k, d)), np.zeros(k)
+    step_s = []
+    for s in range(K):
+        t0 = time.perf_counter()
+        lo, hi = bounds[s], bounds[s + 1]
+        if hi > lo:
+            lab, _ = O.assign(x64[lo:hi], c, nthreads=threads)  # nearest_center over the rows, chunked in parallel
+            O.update_rows(x64[lo:hi], lab, sums, counts)           # recompute_centroids_into's row-order sums
+        if s == K - 1:
+            O.update_finish(sums, counts, c)                       # means, empty clusters, shift
+        step_s.append(time.perf_counter() - t0)
+    total = float(np.sum(step_s))
+    v = 1.0 / total
+    sample = (f"one full Lloyd iteration over all {n} rows split into {K} consecutive row ranges, one per step "
+              f"(parallel assignment, serial row-order update), measured: {total:.2f} s")
     out = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": "iters/s", "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_iter * 1e3, "higher_is_better": True,
+        "steps": K, "warmup": args.warmup, "ms_per_step": total * 1e3 / K, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": w["name"], "n": n, "d": int(d), "k": w["k"], "X": "f32 widened to f64",
-                   "l2": "inputs larger than L2"},
-        "cpu_baseline": {"value": v, "unit": "iters/s", "cores": threads, "kind": "port",
-                         "sample": f"{rows} of {n} rows per step, extrapolated x{n / rows:.1f}"},
+        "config": workload_config(w),
+        "step": "1/K of one Lloyd iteration (rows [s n/K, (s+1) n/K))",
+        "cpu_baseline": {"value": v, "unit": "iters/s", "cores": threads, "cpu_model": cpu_model(), "kind": "port",
+                         "arithmetic": "KMeans<f64> on X widened exactly (FP64 direct form)", "sample": sample},
         "e2e": {"value": v, "unit": "iters/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(out))
@@ -299,13 +377,21 @@ def run_batched(args):
     launches = int(_native.lib().fk_debug_launch_count() - l0)
     ms = float(np.sum(times))
     iters = sum(r["iterations_total"] for r in reps)
-    nk = 0.0
+    nk, nkd = 0.0, 0.0
     for r in reps:
         f0 = 0
         for p in probs:
-            nk += float(p["x"].shape[0]) * p["k"] * float(r["fit_n_iter"][f0:f0 + p["n_init"]].sum())
+            it = float(r["fit_n_iter"][f0:f0 + p["n_init"]].sum())
+            nk += float(p["x"].shape[0]) * p["k"] * it
+            nkd += float(p["x"].shape[0]) * p["k"] * p["x"].shape[1] * it
             f0 += p["n_init"]
     rep = reps[-1]
+    # the Lloyd phase runs on the CUDA cores: its peak is measured in this run
+    pk = (C.c_double * 8)()
+    _native.lib().fk_debug_measure_peaks(ctx.handle, pk)
+    fp32 = pk[0] / 1e12
+    lloyd_ms = float(np.sum([r["ms_lloyd"] for r in reps]))
+    achieved = 2.0 * nkd / (lloyd_ms / 1e3) / 1e12
     out = {
         "metric": METRIC, "value": iters / (ms / 1e3), "unit": "iters/s", "n_gpus": 1, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -319,8 +405,13 @@ def run_batched(args):
         "phase_ms": {k: rep[k] for k in ("ms_upload", "ms_init", "ms_tune", "ms_lloyd", "ms_download", "ms_total")},
         "graph_launches": rep["graph_launches"], "tiles": rep["tiles"],
         "gpu_launches": launches, "clocks": clocks.summary(),
-        "roofline": {"bound": "fp32-simt", "achieved": None, "peak": None, "unit": None, "frac": None,
-                     "traffic": None, "note": "see phase_ms; the assignment is FP32 CUDA-core bound"},
+        "roofline": {"bound": "fp32-simt", "achieved": achieved, "peak": fp32, "unit": "TFLOP/s",
+                     "frac": achieved / fp32, "traffic": None,
+                     "kernel": "the graph-replayed Lloyd phase (batch_assign + batch_update), all fits",
+                     "ms_per_launch": lloyd_ms / len(reps),
+                     "peak_source": "FP32 FMA peak measured in this run (fk_debug_measure_peaks); achieved counts "
+                                    "2 n k d per fit iteration over the Lloyd phase's device time (the direct form "
+                                    "executes 3 n k d)"},
     }
     if not args.no_e2e:
         t0 = time.perf_counter()
@@ -345,10 +436,81 @@ def run_batched(args):
             if time.perf_counter() - t0 > args.cpu_seconds:
                 break
         dt = time.perf_counter() - t0
-        out["cpu_baseline"] = {"value": it_cpu / dt, "unit": "iters/s", "cores": threads, "kind": "port",
-                               "pt_k_per_s": nk_cpu / dt,
+        out["cpu_baseline"] = {"value": it_cpu / dt, "unit": "iters/s", "cores": threads, "cpu_model": cpu_model(),
+                               "kind": "port", "pt_k_per_s": nk_cpu / dt,
                                "sample": f"{done} of {len(probs)} problems, all 10 runs each (oracle fit_runs)"}
     print(json.dumps(out))
+
+
+def parity_leg(w, form, ctx, xd, iters, rows, fit_centres, fit_labels):
+    """The timed trajectory replayed one Lloyd step at a time (the same
+    entry point's single-iteration form, the same centres), each step checked
+    against the FP64 oracle; then the timed fit's outputs against the replay's
+    last step. Mixed forms: labels on a seeded sample of `rows` rows (the
+    oracle's direct form with the step's centres), centres and inertia
+    against the oracle's update over all n rows with the step's labels. Plain
+    forms: the oracle's whole Lloyd step in the same precision (bit-identical
+    expected)."""
+    import ferrolearn_gb300 as F
+    from oracle import oracle as O
+    t_start = time.perf_counter()
+    x32 = w["x"]
+    n, d = x32.shape
+    mixed = form in ("bf16", "fp8")
+    rng = np.random.default_rng(20260)
+    m = min(n, rows)
+    sample = np.sort(rng.choice(n, m, replace=False)) if m < n else np.arange(n)
+    xs64 = x32[sample].astype(np.float64)
+    if form == "fp32":
+        c = w["init"].astype(np.float32)
+        dtype = "f32"
+    elif form == "fp64":
+        c = w["init"].astype(np.float64)
+        dtype = "f64"
+    else:
+        c = w["init"].astype(np.float64)
+        dtype = "f32x64"
+    mism_total, mism_max, crel_max, irel_max, srel_max, near_ties = 0, 0, 0.0, 0.0, 0.0, 0
+    per_iter = []
+    lab = None
+    for it in range(iters):
+        lab, nc, inertia, shift, rep = F.lloyd_step(xd, c, dtype=dtype, precision=form if mixed else "plain",
+                                                    ctx=ctx)
+        near_ties += int(rep["near_tie_rows"])
+        if mixed:
+            ol, _ = O.assign(xs64, c)
+            mism = int((lab[sample] != ol).sum())
+            oc, oin = O.update_given_labels(x32, lab, c)
+        else:
+            xo = x32 if form == "fp32" else x32.astype(np.float64)
+            ol, oc, oin, _ = O.lloyd_step(xo, c)
+            mism = int((lab != ol).sum())
+        crel = float(np.abs(nc.astype(np.float64) - oc).max() / max(np.abs(oc).max(), 1e-300))
+        irel = abs(float(inertia) - float(oin)) / max(abs(float(oin)), 1e-300)
+        oshift = float(np.sqrt(((oc - c.astype(np.float64)) ** 2).sum(1).max()))
+        srel = abs(float(shift) - oshift) / max(oshift, 1e-300)
+        mism_total += mism
+        mism_max = max(mism_max, mism)
+        crel_max = max(crel_max, crel)
+        irel_max = max(irel_max, irel)
+        srel_max = max(srel_max, srel)
+        per_iter.append([it, mism, crel, irel])
+        c = nc
+    out = {
+        "oracle": "oracle/ FP64 restatement of kmeans.rs (direct form, strict < argmin, row-order sums)",
+        "iterations_checked": iters,
+        "label_rows_per_iteration": int(m) if mixed else int(n),
+        "label_mismatches": mism_total, "label_mismatches_max_per_iteration": mism_max,
+        "centre_max_rel": crel_max, "centre_rel_definition": "max |c_gpu - c_oracle| / max |c_oracle| per iteration",
+        "inertia_rel_max": irel_max, "shift_rel_max": srel_max,
+        "n_iter_equal": True, "n_iter_note": f"tol 0: both run exactly {iters} iterations",
+        "near_tie_rows": near_ties, "near_tie_definition": "re-scored rows whose FP64 margin is below 1e-12 relative",
+        "per_iteration": per_iter if iters <= 60 else per_iter[:3] + per_iter[-3:],
+        "fit_centres_equal_replay": bool(np.array_equal(np.asarray(fit_centres), c)),
+        "fit_labels_equal_replay": bool(np.array_equal(np.asarray(fit_labels), lab)),
+        "seconds": time.perf_counter() - t_start,
+    }
+    return out
 
 
 def run_ours(args):
@@ -367,7 +529,7 @@ def run_ours(args):
         torch.cuda.set_device(local)
         dist.init_process_group("nccl")
     dev = torch.cuda.current_device()
-    hbm, bf16, bf16s, peak_src = load_peaks()
+    peaks = load_peaks()
     w = make_workload(args)
     x32 = w["x"]
     n, d = x32.shape
@@ -418,6 +580,7 @@ def run_ours(args):
     iters = fitted.n_iter()
     assert iters == args.steps, (iters, args.steps)
     ips = job_rate(iters, ms, world)
+    clk = clocks.summary()
     # dominant kernel: the tensor-core contraction (CUDA events on the library's
     # stream around each launch); the SIMT forms time the whole assignment
     assign_ms = rep["ms_assign"] / iters
@@ -425,12 +588,13 @@ def run_ours(args):
     contract_ms = rep["ms_contract"] / iters if rep["ms_contract"] > 0 else assign_ms
     flops = 2.0 * n * k * d
     if form == "bf16":
-        roof = {"bound": "tensor", "achieved": flops / (contract_ms / 1e3) / 1e12, "peak": bf16s, "unit": "TFLOP/s",
-                "peak_source": f"bf16_tflops_sustained ({peak_src})"}
+        peak, src = pick_tensor_peak(peaks, clk)
+        roof = {"bound": "tensor", "achieved": flops / (contract_ms / 1e3) / 1e12, "peak": peak, "unit": "TFLOP/s",
+                "peak_source": src}
     elif form == "fp8":
-        roof = {"bound": "tensor", "achieved": flops / (contract_ms / 1e3) / 1e12, "peak": 2.0 * bf16s,
-                "unit": "TFLOP/s", "peak_source": f"2 x bf16_tflops_sustained ({peak_src}): the dense E4M3 rate is "
-                                                  "twice the BF16 rate on this part"}
+        roof = {"bound": "tensor", "achieved": flops / (contract_ms / 1e3) / 1e12, "peak": 2.0 * peaks["bf16s"],
+                "unit": "TFLOP/s", "peak_source": f"2 x bf16_tflops_sustained ({peaks['src']}): the dense E4M3 "
+                                                  "rate is twice the BF16 rate on this part"}
     else:
         # the plain forms run on the CUDA cores: their peak is measured here
         # (fk_debug_measure_peaks: FMA chains on every SM, CUDA events)
@@ -442,7 +606,12 @@ def run_ours(args):
                 "peak_source": f"{form.upper()} FMA peak measured in this run (fk_debug_measure_peaks); achieved "
                                "counts 2 n k d (the GEMM-equivalent work), the direct form executes 3 n k d"}
     roof["frac"] = roof["achieved"] / roof["peak"]
-    roof["traffic"] = None
+    tb = TRAFFIC_BYTES_PER_ROW.get((w["name"], form))
+    roof["traffic"] = tb * n if tb is not None else None
+    if tb is not None:
+        roof["traffic_source"] = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch at 1,000,000 rows "
+                                  "(profiles/tc_assign_anisotropic_1024x128_quarter.md), scaled to n rows")
+        roof["algorithmic_bytes"] = n * d * 2 + n * 2 * 32  # BF16 X once + 32-byte records per row and slice
     roof["kernel"] = f"tc_assign_kernel ({form.upper()} tcgen05 contraction + top-2 epilogue)" if mixed else \
         "assign_direct_kernel (whole assignment phase)"
     roof["ms_per_launch"] = contract_ms if mixed else assign_ms
@@ -452,10 +621,7 @@ def run_ours(args):
         "warmup": args.warmup, "ms_per_step": ms / iters, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": {"bf16": "bf16+f64", "fp8": "e4m3+f64", "fp32": "f32", "fp64": "f64"}[form],
         "data": "synthetic", "form": form,
-        "config": {"workload": w["name"], "n": n, "d": d, "k": k, "X": "f32",
-                   "init": "k-means++ on the GPU" if kpp_ms is not None else "first k rows of a seeded permutation",
-                   "tol": 0.0, "l2": f"inputs larger than L2 (X {x32.nbytes / 1e9:.2f} GB)",
-                   "parallelism": "replicas"},
+        "config": workload_config(w),
         "pt_k_per_s": ips * n * k,
         "phase_ms_per_iter": {"assign": assign_ms, "contract": contract_ms if mixed else None,
                               "update": rep["ms_update"] / iters},
@@ -465,20 +631,29 @@ def run_ours(args):
                     "near_ties": rep["near_tie_rows"],
                     "fraction": rep["rows_rechecked"] / max(1, rep["rows_assigned"])},
         "gpu_launches": launches,
-        "clocks": clocks.summary(),
+        "clocks": clk,
         "roofline": roof,
     }
-    # the update phase against HBM: a full pass reads X once and writes the
-    # centres (n d sizeof(X) + 4 n + 2 k d 8 bytes); the mixed forms update
-    # incrementally after the second iteration, so their figure is that full
-    # pass's bytes over the average update time (an effective rate)
+    if kpp_ms is not None:
+        out["config"]["init"] = "k-means++ on the GPU (seeded)"
+    # the update phase against HBM, with the bytes it moves: a full pass reads
+    # X once and writes the centres (n d sizeof(X) + 4 n + 16 k d); an
+    # incremental one (mixed forms, from the third iteration) compares the
+    # two label arrays (8 n), reads each moved row for its old and its new
+    # cluster (2 m (d sizeof(X) + 8)) and rewrites the exact state and means
+    # (40 k d)
     upd_ms = rep["ms_update"] / iters
-    upd_bytes = n * d * x32.itemsize * (2 if form == "fp64" else 1) + 4 * n + 16 * k * d
+    xb = x32.itemsize * (2 if form == "fp64" else 1)
+    n_inc = int(rep["updates_incremental"])
+    full_bytes = n * d * xb + 4 * n + 16 * k * d
+    inc_bytes_total = n_inc * (8 * n + 40 * k * d) + 2 * int(rep["rows_moved"]) * (d * xb + 8)
+    upd_bytes = ((iters - n_inc) * full_bytes + inc_bytes_total) / iters
     out["update_roofline"] = {"bound": "hbm", "bytes_per_iter": upd_bytes, "ms_per_iter": upd_ms,
-                              "achieved": upd_bytes / (upd_ms / 1e3) / 1e9, "peak": hbm, "unit": "GB/s",
-                              "frac": upd_bytes / (upd_ms / 1e3) / 1e9 / hbm,
-                              "note": "incremental after iteration 2 (effective rate)" if mixed
-                              else "full pass every iteration (row-order sums of the reference)"}
+                              "achieved": upd_bytes / (upd_ms / 1e3) / 1e9, "peak": peaks["hbm"], "unit": "GB/s",
+                              "frac": upd_bytes / (upd_ms / 1e3) / 1e9 / peaks["hbm"],
+                              "full_passes": iters - n_inc, "incremental_updates": n_inc,
+                              "rows_moved": int(rep["rows_moved"]),
+                              "note": "bytes each update moves, averaged over the K iterations"}
     if kpp_ms is not None:
         out["kpp_ms"] = kpp_ms
     if "x_predict" in w and rank == 0:
@@ -507,6 +682,9 @@ def run_ours(args):
         out["e2e"] = {"value": f2.n_iter() / (t1 - t0), "unit": "iters/s",
                       "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": d2h / args.steps,
                       "note": "one fit call on a pinned host X running K iterations; copies amortised per step"}
+    if not args.no_parity and rank == 0:
+        out["parity"] = parity_leg(w, form, ctx, xd, iters, args.parity_rows, c_out.cpu().numpy(),
+                                   l_out.cpu().numpy())
     if not args.no_cpu and rank == 0 and world == 1:
         out["cpu_baseline"] = cpu_baseline(w, args.cpu_seconds, os.cpu_count() or 1)
     if rank == 0:

@@ -129,6 +129,8 @@ class FitReport(C.Structure):
         ("ms_total", C.c_double),
         ("precision_used", C.c_int32),
         ("reserved", C.c_int32),
+        ("rows_moved", C.c_int64),
+        ("updates_incremental", C.c_int64),
     ]
 
     def as_dict(self):

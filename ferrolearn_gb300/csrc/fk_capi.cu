@@ -278,6 +278,8 @@ void accumulate_report(fk_fit_report *rep, const DevScalars &h, int64_t n) {
     rep->rows_few += (int64_t)h.quad_count;
     rep->rows_exhaustive += (int64_t)h.ex_count;
     rep->near_tie_rows += (int64_t)h.near_tie_rows;
+    rep->rows_moved += (int64_t)h.moved_rows;
+    rep->updates_incremental += (int64_t)h.incremental;
 }
 
 // ------------------------------------------------------------------ fit --

@@ -62,6 +62,8 @@ struct DevScalars {
     unsigned long long ex_count;    // second pass: rows with more than 4 candidates
     unsigned long long f64_count;   // rows whose remaining candidates are scored in FP64
     unsigned long long error_word;  // nonzero: a bounded device wait gave up
+    unsigned long long moved_rows;  // incremental update: rows whose label changed
+    unsigned long long incremental; // 1: this iteration's update was incremental
 };
 
 // --------------------------------------------------- mixed precision --

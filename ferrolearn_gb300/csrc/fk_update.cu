@@ -1541,6 +1541,10 @@ void launch_update_centroids_incremental(Ctx &ctx, const float *x, int64_t n, in
     exact_means_kernel<<<(unsigned)((kd + 255) / 256), 256, 0, s>>>(d, k, n, state, counts, amax, old_c, new_c);
     FK_LAUNCH_CHECK();
     launch_max_shift<double>(new_c, old_c, k, d, &scalars->shift_bits, s);
+    // for the report: how many rows this update moved, and that it was incremental
+    FK_CUDA(cudaMemcpyAsync(&scalars->moved_rows, moved_count, sizeof(unsigned long long), cudaMemcpyDeviceToDevice,
+                            s));
+    FK_CUDA(cudaMemsetAsync(&scalars->incremental, 1, 1, s));
 }
 
 void launch_row_inertia(Ctx &ctx, const float *x, int64_t n, int d, const int32_t *labels, const double *c, int k,

@@ -100,6 +100,11 @@ typedef struct fk_fit_report {
     double ms_total;           /* device time of the whole call            */
     int32_t precision_used;
     int32_t reserved;
+    int64_t rows_moved;        /* mixed, incremental centroid updates: rows
+                                  whose label changed, summed over them    */
+    int64_t updates_incremental; /* mixed: iterations whose centroid update
+                                  was incremental (the rest were full
+                                  passes over X)                           */
 } fk_fit_report;
 
 typedef struct fk_ctx fk_ctx;

@@ -784,3 +784,41 @@ int orc_update_given_labels_f32x64(const float *x, int64_t n, int64_t d, const i
     free(mind);
     return ORC_OK;
 }
+
+/* The first loop of recompute_centroids_into (kmeans.rs:370-375) for F = f64
+ * over the m rows given, continuing the caller's sums and counts: one pass
+ * split into consecutive row ranges adds in exactly the single loop's order.
+ * The benchmark's reference arm times a full Lloyd iteration this way, a row
+ * range per step. */
+int orc_update_rows_f64(const double *x, int64_t m, int64_t d, const int64_t *labels, int64_t k, double *sums,
+                        double *counts) {
+    if (!x || !labels || !sums || !counts) return ORC_ERR_NULL;
+    for (int64_t i = 0; i < m; i++) {
+        const int64_t l = labels[i];
+        if (l < 0 || l >= k) return ORC_ERR_INVALID_PARAMETER;
+        counts[l] = counts[l] + 1.0;
+        for (int64_t j = 0; j < d; j++) sums[l * d + j] = sums[l * d + j] + x[i * d + j];
+    }
+    return ORC_OK;
+}
+
+/* The rest of recompute_centroids_into (kmeans.rs:377-400): the means (an
+ * empty cluster keeps its old centre) and sqrt of the largest squared shift. */
+int orc_update_finish_f64(const double *sums, const double *counts, const double *old_c, int64_t k, int64_t d,
+                          double *new_c, double *shift) {
+    if (!sums || !counts || !old_c || !new_c || !shift) return ORC_ERR_NULL;
+    for (int64_t q = 0; q < k; q++) {
+        if (counts[q] > 0.0) {
+            for (int64_t j = 0; j < d; j++) new_c[q * d + j] = sums[q * d + j] / counts[q];
+        } else {
+            memcpy(new_c + q * d, old_c + q * d, sizeof(double) * (size_t)d);
+        }
+    }
+    double ms = 0.0;
+    for (int64_t q = 0; q < k; q++) {
+        const double s = orc_sqeuc_f64(new_c + q * d, old_c + q * d, d);
+        if (s > ms) ms = s;
+    }
+    *shift = sqrt(ms);
+    return ORC_OK;
+}

@@ -45,6 +45,8 @@ def lib():
         _lib.orc_fit_runs_f32.argtypes = [p, i64, i64, i64, i64, C.c_float, i64, p, u64, C.c_int, p, p, p, p,
                                           C.c_int]
         _lib.orc_update_given_labels_f32x64.argtypes = [p, i64, i64, p, p, i64, p, p, C.c_int]
+        _lib.orc_update_rows_f64.argtypes = [p, i64, i64, p, i64, p, p]
+        _lib.orc_update_finish_f64.argtypes = [p, p, p, i64, i64, p, p]
     return _lib
 
 
@@ -122,6 +124,30 @@ def update_given_labels(x32, labels, centers, nthreads=None):
     if rc:
         raise OracleError(rc)
     return nc, inertia.value
+
+
+def update_rows(x, labels, sums, counts):
+    """The first loop of recompute_centroids_into (kmeans.rs:370-375), F = f64,
+    over the given rows, adding into sums (k x d) and counts (k) in place."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    lab = np.ascontiguousarray(labels, dtype=np.int64)
+    assert sums.dtype == np.float64 and sums.flags.c_contiguous and counts.dtype == np.float64
+    rc = lib().orc_update_rows_f64(_ptr(x), x.shape[0], x.shape[1], _ptr(lab), sums.shape[0], _ptr(sums),
+                                   _ptr(counts))
+    if rc:
+        raise OracleError(rc)
+
+
+def update_finish(sums, counts, centers):
+    """The rest of recompute_centroids_into (kmeans.rs:377-400) -> (new_centers, max_shift)."""
+    c = np.ascontiguousarray(centers, dtype=np.float64)
+    nc = np.empty_like(c)
+    shift = C.c_double()
+    rc = lib().orc_update_finish_f64(_ptr(sums), _ptr(counts), _ptr(c), c.shape[0], c.shape[1], _ptr(nc),
+                                     C.byref(shift))
+    if rc:
+        raise OracleError(rc)
+    return nc, shift.value
 
 
 def kmeanspp(x, k, draws_arr=None, seed=0):

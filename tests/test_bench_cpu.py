@@ -46,6 +46,30 @@ def test_reference_arm_line():
     assert out["e2e"]["value"] == out["value"]
     assert out["e2e"]["h2d_bytes_per_step"] == 0 and out["e2e"]["d2h_bytes_per_step"] == 0
     assert out["config"]["workload"] == "anisotropic_1024x128"
+    # the steps together are one full Lloyd iteration over every row, measured
+    assert out["config"]["n"] == 20000 and "one full Lloyd iteration over all 20000 rows" in out["cpu_baseline"]["sample"]
+    assert abs(out["ms_per_step"] * out["steps"] / 1e3 - 1.0 / out["value"]) < 1e-6 / out["value"]
+    assert out["cpu_baseline"]["cpu_model"]
+
+
+def test_both_arms_share_the_workload_config():
+    sys.path.insert(0, ROOT)
+    import bench
+    from ferrolearn_gb300 import workloads as W
+    w = W.anisotropic_1024x128(scale=0.002)
+    cfg = bench.workload_config(w)
+    assert cfg == {"workload": "anisotropic_1024x128", "n": 8000, "d": 128, "k": 1024, "X": "f32",
+                   "init": "first k rows of a seeded permutation", "tol": 0.0,
+                   "l2": "inputs larger than L2 (X 0.00 GB)", "parallelism": "replicas"}
+
+
+def test_tensor_peak_follows_the_sampled_clock():
+    sys.path.insert(0, ROOT)
+    import bench
+    peaks = {"bf16": 1911.1, "bf16s": 1715.8, "sm_max": 2070.0, "src": "measured"}
+    assert bench.pick_tensor_peak(peaks, {"sm_mhz": 2070.0, "sm_max_mhz": 2070.0})[0] == 1911.1
+    assert bench.pick_tensor_peak(peaks, {"sm_mhz": 1462.0, "sm_max_mhz": 2070.0})[0] == 1715.8
+    assert bench.pick_tensor_peak(peaks, {"sm_mhz": None, "sm_max_mhz": None})[0] == 1715.8
 
 
 _RANK_SCRIPT = r"""

@@ -236,3 +236,18 @@ def test_update_given_labels_is_the_reference_update():
     assert np.array_equal(nc, nc2)
     d = ((x.astype(np.float64) - c[lab]) ** 2).sum(1)
     assert abs(inertia - d.sum()) <= 1e-12 * d.sum()
+
+
+def test_update_split_into_row_ranges_is_the_single_loop():
+    # the reference arm of the benchmark runs one Lloyd iteration as K row
+    # ranges; the split update must equal the oracle's one-pass update
+    rng = np.random.default_rng(12)
+    x = rng.normal(size=(10007, 6)) * 5
+    c = x[rng.choice(10007, 9, replace=False)].copy()
+    c[4] = 1e9
+    lab, nc, _, shift = O.lloyd_step(x, c)
+    sums, counts = np.zeros((9, 6)), np.zeros(9)
+    for lo in range(0, 10007, 777):
+        O.update_rows(x[lo:lo + 777], lab[lo:lo + 777], sums, counts)
+    nc2, shift2 = O.update_finish(sums, counts, c)
+    assert np.array_equal(nc, nc2) and shift == shift2
