@@ -312,6 +312,46 @@ def test_fp8_bisector_fit_and_predict_match_fp64_oracle():
     assert np.array_equal(g.predict(xp), O.predict(g.cluster_centers(), xp.astype(np.float64)))
 
 
+def _plan(n, d, k, precision, topk, sms=152):
+    out = (C.c_int64 * 10)()
+    st = _native.lib().fk_debug_tc_plan(n, d, k, precision, topk, sms, out)
+    assert st == 0
+    return dict(zip(["d_pad", "kp", "parts", "k_pad", "nblocks", "xst", "smem", "grid", "ctas", "tiles"], out))
+
+
+def test_fp8_bisector_at_full_k_and_d_matches_fp64_oracle():
+    # the large-k FP8 workload at its own k = 4096 and d = 256 (200,000 rows,
+    # 10% on bisectors): the E4M3 main pass runs 8 slices of 512 resident
+    # centres and the BF16 top-8 second pass 16 slices of 256, the plans the
+    # full-size workload runs; labels of every iteration, centres, n_iter and
+    # predict on fresh rows must be the FP64 oracle's
+    w = W.bisector_4096x256(scale=0.025, predict_scale=0.01)
+    x32, k = w["x"], w["k"]
+    n = x32.shape[0]
+    assert x32.shape == (200000, 256) and k == 4096
+    torch = pytest.importorskip("torch")
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    assert _plan(n, 256, k, F.MIXED_FP8, 2, sms)["parts"] == 8
+    assert _plan(n // 4, 256, k, F.MIXED_BF16, 8, sms)["parts"] == 16
+    x64 = x32.astype(np.float64)
+    c = w["init"].copy()
+    second = 0
+    for _ in range(2):
+        gl, gc, gi, gs, rep = F.lloyd_step(x32, c, dtype="f32x64", precision="fp8")
+        ol, oc, oi, os_ = O.lloyd_step(x64, c)
+        assert np.array_equal(gl, ol)
+        assert _close(gc, oc)
+        assert abs(gi - oi) <= INERTIA_RTOL_MIXED * oi
+        second += rep["rows_second_pass"]
+        c = gc  # the GPU's own trajectory, which the fit below follows
+    assert second > 0
+    g = F.KMeans(k, dtype="f32x64").with_precision("fp8").with_max_iter(2).with_tol(0.0).with_n_init(1) \
+        .with_init_centers(w["init"]).fit(x32)
+    assert np.array_equal(g.cluster_centers(), gc) and g.n_iter() == 2
+    xp = w["x_predict"]
+    assert np.array_equal(g.predict(xp), O.predict(g.cluster_centers(), xp.astype(np.float64)))
+
+
 @pytest.mark.parametrize("precision", PRECISIONS)
 @pytest.mark.parametrize("scale", [1e-35, 1e-20, 1e15, 1e18])
 def test_mixed_extreme_scales_fall_back_exactly(precision, scale):
