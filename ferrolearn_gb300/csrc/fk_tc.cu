@@ -287,41 +287,43 @@ __device__ __forceinline__ void merge_res(uint32_t &R1, int &I1, uint32_t &R2, i
     }
 }
 
-// Ranks the 128 columns of one half of an accumulator block:
-// four interleaved top-2 chains (three float min/max per element on the keys,
-// which are positive floats), merged with the bound of the rest. A NaN score
-// (NaN row) is ignored by fminf/fmaxf; such rows have non-finite bound
-// ingredients and are always re-scored in full. Returns keys.
 // Key of one score: every score of the launch lies in [2^E, 2^(E+1)), so
 // (T + cgrid) - cgrid rounds it to a multiple of 128 ulp (its low 7 bits
-// become zero) and adding code * ulp writes the column code into those bits
-// exactly. Both steps run on the FMA pipe; keys are positive floats, so
-// their float and unsigned orders agree. Padded columns (T = 0) get tiny
-// keys; NaN scores (NaN rows) give NaN keys, ignored by the min/max below.
-template <int CODE>
-__device__ __forceinline__ float make_key(uint32_t bits, float cgrid, float ulp) {
-    const float t = __fsub_rn(__fadd_rn(__uint_as_float(bits), cgrid), cgrid);
-    return __fmaf_rn(ulp, (float)CODE, t);
-}
-
+// become zero) and adding code * ulp writes the column code (127 - the column
+// within the half) into those bits exactly. Both steps run on the FMA pipe;
+// keys are positive floats, so their float and unsigned orders agree. Padded
+// columns (T = 0) get tiny keys; NaN scores (NaN rows) give NaN keys, ignored
+// by fminf/fmaxf (such rows have non-finite bound ingredients and are always
+// re-scored in full).
+//
+// Four scores per step: their top-2 as a small tournament (the quad's second
+// is max3(loser of the final, loser of each pair): the winner's pair partner
+// or the other pair's best), then one merge into the running top-2. The same
+// 2.5 ALU operations per score as pairwise ranking, but the running chain
+// advances once per four scores, so more of each warp's work is independent.
 template <int CH, int E>
-__device__ __forceinline__ void rank_pair(const uint32_t (&r)[32], float cgrid, float ulp, float &a1, float &a2) {
-    // top-2 of {a1 >= a2, k0, k1}: a1' = max(a1, max(k0,k1)),
-    // a2' = max(min(a1, max(k0,k1)), a2, min(k0,k1))
-    // the grid rounding of both scores as two packed f32x2 operations
-    // (each half is an IEEE round-to-nearest f32 operation), then the codes
-    uint64_t p, cg2;
-    asm("mov.b64 %0, {%1, %2};" : "=l"(p) : "r"(r[E]), "r"(r[E + 1]));
+__device__ __forceinline__ void rank_quad(const uint32_t (&r)[32], float cgrid, float ulp, float &a1, float &a2) {
+    uint64_t p0, p1, cg2;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(p0) : "r"(r[E]), "r"(r[E + 1]));
+    asm("mov.b64 %0, {%1, %2};" : "=l"(p1) : "r"(r[E + 2]), "r"(r[E + 3]));
     asm("mov.b64 %0, {%1, %1};" : "=l"(cg2) : "f"(cgrid));
-    asm("add.rn.f32x2 %0, %0, %1;" : "+l"(p) : "l"(cg2));
-    asm("sub.rn.f32x2 %0, %0, %1;" : "+l"(p) : "l"(cg2));
-    float t0, t1;
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(t0), "=f"(t1) : "l"(p));
+    asm("add.rn.f32x2 %0, %0, %1;" : "+l"(p0) : "l"(cg2));
+    asm("add.rn.f32x2 %0, %0, %1;" : "+l"(p1) : "l"(cg2));
+    asm("sub.rn.f32x2 %0, %0, %1;" : "+l"(p0) : "l"(cg2));
+    asm("sub.rn.f32x2 %0, %0, %1;" : "+l"(p1) : "l"(cg2));
+    float t0, t1, t2, t3;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(t0), "=f"(t1) : "l"(p0));
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(t2), "=f"(t3) : "l"(p1));
     const float k0 = __fmaf_rn(ulp, (float)(127 - ((CH * 32 + E) & 127)), t0);
     const float k1 = __fmaf_rn(ulp, (float)(127 - ((CH * 32 + E + 1) & 127)), t1);
-    const float m = fmaxf(k0, k1), l = fminf(k0, k1);
-    a2 = fmax3(fminf(a1, m), a2, l);
-    a1 = fmaxf(a1, m);
+    const float k2 = __fmaf_rn(ulp, (float)(127 - ((CH * 32 + E + 2) & 127)), t2);
+    const float k3 = __fmaf_rn(ulp, (float)(127 - ((CH * 32 + E + 3) & 127)), t3);
+    const float m01 = fmaxf(k0, k1), l01 = fminf(k0, k1);
+    const float m23 = fmaxf(k2, k3), l23 = fminf(k2, k3);
+    const float M = fmaxf(m01, m23), L = fminf(m01, m23);
+    const float S = fmax3(L, l01, l23);
+    a2 = fmax3(fminf(a1, M), a2, S);
+    a1 = fmaxf(a1, M);
 }
 
 constexpr int NCH = 1;  // top-2 chains per rank pass (measured: 1 ~ 2 < 4 < 8 in time; the ALU pipe bounds it)
@@ -330,48 +332,14 @@ template <int CH, int E>
 struct RankChunk {
     static __device__ __forceinline__ void run(const uint32_t (&r)[32], float cg, float ulp, float (&a1)[NCH],
                                                float (&a2)[NCH]) {
-        rank_pair<CH, E>(r, cg, ulp, a1[(E >> 1) & (NCH - 1)], a2[(E >> 1) & (NCH - 1)]);
-        RankChunk<CH, E + 2>::run(r, cg, ulp, a1, a2);
+        rank_quad<CH, E>(r, cg, ulp, a1[(E >> 2) & (NCH - 1)], a2[(E >> 2) & (NCH - 1)]);
+        RankChunk<CH, E + 4>::run(r, cg, ulp, a1, a2);
     }
 };
 template <int CH>
 struct RankChunk<CH, 32> {
     static __device__ __forceinline__ void run(const uint32_t (&)[32], float, float, float (&)[NCH], float (&)[NCH]) {}
 };
-
-// Ranks the 128 columns of one half of an accumulator block:
-// NCH interleaved top-2 chains over the keys, two elements per step with a
-// three-input max, the next 32 columns loading from TMEM while the current
-// ones are ranked; then the chains are merged with the bound of the rest.
-// Returns keys; the low 7 bits of a key are 127 - (column within the half).
-// Both halves run the same code (the codes are local to the half), so the
-// eight epilogue warps share one copy of it in the instruction cache.
-__device__ __forceinline__ void rank_half(uint32_t col_addr, float cgrid, float ulp, uint32_t &b1, uint32_t &b2,
-                                          uint32_t &bu) {
-    float a1[NCH], a2[NCH];
-#pragma unroll
-    for (int q = 0; q < NCH; q++) a1[q] = a2[q] = 0.f;
-    uint32_t ra[32], rb[32];
-    tmem_ld32(col_addr, ra);
-    tmem_wait(ra);
-    tmem_ld32(col_addr + 32, rb);
-    RankChunk<0, 0>::run(ra, cgrid, ulp, a1, a2);
-    tmem_wait(rb);
-    tmem_ld32(col_addr + 64, ra);
-    RankChunk<1, 0>::run(rb, cgrid, ulp, a1, a2);
-    tmem_wait(ra);
-    tmem_ld32(col_addr + 96, rb);
-    RankChunk<2, 0>::run(ra, cgrid, ulp, a1, a2);
-    tmem_wait(rb);
-    RankChunk<3, 0>::run(rb, cgrid, ulp, a1, a2);
-    b1 = __float_as_uint(a1[0]);
-    b2 = __float_as_uint(a2[0]);
-    bu = b2;
-    int d1 = 0, d2 = 0;  // indices are carried inside the keys
-#pragma unroll
-    for (int qd = 1; qd < NCH; qd++)
-        merge_res(b1, d1, b2, d2, bu, __float_as_uint(a1[qd]), 0, __float_as_uint(a2[qd]), 0, __float_as_uint(a2[qd]));
-}
 
 // ------------------------------------------------ top-8 (second pass) --
 // Sorted insertion of key k into a[0] >= ... >= a[K-1] (2K - 1 min/max).
@@ -594,8 +562,18 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         MergeSlot<FP8> *merge = (MergeSlot<FP8> *)(smem + p.off_merge);
         const int slice0 = part * p.kp;  // the slice's first centre
         const float cgrid = p.stats->cgrid, ulp = p.stats->ulp;
+        const int64_t my_tiles = q < p.tiles ? (p.tiles - 1 - q) / tstride + 1 : 0;
+        const uint32_t items = (uint32_t)(my_tiles * p.nblocks);
         uint32_t item = 0, tile_it = 0;
         bool dead = false;
+        // Software pipeline across accumulator blocks: a block's buffer goes
+        // back to the MMA warp as soon as its last 32 columns are in
+        // registers, and the next block's first 32 columns start loading
+        // (when its MMAs have already committed) while those last columns
+        // are ranked, so the two warps of a sub-partition do not both wait
+        // on a fresh TMEM load at every block. pre: ra holds that load.
+        uint32_t ra[32], rb[32];
+        bool pre = false;
         for (int64_t t = q; t < p.tiles; t += tstride, tile_it++) {
             uint32_t R1 = 0u, R2 = 0u, U = 0u;
             int I1 = -1, I2 = -1;
@@ -609,11 +587,15 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             for (int b = 0; b < p.nblocks; b++, item++) {
                 const int buf = (int)(item & 1u);
                 const uint32_t aph = (item >> 1) & 1u;
-                if (!dead && !mbar_wait(bar_afull(buf), aph, abort_flag, p.err, 16ull)) dead = true;
-                dead = __any_sync(0xffffffffu, dead);  // warp-uniform, for the barriers below
-                if (dead) continue;
-                tc_fence_after();
                 const uint32_t col = lane_addr + (uint32_t)buf * BN + (uint32_t)half * 128u;
+                if (!pre) {
+                    if (!dead && !mbar_wait(bar_afull(buf), aph, abort_flag, p.err, 16ull)) dead = true;
+                    dead = __any_sync(0xffffffffu, dead);  // warp-uniform, for the barriers below
+                    if (dead) continue;
+                    tc_fence_after();
+                    tmem_ld32(col, ra);
+                }
+                pre = false;
                 if (p.dump && blockIdx.x == 0 && t == q) {
                     for (int ch = 0; ch < 4; ch++) {
                         uint32_t r[32];
@@ -624,11 +606,39 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                                 __uint_as_float(r[e]);
                     }
                 }
-                uint32_t b1, b2, bu;
-                rank_half(col, cg, ul, b1, b2, bu);
+                float a1[NCH], a2[NCH];
+#pragma unroll
+                for (int qd = 0; qd < NCH; qd++) a1[qd] = a2[qd] = 0.f;
+                tmem_wait(ra);
+                tmem_ld32(col + 32, rb);
+                RankChunk<0, 0>::run(ra, cg, ul, a1, a2);
+                tmem_wait(rb);
+                tmem_ld32(col + 64, ra);
+                RankChunk<1, 0>::run(rb, cg, ul, a1, a2);
+                tmem_wait(ra);
+                tmem_ld32(col + 96, rb);
+                RankChunk<2, 0>::run(ra, cg, ul, a1, a2);
+                tmem_wait(rb);
+                // every column of this block is in registers: release the buffer
                 tc_fence_before();
                 __syncwarp();
                 if (lane == 0) mbar_arrive(bar_aempty(buf));
+                if (item + 1 < items) {
+                    const int nbuf = (int)((item + 1) & 1u);
+                    const uint32_t naph = ((item + 1) >> 1) & 1u;
+                    if (__all_sync(0xffffffffu, mbar_try_wait(bar_afull(nbuf), naph))) {
+                        tc_fence_after();
+                        tmem_ld32(lane_addr + (uint32_t)nbuf * BN + (uint32_t)half * 128u, ra);
+                        pre = true;
+                    }
+                }
+                RankChunk<3, 0>::run(rb, cg, ul, a1, a2);
+                uint32_t b1 = __float_as_uint(a1[0]), b2 = __float_as_uint(a2[0]), bu = b2;
+                int d1 = 0, d2 = 0;  // indices are carried inside the keys
+#pragma unroll
+                for (int qd = 1; qd < NCH; qd++)
+                    merge_res(b1, d1, b2, d2, bu, __float_as_uint(a1[qd]), 0, __float_as_uint(a2[qd]), 0,
+                              __float_as_uint(a2[qd]));
                 const int base = part * p.kp + b * BN + half * 128 + 127;
                 merge_res(R1, I1, R2, I2, U, b1 & 0xFFFFFF80u, base - (int)(b1 & 0x7Fu), b2 & 0xFFFFFF80u,
                           base - (int)(b2 & 0x7Fu), bu & 0xFFFFFF80u);
@@ -660,6 +670,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                         Top2{__uint_as_float(R1), __uint_as_float(R2), __uint_as_float(U), 0.f, I1, I2, 0, 0};
             }
         }
+        if (pre) tmem_wait(ra);  // a load issued for an item that never ran completes before exit
     } else {
         const int ew = warp - 2;
         const int quarter = warp & 3;
