@@ -42,21 +42,44 @@ def test_validation_errors_before_any_device_work():
 @pytest.mark.gpu
 @pytest.mark.parametrize("precision", ["plain", "bf16"])
 def test_wrapper_fit_predict_transform_on_gpu(precision):
+    # against the FP64 oracle (the same k-means++ stream: run r seeded with
+    # random_state + r); bf16 reads X as f32, so X is made f32-exact first
     rng = np.random.default_rng(4)
     cen = rng.uniform(-10, 10, size=(5, 6))
     x = cen[rng.integers(0, 5, 1500)] + rng.normal(0, 1, size=(1500, 6))
     if precision != "plain":
         x = x.astype(np.float32).astype(np.float64)
     km = KMeans(n_clusters=5, n_init=3, random_state=11, precision=precision).fit(x)
-    ref = F.KMeans(5, dtype="f64").with_n_init(3).with_random_state(11).fit(x)
-    assert np.array_equal(km.labels_, ref.labels())
-    assert np.allclose(km.cluster_centers_, ref.cluster_centers(), rtol=1e-12, atol=0)
-    assert km.n_iter_ == ref.n_iter()
+    o = O.fit(x, 5, n_init=3, seed=11)
+    assert np.array_equal(km.labels_, o["labels"])
+    assert np.allclose(km.cluster_centers_, o["centers"], rtol=1e-13, atol=0)
+    assert km.n_iter_ == o["n_iter"]
+    assert abs(km.inertia_ - o["inertia"]) <= 1e-6 * o["inertia"]
     assert np.array_equal(km.predict(x), O.predict(km.cluster_centers_, x))
     assert np.allclose(km.transform(x[:20]), O.transform(km.cluster_centers_, x[:20]), rtol=1e-12, atol=1e-12)
     assert np.array_equal(km.fit_predict(x), km.labels_)
     km2 = pickle.loads(pickle.dumps(km))
     assert np.array_equal(km2.predict(x), km.predict(x))
+    # predict / transform validate like the reference wrapper (validate_data(reset=False))
+    with pytest.raises(ValueError, match="features"):
+        km.predict(x[:, :4])
+    with pytest.raises(ValueError):
+        km.transform(np.full((2, 6), np.nan))
+
+
+@pytest.mark.gpu
+def test_fit_predict_is_fit_then_predict_on_gpu():
+    # kmeans.rs:522-525: fit, then predict the same rows with the final
+    # centres; labels() is the assignment before the last update, so the two
+    # can differ when the run stops at max_iter
+    rng = np.random.default_rng(9)
+    x = rng.normal(size=(4000, 5)) * 3 + rng.integers(0, 7, size=(4000, 1))
+    km = F.KMeans(7).with_max_iter(2).with_tol(0.0).with_n_init(2).with_random_state(3)
+    got = km.fit_predict(x)
+    o = O.fit(x, 7, max_iter=2, tol=0.0, n_init=2, seed=3)
+    assert np.array_equal(got, O.predict(o["centers"], x))
+    assert not np.array_equal(got, o["labels"])  # the case where they differ
+
 
 
 def test_tensor_core_forms_read_float32_rows():
