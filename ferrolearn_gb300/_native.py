@@ -23,7 +23,7 @@ EXPORTS = [
     "fk_kmeans_predict_f64", "fk_kmeans_predict_f32", "fk_kmeans_predict_f32x64",
     "fk_kmeans_transform_f64", "fk_kmeans_transform_f32",
     "fk_kmeans_plus_plus_f64", "fk_kmeans_plus_plus_f32", "fk_debug_tc_probe",
-    "fk_debug_measure_peaks", "fk_kmeans_score_f64_noalloc", "fk_kmeans_fit_batched_f32", "fk_debug_tc_plan",
+    "fk_debug_measure_peaks", "fk_debug_measure_tc_peaks", "fk_kmeans_score_f64_noalloc", "fk_kmeans_fit_batched_f32", "fk_debug_tc_plan",
     "fk_minibatch_params_default", "fk_minibatch_fit_f64", "fk_minibatch_fit_f32", "fk_minibatch_batch_indices",
     "fk_bisecting_params_default", "fk_bisecting_fit_f64", "fk_bisecting_fit_f32",
 ]
@@ -175,6 +175,8 @@ def _declare(lib):
     lib.fk_debug_tc_probe.restype = st
     lib.fk_debug_measure_peaks.argtypes = [p, p]
     lib.fk_debug_measure_peaks.restype = st
+    lib.fk_debug_measure_tc_peaks.argtypes = [p, p]
+    lib.fk_debug_measure_tc_peaks.restype = st
     lib.fk_kmeans_score_f64_noalloc.argtypes = [p, i64, i64, p, i64, p, p, p]
     lib.fk_kmeans_score_f64_noalloc.restype = st
     lib.fk_kmeans_fit_batched_f32.argtypes = [p, C.POINTER(BatchProblem), i64, i32, C.POINTER(BatchReport)]

@@ -1352,6 +1352,19 @@ fk_status fk_kmeans_plus_plus_f64(fk_ctx *ctx, const double *x, int64_t n, int64
     return guarded(ctx, [&] { return fk::kpp_impl<double>(ctx, x, n, d, k, draws, n_draws, seed, out, used); });
 }
 
+fk_status fk_debug_measure_tc_peaks(fk_ctx *ctx, double *out) {
+    return guarded(ctx, [&] {
+        if (!out) {
+            fk::set_error("required pointer is NULL");
+            return FK_ERR_NULL_POINTER;
+        }
+        fk::Ctx &c = *reinterpret_cast<fk::Ctx *>(ctx);
+        c.bind();
+        fk::measure_tc_peaks(c, out);
+        return FK_OK;
+    });
+}
+
 fk_status fk_debug_measure_peaks(fk_ctx *ctx, double *out) {
     return guarded(ctx, [&] {
         fk::Ctx &c = *reinterpret_cast<fk::Ctx *>(ctx);

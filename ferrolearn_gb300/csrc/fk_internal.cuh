@@ -342,6 +342,8 @@ void launch_mixed_inertia(Ctx &ctx, const double *part, int64_t m, DevScalars *s
 // Tensor-core assignment (fk_tc.cu): plan, then one persistent launch that
 // writes one record per (slice, row): Top2 (topk 2) or Top8 (topk 8).
 void plan_tc(Ctx &ctx, MixedPlan &mp, int64_t n, int d, int k, bool fp8, int topk);
+// Dense BF16 (out[0]) and E4M3 (out[1]) flop/s of a tensor-core MMA loop (fk_tc.cu).
+void measure_tc_peaks(Ctx &ctx, double *out);
 // dump (tests only, nullable): raw accumulators of CTA 0's first tile.
 // n_dev (nullable): the row count is read there at launch (mp.n is then the
 // capacity). FP8 (mp.fp8): xaug is the per-row augmentation tensor (n x 16

@@ -34,6 +34,7 @@
 #include <cudaTypedefs.h>
 #include <cuda_bf16.h>
 
+#include <algorithm>
 #include <cstring>
 
 #include "fk_internal.cuh"
@@ -755,6 +756,69 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     }
 }
 
+// --------------------------------------------- tensor-core peak loop --
+// Dense tensor-core throughput of this GPU with the contraction's own MMA
+// shape: M=128, N=256, K=16 (BF16) or K=32 (E4M3) from 128-byte-swizzled
+// shared memory into a TMEM accumulator. One CTA per SM; one thread issues
+// iters x 4 MMAs back to back (one swizzle atom of K per iteration), commits
+// once and waits (bounded) for completion. The operands are fixed finite
+// patterns written by the threads (then made visible to the tensor core's
+// proxy); only the time matters.
+constexpr uint32_t PEAK_A_BYTES = BM * 128u, PEAK_B_BYTES = BN * 128u;
+
+template <bool FP8>
+__global__ void __launch_bounds__(128, 1) tc_peak_kernel(int iters, unsigned long long *err) {
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    const uint32_t sb = smem_u32(smem);
+    const uint32_t bar = sb + PEAK_A_BYTES + PEAK_B_BYTES;
+    uint32_t *slot = (uint32_t *)(smem + PEAK_A_BYTES + PEAK_B_BYTES + 64);
+    volatile uint32_t *abort_flag = slot + 1;
+    uint32_t *words = (uint32_t *)smem;
+    for (uint32_t i = threadIdx.x; i < (PEAK_A_BYTES + PEAK_B_BYTES) / 4; i += blockDim.x) {
+        const uint32_t v = (i * 2654435761u) >> 27;  // 0..31
+        // E4M3 bytes 0x30..0x3F (0.5 .. 0.94) or BF16 halves 0x3F80..0x3F9F (1.0 .. 1.24)
+        words[i] = FP8 ? 0x30303030u + v * 0x00010101u : (0x3F803F80u + (v << 16) + (v ^ 7u));
+    }
+    if (threadIdx.x == 0) {
+        mbar_init(bar, 1);
+        *abort_flag = 0u;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // the threads' stores, seen by the MMAs
+    if (threadIdx.x < 32) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(slot)),
+                     "r"(256u)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *slot;
+    if (threadIdx.x == 0) {
+        for (int it = 0; it < iters; it++) {
+#pragma unroll
+            for (int kk = 0; kk < 4; kk++) {
+                const uint64_t ad = sdesc(sb + kk * 32u, 1024u, LAYOUT_SW128);
+                const uint64_t bd = sdesc(sb + PEAK_A_BYTES + kk * 32u, 1024u, LAYOUT_SW128);
+                if (FP8)
+                    mma_fp8(tmem, ad, bd, (it | kk) != 0 ? 1u : 0u);
+                else
+                    mma_bf16(tmem, ad, bd, (it | kk) != 0 ? 1u : 0u);
+            }
+        }
+        mma_commit(bar);
+        mbar_wait(bar, 0u, abort_flag, err, 32ull);
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(256u) : "memory");
+    }
+}
+
 // ------------------------------------------------------------- host side --
 PFN_cuTensorMapEncodeTiled_v12000 get_encode(Ctx &ctx) {
     if (!ctx.tmap_fn) {
@@ -931,6 +995,49 @@ void launch_tc_assign(Ctx &ctx, MixedPlan &mp, const void *xb, const void *cb, c
         mp.xst == 2 ? go(tc_assign_kernel<2, false, 2>) : go(tc_assign_kernel<2, false, 1>);
     }
     FK_LAUNCH_CHECK();
+}
+
+
+// Dense BF16 and E4M3 flop/s of tc_peak_kernel (best of three timed launches
+// after one warm-up, CUDA events on the context's stream): out[0] BF16,
+// out[1] E4M3.
+void measure_tc_peaks(Ctx &ctx, double *out) {
+    unsigned long long *err = (unsigned long long *)ctx.get(BUF_OUT2, 64);
+    FK_CUDA(cudaMemsetAsync(err, 0, sizeof(unsigned long long), ctx.stream));
+    const size_t smem = PEAK_A_BYTES + PEAK_B_BYTES + 1024 + 128;
+    const int iters = 4096;
+    for (int fp8 = 0; fp8 < 2; fp8++) {
+        const void *fn = fp8 ? (const void *)tc_peak_kernel<true> : (const void *)tc_peak_kernel<false>;
+        FK_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        auto launch = [&](int it) {
+            if (fp8)
+                tc_peak_kernel<true><<<ctx.num_sms, 128, smem, ctx.stream>>>(it, err);
+            else
+                tc_peak_kernel<false><<<ctx.num_sms, 128, smem, ctx.stream>>>(it, err);
+            FK_LAUNCH_CHECK();
+        };
+        launch(64);
+        double best = 0.0;
+        for (int rep = 0; rep < 3; rep++) {
+            Events<2> ev;
+            FK_CUDA(cudaEventRecord(ev[0], ctx.stream));
+            launch(iters);
+            FK_CUDA(cudaEventRecord(ev[1], ctx.stream));
+            FK_CUDA(cudaEventSynchronize(ev[1]));
+            float ms = 0.f;
+            FK_CUDA(cudaEventElapsedTime(&ms, ev[0], ev[1]));
+            const double flops = (double)ctx.num_sms * iters * 4.0 * 2.0 * BM * BN * (fp8 ? 32.0 : 16.0);
+            best = std::max(best, flops / (ms * 1e-3));
+        }
+        out[fp8] = best;
+    }
+    unsigned long long h = 0;
+    FK_CUDA(cudaMemcpyAsync(&h, err, sizeof(h), cudaMemcpyDeviceToHost, ctx.stream));
+    FK_CUDA(cudaStreamSynchronize(ctx.stream));
+    if (h) {
+        set_error("the tensor-core peak loop's bounded wait gave up (code %llu)", h);
+        fail(FK_ERR_TIMEOUT);
+    }
 }
 
 }  // namespace fk

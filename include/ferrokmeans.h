@@ -371,6 +371,14 @@ fk_status fk_minibatch_batch_indices(uint64_t seed, int64_t pos, int64_t n, int6
  * add op/s, [4] FP64 add latency in cycles, [5] FP32 add latency. */
 fk_status fk_debug_measure_peaks(fk_ctx *ctx, double *out);
 
+/* Diagnostics (no reference counterpart): dense tensor-core throughput of
+ * this GPU measured with the contraction's own MMA shape (tcgen05.mma
+ * M=128 N=256 from 128-byte-swizzled shared memory into TMEM, one CTA per
+ * SM issuing back to back): out[0] BF16 (kind::f16, K=16) flop/s, out[1]
+ * E4M3 (kind::f8f6f4, K=32) flop/s. The roofline denominator of the FP8
+ * form, for which no library measurement exists. */
+fk_status fk_debug_measure_tc_peaks(fk_ctx *ctx, double *out);
+
 /* Diagnostics for the tests (no reference counterpart): one BF16 tensor-core
  * assignment pass of x (n*d f32, device memory) against c (k*d f64, device
  * memory), precision FK_PRECISION_MIXED_BF16 or _FP8. Returns the raw FP32

@@ -198,6 +198,7 @@ unsafe extern "C" {
     pub fn fk_minibatch_batch_indices(seed: u64, pos: i64, n: i64, batch_size: i64, iters: i64, out: *mut i64)
         -> i32;
     pub fn fk_debug_measure_peaks(ctx: *mut fk_ctx, out: *mut f64) -> i32;
+    pub fn fk_debug_measure_tc_peaks(ctx: *mut fk_ctx, out: *mut f64) -> i32;
     pub fn fk_debug_tc_probe(ctx: *mut fk_ctx, x_dev: *const f32, n: i64, d: i64, c_dev: *const f64, k: i64,
                              precision: i32, dump: *mut f32, xq: *mut c_void, cq: *mut c_void, aug: *mut u16,
                              xaug: *mut u16, top: *mut c_void, plan: *mut i32) -> i32;
