@@ -71,7 +71,8 @@ def parse(argv=None):
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--form", default="auto", choices=["auto", "bf16", "fp8", "fp32", "fp64"])
-    ap.add_argument("--workload", default="anisotropic", choices=["anisotropic", "bisector", "dirichlet", "batched"])
+    ap.add_argument("--workload", default="anisotropic",
+                    choices=["anisotropic", "bisector", "dirichlet", "batched", "minibatch", "bisecting"])
     ap.add_argument("--scale", type=float, default=1.0, help="fraction of the full row count")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true")
@@ -81,7 +82,8 @@ def parse(argv=None):
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     args = ap.parse_args(argv)
     if args.steps is None:  # the configurations' own iteration counts (anisotropic: 50 Lloyd iterations)
-        args.steps = {"anisotropic": 50, "bisector": 20, "dirichlet": 20, "batched": 20}[args.workload]
+        args.steps = {"anisotropic": 50, "bisector": 20, "dirichlet": 20, "batched": 20, "minibatch": 100,
+                      "bisecting": 3}[args.workload]
     return args
 
 
@@ -442,6 +444,138 @@ def run_batched(args):
     print(json.dumps(out))
 
 
+def _timed_calls(stream, fn, reps):
+    """Device time (CUDA events on the library's stream) of `reps` calls of fn."""
+    import torch
+    times, out = [], None
+    for _ in range(reps):
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        out = fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        times.append(a.elapsed_time(b))
+    return float(np.sum(times)), out
+
+
+def run_minibatch(args):
+    """MiniBatchKMeans::fit (mini_batch_kmeans.rs:492-591) on the GPU: n =
+    1,000,000 x d = 64, k = 256 (the Dirichlet blob mixture), batch 1024, one
+    run from the first k rows of a seeded permutation, tol 0; a step is one
+    mini-batch iteration; the timed fit includes its final assignment of all
+    n rows (assign_clusters_mb, :343-376)."""
+    import torch
+
+    import ferrolearn_gb300 as F
+    from ferrolearn_gb300 import _native
+    from ferrolearn_gb300 import workloads as W
+    dev = torch.cuda.current_device()
+    w = W.dirichlet_256x64(scale=args.scale, dtype=np.float64)
+    x, k = w["x"], w["k"]
+    n, d = x.shape
+    init = x[np.random.default_rng(1).permutation(n)[:k]][None].copy()
+    stream = torch.cuda.Stream()
+    ctx = F.Context(dev, stream=stream.cuda_stream)
+    xd = torch.from_numpy(x).to(dev)
+
+    def model(iters):
+        return F.MiniBatchKMeans(k).with_batch_size(1024).with_max_iter(iters).with_n_init(1).with_tol(0.0) \
+            .with_init_centers(init)
+    model(args.warmup).fit(xd, ctx=ctx)
+    l0 = _native.lib().fk_debug_launch_count()
+    with ClockSampler(dev) as clocks:
+        clocks.mark_start()
+        ms, fitted = _timed_calls(stream, lambda: model(args.steps).fit(xd, ctx=ctx), 1)
+        clocks.mark_end()
+    launches = int(_native.lib().fk_debug_launch_count() - l0)
+    # the final assignment of all rows alone (the fit's fixed part)
+    c = fitted.cluster_centers()
+    ms_assign, _ = _timed_calls(stream, lambda: F.FittedKMeans(c, None, 0.0, 0, "f64").predict(xd, ctx=ctx), 1)
+    out = {"metric": "MiniBatchKMeans mini-batch iterations/s", "value": args.steps / (ms / 1e3), "unit": "iters/s",
+           "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "form": "minibatch",
+           "config": {"workload": "minibatch_dirichlet_256x64", "n": n, "d": d, "k": k, "batch_size": 1024,
+                      "n_init": 1, "tol": 0.0, "init": "first k rows of a seeded permutation",
+                      "l2": f"inputs larger than L2 (X {x.nbytes / 1e9:.2f} GB)", "parallelism": "replicas"},
+           "fit_ms": ms, "final_assignment_ms": ms_assign,
+           "ms_per_minibatch_iteration": (ms - ms_assign) / args.steps,
+           "gpu_launches": launches, "launches_per_iteration": launches / args.steps, "clocks": clocks.summary(),
+           "roofline": {"bound": "latency", "achieved": None, "peak": None, "unit": None, "frac": None,
+                        "traffic": None,
+                        "note": "a mini-batch iteration is four small launches (gather 1024 rows, their direct-form "
+                                "assignment, the in-order centre update, the shift); profiles/ has the launch list"}}
+    if not args.no_e2e:
+        t0 = time.perf_counter()
+        f2 = model(args.steps).fit(x, ctx=ctx)
+        t1 = time.perf_counter()
+        out["e2e"] = {"value": f2.n_iter() / (t1 - t0), "unit": "iters/s", "h2d_bytes_per_step": x.nbytes / args.steps,
+                      "d2h_bytes_per_step": (n * 8 + k * d * 8) / args.steps,
+                      "note": "one fit call on a host X running K mini-batch iterations"}
+    if not args.no_cpu:
+        from oracle import oracle as O
+        t0 = time.perf_counter()
+        O.minibatch_fit(x, k, batch_size=1024, max_iter=args.steps, n_init=1, init_centers=init)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": args.steps / dt, "unit": "iters/s", "cores": os.cpu_count() or 1,
+                               "cpu_model": cpu_model(), "kind": "port",
+                               "sample": f"the same fit ({args.steps} mini-batch iterations and the final "
+                                         "assignment of all rows)"}
+    print(json.dumps(out), flush=True)
+    ctx.close()
+
+
+def run_bisecting(args):
+    """BisectingKMeans::fit (bisecting_kmeans.rs:326-505) on the GPU: n =
+    200,000 x d = 16, target k = 32 (a 32-blob Dirichlet mixture), n_init 10,
+    max_iter 300, LargestCluster; a step is one whole fit."""
+    import torch
+
+    import ferrolearn_gb300 as F
+    from ferrolearn_gb300 import _native
+    from ferrolearn_gb300 import workloads as W
+    dev = torch.cuda.current_device()
+    w = W.dirichlet_256x64(scale=0.2 * args.scale, k=32, d=16, dtype=np.float64)
+    x, k = w["x"], w["k"]
+    n, d = x.shape
+    stream = torch.cuda.Stream()
+    ctx = F.Context(dev, stream=stream.cuda_stream)
+    xd = torch.from_numpy(x).to(dev)
+
+    def fit():
+        return F.BisectingKMeans(k).with_n_init(10).with_random_state(0).fit(xd, ctx=ctx)
+    for _ in range(max(1, args.warmup)):
+        fit()
+    l0 = _native.lib().fk_debug_launch_count()
+    with ClockSampler(dev) as clocks:
+        clocks.mark_start()
+        ms, _ = _timed_calls(stream, fit, args.steps)
+        clocks.mark_end()
+    launches = int(_native.lib().fk_debug_launch_count() - l0)
+    out = {"metric": "BisectingKMeans fits/s", "value": args.steps / (ms / 1e3), "unit": "fits/s", "n_gpus": 1,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "form": "bisecting",
+           "config": {"workload": "bisecting_dirichlet_32x16", "n": n, "d": d, "k": k, "n_init": 10,
+                      "max_iter": 300, "strategy": "largest_cluster", "random_state": 0,
+                      "l2": "inputs smaller than L2 (X 25.6 MB, re-read by every 2-means iteration)",
+                      "parallelism": "replicas"},
+           "gpu_launches": launches, "launches_per_fit": launches / args.steps, "clocks": clocks.summary(),
+           "roofline": {"bound": "latency", "achieved": None, "peak": None, "unit": None, "frac": None,
+                        "traffic": None,
+                        "note": "hundreds of small launches per fit with a host round trip per 2-means iteration; "
+                                "profiles/ has the launch list"}}
+    if not args.no_cpu:
+        from oracle import oracle as O
+        t0 = time.perf_counter()
+        O.bisecting_fit(x, k, n_init=10, seed=0)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": 1.0 / dt, "unit": "fits/s", "cores": 1, "cpu_model": cpu_model(),
+                               "kind": "port", "sample": "one whole fit (the reference's serial 2-means)"}
+    print(json.dumps(out), flush=True)
+    ctx.close()
+
+
 def parity_leg(w, form, ctx, xd, iters, rows, fit_centres, fit_labels):
     """The timed trajectory replayed one Lloyd step at a time (the same
     entry point's single-iteration form, the same centres), each step checked
@@ -516,6 +650,10 @@ def parity_leg(w, form, ctx, xd, iters, rows, fit_centres, fit_labels):
 def run_ours(args):
     if args.workload == "batched":
         return run_batched(args)
+    if args.workload == "minibatch":
+        return run_minibatch(args)
+    if args.workload == "bisecting":
+        return run_bisecting(args)
     import torch
 
     import ferrolearn_gb300 as F

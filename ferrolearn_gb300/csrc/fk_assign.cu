@@ -7,6 +7,7 @@
 // the lowest index among equal distances and only accepts distances strictly
 // below F::MAX, which is nearest_center's strict `<` from F::max_value()
 // (kmeans.rs:295-309) for any visiting order.
+#include <algorithm>
 #include <cfloat>
 
 #include "fk_internal.cuh"
@@ -44,10 +45,19 @@ __device__ __forceinline__ bool better(T dv, int di, T bv, int bi) {
     return dv < bv || (dv == bv && di < bi);
 }
 
+// Centres [y * c_per, min(k, (y + 1) * c_per)) of split y = blockIdx.y
+// against 64-row tiles (blockIdx.x); with part_v set, each split writes
+// each row's best (distance,
+// index) of its range to part_v / part_i[blockIdx.y * n + row] (index
+// INT32_MAX: none below F::MAX) for assign_combine_kernel, else the labels
+// and minimum distances directly.
 template <typename TX, typename TC, bool WRITE_ALL>
 __global__ void __launch_bounds__(NT)
 assign_direct_kernel(const TX *__restrict__ x, int64_t n, int d, const TC *__restrict__ c, int k,
-                     int32_t *__restrict__ labels, TC *__restrict__ mind, TC *__restrict__ out) {
+                     int32_t *__restrict__ labels, TC *__restrict__ mind, TC *__restrict__ out, int c_per,
+                     TC *__restrict__ part_v, int32_t *__restrict__ part_i) {
+    const int c_begin = (int)blockIdx.y * c_per;
+    const int c_end = min(k, c_begin + c_per);
     using A = Arith<TC>;
     __shared__ __align__(16) TC xs[DJ][BM];
     __shared__ __align__(16) TC cs[DJ][BN];
@@ -62,7 +72,7 @@ assign_direct_kernel(const TX *__restrict__ x, int64_t n, int d, const TC *__res
 #pragma unroll
     for (int a = 0; a < TM; a++) { best_v[a] = A::maxv(); best_i[a] = INT32_MAX; }
 
-    for (int ct = 0; ct < k; ct += BN) {
+    for (int ct = c_begin; ct < c_end; ct += BN) {
         TC acc[TM][TN];
 #pragma unroll
         for (int a = 0; a < TM; a++)
@@ -78,7 +88,7 @@ assign_direct_kernel(const TX *__restrict__ x, int64_t n, int d, const TC *__res
                 int gj = j0 + jj;
                 xs[jj][r] = (gr < n && gj < d) ? (TC)x[gr * d + gj] : TC(0);
                 int gc = ct + r;
-                cs[jj][r] = (gc < k && gj < d) ? c[(int64_t)gc * d + gj] : TC(0);
+                cs[jj][r] = (gc < c_end && gj < d) ? c[(int64_t)gc * d + gj] : TC(0);
             }
             __syncthreads();
             const int jn = min(DJ, d - j0);
@@ -105,7 +115,7 @@ assign_direct_kernel(const TX *__restrict__ x, int64_t n, int d, const TC *__res
 #pragma unroll
             for (int b = 0; b < TN; b++) {
                 int gc = ct + tx * TN + b;
-                if (gc < k) {
+                if (gc < c_end) {
                     TC v = acc[a][b];
                     if (WRITE_ALL) {
                         if (gr < n) out[gr * k + gc] = A::root(v);
@@ -132,11 +142,39 @@ assign_direct_kernel(const TX *__restrict__ x, int64_t n, int d, const TC *__res
         }
         int64_t gr = row0 + ty * TM + a;
         if (tx == 0 && gr < n) {
+            if (part_v) {
+                part_v[(int64_t)blockIdx.y * n + gr] = v;
+                part_i[(int64_t)blockIdx.y * n + gr] = i;
+                continue;
+            }
             if (i == INT32_MAX) { i = 0; v = A::maxv(); }  // nothing below F::MAX
             labels[gr] = i;
             if (mind) mind[gr] = v;
         }
     }
+}
+
+// The splits' bests of each row in split order, lexicographic (distance,
+// index): the lowest index among equal minima, as one pass over every centre.
+template <typename TC>
+__global__ void assign_combine_kernel(const TC *__restrict__ part_v, const int32_t *__restrict__ part_i, int splits,
+                                      int64_t n, int32_t *__restrict__ labels, TC *__restrict__ mind) {
+    using A = Arith<TC>;
+    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    TC v = A::maxv();
+    int i = INT32_MAX;
+    for (int q = 0; q < splits; q++) {
+        const TC pv = part_v[(int64_t)q * n + r];
+        const int pi = part_i[(int64_t)q * n + r];
+        if (pi != INT32_MAX && better(pv, pi, v, i)) {
+            v = pv;
+            i = pi;
+        }
+    }
+    if (i == INT32_MAX) { i = 0; v = A::maxv(); }
+    labels[r] = i;
+    if (mind) mind[r] = v;
 }
 
 // ---------------------------------------------------------- fixed sums --
@@ -196,7 +234,35 @@ void launch_assign_direct(const TX *x, int64_t n, int d, const TC *c, int k, int
                           TC *mind, cudaStream_t s) {
     if (n == 0) return;
     dim3 grid((unsigned)((n + BM - 1) / BM));
-    assign_direct_kernel<TX, TC, false><<<grid, NT, 0, s>>>(x, n, d, c, k, labels, mind, nullptr);
+    assign_direct_kernel<TX, TC, false><<<grid, NT, 0, s>>>(x, n, d, c, k, labels, mind, nullptr, k, nullptr,
+                                                            nullptr);
+    FK_LAUNCH_CHECK();
+}
+
+int assign_splits(int64_t n, int k, int num_sms) {
+    const int64_t tiles = (n + BM - 1) / BM;
+    const int64_t want = (2 * (int64_t)num_sms + tiles - 1) / tiles;  // about two CTAs per SM
+    const int64_t most = (k + BN - 1) / BN;
+    return (int)std::max<int64_t>(1, std::min(want, most));
+}
+
+template <typename TX, typename TC>
+void launch_assign_direct_split(const TX *x, int64_t n, int d, const TC *c, int k, int32_t *labels, TC *mind,
+                                int splits, TC *part_v, int32_t *part_i, cudaStream_t s) {
+    if (n == 0) return;
+    if (splits <= 1) {
+        launch_assign_direct<TX, TC>(x, n, d, c, k, labels, mind, s);
+        return;
+    }
+    // split q takes whole 64-centre tiles [q * per, (q + 1) * per)
+    const int tiles_k = (k + BN - 1) / BN;
+    const int per = (tiles_k + splits - 1) / splits * BN;
+    const int used = (k + per - 1) / per;
+    dim3 grid((unsigned)((n + BM - 1) / BM), (unsigned)used);
+    assign_direct_kernel<TX, TC, false><<<grid, NT, 0, s>>>(x, n, d, c, k, nullptr, nullptr, nullptr, per, part_v,
+                                                            part_i);
+    FK_LAUNCH_CHECK();
+    assign_combine_kernel<TC><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(part_v, part_i, used, n, labels, mind);
     FK_LAUNCH_CHECK();
 }
 
@@ -205,7 +271,7 @@ void launch_transform_direct(const T *x, int64_t n, int d, const T *c, int k, T 
                              cudaStream_t s) {
     if (n == 0) return;
     dim3 grid((unsigned)((n + BM - 1) / BM));
-    assign_direct_kernel<T, T, true><<<grid, NT, 0, s>>>(x, n, d, c, k, nullptr, nullptr, out);
+    assign_direct_kernel<T, T, true><<<grid, NT, 0, s>>>(x, n, d, c, k, nullptr, nullptr, out, k, nullptr, nullptr);
     FK_LAUNCH_CHECK();
 }
 
@@ -247,6 +313,10 @@ template void launch_assign_direct<float, float>(const float *, int64_t, int, co
                                                  int32_t *, float *, cudaStream_t);
 template void launch_assign_direct<float, double>(const float *, int64_t, int, const double *, int,
                                                   int32_t *, double *, cudaStream_t);
+template void launch_assign_direct_split<double, double>(const double *, int64_t, int, const double *, int,
+                                                         int32_t *, double *, int, double *, int32_t *, cudaStream_t);
+template void launch_assign_direct_split<float, float>(const float *, int64_t, int, const float *, int, int32_t *,
+                                                       float *, int, float *, int32_t *, cudaStream_t);
 template void launch_transform_direct<double>(const double *, int64_t, int, const double *, int,
                                               double *, cudaStream_t);
 template void launch_transform_direct<float>(const float *, int64_t, int, const float *, int, float *,

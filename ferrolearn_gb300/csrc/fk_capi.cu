@@ -805,6 +805,10 @@ fk_status minibatch_impl(fk_ctx *ctxp, const T *x_in, int64_t n, int64_t d, cons
     int32_t *didx = (int32_t *)ctx.get(BUF_MB_IDX, sizeof(int32_t) * (size_t)std::max(m * chunk, k));
     T *xb = (T *)ctx.get(BUF_MB_XB, sizeof(T) * (size_t)m * d);
     int32_t *blab = (int32_t *)ctx.get(BUF_MB_LAB, sizeof(int32_t) * (size_t)m);
+    // a batch is too few rows to fill the GPU by row tiles: split the centres too
+    const int splits = assign_splits(m, (int)k, ctx.num_sms);
+    T *part_v = splits > 1 ? (T *)ctx.get(BUF_MB_PARTV, sizeof(T) * (size_t)splits * m) : nullptr;
+    int32_t *part_i = splits > 1 ? (int32_t *)ctx.get(BUF_MB_PARTI, sizeof(int32_t) * (size_t)splits * m) : nullptr;
     std::vector<int32_t> hidx;
     std::unordered_map<int64_t, int64_t> moved;
     std::vector<int64_t> pool;
@@ -848,7 +852,7 @@ fk_status minibatch_impl(fk_ctx *ctxp, const T *x_in, int64_t n, int64_t d, cons
             FK_CUDA(cudaMemcpyAsync(didx, hidx.data(), sizeof(int32_t) * (size_t)(ci * m), cudaMemcpyHostToDevice, s));
             for (int64_t q = 0; q < ci; q++) {
                 launch_gather_rows<T>(x, (int)d, didx + q * m, m, xb, s);
-                launch_assign_direct<T, T>(xb, m, (int)d, c, (int)k, blab, nullptr, s);
+                launch_assign_direct_split<T, T>(xb, m, (int)d, c, (int)k, blab, nullptr, splits, part_v, part_i, s);
                 launch_minibatch_update<T>(xb, blab, m, (int)d, (int)k, c, old, counts, &sc->shift_bits, s);
                 n_iter += 1;
                 if (tol > T(0)) {

@@ -136,7 +136,7 @@ enum BufSlot {
     BUF_XB2, BUF_TOP8, BUF_OCT, BUF_EX, BUF_XAUG, BUF_ROWSCALE, BUF_ROWINFO2, BUF_STATS2, BUF_CB2, BUF_CAUG2,
     BUF_HALF2, BUF_INERTIA2, BUF_C2, BUF_XSTATE, BUF_XCOUNTS, BUF_MOVED, BUF_MOVED_ENT, BUF_MOVED_HIST, BUF_MOVED_TMP,
     BUF_CSPLIT, BUF_RINERT, BUF_F64ITEMS, BUF_INIT,
-    BUF_MB_IDX, BUF_MB_XB, BUF_MB_LAB, BUF_MB_OLD, BUF_MB_COUNTS,
+    BUF_MB_IDX, BUF_MB_XB, BUF_MB_LAB, BUF_MB_OLD, BUF_MB_COUNTS, BUF_MB_PARTV, BUF_MB_PARTI,
     BUF_BK_PERM, BUF_BK_LAB, BUF_BK_CEN, BUF_BK_DIST, BUF_BK_FLAGS, BUF_BK_SCRATCH, BUF_BK_CENTRES, BUF_BK_SEG,
     BUF_BK_FOLD, BUF_BK_LABELS,
     BUF_BX, BUF_BFITS, BUF_BSTATE, BUF_BITEMS, BUF_BPART, BUF_BORDER, BUF_BCTR, BUF_BLAB, BUF_BMEM, BUF_BCEN, BUF_BND, BUF_BXOFF,
@@ -231,6 +231,13 @@ template <typename TX, typename TC>
 void launch_assign_direct(const TX *x, int64_t n, int d, const TC *c, int k, int32_t *labels,
                           TC *mind, cudaStream_t s);
 // Transform (kmeans.rs:568-617): out[i*k+c] = sqrt(direct distance).
+// The assignment with the centres split over `splits` CTA columns (for row
+// counts too small to fill the GPU), then an ordered combine: the same labels
+// and minima as launch_assign_direct. Scratch: splits x n of each.
+int assign_splits(int64_t n, int k, int num_sms);
+template <typename TX, typename TC>
+void launch_assign_direct_split(const TX *x, int64_t n, int d, const TC *c, int k, int32_t *labels, TC *mind,
+                                int splits, TC *part_v, int32_t *part_i, cudaStream_t s);
 template <typename T>
 void launch_transform_direct(const T *x, int64_t n, int d, const T *c, int k, T *out,
                              cudaStream_t s);
