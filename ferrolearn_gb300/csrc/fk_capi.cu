@@ -974,6 +974,36 @@ fk_status bisecting_impl(fk_ctx *ctxp, const T *x_in, int64_t n, int64_t d, cons
     int64_t *seg = (int64_t *)ctx.get(BUF_BK_SEG, sizeof(int64_t) * (2 * (size_t)k + 2));
     int64_t *m0_dev = seg + 2 * k;
     T *fold = (T *)ctx.get(BUF_BK_FOLD, sizeof(T) * (size_t)std::max(runs, 2));
+    // The reference's row-order sums (the 2-means centres and the SSEs) as
+    // exact parallel folds (fk_fold.cu): chains [0, runs * 2 * d) are the
+    // centre sums of the current segment (rows gathered into xseg), the next
+    // runs + 2 the SSE folds.
+    T *xseg = (T *)ctx.get(BUF_BK_XSEG, sizeof(T) * (size_t)n * d);
+    const size_t nsum = (size_t)runs * 2 * d;
+    FoldChain *dchains = (FoldChain *)ctx.get(BUF_BK_CHAINS, sizeof(FoldChain) * (nsum + runs + 2));
+    T *fres = (T *)ctx.get(BUF_BK_FRES, sizeof(T) * (nsum + 8));
+    long long *fcnt = (long long *)ctx.get(BUF_BK_FCNT, sizeof(long long) * (nsum + runs + 8));
+    std::vector<FoldChain> hchains;
+    auto upload_sum_chains = [&](const T *rows, int nr, bool gated) {
+        hchains.assign((size_t)nr * 2 * d, FoldChain{});
+        for (int r = 0; r < nr; r++)
+            for (int side = 0; side < 2; side++)
+                for (int64_t j = 0; j < d; j++)
+                    hchains[((size_t)r * 2 + side) * d + j] =
+                        FoldChain{rows + j, d, lab + (size_t)r * n, side, gated ? r : -1};
+        FK_CUDA(cudaMemcpyAsync(dchains, hchains.data(), sizeof(FoldChain) * hchains.size(), cudaMemcpyHostToDevice,
+                                s));
+    };
+    // folds of `cnt` distance arrays (base + c * stride, optionally masked by
+    // label == c) into fold[0 .. cnt)
+    auto sse_folds = [&](const T *base, int64_t stride, const uint8_t *mask, int cnt, int64_t m) {
+        hchains.assign((size_t)cnt, FoldChain{});
+        for (int c = 0; c < cnt; c++)
+            hchains[(size_t)c] = FoldChain{base + (size_t)c * stride, 1, mask, mask ? c : 0, -1};
+        FK_CUDA(cudaMemcpyAsync(dchains + nsum, hchains.data(), sizeof(FoldChain) * (size_t)cnt,
+                                cudaMemcpyHostToDevice, s));
+        run_exact_folds<T>(ctx, dchains + nsum, cnt, m, nullptr, fold, fcnt + nsum);
+    };
     {
         std::vector<int32_t> iota((size_t)n);
         for (int64_t i = 0; i < n; i++) iota[(size_t)i] = (int32_t)i;
@@ -983,9 +1013,11 @@ fk_status bisecting_impl(fk_ctx *ctxp, const T *x_in, int64_t n, int64_t d, cons
     // compute_cluster_stats of every row (:192-222): the centre (sums / F::from(n)) and the SSE
     std::vector<T> hfold((size_t)std::max(runs, 2));
     FK_CUDA(cudaMemsetAsync(lab, 0, (size_t)n, s));
-    launch_bk_sums<T>(x, (int)d, perm, n, lab, n, cen, nullptr, 1, true, s);
+    upload_sum_chains(x, 1, false);  // every row, in row order (the permutation is the identity)
+    run_exact_folds<T>(ctx, dchains, (int)(2 * d), n, nullptr, fres, fcnt);
+    launch_bk_centres<T>(fres, fcnt, 1, (int)d, nullptr, true, n, cen, s);
     launch_bk_dist<T>(x, (int)d, perm, n, cen, lab, n, dist, n, 1, s);
-    launch_bk_fold<T>(dist, n, nullptr, n, 1, false, fold, s);
+    sse_folds(dist, n, nullptr, 1, n);
     FK_CUDA(cudaMemcpyAsync(centres, cen, sizeof(T) * (size_t)d, cudaMemcpyDeviceToDevice, s));
     FK_CUDA(cudaMemcpyAsync(hfold.data(), fold, sizeof(T), cudaMemcpyDeviceToHost, s));
     FK_CUDA(cudaStreamSynchronize(s));
@@ -1031,6 +1063,8 @@ fk_status bisecting_impl(fk_ctx *ctxp, const T *x_in, int64_t n, int64_t d, cons
         FK_CUDA(cudaMemcpyAsync(picks, hpicks.data(), sizeof(int) * 2 * (size_t)runs, cudaMemcpyHostToDevice, s));
         FK_CUDA(cudaMemcpyAsync(active, hact.data(), sizeof(int) * (size_t)runs, cudaMemcpyHostToDevice, s));
         launch_bk_pick<T>(x, (int)d, segp, picks, runs, cen, s);
+        launch_gather_rows<T>(x, (int)d, segp, m, xseg, s);
+        upload_sum_chains(xseg, runs, true);
         FK_CUDA(cudaMemset2DAsync(lab, (size_t)n, 0, (size_t)m, (size_t)runs, s));
         int nact = runs;
         for (int64_t it = 0; it < p->max_iter && nact > 0; it++) {
@@ -1045,11 +1079,12 @@ fk_status bisecting_impl(fk_ctx *ctxp, const T *x_in, int64_t n, int64_t d, cons
                 }
             if (nact == 0) break;
             FK_CUDA(cudaMemcpyAsync(active, hact.data(), sizeof(int) * (size_t)runs, cudaMemcpyHostToDevice, s));
-            launch_bk_sums<T>(x, (int)d, segp, m, lab, n, cen, active, runs, false, s);
+            run_exact_folds<T>(ctx, dchains, (int)nsum, m, active, fres, fcnt);
+            launch_bk_centres<T>(fres, fcnt, runs, (int)d, active, false, m, cen, s);
         }
         // each run's SSE against its final centres (:300-309)
         launch_bk_dist<T>(x, (int)d, segp, m, cen, lab, n, dist, n, runs, s);
-        launch_bk_fold<T>(dist, n, nullptr, m, runs, false, fold, s);
+        sse_folds(dist, n, nullptr, runs, m);
         FK_CUDA(cudaMemcpyAsync(hfold.data(), fold, sizeof(T) * (size_t)runs, cudaMemcpyDeviceToHost, s));
         FK_CUDA(cudaStreamSynchronize(s));
         int best = -1;
@@ -1066,7 +1101,7 @@ fk_status bisecting_impl(fk_ctx *ctxp, const T *x_in, int64_t n, int64_t d, cons
         }
         const uint8_t *blab = lab + (size_t)best * n;
         // the children's SSEs (:443-463), then their rows (:430-441)
-        launch_bk_fold<T>(dist + (size_t)best * n, 0, blab, m, 2, true, fold, s);
+        sse_folds(dist + (size_t)best * n, 0, blab, 2, m);
         launch_bk_partition(segp, blab, m, scratch, m0_dev, s);
         int64_t m0 = 0;
         FK_CUDA(cudaMemcpyAsync(hfold.data(), fold, sizeof(T) * 2, cudaMemcpyDeviceToHost, s));

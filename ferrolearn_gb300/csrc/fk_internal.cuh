@@ -114,6 +114,8 @@ struct MixedPlan {
     int grid = 0;
     int topk = 2;         // epilogue records: 2 (Top2, main pass) or 8 (Top8, second pass)
     int xst = 2;          // depth of the X tile ring (1 when two stages leave no room for 256 centres)
+    int ep = 2;           // epilogue parts per TMEM lane quarter (4 x ep epilogue warps)
+    int slots = 3;        // rotating tile-merge slots of the top-2 pass
     size_t smem = 0;
     const void *x = nullptr;
     double mu_norm = 0.0;
@@ -138,7 +140,8 @@ enum BufSlot {
     BUF_CSPLIT, BUF_RINERT, BUF_F64ITEMS, BUF_INIT,
     BUF_MB_IDX, BUF_MB_XB, BUF_MB_LAB, BUF_MB_OLD, BUF_MB_COUNTS, BUF_MB_PARTV, BUF_MB_PARTI,
     BUF_BK_PERM, BUF_BK_LAB, BUF_BK_CEN, BUF_BK_DIST, BUF_BK_FLAGS, BUF_BK_SCRATCH, BUF_BK_CENTRES, BUF_BK_SEG,
-    BUF_BK_FOLD, BUF_BK_LABELS,
+    BUF_BK_FOLD, BUF_BK_LABELS, BUF_BK_XSEG, BUF_BK_CHAINS, BUF_BK_FRES, BUF_BK_FCNT, BUF_FOLD_SUM, BUF_FOLD_CNT,
+    BUF_FOLD_MAP,
     BUF_BX, BUF_BFITS, BUF_BSTATE, BUF_BITEMS, BUF_BPART, BUF_BORDER, BUF_BCTR, BUF_BLAB, BUF_BMEM, BUF_BCEN, BUF_BND, BUF_BXOFF,
     BUF_COUNT
 };
@@ -324,6 +327,10 @@ void launch_bk_dist(const T *x, int d, const int32_t *perm, int64_t m, const T *
 template <typename T>
 void launch_bk_fold(const T *dist, int64_t dist_stride, const uint8_t *lab, int64_t m, int nsum, bool by_label, T *out,
                     cudaStream_t s);
+// Centres from the exact folds of chains (run * 2 + side) * d + feature.
+template <typename T>
+void launch_bk_centres(const T *sums, const long long *counts, int runs, int d, const int *active, bool whole,
+                       int64_t m, T *cen, cudaStream_t s);
 size_t bk_partition_scratch_ints(int64_t m);
 void launch_bk_partition(int32_t *seg, const uint8_t *lab, int64_t m, int32_t *scratch, int64_t *m0, cudaStream_t s);
 void launch_bk_labels(const int32_t *perm, const int64_t *seg, int nclusters, int64_t *labels, cudaStream_t s);
@@ -331,6 +338,22 @@ template <typename TS, typename TD>
 void launch_convert(const TS *src, int64_t count, TD *dst, cudaStream_t s);
 
 // k-means++ (kmeans.rs:169-253).
+// One sequential left fold in F per chain, exactly as the loop
+// `acc = acc + v` from zero in index order (fk_fold.cu): chain c folds
+// base[i * stride] over i in [0, m) where mask is null or mask[i] == mval,
+// and is skipped when active_slot >= 0 and active[active_slot] == 0. chains
+// is device memory; result[c] receives the fold, count[c] the values folded.
+struct FoldChain {
+    const void *base;
+    int64_t stride;
+    const uint8_t *mask;
+    int32_t mval;
+    int32_t active_slot;
+};
+template <typename T>
+void run_exact_folds(Ctx &ctx, const FoldChain *chains, int nchains, int64_t m, const int *active, T *result,
+                     long long *count);
+
 template <typename T>
 void run_kmeanspp(Ctx &ctx, const T *x, int64_t n, int d, int k, const double *draws_dev,
                   int64_t n_draws, T *centers_out, int64_t *draws_used);

@@ -44,7 +44,9 @@ namespace {
 
 constexpr int BM = 128;           // rows per tile = TMEM lanes
 constexpr int BN = 256;           // centres per accumulator block
-constexpr int NTHREADS = 320;     // 10 warps
+// Threads of a launch: the TMA warp, the MMA warp and 4 x EP epilogue warps
+// (EP parts of an accumulator block's 256 columns per TMEM lane quarter).
+__host__ __device__ constexpr int tc_threads(int ep) { return 64 + ep * 128; }
 constexpr uint32_t TMEM_COLS = 512;
 constexpr uint32_t X_ATOM_BYTES = BM * 128;  // 128 rows x 64 BF16
 constexpr uint32_t ONES_BYTES = BM * 32;     // 128 rows x 16 BF16
@@ -57,13 +59,15 @@ struct alignas(16) HalfRec {
 __device__ __forceinline__ uint32_t pack_local(int i, int base) { return i < 0 ? 0xFFFFu : (uint32_t)(i - base); }
 __device__ __forceinline__ int unpack_local(uint32_t l, int base) { return l == 0xFFFFu ? -1 : base + (int)l; }
 
-// Shared-memory exchange between the two epilogue halves of a row: three
-// rotating slots for the top-2 pass (see the tile merge in the kernel) --
-// whole records for BF16, 16-byte ones for FP8, whose larger X stages would
-// otherwise leave room for fewer resident centres -- and one slot of top-8
-// records.
-__host__ __device__ constexpr uint32_t merge_bytes(int topk, bool fp8) {
-    return BM * (uint32_t)(topk == 2 ? 3 * (fp8 ? sizeof(HalfRec) : sizeof(Top2)) : sizeof(Top8));
+// Shared-memory exchange between the epilogue parts of a row: for the top-2
+// pass, `slots` rotating slots (see the tile merge in the kernel) of EP - 1
+// records per row -- whole records for BF16 with two parts, 16-byte ones
+// otherwise (FP8, whose larger X stages leave less room, and four parts) --
+// and one slot of top-8 records for the second pass.
+__host__ __device__ constexpr uint32_t merge_bytes(int topk, bool fp8, int ep, int slots) {
+    return topk == 2 ? BM * (uint32_t)slots * (uint32_t)(ep - 1) *
+                           (uint32_t)((fp8 || ep > 2) ? sizeof(HalfRec) : sizeof(Top2))
+                     : BM * (uint32_t)sizeof(Top8);
 }
 
 // The record of one slot (FP8: HalfRec; BF16: Top2, no packing).
@@ -118,6 +122,7 @@ struct TcParams {
     int nblocks;       // kp / 256
     int parts;
     int ctas_per_part;
+    int slots;         // rotating tile-merge slots (top-2 pass)
     uint32_t off_c, off_x, off_aug, off_ones, off_merge, off_bar;
     uint32_t c_atom_bytes;  // kp * 128
     uint32_t x_stage_bytes;
@@ -425,8 +430,8 @@ __device__ __forceinline__ void rank_halfk(uint32_t col_addr, float cgrid, float
 // FP8: X and the centres are E4M3 (1 byte, 128 per swizzle atom) and the
 // augmentation operand is a per-row BF16 tile loaded with each X tile (the
 // row's scale times [1,1,1,0,...]); BF16: a constant ones tile.
-template <int TOPK, bool FP8, int XST>
-__global__ void __launch_bounds__(NTHREADS, 1)
+template <int TOPK, bool FP8, int XST, int EP>
+__global__ void __launch_bounds__(tc_threads(EP), 1)
     tc_assign_kernel(const __grid_constant__ CUtensorMap tm_x, const __grid_constant__ CUtensorMap tm_c,
                      const __grid_constant__ CUtensorMap tm_aug, const __grid_constant__ CUtensorMap tm_ones,
                      TcParams p) {
@@ -459,7 +464,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         }
         for (int b = 0; b < 2; b++) {
             mbar_init(bar_afull(b), 1);
-            mbar_init(bar_aempty(b), 8);
+            mbar_init(bar_aempty(b), 4 * EP);
         }
         *abort_flag = 0u;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -555,12 +560,17 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             if (last_s >= 0) mbar_wait(bar_xempty(last_s), last_ph, abort_flag, p.err, 0ull);
         }
     } else if (TOPK == 2) {
+        constexpr int CP = BN / EP;   // columns of one part
+        constexpr int NCK = CP / 32;  // its 32-column chunks
+        static_assert(NCK == 2 || NCK == 4, "two or four epilogue parts");
+        constexpr int EPI = 4 * EP * 32;  // epilogue threads (the named barriers' count)
+        using Slot = MergeSlot<FP8 || (EP > 2)>;
         const int ew = warp - 2;
         const int quarter = warp & 3;
-        const int half = ew >> 2;
+        const int prt = ew >> 2;
         const int row_local = quarter * 32 + lane;
         const uint32_t lane_addr = tmem + ((uint32_t)(quarter * 32) << 16);
-        MergeSlot<FP8> *merge = (MergeSlot<FP8> *)(smem + p.off_merge);
+        Slot *merge = (Slot *)(smem + p.off_merge);
         const int slice0 = part * p.kp;  // the slice's first centre
         const float cgrid = p.stats->cgrid, ulp = p.stats->ulp;
         const int64_t my_tiles = q < p.tiles ? (p.tiles - 1 - q) / tstride + 1 : 0;
@@ -571,8 +581,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         // back to the MMA warp as soon as its last 32 columns are in
         // registers, and the next block's first 32 columns start loading
         // (when its MMAs have already committed) while those last columns
-        // are ranked, so the two warps of a sub-partition do not both wait
-        // on a fresh TMEM load at every block. pre: ra holds that load.
+        // are ranked, so the warps of a sub-partition do not all wait on a
+        // fresh TMEM load at every block. pre: ra holds that load.
         uint32_t ra[32], rb[32];
         bool pre = false;
         for (int64_t t = q; t < p.tiles; t += tstride, tile_it++) {
@@ -588,7 +598,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             for (int b = 0; b < p.nblocks; b++, item++) {
                 const int buf = (int)(item & 1u);
                 const uint32_t aph = (item >> 1) & 1u;
-                const uint32_t col = lane_addr + (uint32_t)buf * BN + (uint32_t)half * 128u;
+                const uint32_t col = lane_addr + (uint32_t)buf * BN + (uint32_t)prt * CP;
                 if (!pre) {
                     if (!dead && !mbar_wait(bar_afull(buf), aph, abort_flag, p.err, 16ull)) dead = true;
                     dead = __any_sync(0xffffffffu, dead);  // warp-uniform, for the barriers below
@@ -598,12 +608,12 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                 }
                 pre = false;
                 if (p.dump && blockIdx.x == 0 && t == q) {
-                    for (int ch = 0; ch < 4; ch++) {
+                    for (int ch = 0; ch < NCK; ch++) {
                         uint32_t r[32];
                         tmem_ld32(col + ch * 32, r);
                         tmem_wait(r);
                         for (int e = 0; e < 32; e++)
-                            p.dump[(int64_t)row_local * (p.nblocks * BN) + b * BN + half * 128 + ch * 32 + e] =
+                            p.dump[(int64_t)row_local * (p.nblocks * BN) + b * BN + prt * CP + ch * 32 + e] =
                                 __uint_as_float(r[e]);
                     }
                 }
@@ -614,12 +624,14 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                 tmem_ld32(col + 32, rb);
                 RankChunk<0, 0>::run(ra, cg, ul, a1, a2);
                 tmem_wait(rb);
-                tmem_ld32(col + 64, ra);
-                RankChunk<1, 0>::run(rb, cg, ul, a1, a2);
-                tmem_wait(ra);
-                tmem_ld32(col + 96, rb);
-                RankChunk<2, 0>::run(ra, cg, ul, a1, a2);
-                tmem_wait(rb);
+                if (NCK == 4) {
+                    tmem_ld32(col + 64, ra);
+                    RankChunk<1, 0>::run(rb, cg, ul, a1, a2);
+                    tmem_wait(ra);
+                    tmem_ld32(col + 96, rb);
+                    RankChunk<2, 0>::run(ra, cg, ul, a1, a2);
+                    tmem_wait(rb);
+                }
                 // every column of this block is in registers: release the buffer
                 tc_fence_before();
                 __syncwarp();
@@ -629,42 +641,47 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                     const uint32_t naph = ((item + 1) >> 1) & 1u;
                     if (__all_sync(0xffffffffu, mbar_try_wait(bar_afull(nbuf), naph))) {
                         tc_fence_after();
-                        tmem_ld32(lane_addr + (uint32_t)nbuf * BN + (uint32_t)half * 128u, ra);
+                        tmem_ld32(lane_addr + (uint32_t)nbuf * BN + (uint32_t)prt * CP, ra);
                         pre = true;
                     }
                 }
-                RankChunk<3, 0>::run(rb, cg, ul, a1, a2);
+                RankChunk<NCK - 1, 0>::run(rb, cg, ul, a1, a2);
                 uint32_t b1 = __float_as_uint(a1[0]), b2 = __float_as_uint(a2[0]), bu = b2;
                 int d1 = 0, d2 = 0;  // indices are carried inside the keys
 #pragma unroll
                 for (int qd = 1; qd < NCH; qd++)
                     merge_res(b1, d1, b2, d2, bu, __float_as_uint(a1[qd]), 0, __float_as_uint(a2[qd]), 0,
                               __float_as_uint(a2[qd]));
-                const int base = part * p.kp + b * BN + half * 128 + 127;
+                const int base = part * p.kp + b * BN + prt * CP + 127;
                 merge_res(R1, I1, R2, I2, U, b1 & 0xFFFFFF80u, base - (int)(b1 & 0x7Fu), b2 & 0xFFFFFF80u,
                           base - (int)(b2 & 0x7Fu), bu & 0xFFFFFF80u);
             }
-            // Tile merge: half 1 publishes its record in slot tile_it % 3 and
-            // arrives on named barrier 1 + tile_it % 3 without waiting; half 0
-            // waits there, merges and stores. Half 1 cannot reach the same slot
-            // and barrier again (three tiles on) before half 0 has passed this
-            // merge: that tile's accumulators need every epilogue warp to have
-            // released the buffer of an earlier tile of this CTA. An aborting
-            // warp is no longer held back by the MMAs, so it waits instead.
-            const uint32_t sl = tile_it % 3u;
-            MergeSlot<FP8> *slot = merge + sl * BM;
-            if (half == 1) {
-                slot[row_local].put(R1, I1, R2, I2, U, slice0);
+            // Tile merge: parts 1.. publish their records in slot
+            // tile_it % slots and arrive on named barrier 1 + that slot
+            // without waiting; part 0 waits there, merges and stores. A part
+            // cannot reach the same slot and barrier again before part 0 has
+            // passed this merge: that tile's accumulators need every epilogue
+            // warp to have released the buffer of an earlier tile of this
+            // CTA (three slots when a tile is one accumulator block, two
+            // otherwise: the host plans which). An aborting warp is no longer
+            // held back by the MMAs, so it waits instead.
+            const uint32_t sl = tile_it % (uint32_t)p.slots;
+            Slot *slot = merge + sl * (uint32_t)(EP - 1) * BM;
+            if (prt > 0) {
+                slot[(prt - 1) * BM + row_local].put(R1, I1, R2, I2, U, slice0);
                 if (dead)
-                    asm volatile("bar.sync %0, 256;" ::"r"(1u + sl) : "memory");
+                    asm volatile("bar.sync %0, %1;" ::"r"(1u + sl), "r"(EPI) : "memory");
                 else
-                    asm volatile("bar.arrive %0, 256;" ::"r"(1u + sl) : "memory");
+                    asm volatile("bar.arrive %0, %1;" ::"r"(1u + sl), "r"(EPI) : "memory");
             } else {
-                asm volatile("bar.sync %0, 256;" ::"r"(1u + sl) : "memory");
-                uint32_t w1, w2, wu;
-                int j1, j2;
-                slot[row_local].get(w1, j1, w2, j2, wu, slice0);
-                merge_res(R1, I1, R2, I2, U, w1, j1, w2, j2, wu);
+                asm volatile("bar.sync %0, %1;" ::"r"(1u + sl), "r"(EPI) : "memory");
+#pragma unroll
+                for (int o = 1; o < EP; o++) {
+                    uint32_t w1, w2, wu;
+                    int j1, j2;
+                    slot[(o - 1) * BM + row_local].get(w1, j1, w2, j2, wu, slice0);
+                    merge_res(R1, I1, R2, I2, U, w1, j1, w2, j2, wu);
+                }
                 const int64_t row = t * BM + row_local;
                 if (row < p.n && !dead)
                     p.out[(int64_t)part * p.out_stride + row] =
@@ -872,23 +889,38 @@ void plan_shape(MixedPlan &mp, int64_t n, int d, int k, bool fp8, int topk, int 
     const size_t x_stage = (size_t)n_atoms * X_ATOM_BYTES;
     const size_t per_centre = (size_t)n_atoms * 128 + 32;
     // two X stages when 256 resident centres still fit, else one
+    // Two epilogue parts per lane quarter (8 epilogue warps) and three merge
+    // slots. The kernel also takes four parts (16 epilogue warps, 64 columns
+    // each, two slots when a tile has two blocks or more): measured slower at
+    // n = 4M, d = 128, k = 1024 (1.351 against 1.020 ms; 96 registers a
+    // thread and the four-way merges), so it is not planned.
+    mp.ep = 2;
+    mp.slots = 3;
     size_t fixed = 0;
-    int xst = 2;
-    for (; xst >= 1; xst--) {
-        fixed = 1024 + xst * x_stage + (fp8 ? xst * XAUG_BYTES : ONES_BYTES) + merge_bytes(topk, fp8) + BAR_BYTES;
-        if (fixed + BN * per_centre <= SMEM_LIMIT) break;
+    for (;;) {
+        int xst = 2;
+        for (; xst >= 1; xst--) {
+            fixed = 1024 + xst * x_stage + (fp8 ? xst * XAUG_BYTES : ONES_BYTES) +
+                    merge_bytes(topk, fp8, mp.ep, mp.slots) + BAR_BYTES;
+            if (fixed + BN * per_centre <= SMEM_LIMIT) break;
+        }
+        if (xst < 1) {
+            set_error("the resident-slice tensor-core kernel supports d <= %d for this precision (got %d)",
+                      fp8 ? 512 : 256, d);
+            fail(FK_ERR_UNSUPPORTED);
+        }
+        mp.xst = xst;
+        const int kp_max = (int)((SMEM_LIMIT - fixed) / per_centre) / BN * BN;
+        mp.parts = (k + kp_max - 1) / kp_max;
+        mp.kp = ((k + mp.parts - 1) / mp.parts + BN - 1) / BN * BN;
+        mp.k_pad = mp.parts * mp.kp;
+        mp.nblocks = mp.kp / BN;
+        if (topk == 2 && mp.nblocks < 2 && mp.slots < 3) {
+            mp.slots = 3;
+            continue;
+        }
+        break;
     }
-    if (xst < 1) {
-        set_error("the resident-slice tensor-core kernel supports d <= %d for this precision (got %d)",
-                  fp8 ? 512 : 256, d);
-        fail(FK_ERR_UNSUPPORTED);
-    }
-    mp.xst = xst;
-    const int kp_max = (int)((SMEM_LIMIT - fixed) / per_centre) / BN * BN;
-    mp.parts = (k + kp_max - 1) / kp_max;
-    mp.kp = ((k + mp.parts - 1) / mp.parts + BN - 1) / BN * BN;
-    mp.k_pad = mp.parts * mp.kp;
-    mp.nblocks = mp.kp / BN;
     mp.tiles = (n + BM - 1) / BM;
     if (sms < 1) sms = 1;
     mp.ctas_per_part = sms / mp.parts > 0 ? sms / mp.parts : 1;
@@ -960,7 +992,8 @@ void launch_tc_assign(Ctx &ctx, MixedPlan &mp, const void *xb, const void *cb, c
     p.off_ones = p.off_aug + (uint32_t)mp.kp * 32u;
     p.off_xaug = p.off_ones;
     p.off_merge = p.off_ones + (fp8 ? (uint32_t)mp.xst * XAUG_BYTES : ONES_BYTES);
-    p.off_bar = p.off_merge + merge_bytes(mp.topk, mp.fp8);
+    p.off_bar = p.off_merge + merge_bytes(mp.topk, mp.fp8, mp.ep, mp.slots);
+    p.slots = mp.slots;
     p.c_tx_bytes = (uint32_t)p.n_atoms * p.c_atom_bytes + (uint32_t)mp.kp * 32u + (fp8 ? 0u : ONES_BYTES);
     p.out = out;
     p.out8 = out8;
@@ -979,7 +1012,7 @@ void launch_tc_assign(Ctx &ctx, MixedPlan &mp, const void *xb, const void *cb, c
                       *ta = (const CUtensorMap *)mp.tm_aug, *to = (const CUtensorMap *)tmo;
     auto go = [&](auto kern) {
         FK_CUDA(cudaFuncSetAttribute((const void *)kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        kern<<<mp.grid, NTHREADS, smem, ctx.stream>>>(*tx, *tcm, *ta, *to, p);
+        kern<<<mp.grid, tc_threads(mp.ep), smem, ctx.stream>>>(*tx, *tcm, *ta, *to, p);
     };
     // Instantiations: main pass (top-2) BF16 / FP8 with one or two X stages;
     // second pass (top-8) BF16 with one or two X stages.
@@ -988,11 +1021,11 @@ void launch_tc_assign(Ctx &ctx, MixedPlan &mp, const void *xb, const void *cb, c
             set_error("the second pass runs in BF16");
             fail(FK_ERR_UNSUPPORTED);
         }
-        mp.xst == 2 ? go(tc_assign_kernel<8, false, 2>) : go(tc_assign_kernel<8, false, 1>);
+        mp.xst == 2 ? go(tc_assign_kernel<8, false, 2, 2>) : go(tc_assign_kernel<8, false, 1, 2>);
     } else if (fp8) {
-        mp.xst == 2 ? go(tc_assign_kernel<2, true, 2>) : go(tc_assign_kernel<2, true, 1>);
+        mp.xst == 2 ? go(tc_assign_kernel<2, true, 2, 2>) : go(tc_assign_kernel<2, true, 1, 2>);
     } else {
-        mp.xst == 2 ? go(tc_assign_kernel<2, false, 2>) : go(tc_assign_kernel<2, false, 1>);
+        mp.xst == 2 ? go(tc_assign_kernel<2, false, 2, 2>) : go(tc_assign_kernel<2, false, 1, 2>);
     }
     FK_LAUNCH_CHECK();
 }

@@ -1298,6 +1298,25 @@ __global__ void bk_scatter_kernel(const int32_t *__restrict__ seg, const uint8_t
         out[lab[i] == 0 ? (int64_t)pos[i] : *m0 + (i - (int64_t)pos[i])] = seg[i];
 }
 
+// run_2means' centre update (:264-298) and compute_cluster_stats' centre
+// (:192-211) from the exact folds of chain (run * 2 + side) * d + feature:
+// sum / count with the count as the reference forms it -- the fold of
+// F::one() per row, exact up to 2^(MB+1) where it stops growing, or F::from(m)
+// for the whole segment -- an empty side keeping its centre.
+template <typename T>
+__global__ void bk_centres_kernel(const T *__restrict__ sums, const long long *__restrict__ counts, int runs, int d,
+                                  const int *__restrict__ active, int whole, int64_t m, T *__restrict__ cen) {
+    using A = UArith<T>;
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= runs * 2 * d) return;
+    const int r = c / (2 * d);
+    if (active && !active[r]) return;
+    const long long cap = sizeof(T) == 4 ? (1LL << 24) : (1LL << 53);
+    const long long cnt = counts[c];
+    const T cf = whole ? (T)m : (T)(cnt < cap ? cnt : cap);
+    if (cf > T(0)) cen[c] = A::div(sums[c], cf);
+}
+
 // Final labels: cluster ci (block ci) owns the rows of its segment.
 __global__ void bk_labels_kernel(const int32_t *__restrict__ perm, const int64_t *__restrict__ seg,
                                  int64_t *__restrict__ labels) {
@@ -1370,6 +1389,18 @@ void launch_bk_fold(const T *dist, int64_t dist_stride, const uint8_t *lab, int6
     bk_fold_kernel<T><<<1, 32 * ((nsum + 31) / 32), 0, s>>>(dist, dist_stride, lab, m, nsum, by_label ? 1 : 0, out);
     FK_LAUNCH_CHECK();
 }
+
+template <typename T>
+void launch_bk_centres(const T *sums, const long long *counts, int runs, int d, const int *active, bool whole,
+                       int64_t m, T *cen, cudaStream_t s) {
+    const int total = runs * 2 * d;
+    bk_centres_kernel<T><<<(total + 255) / 256, 256, 0, s>>>(sums, counts, runs, d, active, whole ? 1 : 0, m, cen);
+    FK_LAUNCH_CHECK();
+}
+template void launch_bk_centres<double>(const double *, const long long *, int, int, const int *, bool, int64_t,
+                                        double *, cudaStream_t);
+template void launch_bk_centres<float>(const float *, const long long *, int, int, const int *, bool, int64_t, float *,
+                                       cudaStream_t);
 
 size_t bk_partition_scratch_ints(int64_t m) { return 2 * (size_t)m + (size_t)((m + SCAN_TILE - 1) / SCAN_TILE + 1); }
 
