@@ -319,14 +319,8 @@ template <typename T>
 void launch_bk_assign(const T *x, int d, const int32_t *perm, int64_t m, const T *cen, uint8_t *lab,
                       int64_t lab_stride, const int *active, int *changed, int runs, cudaStream_t s);
 template <typename T>
-void launch_bk_sums(const T *x, int d, const int32_t *perm, int64_t m, const uint8_t *lab, int64_t lab_stride,
-                    T *cen, const int *active, int runs, bool whole_count, cudaStream_t s);
-template <typename T>
 void launch_bk_dist(const T *x, int d, const int32_t *perm, int64_t m, const T *cen, const uint8_t *lab,
                     int64_t lab_stride, T *dist, int64_t dist_stride, int runs, cudaStream_t s);
-template <typename T>
-void launch_bk_fold(const T *dist, int64_t dist_stride, const uint8_t *lab, int64_t m, int nsum, bool by_label, T *out,
-                    cudaStream_t s);
 // Centres from the exact folds of chains (run * 2 + side) * d + feature.
 template <typename T>
 void launch_bk_centres(const T *sums, const long long *counts, int runs, int d, const int *active, bool whole,

@@ -1175,67 +1175,6 @@ __global__ void bk_assign_kernel(const T *__restrict__ x, int d, const int32_t *
     if (__syncthreads_or(any) && threadIdx.x == 0) changed[run] = 1;
 }
 
-// run_2means' centre update (:264-298) and compute_cluster_stats' centre
-// (:192-211): per side, the segment's rows summed in row order in F, the
-// count as F (+1 per row, or F::from(m) for the whole segment when
-// whole_count), and sum / count for a side with rows (an empty side keeps
-// its centre). One CTA per run: the rows are staged in shared memory a chunk
-// at a time and every thread keeps the chains of fixed (side, feature)
-// pairs, so each sum has the reference's order.
-constexpr int BK_THREADS = 256;
-constexpr int BK_PER = 8;  // (side, feature) pairs per thread: 2 d <= 2048
-
-template <typename T>
-__global__ void __launch_bounds__(BK_THREADS)
-    bk_sums_kernel(const T *__restrict__ x, int d, const int32_t *__restrict__ perm, int64_t m,
-                   const uint8_t *__restrict__ lab, int64_t lab_stride, T *__restrict__ cen,
-                   const int *__restrict__ active, int chunk, int whole_count) {
-    using A = UArith<T>;
-    const int run = blockIdx.x;
-    if (active && !active[run]) return;  // uniform over the block
-    extern __shared__ __align__(16) unsigned char bk_smem[];
-    T *rows = reinterpret_cast<T *>(bk_smem);
-    uint8_t *labs = reinterpret_cast<uint8_t *>(rows + (size_t)chunk * d);
-    const uint8_t *l = lab + (int64_t)run * lab_stride;
-    const int npairs = 2 * d;
-    int side_of[BK_PER], feat_of[BK_PER];
-    T sum[BK_PER];
-#pragma unroll
-    for (int q = 0; q < BK_PER; q++) {
-        const int t = threadIdx.x + q * BK_THREADS;
-        side_of[q] = t < npairs ? t / d : 2;  // 2: no pair
-        feat_of[q] = t < npairs ? t - (t / d) * d : 0;
-        sum[q] = T(0);
-    }
-    T cnt0 = T(0), cnt1 = T(0);
-    for (int64_t b0 = 0; b0 < m; b0 += chunk) {
-        const int len = (int)(m - b0 < chunk ? m - b0 : chunk);
-        __syncthreads();  // the previous chunk is no longer read
-        for (int e = threadIdx.x; e < len * d; e += BK_THREADS) {
-            const int r = e / d;
-            rows[e] = x[(int64_t)perm[b0 + r] * d + (e - r * d)];
-        }
-        for (int r = threadIdx.x; r < len; r += BK_THREADS) labs[r] = l[b0 + r];
-        __syncthreads();
-        for (int r = 0; r < len; r++) {
-            const int side = labs[r];
-            if (side == 0) cnt0 = A::add(cnt0, T(1));
-            else cnt1 = A::add(cnt1, T(1));
-#pragma unroll
-            for (int q = 0; q < BK_PER; q++)
-                if (side_of[q] == side) sum[q] = A::add(sum[q], rows[r * d + feat_of[q]]);
-        }
-    }
-    if (whole_count) cnt0 = (T)m;
-    T *c = cen + (int64_t)run * 2 * d;
-#pragma unroll
-    for (int q = 0; q < BK_PER; q++) {
-        if (side_of[q] > 1) continue;
-        const T cnt = side_of[q] == 0 ? cnt0 : cnt1;
-        if (cnt > T(0)) c[side_of[q] * d + feat_of[q]] = A::div(sum[q], cnt);
-    }
-}
-
 // Each row's direct-form distance to its run's centre of its label.
 template <typename T>
 __global__ void bk_dist_kernel(const T *__restrict__ x, int d, const int32_t *__restrict__ perm, int64_t m,
@@ -1256,27 +1195,6 @@ __global__ void bk_dist_kernel(const T *__restrict__ x, int d, const int32_t *__
         }
         o[i] = acc;
     }
-}
-
-// The reference's `sse = sse + ...` folds, in row order: thread t sums
-// dist[t * dist_stride + i] over the rows i < m (by_label = 0: every row),
-// or, with by_label, thread t in {0, 1} sums dist[i] over the rows of label t.
-template <typename T>
-__global__ void bk_fold_kernel(const T *__restrict__ dist, int64_t dist_stride, const uint8_t *__restrict__ lab,
-                               int64_t m, int nsum, int by_label, T *__restrict__ out) {
-    using A = UArith<T>;
-    const int t = threadIdx.x;
-    if (t >= nsum) return;
-    const T *v = by_label ? dist : dist + (int64_t)t * dist_stride;
-    T acc = T(0);
-    if (by_label) {
-        for (int64_t i = 0; i < m; i++)
-            if (lab[i] == t) acc = A::add(acc, v[i]);
-    } else {
-#pragma unroll 8
-        for (int64_t i = 0; i < m; i++) acc = A::add(acc, v[i]);
-    }
-    out[t] = acc;
 }
 
 // Stable partition of a segment by labels (label 0 first, each side in row
@@ -1364,15 +1282,6 @@ void launch_bk_assign(const T *x, int d, const int32_t *perm, int64_t m, const T
     FK_LAUNCH_CHECK();
 }
 
-template <typename T>
-void launch_bk_sums(const T *x, int d, const int32_t *perm, int64_t m, const uint8_t *lab, int64_t lab_stride,
-                    T *cen, const int *active, int runs, bool whole_count, cudaStream_t s) {
-    const int chunk = bk_chunk_rows(d, sizeof(T));
-    const size_t smem = (size_t)chunk * d * sizeof(T) + (size_t)chunk;
-    bk_sums_kernel<T><<<(unsigned)runs, BK_THREADS, smem, s>>>(x, d, perm, m, lab, lab_stride, cen, active, chunk,
-                                                               whole_count ? 1 : 0);
-    FK_LAUNCH_CHECK();
-}
 
 template <typename T>
 void launch_bk_dist(const T *x, int d, const int32_t *perm, int64_t m, const T *cen, const uint8_t *lab,
@@ -1383,12 +1292,6 @@ void launch_bk_dist(const T *x, int d, const int32_t *perm, int64_t m, const T *
     FK_LAUNCH_CHECK();
 }
 
-template <typename T>
-void launch_bk_fold(const T *dist, int64_t dist_stride, const uint8_t *lab, int64_t m, int nsum, bool by_label, T *out,
-                    cudaStream_t s) {
-    bk_fold_kernel<T><<<1, 32 * ((nsum + 31) / 32), 0, s>>>(dist, dist_stride, lab, m, nsum, by_label ? 1 : 0, out);
-    FK_LAUNCH_CHECK();
-}
 
 template <typename T>
 void launch_bk_centres(const T *sums, const long long *counts, int runs, int d, const int *active, bool whole,
@@ -1436,17 +1339,10 @@ template void launch_bk_assign<double>(const double *, int, const int32_t *, int
                                        int64_t, const int *, int *, int, cudaStream_t);
 template void launch_bk_assign<float>(const float *, int, const int32_t *, int64_t, const float *, uint8_t *, int64_t,
                                       const int *, int *, int, cudaStream_t);
-template void launch_bk_sums<double>(const double *, int, const int32_t *, int64_t, const uint8_t *, int64_t, double *,
-                                     const int *, int, bool, cudaStream_t);
-template void launch_bk_sums<float>(const float *, int, const int32_t *, int64_t, const uint8_t *, int64_t, float *,
-                                    const int *, int, bool, cudaStream_t);
 template void launch_bk_dist<double>(const double *, int, const int32_t *, int64_t, const double *, const uint8_t *,
                                      int64_t, double *, int64_t, int, cudaStream_t);
 template void launch_bk_dist<float>(const float *, int, const int32_t *, int64_t, const float *, const uint8_t *,
                                     int64_t, float *, int64_t, int, cudaStream_t);
-template void launch_bk_fold<double>(const double *, int64_t, const uint8_t *, int64_t, int, bool, double *,
-                                     cudaStream_t);
-template void launch_bk_fold<float>(const float *, int64_t, const uint8_t *, int64_t, int, bool, float *, cudaStream_t);
 
 template void launch_gather_rows<double>(const double *, int, const int32_t *, int64_t, double *, cudaStream_t);
 template void launch_gather_rows<float>(const float *, int, const int32_t *, int64_t, float *, cudaStream_t);
