@@ -36,7 +36,10 @@ k-means++ init on the GPU (timed separately as kpp_ms); batched = 512
 independent problems (n log-uniform in [2,000, 200,000], d in {8,16,32,64},
 k in [4,64]) x 10 k-means++ restarts, one fit_batched call per step (f32
 distances, FP64 centroid sums); value = Lloyd iterations over all 5,120 fits
-per second of the call, pt_k_per_s = sum of n * k * iterations per second.
+per second of the call, pt_k_per_s = sum of n * k * iterations per second;
+minibatch = MiniBatchKMeans on the dirichlet shape (batch 1024); bisecting =
+BisectingKMeans, n=200,000 d=16 k=32, n_init 10; transform = the n x k
+distance matrix of the dirichlet shape (f32), rows/s, with the bytes written.
 
 --impl reference times the CPU restatement of the reference (oracle/; the
 reference is Rust and cannot be built here) with all host threads: the K
@@ -72,7 +75,8 @@ def parse(argv=None):
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--form", default="auto", choices=["auto", "bf16", "fp8", "fp32", "fp64"])
     ap.add_argument("--workload", default="anisotropic",
-                    choices=["anisotropic", "bisector", "dirichlet", "batched", "minibatch", "bisecting"])
+                    choices=["anisotropic", "bisector", "dirichlet", "batched", "minibatch", "bisecting",
+                             "transform"])
     ap.add_argument("--scale", type=float, default=1.0, help="fraction of the full row count")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true")
@@ -83,7 +87,7 @@ def parse(argv=None):
     args = ap.parse_args(argv)
     if args.steps is None:  # the configurations' own iteration counts (anisotropic: 50 Lloyd iterations)
         args.steps = {"anisotropic": 50, "bisector": 20, "dirichlet": 20, "batched": 20, "minibatch": 100,
-                      "bisecting": 3}[args.workload]
+                      "bisecting": 3, "transform": 20}[args.workload]
     return args
 
 
@@ -576,6 +580,97 @@ def run_bisecting(args):
     ctx.close()
 
 
+def run_transform(args):
+    """Transform::transform (kmeans.rs:568-617) at scale: the n x k distance
+    matrix of n = 1,000,000 rows x d = 64 (the Dirichlet blob mixture, f32)
+    against k = 256 centres (the first k rows of a seeded permutation); a
+    step is one transform call over all rows, the output left on the
+    device. The direct form (x_j - c_j)^2 summed left to right with no fused
+    multiply-add, then the square root, bit for bit the reference's."""
+    import ctypes as C
+
+    import torch
+
+    import ferrolearn_gb300 as F
+    from ferrolearn_gb300 import _native
+    from ferrolearn_gb300 import workloads as W
+    from ferrolearn_gb300.kmeans import _check, _ptr
+    dev = torch.cuda.current_device()
+    w = W.dirichlet_256x64(scale=args.scale, dtype=np.float32)
+    x, k = w["x"], w["k"]
+    n, d = x.shape
+    cen = np.ascontiguousarray(x[np.random.default_rng(1).permutation(n)[:k]])
+    stream = torch.cuda.Stream()
+    ctx = F.Context(dev, stream=stream.cuda_stream)
+    xd = torch.from_numpy(x).to(dev)
+    cd = torch.from_numpy(cen).to(dev)
+    out = torch.empty((n, k), dtype=torch.float32, device=dev)
+    fn = _native.lib().fk_kmeans_transform_f32
+
+    def call():
+        _check(fn(ctx.handle, _ptr(cd), k, d, _ptr(xd), n, d, _ptr(out)))
+    for _ in range(max(3, args.warmup)):
+        call()
+    l0 = _native.lib().fk_debug_launch_count()
+    with ClockSampler(dev) as clocks:
+        clocks.mark_start()
+        ms, _ = _timed_calls(stream, call, args.steps)
+        clocks.mark_end()
+    launches = int(_native.lib().fk_debug_launch_count() - l0)
+    per = ms / args.steps
+    pk = (C.c_double * 8)()
+    _native.lib().fk_debug_measure_peaks(ctx.handle, pk)
+    instr_peak = pk[0] / 2.0 / 1e12  # FP32 FMA instructions per second (one op each)
+    ops = 3.0 * n * k * d  # sub, mul, add per (row, centre, feature); the direct form has no FMA
+    wbytes = 4.0 * n * k
+    out_line = {
+        "metric": "KMeans transform rows/s (n x k distances, f32)", "value": n / (per / 1e3), "unit": "rows/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": per,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "form": "transform",
+        "config": {"workload": "transform_dirichlet_256x64", "n": n, "d": d, "k": k,
+                   "centres": "first k rows of a seeded permutation",
+                   "l2": f"inputs and output larger than L2 (X {x.nbytes / 1e9:.2f} GB, out {wbytes / 1e9:.2f} GB)",
+                   "parallelism": "replicas"},
+        "gpu_launches": launches, "clocks": clocks.summary(),
+        "roofline": {"bound": "fp32-simt", "achieved": ops / (per / 1e3) / 1e12, "peak": instr_peak,
+                     "unit": "T op/s", "frac": ops / (per / 1e3) / 1e12 / instr_peak, "traffic": None,
+                     "kernel": "assign_direct_kernel<f32, f32, write all> (the transform form)",
+                     "ms_per_launch": per,
+                     "peak_source": "FP32 FMA instruction rate measured in this run (fk_debug_measure_peaks / 2); "
+                                    "achieved counts the 3 n k d separate sub, mul and add of the direct form"},
+        "hbm_write": {"bytes_per_step": wbytes, "achieved_gbs": wbytes / (per / 1e3) / 1e9,
+                      "note": "the n x k output written once"},
+    }
+    # parity: a seeded sample of rows against the oracle, bit for bit
+    from oracle import oracle as O
+    rows = np.sort(np.random.default_rng(5).choice(n, min(n, 20000), replace=False))
+    got = out[torch.from_numpy(rows).to(dev)].cpu().numpy()
+    want = O.transform(cen, x[rows])
+    out_line["parity"] = {"oracle": "oracle/ orc_transform_f32 (direct form + sqrt)", "rows_checked": int(len(rows)),
+                          "bit_identical": bool(np.array_equal(got.view(np.uint32), want.view(np.uint32)))}
+    if not args.no_e2e:
+        fitted = F.FittedKMeans(cen, None, 0.0, 0, "f32")
+        fitted.transform(x, ctx=ctx)
+        t0 = time.perf_counter()
+        for _ in range(3):
+            fitted.transform(x, ctx=ctx)
+        dt = (time.perf_counter() - t0) / 3
+        out_line["e2e"] = {"value": n / dt, "unit": "rows/s", "h2d_bytes_per_step": float(x.nbytes),
+                           "d2h_bytes_per_step": wbytes,
+                           "note": "FittedKMeans.transform on a host X into a host n x k array (pageable)"}
+    if not args.no_cpu:
+        m = min(n, 100000)
+        t0 = time.perf_counter()
+        O.transform(cen, x[:m])
+        dt = time.perf_counter() - t0
+        out_line["cpu_baseline"] = {"value": m / dt, "unit": "rows/s", "cores": os.cpu_count() or 1,
+                                    "cpu_model": cpu_model(), "kind": "port",
+                                    "sample": f"the first {m} rows (oracle orc_transform_f32)"}
+    print(json.dumps(out_line), flush=True)
+    ctx.close()
+
+
 def parity_leg(w, form, ctx, xd, iters, rows, fit_centres, fit_labels):
     """The timed trajectory replayed one Lloyd step at a time (the same
     entry point's single-iteration form, the same centres), each step checked
@@ -654,6 +749,8 @@ def run_ours(args):
         return run_minibatch(args)
     if args.workload == "bisecting":
         return run_bisecting(args)
+    if args.workload == "transform":
+        return run_transform(args)
     import torch
 
     import ferrolearn_gb300 as F

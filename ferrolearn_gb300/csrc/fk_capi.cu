@@ -1225,6 +1225,7 @@ fk_status fk_ctx_destroy(fk_ctx *ctx) {
     if (c->host_scalars) cudaFreeHost(c->host_scalars);
     if (c->mixed.ones) cudaFree(c->mixed.ones);
     if (c->mixed2.ones) cudaFree(c->mixed2.ones);
+    if (c->mixedm.ones) cudaFree(c->mixedm.ones);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return FK_OK;

@@ -58,8 +58,8 @@ struct DevScalars {
     unsigned long long near_tie_rows;
     unsigned long long flag_count;  // number of rows queued for re-check
     unsigned long long full_count;  // number of rows queued for a full re-scan
-    unsigned long long quad_count;  // second pass: rows with 2 to 8 candidates
-    unsigned long long ex_count;    // second pass: rows with more than 4 candidates
+    unsigned long long quad_count;  // second pass: rows decided among 2 to 8 (top-8) or 32 (masks) candidates
+    unsigned long long ex_count;    // second pass: rows re-scored against every centre
     unsigned long long f64_count;   // rows whose remaining candidates are scored in FP64
     unsigned long long error_word;  // nonzero: a bounded device wait gave up
     unsigned long long moved_rows;  // incremental update: rows whose label changed
@@ -112,7 +112,7 @@ struct MixedPlan {
     int64_t tiles = 0;    // ceil(n / 128)
     int ctas_per_part = 0;
     int grid = 0;
-    int topk = 2;         // epilogue records: 2 (Top2, main pass) or 8 (Top8, second pass)
+    int topk = 2;         // epilogue records: 2 (Top2, main pass), 8 (Top8, second pass) or 1 (candidate masks)
     int xst = 2;          // depth of the X tile ring (1 when two stages leave no room for 256 centres)
     int ep = 2;           // epilogue parts per TMEM lane quarter (4 x ep epilogue warps)
     int slots = 3;        // rotating tile-merge slots of the top-2 pass
@@ -141,7 +141,7 @@ enum BufSlot {
     BUF_MB_IDX, BUF_MB_XB, BUF_MB_LAB, BUF_MB_OLD, BUF_MB_COUNTS, BUF_MB_PARTV, BUF_MB_PARTI,
     BUF_BK_PERM, BUF_BK_LAB, BUF_BK_CEN, BUF_BK_DIST, BUF_BK_FLAGS, BUF_BK_SCRATCH, BUF_BK_CENTRES, BUF_BK_SEG,
     BUF_BK_FOLD, BUF_BK_LABELS, BUF_BK_XSEG, BUF_BK_CHAINS, BUF_BK_FRES, BUF_BK_FCNT, BUF_FOLD_SUM, BUF_FOLD_CNT,
-    BUF_FOLD_MAP,
+    BUF_FOLD_MAP, BUF_MASKS, BUF_THRESH,
     BUF_BX, BUF_BFITS, BUF_BSTATE, BUF_BITEMS, BUF_BPART, BUF_BORDER, BUF_BCTR, BUF_BLAB, BUF_BMEM, BUF_BCEN, BUF_BND, BUF_BXOFF,
     BUF_COUNT
 };
@@ -163,7 +163,8 @@ struct Ctx {
     };
     std::vector<PendingTimer> pending;  // phase timers read after the loop
     MixedPlan mixed;   // main pass
-    MixedPlan mixed2;  // second pass (BF16, top-8 records) over the rows the main pass left open
+    MixedPlan mixed2;  // second pass (BF16, top-8 records) over the rows an FP8 main pass left open
+    MixedPlan mixedm;  // second pass (BF16, candidate masks) over the rows a BF16 main pass left open
     int batch_variant[20] = {-1, -1, -1, -1, -1, -1, -1, -1, -1, -1,
                              -1, -1, -1, -1, -1, -1, -1, -1, -1, -1};  // autotuned tile shape per (d, k) bucket
     double *contract_acc = nullptr;  // when set: device time of the contraction kernel
@@ -365,7 +366,7 @@ void launch_mixed_inertia(Ctx &ctx, const double *part, int64_t m, DevScalars *s
 
 // Tensor-core assignment (fk_tc.cu): plan, then one persistent launch that
 // writes one record per (slice, row): Top2 (topk 2) or Top8 (topk 8).
-void plan_tc(Ctx &ctx, MixedPlan &mp, int64_t n, int d, int k, bool fp8, int topk);
+void plan_tc(Ctx &ctx, MixedPlan &mp, int64_t n, int d, int k, bool fp8, int topk, int kp_fixed = 0);
 // Dense BF16 (out[0]) and E4M3 (out[1]) flop/s of a tensor-core MMA loop (fk_tc.cu).
 void measure_tc_peaks(Ctx &ctx, double *out);
 // dump (tests only, nullable): raw accumulators of CTA 0's first tile.
@@ -375,11 +376,11 @@ void measure_tc_peaks(Ctx &ctx, double *out);
 // accumulator units.
 // Launch shape only (host arithmetic, no device work); plan_tc adds the
 // device-side constants.
-void plan_shape(MixedPlan &mp, int64_t n, int d, int k, bool fp8, int topk, int sms);
+void plan_shape(MixedPlan &mp, int64_t n, int d, int k, bool fp8, int topk, int sms, int kp_fixed = 0);
 void launch_tc_assign(Ctx &ctx, MixedPlan &mp, const void *xb, const void *cb, const void *caug, Top2 *out,
                       Top8 *out8, DevScalars *sc, const MixedStats *stats, float *dump = nullptr,
                       const unsigned long long *n_dev = nullptr, const void *xaug = nullptr,
-                      const float *rowscale = nullptr);
+                      const float *rowscale = nullptr, uint32_t *masks = nullptr, const float *thresh = nullptr);
 
 // Batched KMeans<f32> fits (fk_batched.cu).
 fk_status batched_fit_impl(Ctx &ctx, fk_batch_problem *problems, int64_t n_problems, int reduction,

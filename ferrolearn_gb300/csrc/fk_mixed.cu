@@ -21,11 +21,16 @@
 // v1 - v2 > thr no other centre can win in the FP64 direct form, so the label
 // is final. Otherwise, if the best value outside the top two is also below
 // v1 - thr, only the top two are re-scored exactly; else the row goes through
-// a second tensor-core pass in BF16 (its own operands, made from the row's
-// f32 values, and its own bound -- 16x tighter than the FP8 one) that keeps
-// the best eight scores, and only the centres inside that pass's bound are
-// re-scored (rows with more than eight such centres, or a non-finite score,
-// are re-scored against every centre, one CTA per row). Every re-score ends
+// a second tensor-core pass. After a BF16 main pass it recomputes the row's
+// scores from the same operands and marks every centre scoring at least
+// v1 - 2 thr (a superset of the centres that can still win); 1 to 32 marked
+// centres are re-scored, more or none send the row to the exhaustive
+// re-score. After an FP8 main pass it runs in BF16 (its own operands, made
+// from the row's f32 values, and its own bound -- 16x tighter than the FP8
+// one) and keeps the best eight scores, and only the centres inside that
+// pass's bound are re-scored (rows with more than eight such centres, or a
+// non-finite score, are re-scored against every centre, one CTA per row).
+// Every re-score ends
 // in the direct-form sum (x_j - c_j)^2 in FP64 with no FMA and the lowest
 // index on ties, i.e. exactly kmeans.rs:159-163 / 295-309, so the labels
 // equal the FP64 oracle's in every case.
@@ -133,13 +138,13 @@ __device__ __forceinline__ float half_warp_sum_f(float v) {
 // This lane's part of the FP32 direct-form squared distance between x and c
 // (f32 rows of d features) when `group` lanes share one distance: lane g of
 // the group takes the features g, g + group, ... in 16-byte pieces when d is
-// a multiple of 4 (rows are then 16-byte aligned), else one at a time. The
+// a multiple of 4 and both rows start 16-byte aligned, else one at a time. The
 // parts are summed by the caller; any summation order stays within the
 // (d + 4) 2^-23 d32 term of bound32.
 __device__ __forceinline__ float sq_partial(const float *__restrict__ x, const float *__restrict__ c, int d, int g,
                                             int group) {
     float acc = 0.f;
-    if ((d & 3) == 0) {
+    if ((d & 3) == 0 && (((uintptr_t)x | (uintptr_t)c) & 15u) == 0) {  // 16-byte pieces need 16-byte rows
         const float4 *x4 = reinterpret_cast<const float4 *>(x), *c4 = reinterpret_cast<const float4 *>(c);
         for (int f = g; f < (d >> 2); f += group) {
             const float4 xv = x4[f], cv = c4[f];
@@ -411,7 +416,7 @@ void launch_prep_rows(Ctx &ctx, const TX *x, int64_t n, int d, int d_pad, const 
                       __nv_bfloat16 *xaug, float4 *rowinfo, MixedStats *stats, const int32_t *list = nullptr,
                       const unsigned long long *count = nullptr) {
     const int64_t pblocks = std::min<int64_t>((n + 7) / 8, (int64_t)ctx.num_sms * 16);
-    if (std::is_same<TX, float>::value && (d & 3) == 0 && d_pad <= 256)
+    if (std::is_same<TX, float>::value && (d & 3) == 0 && d_pad <= 256 && ((uintptr_t)x & 15u) == 0)
         prep_rows4_kernel<FP8><<<(unsigned)pblocks, 256, 0, ctx.stream>>>(
             (const float *)x, n, d, d_pad, mu32, xq, xaug, rowinfo, stats, list, count);
     else
@@ -650,10 +655,11 @@ __global__ void __launch_bounds__(FINALIZE_THREADS)
     finalize_kernel(const Top2 *__restrict__ parts, int nparts, int64_t n, int k, int d,
                                 const float4 *__restrict__ rowinfo, const MixedStats *stats, float acc_rel,
                                 float mu_norm, int32_t *__restrict__ labels, int4 *__restrict__ pair_list,
-                                int32_t *__restrict__ full_list, DevScalars *sc) {
+                                int32_t *__restrict__ full_list, float *__restrict__ full_thresh, DevScalars *sc) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     int cls = -1;  // 0 certain, 1 pair, 2 full
     int i1 = -1, i2 = -1;
+    float th = -INFINITY;
     if (i < n) {
         // all loads first (independent), then the merge
         const float4 ri = rowinfo[i];
@@ -683,12 +689,24 @@ __global__ void __launch_bounds__(FINALIZE_THREADS)
             cls = 1;
         } else {
             cls = 2;
+            // Mask pass threshold (BF16 main pass, whose scores the mask pass
+            // recomputes from the same operands): any centre that can still
+            // win scores at least v1 - 2 thr there. The best centre c* has
+            // T'(c*) >= T'(i1) >= T(i1) - 2E >= v1 - 192 ulp - 2E, and a
+            // centre is needed only within thr of T'(c*); thr >= 2E + 384
+            // ulp covers both. Thresholds below 2^(E-2) (or NaN) become
+            // -inf: every centre is then a candidate.
+            const float t = __fsub_rd(v1, __fmul_ru(2.f, thr));
+            th = t >= stats->ulp * 2097152.f ? t : -INFINITY;
         }
     }
     unsigned long long ps, fs;
     block_reserve2<FINALIZE_THREADS>(&sc->flag_count, cls == 1, &sc->full_count, cls == 2, ps, fs);
     if (cls == 1) pair_list[ps] = make_int4((int)i, i1, i2, 0);
-    if (cls == 2) full_list[fs] = (int32_t)i;
+    if (cls == 2) {
+        full_list[fs] = (int32_t)i;
+        if (full_thresh) full_thresh[fs] = th;
+    }
 }
 
 // ------------------------------------------------------------ re-checks --
@@ -1157,6 +1175,133 @@ __global__ void oct_rescore_kernel(const float *__restrict__ x, int d, const flo
     }
 }
 
+// Mask pass rows (BF16 main pass): slot s of the list holds row list[s] and
+// its candidate mask, wpr words with bit per centre (mask_chunk's layout:
+// word w, bit b < 16 is centre 32 w + 2 (15 - b), bit b >= 16 is centre
+// 32 w + 2 (31 - b) + 1). One warp per row: the candidates below k are
+// collected in order (a warp scan of the words' bit counts); with 1 to 32 of
+// them, FP32 distances with rigorous bounds (four lanes per candidate,
+// eight at a time), then the candidates whose lower bound reaches the
+// smallest upper bound decide: one is the label, up to eight go to FP64,
+// more (or none, or more than 32 candidates) to the exhaustive re-score.
+constexpr int MASK_CANDS = 32;
+constexpr int MASK_WARPS = 8;
+
+__device__ __forceinline__ int mask_column(int w, int b) {
+    return 32 * w + (b < 16 ? 2 * (15 - b) : 2 * (31 - b) + 1);
+}
+
+__global__ void __launch_bounds__(MASK_WARPS * 32)
+    mask_rescore_kernel(const float *__restrict__ x, int d, const float *__restrict__ c32,
+                        const float *__restrict__ ec32, int k, const uint32_t *__restrict__ masks, int wpr,
+                        const int32_t *__restrict__ list, DevScalars *sc, int32_t *__restrict__ labels,
+                        Oct *__restrict__ f64_items, int32_t *__restrict__ ex_list) {
+    __shared__ int cand_sm[MASK_WARPS][MASK_CANDS];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int *cand = cand_sm[wid];
+    const unsigned long long cnt = sc->full_count;
+    const unsigned long long nw = (unsigned long long)gridDim.x * MASK_WARPS;
+    for (unsigned long long s = (unsigned long long)blockIdx.x * MASK_WARPS + wid; s < cnt; s += nw) {
+        const int row = list[s];
+        const uint32_t *mw = masks + (int64_t)s * wpr;
+        int m = 0;  // candidates so far (warp-uniform)
+        for (int w0 = 0; w0 < wpr; w0 += 32) {
+            const int w = w0 + lane;
+            uint32_t word = w < wpr ? mw[w] : 0u;
+            if (32 * w + 32 > k) {  // centres at or above k are padding
+                uint32_t keep = 0u;
+                for (int b = 0; b < 32; b++)
+                    if (mask_column(w, b) < k) keep |= 1u << b;
+                word &= keep;
+            }
+            const int c = __popc(word);
+            int incl = c;
+#pragma unroll
+            for (int off = 1; off < 32; off <<= 1) {
+                const int t = __shfl_up_sync(0xffffffffu, incl, off);
+                if (lane >= off) incl += t;
+            }
+            const int total = __shfl_sync(0xffffffffu, incl, 31);
+            if (m + total <= MASK_CANDS) {
+                // this lane's candidates in increasing centre order
+                int pos = m + incl - c;
+                uint32_t lo = word & 0xFFFFu, hi = word >> 16;
+                for (int j = 0; j < 16; j++) {  // centre 32 w + 2 j + parity: bit 15 - j (even), 31 - j (odd)
+                    if ((lo >> (15 - j)) & 1u) cand[pos++] = 32 * w + 2 * j;
+                    if ((hi >> (15 - j)) & 1u) cand[pos++] = 32 * w + 2 * j + 1;
+                }
+            }
+            m += total;
+        }
+        __syncwarp();
+        bool to_ex = m == 0 || m > MASK_CANDS;
+        if (!to_ex) {
+            float my_dist = 0.f;
+            for (int r0 = 0; r0 < m; r0 += 8) {
+                const int cj = r0 + (lane >> 2);
+                float acc = 0.f;
+                if (cj < m) acc = sq_partial(x + (int64_t)row * d, c32 + (int64_t)cand[cj] * d, d, lane & 3, 4);
+                acc += __shfl_xor_sync(0xffffffffu, acc, 2);
+                acc += __shfl_xor_sync(0xffffffffu, acc, 1);
+#pragma unroll
+                for (int j = 0; j < 8; j++) {
+                    const float v = __shfl_sync(0xffffffffu, acc, 4 * j);
+                    if (lane == r0 + j) my_dist = v;
+                }
+            }
+            const bool is_cand = lane < m;
+            const int my_id = is_cand ? cand[lane] : INT32_MAX;
+            const float my_err = is_cand ? bound32(my_dist, ec32[my_id], d) : 0.f;
+            float ub = is_cand ? __fadd_ru(my_dist, my_err) : INFINITY;
+#pragma unroll
+            for (int off = 16; off >= 1; off >>= 1) ub = fminf(ub, __shfl_xor_sync(0xffffffffu, ub, off));
+            const unsigned surv = __ballot_sync(0xffffffffu, is_cand && !(__fsub_rd(my_dist, my_err) > ub));
+            const int nsurv = __popc(surv);
+            if (nsurv == 1) {
+                const int only = __shfl_sync(0xffffffffu, my_id, __ffs(surv) - 1);
+                if (lane == 0) labels[row] = only;
+                if (lane == 0) atomicAdd(&sc->quad_count, 1ULL);
+            } else {
+                // the survivors (all candidates if no FP32 value was finite)
+                const unsigned take = nsurv == 0 ? __ballot_sync(0xffffffffu, is_cand) : surv;
+                if (__popc(take) <= 8) {
+                    int ids[8];
+                    int mm = 0;
+                    unsigned rest = take;
+#pragma unroll
+                    for (int j = 0; j < 8; j++) {  // take is warp-uniform, so every lane shuffles
+                        const int v = __shfl_sync(0xffffffffu, my_id, rest ? __ffs(rest) - 1 : 0);
+                        ids[j] = rest ? v : 0;
+                        if (rest) {
+                            rest &= rest - 1u;
+                            mm++;
+                        }
+                    }
+                    queue_f64(f64_items, sc, row, mm, ids);
+                    if (lane == 0) atomicAdd(&sc->quad_count, 1ULL);
+                } else {
+                    to_ex = true;
+                }
+            }
+        }
+        if (to_ex && lane == 0) ex_list[atomicAdd(&sc->ex_count, 1ULL)] = row;
+        __syncwarp();  // cand is reused by the next row
+    }
+}
+
+// BF16 rows of the main pass's operand copied for the listed rows (slot s =
+// row list[s]), 16 bytes per thread.
+__global__ void gather_xq_rows_kernel(const uint4 *__restrict__ xq, int pieces, const int32_t *__restrict__ list,
+                                      const unsigned long long *count, uint4 *__restrict__ out) {
+    const unsigned long long total = *count * (unsigned long long)pieces;
+    for (unsigned long long e = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+         e += (unsigned long long)gridDim.x * blockDim.x) {
+        const unsigned long long s = e / (unsigned)pieces;
+        const int q = (int)(e - s * (unsigned)pieces);
+        out[e] = xq[(int64_t)list[s] * pieces + q];
+    }
+}
+
 // The FP64 decisions: one warp per queued row stages the widened row and its
 // candidate centres (rows padded by one double) in shared memory, then lane
 // j < m sums candidate j in the oracle's order (sqeuc64's arithmetic from
@@ -1380,12 +1525,47 @@ float mu_norm_up(double v) {
     return (double)f >= v ? f : std::nextafter(f, INFINITY);
 }
 
-// Second pass over the rows listed in full (count sc->full_count): BF16
-// operands made from their f32 values, a top-8 tensor pass, then the
-// re-score of at most eight candidates, or of every centre.
+// Second pass over the rows listed in full (count sc->full_count). After a
+// BF16 main pass: the rows' BF16 operands gathered from the main pass's
+// copy, a tensor pass that marks every centre scoring at least the row's
+// threshold, then the re-score of at most 32 candidates, or of every centre.
+// After an FP8 main pass: BF16 operands made from the rows' f32 values, a
+// top-8 tensor pass, then the re-score of at most eight candidates, or of
+// every centre.
 void second_pass(Ctx &ctx, const float *x, int64_t n, int d, const double *c, int k, const MixedBufs &B,
-                 double mu_norm, const int32_t *full, int32_t *labels, DevScalars *sc, Oct *f64_items) {
+                 double mu_norm, const int32_t *full, const float *full_thresh, int32_t *labels, DevScalars *sc,
+                 Oct *f64_items) {
     cudaStream_t s = ctx.stream;
+    const int grid = ctx.num_sms * 4;
+    int32_t *ex = (int32_t *)ctx.get(BUF_EX, sizeof(int32_t) * (size_t)n);
+    if (!ctx.mixed.fp8) {
+        // BF16 main pass: the same operands again for the listed rows, with
+        // candidate masks against the thresholds the finalize left.
+        const MixedPlan &mp = ctx.mixed;
+        MixedPlan &mm = ctx.mixedm;
+        if (mm.n != n || mm.d != d || mm.k != k || mm.kp != mp.kp) plan_tc(ctx, mm, n, d, k, false, 1, mp.kp);
+        if (mm.k_pad != mp.k_pad || mm.d_pad != mp.d_pad) {
+            set_error("mask pass plan (k_pad %d, d_pad %d) differs from the main pass (%d, %d)", mm.k_pad, mm.d_pad,
+                      mp.k_pad, mp.d_pad);
+            fail(FK_ERR_CUDA);
+        }
+        void *xb2 = ctx.get(BUF_XB2, sizeof(__nv_bfloat16) * (size_t)n * mm.d_pad);
+        const int wpr = mm.k_pad / 32;
+        uint32_t *masks = (uint32_t *)ctx.get(BUF_MASKS, sizeof(uint32_t) * (size_t)n * wpr);
+        const int pieces = mm.d_pad * 2 / 16;
+        gather_xq_rows_kernel<<<ctx.num_sms * 8, 256, 0, s>>>((const uint4 *)B.xq, pieces, full, &sc->full_count,
+                                                              (uint4 *)xb2);
+        FK_LAUNCH_CHECK();
+        launch_tc_assign(ctx, mm, xb2, B.cq, B.caug, nullptr, nullptr, sc, B.stats, nullptr, &sc->full_count,
+                         nullptr, nullptr, masks, full_thresh);
+        mask_rescore_kernel<<<grid / 2, MASK_WARPS * 32, 0, s>>>(x, d, B.c32, B.ec32, k, masks, wpr, full, sc,
+                                                                  labels, f64_items, ex);
+        FK_LAUNCH_CHECK();
+        exhaustive_rescore_kernel<<<ctx.num_sms * 2, EX_THREADS, exhaustive_smem_bytes(d, k), s>>>(
+            x, d, c, B.c32t, B.ec32, k, ex, &sc->ex_count, sc, labels);
+        FK_LAUNCH_CHECK();
+        return;
+    }
     MixedPlan &m2 = ctx.mixed2;
     if (m2.n != n || m2.d != d || m2.k != k) plan_tc(ctx, m2, n, d, k, false, 8);
     MixedStats *st2 = (MixedStats *)ctx.get(BUF_STATS2, sizeof(MixedStats));
@@ -1396,7 +1576,6 @@ void second_pass(Ctx &ctx, const float *x, int64_t n, int d, const double *c, in
     double *hn2 = (double *)ctx.get(BUF_HALF2, sizeof(double) * (size_t)m2.k_pad);
     Top8 *top8 = (Top8 *)ctx.get(BUF_TOP8, sizeof(Top8) * (size_t)n * m2.parts);
     Oct *octs = (Oct *)ctx.get(BUF_OCT, sizeof(Oct) * (size_t)n);
-    int32_t *ex = (int32_t *)ctx.get(BUF_EX, sizeof(int32_t) * (size_t)n);
     FK_CUDA(cudaMemsetAsync(st2, 0, sizeof(MixedStats), s));
     launch_prep_rows<float, false>(ctx, x, n, d, m2.d_pad, B.mu32, xb2, nullptr, ri2, st2, full, &sc->full_count);
     prep_centres_kernel<false><<<(m2.k_pad + 7) / 8, 256, 0, s>>>(c, k, m2.k_pad, d, m2.d_pad, B.mu, cb2, hn2,
@@ -1406,7 +1585,6 @@ void second_pass(Ctx &ctx, const float *x, int64_t n, int d, const double *c, in
     FK_LAUNCH_CHECK();
     launch_tc_assign(ctx, m2, xb2, cb2, caug2, nullptr, top8, sc, st2, nullptr, &sc->full_count);
     const float acc_rel2 = (float)((double)((size_t)m2.d_pad + 32) * ACC_REL_PER_K);  // exact: integer * 2^-22
-    const int grid = ctx.num_sms * 4;
     finalize8_kernel<<<grid, 256, 0, s>>>(top8, m2.parts, n, k, d, full, ri2, st2, acc_rel2, mu_norm_up(mu_norm),
                                           labels, octs, ex, sc);
     FK_LAUNCH_CHECK();
@@ -1450,9 +1628,11 @@ void run_assign_mixed(Ctx &ctx, const TX *x, int64_t n, int d, const double *c, 
 
     int4 *pairs = (int4 *)ctx.get(BUF_FLAGS, sizeof(int4) * (size_t)n);
     int32_t *full = (int32_t *)ctx.get(BUF_FULL, sizeof(int32_t) * (size_t)n);
+    float *full_thresh = fp8 ? nullptr : (float *)ctx.get(BUF_THRESH, sizeof(float) * (size_t)n);
     const float acc_rel = (float)((double)((size_t)mp.d_pad + 32) * ACC_REL_PER_K);  // exact: integer * 2^-22
     finalize_kernel<<<(unsigned)((n + FINALIZE_THREADS - 1) / FINALIZE_THREADS), FINALIZE_THREADS, 0, s>>>(
-        top, mp.parts, n, k, d, B.rowinfo, B.stats, acc_rel, mu_norm_up(mp.mu_norm), labels, pairs, full, sc);
+        top, mp.parts, n, k, d, B.rowinfo, B.stats, acc_rel, mu_norm_up(mp.mu_norm), labels, pairs, full,
+        full_thresh, sc);
     FK_LAUNCH_CHECK();
     const int grid = ctx.num_sms * 4;
     Oct *f64_items = (Oct *)ctx.get(BUF_F64ITEMS, sizeof(Oct) * (size_t)n);
@@ -1462,7 +1642,7 @@ void run_assign_mixed(Ctx &ctx, const TX *x, int64_t n, int d, const double *c, 
     else
         pair_rescore_kernel<TX><<<grid, 256, 0, s>>>(x, d, c, B.c32, B.ec32, pairs, sc, labels, f64_items);
     FK_LAUNCH_CHECK();
-    second_pass(ctx, x, n, d, c, k, B, mp.mu_norm, full, labels, sc, f64_items);
+    second_pass(ctx, x, n, d, c, k, B, mp.mu_norm, full, full_thresh, labels, sc, f64_items);
     launch_f64_decide<TX>(ctx, x, d, c, f64_items, sc, labels);
 }
 

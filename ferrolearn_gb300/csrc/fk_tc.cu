@@ -63,11 +63,13 @@ __device__ __forceinline__ int unpack_local(uint32_t l, int base) { return l == 
 // pass, `slots` rotating slots (see the tile merge in the kernel) of EP - 1
 // records per row -- whole records for BF16 with two parts, 16-byte ones
 // otherwise (FP8, whose larger X stages leave less room, and four parts) --
-// and one slot of top-8 records for the second pass.
+// and one slot of top-8 records for the second pass; none for the mask pass,
+// whose parts write their own words of the row's candidate mask.
 __host__ __device__ constexpr uint32_t merge_bytes(int topk, bool fp8, int ep, int slots) {
-    return topk == 2 ? BM * (uint32_t)slots * (uint32_t)(ep - 1) *
-                           (uint32_t)((fp8 || ep > 2) ? sizeof(HalfRec) : sizeof(Top2))
-                     : BM * (uint32_t)sizeof(Top8);
+    return topk == 1   ? 0u
+           : topk == 2 ? BM * (uint32_t)slots * (uint32_t)(ep - 1) *
+                             (uint32_t)((fp8 || ep > 2) ? sizeof(HalfRec) : sizeof(Top2))
+                       : BM * (uint32_t)sizeof(Top8);
 }
 
 // The record of one slot (FP8: HalfRec; BF16: Top2, no packing).
@@ -134,6 +136,9 @@ struct TcParams {
     const float *rowscale;    // FP8: per-row power of two 1/(s_i t) that maps scores to this row's units
     uint32_t off_xaug;        // FP8: per-stage augmentation tiles
     float *dump;  // optional: raw accumulators of the first tile of CTA 0 (tests only)
+    uint32_t *masks;       // mask pass: wpr words per row, bit per centre (layout at mask_chunk)
+    const float *thresh;   // mask pass: per-row threshold in score units
+    int wpr;               // mask words per row (k_pad / 32)
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -347,6 +352,33 @@ struct RankChunk<CH, 32> {
     static __device__ __forceinline__ void run(const uint32_t (&)[32], float, float, float (&)[NCH], float (&)[NCH]) {}
 };
 
+// ------------------------------------------------ mask (second pass) --
+// One 32-column chunk of a row's candidate mask: column e is a candidate
+// when its score T_e >= th. fma.sat(T, S, C) with S = 8 / ulp and C = -th S
+// is exactly 0 or 1: T and th are floats of at least 2^(E-2) (the caller
+// sends every lower threshold to -inf), so a nonzero T - th is a multiple
+// of 2^(E-25) and (T - th) S a nonzero multiple of 2, whose rounding keeps
+// its sign; a padded column (T = 0) gives 0, or 1 with th = -inf; NaN
+// gives 0. Horner steps on packed pairs, acc = 2 acc + (bit even, bit
+// odd), exact below 2^16, put the even columns 2j in bits 15 - j of the low
+// half and the odd columns 2j + 1 in bits 31 - j: one saturating FMA per
+// score and one packed FMA per two scores, no ALU instruction.
+__device__ __forceinline__ uint32_t mask_chunk(const uint32_t (&r)[32], float S, float C, uint64_t two2) {
+    uint64_t acc = 0ull;  // {0.f, 0.f}
+#pragma unroll
+    for (int j = 0; j < 16; j++) {
+        float b0, b1;
+        asm("fma.rn.sat.f32 %0, %1, %2, %3;" : "=f"(b0) : "f"(__uint_as_float(r[2 * j])), "f"(S), "f"(C));
+        asm("fma.rn.sat.f32 %0, %1, %2, %3;" : "=f"(b1) : "f"(__uint_as_float(r[2 * j + 1])), "f"(S), "f"(C));
+        uint64_t bb;
+        asm("mov.b64 %0, {%1, %2};" : "=l"(bb) : "f"(b0), "f"(b1));
+        asm("fma.rn.f32x2 %0, %0, %1, %2;" : "+l"(acc) : "l"(two2), "l"(bb));
+    }
+    float e, o;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(e), "=f"(o) : "l"(acc));
+    return (uint32_t)e | ((uint32_t)o << 16);
+}
+
 // ------------------------------------------------ top-8 (second pass) --
 // Sorted insertion of key k into a[0] >= ... >= a[K-1] (2K - 1 min/max).
 template <int K>
@@ -558,6 +590,58 @@ __global__ void __launch_bounds__(tc_threads(EP), 1)
             }
             // Drain: the last commit covers every MMA issued before it.
             if (last_s >= 0) mbar_wait(bar_xempty(last_s), last_ph, abort_flag, p.err, 0ull);
+        }
+    } else if (TOPK == 1) {
+        // Mask pass: every part writes its 128 columns' words of each row's
+        // mask straight to global memory (no exchange between the parts).
+        constexpr int CP = BN / EP;
+        constexpr int NCK = CP / 32;
+        static_assert(NCK == 4, "the mask pass runs with two epilogue parts");
+        const int ew = warp - 2;
+        const int quarter = warp & 3;
+        const int prt = ew >> 2;
+        const int row_local = quarter * 32 + lane;
+        const uint32_t lane_addr = tmem + ((uint32_t)(quarter * 32) << 16);
+        const float S = 8.f / p.stats->ulp;  // a power of two
+        uint64_t two2;
+        asm("mov.b64 %0, {%1, %1};" : "=l"(two2) : "f"(2.f));
+        uint32_t item = 0;
+        bool dead = false;
+        for (int64_t t = q; t < p.tiles; t += tstride) {
+            const int64_t row = t * BM + row_local;
+            const float th = row < p.n ? p.thresh[row] : INFINITY;
+            const float C = -(th * S);  // exact: a float times a power of two
+            for (int b = 0; b < p.nblocks; b++, item++) {
+                const int buf = (int)(item & 1u);
+                const uint32_t aph = (item >> 1) & 1u;
+                if (!dead && !mbar_wait(bar_afull(buf), aph, abort_flag, p.err, 16ull)) dead = true;
+                dead = __any_sync(0xffffffffu, dead);
+                if (dead) continue;
+                tc_fence_after();
+                const uint32_t col = lane_addr + (uint32_t)buf * BN + (uint32_t)prt * CP;
+                uint32_t ra[32], rb[32];
+                uint4 w;
+                tmem_ld32(col, ra);
+                tmem_wait(ra);
+                tmem_ld32(col + 32, rb);
+                w.x = mask_chunk(ra, S, C, two2);
+                tmem_wait(rb);
+                tmem_ld32(col + 64, ra);
+                w.y = mask_chunk(rb, S, C, two2);
+                tmem_wait(ra);
+                tmem_ld32(col + 96, rb);
+                w.z = mask_chunk(ra, S, C, two2);
+                tmem_wait(rb);
+                // every column of this block is in registers: release the buffer
+                tc_fence_before();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(bar_aempty(buf));
+                w.w = mask_chunk(rb, S, C, two2);
+                if (row < p.n) {
+                    const int word = (part * p.kp + b * BN + prt * CP) / 32;  // a multiple of 4
+                    *reinterpret_cast<uint4 *>(p.masks + row * (int64_t)p.wpr + word) = w;
+                }
+            }
         }
     } else if (TOPK == 2) {
         constexpr int CP = BN / EP;   // columns of one part
@@ -877,7 +961,9 @@ constexpr size_t SMEM_LIMIT = 227 * 1024;
 
 // The launch shape of one tensor-core pass (host arithmetic only): the X
 // ring depth, the resident slice of centres that fits next to it, the grid.
-void plan_shape(MixedPlan &mp, int64_t n, int d, int k, bool fp8, int topk, int sms) {
+// kp_fixed > 0 imposes the slice size of another plan (the mask pass reads
+// the main pass's centre operands, so it must slice them the same way).
+void plan_shape(MixedPlan &mp, int64_t n, int d, int k, bool fp8, int topk, int sms, int kp_fixed) {
     mp.n = n;
     mp.d = d;
     mp.k = k;
@@ -902,7 +988,7 @@ void plan_shape(MixedPlan &mp, int64_t n, int d, int k, bool fp8, int topk, int 
         for (; xst >= 1; xst--) {
             fixed = 1024 + xst * x_stage + (fp8 ? xst * XAUG_BYTES : ONES_BYTES) +
                     merge_bytes(topk, fp8, mp.ep, mp.slots) + BAR_BYTES;
-            if (fixed + BN * per_centre <= SMEM_LIMIT) break;
+            if (fixed + (size_t)(kp_fixed > 0 ? kp_fixed : BN) * per_centre <= SMEM_LIMIT) break;
         }
         if (xst < 1) {
             set_error("the resident-slice tensor-core kernel supports d <= %d for this precision (got %d)",
@@ -910,7 +996,7 @@ void plan_shape(MixedPlan &mp, int64_t n, int d, int k, bool fp8, int topk, int 
             fail(FK_ERR_UNSUPPORTED);
         }
         mp.xst = xst;
-        const int kp_max = (int)((SMEM_LIMIT - fixed) / per_centre) / BN * BN;
+        const int kp_max = kp_fixed > 0 ? kp_fixed : (int)((SMEM_LIMIT - fixed) / per_centre) / BN * BN;
         mp.parts = (k + kp_max - 1) / kp_max;
         mp.kp = ((k + mp.parts - 1) / mp.parts + BN - 1) / BN * BN;
         mp.k_pad = mp.parts * mp.kp;
@@ -929,8 +1015,8 @@ void plan_shape(MixedPlan &mp, int64_t n, int d, int k, bool fp8, int topk, int 
     mp.smem = fixed + (size_t)mp.kp * per_centre;
 }
 
-void plan_tc(Ctx &ctx, MixedPlan &mp, int64_t n, int d, int k, bool fp8, int topk) {
-    plan_shape(mp, n, d, k, fp8, topk, ctx.num_sms);
+void plan_tc(Ctx &ctx, MixedPlan &mp, int64_t n, int d, int k, bool fp8, int topk, int kp_fixed) {
+    plan_shape(mp, n, d, k, fp8, topk, ctx.num_sms, kp_fixed);
     mp.tm_x_ptr = mp.tm_c_ptr = mp.tm_aug_ptr = mp.tm_xaug_ptr = nullptr;
     if (!mp.ones) {
         uint16_t h[BM * 16];
@@ -944,9 +1030,11 @@ void plan_tc(Ctx &ctx, MixedPlan &mp, int64_t n, int d, int k, bool fp8, int top
 
 void launch_tc_assign(Ctx &ctx, MixedPlan &mp, const void *xb, const void *cb, const void *caug, Top2 *out,
                       Top8 *out8, DevScalars *sc, const MixedStats *stats, float *dump,
-                      const unsigned long long *n_dev, const void *xaug, const float *rowscale) {
+                      const unsigned long long *n_dev, const void *xaug, const float *rowscale, uint32_t *masks,
+                      const float *thresh) {
     const bool fp8 = mp.fp8;
-    if ((mp.topk == 2) != (out != nullptr) || (mp.topk == 8) != (out8 != nullptr)) {
+    if ((mp.topk == 2) != (out != nullptr) || (mp.topk == 8) != (out8 != nullptr) ||
+        (mp.topk == 1) != (masks != nullptr && thresh != nullptr) || (mp.topk == 1 && fp8)) {
         set_error("tensor-core launch: records do not match the plan");
         fail(FK_ERR_INVALID_PARAMETER);
     }
@@ -1003,6 +1091,9 @@ void launch_tc_assign(Ctx &ctx, MixedPlan &mp, const void *xb, const void *cb, c
     p.stats = stats;
     p.rowscale = rowscale;
     p.dump = dump;
+    p.masks = masks;
+    p.thresh = thresh;
+    p.wpr = mp.k_pad / 32;
     const size_t smem = (size_t)p.off_bar + BAR_BYTES + 1024;
     if (smem > SMEM_LIMIT) {
         set_error("tensor-core plan needs %zu bytes of shared memory", smem);
@@ -1015,8 +1106,10 @@ void launch_tc_assign(Ctx &ctx, MixedPlan &mp, const void *xb, const void *cb, c
         kern<<<mp.grid, tc_threads(mp.ep), smem, ctx.stream>>>(*tx, *tcm, *ta, *to, p);
     };
     // Instantiations: main pass (top-2) BF16 / FP8 with one or two X stages;
-    // second pass (top-8) BF16 with one or two X stages.
-    if (mp.topk == 8) {
+    // second pass (top-8, or candidate masks) BF16 with one or two X stages.
+    if (mp.topk == 1) {
+        mp.xst == 2 ? go(tc_assign_kernel<1, false, 2, 2>) : go(tc_assign_kernel<1, false, 1, 2>);
+    } else if (mp.topk == 8) {
         if (fp8) {
             set_error("the second pass runs in BF16");
             fail(FK_ERR_UNSUPPORTED);

@@ -352,6 +352,75 @@ def test_fp8_bisector_at_full_k_and_d_matches_fp64_oracle():
     assert np.array_equal(g.predict(xp), O.predict(g.cluster_centers(), xp.astype(np.float64)))
 
 
+def test_bf16_mask_pass_at_full_k_and_d_matches_fp64_oracle():
+    # the BF16 form at k = 4096, d = 256 (200,000 rows of the bisector
+    # workload): the main pass and the mask pass both run many centre slices,
+    # so every slice writes its own words of a row's candidate mask; rows
+    # equidistant from three centres of far-apart slices are in the mask
+    # pass for sure; labels, centres and inertia against the FP64 oracle
+    w = W.bisector_4096x256(scale=0.025, predict_scale=0.01)
+    x32, k = w["x"].copy(), w["k"]
+    n = x32.shape[0]
+    torch = pytest.importorskip("torch")
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    assert _plan(n, 256, k, F.MIXED_BF16, 2, sms)["parts"] > 1
+    c = w["init"]
+    rng = np.random.default_rng(23)
+    x32[:400] = _equidistant_rows(c, [7, 2100, 4090], 400, rng).astype(np.float32)
+    x32[400:460] = _equidistant_rows(c, [300, 1300, 2300, 3300, 4000, 4095], 60, rng).astype(np.float32)
+    gl, gc, gi, gs, rep = F.lloyd_step(x32, c, dtype="f32x64", precision="bf16")
+    ol, oc, oi, os_ = O.lloyd_step(x32.astype(np.float64), c)
+    assert np.array_equal(gl, ol)
+    assert _close(gc, oc)
+    assert abs(gi - oi) <= INERTIA_RTOL_MIXED * oi
+    assert rep["rows_second_pass"] >= 400
+
+
+def test_bf16_mask_pass_sends_wide_ties_to_the_exhaustive_rescore():
+    # forty copies of one centre: a row near it has forty exactly tied
+    # candidates, more than the mask pass re-scores (32), so it is re-scored
+    # against every centre; six-way near-ties stay in the mask pass. Labels
+    # are the FP64 oracle's (the lowest index among exact ties).
+    rng = np.random.default_rng(21)
+    d, k = 64, 300
+    c = rng.uniform(-10, 10, size=(k, d))
+    c[10:50] = c[10]
+    c[[101, 102, 103, 104, 106, 107]] = c[101] + rng.normal(0, 0.5, size=(6, d))
+    x = c[rng.integers(0, k, 6000)] + rng.normal(0, 1, size=(6000, d))
+    x[:200] = c[10] + rng.normal(0, 1, size=(200, d))
+    x[200:260] = _equidistant_rows(c, [101, 102, 103, 104, 106, 107], 60, rng)
+    x32 = x.astype(np.float32)
+    gl, gc, gi, gs, rep = F.lloyd_step(x32, c, dtype="f32x64", precision="bf16")
+    ol, oc, oi, os_ = O.lloyd_step(x32.astype(np.float64), c)
+    assert np.array_equal(gl, ol)
+    assert _close(gc, oc)
+    assert rep["rows_exhaustive"] >= 200
+
+
+def test_bf16_rows_not_16_byte_aligned_match_the_oracle():
+    # X on the device one float past a 16-byte boundary: every kernel that
+    # reads the f32 rows in 16-byte pieces must take its one-float path
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(22)
+    n, d, k = 20000, 64, 256
+    c = rng.uniform(-5, 5, size=(k, d))
+    x32 = (c[rng.integers(0, k, n)] + rng.normal(0, 2.0, size=(n, d))).astype(np.float32)
+    buf = torch.empty(n * d + 1, dtype=torch.float32, device="cuda")
+    xd = buf[1:].view(n, d)
+    xd.copy_(torch.from_numpy(x32))
+    assert xd.data_ptr() % 16 == 4
+    x64 = x32.astype(np.float64)
+    gl, gc, gi, gs, rep = F.lloyd_step(xd, c, dtype="f32x64", precision="bf16")
+    ol, oc, oi, os_ = O.lloyd_step(x64, c)
+    assert np.array_equal(gl, ol)
+    assert _close(gc, oc)
+    g = F.KMeans(k, dtype="f32x64").with_precision("bf16").with_max_iter(4).with_tol(0.0).with_n_init(1) \
+        .with_init_centers(c).fit(xd)
+    o = O.fit(x64, k, max_iter=4, tol=0.0, n_init=1, init=c[None])
+    assert np.array_equal(g.labels(), o["labels"])
+    assert _close(g.cluster_centers(), o["centers"])
+
+
 @pytest.mark.parametrize("precision", PRECISIONS)
 @pytest.mark.parametrize("scale", [1e-35, 1e-20, 1e15, 1e18])
 def test_mixed_extreme_scales_fall_back_exactly(precision, scale):
