@@ -830,10 +830,22 @@ def run_ours(args):
         tp = (C.c_double * 2)()
         _native.lib().fk_debug_measure_tc_peaks(ctx.handle, tp)
         tc_loop = {"bf16_tflops": tp[0] / 1e12, "e4m3_tflops": tp[1] / 1e12}
+    n_count = int(rep.get("count_iterations", 0))
+    count_ms = rep["ms_count_pass"] / n_count if n_count else None
+    top2_ms = (rep["ms_contract"] - rep.get("ms_count_pass", 0.0)) / (iters - n_count) if iters > n_count else None
     if form == "bf16":
         peak, src = pick_tensor_peak(peaks, clk)
-        roof = {"bound": "tensor", "achieved": flops / (contract_ms / 1e3) / 1e12, "peak": peak, "unit": "TFLOP/s",
+        # the dominant kernel: the count pass when it ran most iterations
+        dom_ms = count_ms if n_count * 2 > iters else (top2_ms or contract_ms)
+        roof = {"bound": "tensor", "achieved": flops / (dom_ms / 1e3) / 1e12, "peak": peak, "unit": "TFLOP/s",
                 "peak_source": src, "own_mma_loop": tc_loop}
+        if n_count and top2_ms:
+            other = top2_ms if dom_ms == count_ms else count_ms
+            roof["other_main_pass"] = {
+                "kernel": "tc_assign_kernel<2> (top-2 ranking)" if dom_ms == count_ms else
+                          "tc_assign_kernel<3> (count pass)",
+                "iterations": iters - n_count if dom_ms == count_ms else n_count, "ms_per_launch": other,
+                "achieved": flops / (other / 1e3) / 1e12, "frac": flops / (other / 1e3) / 1e12 / peak}
     elif form == "fp8":
         roof = {"bound": "tensor", "achieved": flops / (contract_ms / 1e3) / 1e12, "peak": tc_loop["e4m3_tflops"],
                 "unit": "TFLOP/s", "peak_source": "dense E4M3 rate measured in this run by the library's own "
@@ -856,9 +868,14 @@ def run_ours(args):
         roof["traffic_source"] = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch at 1,000,000 rows "
                                   "(profiles/tc_assign_anisotropic_1024x128_quarter.md), scaled to n rows")
         roof["algorithmic_bytes"] = n * d * 2 + n * 2 * 32  # BF16 X once + 32-byte records per row and slice
-    roof["kernel"] = f"tc_assign_kernel ({form.upper()} tcgen05 contraction + top-2 epilogue)" if mixed else \
-        "assign_direct_kernel (whole assignment phase)"
-    roof["ms_per_launch"] = contract_ms if mixed else assign_ms
+    if form == "bf16" and n_count * 2 > iters:
+        roof["kernel"] = (f"tc_assign_kernel<3> (BF16 tcgen05 contraction + count epilogue against carried "
+                          f"thresholds; {n_count} of {iters} iterations)")
+        roof["ms_per_launch"] = count_ms
+    else:
+        roof["kernel"] = f"tc_assign_kernel ({form.upper()} tcgen05 contraction + top-2 epilogue)" if mixed else \
+            "assign_direct_kernel (whole assignment phase)"
+        roof["ms_per_launch"] = (top2_ms or contract_ms) if mixed else assign_ms
 
     out = {
         "metric": METRIC, "value": ips, "unit": "iters/s", "n_gpus": world, "steps": args.steps,
@@ -869,6 +886,8 @@ def run_ours(args):
         "pt_k_per_s": ips * n * k,
         "phase_ms_per_iter": {"assign": assign_ms, "contract": contract_ms if mixed else None,
                               "update": rep["ms_update"] / iters},
+        "main_pass": {"count_iterations": n_count, "count_ms_per_launch": count_ms,
+                      "top2_iterations": iters - n_count, "top2_ms_per_launch": top2_ms} if mixed else None,
         "recheck": {"rows": rep["rows_rechecked"], "full_rescan": rep["rows_full_rescan"],
                     "fp64_rows": rep["rows_fp64"], "second_pass": rep["rows_second_pass"],
                     "few_candidates": rep["rows_few"], "exhaustive": rep["rows_exhaustive"],

@@ -131,6 +131,8 @@ class FitReport(C.Structure):
         ("reserved", C.c_int32),
         ("rows_moved", C.c_int64),
         ("updates_incremental", C.c_int64),
+        ("count_iterations", C.c_int64),
+        ("ms_count_pass", C.c_double),
     ]
 
     def as_dict(self):

@@ -201,7 +201,8 @@ enum UpdateMode { UPDATE_FULL = 0, UPDATE_FULL_STATE = 1, UPDATE_INCREMENTAL = 2
 template <typename TX, typename TC>
 void lloyd_iteration(Ctx &ctx, const TX *x, int64_t n, int d, const TC *c, int k, int prec, TC *nc,
                      int32_t *labels, DevScalars *sc, const SortPlan &plan, bool x_changed, fk_fit_report *rep,
-                     bool timing, int mode = UPDATE_FULL, const int32_t *prev_labels = nullptr) {
+                     bool timing, int mode = UPDATE_FULL, const int32_t *prev_labels = nullptr,
+                     const TC *prev_c = nullptr) {
     cudaStream_t s = ctx.stream;
     int32_t *members = (int32_t *)ctx.get(BUF_MEMBERS, sizeof(int32_t) * (size_t)n);
     int32_t *seg = (int32_t *)ctx.get(BUF_SEGHIST, sizeof(int32_t) * (size_t)plan.k * plan.nseg);
@@ -209,6 +210,7 @@ void lloyd_iteration(Ctx &ctx, const TX *x, int64_t n, int d, const TC *c, int k
     // the contraction's timer writes into this call's report: set only for
     // the assignment below (a pointer left behind would outlive the report)
     ctx.contract_acc = (timing && rep) ? &rep->ms_contract : nullptr;
+    ctx.count_acc = (timing && rep) ? &rep->ms_count_pass : nullptr;
     {
         Timer t(timing, ctx, rep ? &rep->ms_assign : nullptr);
         if (prec == FK_PRECISION_PLAIN) {
@@ -218,11 +220,13 @@ void lloyd_iteration(Ctx &ctx, const TX *x, int64_t n, int d, const TC *c, int k
             launch_sum_fixed<TC>(mind, n, part, &sc->inertia, s);
         } else {
             if constexpr (std::is_same<TX, float>::value && std::is_same<TC, double>::value) {
-                run_assign_mixed(ctx, x, n, d, c, k, prec, labels, nullptr, sc, x_changed);
+                run_assign_mixed(ctx, x, n, d, c, k, prec, labels, nullptr, sc, x_changed, prev_c,
+                                 prev_c ? prev_labels : nullptr);
             }
         }
     }
     ctx.contract_acc = nullptr;
+    ctx.count_acc = nullptr;
     {
         Timer t(timing, ctx, rep ? &rep->ms_update : nullptr);
         if constexpr (std::is_same<TX, float>::value && std::is_same<TC, double>::value) {
@@ -426,6 +430,19 @@ fk_status fit_impl(fk_ctx *ctxp, const TX *x_in, int64_t n, int64_t d, const fk_
         // GPU never waits for the host. A converged iteration's successor is
         // discarded (it touched neither the converged centres, nor their
         // input, nor the labels).
+        // BF16 on f32 X: from the fourth iteration on, the main pass may be
+        // the count pass (thresholds carried from the previous iteration). It
+        // runs while the last iteration whose statistics are in (they are
+        // read one iteration late) re-checked at most a quarter of the rows;
+        // a count iteration that sent more than a tenth of the rows to the
+        // second pass, or 0.2% to the exhaustive re-score, holds it off for
+        // the next two iterations (the centres still move too much for the
+        // carried bound).
+        bool count_ok = false, calm = false;
+        if constexpr (std::is_same<TX, float>::value && std::is_same<TC, double>::value)
+            count_ok = p->precision == FK_PRECISION_MIXED_BF16;
+        bool was_count[2] = {false, false};
+        int64_t count_from = 3;
         auto finish = [&](int64_t r) {
             FK_CUDA(cudaEventSynchronize(iter_done[r & 1]));
             const DevScalars &h = ctx.host_scalars[1 + (r & 1)];
@@ -433,6 +450,9 @@ fk_status fit_impl(fk_ctx *ctxp, const TX *x_in, int64_t n, int64_t d, const fk_
                 set_error("a bounded device wait gave up (code %llu)", h.error_word);
                 fail(FK_ERR_TIMEOUT);
             }
+            calm = (int64_t)(h.flag_count + h.full_count) <= n / 4;
+            if (was_count[r & 1] && ((int64_t)h.full_count > n / 10 || (int64_t)h.ex_count > n / 500))
+                count_from = std::max(count_from, r + 3);
             accumulate_report(rep, h, n);
             inertia = (TC)h.inertia;
             n_iter = r + 1;
@@ -448,9 +468,13 @@ fk_status fit_impl(fk_ctx *ctxp, const TX *x_in, int64_t n, int64_t d, const fk_
             const int mode = !inc_candidate ? UPDATE_FULL
                              : (it < 2 || !incremental) ? UPDATE_FULL_STATE
                                                         : UPDATE_INCREMENTAL;
+            const bool count = count_ok && calm && it >= count_from;
+            was_count[par] = count;
+            if (count && rep) rep->count_iterations++;
+            // iteration it - 1 read cb3[(it + 2) % 3]; it is not overwritten before iteration it + 1
             lloyd_iteration<TX, TC>(ctx, x, n, (int)d, cb3[it % 3], (int)k, p->precision, cb3[(it + 1) % 3],
                                     labels2 + (size_t)par * n, sc, plan, x_changed, rep, timing, mode,
-                                    labels2 + (size_t)(par ^ 1) * n);
+                                    labels2 + (size_t)(par ^ 1) * n, count ? cb3[(it + 2) % 3] : nullptr);
             if (x_changed && inc_candidate) {
                 // once per fit: X finite and the split's grids valid?
                 MixedStats hs;
@@ -1160,6 +1184,7 @@ void drop_call_state(fk_ctx *ctxp) {
     }
     ctx.pending.clear();
     ctx.contract_acc = nullptr;
+    ctx.count_acc = nullptr;
 }
 
 template <typename F>
@@ -1226,6 +1251,7 @@ fk_status fk_ctx_destroy(fk_ctx *ctx) {
     if (c->mixed.ones) cudaFree(c->mixed.ones);
     if (c->mixed2.ones) cudaFree(c->mixed2.ones);
     if (c->mixedm.ones) cudaFree(c->mixedm.ones);
+    if (c->mixedc.ones) cudaFree(c->mixedc.ones);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return FK_OK;

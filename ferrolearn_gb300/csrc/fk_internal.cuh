@@ -92,6 +92,27 @@ struct alignas(16) Top2 {
     int i1, i2, pad1, pad2;
 };
 
+// The same record as the main pass writes it (16 bytes): both centre indices
+// relative to the slice's first centre, 16 bits each (0xFFFF: none).
+struct alignas(16) SliceTop2 {
+    float v1, v2, u3;
+    uint32_t ids;
+};
+__host__ __device__ inline int slice_index(uint32_t local, int base) {
+    return local == 0xFFFFu ? -1 : base + (int)local;
+}
+
+// One row over one slice in the count pass: the largest score, and the
+// centres scoring at least the row's threshold -- their number (low 16 bits
+// of meta, saturating) and the first two nonzero 32-centre mask words w1, w2
+// with their word indices within the slice (meta bits 16-23 and 24-31, 0xFF:
+// none). The words use the mask pass's bit layout.
+struct alignas(16) SliceCount {
+    float vmax;
+    uint32_t meta;
+    uint32_t w1, w2;
+};
+
 // Best eight scores of one row over one slice (second pass), and u9, a bound
 // of the rest.
 struct alignas(16) Top8 {
@@ -112,7 +133,8 @@ struct MixedPlan {
     int64_t tiles = 0;    // ceil(n / 128)
     int ctas_per_part = 0;
     int grid = 0;
-    int topk = 2;         // epilogue records: 2 (Top2, main pass), 8 (Top8, second pass) or 1 (candidate masks)
+    int topk = 2;         // epilogue records: 2 (Top2, main pass), 3 (SliceCount, count pass), 8 (Top8, second
+                          // pass) or 1 (candidate masks)
     int xst = 2;          // depth of the X tile ring (1 when two stages leave no room for 256 centres)
     int ep = 2;           // epilogue parts per TMEM lane quarter (4 x ep epilogue warps)
     int slots = 3;        // rotating tile-merge slots of the top-2 pass
@@ -141,7 +163,7 @@ enum BufSlot {
     BUF_MB_IDX, BUF_MB_XB, BUF_MB_LAB, BUF_MB_OLD, BUF_MB_COUNTS, BUF_MB_PARTV, BUF_MB_PARTI,
     BUF_BK_PERM, BUF_BK_LAB, BUF_BK_CEN, BUF_BK_DIST, BUF_BK_FLAGS, BUF_BK_SCRATCH, BUF_BK_CENTRES, BUF_BK_SEG,
     BUF_BK_FOLD, BUF_BK_LABELS, BUF_BK_XSEG, BUF_BK_CHAINS, BUF_BK_FRES, BUF_BK_FCNT, BUF_FOLD_SUM, BUF_FOLD_CNT,
-    BUF_FOLD_MAP, BUF_MASKS, BUF_THRESH,
+    BUF_FOLD_MAP, BUF_MASKS, BUF_THRESH, BUF_FLOORS, BUF_SHIFT, BUF_THMAIN,
     BUF_BX, BUF_BFITS, BUF_BSTATE, BUF_BITEMS, BUF_BPART, BUF_BORDER, BUF_BCTR, BUF_BLAB, BUF_BMEM, BUF_BCEN, BUF_BND, BUF_BXOFF,
     BUF_COUNT
 };
@@ -165,9 +187,11 @@ struct Ctx {
     MixedPlan mixed;   // main pass
     MixedPlan mixed2;  // second pass (BF16, top-8 records) over the rows an FP8 main pass left open
     MixedPlan mixedm;  // second pass (BF16, candidate masks) over the rows a BF16 main pass left open
+    MixedPlan mixedc;  // BF16 count pass (main pass from the fourth iteration of a fit)
     int batch_variant[20] = {-1, -1, -1, -1, -1, -1, -1, -1, -1, -1,
                              -1, -1, -1, -1, -1, -1, -1, -1, -1, -1};  // autotuned tile shape per (d, k) bucket
     double *contract_acc = nullptr;  // when set: device time of the contraction kernel
+    double *count_acc = nullptr;     // when set: device time of the count passes among those
 
     void *get(BufSlot s, size_t bytes);  // grow-only device buffer
     void bind();                         // make the device current
@@ -356,10 +380,13 @@ void run_kmeanspp(Ctx &ctx, const T *x, int64_t n, int d, int k, const double *d
 // Mixed-precision assignment (BF16 / FP8 tcgen05 approximate pass, FP32 and
 // FP64 exact re-check) of X stored as f32. Results identical to the FP64
 // direct form.
+// With c_prev and labels_prev (BF16 only: the previous iteration's centres
+// and labels, and this context's row floors from that iteration's pass), the
+// main pass is the count pass.
 template <typename TX>
 void run_assign_mixed(Ctx &ctx, const TX *x, int64_t n, int d, const double *c, int k,
                       int precision, int32_t *labels, double *mind, DevScalars *scalars,
-                      bool x_changed);
+                      bool x_changed, const double *c_prev = nullptr, const int32_t *labels_prev = nullptr);
 // Inertia of the mixed precisions: the per-(cluster, feature) partials of
 // the update pass folded in f64 (relative error about 1e-7).
 void launch_mixed_inertia(Ctx &ctx, const double *part, int64_t m, DevScalars *scalars);
@@ -377,10 +404,11 @@ void measure_tc_peaks(Ctx &ctx, double *out);
 // Launch shape only (host arithmetic, no device work); plan_tc adds the
 // device-side constants.
 void plan_shape(MixedPlan &mp, int64_t n, int d, int k, bool fp8, int topk, int sms, int kp_fixed = 0);
-void launch_tc_assign(Ctx &ctx, MixedPlan &mp, const void *xb, const void *cb, const void *caug, Top2 *out,
+void launch_tc_assign(Ctx &ctx, MixedPlan &mp, const void *xb, const void *cb, const void *caug, SliceTop2 *out,
                       Top8 *out8, DevScalars *sc, const MixedStats *stats, float *dump = nullptr,
                       const unsigned long long *n_dev = nullptr, const void *xaug = nullptr,
-                      const float *rowscale = nullptr, uint32_t *masks = nullptr, const float *thresh = nullptr);
+                      const float *rowscale = nullptr, uint32_t *masks = nullptr, const float *thresh = nullptr,
+                      SliceCount *outc = nullptr);
 
 // Batched KMeans<f32> fits (fk_batched.cu).
 fk_status batched_fit_impl(Ctx &ctx, fk_batch_problem *problems, int64_t n_problems, int reduction,

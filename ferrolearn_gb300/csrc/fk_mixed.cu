@@ -146,7 +146,8 @@ __device__ __forceinline__ float sq_partial(const float *__restrict__ x, const f
     float acc = 0.f;
     if ((d & 3) == 0 && (((uintptr_t)x | (uintptr_t)c) & 15u) == 0) {  // 16-byte pieces need 16-byte rows
         const float4 *x4 = reinterpret_cast<const float4 *>(x), *c4 = reinterpret_cast<const float4 *>(c);
-        for (int f = g; f < (d >> 2); f += group) {
+#pragma unroll 4
+        for (int f = g; f < (d >> 2); f += group) {  // unrolled: the loads of four pieces are in flight at once
             const float4 xv = x4[f], cv = c4[f];
             float t = xv.x - cv.x;
             acc = fmaf(t, t, acc);
@@ -552,27 +553,53 @@ __global__ void prep_aug_kernel(const double *__restrict__ half_norm, int k, int
 }
 
 // --------------------------------------------------------------- finalize --
+// E, the row's bound on |T - S| between a tensor-core score T and the exact
+// score S of the same centre (score units; see the file header). Every step
+// rounds upward, so the result bounds the exact expression.
+__device__ __forceinline__ float row_error(const float4 ri, const MixedStats *stats, float acc_rel) {
+    const float xn = ri.x, ex = ri.y;
+    const float cn = stats->cn_max, ec = stats->ec_max, ch = stats->ch_max, big = stats->big;
+    return __fadd_ru(__fadd_ru(__fmul_ru(ex, cn), __fmul_ru(xn, ec)),
+                     __fadd_ru(__fmul_ru(acc_rel, __fadd_ru(__fmul_ru(xn, ch), big)), __fmul_ru(REPR_REL_F, big)));
+}
+
+// Half the FP64 oracle's rounding bound on two direct-form distances: a
+// centre whose exact score is below another's by more than this cannot win
+// in the oracle.
+__device__ __forceinline__ float row_slack64(const float4 ri, const MixedStats *stats, float mu_norm, int d) {
+    const float xn = ri.x, ex = ri.y, xo = ri.z;
+    const float xo_b = fminf(xo, __fadd_ru(__fadd_ru(xn, ex), mu_norm));  // ||x||: both bounds are valid
+    const float sx = __fadd_ru(xo_b, stats->co_max);
+    const float delta = __fmul_ru(__fmul_ru(__fmul_ru((float)(d + 4), 1.1102230246251565e-16f), sx), sx);
+    return __fmul_ru(0.5f, delta);
+}
+
 // Threshold on a score margin above which no other centre can win in the
 // FP64 direct form (see the file header): 2E + key quantum + FP64 rounding.
 __device__ __forceinline__ float row_threshold(const float4 ri, const MixedStats *stats, float acc_rel, float mu_norm,
                                                int d, float v1) {
-    // every step rounds upward, so the result bounds the exact expression
-    const float xn = ri.x, ex = ri.y, xo = ri.z;
-    const float cn = stats->cn_max, ec = stats->ec_max, ch = stats->ch_max, big = stats->big;
-    const float co = stats->co_max;
-    const float e = __fadd_ru(__fadd_ru(__fmul_ru(ex, cn), __fmul_ru(xn, ec)),
-                              __fadd_ru(__fmul_ru(acc_rel, __fadd_ru(__fmul_ru(xn, ch), big)),
-                                        __fmul_ru(REPR_REL_F, big)));
+    const float e = row_error(ri, stats, acc_rel);
     // keys: each score rounded to a multiple of 128 ulp (error <= 64 ulp) plus a
     // column code below 128 ulp, so a key is within 192 ulp of its score
     const float q = 384.f * stats->ulp;
-    const float xo_b = fminf(xo, __fadd_ru(__fadd_ru(xn, ex), mu_norm));  // ||x||: both bounds are valid
-    const float sx = __fadd_ru(xo_b, co);
-    const float delta = __fmul_ru(__fmul_ru(__fmul_ru((float)(d + 4), 1.1102230246251565e-16f), sx), sx);  // FP64 rounding
-    float thr = __fadd_ru(__fmul_ru(__fadd_ru(__fadd_ru(__fmul_ru(2.f, e), q), __fmul_ru(0.5f, delta)), 1.0000012f),
+    float thr = __fadd_ru(__fmul_ru(__fadd_ru(__fadd_ru(__fmul_ru(2.f, e), q), row_slack64(ri, stats, mu_norm, d)),
+                                    1.0000012f),
                           1e-30f);
     if (!(v1 >= stats->big * 0.6f)) thr = INFINITY;  // not a real score (NaN row, all slices padded)
     return thr;
+}
+
+// Lower bound, BIG removed, of the exact score S(c) - BIG of whichever centre
+// c the oracle gives the row, from a pass whose best value is v1 (a key, or
+// a raw score with key_slack 0): the winner's exact score is within the
+// FP64 slack of the best exact score, which is at least v1 - key_slack - E.
+// The next iteration's count pass starts from it.
+__device__ __forceinline__ float row_floor(float v1, float key_slack, const float4 ri, const MixedStats *stats,
+                                           float acc_rel, float mu_norm, int d) {
+    float f = __fsub_rd(v1, key_slack);
+    f = __fsub_rd(f, row_error(ri, stats, acc_rel));
+    f = __fsub_rd(f, row_slack64(ri, stats, mu_norm, d));
+    return __fsub_rd(f, stats->big);
 }
 
 // Merge of two slice records: (v1 >= v2, i1, i2) with u3 bounding the rest,
@@ -615,63 +642,112 @@ __device__ __forceinline__ unsigned long long warp_reserve(unsigned long long *c
     return base + (unsigned long long)__popc(want & ((1u << lane) - 1u));
 }
 
-// Block-aggregated appends to two lists: the block's lanes with pa (pb) set
-// get consecutive slots of list A (B) from one atomic per list per block, so
-// the shared counters see a few thousand atomics per pass instead of one per
-// warp. Every thread of the block must call it.
-template <int NT>
-__device__ __forceinline__ void block_reserve2(unsigned long long *ca, bool pa, unsigned long long *cb, bool pb,
-                                               unsigned long long &sa, unsigned long long &sb) {
-    __shared__ unsigned int wa[NT / 32], wb[NT / 32];
-    __shared__ unsigned long long base_a, base_b;
+constexpr int FINALIZE_THREADS = 512;
+constexpr int FIN_ROUNDS = 3;  // rows per finalize block: FIN_ROUNDS x FINALIZE_THREADS
+
+// A row's class after the main pass: 0 decided (the kernel wrote the label),
+// 1 a pair (a, b) for the exact re-score, 2 the second pass with threshold
+// th; -1 no row.
+struct RowClass {
+    int cls, a, b;
+    float th;
+};
+
+// Staged appends of one finalize block: its rows' pair and full entries are
+// placed in shared memory in row order, round by round, then one atomic per
+// list reserves their global slots -- a few thousand atomics per pass on the
+// two shared counters, instead of one or two per 512 rows, whose serialised
+// round trips in L2 bounded the pass.
+struct FinStage {
+    int4 pairs[FIN_ROUNDS * FINALIZE_THREADS];
+    int32_t rows[FIN_ROUNDS * FINALIZE_THREADS];
+    float ths[FIN_ROUNDS * FINALIZE_THREADS];
+    unsigned wa[FINALIZE_THREADS / 32], wb[FINALIZE_THREADS / 32];
+    unsigned na, nb;
+    unsigned long long base_a, base_b;
+};
+
+template <typename Classify>
+__device__ __forceinline__ void finalize_block(int64_t n, Classify classify, int4 *__restrict__ pair_list,
+                                               int32_t *__restrict__ full_list, float *__restrict__ full_thresh,
+                                               DevScalars *sc) {
+    __shared__ FinStage st;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const unsigned ba = __ballot_sync(0xffffffffu, pa), bb = __ballot_sync(0xffffffffu, pb);
-    if (lane == 0) {
-        wa[w] = (unsigned)__popc(ba);
-        wb[w] = (unsigned)__popc(bb);
-    }
-    __syncthreads();
     if (threadIdx.x == 0) {
-        unsigned ta = 0, tb = 0;
-        for (int i = 0; i < NT / 32; i++) {
-            const unsigned xa = wa[i], xb = wb[i];
-            wa[i] = ta;
-            wb[i] = tb;
-            ta += xa;
-            tb += xb;
+        st.na = 0u;
+        st.nb = 0u;
+    }
+    const int64_t row0 = (int64_t)blockIdx.x * FIN_ROUNDS * FINALIZE_THREADS;
+    for (int r = 0; r < FIN_ROUNDS; r++) {
+        const int64_t i = row0 + (int64_t)r * FINALIZE_THREADS + threadIdx.x;
+        RowClass c{-1, -1, -1, 0.f};
+        if (i < n) c = classify(i);
+        const unsigned ba = __ballot_sync(0xffffffffu, c.cls == 1), bb = __ballot_sync(0xffffffffu, c.cls == 2);
+        if (lane == 0) {
+            st.wa[w] = (unsigned)__popc(ba);
+            st.wb[w] = (unsigned)__popc(bb);
         }
-        base_a = ta ? atomicAdd(ca, (unsigned long long)ta) : 0ull;
-        base_b = tb ? atomicAdd(cb, (unsigned long long)tb) : 0ull;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            unsigned ta = st.na, tb = st.nb;
+            for (int q = 0; q < FINALIZE_THREADS / 32; q++) {
+                const unsigned xa = st.wa[q], xb = st.wb[q];
+                st.wa[q] = ta;
+                st.wb[q] = tb;
+                ta += xa;
+                tb += xb;
+            }
+            st.na = ta;
+            st.nb = tb;
+        }
+        __syncthreads();
+        const unsigned below = (1u << lane) - 1u;
+        if (c.cls == 1) st.pairs[st.wa[w] + (unsigned)__popc(ba & below)] = make_int4((int)i, c.a, c.b, 0);
+        if (c.cls == 2) {
+            const unsigned q = st.wb[w] + (unsigned)__popc(bb & below);
+            st.rows[q] = (int32_t)i;
+            st.ths[q] = c.th;
+        }
+        __syncthreads();  // wa, wb are rewritten in the next round
+    }
+    if (threadIdx.x == 0) {
+        st.base_a = st.na ? atomicAdd(&sc->flag_count, (unsigned long long)st.na) : 0ull;
+        st.base_b = st.nb ? atomicAdd(&sc->full_count, (unsigned long long)st.nb) : 0ull;
     }
     __syncthreads();
-    const unsigned below = (1u << lane) - 1u;
-    sa = base_a + wa[w] + (unsigned)__popc(ba & below);
-    sb = base_b + wb[w] + (unsigned)__popc(bb & below);
+    for (unsigned q = threadIdx.x; q < st.na; q += FINALIZE_THREADS) pair_list[st.base_a + q] = st.pairs[q];
+    for (unsigned q = threadIdx.x; q < st.nb; q += FINALIZE_THREADS) {
+        full_list[st.base_b + q] = st.rows[q];
+        if (full_thresh) full_thresh[st.base_b + q] = st.ths[q];
+    }
 }
 
-constexpr int FINALIZE_THREADS = 512;
+unsigned finalize_blocks(int64_t n) {
+    const int64_t per = (int64_t)FIN_ROUNDS * FINALIZE_THREADS;
+    return (unsigned)((n + per - 1) / per);
+}
 
 __global__ void __launch_bounds__(FINALIZE_THREADS)
-    finalize_kernel(const Top2 *__restrict__ parts, int nparts, int64_t n, int k, int d,
-                                const float4 *__restrict__ rowinfo, const MixedStats *stats, float acc_rel,
-                                float mu_norm, int32_t *__restrict__ labels, int4 *__restrict__ pair_list,
-                                int32_t *__restrict__ full_list, float *__restrict__ full_thresh, DevScalars *sc) {
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    int cls = -1;  // 0 certain, 1 pair, 2 full
-    int i1 = -1, i2 = -1;
-    float th = -INFINITY;
-    if (i < n) {
+    finalize_kernel(const SliceTop2 *__restrict__ parts, int nparts, int kp, int64_t n, int k, int d,
+                    const float4 *__restrict__ rowinfo, const MixedStats *stats, float acc_rel, float mu_norm,
+                    int32_t *__restrict__ labels, int4 *__restrict__ pair_list, int32_t *__restrict__ full_list,
+                    float *__restrict__ full_thresh, float *__restrict__ floor_out, DevScalars *sc) {
+    auto classify = [&](int64_t i) {
+        RowClass c{-1, -1, -1, -INFINITY};
         // all loads first (independent), then the merge
         const float4 ri = rowinfo[i];
-        Top2 t = parts[i];
-        Top2 o1 = nparts > 1 ? parts[(int64_t)n + i] : t;
+        const SliceTop2 t = parts[i];
+        const SliceTop2 o1 = nparts > 1 ? parts[(int64_t)n + i] : t;
         float v1 = t.v1, v2 = t.v2, u3 = t.u3;
-        i1 = t.i1;
-        i2 = t.i2;
-        if (nparts > 1) merge_top2(v1, i1, v2, i2, u3, o1.v1, o1.i1, o1.v2, o1.i2, o1.u3);
+        int i1 = slice_index(t.ids & 0xFFFFu, 0);
+        int i2 = slice_index(t.ids >> 16, 0);
+        if (nparts > 1)
+            merge_top2(v1, i1, v2, i2, u3, o1.v1, slice_index(o1.ids & 0xFFFFu, kp), o1.v2,
+                       slice_index(o1.ids >> 16, kp), o1.u3);
         for (int p = 2; p < nparts; p++) {
-            Top2 o = parts[(int64_t)p * n + i];
-            merge_top2(v1, i1, v2, i2, u3, o.v1, o.i1, o.v2, o.i2, o.u3);
+            const SliceTop2 o = parts[(int64_t)p * n + i];
+            merge_top2(v1, i1, v2, i2, u3, o.v1, slice_index(o.ids & 0xFFFFu, p * kp), o.v2,
+                       slice_index(o.ids >> 16, p * kp), o.u3);
         }
         {  // FP8 rows are scored in units of 1/(s_i t): back to score units (exact powers of two)
             const float unit = stats->tscale / ri.w;
@@ -680,15 +756,18 @@ __global__ void __launch_bounds__(FINALIZE_THREADS)
             u3 *= unit;
         }
         const float thr = row_threshold(ri, stats, acc_rel, mu_norm, d, v1);
+        if (floor_out) floor_out[i] = row_floor(v1, 192.f * stats->ulp, ri, stats, acc_rel, mu_norm, d);
         const float m12 = __fsub_rd(v1, v2);  // lower bounds of the margins
         const float m13 = __fsub_rd(v1, u3);
+        c.a = i1;
+        c.b = i2;
         if (i1 >= 0 && i1 < k && m12 > thr) {
-            cls = 0;
+            c.cls = 0;
             labels[i] = i1;
         } else if (i1 >= 0 && i1 < k && i2 >= 0 && i2 < k && i1 != i2 && m13 > thr) {
-            cls = 1;
+            c.cls = 1;
         } else {
-            cls = 2;
+            c.cls = 2;
             // Mask pass threshold (BF16 main pass, whose scores the mask pass
             // recomputes from the same operands): any centre that can still
             // win scores at least v1 - 2 thr there. The best centre c* has
@@ -696,17 +775,155 @@ __global__ void __launch_bounds__(FINALIZE_THREADS)
             // centre is needed only within thr of T'(c*); thr >= 2E + 384
             // ulp covers both. Thresholds below 2^(E-2) (or NaN) become
             // -inf: every centre is then a candidate.
-            const float t = __fsub_rd(v1, __fmul_ru(2.f, thr));
-            th = t >= stats->ulp * 2097152.f ? t : -INFINITY;
+            const float t2 = __fsub_rd(v1, __fmul_ru(2.f, thr));
+            c.th = t2 >= stats->ulp * 2097152.f ? t2 : -INFINITY;
         }
+        return c;
+    };
+    finalize_block(n, classify, pair_list, full_list, full_thresh, sc);
+}
+
+// ------------------------------------------------------------ count pass --
+// From the fourth iteration of a fit on, the main pass can skip the top-2
+// ranking: a row's best score this iteration is bounded below from the
+// previous one, so a threshold th below which no centre can win is known
+// before the pass, which then only counts the centres at or above it (the
+// mask pass's exact marks) and keeps the row's largest score. One marked
+// centre is the label; two are a pair for the exact re-score; more (or
+// none) go to the second pass with the same threshold.
+//
+// The bound: with c the centre the oracle gave the row in the previous
+// iteration and F the row floor of that iteration (S_prev(c) - BIG_prev >=
+// F), the exact scores move by S(c) - S_prev(c) = x'.(c - c_prev) - (h(c) -
+// h_prev(c)) + (BIG - BIG_prev), h = ||c'||^2 / 2, so the best score T_max
+// of this pass satisfies T_max >= T(c) >= S(c) - E >= F + BIG - ||x'|| D_c -
+// |dh_c| - E =: L, with D_c = ||c - c_prev|| and ||x'|| <= ||xh|| + ||x' -
+// xh||. A centre that can win in the oracle has S >= S(winner) - slack >=
+// S(c) - slack >= L + E - slack, so its score here is at least L - slack >=
+// L - thr =: th.
+
+// Per centre, upper bounds of ||c - c_prev|| and of |h(c) - h_prev(c)|: one
+// warp per centre, FP64 sums of squares inflated by (d + 8) 2^-52 for their
+// roundings, then rounded up to f32.
+__global__ void centre_shift_kernel(const double *__restrict__ c, const double *__restrict__ cprev,
+                                    const double *__restrict__ mu, int k, int d, float2 *__restrict__ shift) {
+    const int lane = threadIdx.x & 31;
+    const int q = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    if (q >= k) return;  // warp-uniform
+    double dd = 0.0, hn = 0.0, ho = 0.0;
+    for (int j = lane; j < d; j += 32) {
+        const double a = c[(int64_t)q * d + j], b = cprev[(int64_t)q * d + j], m = mu[j];
+        const double t = a - b, u = a - m, v = b - m;
+        dd += t * t;
+        hn += u * u;
+        ho += v * v;
     }
-    unsigned long long ps, fs;
-    block_reserve2<FINALIZE_THREADS>(&sc->flag_count, cls == 1, &sc->full_count, cls == 2, ps, fs);
-    if (cls == 1) pair_list[ps] = make_int4((int)i, i1, i2, 0);
-    if (cls == 2) {
-        full_list[fs] = (int32_t)i;
-        if (full_thresh) full_thresh[fs] = th;
+    dd = warp_sum_d(dd);
+    hn = warp_sum_d(hn);
+    ho = warp_sum_d(ho);
+    if (lane == 0) {
+        const double rel = (double)(d + 8) * 2.220446049250313e-16;
+        const double dist = __dsqrt_ru(__dmul_ru(dd, 1.0 + rel));
+        const double dh = __dadd_ru(__dmul_ru(0.5, fabs(hn - ho)), __dmul_ru(0.5 * rel, __dadd_ru(hn, ho)));
+        const bool ok = dist < 1e30 && dh < 1e30;  // NaN or huge: no usable bound
+        shift[q] = make_float2(ok ? __double2float_ru(dist) : INFINITY, ok ? __double2float_ru(dh) : INFINITY);
     }
+}
+
+// th for every row (score units, directed rounding), or -inf where no usable
+// bound exists (then every centre is marked and the row is re-scored in full).
+__global__ void count_thresh_kernel(int64_t n, int k, int d, const float *__restrict__ floor_prev,
+                                    const int32_t *__restrict__ labels_prev, const float4 *__restrict__ rowinfo,
+                                    const float2 *__restrict__ shift, const MixedStats *stats, float acc_rel,
+                                    float mu_norm, float *__restrict__ th_out) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int l = labels_prev[i];
+    const float4 ri = rowinfo[i];
+    float th = -INFINITY;
+    if (l >= 0 && l < k) {
+        const float2 sh = shift[l];
+        const float xnorm = __fadd_ru(ri.x, ri.y);
+        float lb = __fadd_rd(floor_prev[i], stats->big);
+        lb = __fsub_rd(lb, __fmul_ru(xnorm, sh.x));
+        lb = __fsub_rd(lb, sh.y);
+        lb = __fsub_rd(lb, row_error(ri, stats, acc_rel));
+        const float t = __fsub_rd(lb, row_threshold(ri, stats, acc_rel, mu_norm, d, stats->big));
+        // the marks are exact 0 / 1 only for thresholds of at least 2^(E-2)
+        th = t >= stats->ulp * 2097152.f ? t : -INFINITY;
+    }
+    th_out[i] = th;
+}
+
+// Centre of bit b of mask word w of slice base `base` (the mask pass's layout).
+__device__ __forceinline__ int count_column(int base, int w, int b) {
+    return base + 32 * w + (b < 16 ? 2 * (15 - b) : 2 * (31 - b) + 1);
+}
+
+// Merges the slices' count records of each row and classifies it: one marked
+// centre is the label, two go to the pair re-score, more or none to the
+// second pass with the row's threshold. Also the row floor for the next
+// iteration (the largest score is a raw accumulator: no key slack).
+__global__ void __launch_bounds__(FINALIZE_THREADS)
+    finalize_count_kernel(const SliceCount *__restrict__ parts, int nparts, int kp, int64_t n, int k, int d,
+                          const float4 *__restrict__ rowinfo, const MixedStats *stats, float acc_rel, float mu_norm,
+                          const float *__restrict__ thresh, int32_t *__restrict__ labels,
+                          int4 *__restrict__ pair_list, int32_t *__restrict__ full_list,
+                          float *__restrict__ full_thresh, float *__restrict__ floor_out, DevScalars *sc) {
+    auto classify = [&](int64_t i) {
+        RowClass c{-1, -1, -1, 0.f};
+        float vmax = 0.f;
+        uint32_t cnt = 0, w1 = 0, w2 = 0;
+        int b1 = 0, b2 = 0;  // the words' first centre
+        for (int p = 0; p < nparts; p++) {
+            const SliceCount o = parts[(int64_t)p * n + i];
+            vmax = fmaxf(vmax, o.vmax);
+            cnt += o.meta & 0xFFFFu;
+            const int wi[2] = {(int)((o.meta >> 16) & 0xFFu), (int)(o.meta >> 24)};
+            const uint32_t ow[2] = {o.w1, o.w2};
+#pragma unroll
+            for (int u = 0; u < 2; u++) {
+                if (!ow[u]) continue;
+                if (!w1) {
+                    w1 = ow[u];
+                    b1 = p * kp + 32 * wi[u];
+                } else if (!w2) {
+                    w2 = ow[u];
+                    b2 = p * kp + 32 * wi[u];
+                }
+            }
+        }
+        const float4 ri = rowinfo[i];
+        floor_out[i] = row_floor(vmax, 0.f, ri, stats, acc_rel, mu_norm, d);
+        int a = -1, b = -1;
+        if (cnt == 1 && w1) {
+            a = count_column(b1, 0, __ffs(w1) - 1);
+        } else if (cnt == 2 && w1) {
+            a = count_column(b1, 0, __ffs(w1) - 1);
+            const uint32_t rest = w1 & (w1 - 1u);
+            b = rest ? count_column(b1, 0, __ffs(rest) - 1) : (w2 ? count_column(b2, 0, __ffs(w2) - 1) : -1);
+        }
+        c.a = a;
+        c.b = b;
+        if (cnt == 1 && a >= 0 && a < k) {
+            c.cls = 0;
+            labels[i] = a;
+        } else if (cnt == 2 && a >= 0 && a < k && b >= 0 && b < k && a != b) {
+            c.cls = 1;
+        } else {
+            c.cls = 2;
+            // the second pass's threshold: the carried one, or tighter, from
+            // this pass's exact best score -- a centre that can win scores at
+            // least vmax - 2E - FP64 slack >= vmax - thr in any pass with
+            // error bound E (a wide carried window would send the row to the
+            // exhaustive re-score)
+            const float t2 = __fsub_rd(vmax, row_threshold(ri, stats, acc_rel, mu_norm, d, stats->big));
+            const float t = fmaxf(thresh[i], t2 >= stats->ulp * 2097152.f ? t2 : -INFINITY);
+            c.th = t;
+        }
+        return c;
+    };
+    finalize_block(n, classify, pair_list, full_list, full_thresh, sc);
 }
 
 // ------------------------------------------------------------ re-checks --
@@ -1191,6 +1408,68 @@ __device__ __forceinline__ int mask_column(int w, int b) {
     return 32 * w + (b < 16 ? 2 * (15 - b) : 2 * (31 - b) + 1);
 }
 
+// FP32 distances from one row to candidates cand[0..m) (m <= 32): candidate j's
+// distance ends in lane j. FAST (16-byte rows, d <= 256): the row's 16-byte
+// pieces are in registers (lane l: pieces l and l + 32), and four candidates
+// are scored at a time, each a warp sum, so their loads are in flight
+// together. Otherwise four lanes per candidate, eight candidates at a time.
+template <bool FAST>
+__device__ __forceinline__ float cand_dists(const float *__restrict__ xrow, const float4 (&xv)[2],
+                                            const float *__restrict__ c32, const int *cand, int m, int d) {
+    const int lane = threadIdx.x & 31;
+    float my = 0.f;
+    if constexpr (FAST) {
+        const int d4 = d >> 2;
+        for (int j0 = 0; j0 < m; j0 += 4) {  // m is warp-uniform
+            float acc[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                acc[u] = 0.f;
+                if (j0 + u < m) {
+                    const float4 *cr = reinterpret_cast<const float4 *>(c32 + (int64_t)cand[j0 + u] * d);
+#pragma unroll
+                    for (int h = 0; h < 2; h++) {
+                        const int q = lane + 32 * h;
+                        if (q < d4) {
+                            const float4 cv = cr[q];
+                            float t = xv[h].x - cv.x;
+                            acc[u] = fmaf(t, t, acc[u]);
+                            t = xv[h].y - cv.y;
+                            acc[u] = fmaf(t, t, acc[u]);
+                            t = xv[h].z - cv.z;
+                            acc[u] = fmaf(t, t, acc[u]);
+                            t = xv[h].w - cv.w;
+                            acc[u] = fmaf(t, t, acc[u]);
+                        }
+                    }
+                }
+            }
+#pragma unroll
+            for (int off = 16; off >= 1; off >>= 1)
+#pragma unroll
+                for (int u = 0; u < 4; u++) acc[u] += __shfl_xor_sync(0xffffffffu, acc[u], off);
+#pragma unroll
+            for (int u = 0; u < 4; u++)
+                if (lane == j0 + u) my = acc[u];
+        }
+    } else {
+        for (int r0 = 0; r0 < m; r0 += 8) {
+            const int cj = r0 + (lane >> 2);
+            float acc = 0.f;
+            if (cj < m) acc = sq_partial(xrow, c32 + (int64_t)cand[cj] * d, d, lane & 3, 4);
+            acc += __shfl_xor_sync(0xffffffffu, acc, 2);
+            acc += __shfl_xor_sync(0xffffffffu, acc, 1);
+#pragma unroll
+            for (int j = 0; j < 8; j++) {
+                const float v = __shfl_sync(0xffffffffu, acc, 4 * j);
+                if (lane == r0 + j) my = v;
+            }
+        }
+    }
+    return my;
+}
+
+template <bool FAST>
 __global__ void __launch_bounds__(MASK_WARPS * 32)
     mask_rescore_kernel(const float *__restrict__ x, int d, const float *__restrict__ c32,
                         const float *__restrict__ ec32, int k, const uint32_t *__restrict__ masks, int wpr,
@@ -1201,13 +1480,35 @@ __global__ void __launch_bounds__(MASK_WARPS * 32)
     int *cand = cand_sm[wid];
     const unsigned long long cnt = sc->full_count;
     const unsigned long long nw = (unsigned long long)gridDim.x * MASK_WARPS;
-    for (unsigned long long s = (unsigned long long)blockIdx.x * MASK_WARPS + wid; s < cnt; s += nw) {
-        const int row = list[s];
+    unsigned long long s = (unsigned long long)blockIdx.x * MASK_WARPS + wid;
+    unsigned long long decided = 0;  // rows this warp decided among its candidates (lane 0)
+    // the next row's list entry and first 32 mask words load while this row
+    // is decided
+    int row_next = 0;
+    uint32_t word_next = 0u;
+    if (s < cnt) {
+        row_next = list[s];
+        word_next = lane < wpr ? masks[(int64_t)s * wpr + lane] : 0u;
+    }
+    for (; s < cnt; s += nw) {
+        const int row = row_next;
+        const uint32_t first = word_next;
+        if (s + nw < cnt) {
+            row_next = list[s + nw];
+            word_next = lane < wpr ? masks[(int64_t)(s + nw) * wpr + lane] : 0u;
+        }
+        const float *xrow = x + (int64_t)row * d;
+        float4 xv[2] = {make_float4(0.f, 0.f, 0.f, 0.f), make_float4(0.f, 0.f, 0.f, 0.f)};
+        if constexpr (FAST) {  // the row's pieces load while the mask is decoded
+#pragma unroll
+            for (int h = 0; h < 2; h++)
+                if (lane + 32 * h < (d >> 2)) xv[h] = reinterpret_cast<const float4 *>(xrow)[lane + 32 * h];
+        }
         const uint32_t *mw = masks + (int64_t)s * wpr;
         int m = 0;  // candidates so far (warp-uniform)
         for (int w0 = 0; w0 < wpr; w0 += 32) {
             const int w = w0 + lane;
-            uint32_t word = w < wpr ? mw[w] : 0u;
+            uint32_t word = w0 == 0 ? first : (w < wpr ? mw[w] : 0u);
             if (32 * w + 32 > k) {  // centres at or above k are padding
                 uint32_t keep = 0u;
                 for (int b = 0; b < 32; b++)
@@ -1225,7 +1526,7 @@ __global__ void __launch_bounds__(MASK_WARPS * 32)
             if (m + total <= MASK_CANDS) {
                 // this lane's candidates in increasing centre order
                 int pos = m + incl - c;
-                uint32_t lo = word & 0xFFFFu, hi = word >> 16;
+                const uint32_t lo = word & 0xFFFFu, hi = word >> 16;
                 for (int j = 0; j < 16; j++) {  // centre 32 w + 2 j + parity: bit 15 - j (even), 31 - j (odd)
                     if ((lo >> (15 - j)) & 1u) cand[pos++] = 32 * w + 2 * j;
                     if ((hi >> (15 - j)) & 1u) cand[pos++] = 32 * w + 2 * j + 1;
@@ -1236,22 +1537,11 @@ __global__ void __launch_bounds__(MASK_WARPS * 32)
         __syncwarp();
         bool to_ex = m == 0 || m > MASK_CANDS;
         if (!to_ex) {
-            float my_dist = 0.f;
-            for (int r0 = 0; r0 < m; r0 += 8) {
-                const int cj = r0 + (lane >> 2);
-                float acc = 0.f;
-                if (cj < m) acc = sq_partial(x + (int64_t)row * d, c32 + (int64_t)cand[cj] * d, d, lane & 3, 4);
-                acc += __shfl_xor_sync(0xffffffffu, acc, 2);
-                acc += __shfl_xor_sync(0xffffffffu, acc, 1);
-#pragma unroll
-                for (int j = 0; j < 8; j++) {
-                    const float v = __shfl_sync(0xffffffffu, acc, 4 * j);
-                    if (lane == r0 + j) my_dist = v;
-                }
-            }
             const bool is_cand = lane < m;
             const int my_id = is_cand ? cand[lane] : INT32_MAX;
-            const float my_err = is_cand ? bound32(my_dist, ec32[my_id], d) : 0.f;
+            const float my_ec = is_cand ? ec32[my_id] : 0.f;  // in flight during the distances
+            const float my_dist = cand_dists<FAST>(xrow, xv, c32, cand, m, d);
+            const float my_err = is_cand ? bound32(my_dist, my_ec, d) : 0.f;
             float ub = is_cand ? __fadd_ru(my_dist, my_err) : INFINITY;
 #pragma unroll
             for (int off = 16; off >= 1; off >>= 1) ub = fminf(ub, __shfl_xor_sync(0xffffffffu, ub, off));
@@ -1259,8 +1549,10 @@ __global__ void __launch_bounds__(MASK_WARPS * 32)
             const int nsurv = __popc(surv);
             if (nsurv == 1) {
                 const int only = __shfl_sync(0xffffffffu, my_id, __ffs(surv) - 1);
-                if (lane == 0) labels[row] = only;
-                if (lane == 0) atomicAdd(&sc->quad_count, 1ULL);
+                if (lane == 0) {
+                    labels[row] = only;
+                    decided++;
+                }
             } else {
                 // the survivors (all candidates if no FP32 value was finite)
                 const unsigned take = nsurv == 0 ? __ballot_sync(0xffffffffu, is_cand) : surv;
@@ -1278,7 +1570,7 @@ __global__ void __launch_bounds__(MASK_WARPS * 32)
                         }
                     }
                     queue_f64(f64_items, sc, row, mm, ids);
-                    if (lane == 0) atomicAdd(&sc->quad_count, 1ULL);
+                    if (lane == 0) decided++;
                 } else {
                     to_ex = true;
                 }
@@ -1287,6 +1579,8 @@ __global__ void __launch_bounds__(MASK_WARPS * 32)
         if (to_ex && lane == 0) ex_list[atomicAdd(&sc->ex_count, 1ULL)] = row;
         __syncwarp();  // cand is reused by the next row
     }
+    // one add per warp: a per-row atomic on the shared counter serialises in L2
+    if (lane == 0 && decided) atomicAdd(&sc->quad_count, decided);
 }
 
 // BF16 rows of the main pass's operand copied for the listed rows (slot s =
@@ -1325,11 +1619,18 @@ __global__ void __launch_bounds__(F64_WARPS * 32)
         for (int j = lane; j < d; j += 32) xs[j] = (double)x[(int64_t)it.row * d + j];
         int my_id = INT32_MAX;
 #pragma unroll
-        for (int t = 0; t < 8; t++) {
-            if (t < it.m) {
-                for (int j = lane; j < d; j += 32) cs[(size_t)t * (d + 1) + j] = c[(int64_t)it.ids[t] * d + j];
-                if (t == lane) my_id = it.ids[t];
-            }
+        for (int t = 0; t < 8; t++)
+            if (t < it.m && t == lane) my_id = it.ids[t];
+        // the candidates' rows as one flat index space, so every load of the
+        // staging is independent of the others
+        const int md = it.m * d;
+        for (int e = lane; e < md; e += 32) {
+            const int t = e / d, j = e - t * d;
+            int id = it.ids[0];
+#pragma unroll
+            for (int u = 1; u < 8; u++)
+                if (u == t) id = it.ids[u];
+            cs[(size_t)t * (d + 1) + j] = c[(int64_t)id * d + j];
         }
         __syncwarp();
         double v = DBL_MAX;
@@ -1337,7 +1638,8 @@ __global__ void __launch_bounds__(F64_WARPS * 32)
         if (lane < it.m) {
             const double *cr = cs + (size_t)lane * (d + 1);
             double acc = 0.0;
-            for (int j = 0; j < d; j++) {
+#pragma unroll 8
+            for (int j = 0; j < d; j++) {  // unrolled: the loads and squares run ahead of the add chain
                 const double t = __dsub_rn(xs[j], cr[j]);
                 acc = __dadd_rn(acc, __dmul_rn(t, t));
             }
@@ -1511,6 +1813,14 @@ MixedBufs prepare_mixed(Ctx &ctx, const TX *x, int64_t n, int d, const double *c
     return B;
 }
 
+// Blocks of `threads` threads that fit on one SM at once (the grid of a
+// latency-bound grid-stride kernel: every warp resident, no second wave).
+int resident_blocks(const void *fn, int threads) {
+    int b = 0;
+    FK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, fn, threads, 0));
+    return b > 0 ? b : 1;
+}
+
 // FP8: r = 2^-sh_row * 2^-sh_t, the factor between a row's scores and its
 // accumulators (exact: a product of powers of two in range).
 __global__ void rowscale_kernel(const float4 *__restrict__ rowinfo, int64_t n, const MixedStats *stats,
@@ -1558,8 +1868,16 @@ void second_pass(Ctx &ctx, const float *x, int64_t n, int d, const double *c, in
         FK_LAUNCH_CHECK();
         launch_tc_assign(ctx, mm, xb2, B.cq, B.caug, nullptr, nullptr, sc, B.stats, nullptr, &sc->full_count,
                          nullptr, nullptr, masks, full_thresh);
-        mask_rescore_kernel<<<grid / 2, MASK_WARPS * 32, 0, s>>>(x, d, B.c32, B.ec32, k, masks, wpr, full, sc,
-                                                                  labels, f64_items, ex);
+        // latency-bound (a few dependent loads per row): as many warps as the SMs hold
+        if (d % 4 == 0 && d <= 256 && (((uintptr_t)x | (uintptr_t)B.c32) & 15u) == 0) {
+            static const int mask_blocks = resident_blocks((const void *)mask_rescore_kernel<true>, MASK_WARPS * 32);
+            mask_rescore_kernel<true><<<ctx.num_sms * mask_blocks, MASK_WARPS * 32, 0, s>>>(
+                x, d, B.c32, B.ec32, k, masks, wpr, full, sc, labels, f64_items, ex);
+        } else {
+            static const int mask_blocks = resident_blocks((const void *)mask_rescore_kernel<false>, MASK_WARPS * 32);
+            mask_rescore_kernel<false><<<ctx.num_sms * mask_blocks, MASK_WARPS * 32, 0, s>>>(
+                x, d, B.c32, B.ec32, k, masks, wpr, full, sc, labels, f64_items, ex);
+        }
         FK_LAUNCH_CHECK();
         exhaustive_rescore_kernel<<<ctx.num_sms * 2, EX_THREADS, exhaustive_smem_bytes(d, k), s>>>(
             x, d, c, B.c32t, B.ec32, k, ex, &sc->ex_count, sc, labels);
@@ -1599,7 +1917,8 @@ void second_pass(Ctx &ctx, const float *x, int64_t n, int d, const double *c, in
 
 template <typename TX>
 void run_assign_mixed(Ctx &ctx, const TX *x, int64_t n, int d, const double *c, int k, int precision,
-                      int32_t *labels, double *, DevScalars *sc, bool x_changed) {
+                      int32_t *labels, double *, DevScalars *sc, bool x_changed, const double *c_prev,
+                      const int32_t *labels_prev) {
     cudaStream_t s = ctx.stream;
     MixedPlan &mp = ctx.mixed;
     if (precision != FK_PRECISION_MIXED_BF16 && precision != FK_PRECISION_MIXED_FP8) {
@@ -1620,26 +1939,60 @@ void run_assign_mixed(Ctx &ctx, const TX *x, int64_t n, int d, const double *c, 
         FK_LAUNCH_CHECK();
     }
 
-    Top2 *top = (Top2 *)ctx.get(BUF_TOP2, sizeof(Top2) * (size_t)n * mp.parts);
-    {
-        Timer t(ctx.contract_acc != nullptr, ctx, ctx.contract_acc);
-        launch_tc_assign(ctx, mp, B.xq, B.cq, B.caug, top, nullptr, sc, B.stats, nullptr, nullptr, B.xaug, rowscale);
-    }
-
     int4 *pairs = (int4 *)ctx.get(BUF_FLAGS, sizeof(int4) * (size_t)n);
     int32_t *full = (int32_t *)ctx.get(BUF_FULL, sizeof(int32_t) * (size_t)n);
     float *full_thresh = fp8 ? nullptr : (float *)ctx.get(BUF_THRESH, sizeof(float) * (size_t)n);
+    // BF16: every pass leaves each row's floor for a count pass in the next iteration
+    float *floors = fp8 ? nullptr : (float *)ctx.get(BUF_FLOORS, sizeof(float) * (size_t)n);
     const float acc_rel = (float)((double)((size_t)mp.d_pad + 32) * ACC_REL_PER_K);  // exact: integer * 2^-22
-    finalize_kernel<<<(unsigned)((n + FINALIZE_THREADS - 1) / FINALIZE_THREADS), FINALIZE_THREADS, 0, s>>>(
-        top, mp.parts, n, k, d, B.rowinfo, B.stats, acc_rel, mu_norm_up(mp.mu_norm), labels, pairs, full,
-        full_thresh, sc);
-    FK_LAUNCH_CHECK();
+    const float mun = mu_norm_up(mp.mu_norm);
+    const unsigned fin_blocks = finalize_blocks(n);
+    if (!fp8 && c_prev && labels_prev) {
+        // count pass, against thresholds carried from the previous iteration
+        MixedPlan &mc = ctx.mixedc;
+        if (mc.n != n || mc.d != d || mc.k != k || mc.kp != mp.kp) plan_tc(ctx, mc, n, d, k, false, 3, mp.kp);
+        if (mc.k_pad != mp.k_pad || mc.d_pad != mp.d_pad) {
+            set_error("count pass plan (k_pad %d, d_pad %d) differs from the main pass (%d, %d)", mc.k_pad, mc.d_pad,
+                      mp.k_pad, mp.d_pad);
+            fail(FK_ERR_CUDA);
+        }
+        float2 *shift = (float2 *)ctx.get(BUF_SHIFT, sizeof(float2) * (size_t)k);
+        centre_shift_kernel<<<(unsigned)(((int64_t)k * 32 + 255) / 256), 256, 0, s>>>(c, c_prev, B.mu, k, d, shift);
+        FK_LAUNCH_CHECK();
+        float *th = (float *)ctx.get(BUF_THMAIN, sizeof(float) * (size_t)n);
+        count_thresh_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, k, d, floors, labels_prev, B.rowinfo,
+                                                                      shift, B.stats, acc_rel, mun, th);
+        FK_LAUNCH_CHECK();
+        SliceCount *cnt = (SliceCount *)ctx.get(BUF_TOP2, sizeof(SliceCount) * (size_t)n * mc.parts);
+        {
+            Timer t(ctx.contract_acc != nullptr, ctx, ctx.contract_acc);
+            Timer tc(ctx.count_acc != nullptr, ctx, ctx.count_acc);
+            launch_tc_assign(ctx, mc, B.xq, B.cq, B.caug, nullptr, nullptr, sc, B.stats, nullptr, nullptr, nullptr,
+                             nullptr, nullptr, th, cnt);
+        }
+        finalize_count_kernel<<<fin_blocks, FINALIZE_THREADS, 0, s>>>(cnt, mc.parts, mc.kp, n, k, d, B.rowinfo,
+                                                                      B.stats, acc_rel, mun, th, labels, pairs, full,
+                                                                      full_thresh, floors, sc);
+        FK_LAUNCH_CHECK();
+    } else {
+        SliceTop2 *top = (SliceTop2 *)ctx.get(BUF_TOP2, sizeof(SliceTop2) * (size_t)n * mp.parts);
+        {
+            Timer t(ctx.contract_acc != nullptr, ctx, ctx.contract_acc);
+            launch_tc_assign(ctx, mp, B.xq, B.cq, B.caug, top, nullptr, sc, B.stats, nullptr, nullptr, B.xaug,
+                             rowscale);
+        }
+        finalize_kernel<<<fin_blocks, FINALIZE_THREADS, 0, s>>>(top, mp.parts, mp.kp, n, k, d, B.rowinfo, B.stats,
+                                                                acc_rel, mun, labels, pairs, full, full_thresh,
+                                                                floors, sc);
+        FK_LAUNCH_CHECK();
+    }
     const int grid = ctx.num_sms * 4;
     Oct *f64_items = (Oct *)ctx.get(BUF_F64ITEMS, sizeof(Oct) * (size_t)n);
-    if (std::is_same<TX, float>::value && d % 4 == 0 && d <= 128 && ((uintptr_t)x & 15u) == 0)
-        pair_rescore4_kernel<<<grid, 256, 0, s>>>((const float *)x, d, c, B.c32, B.ec32, pairs, sc, labels,
-                                                  f64_items);
-    else
+    if (std::is_same<TX, float>::value && d % 4 == 0 && d <= 128 && ((uintptr_t)x & 15u) == 0) {
+        static const int pair_blocks = resident_blocks((const void *)pair_rescore4_kernel, 256);
+        pair_rescore4_kernel<<<ctx.num_sms * pair_blocks, 256, 0, s>>>((const float *)x, d, c, B.c32, B.ec32, pairs,
+                                                                       sc, labels, f64_items);
+    } else
         pair_rescore_kernel<TX><<<grid, 256, 0, s>>>(x, d, c, B.c32, B.ec32, pairs, sc, labels, f64_items);
     FK_LAUNCH_CHECK();
     second_pass(ctx, x, n, d, c, k, B, mp.mu_norm, full, full_thresh, labels, sc, f64_items);
@@ -1655,7 +2008,7 @@ void launch_mixed_inertia(Ctx &ctx, const double *part, int64_t m, DevScalars *s
 }
 
 template void run_assign_mixed<float>(Ctx &, const float *, int64_t, int, const double *, int, int, int32_t *,
-                                      double *, DevScalars *, bool);
+                                      double *, DevScalars *, bool, const double *, const int32_t *);
 
 // Diagnostics for the tests: one tensor-core pass over x (f32, on the device)
 // against c (f64), returning the raw accumulators of CTA 0's first tile and
@@ -1676,7 +2029,7 @@ void debug_tc_probe(Ctx &ctx, const float *x, int64_t n, int d, const double *c,
         rowscale_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(B.rowinfo, n, B.stats, rowscale);
         FK_LAUNCH_CHECK();
     }
-    Top2 *top = (Top2 *)ctx.get(BUF_TOP2, sizeof(Top2) * (size_t)n * mp.parts);
+    SliceTop2 *top = (SliceTop2 *)ctx.get(BUF_TOP2, sizeof(SliceTop2) * (size_t)n * mp.parts);
     float *dump = (float *)ctx.get(BUF_OUT, sizeof(float) * 128 * (size_t)mp.kp);
     FK_CUDA(cudaMemsetAsync(dump, 0, sizeof(float) * 128 * (size_t)mp.kp, s));
     launch_tc_assign(ctx, mp, B.xq, B.cq, B.caug, top, nullptr, sc, B.stats, dump, nullptr, B.xaug, rowscale);
@@ -1688,9 +2041,16 @@ void debug_tc_probe(Ctx &ctx, const float *x, int64_t n, int d, const double *c,
     FK_CUDA(cudaMemcpyAsync(aug_out, B.caug, sizeof(uint16_t) * (size_t)mp.k_pad * 16, cudaMemcpyDeviceToHost, s));
     if (fp8)
         FK_CUDA(cudaMemcpyAsync(xaug_out, B.xaug, sizeof(uint16_t) * 16 * (size_t)rows, cudaMemcpyDeviceToHost, s));
-    FK_CUDA(cudaMemcpyAsync(top_out, top, sizeof(Top2) * (size_t)n * mp.parts, cudaMemcpyDeviceToHost, s));
+    std::vector<SliceTop2> recs((size_t)n * mp.parts);
+    FK_CUDA(cudaMemcpyAsync(recs.data(), top, sizeof(SliceTop2) * recs.size(), cudaMemcpyDeviceToHost, s));
     FK_CUDA(cudaMemcpyAsync(ctx.host_scalars, sc, sizeof(DevScalars), cudaMemcpyDeviceToHost, s));
     FK_CUDA(cudaStreamSynchronize(s));
+    for (size_t e = 0; e < recs.size(); e++) {  // the records with absolute centre indices
+        const int base = (int)(e / (size_t)n) * mp.kp;
+        const SliceTop2 &r = recs[e];
+        top_out[e] = Top2{r.v1, r.v2, r.u3, 0.f, slice_index(r.ids & 0xFFFFu, base), slice_index(r.ids >> 16, base),
+                          0, 0};
+    }
     plan_out[0] = mp.d_pad;
     plan_out[1] = mp.kp;
     plan_out[2] = mp.parts;

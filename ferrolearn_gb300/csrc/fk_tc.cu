@@ -64,11 +64,13 @@ __device__ __forceinline__ int unpack_local(uint32_t l, int base) { return l == 
 // records per row -- whole records for BF16 with two parts, 16-byte ones
 // otherwise (FP8, whose larger X stages leave less room, and four parts) --
 // and one slot of top-8 records for the second pass; none for the mask pass,
-// whose parts write their own words of the row's candidate mask.
+// whose parts write their own words of the row's candidate mask; the count
+// pass rotates its slots like the top-2 pass, with SliceCount records.
 __host__ __device__ constexpr uint32_t merge_bytes(int topk, bool fp8, int ep, int slots) {
     return topk == 1   ? 0u
            : topk == 2 ? BM * (uint32_t)slots * (uint32_t)(ep - 1) *
                              (uint32_t)((fp8 || ep > 2) ? sizeof(HalfRec) : sizeof(Top2))
+           : topk == 3 ? BM * (uint32_t)slots * (uint32_t)(ep - 1) * (uint32_t)sizeof(SliceCount)
                        : BM * (uint32_t)sizeof(Top8);
 }
 
@@ -129,7 +131,7 @@ struct TcParams {
     uint32_t c_atom_bytes;  // kp * 128
     uint32_t x_stage_bytes;
     uint32_t c_tx_bytes;
-    Top2 *out;                // top-2 records (main pass)
+    SliceTop2 *out;           // top-2 records (main pass)
     Top8 *out8;               // top-8 records (second pass)
     unsigned long long *err;
     const MixedStats *stats;  // cgrid, ulp of this launch
@@ -137,7 +139,8 @@ struct TcParams {
     uint32_t off_xaug;        // FP8: per-stage augmentation tiles
     float *dump;  // optional: raw accumulators of the first tile of CTA 0 (tests only)
     uint32_t *masks;       // mask pass: wpr words per row, bit per centre (layout at mask_chunk)
-    const float *thresh;   // mask pass: per-row threshold in score units
+    const float *thresh;   // mask and count passes: per-row threshold in score units
+    SliceCount *outc;      // count pass records
     int wpr;               // mask words per row (k_pad / 32)
 };
 
@@ -264,6 +267,52 @@ __device__ __forceinline__ void tmem_wait(uint32_t (&r)[32]) {
         : "memory");
 }
 
+// 64 consecutive columns of this thread's TMEM lane (asynchronous, as tmem_ld32).
+__device__ __forceinline__ void tmem_ld64(uint32_t taddr, uint32_t (&r)[64]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x64.b32 {"
+        "%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,"
+        "%32,%33,%34,%35,%36,%37,%38,%39,%40,%41,%42,%43,%44,%45,%46,%47,"
+        "%48,%49,%50,%51,%52,%53,%54,%55,%56,%57,%58,%59,%60,%61,%62,%63"
+        "}, [%64];"
+        :
+          "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31]),
+          "=r"(r[32]), "=r"(r[33]), "=r"(r[34]), "=r"(r[35]), "=r"(r[36]), "=r"(r[37]), "=r"(r[38]), "=r"(r[39]),
+          "=r"(r[40]), "=r"(r[41]), "=r"(r[42]), "=r"(r[43]), "=r"(r[44]), "=r"(r[45]), "=r"(r[46]), "=r"(r[47]),
+          "=r"(r[48]), "=r"(r[49]), "=r"(r[50]), "=r"(r[51]), "=r"(r[52]), "=r"(r[53]), "=r"(r[54]), "=r"(r[55]),
+          "=r"(r[56]), "=r"(r[57]), "=r"(r[58]), "=r"(r[59]), "=r"(r[60]), "=r"(r[61]), "=r"(r[62]), "=r"(r[63])
+        : "r"(taddr)
+        : "memory");
+}
+
+__device__ __forceinline__ void tmem_wait(uint32_t (&r)[64]) {
+    asm volatile(
+        "tcgen05.wait::ld.sync.aligned;"
+        :
+          "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7]),
+          "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]), "+r"(r[14]), "+r"(r[15]),
+          "+r"(r[16]), "+r"(r[17]), "+r"(r[18]), "+r"(r[19]), "+r"(r[20]), "+r"(r[21]), "+r"(r[22]), "+r"(r[23]),
+          "+r"(r[24]), "+r"(r[25]), "+r"(r[26]), "+r"(r[27]), "+r"(r[28]), "+r"(r[29]), "+r"(r[30]), "+r"(r[31]),
+          "+r"(r[32]), "+r"(r[33]), "+r"(r[34]), "+r"(r[35]), "+r"(r[36]), "+r"(r[37]), "+r"(r[38]), "+r"(r[39]),
+          "+r"(r[40]), "+r"(r[41]), "+r"(r[42]), "+r"(r[43]), "+r"(r[44]), "+r"(r[45]), "+r"(r[46]), "+r"(r[47]),
+          "+r"(r[48]), "+r"(r[49]), "+r"(r[50]), "+r"(r[51]), "+r"(r[52]), "+r"(r[53]), "+r"(r[54]), "+r"(r[55]),
+          "+r"(r[56]), "+r"(r[57]), "+r"(r[58]), "+r"(r[59]), "+r"(r[60]), "+r"(r[61]), "+r"(r[62]), "+r"(r[63])
+        :
+        : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld(uint32_t taddr, uint32_t (&r)[32]) { tmem_ld32(taddr, r); }
+__device__ __forceinline__ void tmem_ld(uint32_t taddr, uint32_t (&r)[64]) { tmem_ld64(taddr, r); }
+
+// Columns per TMEM load in the top-2 epilogue. 64-column loads (two 64-register
+// buffers) exceed the 168 registers a thread of a 320-thread CTA can hold and
+// spill, so the epilogue loads 32 columns at a time.
+constexpr int TOP2_LOAD_COLS = 32;
+
 __device__ __forceinline__ float fmax3(float a, float b, float c) {
     float r;
     asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
@@ -312,8 +361,8 @@ __device__ __forceinline__ void merge_res(uint32_t &R1, int &I1, uint32_t &R2, i
 // or the other pair's best), then one merge into the running top-2. The same
 // 2.5 ALU operations per score as pairwise ranking, but the running chain
 // advances once per four scores, so more of each warp's work is independent.
-template <int CH, int E>
-__device__ __forceinline__ void rank_quad(const uint32_t (&r)[32], float cgrid, float ulp, float &a1, float &a2) {
+template <int COL0, int E, int N>
+__device__ __forceinline__ void rank_quad(const uint32_t (&r)[N], float cgrid, float ulp, float &a1, float &a2) {
     uint64_t p0, p1, cg2;
     asm("mov.b64 %0, {%1, %2};" : "=l"(p0) : "r"(r[E]), "r"(r[E + 1]));
     asm("mov.b64 %0, {%1, %2};" : "=l"(p1) : "r"(r[E + 2]), "r"(r[E + 3]));
@@ -325,10 +374,10 @@ __device__ __forceinline__ void rank_quad(const uint32_t (&r)[32], float cgrid, 
     float t0, t1, t2, t3;
     asm("mov.b64 {%0, %1}, %2;" : "=f"(t0), "=f"(t1) : "l"(p0));
     asm("mov.b64 {%0, %1}, %2;" : "=f"(t2), "=f"(t3) : "l"(p1));
-    const float k0 = __fmaf_rn(ulp, (float)(127 - ((CH * 32 + E) & 127)), t0);
-    const float k1 = __fmaf_rn(ulp, (float)(127 - ((CH * 32 + E + 1) & 127)), t1);
-    const float k2 = __fmaf_rn(ulp, (float)(127 - ((CH * 32 + E + 2) & 127)), t2);
-    const float k3 = __fmaf_rn(ulp, (float)(127 - ((CH * 32 + E + 3) & 127)), t3);
+    const float k0 = __fmaf_rn(ulp, (float)(127 - ((COL0 + E) & 127)), t0);
+    const float k1 = __fmaf_rn(ulp, (float)(127 - ((COL0 + E + 1) & 127)), t1);
+    const float k2 = __fmaf_rn(ulp, (float)(127 - ((COL0 + E + 2) & 127)), t2);
+    const float k3 = __fmaf_rn(ulp, (float)(127 - ((COL0 + E + 3) & 127)), t3);
     const float m01 = fmaxf(k0, k1), l01 = fminf(k0, k1);
     const float m23 = fmaxf(k2, k3), l23 = fminf(k2, k3);
     const float M = fmaxf(m01, m23), L = fminf(m01, m23);
@@ -339,17 +388,18 @@ __device__ __forceinline__ void rank_quad(const uint32_t (&r)[32], float cgrid, 
 
 constexpr int NCH = 1;  // top-2 chains per rank pass (measured: 1 ~ 2 < 4 < 8 in time; the ALU pipe bounds it)
 
-template <int CH, int E>
+// Ranks the N scores of one TMEM load whose first column is COL0 within the part.
+template <int COL0, int E, int N>
 struct RankChunk {
-    static __device__ __forceinline__ void run(const uint32_t (&r)[32], float cg, float ulp, float (&a1)[NCH],
+    static __device__ __forceinline__ void run(const uint32_t (&r)[N], float cg, float ulp, float (&a1)[NCH],
                                                float (&a2)[NCH]) {
-        rank_quad<CH, E>(r, cg, ulp, a1[(E >> 2) & (NCH - 1)], a2[(E >> 2) & (NCH - 1)]);
-        RankChunk<CH, E + 4>::run(r, cg, ulp, a1, a2);
+        rank_quad<COL0, E, N>(r, cg, ulp, a1[(E >> 2) & (NCH - 1)], a2[(E >> 2) & (NCH - 1)]);
+        RankChunk<COL0, E + 4, N>::run(r, cg, ulp, a1, a2);
     }
 };
-template <int CH>
-struct RankChunk<CH, 32> {
-    static __device__ __forceinline__ void run(const uint32_t (&)[32], float, float, float (&)[NCH], float (&)[NCH]) {}
+template <int COL0, int N>
+struct RankChunk<COL0, N, N> {
+    static __device__ __forceinline__ void run(const uint32_t (&)[N], float, float, float (&)[NCH], float (&)[NCH]) {}
 };
 
 // ------------------------------------------------ mask (second pass) --
@@ -377,6 +427,55 @@ __device__ __forceinline__ uint32_t mask_chunk(const uint32_t (&r)[32], float S,
     float e, o;
     asm("mov.b64 {%0, %1}, %2;" : "=f"(e), "=f"(o) : "l"(acc));
     return (uint32_t)e | ((uint32_t)o << 16);
+}
+
+// Count pass: one 32-column chunk folded into a row's running state -- the
+// largest score (three-input max on the raw accumulators; NaN is ignored,
+// and real scores are positive, so 0 means none), the number of marked
+// centres, and the first two nonzero mask words with their word index gw.
+struct CountState {
+    float vmax;
+    uint32_t cnt, w1, w2;
+    int wi1, wi2;
+};
+
+__device__ __forceinline__ void count_add_word(CountState &s, uint32_t word, int gw) {
+    if (word) {
+        if (!s.w1) {
+            s.w1 = word;
+            s.wi1 = gw;
+        } else if (!s.w2) {
+            s.w2 = word;
+            s.wi2 = gw;
+        }
+    }
+}
+
+__device__ __forceinline__ void count_chunk(const uint32_t (&r)[32], float S, float C, uint64_t two2, int gw,
+                                            CountState &s) {
+    const uint32_t word = mask_chunk(r, S, C, two2);
+    float m0 = s.vmax, m1 = 0.f;  // two chains: more independent work per step
+#pragma unroll
+    for (int e = 0; e < 32; e += 4) {
+        m0 = fmax3(m0, __uint_as_float(r[e]), __uint_as_float(r[e + 1]));
+        m1 = fmax3(m1, __uint_as_float(r[e + 2]), __uint_as_float(r[e + 3]));
+    }
+    s.vmax = fmaxf(m0, m1);
+    s.cnt += (uint32_t)__popc(word);
+    count_add_word(s, word, gw);
+}
+
+__device__ __forceinline__ SliceCount count_pack(const CountState &s) {
+    const uint32_t c = s.cnt < 0xFFFFu ? s.cnt : 0xFFFFu;
+    return SliceCount{s.vmax, c | ((uint32_t)(s.w1 ? s.wi1 : 0xFF) << 16) | ((uint32_t)(s.w2 ? s.wi2 : 0xFF) << 24),
+                      s.w1, s.w2};
+}
+
+__device__ __forceinline__ void count_merge(CountState &s, const SliceCount &o) {
+    s.vmax = fmaxf(s.vmax, o.vmax);
+    s.cnt += o.meta & 0xFFFFu;
+    count_add_word(s, o.w1, (int)((o.meta >> 16) & 0xFFu));
+    count_add_word(s, o.w2, (int)(o.meta >> 24));
 }
 
 // ------------------------------------------------ top-8 (second pass) --
@@ -607,9 +706,14 @@ __global__ void __launch_bounds__(tc_threads(EP), 1)
         asm("mov.b64 %0, {%1, %1};" : "=l"(two2) : "f"(2.f));
         uint32_t item = 0;
         bool dead = false;
+        float th_next = q * BM + row_local < p.n ? p.thresh[q * BM + row_local] : INFINITY;  // one tile ahead
         for (int64_t t = q; t < p.tiles; t += tstride) {
             const int64_t row = t * BM + row_local;
-            const float th = row < p.n ? p.thresh[row] : INFINITY;
+            const float th = th_next;
+            {
+                const int64_t nrow = (t + tstride) * BM + row_local;
+                th_next = nrow < p.n ? p.thresh[nrow] : INFINITY;
+            }
             const float C = -(th * S);  // exact: a float times a power of two
             for (int b = 0; b < p.nblocks; b++, item++) {
                 const int buf = (int)(item & 1u);
@@ -643,10 +747,86 @@ __global__ void __launch_bounds__(tc_threads(EP), 1)
                 }
             }
         }
+    } else if (TOPK == 3) {
+        // Count pass: per row, against the row's threshold, the largest score
+        // and the marked centres' number and first mask words; the parts of a
+        // row meet once per tile through the rotating slots, as in the top-2
+        // pass below.
+        constexpr int CP = BN / EP;
+        static_assert(CP == 128, "the count pass runs with two epilogue parts");
+        constexpr int EPI = 4 * EP * 32;  // epilogue threads (the named barriers' count)
+        const int ew = warp - 2;
+        const int quarter = warp & 3;
+        const int prt = ew >> 2;
+        const int row_local = quarter * 32 + lane;
+        const uint32_t lane_addr = tmem + ((uint32_t)(quarter * 32) << 16);
+        SliceCount *merge = (SliceCount *)(smem + p.off_merge);
+        const float S = 8.f / p.stats->ulp;  // a power of two
+        uint64_t two2;
+        asm("mov.b64 %0, {%1, %1};" : "=l"(two2) : "f"(2.f));
+        uint32_t item = 0, tile_it = 0;
+        bool dead = false;
+        // the row's threshold one tile ahead, so that no tile starts on a
+        // global load
+        float th_next = q * BM + row_local < p.n ? p.thresh[q * BM + row_local] : INFINITY;
+        for (int64_t t = q; t < p.tiles; t += tstride, tile_it++) {
+            const int64_t row = t * BM + row_local;
+            const float th = th_next;
+            {
+                const int64_t nrow = (t + tstride) * BM + row_local;
+                th_next = nrow < p.n ? p.thresh[nrow] : INFINITY;
+            }
+            const float C = -(th * S);  // exact: a float times a power of two
+            CountState st{0.f, 0u, 0u, 0u, 0, 0};
+            for (int b = 0; b < p.nblocks; b++, item++) {
+                const int buf = (int)(item & 1u);
+                const uint32_t aph = (item >> 1) & 1u;
+                if (!dead && !mbar_wait(bar_afull(buf), aph, abort_flag, p.err, 16ull)) dead = true;
+                dead = __any_sync(0xffffffffu, dead);  // warp-uniform, for the barriers below
+                if (dead) continue;
+                tc_fence_after();
+                const uint32_t col = lane_addr + (uint32_t)buf * BN + (uint32_t)prt * CP;
+                const int wbase = (b * BN + prt * CP) / 32;  // word index within the slice
+                uint32_t ra[32], rb[32];
+                tmem_ld32(col, ra);
+                tmem_wait(ra);
+                tmem_ld32(col + 32, rb);
+                count_chunk(ra, S, C, two2, wbase, st);
+                tmem_wait(rb);
+                tmem_ld32(col + 64, ra);
+                count_chunk(rb, S, C, two2, wbase + 1, st);
+                tmem_wait(ra);
+                tmem_ld32(col + 96, rb);
+                count_chunk(ra, S, C, two2, wbase + 2, st);
+                tmem_wait(rb);
+                // every column of this block is in registers: release the buffer
+                tc_fence_before();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(bar_aempty(buf));
+                count_chunk(rb, S, C, two2, wbase + 3, st);
+            }
+            // tile merge: the slot and barrier protocol of the top-2 pass
+            const uint32_t sl = tile_it % (uint32_t)p.slots;
+            SliceCount *slot = merge + sl * (uint32_t)(EP - 1) * BM;
+            if (prt > 0) {
+                slot[(prt - 1) * BM + row_local] = count_pack(st);
+                if (dead)
+                    asm volatile("bar.sync %0, %1;" ::"r"(1u + sl), "r"(EPI) : "memory");
+                else
+                    asm volatile("bar.arrive %0, %1;" ::"r"(1u + sl), "r"(EPI) : "memory");
+            } else {
+                asm volatile("bar.sync %0, %1;" ::"r"(1u + sl), "r"(EPI) : "memory");
+#pragma unroll
+                for (int o = 1; o < EP; o++) count_merge(st, slot[(o - 1) * BM + row_local]);
+                if (row < p.n && !dead) p.outc[(int64_t)part * p.out_stride + row] = count_pack(st);
+            }
+        }
     } else if (TOPK == 2) {
         constexpr int CP = BN / EP;   // columns of one part
         constexpr int NCK = CP / 32;  // its 32-column chunks
         static_assert(NCK == 2 || NCK == 4, "two or four epilogue parts");
+        constexpr int LDW = TOP2_LOAD_COLS;  // columns per TMEM load
+        static_assert(CP / LDW == 2 || CP / LDW == 4, "two or four loads per part");
         constexpr int EPI = 4 * EP * 32;  // epilogue threads (the named barriers' count)
         using Slot = MergeSlot<FP8 || (EP > 2)>;
         const int ew = warp - 2;
@@ -667,15 +847,19 @@ __global__ void __launch_bounds__(tc_threads(EP), 1)
         // (when its MMAs have already committed) while those last columns
         // are ranked, so the warps of a sub-partition do not all wait on a
         // fresh TMEM load at every block. pre: ra holds that load.
-        uint32_t ra[32], rb[32];
+        uint32_t ra[LDW], rb[LDW];
         bool pre = false;
+        // FP8: the row's scale one tile ahead, so that no tile starts on a global load
+        float rs_next = 1.f;
+        if (FP8 && q * BM + row_local < p.n) rs_next = p.rowscale[q * BM + row_local];
         for (int64_t t = q; t < p.tiles; t += tstride, tile_it++) {
             uint32_t R1 = 0u, R2 = 0u, U = 0u;
             int I1 = -1, I2 = -1;
             float cg = cgrid, ul = ulp;
             if (FP8) {
-                const int64_t rrow = t * BM + row_local;
-                const float rs = rrow < p.n ? p.rowscale[rrow] : 1.f;
+                const float rs = rs_next;
+                const int64_t nrow = (t + tstride) * BM + row_local;
+                rs_next = nrow < p.n ? p.rowscale[nrow] : 1.f;
                 cg = cgrid * rs;
                 ul = ulp * rs;
             }
@@ -688,7 +872,7 @@ __global__ void __launch_bounds__(tc_threads(EP), 1)
                     dead = __any_sync(0xffffffffu, dead);  // warp-uniform, for the barriers below
                     if (dead) continue;
                     tc_fence_after();
-                    tmem_ld32(col, ra);
+                    tmem_ld(col, ra);
                 }
                 pre = false;
                 if (p.dump && blockIdx.x == 0 && t == q) {
@@ -705,15 +889,15 @@ __global__ void __launch_bounds__(tc_threads(EP), 1)
 #pragma unroll
                 for (int qd = 0; qd < NCH; qd++) a1[qd] = a2[qd] = 0.f;
                 tmem_wait(ra);
-                tmem_ld32(col + 32, rb);
-                RankChunk<0, 0>::run(ra, cg, ul, a1, a2);
+                tmem_ld(col + LDW, rb);
+                RankChunk<0, 0, LDW>::run(ra, cg, ul, a1, a2);
                 tmem_wait(rb);
-                if (NCK == 4) {
-                    tmem_ld32(col + 64, ra);
-                    RankChunk<1, 0>::run(rb, cg, ul, a1, a2);
+                if (CP / LDW == 4) {
+                    tmem_ld(col + 2 * LDW, ra);
+                    RankChunk<LDW, 0, LDW>::run(rb, cg, ul, a1, a2);
                     tmem_wait(ra);
-                    tmem_ld32(col + 96, rb);
-                    RankChunk<2, 0>::run(ra, cg, ul, a1, a2);
+                    tmem_ld(col + 3 * LDW, rb);
+                    RankChunk<2 * LDW, 0, LDW>::run(ra, cg, ul, a1, a2);
                     tmem_wait(rb);
                 }
                 // every column of this block is in registers: release the buffer
@@ -725,11 +909,11 @@ __global__ void __launch_bounds__(tc_threads(EP), 1)
                     const uint32_t naph = ((item + 1) >> 1) & 1u;
                     if (__all_sync(0xffffffffu, mbar_try_wait(bar_afull(nbuf), naph))) {
                         tc_fence_after();
-                        tmem_ld32(lane_addr + (uint32_t)nbuf * BN + (uint32_t)prt * CP, ra);
+                        tmem_ld(lane_addr + (uint32_t)nbuf * BN + (uint32_t)prt * CP, ra);
                         pre = true;
                     }
                 }
-                RankChunk<NCK - 1, 0>::run(rb, cg, ul, a1, a2);
+                RankChunk<CP - LDW, 0, LDW>::run(rb, cg, ul, a1, a2);
                 uint32_t b1 = __float_as_uint(a1[0]), b2 = __float_as_uint(a2[0]), bu = b2;
                 int d1 = 0, d2 = 0;  // indices are carried inside the keys
 #pragma unroll
@@ -769,7 +953,8 @@ __global__ void __launch_bounds__(tc_threads(EP), 1)
                 const int64_t row = t * BM + row_local;
                 if (row < p.n && !dead)
                     p.out[(int64_t)part * p.out_stride + row] =
-                        Top2{__uint_as_float(R1), __uint_as_float(R2), __uint_as_float(U), 0.f, I1, I2, 0, 0};
+                        SliceTop2{__uint_as_float(R1), __uint_as_float(R2), __uint_as_float(U),
+                                  pack_local(I1, slice0) | (pack_local(I2, slice0) << 16)};
             }
         }
         if (pre) tmem_wait(ra);  // a load issued for an item that never ran completes before exit
@@ -1001,7 +1186,7 @@ void plan_shape(MixedPlan &mp, int64_t n, int d, int k, bool fp8, int topk, int 
         mp.kp = ((k + mp.parts - 1) / mp.parts + BN - 1) / BN * BN;
         mp.k_pad = mp.parts * mp.kp;
         mp.nblocks = mp.kp / BN;
-        if (topk == 2 && mp.nblocks < 2 && mp.slots < 3) {
+        if ((topk == 2 || topk == 3) && mp.nblocks < 2 && mp.slots < 3) {
             mp.slots = 3;
             continue;
         }
@@ -1028,13 +1213,14 @@ void plan_tc(Ctx &ctx, MixedPlan &mp, int64_t n, int d, int k, bool fp8, int top
     }
 }
 
-void launch_tc_assign(Ctx &ctx, MixedPlan &mp, const void *xb, const void *cb, const void *caug, Top2 *out,
+void launch_tc_assign(Ctx &ctx, MixedPlan &mp, const void *xb, const void *cb, const void *caug, SliceTop2 *out,
                       Top8 *out8, DevScalars *sc, const MixedStats *stats, float *dump,
                       const unsigned long long *n_dev, const void *xaug, const float *rowscale, uint32_t *masks,
-                      const float *thresh) {
+                      const float *thresh, SliceCount *outc) {
     const bool fp8 = mp.fp8;
     if ((mp.topk == 2) != (out != nullptr) || (mp.topk == 8) != (out8 != nullptr) ||
-        (mp.topk == 1) != (masks != nullptr && thresh != nullptr) || (mp.topk == 1 && fp8)) {
+        (mp.topk == 1) != (masks != nullptr) || (mp.topk == 3) != (outc != nullptr) ||
+        ((mp.topk == 1 || mp.topk == 3) != (thresh != nullptr)) || ((mp.topk == 1 || mp.topk == 3) && fp8)) {
         set_error("tensor-core launch: records do not match the plan");
         fail(FK_ERR_INVALID_PARAMETER);
     }
@@ -1093,6 +1279,7 @@ void launch_tc_assign(Ctx &ctx, MixedPlan &mp, const void *xb, const void *cb, c
     p.dump = dump;
     p.masks = masks;
     p.thresh = thresh;
+    p.outc = outc;
     p.wpr = mp.k_pad / 32;
     const size_t smem = (size_t)p.off_bar + BAR_BYTES + 1024;
     if (smem > SMEM_LIMIT) {
@@ -1109,6 +1296,8 @@ void launch_tc_assign(Ctx &ctx, MixedPlan &mp, const void *xb, const void *cb, c
     // second pass (top-8, or candidate masks) BF16 with one or two X stages.
     if (mp.topk == 1) {
         mp.xst == 2 ? go(tc_assign_kernel<1, false, 2, 2>) : go(tc_assign_kernel<1, false, 1, 2>);
+    } else if (mp.topk == 3) {
+        mp.xst == 2 ? go(tc_assign_kernel<3, false, 2, 2>) : go(tc_assign_kernel<3, false, 1, 2>);
     } else if (mp.topk == 8) {
         if (fp8) {
             set_error("the second pass runs in BF16");

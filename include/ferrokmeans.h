@@ -84,10 +84,12 @@ typedef struct fk_fit_report {
     int64_t rows_full_rescan;  /* mixed: of those, rows whose third score
                                   was also inside the bound                */
     int64_t rows_fp64;         /* mixed: rows that needed FP64 scores      */
-    int64_t rows_second_pass;  /* mixed: rows scored again by the BF16
-                                  top-8 tensor pass (= rows_full_rescan)   */
+    int64_t rows_second_pass;  /* mixed: rows scored again by a second
+                                  tensor pass (= rows_full_rescan): BF16
+                                  candidate masks after a BF16 main pass,
+                                  BF16 top-8 after an FP8 one              */
     int64_t rows_few;          /* mixed: of those, rows resolved among at
-                                  most eight candidates                    */
+                                  most 32 (masks) or 8 (top-8) candidates  */
     int64_t rows_exhaustive;   /* mixed: rows re-scored against every
                                   centre after the second pass             */
     int64_t near_tie_rows;     /* mixed: re-scored rows whose FP64 margin
@@ -105,6 +107,12 @@ typedef struct fk_fit_report {
     int64_t updates_incremental; /* mixed: iterations whose centroid update
                                   was incremental (the rest were full
                                   passes over X)                           */
+    int64_t count_iterations;  /* BF16 fits: iterations whose main pass was
+                                  the count pass (thresholds carried from
+                                  the previous iteration; the rest ranked
+                                  a top-2)                                 */
+    double ms_count_pass;      /* device time of those count passes (part
+                                  of ms_contract)                          */
 } fk_fit_report;
 
 typedef struct fk_ctx fk_ctx;

@@ -72,6 +72,8 @@ pub struct fk_fit_report {
     pub reserved: i32,
     pub rows_moved: i64,
     pub updates_incremental: i64,
+    pub count_iterations: i64,
+    pub ms_count_pass: f64,
 }
 
 #[repr(C)]

@@ -376,6 +376,29 @@ def test_bf16_mask_pass_at_full_k_and_d_matches_fp64_oracle():
     assert rep["rows_second_pass"] >= 400
 
 
+def test_bf16_count_pass_fit_matches_fp64_oracle_and_single_steps():
+    # from the fourth iteration of a fit on, the BF16 main pass is the count
+    # pass (thresholds carried from the previous iteration); the fit's labels,
+    # centres and n_iter must be the FP64 oracle's, and its centres bit for
+    # bit those of single steps, which always rank a top-2
+    w = W.anisotropic_1024x128(scale=0.01)  # 40,000 rows, d = 128, k = 1024
+    x32, k = w["x"].copy(), w["k"]
+    rng = np.random.default_rng(24)
+    x32[:300] = _equidistant_rows(w["init"], [3, 500, 1000], 300, rng).astype(np.float32)
+    iters = 12
+    g = F.KMeans(k, dtype="f32x64").with_precision("bf16").with_max_iter(iters).with_tol(0.0).with_n_init(1) \
+        .with_init_centers(w["init"]).fit(x32)
+    o = O.fit(x32.astype(np.float64), k, max_iter=iters, tol=0.0, n_init=1, init=w["init"][None])
+    assert np.array_equal(g.labels(), o["labels"])
+    assert _close(g.cluster_centers(), o["centers"])
+    assert g.n_iter() == o["n_iter"] == iters
+    assert g.report["count_iterations"] >= 3
+    c = w["init"]
+    for _ in range(iters):
+        gl, c, gi, gs, rep = F.lloyd_step(x32, c, dtype="f32x64", precision="bf16")
+    assert np.array_equal(g.cluster_centers(), c)
+
+
 def test_bf16_mask_pass_sends_wide_ties_to_the_exhaustive_rescore():
     # forty copies of one centre: a row near it has forty exactly tied
     # candidates, more than the mask pass re-scores (32), so it is re-scored
