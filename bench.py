@@ -93,12 +93,14 @@ def parse(argv=None):
 
 METRIC = "KMeans Lloyd iters/s & pt·k/s: BF16+FP64 recheck vs plain FP32, labels=FP64"
 
-# DRAM traffic of the dominant kernel per row of X (ncu dram__bytes_read.sum +
+# DRAM traffic of the main pass per row of X (ncu dram__bytes_read.sum +
 # dram__bytes_write.sum of one launch, divided by the rows it processed; the
 # traffic grows in proportion to the rows: X read once, records written once).
-# Source: profiles/tc_assign_anisotropic_1024x128_quarter.md, a 1,000,000-row
-# capture of tc_assign_kernel<2, BF16> (256.4 MB read + 48.4 MB written).
-TRAFFIC_BYTES_PER_ROW = {("anisotropic_1024x128", "bf16"): (256.4e6 + 48.4e6) / 1e6}
+# Source: profiles/tc_count_anisotropic_1024x128_quarter.md, 1,000,000-row
+# captures of tc_assign_kernel<3> (count pass: 260.4 MB read + 25.5 MB
+# written) and tc_assign_kernel<2> (top-2 pass: 256.4 + 25.1 MB).
+TRAFFIC_BYTES_PER_ROW = {("anisotropic_1024x128", "bf16", "count"): (260.4e6 + 25.5e6) / 1e6,
+                         ("anisotropic_1024x128", "bf16", "top2"): (256.4e6 + 25.1e6) / 1e6}
 
 
 def load_peaks():
@@ -862,12 +864,14 @@ def run_ours(args):
                 "peak_source": f"{form.upper()} FMA peak measured in this run (fk_debug_measure_peaks); achieved "
                                "counts 2 n k d (the GEMM-equivalent work), the direct form executes 3 n k d"}
     roof["frac"] = roof["achieved"] / roof["peak"]
-    tb = TRAFFIC_BYTES_PER_ROW.get((w["name"], form))
+    dom_count = form == "bf16" and n_count * 2 > iters
+    tb = TRAFFIC_BYTES_PER_ROW.get((w["name"], form, "count" if dom_count else "top2"))
     roof["traffic"] = tb * n if tb is not None else None
     if tb is not None:
         roof["traffic_source"] = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch at 1,000,000 rows "
-                                  "(profiles/tc_assign_anisotropic_1024x128_quarter.md), scaled to n rows")
-        roof["algorithmic_bytes"] = n * d * 2 + n * 2 * 32  # BF16 X once + 32-byte records per row and slice
+                                  "(profiles/tc_count_anisotropic_1024x128_quarter.md), scaled to n rows")
+        # BF16 X once + 16-byte records per row and slice (+ the count pass's per-row threshold)
+        roof["algorithmic_bytes"] = n * d * 2 + n * 2 * 16 + (4 * n if dom_count else 0)
     if form == "bf16" and n_count * 2 > iters:
         roof["kernel"] = (f"tc_assign_kernel<3> (BF16 tcgen05 contraction + count epilogue against carried "
                           f"thresholds; {n_count} of {iters} iterations)")

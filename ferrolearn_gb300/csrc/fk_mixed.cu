@@ -643,7 +643,6 @@ __device__ __forceinline__ unsigned long long warp_reserve(unsigned long long *c
 }
 
 constexpr int FINALIZE_THREADS = 512;
-constexpr int FIN_ROUNDS = 3;  // rows per finalize block: FIN_ROUNDS x FINALIZE_THREADS
 
 // A row's class after the main pass: 0 decided (the kernel wrote the label),
 // 1 a pair (a, b) for the exact re-score, 2 the second pass with threshold
@@ -653,78 +652,87 @@ struct RowClass {
     float th;
 };
 
-// Staged appends of one finalize block: its rows' pair and full entries are
-// placed in shared memory in row order, round by round, then one atomic per
-// list reserves their global slots -- a few thousand atomics per pass on the
-// two shared counters, instead of one or two per 512 rows, whose serialised
-// round trips in L2 bounded the pass.
-struct FinStage {
-    int4 pairs[FIN_ROUNDS * FINALIZE_THREADS];
-    int32_t rows[FIN_ROUNDS * FINALIZE_THREADS];
-    float ths[FIN_ROUNDS * FINALIZE_THREADS];
-    unsigned wa[FINALIZE_THREADS / 32], wb[FINALIZE_THREADS / 32];
-    unsigned na, nb;
-    unsigned long long base_a, base_b;
-};
-
-template <typename Classify>
-__device__ __forceinline__ void finalize_block(int64_t n, Classify classify, int4 *__restrict__ pair_list,
-                                               int32_t *__restrict__ full_list, float *__restrict__ full_thresh,
-                                               DevScalars *sc) {
-    __shared__ FinStage st;
+// Persistent finalize loop: each block takes chunks of FINALIZE_THREADS rows
+// (grid-stride), with the next chunk's records (load) in flight while this
+// chunk is classified (classify). A chunk's pair and full entries get
+// consecutive list slots after a block scan of the warps' ballots and one
+// atomic per list, which thread 0 issues for chunk i and whose results are
+// only read while chunk i + 1 is handled: the entries of chunk i are written
+// one iteration late, so no chunk waits on an atomic's round trip.
+template <typename Load, typename Classify>
+__device__ __forceinline__ void finalize_rows(int64_t n, Load load, Classify classify, int4 *__restrict__ pair_list,
+                                              int32_t *__restrict__ full_list, float *__restrict__ full_thresh,
+                                              DevScalars *sc) {
+    __shared__ unsigned wa[2][FINALIZE_THREADS / 32], wb[2][FINALIZE_THREADS / 32];
+    __shared__ unsigned long long base_a, base_b;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    if (threadIdx.x == 0) {
-        st.na = 0u;
-        st.nb = 0u;
-    }
-    const int64_t row0 = (int64_t)blockIdx.x * FIN_ROUNDS * FINALIZE_THREADS;
-    for (int r = 0; r < FIN_ROUNDS; r++) {
-        const int64_t i = row0 + (int64_t)r * FINALIZE_THREADS + threadIdx.x;
+    const unsigned below = (1u << lane) - 1u;
+    const int64_t chunks = (n + FINALIZE_THREADS - 1) / FINALIZE_THREADS;
+    int64_t ch = blockIdx.x;
+    decltype(load(int64_t(0))) cur{}, nxt{};
+    if (ch < chunks && ch * FINALIZE_THREADS + threadIdx.x < n) cur = load(ch * FINALIZE_THREADS + threadIdx.x);
+    // the previous chunk's entry of this thread, its warp's ballots, and
+    // (thread 0) the atomics' pending results
+    RowClass pc{-1, -1, -1, 0.f};
+    int64_t pi = -1;
+    unsigned pba = 0u, pbb = 0u;
+    unsigned long long pend_a = 0ull, pend_b = 0ull;
+    int buf = 0;
+    bool have_prev = false;
+    auto write_prev = [&](int pbuf) {
+        if (pc.cls == 1) pair_list[base_a + wa[pbuf][w] + (unsigned)__popc(pba & below)] = make_int4((int)pi, pc.a, pc.b, 0);
+        if (pc.cls == 2) {
+            const unsigned long long q = base_b + wb[pbuf][w] + (unsigned)__popc(pbb & below);
+            full_list[q] = (int32_t)pi;
+            if (full_thresh) full_thresh[q] = pc.th;
+        }
+    };
+    for (; ch < chunks; ch += gridDim.x) {
+        const int64_t nrow = (ch + gridDim.x) * FINALIZE_THREADS + threadIdx.x;
+        if (ch + gridDim.x < chunks && nrow < n) nxt = load(nrow);
+        const int64_t i = ch * FINALIZE_THREADS + threadIdx.x;
         RowClass c{-1, -1, -1, 0.f};
-        if (i < n) c = classify(i);
+        if (i < n) c = classify(i, cur);
         const unsigned ba = __ballot_sync(0xffffffffu, c.cls == 1), bb = __ballot_sync(0xffffffffu, c.cls == 2);
         if (lane == 0) {
-            st.wa[w] = (unsigned)__popc(ba);
-            st.wb[w] = (unsigned)__popc(bb);
+            wa[buf][w] = (unsigned)__popc(ba);
+            wb[buf][w] = (unsigned)__popc(bb);
         }
         __syncthreads();
         if (threadIdx.x == 0) {
-            unsigned ta = st.na, tb = st.nb;
+            // the previous chunk's bases (its atomics have had a whole chunk to return)
+            base_a = pend_a;
+            base_b = pend_b;
+            unsigned ta = 0, tb = 0;
             for (int q = 0; q < FINALIZE_THREADS / 32; q++) {
-                const unsigned xa = st.wa[q], xb = st.wb[q];
-                st.wa[q] = ta;
-                st.wb[q] = tb;
+                const unsigned xa = wa[buf][q], xb = wb[buf][q];
+                wa[buf][q] = ta;
+                wb[buf][q] = tb;
                 ta += xa;
                 tb += xb;
             }
-            st.na = ta;
-            st.nb = tb;
+            pend_a = ta ? atomicAdd(&sc->flag_count, (unsigned long long)ta) : 0ull;
+            pend_b = tb ? atomicAdd(&sc->full_count, (unsigned long long)tb) : 0ull;
         }
         __syncthreads();
-        const unsigned below = (1u << lane) - 1u;
-        if (c.cls == 1) st.pairs[st.wa[w] + (unsigned)__popc(ba & below)] = make_int4((int)i, c.a, c.b, 0);
-        if (c.cls == 2) {
-            const unsigned q = st.wb[w] + (unsigned)__popc(bb & below);
-            st.rows[q] = (int32_t)i;
-            st.ths[q] = c.th;
+        if (have_prev) write_prev(buf ^ 1);
+        pc = c;
+        pi = i;
+        pba = ba;
+        pbb = bb;
+        have_prev = true;
+        buf ^= 1;
+        cur = nxt;
+        __syncthreads();  // base_a, base_b and this buffer's offsets are rewritten next
+    }
+    if (have_prev) {
+        if (threadIdx.x == 0) {
+            base_a = pend_a;
+            base_b = pend_b;
         }
-        __syncthreads();  // wa, wb are rewritten in the next round
+        __syncthreads();
+        write_prev(buf ^ 1);
     }
-    if (threadIdx.x == 0) {
-        st.base_a = st.na ? atomicAdd(&sc->flag_count, (unsigned long long)st.na) : 0ull;
-        st.base_b = st.nb ? atomicAdd(&sc->full_count, (unsigned long long)st.nb) : 0ull;
-    }
-    __syncthreads();
-    for (unsigned q = threadIdx.x; q < st.na; q += FINALIZE_THREADS) pair_list[st.base_a + q] = st.pairs[q];
-    for (unsigned q = threadIdx.x; q < st.nb; q += FINALIZE_THREADS) {
-        full_list[st.base_b + q] = st.rows[q];
-        if (full_thresh) full_thresh[st.base_b + q] = st.ths[q];
-    }
-}
-
-unsigned finalize_blocks(int64_t n) {
-    const int64_t per = (int64_t)FIN_ROUNDS * FINALIZE_THREADS;
-    return (unsigned)((n + per - 1) / per);
 }
 
 __global__ void __launch_bounds__(FINALIZE_THREADS)
@@ -732,12 +740,21 @@ __global__ void __launch_bounds__(FINALIZE_THREADS)
                     const float4 *__restrict__ rowinfo, const MixedStats *stats, float acc_rel, float mu_norm,
                     int32_t *__restrict__ labels, int4 *__restrict__ pair_list, int32_t *__restrict__ full_list,
                     float *__restrict__ full_thresh, float *__restrict__ floor_out, DevScalars *sc) {
-    auto classify = [&](int64_t i) {
+    struct Rec {
+        float4 ri;
+        SliceTop2 t, o1;
+    };
+    auto load = [&](int64_t i) {
+        Rec r;
+        r.ri = rowinfo[i];
+        r.t = parts[i];
+        r.o1 = nparts > 1 ? parts[(int64_t)n + i] : r.t;
+        return r;
+    };
+    auto classify = [&](int64_t i, const Rec &rec) {
         RowClass c{-1, -1, -1, -INFINITY};
-        // all loads first (independent), then the merge
-        const float4 ri = rowinfo[i];
-        const SliceTop2 t = parts[i];
-        const SliceTop2 o1 = nparts > 1 ? parts[(int64_t)n + i] : t;
+        const float4 ri = rec.ri;
+        const SliceTop2 t = rec.t, o1 = rec.o1;
         float v1 = t.v1, v2 = t.v2, u3 = t.u3;
         int i1 = slice_index(t.ids & 0xFFFFu, 0);
         int i2 = slice_index(t.ids >> 16, 0);
@@ -780,7 +797,7 @@ __global__ void __launch_bounds__(FINALIZE_THREADS)
         }
         return c;
     };
-    finalize_block(n, classify, pair_list, full_list, full_thresh, sc);
+    finalize_rows(n, load, classify, pair_list, full_list, full_thresh, sc);
 }
 
 // ------------------------------------------------------------ count pass --
@@ -870,13 +887,26 @@ __global__ void __launch_bounds__(FINALIZE_THREADS)
                           const float *__restrict__ thresh, int32_t *__restrict__ labels,
                           int4 *__restrict__ pair_list, int32_t *__restrict__ full_list,
                           float *__restrict__ full_thresh, float *__restrict__ floor_out, DevScalars *sc) {
-    auto classify = [&](int64_t i) {
+    struct Rec {
+        float4 ri;
+        SliceCount o0, o1;
+        float th;
+    };
+    auto load = [&](int64_t i) {
+        Rec r;
+        r.ri = rowinfo[i];
+        r.o0 = parts[i];
+        r.o1 = nparts > 1 ? parts[(int64_t)n + i] : r.o0;
+        r.th = thresh[i];
+        return r;
+    };
+    auto classify = [&](int64_t i, const Rec &rec) {
         RowClass c{-1, -1, -1, 0.f};
         float vmax = 0.f;
         uint32_t cnt = 0, w1 = 0, w2 = 0;
         int b1 = 0, b2 = 0;  // the words' first centre
         for (int p = 0; p < nparts; p++) {
-            const SliceCount o = parts[(int64_t)p * n + i];
+            const SliceCount o = p == 0 ? rec.o0 : p == 1 ? rec.o1 : parts[(int64_t)p * n + i];
             vmax = fmaxf(vmax, o.vmax);
             cnt += o.meta & 0xFFFFu;
             const int wi[2] = {(int)((o.meta >> 16) & 0xFFu), (int)(o.meta >> 24)};
@@ -893,7 +923,7 @@ __global__ void __launch_bounds__(FINALIZE_THREADS)
                 }
             }
         }
-        const float4 ri = rowinfo[i];
+        const float4 ri = rec.ri;
         floor_out[i] = row_floor(vmax, 0.f, ri, stats, acc_rel, mu_norm, d);
         int a = -1, b = -1;
         if (cnt == 1 && w1) {
@@ -918,12 +948,11 @@ __global__ void __launch_bounds__(FINALIZE_THREADS)
             // error bound E (a wide carried window would send the row to the
             // exhaustive re-score)
             const float t2 = __fsub_rd(vmax, row_threshold(ri, stats, acc_rel, mu_norm, d, stats->big));
-            const float t = fmaxf(thresh[i], t2 >= stats->ulp * 2097152.f ? t2 : -INFINITY);
-            c.th = t;
+            c.th = fmaxf(rec.th, t2 >= stats->ulp * 2097152.f ? t2 : -INFINITY);
         }
         return c;
     };
-    finalize_block(n, classify, pair_list, full_list, full_thresh, sc);
+    finalize_rows(n, load, classify, pair_list, full_list, full_thresh, sc);
 }
 
 // ------------------------------------------------------------ re-checks --
@@ -1045,7 +1074,8 @@ __global__ void pair_rescore_kernel(const TX *__restrict__ x, int d, const doubl
 
 // pair_rescore_kernel for f32 rows with d % 4 == 0 and d <= 128: the same
 // decisions, software-pipelined -- the list entry two rows ahead and the
-// feature and centre pieces one row ahead load while this row is decided.
+// feature and centre pieces (and the centres' rounding errors) one row ahead
+// load while this row is decided.
 // Lanes 0-15 hold centre a, lanes 16-31 centre b, 16-byte pieces hl, hl + 16.
 __global__ void __launch_bounds__(256)
     pair_rescore4_kernel(const float *__restrict__ x, int d, const double *__restrict__ c,
@@ -1058,7 +1088,9 @@ __global__ void __launch_bounds__(256)
     const int d4 = d >> 2;
     const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
     auto entry = [&](unsigned long long q) { return q < cnt ? list[q] : make_int4(-1, 0, 0, 0); };
-    auto pieces = [&](const int4 &e, float4 (&xv)[2], float4 (&cv)[2]) {
+    // this lane's pieces of the row and of its centre (a for lanes 0-15, b for
+    // 16-31), and that centre's rounding error
+    auto pieces = [&](const int4 &e, float4 (&xv)[2], float4 (&cv)[2], float &ec) {
         const int a = min(e.y, e.z), b = max(e.y, e.z);
 #pragma unroll
         for (int i = 0; i < 2; i++) {
@@ -1067,15 +1099,18 @@ __global__ void __launch_bounds__(256)
             xv[i] = ok ? reinterpret_cast<const float4 *>(x + (int64_t)e.x * d)[q] : z4;
             cv[i] = ok ? reinterpret_cast<const float4 *>(c32 + (int64_t)(lane < 16 ? a : b) * d)[q] : z4;
         }
+        ec = e.x >= 0 ? ec32[lane < 16 ? a : b] : 0.f;
     };
     unsigned long long s = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     int4 e0 = entry(s), e1 = entry(s + nw);
     float4 xa[2], ca[2];
-    pieces(e0, xa, ca);
+    float eca;
+    pieces(e0, xa, ca, eca);
     for (; s < cnt; s += nw) {
         const int4 e2 = entry(s + 2 * nw);
         float4 xb[2], cb[2];
-        pieces(e1, xb, cb);
+        float ecb;
+        pieces(e1, xb, cb, ecb);
         float acc = 0.f;  // padding pieces are zero on both sides
 #pragma unroll
         for (int i = 0; i < 2; i++) {
@@ -1091,7 +1126,8 @@ __global__ void __launch_bounds__(256)
         acc = half_warp_sum_f(acc);
         const float sa = __shfl_sync(0xffffffffu, acc, 0), sb = __shfl_sync(0xffffffffu, acc, 16);
         const int a = min(e0.y, e0.z), b = max(e0.y, e0.z);
-        const float ea = bound32(sa, ec32[a], d), eb = bound32(sb, ec32[b], d);
+        const float ea = bound32(sa, __shfl_sync(0xffffffffu, eca, 0), d),
+                    eb = bound32(sb, __shfl_sync(0xffffffffu, eca, 16), d);
         if (below(sa, ea, sb, eb)) {
             if (lane == 0) labels[e0.x] = a;
         } else if (below(sb, eb, sa, ea)) {
@@ -1102,6 +1138,7 @@ __global__ void __launch_bounds__(256)
         }
         e0 = e1;
         e1 = e2;
+        eca = ecb;
 #pragma unroll
         for (int i = 0; i < 2; i++) {
             xa[i] = xb[i];
@@ -1396,7 +1433,7 @@ __global__ void oct_rescore_kernel(const float *__restrict__ x, int d, const flo
 // its candidate mask, wpr words with bit per centre (mask_chunk's layout:
 // word w, bit b < 16 is centre 32 w + 2 (15 - b), bit b >= 16 is centre
 // 32 w + 2 (31 - b) + 1). One warp per row: the candidates below k are
-// collected in order (a warp scan of the words' bit counts); with 1 to 32 of
+// collected (a warp scan of the words' bit counts places them); with 1 to 32 of
 // them, FP32 distances with rigorous bounds (four lanes per candidate,
 // eight at a time), then the candidates whose lower bound reaches the
 // smallest upper bound decide: one is the label, up to eight go to FP64,
@@ -1524,13 +1561,9 @@ __global__ void __launch_bounds__(MASK_WARPS * 32)
             }
             const int total = __shfl_sync(0xffffffffu, incl, 31);
             if (m + total <= MASK_CANDS) {
-                // this lane's candidates in increasing centre order
+                // this lane's candidates (one step per set bit; any order)
                 int pos = m + incl - c;
-                const uint32_t lo = word & 0xFFFFu, hi = word >> 16;
-                for (int j = 0; j < 16; j++) {  // centre 32 w + 2 j + parity: bit 15 - j (even), 31 - j (odd)
-                    if ((lo >> (15 - j)) & 1u) cand[pos++] = 32 * w + 2 * j;
-                    if ((hi >> (15 - j)) & 1u) cand[pos++] = 32 * w + 2 * j + 1;
-                }
+                for (uint32_t rest = word; rest; rest &= rest - 1u) cand[pos++] = mask_column(w, __ffs(rest) - 1);
             }
             m += total;
         }
@@ -1946,7 +1979,9 @@ void run_assign_mixed(Ctx &ctx, const TX *x, int64_t n, int d, const double *c, 
     float *floors = fp8 ? nullptr : (float *)ctx.get(BUF_FLOORS, sizeof(float) * (size_t)n);
     const float acc_rel = (float)((double)((size_t)mp.d_pad + 32) * ACC_REL_PER_K);  // exact: integer * 2^-22
     const float mun = mu_norm_up(mp.mu_norm);
-    const unsigned fin_blocks = finalize_blocks(n);
+    static const int fin_top2 = resident_blocks((const void *)finalize_kernel, FINALIZE_THREADS);
+    static const int fin_count = resident_blocks((const void *)finalize_count_kernel, FINALIZE_THREADS);
+    const int64_t fin_chunks = (n + FINALIZE_THREADS - 1) / FINALIZE_THREADS;
     if (!fp8 && c_prev && labels_prev) {
         // count pass, against thresholds carried from the previous iteration
         MixedPlan &mc = ctx.mixedc;
@@ -1970,7 +2005,8 @@ void run_assign_mixed(Ctx &ctx, const TX *x, int64_t n, int d, const double *c, 
             launch_tc_assign(ctx, mc, B.xq, B.cq, B.caug, nullptr, nullptr, sc, B.stats, nullptr, nullptr, nullptr,
                              nullptr, nullptr, th, cnt);
         }
-        finalize_count_kernel<<<fin_blocks, FINALIZE_THREADS, 0, s>>>(cnt, mc.parts, mc.kp, n, k, d, B.rowinfo,
+        finalize_count_kernel<<<(unsigned)std::min<int64_t>(fin_chunks, (int64_t)ctx.num_sms * fin_count),
+                                FINALIZE_THREADS, 0, s>>>(cnt, mc.parts, mc.kp, n, k, d, B.rowinfo,
                                                                       B.stats, acc_rel, mun, th, labels, pairs, full,
                                                                       full_thresh, floors, sc);
         FK_LAUNCH_CHECK();
@@ -1981,7 +2017,8 @@ void run_assign_mixed(Ctx &ctx, const TX *x, int64_t n, int d, const double *c, 
             launch_tc_assign(ctx, mp, B.xq, B.cq, B.caug, top, nullptr, sc, B.stats, nullptr, nullptr, B.xaug,
                              rowscale);
         }
-        finalize_kernel<<<fin_blocks, FINALIZE_THREADS, 0, s>>>(top, mp.parts, mp.kp, n, k, d, B.rowinfo, B.stats,
+        finalize_kernel<<<(unsigned)std::min<int64_t>(fin_chunks, (int64_t)ctx.num_sms * fin_top2), FINALIZE_THREADS,
+                          0, s>>>(top, mp.parts, mp.kp, n, k, d, B.rowinfo, B.stats,
                                                                 acc_rel, mun, labels, pairs, full, full_thresh,
                                                                 floors, sc);
         FK_LAUNCH_CHECK();

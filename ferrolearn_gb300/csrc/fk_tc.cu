@@ -267,50 +267,12 @@ __device__ __forceinline__ void tmem_wait(uint32_t (&r)[32]) {
         : "memory");
 }
 
-// 64 consecutive columns of this thread's TMEM lane (asynchronous, as tmem_ld32).
-__device__ __forceinline__ void tmem_ld64(uint32_t taddr, uint32_t (&r)[64]) {
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x64.b32 {"
-        "%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,"
-        "%32,%33,%34,%35,%36,%37,%38,%39,%40,%41,%42,%43,%44,%45,%46,%47,"
-        "%48,%49,%50,%51,%52,%53,%54,%55,%56,%57,%58,%59,%60,%61,%62,%63"
-        "}, [%64];"
-        :
-          "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
-          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
-          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31]),
-          "=r"(r[32]), "=r"(r[33]), "=r"(r[34]), "=r"(r[35]), "=r"(r[36]), "=r"(r[37]), "=r"(r[38]), "=r"(r[39]),
-          "=r"(r[40]), "=r"(r[41]), "=r"(r[42]), "=r"(r[43]), "=r"(r[44]), "=r"(r[45]), "=r"(r[46]), "=r"(r[47]),
-          "=r"(r[48]), "=r"(r[49]), "=r"(r[50]), "=r"(r[51]), "=r"(r[52]), "=r"(r[53]), "=r"(r[54]), "=r"(r[55]),
-          "=r"(r[56]), "=r"(r[57]), "=r"(r[58]), "=r"(r[59]), "=r"(r[60]), "=r"(r[61]), "=r"(r[62]), "=r"(r[63])
-        : "r"(taddr)
-        : "memory");
-}
-
-__device__ __forceinline__ void tmem_wait(uint32_t (&r)[64]) {
-    asm volatile(
-        "tcgen05.wait::ld.sync.aligned;"
-        :
-          "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7]),
-          "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]), "+r"(r[14]), "+r"(r[15]),
-          "+r"(r[16]), "+r"(r[17]), "+r"(r[18]), "+r"(r[19]), "+r"(r[20]), "+r"(r[21]), "+r"(r[22]), "+r"(r[23]),
-          "+r"(r[24]), "+r"(r[25]), "+r"(r[26]), "+r"(r[27]), "+r"(r[28]), "+r"(r[29]), "+r"(r[30]), "+r"(r[31]),
-          "+r"(r[32]), "+r"(r[33]), "+r"(r[34]), "+r"(r[35]), "+r"(r[36]), "+r"(r[37]), "+r"(r[38]), "+r"(r[39]),
-          "+r"(r[40]), "+r"(r[41]), "+r"(r[42]), "+r"(r[43]), "+r"(r[44]), "+r"(r[45]), "+r"(r[46]), "+r"(r[47]),
-          "+r"(r[48]), "+r"(r[49]), "+r"(r[50]), "+r"(r[51]), "+r"(r[52]), "+r"(r[53]), "+r"(r[54]), "+r"(r[55]),
-          "+r"(r[56]), "+r"(r[57]), "+r"(r[58]), "+r"(r[59]), "+r"(r[60]), "+r"(r[61]), "+r"(r[62]), "+r"(r[63])
-        :
-        : "memory");
-}
-
 __device__ __forceinline__ void tmem_ld(uint32_t taddr, uint32_t (&r)[32]) { tmem_ld32(taddr, r); }
-__device__ __forceinline__ void tmem_ld(uint32_t taddr, uint32_t (&r)[64]) { tmem_ld64(taddr, r); }
 
-// Columns per TMEM load in the top-2 epilogue. 64-column loads (two 64-register
-// buffers) exceed the 168 registers a thread of a 320-thread CTA can hold and
-// spill, so the epilogue loads 32 columns at a time.
+// Columns per TMEM load in the top-2 epilogue. 64-column loads (32x32b.x64,
+// two 64-register buffers) were tried: they exceed the 168 registers a thread
+// of a 320-thread CTA can hold and spill, so the epilogue loads 32 columns at
+// a time.
 constexpr int TOP2_LOAD_COLS = 32;
 
 __device__ __forceinline__ float fmax3(float a, float b, float c) {
@@ -412,7 +374,9 @@ struct RankChunk<COL0, N, N> {
 // gives 0. Horner steps on packed pairs, acc = 2 acc + (bit even, bit
 // odd), exact below 2^16, put the even columns 2j in bits 15 - j of the low
 // half and the odd columns 2j + 1 in bits 31 - j: one saturating FMA per
-// score and one packed FMA per two scores, no ALU instruction.
+// score and one packed FMA per two scores, no ALU instruction. (Tried and
+// slower: two 8-step chains joined by one more step, a magic-number add and a
+// byte permute in place of the two conversions, a branch-free word record.)
 __device__ __forceinline__ uint32_t mask_chunk(const uint32_t (&r)[32], float S, float C, uint64_t two2) {
     uint64_t acc = 0ull;  // {0.f, 0.f}
 #pragma unroll
@@ -690,7 +654,7 @@ __global__ void __launch_bounds__(tc_threads(EP), 1)
             // Drain: the last commit covers every MMA issued before it.
             if (last_s >= 0) mbar_wait(bar_xempty(last_s), last_ph, abort_flag, p.err, 0ull);
         }
-    } else if (TOPK == 1) {
+    } else if constexpr (TOPK == 1) {
         // Mask pass: every part writes its 128 columns' words of each row's
         // mask straight to global memory (no exchange between the parts).
         constexpr int CP = BN / EP;
@@ -747,13 +711,14 @@ __global__ void __launch_bounds__(tc_threads(EP), 1)
                 }
             }
         }
-    } else if (TOPK == 3) {
+    } else if constexpr (TOPK == 3) {
         // Count pass: per row, against the row's threshold, the largest score
         // and the marked centres' number and first mask words; the parts of a
         // row meet once per tile through the rotating slots, as in the top-2
         // pass below.
         constexpr int CP = BN / EP;
-        static_assert(CP == 128, "the count pass runs with two epilogue parts");
+        constexpr int NCK = CP / 32;
+        static_assert(NCK == 2 || NCK == 4, "two or four epilogue parts");
         constexpr int EPI = 4 * EP * 32;  // epilogue threads (the named barriers' count)
         const int ew = warp - 2;
         const int quarter = warp & 3;
@@ -793,17 +758,19 @@ __global__ void __launch_bounds__(tc_threads(EP), 1)
                 tmem_ld32(col + 32, rb);
                 count_chunk(ra, S, C, two2, wbase, st);
                 tmem_wait(rb);
-                tmem_ld32(col + 64, ra);
-                count_chunk(rb, S, C, two2, wbase + 1, st);
-                tmem_wait(ra);
-                tmem_ld32(col + 96, rb);
-                count_chunk(ra, S, C, two2, wbase + 2, st);
-                tmem_wait(rb);
+                if (NCK == 4) {
+                    tmem_ld32(col + 64, ra);
+                    count_chunk(rb, S, C, two2, wbase + 1, st);
+                    tmem_wait(ra);
+                    tmem_ld32(col + 96, rb);
+                    count_chunk(ra, S, C, two2, wbase + 2, st);
+                    tmem_wait(rb);
+                }
                 // every column of this block is in registers: release the buffer
                 tc_fence_before();
                 __syncwarp();
                 if (lane == 0) mbar_arrive(bar_aempty(buf));
-                count_chunk(rb, S, C, two2, wbase + 3, st);
+                count_chunk(rb, S, C, two2, wbase + NCK - 1, st);
             }
             // tile merge: the slot and barrier protocol of the top-2 pass
             const uint32_t sl = tile_it % (uint32_t)p.slots;
@@ -821,7 +788,7 @@ __global__ void __launch_bounds__(tc_threads(EP), 1)
                 if (row < p.n && !dead) p.outc[(int64_t)part * p.out_stride + row] = count_pack(st);
             }
         }
-    } else if (TOPK == 2) {
+    } else if constexpr (TOPK == 2) {
         constexpr int CP = BN / EP;   // columns of one part
         constexpr int NCK = CP / 32;  // its 32-column chunks
         static_assert(NCK == 2 || NCK == 4, "two or four epilogue parts");
@@ -1160,11 +1127,11 @@ void plan_shape(MixedPlan &mp, int64_t n, int d, int k, bool fp8, int topk, int 
     const size_t x_stage = (size_t)n_atoms * X_ATOM_BYTES;
     const size_t per_centre = (size_t)n_atoms * 128 + 32;
     // two X stages when 256 resident centres still fit, else one
-    // Two epilogue parts per lane quarter (8 epilogue warps) and three merge
-    // slots. The kernel also takes four parts (16 epilogue warps, 64 columns
-    // each, two slots when a tile has two blocks or more): measured slower at
-    // n = 4M, d = 128, k = 1024 (1.351 against 1.020 ms; 96 registers a
-    // thread and the four-way merges), so it is not planned.
+    // Two epilogue parts per lane quarter (8 epilogue warps, three merge
+    // slots). The kernel also takes four (16 warps, 64 columns each, two
+    // slots when a tile has two blocks or more), measured slower at n = 4M,
+    // d = 128, k = 1024: top-2 pass 1.351 against 1.020 ms (96 registers a
+    // thread, four-way merges), count pass 0.873 against 0.812 ms.
     mp.ep = 2;
     mp.slots = 3;
     size_t fixed = 0;
@@ -1188,6 +1155,10 @@ void plan_shape(MixedPlan &mp, int64_t n, int d, int k, bool fp8, int topk, int 
         mp.nblocks = mp.kp / BN;
         if ((topk == 2 || topk == 3) && mp.nblocks < 2 && mp.slots < 3) {
             mp.slots = 3;
+            continue;
+        }
+        if (topk == 3 && mp.ep == 4 && mp.nblocks >= 2 && mp.slots == 3) {
+            mp.slots = 2;  // a smaller exchange; the slice stays as planned
             continue;
         }
         break;
@@ -1297,7 +1268,10 @@ void launch_tc_assign(Ctx &ctx, MixedPlan &mp, const void *xb, const void *cb, c
     if (mp.topk == 1) {
         mp.xst == 2 ? go(tc_assign_kernel<1, false, 2, 2>) : go(tc_assign_kernel<1, false, 1, 2>);
     } else if (mp.topk == 3) {
-        mp.xst == 2 ? go(tc_assign_kernel<3, false, 2, 2>) : go(tc_assign_kernel<3, false, 1, 2>);
+        if (mp.ep == 4)
+            mp.xst == 2 ? go(tc_assign_kernel<3, false, 2, 4>) : go(tc_assign_kernel<3, false, 1, 4>);
+        else
+            mp.xst == 2 ? go(tc_assign_kernel<3, false, 2, 2>) : go(tc_assign_kernel<3, false, 1, 2>);
     } else if (mp.topk == 8) {
         if (fp8) {
             set_error("the second pass runs in BF16");
