@@ -430,7 +430,7 @@ fk_status fit_impl(fk_ctx *ctxp, const TX *x_in, int64_t n, int64_t d, const fk_
         // GPU never waits for the host. A converged iteration's successor is
         // discarded (it touched neither the converged centres, nor their
         // input, nor the labels).
-        // BF16 on f32 X: from the fourth iteration on, the main pass may be
+        // Mixed forms on f32 X: from the fourth iteration on, the main pass may be
         // the count pass (thresholds carried from the previous iteration). It
         // runs while the last iteration whose statistics are in (they are
         // read one iteration late) re-checked at most a quarter of the rows;
@@ -440,7 +440,7 @@ fk_status fit_impl(fk_ctx *ctxp, const TX *x_in, int64_t n, int64_t d, const fk_
         // carried bound).
         bool count_ok = false, calm = false;
         if constexpr (std::is_same<TX, float>::value && std::is_same<TC, double>::value)
-            count_ok = p->precision == FK_PRECISION_MIXED_BF16;
+            count_ok = p->precision == FK_PRECISION_MIXED_BF16 || p->precision == FK_PRECISION_MIXED_FP8;
         bool was_count[2] = {false, false};
         int64_t count_from = 3;
         auto finish = [&](int64_t r) {
@@ -1251,6 +1251,7 @@ fk_status fk_ctx_destroy(fk_ctx *ctx) {
     if (c->mixed.ones) cudaFree(c->mixed.ones);
     if (c->mixed2.ones) cudaFree(c->mixed2.ones);
     if (c->mixedm.ones) cudaFree(c->mixedm.ones);
+    if (c->mixedm2.ones) cudaFree(c->mixedm2.ones);
     if (c->mixedc.ones) cudaFree(c->mixedc.ones);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
     delete c;
@@ -1462,7 +1463,8 @@ fk_status fk_debug_tc_probe(fk_ctx *ctx, const float *x_dev, int64_t n, int64_t 
 fk_status fk_debug_tc_plan(int64_t n, int64_t d, int64_t k, int32_t precision, int32_t topk, int32_t num_sms,
                            int64_t *out) {
     if (!out) return FK_ERR_NULL_POINTER;
-    if ((precision != FK_PRECISION_MIXED_BF16 && precision != FK_PRECISION_MIXED_FP8) || (topk != 2 && topk != 8) ||
+    if ((precision != FK_PRECISION_MIXED_BF16 && precision != FK_PRECISION_MIXED_FP8) ||
+        (topk != 1 && topk != 2 && topk != 3 && topk != 8) ||
         n < 1 || d < 1 || k < 1 || d > (1 << 16) || k > (1 << 20)) {
         fk::set_error("fk_debug_tc_plan: unsupported arguments");
         return FK_ERR_INVALID_PARAMETER;

@@ -64,6 +64,7 @@ struct DevScalars {
     unsigned long long error_word;  // nonzero: a bounded device wait gave up
     unsigned long long moved_rows;  // incremental update: rows whose label changed
     unsigned long long incremental; // 1: this iteration's update was incremental
+    unsigned long long mask_count;  // FP8 second pass: rows left to its mask pass
 };
 
 // --------------------------------------------------- mixed precision --
@@ -163,7 +164,8 @@ enum BufSlot {
     BUF_MB_IDX, BUF_MB_XB, BUF_MB_LAB, BUF_MB_OLD, BUF_MB_COUNTS, BUF_MB_PARTV, BUF_MB_PARTI,
     BUF_BK_PERM, BUF_BK_LAB, BUF_BK_CEN, BUF_BK_DIST, BUF_BK_FLAGS, BUF_BK_SCRATCH, BUF_BK_CENTRES, BUF_BK_SEG,
     BUF_BK_FOLD, BUF_BK_LABELS, BUF_BK_XSEG, BUF_BK_CHAINS, BUF_BK_FRES, BUF_BK_FCNT, BUF_FOLD_SUM, BUF_FOLD_CNT,
-    BUF_FOLD_MAP, BUF_MASKS, BUF_THRESH, BUF_FLOORS, BUF_SHIFT, BUF_THMAIN,
+    BUF_FOLD_MAP, BUF_MASKS, BUF_THRESH, BUF_FLOORS, BUF_SHIFT, BUF_THMAIN, BUF_TH2, BUF_CNT2, BUF_LIST3,
+    BUF_SLOT3, BUF_TH3, BUF_XB3,
     BUF_BX, BUF_BFITS, BUF_BSTATE, BUF_BITEMS, BUF_BPART, BUF_BORDER, BUF_BCTR, BUF_BLAB, BUF_BMEM, BUF_BCEN, BUF_BND, BUF_BXOFF,
     BUF_COUNT
 };
@@ -185,9 +187,10 @@ struct Ctx {
     };
     std::vector<PendingTimer> pending;  // phase timers read after the loop
     MixedPlan mixed;   // main pass
-    MixedPlan mixed2;  // second pass (BF16, top-8 records) over the rows an FP8 main pass left open
+    MixedPlan mixed2;  // second pass (BF16 count pass) over the rows an FP8 main pass left open
+    MixedPlan mixedm2; // its mask pass (BF16, the slicing of mixed2)
     MixedPlan mixedm;  // second pass (BF16, candidate masks) over the rows a BF16 main pass left open
-    MixedPlan mixedc;  // BF16 count pass (main pass from the fourth iteration of a fit)
+    MixedPlan mixedc;  // count pass (main pass from the fourth iteration of a fit)
     int batch_variant[20] = {-1, -1, -1, -1, -1, -1, -1, -1, -1, -1,
                              -1, -1, -1, -1, -1, -1, -1, -1, -1, -1};  // autotuned tile shape per (d, k) bucket
     double *contract_acc = nullptr;  // when set: device time of the contraction kernel
@@ -380,9 +383,9 @@ void run_kmeanspp(Ctx &ctx, const T *x, int64_t n, int d, int k, const double *d
 // Mixed-precision assignment (BF16 / FP8 tcgen05 approximate pass, FP32 and
 // FP64 exact re-check) of X stored as f32. Results identical to the FP64
 // direct form.
-// With c_prev and labels_prev (BF16 only: the previous iteration's centres
-// and labels, and this context's row floors from that iteration's pass), the
-// main pass is the count pass.
+// With c_prev and labels_prev (the previous iteration's centres and labels,
+// and this context's row floors from that iteration's pass), the main pass is
+// the count pass.
 template <typename TX>
 void run_assign_mixed(Ctx &ctx, const TX *x, int64_t n, int d, const double *c, int k,
                       int precision, int32_t *labels, double *mind, DevScalars *scalars,

@@ -735,7 +735,7 @@ __device__ __forceinline__ void finalize_rows(int64_t n, Load load, Classify cla
     }
 }
 
-__global__ void __launch_bounds__(FINALIZE_THREADS)
+__global__ void __launch_bounds__(FINALIZE_THREADS, 2)
     finalize_kernel(const SliceTop2 *__restrict__ parts, int nparts, int kp, int64_t n, int k, int d,
                     const float4 *__restrict__ rowinfo, const MixedStats *stats, float acc_rel, float mu_norm,
                     int32_t *__restrict__ labels, int4 *__restrict__ pair_list, int32_t *__restrict__ full_list,
@@ -881,7 +881,7 @@ __device__ __forceinline__ int count_column(int base, int w, int b) {
 // centre is the label, two go to the pair re-score, more or none to the
 // second pass with the row's threshold. Also the row floor for the next
 // iteration (the largest score is a raw accumulator: no key slack).
-__global__ void __launch_bounds__(FINALIZE_THREADS)
+__global__ void __launch_bounds__(FINALIZE_THREADS, 2)  // two blocks an SM: 64 registers a thread
     finalize_count_kernel(const SliceCount *__restrict__ parts, int nparts, int kp, int64_t n, int k, int d,
                           const float4 *__restrict__ rowinfo, const MixedStats *stats, float acc_rel, float mu_norm,
                           const float *__restrict__ thresh, int32_t *__restrict__ labels,
@@ -924,6 +924,7 @@ __global__ void __launch_bounds__(FINALIZE_THREADS)
             }
         }
         const float4 ri = rec.ri;
+        vmax *= stats->tscale / ri.w;  // FP8: back to score units (a power of two; 1 for BF16)
         floor_out[i] = row_floor(vmax, 0.f, ri, stats, acc_rel, mu_norm, d);
         int a = -1, b = -1;
         if (cnt == 1 && w1) {
@@ -1510,12 +1511,12 @@ template <bool FAST>
 __global__ void __launch_bounds__(MASK_WARPS * 32)
     mask_rescore_kernel(const float *__restrict__ x, int d, const float *__restrict__ c32,
                         const float *__restrict__ ec32, int k, const uint32_t *__restrict__ masks, int wpr,
-                        const int32_t *__restrict__ list, DevScalars *sc, int32_t *__restrict__ labels,
-                        Oct *__restrict__ f64_items, int32_t *__restrict__ ex_list) {
+                        const int32_t *__restrict__ list, const unsigned long long *count, DevScalars *sc,
+                        int32_t *__restrict__ labels, Oct *__restrict__ f64_items, int32_t *__restrict__ ex_list) {
     __shared__ int cand_sm[MASK_WARPS][MASK_CANDS];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     int *cand = cand_sm[wid];
-    const unsigned long long cnt = sc->full_count;
+    const unsigned long long cnt = *count;
     const unsigned long long nw = (unsigned long long)gridDim.x * MASK_WARPS;
     unsigned long long s = (unsigned long long)blockIdx.x * MASK_WARPS + wid;
     unsigned long long decided = 0;  // rows this warp decided among its candidates (lane 0)
@@ -1614,6 +1615,70 @@ __global__ void __launch_bounds__(MASK_WARPS * 32)
     }
     // one add per warp: a per-row atomic on the shared counter serialises in L2
     if (lane == 0 && decided) atomicAdd(&sc->quad_count, decided);
+}
+
+// FP8 second pass, slot s = row list[s] of the main pass's full list. The
+// BF16 count pass there runs against th[s] = F + BIG2 - slack - E2: the
+// oracle's winner w has S(w) - BIG >= F (the row floor of the FP8 pass), so
+// its BF16 score is at least F + BIG2 - E2 -- it is always marked, and one
+// mark is the label.
+__global__ void second_thresh_kernel(const int32_t *__restrict__ list, const unsigned long long *count,
+                                     const float *__restrict__ floors, const float4 *__restrict__ rowinfo2,
+                                     const MixedStats *st2, float acc_rel2, float mu_norm, int d,
+                                     float *__restrict__ th) {
+    const unsigned long long cnt = *count;
+    for (unsigned long long s = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; s < cnt;
+         s += (unsigned long long)gridDim.x * blockDim.x) {
+        const float4 ri = rowinfo2[s];
+        float t = __fadd_rd(floors[list[s]], st2->big);
+        t = __fsub_rd(t, row_slack64(ri, st2, mu_norm, d));
+        t = __fsub_rd(t, row_error(ri, st2, acc_rel2));
+        th[s] = t >= st2->ulp * 2097152.f ? t : -INFINITY;
+    }
+}
+
+// After that count pass: one mark is the label; none (a NaN row) the
+// exhaustive re-score; more go to the mask pass with max(th, vmax - thr),
+// vmax the pass's exact best score (the winner scores at least vmax - 2 E2 -
+// FP64 slack there). list3 / slot3 hold the row and its slot here.
+__global__ void second_finalize_kernel(const SliceCount *__restrict__ parts, int nparts, int kp, int64_t cap, int k,
+                                       int d, const int32_t *__restrict__ list, const unsigned long long *count,
+                                       const float4 *__restrict__ rowinfo2, const MixedStats *st2, float acc_rel2,
+                                       float mu_norm, const float *__restrict__ th, int32_t *__restrict__ labels,
+                                       int32_t *__restrict__ ex_list, int32_t *__restrict__ list3,
+                                       int32_t *__restrict__ slot3, float *__restrict__ th3, DevScalars *sc) {
+    const unsigned long long cnt = *count;
+    for (unsigned long long s = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; s < cnt;
+         s += (unsigned long long)gridDim.x * blockDim.x) {
+        float vmax = 0.f;
+        uint32_t marks = 0, w1 = 0;
+        int b1 = 0;
+        for (int p = 0; p < nparts; p++) {
+            const SliceCount o = parts[(int64_t)p * cap + s];
+            vmax = fmaxf(vmax, o.vmax);
+            marks += o.meta & 0xFFFFu;
+            if (!w1 && o.w1) {
+                w1 = o.w1;
+                b1 = p * kp + 32 * (int)((o.meta >> 16) & 0xFFu);
+            }
+        }
+        const int row = list[s];
+        const int a = (marks == 1 && w1) ? count_column(b1, 0, __ffs(w1) - 1) : -1;
+        const bool decided = marks == 1 && a >= 0 && a < k;
+        const bool to_ex = !decided && marks == 0;
+        const bool to_mask = !decided && !to_ex;
+        if (decided) labels[row] = a;
+        const unsigned long long es = warp_reserve(&sc->ex_count, to_ex);
+        const unsigned long long ms = warp_reserve(&sc->mask_count, to_mask);
+        if (to_ex) ex_list[es] = row;
+        if (to_mask) {
+            const float4 ri = rowinfo2[s];
+            const float t2 = __fsub_rd(vmax, row_threshold(ri, st2, acc_rel2, mu_norm, d, st2->big));
+            list3[ms] = row;
+            slot3[ms] = (int32_t)s;
+            th3[ms] = fmaxf(th[s], t2 >= st2->ulp * 2097152.f ? t2 : -INFINITY);
+        }
+    }
 }
 
 // BF16 rows of the main pass's operand copied for the listed rows (slot s =
@@ -1905,11 +1970,11 @@ void second_pass(Ctx &ctx, const float *x, int64_t n, int d, const double *c, in
         if (d % 4 == 0 && d <= 256 && (((uintptr_t)x | (uintptr_t)B.c32) & 15u) == 0) {
             static const int mask_blocks = resident_blocks((const void *)mask_rescore_kernel<true>, MASK_WARPS * 32);
             mask_rescore_kernel<true><<<ctx.num_sms * mask_blocks, MASK_WARPS * 32, 0, s>>>(
-                x, d, B.c32, B.ec32, k, masks, wpr, full, sc, labels, f64_items, ex);
+                x, d, B.c32, B.ec32, k, masks, wpr, full, &sc->full_count, sc, labels, f64_items, ex);
         } else {
             static const int mask_blocks = resident_blocks((const void *)mask_rescore_kernel<false>, MASK_WARPS * 32);
             mask_rescore_kernel<false><<<ctx.num_sms * mask_blocks, MASK_WARPS * 32, 0, s>>>(
-                x, d, B.c32, B.ec32, k, masks, wpr, full, sc, labels, f64_items, ex);
+                x, d, B.c32, B.ec32, k, masks, wpr, full, &sc->full_count, sc, labels, f64_items, ex);
         }
         FK_LAUNCH_CHECK();
         exhaustive_rescore_kernel<<<ctx.num_sms * 2, EX_THREADS, exhaustive_smem_bytes(d, k), s>>>(
@@ -1917,16 +1982,36 @@ void second_pass(Ctx &ctx, const float *x, int64_t n, int d, const double *c, in
         FK_LAUNCH_CHECK();
         return;
     }
+    // FP8 main pass: BF16 operands made from the listed rows' f32 values
+    // (their own statistics, a bound 16x tighter), a BF16 count pass against
+    // thresholds from the rows' floors, then the mask pass over the rows it
+    // leaves open and the re-score of at most 32 candidates
     MixedPlan &m2 = ctx.mixed2;
-    if (m2.n != n || m2.d != d || m2.k != k) plan_tc(ctx, m2, n, d, k, false, 8);
+    if (m2.n != n || m2.d != d || m2.k != k || m2.topk != 3) plan_tc(ctx, m2, n, d, k, false, 3);
+    MixedPlan &mm = ctx.mixedm2;
+    if (mm.n != n || mm.d != d || mm.k != k || mm.kp != m2.kp) plan_tc(ctx, mm, n, d, k, false, 1, m2.kp);
+    if (mm.k_pad != m2.k_pad || mm.d_pad != m2.d_pad) {
+        set_error("second mask pass plan (k_pad %d, d_pad %d) differs from its count pass (%d, %d)", mm.k_pad,
+                  mm.d_pad, m2.k_pad, m2.d_pad);
+        fail(FK_ERR_CUDA);
+    }
     MixedStats *st2 = (MixedStats *)ctx.get(BUF_STATS2, sizeof(MixedStats));
     void *xb2 = ctx.get(BUF_XB2, sizeof(__nv_bfloat16) * (size_t)n * m2.d_pad);
     float4 *ri2 = (float4 *)ctx.get(BUF_ROWINFO2, sizeof(float4) * (size_t)n);
     void *cb2 = ctx.get(BUF_CB2, sizeof(__nv_bfloat16) * (size_t)m2.k_pad * m2.d_pad);
     __nv_bfloat16 *caug2 = (__nv_bfloat16 *)ctx.get(BUF_CAUG2, sizeof(__nv_bfloat16) * (size_t)m2.k_pad * 16 + 8192);
     double *hn2 = (double *)ctx.get(BUF_HALF2, sizeof(double) * (size_t)m2.k_pad);
-    Top8 *top8 = (Top8 *)ctx.get(BUF_TOP8, sizeof(Top8) * (size_t)n * m2.parts);
-    Oct *octs = (Oct *)ctx.get(BUF_OCT, sizeof(Oct) * (size_t)n);
+    float *th2 = (float *)ctx.get(BUF_TH2, sizeof(float) * (size_t)n);
+    SliceCount *cnt2 = (SliceCount *)ctx.get(BUF_CNT2, sizeof(SliceCount) * (size_t)n * m2.parts);
+    int32_t *list3 = (int32_t *)ctx.get(BUF_LIST3, sizeof(int32_t) * (size_t)n);
+    int32_t *slot3 = (int32_t *)ctx.get(BUF_SLOT3, sizeof(int32_t) * (size_t)n);
+    float *th3 = (float *)ctx.get(BUF_TH3, sizeof(float) * (size_t)n);
+    void *xb3 = ctx.get(BUF_XB3, sizeof(__nv_bfloat16) * (size_t)n * m2.d_pad);
+    const int wpr = mm.k_pad / 32;
+    uint32_t *masks = (uint32_t *)ctx.get(BUF_MASKS, sizeof(uint32_t) * (size_t)n * wpr);
+    const float *floors = (const float *)ctx.get(BUF_FLOORS, sizeof(float) * (size_t)n);
+    const float acc_rel2 = (float)((double)((size_t)m2.d_pad + 32) * ACC_REL_PER_K);  // exact: integer * 2^-22
+    const float mun = mu_norm_up(mu_norm);
     FK_CUDA(cudaMemsetAsync(st2, 0, sizeof(MixedStats), s));
     launch_prep_rows<float, false>(ctx, x, n, d, m2.d_pad, B.mu32, xb2, nullptr, ri2, st2, full, &sc->full_count);
     prep_centres_kernel<false><<<(m2.k_pad + 7) / 8, 256, 0, s>>>(c, k, m2.k_pad, d, m2.d_pad, B.mu, cb2, hn2,
@@ -1934,12 +2019,28 @@ void second_pass(Ctx &ctx, const float *x, int64_t n, int d, const double *c, in
     FK_LAUNCH_CHECK();
     prep_aug_kernel<<<(m2.k_pad + 255) / 256, 256, 0, s>>>(hn2, k, m2.k_pad, false, caug2, st2);
     FK_LAUNCH_CHECK();
-    launch_tc_assign(ctx, m2, xb2, cb2, caug2, nullptr, top8, sc, st2, nullptr, &sc->full_count);
-    const float acc_rel2 = (float)((double)((size_t)m2.d_pad + 32) * ACC_REL_PER_K);  // exact: integer * 2^-22
-    finalize8_kernel<<<grid, 256, 0, s>>>(top8, m2.parts, n, k, d, full, ri2, st2, acc_rel2, mu_norm_up(mu_norm),
-                                          labels, octs, ex, sc);
+    second_thresh_kernel<<<grid, 256, 0, s>>>(full, &sc->full_count, floors, ri2, st2, acc_rel2, mun, d, th2);
     FK_LAUNCH_CHECK();
-    oct_rescore_kernel<<<grid, 256, 0, s>>>(x, d, B.c32, B.ec32, octs, sc, labels, f64_items);
+    launch_tc_assign(ctx, m2, xb2, cb2, caug2, nullptr, nullptr, sc, st2, nullptr, &sc->full_count, nullptr, nullptr,
+                     nullptr, th2, cnt2);
+    second_finalize_kernel<<<grid, 256, 0, s>>>(cnt2, m2.parts, m2.kp, n, k, d, full, &sc->full_count, ri2, st2,
+                                                acc_rel2, mun, th2, labels, ex, list3, slot3, th3, sc);
+    FK_LAUNCH_CHECK();
+    const int pieces = m2.d_pad * 2 / 16;
+    gather_xq_rows_kernel<<<ctx.num_sms * 8, 256, 0, s>>>((const uint4 *)xb2, pieces, slot3, &sc->mask_count,
+                                                          (uint4 *)xb3);
+    FK_LAUNCH_CHECK();
+    launch_tc_assign(ctx, mm, xb3, cb2, caug2, nullptr, nullptr, sc, st2, nullptr, &sc->mask_count, nullptr,
+                     nullptr, masks, th3);
+    if (d % 4 == 0 && d <= 256 && (((uintptr_t)x | (uintptr_t)B.c32) & 15u) == 0) {
+        static const int mask_blocks = resident_blocks((const void *)mask_rescore_kernel<true>, MASK_WARPS * 32);
+        mask_rescore_kernel<true><<<ctx.num_sms * mask_blocks, MASK_WARPS * 32, 0, s>>>(
+            x, d, B.c32, B.ec32, k, masks, wpr, list3, &sc->mask_count, sc, labels, f64_items, ex);
+    } else {
+        static const int mask_blocks = resident_blocks((const void *)mask_rescore_kernel<false>, MASK_WARPS * 32);
+        mask_rescore_kernel<false><<<ctx.num_sms * mask_blocks, MASK_WARPS * 32, 0, s>>>(
+            x, d, B.c32, B.ec32, k, masks, wpr, list3, &sc->mask_count, sc, labels, f64_items, ex);
+    }
     FK_LAUNCH_CHECK();
     exhaustive_rescore_kernel<<<ctx.num_sms * 2, EX_THREADS, exhaustive_smem_bytes(d, k), s>>>(
         x, d, c, B.c32t, B.ec32, k, ex, &sc->ex_count, sc, labels);
@@ -1975,17 +2076,18 @@ void run_assign_mixed(Ctx &ctx, const TX *x, int64_t n, int d, const double *c, 
     int4 *pairs = (int4 *)ctx.get(BUF_FLAGS, sizeof(int4) * (size_t)n);
     int32_t *full = (int32_t *)ctx.get(BUF_FULL, sizeof(int32_t) * (size_t)n);
     float *full_thresh = fp8 ? nullptr : (float *)ctx.get(BUF_THRESH, sizeof(float) * (size_t)n);
-    // BF16: every pass leaves each row's floor for a count pass in the next iteration
-    float *floors = fp8 ? nullptr : (float *)ctx.get(BUF_FLOORS, sizeof(float) * (size_t)n);
+    // every pass leaves each row's floor for a count pass in the next iteration
+    float *floors = (float *)ctx.get(BUF_FLOORS, sizeof(float) * (size_t)n);
     const float acc_rel = (float)((double)((size_t)mp.d_pad + 32) * ACC_REL_PER_K);  // exact: integer * 2^-22
     const float mun = mu_norm_up(mp.mu_norm);
     static const int fin_top2 = resident_blocks((const void *)finalize_kernel, FINALIZE_THREADS);
     static const int fin_count = resident_blocks((const void *)finalize_count_kernel, FINALIZE_THREADS);
     const int64_t fin_chunks = (n + FINALIZE_THREADS - 1) / FINALIZE_THREADS;
-    if (!fp8 && c_prev && labels_prev) {
+    if (c_prev && labels_prev) {
         // count pass, against thresholds carried from the previous iteration
         MixedPlan &mc = ctx.mixedc;
-        if (mc.n != n || mc.d != d || mc.k != k || mc.kp != mp.kp) plan_tc(ctx, mc, n, d, k, false, 3, mp.kp);
+        if (mc.n != n || mc.d != d || mc.k != k || mc.kp != mp.kp || mc.fp8 != fp8)
+            plan_tc(ctx, mc, n, d, k, fp8, 3, mp.kp);
         if (mc.k_pad != mp.k_pad || mc.d_pad != mp.d_pad) {
             set_error("count pass plan (k_pad %d, d_pad %d) differs from the main pass (%d, %d)", mc.k_pad, mc.d_pad,
                       mp.k_pad, mp.d_pad);
@@ -2002,8 +2104,8 @@ void run_assign_mixed(Ctx &ctx, const TX *x, int64_t n, int d, const double *c, 
         {
             Timer t(ctx.contract_acc != nullptr, ctx, ctx.contract_acc);
             Timer tc(ctx.count_acc != nullptr, ctx, ctx.count_acc);
-            launch_tc_assign(ctx, mc, B.xq, B.cq, B.caug, nullptr, nullptr, sc, B.stats, nullptr, nullptr, nullptr,
-                             nullptr, nullptr, th, cnt);
+            launch_tc_assign(ctx, mc, B.xq, B.cq, B.caug, nullptr, nullptr, sc, B.stats, nullptr, nullptr, B.xaug,
+                             rowscale, nullptr, th, cnt);
         }
         finalize_count_kernel<<<(unsigned)std::min<int64_t>(fin_chunks, (int64_t)ctx.num_sms * fin_count),
                                 FINALIZE_THREADS, 0, s>>>(cnt, mc.parts, mc.kp, n, k, d, B.rowinfo,

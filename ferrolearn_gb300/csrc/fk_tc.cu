@@ -731,17 +731,25 @@ __global__ void __launch_bounds__(tc_threads(EP), 1)
         asm("mov.b64 %0, {%1, %1};" : "=l"(two2) : "f"(2.f));
         uint32_t item = 0, tile_it = 0;
         bool dead = false;
-        // the row's threshold one tile ahead, so that no tile starts on a
-        // global load
-        float th_next = q * BM + row_local < p.n ? p.thresh[q * BM + row_local] : INFINITY;
+        // the row's threshold (and FP8 scale) one tile ahead, so that no tile
+        // starts on a global load
+        float th_next = INFINITY, rs_next = 1.f;
+        if (q * BM + row_local < p.n) {
+            th_next = p.thresh[q * BM + row_local];
+            if (FP8) rs_next = p.rowscale[q * BM + row_local];
+        }
         for (int64_t t = q; t < p.tiles; t += tstride, tile_it++) {
             const int64_t row = t * BM + row_local;
-            const float th = th_next;
+            const float th = th_next, rs = rs_next;
             {
                 const int64_t nrow = (t + tstride) * BM + row_local;
                 th_next = nrow < p.n ? p.thresh[nrow] : INFINITY;
+                if (FP8) rs_next = nrow < p.n ? p.rowscale[nrow] : 1.f;
             }
             const float C = -(th * S);  // exact: a float times a power of two
+            // FP8 accumulators are the row's scores times rs (a power of two):
+            // T_acc (S / rs) - th S is exactly (T - th) S
+            const float Sr = FP8 ? S / rs : S;
             CountState st{0.f, 0u, 0u, 0u, 0, 0};
             for (int b = 0; b < p.nblocks; b++, item++) {
                 const int buf = (int)(item & 1u);
@@ -756,21 +764,21 @@ __global__ void __launch_bounds__(tc_threads(EP), 1)
                 tmem_ld32(col, ra);
                 tmem_wait(ra);
                 tmem_ld32(col + 32, rb);
-                count_chunk(ra, S, C, two2, wbase, st);
+                count_chunk(ra, Sr, C, two2, wbase, st);
                 tmem_wait(rb);
                 if (NCK == 4) {
                     tmem_ld32(col + 64, ra);
-                    count_chunk(rb, S, C, two2, wbase + 1, st);
+                    count_chunk(rb, Sr, C, two2, wbase + 1, st);
                     tmem_wait(ra);
                     tmem_ld32(col + 96, rb);
-                    count_chunk(ra, S, C, two2, wbase + 2, st);
+                    count_chunk(ra, Sr, C, two2, wbase + 2, st);
                     tmem_wait(rb);
                 }
                 // every column of this block is in registers: release the buffer
                 tc_fence_before();
                 __syncwarp();
                 if (lane == 0) mbar_arrive(bar_aempty(buf));
-                count_chunk(rb, S, C, two2, wbase + NCK - 1, st);
+                count_chunk(rb, Sr, C, two2, wbase + NCK - 1, st);
             }
             // tile merge: the slot and barrier protocol of the top-2 pass
             const uint32_t sl = tile_it % (uint32_t)p.slots;
@@ -1191,7 +1199,7 @@ void launch_tc_assign(Ctx &ctx, MixedPlan &mp, const void *xb, const void *cb, c
     const bool fp8 = mp.fp8;
     if ((mp.topk == 2) != (out != nullptr) || (mp.topk == 8) != (out8 != nullptr) ||
         (mp.topk == 1) != (masks != nullptr) || (mp.topk == 3) != (outc != nullptr) ||
-        ((mp.topk == 1 || mp.topk == 3) != (thresh != nullptr)) || ((mp.topk == 1 || mp.topk == 3) && fp8)) {
+        ((mp.topk == 1 || mp.topk == 3) != (thresh != nullptr)) || (mp.topk == 1 && fp8)) {
         set_error("tensor-core launch: records do not match the plan");
         fail(FK_ERR_INVALID_PARAMETER);
     }
@@ -1268,7 +1276,9 @@ void launch_tc_assign(Ctx &ctx, MixedPlan &mp, const void *xb, const void *cb, c
     if (mp.topk == 1) {
         mp.xst == 2 ? go(tc_assign_kernel<1, false, 2, 2>) : go(tc_assign_kernel<1, false, 1, 2>);
     } else if (mp.topk == 3) {
-        if (mp.ep == 4)
+        if (fp8)
+            mp.xst == 2 ? go(tc_assign_kernel<3, true, 2, 2>) : go(tc_assign_kernel<3, true, 1, 2>);
+        else if (mp.ep == 4)
             mp.xst == 2 ? go(tc_assign_kernel<3, false, 2, 4>) : go(tc_assign_kernel<3, false, 1, 4>);
         else
             mp.xst == 2 ? go(tc_assign_kernel<3, false, 2, 2>) : go(tc_assign_kernel<3, false, 1, 2>);

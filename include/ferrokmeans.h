@@ -402,7 +402,8 @@ fk_status fk_debug_tc_probe(fk_ctx *ctx, const float *x_dev, int64_t n, int64_t 
 
 /* Diagnostics (no reference counterpart, no GPU needed): the launch plan of
  * one tensor-core pass for a shape -- precision FK_PRECISION_MIXED_BF16 or
- * _FP8, topk 2 (main pass) or 8 (second pass), on num_sms SMs. out[0..9] =
+ * _FP8, topk 2 (top-2 main pass), 3 (count pass), 1 (BF16 mask pass) or 8
+ * (BF16 top-8 pass), on num_sms SMs. out[0..9] =
  * {d_pad, kp (resident centres per slice), parts (slices), k_pad, nblocks
  * (256-centre accumulator blocks per slice), xst (X ring depth), dynamic
  * shared memory bytes, grid, CTAs per slice, 128-row tiles}. */

@@ -322,9 +322,10 @@ def _plan(n, d, k, precision, topk, sms=152):
 def test_fp8_bisector_at_full_k_and_d_matches_fp64_oracle():
     # the large-k FP8 workload at its own k = 4096 and d = 256 (200,000 rows,
     # 10% on bisectors): the E4M3 main pass runs 8 slices of 512 resident
-    # centres and the BF16 top-8 second pass 16 slices of 256, the plans the
-    # full-size workload runs; labels of every iteration, centres, n_iter and
-    # predict on fresh rows must be the FP64 oracle's
+    # centres and the BF16 second pass (count pass, then mask pass) 16 slices
+    # of 256, the plans the full-size workload runs; labels of every
+    # iteration, centres, n_iter and predict on fresh rows must be the FP64
+    # oracle's
     w = W.bisector_4096x256(scale=0.025, predict_scale=0.01)
     x32, k = w["x"], w["k"]
     n = x32.shape[0]
@@ -332,7 +333,7 @@ def test_fp8_bisector_at_full_k_and_d_matches_fp64_oracle():
     torch = pytest.importorskip("torch")
     sms = torch.cuda.get_device_properties(0).multi_processor_count
     assert _plan(n, 256, k, F.MIXED_FP8, 2, sms)["parts"] == 8
-    assert _plan(n // 4, 256, k, F.MIXED_BF16, 8, sms)["parts"] == 16
+    assert _plan(n // 4, 256, k, F.MIXED_BF16, 3, sms)["parts"] == 16
     x64 = x32.astype(np.float64)
     c = w["init"].copy()
     second = 0
@@ -396,6 +397,26 @@ def test_bf16_count_pass_fit_matches_fp64_oracle_and_single_steps():
     c = w["init"]
     for _ in range(iters):
         gl, c, gi, gs, rep = F.lloyd_step(x32, c, dtype="f32x64", precision="bf16")
+    assert np.array_equal(g.cluster_centers(), c)
+
+
+def test_fp8_count_pass_fit_matches_fp64_oracle_and_single_steps():
+    # the FP8 form's count pass: E4M3 accumulators are the row's scores times
+    # a power of two, so the marks and the carried floors scale exactly; the
+    # fit must equal the FP64 oracle and the single (top-2) steps
+    w = W.anisotropic_1024x128(scale=0.01)  # 40,000 rows, d = 128, k = 1024
+    x32, k = w["x"], w["k"]
+    iters = 10
+    g = F.KMeans(k, dtype="f32x64").with_precision("fp8").with_max_iter(iters).with_tol(0.0).with_n_init(1) \
+        .with_init_centers(w["init"]).fit(x32)
+    o = O.fit(x32.astype(np.float64), k, max_iter=iters, tol=0.0, n_init=1, init=w["init"][None])
+    assert np.array_equal(g.labels(), o["labels"])
+    assert _close(g.cluster_centers(), o["centers"])
+    assert g.n_iter() == o["n_iter"] == iters
+    assert g.report["count_iterations"] >= 2
+    c = w["init"]
+    for _ in range(iters):
+        gl, c, gi, gs, rep = F.lloyd_step(x32, c, dtype="f32x64", precision="fp8")
     assert np.array_equal(g.cluster_centers(), c)
 
 
