@@ -1464,7 +1464,7 @@ fk_status fk_debug_tc_plan(int64_t n, int64_t d, int64_t k, int32_t precision, i
                            int64_t *out) {
     if (!out) return FK_ERR_NULL_POINTER;
     if ((precision != FK_PRECISION_MIXED_BF16 && precision != FK_PRECISION_MIXED_FP8) ||
-        (topk != 1 && topk != 2 && topk != 3 && topk != 8) ||
+        (topk != 1 && topk != 2 && topk != 3) ||
         n < 1 || d < 1 || k < 1 || d > (1 << 16) || k > (1 << 20)) {
         fk::set_error("fk_debug_tc_plan: unsupported arguments");
         return FK_ERR_INVALID_PARAMETER;

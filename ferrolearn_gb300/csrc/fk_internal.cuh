@@ -58,7 +58,7 @@ struct DevScalars {
     unsigned long long near_tie_rows;
     unsigned long long flag_count;  // number of rows queued for re-check
     unsigned long long full_count;  // number of rows queued for a full re-scan
-    unsigned long long quad_count;  // second pass: rows decided among 2 to 8 (top-8) or 32 (masks) candidates
+    unsigned long long quad_count;  // second pass: rows decided among at most 32 candidates
     unsigned long long ex_count;    // second pass: rows re-scored against every centre
     unsigned long long f64_count;   // rows whose remaining candidates are scored in FP64
     unsigned long long error_word;  // nonzero: a bounded device wait gave up
@@ -114,13 +114,6 @@ struct alignas(16) SliceCount {
     uint32_t w1, w2;
 };
 
-// Best eight scores of one row over one slice (second pass), and u9, a bound
-// of the rest.
-struct alignas(16) Top8 {
-    float v[8];
-    int i[8];
-    float u9, pad0, pad1, pad2;
-};
 
 // Launch plan of the tensor-core assignment (fk_tc.cu).
 struct MixedPlan {
@@ -134,8 +127,7 @@ struct MixedPlan {
     int64_t tiles = 0;    // ceil(n / 128)
     int ctas_per_part = 0;
     int grid = 0;
-    int topk = 2;         // epilogue records: 2 (Top2, main pass), 3 (SliceCount, count pass), 8 (Top8, second
-                          // pass) or 1 (candidate masks)
+    int topk = 2;         // epilogue records: 2 (top-2 main pass), 3 (count pass) or 1 (candidate masks)
     int xst = 2;          // depth of the X tile ring (1 when two stages leave no room for 256 centres)
     int ep = 2;           // epilogue parts per TMEM lane quarter (4 x ep epilogue warps)
     int slots = 3;        // rotating tile-merge slots of the top-2 pass
@@ -158,7 +150,7 @@ enum BufSlot {
     BUF_MEMBERS, BUF_SEGHIST, BUF_SCAN_TMP, BUF_COUNTS, BUF_PARTIAL, BUF_SCALARS,
     BUF_OUT, BUF_OUT2, BUF_KPP0, BUF_KPP1, BUF_KPP2, BUF_KPP3, BUF_DRAWS,
     BUF_XB, BUF_XNORM, BUF_CB, BUF_CAUX, BUF_TOP2, BUF_FLAGS, BUF_FULL, BUF_CF32, BUF_CF32C, BUF_FIXPART,
-    BUF_XB2, BUF_TOP8, BUF_OCT, BUF_EX, BUF_XAUG, BUF_ROWSCALE, BUF_ROWINFO2, BUF_STATS2, BUF_CB2, BUF_CAUG2,
+    BUF_XB2, BUF_EX, BUF_XAUG, BUF_ROWSCALE, BUF_ROWINFO2, BUF_STATS2, BUF_CB2, BUF_CAUG2,
     BUF_HALF2, BUF_INERTIA2, BUF_C2, BUF_XSTATE, BUF_XCOUNTS, BUF_MOVED, BUF_MOVED_ENT, BUF_MOVED_HIST, BUF_MOVED_TMP,
     BUF_CSPLIT, BUF_RINERT, BUF_F64ITEMS, BUF_INIT,
     BUF_MB_IDX, BUF_MB_XB, BUF_MB_LAB, BUF_MB_OLD, BUF_MB_COUNTS, BUF_MB_PARTV, BUF_MB_PARTI,
@@ -395,7 +387,8 @@ void run_assign_mixed(Ctx &ctx, const TX *x, int64_t n, int d, const double *c, 
 void launch_mixed_inertia(Ctx &ctx, const double *part, int64_t m, DevScalars *scalars);
 
 // Tensor-core assignment (fk_tc.cu): plan, then one persistent launch that
-// writes one record per (slice, row): Top2 (topk 2) or Top8 (topk 8).
+// writes per (slice, row) a SliceTop2 (topk 2) or SliceCount (topk 3)
+// record, or per row its candidate mask words (topk 1).
 void plan_tc(Ctx &ctx, MixedPlan &mp, int64_t n, int d, int k, bool fp8, int topk, int kp_fixed = 0);
 // Dense BF16 (out[0]) and E4M3 (out[1]) flop/s of a tensor-core MMA loop (fk_tc.cu).
 void measure_tc_peaks(Ctx &ctx, double *out);
@@ -408,7 +401,7 @@ void measure_tc_peaks(Ctx &ctx, double *out);
 // device-side constants.
 void plan_shape(MixedPlan &mp, int64_t n, int d, int k, bool fp8, int topk, int sms, int kp_fixed = 0);
 void launch_tc_assign(Ctx &ctx, MixedPlan &mp, const void *xb, const void *cb, const void *caug, SliceTop2 *out,
-                      Top8 *out8, DevScalars *sc, const MixedStats *stats, float *dump = nullptr,
+                      DevScalars *sc, const MixedStats *stats, float *dump = nullptr,
                       const unsigned long long *n_dev = nullptr, const void *xaug = nullptr,
                       const float *rowscale = nullptr, uint32_t *masks = nullptr, const float *thresh = nullptr,
                       SliceCount *outc = nullptr);

@@ -369,16 +369,33 @@ template <typename T> struct TrialTile;
 template <> struct TrialTile<float> { static constexpr int DJ = 8; };
 template <> struct TrialTile<double> { static constexpr int DJ = 4; };
 
+// Two stages of the staged tile (rows and trial candidates), filled with
+// asynchronous copies one feature round ahead.
 template <typename T, int TT>
 constexpr size_t trial_smem() {
-    return sizeof(T) * ((size_t)TrialTile<T>::DJ * (KPP_CH + KPP_PAD) + (size_t)TrialTile<T>::DJ * TT);
+    return 2 * sizeof(T) * ((size_t)TrialTile<T>::DJ * (KPP_CH + KPP_PAD) + (size_t)TrialTile<T>::DJ * TT);
 }
+
+// One element from global to shared memory, asynchronously (cp.async of 4
+// or 8 bytes); ok == false writes zero (src-size 0: nothing is read).
+template <typename T>
+__device__ __forceinline__ void cp_async_elem(T *dst, const T *src, bool ok) {
+    const uint32_t d = (uint32_t)__cvta_generic_to_shared(dst);
+    const int n = ok ? (int)sizeof(T) : 0;
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2, %3;" ::"r"(d), "l"(src), "n"((int)sizeof(T)), "r"(n)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 
 // One CTA per chunk of KPP_CH rows, 4 rows per thread, all TT trial slots per
 // thread (ntr <= TT of them live): every trial's min(D^2, d(x, candidate))
 // (INIT: d(x, first row), the first D^2 array; kmeans.rs:188-195, 225-233)
 // with the direct form folded over the features in order, and the chunk's
-// sums (only an estimate for the fold's binade windows).
+// sums (only an estimate for the fold's binade windows). The features come
+// in rounds of DJ, staged in shared memory by asynchronous copies one round
+// ahead of the arithmetic (two stages).
 template <typename T, int TT, bool INIT>
 __global__ void __launch_bounds__(KPP_THREADS)
     kpp_trials_kernel(const T *__restrict__ x, long long n, int d, T *__restrict__ chains, int tstride,
@@ -387,8 +404,9 @@ __global__ void __launch_bounds__(KPP_THREADS)
     constexpr int DJ = TrialTile<T>::DJ;
     constexpr int XS = KPP_CH + KPP_PAD;  // row length of the staged tile
     extern __shared__ __align__(16) unsigned char kpp_smem[];
-    T *xs = reinterpret_cast<T *>(kpp_smem);  // [DJ][XS]: feature-major, rows contiguous
-    T *cs = xs + DJ * XS;                     // [DJ][TT]
+    constexpr int STAGE = DJ * XS + DJ * TT;  // elements of one stage
+    // stage q: xs = [DJ][XS] (feature-major, rows contiguous), then cs = [DJ][TT]
+    T *const stages = reinterpret_cast<T *>(kpp_smem);
     __shared__ long long cand[TT];
     __shared__ double red[TT][KPP_THREADS / 32];
     const int tid = threadIdx.x;
@@ -402,19 +420,36 @@ __global__ void __launch_bounds__(KPP_THREADS)
     for (int a = 0; a < 4; a++)
 #pragma unroll
         for (int b = 0; b < TT; b++) acc[a][b] = T(0);
-    for (int j0 = 0; j0 < d; j0 += DJ) {
+    __syncthreads();  // cand
+    auto stage_round = [&](int j0, int q) {
+        T *xs = stages + q * STAGE;
+        T *cs = xs + DJ * XS;
         const int jn = min(DJ, d - j0);
-        __syncthreads();
         for (int e = tid; e < KPP_CH * DJ; e += KPP_THREADS) {
             const int r = e / DJ, jj = e - r * DJ;
             const long long gr = base + r;
-            xs[jj * XS + r] = (gr < n && jj < jn) ? x[gr * d + j0 + jj] : T(0);
+            const bool ok = gr < n && jj < jn;
+            cp_async_elem(xs + jj * XS + r, ok ? x + gr * d + j0 + jj : x, ok);
         }
         for (int e = tid; e < TT * DJ; e += KPP_THREADS) {
             const int t = e / DJ, jj = e - t * DJ;
-            cs[jj * TT + t] = (t < ntr && jj < jn) ? x[cand[t] * d + j0 + jj] : T(0);
+            const bool ok = t < ntr && jj < jn;
+            cp_async_elem(cs + jj * TT + t, ok ? x + cand[t] * d + j0 + jj : x, ok);
         }
-        __syncthreads();
+        cp_async_commit();
+    };
+    stage_round(0, 0);
+    for (int j0 = 0, q = 0; j0 < d; j0 += DJ, q ^= 1) {
+        const int jn = min(DJ, d - j0);
+        if (j0 + DJ < d) {
+            stage_round(j0 + DJ, q ^ 1);  // the next round's copies fly during this round
+            cp_async_wait<1>();
+        } else {
+            cp_async_wait<0>();
+        }
+        __syncthreads();  // every thread's copies of this round have landed
+        const T *xs = stages + q * STAGE;
+        const T *cs = xs + DJ * XS;
         for (int jj = 0; jj < jn; jj++) {
             T xv[4], cvv[TT];
 #pragma unroll
@@ -429,6 +464,7 @@ __global__ void __launch_bounds__(KPP_THREADS)
                     acc[a][b] = kpp_add(acc[a][b], kpp_mul(df, df));
                 }
         }
+        __syncthreads();  // this stage is refilled by the next round's staging
     }
     double psum[TT];
 #pragma unroll
@@ -707,7 +743,9 @@ template <typename T, int TT, bool INIT>
 void launch_trials(const T *x, long long n, int d, T *chains, int ts, const KppState *st, int ntr, double *csum,
                    long long nch, cudaStream_t s) {
     constexpr size_t smem = trial_smem<T, TT>();
-    static_assert(smem <= 48 * 1024, "the trial tile fits the default shared-memory limit");
+    static_assert(smem <= 227 * 1024, "two stages of the trial tile fit in shared memory");
+    FK_CUDA(cudaFuncSetAttribute((const void *)kpp_trials_kernel<T, TT, INIT>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     kpp_trials_kernel<T, TT, INIT><<<(unsigned)nch, KPP_THREADS, smem, s>>>(x, n, d, chains, ts, st, ntr, csum, nch);
     FK_LAUNCH_CHECK();
 }

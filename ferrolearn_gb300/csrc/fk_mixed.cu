@@ -27,9 +27,10 @@
 // centres are re-scored, more or none send the row to the exhaustive
 // re-score. After an FP8 main pass it runs in BF16 (its own operands, made
 // from the row's f32 values, and its own bound -- 16x tighter than the FP8
-// one) and keeps the best eight scores, and only the centres inside that
-// pass's bound are re-scored (rows with more than eight such centres, or a
-// non-finite score, are re-scored against every centre, one CTA per row).
+// one): a count pass against the row's floor, then the mask pass with the
+// threshold its exact best score gives (rows with more than 32 such centres,
+// or a non-finite score, are re-scored against every centre, one CTA per
+// row).
 // Every re-score ends
 // in the direct-form sum (x_j - c_j)^2 in FP64 with no FMA and the lowest
 // index on ties, i.e. exactly kmeans.rs:159-163 / 295-309, so the labels
@@ -1286,149 +1287,9 @@ size_t exhaustive_smem_bytes(int d, int k) {
 
 // ------------------------------------------------------- second pass --
 // Rows whose third-best score was inside the bound are scored again by the
-// tensor cores in BF16 (after an FP8 main pass too: a bound 16x tighter),
-// from their f32 values, with a top-8 epilogue; then only the (at most
-// eight) centres inside the second pass's bound are re-scored. Slot s of the
-// second pass holds row list[s]; its row data (rowinfo2) and statistics
-// (stats2) are its own.
-
-__device__ __forceinline__ uint32_t ins8u(uint32_t (&R)[8], int (&I)[8], uint32_t w, int j) {
-#pragma unroll
-    for (int p = 0; p < 8; p++) {
-        if (w > R[p]) {
-            const uint32_t tw = R[p];
-            const int tj = I[p];
-            R[p] = w;
-            I[p] = j;
-            w = tw;
-            j = tj;
-        }
-    }
-    return w;
-}
-
-__global__ void finalize8_kernel(const Top8 *__restrict__ parts, int nparts, int64_t cap, int k, int d,
-                                 const int32_t *__restrict__ list, const float4 *__restrict__ rowinfo2,
-                                 const MixedStats *stats2, float acc_rel, float mu_norm,
-                                 int32_t *__restrict__ labels, Oct *__restrict__ octs, int32_t *__restrict__ ex_list,
-                                 DevScalars *sc) {
-    const unsigned long long cnt = sc->full_count;
-    for (unsigned long long s = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; s < cnt;
-         s += (unsigned long long)gridDim.x * blockDim.x) {
-        uint32_t R[8], U;
-        int I[8];
-        {
-            const Top8 t = parts[s];
-#pragma unroll
-            for (int j = 0; j < 8; j++) {
-                R[j] = __float_as_uint(t.v[j]);
-                I[j] = t.i[j];
-            }
-            U = __float_as_uint(t.u9);
-        }
-        for (int p = 1; p < nparts; p++) {
-            const Top8 o = parts[(int64_t)p * cap + s];
-            U = max(U, __float_as_uint(o.u9));
-#pragma unroll
-            for (int j = 0; j < 8; j++) U = max(U, ins8u(R, I, __float_as_uint(o.v[j]), o.i[j]));
-        }
-        const int32_t row = list[s];
-        const float4 ri = rowinfo2[s];
-        const float v1 = __uint_as_float(R[0]);
-        const float thr = row_threshold(ri, stats2, acc_rel, mu_norm, d, v1);
-        const bool rest_out = __fsub_rd(v1, __uint_as_float(U)) > thr;
-        int m = 0;
-        bool valid = true;
-#pragma unroll
-        for (int j = 0; j < 8; j++) {
-            if (!(__fsub_rd(v1, __uint_as_float(R[j])) > thr)) {
-                m++;
-                if (I[j] < 0 || I[j] >= k) valid = false;
-            }
-        }
-        const bool to_ex = !rest_out || !valid || m == 0;
-        const bool to_oct = !to_ex && m > 1;
-        const unsigned long long es = warp_reserve(&sc->ex_count, to_ex);
-        const unsigned long long os = warp_reserve(&sc->quad_count, to_oct);
-        if (to_ex) {
-            ex_list[es] = row;
-        } else if (m == 1) {
-            labels[row] = I[0];
-        } else {
-            const unsigned long long slot = os;
-            Oct o;
-            o.row = row;
-            o.m = m;
-#pragma unroll
-            for (int j = 0; j < 8; j++) o.ids[j] = I[j];
-            o.pad0 = o.pad1 = 0;
-            octs[slot] = o;
-        }
-    }
-}
-
-// One warp per row with at most eight candidates: FP32 distances (lanes over
-// the features) with rigorous bounds; the candidates whose lower bound
-// reaches the smallest upper bound are scored exactly in FP64 (one lane
-// each, direct form), lowest index on ties.
-// Decides one row with at most eight candidates from acc, this lane's part of
-// the FP32 distance to candidate lane >> 2 (four lanes per candidate).
-__device__ __forceinline__ void oct_decide(const Oct &qd, float acc, int d, const float *__restrict__ ec32,
-                                           DevScalars *sc, int32_t *__restrict__ labels, Oct *__restrict__ f64_items) {
-    const int lane = threadIdx.x & 31;
-    acc += __shfl_xor_sync(0xffffffffu, acc, 2);
-    acc += __shfl_xor_sync(0xffffffffu, acc, 1);
-    // lane j < m holds candidate j: its distance, bound and interval
-    const bool cand = lane < qd.m;
-    int my_id = INT32_MAX;
-#pragma unroll
-    for (int j = 0; j < 8; j++)  // qd.ids[lane] without indexing a register array
-        if (cand && j == lane) my_id = qd.ids[j];
-    const float my_dist = __shfl_sync(0xffffffffu, acc, (4 * lane) & 31);
-    const float my_err = cand ? bound32(my_dist, ec32[my_id], d) : 0.f;
-    float ub = cand ? __fadd_ru(my_dist, my_err) : INFINITY;
-#pragma unroll
-    for (int off = 4; off >= 1; off >>= 1) ub = fminf(ub, __shfl_xor_sync(0xffffffffu, ub, off));
-    ub = __shfl_sync(0xffffffffu, ub, 0);  // the minimum over lanes 0-7 (NaN values never lower it)
-    const unsigned surv = __ballot_sync(0xffffffffu, cand && !(__fsub_rd(my_dist, my_err) > ub));
-    const int nsurv = __popc(surv);
-    if (nsurv == 1) {
-        const int only = __shfl_sync(0xffffffffu, my_id, __ffs(surv) - 1);
-        if (lane == 0) labels[qd.row] = only;
-        return;
-    }
-    // the survivors (all candidates if no FP32 value was finite) go to FP64
-    const unsigned take = nsurv == 0 ? __ballot_sync(0xffffffffu, cand) : surv;
-    int ids[8];
-    int m = 0;
-#pragma unroll
-    for (int j = 0; j < 8; j++) {
-        const int idj = __shfl_sync(0xffffffffu, my_id, j);
-        ids[j] = 0;
-        if ((take >> j) & 1u) ids[m++] = idj;  // any order: ties go to the lowest index
-    }
-    queue_f64(f64_items, sc, qd.row, m, ids);
-}
-
-__global__ void oct_rescore_kernel(const float *__restrict__ x, int d, const float *__restrict__ c32,
-                                   const float *__restrict__ ec32, const Oct *__restrict__ octs, DevScalars *sc,
-                                   int32_t *__restrict__ labels, Oct *__restrict__ f64_items) {
-    const unsigned long long cnt = sc->quad_count;
-    const int lane = threadIdx.x & 31;
-    const unsigned long long wid = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const unsigned long long nw = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
-    for (unsigned long long s = wid; s < cnt; s += nw) {
-        const Oct qd = octs[s];
-        const int cj = lane >> 2;  // candidate cj scored by four lanes at once
-        int cid = 0;
-#pragma unroll
-        for (int j = 0; j < 8; j++)
-            if (j == cj) cid = qd.ids[j];
-        float acc = 0.f;
-        if (cj < qd.m) acc = sq_partial(x + (int64_t)qd.row * d, c32 + (int64_t)cid * d, d, lane & 3, 4);
-        oct_decide(qd, acc, d, ec32, sc, labels, f64_items);
-    }
-}
+// tensor cores in BF16 with candidate-marking epilogues (second_pass below):
+// slot s of a second-pass list holds row list[s]; after an FP8 main pass its
+// row data (rowinfo2) and statistics (stats2) are its own.
 
 // Mask pass rows (BF16 main pass): slot s of the list holds row list[s] and
 // its candidate mask, wpr words with bit per centre (mask_chunk's layout:
@@ -1938,8 +1799,8 @@ float mu_norm_up(double v) {
 // copy, a tensor pass that marks every centre scoring at least the row's
 // threshold, then the re-score of at most 32 candidates, or of every centre.
 // After an FP8 main pass: BF16 operands made from the rows' f32 values, a
-// top-8 tensor pass, then the re-score of at most eight candidates, or of
-// every centre.
+// BF16 count pass against thresholds from the rows' floors, the mask pass
+// over the rows it leaves open, then the same re-score.
 void second_pass(Ctx &ctx, const float *x, int64_t n, int d, const double *c, int k, const MixedBufs &B,
                  double mu_norm, const int32_t *full, const float *full_thresh, int32_t *labels, DevScalars *sc,
                  Oct *f64_items) {
@@ -1964,7 +1825,7 @@ void second_pass(Ctx &ctx, const float *x, int64_t n, int d, const double *c, in
         gather_xq_rows_kernel<<<ctx.num_sms * 8, 256, 0, s>>>((const uint4 *)B.xq, pieces, full, &sc->full_count,
                                                               (uint4 *)xb2);
         FK_LAUNCH_CHECK();
-        launch_tc_assign(ctx, mm, xb2, B.cq, B.caug, nullptr, nullptr, sc, B.stats, nullptr, &sc->full_count,
+        launch_tc_assign(ctx, mm, xb2, B.cq, B.caug, nullptr, sc, B.stats, nullptr, &sc->full_count,
                          nullptr, nullptr, masks, full_thresh);
         // latency-bound (a few dependent loads per row): as many warps as the SMs hold
         if (d % 4 == 0 && d <= 256 && (((uintptr_t)x | (uintptr_t)B.c32) & 15u) == 0) {
@@ -2021,7 +1882,7 @@ void second_pass(Ctx &ctx, const float *x, int64_t n, int d, const double *c, in
     FK_LAUNCH_CHECK();
     second_thresh_kernel<<<grid, 256, 0, s>>>(full, &sc->full_count, floors, ri2, st2, acc_rel2, mun, d, th2);
     FK_LAUNCH_CHECK();
-    launch_tc_assign(ctx, m2, xb2, cb2, caug2, nullptr, nullptr, sc, st2, nullptr, &sc->full_count, nullptr, nullptr,
+    launch_tc_assign(ctx, m2, xb2, cb2, caug2, nullptr, sc, st2, nullptr, &sc->full_count, nullptr, nullptr,
                      nullptr, th2, cnt2);
     second_finalize_kernel<<<grid, 256, 0, s>>>(cnt2, m2.parts, m2.kp, n, k, d, full, &sc->full_count, ri2, st2,
                                                 acc_rel2, mun, th2, labels, ex, list3, slot3, th3, sc);
@@ -2030,7 +1891,7 @@ void second_pass(Ctx &ctx, const float *x, int64_t n, int d, const double *c, in
     gather_xq_rows_kernel<<<ctx.num_sms * 8, 256, 0, s>>>((const uint4 *)xb2, pieces, slot3, &sc->mask_count,
                                                           (uint4 *)xb3);
     FK_LAUNCH_CHECK();
-    launch_tc_assign(ctx, mm, xb3, cb2, caug2, nullptr, nullptr, sc, st2, nullptr, &sc->mask_count, nullptr,
+    launch_tc_assign(ctx, mm, xb3, cb2, caug2, nullptr, sc, st2, nullptr, &sc->mask_count, nullptr,
                      nullptr, masks, th3);
     if (d % 4 == 0 && d <= 256 && (((uintptr_t)x | (uintptr_t)B.c32) & 15u) == 0) {
         static const int mask_blocks = resident_blocks((const void *)mask_rescore_kernel<true>, MASK_WARPS * 32);
@@ -2104,7 +1965,7 @@ void run_assign_mixed(Ctx &ctx, const TX *x, int64_t n, int d, const double *c, 
         {
             Timer t(ctx.contract_acc != nullptr, ctx, ctx.contract_acc);
             Timer tc(ctx.count_acc != nullptr, ctx, ctx.count_acc);
-            launch_tc_assign(ctx, mc, B.xq, B.cq, B.caug, nullptr, nullptr, sc, B.stats, nullptr, nullptr, B.xaug,
+            launch_tc_assign(ctx, mc, B.xq, B.cq, B.caug, nullptr, sc, B.stats, nullptr, nullptr, B.xaug,
                              rowscale, nullptr, th, cnt);
         }
         finalize_count_kernel<<<(unsigned)std::min<int64_t>(fin_chunks, (int64_t)ctx.num_sms * fin_count),
@@ -2116,7 +1977,7 @@ void run_assign_mixed(Ctx &ctx, const TX *x, int64_t n, int d, const double *c, 
         SliceTop2 *top = (SliceTop2 *)ctx.get(BUF_TOP2, sizeof(SliceTop2) * (size_t)n * mp.parts);
         {
             Timer t(ctx.contract_acc != nullptr, ctx, ctx.contract_acc);
-            launch_tc_assign(ctx, mp, B.xq, B.cq, B.caug, top, nullptr, sc, B.stats, nullptr, nullptr, B.xaug,
+            launch_tc_assign(ctx, mp, B.xq, B.cq, B.caug, top, sc, B.stats, nullptr, nullptr, B.xaug,
                              rowscale);
         }
         finalize_kernel<<<(unsigned)std::min<int64_t>(fin_chunks, (int64_t)ctx.num_sms * fin_top2), FINALIZE_THREADS,
@@ -2171,7 +2032,7 @@ void debug_tc_probe(Ctx &ctx, const float *x, int64_t n, int d, const double *c,
     SliceTop2 *top = (SliceTop2 *)ctx.get(BUF_TOP2, sizeof(SliceTop2) * (size_t)n * mp.parts);
     float *dump = (float *)ctx.get(BUF_OUT, sizeof(float) * 128 * (size_t)mp.kp);
     FK_CUDA(cudaMemsetAsync(dump, 0, sizeof(float) * 128 * (size_t)mp.kp, s));
-    launch_tc_assign(ctx, mp, B.xq, B.cq, B.caug, top, nullptr, sc, B.stats, dump, nullptr, B.xaug, rowscale);
+    launch_tc_assign(ctx, mp, B.xq, B.cq, B.caug, top, sc, B.stats, dump, nullptr, B.xaug, rowscale);
     const size_t es = fp8 ? 1 : 2;
     FK_CUDA(cudaMemcpyAsync(dump_out, dump, sizeof(float) * 128 * (size_t)mp.kp, cudaMemcpyDeviceToHost, s));
     const int64_t rows = n < 128 ? n : 128;

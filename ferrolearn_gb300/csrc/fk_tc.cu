@@ -18,13 +18,16 @@
 //            for FP8); tcgen05.commit signals the epilogue. Two TMEM
 //            accumulators (2 x 256 columns) alternate, so the MMAs of block
 //            b+1 overlap the epilogue of block b.
-//   warps 2-9 epilogue: tcgen05.ld (32x32b, one row per thread), every score
-//            turned into a key -- rounded to a 128-ulp grid with the column
-//            code in the freed 7 bits (three FMA-pipe operations; all scores
-//            of a launch share one binade) -- and ranked: a running top-2
-//            with a bound of the rest (main pass, three-input float max) or a
-//            running top-8 (second pass). The grid quantum is part of the
-//            error bound of the re-check.
+//   warps 2-9 epilogue: tcgen05.ld (32x32b, one row per thread). The
+//            top-2 pass turns every score into a key -- rounded to a 128-ulp
+//            grid with the column code in the freed 7 bits (three FMA-pipe
+//            operations; all scores of a launch share one binade) -- and
+//            keeps a running top-2 with a bound of the rest (three-input
+//            float max); the grid quantum is part of the error bound of the
+//            re-check. The count and mask passes mark the centres scoring at
+//            least a per-row threshold (one saturating FMA per score) and
+//            keep their number, first mask words and the largest score, or
+//            write the row's mask.
 //
 // Every wait on an mbarrier is bounded (about two seconds of SM clock); on
 // expiry the CTA records an error word, stops issuing work, drains what it
@@ -63,15 +66,14 @@ __device__ __forceinline__ int unpack_local(uint32_t l, int base) { return l == 
 // pass, `slots` rotating slots (see the tile merge in the kernel) of EP - 1
 // records per row -- whole records for BF16 with two parts, 16-byte ones
 // otherwise (FP8, whose larger X stages leave less room, and four parts) --
-// and one slot of top-8 records for the second pass; none for the mask pass,
-// whose parts write their own words of the row's candidate mask; the count
-// pass rotates its slots like the top-2 pass, with SliceCount records.
+// none for the mask pass, whose parts write their own words of the row's
+// candidate mask; the count pass rotates its slots like the top-2 pass, with
+// SliceCount records.
 __host__ __device__ constexpr uint32_t merge_bytes(int topk, bool fp8, int ep, int slots) {
     return topk == 1   ? 0u
            : topk == 2 ? BM * (uint32_t)slots * (uint32_t)(ep - 1) *
                              (uint32_t)((fp8 || ep > 2) ? sizeof(HalfRec) : sizeof(Top2))
-           : topk == 3 ? BM * (uint32_t)slots * (uint32_t)(ep - 1) * (uint32_t)sizeof(SliceCount)
-                       : BM * (uint32_t)sizeof(Top8);
+                       : BM * (uint32_t)slots * (uint32_t)(ep - 1) * (uint32_t)sizeof(SliceCount);
 }
 
 // The record of one slot (FP8: HalfRec; BF16: Top2, no packing).
@@ -132,7 +134,6 @@ struct TcParams {
     uint32_t x_stage_bytes;
     uint32_t c_tx_bytes;
     SliceTop2 *out;           // top-2 records (main pass)
-    Top8 *out8;               // top-8 records (second pass)
     unsigned long long *err;
     const MixedStats *stats;  // cgrid, ulp of this launch
     const float *rowscale;    // FP8: per-row power of two 1/(s_i t) that maps scores to this row's units
@@ -442,86 +443,6 @@ __device__ __forceinline__ void count_merge(CountState &s, const SliceCount &o) 
     count_add_word(s, o.w2, (int)(o.meta >> 24));
 }
 
-// ------------------------------------------------ top-8 (second pass) --
-// Sorted insertion of key k into a[0] >= ... >= a[K-1] (2K - 1 min/max).
-template <int K>
-__device__ __forceinline__ void insk(float (&a)[K], float k) {
-#pragma unroll
-    for (int p = 0; p < K - 1; p++) {
-        const float t = fmaxf(a[p], k);
-        k = fminf(a[p], k);
-        a[p] = t;
-    }
-    a[K - 1] = fmaxf(a[K - 1], k);
-}
-
-// Inserts (w, j) into the sorted running list (R, I); returns what falls out.
-template <int K>
-__device__ __forceinline__ uint32_t inski(uint32_t (&R)[K], int (&I)[K], uint32_t w, int j) {
-#pragma unroll
-    for (int p = 0; p < K; p++) {
-        if (w > R[p]) {
-            const uint32_t tw = R[p];
-            const int tj = I[p];
-            R[p] = w;
-            I[p] = j;
-            w = tw;
-            j = tj;
-        }
-    }
-    return w;
-}
-
-template <int K, int CH>
-__device__ __forceinline__ void rank_chunkk(const uint32_t (&r)[32], float cgrid, float ulp, float (&c0)[K],
-                                            float (&c1)[K]) {
-    uint64_t cg2;
-    asm("mov.b64 %0, {%1, %1};" : "=l"(cg2) : "f"(cgrid));
-#pragma unroll
-    for (int e = 0; e < 32; e += 2) {
-        uint64_t p;  // grid rounding of two scores as packed f32x2 operations
-        asm("mov.b64 %0, {%1, %2};" : "=l"(p) : "r"(r[e]), "r"(r[e + 1]));
-        asm("add.rn.f32x2 %0, %0, %1;" : "+l"(p) : "l"(cg2));
-        asm("sub.rn.f32x2 %0, %0, %1;" : "+l"(p) : "l"(cg2));
-        float t0, t1;
-        asm("mov.b64 {%0, %1}, %2;" : "=f"(t0), "=f"(t1) : "l"(p));
-        insk<K>(c0, __fmaf_rn(ulp, (float)(127 - ((CH * 32 + e) & 127)), t0));
-        insk<K>(c1, __fmaf_rn(ulp, (float)(127 - ((CH * 32 + e + 1) & 127)), t1));
-    }
-}
-
-// Top-K keys of the 128 columns of one accumulator half, and a bound of the
-// rest (two chains; a chain's elements outside its top-K are <= its K-th).
-template <int K>
-__device__ __forceinline__ void rank_halfk(uint32_t col_addr, float cgrid, float ulp, uint32_t (&KK)[K],
-                                           uint32_t &ku) {
-    float c0[K], c1[K];
-#pragma unroll
-    for (int p = 0; p < K; p++) c0[p] = c1[p] = 0.f;
-    uint32_t ra[32], rb[32];
-    tmem_ld32(col_addr, ra);
-    tmem_wait(ra);
-    tmem_ld32(col_addr + 32, rb);
-    rank_chunkk<K, 0>(ra, cgrid, ulp, c0, c1);
-    tmem_wait(rb);
-    tmem_ld32(col_addr + 64, ra);
-    rank_chunkk<K, 1>(rb, cgrid, ulp, c0, c1);
-    tmem_wait(ra);
-    tmem_ld32(col_addr + 96, rb);
-    rank_chunkk<K, 2>(ra, cgrid, ulp, c0, c1);
-    tmem_wait(rb);
-    rank_chunkk<K, 3>(rb, cgrid, ulp, c0, c1);
-    int dummy[K];
-#pragma unroll
-    for (int p = 0; p < K; p++) {
-        KK[p] = __float_as_uint(c0[p]);
-        dummy[p] = 0;
-    }
-    ku = max(__float_as_uint(c0[K - 1]), __float_as_uint(c1[K - 1]));
-#pragma unroll
-    for (int p = 0; p < K; p++) ku = max(ku, inski<K>(KK, dummy, __float_as_uint(c1[p]), 0));
-}
-
 // FP8: X and the centres are E4M3 (1 byte, 128 per swizzle atom) and the
 // augmentation operand is a per-row BF16 tile loaded with each X tile (the
 // row's scale times [1,1,1,0,...]); BF16: a constant ones tile.
@@ -796,7 +717,8 @@ __global__ void __launch_bounds__(tc_threads(EP), 1)
                 if (row < p.n && !dead) p.outc[(int64_t)part * p.out_stride + row] = count_pack(st);
             }
         }
-    } else if constexpr (TOPK == 2) {
+    } else {
+        static_assert(TOPK == 2, "pass kinds: 1 masks, 2 top-2, 3 count");
         constexpr int CP = BN / EP;   // columns of one part
         constexpr int NCK = CP / 32;  // its 32-column chunks
         static_assert(NCK == 2 || NCK == 4, "two or four epilogue parts");
@@ -933,80 +855,6 @@ __global__ void __launch_bounds__(tc_threads(EP), 1)
             }
         }
         if (pre) tmem_wait(ra);  // a load issued for an item that never ran completes before exit
-    } else {
-        const int ew = warp - 2;
-        const int quarter = warp & 3;
-        const int half = ew >> 2;
-        const int row_local = quarter * 32 + lane;
-        const uint32_t lane_addr = tmem + ((uint32_t)(quarter * 32) << 16);
-        Top8 *merge = (Top8 *)(smem + p.off_merge);
-        const float cgrid = p.stats->cgrid, ulp = p.stats->ulp;
-        uint32_t item = 0;
-        bool dead = false;
-        for (int64_t t = q; t < p.tiles; t += tstride) {
-            uint32_t R[8], U = 0u;
-            int I[8];
-#pragma unroll
-            for (int j = 0; j < 8; j++) {
-                R[j] = 0u;
-                I[j] = -1;
-            }
-            float cg = cgrid, ul = ulp;
-            if (FP8) {
-                const int64_t rrow = t * BM + row_local;
-                const float rs = rrow < p.n ? p.rowscale[rrow] : 1.f;
-                cg = cgrid * rs;
-                ul = ulp * rs;
-            }
-            for (int b = 0; b < p.nblocks; b++, item++) {
-                const int buf = (int)(item & 1u);
-                const uint32_t aph = (item >> 1) & 1u;
-                if (!dead && !mbar_wait(bar_afull(buf), aph, abort_flag, p.err, 16ull)) dead = true;
-                dead = __any_sync(0xffffffffu, dead);  // warp-uniform, for the barriers below
-                if (dead) continue;
-                tc_fence_after();
-                const uint32_t col = lane_addr + (uint32_t)buf * BN + (uint32_t)half * 128u;
-                uint32_t K[8], ku;
-                rank_halfk<8>(col, cg, ul, K, ku);
-                tc_fence_before();
-                __syncwarp();
-                if (lane == 0) mbar_arrive(bar_aempty(buf));
-                const int base = part * p.kp + b * BN + half * 128 + 127;
-                U = max(U, ku & 0xFFFFFF80u);
-#pragma unroll
-                for (int j = 0; j < 8; j++)
-                    U = max(U, inski<8>(R, I, K[j] & 0xFFFFFF80u, base - (int)(K[j] & 0x7Fu)));
-            }
-            if (half == 1) {
-                Top8 rec;
-#pragma unroll
-                for (int j = 0; j < 8; j++) {
-                    rec.v[j] = __uint_as_float(R[j]);
-                    rec.i[j] = I[j];
-                }
-                rec.u9 = __uint_as_float(U);
-                merge[row_local] = rec;
-            }
-            epi_bar();
-            if (half == 0) {
-                const Top8 o = merge[row_local];
-                U = max(U, __float_as_uint(o.u9));
-#pragma unroll
-                for (int j = 0; j < 8; j++) U = max(U, inski<8>(R, I, __float_as_uint(o.v[j]), o.i[j]));
-                const int64_t row = t * BM + row_local;
-                if (row < p.n && !dead) {
-                    Top8 rec;
-#pragma unroll
-                    for (int j = 0; j < 8; j++) {
-                        rec.v[j] = __uint_as_float(R[j]);
-                        rec.i[j] = I[j];
-                    }
-                    rec.u9 = __uint_as_float(U);
-                    p.out8[(int64_t)part * p.out_stride + row] = rec;
-                }
-            }
-            epi_bar();
-        }
     }
 
     tc_fence_before();
@@ -1193,12 +1041,11 @@ void plan_tc(Ctx &ctx, MixedPlan &mp, int64_t n, int d, int k, bool fp8, int top
 }
 
 void launch_tc_assign(Ctx &ctx, MixedPlan &mp, const void *xb, const void *cb, const void *caug, SliceTop2 *out,
-                      Top8 *out8, DevScalars *sc, const MixedStats *stats, float *dump,
+                      DevScalars *sc, const MixedStats *stats, float *dump,
                       const unsigned long long *n_dev, const void *xaug, const float *rowscale, uint32_t *masks,
                       const float *thresh, SliceCount *outc) {
     const bool fp8 = mp.fp8;
-    if ((mp.topk == 2) != (out != nullptr) || (mp.topk == 8) != (out8 != nullptr) ||
-        (mp.topk == 1) != (masks != nullptr) || (mp.topk == 3) != (outc != nullptr) ||
+    if ((mp.topk == 2) != (out != nullptr) || (mp.topk == 1) != (masks != nullptr) || (mp.topk == 3) != (outc != nullptr) ||
         ((mp.topk == 1 || mp.topk == 3) != (thresh != nullptr)) || (mp.topk == 1 && fp8)) {
         set_error("tensor-core launch: records do not match the plan");
         fail(FK_ERR_INVALID_PARAMETER);
@@ -1249,7 +1096,6 @@ void launch_tc_assign(Ctx &ctx, MixedPlan &mp, const void *xb, const void *cb, c
     p.slots = mp.slots;
     p.c_tx_bytes = (uint32_t)p.n_atoms * p.c_atom_bytes + (uint32_t)mp.kp * 32u + (fp8 ? 0u : ONES_BYTES);
     p.out = out;
-    p.out8 = out8;
     p.n_dev = n_dev;
     p.out_stride = mp.n;
     p.err = &sc->error_word;
@@ -1271,8 +1117,8 @@ void launch_tc_assign(Ctx &ctx, MixedPlan &mp, const void *xb, const void *cb, c
         FK_CUDA(cudaFuncSetAttribute((const void *)kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         kern<<<mp.grid, tc_threads(mp.ep), smem, ctx.stream>>>(*tx, *tcm, *ta, *to, p);
     };
-    // Instantiations: main pass (top-2) BF16 / FP8 with one or two X stages;
-    // second pass (top-8, or candidate masks) BF16 with one or two X stages.
+    // Instantiations, each with one or two X stages: the top-2 and count
+    // passes in BF16 and FP8, the mask pass in BF16.
     if (mp.topk == 1) {
         mp.xst == 2 ? go(tc_assign_kernel<1, false, 2, 2>) : go(tc_assign_kernel<1, false, 1, 2>);
     } else if (mp.topk == 3) {
@@ -1282,12 +1128,9 @@ void launch_tc_assign(Ctx &ctx, MixedPlan &mp, const void *xb, const void *cb, c
             mp.xst == 2 ? go(tc_assign_kernel<3, false, 2, 4>) : go(tc_assign_kernel<3, false, 1, 4>);
         else
             mp.xst == 2 ? go(tc_assign_kernel<3, false, 2, 2>) : go(tc_assign_kernel<3, false, 1, 2>);
-    } else if (mp.topk == 8) {
-        if (fp8) {
-            set_error("the second pass runs in BF16");
-            fail(FK_ERR_UNSUPPORTED);
-        }
-        mp.xst == 2 ? go(tc_assign_kernel<8, false, 2, 2>) : go(tc_assign_kernel<8, false, 1, 2>);
+    } else if (mp.topk != 2) {
+        set_error("tensor-core launch: unknown pass kind %d", mp.topk);
+        fail(FK_ERR_INVALID_PARAMETER);
     } else if (fp8) {
         mp.xst == 2 ? go(tc_assign_kernel<2, true, 2, 2>) : go(tc_assign_kernel<2, true, 1, 2>);
     } else {

@@ -87,9 +87,10 @@ typedef struct fk_fit_report {
     int64_t rows_second_pass;  /* mixed: rows scored again by a second
                                   tensor pass (= rows_full_rescan): BF16
                                   candidate masks after a BF16 main pass,
-                                  BF16 top-8 after an FP8 one              */
+                                  a BF16 count pass (and masks) after an
+                                  FP8 one                                  */
     int64_t rows_few;          /* mixed: of those, rows resolved among at
-                                  most 32 (masks) or 8 (top-8) candidates  */
+                                  most 32 candidates                       */
     int64_t rows_exhaustive;   /* mixed: rows re-scored against every
                                   centre after the second pass             */
     int64_t near_tie_rows;     /* mixed: re-scored rows whose FP64 margin
@@ -402,8 +403,8 @@ fk_status fk_debug_tc_probe(fk_ctx *ctx, const float *x_dev, int64_t n, int64_t 
 
 /* Diagnostics (no reference counterpart, no GPU needed): the launch plan of
  * one tensor-core pass for a shape -- precision FK_PRECISION_MIXED_BF16 or
- * _FP8, topk 2 (top-2 main pass), 3 (count pass), 1 (BF16 mask pass) or 8
- * (BF16 top-8 pass), on num_sms SMs. out[0..9] =
+ * _FP8, topk 2 (top-2 main pass), 3 (count pass) or 1 (BF16 mask pass), on
+ * num_sms SMs. out[0..9] =
  * {d_pad, kp (resident centres per slice), parts (slices), k_pad, nblocks
  * (256-centre accumulator blocks per slice), xst (X ring depth), dynamic
  * shared memory bytes, grid, CTAs per slice, 128-row tiles}. */

@@ -140,11 +140,14 @@ def test_tensor_core_plans_of_the_workloads():
     st, p = _plan(8_000_000, 256, 4096, F.MIXED_FP8, 2)
     assert st == 0 and (p["d_pad"], p["kp"], p["parts"], p["xst"]) == (256, 512, 8, 2)
     assert p["grid"] == 152 and p["smem"] <= 227 * 1024
-    st, p = _plan(2_000_000, 256, 4096, F.MIXED_BF16, 8)  # the second pass of the FP8 form: BF16 rows of
-    # 512 bytes leave room for one X stage and 256 resident centres
+    st, p = _plan(2_000_000, 256, 4096, F.MIXED_BF16, 3)  # the second pass of the FP8 form (count pass): BF16
+    # rows of 512 bytes leave room for one X stage and 256 resident centres
     assert st == 0 and (p["kp"], p["parts"], p["xst"], p["grid"]) == (256, 16, 1, 144) and p["smem"] <= 227 * 1024
-    st, p = _plan(100_000, 128, 1024, F.MIXED_BF16, 8)
-    assert st == 0 and (p["kp"], p["xst"]) == (512, 2)
+    st, p = _plan(2_000_000, 256, 4096, F.MIXED_FP8, 3)  # the FP8 count pass: the FP8 top-2 pass's slices
+    assert st == 0 and (p["kp"], p["parts"], p["xst"]) == (512, 8, 2) and p["smem"] <= 227 * 1024
+    for topk in (1, 3):  # the BF16 mask and count passes fit the main pass's slices at cfg3
+        st, p = _plan(100_000, 128, 1024, F.MIXED_BF16, topk)
+        assert st == 0 and (p["kp"], p["xst"]) == (512, 2)
     # small shapes: one padded slice, grid no larger than the tiles
     st, p = _plan(1, 1, 1, F.MIXED_BF16, 2)
     assert st == 0 and (p["d_pad"], p["kp"], p["parts"], p["k_pad"], p["grid"], p["tiles"]) == (64, 256, 1, 256, 1, 1)
