@@ -60,6 +60,7 @@ void *Ctx::get(BufSlot s, size_t bytes) {
     }
     size_t want = bytes + bytes / 8;  // headroom for slightly larger calls
     void *p = nullptr;
+    buf_gen++;  // captured iterations that used the old buffer are retired
     cudaError_t e = cudaMalloc(&p, want);
     if (e != cudaSuccess) {
         (void)cudaGetLastError();
@@ -195,6 +196,75 @@ fk_status check_shape(int64_t n, int64_t d, int64_t k) {
 // changed since the previous assignment (no inertia: the fit computes it
 // once, for the assignment it keeps).
 enum UpdateMode { UPDATE_FULL = 0, UPDATE_FULL_STATE = 1, UPDATE_INCREMENTAL = 2 };
+
+// One fit iteration through a CUDA graph: the first time a key is seen the
+// body is captured (relaxed mode; nothing runs while capturing) and launched
+// as a graph, and every later time the graph is replayed -- one launch for
+// the iteration's twenty-odd kernels, memsets and copies. A capture that
+// fails (a first use that allocates a buffer or plans a pass, which
+// synchronises) runs the body as usual and is tried once more at the key's
+// next occurrence, then given up.
+template <typename Body>
+void run_graphed(Ctx &ctx, const uint64_t (&key)[10], Body &&body) {
+    if (ctx.graph_gen != ctx.buf_gen || ctx.iter_graphs.size() > 64) {
+        for (auto &g : ctx.iter_graphs)
+            if (g.exec) cudaGraphExecDestroy(g.exec);
+        ctx.iter_graphs.clear();
+        ctx.graph_gen = ctx.buf_gen;
+    }
+    Ctx::IterGraph *e = nullptr;
+    for (auto &g : ctx.iter_graphs)
+        if (memcmp(g.key, key, sizeof(g.key)) == 0) e = &g;
+    if (!e) {
+        Ctx::IterGraph g{};
+        memcpy(g.key, key, sizeof(g.key));
+        g.exec = nullptr;
+        g.launches = 0;
+        g.state = 0;
+        g.tries = 0;
+        ctx.iter_graphs.push_back(g);
+        e = &ctx.iter_graphs.back();
+    }
+    if (e->state == 1) {
+        FK_CUDA(cudaGraphLaunch(e->exec, ctx.stream));
+        __atomic_add_fetch(&g_launch_count, e->launches, __ATOMIC_RELAXED);
+        return;
+    }
+    if (e->state == 2) {
+        body();
+        return;
+    }
+    const uint64_t gen0 = ctx.buf_gen;
+    const unsigned long long l0 = __atomic_load_n(&g_launch_count, __ATOMIC_RELAXED);
+    FK_CUDA(cudaStreamBeginCapture(ctx.stream, cudaStreamCaptureModeRelaxed));
+    bool ok = true;
+    try {
+        body();
+    } catch (const Error &) {
+        ok = false;
+    }
+    cudaGraph_t graph = nullptr;
+    cudaError_t err = cudaStreamEndCapture(ctx.stream, &graph);
+    cudaGraphExec_t exec = nullptr;
+    if (err == cudaSuccess && graph && ok && ctx.buf_gen == gen0) err = cudaGraphInstantiate(&exec, graph, 0);
+    if (graph) cudaGraphDestroy(graph);
+    // the entry may have moved if body() grew the cache: find it again
+    for (auto &g : ctx.iter_graphs)
+        if (memcmp(g.key, key, sizeof(g.key)) == 0) e = &g;
+    if (err != cudaSuccess || !exec || !ok || ctx.buf_gen != gen0) {
+        (void)cudaGetLastError();
+        if (exec) cudaGraphExecDestroy(exec);
+        g_last_error.clear();
+        __atomic_store_n(&g_launch_count, l0, __ATOMIC_RELAXED);
+        e->state = ++e->tries >= 2 ? 2 : 0;
+        body();
+        return;
+    }
+    e->exec = exec;
+    e->launches = __atomic_load_n(&g_launch_count, __ATOMIC_RELAXED) - l0;
+    e->state = 1;
+    FK_CUDA(cudaGraphLaunch(exec, ctx.stream));
+}
 
 // Assignment against c (labels, inertia into scalars), then the update into
 // nc (+ shift bits). Mixed precisions fold the inertia into the update pass.
@@ -462,7 +532,6 @@ fk_status fit_impl(fk_ctx *ctxp, const TX *x_in, int64_t n, int64_t d, const fk_
         int64_t launched = 0;
         for (int64_t it = 0; it < p->max_iter && !stop; it++) {
             const int par = (int)(it & 1);
-            FK_CUDA(cudaMemsetAsync(sc, 0, sizeof(DevScalars), s));
             // the first two iterations move many rows (a third of them is
             // common in the second): the full pass is cheaper there
             const int mode = !inc_candidate ? UPDATE_FULL
@@ -472,9 +541,30 @@ fk_status fit_impl(fk_ctx *ctxp, const TX *x_in, int64_t n, int64_t d, const fk_
             was_count[par] = count;
             if (count && rep) rep->count_iterations++;
             // iteration it - 1 read cb3[(it + 2) % 3]; it is not overwritten before iteration it + 1
-            lloyd_iteration<TX, TC>(ctx, x, n, (int)d, cb3[it % 3], (int)k, p->precision, cb3[(it + 1) % 3],
-                                    labels2 + (size_t)par * n, sc, plan, x_changed, rep, timing, mode,
-                                    labels2 + (size_t)(par ^ 1) * n, count ? cb3[(it + 2) % 3] : nullptr);
+            auto iteration = [&] {
+                lloyd_iteration<TX, TC>(ctx, x, n, (int)d, cb3[it % 3], (int)k, p->precision, cb3[(it + 1) % 3],
+                                        labels2 + (size_t)par * n, sc, plan, x_changed, rep, timing, mode,
+                                        labels2 + (size_t)(par ^ 1) * n, count ? cb3[(it + 2) % 3] : nullptr);
+            };
+            if (!timing && !x_changed && it >= 2) {
+                // steady state: the memset, the iteration and the scalars' copy as one graph
+                // (phase timers record events, so timed fits run without graphs)
+                const uint64_t key[10] = {(uint64_t)(uintptr_t)x, (uint64_t)n, (uint64_t)d, (uint64_t)k,
+                                          (uint64_t)p->precision, (uint64_t)(it % 6), (uint64_t)mode,
+                                          (uint64_t)count, (uint64_t)(uintptr_t)sc, sizeof(TX) * 16 + sizeof(TC)};
+                run_graphed(ctx, key, [&] {
+                    FK_CUDA(cudaMemsetAsync(sc, 0, sizeof(DevScalars), s));
+                    iteration();
+                    FK_CUDA(cudaMemcpyAsync(&ctx.host_scalars[1 + par], sc, sizeof(DevScalars),
+                                            cudaMemcpyDeviceToHost, s));
+                });
+                FK_CUDA(cudaEventRecord(iter_done[par], s));
+                launched = it + 1;
+                if (it > 0) stop = finish(it - 1);
+                continue;
+            }
+            FK_CUDA(cudaMemsetAsync(sc, 0, sizeof(DevScalars), s));
+            iteration();
             if (x_changed && inc_candidate) {
                 // once per fit: X finite and the split's grids valid?
                 MixedStats hs;
@@ -1253,6 +1343,8 @@ fk_status fk_ctx_destroy(fk_ctx *ctx) {
     if (c->mixedm.ones) cudaFree(c->mixedm.ones);
     if (c->mixedm2.ones) cudaFree(c->mixedm2.ones);
     if (c->mixedc.ones) cudaFree(c->mixedc.ones);
+    for (auto &g : c->iter_graphs)
+        if (g.exec) cudaGraphExecDestroy(g.exec);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return FK_OK;

@@ -183,6 +183,18 @@ struct Ctx {
     MixedPlan mixedm2; // its mask pass (BF16, the slicing of mixed2)
     MixedPlan mixedm;  // second pass (BF16, candidate masks) over the rows a BF16 main pass left open
     MixedPlan mixedc;  // count pass (main pass from the fourth iteration of a fit)
+    // Captured steady-state fit iterations (fk_capi.cu), keyed by what the
+    // iteration's launches depend on; a buffer (re)allocation bumps buf_gen,
+    // which retires them all (their pointers would be stale).
+    struct IterGraph {
+        uint64_t key[10];
+        cudaGraphExec_t exec;
+        unsigned long long launches;  // kernel launches one replay stands for
+        int state;                    // 0 not captured yet, 1 captured, 2 not capturable
+        int tries;                    // failed captures so far
+    };
+    std::vector<IterGraph> iter_graphs;
+    uint64_t buf_gen = 0, graph_gen = 0;
     int batch_variant[20] = {-1, -1, -1, -1, -1, -1, -1, -1, -1, -1,
                              -1, -1, -1, -1, -1, -1, -1, -1, -1, -1};  // autotuned tile shape per (d, k) bucket
     double *contract_acc = nullptr;  // when set: device time of the contraction kernel

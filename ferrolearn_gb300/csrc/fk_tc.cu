@@ -1027,17 +1027,27 @@ void plan_shape(MixedPlan &mp, int64_t n, int d, int k, bool fp8, int topk, int 
     mp.smem = fixed + (size_t)mp.kp * per_centre;
 }
 
+// The plan changes only once everything it needs exists: the ones tile is
+// allocated, filled and mapped first (a failure frees it and leaves the plan
+// as it was, e.g. a synchronous copy refused while the stream is captured).
 void plan_tc(Ctx &ctx, MixedPlan &mp, int64_t n, int d, int k, bool fp8, int topk, int kp_fixed) {
-    plan_shape(mp, n, d, k, fp8, topk, ctx.num_sms, kp_fixed);
-    mp.tm_x_ptr = mp.tm_c_ptr = mp.tm_aug_ptr = mp.tm_xaug_ptr = nullptr;
     if (!mp.ones) {
         uint16_t h[BM * 16];
         for (int r = 0; r < BM; r++)
             for (int j = 0; j < 16; j++) h[r * 16 + j] = j < 3 ? 0x3F80 : 0;  // BF16 1.0 = 0x3F80
-        FK_CUDA(cudaMalloc(&mp.ones, sizeof(h)));
-        FK_CUDA(cudaMemcpy(mp.ones, h, sizeof(h), cudaMemcpyHostToDevice));
-        encode_2d(ctx, mp.tm_ones, mp.ones, 16, BM, 32, 16, BM, CU_TENSOR_MAP_SWIZZLE_32B);
+        void *ones = nullptr;
+        FK_CUDA(cudaMalloc(&ones, sizeof(h)));
+        try {
+            FK_CUDA(cudaMemcpy(ones, h, sizeof(h), cudaMemcpyHostToDevice));
+            encode_2d(ctx, mp.tm_ones, ones, 16, BM, 32, 16, BM, CU_TENSOR_MAP_SWIZZLE_32B);
+        } catch (...) {
+            cudaFree(ones);
+            throw;
+        }
+        mp.ones = ones;
     }
+    plan_shape(mp, n, d, k, fp8, topk, ctx.num_sms, kp_fixed);
+    mp.tm_x_ptr = mp.tm_c_ptr = mp.tm_aug_ptr = mp.tm_xaug_ptr = nullptr;
 }
 
 void launch_tc_assign(Ctx &ctx, MixedPlan &mp, const void *xb, const void *cb, const void *caug, SliceTop2 *out,

@@ -325,7 +325,7 @@ class KMeans:
         fn = getattr(_native.lib(), f"fk_kmeans_fit_{suf}")
         _check(fn(ctx.handle, _ptr(x), n, d, C.byref(params), _ptr(init), _ptr(centers), _ptr(labels),
                   C.byref(inertia), C.byref(n_iter), C.byref(rep)))
-        lab = labels if out is not None else labels.astype(np.int64)
+        lab = labels if out is not None else labels.view(np.int64)  # labels < 2^63: the same bits, no copy
         return FittedKMeans(centers, lab, inertia.value, n_iter.value, self.dtype, rep.as_dict(), self.precision)
 
     def fit_predict(self, x, ctx=None):
@@ -368,7 +368,7 @@ class FittedKMeans:
         fn = getattr(_native.lib(), f"fk_kmeans_predict_{suf}")
         _check(fn(ctx.handle, _ptr(self._centers), self._centers.shape[0], self._centers.shape[1], _ptr(x), n, d,
                   prec, _ptr(labels)))
-        return labels.astype(np.int64)
+        return labels.view(np.int64)
 
     def transform(self, x, ctx=None):
         """Transform::transform (kmeans.rs:568-617)."""
@@ -401,7 +401,7 @@ def lloyd_step(x, centers, dtype="f64", precision=PLAIN, ctx=None):
     fn = getattr(_native.lib(), f"fk_lloyd_step_{suf}")
     _check(fn(ctx.handle, _ptr(x), n, d, _ptr(c), k, _prec(precision), _ptr(labels), _ptr(nc), C.byref(inertia),
               C.byref(shift), C.byref(rep)))
-    return labels.astype(np.int64), nc, inertia.value, shift.value, rep.as_dict()
+    return labels.view(np.int64), nc, inertia.value, shift.value, rep.as_dict()
 
 
 def kmeans_plus_plus(x, k, draws_arr=None, seed=0, dtype="f64", ctx=None):

@@ -140,7 +140,7 @@ class MiniBatchKMeans:
         fn = getattr(_native.lib(), f"fk_minibatch_fit_{suf}")
         _check(fn(ctx.handle, _ptr(x), n, d, C.byref(params), _ptr(init), _ptr(centers), _ptr(labels),
                   C.byref(inertia), C.byref(n_iter), C.byref(best), C.byref(rep)))
-        lab = labels if out is not None else labels.astype(np.int64)
+        lab = labels if out is not None else labels.view(np.int64)  # labels < 2^63: the same bits, no copy
         report = rep.as_dict()
         report["best_run"] = best.value
         return FittedMiniBatchKMeans(centers, lab, inertia.value, n_iter.value, self.dtype, report)
