@@ -9,7 +9,10 @@ so every iteration runs. A step is one Lloyd iteration over all n rows
   value   Lloyd iterations/s of the chosen form with X already resident in
           HBM: one fit call running W warm-up iterations, then one fit call
           running exactly K iterations (results into device tensors) timed
-          with CUDA events on the stream the library launches on.
+          with CUDA events on the stream the library launches on (no phase
+          timers in it, so its steady-state iterations replay CUDA graphs;
+          the phase breakdown comes from a second, timed run of the same
+          fit).
   e2e     the same metric through the public API with host buffers: one fit
           call on a pinned host X (H2D of X, K iterations, D2H of labels and
           centres inside the timed region).
