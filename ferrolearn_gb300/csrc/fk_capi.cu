@@ -83,6 +83,12 @@ int kpp_trials_host(int64_t k) {
     return t < 1 ? 1 : (int)t;
 }
 
+// First iteration whose main pass may be the count pass (it needs the row
+// floors of a previous pass, and the centres' shifts to have settled).
+#ifndef FK_COUNT_FROM
+#define FK_COUNT_FROM 3
+#endif
+
 namespace {
 
 // True for device (or managed) memory the call can use in place, false for
@@ -512,7 +518,7 @@ fk_status fit_impl(fk_ctx *ctxp, const TX *x_in, int64_t n, int64_t d, const fk_
         if constexpr (std::is_same<TX, float>::value && std::is_same<TC, double>::value)
             count_ok = p->precision == FK_PRECISION_MIXED_BF16 || p->precision == FK_PRECISION_MIXED_FP8;
         bool was_count[2] = {false, false};
-        int64_t count_from = 3;
+        int64_t count_from = FK_COUNT_FROM;
         auto finish = [&](int64_t r) {
             FK_CUDA(cudaEventSynchronize(iter_done[r & 1]));
             const DevScalars &h = ctx.host_scalars[1 + (r & 1)];
