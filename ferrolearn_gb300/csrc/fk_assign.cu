@@ -127,29 +127,29 @@ assign_direct_kernel(const TX *__restrict__ x, int64_t n, int d, const TC *__res
             }
         }
     }
-    if (WRITE_ALL) return;
-
-    // Reduce over the 16 centre groups that share these rows (same half-warp).
+    if constexpr (!WRITE_ALL) {
+        // Reduce over the 16 centre groups that share these rows (same half-warp).
 #pragma unroll
-    for (int a = 0; a < TM; a++) {
-        TC v = best_v[a];
-        int i = best_i[a];
+        for (int a = 0; a < TM; a++) {
+            TC v = best_v[a];
+            int i = best_i[a];
 #pragma unroll
-        for (int off = 8; off >= 1; off >>= 1) {
-            TC ov = __shfl_xor_sync(0xffffffffu, v, off);
-            int oi = __shfl_xor_sync(0xffffffffu, i, off);
-            if (better(ov, oi, v, i)) { v = ov; i = oi; }
-        }
-        int64_t gr = row0 + ty * TM + a;
-        if (tx == 0 && gr < n) {
-            if (part_v) {
-                part_v[(int64_t)blockIdx.y * n + gr] = v;
-                part_i[(int64_t)blockIdx.y * n + gr] = i;
-                continue;
+            for (int off = 8; off >= 1; off >>= 1) {
+                TC ov = __shfl_xor_sync(0xffffffffu, v, off);
+                int oi = __shfl_xor_sync(0xffffffffu, i, off);
+                if (better(ov, oi, v, i)) { v = ov; i = oi; }
             }
-            if (i == INT32_MAX) { i = 0; v = A::maxv(); }  // nothing below F::MAX
-            labels[gr] = i;
-            if (mind) mind[gr] = v;
+            int64_t gr = row0 + ty * TM + a;
+            if (tx == 0 && gr < n) {
+                if (part_v) {
+                    part_v[(int64_t)blockIdx.y * n + gr] = v;
+                    part_i[(int64_t)blockIdx.y * n + gr] = i;
+                    continue;
+                }
+                if (i == INT32_MAX) { i = 0; v = A::maxv(); }  // nothing below F::MAX
+                labels[gr] = i;
+                if (mind) mind[gr] = v;
+            }
         }
     }
 }

@@ -1001,19 +1001,6 @@ __device__ __forceinline__ bool near_tie(double a, double b) {
     return fabs(a - b) <= 1e-12 * lo;
 }
 
-// FP32 direct form with a rigorous bound of its distance from the exact
-// real distance: (d+3) 2^-23 d32 for the roundings of the differences, the
-// squares and the running sum, plus the effect of the centre's rounding to
-// f32 (ec = ||c - c32||), plus the FP64 oracle's own rounding.
-__device__ __forceinline__ float sqeuc32(const float *__restrict__ x, const float *__restrict__ c, int d) {
-    float acc = 0.f;
-    for (int j = 0; j < d; j++) {
-        float t = x[j] - c[j];
-        acc = fmaf(t, t, acc);
-    }
-    return acc;
-}
-
 // Upper bound, in f32 with upward rounding, of |d32 - D| + |D64 - D| where D
 // is the exact real distance and D64 the oracle's FP64 direct form:
 // ((d+4) 2^-23 d32 + 2 sqrt(d32) ec + 3 ec^2) * 1.01. 2 sqrt(d32) is bounded

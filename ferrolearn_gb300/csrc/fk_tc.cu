@@ -282,8 +282,6 @@ __device__ __forceinline__ float fmax3(float a, float b, float c) {
     return r;
 }
 
-__device__ __forceinline__ void epi_bar() { asm volatile("bar.sync 1, 256;" ::: "memory"); }
-
 // Running top-2 merge with a bound of the rest. (R1 >= R2, I1, I2) are the
 // best two keys so far and U bounds every key seen but not kept. The merged
 // result (w1 >= w2, j1, j2) comes with wu, a bound of its own rest (wu <= w2).
