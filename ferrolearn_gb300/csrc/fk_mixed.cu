@@ -274,51 +274,78 @@ __global__ void prep_rows_kernel(const TX *__restrict__ x, int64_t n, int d, int
     }
 }
 
-// The same outputs as prep_rows_kernel for f32 rows with d a multiple of 4 and
-// d_pad <= 256: lane l owns the 4-feature pieces l and l + 32 of the row,
-// loaded once with 16-byte loads, and the next row's pieces are in flight
-// while this one is processed. The norms are summed in another order than in
-// prep_rows_kernel, which the upward inflation by (d + 64) 2^-23 covers.
-template <bool FP8>
+// The same outputs as prep_rows_kernel for f32 rows with d a multiple of 4
+// and d_pad <= 16 LPR: LPR lanes per row (32 / LPR rows a warp), lane l of a
+// row owning its 4-feature pieces l, l + LPR, l + 2 LPR, l + 3 LPR, loaded
+// with 16-byte loads, the warp's next rows in flight while these are
+// processed; the reductions run over the row's LPR lanes. The norms are
+// summed in another order than in prep_rows_kernel, which the upward
+// inflation by (d + 64) 2^-23 covers.
+template <int LPR>
+__device__ __forceinline__ float group_sum_f(float v) {
+#pragma unroll
+    for (int off = LPR / 2; off >= 1; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    return v;
+}
+
+template <int LPR>
+__device__ __forceinline__ float group_max_f(float v) {
+#pragma unroll
+    for (int off = LPR / 2; off >= 1; off >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, off));
+    return v;
+}
+
+template <bool FP8, int LPR>
 __global__ void prep_rows4_kernel(const float *__restrict__ x, int64_t n, int d, int d_pad,
                                   const float *__restrict__ mu32, void *__restrict__ xq_out,
                                   __nv_bfloat16 *__restrict__ xaug, float4 *__restrict__ rowinfo, MixedStats *stats,
                                   const int32_t *__restrict__ list, const unsigned long long *count) {
+    constexpr int RPW = 32 / LPR;  // rows a warp
+    constexpr int NPL = 4;         // 4-feature pieces a lane
     __shared__ float sh_xn[32], sh_am[32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    const int sl = lane % LPR, g = lane / LPR;
+    const int64_t stride = (int64_t)gridDim.x * (blockDim.x >> 5) * RPW;
     const int64_t slots = list ? (int64_t)*count : n;
     const int d4 = d >> 2, dp4 = d_pad >> 2;
     const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
-    float4 m4[2];
+    float4 m4[NPL];
 #pragma unroll
-    for (int i = 0; i < 2; i++) {
-        const int q = lane + 32 * i;
+    for (int i = 0; i < NPL; i++) {
+        const int q = sl + LPR * i;
         m4[i] = q < d4 ? reinterpret_cast<const float4 *>(mu32)[q] : zero4;
     }
-    auto load_row = [&](int64_t sl, float4 (&v)[2]) {
-        const int64_t row = list ? (int64_t)list[sl] : sl;
+    auto load_row = [&](int64_t sl0, float4 (&v)[NPL]) {
+        const int64_t slot = sl0 + g;
+        const bool ok = slot < slots;
+        const int64_t row = !ok ? 0 : list ? (int64_t)list[slot] : slot;
         const float4 *r4 = reinterpret_cast<const float4 *>(x + row * d);
 #pragma unroll
-        for (int i = 0; i < 2; i++) {
-            const int q = lane + 32 * i;
-            v[i] = q < d4 ? r4[q] : zero4;
+        for (int i = 0; i < NPL; i++) {
+            const int q = sl + LPR * i;
+            v[i] = ok && q < d4 ? r4[q] : zero4;
         }
     };
     float xn_hi = 0.f, am_hi = 0.f, nonfin = 0.f;
-    int64_t slot = (int64_t)blockIdx.x * (blockDim.x >> 5) + w;
-    float4 cur[2] = {zero4, zero4};
-    if (slot < slots) load_row(slot, cur);
-    for (; slot < slots; slot += nwarps) {
-        float4 nxt[2] = {zero4, zero4};
-        if (slot + nwarps < slots) load_row(slot + nwarps, nxt);
+    int64_t base = ((int64_t)blockIdx.x * (blockDim.x >> 5) + w) * RPW;  // warp-uniform
+    float4 cur[NPL];
+#pragma unroll
+    for (int i = 0; i < NPL; i++) cur[i] = zero4;
+    if (base < slots) load_row(base, cur);
+    for (; base < slots; base += stride) {
+        float4 nxt[NPL];
+#pragma unroll
+        for (int i = 0; i < NPL; i++) nxt[i] = zero4;
+        if (base + stride < slots) load_row(base + stride, nxt);
+        const int64_t slot = base + g;
+        const bool ok = slot < slots;  // every lane stays for the shuffles
         float xn2 = 0.f, ex2 = 0.f, tn2 = 0.f, xo2 = 0.f, amax = 0.f;
         float scale = 1.f, inv = 1.f;
         if (FP8) {
             float tmax = 0.f;
 #pragma unroll
-            for (int i = 0; i < 2; i++) {
-                if (lane + 32 * i >= d4) continue;
+            for (int i = 0; i < NPL; i++) {
+                if (sl + LPR * i >= d4) continue;
                 const float xs[4] = {cur[i].x, cur[i].y, cur[i].z, cur[i].w};
                 const float ms[4] = {m4[i].x, m4[i].y, m4[i].z, m4[i].w};
 #pragma unroll
@@ -327,8 +354,7 @@ __global__ void prep_rows4_kernel(const float *__restrict__ x, int64_t n, int d,
                     if (tv < INFINITY) tmax = fmaxf(tmax, tv);
                 }
             }
-#pragma unroll
-            for (int off = 16; off >= 1; off >>= 1) tmax = fmaxf(tmax, __shfl_xor_sync(0xffffffffu, tmax, off));
+            tmax = group_max_f<LPR>(tmax);
             const int sh_t = fp8_scale_exp(stats->tmax);
             int sh = tmax > 0.f ? fp8_scale_exp(tmax) : sh_t;
             sh = max(min(sh, sh_t + FP8_ROW_ABOVE), sh_t - FP8_ROW_BELOW);
@@ -337,8 +363,8 @@ __global__ void prep_rows4_kernel(const float *__restrict__ x, int64_t n, int d,
             inv = ldexpf(1.f, -sh);
         }
 #pragma unroll
-        for (int i = 0; i < 2; i++) {
-            const int q = lane + 32 * i;
+        for (int i = 0; i < NPL; i++) {
+            const int q = sl + LPR * i;
             if (q >= dp4) continue;
             if (q < d4) {
                 const float xs[4] = {cur[i].x, cur[i].y, cur[i].z, cur[i].w};
@@ -365,36 +391,46 @@ __global__ void prep_rows4_kernel(const float *__restrict__ x, int64_t n, int d,
                     xo2 = __fmaf_rn(xv, xv, xo2);
                     if (fabsf(xv) < INFINITY) amax = fmaxf(amax, fabsf(xv));  // finite values only
                 }
+                if (ok) {
+                    if (FP8)
+                        reinterpret_cast<uint32_t *>(xq_out)[slot * dp4 + q] = packed[0];
+                    else
+                        reinterpret_cast<uint2 *>(xq_out)[slot * dp4 + q] = make_uint2(packed[0], packed[1]);
+                }
+            } else if (ok) {
                 if (FP8)
-                    reinterpret_cast<uint32_t *>(xq_out)[slot * dp4 + q] = packed[0];
+                    reinterpret_cast<uint32_t *>(xq_out)[slot * dp4 + q] = 0u;
                 else
-                    reinterpret_cast<uint2 *>(xq_out)[slot * dp4 + q] = make_uint2(packed[0], packed[1]);
-            } else if (FP8) {
-                reinterpret_cast<uint32_t *>(xq_out)[slot * dp4 + q] = 0u;
-            } else {
-                reinterpret_cast<uint2 *>(xq_out)[slot * dp4 + q] = make_uint2(0u, 0u);
+                    reinterpret_cast<uint2 *>(xq_out)[slot * dp4 + q] = make_uint2(0u, 0u);
             }
         }
-        xn2 = warp_sum_f(xn2);
-        ex2 = warp_sum_f(ex2);
-        tn2 = warp_sum_f(tn2);
-        xo2 = warp_sum_f(xo2);
-#pragma unroll
-        for (int off = 16; off >= 1; off >>= 1) amax = fmaxf(amax, __shfl_xor_sync(0xffffffffu, amax, off));
+        xn2 = group_sum_f<LPR>(xn2);
+        ex2 = group_sum_f<LPR>(ex2);
+        tn2 = group_sum_f<LPR>(tn2);
+        xo2 = group_sum_f<LPR>(xo2);
+        amax = group_max_f<LPR>(amax);
         const float up = 1.0f + (float)(d + 64) * 1.1920929e-07f;
         const float xn = __fsqrt_ru(__fmul_ru(xn2, up));
         const float ex =
             __fadd_ru(__fsqrt_ru(__fmul_ru(ex2, up)), __fmul_ru(__fsqrt_ru(__fmul_ru(tn2, up)), 5.9604645e-08f));
         const float xo = __fsqrt_ru(__fmul_ru(xo2, up));
-        if (lane == 0) rowinfo[slot] = make_float4(xn, ex, xo, inv);
-        if (FP8 && lane < 16)
-            xaug[slot * 16 + lane] = lane < 3 ? __float2bfloat16_rn(inv) : __float2bfloat16_rn(0.f);
-        if (xn < INFINITY) xn_hi = fmaxf(xn_hi, xn);  // NaN / inf rows are re-scored in full
-        if (!(xo < INFINITY)) nonfin = 1.f;
-        am_hi = fmaxf(am_hi, amax);
+        if (ok) {
+            if (sl == 0) rowinfo[slot] = make_float4(xn, ex, xo, inv);
+            if (FP8) {
 #pragma unroll
-        for (int i = 0; i < 2; i++) cur[i] = nxt[i];
+                for (int j = sl; j < 16; j += LPR)
+                    xaug[slot * 16 + j] = j < 3 ? __float2bfloat16_rn(inv) : __float2bfloat16_rn(0.f);
+            }
+            if (xn < INFINITY) xn_hi = fmaxf(xn_hi, xn);  // NaN / inf rows are re-scored in full
+            if (!(xo < INFINITY)) nonfin = 1.f;
+            am_hi = fmaxf(am_hi, amax);
+        }
+#pragma unroll
+        for (int i = 0; i < NPL; i++) cur[i] = nxt[i];
     }
+    // the warp's maxima (every lane holds its rows' values)
+    xn_hi = group_max_f<32>(xn_hi);
+    am_hi = group_max_f<32>(am_hi);
     if (lane == 0) {
         sh_xn[w] = xn_hi;
         sh_am[w] = am_hi;
@@ -418,12 +454,20 @@ void launch_prep_rows(Ctx &ctx, const TX *x, int64_t n, int d, int d_pad, const 
                       __nv_bfloat16 *xaug, float4 *rowinfo, MixedStats *stats, const int32_t *list = nullptr,
                       const unsigned long long *count = nullptr) {
     const int64_t pblocks = std::min<int64_t>((n + 7) / 8, (int64_t)ctx.num_sms * 16);
-    if (std::is_same<TX, float>::value && (d & 3) == 0 && d_pad <= 256 && ((uintptr_t)x & 15u) == 0)
-        prep_rows4_kernel<FP8><<<(unsigned)pblocks, 256, 0, ctx.stream>>>(
-            (const float *)x, n, d, d_pad, mu32, xq, xaug, rowinfo, stats, list, count);
-    else
+    if (std::is_same<TX, float>::value && (d & 3) == 0 && d_pad <= 256 && ((uintptr_t)x & 15u) == 0) {
+        // 8 lanes a row up to 128 features (4 rows a warp), else 16 (2 rows a warp)
+        if (d_pad <= 128)
+            prep_rows4_kernel<FP8, 8><<<(unsigned)std::min<int64_t>((n + 31) / 32, (int64_t)ctx.num_sms * 16), 256,
+                                        0, ctx.stream>>>((const float *)x, n, d, d_pad, mu32, xq, xaug, rowinfo,
+                                                         stats, list, count);
+        else
+            prep_rows4_kernel<FP8, 16><<<(unsigned)std::min<int64_t>((n + 15) / 16, (int64_t)ctx.num_sms * 16),
+                                         256, 0, ctx.stream>>>((const float *)x, n, d, d_pad, mu32, xq, xaug, rowinfo,
+                                                               stats, list, count);
+    } else {
         prep_rows_kernel<TX, FP8><<<(unsigned)pblocks, 256, 0, ctx.stream>>>(x, n, d, d_pad, mu32, xq, xaug,
                                                                              rowinfo, stats, list, count);
+    }
     FK_LAUNCH_CHECK();
 }
 

@@ -14,11 +14,13 @@ with the oracle in tests/test_sklearn_wrapper.py."""
 import numpy as np
 import pytest
 
-pytest.importorskip("sklearn")
-from sklearn.utils.estimator_checks import parametrize_with_checks  # noqa: E402
+import ferrolearn_gb300.sklearn as S
+from oracle import oracle as O
 
-import ferrolearn_gb300.sklearn as S  # noqa: E402
-from oracle import oracle as O  # noqa: E402
+try:  # a module-level skip would count as a skipped test in every selection
+    from sklearn.utils.estimator_checks import parametrize_with_checks
+except ImportError:
+    parametrize_with_checks = None
 
 
 def _oracle_fit(x, est):
@@ -42,6 +44,10 @@ def _oracle_in_place_of_the_gpu(monkeypatch):
     monkeypatch.setattr(S, "_transform", _oracle_transform)
 
 
-@parametrize_with_checks([S.KMeans(n_clusters=3, random_state=42, n_init=2)])
-def test_estimator_contract(estimator, check):
-    check(estimator)
+if parametrize_with_checks is not None:
+    @parametrize_with_checks([S.KMeans(n_clusters=3, random_state=42, n_init=2)])
+    def test_estimator_contract(estimator, check):
+        check(estimator)
+else:
+    def test_estimator_contract():
+        pytest.skip("scikit-learn is not installed")
