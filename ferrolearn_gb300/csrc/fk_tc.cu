@@ -105,6 +105,7 @@ template <> struct MergeSlot<false> {
     }
 };
 constexpr uint32_t BAR_BYTES = 256;
+constexpr uint32_t ATOM_RING = 4;  // atom slots of a one-stage ring (d_pad <= 4 atoms)
 constexpr long long WAIT_LIMIT_CYCLES = 4000000000LL;
 
 // Instruction descriptor, kind::f16: D = F32 (bits 4-5 = 1), A = B = BF16
@@ -472,17 +473,21 @@ __global__ void __launch_bounds__(tc_threads(EP), 1)
     const int64_t q = blockIdx.x / p.parts;
     const int64_t tstride = p.ctas_per_part;
 
+    // With one X stage the stage is a ring of its atoms (at most ATOM_RING),
+    // each with its own full / empty barrier: the next tile's first atoms load
+    // while the MMAs still read this tile's last ones.
+    constexpr uint32_t NXB = XST == 1 ? ATOM_RING : XST;  // X barriers of each kind
     const uint32_t bar_c = sb + p.off_bar;
     auto bar_xfull = [&](int s) { return bar_c + 8u * (1u + (uint32_t)s); };
-    auto bar_xempty = [&](int s) { return bar_c + 8u * (1u + XST + (uint32_t)s); };
-    auto bar_afull = [&](int b) { return bar_c + 8u * (1u + 2 * XST + (uint32_t)b); };
-    auto bar_aempty = [&](int b) { return bar_c + 8u * (3u + 2 * XST + (uint32_t)b); };
+    auto bar_xempty = [&](int s) { return bar_c + 8u * (1u + NXB + (uint32_t)s); };
+    auto bar_afull = [&](int b) { return bar_c + 8u * (1u + 2 * NXB + (uint32_t)b); };
+    auto bar_aempty = [&](int b) { return bar_c + 8u * (3u + 2 * NXB + (uint32_t)b); };
     uint32_t *slot = (uint32_t *)(smem + p.off_bar + 128);
     volatile uint32_t *abort_flag = slot + 1;
 
     if (threadIdx.x == 0) {
         mbar_init(bar_c, 1);
-        for (int s = 0; s < XST; s++) {
+        for (int s = 0; s < (XST == 1 ? p.n_atoms : XST); s++) {
             mbar_init(bar_xfull(s), 1);
             mbar_init(bar_xempty(s), 1);
         }
@@ -515,22 +520,43 @@ __global__ void __launch_bounds__(tc_threads(EP), 1)
                                 a * (FP8 ? 128 : 64), crow0 + r);
             for (int r = 0; r < p.kp; r += BN) tma_load_2d(sb + p.off_aug + (uint32_t)r * 32u, &tm_aug, bar_c, 0, crow0 + r);
             if (!FP8) tma_load_2d(sb + p.off_ones, &tm_ones, bar_c, 0, 0);
+            // ring entries: whole tiles (two stages) or single atoms (one stage)
+            const int nring = XST == 1 ? p.n_atoms : XST;
             int it = 0;
-            for (int64_t t = q; t < p.tiles; t += tstride, ++it) {
-                const int s = it % XST;
-                const uint32_t ph = (uint32_t)(it / XST) & 1u;
-                if (!mbar_wait(bar_xempty(s), ph ^ 1u, abort_flag, p.err, 1ull)) break;
-                mbar_expect_tx(bar_xfull(s), p.x_stage_bytes + (FP8 ? XAUG_BYTES : 0u));
-                for (int a = 0; a < p.n_atoms; a++)
-                    tma_load_2d(sb + p.off_x + (uint32_t)s * p.x_stage_bytes + (uint32_t)a * X_ATOM_BYTES, &tm_x,
-                                bar_xfull(s), a * (FP8 ? 128 : 64), (int)(t * BM));
-                if (FP8)
-                    tma_load_2d(sb + p.off_xaug + (uint32_t)s * XAUG_BYTES, &tm_ones, bar_xfull(s), 0, (int)(t * BM));
+            bool stop = false;
+            for (int64_t t = q; t < p.tiles && !stop; t += tstride) {
+                if constexpr (XST == 1) {
+                    for (int a = 0; a < p.n_atoms; a++, ++it) {
+                        const uint32_t ph = (uint32_t)(it / nring) & 1u;  // it % nring == a
+                        if (!mbar_wait(bar_xempty(a), ph ^ 1u, abort_flag, p.err, 1ull)) {
+                            stop = true;
+                            break;
+                        }
+                        // FP8: the tile's augmentation rows ride with its last atom
+                        const bool aug = FP8 && a == p.n_atoms - 1;
+                        mbar_expect_tx(bar_xfull(a), X_ATOM_BYTES + (aug ? XAUG_BYTES : 0u));
+                        tma_load_2d(sb + p.off_x + (uint32_t)a * X_ATOM_BYTES, &tm_x, bar_xfull(a),
+                                    a * (FP8 ? 128 : 64), (int)(t * BM));
+                        if (aug) tma_load_2d(sb + p.off_xaug, &tm_ones, bar_xfull(a), 0, (int)(t * BM));
+                    }
+                } else {
+                    const int s = it % XST;
+                    const uint32_t ph = (uint32_t)(it / XST) & 1u;
+                    if (!mbar_wait(bar_xempty(s), ph ^ 1u, abort_flag, p.err, 1ull)) break;
+                    mbar_expect_tx(bar_xfull(s), p.x_stage_bytes + (FP8 ? XAUG_BYTES : 0u));
+                    for (int a = 0; a < p.n_atoms; a++)
+                        tma_load_2d(sb + p.off_x + (uint32_t)s * p.x_stage_bytes + (uint32_t)a * X_ATOM_BYTES, &tm_x,
+                                    bar_xfull(s), a * (FP8 ? 128 : 64), (int)(t * BM));
+                    if (FP8)
+                        tma_load_2d(sb + p.off_xaug + (uint32_t)s * XAUG_BYTES, &tm_ones, bar_xfull(s), 0,
+                                    (int)(t * BM));
+                    ++it;
+                }
             }
             // Drain: every issued X load must land before the CTA can exit.
             const int issued = it;
-            for (int j = issued > XST ? issued - XST : 0; j < issued; j++)
-                mbar_wait(bar_xfull(j % XST), (uint32_t)(j / XST) & 1u, abort_flag, p.err, 0ull);
+            for (int j = issued > nring ? issued - nring : 0; j < issued; j++)
+                mbar_wait(bar_xfull(j % nring), (uint32_t)(j / nring) & 1u, abort_flag, p.err, 0ull);
             mbar_wait(bar_c, 0u, abort_flag, p.err, 0ull);
         }
     } else if (warp == 1) {
@@ -543,10 +569,13 @@ __global__ void __launch_bounds__(tc_threads(EP), 1)
                 tc_fence_after();
                 bool ok = true;
                 for (int64_t t = q; t < p.tiles && ok; t += tstride, ++it) {
-                    const int s = it % XST;
-                    const uint32_t ph = (uint32_t)(it / XST) & 1u;
-                    if (!mbar_wait(bar_xfull(s), ph, abort_flag, p.err, 4ull)) break;
-                    tc_fence_after();
+                    // one stage: ring entry (it, a) is atom slot a in phase it & 1
+                    const int s = XST == 1 ? 0 : it % XST;
+                    const uint32_t ph = (uint32_t)(XST == 1 ? it : it / XST) & 1u;
+                    if (XST != 1) {
+                        if (!mbar_wait(bar_xfull(s), ph, abort_flag, p.err, 4ull)) break;
+                        tc_fence_after();
+                    }
                     const uint32_t xs = sb + p.off_x + (uint32_t)s * p.x_stage_bytes;
                     for (int b = 0; b < p.nblocks; b++, item++) {
                         const int buf = (int)(item & 1u);
@@ -556,9 +585,17 @@ __global__ void __launch_bounds__(tc_threads(EP), 1)
                             break;
                         }
                         tc_fence_after();
+                        const bool last_b = b == p.nblocks - 1;
                         const uint32_t dt = tmem + (uint32_t)buf * BN;
                         const uint32_t cs = sb + p.off_c + (uint32_t)b * BN * 128u;
                         for (int a = 0; a < p.n_atoms; a++) {
+                            if (XST == 1 && b == 0) {
+                                if (!mbar_wait(bar_xfull(a), ph, abort_flag, p.err, 4ull)) {
+                                    ok = false;
+                                    break;
+                                }
+                                tc_fence_after();
+                            }
 #pragma unroll
                             for (int kk = 0; kk < 4; kk++) {
                                 const uint64_t ad = sdesc(xs + (uint32_t)a * X_ATOM_BYTES + kk * 32u, 1024u, LAYOUT_SW128);
@@ -568,16 +605,31 @@ __global__ void __launch_bounds__(tc_threads(EP), 1)
                                 else
                                     mma_bf16(dt, ad, bd, (a | kk) != 0 ? 1u : 0u);
                             }
+                            // the tile's last block has read this atom: its slot is free
+                            // (FP8: the last atom's slot also holds the augmentation rows)
+                            if (XST == 1 && last_b && !(FP8 && a == p.n_atoms - 1)) {
+                                mma_commit(bar_xempty(a));
+                                last_s = a;
+                                last_ph = ph;
+                            }
                         }
+                        if (!ok) break;
                         const uint32_t aug_a = FP8 ? sb + p.off_xaug + (uint32_t)s * XAUG_BYTES : sb + p.off_ones;
                         mma_bf16(dt, sdesc(aug_a, 256u, LAYOUT_SW32),
                                  sdesc(sb + p.off_aug + (uint32_t)b * BN * 32u, 256u, LAYOUT_SW32), 1u);
+                        if (XST == 1 && FP8 && last_b) {
+                            mma_commit(bar_xempty(p.n_atoms - 1));
+                            last_s = p.n_atoms - 1;
+                            last_ph = ph;
+                        }
                         mma_commit(bar_afull(buf));
                     }
                     if (!ok) break;
-                    mma_commit(bar_xempty(s));
-                    last_s = s;
-                    last_ph = ph;
+                    if (XST != 1) {
+                        mma_commit(bar_xempty(s));
+                        last_s = s;
+                        last_ph = ph;
+                    }
                 }
             }
             // Drain: the last commit covers every MMA issued before it.
@@ -1012,6 +1064,10 @@ void plan_shape(MixedPlan &mp, int64_t n, int d, int k, bool fp8, int topk, int 
             fail(FK_ERR_UNSUPPORTED);
         }
         mp.xst = xst;
+        if (xst == 1 && n_atoms > (int)ATOM_RING) {
+            set_error("one-stage tensor-core plan with %d atoms (the ring holds %u)", n_atoms, ATOM_RING);
+            fail(FK_ERR_UNSUPPORTED);
+        }
         const int kp_max = kp_fixed > 0 ? kp_fixed : (int)((SMEM_LIMIT - fixed) / per_centre) / BN * BN;
         mp.parts = (k + kp_max - 1) / kp_max;
         mp.kp = ((k + mp.parts - 1) / mp.parts + BN - 1) / BN * BN;

@@ -248,9 +248,13 @@ def test_fixed_point_sums_handle_extremes(precision):
 
 
 @pytest.mark.parametrize("precision", [F.MIXED_BF16, F.MIXED_FP8])
-def test_mixed_predict_matches_oracle(precision):
-    x32, cen = _aniso(6000, 128, 500, seed=3)
-    fitted = F.FittedKMeans(cen.astype(np.float64), np.zeros(6000, dtype=np.int64), 0.0, 0, "f32x64",
+@pytest.mark.parametrize("n,d,k", [(6000, 128, 500), (40000, 256, 600)])
+def test_mixed_predict_matches_oracle(precision, n, d, k):
+    # (40000, 256, 600): BF16 at d = 256 runs its one X stage as a ring of four
+    # atom slots; 313 tiles over 50 CTAs a centre slice take every slot through
+    # both barrier phases several times
+    x32, cen = _aniso(n, d, k, seed=3)
+    fitted = F.FittedKMeans(cen.astype(np.float64), np.zeros(n, dtype=np.int64), 0.0, 0, "f32x64",
                             precision=precision)
     assert np.array_equal(fitted.predict(x32), O.predict(cen, x32.astype(np.float64)))
 
