@@ -4,9 +4,12 @@
 // memory, 512 TMEM columns). The centres are cut into `parts` slices of kp
 // centres; CTA (slice p, index q) keeps its slice resident in shared memory
 // for the whole launch and streams the row tiles q, q+Q, q+2Q, ... of X
-// through a TMA ring of one or two stages, so X is read once per slice (the
-// other slices' CTAs find it in L2) and the n x k score matrix never leaves
-// the SM.
+// through a TMA ring -- two whole-tile stages where they fit beside the
+// slice, else one stage used as a ring of its 16 KB atoms with a full /
+// empty mbarrier each, so the next tile's first atoms load while the MMAs
+// read this tile's last ones -- so X is read once per slice (the other
+// slices' CTAs find it in L2) and the n x k score matrix never leaves the
+// SM.
 //
 //   warp 0   TMA producer: the resident slice once, then 128-row X tiles
 //            (cp.async.bulk.tensor, 128-byte swizzle, mbarrier complete_tx);
@@ -1042,7 +1045,8 @@ void plan_shape(MixedPlan &mp, int64_t n, int d, int k, bool fp8, int topk, int 
     const int n_atoms = mp.d_pad / per_atom;
     const size_t x_stage = (size_t)n_atoms * X_ATOM_BYTES;
     const size_t per_centre = (size_t)n_atoms * 128 + 32;
-    // two X stages when 256 resident centres still fit, else one
+    // two X stages when 256 resident centres still fit, else one (run as a
+    // ring of its atoms)
     // Two epilogue parts per lane quarter (8 epilogue warps, three merge
     // slots). The kernel also takes four (16 warps, 64 columns each, two
     // slots when a tile has two blocks or more), measured slower at n = 4M,
