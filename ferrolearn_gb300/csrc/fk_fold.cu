@@ -21,9 +21,11 @@
 // around the chunk's estimated starting sum (the f64 prefix of the chunk sums
 // -- it steers speed, never the result); fold_walk_kernel walks each chain
 // with one warp: 32 chunk maps scanned at a time, a chunk whose map does not
-// apply walked by its 32-value groups (their maps recomputed for the sum's
-// current sign and binade), a group whose map does not apply walked value by
-// value, with one exact F addition where the sign or the binade changes.
+// apply walked by its 32-value groups (its values staged in shared memory,
+// the groups' maps recomputed for the sum's current sign and binade), a group
+// whose map does not apply walked value by value, with one exact F addition
+// where the sign or the binade changes (and, after a second change within 32
+// values, exact additions for the rest of them).
 //
 // A chain is a strided array with an optional mask: chain c folds
 // base[i * stride] over i in [0, m) in order, skipping i where
@@ -205,13 +207,18 @@ __device__ __forceinline__ bool takes(const Chain<T> &c, int64_t i) {
 }
 
 // Up to 32 values (lane i holds value i, `live` marks the chain's values,
-// len values in all) added to p in order, exactly as the sequential fold.
+// len values in all) added to p in order, exactly as the sequential fold:
+// the values' maps for p's sign and binade scanned at once, one exact F
+// addition where the sum leaves them, one more scan for the rest; a sum that
+// leaves its binade twice in 32 values (a fold near zero, where the binade
+// changes every few values) takes the rest one exact addition at a time,
+// which costs less than a scan per change.
 template <typename T>
 __device__ T walk_values(T p, T v, bool live, int len) {
     using B = FB<T>;
     const int lane = threadIdx.x & 31;
     int start = 0;
-    while (start < len) {
+    for (int scans = 0; scans < 2 && start < len; scans++) {
         const unsigned rest = __ballot_sync(0xffffffffu, live && lane >= start && lane < len);
         if (!rest) return p;
         start = __ffs(rest) - 1;  // the next value of the chain
@@ -238,6 +245,9 @@ __device__ T walk_values(T p, T v, bool live, int len) {
         p = B::add(p, __shfl_sync(0xffffffffu, v, f0));  // the one exact addition there
         start = f0 + 1;
     }
+    // the rest in order, one exact addition each
+    for (unsigned rest = __ballot_sync(0xffffffffu, live && lane >= start && lane < len); rest; rest &= rest - 1u)
+        p = B::add(p, __shfl_sync(0xffffffffu, v, __ffs(rest) - 1));
     return p;
 }
 
@@ -337,22 +347,33 @@ __global__ void __launch_bounds__(FWARPS * 32)
     }
 }
 
-// One chunk (values [lo, lo + len) of the chain) added to p exactly: the 32
-// groups' maps for p's current sign and binade scanned at once, a group
-// whose map does not apply walked value by value.
+// One chunk (values [lo, lo + len) of the chain) added to p exactly: the
+// chunk's values and take flags staged in shared memory (independent loads,
+// issued together), the 32 groups' maps for p's current sign and binade
+// scanned at once, a group whose map does not apply walked value by value.
 template <typename T>
-__device__ T walk_chunk_values(T p, const Chain<T> &ch, int64_t lo, int len) {
+__device__ T walk_chunk_values(T p, const Chain<T> &ch, int64_t lo, int len, T *__restrict__ sv,
+                               uint8_t *__restrict__ sm) {
     const int lane = threadIdx.x & 31;
     const int ng = (len + 31) / 32;
+#pragma unroll 8
+    for (int q = 0; q < 32; q++) {
+        const int i = q * 32 + lane;
+        if (i < len) {
+            sv[i] = ch.base[(lo + i) * ch.stride];
+            sm[i] = takes(ch, lo + i) ? 1 : 0;
+        }
+    }
+    __syncwarp();
     int start = 0;
     while (start < ng) {
         int s, be;
         long long P;
         if (!split(p, s, be, P)) {
             // no binade: the next group value by value
-            const int64_t i = lo + (int64_t)start * 32 + lane;
-            const bool live = lane < min(32, len - start * 32) && takes(ch, i);
-            const T v = live ? ch.base[i * ch.stride] : T(0);
+            const int i = start * 32 + lane;
+            const bool live = lane < min(32, len - start * 32) && sm[i];
+            const T v = live ? sv[i] : T(0);
             p = walk_values<T>(p, v, live, 32);
             start++;
             continue;
@@ -360,23 +381,24 @@ __device__ T walk_chunk_values(T p, const Chain<T> &ch, int64_t lo, int len) {
         // this lane's group map for the current sign and binade
         SMap g = smap_ident();
         if (lane >= start && lane < ng) {
-            const int64_t g0 = lo + (int64_t)lane * 32;
+            const int g0 = lane * 32;
             const int gl = min(32, len - lane * 32);
             for (int q = 0; q < gl; q++)
-                if (takes(ch, g0 + q)) g = smap_compose(g, smap_of(ch.base[(g0 + q) * ch.stride], be, s));
+                if (sm[g0 + q]) g = smap_compose(g, smap_of(sv[g0 + q], be, s));
         }
         const SMap sc = scan_smap(g);
         const long long Pl = smap_apply<T>(P, sc);
         const unsigned badm = __ballot_sync(0xffffffffu, lane >= start && lane < ng && Pl < 0);
         const int f0 = badm ? __ffs(badm) - 1 : ng;
         if (f0 > start) p = join<T>(s, be, (long long)__shfl_sync(0xffffffffu, (unsigned long long)Pl, f0 - 1));
-        if (f0 >= ng) return p;
-        const int64_t i = lo + (int64_t)f0 * 32 + lane;
-        const bool live = lane < min(32, len - f0 * 32) && takes(ch, i);
-        const T v = live ? ch.base[i * ch.stride] : T(0);
+        if (f0 >= ng) break;
+        const int i = f0 * 32 + lane;
+        const bool live = lane < min(32, len - f0 * 32) && sm[i];
+        const T v = live ? sv[i] : T(0);
         p = walk_values<T>(p, v, live, 32);
         start = f0 + 1;
     }
+    __syncwarp();  // the staging area is refilled by the next slow chunk
     return p;
 }
 
@@ -386,6 +408,8 @@ __global__ void __launch_bounds__(32)
     fold_walk_kernel(const Chain<T> *__restrict__ chains, int nchains, int64_t m, const int *__restrict__ active,
                      int64_t nch, const CMap *__restrict__ cmaps, const int32_t *__restrict__ ccnt,
                      T *__restrict__ result, long long *__restrict__ count) {
+    __shared__ T stage_v[FCH];
+    __shared__ uint8_t stage_m[FCH];
     const int c = blockIdx.x;
     const int lane = threadIdx.x;
     const Chain<T> ch = chains[c];
@@ -424,7 +448,7 @@ __global__ void __launch_bounds__(32)
                 p = join<T>(s, be, (long long)__shfl_sync(0xffffffffu, (unsigned long long)Pl, f0 - 1));
             if (f0 >= nb) break;
             const int64_t lo = (jb + f0) * FCH;
-            p = walk_chunk_values<T>(p, ch, lo, (int)min((int64_t)FCH, m - lo));
+            p = walk_chunk_values<T>(p, ch, lo, (int)min((int64_t)FCH, m - lo), stage_v, stage_m);
             start = f0 + 1;
         }
     }
