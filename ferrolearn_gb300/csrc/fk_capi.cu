@@ -292,7 +292,10 @@ void lloyd_iteration(Ctx &ctx, const TX *x, int64_t n, int d, const TC *c, int k
         if (prec == FK_PRECISION_PLAIN) {
             TC *mind = (TC *)ctx.get(BUF_MIND, sizeof(TC) * (size_t)n);
             double *part = (double *)ctx.get(BUF_PARTIAL, sizeof(double) * (size_t)sum_fixed_partials(n));
-            launch_assign_direct<TX, TC>(x, n, d, c, k, labels, mind, s);
+            if constexpr (std::is_same<TX, double>::value && std::is_same<TC, double>::value)
+                launch_assign_f64_filtered(ctx, x, n, d, c, k, labels, mind, x_changed);
+            else
+                launch_assign_direct<TX, TC>(x, n, d, c, k, labels, mind, s);
             launch_sum_fixed<TC>(mind, n, part, &sc->inertia, s);
         } else {
             if constexpr (std::is_same<TX, float>::value && std::is_same<TC, double>::value) {
@@ -715,7 +718,10 @@ fk_status predict_impl(fk_ctx *ctxp, const TC *c_in, int64_t k, int64_t d_fit, c
     const TC *c = stage_in<TC>(ctx, BUF_C0, c_in, (size_t)k * d);
     int32_t *labels = (int32_t *)ctx.get(BUF_LABELS, sizeof(int32_t) * (size_t)n);
     if (prec == FK_PRECISION_PLAIN) {
-        launch_assign_direct<TX, TC>(x, n, (int)d, c, (int)k, labels, nullptr, s);
+        if constexpr (std::is_same<TX, double>::value && std::is_same<TC, double>::value)
+            launch_assign_f64_filtered(ctx, x, n, (int)d, c, (int)k, labels, nullptr, true);
+        else
+            launch_assign_direct<TX, TC>(x, n, (int)d, c, (int)k, labels, nullptr, s);
     } else {
         if constexpr (std::is_same<TX, float>::value && std::is_same<TC, double>::value) {
             DevScalars *sc = (DevScalars *)ctx.get(BUF_SCALARS, sizeof(DevScalars));
@@ -988,7 +994,10 @@ fk_status minibatch_impl(fk_ctx *ctxp, const T *x_in, int64_t n, int64_t d, cons
         }
         // assign_clusters_mb (:343-376) over every row: the run's labels and inertia
         FK_CUDA(cudaMemsetAsync(sc, 0, sizeof(DevScalars), s));
-        launch_assign_direct<T, T>(x, n, (int)d, c, (int)k, labels, mind, s);
+        if constexpr (std::is_same<T, double>::value)
+            launch_assign_f64_filtered(ctx, x, n, (int)d, c, (int)k, labels, mind, true);
+        else
+            launch_assign_direct<T, T>(x, n, (int)d, c, (int)k, labels, mind, s);
         launch_sum_fixed<T>(mind, n, part, &sc->inertia, s);
         read_scalars(ctx, sc);
         const T inertia = (T)ctx.host_scalars->inertia;

@@ -159,6 +159,7 @@ enum BufSlot {
     BUF_FOLD_MAP, BUF_MASKS, BUF_THRESH, BUF_FLOORS, BUF_SHIFT, BUF_THMAIN, BUF_TH2, BUF_CNT2, BUF_LIST3,
     BUF_SLOT3, BUF_TH3, BUF_XB3,
     BUF_BX, BUF_BFITS, BUF_BSTATE, BUF_BITEMS, BUF_BPART, BUF_BORDER, BUF_BCTR, BUF_BLAB, BUF_BMEM, BUF_BCEN, BUF_BND, BUF_BXOFF,
+    BUF_PF_X32, BUF_PF_XERR, BUF_PF_C32, BUF_PF_CERR, BUF_PF_LIST, BUF_PF_CNT,
     BUF_COUNT
 };
 
@@ -269,6 +270,23 @@ void launch_assign_direct(const TX *x, int64_t n, int d, const TC *c, int k, int
 // The assignment with the centres split over `splits` CTA columns (for row
 // counts too small to fill the GPU), then an ordered combine: the same labels
 // and minima as launch_assign_direct. Scratch: splits x n of each.
+// Upper bound, in f32 with upward rounding, of |d32 - D| + |D64 - D| where D
+// is the exact real distance and D64 the oracle's FP64 direct form:
+// ((d+4) 2^-23 d32 + 2 sqrt(d32) ec + 3 ec^2) * 1.01. 2 sqrt(d32) is bounded
+// by d32 / s + s >= 2 sqrt(d32) (any s > 0; with s the power of two 2^(E/2),
+// 2^E <= d32, it exceeds 2 sqrt(d32) by at most 25%): two directed-rounding
+// operations instead of a correctly rounded square root.
+__device__ __forceinline__ float bound32(float d32, float ec, int d) {
+    const float dd = d32 > 0.f ? d32 : 0.f;
+    const int h = ((int)((__float_as_uint(dd) >> 23) & 0xFFu) - 127) >> 1;  // floor(E / 2), -64..64
+    const float sq2 = dd > 0.f ? __fadd_ru(__fmul_ru(dd, __int_as_float((127 - h) << 23)), __int_as_float((h + 127) << 23))
+                               : 0.f;
+    float e = __fmul_ru((float)(d + 4) * 1.1920929e-07f, dd);
+    e = __fadd_ru(e, __fmul_ru(sq2, ec));
+    e = __fadd_ru(e, __fmul_ru(3.0f, __fmul_ru(ec, ec)));
+    return __fadd_ru(__fmul_ru(e, 1.01f), 1e-30f);
+}
+
 int assign_splits(int64_t n, int k, int num_sms);
 template <typename TX, typename TC>
 void launch_assign_direct_split(const TX *x, int64_t n, int d, const TC *c, int k, int32_t *labels, TC *mind,
@@ -276,6 +294,14 @@ void launch_assign_direct_split(const TX *x, int64_t n, int d, const TC *c, int 
 template <typename T>
 void launch_transform_direct(const T *x, int64_t n, int d, const T *c, int k, T *out,
                              cudaStream_t s);
+// The plain f64 assignment (labels, and mind when set: the FP64 direct form to
+// the label, F::MAX for a row with no distance below it) -- the outputs of
+// launch_assign_direct<double, double> -- through an FP32 pass with rigorous
+// bounds (fk_prefilter.cu): FP64 only for the rows it cannot decide and for
+// each row's distance to its label. fresh_x: X changed since the last call
+// (its f32 copy is rebuilt).
+void launch_assign_f64_filtered(Ctx &ctx, const double *x, int64_t n, int d, const double *c, int k,
+                                int32_t *labels, double *mind, bool fresh_x);
 // Deterministic fixed-order sum of v[0..n) in double into *out.
 template <typename T>
 void launch_sum_fixed(const T *v, int64_t n, double *partial, double *out, cudaStream_t s);

@@ -1045,23 +1045,6 @@ __device__ __forceinline__ bool near_tie(double a, double b) {
     return fabs(a - b) <= 1e-12 * lo;
 }
 
-// Upper bound, in f32 with upward rounding, of |d32 - D| + |D64 - D| where D
-// is the exact real distance and D64 the oracle's FP64 direct form:
-// ((d+4) 2^-23 d32 + 2 sqrt(d32) ec + 3 ec^2) * 1.01. 2 sqrt(d32) is bounded
-// by d32 / s + s >= 2 sqrt(d32) (any s > 0; with s the power of two 2^(E/2),
-// 2^E <= d32, it exceeds 2 sqrt(d32) by at most 25%): two directed-rounding
-// operations instead of a correctly rounded square root.
-__device__ __forceinline__ float bound32(float d32, float ec, int d) {
-    const float dd = d32 > 0.f ? d32 : 0.f;
-    const int h = ((int)((__float_as_uint(dd) >> 23) & 0xFFu) - 127) >> 1;  // floor(E / 2), -64..64
-    const float sq2 = dd > 0.f ? __fadd_ru(__fmul_ru(dd, __int_as_float((127 - h) << 23)), __int_as_float((h + 127) << 23))
-                               : 0.f;
-    float e = __fmul_ru((float)(d + 4) * 1.1920929e-07f, dd);
-    e = __fadd_ru(e, __fmul_ru(sq2, ec));
-    e = __fadd_ru(e, __fmul_ru(3.0f, __fmul_ru(ec, ec)));
-    return __fadd_ru(__fmul_ru(e, 1.01f), 1e-30f);
-}
-
 // a certainly below b (false for any NaN or infinity)
 __device__ __forceinline__ bool below(float da, float ea, float db, float eb) {
     return __fadd_ru(da, ea) < __fsub_rd(db, eb);

@@ -219,65 +219,73 @@ __global__ void centroid_sum_kernel(const TX *__restrict__ x, int d, int k, int6
     }
 }
 
-// Plain f32 update (KMeans<f32>): the same row-order f32 chain per (cluster,
-// feature), but fed from shared memory. A block takes one cluster and a slab
-// of 32 features; all its threads load a page of CH_PAGE member rows (two
-// rows a thread, the slab's features contiguous, 16-byte loads when the rows
-// allow) while warp 0 adds the previous page from shared memory, one lane per
-// feature. One warp loading for itself keeps a few dozen rows in flight and
-// a long chain waits on memory; here the block's loads set the pace and the
-// chain runs at the dependent-add rate. Rows are padded to 33 floats in
-// shared memory so that neither the row-wise stores nor the column-wise
-// reads conflict in a bank.
+// Plain update (KMeans<f32> and KMeans<f64>): the same row-order chain in F
+// per (cluster, feature), but fed from shared memory. A block takes one
+// cluster and a slab of 32 features; all its threads load a page of member
+// rows (two rows a thread for f32, one for f64; the slab's features
+// contiguous, 16-byte loads when the rows allow) while warp 0 adds the
+// previous page from shared memory, one lane per feature. One warp loading
+// for itself keeps a few dozen rows in flight and a long chain waits on
+// memory; here the block's loads set the pace and the chain runs at the
+// dependent-add rate. Rows are padded to 33 values in shared memory so that
+// neither the row-wise stores nor the column-wise reads conflict in a bank.
 constexpr int CH_THREADS = 256;
-constexpr int CH_PAGE = 512;  // rows per page: two per thread
-constexpr int CH_SW = 32;     // features per block
+constexpr int CH_SW = 32;  // features per block
 constexpr int CH_PITCH = CH_SW + 1;
-size_t chain_smem_bytes() { return sizeof(float) * (size_t)CH_PAGE * CH_PITCH; }
+template <typename T> struct ChainPage { static constexpr int rows = 512; };  // two rows a thread
+template <> struct ChainPage<double> { static constexpr int rows = 256; };    // one: the registers
+template <typename T>
+size_t chain_smem_bytes() { return sizeof(T) * (size_t)ChainPage<T>::rows * CH_PITCH; }
 
+template <typename T>
 __global__ void __launch_bounds__(CH_THREADS)
-    centroid_chain_f32_kernel(const float *__restrict__ x, int d, int k, int64_t n,
-                              const int32_t *__restrict__ members, const int32_t *__restrict__ offs, int64_t nseg,
-                              const float *__restrict__ old_c, float *__restrict__ new_c) {
-    extern __shared__ float ch_page[];
+    centroid_chain_kernel(const T *__restrict__ x, int d, int k, int64_t n, const int32_t *__restrict__ members,
+                          const int32_t *__restrict__ offs, int64_t nseg, const T *__restrict__ old_c,
+                          T *__restrict__ new_c) {
+    using A = UArith<T>;
+    constexpr int PAGE = ChainPage<T>::rows;
+    constexpr int RPT = PAGE / CH_THREADS;      // rows a thread
+    constexpr int VW = 16 / (int)sizeof(T);     // values per 16-byte load
+    extern __shared__ __align__(16) unsigned char ch_raw[];
+    T *ch_page = reinterpret_cast<T *>(ch_raw);
     const int c = blockIdx.x;
     const int j0 = blockIdx.y * CH_SW;
     const int sw = min(CH_SW, d - j0);
     const int lane = threadIdx.x & 31;
     const int64_t start = offs[(int64_t)c * nseg];
     const int64_t end = (c + 1 < k) ? (int64_t)offs[(int64_t)(c + 1) * nseg] : n;
-    const bool vec = sw == CH_SW && (d & 3) == 0 && (((uintptr_t)x) & 15u) == 0;  // j0 is a multiple of 32
-    float v[2][CH_SW];
+    // j0 is a multiple of 32: the slab starts on a 16-byte boundary when the rows do
+    const bool vec = sw == CH_SW && (d % VW) == 0 && (((uintptr_t)x) & 15u) == 0;
+    T v[RPT][CH_SW];
     auto load_page = [&](int64_t base) {
 #pragma unroll
-        for (int h = 0; h < 2; h++) {
+        for (int h = 0; h < RPT; h++) {
             const int64_t r = base + threadIdx.x + h * CH_THREADS;
             if (r < end) {
-                const float *row = x + (int64_t)members[r] * d + j0;
+                const T *row = x + (int64_t)members[r] * d + j0;
                 if (vec) {
 #pragma unroll
-                    for (int q = 0; q < CH_SW / 4; q++) {
-                        const float4 f = reinterpret_cast<const float4 *>(row)[q];
-                        v[h][4 * q] = f.x;
-                        v[h][4 * q + 1] = f.y;
-                        v[h][4 * q + 2] = f.z;
-                        v[h][4 * q + 3] = f.w;
+                    for (int q = 0; q < CH_SW / VW; q++) {
+                        const uint4 u = reinterpret_cast<const uint4 *>(row)[q];
+                        const T *e = reinterpret_cast<const T *>(&u);
+#pragma unroll
+                        for (int t = 0; t < VW; t++) v[h][VW * q + t] = e[t];
                     }
                 } else {
 #pragma unroll
-                    for (int f = 0; f < CH_SW; f++) v[h][f] = f < sw ? row[f] : 0.f;
+                    for (int f = 0; f < CH_SW; f++) v[h][f] = f < sw ? row[f] : T(0);
                 }
             }
         }
     };
-    float s = 0.f;
+    T s = T(0);
     int64_t base = start;
     if (base < end) load_page(base);
     while (base < end) {
-        const int cnt = (int)min((int64_t)CH_PAGE, end - base);
+        const int cnt = (int)min((int64_t)PAGE, end - base);
         __syncthreads();  // the previous page has been added
 #pragma unroll
-        for (int h = 0; h < 2; h++) {
+        for (int h = 0; h < RPT; h++) {
             const int r = threadIdx.x + h * CH_THREADS;
             if (r < cnt) {
 #pragma unroll
@@ -285,19 +293,19 @@ __global__ void __launch_bounds__(CH_THREADS)
             }
         }
         __syncthreads();
-        const int64_t next = base + CH_PAGE;
+        const int64_t next = base + PAGE;
         if (next < end) load_page(next);  // in flight while warp 0 adds this page
         if (threadIdx.x < 32 && lane < sw) {
-            const float *col = ch_page + lane;
+            const T *col = ch_page + lane;
 #pragma unroll 8
-            for (int r = 0; r < cnt; r++) s = __fadd_rn(s, col[r * CH_PITCH]);
+            for (int r = 0; r < cnt; r++) s = A::add(s, col[r * CH_PITCH]);
         }
         base = next;
     }
     if (threadIdx.x < 32 && lane < sw) {
         const int64_t cntc = end - start;
         const int64_t o = (int64_t)c * d + j0 + lane;
-        new_c[o] = cntc > 0 ? __fdiv_rn(s, (float)cntc) : old_c[o];
+        new_c[o] = cntc > 0 ? A::div(s, (T)cntc) : old_c[o];
     }
 }
 
@@ -1474,13 +1482,13 @@ void launch_update_centroids(const SortPlan &p, const TX *x, int d, const int32_
                              cudaStream_t s, double *inertia_part) {
     FK_CUDA(cudaMemsetAsync(&scalars->shift_bits, 0, sizeof(unsigned long long), s));
     if (d == 0 || p.k == 0) return;
-    if constexpr (std::is_same<TX, float>::value && std::is_same<TC, float>::value) {
+    if constexpr (std::is_same<TX, TC>::value) {
         if (!inertia_part) {
-            const size_t smem = chain_smem_bytes();
-            FK_CUDA(cudaFuncSetAttribute((const void *)centroid_chain_f32_kernel,
+            const size_t smem = chain_smem_bytes<TC>();
+            FK_CUDA(cudaFuncSetAttribute((const void *)centroid_chain_kernel<TC>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
             dim3 g((unsigned)p.k, (unsigned)((d + CH_SW - 1) / CH_SW));
-            centroid_chain_f32_kernel<<<g, CH_THREADS, smem, s>>>(x, d, p.k, p.n, members, seg_hist, p.nseg, old_c,
+            centroid_chain_kernel<TC><<<g, CH_THREADS, smem, s>>>(x, d, p.k, p.n, members, seg_hist, p.nseg, old_c,
                                                                  new_c);
             FK_LAUNCH_CHECK();
             launch_max_shift<TC>(new_c, old_c, p.k, d, &scalars->shift_bits, s);
