@@ -29,7 +29,8 @@ so every iteration runs. A step is one Lloyd iteration over all n rows
           fp8   = FK_PRECISION_MIXED_FP8, the same with an E4M3 contraction
                   (per-row power-of-two scales).
           fp32  = plain KMeans<f32> (direct-form FP32 on CUDA cores).
-          fp64  = plain KMeans<f64> on the widened X.
+          fp64  = plain KMeans<f64> on f64 data (the dirichlet workload drawn
+                  in f64; k-means++ in f64).
 
 Other workloads (--workload; parity cases of the same path, measured on
 request): bisector = n=8,000,000 d=256 k=4096 with 10% bisector rows, FP8,
@@ -246,7 +247,7 @@ def make_workload(args):
     if args.workload == "bisector":
         return W.bisector_4096x256(scale=args.scale)
     if args.workload == "dirichlet":
-        return W.dirichlet_256x64(scale=args.scale, dtype=np.float32)
+        return W.dirichlet_256x64(scale=args.scale, dtype=np.float64 if args.form == "fp64" else np.float32)
     return W.anisotropic_1024x128(scale=args.scale)
 
 
@@ -256,7 +257,8 @@ DEFAULT_FORM = {"anisotropic": "bf16", "bisector": "fp8", "dirichlet": "fp32", "
 def workload_config(w):
     """The `config` of both arms' JSON lines (the workload, not the arm)."""
     n, d = w["x"].shape
-    return {"workload": w["name"], "n": int(n), "d": int(d), "k": int(w["k"]), "X": "f32",
+    return {"workload": w["name"], "n": int(n), "d": int(d), "k": int(w["k"]),
+            "X": "f64" if w["x"].dtype == np.float64 else "f32",
             "init": "first k rows of a seeded permutation" if w.get("init") is not None or w["name"] != "dirichlet_256x64"
             else "k-means++ (seeded)",
             "tol": 0.0, "l2": f"inputs larger than L2 (X {w['x'].nbytes / 1e9:.2f} GB)", "parallelism": "replicas"}
@@ -272,7 +274,8 @@ def initial_centres(w, xd, ctx):
     import ferrolearn_gb300 as F
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    c, _ = F.kmeans_plus_plus(xd, w["k"], seed=w.get("seed", 0), dtype="f32", ctx=ctx)
+    c, _ = F.kmeans_plus_plus(xd, w["k"], seed=w.get("seed", 0),
+                              dtype="f64" if w["x"].dtype == np.float64 else "f32", ctx=ctx)
     ms = (time.perf_counter() - t0) * 1e3
     w["init"] = c.astype(np.float64)
     return w["init"], ms
@@ -779,11 +782,11 @@ def run_ours(args):
     ctx = F.Context(dev, stream=stream.cuda_stream)
 
     if form == "fp64":
-        xd = torch.from_numpy(x32).to(dev).double()
+        xd = torch.from_numpy(np.ascontiguousarray(x32, dtype=np.float64)).to(dev)
     else:
         xd = torch.from_numpy(x32).to(dev)
     torch.cuda.synchronize()
-    init, kpp_ms = initial_centres(w, xd if form != "fp64" else torch.from_numpy(x32).to(dev), ctx)
+    init, kpp_ms = initial_centres(w, xd, ctx)
 
     def build_model(max_iter):
         if form == "fp32":
@@ -960,7 +963,7 @@ def run_ours(args):
     # cluster (2 m (d sizeof(X) + 8)) and rewrites the exact state and means
     # (40 k d)
     upd_ms = rep["ms_update"] / iters
-    xb = x32.itemsize * (2 if form == "fp64" else 1)
+    xb = 8 if form == "fp64" else x32.itemsize
     n_inc = int(rep["updates_incremental"])
     full_bytes = n * d * xb + 4 * n + 16 * k * d
     inc_bytes_total = n_inc * (8 * n + 40 * k * d) + 2 * int(rep["rows_moved"]) * (d * xb + 8)

@@ -302,6 +302,9 @@ void launch_transform_direct(const T *x, int64_t n, int d, const T *c, int k, T 
 // (its f32 copy is rebuilt).
 void launch_assign_f64_filtered(Ctx &ctx, const double *x, int64_t n, int d, const double *c, int k,
                                 int32_t *labels, double *mind, bool fresh_x);
+// f32 copies of f64 rows and an upper bound of the norm of each row's
+// rounding error (the inputs of the FP32 bounds).
+void launch_f32_copy(Ctx &ctx, const double *x, int64_t n, int d, float *x32, float *err);
 // Deterministic fixed-order sum of v[0..n) in double into *out.
 template <typename T>
 void launch_sum_fixed(const T *v, int64_t n, double *partial, double *out, cudaStream_t s);

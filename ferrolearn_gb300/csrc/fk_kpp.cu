@@ -501,6 +501,170 @@ __global__ void __launch_bounds__(KPP_THREADS)
     }
 }
 
+// The direct form in FP64, in the reference's order (the loads run ahead of
+// the dependent adds).
+__device__ __forceinline__ double sqeuc_f64(const double *__restrict__ a, const double *__restrict__ b, int d) {
+    double v = 0.0;
+#pragma unroll 8
+    for (int j = 0; j < d; j++) {
+        const double df = __dsub_rn(a[j], b[j]);
+        v = __dadd_rn(v, __dmul_rn(df, df));
+    }
+    return v;
+}
+
+constexpr int KPP_OPEN = 2048;  // listed open pairs a chunk (row within the chunk << 4 | trial)
+static_assert(KPP_CH <= 4096, "a chunk row fits the list entry's 12 bits");
+
+// The f64 trial pass through FP32 bounds: the same outputs as
+// kpp_trials_kernel<double, TT, false>, bit for bit. The distances are first
+// formed in FP32 from the rows' f32 copies (t = x - c, fma), with the
+// rigorous bound b = bound32(d32, e_row + e_candidate, d) of their distance
+// from the exact distance and from the FP64 direct form. Where d32 - b (down)
+// exceeds the row's current D^2 value m, the FP64 distance v is larger too and
+// min(v, m) is m (kmeans.rs:230-232); only the other (row, trial) pairs --
+// rows the candidate may come closer to, non-finite values, values beyond the
+// f32 range -- form v with the direct form in FP64, in the reference's order.
+template <int TT>
+__global__ void __launch_bounds__(KPP_THREADS)
+    kpp_trials_f64f_kernel(const double *__restrict__ x, const float *__restrict__ x32,
+                           const float *__restrict__ xerr, long long n, int d, double *__restrict__ chains,
+                           int tstride, const KppState *__restrict__ st, int ntr, double *__restrict__ csum,
+                           long long nch) {
+    if (st->direct) return;
+    constexpr int DJ = TrialTile<float>::DJ;
+    constexpr int XS = KPP_CH + KPP_PAD;  // row length of the staged tile
+    extern __shared__ __align__(16) unsigned char kpp_smem[];
+    constexpr int STAGE = DJ * XS + DJ * TT;  // elements of one stage
+    float *const stages = reinterpret_cast<float *>(kpp_smem);
+    __shared__ long long cand[TT];
+    __shared__ float cerr[TT];
+    __shared__ double red[TT][KPP_THREADS / 32];
+    __shared__ double open_sum[TT];
+    __shared__ unsigned short open_pairs[KPP_OPEN];
+    __shared__ int open_n;
+    const int tid = threadIdx.x;
+    if (tid < TT) {
+        cand[tid] = tid < ntr ? st->cand[tid] : 0;
+        cerr[tid] = tid < ntr ? xerr[st->cand[tid]] : 0.f;
+        open_sum[tid] = 0.0;
+    }
+    if (tid == 0) open_n = 0;
+    const int cur = st->cur, cur_trial = st->cur_trial, wbuf = 1 - cur;
+    const double *mind = chains + ((long long)cur * tstride + cur_trial) * n;
+    double *out = chains + (long long)wbuf * tstride * n;
+    const long long base = (long long)blockIdx.x * KPP_CH;
+    float acc[4][TT];
+#pragma unroll
+    for (int a = 0; a < 4; a++)
+#pragma unroll
+        for (int b = 0; b < TT; b++) acc[a][b] = 0.f;
+    __syncthreads();  // cand, cerr
+    auto stage_round = [&](int j0, int q) {
+        float *xs = stages + q * STAGE;
+        float *cs = xs + DJ * XS;
+        const int jn = min(DJ, d - j0);
+        for (int e = tid; e < KPP_CH * DJ; e += KPP_THREADS) {
+            const int r = e / DJ, jj = e - r * DJ;
+            const long long gr = base + r;
+            const bool ok = gr < n && jj < jn;
+            cp_async_elem(xs + jj * XS + r, ok ? x32 + gr * d + j0 + jj : x32, ok);
+        }
+        for (int e = tid; e < TT * DJ; e += KPP_THREADS) {
+            const int t = e / DJ, jj = e - t * DJ;
+            const bool ok = t < ntr && jj < jn;
+            cp_async_elem(cs + jj * TT + t, ok ? x32 + cand[t] * d + j0 + jj : x32, ok);
+        }
+        cp_async_commit();
+    };
+    stage_round(0, 0);
+    for (int j0 = 0, q = 0; j0 < d; j0 += DJ, q ^= 1) {
+        const int jn = min(DJ, d - j0);
+        if (j0 + DJ < d) {
+            stage_round(j0 + DJ, q ^ 1);  // the next round's copies fly during this round
+            cp_async_wait<1>();
+        } else {
+            cp_async_wait<0>();
+        }
+        __syncthreads();  // every thread's copies of this round have landed
+        const float *xs = stages + q * STAGE;
+        const float *cs = xs + DJ * XS;
+        for (int jj = 0; jj < jn; jj++) {
+            float xv[4], cvv[TT];
+#pragma unroll
+            for (int a = 0; a < 4; a++) xv[a] = xs[jj * XS + tid * 4 + a];
+#pragma unroll
+            for (int b = 0; b < TT; b++) cvv[b] = cs[jj * TT + b];
+#pragma unroll
+            for (int a = 0; a < 4; a++)
+#pragma unroll
+                for (int b = 0; b < TT; b++) {
+                    const float df = __fsub_rn(xv[a], cvv[b]);
+                    acc[a][b] = __fmaf_rn(df, df, acc[a][b]);
+                }
+        }
+        __syncthreads();  // this stage is refilled by the next round's staging
+    }
+    // Pairs the bounds leave open are listed (row within the chunk, trial)
+    // and formed in FP64 by the whole block afterwards, one pair a thread:
+    // a warp whose lanes waited on one lane's FP64 chain would run it for
+    // nearly every row slot. A pair beyond the list's room is formed in place.
+    double psum[TT];
+#pragma unroll
+    for (int b = 0; b < TT; b++) psum[b] = 0.0;
+#pragma unroll
+    for (int a = 0; a < 4; a++) {
+        const long long row = base + tid * 4 + a;
+        if (row < n) {
+            const double m = mind[row];
+            const float er = xerr[row];
+#pragma unroll
+            for (int b = 0; b < TT; b++) {
+                if (b < ntr) {
+                    const float bnd = bound32(acc[a][b], __fadd_ru(er, cerr[b]), d);
+                    double r = m;  // v >= d32 - bnd > m: min(v, m) = m (kmeans.rs:230-232)
+                    if (!((double)__fsub_rd(acc[a][b], bnd) > m)) {
+                        const int slot = atomicAdd(&open_n, 1);
+                        if (slot < KPP_OPEN) {
+                            open_pairs[slot] = (unsigned short)(((tid * 4 + a) << 4) | b);
+                            continue;
+                        }
+                        const double v = sqeuc_f64(x + row * d, x + cand[b] * d, d);
+                        r = v < m ? v : m;
+                    }
+                    out[(long long)b * n + row] = r;
+                    psum[b] += r;
+                }
+            }
+        }
+    }
+    __syncthreads();  // the list is complete
+    for (int q = tid; q < min(open_n, KPP_OPEN); q += KPP_THREADS) {
+        const int e = open_pairs[q];
+        const int b = e & 15;
+        const long long row = base + (e >> 4);
+        const double m = mind[row];
+        const double v = sqeuc_f64(x + row * d, x + cand[b] * d, d);
+        const double r = v < m ? v : m;
+        out[(long long)b * n + row] = r;
+        atomicAdd(&open_sum[b], r);  // the chunk sums only steer the folds' windows
+    }
+    const int lane = tid & 31, w = tid >> 5;
+#pragma unroll
+    for (int b = 0; b < TT; b++) {
+        double vv = psum[b];
+#pragma unroll
+        for (int off = 16; off >= 1; off >>= 1) vv += __shfl_xor_sync(0xffffffffu, vv, off);
+        if (lane == 0) red[b][w] = vv;
+    }
+    __syncthreads();
+    if (tid < ntr) {
+        double vv = open_sum[tid];
+        for (int q = 0; q < KPP_THREADS / 32; q++) vv += red[tid][q];
+        csum[(long long)tid * nch + blockIdx.x] = vv;
+    }
+}
+
 // One warp per (chunk, trial): the maps of the chunk's 32 groups (lane g
 // folds group g) and of the whole chunk (ordered warp reduction), each for
 // the three binades around the chunk's estimated starting sum (an f64 sum of
@@ -750,6 +914,37 @@ void launch_trials(const T *x, long long n, int d, T *chains, int ts, const KppS
     FK_LAUNCH_CHECK();
 }
 
+template <int TT>
+void launch_trials_f64f(const double *x, const float *x32, const float *xerr, long long n, int d, double *chains,
+                        int ts, const KppState *st, int ntr, double *csum, long long nch, cudaStream_t s) {
+    constexpr size_t smem = trial_smem<float, TT>();
+    FK_CUDA(cudaFuncSetAttribute((const void *)kpp_trials_f64f_kernel<TT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem));
+    kpp_trials_f64f_kernel<TT><<<(unsigned)nch, KPP_THREADS, smem, s>>>(x, x32, xerr, n, d, chains, ts, st, ntr,
+                                                                        csum, nch);
+    FK_LAUNCH_CHECK();
+}
+
+void launch_trials_f64f_any(const double *x, const float *x32, const float *xerr, long long n, int d,
+                            double *chains, int ts, const KppState *st, int ntr, double *csum, long long nch,
+                            cudaStream_t s) {
+    switch (ntr) {
+        case 1: launch_trials_f64f<1>(x, x32, xerr, n, d, chains, ts, st, ntr, csum, nch, s); break;
+        case 2: launch_trials_f64f<2>(x, x32, xerr, n, d, chains, ts, st, ntr, csum, nch, s); break;
+        case 3: launch_trials_f64f<3>(x, x32, xerr, n, d, chains, ts, st, ntr, csum, nch, s); break;
+        case 4: launch_trials_f64f<4>(x, x32, xerr, n, d, chains, ts, st, ntr, csum, nch, s); break;
+        case 5: launch_trials_f64f<5>(x, x32, xerr, n, d, chains, ts, st, ntr, csum, nch, s); break;
+        case 6: launch_trials_f64f<6>(x, x32, xerr, n, d, chains, ts, st, ntr, csum, nch, s); break;
+        case 7: launch_trials_f64f<7>(x, x32, xerr, n, d, chains, ts, st, ntr, csum, nch, s); break;
+        case 8: launch_trials_f64f<8>(x, x32, xerr, n, d, chains, ts, st, ntr, csum, nch, s); break;
+        case 9: launch_trials_f64f<9>(x, x32, xerr, n, d, chains, ts, st, ntr, csum, nch, s); break;
+        case 10: launch_trials_f64f<10>(x, x32, xerr, n, d, chains, ts, st, ntr, csum, nch, s); break;
+        case 11: launch_trials_f64f<11>(x, x32, xerr, n, d, chains, ts, st, ntr, csum, nch, s); break;
+        case 12: launch_trials_f64f<12>(x, x32, xerr, n, d, chains, ts, st, ntr, csum, nch, s); break;
+        default: launch_trials_f64f<16>(x, x32, xerr, n, d, chains, ts, st, ntr, csum, nch, s); break;
+    }
+}
+
 // The trial pass with the smallest trial-slot count that holds ntr trials.
 template <typename T>
 void launch_trials_any(const T *x, long long n, int d, T *chains, int ts, const KppState *st, int ntr, double *csum,
@@ -807,6 +1002,15 @@ void run_kmeanspp(Ctx &ctx, const T *x, int64_t n, int d, int k, const double *d
 
     kpp_first_kernel<T><<<1, 128, 0, s>>>(x, n, d, draws_dev, n_draws, st, centers_out);
     FK_LAUNCH_CHECK();
+    // f64: the rows' f32 copies and rounding-error norms for the trials' FP32 bounds
+    float *x32 = nullptr, *xerr = nullptr;
+    if constexpr (std::is_same<T, double>::value) {
+        if (k > 1) {
+            x32 = (float *)ctx.get(BUF_PF_X32, sizeof(float) * (size_t)n * d);
+            xerr = (float *)ctx.get(BUF_PF_XERR, sizeof(float) * (size_t)n);
+            launch_f32_copy(ctx, x, n, d, x32, xerr);
+        }
+    }
     if (k == 1) {
         if (draws_used) *draws_used = 1;
         return;
@@ -823,7 +1027,10 @@ void run_kmeanspp(Ctx &ctx, const T *x, int64_t n, int d, int k, const double *d
                                                             n_trials, c, k, st, centers_out);
         FK_LAUNCH_CHECK();
         if (c == k) break;
-        launch_trials_any<T>(x, n, d, chains, ts, st, n_trials, csum, nch, s);
+        if constexpr (std::is_same<T, double>::value)
+            launch_trials_f64f_any(x, x32, xerr, n, d, chains, ts, st, n_trials, csum, nch, s);
+        else
+            launch_trials_any<T>(x, n, d, chains, ts, st, n_trials, csum, nch, s);
         kpp_compose_kernel<T><<<dim3(cgrid, (unsigned)n_trials), KPP_THREADS, 0, s>>>(chains, n, ts, st, false, csum,
                                                                                      nch, fs);
         FK_LAUNCH_CHECK();

@@ -241,6 +241,13 @@ __global__ void f64_open_rows_kernel(const double *__restrict__ x, int d, const 
 
 }  // namespace
 
+void launch_f32_copy(Ctx &ctx, const double *x, int64_t n, int d, float *x32, float *err) {
+    if (n == 0) return;
+    f32_copy_rows_kernel<<<(unsigned)std::min<int64_t>((n + 7) / 8, (int64_t)ctx.num_sms * 8), 256, 0, ctx.stream>>>(
+        x, n, d, x32, err);
+    FK_LAUNCH_CHECK();
+}
+
 void launch_assign_f64_filtered(Ctx &ctx, const double *x, int64_t n, int d, const double *c, int k,
                                 int32_t *labels, double *mind, bool fresh_x) {
     if (n == 0) return;
