@@ -31,11 +31,16 @@ template <> struct Arith<double> {
     static __device__ __forceinline__ double root(double v) { return __dsqrt_rn(v); }
 };
 
-constexpr int BM = 64;   // rows per block tile
-constexpr int BN = 64;   // centres per block tile
+// Per-thread output tile: 8 x 8 in f32 (16 shared-memory loads per 192
+// operations), 4 x 4 in f64 (its registers; the f64 direct form waits on the
+// FP64 pipe, not on loads). 16 x 16 threads a block.
+// The transform (every distance stored) keeps 4 x 4 in both: its stores, not
+// its loads, set its pace.
+template <typename TC, bool WRITE_ALL = false> struct Tile { static constexpr int TM = 8, TN = 8; };
+template <bool WRITE_ALL> struct Tile<double, WRITE_ALL> { static constexpr int TM = 4, TN = 4; };
+template <> struct Tile<float, true> { static constexpr int TM = 4, TN = 4; };
 constexpr int DJ = 16;   // feature chunk staged in shared memory
-constexpr int TM = 4;    // rows per thread
-constexpr int TN = 4;    // centres per thread
+
 constexpr int NT = 256;  // threads per block (16 x 16)
 
 // Lexicographic (distance, index) order: a strictly better candidate has a
@@ -46,7 +51,7 @@ __device__ __forceinline__ bool better(T dv, int di, T bv, int bi) {
 }
 
 // Centres [y * c_per, min(k, (y + 1) * c_per)) of split y = blockIdx.y
-// against 64-row tiles (blockIdx.x); with part_v set, each split writes
+// against row tiles (blockIdx.x); with part_v set, each split writes
 // each row's best (distance,
 // index) of its range to part_v / part_i[blockIdx.y * n + row] (index
 // INT32_MAX: none below F::MAX) for assign_combine_kernel, else the labels
@@ -56,6 +61,9 @@ __global__ void __launch_bounds__(NT)
 assign_direct_kernel(const TX *__restrict__ x, int64_t n, int d, const TC *__restrict__ c, int k,
                      int32_t *__restrict__ labels, TC *__restrict__ mind, TC *__restrict__ out, int c_per,
                      TC *__restrict__ part_v, int32_t *__restrict__ part_i) {
+    constexpr int TM = Tile<TC, WRITE_ALL>::TM, TN = Tile<TC, WRITE_ALL>::TN;
+    constexpr int BM = 16 * TM, BN = 16 * TN;  // rows and centres of a block tile
+    static_assert(BM == BN, "the staging loop fills both tiles with one index");
     const int c_begin = (int)blockIdx.y * c_per;
     const int c_end = min(k, c_begin + c_per);
     using A = Arith<TC>;
@@ -233,13 +241,16 @@ template <typename TX, typename TC>
 void launch_assign_direct(const TX *x, int64_t n, int d, const TC *c, int k, int32_t *labels,
                           TC *mind, cudaStream_t s) {
     if (n == 0) return;
+    constexpr int BM = 16 * Tile<TC>::TM;
     dim3 grid((unsigned)((n + BM - 1) / BM));
     assign_direct_kernel<TX, TC, false><<<grid, NT, 0, s>>>(x, n, d, c, k, labels, mind, nullptr, k, nullptr,
                                                             nullptr);
     FK_LAUNCH_CHECK();
 }
 
+template <typename TC>
 int assign_splits(int64_t n, int k, int num_sms) {
+    constexpr int BM = 16 * Tile<TC>::TM, BN = 16 * Tile<TC>::TN;
     const int64_t tiles = (n + BM - 1) / BM;
     const int64_t want = (2 * (int64_t)num_sms + tiles - 1) / tiles;  // about two CTAs per SM
     const int64_t most = (k + BN - 1) / BN;
@@ -254,7 +265,8 @@ void launch_assign_direct_split(const TX *x, int64_t n, int d, const TC *c, int 
         launch_assign_direct<TX, TC>(x, n, d, c, k, labels, mind, s);
         return;
     }
-    // split q takes whole 64-centre tiles [q * per, (q + 1) * per)
+    // split q takes whole centre tiles [q * per, (q + 1) * per)
+    constexpr int BM = 16 * Tile<TC>::TM, BN = 16 * Tile<TC>::TN;
     const int tiles_k = (k + BN - 1) / BN;
     const int per = (tiles_k + splits - 1) / splits * BN;
     const int used = (k + per - 1) / per;
@@ -270,6 +282,7 @@ template <typename T>
 void launch_transform_direct(const T *x, int64_t n, int d, const T *c, int k, T *out,
                              cudaStream_t s) {
     if (n == 0) return;
+    constexpr int BM = 16 * Tile<T, true>::TM;
     dim3 grid((unsigned)((n + BM - 1) / BM));
     assign_direct_kernel<T, T, true><<<grid, NT, 0, s>>>(x, n, d, c, k, nullptr, nullptr, out, k, nullptr, nullptr);
     FK_LAUNCH_CHECK();
@@ -307,6 +320,8 @@ void launch_convert(const TS *src, int64_t count, TD *dst, cudaStream_t s) {
     FK_LAUNCH_CHECK();
 }
 
+template int assign_splits<float>(int64_t, int, int);
+template int assign_splits<double>(int64_t, int, int);
 template void launch_assign_direct<double, double>(const double *, int64_t, int, const double *, int,
                                                    int32_t *, double *, cudaStream_t);
 template void launch_assign_direct<float, float>(const float *, int64_t, int, const float *, int,

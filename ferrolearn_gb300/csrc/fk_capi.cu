@@ -932,7 +932,7 @@ fk_status minibatch_impl(fk_ctx *ctxp, const T *x_in, int64_t n, int64_t d, cons
     T *xb = (T *)ctx.get(BUF_MB_XB, sizeof(T) * (size_t)m * d);
     int32_t *blab = (int32_t *)ctx.get(BUF_MB_LAB, sizeof(int32_t) * (size_t)m);
     // a batch is too few rows to fill the GPU by row tiles: split the centres too
-    const int splits = assign_splits(m, (int)k, ctx.num_sms);
+    const int splits = assign_splits<T>(m, (int)k, ctx.num_sms);
     T *part_v = splits > 1 ? (T *)ctx.get(BUF_MB_PARTV, sizeof(T) * (size_t)splits * m) : nullptr;
     int32_t *part_i = splits > 1 ? (int32_t *)ctx.get(BUF_MB_PARTI, sizeof(int32_t) * (size_t)splits * m) : nullptr;
     std::vector<int32_t> hidx;

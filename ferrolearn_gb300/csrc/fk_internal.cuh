@@ -287,6 +287,7 @@ __device__ __forceinline__ float bound32(float d32, float ec, int d) {
     return __fadd_ru(__fmul_ru(e, 1.01f), 1e-30f);
 }
 
+template <typename TC>
 int assign_splits(int64_t n, int k, int num_sms);
 template <typename TX, typename TC>
 void launch_assign_direct_split(const TX *x, int64_t n, int d, const TC *c, int k, int32_t *labels, TC *mind,

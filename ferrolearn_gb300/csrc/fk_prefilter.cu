@@ -27,11 +27,11 @@
 namespace fk {
 namespace {
 
-constexpr int PBM = 64;   // rows per block tile
-constexpr int PBN = 64;   // centres per block tile
+constexpr int PBM = 128;  // rows per block tile
+constexpr int PBN = 128;  // centres per block tile
 constexpr int PDJ = 16;   // feature chunk staged in shared memory
-constexpr int PTM = 4;    // rows per thread
-constexpr int PTN = 4;    // centres per thread
+constexpr int PTM = 8;    // rows per thread
+constexpr int PTN = 8;    // centres per thread
 constexpr int PNT = 256;  // threads per block (16 x 16)
 
 // f32 copies of f64 rows (one warp per row) and an upper bound of the norm
@@ -90,7 +90,7 @@ __device__ __forceinline__ void rb_merge(RowBound &r, const RowBound &o) {
     }
 }
 
-// FP32 pass over 64-row tiles and every centre: decided rows get their label,
+// FP32 pass over 128-row tiles and every centre: decided rows get their label,
 // open rows label -1 and a slot in the list.
 __global__ void __launch_bounds__(PNT)
     f32_filter_kernel(const float *__restrict__ x32, const float *__restrict__ xerr, int64_t n, int d,
