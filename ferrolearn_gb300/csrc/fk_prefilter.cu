@@ -6,7 +6,7 @@
 // FP64 ones, bit for bit:
 //
 //   1. X and the centres get f32 copies and, per row, an upper bound of the
-//      norm of their rounding error, e = ||x - x32|| (f64, rounded up).
+//      norm of their rounding error, e = ||x - x32|| (rounded up).
 //   2. A tiled FP32 pass forms each row's direct-form distances to every
 //      centre from the f32 copies (t = x - c, acc = fma(t, t, acc)) and the
 //      interval [d32 - b, d32 + b] with b = bound32(d32, e_x + e_c, d), which
@@ -36,24 +36,27 @@ constexpr int PNT = 256;  // threads per block (16 x 16)
 
 // f32 copies of f64 rows (one warp per row) and an upper bound of the norm
 // of each row's rounding error (+inf or NaN when a value does not fit f32).
+// Each error is bounded in FP64 (two directed subtractions), then rounded up
+// to f32; the squares, the sum and the root run in FP32 rounded up (FP64 is
+// slow here, its square root most of all).
 __global__ void f32_copy_rows_kernel(const double *__restrict__ x, int64_t n, int d, float *__restrict__ x32,
                                      float *__restrict__ err) {
     const int lane = threadIdx.x & 31;
     const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
     for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < n; r += nw) {
-        double s = 0.0;
+        float s = 0.f;
         for (int j = lane; j < d; j += 32) {
             const double v = x[r * d + j];
             const float f = __double2float_rn(v);
             x32[r * d + j] = f;
             const double fd = (double)f;
             const double hi = fabs(__dsub_ru(v, fd)), lo = fabs(__dsub_rd(v, fd));
-            const double e = hi > lo ? hi : lo;  // NaN stays NaN
-            s = __dadd_ru(s, __dmul_ru(e, e));
+            const float e = __double2float_ru(hi > lo ? hi : lo);  // NaN stays NaN
+            s = __fadd_ru(s, __fmul_ru(e, e));
         }
 #pragma unroll
-        for (int off = 16; off >= 1; off >>= 1) s = __dadd_ru(s, __shfl_xor_sync(0xffffffffu, s, off));
-        if (lane == 0) err[r] = __double2float_ru(__dsqrt_ru(s));
+        for (int off = 16; off >= 1; off >>= 1) s = __fadd_ru(s, __shfl_xor_sync(0xffffffffu, s, off));
+        if (lane == 0) err[r] = __fsqrt_ru(s);
     }
 }
 
