@@ -34,11 +34,32 @@ constexpr int PTM = 8;    // rows per thread
 constexpr int PTN = 8;    // centres per thread
 constexpr int PNT = 256;  // threads per block (16 x 16)
 
+// |v - f| for f = v rounded to f32, as an f32 rounded up. For v in the f32
+// normal range the error is exact integer arithmetic on v's bits: with E the
+// exponent and r the 29 mantissa bits below f32's precision, |v - f| =
+// min(r, 2^29 - r) 2^(E - 52) (rounding up into the next binade included).
+// Zeros, f32 subnormals, overflow and NaN take two directed FP64
+// subtractions (NaN stays NaN, overflow gives inf).
+__device__ __forceinline__ float round_err(double v, float f) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    const int E = (int)((b >> 52) & 0x7FFull) - 1023;
+    if (E >= -126 && E <= 127 && fabsf(f) <= FLT_MAX) {
+        const unsigned long long low = b & ((1ull << 29) - 1ull);
+        const unsigned long long q = low < (1ull << 28) ? low : (1ull << 29) - low;  // <= 2^28
+        const float qs = __fmul_rn(__ull2float_ru(q), 1.862645149230957e-09f);       // q (up) 2^-29: exact
+        const int pe = E - 23;                                                         // >= -149
+        const float p2 = pe >= -126 ? __int_as_float((pe + 127) << 23) : __int_as_float(1 << (pe + 149));
+        return __fmul_ru(qs, p2);
+    }
+    const double fd = (double)f;
+    const double hi = fabs(__dsub_ru(v, fd)), lo = fabs(__dsub_rd(v, fd));
+    return __double2float_ru(hi > lo ? hi : lo);
+}
+
 // f32 copies of f64 rows (one warp per row) and an upper bound of the norm
-// of each row's rounding error (+inf or NaN when a value does not fit f32).
-// Each error is bounded in FP64 (two directed subtractions), then rounded up
-// to f32; the squares, the sum and the root run in FP32 rounded up (FP64 is
-// slow here, its square root most of all).
+// of each row's rounding error (+inf or NaN when a value does not fit f32);
+// the squares, the sum and the root in FP32 rounded up (FP64 is slow here,
+// its square root most of all).
 __global__ void f32_copy_rows_kernel(const double *__restrict__ x, int64_t n, int d, float *__restrict__ x32,
                                      float *__restrict__ err) {
     const int lane = threadIdx.x & 31;
@@ -49,9 +70,7 @@ __global__ void f32_copy_rows_kernel(const double *__restrict__ x, int64_t n, in
             const double v = x[r * d + j];
             const float f = __double2float_rn(v);
             x32[r * d + j] = f;
-            const double fd = (double)f;
-            const double hi = fabs(__dsub_ru(v, fd)), lo = fabs(__dsub_rd(v, fd));
-            const float e = __double2float_ru(hi > lo ? hi : lo);  // NaN stays NaN
+            const float e = round_err(v, f);
             s = __fadd_ru(s, __fmul_ru(e, e));
         }
 #pragma unroll
