@@ -33,7 +33,9 @@
 // candidate (the first row whose running sum reaches its threshold: a 32-ary
 // search over the recorded chunk states, then the chunk walked exactly);
 // kpp_trials_kernel forms min(D^2, d(x, candidate)) for every trial in one
-// pass over X (direct-form distances, no FMA, identical to the reference);
+// pass over X (direct-form distances, no FMA, identical to the reference; in
+// f64, kpp_trials_f64f_kernel bounds them in FP32 first and forms the FP64
+// distance only where the candidate may come closer than D^2);
 // compose and walk give every trial's potential and its chunk states, which
 // the next centre's search uses (the chosen trial's D^2 array becomes the new
 // one without a copy: two buffers alternate). A non-positive total takes one
