@@ -22,7 +22,7 @@
 // is final. Otherwise, if the best value outside the top two is also below
 // v1 - thr, only the top two are re-scored exactly; else the row goes through
 // a second tensor-core pass. After a BF16 main pass it recomputes the row's
-// scores from the same operands and marks every centre scoring at least
+// scores from the same operands and marks every centre scoring above
 // v1 - 2 thr (a superset of the centres that can still win); 1 to 32 marked
 // centres are re-scored, more or none send the row to the exhaustive
 // re-score. After an FP8 main pass it runs in BF16 (its own operands, made
@@ -1810,7 +1810,7 @@ float mu_norm_up(double v) {
 
 // Second pass over the rows listed in full (count sc->full_count). After a
 // BF16 main pass: the rows' BF16 operands gathered from the main pass's
-// copy, a tensor pass that marks every centre scoring at least the row's
+// copy, a tensor pass that marks every centre scoring above the row's
 // threshold, then the re-score of at most 32 candidates, or of every centre.
 // After an FP8 main pass: BF16 operands made from the rows' f32 values, a
 // BF16 count pass against thresholds from the rows' floors, the mask pass

@@ -369,12 +369,14 @@ struct RankChunk<COL0, N, N> {
 
 // ------------------------------------------------ mask (second pass) --
 // One 32-column chunk of a row's candidate mask: column e is a candidate
-// when its score T_e >= th. fma.sat(T, S, C) with S = 8 / ulp and C = -th S
+// when its score T_e > th. fma.sat(T, S, C) with S = 8 / ulp and C = -th S
 // is exactly 0 or 1: T and th are floats of at least 2^(E-2) (the caller
 // sends every lower threshold to -inf), so a nonzero T - th is a multiple
 // of 2^(E-25) and (T - th) S a nonzero multiple of 2, whose rounding keeps
-// its sign; a padded column (T = 0) gives 0, or 1 with th = -inf; NaN
-// gives 0. Horner steps on packed pairs, acc = 2 acc + (bit even, bit
+// its sign; T = th gives 0; a padded column (T = 0) gives 0, or 1 with th =
+// -inf; NaN gives 0. Every threshold lies strictly below the scores that
+// can win (its margin holds 384 ulp, and its roundings go down), so the
+// strict comparison loses no candidate. Horner steps on packed pairs, acc = 2 acc + (bit even, bit
 // odd), exact below 2^16, put the even columns 2j in bits 15 - j of the low
 // half and the odd columns 2j + 1 in bits 31 - j: one saturating FMA per
 // score and one packed FMA per two scores, no ALU instruction. The steps
