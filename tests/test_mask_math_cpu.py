@@ -67,6 +67,20 @@ def test_marks_are_exact_zero_one_and_strict():
             assert m == (1 if t > th else 0), (e, float(t), float(th))
 
 
+def test_marks_at_the_binade_edges():
+    # T at the bottom of its binade and thresholds just below it, in the two
+    # binades beneath (spacings ulp / 2 and ulp / 4): the smallest nonzero
+    # T - th the marks must resolve
+    for e in (-5, 0, 12, 33):
+        ulp = Fraction(2) ** (e - 23)
+        s = 8 / ulp
+        t = Fraction(2) ** e
+        for th in (t - ulp / 2, t - ulp, Fraction(2) ** (e - 1) - ulp / 4, Fraction(2) ** (e - 2), t, t + ulp):
+            assert _f32(float(th)) == th
+            m = _fma_sat(t, s, _round32(-th * s))
+            assert m == (1 if t > th else 0), (e, float(th))
+
+
 def _horner_word(bits):
     """Two 8-step chains over columns 0-15 and 16-31, pairs (2j, 2j+1) packed,
     joined as hi 2^8 + lo; returns e | o << 16."""
