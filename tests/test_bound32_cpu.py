@@ -13,48 +13,15 @@ import math
 from fractions import Fraction
 
 import numpy as np
-
-F32_MAX = Fraction(2) ** 127 * (2 - Fraction(1, 2 ** 23))
-
-
-def _round32(q, mode):
-    """q rounded to an f32 value: 'n' nearest-even, 'u' toward +inf."""
-    if q == 0:
-        return Fraction(0)
-    sign = 1 if q > 0 else -1
-    a = abs(q)
-    e = a.numerator.bit_length() - a.denominator.bit_length()
-    if Fraction(2) ** e > a:
-        e -= 1
-    ue = max(e, -126) - 23
-    s = a / Fraction(2) ** ue
-    i = s.numerator // s.denominator
-    r = s - i
-    if mode == "n":
-        if r > Fraction(1, 2) or (r == Fraction(1, 2) and i % 2 == 1):
-            i += 1
-    elif mode == "u":
-        if sign > 0 and r > 0:
-            i += 1
-    out = sign * i * Fraction(2) ** ue
-    if abs(out) > F32_MAX:
-        return Fraction(10) ** 40 * sign  # overflow: the tests stay far below it
-    return out
-
-
-def _f32(v):
-    return _round32(Fraction(float(v)), "n")
+from exact32 import exponent, f32, round32
 
 
 def _bound32(d32, ec, d):
     """bound32, operation by operation (fk_internal.cuh)."""
-    u = lambda q: _round32(q, "u")  # noqa: E731
+    u = lambda q: round32(q, "u")  # noqa: E731
     dd = d32 if d32 > 0 else Fraction(0)
     if dd > 0:
-        ex = dd.numerator.bit_length() - dd.denominator.bit_length()
-        if Fraction(2) ** ex > dd:
-            ex -= 1
-        h = math.floor(ex / 2)
+        h = math.floor(exponent(dd) / 2)
         sq2 = u(u(dd * Fraction(2) ** (-h)) + Fraction(2) ** h)
     else:
         sq2 = Fraction(0)
@@ -67,18 +34,18 @@ def _bound32(d32, ec, d):
 
 def _check(x, c):
     d = len(x)
-    x32 = [_f32(v) for v in x]
-    c32 = [_f32(v) for v in c]
+    x32 = [f32(v) for v in x]
+    c32 = [f32(v) for v in c]
     acc = Fraction(0)
     for a, b in zip(x32, c32):
-        t = _round32(a - b, "n")
-        acc = _round32(t * t + acc, "n")  # fma: one rounding
-    ex = _round32(Fraction(math.sqrt(float(sum((Fraction(float(v)) - w) ** 2 for v, w in zip(x, x32))))), "u")
-    ec = _round32(Fraction(math.sqrt(float(sum((Fraction(float(v)) - w) ** 2 for v, w in zip(c, c32))))), "u")
+        t = round32(a - b, "n")
+        acc = round32(t * t + acc, "n")  # fma: one rounding
+    ex = round32(Fraction(math.sqrt(float(sum((Fraction(float(v)) - w) ** 2 for v, w in zip(x, x32))))), "u")
+    ec = round32(Fraction(math.sqrt(float(sum((Fraction(float(v)) - w) ** 2 for v, w in zip(c, c32))))), "u")
     # the sqrt above is rounded to nearest in f64: widen by one part in 2^50 to keep it an upper bound
-    ex = _round32(ex * (1 + Fraction(1, 2 ** 50)), "u")
-    ec = _round32(ec * (1 + Fraction(1, 2 ** 50)), "u")
-    b = _bound32(acc, _round32(ex + ec, "u"), d)
+    ex = round32(ex * (1 + Fraction(1, 2 ** 50)), "u")
+    ec = round32(ec * (1 + Fraction(1, 2 ** 50)), "u")
+    b = _bound32(acc, round32(ex + ec, "u"), d)
     exact = sum((Fraction(float(p)) - Fraction(float(q))) ** 2 for p, q in zip(x, c))
     d64 = 0.0
     for p, q in zip(x, c):

@@ -8,36 +8,12 @@ the word whose bit b < 16 is column 2(15 - b) and bit b >= 16 column
 from fractions import Fraction
 
 import numpy as np
-
-F32_MAX = Fraction(2) ** 127 * (2 - Fraction(1, 2 ** 23))
-
-
-def _round32(q):
-    """q rounded to the nearest f32 (ties to even), overflow to +-inf."""
-    if q == 0:
-        return Fraction(0)
-    sign = 1 if q > 0 else -1
-    a = abs(q)
-    e = a.numerator.bit_length() - a.denominator.bit_length()
-    if Fraction(2) ** e > a:
-        e -= 1
-    ue = max(e, -126) - 23
-    s = a / Fraction(2) ** ue
-    i = s.numerator // s.denominator
-    r = s - i
-    if r > Fraction(1, 2) or (r == Fraction(1, 2) and i % 2 == 1):
-        i += 1
-    out = sign * i * Fraction(2) ** ue
-    return out if abs(out) <= F32_MAX else Fraction(10) ** 40 * sign
+from exact32 import f32, round32
 
 
 def _fma_sat(t, s, c):
-    r = _round32(t * s + c)
+    r = round32(t * s + c)
     return min(max(r, Fraction(0)), Fraction(1))
-
-
-def _f32(x):
-    return Fraction(float(np.float32(x)))
 
 
 def test_marks_are_exact_zero_one_and_strict():
@@ -47,7 +23,7 @@ def test_marks_are_exact_zero_one_and_strict():
         s = 8 / ulp
         lo, hi = Fraction(2) ** e, Fraction(2) ** (e + 1)
         for _ in range(300):
-            t = _f32(float(lo) * (1 + rng.random()))
+            t = f32(float(lo) * (1 + rng.random()))
             assert lo <= t < hi
             kind = rng.integers(0, 4)
             if kind == 0:
@@ -55,12 +31,12 @@ def test_marks_are_exact_zero_one_and_strict():
             elif kind == 1:
                 th = t + ulp * rng.choice([-1, 1])       # one ulp either side
             elif kind == 2:
-                th = _f32(float(Fraction(2) ** (e - 2)) * (1 + 7 * rng.random()))  # anywhere from 2^(E-2)
+                th = f32(float(Fraction(2) ** (e - 2)) * (1 + 7 * rng.random()))  # anywhere from 2^(E-2)
             else:
-                th = _f32(float(t) * (1 + (rng.random() - 0.5) * 1e-6))  # within a few ulp
+                th = f32(float(t) * (1 + (rng.random() - 0.5) * 1e-6))  # within a few ulp
             if th < Fraction(2) ** (e - 2):
                 continue
-            c = _round32(-th * s)
+            c = round32(-th * s)
             assert c == -th * s  # exact: a float times a power of two
             m = _fma_sat(t, s, c)
             assert m in (0, 1)
@@ -76,8 +52,8 @@ def test_marks_at_the_binade_edges():
         s = 8 / ulp
         t = Fraction(2) ** e
         for th in (t - ulp / 2, t - ulp, Fraction(2) ** (e - 1) - ulp / 4, Fraction(2) ** (e - 2), t, t + ulp):
-            assert _f32(float(th)) == th
-            m = _fma_sat(t, s, _round32(-th * s))
+            assert f32(float(th)) == th
+            m = _fma_sat(t, s, round32(-th * s))
             assert m == (1 if t > th else 0), (e, float(th))
 
 
